@@ -1,0 +1,200 @@
+"""ctypes front end for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries share this interface:
+  * liboracle.so              -- this project's C restatement ("orc_"),
+  * _ref/libcosmolike_ref.so  -- the reference's own sources driven by
+                                 ref_harness.c ("ref_"); it exists only where
+                                 the reference tree was available to build it.
+Both keep process-global state, so one process drives one configuration of
+the reference library (its pair maps are built once per process).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
+from cl2pt import abi  # noqa: E402
+
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libcosmolike_ref.so")
+REFERENCE_TREE = "/root/reference"
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build(ref: bool | None = None, quiet: bool = True) -> None:
+    """Build liboracle.so (and the reference library when its tree exists)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"], check=True,
+                   stdout=out)
+    if ref is None:
+        ref = os.path.isdir(os.path.join(REFERENCE_TREE, "cosmolike"))
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"-j{os.cpu_count() or 4}",
+                        f"REF={REFERENCE_TREE}"], check=True, stdout=out)
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Oracle:
+    """One loaded oracle library with prefix 'orc' or 'ref'."""
+
+    def __init__(self, which: str = "orc"):
+        self.which = which
+        path = ORACLE_SO if which == "orc" else REF_SO
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.cfg = None
+        self._keep = []
+        pre = which + "_"
+        d = C.c_double
+        for name, args in {
+            "nz_source": [d, C.c_int], "nz_lens": [d, C.c_int], "g_tomo": [d, C.c_int],
+            "g_lens": [d, C.c_int], "chi": [d], "a_chi": [d], "growfac": [d],
+            "f_growth": [d], "p_nonlin": [d, d], "amin_lens": [C.c_int],
+            "amax_lens": [C.c_int], "zmean_lens": [C.c_int],
+            "C_ss_nointerp": [d, C.c_int, C.c_int, C.c_int],
+            "C_gs_nointerp": [d, C.c_int, C.c_int],
+            "C_gg_nointerp": [d, C.c_int, C.c_int],
+            "C_ss_limber": [d, C.c_int, C.c_int, C.c_int],
+            "C_gs_limber": [d, C.c_int, C.c_int], "C_gg_limber": [d, C.c_int],
+        }.items():
+            f = getattr(self.lib, pre + name)
+            f.restype = C.c_double
+            f.argtypes = args
+            setattr(self, name, f)
+
+    # ---- state
+    def setup(self, cfg, src_table, lens_table):
+        self.cfg = cfg
+        self._src = abi.make_nz(src_table)
+        self._lens = abi.make_nz(lens_table)
+        st = getattr(self.lib, self.which + "_setup")(C.byref(cfg), C.byref(self._src.struct),
+                                                      C.byref(self._lens.struct))
+        if st != 0:
+            raise RuntimeError(f"setup failed: {st}")
+
+    def set_point(self, tables, nuisance):
+        self._cosmo = abi.make_cosmo(tables)
+        self._nu = nuisance
+        st = getattr(self.lib, self.which + "_set_point")(C.byref(self._cosmo.struct),
+                                                          C.byref(nuisance))
+        if st != 0:
+            raise RuntimeError(f"set_point failed: {st}")
+
+    @property
+    def npairs(self):
+        return abi.n_pairs(self.cfg)
+
+    # ---- outputs
+    def xi_pm(self):
+        pss = self.npairs[0]
+        nt = self.cfg.ntheta
+        xp = np.zeros(pss * nt)
+        xm = np.zeros(pss * nt)
+        getattr(self.lib, self.which + "_xi_pm")(_p(xp), _p(xm))
+        return xp.reshape(pss, nt), xm.reshape(pss, nt)
+
+    def w_gammat(self):
+        pgs = self.npairs[1]
+        out = np.zeros(pgs * self.cfg.ntheta + 1)
+        getattr(self.lib, self.which + "_w_gammat")(_p(out))
+        return out[:-1].reshape(pgs, self.cfg.ntheta)
+
+    def w_gg(self):
+        pgg = self.npairs[2]
+        out = np.zeros(pgg * self.cfg.ntheta + 1)
+        getattr(self.lib, self.which + "_w_gg")(_p(out))
+        return out[:-1].reshape(pgg, self.cfg.ntheta)
+
+    def C_cl_tomo(self):
+        nl, L = self.cfg.n_lens, self.cfg.lmax_nolimber
+        out = np.zeros(nl * L)
+        f = getattr(self.lib, self.which + "_C_cl_tomo")
+        if self.which == "orc":
+            conv = np.zeros(nl, dtype=np.int32)
+            f(_p(out), conv.ctypes.data_as(_ip))
+            return out.reshape(nl, L), conv
+        f(_p(out))
+        return out.reshape(nl, L), None
+
+    def data_vector_real(self, mask=None, pm=None):
+        pss, pgs, pgg = self.npairs
+        n = self.cfg.ntheta * (2 * pss + pgs + pgg)
+        if mask is None:
+            mask = np.ones(n, dtype=np.int32)
+        mask = np.ascontiguousarray(mask, dtype=np.int32)
+        dv = np.zeros(n)
+        pmp = None
+        if pm is not None:
+            pm = np.ascontiguousarray(pm, dtype=np.float64)
+            pmp = _p(pm)
+        getattr(self.lib, self.which + "_data_vector_real")(mask.ctypes.data_as(_ip), pmp, _p(dv))
+        return dv
+
+    def data_vector_fourier(self, ell, lmax_shear=1e30, use_nonlimber=1, mask=None):
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        pss, pgs, pgg = self.npairs
+        n = len(ell) * (pss + pgs + pgg)
+        if mask is None:
+            mask = np.ones(n, dtype=np.int32)
+        mask = np.ascontiguousarray(mask, dtype=np.int32)
+        dv = np.zeros(n)
+        f = getattr(self.lib, "orc_data_vector_fourier")
+        f.argtypes = [C.c_int, _dp, C.c_double, C.c_int, _ip, _dp]
+        f(len(ell), _p(ell), lmax_shear, use_nonlimber, mask.ctypes.data_as(_ip), _p(dv))
+        return dv
+
+    def limber_tables(self):
+        assert self.which == "orc"
+        pss, pgs, pgg = self.npairs
+        ne = self.cfg.n_ell
+        ss = np.zeros(2 * pss * ne)
+        gs = np.zeros(pgs * ne + 1)
+        gg = np.zeros(pgg * ne + 1)
+        self.lib.orc_limber_tables(_p(ss), _p(gs), _p(gg))
+        return ss.reshape(2, pss, ne), gs[:-1].reshape(pgs, ne), gg[:-1].reshape(pgg, ne)
+
+    def ell_nodes(self, which):
+        out = np.zeros(self.cfg.n_ell)
+        self.lib.orc_ell_nodes(which, _p(out))
+        return out
+
+    def legendre_filters(self):
+        nt, L = self.cfg.ntheta, self.cfg.lmax
+        out = np.zeros(4 * nt * L)
+        self.lib.orc_legendre_filters(_p(out))
+        return out.reshape(4, nt, L)
+
+    def fpt_bias(self):
+        n = C.c_int(0)
+        f = getattr(self.lib, self.which + "_fpt_bias")
+        f(None, C.byref(n))
+        out = np.zeros(8 * n.value)
+        f(_p(out), C.byref(n))
+        return out.reshape(8, n.value)
+
+    def J_abl(self, x, fx, alpha, beta, ell, nu=-2.0, c_window=0.65, npad=1500,
+              nlow=500, nhigh=500):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(fx, dtype=np.float64)
+        ia = lambda v: np.ascontiguousarray(v, dtype=np.int32)
+        a, b, l = ia(alpha), ia(beta), ia(ell)
+        Fy = np.zeros(len(a) * len(x))
+        f = getattr(self.lib, self.which + "_J_abl")
+        f.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, C.c_int, C.c_double, C.c_double,
+                      C.c_long, C.c_long, C.c_long, _dp]
+        f(_p(x), _p(fx), len(x), a.ctypes.data_as(_ip), b.ctypes.data_as(_ip),
+          l.ctypes.data_as(_ip), len(a), nu, c_window, npad, nlow, nhigh, _p(Fy))
+        return Fy.reshape(len(a), len(x))

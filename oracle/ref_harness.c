@@ -1,0 +1,411 @@
+/*
+ * ref_harness.c -- drives the reference's own hot-path C code (compiled
+ * unchanged from its sources into oracle/_ref/libcosmolike_ref.so) from a
+ * cl2pt description.  TEST INFRASTRUCTURE ONLY: it pins the oracle
+ * restatement and generates the golden fixtures; nothing shipped links it.
+ *
+ * The setter semantics of the reference's C++ interface cannot be compiled
+ * here (armadillo, spdlog, boost and carma are absent), so this file
+ * restates the parts the hot path depends on, citing each:
+ *   initial_setup              cosmolike/generic_interface.cpp:236-277
+ *   init_binning_real_space    cosmolike/generic_interface.cpp:479-503
+ *   init_ntomo_powerspectra    cosmolike/generic_interface.cpp:775-802
+ *   set_cosmological_parameters cosmolike/generic_interface.cpp:912-939
+ *   set_distances / set_growth cosmolike/generic_interface.cpp:1085-1190
+ *   set_*linear_power_spectrum cosmolike/generic_interface.cpp:1194-1356
+ *   set_nuisance_*             cosmolike/generic_interface.cpp:1358-1782
+ *   set_lens_sample            cosmolike/generic_interface.cpp:1802-1887
+ *   set_source_sample          cosmolike/generic_interface.cpp:1907-1988
+ *   data-vector assembly       cosmolike/generic_interface.hpp:800-1040
+ * Every call to ref_set_point bumps every cache token, as a sampler step
+ * with new values does.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "basics.h"
+#include "bias.h"
+#include "cosmo2D.h"
+#include "cosmo3D.h"
+#include "IA.h"
+#include "pt_cfastpt.h"
+#include "radial_weights.h"
+#include "redshift_spline.h"
+#include "structs.h"
+#include "cfastpt/cfastpt.h"
+
+#include "cl2pt_types.h"
+
+/* defined in cosmolike/cosmo2D.c:2614 but not declared in its header */
+double C_gg_tomo_limber_linpsopt_nointerp(const double l, const int ni, const int nj,
+                                          const int use_linear_ps, const int init);
+
+static uint64_t g_token = 1000;
+static uint64_t next_token(void) { return ++g_token; }
+static cl2pt_config g_cfg;
+
+static double** alloc2(int nx, int ny)
+{
+  return (double**)malloc2d(nx, ny);
+}
+
+static void set_nz_table(int is_source, const cl2pt_nz* nz)
+{
+  const int Ntomo = nz->ntomo;
+  const int nzbins = nz->nzbins;
+  double** tab = alloc2(Ntomo + 1, nzbins);
+  double* z_v = tab[Ntomo];
+  for (int i = 0; i < nzbins; i++) {
+    z_v[i] = nz->table[i * (Ntomo + 1)];
+    for (int k = 0; k < Ntomo; k++) tab[k][i] = nz->table[i * (Ntomo + 1) + k + 1];
+  }
+  const double zmin_all = fmax(z_v[0], 1.e-5);
+  const double zmax_all = z_v[nzbins - 1] + (z_v[nzbins - 1] - z_v[0]) / ((double)nzbins - 1.);
+  double zmin[CL2PT_MAX_BINS], zmax[CL2PT_MAX_BINS];
+  for (int k = 0; k < Ntomo; k++) {
+    double mx = -INFINITY;
+    for (int i = 0; i < nzbins; i++) mx = fmax(mx, tab[k][i]);
+    int first = -1, last = -1;
+    for (int i = 0; i < nzbins; i++) {
+      if (tab[k][i] > 0.999e-8 * mx) {
+        if (first < 0) first = i;
+        last = i;
+      }
+    }
+    zmin[k] = is_source ? fmax(z_v[first], 1.001e-5) : z_v[first];
+    zmax[k] = z_v[last];
+  }
+  if (is_source) {
+    redshift.shear_nzbins = nzbins;
+    redshift.shear_zdist_table = tab;
+    redshift.shear_zdist_zmin_all = zmin_all;
+    redshift.shear_zdist_zmax_all = zmax_all;
+    for (int k = 0; k < Ntomo; k++) {
+      redshift.shear_zdist_zmin[k] = zmin[k];
+      redshift.shear_zdist_zmax[k] = zmax[k];
+    }
+    redshift.random_shear = next_token();
+    nz_source_photoz(0.1, 0);
+  } else {
+    redshift.clustering_nzbins = nzbins;
+    redshift.clustering_zdist_table = tab;
+    redshift.clustering_zdist_zmin_all = zmin_all;
+    redshift.clustering_zdist_zmax_all = zmax_all;
+    for (int k = 0; k < Ntomo; k++) {
+      redshift.clustering_zdist_zmin[k] = zmin[k];
+      redshift.clustering_zdist_zmax[k] = zmax[k];
+    }
+    redshift.random_clustering = next_token();
+    nz_lens_photoz(0.1, 0);
+    for (int k = 0; k < Ntomo; k++) redshift.clustering_zdist_zmean[k] = zmean(k);
+  }
+}
+
+int ref_setup(const cl2pt_config* cfg, const cl2pt_nz* src, const cl2pt_nz* lens)
+{
+  g_cfg = *cfg;
+  /* initial_setup */
+  reset_redshift_struct();
+  reset_nuisance_struct();
+  reset_cosmology_struct();
+  reset_tomo_struct();
+  reset_Ntable_struct();
+  reset_like_struct();
+  reset_cmb_struct();
+  like.adopt_limber_gg = cfg->adopt_limber_gg;
+  snprintf(pdeltaparams.runmode, sizeof(pdeltaparams.runmode), "%s",
+           cfg->linear_pk ? "linear" : "Halofit");
+  /* accuracy / binning */
+  Ntable.LMAX = cfg->lmax;
+  Ntable.N_ell = cfg->n_ell;
+  Ntable.N_a = cfg->n_a;
+  Ntable.NL_Nchi = cfg->nl_nchi;
+  Ntable.high_def_integration = cfg->high_def_integration;
+  Ntable.random = next_token();
+  Ntable.Ntheta = cfg->ntheta;
+  Ntable.vtmin = cfg->theta_min_arcmin * 2.90888208665721580e-4;
+  Ntable.vtmax = cfg->theta_max_arcmin * 2.90888208665721580e-4;
+  limits.LMIN_tab = cfg->lmin_tab;
+  limits.LMAX_NOLIMBER = cfg->lmax_nolimber;
+  limits.a_min = cfg->a_min;
+  like.shear_shear = (cfg->probes & CL2PT_PROBE_XI) ? 1 : 0;
+  like.shear_pos = (cfg->probes & CL2PT_PROBE_GAMMAT) ? 1 : 0;
+  like.pos_pos = (cfg->probes & CL2PT_PROBE_WTHETA) ? 1 : 0;
+  for (int i = 0; i < 6; i++) like.galaxy_bias_model[i] = cfg->bias_model[i];
+  nuisance.IA_MODEL = cfg->ia_model;
+  nuisance.IA = cfg->ia_mode;
+  nuisance.IA_code = 0;
+  if (cfg->n_ggl_exclude > 0) {
+    tomo.ggl_exclude = (int*)malloc(sizeof(int) * 2 * cfg->n_ggl_exclude);
+    for (int i = 0; i < 2 * cfg->n_ggl_exclude; i++) tomo.ggl_exclude[i] = cfg->ggl_exclude[i];
+    tomo.N_ggl_exclude = cfg->n_ggl_exclude;
+  }
+  /* samples */
+  redshift.shear_nbin = cfg->n_source;
+  redshift.shear_photoz = 4;
+  redshift.clustering_nbin = cfg->n_lens;
+  redshift.clustering_photoz = 4;
+  set_nz_table(1, src);
+  set_nz_table(0, lens);
+  /* init_ntomo_powerspectra */
+  tomo.shear_Npowerspectra = redshift.shear_nbin * (redshift.shear_nbin + 1) / 2;
+  int n = 0;
+  for (int i = 0; i < redshift.clustering_nbin; i++)
+    for (int j = 0; j < redshift.shear_nbin; j++) n += test_zoverlap(i, j);
+  tomo.ggl_Npowerspectra = n;
+  tomo.clustering_Npowerspectra = redshift.clustering_nbin;
+  return 0;
+}
+
+static double** table_kz(int nk, int nz, const double* log10k, const double* z,
+                         const double* lnP)
+{
+  double** t = alloc2(nk + 1, nz + 1);
+  for (int i = 0; i < nk; i++) t[i][nz] = log10k[i];
+  for (int j = 0; j < nz; j++) t[nk][j] = z[j];
+  for (int i = 0; i < nk; i++)
+    for (int j = 0; j < nz; j++) t[i][j] = lnP[i * nz + j];
+  return t;
+}
+
+int ref_set_point(const cl2pt_cosmo* c, const cl2pt_nuisance* nu)
+{
+  cosmology.Omega_m = c->omega_m;
+  cosmology.Omega_v = 1.0 - c->omega_m;
+  cosmology.Omega_nu = 0.1;
+  cosmology.h0 = c->h0;
+  cosmology.MGSigma = 0.0;
+  cosmology.MGmu = 0.0;
+  if (cosmology.chi) free(cosmology.chi);
+  cosmology.chi_nz = c->chi_nz;
+  cosmology.chi = alloc2(2, c->chi_nz);
+  for (int i = 0; i < c->chi_nz; i++) {
+    cosmology.chi[0][i] = c->chi_z[i];
+    cosmology.chi[1][i] = c->chi[i];
+  }
+  if (cosmology.G) free(cosmology.G);
+  cosmology.G_nz = c->G_nz;
+  cosmology.G = alloc2(2, c->G_nz);
+  for (int i = 0; i < c->G_nz; i++) {
+    cosmology.G[0][i] = c->G_z[i];
+    cosmology.G[1][i] = c->G[i];
+  }
+  if (cosmology.lnP) free(cosmology.lnP);
+  cosmology.lnP_nk = c->pk_nk;
+  cosmology.lnP_nz = c->pk_nz;
+  cosmology.lnP = table_kz(c->pk_nk, c->pk_nz, c->pk_log10k, c->pk_z, c->lnP);
+  if (cosmology.lnPL) free(cosmology.lnPL);
+  cosmology.lnPL_nk = c->pkl_nk;
+  cosmology.lnPL_nz = c->pkl_nz;
+  cosmology.lnPL = table_kz(c->pkl_nk, c->pkl_nz, c->pkl_log10k, c->pkl_z, c->lnPL);
+  cosmology.random = next_token();
+
+  for (int i = 0; i < CL2PT_MAX_BINS; i++) {
+    nuisance.photoz[0][0][i] = nu->src_dz[i];
+    nuisance.photoz[1][0][i] = nu->lens_dz[i];
+    nuisance.photoz[1][1][i] = nu->lens_stretch[i];
+    nuisance.shear_calibration_m[i] = nu->shear_m[i];
+    for (int k = 0; k < 6; k++) nuisance.gb[k][i] = nu->gb[k][i];
+    for (int k = 0; k < 3; k++) nuisance.ia[k][i] = nu->ia[k][i];
+  }
+  nuisance.c1rhocrit_ia = 0.01389;
+  if (nuisance.IA == IA_REDSHIFT_EVOLUTION) nuisance.oneplusz0_ia = 1.62;
+  nuisance.random_photoz_shear = next_token();
+  nuisance.random_photoz_clustering = next_token();
+  nuisance.random_ia = next_token();
+  nuisance.random_galaxy_bias = next_token();
+  return 0;
+}
+
+/* ---------------- thin accessors over the reference functions ------------- */
+double ref_nz_source(double z, int ni) { return nz_source_photoz(z, ni); }
+double ref_nz_lens(double z, int ni) { return nz_lens_photoz(z, ni); }
+double ref_zmean_lens(int ni) { return redshift.clustering_zdist_zmean[ni]; }
+double ref_g_tomo(double a, int ni) { return g_tomo(a, ni); }
+double ref_g_lens(double a, int ni) { return g_lens(a, ni); }
+double ref_chi(double a) { return chi(a); }
+double ref_a_chi(double c) { return a_chi(c); }
+double ref_growfac(double a) { return growfac(a); }
+double ref_f_growth(double z) { return f_growth(z); }
+double ref_p_nonlin(double k, double a) { return p_nonlin(k, a); }
+double ref_amin_lens(int ni) { return amin_lens(ni); }
+double ref_amax_lens(int ni) { return amax_lens(ni); }
+
+double ref_C_ss_nointerp(double l, int ni, int nj, int EE)
+{
+  return C_ss_tomo_limber_nointerp(l, ni, nj, EE, 0);
+}
+double ref_C_gs_nointerp(double l, int nl, int ns)
+{
+  return C_gs_tomo_limber_nointerp(l, nl, ns, 0);
+}
+double ref_C_gg_nointerp(double l, int ni, int use_linear_ps)
+{
+  return C_gg_tomo_limber_linpsopt_nointerp(l, ni, ni, use_linear_ps, 0);
+}
+double ref_C_ss_limber(double l, int ni, int nj, int EE)
+{
+  return C_ss_tomo_limber(l, ni, nj, EE);
+}
+double ref_C_gs_limber(double l, int nl, int ns) { return C_gs_tomo_limber(l, nl, ns); }
+double ref_C_gg_limber(double l, int ni) { return C_gg_tomo_limber(l, ni, ni); }
+
+int ref_xi_pm(double* xp, double* xm)
+{
+  const int nt = Ntable.Ntheta;
+  for (int p = 0; p < tomo.shear_Npowerspectra; p++)
+    for (int i = 0; i < nt; i++) {
+      xp[p * nt + i] = xi_pm_tomo(1, i, Z1(p), Z2(p), 1);
+      xm[p * nt + i] = xi_pm_tomo(-1, i, Z1(p), Z2(p), 1);
+    }
+  return 0;
+}
+
+int ref_w_gammat(double* out)
+{
+  const int nt = Ntable.Ntheta;
+  for (int p = 0; p < tomo.ggl_Npowerspectra; p++)
+    for (int i = 0; i < nt; i++) out[p * nt + i] = w_gammat_tomo(i, ZL(p), ZS(p), 1);
+  return 0;
+}
+
+int ref_w_gg(double* out)
+{
+  const int nt = Ntable.Ntheta;
+  for (int p = 0; p < tomo.clustering_Npowerspectra; p++)
+    for (int i = 0; i < nt; i++) out[p * nt + i] = w_gg_tomo(i, p, p, like.adopt_limber_gg);
+  return 0;
+}
+
+/* Cl[nl][lmax_nolimber] from the non-Limber FFTLog path */
+int ref_C_cl_tomo(double* out)
+{
+  const int nb = redshift.clustering_nbin;
+  const int L = limits.LMAX_NOLIMBER;
+  double** Cl = alloc2(nb, L + 1);
+  C_cl_tomo((double* const*)Cl, 0.01);
+  for (int i = 0; i < nb; i++)
+    for (int l = 0; l < L; l++) out[i * L + l] = Cl[i][l];
+  free(Cl);
+  return 0;
+}
+
+int ref_fpt_bias(double* out, int* n_out)
+{
+  get_FPT_bias();
+  *n_out = FPTbias.N;
+  if (out)
+    for (int r = 0; r < 8; r++)
+      for (int j = 0; j < FPTbias.N; j++) out[r * FPTbias.N + j] = FPTbias.tab[r][j];
+  return 0;
+}
+
+int ref_fpt_ia(double* out, int* n_out)
+{
+  get_FPT_IA();
+  *n_out = FPTIA.N;
+  if (out)
+    for (int r = 0; r < 12; r++)
+      for (int j = 0; j < FPTIA.N; j++) out[r * FPTIA.N + j] = FPTIA.tab[r][j];
+  return 0;
+}
+
+void ref_J_abl(const double* x, const double* fx, long N, const int* alpha,
+               const int* beta, const int* ell, int nterms, double nu,
+               double c_window, long npad, long nlow, long nhigh, double* Fy)
+{
+  fastpt_config cfg = {nu, c_window, npad, nlow, nhigh};
+  double** rows = (double**)malloc(sizeof(double*) * nterms);
+  int* isp = (int*)calloc(nterms, sizeof(int));
+  for (int i = 0; i < nterms; i++) rows[i] = Fy + (long)i * N;
+  J_abl(x, fx, N, alpha, beta, ell, isp, nterms, &cfg, rows);
+  free(rows);
+  free(isp);
+}
+
+void ref_J_abJ1J2Jk(const double* x, const double* fx, long N, const int* alpha,
+                    const int* beta, const int* J1, const int* J2, const int* Jk,
+                    int nterms, double nu, double c_window, long npad, long nlow,
+                    long nhigh, double* Fy)
+{
+  fastpt_config cfg = {nu, c_window, npad, nlow, nhigh};
+  double** rows = (double**)malloc(sizeof(double*) * nterms);
+  for (int i = 0; i < nterms; i++) rows[i] = Fy + (long)i * N;
+  J_abJ1J2Jk(x, fx, N, alpha, beta, J1, J2, Jk, nterms, &cfg, rows);
+  free(rows);
+}
+
+/* Real-space 3x2pt data vector in the order xi+, xi-, gamma_t, w (ord =
+ * 0,1,2), masked, with shear calibration and the gamma_t point-mass term
+ * (pm[zl]; all zero reproduces a run without point masses). */
+int ref_data_vector_real(const int* mask, const double* pm, double* dv)
+{
+  const int nt = Ntable.Ntheta;
+  const int nss = tomo.shear_Npowerspectra;
+  const int ngs = tomo.ggl_Npowerspectra;
+  const int ngg = tomo.clustering_Npowerspectra;
+  const int s0 = 0, s1 = 2 * nt * nss, s2 = s1 + nt * ngs;
+  const int ntot = s2 + nt * ngg;
+  for (int i = 0; i < ntot; i++) dv[i] = 0.0;
+  const double logvtmin = log(Ntable.vtmin);
+  const double logdt = (log(Ntable.vtmax) - logvtmin) / nt;
+  if (like.shear_shear) {
+    for (int p = 0; p < nss; p++) {
+      const int z1 = Z1(p), z2 = Z2(p);
+      const double m = (1.0 + nuisance.shear_calibration_m[z1]) *
+                       (1.0 + nuisance.shear_calibration_m[z2]);
+      for (int i = 0; i < nt; i++) {
+        int idx = s0 + nt * p + i;
+        if (mask[idx]) dv[idx] = xi_pm_tomo(1, i, z1, z2, 1) * m;
+        idx += nt * nss;
+        if (mask[idx]) dv[idx] = xi_pm_tomo(-1, i, z1, z2, 1) * m;
+      }
+    }
+  }
+  if (like.shear_pos) {
+    for (int p = 0; p < ngs; p++) {
+      const int zl = ZL(p), zs = ZS(p);
+      for (int i = 0; i < nt; i++) {
+        const int idx = s1 + nt * p + i;
+        if (!mask[idx]) continue;
+        double v = w_gammat_tomo(i, zl, zs, 1);
+        if (pm) {
+          const double tmin = exp(logvtmin + i * logdt);
+          const double tmax = exp(logvtmin + (i + 1.0) * logdt);
+          const double theta = (2. / 3.) * (pow(tmax, 3) - pow(tmin, 3)) /
+                               (tmax * tmax - tmin * tmin);
+          const double a_lens = 1.0 / (1.0 + zmean(zl));
+          const double chi_lens = chi(a_lens);
+          v += 4 * M_PI * 1.6e-23 * pm[zl] * 1.e+13 * g_tomo(a_lens, zs) /
+               (theta * theta) / (chi_lens * a_lens * a_lens * a_lens);
+        }
+        dv[idx] = v * (1.0 + nuisance.shear_calibration_m[zs]);
+      }
+    }
+  }
+  if (like.pos_pos) {
+    for (int p = 0; p < ngg; p++)
+      for (int i = 0; i < nt; i++) {
+        const int idx = s2 + nt * p + i;
+        if (mask[idx]) dv[idx] = w_gg_tomo(i, p, p, like.adopt_limber_gg);
+      }
+  }
+  return ntot;
+}
+
+/* ---- link stubs for symbols only referenced off the hot path ---------- */
+#include "baryons.h"
+barypara bary = {0};
+static void off_path(const char* f)
+{
+  fprintf(stderr, "reference harness: %s is outside the oracle's scope\n", f);
+  abort();
+}
+double p_mm(const double k, const double a) { (void)k; (void)a; off_path("p_mm"); return 0; }
+double p_gm(const double k, const double a, const int ni) { (void)k; (void)a; (void)ni; off_path("p_gm"); return 0; }
+double p_gg(const double k, const double a, const int ni, const int nj) { (void)k; (void)a; (void)ni; (void)nj; off_path("p_gg"); return 0; }
+double p_my(const double k, const double a) { (void)k; (void)a; off_path("p_my"); return 0; }
+double p_yy(const double k, const double a) { (void)k; (void)a; off_path("p_yy"); return 0; }
