@@ -1,0 +1,319 @@
+"""Benchmark: batched real-space 3x2pt data vectors per second on GB300.
+
+Workload (the real_3x2pt configuration): 10 source + 5 lens bins, 55 xi+/xi-
++ 50 gamma_t + 5 w(theta) spectra on 20 log theta bins in 2.5-250 arcmin,
+Legendre sums to l = 50000 from 1000 log-spaced C_l nodes, 600 x 200
+P(k, z) table per point, non-Limber w(theta) (the reference default), one
+step = one batch of `--batch` distinct parameter points (each with its own
+P(k,z), distances, growth and nuisances), synthetic inputs.
+
+`value`: data vectors/s with inputs resident in HBM (torch CUDA tensors,
+one CUDA-event-timed region over --steps batches); the inputs of one batch
+(~1 MB of FP64 P(k,z) per point) exceed the 129 MB L2, so no flush is
+needed.  `e2e`: the same metric through the public C-ABI call with host
+(pinned) buffers, host->device copies of every input and device->host of
+the data vectors inside the timed region.  Per-kernel durations come from
+CUDA events the library records around each launch during the timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
+
+METRIC = "3x2pt data vectors/s (real-space, <=1e-4 rel err vs FP64)"
+UNIT = "data vectors/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling in the background during the timed region."""
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_batch(w, B, seed):
+    from cl2pt import abi, workloads
+    tabs, nus = workloads.points(w, B, seed=seed)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    nub = np.frombuffer(b"".join(bytes(n) for n in nus), dtype=np.uint8).copy()
+    return dict(om=om, h0=h0, chi=chi, G=G, lnP=lnP, nus=nus, nub=nub, tabs=tabs)
+
+
+def cpu_sample(w, data, budget_s=12.0, min_pts=2, threads=None):
+    """Time the oracle port (the reference algorithm restated in C, OpenMP
+    over all host cores) on consecutive points of the same batch."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.set_point(data["tabs"][n % len(data["tabs"])], data["nus"][n % len(data["nus"])])
+        o.data_vector_real()
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= budget_s and n >= min_pts) or n >= 200:
+            break
+    return n, el
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(ref=False)
+    from cl2pt import workloads
+    w = workloads.make(args.workload)
+    data = make_batch(w, 8, seed=1)
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    for _ in range(args.warmup):
+        cpu_sample(w, data, budget_s=0.0, min_pts=1)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, t = cpu_sample(w, data, budget_s=2.0, min_pts=2)
+        tot_n += n
+        tot_t += t
+    v = tot_n / tot_t
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (EH no-wiggle P(k,z), LCDM chi/D, seeded n(z) and nuisances)",
+        "config": {"workload": args.workload, "points_per_step": tot_n / args.steps},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{tot_n} points over {args.steps} steps"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--workload", default="real_3x2pt")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cl2pt import lib, workloads
+    from cl2pt import build as cbuild
+    cbuild.build()
+    w = workloads.make(args.workload)
+    B = args.batch
+    data = make_batch(w, B, seed=100 + rank)  # replicas: each rank its own walkers
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=B)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_om, d_h0, d_chi, d_G, d_lnP = (T(data[k]) for k in ("om", "h0", "chi", "G", "lnP"))
+    d_nu = T(data["nub"])
+    out = torch.empty((B, plan.n_total), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step(p=plan, o=out):
+        p.eval_real_device(d_om, d_h0, d_chi, d_G, d_lnP, d_nu, o, stream=sptr)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    plan.check_errors(sptr)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    plan.set_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    kms, kl = plan.kernel_times()
+    plan.set_timing(False)
+    plan.check_errors(sptr)
+    launches = plan.launches() * args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * B * args.steps / (ms / 1e3)
+
+    # ---- e2e through the C ABI with pinned host buffers
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h = {k: pin(data[k]) for k in ("om", "h0", "chi", "G", "lnP")}
+    for _ in range(2):
+        plan.eval_real(h["om"], h["h0"], h["chi"], h["G"], h["lnP"], data["nus"])
+    torch.cuda.synchronize()
+    barrier()
+    e2e_steps = max(2, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dv_host = plan.eval_real(h["om"], h["h0"], h["chi"], h["G"], h["lnP"], data["nus"])
+    te = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([te], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        te = float(t.item())
+    e2e = world * B * e2e_steps / te
+    h2d = sum(h[k].nbytes for k in h) + B * 13 * 20 * 8
+    d2h = dv_host.nbytes
+
+    # ---- plain FP64 GPU form of the same pipeline
+    fp64 = None
+    if not args.no_fp64:
+        p64 = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=B)
+        o64 = torch.empty_like(out)
+        for _ in range(3):
+            step(p64, o64)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n64 = max(2, args.steps // 2)
+        a.record(stream)
+        for _ in range(n64):
+            step(p64, o64)
+        b.record(stream)
+        torch.cuda.synchronize()
+        fp64 = B * n64 / (a.elapsed_time(b) / 1e3)
+        p64.close()
+
+    # ---- roofline of the dominant kernel
+    hbm, src = peaks()
+    top = max(kms, key=lambda k: kms[k])
+    per_launch_ms = kms[top] / max(kl[top], 1)
+    nk, nz = plan.shapes["nk"], plan.shapes["nz"]
+    pss, pgs, pgg = plan.n_xi // (2 * w.cfg.ntheta), plan.n_gammat // w.cfg.ntheta, w.cfg.n_lens
+    nnode = w.cfg.lmin_tab - 1 + w.cfg.n_ell
+    # algorithmic bytes per point for each kernel (roofline rules)
+    per_point = {
+        "k_limber_ss": 8 * nk * nz + 8 * pss * nnode,
+        "k_limber_gs": 8 * nk * nz + 8 * pgs * nnode,
+        "k_limber_gg": 8 * nk * nz + 8 * pgg * nnode,
+        "k_limber_ggl": 8 * nk * nz + 16 * pgg * w.cfg.lmax_nolimber,
+        "k_nonlimber": 8 * (plan.shapes["chi"] + plan.shapes["G"]) + 8 * pgg * w.cfg.lmax_nolimber,
+        "k_contract": 8 * (pss + pgs + pgg) * nnode + 8 * plan.n_total,
+        "k_gtab": 8 * plan.shapes["chi"] + 8 * w.cfg.n_source * w.cfg.n_a,
+        "k_nodes": 8 * (plan.shapes["chi"] + plan.shapes["G"]),
+        "k_assemble": 16 * plan.n_total,
+    }
+    pts_per_launch = min(B, 256)
+    alg = per_point[top] * pts_per_launch
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (EH no-wiggle P(k,z) per point, LCDM chi/D, seeded n(z) and nuisances)",
+        "config": {"workload": args.workload, "points_per_step_per_gpu": B,
+                   "n_data": plan.n_total, "lmax": w.cfg.lmax, "n_ell": w.cfg.n_ell,
+                   "pk_table": [nk, nz], "l2": "inputs > L2 (no flush)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_source": src},
+        "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items()},
+        "clocks": clocks,
+        "fp64_plain_gpu": {"value": fp64, "unit": UNIT,
+                           "speedup_of_mixed": (value / world) / fp64 if fp64 else None},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        n, t = cpu_sample(w, data, budget_s=12.0)
+        line["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": f"{n} points of the same batch, {t:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line))
+    plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+"""ctypes binding of libcl2pt.so (the C ABI in include/cl2pt.h).
+
+The library is the only compute path: if it is missing or fails to load,
+every entry point raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcl2pt.so")
+
+PREC_MIXED, PREC_FP64 = 0, 1
+# kernel ids of cl2pt_kernel_times (CL2PT_K_* in include/cl2pt.h)
+KERNELS = ["k_gtab", "k_nodes", "k_limber_ss", "k_limber_gs", "k_limber_gg", "k_limber_ggl",
+           "k_nonlimber", "k_contract", "k_assemble"]
+HOST, DEVICE = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("chi_nz", C.c_int), ("chi_z", _dp), ("G_nz", C.c_int), ("G_z", _dp),
+        ("pk_nk", C.c_int), ("pk_nz", C.c_int), ("pk_log10k", _dp), ("pk_z", _dp),
+        ("pkl_nk", C.c_int), ("pkl_nz", C.c_int), ("pkl_log10k", _dp), ("pkl_z", _dp),
+    ]
+
+
+class Batch(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("where", C.c_int), ("omega_m", _dp), ("h0", _dp), ("chi", _dp),
+        ("G", _dp), ("lnP", _dp), ("lnPL", _dp), ("nuisance", C.POINTER(abi.Nuisance)),
+    ]
+
+
+class CL2PTError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libcl2pt.so once (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CL2PTError(f"{path} is missing: build it with cl2pt.build.build()")
+    lib = C.CDLL(path)
+    lib.cl2pt_plan_create.argtypes = [C.POINTER(abi.Config), C.POINTER(abi.NZ), C.POINTER(abi.NZ),
+                                      C.POINTER(Grid), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+    lib.cl2pt_plan_destroy.argtypes = [C.c_void_p]
+    lib.cl2pt_real_sizes.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
+    lib.cl2pt_eval_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]
+    lib.cl2pt_check_errors.argtypes = [C.c_void_p, C.c_void_p]
+    lib.cl2pt_debug_limber_tables.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
+    lib.cl2pt_debug_nonlimber.argtypes = [C.c_void_p, C.c_int, _dp, _ip]
+    lib.cl2pt_debug_g_tables.argtypes = [C.c_void_p, C.c_int, _dp]
+    lib.cl2pt_last_launch_count.argtypes = [C.c_void_p]
+    lib.cl2pt_set_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.cl2pt_kernel_times.argtypes = [C.c_void_p, _dp, _ip]
+    lib.cl2pt_status_string.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def check(st: int, what: str = "cl2pt"):
+    if st != 0:
+        msg = load().cl2pt_status_string(st).decode()
+        raise CL2PTError(f"{what}: status {st} ({msg})")
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+class Plan:
+    """A cl2pt plan: geometry, redshift samples, shared axes and workspace."""
+
+    def __init__(self, cfg: abi.Config, src_table, lens_table, tables, precision=PREC_MIXED,
+                 max_batch=1):
+        lib = load()
+        self.cfg = cfg
+        self._src = abi.make_nz(src_table)
+        self._lens = abi.make_nz(lens_table)
+        ax = [np.ascontiguousarray(np.asarray(a, dtype=np.float64)) for a in
+              (tables.chi_z, tables.G_z, tables.log10k, tables.pk_z)]
+        self._axes = ax
+        g = Grid()
+        g.chi_nz, g.chi_z = len(ax[0]), _p(ax[0])
+        g.G_nz, g.G_z = len(ax[1]), _p(ax[1])
+        g.pk_nk, g.pk_nz, g.pk_log10k, g.pk_z = len(ax[2]), len(ax[3]), _p(ax[2]), _p(ax[3])
+        g.pkl_nk = 0
+        self.grid = g
+        self.shapes = dict(chi=len(ax[0]), G=len(ax[1]), nk=len(ax[2]), nz=len(ax[3]))
+        h = C.c_void_p()
+        check(lib.cl2pt_plan_create(C.byref(cfg), C.byref(self._src.struct),
+                                    C.byref(self._lens.struct), C.byref(g), precision, max_batch,
+                                    C.byref(h)), "cl2pt_plan_create")
+        self.h = h
+        self.max_batch = max_batch
+        sz = [C.c_int() for _ in range(4)]
+        check(lib.cl2pt_real_sizes(h, *[C.byref(s) for s in sz]))
+        self.n_xi, self.n_gammat, self.n_w, self.n_total = (s.value for s in sz)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cl2pt_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- host
+    def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None):
+        """Host arrays in, host data vectors out ([n][n_total])."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        hh = np.ascontiguousarray(h0, dtype=np.float64)
+        ch = np.ascontiguousarray(chi, dtype=np.float64)
+        gg = np.ascontiguousarray(G, dtype=np.float64)
+        lp = np.ascontiguousarray(lnP, dtype=np.float64)
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), _p(hh), _p(ch), _p(gg), _p(lp)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        out = np.zeros((n, self.n_total))
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
+        check(load().cl2pt_eval_real(self.h, C.byref(b),
+                                     mk.ctypes.data if mk is not None else None,
+                                     pmm.ctypes.data if pmm is not None else None,
+                                     out.ctypes.data, None), "cl2pt_eval_real")
+        return out
+
+    # ------------------------------------------------------------ device
+    def eval_real_device(self, omega_m, h0, chi, G, lnP, nuisance, out, mask=None, pm=None,
+                         lnPL=None, stream=None):
+        """torch CUDA tensors in and out (float64, contiguous); nuisance is
+        a uint8 CUDA tensor holding n packed cl2pt_nuisance structs."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        st = load().cl2pt_eval_real(self.h, C.byref(b),
+                                    None if mask is None else mask.data_ptr(),
+                                    None if pm is None else pm.data_ptr(),
+                                    out.data_ptr(), stream)
+        check(st, "cl2pt_eval_real")
+
+    def check_errors(self, stream=None):
+        check(load().cl2pt_check_errors(self.h, stream), "device check")
+
+    def set_timing(self, on: bool):
+        check(load().cl2pt_set_timing(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        """(ms per kernel id, launches per kernel id) since the last call."""
+        ms = np.zeros(len(KERNELS))
+        n = np.zeros(len(KERNELS), dtype=np.int32)
+        check(load().cl2pt_kernel_times(self.h, _p(ms), n.ctypes.data_as(_ip)))
+        return dict(zip(KERNELS, ms)), dict(zip(KERNELS, n.tolist()))
+
+    def launches(self) -> int:
+        return load().cl2pt_last_launch_count(self.h)
+
+    # ------------------------------------------------------------- debug
+    def limber_tables(self, point=0):
+        pss, pgs, pgg = abi.n_pairs(self.cfg)
+        nn = self.cfg.lmin_tab - 1 + self.cfg.n_ell
+        ss = np.zeros(pss * nn)
+        gs = np.zeros(max(pgs, 1) * nn)
+        gg = np.zeros(pgg * nn)
+        check(load().cl2pt_debug_limber_tables(self.h, point, _p(ss), _p(gs), _p(gg)))
+        return ss.reshape(pss, nn), gs[: pgs * nn].reshape(pgs, nn), gg.reshape(pgg, nn)
+
+    def nonlimber(self, point=0):
+        nl, L = self.cfg.n_lens, self.cfg.lmax_nolimber
+        cl = np.zeros(nl * L)
+        conv = np.zeros(nl, dtype=np.int32)
+        check(load().cl2pt_debug_nonlimber(self.h, point, _p(cl), conv.ctypes.data_as(_ip)))
+        return cl.reshape(nl, L), conv
+
+    def g_tables(self, point=0):
+        out = np.zeros(self.cfg.n_source * self.cfg.n_a)
+        check(load().cl2pt_debug_g_tables(self.h, point, _p(out)))
+        return out.reshape(self.cfg.n_source, self.cfg.n_a)

@@ -1,0 +1,98 @@
+"""Named 2-point workloads with seeded synthetic inputs.
+
+  cosmic_shear_fourier   5 source bins -> 15 shear spectra at 20 log-spaced
+                         l in 20-3000; P(k,z) 400 x 100
+  real_3x2pt             10 source + 5 lens bins -> 55 xi+/xi-, 50 gamma_t,
+                         5 w(theta) spectra on 20 log theta bins in
+                         2.5-250 arcmin, Legendre sums to l = 50000 from
+                         1000 log-spaced C_l nodes; P(k,z) 600 x 200;
+                         b1 ~ U(1.2, 2.2); non-Limber w(theta)
+  real_3x2pt_small       a reduced real_3x2pt (4 + 3 bins, 10 theta bins,
+                         l <= 5000, 200 nodes) for fast checks
+
+Per-point variation: every walker gets its own P(k,z) amplitude/tilt,
+source photo-z shifts N(0, 0.02), shear calibration N(0, 0.01) and lens
+biases, so each point carries distinct tables and nuisances.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import abi, synthetic
+
+SEED0 = 20261203
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    cfg: abi.Config
+    src: np.ndarray
+    lens: np.ndarray
+    base: synthetic.CosmoTables
+    ell: np.ndarray | None = None  # Fourier multipoles
+
+
+def _fourier_ells(nell, lmin, lmax):
+    # init_binning_fourier (generic_interface.cpp:448-456)
+    logdl = (np.log(lmax) - np.log(lmin)) / nell
+    return np.exp(np.log(lmin) + (np.arange(nell) + 0.5) * logdl)
+
+
+def make(name: str) -> Workload:
+    if name == "cosmic_shear_fourier":
+        cfg = abi.make_config(n_source=5, n_lens=1, probes=abi.PROBE_XI)
+        base = synthetic.make_cosmo_tables(nk=400, nz=100)
+        return Workload(name, cfg, synthetic.source_nz(5), synthetic.lens_nz(1), base,
+                        _fourier_ells(20, 20.0, 3000.0))
+    if name == "real_3x2pt":
+        cfg = abi.make_config(n_source=10, n_lens=5, ntheta=20, theta_min=2.5,
+                              theta_max=250.0, lmax=50000, n_ell=1000)
+        base = synthetic.make_cosmo_tables(nk=600, nz=200)
+        return Workload(name, cfg, synthetic.source_nz(10), synthetic.lens_nz(5), base)
+    if name == "real_3x2pt_limber":
+        w = make("real_3x2pt")
+        w.cfg.adopt_limber_gg = 1
+        w.name = name
+        return w
+    if name == "real_3x2pt_small":
+        cfg = abi.make_config(n_source=4, n_lens=3, ntheta=10, theta_min=2.5,
+                              theta_max=250.0, lmax=5000, n_ell=200)
+        base = synthetic.make_cosmo_tables(nk=400, nz=100)
+        return Workload(name, cfg, synthetic.source_nz(4), synthetic.lens_nz(3), base)
+    if name == "real_3x2pt_small_limber":
+        w = make("real_3x2pt_small")
+        w.cfg.adopt_limber_gg = 1
+        w.name = name
+        return w
+    raise KeyError(name)
+
+
+def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True):
+    """n parameter points: (list of CosmoTables, list of abi.Nuisance)."""
+    rng = np.random.default_rng(SEED0 + seed)
+    ns, nl = w.cfg.n_source, w.cfg.n_lens
+    tabs, nus = [], []
+    for _ in range(n):
+        t = synthetic.perturb_tables(w.base, rng) if vary_cosmo else w.base
+        nu = abi.make_nuisance(
+            src_dz=rng.normal(0.0, 0.02, ns),
+            lens_dz=rng.normal(0.0, 0.005, nl),
+            shear_m=rng.normal(0.0, 0.01, ns),
+            b1=rng.uniform(1.2, 2.2, nl),
+        )
+        tabs.append(t)
+        nus.append(nu)
+    return tabs, nus
+
+
+def stack(tabs):
+    """Per-point arrays of a batch: omega_m, h0, chi, G, lnP (numpy)."""
+    om = np.array([t.omega_m for t in tabs])
+    h0 = np.array([t.h0 for t in tabs])
+    chi = np.stack([t.chi for t in tabs])
+    G = np.stack([t.G for t in tabs])
+    lnP = np.stack([t.lnP.reshape(-1) for t in tabs])
+    return om, h0, chi, G, lnP

@@ -1,0 +1,235 @@
+// common.cuh -- device-side data layout and FP64 lookup helpers shared by
+// the cl2pt kernels.  The helpers restate the reference's table lookups
+// exactly (same bracketing search, same interpolation formulas), since
+// the data vector must match the reference to 1e-4.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cl2pt.h"
+
+#define CL2PT_COVERH0 2997.92458
+#define CL2PT_MAXB CL2PT_MAX_BINS
+
+namespace cl2pt {
+
+// Number of 1-D node sets of one point: ss (shared by all source bins),
+// gs per lens bin, gg per lens bin.
+struct NodeSet {
+  double* a;
+  double* wt;
+  double* fK;      // chi / (c/H0)
+  double* dchida;
+  double* D;       // growth
+  double* H;       // H/H0
+  int* jz;         // P-table z cell
+  double* dyz;     // z fraction inside the cell
+};
+
+// Everything a kernel needs, by value (device pointers only).
+struct Params {
+  // configuration scalars (cl2pt_config)
+  int ns, nl, ntheta, lmax, n_ell, hdi, lmin_tab, lmax_nolimber, nl_nchi;
+  double a_min, theta_min_rad, theta_max_rad;
+  int adopt_limber_gg, ia_model, ia_mode, linear_pk, probes;
+  int bias_model[6];
+  int prec;            // CL2PT_PREC_*
+  int B;               // points in this wave
+  int pss, pgs, pgg;
+  int n_a;             // lens-efficiency table length
+  int n_ss, n_gg;      // GL nodes of the ss/gs and gg integrals
+  int nnode_ss, nnode_g;    // C_l nodes: (lmin_tab-1) integer + n_ell log nodes
+  int nint;                 // integer multipoles below lmin_tab (lmin_tab-1)
+  double lim_ss[3], lim_g[3];
+  // shared axes
+  int chi_nz, G_nz, pk_nk, pk_nz, pkl_nk, pkl_nz;
+  const double *chi_z, *G_z, *pk_lk, *pk_z, *pkl_lk, *pkl_z;
+  double pk_lk0, pk_dlk;   // uniform-grid description when pk_uniform
+  int pk_uniform;
+  // n(z) splines: zc [nz], y/c [(ntomo+1)][nz]
+  int src_nz, lens_nz;
+  const double *src_zc, *src_y, *src_c, *lens_zc, *lens_y, *lens_c;
+  double src_zmin_all, src_zmax_all, lens_zmax_all;
+  double lens_zmin[CL2PT_MAXB], lens_zmax[CL2PT_MAXB], zmean_lens[CL2PT_MAXB];
+  // quadrature rules on [-1, 1]
+  const double *gl_ss_x, *gl_ss_w, *gl_gg_x, *gl_gg_w;
+  // pair maps (device): z1, z2 [pss]; zl, zs [pgs]
+  const int *z1, *z2, *zl, *zs;
+  // per-point inputs (device), strided by point
+  const double* omega_m;
+  const double* h0;
+  const double* chi;        // [B][chi_nz]
+  const double* G;          // [B][G_nz]
+  const double* lnP;        // [B][pk_nk*pk_nz]
+  const double* lnPL;       // [B][pkl_nk*pkl_nz]
+  const cl2pt_nuisance* nu; // [B]
+  // workspace (device), strided by point
+  double* gsrc;             // [B][ns][n_a]
+  double* glens;            // [B][nl][n_a]
+  double* node;             // [B][NODE_FIELDS][node_stride]
+  int* node_j;              // [B][node_stride]
+  int node_stride;          // n_ss + nl*n_ss + nl*n_gg
+  double* wss;              // [B][ns][n_ss]   (WK - WS C1) at ss nodes
+  double* wgs_x;            // [B][nl][ns][n_ss] (WK - WS C1) at gs nodes
+  double* wgs_l;            // [B][nl][n_ss]   WGAL b1
+  double* wgs_m;            // [B][nl][n_ss]   WMAG bmag
+  double* wgg_l;            // [B][nl][n_gg]   WGAL b1
+  double* wgg_m;            // [B][nl][n_gg]   WMAG bmag
+  double* wgg_r0;           // [B][nl][n_gg]   n H f at a0 (RSD term 0)
+  double* chi_amin;         // [B] chi(a_min)
+  double* tab_ss;           // [B][pss][nnode_ss]
+  double* tab_gs;           // [B][pgs][nnode_g]
+  double* tab_gg;           // [B][nl][nnode_g]
+  double* ggl;              // [B][nl][lmax_nolimber][2]  Limber (nonlin, lin) at integer l
+  double* cnl;              // [B][nl][lmax_nolimber]
+  int* conv_l;              // [B][nl]
+  double* obs;              // [B][n_total]  xi+, xi-, gamma_t, w
+  int* err;                 // device error flag
+};
+
+enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };
+
+// ---------------------------------------------------------------------
+// FP64 lookups (restating cosmolike/cosmo3D.c and redshift_spline.c)
+// ---------------------------------------------------------------------
+// Bracketing search used by every reference table lookup: largest i with
+// x[i] <= v, clamped to [0, n-2] (cosmo3D.c:45-56).
+__device__ __forceinline__ int bsearch_d(const double* __restrict__ x, int n, double v)
+{
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+struct Chis { double chi, dchida; };
+
+// chi_all: cosmo3D.c:40-92.  The derivative's upper difference reads
+// entry j+2; it is clamped to the table end (inputs keep every query out
+// of the last interval, where the reference would read past the table).
+__device__ __forceinline__ Chis chi_all_d(const double* __restrict__ Z,
+                                         const double* __restrict__ X, int n, double a)
+{
+  const double z = 1.0 / a - 1.0;
+  const int j = bsearch_d(Z, n, z);
+  const double dy = (z - Z[j]) / (Z[j + 1] - Z[j]);
+  const double c0 = X[j] + dy * (X[j + 1] - X[j]);
+  const int j2 = (j + 2 < n) ? j + 2 : n - 1;
+  const double up = (X[j2] - X[j]) / (Z[j2] - Z[j]);
+  const double down = (j > 0) ? (X[j + 1] - X[j - 1]) / (Z[j + 1] - Z[j - 1])
+                              : (X[j + 1] - X[j]) / (Z[j + 1] - Z[j]);
+  double d = down + dy * (up - down);
+  d = d / CL2PT_COVERH0;
+  d = d / (a * a);
+  Chis r;
+  r.chi = c0 / CL2PT_COVERH0;
+  r.dchida = d;
+  return r;
+}
+
+// a_chi: cosmo3D.c:109-133
+__device__ __forceinline__ double a_chi_d(const double* __restrict__ Z,
+                                          const double* __restrict__ X, int n, double io_chi)
+{
+  const double c = io_chi * CL2PT_COVERH0;
+  const int j = bsearch_d(X, n, c);
+  const double dy = (c - X[j]) / (X[j + 1] - X[j]);
+  const double z = Z[j] + dy * (Z[j + 1] - Z[j]);
+  return 1.0 / (1.0 + z);
+}
+
+__device__ __forceinline__ double G_at_d(const double* __restrict__ Z,
+                                         const double* __restrict__ Gv, int n, double z,
+                                         double* slope)
+{
+  const int j = bsearch_d(Z, n, z);
+  const double dy = (z - Z[j]) / (Z[j + 1] - Z[j]);
+  if (slope) *slope = (Gv[j + 1] - Gv[j]) / (Z[j + 1] - Z[j]);
+  return Gv[j] + dy * (Gv[j + 1] - Gv[j]);
+}
+
+// norm_growfac(a, true): cosmo3D.c:148-198 (g1 = G at z = 0 passed in)
+__device__ __forceinline__ double growfac_d(const double* Z, const double* Gv, int n,
+                                            double g1, double a)
+{
+  const double z = 1.0 / a - 1.0;
+  return (G_at_d(Z, Gv, n, z, nullptr) * a) / g1;
+}
+
+// f_growth: cosmo3D.c:200-228
+__device__ __forceinline__ double f_growth_d(const double* Z, const double* Gv, int n, double z)
+{
+  double s;
+  const double G = G_at_d(Z, Gv, n, z, &s);
+  const double dlnGdlnz = s * z / G;
+  const double dlnGdlna = -dlnGdlnz * (1 + z) / z;
+  return 1 + dlnGdlna;
+}
+
+// natural cubic spline evaluation on nodes zc (the n(z) splines)
+__device__ __forceinline__ double spline_d(const double* __restrict__ x,
+                                           const double* __restrict__ y,
+                                           const double* __restrict__ c, int n, double v)
+{
+  const int i = bsearch_d(x, n, v);
+  const double h = x[i + 1] - x[i];
+  const double dy = y[i + 1] - y[i];
+  const double t = v - x[i];
+  const double ci = c[i], ci1 = c[i + 1];
+  const double b = dy / h - h * (ci1 + 2.0 * ci) / 3.0;
+  const double d = (ci1 - ci) / (3.0 * h);
+  return y[i] + t * (b + t * (ci + t * d));
+}
+
+// nz_source_photoz evaluation: redshift_spline.c:523-536
+__device__ __forceinline__ double nz_source_d(const Params& P, double zz, int nj, double dz)
+{
+  zz = zz - dz;
+  if (zz < P.src_zc[0] || zz > P.src_zc[P.src_nz - 1]) return 0.0;
+  return spline_d(P.src_zc, P.src_y + (nj + 1) * P.src_nz, P.src_c + (nj + 1) * P.src_nz,
+                  P.src_nz, zz);
+}
+
+// nz_lens_photoz evaluation: redshift_spline.c:740-760
+__device__ __forceinline__ double nz_lens_d(const Params& P, double zz, int nj, double dz,
+                                            double stretch)
+{
+  const double zm = P.zmean_lens[nj];
+  zz = (zz - dz - zm) / stretch + zm;
+  if (zz <= P.lens_zc[0] || zz >= P.lens_zc[P.lens_nz - 1]) return 0.0;
+  const double r = spline_d(P.lens_zc, P.lens_y + (nj + 1) * P.lens_nz,
+                            P.lens_c + (nj + 1) * P.lens_nz, P.lens_nz, zz);
+  return r / stretch;
+}
+
+// interpol1d: basics.c:457-480 (constant extrapolation)
+__device__ __forceinline__ double interpol1d_d(const double* f, int n, double a,
+                                               double dx, double x)
+{
+  if (x < a) return f[0];
+  const double r = (x - a) / dx;
+  const int i = (int)floor(r);
+  if (i + 1 >= n) return f[n - 1];
+  return (r - i) * (f[i + 1] - f[i]) + f[i];
+}
+
+// p_lin / p_nonlin: cosmo3D.c:306-417, FP64
+__device__ __forceinline__ double pk_d(const double* __restrict__ lk, int nk,
+                                       const double* __restrict__ zz, int nz,
+                                       const double* __restrict__ lnP, double k, double a)
+{
+  const double log10k = log10(k / CL2PT_COVERH0);
+  const double z = 1.0 / a - 1.0;
+  const int i = bsearch_d(lk, nk, log10k);
+  const int j = bsearch_d(zz, nz, z);
+  const double dx = (log10k - lk[i]) / (lk[i + 1] - lk[i]);
+  const double dy = (z - zz[j]) / (zz[j + 1] - zz[j]);
+  const double v = (1 - dx) * (1 - dy) * lnP[i * nz + j] + (1 - dx) * dy * lnP[i * nz + j + 1] +
+                   dx * (1 - dy) * lnP[(i + 1) * nz + j] + dx * dy * lnP[(i + 1) * nz + j + 1];
+  return exp(v) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
+}
+
+}  // namespace cl2pt

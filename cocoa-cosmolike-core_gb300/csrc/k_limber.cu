@@ -1,0 +1,364 @@
+// k_limber.cu -- Limber C_l tables on the C_l nodes.
+//
+// The reference tabulates C_l^{ss,gs,gg} on N_ell log-spaced multipoles
+// and evaluates l < LMIN_tab directly, each as a fixed Gauss-Legendre sum
+// in a over the same nodes (cosmo2D.c:1617-1778, 2195-2392, 2693-2761,
+// 1562-1604, 2125-2182, 2614-2666).  Per point, the integrand factorises
+// into an l-dependent table walk P(k = (l+1/2)/chi_p, z_p) and node weights
+// that do not depend on l, so one CTA handles a tile of LT multipoles of
+// one point:
+//   phase 1  each thread walks the P(k, z) table for its multipole at
+//            every node of a chunk (FP32 in the mixed plan, FP64 in the
+//            FP64 plan) into shared memory;
+//   phase 2  each thread contracts its column with the per-pair node
+//            weights held in shared memory (broadcast reads).
+// gg carries the l-dependent redshift-space term W_RSD (evaluated at
+// a_chi((l+3/2)/k)), so it is summed node by node instead.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cl2pt {
+
+constexpr int LT = 128;   // multipoles per CTA
+constexpr int PCH = 64;   // quadrature nodes per shared-memory chunk
+
+template <typename T> __device__ __forceinline__ T exp_t(T x);
+template <> __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
+template <typename T> __device__ __forceinline__ T log10_t(T x);
+template <> __device__ __forceinline__ float log10_t<float>(float x) { return log10f(x); }
+template <> __device__ __forceinline__ double log10_t<double>(double x) { return log10(x); }
+
+template <typename T>
+__device__ __forceinline__ int bsearch_t(const T* __restrict__ x, int n, T v)
+{
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// Bilinear lnP walk (p_nonlin / p_lin, cosmo3D.c:306-417) at log10(k)
+// given the z cell (j, dy) of the node; lk: log10 k axis in shared memory.
+template <typename T>
+__device__ __forceinline__ T pk_walk(const T* __restrict__ lk, int nk,
+                                     const double* __restrict__ tab, int nz, T log10k, int j,
+                                     T dy)
+{
+  const int i = bsearch_t(lk, nk, log10k);
+  const T dx = (log10k - lk[i]) / (lk[i + 1] - lk[i]);
+  const double* r0 = tab + (size_t)i * nz + j;
+  const double* r1 = r0 + nz;
+  const T v00 = (T)__ldg(r0), v01 = (T)__ldg(r0 + 1), v10 = (T)__ldg(r1), v11 = (T)__ldg(r1 + 1);
+  const T v = (1 - dx) * (1 - dy) * v00 + (1 - dx) * dy * v01 + dx * (1 - dy) * v10 + dx * dy * v11;
+  return exp_t<T>(v) * (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
+struct PdeltaTable {
+  const double* tab;
+  const double* lk;
+  const double* z;
+  int nk, nz;
+};
+__device__ __forceinline__ PdeltaTable pdelta_table(const Params& P, int pt, bool linear)
+{
+  PdeltaTable t;
+  if (linear) {
+    t.tab = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    t.lk = P.pkl_lk; t.z = P.pkl_z; t.nk = P.pkl_nk; t.nz = P.pkl_nz;
+  } else {
+    t.tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+    t.lk = P.pk_lk; t.z = P.pk_z; t.nk = P.pk_nk; t.nz = P.pk_nz;
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------- ss
+template <typename T>
+__global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __restrict__ ell)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int L = blockIdx.y * LT + tid;
+  const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
+  T* lk = (T*)smem_raw;
+  T* Ps = lk + pd.nk;
+  T* X = Ps + PCH * LT;
+  T* nfk = X + (size_t)P.pss * PCH;
+  T* ndy = nfk + PCH;
+  int* nj = (int*)(ndy + PCH);
+  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const int* nodej = P.node_j + (size_t)pt * P.node_stride;
+  const double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
+  const bool valid = L < P.nnode_ss;
+  const double l = valid ? ell[L] : 1.0;
+  const double lp = l + 0.5;
+  const T pref = (T)(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
+  double* out = P.tab_ss + (size_t)pt * P.pss * P.nnode_ss;
+  for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
+    const int np = min(PCH, P.n_ss - p0);
+    __syncthreads();
+    for (int p = tid; p < np; p += LT) {
+      nfk[p] = (T)(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
+      ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + p0 + p];
+      nj[p] = nodej[p0 + p];
+    }
+    for (int idx = tid; idx < P.pss * np; idx += LT) {
+      const int pair = idx / np, p = idx - pair * np;
+      const double fK = node[(size_t)NF_FK * P.node_stride + p0 + p];
+      const double dch = node[(size_t)NF_DCHIDA * P.node_stride + p0 + p];
+      const double wt = node[(size_t)NF_WT * P.node_stride + p0 + p];
+      X[pair * PCH + p] = (T)(wt * dch / (fK * fK) * w[P.z1[pair] * P.n_ss + p0 + p] *
+                              w[P.z2[pair] * P.n_ss + p0 + p]);
+    }
+    __syncthreads();
+    if (!valid) continue;
+    const T lpt = (T)lp;
+    for (int p = 0; p < np; p++) {
+      const T log10k = log10_t<T>(lpt / nfk[p]);
+      Ps[p * LT + tid] = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], ndy[p]);
+    }
+    for (int pair = 0; pair < P.pss; pair++) {
+      T acc = 0;
+      const T* xr = X + pair * PCH;
+      for (int p = 0; p < np; p++) acc += xr[p] * Ps[p * LT + tid];
+      const double v = (double)(pref * acc);
+      double* o = out + (size_t)pair * P.nnode_ss + L;
+      *o = (p0 == 0) ? v : *o + v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- gs
+template <typename T>
+__global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __restrict__ ell)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x;
+  const int q = blockIdx.z;
+  const int tid = threadIdx.x;
+  const int L = blockIdx.y * LT + tid;
+  const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
+  // pairs of this lens bin
+  __shared__ int kk[CL2PT_MAXB], ss_[CL2PT_MAXB];
+  __shared__ int npair, use_m;
+  if (tid == 0) {
+    int n = 0;
+    for (int k = 0; k < P.pgs; k++)
+      if (P.zl[k] == q) { kk[n] = k; ss_[n] = P.zs[k]; n++; }
+    npair = n;
+    use_m = (P.nu[pt].gb[4][q] != 0.0);
+  }
+  __syncthreads();
+  const int np_ = npair;
+  const int nterm = use_m ? 2 : 1;
+  T* lk = (T*)smem_raw;
+  T* Ps = lk + pd.nk;
+  T* X = Ps + PCH * LT;                  // [nterm][npair][PCH]
+  T* nfk = X + (size_t)2 * CL2PT_MAXB * PCH;
+  T* ndy = nfk + PCH;
+  int* nj = (int*)(ndy + PCH);
+  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
+  const int off = P.n_ss + q * P.n_ss;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const int* nodej = P.node_j + (size_t)pt * P.node_stride;
+  const size_t b0 = (size_t)pt * P.nl + q;
+  const double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
+  const double* wl = P.wgs_l + b0 * P.n_ss;
+  const double* wm = P.wgs_m + b0 * P.n_ss;
+  const bool valid = L < P.nnode_g;
+  const double l = valid ? ell[L] : 1.0;
+  const double lp = l + 0.5;
+  const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
+  const T pref2 = (T)((tmp > 0) ? sqrt(tmp) / (lp * lp) : 0.0);
+  const T pref = (T)(l * (l + 1.) / (lp * lp));
+  double* out = P.tab_gs + (size_t)pt * P.pgs * P.nnode_g;
+  for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
+    const int np = min(PCH, P.n_ss - p0);
+    __syncthreads();
+    for (int p = tid; p < np; p += LT) {
+      nfk[p] = (T)(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
+      ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
+      nj[p] = nodej[off + p0 + p];
+    }
+    for (int idx = tid; idx < nterm * np_ * np; idx += LT) {
+      const int t = idx / (np_ * np);
+      const int r = idx - t * np_ * np;
+      const int m = r / np, p = r - m * np;
+      const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
+      const double dch = node[(size_t)NF_DCHIDA * P.node_stride + off + p0 + p];
+      const double wt = node[(size_t)NF_WT * P.node_stride + off + p0 + p];
+      const double lens = t == 0 ? wl[p0 + p] : wm[p0 + p];
+      X[(t * CL2PT_MAXB + m) * PCH + p] =
+          (T)(wt * dch / (fK * fK) * wx[ss_[m] * P.n_ss + p0 + p] * lens);
+    }
+    __syncthreads();
+    if (!valid) continue;
+    const T lpt = (T)lp;
+    for (int p = 0; p < np; p++) {
+      const T log10k = log10_t<T>(lpt / nfk[p]);
+      Ps[p * LT + tid] = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], ndy[p]);
+    }
+    for (int m = 0; m < np_; m++) {
+      T a0 = 0, a1 = 0;
+      const T* x0 = X + (0 * CL2PT_MAXB + m) * PCH;
+      for (int p = 0; p < np; p++) a0 += x0[p] * Ps[p * LT + tid];
+      if (use_m) {
+        const T* x1 = X + (1 * CL2PT_MAXB + m) * PCH;
+        for (int p = 0; p < np; p++) a1 += x1[p] * Ps[p * LT + tid];
+      }
+      const double v = (double)(pref2 * (a0 + pref * a1));
+      double* o = out + (size_t)kk[m] * P.nnode_g + L;
+      *o = (p0 == 0) ? v : *o + v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- gg
+// int_for_C_gg_tomo_limber (cosmo2D.c:2490-2608) summed over the gg nodes.
+// mode 0: C_l nodes -> tab_gg (Pdelta);  mode 1: integer l = 0..LNL-1 ->
+// ggl (Pdelta and p_lin, for the non-Limber corrections and hand-over).
+template <typename T>
+__global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __restrict__ ell,
+                                                  int mode)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x;
+  const int q = blockIdx.z;
+  const int tid = threadIdx.x;
+  const int L = blockIdx.y * LT + tid;
+  const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
+  const PdeltaTable pl = pdelta_table(P, pt, true);
+  T* lk = (T*)smem_raw;               // Pdelta axis
+  T* lkl = lk + pd.nk;                // linear axis
+  // node data [8][PCH] after the two axes, 16-byte aligned
+  const size_t nd_off = ((size_t)(pd.nk + pl.nk) * sizeof(T) + 15) & ~(size_t)15;
+  double* nd = (double*)(smem_raw + nd_off);
+  int* nj = (int*)(nd + 8 * PCH);     // [2][PCH]
+  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
+  for (int i = tid; i < pl.nk; i += LT) lkl[i] = (T)pl.lk[i];
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const int off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const int* nodej = P.node_j + (size_t)pt * P.node_stride;
+  const size_t b0 = (size_t)pt * P.nl + q;
+  const int nL = (mode == 0) ? P.nnode_g : P.lmax_nolimber;
+  const bool valid = L < nL;
+  const double l = valid ? ((mode == 0) ? ell[L] : (double)L) : 1.0;
+  const double lp = l + 0.5;
+  const double pref = l * (l + 1.) / (lp * lp);
+  const double c0 = (1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.));
+  const double c1 = 4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.));
+  const double chi_amin = P.chi_amin[pt];
+  double sum_nl = 0.0, sum_lin = 0.0;
+  for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
+    const int np = min(PCH, P.n_gg - p0);
+    __syncthreads();
+    for (int p = tid; p < np; p += LT) {
+      const double a = node[(size_t)NF_A * P.node_stride + off + p0 + p];
+      const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
+      nd[0 * PCH + p] = fK;
+      nd[1 * PCH + p] = node[(size_t)NF_WT * P.node_stride + off + p0 + p] *
+                        node[(size_t)NF_DCHIDA * P.node_stride + off + p0 + p] / (fK * fK);
+      nd[2 * PCH + p] = node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
+      nd[3 * PCH + p] = P.wgg_l[b0 * P.n_gg + p0 + p];
+      nd[4 * PCH + p] = P.wgg_m[b0 * P.n_gg + p0 + p];
+      nd[5 * PCH + p] = P.wgg_r0[b0 * P.n_gg + p0 + p];
+      nj[p] = nodej[off + p0 + p];
+      // linear-table z cell of the node
+      const double z = 1.0 / a - 1.0;
+      const int jl = bsearch_d(pl.z, pl.nz, z);
+      nj[PCH + p] = jl;
+      nd[6 * PCH + p] = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
+    }
+    __syncthreads();
+    if (!valid) continue;
+    for (int p = 0; p < np; p++) {
+      const double fK = nd[0 * PCH + p];
+      const double chi1 = fK * (lp + 1.0) / lp;  // (l+3/2)/k
+      if (chi1 > chi_amin) continue;
+      const double a1 = a_chi_d(P.chi_z, X, P.chi_nz, chi1);
+      const double z1 = 1. / a1 - 1.;
+      const double H1 = 1.0 / ((a1 * a1) * chi_all_d(P.chi_z, X, P.chi_nz, a1).dchida);
+      const double R1 = nz_lens_d(P, z1, q, nu.lens_dz[q], nu.lens_stretch[q]) * H1 *
+                        f_growth_d(P.G_z, Gv, P.G_nz, z1);
+      const double wrsd = c0 * nd[5 * PCH + p] - c1 * R1;
+      const double s = nd[3 * PCH + p] + nd[4 * PCH + p] * pref + wrsd;
+      const double s2w = s * s * nd[1 * PCH + p];
+      const T log10k = log10_t<T>((T)(lp / (fK * CL2PT_COVERH0)));
+      const T Pnl = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
+      sum_nl += s2w * (double)Pnl;
+      if (mode == 1) {
+        const T Pl = pk_walk<T>(lkl, pl.nk, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
+        sum_lin += s2w * (double)Pl;
+      }
+    }
+  }
+  if (!valid) return;
+  if (mode == 0) {
+    P.tab_gg[b0 * P.nnode_g + L] = sum_nl;
+  } else {
+    P.ggl[(b0 * P.lmax_nolimber + L) * 2 + 0] = sum_nl;
+    P.ggl[(b0 * P.lmax_nolimber + L) * 2 + 1] = sum_lin;
+  }
+}
+
+template <typename T>
+static void launch_limber_t(const Params& P, const double* ell_ss, const double* ell_g,
+                            cudaStream_t s, int* launches, const Hook& hk)
+{
+  if (P.probes & CL2PT_PROBE_XI) {
+    const size_t sm = sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + 2 * PCH) +
+                      sizeof(int) * PCH + 64;
+    cudaFuncSetAttribute(k_limber_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    dim3 g(P.B, (P.nnode_ss + LT - 1) / LT);
+    hk(CL2PT_K_LIMBER_SS, 1);
+    k_limber_ss<T><<<g, LT, sm, s>>>(P, ell_ss);
+    hk(CL2PT_K_LIMBER_SS, 0);
+    (*launches)++;
+  }
+  if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
+    const size_t sm = sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + 2 * PCH) +
+                      sizeof(int) * PCH + 64;
+    cudaFuncSetAttribute(k_limber_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
+    hk(CL2PT_K_LIMBER_GS, 1);
+    k_limber_gs<T><<<g, LT, sm, s>>>(P, ell_g);
+    hk(CL2PT_K_LIMBER_GS, 0);
+    (*launches)++;
+  }
+  if (P.probes & CL2PT_PROBE_WTHETA) {
+    const size_t sm = sizeof(T) * (P.pk_nk + P.pkl_nk + 2) + sizeof(double) * 8 * PCH +
+                      sizeof(int) * 2 * PCH + 64;
+    cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
+    hk(CL2PT_K_LIMBER_GG, 1);
+    k_limber_gg<T><<<g, LT, sm, s>>>(P, ell_g, 0);
+    hk(CL2PT_K_LIMBER_GG, 0);
+    (*launches)++;
+    if (!P.adopt_limber_gg) {
+      dim3 g2(P.B, (P.lmax_nolimber + LT - 1) / LT, P.nl);
+      hk(CL2PT_K_LIMBER_GGL, 1);
+      k_limber_gg<T><<<g2, LT, sm, s>>>(P, ell_g, 1);
+      hk(CL2PT_K_LIMBER_GGL, 0);
+      (*launches)++;
+    }
+  }
+}
+
+void launch_limber(const Params& P, const double* ell_ss, const double* ell_g, cudaStream_t s,
+                   int* launches, const Hook& hk)
+{
+  if (P.prec == CL2PT_PREC_FP64)
+    launch_limber_t<double>(P, ell_ss, ell_g, s, launches, hk);
+  else
+    launch_limber_t<float>(P, ell_ss, ell_g, s, launches, hk);
+}
+
+}  // namespace cl2pt

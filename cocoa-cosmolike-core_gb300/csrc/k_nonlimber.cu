@@ -1,0 +1,371 @@
+// k_nonlimber.cu -- non-Limber galaxy clustering C_l by FFTLog
+// (C_cl_tomo + cfftlog_ells_p1/p2, cosmo2D.c:3995-4769), FP64.
+//
+// One CTA per (point, lens bin).  The CTA builds the three radial kernels
+// f_j(chi) (galaxy bias, RSD, magnification) on the log-chi grid, takes
+// their r2c transforms with the c-window taper, and then walks the
+// multipoles in blocks of 16 exactly as the reference does: for every l
+// it multiplies each spectrum by the phase and the Gamma-ratio kernel g_l
+// (direct Lanczos evaluation for the first two l of a block, the two-step
+// recurrence after that), runs one c2r transform per kernel in shared
+// memory, sums F = F_0 + F_1 + bmag l(l+1) F_2 / y^2 and integrates
+// F^2 k^3 P_lin(k, z=0) over chi.  At the end of every block it applies
+// the reference's 1% convergence test against the Limber C_l and hands
+// the remaining multipoles to Limber.
+//
+// The FFT is a Stockham autosort transform (Govindaraju et al. 2008
+// formulation) over the factors 4, 2, 3, 5, 7, one butterfly per thread per
+// stage, ping-ponging two shared-memory buffers, with twiddles read from a
+// per-size table.
+#include <math.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "nonlimber.h"
+
+namespace cl2pt {
+
+struct cd { double x, y; };
+__device__ __forceinline__ cd cmk(double a, double b) { cd r; r.x = a; r.y = b; return r; }
+__device__ __forceinline__ cd cadd(cd a, cd b) { return cmk(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ cd csub(cd a, cd b) { return cmk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ cd cmul(cd a, cd b) { return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ cd cscale(cd a, double s) { return cmk(a.x * s, a.y * s); }
+__device__ __forceinline__ cd cconj(cd a) { return cmk(a.x, -a.y); }
+__device__ __forceinline__ cd cdivc(cd a, cd b)
+{
+  // Smith's algorithm
+  if (fabs(b.x) >= fabs(b.y)) {
+    const double r = b.y / b.x, d = b.x + b.y * r;
+    return cmk((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const double r = b.x / b.y, d = b.x * r + b.y;
+  return cmk((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+__device__ __forceinline__ cd clog_(cd a) { return cmk(log(hypot(a.x, a.y)), atan2(a.y, a.x)); }
+__device__ __forceinline__ cd cexp_(cd a)
+{
+  const double m = exp(a.x);
+  double s, c;
+  sincos(a.y, &s, &c);
+  return cmk(m * c, m * s);
+}
+__device__ __forceinline__ cd csin_(cd a)
+{
+  double s, c;
+  sincos(a.x, &s, &c);
+  return cmk(s * cosh(a.y), c * sinh(a.y));
+}
+
+__constant__ double c_lanczos[9] = {
+    0.99999999999980993227684700473478, 676.520368121885098567009190444019,
+    -1259.13921672240287047156078755283, 771.3234287776530788486528258894,
+    -176.61502916214059906584551354, 12.507343278686904814458936853,
+    -0.13857109526572011689554707, 9.984369578019570859563e-6,
+    1.50563273514931155834e-7};
+
+// ln Gamma(a), Lanczos g = 7 with reflection for Re a < 1/2
+// (cosmo2D.c:4273-4294)
+__device__ cd lngamma_refl(cd a)
+{
+  const double ln2pio2 = 0.5 * log(2 * M_PI);
+  if (a.x < 0.5) {
+    const cd ma = cmk(-a.x, -a.y);
+    cd tmp = cmk(c_lanczos[0], 0.0);
+    for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(ma.x + w, ma.y)));
+    const cd t = cmk(ma.x + 7.5, ma.y);
+    const cd lt = clog_(t);
+    const cd inner = cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(ma.x + 0.5, ma.y), lt)), t), clog_(tmp));
+    const cd s = clog_(csin_(cscale(a, M_PI)));
+    return csub(csub(cmk(log(M_PI), 0.0), s), inner);
+  }
+  cd tmp = cmk(c_lanczos[0], 0.0);
+  for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(a.x - 1 + w, a.y)));
+  const cd t = cmk(a.x - 1 + 7.5, a.y);
+  return cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(a.x - 1 + 0.5, a.y), clog_(t))), t), clog_(tmp));
+}
+
+// g_l(z) for the three derivative orders (cosmo2D.c:4259-4430)
+__device__ cd gl_direct(int deriv, double nu, double eta, int k)
+{
+  const double ln2 = log(2.);
+  const cd z = cmk(nu, eta);
+  if (deriv == 0) {
+    const cd p1 = lngamma_refl(cscale(cmk(k + z.x, z.y), 0.5));
+    const cd p2 = lngamma_refl(cscale(cmk(3 + k - z.x, -z.y), 0.5));
+    return cexp_(cadd(cscale(z, ln2), csub(p1, p2)));
+  }
+  if (deriv == 1) {
+    const cd p1 = lngamma_refl(cscale(cmk(k + z.x - 1., z.y), 0.5));
+    const cd p2 = lngamma_refl(cscale(cmk(4 + k - z.x, -z.y), 0.5));
+    const cd e = cexp_(cadd(cscale(cmk(z.x - 1, z.y), ln2), csub(p1, p2)));
+    return cmul(cmk(-(z.x - 1), -z.y), e);
+  }
+  const cd p1 = lngamma_refl(cscale(cmk(k + z.x - 2, z.y), 0.5));
+  const cd p2 = lngamma_refl(cscale(cmk(5 + k - z.x, -z.y), 0.5));
+  const cd e = cexp_(cadd(cscale(cmk(z.x - 2, z.y), ln2), csub(p1, p2)));
+  return cmul(cmul(cmk(z.x - 1, z.y), cmk(z.x - 2, z.y)), e);
+}
+__device__ __forceinline__ cd gl_ratio(int deriv, double nu, double eta, int k)
+{
+  const cd z = cmk(nu, eta);
+  if (deriv == 0) return cdivc(cmk(k - 2 + z.x, z.y), cmk(k + 1 - z.x, -z.y));
+  if (deriv == 1) return cdivc(cmk(k - 3 + z.x, z.y), cmk(k + 2 - z.x, -z.y));
+  return cdivc(cmk(k - 4 + z.x, z.y), cmk(k + 3 - z.x, -z.y));
+}
+
+constexpr int NL_NT = 256;
+
+// One Stockham transform of size N (factors fac[0..nf-1]) on in/out
+// (shared), twiddles tw[k] = exp(+2 pi i k / N); sign -1 = forward.
+// Returns the buffer holding the result.
+__device__ cd* block_fft(cd* in, cd* out, int N, const int* fac, int nf, const cd* __restrict__ tw,
+                         int sign)
+{
+  int Ns = 1;
+  for (int s = 0; s < nf; s++) {
+    const int R = fac[s];
+    const int NR = N / R;
+    const int tstep = N / (Ns * R);
+    for (int j = threadIdx.x; j < NR; j += NL_NT) {
+      const int k = j % Ns;
+      cd v[7];
+      for (int r = 0; r < R; r++) {
+        cd x = in[j + r * NR];
+        if (r && k) {
+          cd w = tw[(r * k * tstep) % N];
+          if (sign < 0) w.y = -w.y;
+          x = cmul(x, w);
+        }
+        v[r] = x;
+      }
+      // radix-R DFT with roots tw[m N / R]
+      cd o[7];
+      for (int t = 0; t < R; t++) {
+        cd acc = v[0];
+        for (int r = 1; r < R; r++) {
+          cd w = tw[((r * t) % R) * NR];
+          if (sign < 0) w.y = -w.y;
+          acc = cadd(acc, cmul(v[r], w));
+        }
+        o[t] = acc;
+      }
+      const int dst = (j / Ns) * Ns * R + k;
+      for (int r = 0; r < R; r++) out[dst + r * Ns] = o[r];
+    }
+    __syncthreads();
+    cd* t = in;
+    in = out;
+    out = t;
+    Ns *= R;
+  }
+  return in;
+}
+
+__device__ double block_sum(double v, double* sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < NL_NT / 32; w++) s += sh[w];
+    sh[0] = s;
+  }
+  __syncthreads();
+  s = sh[0];
+  __syncthreads();
+  return s;
+}
+
+__global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int nchi = P.nl_nchi;
+  const int LNL = P.lmax_nolimber;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
+  const double om = P.omega_m[pt];
+  const double bmag = nu.gb[4][q];
+  const int nj = (bmag != 0.0) ? 3 : 2;
+  cd* bufA = (cd*)smem_raw;
+  cd* bufB = bufA + Q.nmax;
+  double* F = (double*)(bufB + Q.nmax);
+  double* xg = F + nchi;
+  __shared__ double red[NL_NT / 32];
+  const size_t cta = (size_t)pt * P.nl + q;
+  cd* tout = (cd*)Q.tout + cta * Q.tout_stride;   // [3][nmax/2+1]
+  cd* gst = (cd*)Q.gstate + cta * Q.gst_stride;   // [3][2][nmax/2+1]
+  double* Cl = P.cnl + cta * LNL;
+  const double* ggl = P.ggl + cta * LNL * 2;
+  const double rc = CL2PT_COVERH0 / P.h0[pt];
+  const double chi_min = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 0.002)).chi * rc;
+  const double chi_max = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 4.0)).chi * rc;
+  const double dlnchi = log(chi_max / chi_min) / ((double)nchi - 1.0);
+  for (int j = tid; j < nchi; j += NL_NT) xg[j] = chi_min * exp(dlnchi * j);
+  __syncthreads();
+  const double dlnx = log(xg[1] / xg[0]);
+  const double* glens = P.glens + ((size_t)pt * P.nl + q) * P.n_a;
+  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
+  // ---- cfftlog_ells_p1: r2c of f_j / x^nu_j with the c-window
+  for (int j = 0; j < nj; j++) {
+    const int N = Q.N[j];
+    for (int i = tid; i < N; i += NL_NT) {
+      double v = 0.0;
+      const int qq = i - Q.pad[j];
+      if (qq >= 0 && qq < nchi) {
+        const double chi = xg[qq] / rc;
+        const double a = a_chi_d(P.chi_z, X, P.chi_nz, chi);
+        const double z = 1. / a - 1.;
+        if (!(z < P.lens_zmin[q] || z > P.lens_zmax[q])) {
+          const double H = 1.0 / ((a * a) * chi_all_d(P.chi_z, X, P.chi_nz, a).dchida);
+          const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+          const double pf = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]);
+          double fx;
+          if (j == 0) {
+            double b1;
+            switch (P.bias_model[0]) {
+              case 0: b1 = nu.gb[0][q]; break;
+              case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
+              case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
+              case 4: b1 = nu.gb[0][0] * pow(1 + z, nu.gb[0][1]); break;
+              default: {
+                const double zev = growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)) /
+                                   growfac_d(P.G_z, Gv, P.G_nz, g1,
+                                             1. / (1. + 0.5 * (P.lens_zmin[q] + P.lens_zmax[q])));
+                b1 = (nu.gb[0][q] - 1.) / zev + 1.;
+              }
+            }
+            fx = chi * pf * D * H * b1;
+          } else if (j == 1) {
+            fx = -chi * pf * D * H * f_growth_d(P.G_z, Gv, P.G_nz, z);
+          } else {
+            // W_mag with the coarse g_lens table (interpol1d)
+            const double amax = 0.999999;
+            const double dac = (amax - amin_lensg) / ((double)P.n_a - 1.0);
+            const double gl = (a < amin_lensg || a > 1.0 - dac)
+                                  ? 0.0 : interpol1d_d(glens, P.n_a, amin_lensg, dac, a);
+            const double WM = (1.5 * om * chi / a) * gl;
+            fx = (WM / chi / (rc * rc)) * D;
+          }
+          v = fx / pow(xg[qq], Q.nu[j]);
+        }
+      }
+      bufA[i] = cmk(v, 0.0);
+    }
+    __syncthreads();
+    cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
+    const int halfN = N / 2;
+    const int kmax = (int)(halfN * 0.25);
+    for (int i = tid; i <= halfN; i += NL_NT) {
+      cd v = r[i];
+      const int k = halfN - i;  // window on the right side
+      if (k <= kmax) {
+        const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
+        v = cscale(v, W);
+      }
+      tout[j * Q.hstride + i] = v;
+    }
+    __syncthreads();
+  }
+  // ---- multipole blocks
+  int LM = LNL, done = 0;
+  const int BLOCK = 16;
+  for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
+    const int ke = (ks + BLOCK < LNL) ? ks + BLOCK : LNL;
+    for (int k = ks; k < ke; k++) {
+      for (int i = tid; i < nchi; i += NL_NT) F[i] = 0.0;
+      for (int j = 0; j < nj; j++) {
+        const int N = Q.N[j];
+        const int nq = N / 2 + 1;
+        const double base = xg[0] / exp(2 * Q.pad[j] * dlnx);
+        const double y0 = (k + 1.) / xg[nchi - 1];
+        const double lnbase = log(base * y0);
+        __syncthreads();
+        for (int i = tid; i < nq; i += NL_NT) {
+          const double eta = (2.0 * M_PI / (dlnx * N)) * i;
+          cd g;
+          cd* gs = gst + (size_t)j * 2 * Q.hstride;
+          if (k < ks + 2) g = gl_direct(Q.deriv[j], Q.nu[j], eta, k);
+          else g = cmul(gs[((k - ks) & 1) * Q.hstride + i], gl_ratio(Q.deriv[j], Q.nu[j], eta, k));
+          gs[((k - ks) & 1) * Q.hstride + i] = g;
+          cd val = tout[j * Q.hstride + i];
+          double sp, cp;
+          sincos(-eta * lnbase, &sp, &cp);
+          val = cmul(cmul(val, cmk(cp, sp)), g);
+          val = cconj(val);
+          bufA[i] = val;
+          if (i > 0 && i < N - i) bufA[N - i] = cconj(val);  // Hermitian completion
+        }
+        __syncthreads();
+        if (tid == 0) {
+          bufA[0].y = 0.0;
+          if ((N & 1) == 0) bufA[N / 2].y = 0.0;
+        }
+        __syncthreads();
+        cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], +1);
+        const double sqpi = sqrt(M_PI);
+        for (int i = tid; i < nchi; i += NL_NT) {
+          const double y = (k + 1.) / xg[nchi - 1 - i];
+          double fy = r[Q.pad[j] + i].x * sqpi / (4. * N * pow(y, Q.nu[j]));
+          if (j == 2) fy = bmag * (k * (k + 1.)) * fy / (y * y);
+          F[i] += fy;
+        }
+        __syncthreads();
+      }
+      // chi sum of F^2 k^3 P_lin(k, a = 1)
+      double part = 0.0;
+      const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+      for (int i = tid; i < nchi; i += NL_NT) {
+        const double ty = (k + 1.) / xg[nchi - 1 - i];
+        const double k1 = ty * rc;
+        part += F[i] * F[i] * (k1 * k1 * k1) *
+                pk_d(P.pkl_lk, P.pkl_nk, P.pkl_z, P.pkl_nz, tabL, k1, 1.0);
+      }
+      const double tcl = block_sum(part, red);
+      if (tid == 0)
+        Cl[k] = tcl * dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+    }
+    __syncthreads();
+    // convergence at the block end (cosmo2D.c:4741-4750)
+    const int L = ke - 1;
+    const double denom = ggl[L * 2 + 0];
+    if (fabs(denom) > 1e-300) {
+      const double dev = Cl[L] / denom - 1.0;
+      if (isfinite(dev) && fabs(dev) < 0.01) {
+        done = 1;
+        LM = ke;
+      }
+    }
+  }
+  // hand over to Limber (cosmo2D.c:4760-4765)
+  if (tid == 0) {
+    P.conv_l[cta] = LM;
+    const double* tg = P.tab_gg + cta * P.nnode_g + P.nint;
+    for (int k = LM; k < LNL; k++) {
+      if (k > P.lmin_tab)
+        Cl[k] = interpol1d_d(tg, P.n_ell, P.lim_g[0], P.lim_g[2], log((double)k));
+      else
+        Cl[k] = ggl[k * 2 + 0];
+    }
+  }
+}
+
+void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
+                      const Hook& hk)
+{
+  const size_t sm = sizeof(double) * 2 * 2 * Q.nmax + sizeof(double) * 2 * P.nl_nchi + 64;
+  cudaFuncSetAttribute(k_nonlimber, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 g(P.B, P.nl);
+  hk(CL2PT_K_NONLIMBER, 1);
+  k_nonlimber<<<g, NL_NT, sm, s>>>(P, Q);
+  hk(CL2PT_K_NONLIMBER, 0);
+  (*launches)++;
+}
+
+}  // namespace cl2pt

@@ -1,0 +1,330 @@
+// k_setup.cu -- per-point FP64 set-up stage of the batched 2-point path.
+//
+//   k_gtab   lens-efficiency tables g(a) of every source bin (g_tomo,
+//            redshift_spline.c:852-923) and, when magnification is on, of
+//            every lens bin (g_lens, redshift_spline.c:1014-1109): one CTA
+//            per (point, bin), the cumulative trapezoid done as a block scan.
+//   k_nodes  Gauss-Legendre nodes in a with chi, dchi/da, D, H/H0 at each
+//            node (create_cosmo_nodes, cosmo2D.c:1331-1356) and the radial
+//            weights the Limber integrands need (radial_weights.c:15-105,
+//            bias.c:17-210, IA.c:238-415), for the ss node set and the gs/gg
+//            node sets of every lens bin: one CTA per (point, node set).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cl2pt {
+
+// Inclusive block scan (sum) of one double per thread.
+template <int NT>
+__device__ double block_scan(double v, double* sh)
+{
+  const int t = threadIdx.x;
+  const int lane = t & 31, w = t >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double s = (lane < NT / 32) ? sh[lane] : 0.0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < NT / 32) sh[lane] = s;
+  }
+  __syncthreads();
+  const double r = v + (w > 0 ? sh[w - 1] : 0.0);
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double n_of_z_bin(const Params& P, const cl2pt_nuisance& nu, int lens,
+                                             int b, double z)
+{
+  return lens ? nz_lens_d(P, z, b, nu.lens_dz[b], nu.lens_stretch[b])
+              : nz_source_d(P, z, b, nu.src_dz[b]);
+}
+
+// One lens-efficiency table: integrate n(z(a))/a^2 and n/(chi a^2) from
+// a_lo on a fine grid of Na points (step da), recording P - chi Q every
+// x points into tab[0..n_a-1].  tab[0] is set by the caller.
+constexpr int GT_NT = 256;
+
+__global__ void __launch_bounds__(GT_NT) k_gtab(Params P)
+{
+  const int pt = blockIdx.x;
+  const int bin = blockIdx.y;
+  const int lens = bin >= P.ns;
+  const int b = lens ? bin - P.ns : bin;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  if (lens) {
+    // g_lens is only needed by magnification terms (W_mag x bmag); skip
+    // the bins whose magnification bias is zero.
+    if (nu.gb[4][b] == 0.0) return;
+  }
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const int x = 25 * (1 + abs(P.hdi));
+  const int Na = x * (P.n_a - 1) + 1;
+  const double amax = 0.999999;
+  const double amin = 1.0 / ((lens ? P.lens_zmax_all : P.src_zmax_all) + 1.0);
+  const double da = (amax - amin) / ((double)Na - 1.0);
+  double* tab = (lens ? P.glens + ((size_t)pt * P.nl + b) * P.n_a
+                      : P.gsrc + ((size_t)pt * P.ns + b) * P.n_a);
+  __shared__ double sh[32];
+  __shared__ double carry[3];
+  double P0 = 0.0, Q0 = 0.0;
+  if (lens) {
+    // integral from the source table's amin up to the lens amin
+    // (redshift_spline.c:1048-1069)
+    const double amin_s = 1.0 / (P.src_zmax_all + 1.0);
+    const int Na0 = (amin_s < amin) ? (int)ceil((amin - amin_s) / da) + 1 : 1;
+    const double da0 = (Na0 > 1) ? (amin - amin_s) / ((double)Na0 - 1.) : 0.0;
+    double sp = 0.0, sq = 0.0;
+    for (int i = 1 + threadIdx.x; i < Na0; i += GT_NT) {
+      const double apl = amin_s + (i - 1) * da0, aph = amin_s + i * da0;
+      const double fl = n_of_z_bin(P, nu, 1, b, 1.0 / apl - 1.0) / (apl * apl);
+      const double fh = n_of_z_bin(P, nu, 1, b, 1.0 / aph - 1.0) / (aph * aph);
+      sp += 0.5 * da0 * (fl + fh);
+      sq += 0.5 * da0 * (fl / chi_all_d(P.chi_z, X, P.chi_nz, apl).chi +
+                         fh / chi_all_d(P.chi_z, X, P.chi_nz, aph).chi);
+    }
+    // block reductions
+    for (int o = 16; o > 0; o >>= 1) {
+      sp += __shfl_down_sync(0xffffffffu, sp, o);
+      sq += __shfl_down_sync(0xffffffffu, sq, o);
+    }
+    __shared__ double r2[2][GT_NT / 32];
+    if ((threadIdx.x & 31) == 0) { r2[0][threadIdx.x >> 5] = sp; r2[1][threadIdx.x >> 5] = sq; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a0 = 0, b0 = 0;
+      for (int w = 0; w < GT_NT / 32; w++) { a0 += r2[0][w]; b0 += r2[1][w]; }
+      carry[0] = a0;
+      carry[1] = b0;
+    }
+    __syncthreads();
+    P0 = carry[0];
+    Q0 = carry[1];
+    if (threadIdx.x == 0) tab[0] = P0 - chi_all_d(P.chi_z, X, P.chi_nz, amin).chi * Q0;
+  } else {
+    if (threadIdx.x == 0) tab[0] = 0.0;
+  }
+  __syncthreads();
+  // running sums over chunks of GT_NT fine points; element i contributes
+  // the trapezoid 0.5 da (f[i-1] + f[i]) for i >= 1.
+  double runP = P0, runQ = Q0;
+  double prevP = 0.0, prevQ = 0.0;  // integrand at the last point of the previous chunk
+  __shared__ double lastf[2];
+  for (int base = 0; base < Na; base += GT_NT) {
+    const int i = base + threadIdx.x;
+    double fP = 0.0, fQ = 0.0, c = 1.0;
+    if (i < Na) {
+      const double a = amin + i * da;
+      c = chi_all_d(P.chi_z, X, P.chi_nz, a).chi;
+      fP = n_of_z_bin(P, nu, lens, b, 1. / a - 1.) / (a * a);
+      fQ = fP / c;
+    }
+    // neighbour value f[i-1]
+    __shared__ double fprev[2][GT_NT];
+    fprev[0][threadIdx.x] = fP;
+    fprev[1][threadIdx.x] = fQ;
+    if (threadIdx.x == 0) { lastf[0] = prevP; lastf[1] = prevQ; }
+    __syncthreads();
+    const double pP = threadIdx.x ? fprev[0][threadIdx.x - 1] : lastf[0];
+    const double pQ = threadIdx.x ? fprev[1][threadIdx.x - 1] : lastf[1];
+    const double incP = (i >= 1 && i < Na) ? 0.5 * da * (pP + fP) : 0.0;
+    const double incQ = (i >= 1 && i < Na) ? 0.5 * da * (pQ + fQ) : 0.0;
+    const double sP = block_scan<GT_NT>(incP, sh) + runP;
+    const double sQ = block_scan<GT_NT>(incQ, sh) + runQ;
+    if (i >= 1 && i < Na && (i % x) == 0) tab[i / x] = sP - c * sQ;
+    // carry to the next chunk
+    if (threadIdx.x == GT_NT - 1) {
+      carry[0] = sP;
+      carry[1] = sQ;
+      carry[2] = fP;
+      lastf[1] = fQ;
+    }
+    __syncthreads();
+    runP = carry[0];
+    runQ = carry[1];
+    prevP = carry[2];
+    prevQ = lastf[1];
+    __syncthreads();
+  }
+}
+
+// g_tomo / g_lens lookup: interpol1d on the coarse table
+__device__ __forceinline__ double g_lookup(const double* tab, int n_a, double amin, double a,
+                                           bool open_lo)
+{
+  const double amax = 0.999999;
+  const double dac = (amax - amin) / ((double)n_a - 1.0);
+  if (open_lo ? (a <= amin) : (a < amin)) return 0.0;
+  if (a > 1.0 - dac) return 0.0;
+  return interpol1d_d(tab, n_a, amin, dac, a);
+}
+
+__device__ double gb1_d(const Params& P, const cl2pt_nuisance& nu, double z, int ni, double g1,
+                        const double* Zg, const double* Gv)
+{
+  switch (P.bias_model[0]) {
+    case 0: return nu.gb[0][ni];
+    case 1: return nu.gb[0][ni] * ((1.0 + z) / (1. + P.zmean_lens[ni]));
+    case 2: {
+      const double zev = growfac_d(Zg, Gv, P.G_nz, g1, 1. / (z + 1.)) /
+                         growfac_d(Zg, Gv, P.G_nz, g1,
+                                   1. / (1. + 0.5 * (P.lens_zmin[ni] + P.lens_zmax[ni])));
+      return (nu.gb[0][ni] - 1.) / zev + 1.;
+    }
+    case 3: return nu.gb[0][0] / growfac_d(Zg, Gv, P.G_nz, g1, 1. / (z + 1.));
+    case 4: return nu.gb[0][0] * pow(1 + z, nu.gb[0][1]);
+    default: return 0.0;
+  }
+}
+
+// IA_A1_Z1: IA.c:238-296 (amplitude of one bin)
+__device__ __forceinline__ double ia_a1(const Params& P, const cl2pt_nuisance& nu, double om,
+                                        double a, double D, int n)
+{
+  double A = 0.0;
+  if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) A = nu.ia[0][n];
+  else if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION)
+    A = nu.ia[0][0] * pow((1.0 / a) / 1.62, nu.ia[0][1]);
+  return A * (om * 0.01389 / D);
+}
+
+__device__ __forceinline__ double amin_lens_d(const Params& P, const cl2pt_nuisance& nu, int q)
+{
+  const double zm = P.zmean_lens[q];
+  const double zmax = (P.lens_zmax[q] - zm) * nu.lens_stretch[q] + zm;
+  return 1. / (1 + zmax + 2. * fabs(nu.lens_dz[q]));
+}
+__device__ __forceinline__ double amax_lens_d(const Params& P, const cl2pt_nuisance& nu, int q)
+{
+  const double zm = P.zmean_lens[q];
+  const double zmin = (P.lens_zmin[q] - zm) * nu.lens_stretch[q] + zm;
+  if (nu.gb[4][q] != 0) return 1. / (1. + fmax(P.src_zmin_all, 0.001));
+  return 1. / (1 + fmax(zmin - 2. * fabs(nu.lens_dz[q]), 0.001));
+}
+
+constexpr int ND_NT = 128;
+
+__global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
+{
+  const int pt = blockIdx.x;
+  const int set = blockIdx.y;  // 0: ss, 1..nl: gs lens q, nl+1..2nl: gg lens q
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double om = P.omega_m[pt];
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
+  const double* gsrc = P.gsrc + (size_t)pt * P.ns * P.n_a;
+  const double* glens = P.glens + (size_t)pt * P.nl * P.n_a;
+  const double amin_src = 1.0 / (P.src_zmax_all + 1.0);
+  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
+  int n, off, q = -1;
+  double amin, amax;
+  const double *glx, *glw;
+  if (set == 0) {
+    n = P.n_ss; off = 0;
+    amin = 1. / (P.src_zmax_all + 1.);
+    amax = 1. / (1. + fmax(P.src_zmin_all, 1e-6));
+    glx = P.gl_ss_x; glw = P.gl_ss_w;
+  } else if (set <= P.nl) {
+    q = set - 1;
+    n = P.n_ss; off = P.n_ss + q * P.n_ss;
+    amin = amin_lens_d(P, nu, q);
+    amax = amax_lens_d(P, nu, q);
+    glx = P.gl_ss_x; glw = P.gl_ss_w;
+  } else {
+    q = set - 1 - P.nl;
+    n = P.n_gg; off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
+    amin = amin_lens_d(P, nu, q);
+    amax = amax_lens_d(P, nu, q);
+    glx = P.gl_gg_x; glw = P.gl_gg_w;
+  }
+  if (!(amin > 0) || !(amin < amax) || !(amax < 1)) {
+    if (threadIdx.x == 0) atomicOr(P.err, 1);
+    return;
+  }
+  if (set == 0 && threadIdx.x == 0) P.chi_amin[pt] = chi_all_d(P.chi_z, X, P.chi_nz, P.a_min).chi;
+  double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  int* nj = P.node_j + (size_t)pt * P.node_stride;
+  const double A = 0.5 * (amax - amin), Bc = 0.5 * (amax + amin);
+  for (int p = threadIdx.x; p < n; p += ND_NT) {
+    const double a = Bc + A * glx[p];
+    const double wt = A * glw[p];
+    const Chis c = chi_all_d(P.chi_z, X, P.chi_nz, a);
+    const double fK = c.chi;
+    const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+    const double H = 1.0 / ((a * a) * c.dchida);
+    const double z = 1.0 / a - 1.0;
+    // z cell of the table Pdelta reads (nonlinear, or linear in the
+    // "linear" run mode), for the table walk
+    const double* pz = P.linear_pk ? P.pkl_z : P.pk_z;
+    const int pnz = P.linear_pk ? P.pkl_nz : P.pk_nz;
+    const int jz = bsearch_d(pz, pnz, z);
+    const double dyz = (z - pz[jz]) / (pz[jz + 1] - pz[jz]);
+    node[(size_t)NF_A * P.node_stride + off + p] = a;
+    node[(size_t)NF_WT * P.node_stride + off + p] = wt;
+    node[(size_t)NF_FK * P.node_stride + off + p] = fK;
+    node[(size_t)NF_DCHIDA * P.node_stride + off + p] = c.dchida;
+    node[(size_t)NF_D * P.node_stride + off + p] = D;
+    node[(size_t)NF_H * P.node_stride + off + p] = H;
+    node[(size_t)NF_DYZ * P.node_stride + off + p] = dyz;
+    nj[off + p] = jz;
+    const double pre = 1.5 * om * fK / a;
+    if (set == 0) {
+      double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
+      for (int s = 0; s < P.ns; s++) {
+        const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
+        const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
+        w[s * P.n_ss + p] = WK - WS * ia_a1(P, nu, om, a, D, s);
+      }
+    } else if (set <= P.nl) {
+      const double WGAL = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
+      const double bmag = nu.gb[4][q];
+      const double WMAG = (bmag != 0.0) ? pre * g_lookup(glens + q * P.n_a, P.n_a, amin_lensg, a, false) : 0.0;
+      const size_t b0 = (size_t)pt * P.nl + q;
+      P.wgs_l[b0 * P.n_ss + p] = WGAL * gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      P.wgs_m[b0 * P.n_ss + p] = WMAG * bmag;
+      double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
+      for (int s = 0; s < P.ns; s++) {
+        const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
+        const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
+        wx[s * P.n_ss + p] = WK - WS * ia_a1(P, nu, om, a, D, s);
+      }
+    } else {
+      const double WGAL = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
+      const double bmag = nu.gb[4][q];
+      const double WMAG = (bmag != 0.0) ? pre * g_lookup(glens + q * P.n_a, P.n_a, amin_lensg, a, false) : 0.0;
+      const size_t b0 = (size_t)pt * P.nl + q;
+      P.wgg_l[b0 * P.n_gg + p] = WGAL * gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      P.wgg_m[b0 * P.n_gg + p] = WMAG * bmag;
+      // RSD term at a0 = a_chi(chi_0), chi_0 = (l+1/2)/k = fK
+      // (cosmo2D.c:2540-2547, radial_weights.c:87-105)
+      const double a0 = a_chi_d(P.chi_z, X, P.chi_nz, fK);
+      const double z0 = 1. / a0 - 1.;
+      const double H0v = 1.0 / ((a0 * a0) * chi_all_d(P.chi_z, X, P.chi_nz, a0).dchida);
+      P.wgg_r0[b0 * P.n_gg + p] = nz_lens_d(P, z0, q, nu.lens_dz[q], nu.lens_stretch[q]) * H0v *
+                                  f_growth_d(P.G_z, Gv, P.G_nz, z0);
+    }
+  }
+}
+
+void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk)
+{
+  dim3 g1(P.B, P.ns + P.nl);
+  hk(CL2PT_K_GTAB, 1);
+  k_gtab<<<g1, GT_NT, 0, s>>>(P);
+  hk(CL2PT_K_GTAB, 0);
+  dim3 g2(P.B, 1 + 2 * P.nl);
+  hk(CL2PT_K_NODES, 1);
+  k_nodes<<<g2, ND_NT, 0, s>>>(P);
+  hk(CL2PT_K_NODES, 0);
+  *launches += 2;
+}
+
+}  // namespace cl2pt

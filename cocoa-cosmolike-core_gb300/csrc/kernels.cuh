@@ -1,0 +1,32 @@
+// kernels.cuh -- launchers of the cl2pt pipeline stages.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cl2pt {
+
+// Kernel ids for per-kernel timing (CL2PT_K_* in cl2pt.h).
+// Every launcher brackets each launch with hook(ctx, id, 1) / (ctx, id, 0).
+struct Hook {
+  void* ctx = nullptr;
+  void (*fn)(void* ctx, int kernel, int begin) = nullptr;
+  void operator()(int k, int b) const { if (fn) fn(ctx, k, b); }
+};
+
+void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk);
+// Limber C_l tables on the C_l nodes (ss, gs, gg) and, when the non-Limber
+// w(theta) path is on, the Limber gg C_l at integer l < lmax_nolimber for
+// both power spectra.  ell_ss / ell_g: node multipoles (device).
+void launch_limber(const Params& P, const double* ell_ss, const double* ell_g,
+                   cudaStream_t s, int* launches, const Hook& hk);
+// xi+-, gamma_t, w on the theta bins: obs[pt][n_total]
+void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
+                     const double* filt_gg, const double* filt_gg_nl, double* scratch,
+                     cudaStream_t s, int* launches, const Hook& hk);
+// masked, calibrated data vector dv[pt][n_total] from obs
+void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
+                     cudaStream_t s, int* launches, const Hook& hk);
+
+}  // namespace cl2pt

@@ -1,0 +1,28 @@
+// nonlimber.h -- constants of the non-Limber FFTLog stage.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cl2pt {
+
+struct NLParams {
+  int N[3];         // transform sizes of the three radial kernels
+  int pad[3];       // zero padding on each side (cosmo2D.c:4564-4577)
+  double nu[3];     // power-law bias exponents
+  int deriv[3];     // derivative orders of the Gamma-ratio kernels
+  int fac[3][16];   // Stockham factors of N[j]
+  int nfac[3];
+  const double* tw[3];  // exp(+2 pi i k / N[j]) as (re, im) pairs
+  int nmax;         // max N[j]
+  int hstride;      // nmax / 2 + 1
+  double* tout;     // [CTA][3][hstride] complex spectra
+  size_t tout_stride;   // complex entries per CTA
+  double* gstate;   // [CTA][3][2][hstride] complex recurrence state
+  size_t gst_stride;
+};
+
+void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
+                      const Hook& hk);
+
+}  // namespace cl2pt

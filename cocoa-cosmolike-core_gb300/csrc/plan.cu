@@ -1,0 +1,876 @@
+// plan.cu -- plan construction (FP64 host geometry) and the batched
+// evaluation entry points of libcl2pt.
+//
+// Host-side geometry restates, in this library's own code:
+//   n(z) normalisation + natural cubic splines  redshift_spline.c:412-537, 630-762
+//   lens mean redshift                          redshift_spline.c:794-844
+//   pair maps Z1/Z2/ZL/ZS                        redshift_spline.c:151-297
+//   C_l node positions                           cosmo2D.c:1628-1634, 2204-2207, 2704-2707
+//   bin-averaged Legendre filters                basics.c:382-455, cosmo2D.c:412-453, 631-639, 808-815
+// and folds the filters onto the C_l nodes: the reference fills C_l at every
+// integer l by linear interpolation in ln l between nodes (cosmo2D.c:1784-1880)
+// and then sums filter x C_l over l; since the fill is linear, the same sum
+// equals (folded filter) x (C on nodes), which is what the kernels compute.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <thread>
+#include <vector>
+
+#include "plan.h"
+#include "kernels.cuh"
+
+using cl2pt::Params;
+
+#define CUDA_OK(x)                                          \
+  do {                                                      \
+    cudaError_t e_ = (x);                                   \
+    if (e_ != cudaSuccess) {                                \
+      fprintf(stderr, "cl2pt: %s (%s:%d)\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return CL2PT_ERR_CUDA;                                \
+    }                                                       \
+  } while (0)
+
+namespace {
+
+// ---------------------------------------------------------------- numerics
+void gl_rule(int n, std::vector<double>& x, std::vector<double>& w)
+{
+  // Gauss-Legendre nodes by Newton iteration on P_n (Tricomi initial guess)
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const int m = (n + 1) / 2;
+  for (int i = 0; i < m; i++) {
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+    double dp = 0.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        const double pm = p1;
+        p1 = p0;
+        p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * pm) / j;
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0);
+      const double dz = p0 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) {
+        p0 = 1.0; p1 = 0.0;
+        for (int j = 1; j <= n; j++) {
+          const double pm = p1;
+          p1 = p0;
+          p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * pm) / j;
+        }
+        dp = n * (z * p0 - p1) / (z * z - 1.0);
+        break;
+      }
+    }
+    const double wt = 2.0 / ((1.0 - z * z) * dp * dp);
+    x[n - 1 - i] = z;
+    x[i] = -z;
+    w[n - 1 - i] = wt;
+    w[i] = wt;
+  }
+  if (n % 2 == 1) x[m - 1] = 0.0;
+}
+
+void natural_spline(const double* x, const double* y, int n, double* c)
+{
+  const int ns = n - 2;
+  std::vector<double> d(ns), o(ns), r(ns);
+  for (int i = 0; i < ns; i++) {
+    const double h0 = x[i + 1] - x[i], h1 = x[i + 2] - x[i + 1];
+    d[i] = 2.0 * (h0 + h1);
+    o[i] = h1;
+    r[i] = 3.0 * ((y[i + 2] - y[i + 1]) / h1 - (y[i + 1] - y[i]) / h0);
+  }
+  for (int i = 1; i < ns; i++) {
+    const double m = o[i - 1] / d[i - 1];
+    d[i] -= m * o[i - 1];
+    r[i] -= m * r[i - 1];
+  }
+  c[0] = 0.0;
+  c[n - 1] = 0.0;
+  if (ns > 0) {
+    c[ns] = r[ns - 1] / d[ns - 1];
+    for (int i = ns - 2; i >= 0; i--) c[i + 1] = (r[i] - o[i] * c[i + 2]) / d[i];
+  }
+}
+
+int bsearch_h(const double* x, int n, double v)
+{
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) / 2;
+    if (x[mid] > v) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+double spline_h(const double* x, const double* y, const double* c, int n, double v)
+{
+  const int i = bsearch_h(x, n, v);
+  const double h = x[i + 1] - x[i], t = v - x[i];
+  const double b = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+  const double d = (c[i + 1] - c[i]) / (3.0 * h);
+  return y[i] + t * (b + t * (c[i] + t * d));
+}
+
+// set_*_sample + the n(z) table of nz_*_photoz (see file header)
+int load_nz(NZHost& t, const cl2pt_nz* nz, bool is_source)
+{
+  const int N = nz->ntomo, n = nz->nzbins;
+  if (N < 1 || N > CL2PT_MAX_BINS || n < 3 || !nz->table) return CL2PT_ERR_ARG;
+  t.ntomo = N;
+  t.nzbins = n;
+  std::vector<double> zv(n), raw((size_t)N * n);
+  for (int i = 0; i < n; i++) {
+    zv[i] = nz->table[i * (N + 1)];
+    if (std::isnan(zv[i])) return CL2PT_ERR_ARG;
+    for (int k = 0; k < N; k++) {
+      const double v = nz->table[i * (N + 1) + k + 1];
+      if (std::isnan(v)) return CL2PT_ERR_ARG;
+      raw[(size_t)k * n + i] = v;
+    }
+  }
+  for (int i = 1; i < n; i++)
+    if (!(zv[i] > zv[i - 1])) return CL2PT_ERR_ARG;
+  t.zmin_all = fmax(zv[0], 1.e-5);
+  t.zmax_all = zv[n - 1] + (zv[n - 1] - zv[0]) / ((double)n - 1.);
+  for (int k = 0; k < N; k++) {
+    double mx = -INFINITY;
+    for (int i = 0; i < n; i++) mx = fmax(mx, raw[(size_t)k * n + i]);
+    int first = -1, last = -1;
+    for (int i = 0; i < n; i++)
+      if (raw[(size_t)k * n + i] > 0.999e-8 * mx) {
+        if (first < 0) first = i;
+        last = i;
+      }
+    if (first < 0) return CL2PT_ERR_NZ;
+    t.zmin[k] = is_source ? fmax(zv[first], 1.001e-5) : zv[first];
+    t.zmax[k] = zv[last];
+  }
+  t.zc.resize(n);
+  t.y.assign((size_t)(N + 1) * n, 0.0);
+  t.c.assign((size_t)(N + 1) * n, 0.0);
+  const double dz = (t.zmax_all - t.zmin_all) / ((double)n);
+  for (int k = 0; k < n; k++) t.zc[k] = t.zmin_all + (k + 0.5) * dz;
+  const double dzh = (zv[n - 1] - zv[0]) / ((double)n - 1.);
+  std::vector<double> h((size_t)N * n);
+  double NORM[CL2PT_MAX_BINS], norm = 0.0;
+  for (int i = 0; i < N; i++) {
+    NORM[i] = 0.0;
+    for (int k = 0; k < n; k++) {
+      const double z = t.zc[k];
+      double v = 0.0;
+      if (z >= t.zmin_all && z < t.zmax_all) {
+        const int nj = (int)floor((z - zv[0]) / dzh);
+        if (nj < 0 || nj > n - 1) return CL2PT_ERR_ARG;
+        v = raw[(size_t)i * n + nj];
+      }
+      h[(size_t)i * n + k] = v;
+      NORM[i] += v * dz;
+    }
+    if (!(NORM[i] > 0.0)) return CL2PT_ERR_NZ;
+    norm += NORM[i];
+  }
+  for (int k = 0; k < n; k++) {
+    for (int i = 0; i < N; i++) {
+      t.y[(size_t)(i + 1) * n + k] = h[(size_t)i * n + k] / NORM[i];
+      t.y[k] += t.y[(size_t)(i + 1) * n + k] * NORM[i] / norm;
+    }
+  }
+  for (int i = 0; i < N + 1; i++)
+    natural_spline(t.zc.data(), t.y.data() + (size_t)i * n, n, t.c.data() + (size_t)i * n);
+  return CL2PT_OK;
+}
+
+double nz_lens_h(const NZHost& t, double zz, int nj, double shift, double stretch, double zm)
+{
+  zz = (zz - shift - zm) / stretch + zm;
+  if (zz <= t.zc[0] || zz >= t.zc[t.nzbins - 1]) return 0.0;
+  return spline_h(t.zc.data(), t.y.data() + (size_t)(nj + 1) * t.nzbins,
+                  t.c.data() + (size_t)(nj + 1) * t.nzbins, t.nzbins, zz) / stretch;
+}
+
+// Bin-averaged Legendre filters of one theta bin for l = 1..L-1
+void legendre_filters(int L, double xmin, double xmax, double* Gp, double* Gm, double* Pgt,
+                      double* Pgg)
+{
+  std::vector<double> Pn(L + 1), Px(L + 1), dPn(L + 1), dPx(L + 1);
+  auto pl = [&](double x, double* P, double* dP) {
+    P[0] = 1.0; dP[0] = 0.0;
+    P[1] = x; dP[1] = 1.0;
+    for (int l = 2; l <= L; l++) P[l] = (x * (2.0 * l - 1.0) * P[l - 1] - (l - 1.0) * P[l - 2]) / l;
+    const double ap = 1.0 + x, am = 1.0 - x;
+    for (int l = 2; l <= L; l++) dP[l] = -l * (x * P[l] - P[l - 1]) / (ap * am);
+  };
+  pl(xmin, Pn.data(), dPn.data());
+  pl(xmax, Px.data(), dPx.data());
+  Gp[0] = Gm[0] = Pgt[0] = Pgg[0] = 0.0;
+  for (int l = 1; l < L; l++) {
+    const double A = -l * (l - 1.) / 2 * (l + 2. / (2 * l + 1)) * (Pn[l - 1] - Px[l - 1]);
+    const double Bq = -l * (l - 1.) * (2. - l) / 2 * (xmin * Pn[l] - xmax * Px[l]);
+    const double Cq = +l * (l - 1.) / (2. * l + 1) * (Pn[l + 1] - Px[l + 1]);
+    const double Dq = +(4 - l) * (dPn[l] - dPx[l]);
+    const double E = +(l + 2) * (xmin * dPn[l - 1] - xmax * dPx[l - 1] - Pn[l - 1] + Px[l - 1]);
+    const double F = 2 * (l - 1) * (xmin * dPn[l] - xmax * dPx[l] - Pn[l] + Px[l]);
+    const double Gq = 2 * (l + 2) * (dPn[l - 1] - dPx[l - 1]);
+    const double pre = (2. * l + 1) / (2. * M_PI * l * l * (l + 1) * (l + 1));
+    Gp[l] = pre * (A + Bq + Cq + Dq + E + F - Gq) / (xmin - xmax);
+    Gm[l] = pre * (A + Bq + Cq + Dq + E - F + Gq) / (xmin - xmax);
+    Pgt[l] = (2. * l + 1) / (4. * M_PI * l * (l + 1) * (xmin - xmax)) *
+             ((l + 2. / (2 * l + 1.)) * (Pn[l - 1] - Px[l - 1]) +
+              (2 - l) * (xmin * Pn[l] - xmax * Px[l]) - 2. / (2 * l + 1.) * (Pn[l + 1] - Px[l + 1]));
+    Pgg[l] = (1.0 / (xmin - xmax)) * (1. / (4.0 * M_PI)) *
+             (Pn[l + 1] - Px[l + 1] - Pn[l - 1] + Px[l - 1]);
+  }
+}
+
+// Fold a per-l filter f[1..L-1] onto C_l nodes: integer multipoles
+// 1..nint stay as they are (columns 0..nint-1), multipoles lfill..L-1 are
+// spread on the n_ell log nodes (columns nint..) with the fill's weights.
+void fold(const double* f, int L, int nint, int lfill, const double* lim, int nell, double* out)
+{
+  for (int l = 1; l <= nint && l < L; l++) out[l - 1] = f[l];
+  const double inv = 1.0 / lim[2];
+  for (int l = lfill; l < L; l++) {
+    const double r = (log((double)l) - lim[0]) * inv;
+    const int i = (int)floor(r);
+    const int ic = i < 0 ? 0 : (i >= nell - 1 ? nell - 2 : i);
+    const double t = r - ic;
+    out[nint + ic] += f[l] * (1.0 - t);
+    out[nint + ic + 1] += f[l] * t;
+  }
+}
+
+template <typename T>
+int dupload(cl2pt_plan* p, T** dst, const T* src, size_t n)
+{
+  void* d = nullptr;
+  CUDA_OK(cudaMalloc(&d, std::max<size_t>(n, 1) * sizeof(T)));
+  p->dbufs.push_back(d);
+  if (n) CUDA_OK(cudaMemcpy(d, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = (T*)d;
+  return CL2PT_OK;
+}
+
+template <typename T>
+int dalloc(cl2pt_plan* p, T** dst, size_t n)
+{
+  void* d = nullptr;
+  CUDA_OK(cudaMalloc(&d, std::max<size_t>(n, 1) * sizeof(T)));
+  p->dbufs.push_back(d);
+  *dst = (T*)d;
+  return CL2PT_OK;
+}
+
+long next7(long n)
+{
+  for (;;) {
+    long m = n;
+    while (m % 2 == 0) m /= 2;
+    while (m % 3 == 0) m /= 3;
+    while (m % 5 == 0) m /= 5;
+    while (m % 7 == 0) m /= 7;
+    if (m == 1) return n;
+    n++;
+  }
+}
+
+bool all_finite(const double* p, int n)
+{
+  for (int i = 0; i < n; i++)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+bool increasing(const double* p, int n)
+{
+  for (int i = 1; i < n; i++)
+    if (!(p[i] > p[i - 1])) return false;
+  return true;
+}
+
+}  // namespace
+
+#define TRY(x)                      \
+  do {                              \
+    int st_ = (x);                  \
+    if (st_ != CL2PT_OK) {          \
+      cl2pt_plan_destroy(p);        \
+      return st_;                   \
+    }                               \
+  } while (0)
+
+extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
+                                 const cl2pt_nz* lens, const cl2pt_grid* grid, int precision,
+                                 int max_batch, cl2pt_plan** out)
+{
+  if (!cfg || !src || !lens || !grid || !out || max_batch < 1) return CL2PT_ERR_ARG;
+  *out = nullptr;
+  if (cfg->n_source < 1 || cfg->n_source > CL2PT_MAX_BINS || cfg->n_lens < 1 ||
+      cfg->n_lens > CL2PT_MAX_BINS || cfg->n_source != src->ntomo || cfg->n_lens != lens->ntomo)
+    return CL2PT_ERR_ARG;
+  if (cfg->ntheta < 1 || cfg->lmax < 3 || cfg->n_ell < 2 || cfg->n_a < 2 || cfg->lmin_tab < 2 ||
+      cfg->lmax_nolimber < 2 || cfg->lmax_nolimber > cfg->lmax || cfg->nl_nchi < 8 ||
+      !(cfg->theta_max_arcmin > cfg->theta_min_arcmin) || !(cfg->theta_min_arcmin > 0))
+    return CL2PT_ERR_ARG;
+  if (precision != CL2PT_PREC_MIXED && precision != CL2PT_PREC_FP64) return CL2PT_ERR_ARG;
+  if (cfg->ia_mode == CL2PT_IA_NLA_LF) return CL2PT_ERR_UNSUPPORTED;
+  if (cfg->ia_model == CL2PT_IA_TATT) return CL2PT_ERR_UNSUPPORTED;
+  if (cfg->bias_model[4] != 0 || cfg->bias_model[5] != 0) return CL2PT_ERR_ARG;
+  if (grid->chi_nz < 5 || grid->G_nz < 2 || grid->pk_nk < 2 || grid->pk_nz < 2)
+    return CL2PT_ERR_ARG;
+  if (!increasing(grid->chi_z, grid->chi_nz) || !increasing(grid->G_z, grid->G_nz) ||
+      !increasing(grid->pk_log10k, grid->pk_nk) || !increasing(grid->pk_z, grid->pk_nz))
+    return CL2PT_ERR_ARG;
+
+  cl2pt_plan* p = new cl2pt_plan();
+  p->cfg = *cfg;
+  p->prec = precision;
+  p->max_batch = max_batch;
+  TRY(load_nz(p->src, src, true));
+  TRY(load_nz(p->lens, lens, false));
+
+  // lens mean redshift with zero shift, unit stretch (redshift_spline.c:794-844)
+  {
+    const int h = abs(cfg->high_def_integration);
+    const int sz = (h == 0) ? 256 : (h == 1) ? 512 : 1024;
+    std::vector<double> x, w;
+    gl_rule(sz, x, w);
+    for (int i = 0; i < cfg->n_lens; i++) {
+      const double a = p->lens.zmin[i], b = p->lens.zmax[i];
+      const double A = 0.5 * (b - a), Bc = 0.5 * (b + a);
+      double num = 0.0, den = 0.0;
+      for (int q = 0; q < sz; q++) {
+        const double z = Bc + A * x[q], wt = A * w[q];
+        const double v = nz_lens_h(p->lens, z, i, 0.0, 1.0, 0.0);
+        num += wt * z * v;
+        den += wt * v;
+      }
+      if (!(den > 0.0)) TRY(CL2PT_ERR_NZ);
+      p->zmean_lens[i] = num / den;
+    }
+  }
+  // pair maps
+  {
+    int n = 0;
+    for (int i = 0; i < cfg->n_source; i++)
+      for (int j = i; j < cfg->n_source; j++) {
+        p->z1[n] = i;
+        p->z2[n] = j;
+        n++;
+      }
+    p->pss = n;
+    n = 0;
+    for (int i = 0; i < cfg->n_lens; i++)
+      for (int j = 0; j < cfg->n_source; j++) {
+        bool ok = true;
+        for (int e = 0; e < cfg->n_ggl_exclude; e++)
+          if (cfg->ggl_exclude[2 * e] == i && cfg->ggl_exclude[2 * e + 1] == j) ok = false;
+        if (ok) {
+          p->zl[n] = i;
+          p->zs[n] = j;
+          n++;
+        }
+      }
+    p->pgs = n;
+    p->pgg = cfg->n_lens;
+    const int nt = cfg->ntheta;
+    p->n_xi = 2 * nt * p->pss;
+    p->n_gammat = nt * p->pgs;
+    p->n_w = nt * p->pgg;
+    p->n_total = p->n_xi + p->n_gammat + p->n_w;
+  }
+  // quadrature sizes (cosmo2D.c:1577-1581, 2636-2639)
+  {
+    const int h = abs(cfg->high_def_integration);
+    p->n_ss = h == 0 ? 64 : h == 1 ? 96 : h == 2 ? 128 : h == 3 ? 256 : 512;
+    p->n_gg = h == 0 ? 96 : h == 1 ? 128 : h == 2 ? 256 : h == 3 ? 512 : 1024;
+  }
+  // C_l nodes
+  p->nint = cfg->lmin_tab - 1;
+  p->nnode_ss = p->nint + cfg->n_ell;
+  p->nnode_g = p->nint + cfg->n_ell;
+  p->lim_ss[0] = log(fmax(cfg->lmin_tab - 1., 1.0));
+  p->lim_ss[1] = log(cfg->lmax + 1.0);
+  p->lim_ss[2] = (p->lim_ss[1] - p->lim_ss[0]) / ((double)cfg->n_ell - 1.);
+  p->lim_g[0] = log(fmax((double)cfg->lmin_tab, 1.0));
+  p->lim_g[1] = log(cfg->lmax + 1.0);
+  p->lim_g[2] = (p->lim_g[1] - p->lim_g[0]) / ((double)cfg->n_ell - 1.);
+  std::vector<double> ell_ss(p->nnode_ss), ell_g(p->nnode_g);
+  for (int l = 1; l <= p->nint; l++) ell_ss[l - 1] = ell_g[l - 1] = (double)l;
+  for (int i = 0; i < cfg->n_ell; i++) {
+    ell_ss[p->nint + i] = exp(p->lim_ss[0] + i * p->lim_ss[2]);
+    ell_g[p->nint + i] = exp(p->lim_g[0] + i * p->lim_g[2]);
+  }
+  // Legendre filters, folded
+  const int nt = cfg->ntheta, L = cfg->lmax, LNL = cfg->lmax_nolimber;
+  std::vector<double> fxi((size_t)2 * nt * p->nnode_ss, 0.0), fgt((size_t)nt * p->nnode_g, 0.0),
+      fgg((size_t)nt * p->nnode_g, 0.0), fggnl((size_t)nt * (LNL + p->nnode_g), 0.0);
+  {
+    const double vtmin = cfg->theta_min_arcmin * 2.90888208665721580e-4;
+    const double vtmax = cfg->theta_max_arcmin * 2.90888208665721580e-4;
+    const double logdt = (log(vtmax) - log(vtmin)) / nt;
+    auto work = [&](int i) {
+      const double xmin = cos(exp(log(vtmin) + (i + 0.) * logdt));
+      const double xmax = cos(exp(log(vtmin) + (i + 1.) * logdt));
+      std::vector<double> Gp(L), Gm(L), Pgt(L), Pgg(L);
+      legendre_filters(L, xmin, xmax, Gp.data(), Gm.data(), Pgt.data(), Pgg.data());
+      fold(Gp.data(), L, p->nint, cfg->lmin_tab, p->lim_ss, cfg->n_ell,
+           fxi.data() + (size_t)(0 * nt + i) * p->nnode_ss);
+      fold(Gm.data(), L, p->nint, cfg->lmin_tab, p->lim_ss, cfg->n_ell,
+           fxi.data() + (size_t)(1 * nt + i) * p->nnode_ss);
+      fold(Pgt.data(), L, p->nint, cfg->lmin_tab, p->lim_g, cfg->n_ell,
+           fgt.data() + (size_t)i * p->nnode_g);
+      fold(Pgg.data(), L, p->nint, cfg->lmin_tab, p->lim_g, cfg->n_ell,
+           fgg.data() + (size_t)i * p->nnode_g);
+      // non-Limber w: explicit l = 0..LNL-1 head (l = 0 has no weight), then
+      // the fill from LMAX_NOLIMBER on the log nodes (cosmo2D.c:850-857)
+      double* o = fggnl.data() + (size_t)i * (LNL + p->nnode_g);
+      for (int l = 1; l < LNL; l++) o[l] = Pgg[l];
+      fold(Pgg.data(), L, 0, LNL, p->lim_g, cfg->n_ell, o + LNL + p->nint);
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < nt; i++) th.emplace_back(work, i);
+    for (auto& t : th) t.join();
+  }
+  // shared axes
+  p->chi_z.assign(grid->chi_z, grid->chi_z + grid->chi_nz);
+  p->G_z.assign(grid->G_z, grid->G_z + grid->G_nz);
+  p->pk_lk.assign(grid->pk_log10k, grid->pk_log10k + grid->pk_nk);
+  p->pk_z.assign(grid->pk_z, grid->pk_z + grid->pk_nz);
+  if (grid->pkl_nk > 0) {
+    if (grid->pkl_nk < 2 || grid->pkl_nz < 2 || !increasing(grid->pkl_log10k, grid->pkl_nk) ||
+        !increasing(grid->pkl_z, grid->pkl_nz))
+      TRY(CL2PT_ERR_ARG);
+    p->pkl_lk.assign(grid->pkl_log10k, grid->pkl_log10k + grid->pkl_nk);
+    p->pkl_z.assign(grid->pkl_z, grid->pkl_z + grid->pkl_nz);
+  } else {
+    p->pkl_lk = p->pk_lk;
+    p->pkl_z = p->pk_z;
+  }
+  // device constants
+  std::vector<double> glx, glw, ggx, ggw;
+  gl_rule(p->n_ss, glx, glw);
+  gl_rule(p->n_gg, ggx, ggw);
+  TRY(dupload(p, &p->d_chi_z, p->chi_z.data(), p->chi_z.size()));
+  TRY(dupload(p, &p->d_G_z, p->G_z.data(), p->G_z.size()));
+  TRY(dupload(p, &p->d_pk_lk, p->pk_lk.data(), p->pk_lk.size()));
+  TRY(dupload(p, &p->d_pk_z, p->pk_z.data(), p->pk_z.size()));
+  TRY(dupload(p, &p->d_pkl_lk, p->pkl_lk.data(), p->pkl_lk.size()));
+  TRY(dupload(p, &p->d_pkl_z, p->pkl_z.data(), p->pkl_z.size()));
+  TRY(dupload(p, &p->d_src_zc, p->src.zc.data(), p->src.zc.size()));
+  TRY(dupload(p, &p->d_src_y, p->src.y.data(), p->src.y.size()));
+  TRY(dupload(p, &p->d_src_c, p->src.c.data(), p->src.c.size()));
+  TRY(dupload(p, &p->d_lens_zc, p->lens.zc.data(), p->lens.zc.size()));
+  TRY(dupload(p, &p->d_lens_y, p->lens.y.data(), p->lens.y.size()));
+  TRY(dupload(p, &p->d_lens_c, p->lens.c.data(), p->lens.c.size()));
+  TRY(dupload(p, &p->d_gl_ss_x, glx.data(), glx.size()));
+  TRY(dupload(p, &p->d_gl_ss_w, glw.data(), glw.size()));
+  TRY(dupload(p, &p->d_gl_gg_x, ggx.data(), ggx.size()));
+  TRY(dupload(p, &p->d_gl_gg_w, ggw.data(), ggw.size()));
+  TRY(dupload(p, &p->d_ell_ss, ell_ss.data(), ell_ss.size()));
+  TRY(dupload(p, &p->d_ell_g, ell_g.data(), ell_g.size()));
+  TRY(dupload(p, &p->d_filt_xi, fxi.data(), fxi.size()));
+  TRY(dupload(p, &p->d_filt_gt, fgt.data(), fgt.size()));
+  TRY(dupload(p, &p->d_filt_gg, fgg.data(), fgg.size()));
+  TRY(dupload(p, &p->d_filt_gg_nl, fggnl.data(), fggnl.size()));
+  int *dz1, *dz2, *dzl, *dzs;
+  TRY(dupload(p, &dz1, p->z1, p->pss));
+  TRY(dupload(p, &dz2, p->z2, p->pss));
+  TRY(dupload(p, &dzl, p->zl, std::max(p->pgs, 1)));
+  TRY(dupload(p, &dzs, p->zs, std::max(p->pgs, 1)));
+
+  // workspace sized for one wave of points
+  p->wave = std::min(max_batch, 256);
+  const int W = p->wave, ns = cfg->n_source, nl = cfg->n_lens;
+  p->node_stride = p->n_ss + nl * p->n_ss + nl * p->n_gg;
+  Params& P = p->P;
+  memset(&P, 0, sizeof(P));
+  P.ns = ns; P.nl = nl; P.ntheta = nt; P.lmax = L; P.n_ell = cfg->n_ell;
+  P.hdi = cfg->high_def_integration; P.lmin_tab = cfg->lmin_tab; P.lmax_nolimber = LNL;
+  P.nl_nchi = cfg->nl_nchi; P.a_min = cfg->a_min; P.adopt_limber_gg = cfg->adopt_limber_gg;
+  P.ia_model = cfg->ia_model; P.ia_mode = cfg->ia_mode; P.linear_pk = cfg->linear_pk;
+  P.probes = cfg->probes;
+  for (int i = 0; i < 6; i++) P.bias_model[i] = cfg->bias_model[i];
+  P.prec = precision;
+  P.pss = p->pss; P.pgs = p->pgs; P.pgg = p->pgg;
+  P.n_a = cfg->n_a; P.n_ss = p->n_ss; P.n_gg = p->n_gg;
+  P.nnode_ss = p->nnode_ss; P.nnode_g = p->nnode_g; P.nint = p->nint;
+  for (int i = 0; i < 3; i++) { P.lim_ss[i] = p->lim_ss[i]; P.lim_g[i] = p->lim_g[i]; }
+  P.chi_nz = grid->chi_nz; P.G_nz = grid->G_nz;
+  P.pk_nk = grid->pk_nk; P.pk_nz = grid->pk_nz;
+  P.pkl_nk = (int)p->pkl_lk.size(); P.pkl_nz = (int)p->pkl_z.size();
+  P.chi_z = p->d_chi_z; P.G_z = p->d_G_z; P.pk_lk = p->d_pk_lk; P.pk_z = p->d_pk_z;
+  P.pkl_lk = p->d_pkl_lk; P.pkl_z = p->d_pkl_z;
+  P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
+  P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
+  P.lens_zc = p->d_lens_zc; P.lens_y = p->d_lens_y; P.lens_c = p->d_lens_c;
+  P.src_zmin_all = p->src.zmin_all; P.src_zmax_all = p->src.zmax_all;
+  P.lens_zmax_all = p->lens.zmax_all;
+  for (int i = 0; i < nl; i++) {
+    P.lens_zmin[i] = p->lens.zmin[i];
+    P.lens_zmax[i] = p->lens.zmax[i];
+    P.zmean_lens[i] = p->zmean_lens[i];
+  }
+  P.gl_ss_x = p->d_gl_ss_x; P.gl_ss_w = p->d_gl_ss_w;
+  P.gl_gg_x = p->d_gl_gg_x; P.gl_gg_w = p->d_gl_gg_w;
+  P.z1 = dz1; P.z2 = dz2; P.zl = dzl; P.zs = dzs;
+  P.node_stride = p->node_stride;
+  TRY(dalloc(p, &P.gsrc, (size_t)W * ns * cfg->n_a));
+  TRY(dalloc(p, &P.glens, (size_t)W * nl * cfg->n_a));
+  TRY(dalloc(p, &P.node, (size_t)W * cl2pt::NF_COUNT * p->node_stride));
+  TRY(dalloc(p, &P.node_j, (size_t)W * p->node_stride));
+  TRY(dalloc(p, &P.wss, (size_t)W * ns * p->n_ss));
+  TRY(dalloc(p, &P.wgs_x, (size_t)W * nl * ns * p->n_ss));
+  TRY(dalloc(p, &P.wgs_l, (size_t)W * nl * p->n_ss));
+  TRY(dalloc(p, &P.wgs_m, (size_t)W * nl * p->n_ss));
+  TRY(dalloc(p, &P.wgg_l, (size_t)W * nl * p->n_gg));
+  TRY(dalloc(p, &P.wgg_m, (size_t)W * nl * p->n_gg));
+  TRY(dalloc(p, &P.wgg_r0, (size_t)W * nl * p->n_gg));
+  TRY(dalloc(p, &P.chi_amin, (size_t)W));
+  TRY(dalloc(p, &P.tab_ss, (size_t)W * p->pss * p->nnode_ss));
+  TRY(dalloc(p, &P.tab_gs, (size_t)W * std::max(p->pgs, 1) * p->nnode_g));
+  TRY(dalloc(p, &P.tab_gg, (size_t)W * nl * p->nnode_g));
+  TRY(dalloc(p, &P.ggl, (size_t)W * nl * LNL * 2));
+  TRY(dalloc(p, &P.cnl, (size_t)W * nl * LNL));
+  TRY(dalloc(p, &P.conv_l, (size_t)W * nl));
+  TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
+  TRY(dalloc(p, &p->d_err, 4));
+  P.err = p->d_err;
+  // staging for host batches
+  const size_t B = (size_t)max_batch;
+  TRY(dalloc(p, &p->d_in_om, B));
+  TRY(dalloc(p, &p->d_in_h0, B));
+  TRY(dalloc(p, &p->d_in_chi, B * grid->chi_nz));
+  TRY(dalloc(p, &p->d_in_G, B * grid->G_nz));
+  TRY(dalloc(p, &p->d_in_lnP, B * grid->pk_nk * grid->pk_nz));
+  if (grid->pkl_nk > 0) TRY(dalloc(p, &p->d_in_lnPL, B * P.pkl_nk * P.pkl_nz));
+  TRY(dalloc(p, &p->d_in_nu, B));
+  TRY(dalloc(p, &p->d_mask, (size_t)p->n_total));
+  TRY(dalloc(p, &p->d_pm, B * nl));
+  TRY(dalloc(p, &p->d_dv, B * p->n_total));
+  P.theta_min_rad = cfg->theta_min_arcmin * 2.90888208665721580e-4;
+  P.theta_max_rad = cfg->theta_max_arcmin * 2.90888208665721580e-4;
+  // non-Limber FFTLog constants (cosmo2D.c:4564-4577, 4622-4637)
+  {
+    cl2pt::NLParams& Q = p->nlq;
+    memset(&Q, 0, sizeof(Q));
+    const double nu3[3] = {1., 1.01, 1.};
+    const int der3[3] = {0, 2, 0}, pad3[3] = {200, 500, 500};
+    Q.nmax = 0;
+    for (int j = 0; j < 3; j++) {
+      Q.nu[j] = nu3[j];
+      Q.deriv[j] = der3[j];
+      Q.pad[j] = pad3[j];
+      long raw = 2 * pad3[j] + cfg->nl_nchi;
+      if (raw % 2) raw++;
+      long Nn = next7(raw);
+      if (Nn % 2) Nn = next7(Nn + 1);
+      Q.N[j] = (int)Nn;
+      Q.nmax = std::max(Q.nmax, Q.N[j]);
+      // Stockham factors: 4s, then 2, 3, 5, 7
+      long m = Nn;
+      int nf = 0;
+      const int fs[5] = {4, 2, 3, 5, 7};
+      for (int f = 0; f < 5; f++)
+        while (m % fs[f] == 0 && nf < 16) { Q.fac[j][nf++] = fs[f]; m /= fs[f]; }
+      if (m != 1) TRY(CL2PT_ERR_ARG);
+      Q.nfac[j] = nf;
+      std::vector<double> tw(2 * (size_t)Nn);
+      for (long k = 0; k < Nn; k++) {
+        const double ang = 2.0 * M_PI * (double)k / (double)Nn;
+        tw[2 * k] = cos(ang);
+        tw[2 * k + 1] = sin(ang);
+      }
+      double* dtw;
+      TRY(dupload(p, &dtw, tw.data(), tw.size()));
+      Q.tw[j] = dtw;
+    }
+    Q.hstride = Q.nmax / 2 + 1;
+    Q.tout_stride = (size_t)3 * Q.hstride;
+    Q.gst_stride = (size_t)3 * 2 * Q.hstride;
+    if (!cfg->adopt_limber_gg && (cfg->probes & CL2PT_PROBE_WTHETA)) {
+      TRY(dalloc(p, &Q.tout, (size_t)W * nl * Q.tout_stride * 2));
+      TRY(dalloc(p, &Q.gstate, (size_t)W * nl * Q.gst_stride * 2));
+    }
+  }
+  CUDA_OK(cudaMemset(p->d_err, 0, 4));
+  *out = p;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_plan_destroy(cl2pt_plan* p)
+{
+  if (!p) return CL2PT_OK;
+  for (void* d : p->dbufs) cudaFree(d);
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  delete p;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_real_sizes(const cl2pt_plan* p, int* n_xi, int* n_gammat, int* n_w,
+                                int* n_total)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (n_xi) *n_xi = p->n_xi;
+  if (n_gammat) *n_gammat = p->n_gammat;
+  if (n_w) *n_w = p->n_w;
+  if (n_total) *n_total = p->n_total;
+  return CL2PT_OK;
+}
+
+extern "C" const char* cl2pt_status_string(int s)
+{
+  switch (s) {
+    case CL2PT_OK: return "ok";
+    case CL2PT_ERR_ARG: return "invalid argument";
+    case CL2PT_ERR_NZ: return "n(z) normalisation is not positive";
+    case CL2PT_ERR_CUDA: return "CUDA runtime error";
+    case CL2PT_ERR_UNSUPPORTED: return "option not supported";
+    case CL2PT_ERR_STATE: return "call made before its prerequisites";
+    case CL2PT_ERR_DEVICE: return "device-side check failed";
+    case CL2PT_ERR_FFT: return "FFT log-extrapolation failed";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int cl2pt_last_launch_count(const cl2pt_plan* p) { return p ? p->last_launches : 0; }
+
+// ------------------------------------------------------------ evaluation
+static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b)
+{
+  if (!b || b->n < 1 || b->n > p->max_batch) return CL2PT_ERR_ARG;
+  if (!b->omega_m || !b->h0 || !b->chi || !b->G || !b->lnP || !b->nuisance) return CL2PT_ERR_ARG;
+  if (b->where != CL2PT_HOST && b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
+  if (b->where == CL2PT_HOST) {
+    // host-side validation of the inputs the reference rejects (NaN checks
+    // of every setter, generic_interface.cpp:993-1267)
+    const int n = b->n;
+    if (!all_finite(b->omega_m, n) || !all_finite(b->h0, n)) return CL2PT_ERR_ARG;
+    if (!all_finite(b->chi, n * p->P.chi_nz) || !all_finite(b->G, n * p->P.G_nz))
+      return CL2PT_ERR_ARG;
+    if (!all_finite(b->lnP, n * p->P.pk_nk * p->P.pk_nz)) return CL2PT_ERR_ARG;
+    for (int i = 0; i < n; i++) {
+      const cl2pt_nuisance& nu = b->nuisance[i];
+      if (!all_finite((const double*)&nu, sizeof(nu) / sizeof(double))) return CL2PT_ERR_ARG;
+      for (int q = 0; q < p->cfg.n_lens; q++)
+        if (!(nu.lens_stretch[q] > 0)) return CL2PT_ERR_ARG;
+    }
+  }
+  return CL2PT_OK;
+}
+
+int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
+                             const double* pm, double* dv, cudaStream_t s);
+
+extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
+                               const double* pm, double* dv, void* stream)
+{
+  if (!p || !dv) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  return cl2pt_internal_eval_real(p, b, mask, pm, dv, (cudaStream_t)stream);
+}
+
+// Stage the batch on the device (when it lives on the host), then run the
+// pipeline wave by wave so the per-wave workspace stays L2-sized.
+int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
+                             const double* pm, double* dv, cudaStream_t s)
+{
+  const int n = b->n;
+  const Params& T = p->P;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz,
+               nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const double *om, *h0, *chi, *G, *lnP, *lnPL;
+  const cl2pt_nuisance* nu;
+  const int* dmask = nullptr;
+  const double* dpm = nullptr;
+  double* ddv;
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaMemcpyAsync(p->d_in_om, b->omega_m, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_h0, b->h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_chi, b->chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_G, b->G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_lnP, b->lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (b->lnPL && p->d_in_lnPL)
+      CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL, b->lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_nu, b->nuisance, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
+    om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP;
+    lnPL = (b->lnPL && p->d_in_lnPL) ? p->d_in_lnPL : p->d_in_lnP;
+    nu = p->d_in_nu;
+    if (mask) {
+      CUDA_OK(cudaMemcpyAsync(p->d_mask, mask, p->n_total * sizeof(int), cudaMemcpyHostToDevice, s));
+      dmask = p->d_mask;
+    }
+    if (pm) {
+      CUDA_OK(cudaMemcpyAsync(p->d_pm, pm, (size_t)n * p->cfg.n_lens * sizeof(double), cudaMemcpyHostToDevice, s));
+      dpm = p->d_pm;
+    }
+    ddv = p->d_dv;
+  } else {
+    om = b->omega_m; h0 = b->h0; chi = b->chi; G = b->G; lnP = b->lnP;
+    lnPL = b->lnPL ? b->lnPL : b->lnP;
+    nu = b->nuisance;
+    dmask = mask;
+    dpm = pm;
+    ddv = dv;
+  }
+  if (!b->lnPL && (T.pkl_nk != T.pk_nk || T.pkl_nz != T.pk_nz)) return CL2PT_ERR_ARG;
+  int launches = 0;
+  struct HookCtx { cl2pt_plan* p; cudaStream_t s; cudaEvent_t (*ev)(cl2pt_plan*); };
+  cl2pt::Hook hk;
+  HookCtx hc{p, s, [](cl2pt_plan* pp) -> cudaEvent_t {
+    if (pp->ev_used == pp->ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pp->ev_pool.push_back(e);
+    }
+    return pp->ev_pool[pp->ev_used++];
+  }};
+  if (p->timing) {
+    hk.ctx = &hc;
+    hk.fn = [](void* c, int k, int begin) {
+      HookCtx* h = (HookCtx*)c;
+      cudaEvent_t e = h->ev(h->p);
+      cudaEventRecord(e, h->s);
+      if (begin) {
+        cl2pt_plan::Rec r;
+        r.stage = k;
+        r.a = e;
+        r.b = nullptr;
+        r.launches = 1;
+        h->p->recs.push_back(r);
+      } else {
+        h->p->recs.back().b = e;
+      }
+    };
+  }
+  for (int w0 = 0; w0 < n; w0 += p->wave) {
+    Params P = T;
+    P.B = std::min(p->wave, n - w0);
+    P.omega_m = om + w0;
+    P.h0 = h0 + w0;
+    P.chi = chi + (size_t)w0 * nchi;
+    P.G = G + (size_t)w0 * nG;
+    P.lnP = lnP + (size_t)w0 * nP;
+    P.lnPL = lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    P.nu = nu + w0;
+    cl2pt::launch_setup(P, s, &launches, hk);
+    cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+    if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg)
+      cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
+    cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
+                           s, &launches, hk);
+    cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
+                           ddv + (size_t)w0 * p->n_total, s, &launches, hk);
+  }
+  CUDA_OK(cudaGetLastError());
+  p->last_launches = launches;
+  p->last_batch = n;
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaMemcpyAsync(dv, p->d_dv, (size_t)n * p->n_total * sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+    int err = 0;
+    CUDA_OK(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    if (err) {
+      cudaMemsetAsync(p->d_err, 0, sizeof(int), s);
+      return CL2PT_ERR_DEVICE;
+    }
+  }
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_check_errors(cl2pt_plan* p, void* stream)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int err = 0;
+  CUDA_OK(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_OK(cudaStreamSynchronize(s));
+  if (err) {
+    CUDA_OK(cudaMemset(p->d_err, 0, sizeof(int)));
+    return CL2PT_ERR_DEVICE;
+  }
+  return CL2PT_OK;
+}
+
+// ---------------------------------------------------------- debug copies
+// These read the workspace of the last wave, so `point` indexes into the
+// last wave (callers use batches no larger than one wave).
+extern "C" int cl2pt_debug_limber_tables(const cl2pt_plan* p, int point, double* ss, double* gs,
+                                         double* gg)
+{
+  if (!p || point < 0 || point >= std::min(p->wave, p->last_batch)) return CL2PT_ERR_ARG;
+  CUDA_OK(cudaDeviceSynchronize());
+  const Params& P = p->P;
+  if (ss) {
+    CUDA_OK(cudaMemcpy(ss, P.tab_ss + (size_t)point * p->pss * p->nnode_ss,
+                       sizeof(double) * p->pss * p->nnode_ss, cudaMemcpyDeviceToHost));
+  }
+  if (gs && p->pgs) {
+    CUDA_OK(cudaMemcpy(gs, P.tab_gs + (size_t)point * p->pgs * p->nnode_g,
+                       sizeof(double) * p->pgs * p->nnode_g, cudaMemcpyDeviceToHost));
+  }
+  if (gg) {
+    CUDA_OK(cudaMemcpy(gg, P.tab_gg + (size_t)point * p->pgg * p->nnode_g,
+                       sizeof(double) * p->pgg * p->nnode_g, cudaMemcpyDeviceToHost));
+  }
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_debug_nonlimber(const cl2pt_plan* p, int point, double* cl, int* conv_l)
+{
+  if (!p || point < 0 || point >= std::min(p->wave, p->last_batch)) return CL2PT_ERR_ARG;
+  CUDA_OK(cudaDeviceSynchronize());
+  const Params& P = p->P;
+  const int nl = p->cfg.n_lens, L = p->cfg.lmax_nolimber;
+  if (cl) CUDA_OK(cudaMemcpy(cl, P.cnl + (size_t)point * nl * L, sizeof(double) * nl * L,
+                             cudaMemcpyDeviceToHost));
+  if (conv_l) CUDA_OK(cudaMemcpy(conv_l, P.conv_l + (size_t)point * nl, sizeof(int) * nl,
+                                 cudaMemcpyDeviceToHost));
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_debug_g_tables(const cl2pt_plan* p, int point, double* gsrc)
+{
+  if (!p || point < 0 || point >= std::min(p->wave, p->last_batch)) return CL2PT_ERR_ARG;
+  CUDA_OK(cudaDeviceSynchronize());
+  const Params& P = p->P;
+  CUDA_OK(cudaMemcpy(gsrc, P.gsrc + (size_t)point * p->cfg.n_source * p->cfg.n_a,
+                     sizeof(double) * p->cfg.n_source * p->cfg.n_a, cudaMemcpyDeviceToHost));
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_set_timing(cl2pt_plan* p, int enable)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  p->timing = enable != 0;
+  p->recs.clear();
+  p->ev_used = 0;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_kernel_times(cl2pt_plan* p, double* ms, int* launches)
+{
+  if (!p || !ms) return CL2PT_ERR_ARG;
+  for (int i = 0; i < CL2PT_NKERNEL; i++) {
+    ms[i] = 0.0;
+    if (launches) launches[i] = 0;
+  }
+  for (auto& r : p->recs) {
+    CUDA_OK(cudaEventSynchronize(r.b));
+    float t = 0.f;
+    CUDA_OK(cudaEventElapsedTime(&t, r.a, r.b));
+    ms[r.stage] += t;
+    if (launches) launches[r.stage] += r.launches;
+  }
+  p->recs.clear();
+  p->ev_used = 0;
+  return CL2PT_OK;
+}

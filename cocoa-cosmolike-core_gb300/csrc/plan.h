@@ -1,0 +1,71 @@
+// plan.h -- host-side plan object of libcl2pt.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "cl2pt.h"
+#include "common.cuh"
+#include "nonlimber.h"
+
+struct NZHost {
+  int ntomo = 0, nzbins = 0;
+  double zmin_all = 0, zmax_all = 0;
+  double zmin[CL2PT_MAX_BINS] = {0}, zmax[CL2PT_MAX_BINS] = {0};
+  std::vector<double> zc;  // spline nodes [nzbins]
+  std::vector<double> y;   // [(ntomo+1)][nzbins]
+  std::vector<double> c;   // spline coefficients, same shape
+};
+
+struct cl2pt_plan {
+  cl2pt_config cfg;
+  int prec = CL2PT_PREC_MIXED;
+  int max_batch = 0;
+  int wave = 0;          // points per internal wave (workspace size)
+  NZHost src, lens;
+  double zmean_lens[CL2PT_MAX_BINS] = {0};
+  int pss = 0, pgs = 0, pgg = 0;
+  int n_xi = 0, n_gammat = 0, n_w = 0, n_total = 0;
+  int z1[CL2PT_MAX_BINS * CL2PT_MAX_BINS], z2[CL2PT_MAX_BINS * CL2PT_MAX_BINS];
+  int zl[CL2PT_MAX_BINS * CL2PT_MAX_BINS], zs[CL2PT_MAX_BINS * CL2PT_MAX_BINS];
+  int n_ss = 0, n_gg = 0;
+  int nint = 0, nnode_ss = 0, nnode_g = 0;
+  double lim_ss[3], lim_g[3];
+  // host copies of shared axes
+  std::vector<double> chi_z, G_z, pk_lk, pk_z, pkl_lk, pkl_z;
+  // device buffers owned by the plan
+  std::vector<void*> dbufs;
+  double *d_chi_z = nullptr, *d_G_z = nullptr, *d_pk_lk = nullptr, *d_pk_z = nullptr,
+         *d_pkl_lk = nullptr, *d_pkl_z = nullptr;
+  double *d_src_zc = nullptr, *d_src_y = nullptr, *d_src_c = nullptr;
+  double *d_lens_zc = nullptr, *d_lens_y = nullptr, *d_lens_c = nullptr;
+  double *d_gl_ss_x = nullptr, *d_gl_ss_w = nullptr, *d_gl_gg_x = nullptr, *d_gl_gg_w = nullptr;
+  double *d_ell_ss = nullptr, *d_ell_g = nullptr;       // C_l node multipoles
+  double* d_filt_xi = nullptr;   // [2][ntheta][nnode_ss]   G+, G- folded
+  double* d_filt_gt = nullptr;   // [ntheta][nnode_g]
+  double* d_filt_gg = nullptr;   // [ntheta][nnode_g]       folded from lmin_tab
+  double* d_filt_gg_nl = nullptr;// [ntheta][lmax_nolimber + nnode_g] head + folded from LNL
+  // per-point inputs staged on device when the batch is on the host
+  double *d_in_om = nullptr, *d_in_h0 = nullptr, *d_in_chi = nullptr, *d_in_G = nullptr,
+         *d_in_lnP = nullptr, *d_in_lnPL = nullptr;
+  cl2pt_nuisance* d_in_nu = nullptr;
+  int* d_mask = nullptr;
+  double* d_pm = nullptr;
+  double* d_dv = nullptr;
+  // workspace
+  cl2pt::Params P;  // template with everything but per-wave pointers
+  cl2pt::NLParams nlq;
+  int node_stride = 0;
+  int* d_err = nullptr;
+  int last_launches = 0;
+  // stage timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Rec { int stage; cudaEvent_t a, b; int launches; };
+  std::vector<Rec> recs;
+  size_t ev_used = 0;
+  int last_batch = 0;
+};
+

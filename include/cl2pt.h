@@ -1,0 +1,143 @@
+/*
+ * cl2pt.h -- C ABI of the GB300 2-point theory library (libcl2pt.so).
+ *
+ * The reference evaluates one parameter point at a time through global
+ * state and scalar entry points (cosmolike/cosmo2D.h:30-147,
+ * cosmolike/generic_interface.hpp:506-1159).  This ABI evaluates a batch
+ * of points per call on one GPU.  A plan holds everything that depends
+ * only on the configuration and the redshift samples (quadrature rules,
+ * bin-averaged Legendre filters folded onto the C_l nodes, n(z) splines,
+ * device workspace); a batch carries the per-point cosmology tables and
+ * nuisance parameters.
+ *
+ * Conventions: every function returns an int status (CL2PT_OK = 0, a
+ * negative CL2PT_ERR_* otherwise) and never exits the process.  Arrays
+ * are plain row-major doubles.  Pointers marked "host or device" are read
+ * from where cl2pt_batch.where says.  Streams are cudaStream_t passed as
+ * void* (NULL = the default stream).
+ */
+#ifndef CL2PT_H
+#define CL2PT_H
+
+#include "cl2pt_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cl2pt_plan cl2pt_plan;
+
+/* Compute-precision plans. */
+enum {
+  CL2PT_PREC_MIXED = 0, /* FP64 tables/filters/accumulation, FP32 table walks */
+  CL2PT_PREC_FP64 = 1   /* every stage in FP64 (the plain FP64 GPU form)    */
+};
+
+/* Where the arrays of a batch live. */
+enum { CL2PT_HOST = 0, CL2PT_DEVICE = 1 };
+
+/* Axes shared by every point of a batch (a sampler keeps them fixed):
+ * the z grids of the distance and growth tables and the (log10 k, z)
+ * axes of the nonlinear and linear power-spectrum tables.  Host memory. */
+typedef struct cl2pt_grid {
+  int chi_nz;
+  const double* chi_z;
+  int G_nz;
+  const double* G_z;
+  int pk_nk, pk_nz;
+  const double* pk_log10k;
+  const double* pk_z;
+  int pkl_nk, pkl_nz;       /* 0 = same axes as the nonlinear table */
+  const double* pkl_log10k;
+  const double* pkl_z;
+} cl2pt_grid;
+
+/* Per-point inputs of a batch of n points (host or device). */
+typedef struct cl2pt_batch {
+  int n;
+  int where;                        /* CL2PT_HOST or CL2PT_DEVICE */
+  const double* omega_m;            /* [n] */
+  const double* h0;                 /* [n]  H0 / 100 */
+  const double* chi;                /* [n][chi_nz]  Mpc/h */
+  const double* G;                  /* [n][G_nz]    D = G a */
+  const double* lnP;                /* [n][pk_nk * pk_nz]  row-major [i_k*nz + j_z] */
+  const double* lnPL;               /* [n][pkl_nk * pkl_nz] or NULL (= lnP) */
+  const cl2pt_nuisance* nuisance;   /* [n] */
+} cl2pt_batch;
+
+/* Build a plan.  Replaces the reference's init_* calls and its
+ * geometry caches (set_bin_average, cosmo2D.c:353-453).  max_batch
+ * bounds n of every later batch; the plan owns all device memory. */
+int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
+                      const cl2pt_nz* lens, const cl2pt_grid* grid,
+                      int precision, int max_batch, cl2pt_plan** plan);
+int cl2pt_plan_destroy(cl2pt_plan* plan);
+
+/* Sizes of the real-space data vector blocks: xi+ and xi- (P_ss*ntheta
+ * each), gamma_t (P_gs*ntheta), w (n_lens*ntheta) -- the reference's
+ * compute_data_vector_Mx2pt_N_sizes<0,3> (generic_interface.hpp:701-729). */
+int cl2pt_real_sizes(const cl2pt_plan* plan, int* n_xi, int* n_gammat,
+                     int* n_w, int* n_total);
+
+/* Evaluate the masked real-space 3x2pt data vector of every point of the
+ * batch: xi+, xi-, gamma_t, w(theta) in the reference's order (ord =
+ * 0,1,2), shear calibration applied, masked entries zero -- the batched
+ * form of compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159)
+ * over xi_pm_tomo / w_gammat_tomo / w_gg_tomo (cosmo2D.h:30-41).
+ * mask: [n_total] ints shared by the batch, or NULL (all kept).
+ * pm:   [n][n_lens] gamma_t point masses or NULL (PointMass::get_pm,
+ *       generic_interface.cpp:2626-2641).
+ * dv:   [n][n_total] doubles, host or device per batch->where.
+ * stream: cudaStream_t (void*). */
+int cl2pt_eval_real(cl2pt_plan* plan, const cl2pt_batch* batch,
+                    const int* mask, const double* pm, double* dv,
+                    void* stream);
+
+/* Wait for the stream and report any device-side check that failed since
+ * the last call (a device-resident batch does not synchronise). */
+int cl2pt_check_errors(cl2pt_plan* plan, void* stream);
+
+/* ---- per-stage results of the last cl2pt_eval_real call (host copies),
+ * for verification against the oracle. ---- */
+/* Limber C_l on the nodes of point `point`: ss [P_ss][nnode],
+ * gs [P_gs][nnode], gg [n_lens][nnode], where nnode = (lmin_tab - 1)
+ * integer multipoles 1..lmin_tab-1 followed by the n_ell log-spaced table
+ * multipoles; NULL pointers are skipped. */
+int cl2pt_debug_limber_tables(const cl2pt_plan* plan, int point, double* ss,
+                              double* gs, double* gg);
+/* Non-Limber C_l [n_lens][lmax_nolimber] of point `point`; conv_l gets the
+ * per-bin multipole where the FFTLog result handed over to Limber. */
+int cl2pt_debug_nonlimber(const cl2pt_plan* plan, int point, double* cl,
+                          int* conv_l);
+/* Lens-efficiency tables g(a) [n_source][n_a] of point `point`. */
+int cl2pt_debug_g_tables(const cl2pt_plan* plan, int point, double* gsrc);
+
+/* Per-kernel device timing.  When enabled, every eval call records CUDA
+ * events around each kernel launch on its stream; cl2pt_kernel_times
+ * waits for them and returns, per kernel id, the summed milliseconds and
+ * the number of launches since the last call (or since enabling). */
+enum {
+  CL2PT_K_GTAB = 0,        /* lens-efficiency tables */
+  CL2PT_K_NODES = 1,       /* quadrature nodes and radial weights */
+  CL2PT_K_LIMBER_SS = 2,   /* Limber C_ss on the C_l nodes */
+  CL2PT_K_LIMBER_GS = 3,   /* Limber C_gs */
+  CL2PT_K_LIMBER_GG = 4,   /* Limber C_gg */
+  CL2PT_K_LIMBER_GGL = 5,  /* Limber C_gg at integer l < lmax_nolimber */
+  CL2PT_K_NONLIMBER = 6,   /* FFTLog clustering C_l */
+  CL2PT_K_LEGENDRE = 7,    /* bin-averaged Legendre contraction */
+  CL2PT_K_ASSEMBLE = 8,    /* mask, calibration, point masses */
+  CL2PT_NKERNEL = 9
+};
+int cl2pt_set_timing(cl2pt_plan* plan, int enable);
+int cl2pt_kernel_times(cl2pt_plan* plan, double* ms, int* launches);
+
+/* Number of kernel launches issued by the last eval call. */
+int cl2pt_last_launch_count(const cl2pt_plan* plan);
+
+/* Human-readable text for a status code. */
+const char* cl2pt_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,72 @@
+"""Generate the golden fixtures from the reference's own code.
+
+Runs each case in its own process against oracle/_ref/libcosmolike_ref.so
+(the reference's hot-path sources compiled unchanged against this
+project's GSL/FFTW stand-ins; built by `make -C oracle ref`, which needs
+the reference source tree) on the seeded synthetic inputs of
+cl2pt.workloads, and writes tests/golden/<case>.npz.
+
+    python tests/golden/make_golden.py [case ...]
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
+         "fastpt_bias"]
+
+
+def run_case(case, which="ref"):
+    """Outputs of one case from the 'ref' or 'orc' library (dict of arrays)."""
+    import oracle as O
+    from cl2pt import abi, workloads
+    o = O.Oracle(which)
+    out = {}
+    if case == "fastpt_bias":
+        w = workloads.make("real_3x2pt_small")
+        o.setup(w.cfg, w.src, w.lens)
+        o.set_point(w.base, abi.make_nuisance())
+        out["fpt_bias"] = o.fpt_bias()
+        return out
+    w = workloads.make(case)
+    o.setup(w.cfg, w.src, w.lens)
+    tabs, nus = workloads.points(w, 2, seed=11)
+    for i in range(2):
+        o.set_point(tabs[i], nus[i])
+        if case == "cosmic_shear_fourier":
+            pairs = abi.shear_pairs(w.cfg.n_source)
+            out[f"Css_EE_{i}"] = np.array([[o.C_ss_nointerp(l, a, b, 1) for l in w.ell] for a, b in pairs])
+            out[f"Css_EE_tab_{i}"] = np.array([[o.C_ss_limber(l, a, b, 1) for l in w.ell] for a, b in pairs])
+        else:
+            out[f"dv_{i}"] = o.data_vector_real()
+            if not w.cfg.adopt_limber_gg:
+                out[f"cl_nonlimber_{i}"] = o.C_cl_tomo()[0]
+            if case == "real_3x2pt_small" and i == 0:
+                out["Cgs_l"] = np.array([o.C_gs_nointerp(l, 1, 2) for l in (3.0, 30.0, 300.0)])
+                out["Cgg_l"] = np.array([o.C_gg_nointerp(l, 1, 0) for l in (3.0, 30.0, 300.0)])
+                out["Cgg_lin_l"] = np.array([o.C_gg_nointerp(l, 1, 1) for l in (3.0, 30.0, 300.0)])
+        if case == "real_3x2pt":
+            break
+    return out
+
+
+def main(cases):
+    for c in cases:
+        if os.environ.get("CL2PT_GOLDEN_CHILD") == c:
+            np.savez_compressed(os.path.join(HERE, f"{c}.npz"), **run_case(c))
+            return
+    for c in cases:
+        env = dict(os.environ, CL2PT_GOLDEN_CHILD=c)
+        subprocess.run([sys.executable, __file__, c], check=True, env=env)
+        print("wrote", c)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or CASES)

@@ -1,0 +1,110 @@
+"""CPU checks of the oracle (no GPU): its numerical kernels against
+scipy/numpy, and its outputs against the golden fixtures produced by the
+reference's own code (tests/golden/make_golden.py)."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+
+_dp = C.POINTER(C.c_double)
+
+
+def _lib(oracle_built):
+    import oracle
+    return C.CDLL(oracle.ORACLE_SO)
+
+
+def test_gl_rule(oracle_built):
+    lib = _lib(oracle_built)
+    for n in (64, 96, 256, 1024):
+        x = np.zeros(n)
+        w = np.zeros(n)
+        lib.num_gl_rule(n, x.ctypes.data_as(_dp), w.ctypes.data_as(_dp))
+        xr, wr = np.polynomial.legendre.leggauss(n)
+        assert np.allclose(x, xr, rtol=0, atol=1e-14)
+        # endpoint weights lose a few digits to 1 - z^2; ample for 1e-4 parity
+        assert np.allclose(w, wr, rtol=5e-9, atol=0)
+
+
+def test_legendre(oracle_built):
+    from scipy.special import eval_legendre
+    lib = _lib(oracle_built)
+    L = 2000
+    for x in (np.cos(2.5 * 2.90888208665721580e-4), 0.3, -0.77):
+        P = np.zeros(L + 1)
+        dP = np.zeros(L + 1)
+        lib.num_legendre_pl_deriv(L, C.c_double(x), P.ctypes.data_as(_dp), dP.ctypes.data_as(_dp))
+        ls = np.array([0, 1, 2, 10, 333, 1999])
+        assert np.allclose(P[ls], eval_legendre(ls, x), rtol=1e-10, atol=1e-12)
+        # derivative identity checked by central difference
+        h = 1e-7 * (1 - abs(x)) + 1e-9
+        for l in (5, 50):
+            d = (eval_legendre(l, x + h) - eval_legendre(l, x - h)) / (2 * h)
+            assert abs(dP[l] - d) <= 1e-5 * max(1.0, abs(d))
+
+
+def test_cspline(oracle_built):
+    from scipy.interpolate import CubicSpline
+    lib = _lib(oracle_built)
+    x = np.sort(np.random.default_rng(1).uniform(0, 4, 50))
+    y = np.sin(3 * x) * np.exp(-x)
+    c = np.zeros(50)
+    lib.num_cspline_init(x.ctypes.data_as(_dp), y.ctypes.data_as(_dp), 50, c.ctypes.data_as(_dp))
+    lib.num_cspline_eval.restype = C.c_double
+    cs = CubicSpline(x, y, bc_type="natural")
+    for v in np.linspace(x[0], x[-1], 97):
+        got = lib.num_cspline_eval(x.ctypes.data_as(_dp), y.ctypes.data_as(_dp),
+                                   c.ctypes.data_as(_dp), 50, C.c_double(v))
+        assert abs(got - cs(v)) < 1e-12
+
+
+def test_fft(oracle_built):
+    lib = _lib(oracle_built)
+    rng = np.random.default_rng(2)
+    for n in (900, 1500, 2450, 3072, 6142, 12150):
+        a = rng.normal(size=n)
+        out = np.zeros(n // 2 + 1, dtype=np.complex128)
+        lib.num_fft_r2c(C.c_long(n), a.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
+        assert np.allclose(out, np.fft.rfft(a), rtol=0, atol=1e-10 * np.sqrt(n))
+        back = np.zeros(n)
+        lib.num_fft_c2r(C.c_long(n), out.ctypes.data_as(_dp), back.ctypes.data_as(_dp))
+        assert np.allclose(back / n, a, atol=1e-12)
+
+
+def _gold(name):
+    p = os.path.join(GOLD, name + ".npz")
+    return dict(np.load(p))
+
+
+@pytest.mark.parametrize("case", ["cosmic_shear_fourier", "real_3x2pt_small",
+                                  "real_3x2pt_small_limber", "real_3x2pt", "fastpt_bias"])
+def test_oracle_matches_reference_golden(oracle_built, case):
+    """The restatement reproduces the reference's outputs (fixtures made by
+    running the reference's own sources)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); sys.path.insert(0, %r);"
+        "import make_golden as m; out = m.run_case(%r, 'orc');"
+        "np.savez(%r, **out)"
+    ) % (os.path.join(HERE, "golden"), os.path.join(os.path.dirname(HERE), "cocoa-cosmolike-core_gb300"),
+         case, os.path.join("/tmp", f"cl2pt_orc_{case}.npz"))
+    env = dict(os.environ, PYTHONPATH=os.path.join(os.path.dirname(HERE), "oracle"))
+    subprocess.run([sys.executable, "-c", code], check=True, env=env)
+    got = dict(np.load(os.path.join("/tmp", f"cl2pt_orc_{case}.npz")))
+    ref = _gold(case)
+    assert set(got) == set(ref)
+    for k in ref:
+        r, g = ref[k], got[k]
+        if k == "fpt_bias":
+            # row 5 (P_d1p3) interpolates a table embedded in the reference
+            # (pt_cfastpt.h:7-146); the oracle takes it from the caller and
+            # none is passed here, so that row is not compared.
+            r, g = np.delete(r, 5, axis=0), np.delete(g, 5, axis=0)
+        scale = np.max(np.abs(r))
+        err = np.max(np.abs(g - r) / np.maximum(np.abs(r), 1e-12 * scale))
+        assert err < 1e-9, (case, k, err)
