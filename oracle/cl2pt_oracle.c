@@ -16,6 +16,7 @@
 
 #include <complex.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -114,20 +115,31 @@ static int gl_size_gg(void) /* cosmo2D.c:2636-2639 */
   return h == 0 ? 96 : h == 1 ? 128 : h == 2 ? 256 : h == 3 ? 512 : 1024;
 }
 
+/* Gauss-Legendre rules, built once and shared by the OpenMP loops; the
+ * cache is filled under a lock (orc_setup also pre-builds every size). */
 typedef struct { int n; double* x; double* w; } glrule;
 static glrule g_rules[8];
-static int g_nrules = 0;
+static volatile int g_nrules = 0;
+static pthread_mutex_t g_rule_lock = PTHREAD_MUTEX_INITIALIZER;
 static const glrule* rule(int n)
 {
   for (int i = 0; i < g_nrules; i++)
     if (g_rules[i].n == n) return &g_rules[i];
+  pthread_mutex_lock(&g_rule_lock);
+  for (int i = 0; i < g_nrules; i++)
+    if (g_rules[i].n == n) {
+      pthread_mutex_unlock(&g_rule_lock);
+      return &g_rules[i];
+    }
   if (g_nrules >= 8) fatal("too many GL rules");
   glrule* r = &g_rules[g_nrules];
   r->n = n;
   r->x = malloc(sizeof(double) * n);
   r->w = malloc(sizeof(double) * n);
   num_gl_rule(n, r->x, r->w);
-  g_nrules++;
+  __sync_synchronize();
+  g_nrules = g_nrules + 1;
+  pthread_mutex_unlock(&g_rule_lock);
   return r;
 }
 
@@ -1555,6 +1567,8 @@ int orc_setup(const cl2pt_config* cfg, const cl2pt_nz* src, const cl2pt_nz* lens
   if (st) return st;
   /* zmean uses zero shift / unit stretch */
   compute_zmean();
+  (void)rule(gl_size_ss());
+  (void)rule(gl_size_gg());
   /* pair maps: Z1/Z2/ZL/ZS/N_shear/N_ggl/test_zoverlap,
    * redshift_spline.c:115-373 */
   int n = 0;
