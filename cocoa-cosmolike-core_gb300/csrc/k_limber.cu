@@ -222,6 +222,19 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
 // int_for_C_gg_tomo_limber (cosmo2D.c:2490-2608) summed over the gg nodes.
 // mode 0: C_l nodes -> tab_gg (Pdelta);  mode 1: integer l = 0..LNL-1 ->
 // ggl (Pdelta and p_lin, for the non-Limber corrections and hand-over).
+// The redshift-space term needs, per (l, node), a_chi((l+3/2)/k), H/H0 and
+// f there and n_lens: the point's distance and growth tables and the
+// bin's n(z) spline sit in shared memory in the loop precision T, and the
+// bracketing cell found by a_chi is reused by the chi_all/growth lookups
+// (it is the cell their own search would return; checked, with a full
+// search when it is not).
+template <typename T>
+__device__ __forceinline__ int bsearch_from(const T* __restrict__ x, int n, T v, int j)
+{
+  if (j >= 0 && j <= n - 2 && x[j] <= v && (v < x[j + 1] || j == n - 2)) return j;
+  return bsearch_t(x, n, v);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __restrict__ ell,
                                                   int mode)
@@ -233,17 +246,33 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
   const int L = blockIdx.y * LT + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   const PdeltaTable pl = pdelta_table(P, pt, true);
-  T* lk = (T*)smem_raw;               // Pdelta axis
-  T* lkl = lk + pd.nk;                // linear axis
-  // node data [8][PCH] after the two axes, 16-byte aligned
-  const size_t nd_off = ((size_t)(pd.nk + pl.nk) * sizeof(T) + 15) & ~(size_t)15;
-  double* nd = (double*)(smem_raw + nd_off);
-  int* nj = (int*)(nd + 8 * PCH);     // [2][PCH]
+  const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
+  const bool same_axis = P.G_same_axis != 0;
+  // node data [8][PCH] doubles, then int [2][PCH], then T arrays
+  double* nd = (double*)smem_raw;
+  int* nj = (int*)(nd + 8 * PCH);
+  T* lk = (T*)(nj + 2 * PCH);       // Pdelta axis
+  T* lkl = lk + pd.nk;              // linear axis
+  T* cz = lkl + pl.nk;              // chi table z axis
+  T* cx = cz + nc;                  // chi values (Mpc/h)
+  T* gz = cx + nc;                  // growth table z axis (unused if same as cz)
+  T* gv = gz + ng;                  // growth values
+  T* szc = gv + ng;                 // n(z) spline nodes, values, coefficients of bin q
+  T* sy = szc + nzs;
+  T* sc = sy + nzs;
+  const double* Xg = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gg = P.G + (size_t)pt * P.G_nz;
   for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
   for (int i = tid; i < pl.nk; i += LT) lkl[i] = (T)pl.lk[i];
+  for (int i = tid; i < nc; i += LT) { cz[i] = (T)P.chi_z[i]; cx[i] = (T)Xg[i]; }
+  for (int i = tid; i < ng; i += LT) { gz[i] = (T)P.G_z[i]; gv[i] = (T)Gg[i]; }
+  for (int i = tid; i < nzs; i += LT) {
+    szc[i] = (T)P.lens_zc[i];
+    sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
+    sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
+  }
   const cl2pt_nuisance& nu = P.nu[pt];
-  const double* X = P.chi + (size_t)pt * P.chi_nz;
-  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const T ldz = (T)nu.lens_dz[q], lst = (T)nu.lens_stretch[q], lzm = (T)P.zmean_lens[q];
   const int off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
@@ -252,10 +281,11 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
   const bool valid = L < nL;
   const double l = valid ? ((mode == 0) ? ell[L] : (double)L) : 1.0;
   const double lp = l + 0.5;
-  const double pref = l * (l + 1.) / (lp * lp);
-  const double c0 = (1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.));
-  const double c1 = 4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.));
+  const T pref = (T)(l * (l + 1.) / (lp * lp));
+  const T c0 = (T)((1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.)));
+  const T c1 = (T)(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
   const double chi_amin = P.chi_amin[pt];
+  const T cH0 = (T)CL2PT_COVERH0;
   double sum_nl = 0.0, sum_lin = 0.0;
   for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
     const int np = min(PCH, P.n_gg - p0);
@@ -283,14 +313,41 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
       const double fK = nd[0 * PCH + p];
       const double chi1 = fK * (lp + 1.0) / lp;  // (l+3/2)/k
       if (chi1 > chi_amin) continue;
-      const double a1 = a_chi_d(P.chi_z, X, P.chi_nz, chi1);
-      const double z1 = 1. / a1 - 1.;
-      const double H1 = 1.0 / ((a1 * a1) * chi_all_d(P.chi_z, X, P.chi_nz, a1).dchida);
-      const double R1 = nz_lens_d(P, z1, q, nu.lens_dz[q], nu.lens_stretch[q]) * H1 *
-                        f_growth_d(P.G_z, Gv, P.G_nz, z1);
-      const double wrsd = c0 * nd[5 * PCH + p] - c1 * R1;
-      const double s = nd[3 * PCH + p] + nd[4 * PCH + p] * pref + wrsd;
-      const double s2w = s * s * nd[1 * PCH + p];
+      // a_chi (cosmo3D.c:109-133)
+      const T c = (T)(chi1 * CL2PT_COVERH0);
+      const int j = bsearch_t(cx, nc, c);
+      const T dyc = (c - cx[j]) / (cx[j + 1] - cx[j]);
+      const T z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
+      const T a1 = (T)1 / ((T)1 + z1);
+      // chi_all(a1).dchida (cosmo3D.c:40-92)
+      const T zz = (T)1 / a1 - (T)1;
+      const int jc = bsearch_from(cz, nc, zz, j);
+      const T dy2 = (zz - cz[jc]) / (cz[jc + 1] - cz[jc]);
+      const int j2 = (jc + 2 < nc) ? jc + 2 : nc - 1;
+      const T up = (cx[j2] - cx[jc]) / (cz[j2] - cz[jc]);
+      const T dn = (jc > 0) ? (cx[jc + 1] - cx[jc - 1]) / (cz[jc + 1] - cz[jc - 1])
+                            : (cx[jc + 1] - cx[jc]) / (cz[jc + 1] - cz[jc]);
+      const T dchida = (dn + dy2 * (up - dn)) / cH0 / (a1 * a1);
+      const T H1 = (T)1 / ((a1 * a1) * dchida);
+      // f_growth(z1) (cosmo3D.c:200-228)
+      const T* gza = same_axis ? cz : gz;
+      const int jg = same_axis ? bsearch_from(gza, ng, z1, jc) : bsearch_t(gza, ng, z1);
+      const T sl = (gv[jg + 1] - gv[jg]) / (gza[jg + 1] - gza[jg]);
+      const T Gz = gv[jg] + (z1 - gza[jg]) / (gza[jg + 1] - gza[jg]) * (gv[jg + 1] - gv[jg]);
+      const T f1 = (T)1 - sl * z1 / Gz * ((T)1 + z1) / z1;
+      // nz_lens_photoz (redshift_spline.c:740-760)
+      const T zs = (z1 - ldz - lzm) / lst + lzm;
+      T n1 = (T)0;
+      if (!(zs <= szc[0] || zs >= szc[nzs - 1])) {
+        const int i = bsearch_t(szc, nzs, zs);
+        const T h = szc[i + 1] - szc[i], t = zs - szc[i];
+        const T bq = (sy[i + 1] - sy[i]) / h - h * (sc[i + 1] + (T)2 * sc[i]) / (T)3;
+        const T dq = (sc[i + 1] - sc[i]) / ((T)3 * h);
+        n1 = (sy[i] + t * (bq + t * (sc[i] + t * dq))) / lst;
+      }
+      const T wrsd = c0 * (T)nd[5 * PCH + p] - c1 * n1 * H1 * f1;
+      const T s = (T)nd[3 * PCH + p] + (T)nd[4 * PCH + p] * pref + wrsd;
+      const double s2w = (double)(s * s) * nd[1 * PCH + p];
       const T log10k = log10_t<T>((T)(lp / (fK * CL2PT_COVERH0)));
       const T Pnl = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
       sum_nl += s2w * (double)Pnl;
@@ -334,8 +391,8 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    const size_t sm = sizeof(T) * (P.pk_nk + P.pkl_nk + 2) + sizeof(double) * 8 * PCH +
-                      sizeof(int) * 2 * PCH + 64;
+    const size_t sm = sizeof(double) * 8 * PCH + sizeof(int) * 2 * PCH +
+                      sizeof(T) * (P.pk_nk + P.pkl_nk + 2 * P.chi_nz + 2 * P.G_nz + 3 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);

@@ -179,6 +179,119 @@ __device__ double block_sum(double v, double* sh)
   return s;
 }
 
+// complex arithmetic in the multipole loop's precision
+template <typename T> struct ct { T x, y; };
+template <typename T> __device__ __forceinline__ ct<T> tmk(T a, T b) { ct<T> r; r.x = a; r.y = b; return r; }
+template <typename T> __device__ __forceinline__ ct<T> tmul(ct<T> a, ct<T> b)
+{
+  return tmk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ ct<T> tadd(ct<T> a, ct<T> b) { return tmk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ ct<T> tdiv(ct<T> a, ct<T> b)
+{
+  if (fabs(b.x) >= fabs(b.y)) {
+    const T r = b.y / b.x, d = b.x + b.y * r;
+    return tmk<T>((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  }
+  const T r = b.x / b.y, d = b.x * r + b.y;
+  return tmk<T>((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+template <typename T> __device__ __forceinline__ void tsincos(T a, T* s, T* c);
+template <> __device__ __forceinline__ void tsincos<float>(float a, float* s, float* c) { __sincosf(a, s, c); }
+template <> __device__ __forceinline__ void tsincos<double>(double a, double* s, double* c) { sincos(a, s, c); }
+template <typename T> __device__ __forceinline__ T texp(T a);
+template <> __device__ __forceinline__ float texp<float>(float a) { return expf(a); }
+template <> __device__ __forceinline__ double texp<double>(double a) { return exp(a); }
+template <typename T> __device__ __forceinline__ T tlog10(T a);
+template <> __device__ __forceinline__ float tlog10<float>(float a) { return log10f(a); }
+template <> __device__ __forceinline__ double tlog10<double>(double a) { return log10(a); }
+
+// radix-R butterfly on v[0..R-1] with the R-th roots of unity w[m] = exp(sign 2 pi i m / R)
+template <typename T, int R>
+__device__ __forceinline__ void dft_small(ct<T>* v, const ct<T>* w)
+{
+  ct<T> o[R];
+#pragma unroll
+  for (int t = 0; t < R; t++) {
+    ct<T> acc = v[0];
+#pragma unroll
+    for (int r = 1; r < R; r++) acc = tadd(acc, tmul(v[r], w[(r * t) % R]));
+    o[t] = acc;
+  }
+#pragma unroll
+  for (int t = 0; t < R; t++) v[t] = o[t];
+}
+template <typename T>
+__device__ __forceinline__ void dft2(ct<T>* v)
+{
+  const ct<T> a = v[0], b = v[1];
+  v[0] = tmk<T>(a.x + b.x, a.y + b.y);
+  v[1] = tmk<T>(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__device__ __forceinline__ void dft4(ct<T>* v, int sign)
+{
+  const ct<T> a = tmk<T>(v[0].x + v[2].x, v[0].y + v[2].y);
+  const ct<T> b = tmk<T>(v[0].x - v[2].x, v[0].y - v[2].y);
+  const ct<T> c = tmk<T>(v[1].x + v[3].x, v[1].y + v[3].y);
+  ct<T> d = tmk<T>(v[1].x - v[3].x, v[1].y - v[3].y);
+  // d * (sign i)
+  d = (sign > 0) ? tmk<T>(-d.y, d.x) : tmk<T>(d.y, -d.x);
+  v[0] = tmk<T>(a.x + c.x, a.y + c.y);
+  v[2] = tmk<T>(a.x - c.x, a.y - c.y);
+  v[1] = tmk<T>(b.x + d.x, b.y + d.y);
+  v[3] = tmk<T>(b.x - d.x, b.y - d.y);
+}
+
+// Stockham transform of size N in the loop precision (same structure as
+// block_fft, with specialised radix-2/4 butterflies).
+template <typename T>
+__device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, int N, const int* fac, int nf,
+                              const ct<T>* __restrict__ tw, int sign)
+{
+  int Ns = 1;
+  for (int s = 0; s < nf; s++) {
+    const int R = fac[s];
+    const int NR = N / R;
+    const int tstep = N / (Ns * R);
+    ct<T> w[7];
+    for (int m = 0; m < R; m++) {
+      ct<T> x = tw[m * NR];
+      if (sign < 0) x.y = -x.y;
+      w[m] = x;
+    }
+    for (int j = threadIdx.x; j < NR; j += NL_NT) {
+      const int k = j % Ns;
+      ct<T> v[7];
+      for (int r = 0; r < R; r++) {
+        ct<T> x = in[j + r * NR];
+        if (r && k) {
+          ct<T> tw_ = tw[r * k * tstep];
+          if (sign < 0) tw_.y = -tw_.y;
+          x = tmul(x, tw_);
+        }
+        v[r] = x;
+      }
+      switch (R) {
+        case 2: dft2(v); break;
+        case 4: dft4(v, sign); break;
+        case 3: dft_small<T, 3>(v, w); break;
+        case 5: dft_small<T, 5>(v, w); break;
+        default: dft_small<T, 7>(v, w); break;
+      }
+      const int dst = (j / Ns) * Ns * R + k;
+      for (int r = 0; r < R; r++) out[dst + r * Ns] = v[r];
+    }
+    __syncthreads();
+    ct<T>* t = in;
+    in = out;
+    out = t;
+    Ns *= R;
+  }
+  return in;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -193,14 +306,19 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
   const double om = P.omega_m[pt];
   const double bmag = nu.gb[4][q];
   const int nj = (bmag != 0.0) ? 3 : 2;
+  // shared layout: [FFT work: 2 x nmax complex doubles] [xg: nchi doubles]
+  //                [F, xpow[3]: nchi T each] [Pslice, lk: nk T each]
   cd* bufA = (cd*)smem_raw;
   cd* bufB = bufA + Q.nmax;
-  double* F = (double*)(bufB + Q.nmax);
-  double* xg = F + nchi;
+  double* xg = (double*)(bufB + Q.nmax);
+  T* F = (T*)(xg + nchi);
+  T* xpow = F + nchi;
+  T* psl = xpow + 3 * nchi;
+  T* plk = psl + P.pkl_nk;
   __shared__ double red[NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
-  cd* tout = (cd*)Q.tout + cta * Q.tout_stride;   // [3][nmax/2+1]
-  cd* gst = (cd*)Q.gstate + cta * Q.gst_stride;   // [3][2][nmax/2+1]
+  ct<T>* tout = (ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
+  ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride; // [3][2][hstride]
   double* Cl = P.cnl + cta * LNL;
   const double* ggl = P.ggl + cta * LNL * 2;
   const double rc = CL2PT_COVERH0 / P.h0[pt];
@@ -208,11 +326,23 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
   const double chi_max = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 4.0)).chi * rc;
   const double dlnchi = log(chi_max / chi_min) / ((double)nchi - 1.0);
   for (int j = tid; j < nchi; j += NL_NT) xg[j] = chi_min * exp(dlnchi * j);
+  // P_lin(k, z = 0) slice of the linear table (p_lin(k, 1), cosmo3D.c:306-358)
+  {
+    const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
+    const double dy = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
+    for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+      psl[i] = (T)((1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1]);
+      plk[i] = (T)P.pkl_lk[i];
+    }
+  }
   __syncthreads();
+  for (int j = 0; j < 3; j++)
+    for (int i = tid; i < nchi; i += NL_NT) xpow[j * nchi + i] = (T)pow(xg[nchi - 1 - i], Q.nu[j]);
   const double dlnx = log(xg[1] / xg[0]);
   const double* glens = P.glens + ((size_t)pt * P.nl + q) * P.n_a;
   const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
-  // ---- cfftlog_ells_p1: r2c of f_j / x^nu_j with the c-window
+  // ---- cfftlog_ells_p1 (FP64): r2c of f_j / x^nu_j with the c-window
   for (int j = 0; j < nj; j++) {
     const int N = Q.N[j];
     for (int i = tid; i < N; i += NL_NT) {
@@ -269,67 +399,97 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
         const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
         v = cscale(v, W);
       }
-      tout[j * Q.hstride + i] = v;
+      tout[j * Q.hstride + i] = tmk<T>((T)v.x, (T)v.y);
     }
     __syncthreads();
   }
-  // ---- multipole blocks
+  // ---- multipole loop (loop precision T)
+  ct<T>* fa = (ct<T>*)smem_raw;
+  ct<T>* fb = fa + Q.nmax;
+  const bool exact_blocks = (sizeof(T) == sizeof(double));
   int LM = LNL, done = 0;
   const int BLOCK = 16;
+  const double sqpi = sqrt(M_PI);
   for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
     const int ke = (ks + BLOCK < LNL) ? ks + BLOCK : LNL;
     for (int k = ks; k < ke; k++) {
-      for (int i = tid; i < nchi; i += NL_NT) F[i] = 0.0;
+      for (int i = tid; i < nchi; i += NL_NT) F[i] = (T)0;
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
         const double base = xg[0] / exp(2 * Q.pad[j] * dlnx);
         const double y0 = (k + 1.) / xg[nchi - 1];
         const double lnbase = log(base * y0);
+        const double deta = 2.0 * M_PI / (dlnx * N);
         __syncthreads();
+        ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
+        // Gamma-ratio kernels: direct for the first two multipoles (of every
+        // 16-block in the FP64 plan, as the reference does; of the whole
+        // walk in the mixed plan), two-step recurrence otherwise.
+        const bool direct = exact_blocks ? (k < ks + 2) : (k < 2);
+        const int slot = exact_blocks ? ((k - ks) & 1) : (k & 1);
         for (int i = tid; i < nq; i += NL_NT) {
-          const double eta = (2.0 * M_PI / (dlnx * N)) * i;
-          cd g;
-          cd* gs = gst + (size_t)j * 2 * Q.hstride;
-          if (k < ks + 2) g = gl_direct(Q.deriv[j], Q.nu[j], eta, k);
-          else g = cmul(gs[((k - ks) & 1) * Q.hstride + i], gl_ratio(Q.deriv[j], Q.nu[j], eta, k));
-          gs[((k - ks) & 1) * Q.hstride + i] = g;
-          cd val = tout[j * Q.hstride + i];
-          double sp, cp;
-          sincos(-eta * lnbase, &sp, &cp);
-          val = cmul(cmul(val, cmk(cp, sp)), g);
-          val = cconj(val);
-          bufA[i] = val;
-          if (i > 0 && i < N - i) bufA[N - i] = cconj(val);  // Hermitian completion
+          const double eta = deta * i;
+          ct<T> g;
+          if (direct) {
+            const cd gd = gl_direct(Q.deriv[j], Q.nu[j], eta, k);
+            g = tmk<T>((T)gd.x, (T)gd.y);
+          } else {
+            const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)eta;
+            ct<T> num, den;
+            if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
+            else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
+            else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
+            g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
+          }
+          gs[slot * Q.hstride + i] = g;
+          // phase exp(-i eta lnbase), argument reduced in FP64
+          double ph = -eta * lnbase;
+          ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
+          T sp, cp;
+          tsincos<T>((T)ph, &sp, &cp);
+          ct<T> val = tmul(tmul(tout[j * Q.hstride + i], tmk<T>(cp, sp)), g);
+          val.y = -val.y;  // conj
+          fa[i] = val;
+          if (i > 0 && i < N - i) fa[N - i] = tmk<T>(val.x, -val.y);  // Hermitian completion
         }
         __syncthreads();
         if (tid == 0) {
-          bufA[0].y = 0.0;
-          if ((N & 1) == 0) bufA[N / 2].y = 0.0;
+          fa[0].y = (T)0;
+          if ((N & 1) == 0) fa[N / 2].y = (T)0;
         }
         __syncthreads();
-        cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], +1);
-        const double sqpi = sqrt(M_PI);
+        ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
+        const T scale = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
+        const T magf = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
         for (int i = tid; i < nchi; i += NL_NT) {
-          const double y = (k + 1.) / xg[nchi - 1 - i];
-          double fy = r[Q.pad[j] + i].x * sqpi / (4. * N * pow(y, Q.nu[j]));
-          if (j == 2) fy = bmag * (k * (k + 1.)) * fy / (y * y);
+          T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
+          if (j == 2) {
+            const T xx = (T)xg[nchi - 1 - i];
+            fy = magf * fy * xx * xx;
+          }
           F[i] += fy;
         }
         __syncthreads();
       }
       // chi sum of F^2 k^3 P_lin(k, a = 1)
       double part = 0.0;
-      const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+      const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
       for (int i = tid; i < nchi; i += NL_NT) {
-        const double ty = (k + 1.) / xg[nchi - 1 - i];
-        const double k1 = ty * rc;
-        part += F[i] * F[i] * (k1 * k1 * k1) *
-                pk_d(P.pkl_lk, P.pkl_nk, P.pkl_z, P.pkl_nz, tabL, k1, 1.0);
+        const double k1 = (k + 1.) / xg[nchi - 1 - i] * rc;
+        const T lkv = tlog10<T>((T)(k1 / CL2PT_COVERH0));
+        int lo = 0, hi = P.pkl_nk - 1;
+        while (hi > lo + 1) {
+          const int mid = (lo + hi) >> 1;
+          if (plk[mid] > lkv) hi = mid; else lo = mid;
+        }
+        const T dx = (lkv - plk[lo]) / (plk[lo + 1] - plk[lo]);
+        const T pl = texp<T>(psl[lo] + dx * (psl[lo + 1] - psl[lo])) * lc3;
+        const T k3 = (T)(k1 * k1 * k1);
+        part += (double)(F[i] * F[i] * k3 * pl);
       }
       const double tcl = block_sum(part, red);
-      if (tid == 0)
-        Cl[k] = tcl * dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+      if (tid == 0) Cl[k] = tcl * dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
     }
     __syncthreads();
     // convergence at the block end (cosmo2D.c:4741-4750)
@@ -359,11 +519,19 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
                       const Hook& hk)
 {
-  const size_t sm = sizeof(double) * 2 * 2 * Q.nmax + sizeof(double) * 2 * P.nl_nchi + 64;
-  cudaFuncSetAttribute(k_nonlimber, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const bool fp64 = P.prec == CL2PT_PREC_FP64;
+  const size_t tsz = fp64 ? sizeof(double) : sizeof(float);
+  const size_t sm = sizeof(double) * 2 * 2 * Q.nmax + sizeof(double) * P.nl_nchi +
+                    tsz * (4 * (size_t)P.nl_nchi + 2 * P.pkl_nk) + 64;
   dim3 g(P.B, P.nl);
   hk(CL2PT_K_NONLIMBER, 1);
-  k_nonlimber<<<g, NL_NT, sm, s>>>(P, Q);
+  if (fp64) {
+    cudaFuncSetAttribute(k_nonlimber<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_nonlimber<double><<<g, NL_NT, sm, s>>>(P, Q);
+  } else {
+    cudaFuncSetAttribute(k_nonlimber<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_nonlimber<float><<<g, NL_NT, sm, s>>>(P, Q);
+  }
   hk(CL2PT_K_NONLIMBER, 0);
   (*launches)++;
 }

@@ -13,12 +13,13 @@ struct NLParams {
   int deriv[3];     // derivative orders of the Gamma-ratio kernels
   int fac[3][16];   // Stockham factors of N[j]
   int nfac[3];
-  const double* tw[3];  // exp(+2 pi i k / N[j]) as (re, im) pairs
+  const double* tw[3];  // exp(+2 pi i k / N[j]) as (re, im) pairs, FP64
+  const void* twt[3];   // the same table in the multipole-loop precision
   int nmax;         // max N[j]
   int hstride;      // nmax / 2 + 1
-  double* tout;     // [CTA][3][hstride] complex spectra
+  void* tout;       // [CTA][3][hstride] complex spectra (loop precision)
   size_t tout_stride;   // complex entries per CTA
-  double* gstate;   // [CTA][3][2][hstride] complex recurrence state
+  void* gstate;     // [CTA][3][2][hstride] complex recurrence state (loop precision)
   size_t gst_stride;
 };
 

@@ -505,7 +505,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.chi_nz = grid->chi_nz; P.G_nz = grid->G_nz;
   P.pk_nk = grid->pk_nk; P.pk_nz = grid->pk_nz;
   P.pkl_nk = (int)p->pkl_lk.size(); P.pkl_nz = (int)p->pkl_z.size();
-  P.chi_z = p->d_chi_z; P.G_z = p->d_G_z; P.pk_lk = p->d_pk_lk; P.pk_z = p->d_pk_z;
+  P.chi_z = p->d_chi_z; P.G_z = p->d_G_z;
+  P.G_same_axis = (p->chi_z.size() == p->G_z.size()) &&
+                  std::equal(p->chi_z.begin(), p->chi_z.end(), p->G_z.begin()); P.pk_lk = p->d_pk_lk; P.pk_z = p->d_pk_z;
   P.pkl_lk = p->d_pkl_lk; P.pkl_z = p->d_pkl_z;
   P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
   P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
@@ -590,13 +592,24 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       double* dtw;
       TRY(dupload(p, &dtw, tw.data(), tw.size()));
       Q.tw[j] = dtw;
+      if (precision == CL2PT_PREC_FP64) {
+        Q.twt[j] = dtw;
+      } else {
+        std::vector<float> twf(tw.begin(), tw.end());
+        float* dtwf;
+        TRY(dupload(p, &dtwf, twf.data(), twf.size()));
+        Q.twt[j] = dtwf;
+      }
     }
     Q.hstride = Q.nmax / 2 + 1;
     Q.tout_stride = (size_t)3 * Q.hstride;
     Q.gst_stride = (size_t)3 * 2 * Q.hstride;
     if (!cfg->adopt_limber_gg && (cfg->probes & CL2PT_PROBE_WTHETA)) {
-      TRY(dalloc(p, &Q.tout, (size_t)W * nl * Q.tout_stride * 2));
-      TRY(dalloc(p, &Q.gstate, (size_t)W * nl * Q.gst_stride * 2));
+      double *t1, *t2;  // sized for FP64 complex entries
+      TRY(dalloc(p, &t1, (size_t)W * nl * Q.tout_stride * 2));
+      TRY(dalloc(p, &t2, (size_t)W * nl * Q.gst_stride * 2));
+      Q.tout = t1;
+      Q.gstate = t2;
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
