@@ -56,6 +56,65 @@ __device__ __forceinline__ T pk_walk(const T* __restrict__ lk, int nk,
   return exp_t<T>(v) * (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
 }
 
+// Table walk used by the kernels.  FP64 plan: the reference formula above.
+// Mixed plan: the cell search runs on an FP32 copy of the log10 k axis, but
+// the in-cell offset and the lnP differences are formed in FP64 and the
+// exponent is split as exp(hi) exp(lo + delta) with hi = (float) lnP_00, so
+// that FP32 rounding of |lnP| ~ 10 does not cost ~1e-6 in P.
+template <typename T>
+struct Axis {
+  const T* lk;       // search copy (loop precision)
+  const double* lkd; // FP64 axis
+  const double* inv; // 1 / (lkd[i+1] - lkd[i])
+  int nk;
+};
+template <typename T>
+__device__ __forceinline__ T pk_eval(const Axis<T>& ax, const double* __restrict__ tab, int nz,
+                                     double log10k, int j, T dy);
+template <>
+__device__ __forceinline__ double pk_eval<double>(const Axis<double>& ax,
+                                                  const double* __restrict__ tab, int nz,
+                                                  double log10k, int j, double dy)
+{
+  return pk_walk<double>(ax.lk, ax.nk, tab, nz, log10k, j, dy);
+}
+template <>
+__device__ __forceinline__ float pk_eval<float>(const Axis<float>& ax,
+                                                const double* __restrict__ tab, int nz,
+                                                double log10k, int j, float dy)
+{
+  const int i = bsearch_t(ax.lk, ax.nk, (float)log10k);
+  const float dx = (float)((log10k - ax.lkd[i]) * ax.inv[i]);
+  const double* r0 = tab + (size_t)i * nz + j;
+  const double* r1 = r0 + nz;
+  const double a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
+  const float d01 = (float)(a01 - a00), d10 = (float)(a10 - a00);
+  const float d11 = (float)((a11 - a10) - (a01 - a00));
+  const float hi = (float)a00;
+  const float lo = (float)(a00 - (double)hi);
+  const float del = lo + dy * d01 + dx * d10 + dx * dy * d11;
+  return expf(hi) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
+// Load one log10 k axis into shared memory (search copy, FP64 copy and
+// inverse cell widths).
+template <typename T>
+__device__ __forceinline__ Axis<T> load_axis(const double* __restrict__ lk, int nk, T* sk,
+                                             double* sd, double* si)
+{
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    sk[i] = (T)lk[i];
+    sd[i] = lk[i];
+    si[i] = (i + 1 < nk) ? 1.0 / (lk[i + 1] - lk[i]) : 0.0;
+  }
+  Axis<T> a;
+  a.lk = sk;
+  a.lkd = sd;
+  a.inv = si;
+  a.nk = nk;
+  return a;
+}
+
 struct PdeltaTable {
   const double* tab;
   const double* lk;
@@ -84,13 +143,15 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   const int tid = threadIdx.x;
   const int L = blockIdx.y * LT + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
-  T* lk = (T*)smem_raw;
+  double* sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
+  double* si = sd + pd.nk;
+  double* nlc = si + pd.nk;
+  T* lk = (T*)(nlc + PCH);
   T* Ps = lk + pd.nk;
   T* X = Ps + PCH * LT;
-  T* nfk = X + (size_t)P.pss * PCH;
-  T* ndy = nfk + PCH;
+  T* ndy = X + (size_t)P.pss * PCH;
   int* nj = (int*)(ndy + PCH);
-  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
+  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
   const double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
@@ -103,7 +164,7 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
     for (int p = tid; p < np; p += LT) {
-      nfk[p] = (T)(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
+      nlc[p] = log10(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + p0 + p];
       nj[p] = nodej[p0 + p];
     }
@@ -117,11 +178,9 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     }
     __syncthreads();
     if (!valid) continue;
-    const T lpt = (T)lp;
-    for (int p = 0; p < np; p++) {
-      const T log10k = log10_t<T>(lpt / nfk[p]);
-      Ps[p * LT + tid] = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], ndy[p]);
-    }
+    const double llp = log10(lp);
+    for (int p = 0; p < np; p++)
+      Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     for (int pair = 0; pair < P.pss; pair++) {
       T acc = 0;
       const T* xr = X + pair * PCH;
@@ -156,13 +215,15 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   __syncthreads();
   const int np_ = npair;
   const int nterm = use_m ? 2 : 1;
-  T* lk = (T*)smem_raw;
+  double* sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
+  double* si = sd + pd.nk;
+  double* nlc = si + pd.nk;
+  T* lk = (T*)(nlc + PCH);
   T* Ps = lk + pd.nk;
   T* X = Ps + PCH * LT;                  // [nterm][npair][PCH]
-  T* nfk = X + (size_t)2 * CL2PT_MAXB * PCH;
-  T* ndy = nfk + PCH;
+  T* ndy = X + (size_t)2 * CL2PT_MAXB * PCH;
   int* nj = (int*)(ndy + PCH);
-  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
+  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const int off = P.n_ss + q * P.n_ss;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
@@ -181,7 +242,7 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
     for (int p = tid; p < np; p += LT) {
-      nfk[p] = (T)(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
+      nlc[p] = log10(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
       nj[p] = nodej[off + p0 + p];
     }
@@ -198,11 +259,9 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     }
     __syncthreads();
     if (!valid) continue;
-    const T lpt = (T)lp;
-    for (int p = 0; p < np; p++) {
-      const T log10k = log10_t<T>(lpt / nfk[p]);
-      Ps[p * LT + tid] = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], ndy[p]);
-    }
+    const double llp = log10(lp);
+    for (int p = 0; p < np; p++)
+      Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     for (int m = 0; m < np_; m++) {
       T a0 = 0, a1 = 0;
       const T* x0 = X + (0 * CL2PT_MAXB + m) * PCH;
@@ -248,9 +307,14 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
   const PdeltaTable pl = pdelta_table(P, pt, true);
   const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
   const bool same_axis = P.G_same_axis != 0;
-  // node data [8][PCH] doubles, then int [2][PCH], then T arrays
+  // node data [8][PCH] doubles, FP64 axes + inverse widths of both tables,
+  // then int [2][PCH], then T arrays
   double* nd = (double*)smem_raw;
-  int* nj = (int*)(nd + 8 * PCH);
+  double* sd = nd + 8 * PCH;
+  double* si = sd + pd.nk;
+  double* sdl = si + pd.nk;
+  double* sil = sdl + pl.nk;
+  int* nj = (int*)(sil + pl.nk);
   T* lk = (T*)(nj + 2 * PCH);       // Pdelta axis
   T* lkl = lk + pd.nk;              // linear axis
   T* cz = lkl + pl.nk;              // chi table z axis
@@ -262,8 +326,8 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
   T* sc = sy + nzs;
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
-  for (int i = tid; i < pd.nk; i += LT) lk[i] = (T)pd.lk[i];
-  for (int i = tid; i < pl.nk; i += LT) lkl[i] = (T)pl.lk[i];
+  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
+  const Axis<T> axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
   for (int i = tid; i < nc; i += LT) { cz[i] = (T)P.chi_z[i]; cx[i] = (T)Xg[i]; }
   for (int i = tid; i < ng; i += LT) { gz[i] = (T)P.G_z[i]; gv[i] = (T)Gg[i]; }
   for (int i = tid; i < nzs; i += LT) {
@@ -306,9 +370,11 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
       const int jl = bsearch_d(pl.z, pl.nz, z);
       nj[PCH + p] = jl;
       nd[6 * PCH + p] = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
+      nd[7 * PCH + p] = log10(fK * CL2PT_COVERH0);
     }
     __syncthreads();
     if (!valid) continue;
+    const double llp = log10(lp);
     for (int p = 0; p < np; p++) {
       const double fK = nd[0 * PCH + p];
       const double chi1 = fK * (lp + 1.0) / lp;  // (l+3/2)/k
@@ -348,11 +414,11 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
       const T wrsd = c0 * (T)nd[5 * PCH + p] - c1 * n1 * H1 * f1;
       const T s = (T)nd[3 * PCH + p] + (T)nd[4 * PCH + p] * pref + wrsd;
       const double s2w = (double)(s * s) * nd[1 * PCH + p];
-      const T log10k = log10_t<T>((T)(lp / (fK * CL2PT_COVERH0)));
-      const T Pnl = pk_walk<T>(lk, pd.nk, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
+      const double log10k = llp - nd[7 * PCH + p];
+      const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
       sum_nl += s2w * (double)Pnl;
       if (mode == 1) {
-        const T Pl = pk_walk<T>(lkl, pl.nk, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
+        const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
         sum_lin += s2w * (double)Pl;
       }
     }
@@ -371,7 +437,8 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
                             cudaStream_t s, int* launches, const Hook& hk)
 {
   if (P.probes & CL2PT_PROBE_XI) {
-    const size_t sm = sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + 2 * PCH) +
+    const size_t sm = sizeof(double) * (2 * P.pk_nk + PCH) +
+                      sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + PCH) +
                       sizeof(int) * PCH + 64;
     cudaFuncSetAttribute(k_limber_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_ss + LT - 1) / LT);
@@ -381,7 +448,8 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    const size_t sm = sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + 2 * PCH) +
+    const size_t sm = sizeof(double) * (2 * P.pk_nk + PCH) +
+                      sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + PCH) +
                       sizeof(int) * PCH + 64;
     cudaFuncSetAttribute(k_limber_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
@@ -391,7 +459,7 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    const size_t sm = sizeof(double) * 8 * PCH + sizeof(int) * 2 * PCH +
+    const size_t sm = sizeof(double) * (8 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
                       sizeof(T) * (P.pk_nk + P.pkl_nk + 2 * P.chi_nz + 2 * P.G_nz + 3 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);

@@ -291,8 +291,131 @@ __device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, int N, const int* fac, int 
   return in;
 }
 
+// Shared pieces of the three FFTLog kernels.
+struct NLGeom {
+  double rc, dlnchi, dlnx, x0, xlast;
+};
+__device__ __forceinline__ NLGeom nl_geom(const Params& P, int pt)
+{
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  NLGeom g;
+  g.rc = CL2PT_COVERH0 / P.h0[pt];
+  const double chi_min = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 0.002)).chi * g.rc;
+  const double chi_max = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 4.0)).chi * g.rc;
+  g.dlnchi = log(chi_max / chi_min) / ((double)P.nl_nchi - 1.0);
+  g.x0 = chi_min;
+  g.xlast = chi_min * exp(g.dlnchi * (P.nl_nchi - 1));
+  g.dlnx = log((chi_min * exp(g.dlnchi)) / chi_min);
+  return g;
+}
+
+// ---- 1. forward transforms (cfftlog_ells_p1, cosmo2D.c:4047-4130), FP64:
+// one CTA per (point, lens bin, radial kernel j).
 template <typename T>
-__global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
+__global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.y, j = blockIdx.z;
+  const int tid = threadIdx.x;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  if (j == 2 && nu.gb[4][q] == 0.0) return;  // magnification kernel unused
+  const int nchi = P.nl_nchi;
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
+  const double om = P.omega_m[pt];
+  const NLGeom geo = nl_geom(P, pt);
+  const double rc = geo.rc;
+  cd* bufA = (cd*)smem_raw;
+  cd* bufB = bufA + Q.nmax;
+  const double* glens = P.glens + ((size_t)pt * P.nl + q) * P.n_a;
+  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
+  const int N = Q.N[j];
+  for (int i = tid; i < N; i += NL_NT) {
+    double v = 0.0;
+    const int qq = i - Q.pad[j];
+    if (qq >= 0 && qq < nchi) {
+      const double xq = geo.x0 * exp(geo.dlnchi * qq);
+      const double chi = xq / rc;
+      const double a = a_chi_d(P.chi_z, X, P.chi_nz, chi);
+      const double z = 1. / a - 1.;
+      if (!(z < P.lens_zmin[q] || z > P.lens_zmax[q])) {
+        const double H = 1.0 / ((a * a) * chi_all_d(P.chi_z, X, P.chi_nz, a).dchida);
+        const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+        const double pf = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]);
+        double fx;
+        if (j == 0) {
+          double b1;
+          switch (P.bias_model[0]) {
+            case 0: b1 = nu.gb[0][q]; break;
+            case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
+            case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
+            case 4: b1 = nu.gb[0][0] * pow(1 + z, nu.gb[0][1]); break;
+            default: {
+              const double zev = growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)) /
+                                 growfac_d(P.G_z, Gv, P.G_nz, g1,
+                                           1. / (1. + 0.5 * (P.lens_zmin[q] + P.lens_zmax[q])));
+              b1 = (nu.gb[0][q] - 1.) / zev + 1.;
+            }
+          }
+          fx = chi * pf * D * H * b1;
+        } else if (j == 1) {
+          fx = -chi * pf * D * H * f_growth_d(P.G_z, Gv, P.G_nz, z);
+        } else {
+          // W_mag with the coarse g_lens table (interpol1d)
+          const double amax = 0.999999;
+          const double dac = (amax - amin_lensg) / ((double)P.n_a - 1.0);
+          const double gl = (a < amin_lensg || a > 1.0 - dac)
+                                ? 0.0 : interpol1d_d(glens, P.n_a, amin_lensg, dac, a);
+          const double WM = (1.5 * om * chi / a) * gl;
+          fx = (WM / chi / (rc * rc)) * D;
+        }
+        v = fx / pow(xq, Q.nu[j]);
+      }
+    }
+    bufA[i] = cmk(v, 0.0);
+  }
+  __syncthreads();
+  cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
+  const int halfN = N / 2;
+  const int kmax = (int)(halfN * 0.25);
+  ct<T>* tout = (ct<T>*)Q.tout + ((size_t)pt * P.nl + q) * Q.tout_stride;
+  for (int i = tid; i <= halfN; i += NL_NT) {
+    cd v = r[i];
+    const int k = halfN - i;  // window on the right side
+    if (k <= kmax) {
+      const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
+      v = cscale(v, W);
+    }
+    tout[j * Q.hstride + i] = tmk<T>((T)v.x, (T)v.y);
+  }
+}
+
+// ---- 2. Gamma-ratio kernels evaluated directly (Lanczos, FP64) at the
+// multipoles where the recurrence (re)starts: l = 0, 1 in the mixed plan;
+// the first two multipoles of every 16-block in the FP64 plan, as the
+// reference does.  One CTA per (point, radial kernel, start multipole).
+__global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
+{
+  const int pt = blockIdx.x, j = blockIdx.y, d = blockIdx.z;
+  const int k = Q.direct_every ? (d / 2) * 16 + (d & 1) : d;
+  if (k >= P.lmax_nolimber) return;
+  const NLGeom geo = nl_geom(P, pt);
+  const int N = Q.N[j];
+  const int nq = N / 2 + 1;
+  const double deta = 2.0 * M_PI / (geo.dlnx * N);
+  double* out = Q.gdir + (((size_t)pt * 3 + j) * Q.ndirect + d) * Q.hstride * 2;
+  for (int i = threadIdx.x; i < nq; i += NL_NT) {
+    const cd g = gl_direct(Q.deriv[j], Q.nu[j], deta * i, k);
+    out[2 * i] = g.x;
+    out[2 * i + 1] = g.y;
+  }
+}
+
+// ---- 3. multipole loop (cfftlog_ells_p2 + C_cl_tomo sums and convergence,
+// cosmo2D.c:4132-4769) in the loop precision T: one CTA per (point, bin).
+template <typename T>
+__global__ void __launch_bounds__(NL_NT, 3) k_nl_loop(Params P, NLParams Q)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x, q = blockIdx.y;
@@ -300,142 +423,80 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
   const int nchi = P.nl_nchi;
   const int LNL = P.lmax_nolimber;
   const cl2pt_nuisance& nu = P.nu[pt];
-  const double* X = P.chi + (size_t)pt * P.chi_nz;
-  const double* Gv = P.G + (size_t)pt * P.G_nz;
-  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
-  const double om = P.omega_m[pt];
   const double bmag = nu.gb[4][q];
   const int nj = (bmag != 0.0) ? 3 : 2;
-  // shared layout: [FFT work: 2 x nmax complex doubles] [xg: nchi doubles]
-  //                [F, xpow[3]: nchi T each] [Pslice, lk: nk T each]
-  cd* bufA = (cd*)smem_raw;
-  cd* bufB = bufA + Q.nmax;
-  double* xg = (double*)(bufB + Q.nmax);
-  T* F = (T*)(xg + nchi);
+  const NLGeom geo = nl_geom(P, pt);
+  // shared: [psl, plkd, pinv: nk doubles][lxk: nchi doubles]
+  //         [fa, fb: nmax complex T][F, xpow[3], xx2, rx3: nchi T][plk: nk T]
+  double* psl = (double*)smem_raw;
+  double* plkd = psl + P.pkl_nk;
+  double* pinv = plkd + P.pkl_nk;
+  double* lxk = pinv + P.pkl_nk;
+  ct<T>* fa = (ct<T>*)(lxk + nchi);
+  ct<T>* fb = fa + Q.nmax;
+  T* F = (T*)(fb + Q.nmax);
   T* xpow = F + nchi;
-  T* psl = xpow + 3 * nchi;
-  T* plk = psl + P.pkl_nk;
+  T* xx2 = xpow + 3 * nchi;
+  T* rx3 = xx2 + nchi;
+  T* plk = rx3 + nchi;
   __shared__ double red[NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
-  ct<T>* tout = (ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
-  ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride; // [3][2][hstride]
+  const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
+  ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;              // [3][2][hstride]
   double* Cl = P.cnl + cta * LNL;
   const double* ggl = P.ggl + cta * LNL * 2;
-  const double rc = CL2PT_COVERH0 / P.h0[pt];
-  const double chi_min = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 0.002)).chi * rc;
-  const double chi_max = chi_all_d(P.chi_z, X, P.chi_nz, 1. / (1.0 + 4.0)).chi * rc;
-  const double dlnchi = log(chi_max / chi_min) / ((double)nchi - 1.0);
-  for (int j = tid; j < nchi; j += NL_NT) xg[j] = chi_min * exp(dlnchi * j);
+  const double rc = geo.rc;
   // P_lin(k, z = 0) slice of the linear table (p_lin(k, 1), cosmo3D.c:306-358)
   {
     const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
     const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
     const double dy = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
     for (int i = tid; i < P.pkl_nk; i += NL_NT) {
-      psl[i] = (T)((1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1]);
+      psl[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
       plk[i] = (T)P.pkl_lk[i];
+      plkd[i] = P.pkl_lk[i];
+      pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
     }
   }
-  __syncthreads();
-  for (int j = 0; j < 3; j++)
-    for (int i = tid; i < nchi; i += NL_NT) xpow[j * nchi + i] = (T)pow(xg[nchi - 1 - i], Q.nu[j]);
-  const double dlnx = log(xg[1] / xg[0]);
-  const double* glens = P.glens + ((size_t)pt * P.nl + q) * P.n_a;
-  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
-  // ---- cfftlog_ells_p1 (FP64): r2c of f_j / x^nu_j with the c-window
-  for (int j = 0; j < nj; j++) {
-    const int N = Q.N[j];
-    for (int i = tid; i < N; i += NL_NT) {
-      double v = 0.0;
-      const int qq = i - Q.pad[j];
-      if (qq >= 0 && qq < nchi) {
-        const double chi = xg[qq] / rc;
-        const double a = a_chi_d(P.chi_z, X, P.chi_nz, chi);
-        const double z = 1. / a - 1.;
-        if (!(z < P.lens_zmin[q] || z > P.lens_zmax[q])) {
-          const double H = 1.0 / ((a * a) * chi_all_d(P.chi_z, X, P.chi_nz, a).dchida);
-          const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
-          const double pf = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]);
-          double fx;
-          if (j == 0) {
-            double b1;
-            switch (P.bias_model[0]) {
-              case 0: b1 = nu.gb[0][q]; break;
-              case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
-              case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
-              case 4: b1 = nu.gb[0][0] * pow(1 + z, nu.gb[0][1]); break;
-              default: {
-                const double zev = growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)) /
-                                   growfac_d(P.G_z, Gv, P.G_nz, g1,
-                                             1. / (1. + 0.5 * (P.lens_zmin[q] + P.lens_zmax[q])));
-                b1 = (nu.gb[0][q] - 1.) / zev + 1.;
-              }
-            }
-            fx = chi * pf * D * H * b1;
-          } else if (j == 1) {
-            fx = -chi * pf * D * H * f_growth_d(P.G_z, Gv, P.G_nz, z);
-          } else {
-            // W_mag with the coarse g_lens table (interpol1d)
-            const double amax = 0.999999;
-            const double dac = (amax - amin_lensg) / ((double)P.n_a - 1.0);
-            const double gl = (a < amin_lensg || a > 1.0 - dac)
-                                  ? 0.0 : interpol1d_d(glens, P.n_a, amin_lensg, dac, a);
-            const double WM = (1.5 * om * chi / a) * gl;
-            fx = (WM / chi / (rc * rc)) * D;
-          }
-          v = fx / pow(xg[qq], Q.nu[j]);
-        }
-      }
-      bufA[i] = cmk(v, 0.0);
-    }
-    __syncthreads();
-    cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
-    const int halfN = N / 2;
-    const int kmax = (int)(halfN * 0.25);
-    for (int i = tid; i <= halfN; i += NL_NT) {
-      cd v = r[i];
-      const int k = halfN - i;  // window on the right side
-      if (k <= kmax) {
-        const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
-        v = cscale(v, W);
-      }
-      tout[j * Q.hstride + i] = tmk<T>((T)v.x, (T)v.y);
-    }
-    __syncthreads();
+  // per chi point: x^nu_j, log10(rc / (x coverH0)) and x^2 at the reversed
+  // index nchi-1-i (y = (l+1)/x[nchi-1-i])
+  for (int i = tid; i < nchi; i += NL_NT) {
+    const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
+    for (int j = 0; j < 3; j++) xpow[j * nchi + i] = (T)pow(xr, Q.nu[j]);
+    lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
+    xx2[i] = (T)(xr * xr);
+    rx3[i] = (T)((rc / xr) * (rc / xr) * (rc / xr));
   }
-  // ---- multipole loop (loop precision T)
-  ct<T>* fa = (ct<T>*)smem_raw;
-  ct<T>* fb = fa + Q.nmax;
-  const bool exact_blocks = (sizeof(T) == sizeof(double));
+  const bool exact_blocks = Q.direct_every != 0;
+  const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
   int LM = LNL, done = 0;
   const int BLOCK = 16;
   const double sqpi = sqrt(M_PI);
+  const double dlnx = geo.dlnx;
   for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
     const int ke = (ks + BLOCK < LNL) ? ks + BLOCK : LNL;
     for (int k = ks; k < ke; k++) {
+      __syncthreads();
       for (int i = tid; i < nchi; i += NL_NT) F[i] = (T)0;
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
-        const double base = xg[0] / exp(2 * Q.pad[j] * dlnx);
-        const double y0 = (k + 1.) / xg[nchi - 1];
+        const double base = geo.x0 / exp(2 * Q.pad[j] * dlnx);
+        const double y0 = (k + 1.) / geo.xlast;
         const double lnbase = log(base * y0);
         const double deta = 2.0 * M_PI / (dlnx * N);
         __syncthreads();
         ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
-        // Gamma-ratio kernels: direct for the first two multipoles (of every
-        // 16-block in the FP64 plan, as the reference does; of the whole
-        // walk in the mixed plan), two-step recurrence otherwise.
         const bool direct = exact_blocks ? (k < ks + 2) : (k < 2);
         const int slot = exact_blocks ? ((k - ks) & 1) : (k & 1);
+        const int di = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
+        const double* gd = gdir + ((size_t)j * Q.ndirect + (direct ? di : 0)) * Q.hstride * 2;
         for (int i = tid; i < nq; i += NL_NT) {
-          const double eta = deta * i;
           ct<T> g;
           if (direct) {
-            const cd gd = gl_direct(Q.deriv[j], Q.nu[j], eta, k);
-            g = tmk<T>((T)gd.x, (T)gd.y);
+            g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
           } else {
-            const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)eta;
+            const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
             ct<T> num, den;
             if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
             else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
@@ -444,7 +505,7 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
           }
           gs[slot * Q.hstride + i] = g;
           // phase exp(-i eta lnbase), argument reduced in FP64
-          double ph = -eta * lnbase;
+          double ph = -(deta * i) * lnbase;
           ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
           T sp, cp;
           tsincos<T>((T)ph, &sp, &cp);
@@ -464,10 +525,7 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
         const T magf = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
         for (int i = tid; i < nchi; i += NL_NT) {
           T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
-          if (j == 2) {
-            const T xx = (T)xg[nchi - 1 - i];
-            fy = magf * fy * xx * xx;
-          }
+          if (j == 2) fy = magf * fy * xx2[i];
           F[i] += fy;
         }
         __syncthreads();
@@ -475,21 +533,33 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
       // chi sum of F^2 k^3 P_lin(k, a = 1)
       double part = 0.0;
       const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+      const double lk1 = log10(k + 1.);
+      const T cub = (T)((k + 1.) * (k + 1.) * (k + 1.));
       for (int i = tid; i < nchi; i += NL_NT) {
-        const double k1 = (k + 1.) / xg[nchi - 1 - i] * rc;
-        const T lkv = tlog10<T>((T)(k1 / CL2PT_COVERH0));
+        // p_lin(k, 1): search on the loop-precision axis, in-cell offset and
+        // lnP difference in FP64, exponent split as in the Limber walk
+        const double lkv = lk1 + lxk[i];
         int lo = 0, hi = P.pkl_nk - 1;
+        const T lkt = (T)lkv;
         while (hi > lo + 1) {
           const int mid = (lo + hi) >> 1;
-          if (plk[mid] > lkv) hi = mid; else lo = mid;
+          if (plk[mid] > lkt) hi = mid; else lo = mid;
         }
-        const T dx = (lkv - plk[lo]) / (plk[lo + 1] - plk[lo]);
-        const T pl = texp<T>(psl[lo] + dx * (psl[lo + 1] - psl[lo])) * lc3;
-        const T k3 = (T)(k1 * k1 * k1);
+        const double dxd = (lkv - plkd[lo]) * pinv[lo];
+        T pl;
+        if (sizeof(T) == sizeof(double)) {
+          pl = (T)(exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+        } else {
+          const T h0f = (T)psl[lo];
+          const T del = (T)(psl[lo] - (double)h0f) + (T)dxd * (T)(psl[lo + 1] - psl[lo]);
+          pl = texp<T>(h0f) * texp<T>(del) * lc3;
+        }
+        // k^3 = ((l+1) rc / x)^3
+        const T k3 = cub * rx3[i];
         part += (double)(F[i] * F[i] * k3 * pl);
       }
       const double tcl = block_sum(part, red);
-      if (tid == 0) Cl[k] = tcl * dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+      if (tid == 0) Cl[k] = tcl * geo.dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
     }
     __syncthreads();
     // convergence at the block end (cosmo2D.c:4741-4750)
@@ -516,24 +586,27 @@ __global__ void __launch_bounds__(NL_NT) k_nonlimber(Params P, NLParams Q)
   }
 }
 
+template <typename T>
+static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
+{
+  const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
+  cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q);
+  k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
+  const size_t sm3 = sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi) +
+                     sizeof(T) * (2 * 2 * (size_t)Q.nmax + 6 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
+  cudaFuncSetAttribute(k_nl_loop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+  k_nl_loop<T><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q);
+}
+
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
                       const Hook& hk)
 {
-  const bool fp64 = P.prec == CL2PT_PREC_FP64;
-  const size_t tsz = fp64 ? sizeof(double) : sizeof(float);
-  const size_t sm = sizeof(double) * 2 * 2 * Q.nmax + sizeof(double) * P.nl_nchi +
-                    tsz * (4 * (size_t)P.nl_nchi + 2 * P.pkl_nk) + 64;
-  dim3 g(P.B, P.nl);
   hk(CL2PT_K_NONLIMBER, 1);
-  if (fp64) {
-    cudaFuncSetAttribute(k_nonlimber<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_nonlimber<double><<<g, NL_NT, sm, s>>>(P, Q);
-  } else {
-    cudaFuncSetAttribute(k_nonlimber<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_nonlimber<float><<<g, NL_NT, sm, s>>>(P, Q);
-  }
+  if (P.prec == CL2PT_PREC_FP64) launch_nl_t<double>(P, Q, s);
+  else launch_nl_t<float>(P, Q, s);
   hk(CL2PT_K_NONLIMBER, 0);
-  (*launches)++;
+  (*launches) += 3;
 }
 
 }  // namespace cl2pt

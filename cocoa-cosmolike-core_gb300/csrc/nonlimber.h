@@ -20,6 +20,9 @@ struct NLParams {
   void* tout;       // [CTA][3][hstride] complex spectra (loop precision)
   size_t tout_stride;   // complex entries per CTA
   void* gstate;     // [CTA][3][2][hstride] complex recurrence state (loop precision)
+  double* gdir;     // [point][3][ndirect][hstride] directly evaluated g_l (FP64 complex)
+  int ndirect;      // multipoles evaluated directly per kernel
+  int direct_every; // 1: restart the recurrence every 16-block (FP64 plan)
   size_t gst_stride;
 };
 

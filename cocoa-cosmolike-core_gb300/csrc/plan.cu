@@ -610,6 +610,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(dalloc(p, &t2, (size_t)W * nl * Q.gst_stride * 2));
       Q.tout = t1;
       Q.gstate = t2;
+      Q.direct_every = (precision == CL2PT_PREC_FP64) ? 1 : 0;
+      Q.ndirect = Q.direct_every ? 2 * ((LNL + 15) / 16) : 2;
+      TRY(dalloc(p, &Q.gdir, (size_t)W * 3 * Q.ndirect * Q.hstride * 2));
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
