@@ -294,43 +294,67 @@ __device__ __forceinline__ int bsearch_from(const T* __restrict__ x, int n, T v,
   return bsearch_t(x, n, v);
 }
 
+constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
+
 template <typename T>
-__global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __restrict__ ell,
-                                                  int mode)
+__global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __restrict__ ell,
+                                                   int mode)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
   const int q = blockIdx.z;
   const int tid = threadIdx.x;
-  const int L = blockIdx.y * LT + tid;
+  const int L = blockIdx.y * LTG + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   const PdeltaTable pl = pdelta_table(P, pt, true);
   const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
   const bool same_axis = P.G_same_axis != 0;
-  // node data [8][PCH] doubles, FP64 axes + inverse widths of both tables,
-  // then int [2][PCH], then T arrays
+  // shared: node data [8][PCH], FP64 axes + inverse widths of both P tables,
+  // int [2][PCH], then T arrays: P axes, distance table (chi, z, and the
+  // per-cell slopes chi_all interpolates), growth table (value, slope, z),
+  // n(z) spline of bin q.
   double* nd = (double*)smem_raw;
   double* sd = nd + 8 * PCH;
   double* si = sd + pd.nk;
   double* sdl = si + pd.nk;
   double* sil = sdl + pl.nk;
   int* nj = (int*)(sil + pl.nk);
-  T* lk = (T*)(nj + 2 * PCH);       // Pdelta axis
-  T* lkl = lk + pd.nk;              // linear axis
-  T* cz = lkl + pl.nk;              // chi table z axis
-  T* cx = cz + nc;                  // chi values (Mpc/h)
-  T* gz = cx + nc;                  // growth table z axis (unused if same as cz)
-  T* gv = gz + ng;                  // growth values
-  T* szc = gv + ng;                 // n(z) spline nodes, values, coefficients of bin q
+  T* lk = (T*)(nj + 2 * PCH);
+  T* lkl = lk + pd.nk;
+  T* cx = lkl + pl.nk;   // chi (Mpc/h)
+  T* cz = cx + nc;       // z
+  T* cdn = cz + nc;      // chi_all 'down' slope of cell j (dchi/dz)
+  T* cup = cdn + nc;     // chi_all 'up' slope of cell j
+  T* gv = cup + nc;      // growth G
+  T* gs = gv + ng;       // growth slope of cell j
+  T* gz = gs + ng;       // growth z axis (when it differs from the distance axis)
+  T* szc = gz + ng;      // n(z) spline nodes, values, coefficients of bin q
   T* sy = szc + nzs;
   T* sc = sy + nzs;
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
   const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const Axis<T> axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
-  for (int i = tid; i < nc; i += LT) { cz[i] = (T)P.chi_z[i]; cx[i] = (T)Xg[i]; }
-  for (int i = tid; i < ng; i += LT) { gz[i] = (T)P.G_z[i]; gv[i] = (T)Gg[i]; }
-  for (int i = tid; i < nzs; i += LT) {
+  const double* Z = P.chi_z;
+  for (int i = tid; i < nc; i += LTG) {
+    cx[i] = (T)Xg[i];
+    cz[i] = (T)Z[i];
+    if (i + 1 < nc) {
+      // slopes of chi_all (cosmo3D.c:60-72), formed in FP64
+      const int j2 = (i + 2 < nc) ? i + 2 : nc - 1;
+      cup[i] = (T)((Xg[j2] - Xg[i]) / (Z[j2] - Z[i]));
+      cdn[i] = (T)((i > 0) ? (Xg[i + 1] - Xg[i - 1]) / (Z[i + 1] - Z[i - 1])
+                           : (Xg[i + 1] - Xg[i]) / (Z[i + 1] - Z[i]));
+    } else {
+      cup[i] = cdn[i] = (T)0;
+    }
+  }
+  for (int i = tid; i < ng; i += LTG) {
+    gv[i] = (T)Gg[i];
+    gz[i] = (T)P.G_z[i];
+    gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
+  }
+  for (int i = tid; i < nzs; i += LTG) {
     szc[i] = (T)P.lens_zc[i];
     sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
     sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
@@ -350,11 +374,12 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
   const T c1 = (T)(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
   const double chi_amin = P.chi_amin[pt];
   const T cH0 = (T)CL2PT_COVERH0;
+  const T ratio = (T)((lp + 1.0) / lp);
   double sum_nl = 0.0, sum_lin = 0.0;
   for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
     const int np = min(PCH, P.n_gg - p0);
     __syncthreads();
-    for (int p = tid; p < np; p += LT) {
+    for (int p = tid; p < np; p += LTG) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p0 + p];
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
       nd[0 * PCH + p] = fK;
@@ -365,7 +390,6 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
       nd[4 * PCH + p] = P.wgg_m[b0 * P.n_gg + p0 + p];
       nd[5 * PCH + p] = P.wgg_r0[b0 * P.n_gg + p0 + p];
       nj[p] = nodej[off + p0 + p];
-      // linear-table z cell of the node
       const double z = 1.0 / a - 1.0;
       const int jl = bsearch_d(pl.z, pl.nz, z);
       nj[PCH + p] = jl;
@@ -379,28 +403,21 @@ __global__ void __launch_bounds__(LT) k_limber_gg(Params P, const double* __rest
       const double fK = nd[0 * PCH + p];
       const double chi1 = fK * (lp + 1.0) / lp;  // (l+3/2)/k
       if (chi1 > chi_amin) continue;
-      // a_chi (cosmo3D.c:109-133)
-      const T c = (T)(chi1 * CL2PT_COVERH0);
+      // a_chi at chi1 (cosmo3D.c:109-133)
+      const T c = (T)(fK * CL2PT_COVERH0) * ratio;
       const int j = bsearch_t(cx, nc, c);
       const T dyc = (c - cx[j]) / (cx[j + 1] - cx[j]);
       const T z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
-      const T a1 = (T)1 / ((T)1 + z1);
-      // chi_all(a1).dchida (cosmo3D.c:40-92)
-      const T zz = (T)1 / a1 - (T)1;
-      const int jc = bsearch_from(cz, nc, zz, j);
-      const T dy2 = (zz - cz[jc]) / (cz[jc + 1] - cz[jc]);
-      const int j2 = (jc + 2 < nc) ? jc + 2 : nc - 1;
-      const T up = (cx[j2] - cx[jc]) / (cz[j2] - cz[jc]);
-      const T dn = (jc > 0) ? (cx[jc + 1] - cx[jc - 1]) / (cz[jc + 1] - cz[jc - 1])
-                            : (cx[jc + 1] - cx[jc]) / (cz[jc + 1] - cz[jc]);
-      const T dchida = (dn + dy2 * (up - dn)) / cH0 / (a1 * a1);
-      const T H1 = (T)1 / ((a1 * a1) * dchida);
+      // H/H0 at a1 = 1/(1+z1): chi_all's slope interpolated in the cell
+      // found by its own search (the a_chi cell when z1 lies inside it)
+      const int jc = bsearch_from(cz, nc, z1, j);
+      const T dy2 = (jc == j) ? dyc : (z1 - cz[jc]) / (cz[jc + 1] - cz[jc]);
+      const T H1 = cH0 / (cdn[jc] + dy2 * (cup[jc] - cdn[jc]));
       // f_growth(z1) (cosmo3D.c:200-228)
-      const T* gza = same_axis ? cz : gz;
-      const int jg = same_axis ? bsearch_from(gza, ng, z1, jc) : bsearch_t(gza, ng, z1);
-      const T sl = (gv[jg + 1] - gv[jg]) / (gza[jg + 1] - gza[jg]);
-      const T Gz = gv[jg] + (z1 - gza[jg]) / (gza[jg + 1] - gza[jg]) * (gv[jg + 1] - gv[jg]);
-      const T f1 = (T)1 - sl * z1 / Gz * ((T)1 + z1) / z1;
+      const int jg = same_axis ? jc : bsearch_t(gz, ng, z1);
+      const T dyg = same_axis ? dy2 : (z1 - gz[jg]) / (gz[jg + 1] - gz[jg]);
+      const T Gz = gv[jg] + dyg * (gv[jg + 1] - gv[jg]);
+      const T f1 = (T)1 - gs[jg] * ((T)1 + z1) / Gz;
       // nz_lens_photoz (redshift_spline.c:740-760)
       const T zs = (z1 - ldz - lzm) / lst + lzm;
       T n1 = (T)0;
@@ -460,17 +477,17 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
     const size_t sm = sizeof(double) * (8 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
-                      sizeof(T) * (P.pk_nk + P.pkl_nk + 2 * P.chi_nz + 2 * P.G_nz + 3 * P.lens_nz) + 64;
+                      sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
+    dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
-    k_limber_gg<T><<<g, LT, sm, s>>>(P, ell_g, 0);
+    k_limber_gg<T><<<g, LTG, sm, s>>>(P, ell_g, 0);
     hk(CL2PT_K_LIMBER_GG, 0);
     (*launches)++;
     if (!P.adopt_limber_gg) {
-      dim3 g2(P.B, (P.lmax_nolimber + LT - 1) / LT, P.nl);
+      dim3 g2(P.B, (P.lmax_nolimber + LTG - 1) / LTG, P.nl);
       hk(CL2PT_K_LIMBER_GGL, 1);
-      k_limber_gg<T><<<g2, LT, sm, s>>>(P, ell_g, 1);
+      k_limber_gg<T><<<g2, LTG, sm, s>>>(P, ell_g, 1);
       hk(CL2PT_K_LIMBER_GGL, 0);
       (*launches)++;
     }
