@@ -40,6 +40,12 @@ class Batch(C.Structure):
     ]
 
 
+class FastPTConfig(C.Structure):
+    """cl2pt_fastpt_config (the reference's fastpt_config)."""
+    _fields_ = [("nu", C.c_double), ("c_window_width", C.c_double), ("N_pad", C.c_long),
+                ("N_extrap_low", C.c_long), ("N_extrap_high", C.c_long)]
+
+
 class CL2PTError(RuntimeError):
     pass
 
@@ -69,6 +75,18 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_set_timing.argtypes = [C.c_void_p, C.c_int]
     lib.cl2pt_kernel_times.argtypes = [C.c_void_p, _dp, _ip]
     lib.cl2pt_status_string.restype = C.c_char_p
+    lib.cl2pt_fastpt_plan_create.argtypes = [_dp, C.c_long, _ip, _ip, _ip, C.c_int,
+                                             C.POINTER(FastPTConfig), C.c_int,
+                                             C.POINTER(C.c_void_p)]
+    lib.cl2pt_fastpt_plan_destroy.argtypes = [C.c_void_p]
+    lib.cl2pt_fastpt_J_abl.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                       C.c_void_p]
+    lib.cl2pt_fastpt_bias.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_void_p]
+    lib.cl2pt_fastpt_check_errors.argtypes = [C.c_void_p]
+    lib.cl2pt_fastpt_bias_terms.argtypes = [_ip, _ip, _ip, _ip, _dp]
+    lib.cl2pt_J_abl.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, _ip, C.c_int,
+                                C.POINTER(FastPTConfig), C.POINTER(_dp)]
     _lib = lib
     return lib
 
@@ -202,3 +220,100 @@ class Plan:
         out = np.zeros(self.cfg.n_source * self.cfg.n_a)
         check(load().cl2pt_debug_g_tables(self.h, point, _p(out)))
         return out.reshape(self.cfg.n_source, self.cfg.n_a)
+
+
+# ------------------------------------------------------------------ FAST-PT
+def _ints(v):
+    return np.ascontiguousarray(v, dtype=np.int32)
+
+
+def fastpt_config(nu=-2.0, c_window=0.65, npad=1500, nlow=500, nhigh=500) -> FastPTConfig:
+    """Defaults: the settings get_FPT_bias passes (pt_cfastpt.c:130-135)."""
+    c = FastPTConfig()
+    c.nu, c.c_window_width, c.N_pad, c.N_extrap_low, c.N_extrap_high = nu, c_window, npad, nlow, nhigh
+    return c
+
+
+def bias_terms():
+    """(alpha, beta, ell, output index, coefficient) of the 13 bias terms."""
+    a, b, l, o = (np.zeros(13, dtype=np.int32) for _ in range(4))
+    c = np.zeros(13)
+    n = load().cl2pt_fastpt_bias_terms(*(v.ctypes.data_as(_ip) for v in (a, b, l, o)), _p(c))
+    assert n == 13
+    return a, b, l, o, c
+
+
+class FastPT:
+    """Batched J_abl over spectra on one log-spaced grid x."""
+
+    def __init__(self, x, alpha, beta, ell, cfg: FastPTConfig | None = None, max_spec=1):
+        lib = load()
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.alpha, self.beta, self.ell = _ints(alpha), _ints(beta), _ints(ell)
+        self.nterms = len(self.alpha)
+        self.cfg = cfg if cfg is not None else fastpt_config()
+        self.max_spec = max_spec
+        h = C.c_void_p()
+        check(lib.cl2pt_fastpt_plan_create(_p(self.x), len(self.x), self.alpha.ctypes.data_as(_ip),
+                                           self.beta.ctypes.data_as(_ip),
+                                           self.ell.ctypes.data_as(_ip), self.nterms,
+                                           C.byref(self.cfg), max_spec, C.byref(h)),
+              "cl2pt_fastpt_plan_create")
+        self.h = h
+
+    @classmethod
+    def for_bias(cls, x, max_spec=1, cfg: FastPTConfig | None = None):
+        a, b, l, _, _ = bias_terms()
+        return cls(x, a, b, l, cfg, max_spec)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cl2pt_fastpt_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _run(self, fn, fx, nout):
+        fx = np.ascontiguousarray(np.atleast_2d(fx), dtype=np.float64)
+        out = np.zeros((fx.shape[0], nout, len(self.x)))
+        check(fn(self.h, fx.ctypes.data, fx.shape[0], out.ctypes.data, HOST, None), "fastpt")
+        return out
+
+    def J_abl(self, fx):
+        """fx [n][N0] (host) -> [n][nterms][N0]."""
+        return self._run(load().cl2pt_fastpt_J_abl, fx, self.nterms)
+
+    def bias(self, fx):
+        """fx [n][N0] (host) -> [n][5][N0]: P_d1d2, P_d2d2, P_d1s2, P_d2s2, P_s2s2."""
+        return self._run(load().cl2pt_fastpt_bias, fx, 5)
+
+    def J_abl_device(self, fx, out, stream=None):
+        """torch CUDA float64 tensors fx [n][N0], out [n][nterms][N0]."""
+        check(load().cl2pt_fastpt_J_abl(self.h, fx.data_ptr(), int(fx.shape[0]), out.data_ptr(),
+                                        DEVICE, stream), "fastpt")
+
+    def bias_device(self, fx, out, stream=None):
+        """torch CUDA float64 tensors fx [n][N0], out [n][5][N0]."""
+        check(load().cl2pt_fastpt_bias(self.h, fx.data_ptr(), int(fx.shape[0]), out.data_ptr(),
+                                       DEVICE, stream), "fastpt")
+
+    def check_errors(self):
+        check(load().cl2pt_fastpt_check_errors(self.h), "fastpt device check")
+
+
+def J_abl(x, fx, alpha, beta, ell, cfg: FastPTConfig | None = None):
+    """The reference-shaped entry point cl2pt_J_abl (one spectrum, host
+    arrays, Fy as an array of row pointers)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    fx = np.ascontiguousarray(fx, dtype=np.float64)
+    a, b, l = _ints(alpha), _ints(beta), _ints(ell)
+    cfg = cfg if cfg is not None else fastpt_config()
+    out = np.zeros((len(a), len(x)))
+    rows = (_dp * len(a))(*[out[t].ctypes.data_as(_dp) for t in range(len(a))])
+    check(load().cl2pt_J_abl(_p(x), _p(fx), len(x), a.ctypes.data_as(_ip), b.ctypes.data_as(_ip),
+                             l.ctypes.data_as(_ip), None, len(a), C.byref(cfg), rows), "cl2pt_J_abl")
+    return out

@@ -96,3 +96,25 @@ def stack(tabs):
     G = np.stack([t.G for t in tabs])
     lnP = np.stack([t.lnP.reshape(-1) for t in tabs])
     return om, h0, chi, G, lnP
+
+
+# ------------------------------------------------------------- FAST-PT batch
+FASTPT_NK = 2048
+FASTPT_KMIN, FASTPT_KMAX = 1e-5, 1e3  # h/Mpc
+
+
+def fastpt_spectra(n: int, seed: int = 0, nk: int = FASTPT_NK):
+    """Batched FAST-PT workload: n linear P(k, z=0) spectra (Eisenstein-Hu
+    no-wiggle, sigma_8 normalised) on nk log-spaced k in 1e-5..1e3 h/Mpc,
+    each with its own (Omega_m, h, n_s, sigma_8) drawn uniformly from
+    [0.25, 0.35] x [0.6, 0.8] x [0.92, 1.0] x [0.7, 0.9].
+    Returns (k [nk], P [n][nk], params [n][4])."""
+    rng = np.random.default_rng(SEED0 + 3 + seed)
+    k = np.geomspace(FASTPT_KMIN, FASTPT_KMAX, nk)
+    lo = np.array([0.25, 0.6, 0.92, 0.7])
+    hi = np.array([0.35, 0.8, 1.0, 0.9])
+    par = lo + (hi - lo) * rng.uniform(size=(n, 4))
+    P = np.empty((n, nk))
+    for i, (om, h, ns, s8) in enumerate(par):
+        P[i] = synthetic.plin_z0(k, synthetic.Cosmo(omega_m=om, h=h, ns=ns, sigma8=s8))
+    return k, P, par

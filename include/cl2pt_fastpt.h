@@ -1,0 +1,77 @@
+/*
+ * cl2pt_fastpt.h -- FAST-PT convolutions on the GPU (libcl2pt.so).
+ *
+ * The reference computes the one-loop bias spectra and the TATT IA terms
+ * with FAST-PT's J_abl / J_abJ1J2Jk FFT convolutions on the CPU
+ * (cfastpt/cfastpt.h:16-41, cosmolike/pt_cfastpt.c:47-177), one power
+ * spectrum at a time.  Here a FAST-PT plan fixes the k grid, the term list
+ * and the padding/window configuration (everything the transforms' Gamma-
+ * ratio kernels depend on) and evaluates a batch of spectra per call.
+ * Arithmetic is FP64 throughout: FP32 transforms lose ~1e-3 on individual
+ * terms.
+ */
+#ifndef CL2PT_FASTPT_H
+#define CL2PT_FASTPT_H
+
+#include "cl2pt_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same fields and order as the reference's fastpt_config
+ * (cfastpt/cfastpt.h:8-15). */
+typedef struct cl2pt_fastpt_config {
+  double nu;             /* power-law bias (scalar J_abl) */
+  double c_window_width; /* fraction of the spectrum tapered at each end */
+  long N_pad;            /* zero padding on each side */
+  long N_extrap_low;     /* log-extrapolated points below the grid */
+  long N_extrap_high;    /* log-extrapolated points above the grid */
+} cl2pt_fastpt_config;
+
+typedef struct cl2pt_fastpt_plan cl2pt_fastpt_plan;
+
+/* Plan for J_abl over spectra sampled on the log-spaced grid x[0..N-1]
+ * with the term list (alpha[t], beta[t], ell[t]), t < nterms.
+ * max_spec bounds the spectra of one call. */
+int cl2pt_fastpt_plan_create(const double* x, long N, const int* alpha,
+                             const int* beta, const int* ell, int nterms,
+                             const cl2pt_fastpt_config* cfg, int max_spec,
+                             cl2pt_fastpt_plan** plan);
+int cl2pt_fastpt_plan_destroy(cl2pt_fastpt_plan* plan);
+
+/* J_abl for nspec spectra: fx [nspec][N] -> Fy [nspec][nterms][N].
+ * where: CL2PT_HOST or CL2PT_DEVICE for both arrays.  Returns
+ * CL2PT_ERR_FFT when a spectrum cannot be log-extrapolated (zero or sign
+ * change at an end, cfastpt.c:1149-1187). */
+int cl2pt_fastpt_J_abl(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                       double* Fy, int where, void* stream);
+
+/* Waits for the device and reports the extrapolation check of the calls
+ * made with CL2PT_DEVICE arrays since the last call (CL2PT_ERR_FFT if a
+ * spectrum failed it; its outputs are NaN). */
+int cl2pt_fastpt_check_errors(cl2pt_fastpt_plan* plan);
+
+/* One-loop bias spectra of get_FPT_bias (pt_cfastpt.c:47-177) for the
+ * plan's 13-term bias list (cl2pt_fastpt_bias_terms): out [nspec][5][N] =
+ * P_d1d2, P_d2d2, P_d1s2, P_d2s2, P_s2s2.  where as above. */
+int cl2pt_fastpt_bias(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                      double* out, int where, void* stream);
+
+/* The 13 (alpha, beta, ell) terms, their output spectrum and coefficient
+ * (the FAST-PT one-loop bias decomposition used by get_FPT_bias). */
+int cl2pt_fastpt_bias_terms(int* alpha, int* beta, int* ell, int* out_index,
+                            double* coeff);
+
+/* Drop-in for the reference's J_abl (cfastpt/cfastpt.h:16-27): same
+ * arguments (host arrays; Fy[t] rows of length N; isP13type unused), run
+ * on the current CUDA device.  Returns 0 on success, a CL2PT_ERR_* status
+ * otherwise (the reference exits instead). */
+int cl2pt_J_abl(const double* x, const double* fx, long N, const int* alpha,
+                const int* beta, const int* ell, const int* isP13type,
+                int Nterms, const cl2pt_fastpt_config* config, double** Fy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
