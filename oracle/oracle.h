@@ -82,6 +82,15 @@ void orc_J_abJ1J2Jk(const double* x, const double* fx, long N,
 int orc_fpt_bias(double* out, int* n_out);
 /* TATT table [12][N] of the current point (get_FPT_IA) */
 int orc_fpt_ia(double* out, int* n_out);
+/* get_FPT_IA's table [12][N0] for a given spectrum on a given log grid */
+void orc_fpt_ia_spectrum(const double* k, const double* Pin, long N0, double* out);
+/* J_table expansion of {alpha, beta, l1, l2, l} rows (returns row count) */
+int orc_J_table(int nin, const int (*terms)[5], const double* cA, int out_cap,
+                int (*out)[5], double* cout);
+/* all TATT J-rows: start[9] group offsets, tab_row[8] FPTIA rows */
+int orc_ia_jrows(int cap, int (*rows)[5], double* coeff, int* start, int* tab_row);
+/* delta-E2 (which = 0) / mix-B (which = 1) direct kernel f[2 N0 - 1] */
+void orc_ia_direct_kernel(int which, long N0, double dL, double* f);
 
 #ifdef __cplusplus
 }

@@ -185,6 +185,48 @@ class Oracle:
         f(_p(out), C.byref(n))
         return out.reshape(8, n.value)
 
+    def fpt_ia(self):
+        n = C.c_int(0)
+        f = getattr(self.lib, self.which + "_fpt_ia")
+        f(None, C.byref(n))
+        out = np.zeros(12 * n.value)
+        f(_p(out), C.byref(n))
+        return out.reshape(12, n.value)
+
+    def fpt_ia_spectrum(self, k, P):
+        """get_FPT_IA's [12][N0] table for spectrum P on log grid k (oracle only)."""
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        out = np.zeros(12 * len(k))
+        self.lib.orc_fpt_ia_spectrum.argtypes = [_dp, _dp, C.c_long, _dp]
+        self.lib.orc_fpt_ia_spectrum(_p(k), _p(P), len(k), _p(out))
+        return out.reshape(12, len(k))
+
+    def ia_jrows(self):
+        """(rows [n][5] = alpha, beta, J1, J2, Jk; coeff [n]; start [9]; tab_row [8])."""
+        cap = 512
+        rows = np.zeros((cap, 5), dtype=np.int32)
+        coeff = np.zeros(cap)
+        start = np.zeros(9, dtype=np.int32)
+        trow = np.zeros(8, dtype=np.int32)
+        n = self.lib.orc_ia_jrows(cap, rows.ctypes.data_as(_ip), _p(coeff),
+                                  start.ctypes.data_as(_ip), trow.ctypes.data_as(_ip))
+        return rows[:n], coeff[:n], start, trow
+
+    def J_abJ1J2Jk(self, x, fx, alpha, beta, J1, J2, Jk, c_window=0.65, npad=1500, nlow=500,
+                   nhigh=500):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        fx = np.ascontiguousarray(fx, dtype=np.float64)
+        ia = lambda v: np.ascontiguousarray(v, dtype=np.int32)
+        a, b, j1, j2, jk = ia(alpha), ia(beta), ia(J1), ia(J2), ia(Jk)
+        Fy = np.zeros(len(a) * len(x))
+        f = getattr(self.lib, self.which + "_J_abJ1J2Jk")
+        f.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, _ip, _ip, C.c_int, C.c_double,
+                      C.c_double, C.c_long, C.c_long, C.c_long, _dp]
+        f(_p(x), _p(fx), len(x), *(v.ctypes.data_as(_ip) for v in (a, b, j1, j2, jk)), len(a),
+          0.0, c_window, npad, nlow, nhigh, _p(Fy))
+        return Fy.reshape(len(a), len(x))
+
     def J_abl(self, x, fx, alpha, beta, ell, nu=-2.0, c_window=0.65, npad=1500,
               nlow=500, nhigh=500):
         x = np.ascontiguousarray(x, dtype=np.float64)

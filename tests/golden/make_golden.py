@@ -20,7 +20,10 @@ sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
-         "fastpt_bias"]
+         "fastpt_bias", "fastpt_ia"]
+
+# J_abJ1J2Jk rows {alpha, beta, J1, J2, Jk} checked on the batched FAST-PT grid
+JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]
 
 
 def run_case(case, which="ref"):
@@ -34,6 +37,15 @@ def run_case(case, which="ref"):
         o.setup(w.cfg, w.src, w.lens)
         o.set_point(w.base, abi.make_nuisance())
         out["fpt_bias"] = o.fpt_bias()
+        return out
+    if case == "fastpt_ia":
+        w = workloads.make("real_3x2pt_small")
+        o.setup(w.cfg, w.src, w.lens)
+        o.set_point(w.base, abi.make_nuisance())
+        out["fpt_ia"] = o.fpt_ia()
+        k, P, _ = workloads.fastpt_spectra(1, seed=1)
+        r = np.array(JK_ROWS)
+        out["J_abJ1J2Jk"] = o.J_abJ1J2Jk(k, P[0], r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
         return out
     w = workloads.make(case)
     o.setup(w.cfg, w.src, w.lens)
