@@ -87,6 +87,18 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_fastpt_bias_terms.argtypes = [_ip, _ip, _ip, _ip, _dp]
     lib.cl2pt_J_abl.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, _ip, C.c_int,
                                 C.POINTER(FastPTConfig), C.POINTER(_dp)]
+    lib.cl2pt_fastpt_jk_plan_create.argtypes = [_dp, C.c_long, _ip, _ip, _ip, _ip, _ip, C.c_int,
+                                                C.POINTER(FastPTConfig), C.c_int,
+                                                C.POINTER(C.c_void_p)]
+    lib.cl2pt_fastpt_ia_plan_create.argtypes = [_dp, C.c_long, C.POINTER(FastPTConfig), C.c_int,
+                                                C.POINTER(C.c_void_p)]
+    lib.cl2pt_fastpt_J_abJ1J2Jk.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                            C.c_void_p]
+    lib.cl2pt_fastpt_ia.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                    C.c_void_p]
+    lib.cl2pt_fastpt_ia_terms.argtypes = [C.c_int, _ip, _ip, _ip, _ip, _ip, _ip, _dp]
+    lib.cl2pt_J_abJ1J2Jk.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, _ip, _ip, C.c_int,
+                                     C.POINTER(FastPTConfig), C.POINTER(_dp)]
     _lib = lib
     return lib
 
@@ -243,28 +255,62 @@ def bias_terms():
     return a, b, l, o, c
 
 
-class FastPT:
-    """Batched J_abl over spectra on one log-spaced grid x."""
+def ia_terms():
+    """(alpha, beta, J1, J2, Jk, output row, coefficient) of the 184 TATT J-rows."""
+    cols = [np.zeros(512, dtype=np.int32) for _ in range(6)]
+    c = np.zeros(512)
+    n = load().cl2pt_fastpt_ia_terms(512, *(v.ctypes.data_as(_ip) for v in cols), _p(c))
+    return tuple(v[:n] for v in cols) + (c[:n],)
 
-    def __init__(self, x, alpha, beta, ell, cfg: FastPTConfig | None = None, max_spec=1):
+
+class FastPT:
+    """Batched FAST-PT over spectra on one log-spaced grid x.
+
+    FastPT(x, alpha, beta, ell)            J_abl terms (bias list: .bias())
+    FastPT.jk(x, alpha, beta, J1, J2, Jk)  J_abJ1J2Jk terms
+    FastPT.for_ia(x)                       get_FPT_IA tables (.ia())
+    """
+
+    def __init__(self, x, alpha=None, beta=None, ell=None, cfg: FastPTConfig | None = None,
+                 max_spec=1, _kind="jabl", _jk=None):
         lib = load()
         self.x = np.ascontiguousarray(x, dtype=np.float64)
-        self.alpha, self.beta, self.ell = _ints(alpha), _ints(beta), _ints(ell)
-        self.nterms = len(self.alpha)
         self.cfg = cfg if cfg is not None else fastpt_config()
         self.max_spec = max_spec
+        self.kind = _kind
         h = C.c_void_p()
-        check(lib.cl2pt_fastpt_plan_create(_p(self.x), len(self.x), self.alpha.ctypes.data_as(_ip),
-                                           self.beta.ctypes.data_as(_ip),
-                                           self.ell.ctypes.data_as(_ip), self.nterms,
-                                           C.byref(self.cfg), max_spec, C.byref(h)),
-              "cl2pt_fastpt_plan_create")
+        if _kind == "jabl":
+            self.alpha, self.beta, self.ell = _ints(alpha), _ints(beta), _ints(ell)
+            self.nterms = len(self.alpha)
+            st = lib.cl2pt_fastpt_plan_create(_p(self.x), len(self.x), self.alpha.ctypes.data_as(_ip),
+                                              self.beta.ctypes.data_as(_ip),
+                                              self.ell.ctypes.data_as(_ip), self.nterms,
+                                              C.byref(self.cfg), max_spec, C.byref(h))
+        elif _kind == "jk":
+            self._cols = [_ints(v) for v in _jk]
+            self.nterms = len(self._cols[0])
+            st = lib.cl2pt_fastpt_jk_plan_create(_p(self.x), len(self.x),
+                                                 *(v.ctypes.data_as(_ip) for v in self._cols),
+                                                 self.nterms, C.byref(self.cfg), max_spec, C.byref(h))
+        else:
+            self.nterms = len(ia_terms()[0])
+            st = lib.cl2pt_fastpt_ia_plan_create(_p(self.x), len(self.x), C.byref(self.cfg), max_spec,
+                                                 C.byref(h))
+        check(st, "FAST-PT plan")
         self.h = h
 
     @classmethod
     def for_bias(cls, x, max_spec=1, cfg: FastPTConfig | None = None):
         a, b, l, _, _ = bias_terms()
         return cls(x, a, b, l, cfg, max_spec)
+
+    @classmethod
+    def jk(cls, x, alpha, beta, J1, J2, Jk, max_spec=1, cfg: FastPTConfig | None = None):
+        return cls(x, cfg=cfg, max_spec=max_spec, _kind="jk", _jk=(alpha, beta, J1, J2, Jk))
+
+    @classmethod
+    def for_ia(cls, x, max_spec=1, cfg: FastPTConfig | None = None):
+        return cls(x, cfg=cfg, max_spec=max_spec, _kind="ia")
 
     def close(self):
         if getattr(self, "h", None):
@@ -291,6 +337,19 @@ class FastPT:
         """fx [n][N0] (host) -> [n][5][N0]: P_d1d2, P_d2d2, P_d1s2, P_d2s2, P_s2s2."""
         return self._run(load().cl2pt_fastpt_bias, fx, 5)
 
+    def J_abJ1J2Jk(self, fx):
+        """fx [n][N0] (host) -> [n][nterms][N0] (jk and ia plans)."""
+        return self._run(load().cl2pt_fastpt_J_abJ1J2Jk, fx, self.nterms)
+
+    def ia(self, fx):
+        """fx [n][N0] (host) -> [n][10][N0]: the get_FPT_IA table rows 0-9."""
+        return self._run(load().cl2pt_fastpt_ia, fx, 10)
+
+    def ia_device(self, fx, out, stream=None):
+        """torch CUDA float64 tensors fx [n][N0], out [n][10][N0]."""
+        check(load().cl2pt_fastpt_ia(self.h, fx.data_ptr(), int(fx.shape[0]), out.data_ptr(),
+                                     DEVICE, stream), "fastpt")
+
     def J_abl_device(self, fx, out, stream=None):
         """torch CUDA float64 tensors fx [n][N0], out [n][nterms][N0]."""
         check(load().cl2pt_fastpt_J_abl(self.h, fx.data_ptr(), int(fx.shape[0]), out.data_ptr(),
@@ -316,4 +375,18 @@ def J_abl(x, fx, alpha, beta, ell, cfg: FastPTConfig | None = None):
     rows = (_dp * len(a))(*[out[t].ctypes.data_as(_dp) for t in range(len(a))])
     check(load().cl2pt_J_abl(_p(x), _p(fx), len(x), a.ctypes.data_as(_ip), b.ctypes.data_as(_ip),
                              l.ctypes.data_as(_ip), None, len(a), C.byref(cfg), rows), "cl2pt_J_abl")
+    return out
+
+
+def J_abJ1J2Jk(x, fx, alpha, beta, J1, J2, Jk, cfg: FastPTConfig | None = None):
+    """The reference-shaped entry point cl2pt_J_abJ1J2Jk (one spectrum)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    fx = np.ascontiguousarray(fx, dtype=np.float64)
+    cols = [_ints(v) for v in (alpha, beta, J1, J2, Jk)]
+    cfg = cfg if cfg is not None else fastpt_config()
+    n = len(cols[0])
+    out = np.zeros((n, len(x)))
+    rows = (_dp * n)(*[out[t].ctypes.data_as(_dp) for t in range(n)])
+    check(load().cl2pt_J_abJ1J2Jk(_p(x), _p(fx), len(x), *(v.ctypes.data_as(_ip) for v in cols), n,
+                                  C.byref(cfg), rows), "cl2pt_J_abJ1J2Jk")
     return out

@@ -1,21 +1,27 @@
-// fastpt.h -- device-side description of a batched FAST-PT J_abl program.
+// fastpt.h -- device-side description of a batched FAST-PT program.
 //
-// A program is the reference's term list (alpha_t, beta_t, ell_t)
-// (cfastpt/cfastpt.c:875-1430) regrouped for the GPU:
-//   inputs u   distinct (q, ell) pairs; the padded Hermitian sequence
-//              x_u[halfN + i] = out[i] * g_m(ell + 1/2, 1.5 + nu + q; eta_i) / N
-//              (out = windowed r2c of the biased spectrum) is what one
-//              forward transform of size Ntot sees.  Terms that share
-//              alpha or beta and ell share an input.
-//   rows j     output spectra; row j = sum over its terms of c_t * J_t.
-//              J_abl has one row per term; get_FPT_bias sums 13 terms into
-//              5 rows.  All terms of a row share p = -5 - 2 nu - alpha - beta,
-//              hence the final multiplier conj(f_z(p + 1)) 2^{i tau} and the
-//              k power, so the sum is taken before the inverse transform.
+// A program regroups the reference's term lists (J_abl: (alpha, beta, ell),
+// cfastpt/cfastpt.c:875-1430; J_abJ1J2Jk: (alpha, beta, J1, J2, Jk),
+// cfastpt.c:91-768) for the GPU:
+//   biases b   the power-law biased copies of the padded spectrum, f / x^nu_b
+//              (J_abl: nu; J_abJ1J2Jk: nu = -2 - alpha for every distinct
+//              alpha or beta); each is transformed once per spectrum.
+//   inputs u   distinct (bias, Gamma kernel) pairs; the padded Hermitian
+//              sequence x_u[halfN + i] = out_b(u)[i] * G_u[i] with
+//              G_u = window * g_m(...) / N is what one forward transform of
+//              size Ntot sees.  Terms sharing a side share an input.
+//   rows j     sums over terms of c_t * R_a(t) R_b(t) (the convolution's
+//              spectrum) whose lag-domain result takes one final multiplier
+//              H_j: conj(f_z(p + 1)) 2^{i tau} (J_abl) or conj(g_m(Jk + 1/2,
+//              -1/2)) (J_abJ1J2Jk).
+//   groups g   output spectra: the c2r of the sum of their rows' products,
+//              times the k power kpow_g.  J_abl and the bias sums have one
+//              row per group; the TATT groups have one row per Jk.
 // Transforms are paired: a zero-padded Hermitian sequence transforms to
 // exp(-i pi N k / Ntot) times a real sequence, so two inputs share one
-// complex FFT; two rows' real products likewise share one inverse FFT,
-// and two rows' real outputs one size-N c2r.
+// complex FFT; two rows' real spectra share one inverse FFT; two groups'
+// real outputs share one size-N c2r; two biased real inputs share one
+// size-N forward transform.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -25,36 +31,55 @@ namespace cl2pt {
 
 struct FPTDev {
   int N0, N, half, Ntot, npad, nlow, nhigh, off;  // off = npad + nlow
-  int n_in, n_fp, n_row, n_ip;
+  int n_bias, n_in, n_fp, n_row, n_ip, n_grp, n_gp;
   fft64::Desc dN, dT;
   const double2* twN;       // exp(-2 pi i j / N), j < N
   const double2* twT;       // exp(-2 pi i j / Ntot)
   const double2* phT;       // exp(-i pi N rev(p) / Ntot) at each DIF position p
   const int* posN;          // frequency k -> DIF position, size N
-  const double* den_main;   // x_i^nu on the grid [N0]
-  const double* den_low;    // x^nu at the low extrapolated points [nlow]
-  const double* den_high;   // x^nu at the high extrapolated points [nhigh]
+  const double* den;        // [n_bias][N] x_full^nu_b on the padded grid (1 in the pads)
   const double2* G;         // [n_in][half + 1] window * g_m / N
-  const double2* H;         // [n_p][N + 1] conj(f_z(p + 1)) * 2^{i tau}
-  const double* kpow;       // [n_p][N0] x^{-p-2}
+  const int* in_bias;       // [n_in] bias of each input (null: all 0)
+  const double2* H;         // [n_h][N + 1] final multiplier of each row class
+  const double* kpow;       // [n_kp][N0] k power of each group class
   const int2* fpair;        // [n_fp] inputs (u1, u2 | -1)
-  const int* t_ua;          // [terms] input of alpha side
-  const int* t_ub;          // [terms] input of beta side
+  const int* t_ua;          // [terms] input of the alpha side
+  const int* t_ub;          // [terms] input of the beta side
   const double* t_c;        // [terms] coefficient * prefactor / Ntot
   const int* row_start;     // [n_row + 1] term range of each row
-  const int* row_p;         // [n_row] H / kpow row
-  const int* row_out;       // [n_row] output slot
+  const int* row_p;         // [n_row] H row of each row
+  const int* row_out;       // [n_row] output slot (single-row groups)
   const int2* ipair;        // [n_ip] rows (j1, j2 | -1)
+  const int* grp_start;     // [n_grp + 1] row range of each group (multi-row)
+  const int* grp_kp;        // [n_grp] kpow row of each group
+  const int* grp_out;       // [n_grp] output slot of each group
+  const int2* gpair;        // [n_gp] groups (g1, g2 | -1)
   int n_out;                // output slots per spectrum
-  double2* xin;             // scratch [S][half + 1]
+  bool multi;               // some group has several rows: V + c2r kernels
+  double2* xin;             // scratch [S][n_bias][half + 1]
   double* R;                // scratch [S][n_in][Ntot]
+  double2* V;               // scratch [S][n_row][N + 1] (multi-row programs)
   int* err;                 // bit 0: extrapolation sign failure
+};
+
+// direct real convolutions of the spectrum with two fixed kernels (the
+// TATT delta-E2 and mix-B terms, pt_cfastpt.c:681-866)
+struct FPTDirect {
+  int N0, M, slot1, slot2, n_out;
+  fft64::Desc dM;
+  const double2* twM;       // exp(-2 pi i j / M)
+  const double2* F;         // [M] FFT(f1) + i FFT(f2) at DIF positions
+  const double* c1;         // [N0] output factors of the first kernel
+  const double* c2;         // [N0] and of the second
 };
 
 constexpr int FPT_THREADS = 512;
 
-// launchers (k_fastpt.cu); fx [S][N0] and out [S][n_out][N0] on device
 int fpt_smem_setup();
+// fx [S][N0] and out [S][n_out][N0] on device
 void launch_fastpt(const FPTDev& p, const double* fx, int S, double* out, cudaStream_t st);
+void launch_fastpt_direct(const FPTDirect& d, const double* fx, int S, double* out, cudaStream_t st);
+// F = DIF of (f1 + i f2) zero-padded to M, in place on dev_f (M complex)
+void launch_fastpt_kernel_fft(const FPTDirect& d, double2* dev_f, cudaStream_t st);
 
 }  // namespace cl2pt

@@ -1,5 +1,6 @@
-// fft64.cuh -- in-place mixed-radix (2,3,4,5,7) FP64 FFTs on one shared-
-// memory buffer per CTA.
+// fft64.cuh -- in-place mixed-radix FP64 FFTs on one shared-memory buffer
+// per CTA: radices 2, 3, 4, 5, 7 with dedicated butterflies, any other
+// prime through a generic stage.
 //
 // dif<S>: natural order in, digit-reversed order out (Sande-Tukey
 //   decimation in frequency).  Position p then holds X[rev(p)], rev being
@@ -173,6 +174,47 @@ __device__ __forceinline__ void stage(double2* buf, int n, int L, const double2*
   __syncthreads();
 }
 
+// Any other prime radix R (sizes such as 5100 = 2^2 3 5^2 17): each thread
+// computes whole outputs y_k = sum_r x_r w_R^{rk} (times the stage twiddle)
+// from shared memory into registers, then all write after a barrier.
+// O(R) work per output; used for at most one or two stages of a size-N
+// transform.  n <= GENERIC_MAX_PER_THREAD * blockDim.x.
+constexpr int GENERIC_MAX_PER_THREAD = 16;
+
+template <int S, bool DIF>
+__device__ void stage_generic(double2* buf, int n, int L, int R, const double2* __restrict__ tw)
+{
+  const int m = L / R;
+  const int tstep = n / L;
+  const int rstep = n / R;  // w_R^e = tw[e * n / R]
+  double2 y[GENERIC_MAX_PER_THREAD];
+  int cnt = 0;
+  for (int o = threadIdx.x; o < n && cnt < GENERIC_MAX_PER_THREAD; o += blockDim.x, cnt++) {
+    const int q = o / R, k = o - (o / R) * R;  // butterfly q, output k
+    const int b = q / m;
+    const int j = q - b * m;
+    const double2* p = buf + b * L + j;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int r = 0; r < R; r++) {
+      double2 x = p[r * m];
+      if (!DIF && j && r) x = cmul(x, twid<S>(tw, j * r * tstep));
+      const int e = (r * k) % R;
+      acc = e ? cadd(acc, cmul(x, twid<S>(tw, e * rstep))) : cadd(acc, x);
+    }
+    if (DIF && j && k) acc = cmul(acc, twid<S>(tw, j * k * tstep));
+    y[cnt] = acc;
+  }
+  __syncthreads();
+  cnt = 0;
+  for (int o = threadIdx.x; o < n && cnt < GENERIC_MAX_PER_THREAD; o += blockDim.x, cnt++) {
+    const int q = o / R, k = o - (o / R) * R;
+    const int b = q / m;
+    const int j = q - b * m;
+    buf[b * L + j + k * m] = y[cnt];
+  }
+  __syncthreads();
+}
+
 template <int S, bool DIF>
 __device__ __forceinline__ void run_stage(double2* buf, int R, int n, int L, const double2* tw)
 {
@@ -181,7 +223,8 @@ __device__ __forceinline__ void run_stage(double2* buf, int R, int n, int L, con
     case 3: stage<3, S, DIF>(buf, n, L, tw); break;
     case 4: stage<4, S, DIF>(buf, n, L, tw); break;
     case 5: stage<5, S, DIF>(buf, n, L, tw); break;
-    default: stage<7, S, DIF>(buf, n, L, tw); break;
+    case 7: stage<7, S, DIF>(buf, n, L, tw); break;
+    default: stage_generic<S, DIF>(buf, n, L, R, tw); break;
   }
 }
 

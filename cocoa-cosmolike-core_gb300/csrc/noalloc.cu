@@ -41,7 +41,7 @@ namespace {
 
 constexpr int FPT_NOALLOC_MAX_TERMS = 16;
 constexpr int FPT_NOALLOC_MAX_IN = 2 * FPT_NOALLOC_MAX_TERMS;
-constexpr int FPT_NOALLOC_MAX_NTOT = 14528;                    // 227 KB of double2
+constexpr int FPT_NOALLOC_MAX_NTOT = 14464;  // 227 KB of double2 less 1 KB of static shared memory
 constexpr int FPT_NOALLOC_MAX_N = (FPT_NOALLOC_MAX_NTOT - 1) / 2;  // Ntot >= 2N + 1
 constexpr int MAXH = FPT_NOALLOC_MAX_N / 2 + 1;
 
@@ -53,10 +53,8 @@ constexpr size_t OFF_TWN = OFF_X + al(sizeof(double) * FPT_NOALLOC_MAX_N);
 constexpr size_t OFF_TWT = OFF_TWN + al(sizeof(double2) * FPT_NOALLOC_MAX_N);
 constexpr size_t OFF_PHT = OFF_TWT + al(sizeof(double2) * FPT_NOALLOC_MAX_NTOT);
 constexpr size_t OFF_POSN = OFF_PHT + al(sizeof(double2) * FPT_NOALLOC_MAX_NTOT);
-constexpr size_t OFF_DM = OFF_POSN + al(sizeof(int) * FPT_NOALLOC_MAX_N);
-constexpr size_t OFF_DL = OFF_DM + al(sizeof(double) * FPT_NOALLOC_MAX_N);
-constexpr size_t OFF_DH = OFF_DL + al(sizeof(double) * FPT_NOALLOC_MAX_N);
-constexpr size_t OFF_G = OFF_DH + al(sizeof(double) * FPT_NOALLOC_MAX_N);
+constexpr size_t OFF_DEN = OFF_POSN + al(sizeof(int) * FPT_NOALLOC_MAX_N);
+constexpr size_t OFF_G = OFF_DEN + al(sizeof(double) * FPT_NOALLOC_MAX_N);
 constexpr size_t OFF_H = OFF_G + al(sizeof(double2) * FPT_NOALLOC_MAX_IN * MAXH);
 constexpr size_t OFF_KP = OFF_H + al(sizeof(double2) * FPT_NOALLOC_MAX_TERMS * (FPT_NOALLOC_MAX_N + 1));
 constexpr size_t OFF_XIN = OFF_KP + al(sizeof(double) * FPT_NOALLOC_MAX_TERMS * FPT_NOALLOC_MAX_N);
@@ -87,7 +85,7 @@ struct NAProgram {
 };
 
 struct NATables {
-  int N0, N, half, Ntot, nlow, nhigh, jh0, Ncut;
+  int N0, N, half, Ntot, npad, nlow, nhigh, Ncut;
   double nu, dlnx, lnx0, lnxN;
   cl2pt::fft64::Desc dN, dT;
 };
@@ -199,15 +197,12 @@ __global__ void k_noalloc_tables(NATables t, NAProgram g, unsigned char* base)
   double2* phT = (double2*)(base + OFF_PHT);
   int* posN = (int*)(base + OFF_POSN);
   const double* x = (const double*)(base + OFF_X);
-  double* dm = (double*)(base + OFF_DM);
-  double* dl = (double*)(base + OFF_DL);
-  double* dh = (double*)(base + OFF_DH);
+  double* den = (double*)(base + OFF_DEN);
   double2* G = (double2*)(base + OFF_G);
   double2* H = (double2*)(base + OFF_H);
   double* kp = (double*)(base + OFF_KP);
   const int H1 = t.half + 1;
-  const long nA = t.N, nB = nA + t.Ntot, nC = nB + t.N0, nD = nC + t.nlow, nE = nD + t.nhigh,
-             nF = nE + (long)g.n_p * t.N0, nG = nF + (long)g.n_in * H1, nH = nG + (long)g.n_p * (t.N + 1);
+  const long nA = t.N, nB = nA + t.Ntot, nE = nB + t.N, nF = nE + (long)g.n_p * t.N0, nG = nF + (long)g.n_in * H1, nH = nG + (long)g.n_p * (t.N + 1);
   const long stride = (long)gridDim.x * blockDim.x;
   for (long w = (long)blockIdx.x * blockDim.x + threadIdx.x; w < nH; w += stride) {
     if (w < nA) {
@@ -224,15 +219,19 @@ __global__ void k_noalloc_tables(NATables t, NAProgram g, unsigned char* base)
       const long k = ((long)t.N * na_rev(t.dT, j)) % (2L * t.Ntot);
       sincos(-M_PI * (double)k / (double)t.Ntot, &s, &c);
       phT[j] = make_double2(c, s);
-    } else if (w < nC) {
-      const int i = (int)(w - nB);
-      dm[i] = pow(x[i], t.nu);
-    } else if (w < nD) {
-      const int h = (int)(w - nC);
-      dl[h] = pow(exp(t.lnx0 + (double)(h - t.nlow) * t.dlnx), t.nu);
     } else if (w < nE) {
-      const int h = (int)(w - nD);
-      dh[h] = pow(exp(t.lnxN + (double)(h + t.jh0) * t.dlnx), t.nu);
+      // x^nu on the padded grid: extrapolated points below and above the
+      // data, the data grid itself, 1 in the zero pads
+      const int n = (int)(w - nB);
+      const int off = t.npad + t.nlow;
+      double v = 1.0;
+      if (n >= t.npad && n < off)
+        v = pow(exp(t.lnx0 + (double)(n - off) * t.dlnx), t.nu);
+      else if (n >= off && n < off + t.N0)
+        v = pow(x[n - off], t.nu);
+      else if (n >= t.N - t.npad - t.nhigh && n < t.N - t.npad)
+        v = pow(exp(t.lnxN + (double)(n - off - t.N0) * t.dlnx), t.nu);
+      den[n] = v;
     } else if (w < nF) {
       const long r = w - nE;
       const int j = (int)(r / t.N0), i = (int)(r % t.N0);
@@ -264,6 +263,8 @@ __global__ void k_noalloc_tables(NATables t, NAProgram g, unsigned char* base)
     int* rs = ub + FPT_NOALLOC_MAX_TERMS;
     int* rp = rs + FPT_NOALLOC_MAX_TERMS + 1;
     int* ro = rp + FPT_NOALLOC_MAX_TERMS;
+    int* gk = ro + FPT_NOALLOC_MAX_TERMS;
+    int* go = gk + FPT_NOALLOC_MAX_TERMS;
     int2* fp = (int2*)(base + OFF_PROG + 1024);
     int2* ip = fp + FPT_NOALLOC_MAX_IN;
     double* tc = (double*)(base + OFF_PROG + 2048);
@@ -273,6 +274,8 @@ __global__ void k_noalloc_tables(NATables t, NAProgram g, unsigned char* base)
       rs[k] = k;
       rp[k] = g.tp[k];
       ro[k] = k;
+      gk[k] = g.tp[k];
+      go[k] = k;
       tc[k] = g.t_c[k];
     }
     rs[g.nterms] = g.nterms;
@@ -423,7 +426,7 @@ extern "C" int cl2pt_J_abl_noalloc(const double* x, const double* fx, long N0, c
   t.Ntot = (int)Ntot;
   t.nlow = (int)cfg->N_extrap_low;
   t.nhigh = (int)cfg->N_extrap_high;
-  t.jh0 = (int)(N - cfg->N_pad - cfg->N_extrap_high - (cfg->N_pad + cfg->N_extrap_low) - N0);
+  t.npad = (int)cfg->N_pad;
   t.Ncut = Ncut;
   t.nu = cfg->nu;
   t.dlnx = std::log(x[1] / x[0]);
@@ -455,9 +458,12 @@ extern "C" int cl2pt_J_abl_noalloc(const double* x, const double* fx, long N0, c
   p.twT = (const double2*)(base + OFF_TWT);
   p.phT = (const double2*)(base + OFF_PHT);
   p.posN = (const int*)(base + OFF_POSN);
-  p.den_main = (const double*)(base + OFF_DM);
-  p.den_low = (const double*)(base + OFF_DL);
-  p.den_high = (const double*)(base + OFF_DH);
+  p.den = (const double*)(base + OFF_DEN);
+  p.n_bias = 1;
+  p.in_bias = nullptr;
+  p.n_grp = nterms;
+  p.n_gp = 0;
+  p.multi = false;
   p.G = (const double2*)(base + OFF_G);
   p.H = (const double2*)(base + OFF_H);
   p.kpow = (const double*)(base + OFF_KP);
@@ -467,6 +473,8 @@ extern "C" int cl2pt_J_abl_noalloc(const double* x, const double* fx, long N0, c
   p.row_start = pr + 2 * FPT_NOALLOC_MAX_TERMS;
   p.row_p = pr + 3 * FPT_NOALLOC_MAX_TERMS + 1;
   p.row_out = pr + 4 * FPT_NOALLOC_MAX_TERMS + 1;
+  p.grp_kp = pr + 5 * FPT_NOALLOC_MAX_TERMS + 1;
+  p.grp_out = pr + 6 * FPT_NOALLOC_MAX_TERMS + 1;
   p.fpair = (const int2*)(base + OFF_PROG + 1024);
   p.ipair = (const int2*)(base + OFF_PROG + 1024) + FPT_NOALLOC_MAX_IN;
   p.t_c = (const double*)(base + OFF_PROG + 2048);

@@ -43,7 +43,8 @@ int cl2pt_fastpt_plan_destroy(cl2pt_fastpt_plan* plan);
 /* J_abl for nspec spectra: fx [nspec][N] -> Fy [nspec][nterms][N].
  * where: CL2PT_HOST or CL2PT_DEVICE for both arrays.  Returns
  * CL2PT_ERR_FFT when a spectrum cannot be log-extrapolated (zero or sign
- * change at an end, cfastpt.c:1149-1187). */
+ * change at an end, cfastpt.c:1149-1187; the same check guards the
+ * J_abJ1J2Jk entry points, where the reference would produce NaN). */
 int cl2pt_fastpt_J_abl(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
                        double* Fy, int where, void* stream);
 
@@ -63,6 +64,47 @@ int cl2pt_fastpt_bias(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
 int cl2pt_fastpt_bias_terms(int* alpha, int* beta, int* ell, int* out_index,
                             double* coeff);
 
+/* Plan for J_abJ1J2Jk (cfastpt/cfastpt.h:29-41) with the term list
+ * (alpha[t], beta[t], J1[t], J2[t], Jk[t]): each side biased by
+ * x^{2 + alpha}, kernels g_m(J + 1/2, -1/2).  cfg->nu is unused; the padded
+ * size N0 + 2 N_pad + N_extrap_low + N_extrap_high must be even. */
+int cl2pt_fastpt_jk_plan_create(const double* x, long N, const int* alpha,
+                                const int* beta, const int* J1, const int* J2,
+                                const int* Jk, int nterms,
+                                const cl2pt_fastpt_config* cfg, int max_spec,
+                                cl2pt_fastpt_plan** plan);
+
+/* J_abJ1J2Jk for nspec spectra: fx [nspec][N0] -> Fy [nspec][nterms][N0].
+ * Plans from cl2pt_fastpt_jk_plan_create or cl2pt_fastpt_ia_plan_create. */
+int cl2pt_fastpt_J_abJ1J2Jk(cl2pt_fastpt_plan* plan, const double* fx,
+                            int nspec, double* Fy, int where, void* stream);
+
+/* Plan for the TATT intrinsic-alignment tables of get_FPT_IA
+ * (cosmolike/pt_cfastpt.c:228-872): the eight J_table-expanded groups
+ * (cl2pt_fastpt_ia_terms) and the two direct convolutions. */
+int cl2pt_fastpt_ia_plan_create(const double* x, long N,
+                                const cl2pt_fastpt_config* cfg, int max_spec,
+                                cl2pt_fastpt_plan** plan);
+
+/* get_FPT_IA for nspec spectra: out [nspec][10][N0] holds the reference's
+ * FPTIA.tab rows 0-9 (tt E, tt B, ta dE1, ta dE2, ta 0E0E, ta 0B0B, mix A,
+ * mix B, mix D_EE, mix D_BB). */
+int cl2pt_fastpt_ia(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                    double* out, int where, void* stream);
+
+/* The J-rows of the TATT groups after J_table (utils_cfastpt.c:226-300):
+ * up to cap rows of (alpha, beta, J1, J2, Jk), the output row each feeds
+ * and its coefficient; returns the row count (184). */
+int cl2pt_fastpt_ia_terms(int cap, int* alpha, int* beta, int* J1, int* J2,
+                          int* Jk, int* slot, double* coeff);
+
+/* Drop-in for the reference's J_abJ1J2Jk (cfastpt/cfastpt.h:29-41): same
+ * arguments (host arrays; Fy[t] rows of length N), current CUDA device. */
+int cl2pt_J_abJ1J2Jk(const double* x, const double* fx, long N,
+                     const int* alpha, const int* beta, const int* J1,
+                     const int* J2, const int* Jk, int Nterms,
+                     const cl2pt_fastpt_config* config, double** Fy);
+
 /* Drop-in for the reference's J_abl (cfastpt/cfastpt.h:16-27): same
  * arguments (host arrays; Fy[t] rows of length N; isP13type unused), run
  * on the current CUDA device.  Returns 0 on success, a CL2PT_ERR_* status
@@ -79,7 +121,7 @@ int cl2pt_J_abl(const double* x, const double* fx, long N, const int* alpha,
  * config are host values as in cl2pt_J_abl.  All tables and workspace are
  * rebuilt per call in one static 10 MiB device array that every GPU
  * loading the library holds until exit, which limits a call to
- * Nterms <= 16 and a padded convolution size Ntot <= 14528 (larger
+ * Nterms <= 16 and a padded convolution size Ntot <= 14464 (larger
  * requests return CL2PT_ERR_ARG with a message on stderr).  Calls share
  * that array: calls whose work overlaps on the GPU race, so serialise
  * them.  The first call on each device looks up the array's address and

@@ -136,3 +136,74 @@ def test_fastpt_device_arrays(gpu_lib):
     plan.bias_device(fx, out, torch.cuda.current_stream().cuda_stream)
     plan.check_errors()
     assert np.array_equal(out.cpu().numpy(), host)
+
+
+# --------------------------------------------------------------- TATT (a14)
+JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]
+
+# Rows 3 (ta delta-E2) and 7 (mix B) are direct real convolutions of P with
+# kernels spanning ~1e10..1e-22 (pt_cfastpt.c:681-866); at high k the
+# output is ~1e-6 of the convolution's scale, and two FP64 FFT convolutions
+# of different lengths (the reference's 3 N0 - 2 and this path's 7-smooth
+# size) already differ there by ~5e-6 of the row peak.  Those rows are held
+# to an absolute 2e-5 of their peak; the other eight to the FAST-PT bar.
+DIRECT_ROWS = (3, 7)
+DIRECT_ABS = 2e-5
+
+
+def ia_check(got, ref):
+    worst = {}
+    for r in range(10):
+        if r in DIRECT_ROWS:
+            e = float(np.max(np.abs(got[r] - ref[r])) / np.max(np.abs(ref[r]))) / DIRECT_ABS * REL
+        else:
+            e = rel_rows(got[r], ref[r])
+        worst[r] = e
+    return max(worst.values()), worst
+
+
+@pytest.mark.gpu
+def test_fastpt_ia_matches_reference_golden(gpu_lib):
+    """get_FPT_IA's ten TATT rows on the reference's own grid (N0 = 1100:
+    N = 5100 = 2^2 3 5^2 17, Ntot = 10206, direct convolutions of 3298)."""
+    gold = np.load(os.path.join(HERE, "golden", "fastpt_ia.npz"))["fpt_ia"]
+    k, P = gold[10], gold[11]
+    plan = lib.FastPT.for_ia(k)
+    got = plan.ia(P)[0]
+    err, rows = ia_check(got, gold[:10])
+    print("ia vs reference (direct rows scaled to the FAST-PT bar)", rows)
+    assert err <= REL, rows
+
+
+@pytest.mark.gpu
+def test_fastpt_J_abJ1J2Jk_vs_reference_golden(gpu_lib):
+    """Individual J_abJ1J2Jk terms on the batched workload's grid."""
+    gold = np.load(os.path.join(HERE, "golden", "fastpt_ia.npz"))["J_abJ1J2Jk"]
+    k, P, _ = workloads.fastpt_spectra(1, seed=1)
+    r = np.array(JK_ROWS)
+    plan = lib.FastPT.jk(k, r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
+    got = plan.J_abJ1J2Jk(P)[0]
+    err = rel_rows(got, gold)
+    print("J_abJ1J2Jk vs reference", err)
+    assert err <= REL, err
+    drop = lib.J_abJ1J2Jk(k, P[0], r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
+    assert rel_rows(drop, gold) <= REL
+
+
+@pytest.mark.gpu
+def test_fastpt_ia_batch(gpu_lib, oracle_built):
+    """The batched workload (2048 k, 1e-5..1e3 h/Mpc): spot checks against
+    the oracle and batch independence."""
+    import oracle as O
+    o = O.Oracle("orc")
+    n = 300
+    k, P, _ = workloads.fastpt_spectra(n, seed=6)
+    plan = lib.FastPT.for_ia(k, max_spec=n)
+    got = plan.ia(P)
+    assert np.all(np.isfinite(got))
+    for i in (0, 255, 256, 299):
+        ref = o.fpt_ia_spectrum(k, P[i])[:10]
+        err, rows = ia_check(got[i], ref)
+        assert err <= REL, (i, rows)
+    one = lib.FastPT.for_ia(k, max_spec=1).ia(P[257:258])
+    assert np.array_equal(one[0], got[257])
