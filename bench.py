@@ -152,18 +152,10 @@ def run_reference(args):
     }))
 
 
-def fastpt_flops(N0, N, Ntot, nterms):
-    """Nominal FLOPs of the reference's J_abl sequence for one spectrum:
-    5 n log2 n per complex FFT and 2.5 n log2 n per real one, one r2c(N)
-    plus per term two c2c(Ntot) forward, one c2c(Ntot) back and one
-    c2r(2N)."""
-    lg = np.log2
-    return 2.5 * N * lg(N) + nterms * (3 * 5 * Ntot * lg(Ntot) + 2.5 * 2 * N * lg(2 * N))
-
-
 def run_fastpt(args):
-    """--workload fastpt_bias: get_FPT_bias's five one-loop bias spectra for
-    a batch of linear spectra (2048 log-k in 1e-5..1e3 h/Mpc)."""
+    """--workload fastpt: the batched FAST-PT workload -- for each linear
+    spectrum (2048 log-k in 1e-5..1e3 h/Mpc) get_FPT_bias's five one-loop
+    bias spectra and get_FPT_IA's ten TATT rows."""
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -176,68 +168,80 @@ def run_fastpt(args):
     cbuild.build()
     B = args.batch
     k, P, _ = workloads.fastpt_spectra(B, seed=100 + rank)
-    plan = lib.FastPT.for_bias(k, max_spec=B)
+    pb = lib.FastPT.for_bias(k, max_spec=B)
+    pi = lib.FastPT.for_ia(k, max_spec=B)
     fx = torch.from_numpy(P).to(dev)
-    out = torch.empty((B, 5, len(k)), dtype=torch.float64, device=dev)
+    ob = torch.empty((B, 5, len(k)), dtype=torch.float64, device=dev)
+    oi = torch.empty((B, 10, len(k)), dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
+
+    def step():
+        pb.bias_device(fx, ob, sptr)
+        pi.ia_device(fx, oi, sptr)
+
     for _ in range(args.warmup):
-        plan.bias_device(fx, out, sptr)
-    plan.check_errors()
+        step()
+    pb.check_errors()
+    pi.check_errors()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clk = Clocks(local)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
     for _ in range(args.steps):
-        plan.bias_device(fx, out, sptr)
-    e1.record(stream)
+        pb.bias_device(fx, ob, sptr)
+    ev[1].record(stream)
+    for _ in range(args.steps):
+        pi.ia_device(fx, oi, sptr)
+    ev[2].record(stream)
     torch.cuda.synchronize()
     clocks = clk.stop()
-    plan.check_errors()
-    ms = e0.elapsed_time(e1)
+    pb.check_errors()
+    pi.check_errors()
+    ms_b, ms_i = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    ms = ms_b + ms_i
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * B * args.steps / (ms / 1e3)
-    waves = -(-B // 512)
-    launches = 3 * waves * args.steps
-    # e2e: host (pinned) spectra in, host spectra out, through the C ABI
+    waves_b, waves_i = -(-B // 512), -(-B // 256)
+    launches = (3 * waves_b + 4 * waves_i + 1) * args.steps
+    # e2e: host (pinned) spectra in, both tables out, through the C ABI
     Ph = torch.from_numpy(P).pin_memory().numpy()
     for _ in range(2):
-        res = plan.bias(Ph)
+        rb, ri = pb.bias(Ph), pi.ia(Ph)
     n_e = max(2, args.steps // 2)
     t0 = time.perf_counter()
     for _ in range(n_e):
-        res = plan.bias(Ph)
+        rb, ri = pb.bias(Ph), pi.ia(Ph)
     te = time.perf_counter() - t0
     e2e = world * B * n_e / te
     N0 = len(k)
-    N, Ntot = 6048, 12150
-    flops = fastpt_flops(N0, N, Ntot, 13)
     hbm, src = peaks()
     alg_bytes = 8 * N0 * (1 + 5) * B
-    achieved = alg_bytes / (ms / args.steps / 1e3) / 1e9
+    achieved = alg_bytes / (ms_b / args.steps / 1e3) / 1e9
     line = {
-        "metric": "FAST-PT one-loop bias spectra/s (5 spectra per input, <=1e-6 rel err vs FP64)",
+        "metric": "FAST-PT spectra/s (one-loop bias + TATT IA tables per input spectrum, FP64)",
         "value": value, "unit": "input spectra/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (EH no-wiggle P(k), per-spectrum Om, h, ns, sigma8 ~ U)",
-        "config": {"workload": "fastpt_bias", "spectra_per_step_per_gpu": B, "nk": N0,
-                   "N": N, "Ntot": Ntot, "nu": -2.0, "c_window": 0.65, "N_pad": 1500,
-                   "N_extrap": [500, 500], "l2": "per-spectrum workspace 680 KB x batch > L2"},
-        "e2e": {"value": e2e, "unit": "input spectra/s", "h2d_bytes_per_step": int(P.nbytes),
-                "d2h_bytes_per_step": int(res.nbytes)},
+        "config": {"workload": "fastpt", "spectra_per_step_per_gpu": B, "nk": N0,
+                   "bias": {"N": 6048, "Ntot": 12150, "nu": -2.0, "terms": 13},
+                   "ia": {"N": 6048, "Ntot": 12150, "terms": 184, "direct_conv": 6144},
+                   "c_window": 0.65, "N_pad": 1500, "N_extrap": [500, 500],
+                   "l2": "per-spectrum workspace > 1 MB x batch > L2"},
+        "split_ms_per_step": {"bias": ms_b / args.steps, "ia": ms_i / args.steps},
+        "e2e": {"value": e2e, "unit": "input spectra/s", "h2d_bytes_per_step": int(2 * P.nbytes),
+                "d2h_bytes_per_step": int(rb.nbytes + ri.nbytes)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_fpt_* (3 kernels)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_fpt_* (bias pass)", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
                      "peak_source": src,
-                     "note": "FP64-pipe bound; the reference FLOP count below"},
-        "reference_flops_per_spectrum": flops,
-        "reference_flop_rate_tflops": flops * B * args.steps / (ms / 1e3) / 1e12,
+                     "note": "FP64-pipe bound (ncu: FP64 pipe 81-84% active); see profiles"},
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -246,16 +250,19 @@ def run_fastpt(args):
         o = O.Oracle("orc")
         a, b, l, _, _ = lib.bias_terms()
         n, t0 = 0, time.perf_counter()
-        while time.perf_counter() - t0 < 10.0 or n < 2:
+        while time.perf_counter() - t0 < 15.0 or n < 2:
             o.J_abl(k, P[n % B], a, b, l)
+            o.fpt_ia_spectrum(k, P[n % B])
             n += 1
         t = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": n / t, "unit": "input spectra/s", "cores": os.cpu_count(),
                                 "kind": "port",
-                                "sample": f"{n} spectra of the same batch (13 J_abl terms each), {t:.1f} s"}
+                                "sample": f"{n} spectra of the same batch (13 J_abl + 184 J_abJ1J2Jk "
+                                          f"terms + 2 direct convolutions each), {t:.1f} s"}
     if rank == 0:
         print(json.dumps(line))
-    plan.close()
+    pb.close()
+    pi.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -274,7 +281,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "fastpt_bias":
+    if args.workload == "fastpt":
         return run_fastpt(args)
 
     import torch
