@@ -9,6 +9,9 @@
                          b1 ~ U(1.2, 2.2); non-Limber w(theta)
   real_3x2pt_small       a reduced real_3x2pt (4 + 3 bins, 10 theta bins,
                          l <= 5000, 200 nodes) for fast checks
+  real_3x2pt_tatt[_small] the same with TATT intrinsic alignments
+                         (redshift evolution: A1, A2, eta, b_TA) and
+                         nonlinear galaxy bias (b2, bs2)
 
 Per-point variation: every walker gets its own P(k,z) amplitude/tilt,
 source photo-z shifts N(0, 0.02), shear calibration N(0, 0.01) and lens
@@ -33,6 +36,7 @@ class Workload:
     lens: np.ndarray
     base: synthetic.CosmoTables
     ell: np.ndarray | None = None  # Fourier multipoles
+    tatt: bool = False             # TATT IA + nonlinear galaxy bias nuisances
 
 
 def _fourier_ells(nell, lmin, lmax):
@@ -67,6 +71,15 @@ def make(name: str) -> Workload:
         w.cfg.adopt_limber_gg = 1
         w.name = name
         return w
+    if name in ("real_3x2pt_tatt", "real_3x2pt_tatt_small"):
+        # the differentiable-3x2pt layout: real_3x2pt plus TATT intrinsic
+        # alignments (redshift-evolution mode) and nonlinear galaxy bias
+        w = make(name.replace("_tatt", ""))
+        w.cfg.ia_model = abi.IA_TATT
+        w.cfg.ia_mode = abi.IA_REDSHIFT_EVOLUTION
+        w.name = name
+        w.tatt = True
+        return w
     raise KeyError(name)
 
 
@@ -77,11 +90,20 @@ def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True):
     tabs, nus = [], []
     for _ in range(n):
         t = synthetic.perturb_tables(w.base, rng) if vary_cosmo else w.base
+        extra = {}
+        if w.tatt:
+            # A1 ~ U(-1, 1), A2 ~ U(-2, 2), eta ~ U(-2, 2) (both IA powers),
+            # b_TA ~ U(0, 2); b2, bs2 ~ U(-1, 1) per lens bin
+            eta = rng.uniform(-2.0, 2.0)
+            extra = dict(ia=[[rng.uniform(-1.0, 1.0), eta], [rng.uniform(-2.0, 2.0), eta],
+                             [rng.uniform(0.0, 2.0)]],
+                         b2=rng.uniform(-1.0, 1.0, nl), bs2=rng.uniform(-1.0, 1.0, nl))
         nu = abi.make_nuisance(
             src_dz=rng.normal(0.0, 0.02, ns),
             lens_dz=rng.normal(0.0, 0.005, nl),
             shear_m=rng.normal(0.0, 0.01, ns),
             b1=rng.uniform(1.2, 2.2, nl),
+            **extra,
         )
         tabs.append(t)
         nus.append(nu)
