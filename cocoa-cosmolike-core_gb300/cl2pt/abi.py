@@ -28,6 +28,7 @@ class Config(C.Structure):
         ("bias_model", C.c_int * 6), ("linear_pk", C.c_int),
         ("probes", C.c_int), ("n_ggl_exclude", C.c_int),
         ("ggl_exclude", C.c_int * (2 * MAX_BINS * MAX_BINS)),
+        ("one_loop_bias", C.c_int),
     ]
 
 
@@ -69,7 +70,7 @@ def make_config(n_source=5, n_lens=5, ntheta=20, theta_min=2.5, theta_max=250.0,
                 adopt_limber_gg=0, ia_model=IA_NLA, ia_mode=NO_IA,
                 bias_model=(0, 0, 0, 0, 0, 0), linear_pk=0,
                 probes=PROBE_XI | PROBE_GAMMAT | PROBE_WTHETA,
-                ggl_exclude=()) -> Config:
+                ggl_exclude=(), one_loop_bias=0) -> Config:
     c = Config()
     c.n_source, c.n_lens, c.ntheta = n_source, n_lens, ntheta
     c.theta_min_arcmin, c.theta_max_arcmin = theta_min, theta_max
@@ -80,6 +81,7 @@ def make_config(n_source=5, n_lens=5, ntheta=20, theta_min=2.5, theta_max=250.0,
     for i, b in enumerate(bias_model):
         c.bias_model[i] = b
     c.linear_pk, c.probes = linear_pk, probes
+    c.one_loop_bias = one_loop_bias
     c.n_ggl_exclude = len(ggl_exclude)
     for i, (zl, zs) in enumerate(ggl_exclude):
         c.ggl_exclude[2 * i] = zl

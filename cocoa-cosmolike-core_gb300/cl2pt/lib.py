@@ -71,6 +71,7 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_debug_limber_tables.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     lib.cl2pt_debug_nonlimber.argtypes = [C.c_void_p, C.c_int, _dp, _ip]
     lib.cl2pt_debug_g_tables.argtypes = [C.c_void_p, C.c_int, _dp]
+    lib.cl2pt_debug_limber_bb.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.cl2pt_last_launch_count.argtypes = [C.c_void_p]
     lib.cl2pt_set_timing.argtypes = [C.c_void_p, C.c_int]
     lib.cl2pt_kernel_times.argtypes = [C.c_void_p, _dp, _ip]
@@ -220,6 +221,14 @@ class Plan:
         gg = np.zeros(pgg * nn)
         check(load().cl2pt_debug_limber_tables(self.h, point, _p(ss), _p(gs), _p(gg)))
         return ss.reshape(pss, nn), gs[: pgs * nn].reshape(pgs, nn), gg.reshape(pgg, nn)
+
+    def limber_bb(self, point=0):
+        """C_ss BB on the C_l nodes [pss][nnode] (TATT plans)."""
+        pss, _, _ = abi.n_pairs(self.cfg)
+        nn = self.cfg.lmin_tab - 1 + self.cfg.n_ell
+        bb = np.zeros(pss * nn)
+        check(load().cl2pt_debug_limber_bb(self.h, point, _p(bb)))
+        return bb.reshape(pss, nn)
 
     def nonlimber(self, point=0):
         nl, L = self.cfg.n_lens, self.cfg.lmax_nolimber

@@ -77,6 +77,7 @@ def make(name: str) -> Workload:
         w = make(name.replace("_tatt", ""))
         w.cfg.ia_model = abi.IA_TATT
         w.cfg.ia_mode = abi.IA_REDSHIFT_EVOLUTION
+        w.cfg.one_loop_bias = 1
         w.name = name
         w.tatt = True
         return w

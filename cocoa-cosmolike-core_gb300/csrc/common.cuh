@@ -87,6 +87,24 @@ struct Params {
   int* conv_l;              // [B][nl]
   double* obs;              // [B][n_total]  xi+, xi-, gamma_t, w
   int* err;                 // device error flag
+  // TATT intrinsic alignments and one-loop galaxy bias (extras pass)
+  int tatt;                 // ia_model == TATT
+  int one_loop;             // one-loop bias terms evaluated (per-point has_b2 gate)
+  int fpt_n;                // FAST-PT k grid: fpt_n points, ln k = fpt_lim0 + i fpt_lim2
+  double fpt_lim0, fpt_lim1, fpt_lim2;
+  double* fpt_plin;         // [B][fpt_n] p_lin(k, a = 1) on the FAST-PT grid
+  double* fpt_ia;           // [B][8][fpt_n] TATT rows: tt_E, ta_dE1+ta_dE2, ta_0E0E,
+                            //   mix_A+mix_B, mix_DEE, tt_B, ta_0B0B, mix_DBB
+  double* fpt_b;            // [B][5][fpt_n] d1d2, d2d2-2s4, d1s2, d2s2-4/3 s4, s2s2-8/9 s4
+  double* wss_b;            // [B][ns][n_ss]   WS C1 b_TA D^2 at ss nodes
+  double* wss_2;            // [B][ns][n_ss]   WS C2 D^2
+  double* wgs_k;            // [B][nl][ns][n_ss] WK at gs nodes
+  double* wgs_b;            // [B][nl][ns][n_ss] WS C1 b_TA D^2
+  double* wgs_2;            // [B][nl][ns][n_ss] WS C2 D^2
+  double* wgs_1l;           // [B][nl][2][n_ss] 0.5 D^4 WGAL (b2, bs2) (0 without b2)
+  double* wgg_1l;           // [B][nl][5][n_gg] WGAL^2 D^4 (b1 b2, b2^2/4, b1 bs2,
+                            //   b2 bs2/2, bs2^2/4) (0 without b2)
+  double* tab_ss_bb;        // [B][pss][nnode_ss] C_ss BB (TATT)
 };
 
 enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };

@@ -16,7 +16,8 @@ namespace cl2pt {
 
 constexpr int BM = 64, BN = 64, BK = 32, CT = 256;
 
-// mode 0: xi (M = 2 ntheta rows G+, G-; N = B*pss)
+// mode 0: xi (M = 2 ntheta rows G+, G-; N = B*pss); K = nnode_ss, or
+//         2 nnode_ss over [C_ss EE; C_ss BB] with TATT
 // mode 1: gamma_t (M = ntheta; N = B*pgs)
 // mode 2: w (M = ntheta; N = B*nl), B columns from tab_gg (Limber)
 // mode 3: w non-Limber: columns are [cnl (LNL), tab_gg (nnode_g)]
@@ -45,7 +46,9 @@ __global__ void __launch_bounds__(CT) k_contract(Params P, const double* __restr
       double v = 0.0;
       if (col < N && k < K) {
         const int pt = col / npair, pr = col - pt * npair;
-        if (mode == 0) v = P.tab_ss[((size_t)pt * P.pss + pr) * P.nnode_ss + k];
+        if (mode == 0)
+          v = (k < P.nnode_ss) ? P.tab_ss[((size_t)pt * P.pss + pr) * P.nnode_ss + k]
+                               : P.tab_ss_bb[((size_t)pt * P.pss + pr) * P.nnode_ss + (k - P.nnode_ss)];
         else if (mode == 1) v = P.tab_gs[((size_t)pt * P.pgs + pr) * P.nnode_g + k];
         else if (mode == 2) v = P.tab_gg[((size_t)pt * P.nl + pr) * P.nnode_g + k];
         else v = (k < LNL) ? P.cnl[((size_t)pt * P.nl + pr) * LNL + k]
@@ -92,7 +95,8 @@ void launch_legendre(const Params& P, const double* filt_xi, const double* filt_
   if (P.probes & CL2PT_PROBE_XI) {
     dim3 g((P.B * P.pss + BN - 1) / BN);
     hk(CL2PT_K_LEGENDRE, 1);
-    k_contract<<<g, CT, 0, s>>>(P, filt_xi, 2 * nt, P.nnode_ss, 0);
+    // with TATT the columns are [EE; BB] and the filters [[G+, G+], [G-, -G-]]
+    k_contract<<<g, CT, 0, s>>>(P, filt_xi, 2 * nt, (P.tatt ? 2 : 1) * P.nnode_ss, 0);
     hk(CL2PT_K_LEGENDRE, 0);
     (*launches)++;
   }

@@ -195,6 +195,42 @@ __device__ __forceinline__ double ia_a1(const Params& P, const cl2pt_nuisance& n
   return A * (om * 0.01389 / D);
 }
 
+// IA_A2_Z1: IA.c:298-356; IA_BTA_Z1: IA.c:358-415
+__device__ __forceinline__ double ia_a2(const Params& P, const cl2pt_nuisance& nu, double om,
+                                        double a, double D, int n)
+{
+  double A = 0.0;
+  if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) A = nu.ia[1][n];
+  else if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION)
+    A = nu.ia[1][0] * pow(1.0 / (a * 1.62), nu.ia[1][1]);
+  return A * (om * 0.01389 / (D * D));
+}
+__device__ __forceinline__ double ia_bta(const Params& P, const cl2pt_nuisance& nu, int n)
+{
+  if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) return nu.ia[2][n];
+  if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) return nu.ia[2][0];
+  return 1.0;
+}
+
+// b2 and bs2 of the selected bias models (bias.c:60-140)
+__device__ __forceinline__ double gb2_d(const Params& P, const cl2pt_nuisance& nu, int ni, double b1)
+{
+  if (P.bias_model[1] == 0) return nu.gb[1][ni];
+  return 0.412 - 2.143 * b1 + 0.929 * b1 * b1 + 0.008 * b1 * b1 * b1;
+}
+__device__ __forceinline__ double gbs2_d(const Params& P, const cl2pt_nuisance& nu, int ni, double b1)
+{
+  if (P.bias_model[2] == 0) return nu.gb[2][ni];
+  return -4. / 7. * (b1 - 1.0);
+}
+// the reference adds the one-loop bias terms when any lens bin has b2 != 0
+__device__ __forceinline__ bool has_b2(const Params& P, const cl2pt_nuisance& nu)
+{
+  for (int i = 0; i < P.nl; i++)
+    if (nu.gb[1][i] != 0.0) return true;
+  return false;
+}
+
 __device__ __forceinline__ double amin_lens_d(const Params& P, const cl2pt_nuisance& nu, int q)
 {
   const double zm = P.zmean_lens[q];
@@ -249,7 +285,17 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
     if (threadIdx.x == 0) atomicOr(P.err, 1);
     return;
   }
-  if (set == 0 && threadIdx.x == 0) P.chi_amin[pt] = chi_all_d(P.chi_z, X, P.chi_nz, P.a_min).chi;
+  const bool hb2 = has_b2(P, nu);
+  if (set == 0 && threadIdx.x == 0) {
+    P.chi_amin[pt] = chi_all_d(P.chi_z, X, P.chi_nz, P.a_min).chi;
+    // b2 != 0 needs the one-loop path; b3 and bK need terms not built here
+    // (the tabulated P_d1p3 of the reference, 2 b1 bK k^2 P)
+    bool bad = hb2 && !P.one_loop;
+    for (int i = 0; i < P.nl; i++)
+      if (hb2 && (nu.gb[3][i] != 0.0 || nu.gb[5][i] != 0.0)) bad = true;
+    if (bad) atomicOr(P.err, 1);
+  }
+  const double nlb = (hb2 && P.one_loop) ? 1.0 : 0.0;
   double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   int* nj = P.node_j + (size_t)pt * P.node_stride;
   const double A = 0.5 * (amax - amin), Bc = 0.5 * (amax + amin);
@@ -276,33 +322,63 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
     node[(size_t)NF_DYZ * P.node_stride + off + p] = dyz;
     nj[off + p] = jz;
     const double pre = 1.5 * om * fK / a;
+    const double D2 = D * D;
     if (set == 0) {
       double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
       for (int s = 0; s < P.ns; s++) {
         const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
         const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
-        w[s * P.n_ss + p] = WK - WS * ia_a1(P, nu, om, a, D, s);
+        const double C1 = ia_a1(P, nu, om, a, D, s);
+        w[s * P.n_ss + p] = WK - WS * C1;
+        if (P.tatt) {
+          const size_t o = ((size_t)pt * P.ns + s) * P.n_ss + p;
+          P.wss_b[o] = WS * C1 * ia_bta(P, nu, s) * D2;
+          P.wss_2[o] = WS * ia_a2(P, nu, om, a, D, s) * D2;
+        }
       }
     } else if (set <= P.nl) {
       const double WGAL = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       const double bmag = nu.gb[4][q];
       const double WMAG = (bmag != 0.0) ? pre * g_lookup(glens + q * P.n_a, P.n_a, amin_lensg, a, false) : 0.0;
       const size_t b0 = (size_t)pt * P.nl + q;
-      P.wgs_l[b0 * P.n_ss + p] = WGAL * gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      const double b1 = gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      P.wgs_l[b0 * P.n_ss + p] = WGAL * b1;
       P.wgs_m[b0 * P.n_ss + p] = WMAG * bmag;
+      if (P.one_loop) {
+        P.wgs_1l[(b0 * 2 + 0) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gb2_d(P, nu, q, b1);
+        P.wgs_1l[(b0 * 2 + 1) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gbs2_d(P, nu, q, b1);
+      }
       double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
       for (int s = 0; s < P.ns; s++) {
         const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
         const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
-        wx[s * P.n_ss + p] = WK - WS * ia_a1(P, nu, om, a, D, s);
+        const double C1 = ia_a1(P, nu, om, a, D, s);
+        wx[s * P.n_ss + p] = WK - WS * C1;
+        const size_t o = (b0 * P.ns + s) * P.n_ss + p;
+        if (P.tatt || P.one_loop) P.wgs_k[o] = WK;
+        if (P.tatt) {
+          P.wgs_b[o] = WS * C1 * ia_bta(P, nu, s) * D2;
+          P.wgs_2[o] = WS * ia_a2(P, nu, om, a, D, s) * D2;
+        }
       }
     } else {
       const double WGAL = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       const double bmag = nu.gb[4][q];
       const double WMAG = (bmag != 0.0) ? pre * g_lookup(glens + q * P.n_a, P.n_a, amin_lensg, a, false) : 0.0;
       const size_t b0 = (size_t)pt * P.nl + q;
-      P.wgg_l[b0 * P.n_gg + p] = WGAL * gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      const double b1 = gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+      P.wgg_l[b0 * P.n_gg + p] = WGAL * b1;
       P.wgg_m[b0 * P.n_gg + p] = WMAG * bmag;
+      if (P.one_loop) {
+        const double b2 = gb2_d(P, nu, q, b1), bs2 = gbs2_d(P, nu, q, b1);
+        const double c = nlb * WGAL * WGAL * D2 * D2;
+        double* o = P.wgg_1l + b0 * 5 * P.n_gg + p;
+        o[0 * P.n_gg] = c * b1 * b2;
+        o[1 * P.n_gg] = c * 0.25 * b2 * b2;
+        o[2 * P.n_gg] = c * b1 * bs2;
+        o[3 * P.n_gg] = c * 0.5 * b2 * bs2;
+        o[4 * P.n_gg] = c * 0.25 * bs2 * bs2;
+      }
       // RSD term at a0 = a_chi(chi_0), chi_0 = (l+1/2)/k = fK
       // (cosmo2D.c:2540-2547, radial_weights.c:87-105)
       const double a0 = a_chi_d(P.chi_z, X, P.chi_nz, fK);

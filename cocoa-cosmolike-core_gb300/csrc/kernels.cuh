@@ -21,6 +21,14 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 // both power spectra.  ell_ss / ell_g: node multipoles (device).
 void launch_limber(const Params& P, const double* ell_ss, const double* ell_g,
                    cudaStream_t s, int* launches, const Hook& hk);
+// TATT / one-loop extras (k_extra.cu): p_lin on the FAST-PT grid, the
+// integrand rows from the FAST-PT outputs, the extra Limber terms
+int extra_smem_setup();
+void launch_fpt_plin(const Params& P, cudaStream_t s, int* launches);
+void launch_fpt_tables(const Params& P, const double* bias, const double* ia, cudaStream_t s,
+                       int* launches);
+void launch_extra(const Params& P, const double* ell_ss, const double* ell_g, cudaStream_t s,
+                  int* launches, const Hook& hk);
 // xi+-, gamma_t, w on the theta bins: obs[pt][n_total]
 void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
                      const double* filt_gg, const double* filt_gg_nl, double* scratch,

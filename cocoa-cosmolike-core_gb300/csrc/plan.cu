@@ -320,7 +320,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     return CL2PT_ERR_ARG;
   if (precision != CL2PT_PREC_MIXED && precision != CL2PT_PREC_FP64) return CL2PT_ERR_ARG;
   if (cfg->ia_mode == CL2PT_IA_NLA_LF) return CL2PT_ERR_UNSUPPORTED;
-  if (cfg->ia_model == CL2PT_IA_TATT) return CL2PT_ERR_UNSUPPORTED;
+  // b3 from b1 would need the reference's tabulated P_d1p3
+  if (cfg->one_loop_bias && cfg->bias_model[3] != 0) return CL2PT_ERR_UNSUPPORTED;
   if (cfg->bias_model[4] != 0 || cfg->bias_model[5] != 0) return CL2PT_ERR_ARG;
   if (grid->chi_nz < 5 || grid->G_nz < 2 || grid->pk_nk < 2 || grid->pk_nz < 2)
     return CL2PT_ERR_ARG;
@@ -438,6 +439,18 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     for (int i = 0; i < nt; i++) th.emplace_back(work, i);
     for (auto& t : th) t.join();
   }
+  if (cfg->ia_model == CL2PT_IA_TATT) {
+    // xi+ = G+ (EE + BB), xi- = G- (EE - BB): one contraction over [EE; BB]
+    const int K = p->nnode_ss;
+    std::vector<double> fx2((size_t)2 * nt * 2 * K);
+    for (int r = 0; r < 2 * nt; r++)
+      for (int k = 0; k < K; k++) {
+        const double v = fxi[(size_t)r * K + k];
+        fx2[(size_t)r * 2 * K + k] = v;
+        fx2[(size_t)r * 2 * K + K + k] = (r < nt) ? v : -v;
+      }
+    fxi.swap(fx2);
+  }
   // shared axes
   p->chi_z.assign(grid->chi_z, grid->chi_z + grid->chi_nz);
   p->G_z.assign(grid->G_z, grid->G_z + grid->G_nz);
@@ -544,6 +557,46 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
   TRY(dalloc(p, &p->d_err, 4));
   P.err = p->d_err;
+  // TATT intrinsic alignments and one-loop galaxy bias: FAST-PT tables per
+  // point on the reference's grid (k in [0.05, 1e6] c/H0 units, 1100
+  // points; pt_cfastpt.c:53-60, 235-240) and the extra node weights
+  P.tatt = cfg->ia_model == CL2PT_IA_TATT;
+  P.one_loop = cfg->one_loop_bias != 0;
+  if (P.tatt || P.one_loop) {
+    if (cl2pt::extra_smem_setup()) {
+      fprintf(stderr, "cl2pt: shared-memory limit of the TATT / one-loop kernels could not be set\n");
+      TRY(CL2PT_ERR_CUDA);
+    }
+    const int nf = 1100;
+    P.fpt_n = nf;
+    P.fpt_lim0 = log(0.05);
+    P.fpt_lim1 = log(1.0e+6);
+    P.fpt_lim2 = (P.fpt_lim1 - P.fpt_lim0) / nf;
+    std::vector<double> kx(nf);
+    for (int i = 0; i < nf; i++) kx[i] = exp(P.fpt_lim0 + i * P.fpt_lim2);
+    const cl2pt_fastpt_config fc = {-2.0, 0.65, 1500, 500, 500};
+    TRY(dalloc(p, &P.fpt_plin, (size_t)W * nf));
+    TRY(dalloc(p, &P.wgs_k, (size_t)W * nl * ns * p->n_ss));
+    if (P.one_loop) {
+      int a[13], bt[13], l[13];
+      cl2pt_fastpt_bias_terms(a, bt, l, nullptr, nullptr);
+      TRY(cl2pt_fastpt_plan_create(kx.data(), nf, a, bt, l, 13, &fc, W, &p->fpt_bias));
+      TRY(dalloc(p, &p->d_fpt_bias_out, (size_t)W * 5 * nf));
+      TRY(dalloc(p, &P.fpt_b, (size_t)W * 5 * nf));
+      TRY(dalloc(p, &P.wgs_1l, (size_t)W * nl * 2 * p->n_ss));
+      TRY(dalloc(p, &P.wgg_1l, (size_t)W * nl * 5 * p->n_gg));
+    }
+    if (P.tatt) {
+      TRY(cl2pt_fastpt_ia_plan_create(kx.data(), nf, &fc, W, &p->fpt_ia));
+      TRY(dalloc(p, &p->d_fpt_ia_out, (size_t)W * 10 * nf));
+      TRY(dalloc(p, &P.fpt_ia, (size_t)W * 8 * nf));
+      TRY(dalloc(p, &P.wss_b, (size_t)W * ns * p->n_ss));
+      TRY(dalloc(p, &P.wss_2, (size_t)W * ns * p->n_ss));
+      TRY(dalloc(p, &P.wgs_b, (size_t)W * nl * ns * p->n_ss));
+      TRY(dalloc(p, &P.wgs_2, (size_t)W * nl * ns * p->n_ss));
+      TRY(dalloc(p, &P.tab_ss_bb, (size_t)W * p->pss * p->nnode_ss));
+    }
+  }
   // staging for host batches
   const size_t B = (size_t)max_batch;
   TRY(dalloc(p, &p->d_in_om, B));
@@ -623,6 +676,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
 extern "C" int cl2pt_plan_destroy(cl2pt_plan* p)
 {
   if (!p) return CL2PT_OK;
+  cl2pt_fastpt_plan_destroy(p->fpt_bias);
+  cl2pt_fastpt_plan_destroy(p->fpt_ia);
   for (void* d : p->dbufs) cudaFree(d);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   delete p;
@@ -778,6 +833,22 @@ int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mas
     P.nu = nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
     cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+    if (P.tatt || P.one_loop) {
+      cl2pt::launch_fpt_plin(P, s, &launches);
+      if (P.one_loop) {
+        const int st2 = cl2pt_fastpt_bias(p->fpt_bias, P.fpt_plin, P.B, p->d_fpt_bias_out,
+                                          CL2PT_DEVICE, s);
+        if (st2) return st2;
+        launches += 3;
+      }
+      if (P.tatt) {
+        const int st2 = cl2pt_fastpt_ia(p->fpt_ia, P.fpt_plin, P.B, p->d_fpt_ia_out, CL2PT_DEVICE, s);
+        if (st2) return st2;
+        launches += 5;
+      }
+      cl2pt::launch_fpt_tables(P, p->d_fpt_bias_out, p->d_fpt_ia_out, s, &launches);
+      cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+    }
     if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg)
       cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
     cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
@@ -850,6 +921,17 @@ extern "C" int cl2pt_debug_nonlimber(const cl2pt_plan* p, int point, double* cl,
                              cudaMemcpyDeviceToHost));
   if (conv_l) CUDA_OK(cudaMemcpy(conv_l, P.conv_l + (size_t)point * nl, sizeof(int) * nl,
                                  cudaMemcpyDeviceToHost));
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_debug_limber_bb(const cl2pt_plan* p, int point, double* bb)
+{
+  if (!p || point < 0 || point >= std::min(p->wave, p->last_batch)) return CL2PT_ERR_ARG;
+  const Params& P = p->P;
+  if (!P.tab_ss_bb) return CL2PT_ERR_STATE;
+  CUDA_OK(cudaDeviceSynchronize());
+  CUDA_OK(cudaMemcpy(bb, P.tab_ss_bb + (size_t)point * p->pss * p->nnode_ss,
+                     sizeof(double) * p->pss * p->nnode_ss, cudaMemcpyDeviceToHost));
   return CL2PT_OK;
 }
 

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "cl2pt.h"
+#include "cl2pt_fastpt.h"
 #include "common.cuh"
 #include "nonlimber.h"
 
@@ -60,6 +61,12 @@ struct cl2pt_plan {
   int node_stride = 0;
   int* d_err = nullptr;
   int last_launches = 0;
+  // TATT / one-loop bias: FAST-PT sub-plans on the reference's k grid and
+  // their per-wave outputs
+  cl2pt_fastpt_plan* fpt_bias = nullptr;
+  cl2pt_fastpt_plan* fpt_ia = nullptr;
+  double* d_fpt_bias_out = nullptr;  // [wave][5][fpt_n]
+  double* d_fpt_ia_out = nullptr;    // [wave][10][fpt_n]
   // stage timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;

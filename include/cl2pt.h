@@ -111,6 +111,9 @@ int cl2pt_debug_nonlimber(const cl2pt_plan* plan, int point, double* cl,
                           int* conv_l);
 /* Lens-efficiency tables g(a) [n_source][n_a] of point `point`. */
 int cl2pt_debug_g_tables(const cl2pt_plan* plan, int point, double* gsrc);
+/* C_ss BB on the C_l nodes [pss][lmin_tab - 1 + n_ell] (TATT plans; the BB
+ * half of the reference's C_ss_tomo_limber table, cosmo2D.c:1617-1778). */
+int cl2pt_debug_limber_bb(const cl2pt_plan* plan, int point, double* bb);
 
 /* Per-kernel device timing.  When enabled, every eval call records CUDA
  * events around each kernel launch on its stream; cl2pt_kernel_times

@@ -68,6 +68,9 @@ typedef struct cl2pt_config {
   int probes;               /* CL2PT_PROBE_* bits */
   int n_ggl_exclude;        /* tomo.N_ggl_exclude */
   int ggl_exclude[2 * CL2PT_MAX_BINS * CL2PT_MAX_BINS]; /* (lens, source) pairs */
+  int one_loop_bias;        /* 1: points may carry b2 != 0 (the reference then adds
+                               the one-loop galaxy-bias terms from get_FPT_bias);
+                               0: a point with b2 != 0 raises the device error flag */
 } cl2pt_config;
 
 /* Cosmology tables of one parameter point (set_distances, set_growth,

@@ -582,11 +582,19 @@ void orc_ia_direct_kernel(int which, long N0, double dL, double* f)
   f[N0 - 1] = (which == 0) ? 96. : -1. / 42.;
 }
 
+/* Transform length of the two direct convolutions: 0 = the reference's
+ * N1 + N2 - 1; a larger value zero-pads further.  Exists to measure the
+ * FP64 conditioning of those terms (any length >= N1 + N2 - 1 gives the
+ * same linear convolution in exact arithmetic). */
+static long g_direct_n = 0;
+void orc_set_direct_conv_size(long n) { g_direct_n = n; }
+
 /* fftconvolve_real: utils_complex_cfastpt.c:235-318 -- linear convolution
  * of in1 [N1] and in2 [N2] into out [N1 + N2 - 1] */
 static void fftconvolve_real(const double* in1, const double* in2, long N1, long N2, double* out)
 {
-  const long n = N1 + N2 - 1;
+  long n = N1 + N2 - 1;
+  if (g_direct_n > n) n = g_direct_n;
   double* a = calloc(n, sizeof(double));
   double* b = calloc(n, sizeof(double));
   double complex* a1 = malloc(sizeof(double complex) * (n / 2 + 1));
@@ -596,8 +604,8 @@ static void fftconvolve_real(const double* in1, const double* in2, long N1, long
   num_fft_r2c(n, a, a1);
   num_fft_r2c(n, b, b1);
   for (long i = 0; i <= n / 2; i++) a1[i] *= b1[i];
-  num_fft_c2r(n, a1, out);
-  for (long i = 0; i < n; i++) out[i] *= 1.0 / (double)n;
+  num_fft_c2r(n, a1, a);  /* a has n entries; out only the N1 + N2 - 1 of the convolution */
+  for (long i = 0; i < N1 + N2 - 1; i++) out[i] = a[i] * (1.0 / (double)n);
   free(a); free(b); free(a1); free(b1);
 }
 

@@ -89,6 +89,9 @@ int orc_J_table(int nin, const int (*terms)[5], const double* cA, int out_cap,
                 int (*out)[5], double* cout);
 /* all TATT J-rows: start[9] group offsets, tab_row[8] FPTIA rows */
 int orc_ia_jrows(int cap, int (*rows)[5], double* coeff, int* start, int* tab_row);
+/* transform length of the delta-E2 / mix-B direct convolutions (0: the
+ * reference's 3 N0 - 2); for measuring their FP64 conditioning */
+void orc_set_direct_conv_size(long n);
 /* delta-E2 (which = 0) / mix-B (which = 1) direct kernel f[2 N0 - 1] */
 void orc_ia_direct_kernel(int which, long N0, double dL, double* f);
 

@@ -185,6 +185,11 @@ class Oracle:
         f(_p(out), C.byref(n))
         return out.reshape(8, n.value)
 
+    def set_direct_conv_size(self, n):
+        """Transform length of the TATT direct convolutions (0: the reference's)."""
+        self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]
+        self.lib.orc_set_direct_conv_size(int(n))
+
     def fpt_ia(self):
         n = C.c_int(0)
         f = getattr(self.lib, self.which + "_fpt_ia")

@@ -27,6 +27,19 @@ def rel_err(got, ref, floor=FLOOR):
 
 PAIR_FLOOR = 1e-4
 
+# TATT: the delta-E2 and mix-B tables come from direct FP64 convolutions
+# whose high-k values are rounding-limited in the reference itself
+# (pt_cfastpt.c:681-866): zero-padding that convolution from the
+# reference's 3298 to 3360 points, which changes nothing in exact
+# arithmetic, moves the reference algorithm's own xi- by up to ~2e-4 and its
+# high-l C_ss EE by ~2e-3 (the size depends on the platform's libm too).
+# With TATT on, an entry passes when
+# |gpu - oracle| <= 1e-4 * max(|oracle|, floor) + ENV_K * max |oracle' - oracle|,
+# oracle' running over the oracle with three such paddings; everything
+# else keeps the plain 1e-4 bar.
+DIRECT_ALT = (3360, 3375, 3430)  # 7-smooth lengths above 3298
+ENV_K = 4.0
+
 
 def rel_err_spectra(got, ref, ntheta, floor=PAIR_FLOOR):
     """Max relative error over spectra of ntheta entries each, with the
@@ -36,6 +49,24 @@ def rel_err_spectra(got, ref, ntheta, floor=PAIR_FLOOR):
     peak = np.max(np.abs(r), axis=1, keepdims=True)
     den = np.maximum(np.abs(r), floor * peak + 1e-300)
     return float(np.max(np.abs(g - r) / den))
+
+
+def rel_err_env(got, ref, alt, floor=FLOOR, ntheta=None):
+    """rel_err / rel_err_spectra with the TATT envelope described above
+    (alt None: plain)."""
+    g = np.asarray(got, dtype=np.float64)
+    r = np.asarray(ref, dtype=np.float64)
+    if ntheta is not None:
+        g, r = g.reshape(-1, ntheta), r.reshape(-1, ntheta)
+        peak = np.max(np.abs(r), axis=1, keepdims=True)
+    else:
+        peak = np.max(np.abs(r)) if r.size else 0.0
+    den = np.maximum(np.abs(r), floor * peak + 1e-300)
+    if alt is not None:
+        alts = alt if isinstance(alt, (list, tuple)) else [alt]
+        dev = np.max([np.abs(np.asarray(a, dtype=np.float64).reshape(r.shape) - r) for a in alts], axis=0)
+        den = den + ENV_K * dev / REL
+    return float(np.max(np.abs(g - r) / den)) if r.size else 0.0
 
 
 def blocks(plan, dv):
@@ -56,18 +87,38 @@ def run_case(name, npts, prec, seed=1, check_tables=True):
     o.setup(w.cfg, w.src, w.lens)
     worst = {}
     nint = w.cfg.lmin_tab - 1
+    tatt = w.cfg.ia_model == abi.IA_TATT
     for i in range(npts):
+        alt = alt_t = None
+        if tatt:
+            alt, alt_t = [], []
+            for n_alt in DIRECT_ALT:
+                o.set_direct_conv_size(n_alt)
+                o.set_point(tabs[i], nus[i])
+                alt.append(o.data_vector_real())
+                alt_t.append([t.copy() for t in o.limber_tables()])
+            o.set_direct_conv_size(0)
         o.set_point(tabs[i], nus[i])
         ref = o.data_vector_real()
         for k, v in blocks(plan, dv[i]).items():
             worst[k] = max(worst.get(k, 0.0),
-                           rel_err_spectra(v, blocks(plan, ref)[k], w.cfg.ntheta))
+                           rel_err_env(v, blocks(plan, ref)[k],
+                                       None if alt is None else [blocks(plan, a)[k] for a in alt],
+                                       floor=PAIR_FLOOR, ntheta=w.cfg.ntheta))
         if check_tables and i < 2:
             gss, ggs, ggg = plan.limber_tables(i)
             oss, ogs, ogg = o.limber_tables()
-            worst["C_ss nodes"] = max(worst.get("C_ss nodes", 0), rel_err(gss[:, nint:], oss[0]))
-            worst["C_gs nodes"] = max(worst.get("C_gs nodes", 0), rel_err(ggs[:, nint:], ogs))
-            worst["C_gg nodes"] = max(worst.get("C_gg nodes", 0), rel_err(ggg[:, nint:], ogg))
+            sel = (lambda f: None) if alt_t is None else (lambda f: [f(t) for t in alt_t])
+            worst["C_ss nodes"] = max(worst.get("C_ss nodes", 0),
+                                      rel_err_env(gss[:, nint:], oss[0], sel(lambda t: t[0][0])))
+            worst["C_gs nodes"] = max(worst.get("C_gs nodes", 0),
+                                      rel_err_env(ggs[:, nint:], ogs, sel(lambda t: t[1])))
+            worst["C_gg nodes"] = max(worst.get("C_gg nodes", 0),
+                                      rel_err_env(ggg[:, nint:], ogg, sel(lambda t: t[2])))
+            if tatt:
+                gbb = plan.limber_bb(i)
+                worst["C_ss BB nodes"] = max(worst.get("C_ss BB nodes", 0),
+                                             rel_err_env(gbb[:, nint:], oss[1], sel(lambda t: t[0][1])))
             lows = [2.0, 7.0, 19.0]
             pss = abi.shear_pairs(w.cfg.n_source)
             for l in lows:
@@ -170,3 +221,45 @@ def test_bad_inputs_rejected(gpu_lib):
         plan.eval_real(om, h0, chi, G, lnP, nus)
     with pytest.raises(lib.CL2PTError):
         plan.eval_real(np.zeros(2), h0, chi, G, lnP, nus)  # n > max_batch
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_tatt_one_loop_small(gpu_lib, oracle_built, prec):
+    """TATT intrinsic alignments (A1, A2, eta, b_TA) and one-loop galaxy bias
+    (b2, bs2) on the small geometry: data vector, C_ss EE/BB, C_gs, C_gg node
+    tables and the non-Limber C_l against the oracle."""
+    worst, _ = run_case("real_3x2pt_tatt_small", 2, prec, seed=11)
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+def test_tatt_one_loop_vs_reference_golden(gpu_lib, oracle_built):
+    """The same inputs as tests/golden/real_3x2pt_tatt_small.npz (made by the
+    reference's own sources): data vectors of two points, with the TATT
+    envelope measured on the oracle."""
+    import os
+    import oracle as O
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                "real_3x2pt_tatt_small.npz"))
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 2, seed=11)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=2)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    for i in range(2):
+        # the envelope: the oracle's own spread over the paddings and this
+        # platform (the fixture was made on another machine's libm)
+        alt = []
+        for n_alt in (0,) + DIRECT_ALT:
+            o.set_direct_conv_size(n_alt)
+            o.set_point(tabs[i], nus[i])
+            alt.append(o.data_vector_real())
+        o.set_direct_conv_size(0)
+        err = rel_err_env(dv[i], gold[f"dv_{i}"], alt, floor=PAIR_FLOOR, ntheta=w.cfg.ntheta)
+        print(i, err)
+        assert err <= REL, (i, err)
