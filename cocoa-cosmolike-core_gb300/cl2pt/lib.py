@@ -68,6 +68,9 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_eval_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]
     lib.cl2pt_check_errors.argtypes = [C.c_void_p, C.c_void_p]
+    lib.cl2pt_eval_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.cl2pt_fourier_sizes.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip]
     lib.cl2pt_debug_limber_tables.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     lib.cl2pt_debug_nonlimber.argtypes = [C.c_void_p, C.c_int, _dp, _ip]
     lib.cl2pt_debug_g_tables.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -177,6 +180,29 @@ class Plan:
                                      mk.ctypes.data if mk is not None else None,
                                      pmm.ctypes.data if pmm is not None else None,
                                      out.ctypes.data, None), "cl2pt_eval_real")
+        return out
+
+    def eval_fourier(self, omega_m, h0, chi, G, lnP, nuisance, ell, lmax_shear=1e30, mask=None,
+                     lnPL=None):
+        """Fourier 3x2pt at multipoles ell: host arrays in, [n][nell (pss + pgs + n_lens)] out."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        nt = C.c_int()
+        check(load().cl2pt_fourier_sizes(self.h, len(ell), None, None, None, C.byref(nt)))
+        out = np.zeros((n, nt.value))
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        check(load().cl2pt_eval_fourier(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                        mk.ctypes.data if mk is not None else None,
+                                        out.ctypes.data, None), "cl2pt_eval_fourier")
         return out
 
     # ------------------------------------------------------------ device

@@ -172,6 +172,55 @@ __global__ void k_assemble(Params P, const int* __restrict__ mask, const double*
   }
 }
 
+// Fourier-space 3x2pt data vector (the C_ss / C_gs / C_gg blocks of the
+// reference's Fourier Mx2pt vector, generic_interface.hpp:968-1128, with
+// C_gg_tomo_cpp's non-Limber override below LMAX_NOLIMBER,
+// cosmo2D_wrapper.cpp:314-340): entries nell * pair + i; shear entries at
+// l >= lmax_shear are 0; calibration (1+m_i)(1+m_j) and (1+m_s).
+__global__ void k_assemble_fourier(Params P, int nell, const double* __restrict__ ell, double lmax_shear,
+                                   int use_nl, const int* __restrict__ mask, double* __restrict__ dv)
+{
+  const int pt = blockIdx.y;
+  const int s1 = nell * P.pss, s2 = s1 + nell * P.pgs, n_total = s2 + nell * P.nl;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  double* d = dv + (size_t)pt * n_total;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_total; i += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    if (!mask || mask[i]) {
+      if (i < s1) {
+        const int pr = i / nell, j = i - pr * nell;
+        if ((P.probes & CL2PT_PROBE_XI) && ell[j] < lmax_shear)
+          v = P.tab_ss[((size_t)pt * P.pss + pr) * P.nnode_ss + j] * (1.0 + nu.shear_m[P.z1[pr]]) *
+              (1.0 + nu.shear_m[P.z2[pr]]);
+      } else if (i < s2) {
+        const int r = i - s1, pr = r / nell, j = r - pr * nell;
+        if (P.probes & CL2PT_PROBE_GAMMAT)
+          v = P.tab_gs[((size_t)pt * P.pgs + pr) * P.nnode_g + j] * (1.0 + nu.shear_m[P.zs[pr]]);
+      } else {
+        const int r = i - s2, q = r / nell, j = r - q * nell;
+        if (P.probes & CL2PT_PROBE_WTHETA) {
+          if (use_nl && ell[j] < P.lmax_nolimber)
+            v = P.cnl[((size_t)pt * P.nl + q) * P.lmax_nolimber + (int)(ell[j] + 1e-13)];
+          else
+            v = P.tab_gg[((size_t)pt * P.nl + q) * P.nnode_g + j];
+        }
+      }
+    }
+    d[i] = v;
+  }
+}
+
+void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,
+                             const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk)
+{
+  const int n_total = nell * (P.pss + P.pgs + P.nl);
+  dim3 g((n_total + 255) / 256, P.B);
+  hk(CL2PT_K_ASSEMBLE, 1);
+  k_assemble_fourier<<<g, 256, 0, s>>>(P, nell, ell, lmax_shear, use_nl, mask, dv);
+  hk(CL2PT_K_ASSEMBLE, 0);
+  (*launches)++;
+}
+
 void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
                      cudaStream_t s, int* launches, const Hook& hk)
 {

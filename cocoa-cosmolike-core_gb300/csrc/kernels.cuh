@@ -33,6 +33,9 @@ void launch_extra(const Params& P, const double* ell_ss, const double* ell_g, cu
 void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
                      const double* filt_gg, const double* filt_gg_nl, double* scratch,
                      cudaStream_t s, int* launches, const Hook& hk);
+// Fourier data vector dv[pt][nell (pss + pgs + nl)] from the node tables
+void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,
+                             const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk);
 // masked, calibrated data vector dv[pt][n_total] from obs
 void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
                      cudaStream_t s, int* launches, const Hook& hk);

@@ -557,6 +557,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
   TRY(dalloc(p, &p->d_err, 4));
   P.err = p->d_err;
+  TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
+  TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   // TATT intrinsic alignments and one-loop galaxy bias: FAST-PT tables per
   // point on the reference's grid (k in [0.05, 1e6] c/H0 units, 1100
   // points; pt_cfastpt.c:53-60, 235-240) and the extra node weights
@@ -736,8 +738,17 @@ static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b)
   return CL2PT_OK;
 }
 
-int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
-                             const double* pm, double* dv, cudaStream_t s);
+// Fourier mode: the Limber stages run on the caller's multipoles (the
+// direct quadrature of C_*_tomo_limber_nointerp at each l) into the node
+// tables, and the Fourier assembly replaces the Legendre contraction.
+struct FourierReq {
+  int nell = 0;
+  const double* ell = nullptr;  // host
+  double lmax_shear = 0;
+};
+
+static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                         double* dv, cudaStream_t s, const FourierReq* fr);
 
 extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
                                const double* pm, double* dv, void* stream)
@@ -745,15 +756,62 @@ extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* m
   if (!p || !dv) return CL2PT_ERR_ARG;
   int st = check_batch(p, b);
   if (st) return st;
-  return cl2pt_internal_eval_real(p, b, mask, pm, dv, (cudaStream_t)stream);
+  return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int cl2pt_fourier_sizes(const cl2pt_plan* p, int nell, int* n_ss, int* n_gs, int* n_gg,
+                                   int* n_total)
+{
+  if (!p || nell < 1) return CL2PT_ERR_ARG;
+  if (n_ss) *n_ss = nell * p->pss;
+  if (n_gs) *n_gs = nell * p->pgs;
+  if (n_gg) *n_gg = nell * p->cfg.n_lens;
+  if (n_total) *n_total = nell * (p->pss + p->pgs + p->cfg.n_lens);
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_eval_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
+                                  double lmax_shear, const int* mask, double* dv, void* stream)
+{
+  if (!p || !dv) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  FourierReq fr;
+  fr.nell = nell;
+  fr.ell = ell;
+  fr.lmax_shear = lmax_shear;
+  return internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr);
 }
 
 // Stage the batch on the device (when it lives on the host), then run the
 // pipeline wave by wave so the per-wave workspace stays L2-sized.
-int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
-                             const double* pm, double* dv, cudaStream_t s)
+static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                         double* dv, cudaStream_t s, const FourierReq* fr)
 {
   const int n = b->n;
+  const bool fourier = fr != nullptr;
+  const int n_total = fourier ? fr->nell * (p->pss + p->pgs + p->cfg.n_lens) : p->n_total;
+  double* d_dv_stage = p->d_dv;
+  int* d_mask_stage = p->d_mask;
+  if (fourier) {
+    if (fr->nell < 1 || fr->nell > std::min(p->nnode_ss, p->nnode_g) || !fr->ell) return CL2PT_ERR_ARG;
+    for (int i = 0; i < fr->nell; i++)
+      if (!(fr->ell[i] >= 1.0) || !std::isfinite(fr->ell[i])) return CL2PT_ERR_ARG;
+    CUDA_OK(cudaMemcpyAsync(p->d_ell_f, fr->ell, sizeof(double) * fr->nell, cudaMemcpyHostToDevice, s));
+    if (b->where == CL2PT_HOST && (size_t)n_total * p->max_batch > p->fourier_cap) {
+      // staging for host Fourier batches, grown on demand
+      void *d1 = nullptr, *d2 = nullptr;
+      CUDA_OK(cudaMalloc(&d1, sizeof(double) * (size_t)n_total * p->max_batch));
+      CUDA_OK(cudaMalloc(&d2, sizeof(int) * (size_t)n_total));
+      p->dbufs.push_back(d1);
+      p->dbufs.push_back(d2);
+      p->d_dv_f = (double*)d1;
+      p->d_mask_f = (int*)d2;
+      p->fourier_cap = (size_t)n_total * p->max_batch;
+    }
+    d_dv_stage = p->d_dv_f;
+    d_mask_stage = p->d_mask_f;
+  }
   const Params& T = p->P;
   const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz,
                nPL = (size_t)T.pkl_nk * T.pkl_nz;
@@ -775,14 +833,14 @@ int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mas
     lnPL = (b->lnPL && p->d_in_lnPL) ? p->d_in_lnPL : p->d_in_lnP;
     nu = p->d_in_nu;
     if (mask) {
-      CUDA_OK(cudaMemcpyAsync(p->d_mask, mask, p->n_total * sizeof(int), cudaMemcpyHostToDevice, s));
-      dmask = p->d_mask;
+      CUDA_OK(cudaMemcpyAsync(d_mask_stage, mask, n_total * sizeof(int), cudaMemcpyHostToDevice, s));
+      dmask = d_mask_stage;
     }
     if (pm) {
       CUDA_OK(cudaMemcpyAsync(p->d_pm, pm, (size_t)n * p->cfg.n_lens * sizeof(double), cudaMemcpyHostToDevice, s));
       dpm = p->d_pm;
     }
-    ddv = p->d_dv;
+    ddv = d_dv_stage;
   } else {
     om = b->omega_m; h0 = b->h0; chi = b->chi; G = b->G; lnP = b->lnP;
     lnPL = b->lnPL ? b->lnPL : b->lnP;
@@ -832,7 +890,6 @@ int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mas
     P.lnPL = lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
     P.nu = nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
-    cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
     if (P.tatt || P.one_loop) {
       cl2pt::launch_fpt_plin(P, s, &launches);
       if (P.one_loop) {
@@ -847,20 +904,49 @@ int cl2pt_internal_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mas
         launches += 5;
       }
       cl2pt::launch_fpt_tables(P, p->d_fpt_bias_out, p->d_fpt_ia_out, s, &launches);
-      cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
     }
-    if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg)
-      cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
-    cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
-                           s, &launches, hk);
-    cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
-                           ddv + (size_t)w0 * p->n_total, s, &launches, hk);
+    if (fourier) {
+      // Limber at the caller's multipoles: shear and ggl into the node
+      // tables (stride nell), clustering into its own table, since the
+      // FFTLog hand-over below reads the clustering table on the log nodes
+      Params Pf = P;
+      Pf.nnode_ss = Pf.nnode_g = fr->nell;
+      Pf.tab_gg = p->d_tab_gg_f;
+      Pf.adopt_limber_gg = 1;  // no integer-l spectra in this pass
+      cl2pt::launch_limber(Pf, p->d_ell_f, p->d_ell_f, s, &launches, hk);
+      if (P.tatt || P.one_loop) cl2pt::launch_extra(Pf, p->d_ell_f, p->d_ell_f, s, &launches, hk);
+      // the FFTLog C_l is only read below LMAX_NOLIMBER (cosmo2D_wrapper.cpp:323-336)
+      bool use_nl = (P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg;
+      if (use_nl) {
+        bool any = false;
+        for (int i = 0; i < fr->nell; i++) any |= fr->ell[i] < P.lmax_nolimber;
+        use_nl = any;
+      }
+      if (use_nl) {
+        Params Pg = P;
+        Pg.probes = CL2PT_PROBE_WTHETA;
+        cl2pt::launch_limber(Pg, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+        if (P.one_loop) cl2pt::launch_extra(Pg, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+        cl2pt::launch_nonlimber(Pg, p->nlq, s, &launches, hk);
+      }
+      cl2pt::launch_assemble_fourier(Pf, fr->nell, p->d_ell_f, fr->lmax_shear, use_nl ? 1 : 0, dmask,
+                                     ddv + (size_t)w0 * n_total, s, &launches, hk);
+    } else {
+      cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+      if (P.tatt || P.one_loop) cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+      if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg)
+        cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
+      cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
+                             s, &launches, hk);
+      cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
+                             ddv + (size_t)w0 * p->n_total, s, &launches, hk);
+    }
   }
   CUDA_OK(cudaGetLastError());
   p->last_launches = launches;
   p->last_batch = n;
   if (b->where == CL2PT_HOST) {
-    CUDA_OK(cudaMemcpyAsync(dv, p->d_dv, (size_t)n * p->n_total * sizeof(double),
+    CUDA_OK(cudaMemcpyAsync(dv, d_dv_stage, (size_t)n * n_total * sizeof(double),
                             cudaMemcpyDeviceToHost, s));
     int err = 0;
     CUDA_OK(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));

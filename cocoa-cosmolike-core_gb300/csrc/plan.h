@@ -61,6 +61,12 @@ struct cl2pt_plan {
   int node_stride = 0;
   int* d_err = nullptr;
   int last_launches = 0;
+  // Fourier path: the caller's multipoles, and staging for host batches
+  double* d_ell_f = nullptr;        // [max(nnode_ss, nnode_g)]
+  double* d_tab_gg_f = nullptr;     // [wave][n_lens][max(nnode_ss, nnode_g)] C_gg at those l
+  double* d_dv_f = nullptr;
+  int* d_mask_f = nullptr;
+  size_t fourier_cap = 0;
   // TATT / one-loop bias: FAST-PT sub-plans on the reference's k grid and
   // their per-wave outputs
   cl2pt_fastpt_plan* fpt_bias = nullptr;

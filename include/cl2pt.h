@@ -93,6 +93,21 @@ int cl2pt_eval_real(cl2pt_plan* plan, const cl2pt_batch* batch,
                     const int* mask, const double* pm, double* dv,
                     void* stream);
 
+/* Fourier-space 3x2pt at the caller's multipoles ell[0..nell-1] (the
+ * reference's Fourier Mx2pt vector, generic_interface.hpp:968-1128, from
+ * C_ss/C_gs_tomo_limber_nointerp and C_gg_tomo_cpp, cosmo2D_wrapper.cpp:
+ * 280-340): dv [n][nell (pss + pgs + n_lens)] with entries nell * pair + i,
+ * shear pairs first, then ggl pairs, then clustering (auto) bins.  C_gg
+ * below lmax_nolimber comes from the non-Limber FFTLog C_l at int(l) unless
+ * adopt_limber_gg; shear entries at l >= lmax_shear are 0.  mask (length
+ * n_total, or NULL) and dv follow batch->where.  nell <= the plan's node
+ * count (lmin_tab - 1 + n_ell). */
+int cl2pt_eval_fourier(cl2pt_plan* plan, const cl2pt_batch* batch, int nell,
+                       const double* ell, double lmax_shear, const int* mask,
+                       double* dv, void* stream);
+int cl2pt_fourier_sizes(const cl2pt_plan* plan, int nell, int* n_ss, int* n_gs,
+                        int* n_gg, int* n_total);
+
 /* Wait for the stream and report any device-side check that failed since
  * the last call (a device-resident batch does not synchronise). */
 int cl2pt_check_errors(cl2pt_plan* plan, void* stream);
