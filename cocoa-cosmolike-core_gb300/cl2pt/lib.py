@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libcl2pt.so")
 PREC_MIXED, PREC_FP64 = 0, 1
 # kernel ids of cl2pt_kernel_times (CL2PT_K_* in include/cl2pt.h)
 KERNELS = ["k_gtab", "k_nodes", "k_limber_ss", "k_limber_gs", "k_limber_gg", "k_limber_ggl",
-           "k_nonlimber", "k_contract", "k_assemble"]
+           "k_nonlimber", "k_contract", "k_assemble", "k_vjp"]
 HOST, DEVICE = 0, 1
 
 _dp = C.POINTER(C.c_double)
@@ -68,6 +68,8 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_eval_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]
     lib.cl2pt_check_errors.argtypes = [C.c_void_p, C.c_void_p]
+    lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_eval_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
                                        C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_fourier_sizes.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip]
@@ -204,6 +206,52 @@ class Plan:
                                         mk.ctypes.data if mk is not None else None,
                                         out.ctypes.data, None), "cl2pt_eval_fourier")
         return out
+
+    def vjp_real(self, omega_m, h0, chi, G, lnP, nuisance, cot, mask=None, pm=None, lnPL=None):
+        """Value and vector-Jacobian product on host arrays: returns
+        (dv [n][n_total], lnP_bar [n][nk*nz], nu_bar [n][13*MAX_BINS] in the
+        flat cl2pt_nuisance layout)."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        cv = np.ascontiguousarray(np.broadcast_to(cot, (n, self.n_total)), dtype=np.float64)
+        dv = np.zeros((n, self.n_total))
+        lbar = np.zeros((n, arrs[3].size // n))
+        nbar = (abi.Nuisance * n)()
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
+        check(load().cl2pt_vjp_real(self.h, C.byref(b),
+                                    mk.ctypes.data if mk is not None else None,
+                                    pmm.ctypes.data if pmm is not None else None,
+                                    cv.ctypes.data, dv.ctypes.data, lbar.ctypes.data,
+                                    C.addressof(nbar), None), "cl2pt_vjp_real")
+        nb = np.frombuffer(bytes(nbar), dtype=np.float64).reshape(n, -1).copy()
+        return dv, lbar, nb
+
+    def vjp_real_device(self, omega_m, h0, chi, G, lnP, nuisance, cot, dv, lnP_bar, nu_bar,
+                        mask=None, pm=None, lnPL=None, stream=None):
+        """Device form of vjp_real: float64 CUDA tensors; nuisance and nu_bar
+        hold n packed cl2pt_nuisance structs (any dtype, contiguous); dv may
+        be None."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        st = load().cl2pt_vjp_real(self.h, C.byref(b),
+                                   None if mask is None else mask.data_ptr(),
+                                   None if pm is None else pm.data_ptr(),
+                                   cot.data_ptr(), None if dv is None else dv.data_ptr(),
+                                   lnP_bar.data_ptr(), nu_bar.data_ptr(), stream)
+        check(st, "cl2pt_vjp_real")
 
     # ------------------------------------------------------------ device
     def eval_real_device(self, omega_m, h0, chi, G, lnP, nuisance, out, mask=None, pm=None,

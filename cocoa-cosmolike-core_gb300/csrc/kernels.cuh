@@ -40,4 +40,27 @@ void launch_assemble_fourier(const Params& P, int nell, const double* ell, doubl
 void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
                      cudaStream_t s, int* launches, const Hook& hk);
 
+// Adjoint of the real-space data vector (k_vjp.cu).  Device pointers of one
+// wave; the accumulated outputs (lnp_bar, nu_bar, wbar_*) are zeroed by the
+// caller.
+struct VJPParams {
+  const double* cot;       // [B][n_total] cotangent of dv
+  const double* dv;        // [B][n_total] forward data vector
+  const int* mask;         // [n_total] or null
+  double* obs_bar;         // [B][n_total]
+  double* cbar_ss;         // [B][pss][nnode_ss]
+  double* cbar_gs;         // [B][pgs][nnode_g]
+  double* cbar_gg;         // [B][nl][nnode_g]
+  double* lnp_bar;         // [B][pk_nk * pk_nz]
+  double* wbar_ss;         // [B][ns][n_ss]
+  double* wbar_gx;         // [B][nl][ns][n_ss]
+  double* lbar_gs;         // [B][nl][2][n_ss]
+  double* lbar_gg;         // [B][nl][n_gg]
+  cl2pt_nuisance* nu_bar;  // [B]
+};
+size_t vjp_ss_smem(const Params& P);
+void launch_vjp(const Params& P, const VJPParams& V, const double* filt_xi, const double* filt_gt,
+                const double* filt_gg, const double* ell_ss, const double* ell_g, cudaStream_t s,
+                int* launches, const Hook& hk);
+
 }  // namespace cl2pt

@@ -747,8 +747,16 @@ struct FourierReq {
   double lmax_shear = 0;
 };
 
+// Adjoint request: cotangent in, table and nuisance gradients out (all
+// per batch->where).
+struct VJPReq {
+  const double* cot = nullptr;
+  double* lnp_bar = nullptr;
+  cl2pt_nuisance* nu_bar = nullptr;
+};
+
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                         double* dv, cudaStream_t s, const FourierReq* fr);
+                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr = nullptr);
 
 extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
                                const double* pm, double* dv, void* stream)
@@ -783,10 +791,45 @@ extern "C" int cl2pt_eval_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell,
   return internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr);
 }
 
+extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                              const double* cot, double* dv, double* lnP_bar, cl2pt_nuisance* nu_bar,
+                              void* stream)
+{
+  if (!p || !cot || !lnP_bar || !nu_bar) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  const cl2pt_config& c = p->cfg;
+  if (c.ia_model != CL2PT_IA_NLA || c.bias_model[0] != 0 || c.linear_pk || c.one_loop_bias ||
+      ((c.probes & CL2PT_PROBE_WTHETA) && !c.adopt_limber_gg))
+    return CL2PT_ERR_UNSUPPORTED;
+  if (cl2pt::vjp_ss_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
+  if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
+  if (!p->d_vjp_ws) {
+    const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
+    const size_t nws = W * p->n_total + W * p->pss * p->nnode_ss + W * p->pgs * p->nnode_g +
+                       W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
+                       W * nl * p->n_gg;
+    // (a failed allocation leaves the plan usable for evaluation)
+    int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
+    if (!a) a = dalloc(p, &p->d_vjp_lnp, (size_t)p->max_batch * p->P.pk_nk * p->P.pk_nz);
+    if (!a) a = dalloc(p, &p->d_vjp_nu, (size_t)p->max_batch);
+    if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
+    if (a) {
+      p->d_vjp_ws = nullptr;
+      return a;
+    }
+  }
+  VJPReq vr;
+  vr.cot = cot;
+  vr.lnp_bar = lnP_bar;
+  vr.nu_bar = nu_bar;
+  return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+}
+
 // Stage the batch on the device (when it lives on the host), then run the
 // pipeline wave by wave so the per-wave workspace stays L2-sized.
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                         double* dv, cudaStream_t s, const FourierReq* fr)
+                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr)
 {
   const int n = b->n;
   const bool fourier = fr != nullptr;
@@ -850,6 +893,37 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     ddv = dv;
   }
   if (!b->lnPL && (T.pkl_nk != T.pk_nk || T.pkl_nz != T.pk_nz)) return CL2PT_ERR_ARG;
+  // adjoint: device views of the cotangent and the gradients, workspace
+  const double* vcot = nullptr;
+  double* vlnp = nullptr;
+  cl2pt_nuisance* vnu = nullptr;
+  cl2pt::VJPParams V0{};
+  if (vr) {
+    if (b->where == CL2PT_HOST) {
+      CUDA_OK(cudaMemcpyAsync(p->d_vjp_cot, vr->cot, (size_t)n * n_total * sizeof(double),
+                              cudaMemcpyHostToDevice, s));
+      vcot = p->d_vjp_cot;
+      vlnp = p->d_vjp_lnp;
+      vnu = p->d_vjp_nu;
+    } else {
+      vcot = vr->cot;
+      vlnp = vr->lnp_bar;
+      vnu = vr->nu_bar;
+    }
+    CUDA_OK(cudaMemsetAsync(vlnp, 0, (size_t)n * nP * sizeof(double), s));
+    CUDA_OK(cudaMemsetAsync(vnu, 0, (size_t)n * sizeof(cl2pt_nuisance), s));
+    const int W = p->wave, ns = p->cfg.n_source, nl = p->cfg.n_lens;
+    double* w = p->d_vjp_ws;
+    V0.obs_bar = w; w += (size_t)W * n_total;
+    V0.cbar_ss = w; w += (size_t)W * p->pss * p->nnode_ss;
+    V0.cbar_gs = w; w += (size_t)W * p->pgs * p->nnode_g;
+    V0.cbar_gg = w; w += (size_t)W * nl * p->nnode_g;
+    V0.wbar_ss = w; w += (size_t)W * ns * p->n_ss;
+    V0.wbar_gx = w; w += (size_t)W * nl * ns * p->n_ss;
+    V0.lbar_gs = w; w += (size_t)W * nl * 2 * p->n_ss;
+    V0.lbar_gg = w;
+    V0.mask = dmask;
+  }
   int launches = 0;
   struct HookCtx { cl2pt_plan* p; cudaStream_t s; cudaEvent_t (*ev)(cl2pt_plan*); };
   cl2pt::Hook hk;
@@ -940,14 +1014,31 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                              s, &launches, hk);
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
                              ddv + (size_t)w0 * p->n_total, s, &launches, hk);
+      if (vr) {
+        const int ns = p->cfg.n_source, nl = p->cfg.n_lens;
+        CUDA_OK(cudaMemsetAsync(V0.wbar_ss, 0, sizeof(double) * (size_t)P.B * ns * p->n_ss, s));
+        CUDA_OK(cudaMemsetAsync(V0.wbar_gx, 0, sizeof(double) * (size_t)P.B * nl * ns * p->n_ss, s));
+        cl2pt::VJPParams V = V0;
+        V.cot = vcot + (size_t)w0 * n_total;
+        V.dv = ddv + (size_t)w0 * n_total;
+        V.lnp_bar = vlnp + (size_t)w0 * nP;
+        V.nu_bar = vnu + w0;
+        cl2pt::launch_vjp(P, V, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_ell_ss, p->d_ell_g, s,
+                          &launches, hk);
+      }
     }
   }
   CUDA_OK(cudaGetLastError());
   p->last_launches = launches;
   p->last_batch = n;
   if (b->where == CL2PT_HOST) {
-    CUDA_OK(cudaMemcpyAsync(dv, d_dv_stage, (size_t)n * n_total * sizeof(double),
-                            cudaMemcpyDeviceToHost, s));
+    if (dv)
+      CUDA_OK(cudaMemcpyAsync(dv, d_dv_stage, (size_t)n * n_total * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    if (vr) {
+      CUDA_OK(cudaMemcpyAsync(vr->lnp_bar, vlnp, (size_t)n * nP * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CUDA_OK(cudaMemcpyAsync(vr->nu_bar, vnu, (size_t)n * sizeof(cl2pt_nuisance), cudaMemcpyDeviceToHost, s));
+    }
     int err = 0;
     CUDA_OK(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_OK(cudaStreamSynchronize(s));

@@ -73,6 +73,12 @@ struct cl2pt_plan {
   cl2pt_fastpt_plan* fpt_ia = nullptr;
   double* d_fpt_bias_out = nullptr;  // [wave][5][fpt_n]
   double* d_fpt_ia_out = nullptr;    // [wave][10][fpt_n]
+  // adjoint (cl2pt_vjp_real): per-wave workspace and host staging, allocated
+  // on first use
+  double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
+  double* d_vjp_cot = nullptr;         // [max_batch][n_total]
+  double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]
+  cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;

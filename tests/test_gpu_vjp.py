@@ -1,0 +1,270 @@
+"""Adjoint of the real-space 3x2pt data vector (cl2pt_vjp_real) against
+central finite differences.
+
+For a seeded cotangent v, the scalar f = v . dv is differentiated
+  * on the GPU: central differences of the FP64 plan's forward,
+  * on the CPU: central differences of the FP64 oracle (the restatement of
+    the reference C path),
+with respect to the shear m-bias, b1, the NLA amplitude and its redshift
+power, and the P(k, z) table (a dense random direction and single entries).
+Step: 1e-4 relative (1e-4 absolute in lnP).  Every quantity here is smooth
+in the parameters (the bilinear table walk is linear in the table values;
+b1 and A1 enter polynomially), so the analytic gradient must match the
+GPU differences to GRAD_REL and the oracle differences to the data-vector
+bar of 1e-4.
+"""
+import numpy as np
+import pytest
+
+from cl2pt import abi, lib, workloads
+
+GRAD_REL = 1e-6   # analytic vs FD of the same FP64 forward
+ORACLE_REL = 1e-4  # analytic vs FD of the oracle
+H = 1e-4
+
+
+def setup_case(ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, seed=21, prec=lib.PREC_FP64, name="real_3x2pt_small_limber"):
+    w = workloads.make(name)
+    w.cfg.ia_mode = ia_mode
+    tabs, nus = workloads.points(w, npts, seed=seed)
+    rng = np.random.default_rng(seed)
+    for nu in nus:
+        if ia_mode == abi.IA_REDSHIFT_EVOLUTION:
+            nu.ia[0][0] = rng.uniform(0.3, 1.0)
+            nu.ia[0][1] = rng.uniform(-1.5, 1.5)
+        elif ia_mode == abi.IA_REDSHIFT_BINNING:
+            for s in range(w.cfg.n_source):
+                nu.ia[0][s] = rng.uniform(-1.0, 1.0)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
+    return w, tabs, nus, plan
+
+
+def nu_get(nu, field, i, j=None):
+    a = getattr(nu, field)
+    return a[i] if j is None else a[i][j]
+
+
+def nu_set(nu, field, i, j, v):
+    a = getattr(nu, field)
+    if j is None:
+        a[i] = v
+    else:
+        a[i][j] = v
+
+
+def flat_index(field, i, j=None):
+    """Index of a cl2pt_nuisance field in the flat float64 layout."""
+    off = {"src_dz": 0, "lens_dz": 1, "lens_stretch": 2, "shear_m": 3, "gb": 4, "ia": 10}[field]
+    if j is None:
+        return off * abi.MAX_BINS + i
+    return (off + i) * abi.MAX_BINS + j
+
+
+def param_list(w, ia_mode):
+    ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
+    ps += [("gb", 0, q) for q in range(w.cfg.n_lens)]
+    if ia_mode == abi.IA_REDSHIFT_EVOLUTION:
+        ps += [("ia", 0, 0), ("ia", 0, 1)]
+    elif ia_mode == abi.IA_REDSHIFT_BINNING:
+        ps += [("ia", 0, s) for s in range(w.cfg.n_source)]
+    return ps
+
+
+def clone(nu):
+    c = abi.Nuisance()
+    C = __import__("ctypes")
+    C.memmove(C.addressof(c), C.addressof(nu), C.sizeof(nu))
+    return c
+
+
+def check_nuisance_fd(plan, w, tabs, nus, v, nbar, ia_mode, point, mask=None, pm=None):
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    sl = slice(point, point + 1)
+    worst = 0.0
+    for field, i, j in param_list(w, ia_mode):
+        x0 = nu_get(nus[point], field, i, j)
+        h = H * max(abs(x0), 0.1)
+        f = []
+        for sgn in (1, -1):
+            nu = clone(nus[point])
+            nu_set(nu, field, i, j, x0 + sgn * h)
+            dv = plan.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl], [nu], mask=mask,
+                                pm=None if pm is None else pm[sl])[0]
+            f.append(float(v[point] @ dv))
+        fd = (f[0] - f[1]) / (2 * h)
+        an = nbar[point, flat_index(field, i, j)]
+        scale = max(abs(fd), 1e-12 * max(abs(f[0]), 1e-300))
+        err = abs(an - fd) / scale
+        worst = max(worst, err)
+        assert err <= GRAD_REL, (field, i, j, an, fd, err)
+    return worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ia_mode", [abi.IA_REDSHIFT_EVOLUTION, abi.IA_REDSHIFT_BINNING, abi.NO_IA])
+def test_vjp_nuisance_vs_gpu_fd(gpu_lib, ia_mode):
+    w, tabs, nus, plan = setup_case(ia_mode)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(5)
+    v = rng.normal(size=(len(tabs), plan.n_total))
+    dv, lbar, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    # the value equals the forward
+    assert np.array_equal(dv, plan.eval_real(om, h0, chi, G, lnP, nus))
+    for pt in range(len(tabs)):
+        worst = check_nuisance_fd(plan, w, tabs, nus, v, nbar, ia_mode, pt)
+        print("nuisance max rel err vs GPU FD", worst)
+    # fields the adjoint does not cover stay zero
+    covered = {flat_index(*p) for p in param_list(w, ia_mode)}
+    other = [k for k in range(nbar.shape[1]) if k not in covered]
+    assert np.all(nbar[:, other] == 0.0)
+
+
+@pytest.mark.gpu
+def test_vjp_lnP_vs_gpu_fd(gpu_lib):
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(6)
+    v = rng.normal(size=(len(tabs), plan.n_total))
+    _, lbar, _ = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    assert np.all(np.isfinite(lbar)) and np.any(lbar != 0)
+    for pt in range(len(tabs)):
+        sl = slice(pt, pt + 1)
+        # dense random direction
+        u = rng.normal(size=lnP.shape[1])
+        f = [float(v[pt] @ plan.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl] + s * H * u, nus[sl])[0])
+             for s in (1, -1)]
+        fd = (f[0] - f[1]) / (2 * H)
+        an = float(lbar[pt] @ u)
+        assert abs(an - fd) <= GRAD_REL * abs(fd), (an, fd)
+        # single entries: the largest gradients and random touched ones
+        top = np.argsort(-np.abs(lbar[pt]))[:4]
+        nz = np.flatnonzero(lbar[pt])
+        pick = np.concatenate([top, rng.choice(nz, 4, replace=False)])
+        for k in pick:
+            e = np.zeros(lnP.shape[1])
+            e[k] = H
+            f = [float(v[pt] @ plan.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl] + s * e, nus[sl])[0])
+                 for s in (1, -1)]
+            fd = (f[0] - f[1]) / (2 * H)
+            assert abs(lbar[pt, k] - fd) <= GRAD_REL * np.max(np.abs(lbar[pt])), (k, lbar[pt, k], fd)
+        # untouched entries have zero gradient: a step there changes nothing
+        zero = np.flatnonzero(lbar[pt] == 0)
+        k = rng.choice(zero)
+        e = np.zeros(lnP.shape[1])
+        e[k] = 1.0
+        d0 = plan.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl], nus[sl])
+        d1 = plan.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl] + e, nus[sl])
+        assert np.array_equal(d0, d1)
+
+
+@pytest.mark.gpu
+def test_vjp_mask_point_mass(gpu_lib):
+    """Masked entries carry no gradient; the point-mass term enters the
+    m-bias gradient of gamma_t."""
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION, npts=1, seed=4)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(8)
+    mask = (rng.uniform(size=plan.n_total) < 0.6).astype(np.int32)
+    pm = rng.uniform(0.0, 3.0, size=(1, w.cfg.n_lens))
+    v = rng.normal(size=(1, plan.n_total))
+    dv, lbar, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v, mask=mask, pm=pm)
+    check_nuisance_fd(plan, w, tabs, nus, v, nbar, abi.IA_REDSHIFT_EVOLUTION, 0, mask=mask, pm=pm)
+    v2 = np.where(mask == 1, v, rng.normal(size=v.shape))  # masked cotangents are ignored
+    _, lbar2, nbar2 = plan.vjp_real(om, h0, chi, G, lnP, nus, v2, mask=mask, pm=pm)
+    np.testing.assert_allclose(lbar2, lbar, rtol=1e-12, atol=1e-12 * np.abs(lbar).max())
+    np.testing.assert_allclose(nbar2, nbar, rtol=1e-12, atol=1e-12 * np.abs(nbar).max())
+
+
+@pytest.mark.gpu
+def test_vjp_mixed_plan_matches_fp64(gpu_lib):
+    """The adjoint kernels are FP64 in both plans; the mixed plan's forward
+    (which feeds the m-bias gradient) is within the 1e-4 bar."""
+    w, tabs, nus, p64 = setup_case(abi.IA_REDSHIFT_EVOLUTION)
+    pmx = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=len(tabs))
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    v = np.random.default_rng(9).normal(size=(len(tabs), p64.n_total))
+    _, l64, n64 = p64.vjp_real(om, h0, chi, G, lnP, nus, v)
+    _, lmx, nmx = pmx.vjp_real(om, h0, chi, G, lnP, nus, v)
+    assert np.max(np.abs(lmx - l64)) <= 1e-10 * np.max(np.abs(l64))
+    assert np.max(np.abs(nmx - n64)) <= 1e-4 * np.max(np.abs(n64))
+
+
+@pytest.mark.gpu
+def test_vjp_vs_oracle_fd(gpu_lib, oracle_built):
+    """Central differences of the FP64 oracle (the reference C path
+    restated) against the analytic gradient: m, b1, A1, eta and a lnP
+    direction of one point."""
+    import oracle as O
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION, npts=1, seed=13)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(10)
+    v = rng.normal(size=(1, plan.n_total))
+    _, lbar, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    import dataclasses
+    worst = 0.0
+    for field, i, j in [("shear_m", 0, None), ("shear_m", 3, None), ("gb", 0, 1), ("ia", 0, 0), ("ia", 0, 1)]:
+        x0 = nu_get(nus[0], field, i, j)
+        h = H * max(abs(x0), 0.1)
+        f = []
+        for s in (1, -1):
+            nu = clone(nus[0])
+            nu_set(nu, field, i, j, x0 + s * h)
+            o.set_point(tabs[0], nu)
+            f.append(float(v[0] @ o.data_vector_real()))
+        fd = (f[0] - f[1]) / (2 * h)
+        an = nbar[0, flat_index(field, i, j)]
+        err = abs(an - fd) / abs(fd)
+        worst = max(worst, err)
+        assert err <= ORACLE_REL, (field, i, j, an, fd)
+    u = rng.normal(size=lnP.shape[1])
+    f = []
+    for s in (1, -1):
+        t = dataclasses.replace(tabs[0], lnP=np.ascontiguousarray(
+            (tabs[0].lnP.reshape(-1) + s * H * u).reshape(tabs[0].lnP.shape)))
+        o.set_point(t, nus[0])
+        f.append(float(v[0] @ o.data_vector_real()))
+    fd = (f[0] - f[1]) / (2 * H)
+    an = float(lbar[0] @ u)
+    worst = max(worst, abs(an - fd) / abs(fd))
+    print("max rel gradient error vs oracle FD", worst)
+    assert abs(an - fd) <= ORACLE_REL * abs(fd), (an, fd)
+
+
+@pytest.mark.gpu
+def test_vjp_torch_autograd(gpu_lib):
+    """torch.autograd.Function: backward of sum(v * dv) equals the VJP, and
+    the fused value_and_vjp agrees."""
+    import torch
+    from cl2pt import autograd as AG
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    v = np.random.default_rng(11).normal(size=(len(tabs), plan.n_total))
+    _, lbar, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    nu_t = T(np.stack([abi.nuisance_to_array(n) for n in nus]))
+    lnP_t = T(lnP).requires_grad_(True)
+    nu_t.requires_grad_(True)
+    dv = AG.real_data_vector(plan, T(om), T(h0), T(chi), T(G), lnP_t, nu_t)
+    (dv * T(v)).sum().backward()
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(lnP_t.grad.cpu().numpy(), lbar, rtol=1e-12, atol=1e-14 * np.abs(lbar).max())
+    np.testing.assert_allclose(nu_t.grad.cpu().numpy(), nbar, rtol=1e-12, atol=1e-14 * np.abs(nbar).max())
+    dv2, l2, n2 = AG.value_and_vjp(plan, T(om), T(h0), T(chi), T(G), T(lnP), nu_t.detach(), T(v))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dv2.cpu().numpy(), dv.detach().cpu().numpy())
+    np.testing.assert_allclose(l2.cpu().numpy(), lbar, rtol=1e-12, atol=1e-14 * np.abs(lbar).max())
+
+
+@pytest.mark.gpu
+def test_vjp_unsupported_plan(gpu_lib):
+    """Non-Limber w(theta) and TATT plans report CL2PT_ERR_UNSUPPORTED."""
+    for name in ("real_3x2pt_small", "real_3x2pt_tatt_small"):
+        w = workloads.make(name)
+        tabs, nus = workloads.points(w, 1, seed=1)
+        plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=1)
+        om, h0, chi, G, lnP = workloads.stack(tabs)
+        with pytest.raises(lib.CL2PTError, match="-4"):
+            plan.vjp_real(om, h0, chi, G, lnP, nus, np.ones(plan.n_total))
