@@ -152,6 +152,59 @@ def run_reference(args):
     }))
 
 
+def value_grad(plan, w, data, d_om, d_h0, d_chi, d_G, d_lnP, d_nu, out, stream, args, p64=None):
+    """value+grad/s: cl2pt_vjp_real with a fixed cotangent on device-resident
+    inputs, CUDA-event timed over --steps batches (mixed plan, then the FP64
+    plan as the plain-FP64 GPU form)."""
+    import torch
+    from cl2pt import abi
+    B = d_om.shape[0]
+    dev = d_om.device
+    cot = torch.from_numpy(np.random.default_rng(7).normal(size=(B, plan.n_total))).to(dev)
+    lbar = torch.empty_like(d_lnP)
+    nbar = torch.empty_like(d_nu)
+    sptr = stream.cuda_stream
+
+    def run(p, n):
+        for _ in range(n):
+            p.vjp_real_device(d_om, d_h0, d_chi, d_G, d_lnP, d_nu, cot, out, lbar, nbar, stream=sptr)
+
+    run(plan, args.warmup)
+    plan.check_errors(sptr)
+    torch.cuda.synchronize()
+    plan.set_timing(True)
+    plan.kernel_times()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run(plan, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kms, _ = plan.kernel_times()
+    plan.set_timing(False)
+    plan.check_errors(sptr)
+    nb = nbar.cpu().numpy().view(np.float64).reshape(B, -1)
+    n_nu = int(np.count_nonzero(np.any(nb != 0.0, axis=0)))
+    res = {"value": B * args.steps / (ms / 1e3), "unit": "value+gradient evaluations/s",
+           "ms_per_step": ms / args.steps,
+           "grad_wrt": f"lnP table ({plan.shapes['nk']}x{plan.shapes['nz']}) and {n_nu} nuisance "
+                       f"parameters (shear m, b1{', IA' if w.cfg.ia_mode else ''})",
+           "n_nuisance": n_nu, "launches_per_step": plan.launches(),
+           "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items() if v > 0}}
+    if p64 is not None:
+        run(p64, 3)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n64 = max(2, args.steps // 2)
+        a.record(stream)
+        run(p64, n64)
+        b.record(stream)
+        torch.cuda.synchronize()
+        res["fp64_plain_gpu"] = B * n64 / (a.elapsed_time(b) / 1e3)
+        p64.close()
+    return res
+
+
 def run_fastpt(args):
     """--workload fastpt: the batched FAST-PT workload -- for each linear
     spectrum (2048 log-k in 1e-5..1e3 h/Mpc) get_FPT_bias's five one-loop
@@ -277,6 +330,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-grad", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -378,6 +432,15 @@ def main():
         fp64 = B * n64 / (a.elapsed_time(b) / 1e3)
         p64.close()
 
+    # ---- value + gradient: cl2pt_vjp_real on the same batch (forward and
+    # hand-written adjoint in one call; gradient w.r.t. the P(k, z) table and
+    # every nuisance parameter the data vector depends on)
+    vg = None
+    if not args.no_grad:
+        vg = value_grad(plan, w, data, d_om, d_h0, d_chi, d_G, d_lnP, d_nu, out, stream, args,
+                        None if args.no_fp64 else lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64,
+                                                           max_batch=B))
+
     # ---- roofline of the dominant kernel
     hbm, src = peaks()
     top = max(kms, key=lambda k: kms[k])
@@ -420,11 +483,22 @@ def main():
         "fp64_plain_gpu": {"value": fp64, "unit": UNIT,
                            "speedup_of_mixed": (value / world) / fp64 if fp64 else None},
     }
+    if vg is not None:
+        vg["value"] *= world
+        line["value_grad"] = vg
     if rank == 0 and world == 1 and not args.no_cpu:
         n, t = cpu_sample(w, data, budget_s=12.0)
         line["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": os.cpu_count(),
                                 "kind": "port",
                                 "sample": f"{n} points of the same batch, {t:.1f} s"}
+        if vg is not None:
+            # central differences on the CPU: 2 evaluations per parameter + 1
+            npar = vg["n_nuisance"]
+            vg["cpu_fd"] = {"value": (n / t) / (2 * npar + 1), "unit": "value+gradient/s",
+                            "kind": "port", "cores": os.cpu_count(),
+                            "note": f"nuisance gradient only ({npar} parameters) by central "
+                                    f"differences; the {nk}x{nz} table gradient would take "
+                                    f"{2 * nk * nz} more evaluations"}
     if rank == 0:
         print(json.dumps(line))
     plan.close()

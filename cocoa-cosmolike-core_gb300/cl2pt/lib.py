@@ -69,7 +69,8 @@ def load(path: str = LIB_PATH):
                                     C.c_void_p, C.c_void_p]
     lib.cl2pt_check_errors.argtypes = [C.c_void_p, C.c_void_p]
     lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
-                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]
     lib.cl2pt_eval_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
                                        C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_fourier_sizes.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip]
@@ -123,7 +124,9 @@ class Plan:
     """A cl2pt plan: geometry, redshift samples, shared axes and workspace."""
 
     def __init__(self, cfg: abi.Config, src_table, lens_table, tables, precision=PREC_MIXED,
-                 max_batch=1):
+                 max_batch=1, linear_table=False):
+        """linear_table: host batches may carry a separate linear P(k, z)
+        table (lnPL) on the same axes as lnP."""
         lib = load()
         self.cfg = cfg
         self._src = abi.make_nz(src_table)
@@ -136,6 +139,8 @@ class Plan:
         g.G_nz, g.G_z = len(ax[1]), _p(ax[1])
         g.pk_nk, g.pk_nz, g.pk_log10k, g.pk_z = len(ax[2]), len(ax[3]), _p(ax[2]), _p(ax[3])
         g.pkl_nk = 0
+        if linear_table:
+            g.pkl_nk, g.pkl_nz, g.pkl_log10k, g.pkl_z = len(ax[2]), len(ax[3]), _p(ax[2]), _p(ax[3])
         self.grid = g
         self.shapes = dict(chi=len(ax[0]), G=len(ax[1]), nk=len(ax[2]), nz=len(ax[3]))
         h = C.c_void_p()
@@ -210,7 +215,7 @@ class Plan:
     def vjp_real(self, omega_m, h0, chi, G, lnP, nuisance, cot, mask=None, pm=None, lnPL=None):
         """Value and vector-Jacobian product on host arrays: returns
         (dv [n][n_total], lnP_bar [n][nk*nz], nu_bar [n][13*MAX_BINS] in the
-        flat cl2pt_nuisance layout)."""
+        flat cl2pt_nuisance layout), plus lnPL_bar when lnPL is given."""
         om = np.ascontiguousarray(omega_m, dtype=np.float64)
         n = om.shape[0]
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
@@ -224,6 +229,7 @@ class Plan:
         cv = np.ascontiguousarray(np.broadcast_to(cot, (n, self.n_total)), dtype=np.float64)
         dv = np.zeros((n, self.n_total))
         lbar = np.zeros((n, arrs[3].size // n))
+        lbarl = None if lpl is None else np.zeros((n, lpl.size // n))
         nbar = (abi.Nuisance * n)()
         mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
         pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
@@ -231,15 +237,18 @@ class Plan:
                                     mk.ctypes.data if mk is not None else None,
                                     pmm.ctypes.data if pmm is not None else None,
                                     cv.ctypes.data, dv.ctypes.data, lbar.ctypes.data,
+                                    None if lbarl is None else lbarl.ctypes.data,
                                     C.addressof(nbar), None), "cl2pt_vjp_real")
         nb = np.frombuffer(bytes(nbar), dtype=np.float64).reshape(n, -1).copy()
+        if lbarl is not None:
+            return dv, lbar, nb, lbarl
         return dv, lbar, nb
 
     def vjp_real_device(self, omega_m, h0, chi, G, lnP, nuisance, cot, dv, lnP_bar, nu_bar,
-                        mask=None, pm=None, lnPL=None, stream=None):
+                        mask=None, pm=None, lnPL=None, lnPL_bar=None, stream=None):
         """Device form of vjp_real: float64 CUDA tensors; nuisance and nu_bar
         hold n packed cl2pt_nuisance structs (any dtype, contiguous); dv may
-        be None."""
+        be None; lnPL_bar is needed with lnPL."""
         b = Batch()
         b.n, b.where = int(omega_m.shape[0]), DEVICE
         cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
@@ -250,7 +259,9 @@ class Plan:
                                    None if mask is None else mask.data_ptr(),
                                    None if pm is None else pm.data_ptr(),
                                    cot.data_ptr(), None if dv is None else dv.data_ptr(),
-                                   lnP_bar.data_ptr(), nu_bar.data_ptr(), stream)
+                                   lnP_bar.data_ptr(),
+                                   None if lnPL_bar is None else lnPL_bar.data_ptr(),
+                                   nu_bar.data_ptr(), stream)
         check(st, "cl2pt_vjp_real")
 
     # ------------------------------------------------------------ device

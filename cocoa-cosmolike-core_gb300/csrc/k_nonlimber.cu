@@ -311,8 +311,10 @@ __device__ __forceinline__ NLGeom nl_geom(const Params& P, int pt)
 
 // ---- 1. forward transforms (cfftlog_ells_p1, cosmo2D.c:4047-4130), FP64:
 // one CTA per (point, lens bin, radial kernel j).
+// unit_b1: the galaxy kernel with b1 = 1 (the adjoint pass differentiates
+// the linear-bias factor out of it; bias model 0 only).
 template <typename T>
-__global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q)
+__global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int unit_b1)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x, q = blockIdx.y, j = blockIdx.z;
@@ -346,7 +348,9 @@ __global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q)
         double fx;
         if (j == 0) {
           double b1;
-          switch (P.bias_model[0]) {
+          if (unit_b1) {
+            b1 = 1.0;
+          } else switch (P.bias_model[0]) {
             case 0: b1 = nu.gb[0][q]; break;
             case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
             case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
@@ -586,12 +590,190 @@ __global__ void __launch_bounds__(NL_NT, 3) k_nl_loop(Params P, NLParams Q)
   }
 }
 
+// ---- 4. adjoint of the FFTLog part of C_cl_tomo.  For l < the hand-over
+// multipole, C_l = (2/pi) dlnchi sum_i F_i^2 k_i^3 P_lin(k_i, 1) + ..., with
+// F = b1 G0 + F_1 + bmag l(l+1) F_2 / y^2 linear in b1 (G0: the galaxy
+// kernel's transform with b1 = 1, written to tout by k_nl_forward with
+// unit_b1).  Given cbar[l] = dL/dC_l, one CTA per (point, bin) walks the
+// same multipole recurrence as k_nl_loop and accumulates
+//   dL/db1     += cbar (2/pi) dlnchi sum_i 2 F_i G0_i k_i^3 P_i
+//   dL/dpsl[m] += cbar (2/pi) dlnchi sum_i F_i^2 k_i^3 P_i (lerp weight)
+// where psl is the z = 0 slice of the linear table; the slice adjoint is
+// spread onto the table's two z columns at the end.
+template <typename T>
+__global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const double* __restrict__ cbar,
+                                                     double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int nchi = P.nl_nchi;
+  const int LNL = P.lmax_nolimber;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double bmag = nu.gb[4][q];
+  const double b1 = nu.gb[0][q];
+  const int nj = (bmag != 0.0) ? 3 : 2;
+  const NLGeom geo = nl_geom(P, pt);
+  double* psl = (double*)smem_raw;
+  double* plkd = psl + P.pkl_nk;
+  double* pinv = plkd + P.pkl_nk;
+  double* pbar = pinv + P.pkl_nk;
+  double* lxk = pbar + P.pkl_nk;
+  ct<T>* fa = (ct<T>*)(lxk + nchi);
+  ct<T>* fb = fa + Q.nmax;
+  T* F = (T*)(fb + Q.nmax);
+  T* G0 = F + nchi;
+  T* xpow = G0 + nchi;
+  T* xx2 = xpow + 3 * nchi;
+  T* rx3 = xx2 + nchi;
+  T* plk = rx3 + nchi;
+  __shared__ double red[NL_NT / 32];
+  const size_t cta = (size_t)pt * P.nl + q;
+  const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;
+  ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;
+  const double* cb = cbar + cta * LNL;
+  const double rc = geo.rc;
+  const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+  const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
+  const double dyz = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
+  for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+    psl[i] = (1 - dyz) * tabL[(size_t)i * P.pkl_nz + j0] + dyz * tabL[(size_t)i * P.pkl_nz + j0 + 1];
+    plk[i] = (T)P.pkl_lk[i];
+    plkd[i] = P.pkl_lk[i];
+    pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
+    pbar[i] = 0.0;
+  }
+  for (int i = tid; i < nchi; i += NL_NT) {
+    const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
+    for (int j = 0; j < 3; j++) xpow[j * nchi + i] = (T)pow(xr, Q.nu[j]);
+    lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
+    xx2[i] = (T)(xr * xr);
+    rx3[i] = (T)((rc / xr) * (rc / xr) * (rc / xr));
+  }
+  const bool exact_blocks = Q.direct_every != 0;
+  const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
+  const int LM = P.conv_l[cta];
+  const double sqpi = sqrt(M_PI);
+  const double dlnx = geo.dlnx;
+  double b1bar = 0.0;
+  for (int k = 0; k < LM; k++) {
+    const int ks = (k / 16) * 16;
+    __syncthreads();
+    for (int i = tid; i < nchi; i += NL_NT) F[i] = G0[i] = (T)0;
+    for (int j = 0; j < nj; j++) {
+      const int N = Q.N[j];
+      const int nq = N / 2 + 1;
+      const double base = geo.x0 / exp(2 * Q.pad[j] * dlnx);
+      const double y0 = (k + 1.) / geo.xlast;
+      const double lnbase = log(base * y0);
+      const double deta = 2.0 * M_PI / (dlnx * N);
+      __syncthreads();
+      ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
+      const bool direct = exact_blocks ? (k < ks + 2) : (k < 2);
+      const int slot = exact_blocks ? ((k - ks) & 1) : (k & 1);
+      const int di = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
+      const double* gd = gdir + ((size_t)j * Q.ndirect + (direct ? di : 0)) * Q.hstride * 2;
+      for (int i = tid; i < nq; i += NL_NT) {
+        ct<T> g;
+        if (direct) {
+          g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
+        } else {
+          const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
+          ct<T> num, den;
+          if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
+          else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
+          else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
+          g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
+        }
+        gs[slot * Q.hstride + i] = g;
+        double ph = -(deta * i) * lnbase;
+        ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
+        T sp, cp;
+        tsincos<T>((T)ph, &sp, &cp);
+        ct<T> val = tmul(tmul(tout[j * Q.hstride + i], tmk<T>(cp, sp)), g);
+        val.y = -val.y;
+        fa[i] = val;
+        if (i > 0 && i < N - i) fa[N - i] = tmk<T>(val.x, -val.y);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        fa[0].y = (T)0;
+        if ((N & 1) == 0) fa[N / 2].y = (T)0;
+      }
+      __syncthreads();
+      ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
+      const T scale = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
+      const T magf = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
+      for (int i = tid; i < nchi; i += NL_NT) {
+        T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
+        if (j == 0) {
+          G0[i] = fy;
+          fy *= (T)b1;
+        }
+        if (j == 2) fy = magf * fy * xx2[i];
+        F[i] += fy;
+      }
+      __syncthreads();
+    }
+    const double wk = cb[k] * geo.dlnchi * 2. / M_PI;
+    if (wk == 0.0) continue;
+    const double cub = (k + 1.) * (k + 1.) * (k + 1.);
+    const double lk1 = log10(k + 1.);
+    double part = 0.0;
+    for (int i = tid; i < nchi; i += NL_NT) {
+      const double lkv = lk1 + lxk[i];
+      const int lo = bsearch_d(plkd, P.pkl_nk, lkv);
+      const double dxd = (lkv - plkd[lo]) * pinv[lo];
+      const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
+                        (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
+      const double k3 = cub * (double)rx3[i];
+      const double f = (double)F[i];
+      const double g = wk * f * f * k3 * pl;
+      atomicAdd(&pbar[lo], g * (1 - dxd));
+      atomicAdd(&pbar[lo + 1], g * dxd);
+      part += 2.0 * f * (double)G0[i] * k3 * pl;
+    }
+    b1bar += wk * block_sum(part, red);
+  }
+  __syncthreads();
+  double* lb = lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
+  for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+    const double v = pbar[i];
+    if (v != 0.0) {
+      atomicAdd(&lb[(size_t)i * P.pkl_nz + j0], (1 - dyz) * v);
+      atomicAdd(&lb[(size_t)i * P.pkl_nz + j0 + 1], dyz * v);
+    }
+  }
+  if (tid == 0) atomicAdd(&nu_bar[pt].gb[0][q], b1bar);
+}
+
+template <typename T>
+static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
+                            cl2pt_nuisance* nu_bar, cudaStream_t s)
+{
+  const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
+  cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  k_nl_forward<T><<<dim3(P.B, P.nl, 1), NL_NT, sm1, s>>>(P, Q, 1);
+  const size_t sm = sizeof(double) * (4 * (size_t)P.pkl_nk + P.nl_nchi) +
+                    sizeof(T) * (2 * 2 * (size_t)Q.nmax + 7 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
+  cudaFuncSetAttribute(k_nl_vjp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_nl_vjp<T><<<dim3(P.B, P.nl), NL_NT, sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+}
+
+void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
+                          cl2pt_nuisance* nu_bar, cudaStream_t s, int* launches)
+{
+  if (P.prec == CL2PT_PREC_FP64) launch_nl_vjp_t<double>(P, Q, cbar, lnpl_bar, nu_bar, s);
+  else launch_nl_vjp_t<float>(P, Q, cbar, lnpl_bar, nu_bar, s);
+  (*launches) += 2;
+}
+
 template <typename T>
 static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
 {
   const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-  k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q);
+  k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
   const size_t sm3 = sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi) +
                      sizeof(T) * (2 * 2 * (size_t)Q.nmax + 6 * (size_t)P.nl_nchi + P.pkl_nk) + 64;

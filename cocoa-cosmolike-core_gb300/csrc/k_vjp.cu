@@ -20,10 +20,16 @@
 //                   the node-weight adjoints
 //   k_vjp_nodes     node-weight adjoints -> b1 and the NLA amplitude (and
 //                   its redshift power) of the nuisance gradient.
+// Non-Limber w(theta) (C_cl_tomo, cosmo2D.c:4528-4769): the w contraction
+// columns are [C_nl(l < LNL); C_gg nodes]; k_vjp_handover splits their
+// adjoint into the FFTLog part (k_nl_vjp, k_nonlimber.cu), the integer-l
+// Limber spectra (nonlinear and linear) and, above the hand-over multipole,
+// the node table through the interpol1d read-back.
 // Every quantity is recomputed from the node tables of the forward wave;
 // nothing of the integrand is stored.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "nonlimber.h"
 
 namespace cl2pt {
 
@@ -135,6 +141,7 @@ __global__ void k_vjp_contract(Params P, VJPParams V, const double* __restrict__
   const int pt = col / npair, pr = col - pt * npair;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
+  // probe 3: non-Limber w, columns [C_nl (LNL); C_gg nodes] -> cbar_w
   const int nt = P.ntheta;
   const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
   const int n_total = n_xi + n_gt + nt * P.nl;
@@ -152,7 +159,56 @@ __global__ void k_vjp_contract(Params P, VJPParams V, const double* __restrict__
   } else {
     const double* ow = ob + n_xi + n_gt + pr * nt;
     for (int t = 0; t < nt; t++) acc += ow[t] * filt[(size_t)t * K + k];
-    V.cbar_gg[((size_t)pt * P.nl + pr) * K + k] = acc;
+    if (probe == 2) V.cbar_gg[((size_t)pt * P.nl + pr) * K + k] = acc;
+    else V.cbar_w[((size_t)pt * P.nl + pr) * K + k] = acc;
+  }
+}
+
+// Adjoint of the non-Limber C_l assembly of one (point, lens bin)
+// (cosmo2D.c:4741-4765): below the hand-over multipole LM,
+// C_l = FFTLog_l + Limber_nl(l) - Limber_lin(l); from LM on, the Limber C_l
+// from the node table (interpol1d in ln l, l > LMIN_tab) or the direct
+// integer-l Limber value.  The hand-over itself is a discrete choice and is
+// held fixed.
+__global__ void k_vjp_handover(Params P, VJPParams V)
+{
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const size_t cta = (size_t)pt * P.nl + q;
+  const int LNL = P.lmax_nolimber, K = P.nnode_g;
+  const double* cw = V.cbar_w + cta * (LNL + K);
+  double* cg = V.cbar_gg + cta * K;
+  double* gb = V.ggl_bar + cta * LNL * 2;
+  double* cn = V.cnl_bar + cta * LNL;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) cg[k] = cw[LNL + k];
+  const int LM = P.conv_l[cta];
+  for (int k = threadIdx.x; k < LNL; k += blockDim.x) {
+    const double c = cw[k];
+    const bool fft = k < LM;
+    cn[k] = fft ? c : 0.0;
+    gb[2 * k + 0] = (fft || k <= P.lmin_tab) ? c : 0.0;
+    gb[2 * k + 1] = fft ? -c : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  // interpol1d read-back of the node table (basics.c:457-480), serial so
+  // that the scatter needs no atomics
+  const int n = P.n_ell;
+  double* tg = cg + P.nint;
+  for (int k = LM > P.lmin_tab + 1 ? LM : P.lmin_tab + 1; k < LNL; k++) {
+    const double c = cw[k];
+    const double x = log((double)k);
+    if (x < P.lim_g[0]) {
+      tg[0] += c;
+      continue;
+    }
+    const double r = (x - P.lim_g[0]) / P.lim_g[2];
+    const int i = (int)floor(r);
+    if (i + 1 >= n) {
+      tg[n - 1] += c;
+      continue;
+    }
+    tg[i] += c * (1.0 - (r - i));
+    tg[i + 1] += c * (r - i);
   }
 }
 
@@ -278,6 +334,41 @@ __global__ void k_vjp_gg(Params P, VJPParams V, const double* __restrict__ ell)
     lbar += 2.0 * cv * s * nf.F * c.P;
     pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, cv * s * s * nf.F * c.P);
   }
+  if (V.ggl_bar) {
+    // integer l < LNL: the nonlinear and linear Limber C_gg of the
+    // non-Limber hand-over (k_limber_gg mode 1)
+    const double a = P.node[(size_t)pt * NF_COUNT * P.node_stride + (size_t)NF_A * P.node_stride + off + p];
+    const double z = 1.0 / a - 1.0;
+    const int jl = bsearch_d(P.pkl_z, P.pkl_nz, z);
+    const double dyl = (z - P.pkl_z[jl]) / (P.pkl_z[jl + 1] - P.pkl_z[jl]);
+    const double* tabl = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    const double* gb = V.ggl_bar + b0 * P.lmax_nolimber * 2;
+    int hl = 0;
+    hint = 0;
+    for (int L = 0; L < P.lmax_nolimber; L++) {
+      const double cn = gb[2 * L], cl = gb[2 * L + 1];
+      if (cn == 0.0 && cl == 0.0) continue;
+      const double l = (double)L, lp = l + 0.5;
+      const double chi1 = nf.fK * (lp + 1.0) / lp;
+      if (chi1 > chi_amin) continue;
+      const double pref = l * (l + 1.) / (lp * lp);
+      const double c0 = (1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.));
+      const double c1 = 4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.));
+      const double a1 = a_chi_d(P.chi_z, X, P.chi_nz, chi1);
+      const double z1 = 1. / a1 - 1.;
+      const double H1 = 1.0 / ((a1 * a1) * chi_all_d(P.chi_z, X, P.chi_nz, a1).dchida);
+      const double n1 = nz_lens_d(P, z1, q, nu.lens_dz[q], nu.lens_stretch[q]);
+      const double wrsd = c0 * r0 - c1 * n1 * H1 * f_growth_d(P.G_z, Gv, P.G_nz, z1);
+      const double s = Lw + pref * Mw + wrsd;
+      const double lk = log10(lp) - nf.lfk;
+      const PkCell c = pk_cell(P.pk_lk, P.pk_nk, P.pk_nz, tab, lk, nf.j, nf.dy, hint);
+      const PkCell cL = pk_cell(P.pkl_lk, P.pkl_nk, P.pkl_nz, tabl, lk, jl, dyl, hl);
+      lbar += 2.0 * s * nf.F * (cn * c.P + cl * cL.P);
+      pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, cn * s * s * nf.F * c.P);
+      pk_scatter(barl, P.pkl_nz, cL, jl, dyl, cl * s * s * nf.F * cL.P);
+    }
+  }
   V.lbar_gg[b0 * nn + p] = lbar;
 }
 
@@ -379,9 +470,9 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
 
 size_t vjp_ss_smem(const Params& P) { return sizeof(double) * (size_t)P.pss * P.n_ss; }
 
-void launch_vjp(const Params& P, const VJPParams& V, const double* filt_xi, const double* filt_gt,
-                const double* filt_gg, const double* ell_ss, const double* ell_g, cudaStream_t s,
-                int* launches, const Hook& hk)
+void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
+                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
+                const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk)
 {
   const int nt = P.ntheta;
   const int n_total = nt * (2 * P.pss + P.pgs + P.nl);
@@ -402,9 +493,20 @@ void launch_vjp(const Params& P, const VJPParams& V, const double* filt_xi, cons
     *launches += 2;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg, 2, P.nnode_g);
-    k_vjp_gg<<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, 0, s>>>(P, V, ell_g);
-    *launches += 2;
+    if (P.adopt_limber_gg) {
+      k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg, 2, P.nnode_g);
+      VJPParams V2 = V;
+      V2.ggl_bar = nullptr;
+      k_vjp_gg<<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, 0, s>>>(P, V2, ell_g);
+      *launches += 2;
+    } else {
+      const int Kw = P.lmax_nolimber + P.nnode_g;
+      k_vjp_contract<<<dim3((Kw + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg_nl, 3, Kw);
+      k_vjp_handover<<<dim3(P.B, P.nl), 256, 0, s>>>(P, V);
+      k_vjp_gg<<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, 0, s>>>(P, V, ell_g);
+      launch_nonlimber_vjp(P, Q, V.cnl_bar, V.lnpl_bar, V.nu_bar, s, launches);
+      *launches += 3;
+    }
   }
   k_vjp_nodes<<<dim3(P.B, 1 + 2 * P.nl), NB_NT, 0, s>>>(P, V);
   (*launches)++;

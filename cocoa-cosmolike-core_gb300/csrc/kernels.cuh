@@ -57,10 +57,16 @@ struct VJPParams {
   double* lbar_gs;         // [B][nl][2][n_ss]
   double* lbar_gg;         // [B][nl][n_gg]
   cl2pt_nuisance* nu_bar;  // [B]
+  // non-Limber w(theta)
+  double* lnpl_bar;        // [B][pkl_nk * pkl_nz] (= lnp_bar when the tables coincide)
+  double* cbar_w;          // [B][nl][LNL + nnode_g] adjoint of the w contraction columns
+  double* ggl_bar;         // [B][nl][LNL][2] adjoint of the integer-l Limber C_gg (nonlinear, linear)
+  double* cnl_bar;         // [B][nl][LNL] adjoint of the FFTLog C_l
 };
+struct NLParams;
 size_t vjp_ss_smem(const Params& P);
-void launch_vjp(const Params& P, const VJPParams& V, const double* filt_xi, const double* filt_gt,
-                const double* filt_gg, const double* ell_ss, const double* ell_g, cudaStream_t s,
-                int* launches, const Hook& hk);
+void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
+                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
+                const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk);
 
 }  // namespace cl2pt

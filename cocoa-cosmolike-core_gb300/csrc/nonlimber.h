@@ -28,5 +28,10 @@ struct NLParams {
 
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
                       const Hook& hk);
+// Adjoint of the FFTLog part (run after the forward wave): cbar [B][nl][LNL]
+// = dL/dC_l below the hand-over multipole; adds into lnpl_bar [B][pkl_nk *
+// pkl_nz] and nu_bar[pt].gb[0][q] (bias model 0).
+void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
+                          cl2pt_nuisance* nu_bar, cudaStream_t s, int* launches);
 
 }  // namespace cl2pt

@@ -752,6 +752,7 @@ struct FourierReq {
 struct VJPReq {
   const double* cot = nullptr;
   double* lnp_bar = nullptr;
+  double* lnpl_bar = nullptr;  // only with a separate linear table
   cl2pt_nuisance* nu_bar = nullptr;
 };
 
@@ -792,27 +793,30 @@ extern "C" int cl2pt_eval_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell,
 }
 
 extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                              const double* cot, double* dv, double* lnP_bar, cl2pt_nuisance* nu_bar,
-                              void* stream)
+                              const double* cot, double* dv, double* lnP_bar, double* lnPL_bar,
+                              cl2pt_nuisance* nu_bar, void* stream)
 {
   if (!p || !cot || !lnP_bar || !nu_bar) return CL2PT_ERR_ARG;
   int st = check_batch(p, b);
   if (st) return st;
+  if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
   const cl2pt_config& c = p->cfg;
-  if (c.ia_model != CL2PT_IA_NLA || c.bias_model[0] != 0 || c.linear_pk || c.one_loop_bias ||
-      ((c.probes & CL2PT_PROBE_WTHETA) && !c.adopt_limber_gg))
+  if (c.ia_model != CL2PT_IA_NLA || c.bias_model[0] != 0 || c.linear_pk || c.one_loop_bias)
     return CL2PT_ERR_UNSUPPORTED;
   if (cl2pt::vjp_ss_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
   if (!p->d_vjp_ws) {
     const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
+    const size_t LNL = c.lmax_nolimber;
     const size_t nws = W * p->n_total + W * p->pss * p->nnode_ss + W * p->pgs * p->nnode_g +
                        W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
-                       W * nl * p->n_gg;
+                       W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL;
     // (a failed allocation leaves the plan usable for evaluation)
     int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
     if (!a) a = dalloc(p, &p->d_vjp_lnp, (size_t)p->max_batch * p->P.pk_nk * p->P.pk_nz);
     if (!a) a = dalloc(p, &p->d_vjp_nu, (size_t)p->max_batch);
+    if (!a && p->d_in_lnPL)
+      a = dalloc(p, &p->d_vjp_lnpl, (size_t)p->max_batch * p->P.pkl_nk * p->P.pkl_nz);
     if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
     if (a) {
       p->d_vjp_ws = nullptr;
@@ -822,6 +826,7 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   VJPReq vr;
   vr.cot = cot;
   vr.lnp_bar = lnP_bar;
+  vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
 }
@@ -896,21 +901,28 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
   // adjoint: device views of the cotangent and the gradients, workspace
   const double* vcot = nullptr;
   double* vlnp = nullptr;
+  double* vlnpl = nullptr;
   cl2pt_nuisance* vnu = nullptr;
   cl2pt::VJPParams V0{};
+  // the linear table is separate exactly when the forward reads one
+  const bool sep_lin = b->lnPL != nullptr && (b->where == CL2PT_DEVICE || p->d_in_lnPL != nullptr);
+  if (vr && b->lnPL && !sep_lin) memset(vr->lnpl_bar, 0, (size_t)n * nPL * sizeof(double));
   if (vr) {
     if (b->where == CL2PT_HOST) {
       CUDA_OK(cudaMemcpyAsync(p->d_vjp_cot, vr->cot, (size_t)n * n_total * sizeof(double),
                               cudaMemcpyHostToDevice, s));
       vcot = p->d_vjp_cot;
       vlnp = p->d_vjp_lnp;
+      vlnpl = sep_lin ? p->d_vjp_lnpl : vlnp;
       vnu = p->d_vjp_nu;
     } else {
       vcot = vr->cot;
       vlnp = vr->lnp_bar;
+      vlnpl = sep_lin ? vr->lnpl_bar : vlnp;
       vnu = vr->nu_bar;
     }
     CUDA_OK(cudaMemsetAsync(vlnp, 0, (size_t)n * nP * sizeof(double), s));
+    if (sep_lin) CUDA_OK(cudaMemsetAsync(vlnpl, 0, (size_t)n * nPL * sizeof(double), s));
     CUDA_OK(cudaMemsetAsync(vnu, 0, (size_t)n * sizeof(cl2pt_nuisance), s));
     const int W = p->wave, ns = p->cfg.n_source, nl = p->cfg.n_lens;
     double* w = p->d_vjp_ws;
@@ -921,7 +933,11 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.wbar_ss = w; w += (size_t)W * ns * p->n_ss;
     V0.wbar_gx = w; w += (size_t)W * nl * ns * p->n_ss;
     V0.lbar_gs = w; w += (size_t)W * nl * 2 * p->n_ss;
-    V0.lbar_gg = w;
+    V0.lbar_gg = w; w += (size_t)W * nl * p->n_gg;
+    const int LNL = p->cfg.lmax_nolimber;
+    V0.cbar_w = w; w += (size_t)W * nl * (LNL + p->nnode_g);
+    V0.ggl_bar = w; w += (size_t)W * nl * LNL * 2;
+    V0.cnl_bar = w;
     V0.mask = dmask;
   }
   int launches = 0;
@@ -1022,9 +1038,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         V.cot = vcot + (size_t)w0 * n_total;
         V.dv = ddv + (size_t)w0 * n_total;
         V.lnp_bar = vlnp + (size_t)w0 * nP;
+        V.lnpl_bar = vlnpl + (size_t)w0 * (sep_lin ? nPL : nP);
         V.nu_bar = vnu + w0;
-        cl2pt::launch_vjp(P, V, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_ell_ss, p->d_ell_g, s,
-                          &launches, hk);
+        cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl,
+                          p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       }
     }
   }
@@ -1037,6 +1054,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                               cudaMemcpyDeviceToHost, s));
     if (vr) {
       CUDA_OK(cudaMemcpyAsync(vr->lnp_bar, vlnp, (size_t)n * nP * sizeof(double), cudaMemcpyDeviceToHost, s));
+      if (sep_lin)
+        CUDA_OK(cudaMemcpyAsync(vr->lnpl_bar, vlnpl, (size_t)n * nPL * sizeof(double), cudaMemcpyDeviceToHost, s));
       CUDA_OK(cudaMemcpyAsync(vr->nu_bar, vnu, (size_t)n * sizeof(cl2pt_nuisance), cudaMemcpyDeviceToHost, s));
     }
     int err = 0;

@@ -78,6 +78,7 @@ struct cl2pt_plan {
   double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
   double* d_vjp_cot = nullptr;         // [max_batch][n_total]
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]
+  double* d_vjp_lnpl = nullptr;        // [max_batch][pkl_nk * pkl_nz]
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;

@@ -112,21 +112,26 @@ int cl2pt_fourier_sizes(const cl2pt_plan* plan, int nell, int* n_ss, int* n_gs,
  * cl2pt_eval_real (dv, when not NULL, receives the value) and then the
  * adjoint of every stage for the cotangent cot [n][n_total] (masked
  * entries ignored):
- *   lnP_bar [n][pk_nk * pk_nz]  d(cot . dv)/d lnP (the nonlinear table)
- *   nu_bar  [n]                 the same for the nuisance parameters, in the
- *                               cl2pt_nuisance layout: shear_m, gb[0] (b1)
- *                               and ia[0] (A1 per source bin in redshift-
- *                               binning mode; A1 and eta in ia[0][0..1] in
- *                               redshift-evolution mode); other fields 0.
+ *   lnP_bar  [n][pk_nk * pk_nz]    d(cot . dv)/d lnP (the nonlinear table)
+ *   lnPL_bar [n][pkl_nk * pkl_nz]  the same for the linear table when the
+ *                                  batch carries one (batch->lnPL != NULL);
+ *                                  otherwise the linear-table terms (non-
+ *                                  Limber w) are part of lnP_bar and lnPL_bar
+ *                                  may be NULL
+ *   nu_bar   [n]                   the nuisance gradient in the cl2pt_nuisance
+ *                                  layout: shear_m, gb[0] (b1) and ia[0] (A1
+ *                                  per source bin in redshift-binning mode;
+ *                                  A1 and eta in ia[0][0..1] in redshift-
+ *                                  evolution mode); other fields 0.
  * Every pointer follows batch->where.  The reference has no derivatives;
  * this replaces the central finite differences a caller would take of
- * compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159).
- * Supported: NLA intrinsic alignments, bias model 0, the nonlinear run mode
- * and Limber w(theta) (adopt_limber_gg = 1, or no w(theta) probe); other
- * plans return CL2PT_ERR_UNSUPPORTED. */
+ * compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159).  The
+ * non-Limber hand-over multipole of w(theta) is a discrete choice and is held
+ * at its forward value.  Supported: NLA intrinsic alignments, bias model 0,
+ * the nonlinear run mode; other plans return CL2PT_ERR_UNSUPPORTED. */
 int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
-                   cl2pt_nuisance* nu_bar, void* stream);
+                   double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
 
 /* Wait for the stream and report any device-side check that failed since
  * the last call (a device-resident batch does not synchronise). */
