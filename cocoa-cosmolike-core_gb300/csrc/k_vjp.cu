@@ -14,10 +14,9 @@
 // Given the cotangent v of dv:
 //   k_vjp_assemble  obs_bar = v mask calibration, and the shear m-bias part
 //   k_vjp_contract  C_bar = filters^T obs_bar (per probe)
-//   k_vjp_ss/gs/gg  one thread per quadrature node sweeping the C_l nodes:
-//                   d/dlnP of every bilinear corner (weight P times the
-//                   corner weight, atomically accumulated into lnP_bar) and
-//                   the node-weight adjoints
+//   k_vjp_ss/gs/gg  (k_vjp_limber.cu) one thread per quadrature node
+//                   sweeping the C_l nodes: d/dlnP of every bilinear corner
+//                   and the node-weight adjoints
 //   k_vjp_nodes     node-weight adjoints -> b1 and the NLA amplitude (and
 //                   its redshift power) of the nuisance gradient.
 // Non-Limber w(theta) (C_cl_tomo, cosmo2D.c:4528-4769): the w contraction
@@ -34,59 +33,6 @@
 namespace cl2pt {
 
 namespace {
-
-// Bilinear cell of the Pdelta walk and P there (cosmo3D.c:362-417).
-struct PkCell {
-  int i;
-  double dx, P;
-};
-__device__ __forceinline__ PkCell pk_cell(const double* __restrict__ lk, int nk, int nz,
-                                          const double* __restrict__ tab, double log10k, int j,
-                                          double dy, int& hint)
-{
-  int i = hint;
-  if (!(i >= 0 && i <= nk - 2 && lk[i] <= log10k && (log10k < lk[i + 1] || i == nk - 2)))
-    i = bsearch_d(lk, nk, log10k);
-  hint = i;
-  PkCell c;
-  c.i = i;
-  c.dx = (log10k - lk[i]) / (lk[i + 1] - lk[i]);
-  const double* r0 = tab + (size_t)i * nz + j;
-  const double* r1 = r0 + nz;
-  const double dx = c.dx;
-  const double v = (1 - dx) * (1 - dy) * r0[0] + (1 - dx) * dy * r0[1] + dx * (1 - dy) * r1[0] + dx * dy * r1[1];
-  c.P = exp(v) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
-  return c;
-}
-// g = dC/dP * P: the derivative with respect to the interpolated lnP, spread
-// over the four corners with their bilinear weights
-__device__ __forceinline__ void pk_scatter(double* __restrict__ bar, int nz, const PkCell& c, int j,
-                                           double dy, double g)
-{
-  if (g == 0.0) return;
-  double* b0 = bar + (size_t)c.i * nz + j;
-  double* b1 = b0 + nz;
-  atomicAdd(b0, g * (1 - c.dx) * (1 - dy));
-  atomicAdd(b0 + 1, g * (1 - c.dx) * dy);
-  atomicAdd(b1, g * c.dx * (1 - dy));
-  atomicAdd(b1 + 1, g * c.dx * dy);
-}
-
-struct NodeF {
-  double F, lfk, dy, fK;
-  int j;
-};
-__device__ __forceinline__ NodeF node_f(const Params& P, int pt, int idx)
-{
-  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
-  NodeF n;
-  n.fK = node[(size_t)NF_FK * P.node_stride + idx];
-  n.F = node[(size_t)NF_WT * P.node_stride + idx] * node[(size_t)NF_DCHIDA * P.node_stride + idx] / (n.fK * n.fK);
-  n.lfk = log10(n.fK * CL2PT_COVERH0);
-  n.dy = node[(size_t)NF_DYZ * P.node_stride + idx];
-  n.j = P.node_j[(size_t)pt * P.node_stride + idx];
-  return n;
-}
 
 // obs_bar and the shear-calibration gradient (add_calib_and_set_mask_X_N,
 // generic_interface.hpp:800-925): xi = obs (1+m_a)(1+m_b);
@@ -212,166 +158,6 @@ __global__ void k_vjp_handover(Params P, VJPParams V)
   }
 }
 
-// ss: CTA = point, thread = ss node p, sweeping every C_l node.
-// xb[pair][p] = sum_l pref C_bar(pair, l) P(l, p) in shared memory.
-__global__ void k_vjp_ss(Params P, VJPParams V, const double* __restrict__ ell)
-{
-  extern __shared__ double xb[];
-  const int pt = blockIdx.x;
-  const int p = threadIdx.x;
-  const int nn = P.n_ss, K = P.nnode_ss;
-  for (int i = p; i < P.pss * nn; i += blockDim.x) xb[i] = 0.0;
-  __syncthreads();
-  if (p >= nn) return;
-  const NodeF nf = node_f(P, pt, p);
-  const double* w = P.wss + (size_t)pt * P.ns * nn;
-  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
-  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
-  const double* cb = V.cbar_ss + (size_t)pt * P.pss * K;
-  int hint = 0;
-  for (int L = 0; L < K; L++) {
-    const double l = ell[L], lp = l + 0.5;
-    const double pref = l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp);
-    const PkCell c = pk_cell(P.pk_lk, P.pk_nk, P.pk_nz, tab, log10(lp) - nf.lfk, nf.j, nf.dy, hint);
-    const double pc = pref * c.P;
-    double pb = 0.0;
-    for (int pr = 0; pr < P.pss; pr++) {
-      const double cv = cb[(size_t)pr * K + L];
-      pb += cv * w[P.z1[pr] * nn + p] * w[P.z2[pr] * nn + p];
-      xb[pr * nn + p] += pc * cv;
-    }
-    pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, pc * nf.F * pb);
-  }
-  // w_bar_i(p) = F sum over the pairs holding i of xb w_other (both terms
-  // on the diagonal)
-  double* wb = V.wbar_ss + (size_t)pt * P.ns * nn;
-  for (int pr = 0; pr < P.pss; pr++) {
-    const int a = P.z1[pr], b = P.z2[pr];
-    const double x = xb[pr * nn + p] * nf.F;
-    wb[a * nn + p] += x * w[b * nn + p];
-    wb[b * nn + p] += x * w[a * nn + p];
-  }
-}
-
-// gs: CTA = (point, lens bin q), thread = node p of that bin's set
-__global__ void k_vjp_gs(Params P, VJPParams V, const double* __restrict__ ell)
-{
-  const int pt = blockIdx.x, q = blockIdx.y;
-  const int p = threadIdx.x;
-  const int nn = P.n_ss, K = P.nnode_g;
-  if (p >= nn) return;
-  const int off = P.n_ss + q * P.n_ss;
-  const NodeF nf = node_f(P, pt, off + p);
-  const size_t b0 = (size_t)pt * P.nl + q;
-  const double Lw = P.wgs_l[b0 * nn + p], Mw = P.wgs_m[b0 * nn + p];
-  const double* wx = P.wgs_x + b0 * P.ns * nn;
-  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
-  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
-  double* xbar = V.wbar_gx + b0 * P.ns * nn;
-  double lb0 = 0.0, lb1 = 0.0;
-  int hint = 0;
-  for (int L = 0; L < K; L++) {
-    const double l = ell[L], lp = l + 0.5;
-    const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
-    const double pref2 = (tmp > 0) ? sqrt(tmp) / (lp * lp) : 0.0;
-    const double pref = l * (l + 1.) / (lp * lp);
-    const PkCell c = pk_cell(P.pk_lk, P.pk_nk, P.pk_nz, tab, log10(lp) - nf.lfk, nf.j, nf.dy, hint);
-    const double g = pref2 * c.P * nf.F;
-    double sx = 0.0;  // sum_s C_bar(q, s) x_s
-    for (int k = 0; k < P.pgs; k++) {
-      if (P.zl[k] != q) continue;
-      const int s = P.zs[k];
-      const double cv = V.cbar_gs[((size_t)pt * P.pgs + k) * K + L];
-      sx += cv * wx[s * nn + p];
-      xbar[s * nn + p] += g * cv * (Lw + pref * Mw);
-    }
-    lb0 += g * sx;
-    lb1 += g * pref * sx;
-    pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, g * (Lw + pref * Mw) * sx);
-  }
-  V.lbar_gs[(b0 * 2 + 0) * nn + p] = lb0;
-  V.lbar_gs[(b0 * 2 + 1) * nn + p] = lb1;
-}
-
-// gg (Limber): CTA = (point, lens bin q), thread = gg node p; s(l, p) is
-// recomputed in FP64 (W_RSD at a_chi((l+3/2)/k), radial_weights.c:87-105;
-// nodes past chi(a_min) give nothing, cosmo2D.c:2538-2551)
-__global__ void k_vjp_gg(Params P, VJPParams V, const double* __restrict__ ell)
-{
-  const int pt = blockIdx.x, q = blockIdx.y;
-  const int p = threadIdx.x;
-  const int nn = P.n_gg, K = P.nnode_g;
-  if (p >= nn) return;
-  const int off = P.n_ss + P.nl * P.n_ss + q * nn;
-  const NodeF nf = node_f(P, pt, off + p);
-  const size_t b0 = (size_t)pt * P.nl + q;
-  const double Lw = P.wgg_l[b0 * nn + p], Mw = P.wgg_m[b0 * nn + p], r0 = P.wgg_r0[b0 * nn + p];
-  const double* X = P.chi + (size_t)pt * P.chi_nz;
-  const double* Gv = P.G + (size_t)pt * P.G_nz;
-  const cl2pt_nuisance& nu = P.nu[pt];
-  const double chi_amin = P.chi_amin[pt];
-  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
-  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
-  const double* cb = V.cbar_gg + b0 * K;
-  double lbar = 0.0;
-  int hint = 0;
-  for (int L = 0; L < K; L++) {
-    const double l = ell[L], lp = l + 0.5;
-    const double chi1 = nf.fK * (lp + 1.0) / lp;
-    if (chi1 > chi_amin) continue;
-    const double cv = cb[L];
-    if (cv == 0.0) continue;
-    const double pref = l * (l + 1.) / (lp * lp);
-    const double c0 = (1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.));
-    const double c1 = 4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.));
-    const double a1 = a_chi_d(P.chi_z, X, P.chi_nz, chi1);
-    const double z1 = 1. / a1 - 1.;
-    const double H1 = 1.0 / ((a1 * a1) * chi_all_d(P.chi_z, X, P.chi_nz, a1).dchida);
-    const double n1 = nz_lens_d(P, z1, q, nu.lens_dz[q], nu.lens_stretch[q]);
-    const double wrsd = c0 * r0 - c1 * n1 * H1 * f_growth_d(P.G_z, Gv, P.G_nz, z1);
-    const double s = Lw + pref * Mw + wrsd;
-    const PkCell c = pk_cell(P.pk_lk, P.pk_nk, P.pk_nz, tab, log10(lp) - nf.lfk, nf.j, nf.dy, hint);
-    lbar += 2.0 * cv * s * nf.F * c.P;
-    pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, cv * s * s * nf.F * c.P);
-  }
-  if (V.ggl_bar) {
-    // integer l < LNL: the nonlinear and linear Limber C_gg of the
-    // non-Limber hand-over (k_limber_gg mode 1)
-    const double a = P.node[(size_t)pt * NF_COUNT * P.node_stride + (size_t)NF_A * P.node_stride + off + p];
-    const double z = 1.0 / a - 1.0;
-    const int jl = bsearch_d(P.pkl_z, P.pkl_nz, z);
-    const double dyl = (z - P.pkl_z[jl]) / (P.pkl_z[jl + 1] - P.pkl_z[jl]);
-    const double* tabl = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
-    double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
-    const double* gb = V.ggl_bar + b0 * P.lmax_nolimber * 2;
-    int hl = 0;
-    hint = 0;
-    for (int L = 0; L < P.lmax_nolimber; L++) {
-      const double cn = gb[2 * L], cl = gb[2 * L + 1];
-      if (cn == 0.0 && cl == 0.0) continue;
-      const double l = (double)L, lp = l + 0.5;
-      const double chi1 = nf.fK * (lp + 1.0) / lp;
-      if (chi1 > chi_amin) continue;
-      const double pref = l * (l + 1.) / (lp * lp);
-      const double c0 = (1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.));
-      const double c1 = 4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.));
-      const double a1 = a_chi_d(P.chi_z, X, P.chi_nz, chi1);
-      const double z1 = 1. / a1 - 1.;
-      const double H1 = 1.0 / ((a1 * a1) * chi_all_d(P.chi_z, X, P.chi_nz, a1).dchida);
-      const double n1 = nz_lens_d(P, z1, q, nu.lens_dz[q], nu.lens_stretch[q]);
-      const double wrsd = c0 * r0 - c1 * n1 * H1 * f_growth_d(P.G_z, Gv, P.G_nz, z1);
-      const double s = Lw + pref * Mw + wrsd;
-      const double lk = log10(lp) - nf.lfk;
-      const PkCell c = pk_cell(P.pk_lk, P.pk_nk, P.pk_nz, tab, lk, nf.j, nf.dy, hint);
-      const PkCell cL = pk_cell(P.pkl_lk, P.pkl_nk, P.pkl_nz, tabl, lk, jl, dyl, hl);
-      lbar += 2.0 * s * nf.F * (cn * c.P + cl * cL.P);
-      pk_scatter(bar, P.pk_nz, c, nf.j, nf.dy, cn * s * s * nf.F * c.P);
-      pk_scatter(barl, P.pkl_nz, cL, jl, dyl, cl * s * s * nf.F * cL.P);
-    }
-  }
-  V.lbar_gg[b0 * nn + p] = lbar;
-}
-
 __device__ __forceinline__ double block_sum_d(double v, double* red)
 {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -468,28 +254,23 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
 
 }  // namespace
 
-size_t vjp_ss_smem(const Params& P) { return sizeof(double) * (size_t)P.pss * P.n_ss; }
-
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
                 const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
                 const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk)
 {
   const int nt = P.ntheta;
   const int n_total = nt * (2 * P.pss + P.pgs + P.nl);
-  const int rnd = 32;
   hk(CL2PT_K_VJP, 1);
   k_vjp_assemble<<<dim3((n_total + 255) / 256, P.B), 256, 0, s>>>(P, V);
   (*launches)++;
   if (P.probes & CL2PT_PROBE_XI) {
     k_vjp_contract<<<dim3((P.nnode_ss + 127) / 128, P.B * P.pss), 128, 0, s>>>(P, V, filt_xi, 0, P.nnode_ss);
-    const size_t sm = vjp_ss_smem(P);
-    cudaFuncSetAttribute(k_vjp_ss, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_vjp_ss<<<P.B, ((P.n_ss + rnd - 1) / rnd) * rnd, sm, s>>>(P, V, ell_ss);
+    launch_vjp_limber(P, V, 0, s);
     *launches += 2;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
     k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.pgs), 128, 0, s>>>(P, V, filt_gt, 1, P.nnode_g);
-    k_vjp_gs<<<dim3(P.B, P.nl), ((P.n_ss + rnd - 1) / rnd) * rnd, 0, s>>>(P, V, ell_g);
+    launch_vjp_limber(P, V, 1, s);
     *launches += 2;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
@@ -497,13 +278,13 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
       k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg, 2, P.nnode_g);
       VJPParams V2 = V;
       V2.ggl_bar = nullptr;
-      k_vjp_gg<<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, 0, s>>>(P, V2, ell_g);
+      launch_vjp_limber(P, V2, 2, s);
       *launches += 2;
     } else {
       const int Kw = P.lmax_nolimber + P.nnode_g;
       k_vjp_contract<<<dim3((Kw + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg_nl, 3, Kw);
       k_vjp_handover<<<dim3(P.B, P.nl), 256, 0, s>>>(P, V);
-      k_vjp_gg<<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, 0, s>>>(P, V, ell_g);
+      launch_vjp_limber(P, V, 2, s);
       launch_nonlimber_vjp(P, Q, V.cnl_bar, V.lnpl_bar, V.nu_bar, s, launches);
       *launches += 3;
     }

@@ -1,0 +1,515 @@
+// k_vjp_limber.cu -- adjoint sweeps of the Limber C_l tables (ss, gs, gg).
+//
+// One CTA per (point[, lens bin]), one thread per quadrature node p, sweeping
+// the C_l nodes l (and, for non-Limber w(theta), the integer l of the
+// hand-over).  For each (l, p) the thread evaluates P(k = (l+1/2)/chi_p, z_p)
+// and, for gg, the redshift-space weight s(l, p), and accumulates
+//   * the lnP-table adjoint: dL/dlnP_interp = (dC/dP) P, spread over the
+//     four bilinear corners; consecutive multipoles of one node mostly stay
+//     in one table cell, so the corner weights are summed over the run of l
+//     inside a cell and flushed with four FP64 atomics when the cell changes;
+//   * the node-weight adjoints (x_bar per pair, L_bar for the lens weight).
+// Precision follows the plan: in the mixed plan the per-(l, p) arithmetic
+// (table walk, W_RSD, products) is FP32 with the forward's split exponent
+// (exp(hi) exp(lo + delta), cell differences formed in FP64), the table
+// coordinate and the in-cell offset are FP64, and every accumulator is FP64
+// (FP32 partial sums over chunks of LC multipoles); in the FP64 plan all of
+// it is FP64.  Per-multipole factors (log10(l+1/2), the l prefactors, the
+// RSD coefficients) are plan constants (VJPParams::lfac_*).
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cl2pt {
+
+namespace {
+
+constexpr int LC = 32;  // multipoles per shared-memory chunk
+
+template <typename T> __device__ __forceinline__ T t_exp(T x);
+template <> __device__ __forceinline__ float t_exp<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double t_exp<double>(double x) { return exp(x); }
+
+// Walk of one node along l on one lnP table (cosmo3D.c:362-417).
+template <typename T>
+struct PWalk {
+  int i = -1;       // current k cell
+  T lo, d01, d10, d11, eh;
+  T acc0 = 0, acc1 = 0;  // sum over the run of g (1 - dx), g dx
+};
+
+template <typename T>
+__device__ __forceinline__ void pw_flush(PWalk<T>& w, double* __restrict__ bar, int nz, int j, double dy)
+{
+  if (w.i < 0 || (w.acc0 == (T)0 && w.acc1 == (T)0)) return;
+  double* b0 = bar + (size_t)w.i * nz + j;
+  double* b1 = b0 + nz;
+  const double a0 = (double)w.acc0, a1 = (double)w.acc1;
+  atomicAdd(b0, a0 * (1 - dy));
+  atomicAdd(b0 + 1, a0 * dy);
+  atomicAdd(b1, a1 * (1 - dy));
+  atomicAdd(b1 + 1, a1 * dy);
+  w.acc0 = w.acc1 = (T)0;
+}
+
+// P at log10 k (FP64 coordinate); dx returned for the scatter weights.
+template <typename T>
+__device__ __forceinline__ T pw_eval(PWalk<T>& w, const double* __restrict__ lkd, const double* __restrict__ inv,
+                                     int nk, const double* __restrict__ tab, int nz, int j, double dy, T dyt,
+                                     double log10k, double* __restrict__ bar, T& dx)
+{
+  int i = w.i;
+  if (!(i >= 0 && lkd[i] <= log10k && (log10k < lkd[i + 1] || i == nk - 2))) {
+    pw_flush(w, bar, nz, j, dy);
+    i = bsearch_d(lkd, nk, log10k);
+    w.i = i;
+    const double* r0 = tab + (size_t)i * nz + j;
+    const double* r1 = r0 + nz;
+    const double a00 = r0[0], a01 = r0[1], a10 = r1[0], a11 = r1[1];
+    w.d01 = (T)(a01 - a00);
+    w.d10 = (T)(a10 - a00);
+    w.d11 = (T)((a11 - a10) - (a01 - a00));
+    const T hi = (T)a00;
+    w.lo = (T)(a00 - (double)hi);
+    w.eh = t_exp<T>(hi);
+  }
+  dx = (T)((log10k - lkd[i]) * inv[i]);
+  const T del = w.lo + dyt * w.d01 + dx * (w.d10 + dyt * w.d11);
+  return w.eh * t_exp<T>(del) * (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+template <typename T>
+__device__ __forceinline__ void pw_acc(PWalk<T>& w, T g, T dx)
+{
+  w.acc0 += g * ((T)1 - dx);
+  w.acc1 += g * dx;
+}
+
+__device__ __forceinline__ void load_axis_d(const double* __restrict__ lk, int nk, double* lkd, double* inv)
+{
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    lkd[i] = lk[i];
+    inv[i] = (i + 1 < nk) ? 1.0 / (lk[i + 1] - lk[i]) : 0.0;
+  }
+}
+
+struct NodeD {
+  double F, lfk, dy, fK, a;
+  int j;
+};
+__device__ __forceinline__ NodeD node_d(const Params& P, int pt, int idx)
+{
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  NodeD n;
+  n.fK = node[(size_t)NF_FK * P.node_stride + idx];
+  n.F = node[(size_t)NF_WT * P.node_stride + idx] * node[(size_t)NF_DCHIDA * P.node_stride + idx] / (n.fK * n.fK);
+  n.lfk = log10(n.fK * CL2PT_COVERH0);
+  n.dy = node[(size_t)NF_DYZ * P.node_stride + idx];
+  n.a = node[(size_t)NF_A * P.node_stride + idx];
+  n.j = P.node_j[(size_t)pt * P.node_stride + idx];
+  return n;
+}
+
+// ------------------------------------------------------------------ ss
+// C_ss(l) = pref(l) sum_p F w_a w_b P  ->  lnP_bar, xb[pair][p] = sum_l pref C_bar P,
+// then w_bar_i(p) = F sum_{pairs with i} xb w_other.
+template <typename T>
+__global__ void k_vjp_ss(Params P, VJPParams V)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x;
+  const int p = threadIdx.x;
+  const int nn = P.n_ss, K = P.nnode_ss, np = P.pss, nk = P.pk_nk;
+  double* lkd = (double*)smem_raw;
+  double* inv = lkd + nk;
+  double* xb = inv + nk;            // [np][nn]
+  T* xt = (T*)(xb + (size_t)np * nn);  // [np][nn] chunk partial sums
+  T* w2 = xt + (size_t)np * nn;     // [np][nn] w_a w_b
+  T* cbs = w2 + (size_t)np * nn;    // [np][LC]
+  load_axis_d(P.pk_lk, nk, lkd, inv);
+  const double* w = P.wss + (size_t)pt * P.ns * nn;
+  for (int i = p; i < np * nn; i += blockDim.x) {
+    const int pr = i / nn, q = i - pr * nn;
+    xb[i] = 0.0;
+    xt[i] = (T)0;
+    w2[i] = (T)(w[P.z1[pr] * nn + q] * w[P.z2[pr] * nn + q]);
+  }
+  const bool act = p < nn;
+  NodeD nd{};
+  if (act) nd = node_d(P, pt, p);
+  const T Ft = (T)nd.F, dyt = (T)nd.dy;
+  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
+  const double* cb = V.cbar_ss + (size_t)pt * np * K;
+  PWalk<T> wk;
+  for (int L0 = 0; L0 < K; L0 += LC) {
+    const int nL = min(LC, K - L0);
+    __syncthreads();
+    for (int i = p; i < np * LC; i += blockDim.x) {
+      const int pr = i / LC, l = i - pr * LC;
+      cbs[i] = (l < nL) ? (T)cb[(size_t)pr * K + L0 + l] : (T)0;
+    }
+    __syncthreads();
+    if (!act) continue;
+    for (int l = 0; l < nL; l++) {
+      const int L = L0 + l;
+      T dx;
+      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, V.lfac_ss[2 * L] - nd.lfk, bar, dx);
+      const T pc = (T)V.lfac_ss[2 * L + 1] * Pv;
+      T pb = 0;
+      for (int pr = 0; pr < np; pr++) {
+        const T cv = cbs[pr * LC + l];
+        pb += cv * w2[pr * nn + p];
+        xt[pr * nn + p] += pc * cv;
+      }
+      pw_acc<T>(wk, pc * Ft * pb, dx);
+    }
+    for (int pr = 0; pr < np; pr++) {
+      xb[pr * nn + p] += (double)xt[pr * nn + p];
+      xt[pr * nn + p] = (T)0;
+    }
+  }
+  if (!act) return;
+  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  double* wb = V.wbar_ss + (size_t)pt * P.ns * nn;
+  for (int pr = 0; pr < np; pr++) {
+    const int a = P.z1[pr], b = P.z2[pr];
+    const double x = xb[pr * nn + p] * nd.F;
+    wb[a * nn + p] += x * w[b * nn + p];
+    wb[b * nn + p] += x * w[a * nn + p];
+  }
+}
+
+// ------------------------------------------------------------------ gs
+// C_gs(l) = pref2 sum_p F x_s (L + pref M) P; CTA = (point, lens q)
+template <typename T>
+__global__ void k_vjp_gs(Params P, VJPParams V)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int kk[CL2PT_MAXB], ss_[CL2PT_MAXB];
+  __shared__ int npq;
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const int p = threadIdx.x;
+  const int nn = P.n_ss, K = P.nnode_g, nk = P.pk_nk;
+  if (p == 0) {
+    int m = 0;
+    for (int k = 0; k < P.pgs; k++)
+      if (P.zl[k] == q) {
+        kk[m] = k;
+        ss_[m] = P.zs[k];
+        m++;
+      }
+    npq = m;
+  }
+  __syncthreads();
+  const int np = npq;
+  if (np == 0) return;
+  double* lkd = (double*)smem_raw;
+  double* inv = lkd + nk;
+  double* xs = inv + nk;               // [np][nn]
+  T* xt = (T*)(xs + (size_t)np * nn);  // [np][nn]
+  T* wxs = xt + (size_t)np * nn;       // [np][nn]
+  T* cbs = wxs + (size_t)np * nn;      // [np][LC]
+  load_axis_d(P.pk_lk, nk, lkd, inv);
+  const size_t b0 = (size_t)pt * P.nl + q;
+  const double* wx = P.wgs_x + b0 * P.ns * nn;
+  for (int i = p; i < np * nn; i += blockDim.x) {
+    const int m = i / nn, r = i - m * nn;
+    xs[i] = 0.0;
+    xt[i] = (T)0;
+    wxs[i] = (T)wx[ss_[m] * nn + r];
+  }
+  const bool act = p < nn;
+  const int off = P.n_ss + q * P.n_ss;
+  NodeD nd{};
+  double Lw = 0, Mw = 0;
+  if (act) {
+    nd = node_d(P, pt, off + p);
+    Lw = P.wgs_l[b0 * nn + p];
+    Mw = P.wgs_m[b0 * nn + p];
+  }
+  const T Ft = (T)nd.F, dyt = (T)nd.dy, Lt = (T)Lw, Mt = (T)Mw;
+  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
+  PWalk<T> wk;
+  double lb0 = 0.0, lb1 = 0.0;
+  for (int L0 = 0; L0 < K; L0 += LC) {
+    const int nL = min(LC, K - L0);
+    __syncthreads();
+    for (int i = p; i < np * LC; i += blockDim.x) {
+      const int m = i / LC, l = i - m * LC;
+      cbs[i] = (l < nL) ? (T)V.cbar_gs[((size_t)pt * P.pgs + kk[m]) * K + L0 + l] : (T)0;
+    }
+    __syncthreads();
+    if (!act) continue;
+    T t0 = 0, t1 = 0;
+    for (int l = 0; l < nL; l++) {
+      const int L = L0 + l;
+      const double* fac = V.lfac_g + 6 * L;
+      T dx;
+      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+      const T pref = (T)fac[2];
+      const T g = (T)fac[1] * Pv * Ft;
+      const T gl = g * (Lt + pref * Mt);
+      T sx = 0;
+      for (int m = 0; m < np; m++) {
+        const T cv = cbs[m * LC + l];
+        sx += cv * wxs[m * nn + p];
+        xt[m * nn + p] += gl * cv;
+      }
+      t0 += g * sx;
+      t1 += g * pref * sx;
+      pw_acc<T>(wk, gl * sx, dx);
+    }
+    lb0 += (double)t0;
+    lb1 += (double)t1;
+    for (int m = 0; m < np; m++) {
+      xs[m * nn + p] += (double)xt[m * nn + p];
+      xt[m * nn + p] = (T)0;
+    }
+  }
+  if (!act) return;
+  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  double* xbar = V.wbar_gx + b0 * P.ns * nn;
+  for (int m = 0; m < np; m++) xbar[ss_[m] * nn + p] += xs[m * nn + p];
+  V.lbar_gs[(b0 * 2 + 0) * nn + p] = lb0;
+  V.lbar_gs[(b0 * 2 + 1) * nn + p] = lb1;
+}
+
+// ------------------------------------------------------------------ gg
+template <typename T>
+__device__ __forceinline__ int hsearch_t(const T* __restrict__ x, int n, T v, int& h)
+{
+  int i = h;
+  if (!(i >= 0 && i <= n - 2 && x[i] <= v && (v < x[i + 1] || i == n - 2))) {
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+      const int mid = (lo + hi) >> 1;
+      if (x[mid] > v) hi = mid; else lo = mid;
+    }
+    i = lo;
+  }
+  h = i;
+  return i;
+}
+
+// C_gg(l) = sum_p F s(l, p)^2 P(l, p) (k_limber_gg's integrand); CTA =
+// (point, lens q), thread = gg node.  W_RSD at a_chi((l+3/2)/k) from
+// shared-memory copies of the point's distance/growth tables and the bin's
+// n(z) spline in the loop precision (the forward's tables and formulas),
+// with hinted searches (monotone in l for one node).
+template <typename T>
+__global__ void k_vjp_gg(Params P, VJPParams V)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const int p = threadIdx.x;
+  const int nn = P.n_gg, K = P.nnode_g, LNL = P.lmax_nolimber;
+  const int nk = P.pk_nk, nkl = P.pkl_nk;
+  const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
+  const bool nonlim = V.ggl_bar != nullptr;
+  double* lkd = (double*)smem_raw;
+  double* inv = lkd + nk;
+  double* lkdl = inv + nk;
+  double* invl = lkdl + nkl;
+  T* cx = (T*)(invl + nkl);
+  T* cz = cx + nc;
+  T* cdn = cz + nc;
+  T* cup = cdn + nc;
+  T* gv = cup + nc;
+  T* gs = gv + ng;
+  T* gz = gs + ng;
+  T* szc = gz + ng;
+  T* sy = szc + nzs;
+  T* sc = sy + nzs;
+  T* cbs = sc + nzs;       // [K] C_bar of this bin
+  T* gbs = cbs + K;        // [LNL][2] integer-l adjoints (non-Limber)
+  load_axis_d(P.pk_lk, nk, lkd, inv);
+  if (nonlim) load_axis_d(P.pkl_lk, nkl, lkdl, invl);
+  const double* Xg = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gg = P.G + (size_t)pt * P.G_nz;
+  const double* Z = P.chi_z;
+  for (int i = p; i < nc; i += blockDim.x) {
+    cx[i] = (T)Xg[i];
+    cz[i] = (T)Z[i];
+    if (i + 1 < nc) {
+      const int j2 = (i + 2 < nc) ? i + 2 : nc - 1;
+      cup[i] = (T)((Xg[j2] - Xg[i]) / (Z[j2] - Z[i]));
+      cdn[i] = (T)((i > 0) ? (Xg[i + 1] - Xg[i - 1]) / (Z[i + 1] - Z[i - 1]) : (Xg[i + 1] - Xg[i]) / (Z[i + 1] - Z[i]));
+    } else {
+      cup[i] = cdn[i] = (T)0;
+    }
+  }
+  for (int i = p; i < ng; i += blockDim.x) {
+    gv[i] = (T)Gg[i];
+    gz[i] = (T)P.G_z[i];
+    gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
+  }
+  for (int i = p; i < nzs; i += blockDim.x) {
+    szc[i] = (T)P.lens_zc[i];
+    sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
+    sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
+  }
+  const size_t b0 = (size_t)pt * P.nl + q;
+  for (int i = p; i < K; i += blockDim.x) cbs[i] = (T)V.cbar_gg[b0 * K + i];
+  if (nonlim)
+    for (int i = p; i < 2 * LNL; i += blockDim.x) gbs[i] = (T)V.ggl_bar[b0 * LNL * 2 + i];
+  __syncthreads();
+  if (p >= nn) return;
+  const int off = P.n_ss + P.nl * P.n_ss + q * nn;
+  const NodeD nd = node_d(P, pt, off + p);
+  const T Ft = (T)nd.F, dyt = (T)nd.dy;
+  const T Lt = (T)P.wgg_l[b0 * nn + p], Mt = (T)P.wgg_m[b0 * nn + p], r0 = (T)P.wgg_r0[b0 * nn + p];
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const T ldz = (T)nu.lens_dz[q], lst = (T)nu.lens_stretch[q], lzm = (T)P.zmean_lens[q];
+  const double chi_amin = P.chi_amin[pt];
+  const bool same_axis = P.G_same_axis != 0;
+  const T cH0 = (T)CL2PT_COVERH0;
+  const T fkc = (T)(nd.fK * CL2PT_COVERH0);
+  const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
+  int hc = 0, hz = 0, hg = 0, hn = 0;
+  // s(l, p) for the multipole factors fac = (log10 lp, pref2, pref, c0, c1, (lp+1)/lp)
+  auto s_of = [&](const double* fac) -> T {
+    const T c = fkc * (T)fac[5];
+    const int j = hsearch_t(cx, nc, c, hc);
+    const T dyc = (c - cx[j]) / (cx[j + 1] - cx[j]);
+    const T z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
+    int jc = j;
+    T dy2 = dyc;
+    if (!(cz[j] <= z1 && (z1 < cz[j + 1] || j == nc - 2))) {
+      jc = hsearch_t(cz, nc, z1, hz);
+      dy2 = (z1 - cz[jc]) / (cz[jc + 1] - cz[jc]);
+    }
+    const T H1 = cH0 / (cdn[jc] + dy2 * (cup[jc] - cdn[jc]));
+    int jg = jc;
+    T dyg = dy2;
+    if (!same_axis) {
+      jg = hsearch_t(gz, ng, z1, hg);
+      dyg = (z1 - gz[jg]) / (gz[jg + 1] - gz[jg]);
+    }
+    const T Gz = gv[jg] + dyg * (gv[jg + 1] - gv[jg]);
+    const T f1 = (T)1 - gs[jg] * ((T)1 + z1) / Gz;
+    const T zs = (z1 - ldz - lzm) / lst + lzm;
+    T n1 = (T)0;
+    if (!(zs <= szc[0] || zs >= szc[nzs - 1])) {
+      const int i = hsearch_t(szc, nzs, zs, hn);
+      const T h = szc[i + 1] - szc[i], t = zs - szc[i];
+      const T bq = (sy[i + 1] - sy[i]) / h - h * (sc[i + 1] + (T)2 * sc[i]) / (T)3;
+      const T dq = (sc[i + 1] - sc[i]) / ((T)3 * h);
+      n1 = (sy[i] + t * (bq + t * (sc[i] + t * dq))) / lst;
+    }
+    const T wrsd = (T)fac[3] * r0 - (T)fac[4] * n1 * H1 * f1;
+    return Lt + Mt * (T)fac[2] + wrsd;
+  };
+  PWalk<T> wk;
+  double lbar = 0.0;
+  for (int L0 = 0; L0 < K; L0 += LC) {
+    const int L1 = min(K, L0 + LC);
+    T lt = 0;
+    for (int L = L0; L < L1; L++) {
+      const double* fac = V.lfac_g + 6 * L;
+      if (nd.fK * fac[5] > chi_amin) continue;
+      const T cv = cbs[L];
+      if (cv == (T)0) continue;
+      const T s = s_of(fac);
+      T dx;
+      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+      const T sp = s * Ft * Pv;
+      lt += (T)2 * cv * sp;
+      pw_acc<T>(wk, cv * s * sp, dx);
+    }
+    lbar += (double)lt;
+  }
+  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  if (nonlim) {
+    // integer l < LNL: nonlinear and linear Limber C_gg of the hand-over
+    const double z = 1.0 / nd.a - 1.0;
+    const int jl = bsearch_d(P.pkl_z, P.pkl_nz, z);
+    const double dyl = (z - P.pkl_z[jl]) / (P.pkl_z[jl + 1] - P.pkl_z[jl]);
+    const T dylt = (T)dyl;
+    const double* tabl = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    PWalk<T> wn, wl;
+    hc = hz = hg = hn = 0;
+    T lt = 0;
+    for (int L = 0; L < LNL; L++) {
+      const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
+      if (cn == (T)0 && cl == (T)0) continue;
+      const double* fac = V.lfac_g + 6 * (K + L);
+      if (nd.fK * fac[5] > chi_amin) continue;
+      const T s = s_of(fac);
+      const double lk = fac[0] - nd.lfk;
+      T dx, dxl;
+      const T Pn = pw_eval<T>(wn, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, lk, bar, dx);
+      const T Pl = pw_eval<T>(wl, lkdl, invl, nkl, tabl, P.pkl_nz, jl, dyl, dylt, lk, barl, dxl);
+      const T sF = s * Ft;
+      lt += (T)2 * sF * (cn * Pn + cl * Pl);
+      pw_acc<T>(wn, cn * s * sF * Pn, dx);
+      pw_acc<T>(wl, cl * s * sF * Pl, dxl);
+    }
+    lbar += (double)lt;
+    pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
+    pw_flush(wl, barl, P.pkl_nz, jl, dyl);
+  }
+  V.lbar_gg[b0 * nn + p] = lbar;
+}
+
+template <typename T>
+size_t ss_smem(const Params& P)
+{
+  const size_t nn = P.n_ss, np = P.pss;
+  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) + 64;
+}
+template <typename T>
+size_t gs_smem(const Params& P)
+{
+  const size_t nn = P.n_ss, np = P.ns;
+  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) + 64;
+}
+template <typename T>
+size_t gg_smem(const Params& P)
+{
+  return 16 * ((size_t)P.pk_nk + P.pkl_nk) +
+         sizeof(T) * (4 * (size_t)P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz + P.nnode_g + 2 * P.lmax_nolimber) + 64;
+}
+
+template <typename T>
+void launch_t(const Params& P, const VJPParams& V, int which, cudaStream_t s)
+{
+  const int rnd = 32;
+  if (which == 0) {
+    const size_t sm = ss_smem<T>(P);
+    cudaFuncSetAttribute(k_vjp_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_vjp_ss<T><<<P.B, ((P.n_ss + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+  } else if (which == 1) {
+    const size_t sm = gs_smem<T>(P);
+    cudaFuncSetAttribute(k_vjp_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_vjp_gs<T><<<dim3(P.B, P.nl), ((P.n_ss + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+  } else {
+    const size_t sm = gg_smem<T>(P);
+    cudaFuncSetAttribute(k_vjp_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_vjp_gg<T><<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+  }
+}
+
+}  // namespace
+
+size_t vjp_limber_smem(const Params& P)
+{
+  size_t m = 0;
+  if (P.prec == CL2PT_PREC_FP64) {
+    m = std::max(ss_smem<double>(P), std::max(gs_smem<double>(P), gg_smem<double>(P)));
+  } else {
+    m = std::max(ss_smem<float>(P), std::max(gs_smem<float>(P), gg_smem<float>(P)));
+  }
+  return m;
+}
+
+void launch_vjp_limber(const Params& P, const VJPParams& V, int which, cudaStream_t s)
+{
+  if (P.prec == CL2PT_PREC_FP64) launch_t<double>(P, V, which, s);
+  else launch_t<float>(P, V, which, s);
+}
+
+}  // namespace cl2pt

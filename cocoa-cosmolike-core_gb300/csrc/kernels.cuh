@@ -62,9 +62,17 @@ struct VJPParams {
   double* cbar_w;          // [B][nl][LNL + nnode_g] adjoint of the w contraction columns
   double* ggl_bar;         // [B][nl][LNL][2] adjoint of the integer-l Limber C_gg (nonlinear, linear)
   double* cnl_bar;         // [B][nl][LNL] adjoint of the FFTLog C_l
+  // per-multipole constants of the plan: ss [nnode_ss][2] = (log10(l+1/2),
+  // l(l-1)(l+1)(l+2)/(l+1/2)^4); g [nnode_g + LNL][6] = (log10(l+1/2),
+  // sqrt((l-1)l(l+1)(l+2))/(l+1/2)^2, l(l+1)/(l+1/2)^2, RSD c0, RSD c1,
+  // (l+3/2)/(l+1/2)) on the C_l nodes, then at l = 0..LNL-1
+  const double* lfac_ss;
+  const double* lfac_g;
 };
 struct NLParams;
-size_t vjp_ss_smem(const Params& P);
+size_t vjp_limber_smem(const Params& P);
+// which: 0 ss, 1 gs, 2 gg (k_vjp_limber.cu)
+void launch_vjp_limber(const Params& P, const VJPParams& V, int which, cudaStream_t s);
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
                 const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
                 const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk);

@@ -488,6 +488,28 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dupload(p, &p->d_gl_gg_w, ggw.data(), ggw.size()));
   TRY(dupload(p, &p->d_ell_ss, ell_ss.data(), ell_ss.size()));
   TRY(dupload(p, &p->d_ell_g, ell_g.data(), ell_g.size()));
+  {
+    // per-multipole constants of the adjoint sweeps (VJPParams::lfac_*)
+    std::vector<double> fs(2 * ell_ss.size()), fg;
+    for (size_t i = 0; i < ell_ss.size(); i++) {
+      const double l = ell_ss[i], lp = l + 0.5;
+      fs[2 * i] = log10(lp);
+      fs[2 * i + 1] = l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp);
+    }
+    std::vector<double> lg(ell_g);
+    for (int l = 0; l < cfg->lmax_nolimber; l++) lg.push_back((double)l);
+    for (double l : lg) {
+      const double lp = l + 0.5, tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
+      fg.push_back(log10(lp));
+      fg.push_back(tmp > 0 ? sqrt(tmp) / (lp * lp) : 0.0);
+      fg.push_back(l * (l + 1.) / (lp * lp));
+      fg.push_back((1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.)));
+      fg.push_back(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
+      fg.push_back((lp + 1.0) / lp);
+    }
+    TRY(dupload(p, &p->d_lfac_ss, fs.data(), fs.size()));
+    TRY(dupload(p, &p->d_lfac_g, fg.data(), fg.size()));
+  }
   TRY(dupload(p, &p->d_filt_xi, fxi.data(), fxi.size()));
   TRY(dupload(p, &p->d_filt_gt, fgt.data(), fgt.size()));
   TRY(dupload(p, &p->d_filt_gg, fgg.data(), fgg.size()));
@@ -803,7 +825,7 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   const cl2pt_config& c = p->cfg;
   if (c.ia_model != CL2PT_IA_NLA || c.bias_model[0] != 0 || c.linear_pk || c.one_loop_bias)
     return CL2PT_ERR_UNSUPPORTED;
-  if (cl2pt::vjp_ss_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
+  if (cl2pt::vjp_limber_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
   if (!p->d_vjp_ws) {
     const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
@@ -939,6 +961,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.ggl_bar = w; w += (size_t)W * nl * LNL * 2;
     V0.cnl_bar = w;
     V0.mask = dmask;
+    V0.lfac_ss = p->d_lfac_ss;
+    V0.lfac_g = p->d_lfac_g;
   }
   int launches = 0;
   struct HookCtx { cl2pt_plan* p; cudaStream_t s; cudaEvent_t (*ev)(cl2pt_plan*); };

@@ -79,6 +79,8 @@ struct cl2pt_plan {
   double* d_vjp_cot = nullptr;         // [max_batch][n_total]
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]
   double* d_vjp_lnpl = nullptr;        // [max_batch][pkl_nk * pkl_nz]
+  double* d_lfac_ss = nullptr;         // per-multipole constants of the adjoint sweeps
+  double* d_lfac_g = nullptr;
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;

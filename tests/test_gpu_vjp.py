@@ -177,16 +177,21 @@ def test_vjp_mask_point_mass(gpu_lib):
 
 @pytest.mark.gpu
 def test_vjp_mixed_plan_matches_fp64(gpu_lib):
-    """The adjoint kernels are FP64 in both plans; the mixed plan's forward
-    (which feeds the m-bias gradient) is within the 1e-4 bar."""
+    """The mixed plan's adjoint (FP32 per-(l, node) arithmetic, FP64
+    accumulators) against the FP64 plan's: 1e-5 of the largest entry for the
+    table gradient, 1e-5 relative for the nuisance gradient."""
     w, tabs, nus, p64 = setup_case(abi.IA_REDSHIFT_EVOLUTION)
     pmx = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=len(tabs))
     om, h0, chi, G, lnP = workloads.stack(tabs)
     v = np.random.default_rng(9).normal(size=(len(tabs), p64.n_total))
     _, l64, n64 = p64.vjp_real(om, h0, chi, G, lnP, nus, v)
     _, lmx, nmx = pmx.vjp_real(om, h0, chi, G, lnP, nus, v)
-    assert np.max(np.abs(lmx - l64)) <= 1e-10 * np.max(np.abs(l64))
-    assert np.max(np.abs(nmx - n64)) <= 1e-4 * np.max(np.abs(n64))
+    err_l = np.max(np.abs(lmx - l64)) / np.max(np.abs(l64))
+    keep = n64 != 0
+    err_n = np.max(np.abs(nmx[keep] - n64[keep]) / np.abs(n64[keep]))
+    print("mixed vs FP64 adjoint:", err_l, err_n)
+    assert err_l <= 1e-5 and err_n <= 1e-5
+    assert np.all(nmx[~keep] == 0)
 
 
 @pytest.mark.gpu
