@@ -203,6 +203,21 @@ __device__ __forceinline__ double spline_d(const double* __restrict__ x,
   return y[i] + t * (b + t * (ci + t * d));
 }
 
+// derivative of the same spline (d/dv)
+__device__ __forceinline__ double spline_deriv_d(const double* __restrict__ x,
+                                                 const double* __restrict__ y,
+                                                 const double* __restrict__ c, int n, double v)
+{
+  const int i = bsearch_d(x, n, v);
+  const double h = x[i + 1] - x[i];
+  const double dy = y[i + 1] - y[i];
+  const double t = v - x[i];
+  const double ci = c[i], ci1 = c[i + 1];
+  const double b = dy / h - h * (ci1 + 2.0 * ci) / 3.0;
+  const double d = (ci1 - ci) / (3.0 * h);
+  return b + t * (2.0 * ci + 3.0 * t * d);
+}
+
 // nz_source_photoz evaluation: redshift_spline.c:523-536
 __device__ __forceinline__ double nz_source_d(const Params& P, double zz, int nj, double dz)
 {
@@ -210,6 +225,15 @@ __device__ __forceinline__ double nz_source_d(const Params& P, double zz, int nj
   if (zz < P.src_zc[0] || zz > P.src_zc[P.src_nz - 1]) return 0.0;
   return spline_d(P.src_zc, P.src_y + (nj + 1) * P.src_nz, P.src_c + (nj + 1) * P.src_nz,
                   P.src_nz, zz);
+}
+
+// d/d(dz) of nz_source_d: -n'(zz - dz) inside the spline range, 0 outside
+__device__ __forceinline__ double nz_source_ddz_d(const Params& P, double zz, int nj, double dz)
+{
+  zz = zz - dz;
+  if (zz < P.src_zc[0] || zz > P.src_zc[P.src_nz - 1]) return 0.0;
+  return -spline_deriv_d(P.src_zc, P.src_y + (nj + 1) * P.src_nz, P.src_c + (nj + 1) * P.src_nz,
+                         P.src_nz, zz);
 }
 
 // nz_lens_photoz evaluation: redshift_spline.c:740-760
@@ -233,6 +257,17 @@ __device__ __forceinline__ double interpol1d_d(const double* f, int n, double a,
   const int i = (int)floor(r);
   if (i + 1 >= n) return f[n - 1];
   return (r - i) * (f[i + 1] - f[i]) + f[i];
+}
+
+// g_tomo / g_lens lookup: interpol1d on the coarse table
+__device__ __forceinline__ double g_lookup(const double* tab, int n_a, double amin, double a,
+                                           bool open_lo)
+{
+  const double amax = 0.999999;
+  const double dac = (amax - amin) / ((double)n_a - 1.0);
+  if (open_lo ? (a <= amin) : (a < amin)) return 0.0;
+  if (a > 1.0 - dac) return 0.0;
+  return interpol1d_d(tab, n_a, amin, dac, a);
 }
 
 // p_lin / p_nonlin: cosmo3D.c:306-417, FP64

@@ -52,13 +52,18 @@ __device__ __forceinline__ double n_of_z_bin(const Params& P, const cl2pt_nuisan
 // x points into tab[0..n_a-1].  tab[0] is set by the caller.
 constexpr int GT_NT = 256;
 
-__global__ void __launch_bounds__(GT_NT) k_gtab(Params P)
+// DZ: the tangent of the source tables with respect to the bin's photo-z
+// shift (the trapezoid sums are linear in n, so n is replaced by
+// d n(z - dz)/d dz); written to dz_out [B][ns][n_a], source bins only.
+template <bool DZ>
+__global__ void __launch_bounds__(GT_NT) k_gtab(Params P, double* dz_out)
 {
   const int pt = blockIdx.x;
   const int bin = blockIdx.y;
   const int lens = bin >= P.ns;
   const int b = lens ? bin - P.ns : bin;
   const cl2pt_nuisance& nu = P.nu[pt];
+  if (DZ && lens) return;
   if (lens) {
     // g_lens is only needed by magnification terms (W_mag x bmag); skip
     // the bins whose magnification bias is zero.
@@ -70,8 +75,9 @@ __global__ void __launch_bounds__(GT_NT) k_gtab(Params P)
   const double amax = 0.999999;
   const double amin = 1.0 / ((lens ? P.lens_zmax_all : P.src_zmax_all) + 1.0);
   const double da = (amax - amin) / ((double)Na - 1.0);
-  double* tab = (lens ? P.glens + ((size_t)pt * P.nl + b) * P.n_a
-                      : P.gsrc + ((size_t)pt * P.ns + b) * P.n_a);
+  double* tab = DZ ? dz_out + ((size_t)pt * P.ns + b) * P.n_a
+                  : (lens ? P.glens + ((size_t)pt * P.nl + b) * P.n_a
+                          : P.gsrc + ((size_t)pt * P.ns + b) * P.n_a);
   __shared__ double sh[32];
   __shared__ double carry[3];
   double P0 = 0.0, Q0 = 0.0;
@@ -123,7 +129,8 @@ __global__ void __launch_bounds__(GT_NT) k_gtab(Params P)
     if (i < Na) {
       const double a = amin + i * da;
       c = chi_all_d(P.chi_z, X, P.chi_nz, a).chi;
-      fP = n_of_z_bin(P, nu, lens, b, 1. / a - 1.) / (a * a);
+      fP = (DZ ? nz_source_ddz_d(P, 1. / a - 1., b, nu.src_dz[b]) : n_of_z_bin(P, nu, lens, b, 1. / a - 1.)) /
+           (a * a);
       fQ = fP / c;
     }
     // neighbour value f[i-1]
@@ -153,17 +160,6 @@ __global__ void __launch_bounds__(GT_NT) k_gtab(Params P)
     prevQ = lastf[1];
     __syncthreads();
   }
-}
-
-// g_tomo / g_lens lookup: interpol1d on the coarse table
-__device__ __forceinline__ double g_lookup(const double* tab, int n_a, double amin, double a,
-                                           bool open_lo)
-{
-  const double amax = 0.999999;
-  const double dac = (amax - amin) / ((double)n_a - 1.0);
-  if (open_lo ? (a <= amin) : (a < amin)) return 0.0;
-  if (a > 1.0 - dac) return 0.0;
-  return interpol1d_d(tab, n_a, amin, dac, a);
 }
 
 __device__ double gb1_d(const Params& P, const cl2pt_nuisance& nu, double z, int ni, double g1,
@@ -394,13 +390,18 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 {
   dim3 g1(P.B, P.ns + P.nl);
   hk(CL2PT_K_GTAB, 1);
-  k_gtab<<<g1, GT_NT, 0, s>>>(P);
+  k_gtab<false><<<g1, GT_NT, 0, s>>>(P, nullptr);
   hk(CL2PT_K_GTAB, 0);
   dim3 g2(P.B, 1 + 2 * P.nl);
   hk(CL2PT_K_NODES, 1);
   k_nodes<<<g2, ND_NT, 0, s>>>(P);
   hk(CL2PT_K_NODES, 0);
   *launches += 2;
+}
+
+void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s)
+{
+  k_gtab<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out);
 }
 
 }  // namespace cl2pt

@@ -65,10 +65,30 @@ __global__ void k_vjp_assemble(Params P, VJPParams V)
       }
     } else if (i < n_xi + n_gt) {
       if (P.probes & CL2PT_PROBE_GAMMAT) {
-        const int zs = P.zs[(i - n_xi) / nt];
+        const int r = i - n_xi, pr = r / nt, it = r - pr * nt;
+        const int zs = P.zs[pr];
         const double c = 1.0 + nu.shear_m[zs];
         b = vi * c;
         if (vi != 0.0) atomicAdd(mbar + zs, vi * dv[i] / c);
+        if (vi != 0.0 && V.pm) {
+          // point-mass term (PointMass::get_pm, generic_interface.cpp:2626-2641):
+          // linear in g_tomo(a_lens), so its photo-z derivative reads the
+          // tangent table
+          const int zl = P.zl[pr];
+          const double lv = log(P.theta_min_rad), dt = (log(P.theta_max_rad) - lv) / nt;
+          const double tmin = exp(lv + it * dt), tmax = exp(lv + (it + 1.) * dt);
+          const double th = (2. / 3.) * (tmax * tmax * tmax - tmin * tmin * tmin) / (tmax * tmax - tmin * tmin);
+          const double al = 1.0 / (1.0 + P.zmean_lens[zl]);
+          const double* X = P.chi + (size_t)pt * P.chi_nz;
+          const double cl = chi_all_d(P.chi_z, X, P.chi_nz, al).chi;
+          const double amin = 1.0 / (P.src_zmax_all + 1.0), amax = 0.999999;
+          const double dac = (amax - amin) / ((double)P.n_a - 1.0);
+          const double* dg = V.dgsrc + ((size_t)pt * P.ns + zs) * P.n_a;
+          const double dgv = (al <= amin || al > 1.0 - dac) ? 0.0 : interpol1d_d(dg, P.n_a, amin, dac, al);
+          const double d = 4 * M_PI * 1.6e-23 * V.pm[(size_t)pt * P.nl + zl] * 1.e+13 * dgv / (th * th) /
+                           (cl * al * al * al);
+          atomicAdd(&V.nu_bar[pt].src_dz[zs], vi * c * d);
+        }
       }
     } else {
       if (P.probes & CL2PT_PROBE_WTHETA) b = vi;
@@ -208,33 +228,50 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
   const int off = (set == 0) ? 0 : P.n_ss + q * P.n_ss;
   const double* wb =
       (set == 0) ? V.wbar_ss + (size_t)pt * P.ns * nn : V.wbar_gx + ((size_t)pt * P.nl + q) * P.ns * nn;
-  if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING || P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) {
-    for (int s = 0; s < P.ns; s++) {
-      double dA = 0.0, dE = 0.0;
-      for (int p = threadIdx.x; p < nn; p += blockDim.x) {
-        const double a = node[(size_t)NF_A * P.node_stride + off + p];
-        const double D = node[(size_t)NF_D * P.node_stride + off + p];
-        const double H = node[(size_t)NF_H * P.node_stride + off + p];
-        const double WS = nz_source_d(P, 1. / a - 1., s, nu.src_dz[s]) * H;
-        const double t = -wb[s * nn + p] * WS * (om * 0.01389 / D);
+  const bool ia = P.ia_mode == CL2PT_IA_REDSHIFT_BINNING || P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION;
+  const double amin_src = 1.0 / (P.src_zmax_all + 1.0);
+  for (int s = 0; s < P.ns; s++) {
+    // w = W_K - W_S C1: d/dA1 (and eta) through C1, d/d(dz_s) through
+    // W_K (tangent g table) and W_S (n'(z - dz))
+    double dA = 0.0, dE = 0.0, dZ = 0.0;
+    const double* dg = V.dgsrc + ((size_t)pt * P.ns + s) * P.n_a;
+    for (int p = threadIdx.x; p < nn; p += blockDim.x) {
+      const double a = node[(size_t)NF_A * P.node_stride + off + p];
+      const double D = node[(size_t)NF_D * P.node_stride + off + p];
+      const double H = node[(size_t)NF_H * P.node_stride + off + p];
+      const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+      const double z = 1. / a - 1.;
+      const double wbar = wb[s * nn + p];
+      double A = 0.0, e = 1.0;
+      if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) A = nu.ia[0][s];
+      else if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) {
+        e = pow((1.0 / a) / 1.62, nu.ia[0][1]);
+        A = nu.ia[0][0] * e;
+      }
+      const double ca = om * 0.01389 / D;
+      const double dWK = 1.5 * om * fK / a * g_lookup(dg, P.n_a, amin_src, a, true);
+      const double dWS = nz_source_ddz_d(P, z, s, nu.src_dz[s]) * H;
+      dZ += wbar * (dWK - dWS * A * ca);
+      if (ia) {
+        const double t = -wbar * nz_source_d(P, z, s, nu.src_dz[s]) * H * ca;
         if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
           dA += t;
         } else {
-          const double r = (1.0 / a) / 1.62;
-          const double e = pow(r, nu.ia[0][1]);
           dA += t * e;
-          dE += t * nu.ia[0][0] * e * log(r);
+          dE += t * nu.ia[0][0] * e * log((1.0 / a) / 1.62);
         }
       }
-      const double sA = block_sum_d(dA, red);
-      const double sE = block_sum_d(dE, red);
-      if (threadIdx.x == 0) {
-        if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
-          atomicAdd(&g.ia[0][s], sA);
-        } else {
-          atomicAdd(&g.ia[0][0], sA);
-          atomicAdd(&g.ia[0][1], sE);
-        }
+    }
+    const double sZ = block_sum_d(dZ, red);
+    const double sA = block_sum_d(dA, red);
+    const double sE = block_sum_d(dE, red);
+    if (threadIdx.x == 0) {
+      atomicAdd(&g.src_dz[s], sZ);
+      if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
+        atomicAdd(&g.ia[0][s], sA);
+      } else if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) {
+        atomicAdd(&g.ia[0][0], sA);
+        atomicAdd(&g.ia[0][1], sE);
       }
     }
   }
@@ -261,6 +298,8 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
   const int nt = P.ntheta;
   const int n_total = nt * (2 * P.pss + P.pgs + P.nl);
   hk(CL2PT_K_VJP, 1);
+  launch_gtab_dz(P, V.dgsrc, s);
+  (*launches)++;
   k_vjp_assemble<<<dim3((n_total + 255) / 256, P.B), 256, 0, s>>>(P, V);
   (*launches)++;
   if (P.probes & CL2PT_PROBE_XI) {

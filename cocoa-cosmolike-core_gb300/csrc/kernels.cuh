@@ -68,7 +68,13 @@ struct VJPParams {
   // (l+3/2)/(l+1/2)) on the C_l nodes, then at l = 0..LNL-1
   const double* lfac_ss;
   const double* lfac_g;
+  // source photo-z: d g_tomo / d dz_s [B][ns][n_a], and the wave's point
+  // masses [B][nl] (or null)
+  double* dgsrc;
+  const double* pm;
 };
+// the photo-z tangent of the source lens-efficiency tables (k_setup.cu)
+void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s);
 struct NLParams;
 size_t vjp_limber_smem(const Params& P);
 // which: 0 ss, 1 gs, 2 gg (k_vjp_limber.cu)

@@ -832,7 +832,8 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
     const size_t LNL = c.lmax_nolimber;
     const size_t nws = W * p->n_total + W * p->pss * p->nnode_ss + W * p->pgs * p->nnode_g +
                        W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
-                       W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL;
+                       W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL +
+                       W * ns * c.n_a;
     // (a failed allocation leaves the plan usable for evaluation)
     int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
     if (!a) a = dalloc(p, &p->d_vjp_lnp, (size_t)p->max_batch * p->P.pk_nk * p->P.pk_nz);
@@ -959,7 +960,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     const int LNL = p->cfg.lmax_nolimber;
     V0.cbar_w = w; w += (size_t)W * nl * (LNL + p->nnode_g);
     V0.ggl_bar = w; w += (size_t)W * nl * LNL * 2;
-    V0.cnl_bar = w;
+    V0.cnl_bar = w; w += (size_t)W * nl * LNL;
+    V0.dgsrc = w;
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
     V0.lfac_g = p->d_lfac_g;
@@ -1064,6 +1066,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         V.lnp_bar = vlnp + (size_t)w0 * nP;
         V.lnpl_bar = vlnpl + (size_t)w0 * (sep_lin ? nPL : nP);
         V.nu_bar = vnu + w0;
+        V.pm = dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr;
         cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl,
                           p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       }

@@ -119,10 +119,11 @@ int cl2pt_fourier_sizes(const cl2pt_plan* plan, int nell, int* n_ss, int* n_gs,
  *                                  Limber w) are part of lnP_bar and lnPL_bar
  *                                  may be NULL
  *   nu_bar   [n]                   the nuisance gradient in the cl2pt_nuisance
- *                                  layout: shear_m, gb[0] (b1) and ia[0] (A1
- *                                  per source bin in redshift-binning mode;
- *                                  A1 and eta in ia[0][0..1] in redshift-
- *                                  evolution mode); other fields 0.
+ *                                  layout: shear_m, src_dz (source photo-z
+ *                                  shifts), gb[0] (b1) and ia[0] (A1 per
+ *                                  source bin in redshift-binning mode; A1 and
+ *                                  eta in ia[0][0..1] in redshift-evolution
+ *                                  mode); other fields 0.
  * Every pointer follows batch->where.  The reference has no derivatives;
  * this replaces the central finite differences a caller would take of
  * compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159).  The

@@ -5,8 +5,8 @@ For a seeded cotangent v, the scalar f = v . dv is differentiated
   * on the GPU: central differences of the FP64 plan's forward,
   * on the CPU: central differences of the FP64 oracle (the restatement of
     the reference C path),
-with respect to the shear m-bias, b1, the NLA amplitude and its redshift
-power, and the P(k, z) table (a dense random direction and single entries).
+with respect to the shear m-bias, the source photo-z shifts, b1, the NLA
+amplitude and its redshift power, and the P(k, z) table (a dense random direction and single entries).
 Step: 1e-4 relative (1e-4 absolute in lnP).  Every quantity here is smooth
 in the parameters (the bilinear table walk is linear in the table values;
 b1 and A1 enter polynomially), so the analytic gradient must match the
@@ -62,6 +62,7 @@ def flat_index(field, i, j=None):
 
 def param_list(w, ia_mode):
     ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
+    ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
     ps += [("gb", 0, q) for q in range(w.cfg.n_lens)]
     if ia_mode == abi.IA_REDSHIFT_EVOLUTION:
         ps += [("ia", 0, 0), ("ia", 0, 1)]
@@ -209,7 +210,8 @@ def test_vjp_vs_oracle_fd(gpu_lib, oracle_built):
     o.setup(w.cfg, w.src, w.lens)
     import dataclasses
     worst = 0.0
-    for field, i, j in [("shear_m", 0, None), ("shear_m", 3, None), ("gb", 0, 1), ("ia", 0, 0), ("ia", 0, 1)]:
+    for field, i, j in [("shear_m", 0, None), ("shear_m", 3, None), ("src_dz", 1, None), ("src_dz", 3, None),
+                        ("gb", 0, 1), ("ia", 0, 0), ("ia", 0, 1)]:
         x0 = nu_get(nus[0], field, i, j)
         h = H * max(abs(x0), 0.1)
         f = []
