@@ -230,10 +230,18 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
       (set == 0) ? V.wbar_ss + (size_t)pt * P.ns * nn : V.wbar_gx + ((size_t)pt * P.nl + q) * P.ns * nn;
   const bool ia = P.ia_mode == CL2PT_IA_REDSHIFT_BINNING || P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION;
   const double amin_src = 1.0 / (P.src_zmax_all + 1.0);
+  const double* wbb = (set == 0) ? V.wbar_ssb + (size_t)pt * P.ns * nn
+                                  : V.wbar_gsb + ((size_t)pt * P.nl + q) * P.ns * nn;
+  const double* wb2 = (set == 0) ? V.wbar_ss2 + (size_t)pt * P.ns * nn
+                                 : V.wbar_gs2 + ((size_t)pt * P.nl + q) * P.ns * nn;
+  const double* wbk = (set == 0) ? nullptr : V.wbar_gsk + ((size_t)pt * P.nl + q) * P.ns * nn;
+  const bool tatt = P.tatt != 0, kterm = set > 0 && P.one_loop;
   for (int s = 0; s < P.ns; s++) {
     // w = W_K - W_S C1: d/dA1 (and eta) through C1, d/d(dz_s) through
-    // W_K (tangent g table) and W_S (n'(z - dz))
-    double dA = 0.0, dE = 0.0, dZ = 0.0;
+    // W_K (tangent g table) and W_S (n'(z - dz)); with TATT also
+    // W_S C1 b_TA D^2 and W_S C2 D^2 (IA.c:238-415), and W_K alone in the
+    // one-loop gs term
+    double dA = 0.0, dE = 0.0, dZ = 0.0, dA2 = 0.0, dE2 = 0.0, dBT = 0.0;
     const double* dg = V.dgsrc + ((size_t)pt * P.ns + s) * P.n_a;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p];
@@ -252,26 +260,74 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
       const double dWK = 1.5 * om * fK / a * g_lookup(dg, P.n_a, amin_src, a, true);
       const double dWS = nz_source_ddz_d(P, z, s, nu.src_dz[s]) * H;
       dZ += wbar * (dWK - dWS * A * ca);
+      const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
+      const double lr = log((1.0 / a) / 1.62);
       if (ia) {
-        const double t = -wbar * nz_source_d(P, z, s, nu.src_dz[s]) * H * ca;
+        const double t = -wbar * WS * ca;
         if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
           dA += t;
         } else {
           dA += t * e;
-          dE += t * nu.ia[0][0] * e * log((1.0 / a) / 1.62);
+          dE += t * nu.ia[0][0] * e * lr;
         }
+      }
+      if (kterm) dZ += wbk[s * nn + p] * dWK;
+      if (tatt && ia) {
+        const double bb = wbb[s * nn + p], cb = wb2[s * nn + p];
+        const double D2 = D * D, c2a = om * 0.01389 / D2;
+        double bTA, A2, e2 = 1.0;
+        if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
+          bTA = nu.ia[2][s];
+          A2 = nu.ia[1][s];
+        } else {
+          bTA = nu.ia[2][0];
+          e2 = pow(1.0 / (a * 1.62), nu.ia[1][1]);
+          A2 = nu.ia[1][0] * e2;
+        }
+        const double C1 = A * ca, C2 = A2 * c2a;
+        // W_S C1 b_TA D^2
+        const double tb = bb * WS * ca * bTA * D2;
+        if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
+          dA += tb;
+        } else {
+          dA += tb * e;
+          dE += tb * nu.ia[0][0] * e * lr;
+        }
+        dBT += bb * WS * C1 * D2;
+        dZ += bb * dWS * C1 * bTA * D2;
+        // W_S C2 D^2
+        const double tc = cb * WS * c2a * D2;
+        if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
+          dA2 += tc;
+        } else {
+          dA2 += tc * e2;
+          dE2 += tc * nu.ia[1][0] * e2 * lr;
+        }
+        dZ += cb * dWS * C2 * D2;
       }
     }
     const double sZ = block_sum_d(dZ, red);
     const double sA = block_sum_d(dA, red);
     const double sE = block_sum_d(dE, red);
+    const double sA2 = tatt ? block_sum_d(dA2, red) : 0.0;
+    const double sE2 = tatt ? block_sum_d(dE2, red) : 0.0;
+    const double sBT = tatt ? block_sum_d(dBT, red) : 0.0;
     if (threadIdx.x == 0) {
       atomicAdd(&g.src_dz[s], sZ);
       if (P.ia_mode == CL2PT_IA_REDSHIFT_BINNING) {
         atomicAdd(&g.ia[0][s], sA);
+        if (tatt) {
+          atomicAdd(&g.ia[1][s], sA2);
+          atomicAdd(&g.ia[2][s], sBT);
+        }
       } else if (P.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) {
         atomicAdd(&g.ia[0][0], sA);
         atomicAdd(&g.ia[0][1], sE);
+        if (tatt) {
+          atomicAdd(&g.ia[1][0], sA2);
+          atomicAdd(&g.ia[1][1], sE2);
+          atomicAdd(&g.ia[2][0], sBT);
+        }
       }
     }
   }
@@ -302,15 +358,28 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
   (*launches)++;
   k_vjp_assemble<<<dim3((n_total + 255) / 256, P.B), 256, 0, s>>>(P, V);
   (*launches)++;
+  if (P.one_loop) {
+    launch_vjp_extra(P, V, -1, s);
+    (*launches)++;
+  }
   if (P.probes & CL2PT_PROBE_XI) {
-    k_vjp_contract<<<dim3((P.nnode_ss + 127) / 128, P.B * P.pss), 128, 0, s>>>(P, V, filt_xi, 0, P.nnode_ss);
+    const int Kx = (P.tatt ? 2 : 1) * P.nnode_ss;
+    k_vjp_contract<<<dim3((Kx + 127) / 128, P.B * P.pss), 128, 0, s>>>(P, V, filt_xi, 0, Kx);
     launch_vjp_limber(P, V, 0, s);
     *launches += 2;
+    if (P.tatt) {
+      launch_vjp_extra(P, V, 0, s);
+      (*launches)++;
+    }
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
     k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.pgs), 128, 0, s>>>(P, V, filt_gt, 1, P.nnode_g);
     launch_vjp_limber(P, V, 1, s);
     *launches += 2;
+    if (P.tatt || P.one_loop) {
+      launch_vjp_extra(P, V, 1, s);
+      (*launches)++;
+    }
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
     if (P.adopt_limber_gg) {
@@ -319,11 +388,19 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
       V2.ggl_bar = nullptr;
       launch_vjp_limber(P, V2, 2, s);
       *launches += 2;
+      if (P.one_loop) {
+        launch_vjp_extra(P, V2, 2, s);
+        (*launches)++;
+      }
     } else {
       const int Kw = P.lmax_nolimber + P.nnode_g;
       k_vjp_contract<<<dim3((Kw + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg_nl, 3, Kw);
       k_vjp_handover<<<dim3(P.B, P.nl), 256, 0, s>>>(P, V);
       launch_vjp_limber(P, V, 2, s);
+      if (P.one_loop) {
+        launch_vjp_extra(P, V, 2, s);
+        (*launches)++;
+      }
       launch_nonlimber_vjp(P, Q, V.cnl_bar, V.lnpl_bar, V.nu_bar, s, launches);
       *launches += 3;
     }

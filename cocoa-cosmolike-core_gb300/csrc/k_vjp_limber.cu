@@ -140,14 +140,15 @@ __global__ void k_vjp_ss(Params P, VJPParams V)
   const T Ft = (T)nd.F, dyt = (T)nd.dy;
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
-  const double* cb = V.cbar_ss + (size_t)pt * np * K;
+  const int Kx = (P.tatt ? 2 : 1) * K;  // with TATT the rows hold [EE; BB]
+  const double* cb = V.cbar_ss + (size_t)pt * np * Kx;
   PWalk<T> wk;
   for (int L0 = 0; L0 < K; L0 += LC) {
     const int nL = min(LC, K - L0);
     __syncthreads();
     for (int i = p; i < np * LC; i += blockDim.x) {
       const int pr = i / LC, l = i - pr * LC;
-      cbs[i] = (l < nL) ? (T)cb[(size_t)pr * K + L0 + l] : (T)0;
+      cbs[i] = (l < nL) ? (T)cb[(size_t)pr * Kx + L0 + l] : (T)0;
     }
     __syncthreads();
     if (!act) continue;

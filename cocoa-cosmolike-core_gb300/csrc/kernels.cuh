@@ -72,7 +72,16 @@ struct VJPParams {
   // masses [B][nl] (or null)
   double* dgsrc;
   const double* pm;
+  // TATT / one-loop bias (k_vjp_extra.cu): adjoints of W_S C1 b_TA D^2 and
+  // W_S C2 D^2 at the ss nodes [B][ns][n_ss] and at the gs nodes (and of W_K
+  // there) [B][nl][ns][n_ss]; coefficient sums [B][5][pss][n_ss]; the
+  // per-point one-loop gate [B]
+  double *wbar_ssb, *wbar_ss2, *wbar_gsb, *wbar_gs2, *wbar_gsk, *cx_ss;
+  int* one_loop_on;
 };
+size_t vjp_extra_smem(const Params& P);
+// which: 0 ss, 1 gs, 2 gg, -1 the one-loop gate (k_vjp_extra.cu)
+void launch_vjp_extra(const Params& P, const VJPParams& V, int which, cudaStream_t s);
 // the photo-z tangent of the source lens-efficiency tables (k_setup.cu)
 void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s);
 struct NLParams;

@@ -823,17 +823,19 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   if (st) return st;
   if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
   const cl2pt_config& c = p->cfg;
-  if (c.ia_model != CL2PT_IA_NLA || c.bias_model[0] != 0 || c.linear_pk || c.one_loop_bias)
+  if (c.bias_model[0] != 0 || c.bias_model[1] != 0 || c.bias_model[2] != 0 || c.linear_pk)
     return CL2PT_ERR_UNSUPPORTED;
   if (cl2pt::vjp_limber_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
+  if ((p->P.tatt || p->P.one_loop) && cl2pt::vjp_extra_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
   if (!p->d_vjp_ws) {
     const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
     const size_t LNL = c.lmax_nolimber;
-    const size_t nws = W * p->n_total + W * p->pss * p->nnode_ss + W * p->pgs * p->nnode_g +
+    const size_t nws = W * p->n_total + 2 * W * p->pss * p->nnode_ss + W * p->pgs * p->nnode_g +
                        W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
                        W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL +
-                       W * ns * c.n_a;
+                       W * ns * c.n_a + 2 * W * ns * p->n_ss + 3 * W * nl * ns * p->n_ss +
+                       5 * W * p->pss * p->n_ss + W;
     // (a failed allocation leaves the plan usable for evaluation)
     int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
     if (!a) a = dalloc(p, &p->d_vjp_lnp, (size_t)p->max_batch * p->P.pk_nk * p->P.pk_nz);
@@ -947,10 +949,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     CUDA_OK(cudaMemsetAsync(vlnp, 0, (size_t)n * nP * sizeof(double), s));
     if (sep_lin) CUDA_OK(cudaMemsetAsync(vlnpl, 0, (size_t)n * nPL * sizeof(double), s));
     CUDA_OK(cudaMemsetAsync(vnu, 0, (size_t)n * sizeof(cl2pt_nuisance), s));
-    const int W = p->wave, ns = p->cfg.n_source, nl = p->cfg.n_lens;
+    const int W = p->wave, ns = p->cfg.n_source, nl = p->cfg.n_lens, c_na = p->cfg.n_a;
     double* w = p->d_vjp_ws;
     V0.obs_bar = w; w += (size_t)W * n_total;
-    V0.cbar_ss = w; w += (size_t)W * p->pss * p->nnode_ss;
+    V0.cbar_ss = w; w += (size_t)2 * W * p->pss * p->nnode_ss;
     V0.cbar_gs = w; w += (size_t)W * p->pgs * p->nnode_g;
     V0.cbar_gg = w; w += (size_t)W * nl * p->nnode_g;
     V0.wbar_ss = w; w += (size_t)W * ns * p->n_ss;
@@ -961,7 +963,14 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.cbar_w = w; w += (size_t)W * nl * (LNL + p->nnode_g);
     V0.ggl_bar = w; w += (size_t)W * nl * LNL * 2;
     V0.cnl_bar = w; w += (size_t)W * nl * LNL;
-    V0.dgsrc = w;
+    V0.dgsrc = w; w += (size_t)W * ns * c_na;
+    V0.wbar_ssb = w; w += (size_t)W * ns * p->n_ss;
+    V0.wbar_ss2 = w; w += (size_t)W * ns * p->n_ss;
+    V0.wbar_gsb = w; w += (size_t)W * nl * ns * p->n_ss;
+    V0.wbar_gs2 = w; w += (size_t)W * nl * ns * p->n_ss;
+    V0.wbar_gsk = w; w += (size_t)W * nl * ns * p->n_ss;
+    V0.cx_ss = w; w += (size_t)5 * W * p->pss * p->n_ss;
+    V0.one_loop_on = (int*)w;
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
     V0.lfac_g = p->d_lfac_g;
@@ -1060,6 +1069,13 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         const int ns = p->cfg.n_source, nl = p->cfg.n_lens;
         CUDA_OK(cudaMemsetAsync(V0.wbar_ss, 0, sizeof(double) * (size_t)P.B * ns * p->n_ss, s));
         CUDA_OK(cudaMemsetAsync(V0.wbar_gx, 0, sizeof(double) * (size_t)P.B * nl * ns * p->n_ss, s));
+        if (P.tatt || P.one_loop) {
+          const size_t a1 = sizeof(double) * (size_t)P.B * ns * p->n_ss;
+          const size_t a2 = sizeof(double) * (size_t)P.B * nl * ns * p->n_ss;
+          for (double* q : {V0.wbar_ssb, V0.wbar_ss2}) CUDA_OK(cudaMemsetAsync(q, 0, a1, s));
+          for (double* q : {V0.wbar_gsb, V0.wbar_gs2, V0.wbar_gsk}) CUDA_OK(cudaMemsetAsync(q, 0, a2, s));
+          CUDA_OK(cudaMemsetAsync(V0.cx_ss, 0, sizeof(double) * (size_t)5 * P.B * p->pss * p->n_ss, s));
+        }
         cl2pt::VJPParams V = V0;
         V.cot = vcot + (size_t)w0 * n_total;
         V.dv = ddv + (size_t)w0 * n_total;

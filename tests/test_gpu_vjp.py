@@ -386,11 +386,63 @@ def test_vjp_nonlimber_vs_oracle_fd(gpu_lib, oracle_built):
     assert abs(an - fd) <= ORACLE_REL * abs(fd), (an, fd)
 
 
+def tatt_params(w):
+    ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
+    ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
+    ps += [("gb", k, q) for k in range(3) for q in range(w.cfg.n_lens)]
+    ps += [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0)]
+    return ps
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_MIXED])
+def test_vjp_tatt_one_loop(gpu_lib, prec):
+    """TATT intrinsic alignments (A1, eta_1, A2, eta_2, b_TA) and one-loop
+    bias (b2, bs2) with non-Limber w(theta): every nuisance gradient and a
+    direction in the nonlinear table (with a separate linear table, whose
+    FAST-PT dependence the adjoint leaves out) against differences of the
+    FP64 forward."""
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 2, seed=41)
+    p64 = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=2, linear_table=True)
+    plan = p64 if prec == lib.PREC_FP64 else lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2,
+                                                      linear_table=True)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    lnPL = np.stack([t.lnPL.reshape(-1) for t in tabs])
+    rng = np.random.default_rng(16)
+    v = rng.normal(size=(2, plan.n_total))
+    dv, lbar, nbar, _ = plan.vjp_real(om, h0, chi, G, lnP, nus, v, lnPL=lnPL)
+    tol = GRAD_REL if prec == lib.PREC_FP64 else 2e-5
+    worst = 0.0
+    for pt in range(2):
+        sl = slice(pt, pt + 1)
+        for field, i, j in tatt_params(w):
+            x0 = nu_get(nus[pt], field, i, j)
+            h = H * max(abs(x0), 0.1)
+            f = []
+            for sgn in (1, -1):
+                nu = clone(nus[pt])
+                nu_set(nu, field, i, j, x0 + sgn * h)
+                f.append(float(v[pt] @ p64.eval_real(om[sl], h0[sl], chi[sl], G[sl], lnP[sl], [nu],
+                                                     lnPL=lnPL[sl])[0]))
+            fd = (f[0] - f[1]) / (2 * h)
+            an = nbar[pt, flat_index(field, i, j)]
+            err = abs(an - fd) / max(abs(fd), 1e-9 * abs(f[0]))
+            worst = max(worst, err)
+            assert err <= tol, (field, i, j, an, fd)
+        u = rng.normal(size=lnP.shape[1])
+        fd = lnp_direction_fd(p64, tabs, nus, v, pt, u, lnPL=lnPL, which="lnP")
+        assert abs(lbar[pt] @ u - fd) <= tol * abs(fd), (lbar[pt] @ u, fd)
+    print("TATT/one-loop max rel gradient error", worst)
+
+
 @pytest.mark.gpu
 def test_vjp_unsupported_plan(gpu_lib):
-    """TATT / one-loop plans report CL2PT_ERR_UNSUPPORTED."""
+    """Plans with b2/bs2 derived from b1 (bias models 1, 2) report
+    CL2PT_ERR_UNSUPPORTED."""
     for name in ("real_3x2pt_tatt_small",):
         w = workloads.make(name)
+        w.cfg.bias_model[1] = 1
         tabs, nus = workloads.points(w, 1, seed=1)
         plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=1)
         om, h0, chi, G, lnP = workloads.stack(tabs)
