@@ -153,6 +153,9 @@ def run_reference(args):
 
 
 def value_grad(plan, w, data, d_om, d_h0, d_chi, d_G, d_lnP, d_nu, out, stream, args, p64=None):
+    if out is None:
+        import torch
+        out = torch.empty((d_om.shape[0], plan.n_total), dtype=torch.float64, device=d_om.device)
     """value+grad/s: cl2pt_vjp_real with a fixed cotangent on device-resident
     inputs, CUDA-event timed over --steps batches (mixed plan, then the FP64
     plan as the plain-FP64 GPU form)."""
@@ -185,10 +188,13 @@ def value_grad(plan, w, data, d_om, d_h0, d_chi, d_G, d_lnP, d_nu, out, stream, 
     plan.check_errors(sptr)
     nb = nbar.cpu().numpy().view(np.float64).reshape(B, -1)
     n_nu = int(np.count_nonzero(np.any(nb != 0.0, axis=0)))
+    tatt = w.cfg.ia_model == 1
+    what = "shear m, source dz, b1" + (", b2, bs2, A1, eta1, A2, eta2, b_TA" if tatt else
+                                      (", A1" if w.cfg.ia_mode else ""))
     res = {"value": B * args.steps / (ms / 1e3), "unit": "value+gradient evaluations/s",
-           "ms_per_step": ms / args.steps,
+           "ms_per_step": ms / args.steps, "workload": w.name, "points_per_step": B,
            "grad_wrt": f"lnP table ({plan.shapes['nk']}x{plan.shapes['nz']}) and {n_nu} nuisance "
-                       f"parameters (shear m, b1{', IA' if w.cfg.ia_mode else ''})",
+                       f"parameters ({what})",
            "n_nuisance": n_nu, "launches_per_step": plan.launches(),
            "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items() if v > 0}}
     if p64 is not None:
@@ -441,6 +447,19 @@ def main():
                         None if args.no_fp64 else lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64,
                                                            max_batch=B))
 
+    # ---- value + gradient of the differentiable layout: TATT intrinsic
+    # alignments, one-loop bias, photo-z shifts and m-bias on the same
+    # geometry (real_3x2pt_tatt)
+    vg4 = None
+    if not args.no_grad:
+        w4 = workloads.make("real_3x2pt_tatt")
+        B4 = min(B, 256)
+        data4 = make_batch(w4, B4, seed=200 + rank)
+        plan4 = lib.Plan(w4.cfg, w4.src, w4.lens, w4.base, lib.PREC_MIXED, max_batch=B4)
+        t4 = [T(data4[k]) for k in ("om", "h0", "chi", "G", "lnP")]
+        vg4 = value_grad(plan4, w4, data4, *t4, T(data4["nub"]), None, stream, args)
+        plan4.close()
+
     # ---- roofline of the dominant kernel
     hbm, src = peaks()
     top = max(kms, key=lambda k: kms[k])
@@ -486,6 +505,9 @@ def main():
     if vg is not None:
         vg["value"] *= world
         line["value_grad"] = vg
+    if vg4 is not None:
+        vg4["value"] *= world
+        line["value_grad_tatt"] = vg4
     if rank == 0 and world == 1 and not args.no_cpu:
         n, t = cpu_sample(w, data, budget_s=12.0)
         line["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": os.cpu_count(),

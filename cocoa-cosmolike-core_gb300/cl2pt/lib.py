@@ -71,6 +71,9 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
+    lib.cl2pt_jacobian_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_int,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
     lib.cl2pt_eval_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
                                        C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_fourier_sizes.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip]
@@ -243,6 +246,40 @@ class Plan:
         if lbarl is not None:
             return dv, lbar, nb, lbarl
         return dv, lbar, nb
+
+    def jacobian_real(self, omega_m, h0, chi, G, lnP, nuisance, rows=None, mask=None, pm=None,
+                      lnPL=None):
+        """Jacobian of one point's data vector (host arrays, n = 1): returns
+        (dv [n_total], J_lnP [nrows][nk*nz], J_nu [nrows][13*MAX_BINS]) and
+        J_lnPL when lnPL is given."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64).reshape(1)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        nus = (abi.Nuisance * 1)(*nuisance)
+        b = Batch()
+        b.n, b.where = 1, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        rw = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+        nr = self.n_total if rw is None else len(rw)
+        dv = np.zeros(self.n_total)
+        jl = np.zeros((nr, arrs[3].size))
+        jll = None if lpl is None else np.zeros((nr, lpl.size))
+        jn = (abi.Nuisance * nr)()
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
+        check(load().cl2pt_jacobian_real(self.h, C.byref(b),
+                                         mk.ctypes.data if mk is not None else None,
+                                         pmm.ctypes.data if pmm is not None else None, nr,
+                                         rw.ctypes.data if rw is not None else None,
+                                         dv.ctypes.data, jl.ctypes.data,
+                                         None if jll is None else jll.ctypes.data,
+                                         C.addressof(jn), None), "cl2pt_jacobian_real")
+        jnu = np.frombuffer(bytes(jn), dtype=np.float64).reshape(nr, -1).copy()
+        if jll is not None:
+            return dv, jl, jnu, jll
+        return dv, jl, jnu
 
     def vjp_real_device(self, omega_m, h0, chi, G, lnP, nuisance, cot, dv, lnP_bar, nu_bar,
                         mask=None, pm=None, lnPL=None, lnPL_bar=None, stream=None):

@@ -814,20 +814,13 @@ extern "C" int cl2pt_eval_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell,
   return internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr);
 }
 
-extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                              const double* cot, double* dv, double* lnP_bar, double* lnPL_bar,
-                              cl2pt_nuisance* nu_bar, void* stream)
+static int vjp_prepare(cl2pt_plan* p)
 {
-  if (!p || !cot || !lnP_bar || !nu_bar) return CL2PT_ERR_ARG;
-  int st = check_batch(p, b);
-  if (st) return st;
-  if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
   const cl2pt_config& c = p->cfg;
   if (c.bias_model[0] != 0 || c.bias_model[1] != 0 || c.bias_model[2] != 0 || c.linear_pk)
     return CL2PT_ERR_UNSUPPORTED;
   if (cl2pt::vjp_limber_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if ((p->P.tatt || p->P.one_loop) && cl2pt::vjp_extra_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
-  if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
   if (!p->d_vjp_ws) {
     const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
     const size_t LNL = c.lmax_nolimber;
@@ -848,12 +841,123 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
       return a;
     }
   }
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                              const double* cot, double* dv, double* lnP_bar, double* lnPL_bar,
+                              cl2pt_nuisance* nu_bar, void* stream)
+{
+  if (!p || !cot || !lnP_bar || !nu_bar) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
+  st = vjp_prepare(p);
+  if (st) return st;
+  if (!dv && b->where == CL2PT_DEVICE) dv = p->d_dv;  // value kept on the device only
   VJPReq vr;
   vr.cot = cot;
   vr.lnp_bar = lnP_bar;
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+}
+
+extern "C" int cl2pt_jacobian_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                                   int nrows, const int* rows, double* dv, double* jac_lnP, double* jac_lnPL,
+                                   cl2pt_nuisance* jac_nu, void* stream)
+{
+  if (!p || !b || b->n != 1 || !jac_lnP || !jac_nu) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (b->lnPL && !jac_lnPL) return CL2PT_ERR_ARG;
+  const int NT = p->n_total;
+  if (rows) {
+    if (nrows < 1) return CL2PT_ERR_ARG;
+    for (int i = 0; i < nrows; i++)
+      if (rows[i] < 0 || rows[i] >= NT) return CL2PT_ERR_ARG;
+  } else {
+    nrows = NT;
+  }
+  st = vjp_prepare(p);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const Params& T = p->P;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const bool sep = b->lnPL != nullptr;
+  if (sep && !p->d_in_lnPL && b->where == CL2PT_HOST) return CL2PT_ERR_UNSUPPORTED;
+  double* d_lnpl_in = sep ? (p->d_in_lnPL ? p->d_in_lnPL : nullptr) : nullptr;
+  if (sep && !d_lnpl_in) return CL2PT_ERR_UNSUPPORTED;
+  const int B = p->max_batch;
+  // the point's inputs in slot 0 of the plan's staging buffers, replicated
+  auto put = [&](double* dst, const double* src, size_t n) -> int {
+    CUDA_OK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, s));
+    for (int k = 1; k < B; k++)
+      CUDA_OK(cudaMemcpyAsync(dst + k * n, dst, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return CL2PT_OK;
+  };
+  if ((st = put(p->d_in_om, b->omega_m, 1)) || (st = put(p->d_in_h0, b->h0, 1)) ||
+      (st = put(p->d_in_chi, b->chi, nchi)) || (st = put(p->d_in_G, b->G, nG)) ||
+      (st = put(p->d_in_lnP, b->lnP, nP)))
+    return st;
+  if (sep && (st = put(d_lnpl_in, b->lnPL, nPL))) return st;
+  CUDA_OK(cudaMemcpyAsync(p->d_in_nu, b->nuisance, sizeof(cl2pt_nuisance), cudaMemcpyDefault, s));
+  for (int k = 1; k < B; k++)
+    CUDA_OK(cudaMemcpyAsync(p->d_in_nu + k, p->d_in_nu, sizeof(cl2pt_nuisance), cudaMemcpyDeviceToDevice, s));
+  const int* dmask = nullptr;
+  if (mask) {
+    CUDA_OK(cudaMemcpyAsync(p->d_mask, mask, NT * sizeof(int), cudaMemcpyDefault, s));
+    dmask = p->d_mask;
+  }
+  const double* dpm = nullptr;
+  if (pm) {
+    if ((st = put(p->d_pm, pm, p->cfg.n_lens))) return st;
+    dpm = p->d_pm;
+  }
+  cl2pt_batch db = *b;
+  db.where = CL2PT_DEVICE;
+  db.omega_m = p->d_in_om;
+  db.h0 = p->d_in_h0;
+  db.chi = p->d_in_chi;
+  db.G = p->d_in_G;
+  db.lnP = p->d_in_lnP;
+  db.lnPL = sep ? d_lnpl_in : nullptr;
+  db.nuisance = p->d_in_nu;
+  std::vector<double> cot((size_t)B * NT);
+  for (int r0 = 0; r0 < nrows; r0 += B) {
+    const int nb = std::min(B, nrows - r0);
+    std::fill(cot.begin(), cot.end(), 0.0);
+    for (int k = 0; k < nb; k++) cot[(size_t)k * NT + (rows ? rows[r0 + k] : r0 + k)] = 1.0;
+    CUDA_OK(cudaMemcpyAsync(p->d_vjp_cot, cot.data(), (size_t)nb * NT * sizeof(double), cudaMemcpyHostToDevice, s));
+    // the host vector is reused by the next chunk: wait for the copy
+    CUDA_OK(cudaStreamSynchronize(s));
+    db.n = nb;
+    VJPReq vr;
+    vr.cot = p->d_vjp_cot;
+    vr.lnp_bar = p->d_vjp_lnp;
+    vr.lnpl_bar = sep ? p->d_vjp_lnpl : nullptr;
+    vr.nu_bar = p->d_vjp_nu;
+    if (sep && !p->d_vjp_lnpl) return CL2PT_ERR_UNSUPPORTED;
+    st = internal_eval(p, &db, dmask, dpm, p->d_dv, s, nullptr, &vr);
+    if (st) return st;
+    CUDA_OK(cudaMemcpyAsync(jac_lnP + (size_t)r0 * nP, p->d_vjp_lnp, (size_t)nb * nP * sizeof(double),
+                            cudaMemcpyDefault, s));
+    if (sep)
+      CUDA_OK(cudaMemcpyAsync(jac_lnPL + (size_t)r0 * nPL, p->d_vjp_lnpl, (size_t)nb * nPL * sizeof(double),
+                              cudaMemcpyDefault, s));
+    CUDA_OK(cudaMemcpyAsync(jac_nu + r0, p->d_vjp_nu, (size_t)nb * sizeof(cl2pt_nuisance), cudaMemcpyDefault, s));
+    if (dv && r0 == 0) CUDA_OK(cudaMemcpyAsync(dv, p->d_dv, NT * sizeof(double), cudaMemcpyDefault, s));
+  }
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaStreamSynchronize(s));
+    int err = 0;
+    CUDA_OK(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+      cudaMemset(p->d_err, 0, sizeof(int));
+      return CL2PT_ERR_DEVICE;
+    }
+  }
+  return CL2PT_OK;
 }
 
 // Stage the batch on the device (when it lives on the host), then run the

@@ -134,6 +134,23 @@ int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
 
+/* Jacobian of the real-space data vector of ONE parameter point
+ * (batch->n == 1) for the data-vector rows rows[0..nrows-1] (host array;
+ * rows NULL: all n_total rows in order):
+ *   jac_lnP  [nrows][pk_nk * pk_nz]    d dv[row] / d lnP
+ *   jac_lnPL [nrows][pkl_nk * pkl_nz]  with a separate linear table, else NULL
+ *   jac_nu   [nrows]                   d dv[row] / d nuisance (as nu_bar of
+ *                                      cl2pt_vjp_real)
+ *   dv       [n_total] or NULL         the value
+ * Evaluated as batches of one-hot cotangents through cl2pt_vjp_real's
+ * kernels, max_batch rows per pass; masked rows come out zero.  Pointers
+ * other than rows follow batch->where; the call returns when the results are
+ * in place for host batches. */
+int cl2pt_jacobian_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
+                        const double* pm, int nrows, const int* rows, double* dv,
+                        double* jac_lnP, double* jac_lnPL, cl2pt_nuisance* jac_nu,
+                        void* stream);
+
 /* Wait for the stream and report any device-side check that failed since
  * the last call (a device-resident batch does not synchronise). */
 int cl2pt_check_errors(cl2pt_plan* plan, void* stream);

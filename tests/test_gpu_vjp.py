@@ -437,6 +437,35 @@ def test_vjp_tatt_one_loop(gpu_lib, prec):
 
 
 @pytest.mark.gpu
+def test_jacobian_rows(gpu_lib):
+    """cl2pt_jacobian_real: rows of the Jacobian equal the VJP of the one-hot
+    cotangent, the value equals the forward, a chunked pass (max_batch
+    smaller than the row count) matches, and a table-entry column matches
+    a central difference."""
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION, npts=3, name="real_3x2pt_small", seed=51)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rows = np.array([0, 7, plan.n_xi // 2 + 3, plan.n_xi + 5, plan.n_total - 1], dtype=np.int32)
+    dv, J, Jn = plan.jacobian_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1], nus[:1], rows=rows)
+    assert np.array_equal(dv, plan.eval_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1], nus[:1])[0])
+    for k, r in enumerate(rows):
+        e = np.zeros((1, plan.n_total))
+        e[0, r] = 1.0
+        _, lb, nb = plan.vjp_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1], nus[:1], e)
+        np.testing.assert_allclose(J[k], lb[0], rtol=1e-12, atol=1e-14 * np.abs(lb).max())
+        np.testing.assert_allclose(Jn[k], nb[0], rtol=1e-12, atol=1e-14 * max(np.abs(nb).max(), 1e-300))
+    # max_batch 3 < 5 rows: two passes
+    _, J2, Jn2 = plan.jacobian_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1], nus[:1], rows=rows)
+    np.testing.assert_allclose(J2, J, rtol=1e-12, atol=1e-14 * np.abs(J).max())
+    k = int(np.argmax(np.abs(J[1])))
+    d = np.zeros(lnP.shape[1])
+    d[k] = H
+    fp = plan.eval_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1] + d, nus[:1])[0][rows[1]]
+    fm = plan.eval_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1] - d, nus[:1])[0][rows[1]]
+    fd = (fp - fm) / (2 * H)
+    assert abs(J[1, k] - fd) <= GRAD_REL * abs(fd), (J[1, k], fd)
+
+
+@pytest.mark.gpu
 def test_vjp_unsupported_plan(gpu_lib):
     """Plans with b2/bs2 derived from b1 (bias models 1, 2) report
     CL2PT_ERR_UNSUPPORTED."""
