@@ -77,6 +77,14 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_eval_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
                                        C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_fourier_sizes.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip]
+    lib.cl2pt_eval_fourier_ragged.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.cl2pt_fourier_graph_create.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.POINTER(C.c_void_p)]
+    lib.cl2pt_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
+    lib.cl2pt_graph_launch_count.argtypes = [C.c_void_p]
+    lib.cl2pt_graph_destroy.argtypes = [C.c_void_p]
     lib.cl2pt_debug_limber_tables.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
     lib.cl2pt_debug_nonlimber.argtypes = [C.c_void_p, C.c_int, _dp, _ip]
     lib.cl2pt_debug_g_tables.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -301,6 +309,48 @@ class Plan:
                                    nu_bar.data_ptr(), stream)
         check(st, "cl2pt_vjp_real")
 
+    def eval_fourier_ragged(self, omega_m, h0, chi, G, lnP, nuisance, ell, row_ptr, idx,
+                            lmax_shear=1e30, lnPL=None):
+        """Ragged Fourier vectors on host arrays: point i keeps idx[row_ptr[i]:
+        row_ptr[i+1]]; returns the compacted values [row_ptr[-1]]."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+        ix = np.ascontiguousarray(idx, dtype=np.int32)
+        out = np.zeros(max(int(rp[-1]), 1))
+        check(load().cl2pt_eval_fourier_ragged(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                               rp.ctypes.data, ix.ctypes.data, out.ctypes.data, None),
+              "cl2pt_eval_fourier_ragged")
+        return out[:int(rp[-1])]
+
+    def fourier_graph(self, omega_m, h0, chi, G, lnP, nuisance, ell, out, lmax_shear=1e30,
+                      mask=None, row_ptr=None, idx=None, lnPL=None, stream=None):
+        """Capture a Fourier evaluation over these CUDA tensors as a graph
+        (see cl2pt_fourier_graph_create); returns a Graph."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        g = C.c_void_p()
+        ptr = lambda t: None if t is None else t.data_ptr()
+        check(load().cl2pt_fourier_graph_create(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                                ptr(mask), ptr(row_ptr), ptr(idx), out.data_ptr(), stream,
+                                                C.byref(g)), "cl2pt_fourier_graph_create")
+        # keep the tensors the graph reads alive with it
+        return Graph(g, (omega_m, h0, chi, G, lnP, nuisance, out, mask, row_ptr, idx, lnPL, self))
+
     # ------------------------------------------------------------ device
     def eval_real_device(self, omega_m, h0, chi, G, lnP, nuisance, out, mask=None, pm=None,
                          lnPL=None, stream=None):
@@ -366,6 +416,31 @@ class Plan:
 
 
 # ------------------------------------------------------------------ FAST-PT
+class Graph:
+    """A captured Fourier evaluation (cl2pt_graph)."""
+
+    def __init__(self, h, keep):
+        self.h = h
+        self._keep = keep
+
+    def launch(self, stream=None):
+        check(load().cl2pt_graph_launch(self.h, stream), "cl2pt_graph_launch")
+
+    def launches(self) -> int:
+        return load().cl2pt_graph_launch_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cl2pt_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _ints(v):
     return np.ascontiguousarray(v, dtype=np.int32)
 

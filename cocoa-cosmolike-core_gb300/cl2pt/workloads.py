@@ -12,6 +12,13 @@
   real_3x2pt_tatt[_small] the same with TATT intrinsic alignments
                          (redshift evolution: A1, A2, eta, b_TA) and
                          nonlinear galaxy bias (b2, bs2)
+  fourier_serving        batched sampler serving: Fourier 3x2pt, 10 source
+                         + 10 lens bins, 26 log-spaced l bins in 20-15000,
+                         non-Limber clustering below l = 200 with the FFTLog
+                         on 2048 log-chi points; per-point scale cuts
+                         (scale_cuts) keep 40-100% of each data vector
+  fourier_serving_small  a reduced serving workload (4 + 3 bins, 500 chi
+                         points) for fast checks
 
 Per-point variation: every walker gets its own P(k,z) amplitude/tilt,
 source photo-z shifts N(0, 0.02), shear calibration N(0, 0.01) and lens
@@ -71,6 +78,17 @@ def make(name: str) -> Workload:
         w.cfg.adopt_limber_gg = 1
         w.name = name
         return w
+    if name == "fourier_serving":
+        cfg = abi.make_config(n_source=10, n_lens=10, lmax_nolimber=200, nl_nchi=2048)
+        base = synthetic.make_cosmo_tables(nk=600, nz=200)
+        return Workload(name, cfg, synthetic.source_nz(10), synthetic.lens_nz(10), base,
+                        _fourier_ells(26, 20.0, 15000.0))
+    if name == "fourier_serving_small":
+        cfg = abi.make_config(n_source=4, n_lens=3, lmax_nolimber=200, nl_nchi=500, lmax=20000,
+                              n_ell=200)
+        base = synthetic.make_cosmo_tables(nk=400, nz=100)
+        return Workload(name, cfg, synthetic.source_nz(4), synthetic.lens_nz(3), base,
+                        _fourier_ells(12, 20.0, 15000.0))
     if name in ("real_3x2pt_tatt", "real_3x2pt_tatt_small"):
         # the differentiable-3x2pt layout: real_3x2pt plus TATT intrinsic
         # alignments (redshift-evolution mode) and nonlinear galaxy bias
@@ -109,6 +127,23 @@ def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True):
         tabs.append(t)
         nus.append(nu)
     return tabs, nus
+
+
+def scale_cuts(w: Workload, n: int, seed: int = 0):
+    """Per-point scale cuts of a Fourier workload as CSR lists (row_ptr
+    [n+1], idx [nnz]): point i draws a kept fraction f ~ U(0.4, 1) and keeps
+    the lowest round(f nell) (at least 1) multipole bins of every spectrum."""
+    rng = np.random.default_rng(SEED0 + 50 + seed)
+    pss, pgs, pgg = abi.n_pairs(w.cfg)
+    nell = len(w.ell)
+    nspec = pss + pgs + w.cfg.n_lens
+    ptr, idx = [0], []
+    for _ in range(n):
+        m = max(1, int(round(rng.uniform(0.4, 1.0) * nell)))
+        for sp in range(nspec):
+            idx.extend(sp * nell + np.arange(m))
+        ptr.append(len(idx))
+    return np.asarray(ptr, dtype=np.int32), np.asarray(idx, dtype=np.int32)
 
 
 def stack(tabs):

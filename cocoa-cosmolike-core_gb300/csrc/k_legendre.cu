@@ -221,6 +221,25 @@ void launch_assemble_fourier(const Params& P, int nell, const double* ell, doubl
   (*launches)++;
 }
 
+// Ragged (CSR) output: out[j] = full[pt][idx[j]] for j in [ptr[pt], ptr[pt+1])
+__global__ void k_gather_csr(const int* __restrict__ ptr, const int* __restrict__ idx,
+                             const double* __restrict__ full, int n_total, int w0, double* __restrict__ out)
+{
+  const int pt = w0 + blockIdx.x;
+  const double* f = full + (size_t)blockIdx.x * n_total;
+  const int a = ptr[pt], b = ptr[pt + 1];
+  for (int j = a + threadIdx.x; j < b; j += blockDim.x) {
+    const int k = idx[j];
+    out[j] = (k >= 0 && k < n_total) ? f[k] : 0.0;
+  }
+}
+
+void launch_gather_csr(const int* ptr, const int* idx, const double* full, int n_total, int w0, int B,
+                       double* out, cudaStream_t s)
+{
+  k_gather_csr<<<B, 256, 0, s>>>(ptr, idx, full, n_total, w0, out);
+}
+
 void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
                      cudaStream_t s, int* launches, const Hook& hk)
 {

@@ -36,6 +36,9 @@ void launch_legendre(const Params& P, const double* filt_xi, const double* filt_
 // Fourier data vector dv[pt][nell (pss + pgs + nl)] from the node tables
 void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,
                              const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk);
+// ragged output of points w0 .. w0+B-1 from their full vectors (k_legendre.cu)
+void launch_gather_csr(const int* ptr, const int* idx, const double* full, int n_total, int w0, int B,
+                       double* out, cudaStream_t s);
 // masked, calibrated data vector dv[pt][n_total] from obs
 void launch_assemble(const Params& P, const int* mask, const double* pm, double* dv,
                      cudaStream_t s, int* launches, const Hook& hk);

@@ -767,7 +767,29 @@ struct FourierReq {
   int nell = 0;
   const double* ell = nullptr;  // host
   double lmax_shear = 0;
+  bool ell_on_device = false;   // ell already in d_ell_f (graph capture)
+  // ragged output: per point the kept entries idx[ptr[pt] .. ptr[pt+1]) of
+  // its full vector, compacted into out[ptr[pt] ..] (device pointers)
+  const int* csr_ptr = nullptr;
+  const int* csr_idx = nullptr;
+  double* csr_out = nullptr;
 };
+
+// Fourier staging (full vectors [max_batch][n_total] and a mask), grown on
+// demand
+static int fourier_staging(cl2pt_plan* p, int n_total)
+{
+  if ((size_t)n_total * p->max_batch <= p->fourier_cap) return CL2PT_OK;
+  void *d1 = nullptr, *d2 = nullptr;
+  CUDA_OK(cudaMalloc(&d1, sizeof(double) * (size_t)n_total * p->max_batch));
+  CUDA_OK(cudaMalloc(&d2, sizeof(int) * (size_t)n_total));
+  p->dbufs.push_back(d1);
+  p->dbufs.push_back(d2);
+  p->d_dv_f = (double*)d1;
+  p->d_mask_f = (int*)d2;
+  p->fourier_cap = (size_t)n_total * p->max_batch;
+  return CL2PT_OK;
+}
 
 // Adjoint request: cotangent in, table and nuisance gradients out (all
 // per batch->where).
@@ -960,6 +982,124 @@ extern "C" int cl2pt_jacobian_real(cl2pt_plan* p, const cl2pt_batch* b, const in
   return CL2PT_OK;
 }
 
+extern "C" int cl2pt_eval_fourier_ragged(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
+                                         double lmax_shear, const int* row_ptr, const int* idx, double* dv,
+                                         void* stream)
+{
+  if (!p || !dv || !row_ptr || !idx) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  int n_total = 0;
+  cl2pt_fourier_sizes(p, nell, nullptr, nullptr, nullptr, &n_total);
+  const int n = b->n;
+  FourierReq fr;
+  fr.nell = nell;
+  fr.ell = ell;
+  fr.lmax_shear = lmax_shear;
+  if (b->where == CL2PT_DEVICE) {
+    fr.csr_ptr = row_ptr;
+    fr.csr_idx = idx;
+    fr.csr_out = dv;
+    return internal_eval(p, b, nullptr, nullptr, nullptr, (cudaStream_t)stream, &fr);
+  }
+  // host: validate and stage the index lists and the compacted output
+  if (row_ptr[0] != 0) return CL2PT_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    if (row_ptr[i + 1] < row_ptr[i] || row_ptr[i + 1] - row_ptr[i] > n_total) return CL2PT_ERR_ARG;
+  const size_t nnz = row_ptr[n];
+  for (size_t j = 0; j < nnz; j++)
+    if (idx[j] < 0 || idx[j] >= n_total) return CL2PT_ERR_ARG;
+  if (nnz + p->max_batch + 1 > p->csr_cap) {
+    int a = dalloc(p, &p->d_csr_ptr, (size_t)p->max_batch + 1);
+    if (!a) a = dalloc(p, &p->d_csr_idx, std::max(nnz, (size_t)1));
+    if (!a) a = dalloc(p, &p->d_csr_out, std::max(nnz, (size_t)1));
+    if (a) return a;
+    p->csr_cap = nnz + p->max_batch + 1;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  CUDA_OK(cudaMemcpyAsync(p->d_csr_ptr, row_ptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  CUDA_OK(cudaMemcpyAsync(p->d_csr_idx, idx, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+  fr.csr_ptr = p->d_csr_ptr;
+  fr.csr_idx = p->d_csr_idx;
+  fr.csr_out = p->d_csr_out;
+  st = internal_eval(p, b, nullptr, nullptr, nullptr, s, &fr);
+  if (st) return st;
+  CUDA_OK(cudaMemcpy(dv, p->d_csr_out, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+  return CL2PT_OK;
+}
+
+// CUDA-graph form of a Fourier evaluation over fixed device buffers.
+struct cl2pt_graph {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t x = nullptr;
+  int launches = 0;
+};
+
+extern "C" int cl2pt_fourier_graph_create(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
+                                          double lmax_shear, const int* mask, const int* row_ptr,
+                                          const int* idx, double* dv, void* stream, cl2pt_graph** out)
+{
+  if (!p || !b || !out || !dv || !stream || b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
+  if ((row_ptr == nullptr) != (idx == nullptr)) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (!ell || nell < 1 || nell > std::min(p->nnode_ss, p->nnode_g)) return CL2PT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FourierReq fr;
+  fr.nell = nell;
+  fr.ell = ell;
+  fr.lmax_shear = lmax_shear;
+  fr.csr_ptr = row_ptr;
+  fr.csr_idx = idx;
+  fr.csr_out = row_ptr ? dv : nullptr;
+  double* full = row_ptr ? nullptr : dv;
+  // one eager evaluation: uploads the multipoles, sets kernel attributes and
+  // allocates the staging the captured launches use
+  st = internal_eval(p, b, mask, nullptr, full, s, &fr);
+  if (st) return st;
+  CUDA_OK(cudaStreamSynchronize(s));
+  fr.ell_on_device = true;
+  const bool timing = p->timing;
+  p->timing = false;
+  cl2pt_graph* G = new cl2pt_graph();
+  CUDA_OK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  st = internal_eval(p, b, mask, nullptr, full, s, &fr);
+  const cudaError_t ec = cudaStreamEndCapture(s, &G->g);
+  p->timing = timing;
+  if (st || ec != cudaSuccess) {
+    if (G->g) cudaGraphDestroy(G->g);
+    delete G;
+    cudaGetLastError();
+    return st ? st : CL2PT_ERR_CUDA;
+  }
+  G->launches = p->last_launches;
+  if (cudaGraphInstantiate(&G->x, G->g, 0) != cudaSuccess) {
+    cudaGraphDestroy(G->g);
+    delete G;
+    return CL2PT_ERR_CUDA;
+  }
+  *out = G;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_graph_launch(cl2pt_graph* g, void* stream)
+{
+  if (!g || !g->x) return CL2PT_ERR_ARG;
+  CUDA_OK(cudaGraphLaunch(g->x, (cudaStream_t)stream));
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_graph_launch_count(const cl2pt_graph* g) { return g ? g->launches : 0; }
+
+extern "C" int cl2pt_graph_destroy(cl2pt_graph* g)
+{
+  if (!g) return CL2PT_OK;
+  if (g->x) cudaGraphExecDestroy(g->x);
+  if (g->g) cudaGraphDestroy(g->g);
+  delete g;
+  return CL2PT_OK;
+}
+
 // Stage the batch on the device (when it lives on the host), then run the
 // pipeline wave by wave so the per-wave workspace stays L2-sized.
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
@@ -974,17 +1114,11 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     if (fr->nell < 1 || fr->nell > std::min(p->nnode_ss, p->nnode_g) || !fr->ell) return CL2PT_ERR_ARG;
     for (int i = 0; i < fr->nell; i++)
       if (!(fr->ell[i] >= 1.0) || !std::isfinite(fr->ell[i])) return CL2PT_ERR_ARG;
-    CUDA_OK(cudaMemcpyAsync(p->d_ell_f, fr->ell, sizeof(double) * fr->nell, cudaMemcpyHostToDevice, s));
-    if (b->where == CL2PT_HOST && (size_t)n_total * p->max_batch > p->fourier_cap) {
-      // staging for host Fourier batches, grown on demand
-      void *d1 = nullptr, *d2 = nullptr;
-      CUDA_OK(cudaMalloc(&d1, sizeof(double) * (size_t)n_total * p->max_batch));
-      CUDA_OK(cudaMalloc(&d2, sizeof(int) * (size_t)n_total));
-      p->dbufs.push_back(d1);
-      p->dbufs.push_back(d2);
-      p->d_dv_f = (double*)d1;
-      p->d_mask_f = (int*)d2;
-      p->fourier_cap = (size_t)n_total * p->max_batch;
+    if (!fr->ell_on_device)
+      CUDA_OK(cudaMemcpyAsync(p->d_ell_f, fr->ell, sizeof(double) * fr->nell, cudaMemcpyHostToDevice, s));
+    if (b->where == CL2PT_HOST || fr->csr_out) {
+      const int st = fourier_staging(p, n_total);
+      if (st) return st;
     }
     d_dv_stage = p->d_dv_f;
     d_mask_stage = p->d_mask_f;
@@ -1024,7 +1158,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     nu = b->nuisance;
     dmask = mask;
     dpm = pm;
-    ddv = dv;
+    ddv = (fourier && fr->csr_out) ? p->d_dv_f : dv;
   }
   if (!b->lnPL && (T.pkl_nk != T.pk_nk || T.pkl_nz != T.pk_nz)) return CL2PT_ERR_ARG;
   // adjoint: device views of the cotangent and the gradients, workspace
@@ -1160,6 +1294,11 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       }
       cl2pt::launch_assemble_fourier(Pf, fr->nell, p->d_ell_f, fr->lmax_shear, use_nl ? 1 : 0, dmask,
                                      ddv + (size_t)w0 * n_total, s, &launches, hk);
+      if (fr->csr_out) {
+        cl2pt::launch_gather_csr(fr->csr_ptr, fr->csr_idx, ddv + (size_t)w0 * n_total, n_total, w0, P.B,
+                                 fr->csr_out, s);
+        launches++;
+      }
     } else {
       cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       if (P.tatt || P.one_loop) cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);

@@ -67,6 +67,11 @@ struct cl2pt_plan {
   double* d_dv_f = nullptr;
   int* d_mask_f = nullptr;
   size_t fourier_cap = 0;
+  // ragged (CSR) output staging for host batches
+  int* d_csr_ptr = nullptr;
+  int* d_csr_idx = nullptr;
+  double* d_csr_out = nullptr;
+  size_t csr_cap = 0;
   // TATT / one-loop bias: FAST-PT sub-plans on the reference's k grid and
   // their per-wave outputs
   cl2pt_fastpt_plan* fpt_bias = nullptr;

@@ -108,6 +108,36 @@ int cl2pt_eval_fourier(cl2pt_plan* plan, const cl2pt_batch* batch, int nell,
 int cl2pt_fourier_sizes(const cl2pt_plan* plan, int nell, int* n_ss, int* n_gs,
                         int* n_gg, int* n_total);
 
+/* Ragged (per-point scale cut) form of cl2pt_eval_fourier: point i keeps the
+ * entries idx[row_ptr[i] .. row_ptr[i+1]) of its full Fourier vector (CSR,
+ * row_ptr[0] = 0, indices in [0, n_total)), and dv [row_ptr[n]] receives them
+ * compacted in that order -- the per-walker masks of a sampler without the
+ * zero-padded layout (the reference's mask is global: IP::set_mask,
+ * generic_interface.hpp:1234-1335).  Pointers follow batch->where; host
+ * index lists are validated, device ones are read as given (an index out of
+ * range yields 0). */
+int cl2pt_eval_fourier_ragged(cl2pt_plan* plan, const cl2pt_batch* batch, int nell,
+                              const double* ell, double lmax_shear, const int* row_ptr,
+                              const int* idx, double* dv, void* stream);
+
+/* A Fourier evaluation captured once as a CUDA graph over fixed device
+ * buffers (batch->where == CL2PT_DEVICE; a non-default stream): every
+ * cl2pt_graph_launch replays all of its kernels on whatever the batch's
+ * device buffers (tables, nuisances, masks) hold at that moment, with no
+ * host work per batch.  row_ptr/idx (device, both or neither) select the
+ * ragged output of cl2pt_eval_fourier_ragged; otherwise dv [n][n_total] with
+ * the shared mask (or NULL).  The plan must outlive the graph and must not
+ * run other evaluations while a replay is in flight. */
+typedef struct cl2pt_graph cl2pt_graph;
+int cl2pt_fourier_graph_create(cl2pt_plan* plan, const cl2pt_batch* batch, int nell,
+                               const double* ell, double lmax_shear, const int* mask,
+                               const int* row_ptr, const int* idx, double* dv,
+                               void* stream, cl2pt_graph** graph);
+int cl2pt_graph_launch(cl2pt_graph* graph, void* stream);
+/* Kernel launches one replay performs. */
+int cl2pt_graph_launch_count(const cl2pt_graph* graph);
+int cl2pt_graph_destroy(cl2pt_graph* graph);
+
 /* Value and vector-Jacobian product of the real-space data vector.  Runs
  * cl2pt_eval_real (dv, when not NULL, receives the value) and then the
  * adjoint of every stage for the cotangent cot [n][n_total] (masked
