@@ -418,8 +418,31 @@ __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
 
 // ---- 3. multipole loop (cfftlog_ells_p2 + C_cl_tomo sums and convergence,
 // cosmo2D.c:4132-4769) in the loop precision T: one CTA per (point, bin).
+// Two consecutive multipoles share one complex inverse transform: both
+// outputs are real, so the spectrum X_k + i X_{k+1} (each Hermitian-
+// completed) transforms to x_k + i x_{k+1}.  The per-chi power factors are
+// formed on the fly from ln x.
 template <typename T>
-__global__ void __launch_bounds__(NL_NT, 3) k_nl_loop(Params P, NLParams Q)
+__device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int slot, bool direct,
+                                     const double* gd, int i, int k, double deta)
+{
+  ct<T> g;
+  if (direct) {
+    g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
+  } else {
+    const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
+    ct<T> num, den;
+    if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
+    else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
+    else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
+    g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
+  }
+  gs[slot * Q.hstride + i] = g;
+  return g;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x, q = blockIdx.y;
@@ -431,19 +454,18 @@ __global__ void __launch_bounds__(NL_NT, 3) k_nl_loop(Params P, NLParams Q)
   const int nj = (bmag != 0.0) ? 3 : 2;
   const NLGeom geo = nl_geom(P, pt);
   // shared: [psl, plkd, pinv: nk doubles][lxk: nchi doubles]
-  //         [fa, fb: nmax complex T][F, xpow[3], xx2, rx3: nchi T][plk: nk T]
+  //         [fa, fb: nmax complex T][F0, F1, xs: nchi T][plk: nk T]
   double* psl = (double*)smem_raw;
   double* plkd = psl + P.pkl_nk;
   double* pinv = plkd + P.pkl_nk;
   double* lxk = pinv + P.pkl_nk;
   ct<T>* fa = (ct<T>*)(lxk + nchi);
   ct<T>* fb = fa + Q.nmax;
-  T* F = (T*)(fb + Q.nmax);
-  T* xpow = F + nchi;
-  T* xx2 = xpow + 3 * nchi;
-  T* rx3 = xx2 + nchi;
-  T* plk = rx3 + nchi;
-  __shared__ double red[NL_NT / 32];
+  T* F0 = (T*)(fb + Q.nmax);
+  T* F1 = F0 + nchi;
+  T* xs = F1 + nchi;
+  T* plk = xs + nchi;
+  __shared__ double red[2][NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
   const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
   ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;              // [3][2][hstride]
@@ -462,108 +484,147 @@ __global__ void __launch_bounds__(NL_NT, 3) k_nl_loop(Params P, NLParams Q)
       pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
     }
   }
-  // per chi point: x^nu_j, log10(rc / (x coverH0)) and x^2 at the reversed
-  // index nchi-1-i (y = (l+1)/x[nchi-1-i])
+  // x and log10(rc / (x coverH0)) at the reversed index nchi-1-i
+  // (y = (l+1)/x[nchi-1-i])
   for (int i = tid; i < nchi; i += NL_NT) {
     const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
-    for (int j = 0; j < 3; j++) xpow[j * nchi + i] = (T)pow(xr, Q.nu[j]);
     lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
-    xx2[i] = (T)(xr * xr);
-    rx3[i] = (T)((rc / xr) * (rc / xr) * (rc / xr));
+    xs[i] = (T)xr;
   }
+  const double lrc = log10(rc / CL2PT_COVERH0);
+  const T rct = (T)rc;
   const bool exact_blocks = Q.direct_every != 0;
   const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
   int LM = LNL, done = 0;
   const int BLOCK = 16;
   const double sqpi = sqrt(M_PI);
   const double dlnx = geo.dlnx;
+  const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
   for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
     const int ke = (ks + BLOCK < LNL) ? ks + BLOCK : LNL;
-    for (int k = ks; k < ke; k++) {
+    for (int k = ks; k < ke; k += 2) {
+      const int k2 = k + 1;
+      const bool two = k2 < ke;
       __syncthreads();
-      for (int i = tid; i < nchi; i += NL_NT) F[i] = (T)0;
+      for (int i = tid; i < nchi; i += NL_NT) F0[i] = F1[i] = (T)0;
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
         const double base = geo.x0 / exp(2 * Q.pad[j] * dlnx);
-        const double y0 = (k + 1.) / geo.xlast;
-        const double lnbase = log(base * y0);
+        const double lnb0 = log(base * (k + 1.) / geo.xlast);
+        const double lnb1 = log(base * (k2 + 1.) / geo.xlast);
         const double deta = 2.0 * M_PI / (dlnx * N);
         __syncthreads();
         ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
-        const bool direct = exact_blocks ? (k < ks + 2) : (k < 2);
-        const int slot = exact_blocks ? ((k - ks) & 1) : (k & 1);
-        const int di = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
-        const double* gd = gdir + ((size_t)j * Q.ndirect + (direct ? di : 0)) * Q.hstride * 2;
+        const bool dir0 = exact_blocks ? (k < ks + 2) : (k < 2);
+        const bool dir1 = exact_blocks ? (k2 < ks + 2) : (k2 < 2);
+        const int sl0 = exact_blocks ? ((k - ks) & 1) : (k & 1);
+        const int di0 = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
+        const double* gd0 = gdir + ((size_t)j * Q.ndirect + (dir0 ? di0 : 0)) * Q.hstride * 2;
+        const double* gd1 = gdir + ((size_t)j * Q.ndirect + (dir1 ? di0 + 1 : 0)) * Q.hstride * 2;
         for (int i = tid; i < nq; i += NL_NT) {
-          ct<T> g;
-          if (direct) {
-            g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
-          } else {
-            const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
-            ct<T> num, den;
-            if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
-            else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
-            else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
-            g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
-          }
-          gs[slot * Q.hstride + i] = g;
+          const ct<T> tv = tout[j * Q.hstride + i];
+          const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, k, deta);
           // phase exp(-i eta lnbase), argument reduced in FP64
-          double ph = -(deta * i) * lnbase;
+          double ph = -(deta * i) * lnb0;
           ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
           T sp, cp;
           tsincos<T>((T)ph, &sp, &cp);
-          ct<T> val = tmul(tmul(tout[j * Q.hstride + i], tmk<T>(cp, sp)), g);
-          val.y = -val.y;  // conj
-          fa[i] = val;
-          if (i > 0 && i < N - i) fa[N - i] = tmk<T>(val.x, -val.y);  // Hermitian completion
-        }
-        __syncthreads();
-        if (tid == 0) {
-          fa[0].y = (T)0;
-          if ((N & 1) == 0) fa[N / 2].y = (T)0;
+          ct<T> v0 = tmul(tmul(tv, tmk<T>(cp, sp)), g0);
+          v0.y = -v0.y;  // conj
+          ct<T> v1 = tmk<T>((T)0, (T)0);
+          if (two) {
+            const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, k2, deta);
+            double ph1 = -(deta * i) * lnb1;
+            ph1 -= 2.0 * M_PI * rint(ph1 * (0.5 / M_PI));
+            tsincos<T>((T)ph1, &sp, &cp);
+            v1 = tmul(tmul(tv, tmk<T>(cp, sp)), g1);
+            v1.y = -v1.y;
+          }
+          if (i == 0 || 2 * i == N) {
+            // Hermitian spectra are real there
+            fa[i] = tmk<T>(v0.x, v1.x);
+          } else {
+            fa[i] = tmk<T>(v0.x - v1.y, v0.y + v1.x);
+            if (i < N - i) fa[N - i] = tmk<T>(v0.x + v1.y, v1.x - v0.y);
+          }
         }
         __syncthreads();
         ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
-        const T scale = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
-        const T magf = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
+        const T sc0 = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
+        const T sc1 = (T)(sqpi / (4. * N * pow(k2 + 1., Q.nu[j])));
+        const T mag0 = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
+        const T mag1 = (T)(bmag * (k2 * (k2 + 1.)) / ((k2 + 1.) * (k2 + 1.)));
+        const double num1 = Q.nu[j] - 1.0;
         for (int i = tid; i < nchi; i += NL_NT) {
-          T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
-          if (j == 2) fy = magf * fy * xx2[i];
-          F[i] += fy;
+          // x^nu (nu = 1 or 1.01) and, for magnification, x^2 more
+          const T x = xs[i];
+          T xp = x;
+          if (num1 != 0.0) xp *= texp<T>((T)(num1 * (lrc - lxk[i]) * 2.302585092994045684));
+          if (j == 2) xp *= x * x;
+          const ct<T> z = r[Q.pad[j] + i];
+          T f0 = z.x * sc0 * xp, f1 = z.y * sc1 * xp;
+          if (j == 2) {
+            f0 *= mag0;
+            f1 *= mag1;
+          }
+          F0[i] += f0;
+          F1[i] += f1;
         }
         __syncthreads();
       }
-      // chi sum of F^2 k^3 P_lin(k, a = 1)
-      double part = 0.0;
-      const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
-      const double lk1 = log10(k + 1.);
-      const T cub = (T)((k + 1.) * (k + 1.) * (k + 1.));
+      // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
+      double part0 = 0.0, part1 = 0.0;
+      const double lk0 = log10(k + 1.), lk1 = log10(k2 + 1.);
+      const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
       for (int i = tid; i < nchi; i += NL_NT) {
-        // p_lin(k, 1): search on the loop-precision axis, in-cell offset and
-        // lnP difference in FP64, exponent split as in the Limber walk
-        const double lkv = lk1 + lxk[i];
-        int lo = 0, hi = P.pkl_nk - 1;
-        const T lkt = (T)lkv;
-        while (hi > lo + 1) {
-          const int mid = (lo + hi) >> 1;
-          if (plk[mid] > lkt) hi = mid; else lo = mid;
+        const T rx = rct / xs[i];
+        const T rx3 = rx * rx * rx;
+        for (int h = 0; h < (two ? 2 : 1); h++) {
+          // p_lin(k, 1): search on the loop-precision axis, in-cell offset and
+          // lnP difference in FP64, exponent split as in the Limber walk
+          const double lkv = (h ? lk1 : lk0) + lxk[i];
+          int lo = 0, hi = P.pkl_nk - 1;
+          const T lkt = (T)lkv;
+          while (hi > lo + 1) {
+            const int mid = (lo + hi) >> 1;
+            if (plk[mid] > lkt) hi = mid; else lo = mid;
+          }
+          const double dxd = (lkv - plkd[lo]) * pinv[lo];
+          T pl;
+          if (sizeof(T) == sizeof(double)) {
+            pl = (T)(exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+          } else {
+            const T h0f = (T)psl[lo];
+            const T del = (T)(psl[lo] - (double)h0f) + (T)dxd * (T)(psl[lo + 1] - psl[lo]);
+            pl = texp<T>(h0f) * texp<T>(del) * lc3;
+          }
+          const T F = h ? F1[i] : F0[i];
+          const T k3 = (h ? cub1 : cub0) * rx3;
+          const double v = (double)(F * F * k3 * pl);
+          if (h) part1 += v; else part0 += v;
         }
-        const double dxd = (lkv - plkd[lo]) * pinv[lo];
-        T pl;
-        if (sizeof(T) == sizeof(double)) {
-          pl = (T)(exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
-        } else {
-          const T h0f = (T)psl[lo];
-          const T del = (T)(psl[lo] - (double)h0f) + (T)dxd * (T)(psl[lo + 1] - psl[lo]);
-          pl = texp<T>(h0f) * texp<T>(del) * lc3;
-        }
-        // k^3 = ((l+1) rc / x)^3
-        const T k3 = cub * rx3[i];
-        part += (double)(F[i] * F[i] * k3 * pl);
       }
-      const double tcl = block_sum(part, red);
-      if (tid == 0) Cl[k] = tcl * geo.dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+      // two block sums
+      for (int o = 16; o > 0; o >>= 1) {
+        part0 += __shfl_down_sync(0xffffffffu, part0, o);
+        part1 += __shfl_down_sync(0xffffffffu, part1, o);
+      }
+      __syncthreads();
+      if ((tid & 31) == 0) {
+        red[0][tid >> 5] = part0;
+        red[1][tid >> 5] = part1;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w2 = 0; w2 < NL_NT / 32; w2++) {
+          t0 += red[0][w2];
+          t1 += red[1][w2];
+        }
+        Cl[k] = t0 * geo.dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+        if (two) Cl[k2] = t1 * geo.dlnchi * 2. / M_PI + ggl[k2 * 2 + 0] - ggl[k2 * 2 + 1];
+      }
     }
     __syncthreads();
     // convergence at the block end (cosmo2D.c:4741-4750)
@@ -776,7 +837,7 @@ static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
   k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
   const size_t sm3 = sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi) +
-                     sizeof(T) * (2 * 2 * (size_t)Q.nmax + 6 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
+                     sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
   cudaFuncSetAttribute(k_nl_loop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   k_nl_loop<T><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q);
 }
