@@ -430,7 +430,15 @@ __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int s
   if (direct) {
     g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
   } else {
-    const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
+    T et;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      // eta = deta i from a two-float split of deta (no FP64 per entry)
+      const float dh = (float)deta, dl = (float)(deta - (double)dh);
+      et = fmaf(dh, (float)i, dl * (float)i);
+    } else {
+      et = deta * i;
+    }
+    const T kk = (T)k, nuj = (T)Q.nu[j];
     ct<T> num, den;
     if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
     else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
@@ -439,6 +447,16 @@ __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int s
   }
   gs[slot * Q.hstride + i] = g;
   return g;
+}
+
+// exp(i a) for an FP64 angle, reduced to [-pi, pi] in FP64
+template <typename T>
+__device__ __forceinline__ ct<T> phasor(double a)
+{
+  a -= 2.0 * M_PI * rint(a * (0.5 / M_PI));
+  T sp, cp;
+  tsincos<T>((T)a, &sp, &cp);
+  return tmk<T>(cp, sp);
 }
 
 template <typename T>
@@ -453,18 +471,24 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
   const double bmag = nu.gb[4][q];
   const int nj = (bmag != 0.0) ? 3 : 2;
   const NLGeom geo = nl_geom(P, pt);
-  // shared: [psl, plkd, pinv: nk doubles][lxk: nchi doubles]
-  //         [fa, fb: nmax complex T][F0, F1, xs: nchi T][plk: nk T]
-  double* psl = (double*)smem_raw;
-  double* plkd = psl + P.pkl_nk;
-  double* pinv = plkd + P.pkl_nk;
-  double* lxk = pinv + P.pkl_nk;
-  ct<T>* fa = (ct<T>*)(lxk + nchi);
+  // shared: [fa, fb: nmax complex T][F0, F1, xs: nchi T][plk: nk T]
+  //   mixed plan: [lxk: nchi float][pcf: 3 nk float, psf: nk float] and the
+  //     FP64 slice psl only during set-up, in fb;
+  //   FP64 plan:  [psl, plkd, pinv: nk double][lxk: nchi double]
+  ct<T>* fa = (ct<T>*)smem_raw;
   ct<T>* fb = fa + Q.nmax;
   T* F0 = (T*)(fb + Q.nmax);
   T* F1 = F0 + nchi;
   T* xs = F1 + nchi;
   T* plk = xs + nchi;
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  float* lxkf = (float*)(plk + P.pkl_nk);
+  float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
+  float* psf = pcf + 3 * P.pkl_nk;  // slope of the slice per cell
+  double* psl = F32 ? (double*)fb : (double*)(plk + P.pkl_nk);
+  double* plkd = psl + P.pkl_nk;
+  double* pinv = plkd + P.pkl_nk;
+  double* lxk = pinv + P.pkl_nk;
   __shared__ double red[2][NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
   const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
@@ -480,15 +504,29 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
     for (int i = tid; i < P.pkl_nk; i += NL_NT) {
       psl[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
       plk[i] = (T)P.pkl_lk[i];
-      plkd[i] = P.pkl_lk[i];
-      pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
+      if (!F32) {
+        plkd[i] = P.pkl_lk[i];
+        pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
+      }
+    }
+    if constexpr (F32) {
+      __syncthreads();
+      for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+        const float h = (float)psl[i];
+        pcf[3 * i] = h;
+        pcf[3 * i + 1] = (float)(psl[i] - (double)h);
+        // the cell width of the FP32 axis, so dx = 1 at the upper edge
+        pcf[3 * i + 2] = (i + 1 < P.pkl_nk) ? 1.0f / ((float)P.pkl_lk[i + 1] - (float)P.pkl_lk[i]) : 0.0f;
+        psf[i] = (i + 1 < P.pkl_nk) ? (float)(psl[i + 1] - psl[i]) : 0.0f;
+      }
     }
   }
   // x and log10(rc / (x coverH0)) at the reversed index nchi-1-i
   // (y = (l+1)/x[nchi-1-i])
   for (int i = tid; i < nchi; i += NL_NT) {
     const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
-    lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
+    if (F32) lxkf[i] = (float)log10(rc / (xr * CL2PT_COVERH0));
+    else lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
     xs[i] = (T)xr;
   }
   const double lrc = log10(rc / CL2PT_COVERH0);
@@ -522,23 +560,28 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
         const int di0 = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
         const double* gd0 = gdir + ((size_t)j * Q.ndirect + (dir0 ? di0 : 0)) * Q.hstride * 2;
         const double* gd1 = gdir + ((size_t)j * Q.ndirect + (dir1 ? di0 + 1 : 0)) * Q.hstride * 2;
+        // phases exp(-i eta_i lnbase): the first entry of this thread from an
+        // FP64-reduced angle, then the FP32 (FP64 plan: FP64) step to the
+        // thread's next entry, i += NL_NT
+        ct<T> e0 = phasor<T>(-(deta * tid) * lnb0), e1 = phasor<T>(-(deta * tid) * lnb1);
+        const ct<T> s0 = phasor<T>(-(deta * NL_NT) * lnb0), s1 = phasor<T>(-(deta * NL_NT) * lnb1);
         for (int i = tid; i < nq; i += NL_NT) {
+          ct<T> c0 = e0, c1 = e1;
+          if constexpr (sizeof(T) == sizeof(double)) {
+            // FP64 plan: exact reduction per entry, as before
+            c0 = phasor<T>(-(deta * i) * lnb0);
+            c1 = phasor<T>(-(deta * i) * lnb1);
+          }
+          e0 = tmul(e0, s0);
+          e1 = tmul(e1, s1);
           const ct<T> tv = tout[j * Q.hstride + i];
           const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, k, deta);
-          // phase exp(-i eta lnbase), argument reduced in FP64
-          double ph = -(deta * i) * lnb0;
-          ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
-          T sp, cp;
-          tsincos<T>((T)ph, &sp, &cp);
-          ct<T> v0 = tmul(tmul(tv, tmk<T>(cp, sp)), g0);
+          ct<T> v0 = tmul(tmul(tv, c0), g0);
           v0.y = -v0.y;  // conj
           ct<T> v1 = tmk<T>((T)0, (T)0);
           if (two) {
             const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, k2, deta);
-            double ph1 = -(deta * i) * lnb1;
-            ph1 -= 2.0 * M_PI * rint(ph1 * (0.5 / M_PI));
-            tsincos<T>((T)ph1, &sp, &cp);
-            v1 = tmul(tmul(tv, tmk<T>(cp, sp)), g1);
+            v1 = tmul(tmul(tv, c1), g1);
             v1.y = -v1.y;
           }
           if (i == 0 || 2 * i == N) {
@@ -560,7 +603,10 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
           // x^nu (nu = 1 or 1.01) and, for magnification, x^2 more
           const T x = xs[i];
           T xp = x;
-          if (num1 != 0.0) xp *= texp<T>((T)(num1 * (lrc - lxk[i]) * 2.302585092994045684));
+          if (num1 != 0.0) {
+            if constexpr (sizeof(T) == sizeof(float)) xp *= __expf((float)num1 * __logf(x));
+            else xp *= texp<T>((T)(num1 * (lrc - lxk[i]) * 2.302585092994045684));
+          }
           if (j == 2) xp *= x * x;
           const ct<T> z = r[Q.pad[j] + i];
           T f0 = z.x * sc0 * xp, f1 = z.y * sc1 * xp;
@@ -576,34 +622,43 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
       double part0 = 0.0, part1 = 0.0;
       const double lk0 = log10(k + 1.), lk1 = log10(k2 + 1.);
+      const float lk0f = (float)lk0, lk1f = (float)lk1;
       const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
+      T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
       for (int i = tid; i < nchi; i += NL_NT) {
         const T rx = rct / xs[i];
         const T rx3 = rx * rx * rx;
         for (int h = 0; h < (two ? 2 : 1); h++) {
-          // p_lin(k, 1): search on the loop-precision axis, in-cell offset and
-          // lnP difference in FP64, exponent split as in the Limber walk
-          const double lkv = (h ? lk1 : lk0) + lxk[i];
+          // p_lin(k, 1) (cosmo3D.c:306-358) on the z = 0 slice
+          const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
           int lo = 0, hi = P.pkl_nk - 1;
-          const T lkt = (T)lkv;
+          const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
           while (hi > lo + 1) {
             const int mid = (lo + hi) >> 1;
             if (plk[mid] > lkt) hi = mid; else lo = mid;
           }
-          const double dxd = (lkv - plkd[lo]) * pinv[lo];
-          T pl;
-          if (sizeof(T) == sizeof(double)) {
-            pl = (T)(exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
-          } else {
-            const T h0f = (T)psl[lo];
-            const T del = (T)(psl[lo] - (double)h0f) + (T)dxd * (T)(psl[lo + 1] - psl[lo]);
-            pl = texp<T>(h0f) * texp<T>(del) * lc3;
-          }
           const T F = h ? F1[i] : F0[i];
           const T k3 = (h ? cub1 : cub0) * rx3;
-          const double v = (double)(F * F * k3 * pl);
-          if (h) part1 += v; else part0 += v;
+          if constexpr (sizeof(T) == sizeof(double)) {
+            const double dxd = (lkv - plkd[lo]) * pinv[lo];
+            const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
+                              (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
+            const double v = F * F * k3 * pl;
+            if (h) part1 += v; else part0 += v;
+          } else {
+            // in-cell offset and exponent in FP32 from the per-cell split
+            // (hi, lo, slope) of the slice
+            const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
+            const float del = pcf[3 * lo + 1] + dx * psf[lo];
+            const float pl = __expf(pcf[3 * lo]) * __expf(del) * lc3;
+            const float v = F * F * k3 * pl;
+            if (h) tp1 += v; else tp0 += v;
+          }
         }
+      }
+      if constexpr (sizeof(T) == sizeof(float)) {
+        part0 = tp0;
+        part1 = tp1;
       }
       // two block sums
       for (int o = 16; o > 0; o >>= 1) {
@@ -836,8 +891,10 @@ static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
-  const size_t sm3 = sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi) +
-                     sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
+  const bool f32 = sizeof(T) == sizeof(float);
+  const size_t sm3 = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
+                     (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
+                          : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
   cudaFuncSetAttribute(k_nl_loop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   k_nl_loop<T><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q);
 }
