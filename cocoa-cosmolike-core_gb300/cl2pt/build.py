@@ -17,6 +17,8 @@ CSRC = os.path.join(PKG, "csrc")
 INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(HERE, "libcl2pt.so")
+LEGACY = os.path.join(HERE, "libcl2pt_legacy.so")
+LEGACY_SRC = os.path.join(CSRC, "legacy", "legacy.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INC}", f"-I{CSRC}"]
@@ -73,7 +75,24 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode:
             print(r.stdout, r.stderr)
             raise RuntimeError("link of libcl2pt.so failed")
+    build_legacy(force)
     return LIB
+
+
+def build_legacy(force: bool = False) -> str:
+    """libcl2pt_legacy.so: the reference-named entry points (host C++ over
+    libcl2pt.so, found next to it at run time)."""
+    if not force and _newer(LEGACY, [LEGACY_SRC, LIB] + headers()):
+        return LEGACY
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", f"-I{INC}", LEGACY_SRC, "-o", LEGACY,
+           f"-L{HERE}", "-lcl2pt", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        print(" ".join(cmd))
+        print(r.stdout, r.stderr)
+        raise RuntimeError("build of libcl2pt_legacy.so failed")
+    return LEGACY
 
 
 if __name__ == "__main__":

@@ -736,6 +736,16 @@ extern "C" const char* cl2pt_status_string(int s)
 
 extern "C" int cl2pt_last_launch_count(const cl2pt_plan* p) { return p ? p->last_launches : 0; }
 
+extern "C" int cl2pt_node_limits(const cl2pt_plan* p, double lim_ss[3], double lim_g[3])
+{
+  if (!p) return CL2PT_ERR_ARG;
+  for (int i = 0; i < 3; i++) {
+    if (lim_ss) lim_ss[i] = p->lim_ss[i];
+    if (lim_g) lim_g[i] = p->lim_g[i];
+  }
+  return CL2PT_OK;
+}
+
 // ------------------------------------------------------------ evaluation
 static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b)
 {

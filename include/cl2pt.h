@@ -226,6 +226,11 @@ int cl2pt_kernel_times(cl2pt_plan* plan, double* ms, int* launches);
 /* Number of kernel launches issued by the last eval call. */
 int cl2pt_last_launch_count(const cl2pt_plan* plan);
 
+/* The C_l node grids of the plan: nodes nint .. of the ss (gs, gg) tables
+ * sit at l = exp(lim[0] + i lim[2]), lim[1] = ln of the last node
+ * (the reference's table limits, cosmo2D.c:1635-1640, 2209-2214). */
+int cl2pt_node_limits(const cl2pt_plan* plan, double lim_ss[3], double lim_g[3]);
+
 /* Human-readable text for a status code. */
 const char* cl2pt_status_string(int status);
 
