@@ -243,8 +243,47 @@ __device__ __forceinline__ void dft4(ct<T>* v, int sign)
   v[3] = tmk<T>(b.x - d.x, b.y - d.y);
 }
 
-// Stockham transform of size N in the loop precision (same structure as
-// block_fft, with specialised radix-2/4 butterflies).
+// One Stockham stage of radix R (compile-time, so the butterfly stays in
+// registers): out[(j/Ns) Ns R + k + r Ns] = DFT_R over r of
+// in[j + r N/R] w^(r k tstep), k = j mod Ns.
+template <typename T, int R>
+__device__ __forceinline__ void stockham_stage(const ct<T>* __restrict__ in, ct<T>* __restrict__ out, int N,
+                                               int Ns, const ct<T>* __restrict__ tw, int sign)
+{
+  const int NR = N / R;
+  const int tstep = N / (Ns * R);
+  ct<T> w[R];
+#pragma unroll
+  for (int m = 0; m < R; m++) {
+    ct<T> x = tw[m * NR];
+    if (sign < 0) x.y = -x.y;
+    w[m] = x;
+  }
+  for (int j = threadIdx.x; j < NR; j += NL_NT) {
+    const int k = j % Ns;
+    ct<T> v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      ct<T> x = in[j + r * NR];
+      if (r && k) {
+        ct<T> t = tw[r * k * tstep];
+        if (sign < 0) t.y = -t.y;
+        x = tmul(x, t);
+      }
+      v[r] = x;
+    }
+    if constexpr (R == 2) dft2(v);
+    else if constexpr (R == 4) dft4(v, sign);
+    else dft_small<T, R>(v, w);
+    const int dst = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) out[dst + r * Ns] = v[r];
+  }
+}
+
+// Stockham transform of size N in the loop precision over the factors
+// fac[0..nf-1] (4, 2, 3, 5, 7), ping-ponging in/out; returns the buffer
+// holding the result.
 template <typename T>
 __device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, int N, const int* fac, int nf,
                               const ct<T>* __restrict__ tw, int sign)
@@ -252,35 +291,12 @@ __device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, int N, const int* fac, int 
   int Ns = 1;
   for (int s = 0; s < nf; s++) {
     const int R = fac[s];
-    const int NR = N / R;
-    const int tstep = N / (Ns * R);
-    ct<T> w[7];
-    for (int m = 0; m < R; m++) {
-      ct<T> x = tw[m * NR];
-      if (sign < 0) x.y = -x.y;
-      w[m] = x;
-    }
-    for (int j = threadIdx.x; j < NR; j += NL_NT) {
-      const int k = j % Ns;
-      ct<T> v[7];
-      for (int r = 0; r < R; r++) {
-        ct<T> x = in[j + r * NR];
-        if (r && k) {
-          ct<T> tw_ = tw[r * k * tstep];
-          if (sign < 0) tw_.y = -tw_.y;
-          x = tmul(x, tw_);
-        }
-        v[r] = x;
-      }
-      switch (R) {
-        case 2: dft2(v); break;
-        case 4: dft4(v, sign); break;
-        case 3: dft_small<T, 3>(v, w); break;
-        case 5: dft_small<T, 5>(v, w); break;
-        default: dft_small<T, 7>(v, w); break;
-      }
-      const int dst = (j / Ns) * Ns * R + k;
-      for (int r = 0; r < R; r++) out[dst + r * Ns] = v[r];
+    switch (R) {
+      case 2: stockham_stage<T, 2>(in, out, N, Ns, tw, sign); break;
+      case 3: stockham_stage<T, 3>(in, out, N, Ns, tw, sign); break;
+      case 4: stockham_stage<T, 4>(in, out, N, Ns, tw, sign); break;
+      case 5: stockham_stage<T, 5>(in, out, N, Ns, tw, sign); break;
+      default: stockham_stage<T, 7>(in, out, N, Ns, tw, sign); break;
     }
     __syncthreads();
     ct<T>* t = in;

@@ -1298,6 +1298,15 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       if (use_nl) {
         Params Pg = P;
         Pg.probes = CL2PT_PROBE_WTHETA;
+        // the FFTLog hand-over reads the node table only below LMAX_NOLIMBER
+        // (interpol1d in ln l): the Limber gg pass stops two nodes past it
+        {
+          const int m = (int)floor((log((double)P.lmax_nolimber) - p->lim_g[0]) / p->lim_g[2]) + 3;
+          if (m >= 2 && m < P.n_ell) {
+            Pg.n_ell = m;
+            Pg.nnode_g = p->nint + m;
+          }
+        }
         cl2pt::launch_limber(Pg, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
         if (P.one_loop) cl2pt::launch_extra(Pg, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
         cl2pt::launch_nonlimber(Pg, p->nlq, s, &launches, hk);
