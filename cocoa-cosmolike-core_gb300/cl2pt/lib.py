@@ -71,6 +71,9 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
+    lib.cl2pt_vjp_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]
     lib.cl2pt_jacobian_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_int,
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p]
@@ -250,6 +253,39 @@ class Plan:
                                     cv.ctypes.data, dv.ctypes.data, lbar.ctypes.data,
                                     None if lbarl is None else lbarl.ctypes.data,
                                     C.addressof(nbar), None), "cl2pt_vjp_real")
+        nb = np.frombuffer(bytes(nbar), dtype=np.float64).reshape(n, -1).copy()
+        if lbarl is not None:
+            return dv, lbar, nb, lbarl
+        return dv, lbar, nb
+
+    def vjp_fourier(self, omega_m, h0, chi, G, lnP, nuisance, ell, cot, lmax_shear=1e30, mask=None,
+                    lnPL=None):
+        """Value and VJP of the Fourier vector on host arrays: (dv, lnP_bar,
+        nu_bar[, lnPL_bar]) as vjp_real."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        nt = C.c_int()
+        check(load().cl2pt_fourier_sizes(self.h, len(ell), None, None, None, C.byref(nt)))
+        cv = np.ascontiguousarray(np.broadcast_to(cot, (n, nt.value)), dtype=np.float64)
+        dv = np.zeros((n, nt.value))
+        lbar = np.zeros((n, arrs[3].size // n))
+        lbarl = None if lpl is None else np.zeros((n, lpl.size // n))
+        nbar = (abi.Nuisance * n)()
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        check(load().cl2pt_vjp_fourier(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                       mk.ctypes.data if mk is not None else None, cv.ctypes.data,
+                                       dv.ctypes.data, lbar.ctypes.data,
+                                       None if lbarl is None else lbarl.ctypes.data,
+                                       C.addressof(nbar), None), "cl2pt_vjp_fourier")
         nb = np.frombuffer(bytes(nbar), dtype=np.float64).reshape(n, -1).copy()
         if lbarl is not None:
             return dv, lbar, nb, lbarl

@@ -178,6 +178,74 @@ __global__ void k_vjp_handover(Params P, VJPParams V)
   }
 }
 
+// Adjoint of k_assemble_fourier: C_bar on the caller's multipoles (shear
+// rows [EE; BB = 0] with TATT), ggl, Limber gg at the caller's
+// multipoles, the FFTLog C_l at int(l) below LMAX_NOLIMBER (cnl_bar, may
+// collect several bins), and the shear-calibration gradient.
+__global__ void k_vjp_assemble_fourier(Params P, VJPParams V, int nell, const double* __restrict__ ell,
+                                       double lmax_shear, int use_nl)
+{
+  const int pt = blockIdx.y;
+  const int s1 = nell * P.pss, s2 = s1 + nell * P.pgs, n_total = s2 + nell * P.nl;
+  const int Kx = (P.tatt ? 2 : 1) * nell;  // C_bar_ss rows: [EE; BB] with TATT
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double* v = V.cot + (size_t)pt * n_total;
+  double* mbar = V.nu_bar[pt].shear_m;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_total; i += gridDim.x * blockDim.x) {
+    const double vi = (V.mask && !V.mask[i]) ? 0.0 : v[i];
+    if (i < s1) {
+      const int pr = i / nell, j = i - pr * nell;
+      double c = 0.0;
+      if ((P.probes & CL2PT_PROBE_XI) && ell[j] < lmax_shear) {
+        const int za = P.z1[pr], zb = P.z2[pr];
+        const double ca = 1.0 + nu.shear_m[za], cb = 1.0 + nu.shear_m[zb];
+        c = vi * ca * cb;
+        const double t = P.tab_ss[((size_t)pt * P.pss + pr) * P.nnode_ss + j];
+        if (vi != 0.0) {
+          atomicAdd(mbar + za, vi * t * cb);
+          atomicAdd(mbar + zb, vi * t * ca);
+        }
+      }
+      V.cbar_ss[((size_t)pt * P.pss + pr) * Kx + j] = c;
+      if (P.tatt) V.cbar_ss[((size_t)pt * P.pss + pr) * Kx + nell + j] = 0.0;
+    } else if (i < s2) {
+      const int r = i - s1, pr = r / nell, j = r - pr * nell;
+      double c = 0.0;
+      if (P.probes & CL2PT_PROBE_GAMMAT) {
+        const int zs = P.zs[pr];
+        const double cs = 1.0 + nu.shear_m[zs];
+        c = vi * cs;
+        if (vi != 0.0) atomicAdd(mbar + zs, vi * P.tab_gs[((size_t)pt * P.pgs + pr) * P.nnode_g + j]);
+      }
+      V.cbar_gs[((size_t)pt * P.pgs + pr) * nell + j] = c;
+    } else {
+      const int r = i - s2, q = r / nell, j = r - q * nell;
+      double c = 0.0;
+      if (P.probes & CL2PT_PROBE_WTHETA) {
+        if (use_nl && ell[j] < P.lmax_nolimber) {
+          if (vi != 0.0)
+            atomicAdd(&V.cnl_bar[((size_t)pt * P.nl + q) * P.lmax_nolimber + (int)(ell[j] + 1e-13)], vi);
+        } else {
+          c = vi;
+        }
+      }
+      V.cbar_gg[((size_t)pt * P.nl + q) * nell + j] = c;
+    }
+  }
+}
+
+// [cnl_bar; 0] as the non-Limber contraction columns of the hand-over adjoint
+__global__ void k_vjp_fourier_w(Params Pg, VJPParams V)
+{
+  const int pt = blockIdx.y;
+  const int LNL = Pg.lmax_nolimber, K = Pg.nnode_g;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Pg.nl * (LNL + K); i += gridDim.x * blockDim.x) {
+    const int q = i / (LNL + K), k = i - q * (LNL + K);
+    V.cbar_w[((size_t)pt * Pg.nl + q) * (LNL + K) + k] =
+        (k < LNL) ? V.cnl_bar[((size_t)pt * Pg.nl + q) * LNL + k] : 0.0;
+  }
+}
+
 __device__ __forceinline__ double block_sum_d(double v, double* red)
 {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -346,6 +414,65 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
 }
 
 }  // namespace
+
+void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, const NLParams& Q, int nell,
+                        const double* ell, double lmax_shear, const double* lfac_g_std, cudaStream_t s,
+                        int* launches)
+{
+  const int n_total = nell * (Pf.pss + Pf.pgs + Pf.nl);
+  launch_gtab_dz(Pf, V.dgsrc, s);
+  if (Pf.one_loop) launch_vjp_extra(Pf, V, -1, s);
+  if (Pg) cudaMemsetAsync(V.cnl_bar, 0, sizeof(double) * (size_t)Pf.B * Pf.nl * Pf.lmax_nolimber, s);
+  k_vjp_assemble_fourier<<<dim3((n_total + 255) / 256, Pf.B), 256, 0, s>>>(Pf, V, nell, ell, lmax_shear,
+                                                                          Pg ? 1 : 0);
+  *launches += 3;
+  // the pass at the caller's multipoles (node tables of stride nell)
+  if (Pf.probes & CL2PT_PROBE_XI) {
+    launch_vjp_limber(Pf, V, 0, s);
+    (*launches)++;
+    if (Pf.tatt) {
+      launch_vjp_extra(Pf, V, 0, s);
+      (*launches)++;
+    }
+  }
+  if ((Pf.probes & CL2PT_PROBE_GAMMAT) && Pf.pgs > 0) {
+    launch_vjp_limber(Pf, V, 1, s);
+    (*launches)++;
+    if (Pf.tatt || Pf.one_loop) {
+      launch_vjp_extra(Pf, V, 1, s);
+      (*launches)++;
+    }
+  }
+  if (Pf.probes & CL2PT_PROBE_WTHETA) {
+    VJPParams V1 = V;
+    V1.ggl_bar = nullptr;
+    launch_vjp_limber(Pf, V1, 2, s);
+    (*launches)++;
+    if (Pf.one_loop) {
+      launch_vjp_extra(Pf, V1, 2, s);
+      (*launches)++;
+    }
+  }
+  // the FFTLog clustering below LMAX_NOLIMBER and its standard-node Limber
+  // hand-over
+  if (Pg) {
+    VJPParams V2 = V;
+    V2.cbar_gg = V.cbar_gg2;
+    V2.lfac_g = lfac_g_std;
+    const int Kw = Pg->lmax_nolimber + Pg->nnode_g;
+    k_vjp_fourier_w<<<dim3((Pg->nl * Kw + 255) / 256, Pg->B), 256, 0, s>>>(*Pg, V2);
+    k_vjp_handover<<<dim3(Pg->B, Pg->nl), 256, 0, s>>>(*Pg, V2);
+    launch_vjp_limber(*Pg, V2, 2, s);
+    *launches += 3;
+    if (Pg->one_loop) {
+      launch_vjp_extra(*Pg, V2, 2, s);
+      (*launches)++;
+    }
+    launch_nonlimber_vjp(*Pg, Q, V2.cnl_bar, V2.lnpl_bar, V2.nu_bar, s, launches);
+  }
+  k_vjp_nodes<<<dim3(Pf.B, 1 + 2 * Pf.nl), NB_NT, 0, s>>>(Pf, V);
+  (*launches)++;
+}
 
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
                 const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,

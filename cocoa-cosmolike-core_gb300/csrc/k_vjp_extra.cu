@@ -322,7 +322,7 @@ __global__ void k_vjpx_gg(Params P, VJPParams V)
     for (int L = 0; L < K; L++) add(V.lfac_g + 6 * L, cb[L]);
     if (V.ggl_bar) {
       const double* gb = V.ggl_bar + b0 * LNL * 2;
-      for (int L = 0; L < LNL; L++) add(V.lfac_g + 6 * (K + L), gb[2 * L]);
+      for (int L = 0; L < LNL; L++) add(V.lfac_gi + 6 * L, gb[2 * L]);
     }
     // wgg_1l = W_gal^2 D^4 (b1 b2, b2^2/4, b1 bs2, b2 bs2/2, bs2^2/4)
     const cl2pt_nuisance& nu = P.nu[pt];

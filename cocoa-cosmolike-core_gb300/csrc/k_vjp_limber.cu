@@ -437,7 +437,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     for (int L = 0; L < LNL; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
-      const double* fac = V.lfac_g + 6 * (K + L);
+      const double* fac = V.lfac_gi + 6 * L;
       if (nd.fK * fac[5] > chi_amin) continue;
       const T s = s_of(fac);
       const double lk = fac[0] - nd.lfk;
@@ -453,7 +453,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
     pw_flush(wl, barl, P.pkl_nz, jl, dyl);
   }
-  V.lbar_gg[b0 * nn + p] = lbar;
+  V.lbar_gg[b0 * nn + p] += lbar;  // zeroed per wave; the Fourier path adds two passes
 }
 
 template <typename T>

@@ -71,6 +71,10 @@ struct VJPParams {
   // (l+3/2)/(l+1/2)) on the C_l nodes, then at l = 0..LNL-1
   const double* lfac_ss;
   const double* lfac_g;
+  const double* lfac_gi;   // the same factors at l = 0..LNL-1
+  // Fourier path: second clustering C_bar (standard nodes of the FFTLog
+  // hand-over pass) [B][nl][nnode_g]
+  double* cbar_gg2;
   // source photo-z: d g_tomo / d dz_s [B][ns][n_a], and the wave's point
   // masses [B][nl] (or null)
   double* dgsrc;
@@ -94,5 +98,12 @@ void launch_vjp_limber(const Params& P, const VJPParams& V, int which, cudaStrea
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
                 const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
                 const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk);
+// Adjoint of the Fourier vector (k_vjp.cu): Pf is the pass at the caller's
+// multipoles (V.lfac_* hold their factors); Pg, when use_nl, the clustering
+// pass on the standard nodes with the FFTLog below LMAX_NOLIMBER (lfac_g_std
+// its node factors)
+void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, const NLParams& Q, int nell,
+                        const double* ell, double lmax_shear, const double* lfac_g_std, cudaStream_t s,
+                        int* launches);
 
 }  // namespace cl2pt

@@ -860,13 +860,15 @@ static int vjp_prepare(cl2pt_plan* p)
                        W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
                        W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL +
                        W * ns * c.n_a + 2 * W * ns * p->n_ss + 3 * W * nl * ns * p->n_ss +
-                       5 * W * p->pss * p->n_ss + W;
+                       5 * W * p->pss * p->n_ss + W * nl * p->nnode_g + W;
     // (a failed allocation leaves the plan usable for evaluation)
     int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
+    p->vjp_cot_cap = (size_t)p->max_batch * p->n_total;
     if (!a) a = dalloc(p, &p->d_vjp_lnp, (size_t)p->max_batch * p->P.pk_nk * p->P.pk_nz);
     if (!a) a = dalloc(p, &p->d_vjp_nu, (size_t)p->max_batch);
     if (!a && p->d_in_lnPL)
       a = dalloc(p, &p->d_vjp_lnpl, (size_t)p->max_batch * p->P.pkl_nk * p->P.pkl_nz);
+    if (!a) a = dalloc(p, &p->d_lfac_f, 8 * (size_t)std::max(p->nnode_ss, p->nnode_g));
     if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
     if (a) {
       p->d_vjp_ws = nullptr;
@@ -893,6 +895,43 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+}
+
+extern "C" int cl2pt_vjp_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
+                                 double lmax_shear, const int* mask, const double* cot, double* dv,
+                                 double* lnP_bar, double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream)
+{
+  if (!p || !cot || !lnP_bar || !nu_bar) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
+  st = vjp_prepare(p);
+  if (st) return st;
+  FourierReq fr;
+  fr.nell = nell;
+  fr.ell = ell;
+  fr.lmax_shear = lmax_shear;
+  int n_total = 0;
+  cl2pt_fourier_sizes(p, nell, nullptr, nullptr, nullptr, &n_total);
+  if (b->where == CL2PT_DEVICE && !dv) {
+    st = fourier_staging(p, n_total);
+    if (st) return st;
+    dv = p->d_dv_f;
+  }
+  if (b->where == CL2PT_HOST && (size_t)n_total * p->max_batch > p->vjp_cot_cap) {
+    // the cotangent staging grows to the Fourier vector length
+    double* c = nullptr;
+    st = dalloc(p, &c, (size_t)n_total * p->max_batch);
+    if (st) return st;
+    p->d_vjp_cot = c;
+    p->vjp_cot_cap = (size_t)n_total * p->max_batch;
+  }
+  VJPReq vr;
+  vr.cot = cot;
+  vr.lnp_bar = lnP_bar;
+  vr.lnpl_bar = lnPL_bar;
+  vr.nu_bar = nu_bar;
+  return internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr, &vr);
 }
 
 extern "C" int cl2pt_jacobian_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
@@ -1218,10 +1257,12 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.wbar_gs2 = w; w += (size_t)W * nl * ns * p->n_ss;
     V0.wbar_gsk = w; w += (size_t)W * nl * ns * p->n_ss;
     V0.cx_ss = w; w += (size_t)5 * W * p->pss * p->n_ss;
+    V0.cbar_gg2 = w; w += (size_t)W * nl * p->nnode_g;
     V0.one_loop_on = (int*)w;
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
     V0.lfac_g = p->d_lfac_g;
+    V0.lfac_gi = p->d_lfac_g + 6 * (size_t)p->nnode_g;
   }
   int launches = 0;
   struct HookCtx { cl2pt_plan* p; cudaStream_t s; cudaEvent_t (*ev)(cl2pt_plan*); };
@@ -1251,6 +1292,48 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         h->p->recs.back().b = e;
       }
     };
+  }
+  // per-wave adjoint set-up: zero the accumulated adjoints, offset the views
+  auto vjp_wave = [&](const Params& P, int w0, cl2pt::VJPParams& V) -> int {
+    const int ns = p->cfg.n_source, nl = p->cfg.n_lens;
+    CUDA_OK(cudaMemsetAsync(V0.wbar_ss, 0, sizeof(double) * (size_t)P.B * ns * p->n_ss, s));
+    CUDA_OK(cudaMemsetAsync(V0.wbar_gx, 0, sizeof(double) * (size_t)P.B * nl * ns * p->n_ss, s));
+    CUDA_OK(cudaMemsetAsync(V0.lbar_gg, 0, sizeof(double) * (size_t)P.B * nl * p->n_gg, s));
+    if (P.tatt || P.one_loop) {
+      const size_t a1 = sizeof(double) * (size_t)P.B * ns * p->n_ss;
+      const size_t a2 = sizeof(double) * (size_t)P.B * nl * ns * p->n_ss;
+      for (double* q : {V0.wbar_ssb, V0.wbar_ss2}) CUDA_OK(cudaMemsetAsync(q, 0, a1, s));
+      for (double* q : {V0.wbar_gsb, V0.wbar_gs2, V0.wbar_gsk}) CUDA_OK(cudaMemsetAsync(q, 0, a2, s));
+      CUDA_OK(cudaMemsetAsync(V0.cx_ss, 0, sizeof(double) * (size_t)5 * P.B * p->pss * p->n_ss, s));
+    }
+    V = V0;
+    V.cot = vcot + (size_t)w0 * n_total;
+    V.dv = ddv + (size_t)w0 * n_total;
+    V.lnp_bar = vlnp + (size_t)w0 * nP;
+    V.lnpl_bar = vlnpl + (size_t)w0 * (sep_lin ? nPL : nP);
+    V.nu_bar = vnu + w0;
+    V.pm = dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr;
+    return CL2PT_OK;
+  };
+  if (vr && fourier) {
+    // multipole factors of the caller's l for the adjoint sweeps
+    std::vector<double> fs, fg;
+    for (int i = 0; i < fr->nell; i++) {
+      const double l = fr->ell[i], lp = l + 0.5, tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
+      fs.push_back(log10(lp));
+      fs.push_back(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
+      fg.push_back(log10(lp));
+      fg.push_back(tmp > 0 ? sqrt(tmp) / (lp * lp) : 0.0);
+      fg.push_back(l * (l + 1.) / (lp * lp));
+      fg.push_back((1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.)));
+      fg.push_back(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
+      fg.push_back((lp + 1.0) / lp);
+    }
+    CUDA_OK(cudaMemcpyAsync(p->d_lfac_f, fs.data(), sizeof(double) * fs.size(), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_lfac_f + 2 * (size_t)fr->nell, fg.data(), sizeof(double) * fg.size(),
+                            cudaMemcpyHostToDevice, s));
+    // the host vectors must outlive the copies
+    CUDA_OK(cudaStreamSynchronize(s));
   }
   for (int w0 = 0; w0 < n; w0 += p->wave) {
     Params P = T;
@@ -1295,8 +1378,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         for (int i = 0; i < fr->nell; i++) any |= fr->ell[i] < P.lmax_nolimber;
         use_nl = any;
       }
+      Params Pg = P;
       if (use_nl) {
-        Params Pg = P;
         Pg.probes = CL2PT_PROBE_WTHETA;
         // the FFTLog hand-over reads the node table only below LMAX_NOLIMBER
         // (interpol1d in ln l): the Limber gg pass stops two nodes past it
@@ -1318,6 +1401,15 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                                  fr->csr_out, s);
         launches++;
       }
+      if (vr) {
+        cl2pt::VJPParams V;
+        const int st2 = vjp_wave(P, w0, V);
+        if (st2) return st2;
+        V.lfac_ss = p->d_lfac_f;
+        V.lfac_g = p->d_lfac_f + 2 * (size_t)fr->nell;
+        cl2pt::launch_vjp_fourier(Pf, use_nl ? &Pg : nullptr, V, p->nlq, fr->nell, p->d_ell_f, fr->lmax_shear,
+                                  p->d_lfac_g, s, &launches);
+      }
     } else {
       cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       if (P.tatt || P.one_loop) cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
@@ -1328,23 +1420,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
                              ddv + (size_t)w0 * p->n_total, s, &launches, hk);
       if (vr) {
-        const int ns = p->cfg.n_source, nl = p->cfg.n_lens;
-        CUDA_OK(cudaMemsetAsync(V0.wbar_ss, 0, sizeof(double) * (size_t)P.B * ns * p->n_ss, s));
-        CUDA_OK(cudaMemsetAsync(V0.wbar_gx, 0, sizeof(double) * (size_t)P.B * nl * ns * p->n_ss, s));
-        if (P.tatt || P.one_loop) {
-          const size_t a1 = sizeof(double) * (size_t)P.B * ns * p->n_ss;
-          const size_t a2 = sizeof(double) * (size_t)P.B * nl * ns * p->n_ss;
-          for (double* q : {V0.wbar_ssb, V0.wbar_ss2}) CUDA_OK(cudaMemsetAsync(q, 0, a1, s));
-          for (double* q : {V0.wbar_gsb, V0.wbar_gs2, V0.wbar_gsk}) CUDA_OK(cudaMemsetAsync(q, 0, a2, s));
-          CUDA_OK(cudaMemsetAsync(V0.cx_ss, 0, sizeof(double) * (size_t)5 * P.B * p->pss * p->n_ss, s));
-        }
-        cl2pt::VJPParams V = V0;
-        V.cot = vcot + (size_t)w0 * n_total;
-        V.dv = ddv + (size_t)w0 * n_total;
-        V.lnp_bar = vlnp + (size_t)w0 * nP;
-        V.lnpl_bar = vlnpl + (size_t)w0 * (sep_lin ? nPL : nP);
-        V.nu_bar = vnu + w0;
-        V.pm = dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr;
+        cl2pt::VJPParams V;
+        const int st2 = vjp_wave(P, w0, V);
+        if (st2) return st2;
         cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl,
                           p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       }

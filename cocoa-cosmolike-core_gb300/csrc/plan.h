@@ -81,11 +81,13 @@ struct cl2pt_plan {
   // adjoint (cl2pt_vjp_real): per-wave workspace and host staging, allocated
   // on first use
   double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
-  double* d_vjp_cot = nullptr;         // [max_batch][n_total]
+  double* d_vjp_cot = nullptr;         // [max_batch][n_total] (grown for Fourier vectors)
+  size_t vjp_cot_cap = 0;
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]
   double* d_vjp_lnpl = nullptr;        // [max_batch][pkl_nk * pkl_nz]
   double* d_lfac_ss = nullptr;         // per-multipole constants of the adjoint sweeps
   double* d_lfac_g = nullptr;
+  double* d_lfac_f = nullptr;          // the same for the caller's multipoles (Fourier)
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;

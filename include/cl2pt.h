@@ -164,6 +164,15 @@ int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
 
+/* Value and vector-Jacobian product of the Fourier vector of
+ * cl2pt_eval_fourier (same arguments; cot [n][n_total(nell)]), with the
+ * gradients of cl2pt_vjp_real: through the Limber passes at the caller's
+ * multipoles and, below LMAX_NOLIMBER, the FFTLog clustering C_l and its
+ * Limber hand-over. */
+int cl2pt_vjp_fourier(cl2pt_plan* plan, const cl2pt_batch* batch, int nell, const double* ell,
+                      double lmax_shear, const int* mask, const double* cot, double* dv,
+                      double* lnP_bar, double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
+
 /* Jacobian of the real-space data vector of ONE parameter point
  * (batch->n == 1) for the data-vector rows rows[0..nrows-1] (host array;
  * rows NULL: all n_total rows in order):
