@@ -291,6 +291,23 @@ class Plan:
             return dv, lbar, nb, lbarl
         return dv, lbar, nb
 
+    def vjp_fourier_device(self, omega_m, h0, chi, G, lnP, nuisance, ell, cot, dv, lnP_bar, nu_bar,
+                           lmax_shear=1e30, mask=None, lnPL=None, lnPL_bar=None, stream=None):
+        """Device form of vjp_fourier (CUDA tensors as in vjp_real_device)."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        st = load().cl2pt_vjp_fourier(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                      None if mask is None else mask.data_ptr(), cot.data_ptr(),
+                                      None if dv is None else dv.data_ptr(), lnP_bar.data_ptr(),
+                                      None if lnPL_bar is None else lnPL_bar.data_ptr(),
+                                      nu_bar.data_ptr(), stream)
+        check(st, "cl2pt_vjp_fourier")
+
     def jacobian_real(self, omega_m, h0, chi, G, lnP, nuisance, rows=None, mask=None, pm=None,
                       lnPL=None):
         """Jacobian of one point's data vector (host arrays, n = 1): returns
