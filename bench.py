@@ -42,6 +42,23 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest x over the ranks of the default process group (the job's
+    time is its slowest rank's); x itself without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def walker_seed(base: int, rank: int) -> int:
+    """Replicas: every rank evaluates its own walkers."""
+    return base + rank
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -230,7 +247,7 @@ def run_serving(args):
     cbuild.build()
     w = workloads.make("fourier_serving")
     B = args.batch if args.batch != 512 else 4096
-    data = make_batch(w, B, seed=300 + rank)
+    data = make_batch(w, B, seed=walker_seed(300, rank))
     ptr, idx = workloads.scale_cuts(w, B, seed=rank)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=B)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
@@ -264,10 +281,7 @@ def run_serving(args):
     plan.check_errors(sptr)
     lat = np.array([evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)])
     ms = float(lat.sum())
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms / 1e3)
     # e2e: host arrays (pinned) through the public ragged call
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -361,6 +375,18 @@ def run_serving(args):
         torch.distributed.destroy_process_group()
 
 
+def profile_traffic(name, points):
+    """DRAM bytes per launch from a committed ncu summary (scaled to the
+    points of one launch), or None."""
+    try:
+        txt = open(os.path.join(ROOT, "profiles", name)).read()
+        b = float(txt.split("traffic_bytes_per_launch:")[1].split()[0])
+        n = float(txt.split("points_per_launch:")[1].split()[0])
+        return b * points / n
+    except (OSError, IndexError, ValueError):
+        return None
+
+
 def plan_fourier_size(plan, nell):
     import ctypes as C
     from cl2pt import lib
@@ -384,7 +410,7 @@ def run_fastpt(args):
     from cl2pt import build as cbuild
     cbuild.build()
     B = args.batch
-    k, P, _ = workloads.fastpt_spectra(B, seed=100 + rank)
+    k, P, _ = workloads.fastpt_spectra(B, seed=walker_seed(100, rank))
     pb = lib.FastPT.for_bias(k, max_spec=B)
     pi = lib.FastPT.for_ia(k, max_spec=B)
     fx = torch.from_numpy(P).to(dev)
@@ -419,10 +445,7 @@ def run_fastpt(args):
     pi.check_errors()
     ms_b, ms_i = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
     ms = ms_b + ms_i
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms / 1e3)
     waves_b, waves_i = -(-B // 512), -(-B // 256)
     launches = (3 * waves_b + 4 * waves_i + 1) * args.steps
@@ -516,7 +539,7 @@ def main():
     cbuild.build()
     w = workloads.make(args.workload)
     B = args.batch
-    data = make_batch(w, B, seed=100 + rank)  # replicas: each rank its own walkers
+    data = make_batch(w, B, seed=walker_seed(100, rank))
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=B)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     d_om, d_h0, d_chi, d_G, d_lnP = (T(data[k]) for k in ("om", "h0", "chi", "G", "lnP"))
@@ -554,10 +577,7 @@ def main():
     plan.set_timing(False)
     plan.check_errors(sptr)
     launches = plan.launches() * args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms / 1e3)
 
     # ---- e2e through the C ABI with pinned host buffers
@@ -572,10 +592,7 @@ def main():
     for _ in range(e2e_steps):
         dv_host = plan.eval_real(h["om"], h["h0"], h["chi"], h["G"], h["lnP"], data["nus"])
     te = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([te], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        te = float(t.item())
+    te = max_over_ranks(te, dev)
     e2e = world * B * e2e_steps / te
     h2d = sum(h[k].nbytes for k in h) + B * 13 * 20 * 8
     d2h = dv_host.nbytes
@@ -614,7 +631,7 @@ def main():
     if not args.no_grad:
         w4 = workloads.make("real_3x2pt_tatt")
         B4 = min(B, 256)
-        data4 = make_batch(w4, B4, seed=200 + rank)
+        data4 = make_batch(w4, B4, seed=walker_seed(200, rank))
         plan4 = lib.Plan(w4.cfg, w4.src, w4.lens, w4.base, lib.PREC_MIXED, max_batch=B4)
         t4 = [T(data4[k]) for k in ("om", "h0", "chi", "G", "lnP")]
         vg4 = value_grad(plan4, w4, data4, *t4, T(data4["nub"]), None, stream, args)
@@ -633,7 +650,7 @@ def main():
         "k_limber_gs": 8 * nk * nz + 8 * pgs * nnode,
         "k_limber_gg": 8 * nk * nz + 8 * pgg * nnode,
         "k_limber_ggl": 8 * nk * nz + 16 * pgg * w.cfg.lmax_nolimber,
-        "k_nonlimber": 8 * (plan.shapes["chi"] + plan.shapes["G"]) + 8 * pgg * w.cfg.lmax_nolimber,
+        "k_nonlimber": 8 * (plan.shapes["chi"] + plan.shapes["G"]) + 16 * nk + 8 * pgg * w.cfg.lmax_nolimber,
         "k_contract": 8 * (pss + pgs + pgg) * nnode + 8 * plan.n_total,
         "k_gtab": 8 * plan.shapes["chi"] + 8 * w.cfg.n_source * w.cfg.n_a,
         "k_nodes": 8 * (plan.shapes["chi"] + plan.shapes["G"]),
@@ -642,6 +659,7 @@ def main():
     pts_per_launch = min(B, 256)
     alg = per_point[top] * pts_per_launch
     achieved = alg / (per_launch_ms / 1e3) / 1e9
+    traffic = profile_traffic("k_nl_loop_real_3x2pt_traffic.md", pts_per_launch) if top == "k_nonlimber" else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -655,8 +673,10 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                     "peak_source": src},
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "traffic_source": "profiles/k_nl_loop_real_3x2pt_traffic.md (ncu, multipole-loop launch)"
+                     if traffic else None,
+                     "algorithmic_bytes_per_launch": alg, "peak_source": src},
         "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items()},
         "clocks": clocks,
         "fp64_plain_gpu": {"value": fp64, "unit": UNIT,

@@ -71,6 +71,7 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
+    lib.cl2pt_cl_nonlimber.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_vjp_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]
@@ -257,6 +258,25 @@ class Plan:
         if lbarl is not None:
             return dv, lbar, nb, lbarl
         return dv, lbar, nb
+
+    def cl_nonlimber(self, omega_m, h0, chi, G, lnP, nuisance, lnPL=None):
+        """Batched non-Limber C_l: (cl [n][n_lens][lmax_nolimber], conv_l [n][n_lens])."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        nl, L = self.cfg.n_lens, self.cfg.lmax_nolimber
+        cl = np.zeros((n, nl, L))
+        conv = np.zeros((n, nl), dtype=np.int32)
+        check(load().cl2pt_cl_nonlimber(self.h, C.byref(b), cl.ctypes.data, conv.ctypes.data, None),
+              "cl2pt_cl_nonlimber")
+        return cl, conv
 
     def vjp_fourier(self, omega_m, h0, chi, G, lnP, nuisance, ell, cot, lmax_shear=1e30, mask=None,
                     lnPL=None):

@@ -810,8 +810,16 @@ struct VJPReq {
   cl2pt_nuisance* nu_bar = nullptr;
 };
 
+// Extra per-wave outputs: the non-Limber C_l and hand-over multipoles
+// (device pointers, [n][n_lens][lmax_nolimber] and [n][n_lens])
+struct ExtraOut {
+  double* cnl = nullptr;
+  int* conv = nullptr;
+};
+
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr = nullptr);
+                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr = nullptr,
+                         const ExtraOut* xo = nullptr);
 
 extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
                                const double* pm, double* dv, void* stream)
@@ -895,6 +903,49 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+}
+
+extern "C" int cl2pt_cl_nonlimber(cl2pt_plan* p, const cl2pt_batch* b, double* cl, int* conv_l, void* stream)
+{
+  if (!p || !cl) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (!(p->cfg.probes & CL2PT_PROBE_WTHETA) || p->cfg.adopt_limber_gg) return CL2PT_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t ncl = (size_t)b->n * p->cfg.n_lens * p->cfg.lmax_nolimber;
+  ExtraOut xo;
+  double* dcl = cl;
+  int* dconv = conv_l;
+  if (b->where == CL2PT_HOST) {
+    // device staging for the host copies
+    st = dalloc(p, &dcl, ncl);
+    if (!st && conv_l) st = dalloc(p, &dconv, (size_t)b->n * p->cfg.n_lens);
+    if (st) return st;
+  }
+  xo.cnl = dcl;
+  xo.conv = conv_l ? dconv : nullptr;
+  // the data vector itself goes to the plan's staging
+  st = internal_eval(p, b, nullptr, nullptr, b->where == CL2PT_DEVICE ? p->d_dv : nullptr, s, nullptr, nullptr,
+                     &xo);
+  if (!st && b->where == CL2PT_HOST) {
+    cudaError_t e = cudaMemcpy(cl, dcl, sizeof(double) * ncl, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && conv_l)
+      e = cudaMemcpy(conv_l, dconv, sizeof(int) * b->n * p->cfg.n_lens, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) st = CL2PT_ERR_CUDA;
+  }
+  if (b->where == CL2PT_HOST) {
+    // the staging is per call: release it
+    for (void* q : {(void*)dcl, (void*)(conv_l ? dconv : nullptr)}) {
+      if (!q) continue;
+      for (size_t i = 0; i < p->dbufs.size(); i++)
+        if (p->dbufs[i] == q) {
+          cudaFree(q);
+          p->dbufs.erase(p->dbufs.begin() + i);
+          break;
+        }
+    }
+  }
+  return st;
 }
 
 extern "C" int cl2pt_vjp_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
@@ -1152,7 +1203,8 @@ extern "C" int cl2pt_graph_destroy(cl2pt_graph* g)
 // Stage the batch on the device (when it lives on the host), then run the
 // pipeline wave by wave so the per-wave workspace stays L2-sized.
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
-                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr)
+                         double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr,
+                         const ExtraOut* xo)
 {
   const int n = b->n;
   const bool fourier = fr != nullptr;
@@ -1413,8 +1465,17 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     } else {
       cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       if (P.tatt || P.one_loop) cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
-      if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg)
+      if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg) {
         cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
+        if (xo && xo->cnl) {
+          const size_t m = (size_t)P.B * P.nl;
+          CUDA_OK(cudaMemcpyAsync(xo->cnl + (size_t)w0 * P.nl * P.lmax_nolimber, P.cnl,
+                                  sizeof(double) * m * P.lmax_nolimber, cudaMemcpyDeviceToDevice, s));
+          if (xo->conv)
+            CUDA_OK(cudaMemcpyAsync(xo->conv + (size_t)w0 * P.nl, P.conv_l, sizeof(int) * m,
+                                    cudaMemcpyDeviceToDevice, s));
+        }
+      }
       cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
                              s, &launches, hk);
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,

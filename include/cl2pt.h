@@ -164,6 +164,15 @@ int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
 
+/* Batched non-Limber clustering C_l (C_cl_tomo, cosmo2D.c:4528-4769, for
+ * every point of the batch): cl [n][n_lens][lmax_nolimber] -- the FFTLog
+ * C_l below each bin's hand-over multipole, the Limber C_l from there on --
+ * and conv_l [n][n_lens] (or NULL), the hand-over multipoles.  Needs a plan
+ * with the w(theta) probe and adopt_limber_gg = 0; pointers follow
+ * batch->where. */
+int cl2pt_cl_nonlimber(cl2pt_plan* plan, const cl2pt_batch* batch, double* cl, int* conv_l,
+                       void* stream);
+
 /* Value and vector-Jacobian product of the Fourier vector of
  * cl2pt_eval_fourier (same arguments; cot [n][n_total(nell)]), with the
  * gradients of cl2pt_vjp_real: through the Limber passes at the caller's

@@ -263,3 +263,22 @@ def test_tatt_one_loop_vs_reference_golden(gpu_lib, oracle_built):
         err = rel_err_env(dv[i], gold[f"dv_{i}"], alt, floor=PAIR_FLOOR, ntheta=w.cfg.ntheta)
         print(i, err)
         assert err <= REL, (i, err)
+
+
+@pytest.mark.gpu
+def test_cl_nonlimber_batched(gpu_lib, oracle_built):
+    """cl2pt_cl_nonlimber: every point's non-Limber C_l and hand-over
+    multipoles against the oracle's C_cl_tomo."""
+    import oracle as O
+    w = workloads.make("real_3x2pt_small")
+    tabs, nus = workloads.points(w, 3, seed=23)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=3)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    cl, conv = plan.cl_nonlimber(om, h0, chi, G, lnP, nus)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    for i in range(3):
+        o.set_point(tabs[i], nus[i])
+        ocl, oconv = o.C_cl_tomo()
+        assert rel_err(cl[i][:, 1:], ocl[:, 1:]) <= REL
+        assert np.array_equal(conv[i], oconv)
