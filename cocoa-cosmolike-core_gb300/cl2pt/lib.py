@@ -71,6 +71,10 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_vjp_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
+    lib.cl2pt_like_create.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.POINTER(C.c_void_p)]
+    lib.cl2pt_like_destroy.argtypes = [C.c_void_p]
+    lib.cl2pt_loglike_real.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_cl_nonlimber.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_vjp_fourier.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -258,6 +262,44 @@ class Plan:
         if lbarl is not None:
             return dv, lbar, nb, lbarl
         return dv, lbar, nb
+
+    def likelihood(self, data, inv_cov, mask=None):
+        """A cl2pt_like over this plan's real-space vector."""
+        d = np.ascontiguousarray(data, dtype=np.float64)
+        ic = np.ascontiguousarray(inv_cov, dtype=np.float64)
+        mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        h = C.c_void_p()
+        check(load().cl2pt_like_create(self.h, mk.ctypes.data if mk is not None else None, _p(d), _p(ic),
+                                       C.byref(h)), "cl2pt_like_create")
+        return Likelihood(h, self)
+
+    def loglike_real(self, like, omega_m, h0, chi, G, lnP, nuisance, pm=None, grad=False, lnPL=None):
+        """chi2 [n] (host arrays); with grad also (lnP_bar, nu_bar) of
+        ln L = -chi2/2."""
+        om = np.ascontiguousarray(omega_m, dtype=np.float64)
+        n = om.shape[0]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), *(_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        chi2 = np.zeros(n)
+        lbar = np.zeros((n, arrs[3].size // n)) if grad else None
+        lbarl = np.zeros((n, lpl.size // n)) if (grad and lpl is not None) else None
+        nbar = (abi.Nuisance * n)() if grad else None
+        pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
+        check(load().cl2pt_loglike_real(self.h, like.h, C.byref(b),
+                                        pmm.ctypes.data if pmm is not None else None, chi2.ctypes.data,
+                                        lbar.ctypes.data if grad else None,
+                                        lbarl.ctypes.data if lbarl is not None else None,
+                                        C.addressof(nbar) if grad else None, None), "cl2pt_loglike_real")
+        if not grad:
+            return chi2
+        nb = np.frombuffer(bytes(nbar), dtype=np.float64).reshape(n, -1).copy()
+        return chi2, lbar, nb
 
     def cl_nonlimber(self, omega_m, h0, chi, G, lnP, nuisance, lnPL=None):
         """Batched non-Limber C_l: (cl [n][n_lens][lmax_nolimber], conv_l [n][n_lens])."""
@@ -489,6 +531,25 @@ class Plan:
 
 
 # ------------------------------------------------------------------ FAST-PT
+class Likelihood:
+    """A cl2pt_like (mask, data, inverse covariance on the device)."""
+
+    def __init__(self, h, plan):
+        self.h = h
+        self._plan = plan
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cl2pt_like_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Graph:
     """A captured Fourier evaluation (cl2pt_graph)."""
 

@@ -36,6 +36,10 @@ void launch_legendre(const Params& P, const double* filt_xi, const double* filt_
 // Fourier data vector dv[pt][nell (pss + pgs + nl)] from the node tables
 void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,
                              const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk);
+// masked chi^2 of points [npt] and, when cot is not null, the cotangent of
+// ln L = -chi^2/2 on the kept entries (k_like.cu)
+void launch_chi2(const double* dv, int n_total, int npt, const int* idx, const double* data, int nsq,
+                 const float* cinv_hi, const float* cinv_lo, double* chi2, double* cot, cudaStream_t s);
 // ragged output of points w0 .. w0+B-1 from their full vectors (k_legendre.cu)
 void launch_gather_csr(const int* ptr, const int* idx, const double* full, int n_total, int w0, int B,
                        double* out, cudaStream_t s);

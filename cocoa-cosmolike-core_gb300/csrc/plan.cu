@@ -810,6 +810,23 @@ struct VJPReq {
   cl2pt_nuisance* nu_bar = nullptr;
 };
 
+// The likelihood of a real-space data vector (IP::set_mask / set_data /
+// set_inv_cov, generic_interface.cpp): the kept entries, the data there and
+// the squeezed inverse covariance split into FP32 head and tail.
+struct cl2pt_like {
+  int n_total = 0, nsq = 0;
+  std::vector<int> mask;
+  int* d_mask = nullptr;
+  int* d_idx = nullptr;
+  double* d_data = nullptr;
+  float *d_hi = nullptr, *d_lo = nullptr;
+};
+
+struct LikeReq {
+  const cl2pt_like* like = nullptr;
+  double* d_chi2 = nullptr;  // [n]
+};
+
 // Extra per-wave outputs: the non-Limber C_l and hand-over multipoles
 // (device pointers, [n][n_lens][lmax_nolimber] and [n][n_lens])
 struct ExtraOut {
@@ -819,7 +836,7 @@ struct ExtraOut {
 
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
                          double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr = nullptr,
-                         const ExtraOut* xo = nullptr);
+                         const ExtraOut* xo = nullptr, const LikeReq* lq = nullptr);
 
 extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask,
                                const double* pm, double* dv, void* stream)
@@ -903,6 +920,113 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+}
+
+extern "C" int cl2pt_like_create(cl2pt_plan* p, const int* mask, const double* data, const double* inv_cov,
+                                 cl2pt_like** out)
+{
+  if (!p || !data || !inv_cov || !out) return CL2PT_ERR_ARG;
+  const int nt = p->n_total;
+  cl2pt_like* L = new cl2pt_like();
+  L->n_total = nt;
+  L->mask.assign(nt, 1);
+  if (mask)
+    for (int i = 0; i < nt; i++) L->mask[i] = mask[i] ? 1 : 0;
+  std::vector<int> idx;
+  for (int i = 0; i < nt; i++)
+    if (L->mask[i]) idx.push_back(i);
+  L->nsq = (int)idx.size();
+  if (L->nsq == 0) {
+    delete L;
+    return CL2PT_ERR_ARG;
+  }
+  const size_t m = idx.size();
+  std::vector<double> d(m);
+  std::vector<float> hi(m * m), lo(m * m);
+  for (size_t a = 0; a < m; a++) {
+    d[a] = data[idx[a]];
+    if (!std::isfinite(d[a])) {
+      delete L;
+      return CL2PT_ERR_ARG;
+    }
+    for (size_t c = 0; c < m; c++) {
+      const double v = inv_cov[(size_t)idx[a] * nt + idx[c]];
+      if (!std::isfinite(v)) {
+        delete L;
+        return CL2PT_ERR_ARG;
+      }
+      const float h = (float)v;
+      hi[a * m + c] = h;
+      lo[a * m + c] = (float)(v - (double)h);
+    }
+  }
+  auto up = [](void** dst, const void* src, size_t bytes) -> int {
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return CL2PT_ERR_CUDA;
+    if (cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return CL2PT_ERR_CUDA;
+    return CL2PT_OK;
+  };
+  int st = up((void**)&L->d_idx, idx.data(), sizeof(int) * m);
+  if (!st) st = up((void**)&L->d_data, d.data(), sizeof(double) * m);
+  if (!st) st = up((void**)&L->d_hi, hi.data(), sizeof(float) * m * m);
+  if (!st) st = up((void**)&L->d_lo, lo.data(), sizeof(float) * m * m);
+  if (!st) st = up((void**)&L->d_mask, L->mask.data(), sizeof(int) * nt);
+  if (st) {
+    cl2pt_like_destroy(L);
+    return st;
+  }
+  *out = L;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_like_destroy(cl2pt_like* L)
+{
+  if (!L) return CL2PT_OK;
+  for (void* q : {(void*)L->d_mask, (void*)L->d_idx, (void*)L->d_data, (void*)L->d_hi, (void*)L->d_lo})
+    if (q) cudaFree(q);
+  delete L;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_loglike_real(cl2pt_plan* p, const cl2pt_like* L, const cl2pt_batch* b, const double* pm,
+                                  double* chi2, double* lnP_bar, double* lnPL_bar, cl2pt_nuisance* nu_bar,
+                                  void* stream)
+{
+  if (!p || !L || !chi2 || L->n_total != p->n_total) return CL2PT_ERR_ARG;
+  if ((lnP_bar == nullptr) != (nu_bar == nullptr)) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  const bool grad = lnP_bar != nullptr;
+  if (grad) {
+    if (b->lnPL && !lnPL_bar) return CL2PT_ERR_ARG;
+    st = vjp_prepare(p);
+    if (st) return st;
+  }
+  if (!p->d_chi2) {
+    st = dalloc(p, &p->d_chi2, (size_t)p->max_batch);
+    if (st) return st;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = b->n;
+  double* dchi = b->where == CL2PT_DEVICE ? chi2 : p->d_chi2;
+  CUDA_OK(cudaMemsetAsync(dchi, 0, sizeof(double) * n, s));
+  LikeReq lq;
+  lq.like = L;
+  lq.d_chi2 = dchi;
+  VJPReq vr;
+  vr.cot = nullptr;
+  vr.lnp_bar = lnP_bar;
+  vr.lnpl_bar = lnPL_bar;
+  vr.nu_bar = nu_bar;
+  const int* mask = b->where == CL2PT_HOST ? L->mask.data() : L->d_mask;
+  double* dv = b->where == CL2PT_DEVICE ? p->d_dv : nullptr;
+  st = internal_eval(p, b, mask, pm, dv, s, nullptr, grad ? &vr : nullptr, nullptr, &lq);
+  if (st) return st;
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaMemcpy(chi2, p->d_chi2, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++)
+      if (!(chi2[i] >= 0.0)) return CL2PT_ERR_DEVICE;  // the reference rejects chi2 < 0
+  }
+  return CL2PT_OK;
 }
 
 extern "C" int cl2pt_cl_nonlimber(cl2pt_plan* p, const cl2pt_batch* b, double* cl, int* conv_l, void* stream)
@@ -1204,7 +1328,7 @@ extern "C" int cl2pt_graph_destroy(cl2pt_graph* g)
 // pipeline wave by wave so the per-wave workspace stays L2-sized.
 static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
                          double* dv, cudaStream_t s, const FourierReq* fr, const VJPReq* vr,
-                         const ExtraOut* xo)
+                         const ExtraOut* xo, const LikeReq* lq)
 {
   const int n = b->n;
   const bool fourier = fr != nullptr;
@@ -1272,7 +1396,13 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
   const bool sep_lin = b->lnPL != nullptr && (b->where == CL2PT_DEVICE || p->d_in_lnPL != nullptr);
   if (vr && b->lnPL && !sep_lin) memset(vr->lnpl_bar, 0, (size_t)n * nPL * sizeof(double));
   if (vr) {
-    if (b->where == CL2PT_HOST) {
+    if (!vr->cot) {
+      // the cotangent of ln L, written per wave by the chi^2 kernel
+      vcot = p->d_vjp_cot;
+      vlnp = b->where == CL2PT_HOST ? p->d_vjp_lnp : vr->lnp_bar;
+      vlnpl = sep_lin ? (b->where == CL2PT_HOST ? p->d_vjp_lnpl : vr->lnpl_bar) : vlnp;
+      vnu = b->where == CL2PT_HOST ? p->d_vjp_nu : vr->nu_bar;
+    } else if (b->where == CL2PT_HOST) {
       CUDA_OK(cudaMemcpyAsync(p->d_vjp_cot, vr->cot, (size_t)n * n_total * sizeof(double),
                               cudaMemcpyHostToDevice, s));
       vcot = p->d_vjp_cot;
@@ -1480,6 +1610,17 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                              s, &launches, hk);
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
                              ddv + (size_t)w0 * p->n_total, s, &launches, hk);
+      if (lq) {
+        double* cw = nullptr;
+        if (vr) {
+          cw = const_cast<double*>(vcot) + (size_t)w0 * n_total;
+          CUDA_OK(cudaMemsetAsync(cw, 0, sizeof(double) * (size_t)P.B * n_total, s));
+        }
+        const cl2pt_like* L = lq->like;
+        cl2pt::launch_chi2(ddv + (size_t)w0 * n_total, n_total, P.B, L->d_idx, L->d_data, L->nsq, L->d_hi, L->d_lo,
+                           lq->d_chi2 + w0, cw, s);
+        launches++;
+      }
       if (vr) {
         cl2pt::VJPParams V;
         const int st2 = vjp_wave(P, w0, V);

@@ -164,6 +164,26 @@ int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);
 
+/* Likelihood epilogue (IP::set_mask / set_data / set_inv_cov and
+ * IP::get_chi2, generic_interface.cpp:2288-2324).  A cl2pt_like holds the
+ * mask [n_total] (NULL: all kept), the data vector [n_total] and the inverse
+ * of the masked covariance [n_total][n_total] (host arrays; only kept
+ * rows/columns are read) of the plan's real-space vector.
+ * cl2pt_loglike_real evaluates the batch and returns chi2 [n] =
+ * (dv - data)^T C^-1 (dv - data) over the kept entries; with lnP_bar and
+ * nu_bar (and lnPL_bar for a separate linear table) it also returns the
+ * gradient of ln L = -chi2 / 2 as cl2pt_vjp_real does, in the same pass.
+ * Pointers follow batch->where; a negative chi2 (an inverse covariance that
+ * is not positive definite) returns CL2PT_ERR_DEVICE for host batches, where
+ * the reference exits. */
+typedef struct cl2pt_like cl2pt_like;
+int cl2pt_like_create(cl2pt_plan* plan, const int* mask, const double* data, const double* inv_cov,
+                      cl2pt_like** like);
+int cl2pt_like_destroy(cl2pt_like* like);
+int cl2pt_loglike_real(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch,
+                       const double* pm, double* chi2, double* lnP_bar, double* lnPL_bar,
+                       cl2pt_nuisance* nu_bar, void* stream);
+
 /* Batched non-Limber clustering C_l (C_cl_tomo, cosmo2D.c:4528-4769, for
  * every point of the batch): cl [n][n_lens][lmax_nolimber] -- the FFTLog
  * C_l below each bin's hand-over multipole, the Limber C_l from there on --
