@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
 // formed on the fly from ln x.
 template <typename T>
 __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int slot, bool direct,
-                                     const double* gd, int i, int k, double deta)
+                                     const double* gd, int i, int k, double deta, float dh, float dl)
 {
   ct<T> g;
   if (direct) {
@@ -448,8 +448,7 @@ __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int s
   } else {
     T et;
     if constexpr (sizeof(T) == sizeof(float)) {
-      // eta = deta i from a two-float split of deta (no FP64 per entry)
-      const float dh = (float)deta, dl = (float)(deta - (double)dh);
+      // eta = deta i from a two-float split (dh, dl) of deta
       et = fmaf(dh, (float)i, dl * (float)i);
     } else {
       et = deta * i;
@@ -549,9 +548,11 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
   const T rct = (T)rc;
   const bool exact_blocks = Q.direct_every != 0;
   const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
+  const double lnx0last = log(geo.x0 / geo.xlast);
+  double deta_j[3];
+  for (int j = 0; j < 3; j++) deta_j[j] = 2.0 * M_PI / (geo.dlnx * Q.N[j]);
   int LM = LNL, done = 0;
   const int BLOCK = 16;
-  const double sqpi = sqrt(M_PI);
   const double dlnx = geo.dlnx;
   const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
   for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
@@ -564,10 +565,13 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
-        const double base = geo.x0 / exp(2 * Q.pad[j] * dlnx);
-        const double lnb0 = log(base * (k + 1.) / geo.xlast);
-        const double lnb1 = log(base * (k2 + 1.) / geo.xlast);
-        const double deta = 2.0 * M_PI / (dlnx * N);
+        // ln(base y0) = ln(x0 / xlast) - 2 pad dlnx + ln(k+1): per-CTA and
+        // per-multipole parts, no transcendental per thread
+        const double lnbj = lnx0last - 2 * Q.pad[j] * dlnx;
+        const double lnb0 = lnbj + Q.lnk1[k];
+        const double lnb1 = lnbj + Q.lnk1[two ? k2 : k];
+        const double deta = deta_j[j];
+        const float dhf = (float)deta, dlf = (float)(deta - (double)dhf);
         __syncthreads();
         ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
         const bool dir0 = exact_blocks ? (k < ks + 2) : (k < 2);
@@ -591,12 +595,12 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
           e0 = tmul(e0, s0);
           e1 = tmul(e1, s1);
           const ct<T> tv = tout[j * Q.hstride + i];
-          const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, k, deta);
+          const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, k, deta, dhf, dlf);
           ct<T> v0 = tmul(tmul(tv, c0), g0);
           v0.y = -v0.y;  // conj
           ct<T> v1 = tmk<T>((T)0, (T)0);
           if (two) {
-            const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, k2, deta);
+            const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, k2, deta, dhf, dlf);
             v1 = tmul(tmul(tv, c1), g1);
             v1.y = -v1.y;
           }
@@ -610,10 +614,11 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
         }
         __syncthreads();
         ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
-        const T sc0 = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
-        const T sc1 = (T)(sqpi / (4. * N * pow(k2 + 1., Q.nu[j])));
-        const T mag0 = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
-        const T mag1 = (T)(bmag * (k2 * (k2 + 1.)) / ((k2 + 1.) * (k2 + 1.)));
+        const T sc0 = (T)Q.sck[j * LNL + k];
+        const T sc1 = (T)Q.sck[j * LNL + (two ? k2 : k)];
+        // bmag l(l+1)/(l+1)^2 = bmag l/(l+1)
+        const T mag0 = (T)bmag * (T)k / (T)(k + 1);
+        const T mag1 = (T)bmag * (T)k2 / (T)(k2 + 1);
         const double num1 = Q.nu[j] - 1.0;
         for (int i = tid; i < nchi; i += NL_NT) {
           // x^nu (nu = 1 or 1.01) and, for magnification, x^2 more
@@ -637,7 +642,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
       }
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
       double part0 = 0.0, part1 = 0.0;
-      const double lk0 = log10(k + 1.), lk1 = log10(k2 + 1.);
+      const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
       const float lk0f = (float)lk0, lk1f = (float)lk1;
       const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
       T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
@@ -785,7 +790,6 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const
   const bool exact_blocks = Q.direct_every != 0;
   const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
   const int LM = P.conv_l[cta];
-  const double sqpi = sqrt(M_PI);
   const double dlnx = geo.dlnx;
   double b1bar = 0.0;
   for (int k = 0; k < LM; k++) {
@@ -795,9 +799,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const
     for (int j = 0; j < nj; j++) {
       const int N = Q.N[j];
       const int nq = N / 2 + 1;
-      const double base = geo.x0 / exp(2 * Q.pad[j] * dlnx);
-      const double y0 = (k + 1.) / geo.xlast;
-      const double lnbase = log(base * y0);
+      const double lnbase = log(geo.x0 / geo.xlast) - 2 * Q.pad[j] * dlnx + Q.lnk1[k];
       const double deta = 2.0 * M_PI / (dlnx * N);
       __syncthreads();
       ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
@@ -834,8 +836,8 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const
       }
       __syncthreads();
       ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
-      const T scale = (T)(sqpi / (4. * N * pow(k + 1., Q.nu[j])));
-      const T magf = (T)(bmag * (k * (k + 1.)) / ((k + 1.) * (k + 1.)));
+      const T scale = (T)Q.sck[j * LNL + k];
+      const T magf = (T)bmag * (T)k / (T)(k + 1);
       for (int i = tid; i < nchi; i += NL_NT) {
         T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
         if (j == 0) {
@@ -850,7 +852,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const
     const double wk = cb[k] * geo.dlnchi * 2. / M_PI;
     if (wk == 0.0) continue;
     const double cub = (k + 1.) * (k + 1.) * (k + 1.);
-    const double lk1 = log10(k + 1.);
+    const double lk1 = Q.l10k1[k];
     double part = 0.0;
     for (int i = tid; i < nchi; i += NL_NT) {
       const double lkv = lk1 + lxk[i];

@@ -24,6 +24,12 @@ struct NLParams {
   int ndirect;      // multipoles evaluated directly per kernel
   int direct_every; // 1: restart the recurrence every 16-block (FP64 plan)
   size_t gst_stride;
+  // per-multipole constants of the loop, once per plan instead of per
+  // thread: ln(k+1), log10(k+1) [LNL] and the c2r scales
+  // sqrt(pi) / (4 N_j (k+1)^nu_j) [3][LNL]
+  const double* lnk1;
+  const double* l10k1;
+  const double* sck;
 };
 
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,

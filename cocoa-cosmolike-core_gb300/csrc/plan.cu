@@ -678,6 +678,21 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
         Q.twt[j] = dtwf;
       }
     }
+    {
+      std::vector<double> a(LNL), b(LNL), c((size_t)3 * LNL);
+      for (int k = 0; k < LNL; k++) {
+        a[k] = log(k + 1.);
+        b[k] = log10(k + 1.);
+        for (int j = 0; j < 3; j++) c[(size_t)j * LNL + k] = sqrt(M_PI) / (4. * Q.N[j] * pow(k + 1., Q.nu[j]));
+      }
+      double *da, *db, *dc;
+      TRY(dupload(p, &da, a.data(), a.size()));
+      TRY(dupload(p, &db, b.data(), b.size()));
+      TRY(dupload(p, &dc, c.data(), c.size()));
+      Q.lnk1 = da;
+      Q.l10k1 = db;
+      Q.sck = dc;
+    }
     Q.hstride = Q.nmax / 2 + 1;
     Q.tout_stride = (size_t)3 * Q.hstride;
     Q.gst_stride = (size_t)3 * 2 * Q.hstride;
