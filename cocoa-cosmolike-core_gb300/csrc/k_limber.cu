@@ -314,7 +314,8 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   // per-cell slopes chi_all interpolates), growth table (value, slope, z),
   // n(z) spline of bin q.
   double* nd = (double*)smem_raw;
-  double* sd = nd + 8 * PCH;
+  double* thr = nd + 8 * PCH;  // [PCH] per-node l+1/2 threshold of the chi(a_min) cut
+  double* sd = thr + PCH;
   double* si = sd + pd.nk;
   double* sdl = si + pd.nk;
   double* sil = sdl + pl.nk;
@@ -395,14 +396,16 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
       nj[PCH + p] = jl;
       nd[6 * PCH + p] = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
       nd[7 * PCH + p] = log10(fK * CL2PT_COVERH0);
+      // chi1 = fK (l+3/2)/(l+1/2) > chi(a_min)  <=>  l+1/2 < fK / (chi(a_min) - fK)
+      // (always when fK >= chi(a_min)): one compare per (l, node)
+      thr[p] = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
     }
     __syncthreads();
     if (!valid) continue;
     const double llp = log10(lp);
     for (int p = 0; p < np; p++) {
       const double fK = nd[0 * PCH + p];
-      const double chi1 = fK * (lp + 1.0) / lp;  // (l+3/2)/k
-      if (chi1 > chi_amin) continue;
+      if (lp < thr[p]) continue;  // (l+3/2)/k beyond chi(a_min)
       // a_chi at chi1 (cosmo3D.c:109-133)
       const T c = (T)(fK * CL2PT_COVERH0) * ratio;
       const int j = bsearch_t(cx, nc, c);
@@ -476,7 +479,7 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    const size_t sm = sizeof(double) * (8 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
+    const size_t sm = sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
                       sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
