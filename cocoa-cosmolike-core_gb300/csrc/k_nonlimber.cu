@@ -474,8 +474,13 @@ __device__ __forceinline__ ct<T> phasor(double a)
   return tmk<T>(cp, sp);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
+// ADJ: the adjoint of the FFTLog part (see section 4 below) on the same
+// multipole walk: the loop stops at the forward's hand-over multipole, keeps
+// the b1-free galaxy term G0 of both multipoles, and accumulates the P_lin
+// slice adjoint and d/db1 from cbar = dL/dC_l instead of writing C_l.
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
+                                                      double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x, q = blockIdx.y;
@@ -490,20 +495,25 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
   //   mixed plan: [lxk: nchi float][pcf: 3 nk float, psf: nk float] and the
   //     FP64 slice psl only during set-up, in fb;
   //   FP64 plan:  [psl, plkd, pinv: nk double][lxk: nchi double]
+  //   adjoint: [G00, G01: nchi T] after xs, the slice adjoint [nk] last
   ct<T>* fa = (ct<T>*)smem_raw;
   ct<T>* fb = fa + Q.nmax;
   T* F0 = (T*)(fb + Q.nmax);
   T* F1 = F0 + nchi;
   T* xs = F1 + nchi;
-  T* plk = xs + nchi;
+  T* G00 = xs + nchi;
+  T* G01 = G00 + nchi;
+  T* plk = ADJ ? G01 + nchi : xs + nchi;
   constexpr bool F32 = sizeof(T) == sizeof(float);
   float* lxkf = (float*)(plk + P.pkl_nk);
   float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
   float* psf = pcf + 3 * P.pkl_nk;  // slope of the slice per cell
+  float* pbarf = psf + P.pkl_nk;
   double* psl = F32 ? (double*)fb : (double*)(plk + P.pkl_nk);
   double* plkd = psl + P.pkl_nk;
   double* pinv = plkd + P.pkl_nk;
   double* lxk = pinv + P.pkl_nk;
+  double* pbard = lxk + nchi;
   __shared__ double red[2][NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
   const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
@@ -512,11 +522,16 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
   const double* ggl = P.ggl + cta * LNL * 2;
   const double rc = geo.rc;
   // P_lin(k, z = 0) slice of the linear table (p_lin(k, 1), cosmo3D.c:306-358)
+  const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
+  const double dyz = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
   {
     const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
-    const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
-    const double dy = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
+    const double dy = dyz;
     for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+      if (ADJ) {
+        if (F32) pbarf[i] = 0.0f;
+        else pbard[i] = 0.0;
+      }
       psl[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
       plk[i] = (T)P.pkl_lk[i];
       if (!F32) {
@@ -555,8 +570,13 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
   const int BLOCK = 16;
   const double dlnx = geo.dlnx;
   const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
-  for (int ks = 0; ks < LNL && !done; ks += BLOCK) {
-    const int ke = (ks + BLOCK < LNL) ? ks + BLOCK : LNL;
+  // adjoint: the forward's hand-over multipole bounds the walk
+  const int LEND = ADJ ? P.conv_l[cta] : LNL;
+  const T b1t = ADJ ? (T)nu.gb[0][q] : (T)1;
+  double b1bar = 0.0;
+  const double* cb = ADJ ? cbar + cta * LNL : nullptr;
+  for (int ks = 0; ks < LEND && !done; ks += BLOCK) {
+    const int ke = (ks + BLOCK < LEND) ? ks + BLOCK : LEND;
     for (int k = ks; k < ke; k += 2) {
       const int k2 = k + 1;
       const bool two = k2 < ke;
@@ -635,74 +655,139 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
             f0 *= mag0;
             f1 *= mag1;
           }
+          if (ADJ && j == 0) {
+            // the galaxy transform was taken with b1 = 1
+            G00[i] = f0;
+            G01[i] = f1;
+            f0 *= b1t;
+            f1 *= b1t;
+          }
           F0[i] += f0;
           F1[i] += f1;
         }
         __syncthreads();
       }
+      if constexpr (ADJ) {
+        // adjoint of C_l = (2/pi) dlnchi sum_i F_i^2 k_i^3 P_i for both
+        // multipoles: P_lin slice adjoint (FP32 shared atomics in the mixed
+        // plan) and d/db1 through F = b1 G0 + ...
+        const double w0 = cb[k] * geo.dlnchi * 2. / M_PI;
+        const double w1 = two ? cb[k2] * geo.dlnchi * 2. / M_PI : 0.0;
+        double bp = 0.0;
+        if (w0 != 0.0 || w1 != 0.0) {
+          const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
+          const float lk0f = (float)lk0, lk1f = (float)lk1;
+          const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
+          const T wt0 = (T)w0, wt1 = (T)w1;
+          T tb = 0;
+          for (int i = tid; i < nchi; i += NL_NT) {
+            const T rx = rct / xs[i];
+            const T rx3 = rx * rx * rx;
+            for (int h = 0; h < (two ? 2 : 1); h++) {
+              const T wt = h ? wt1 : wt0;
+              if (wt == (T)0) continue;
+              const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
+              const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
+              int lo = 0, hi = P.pkl_nk - 1;
+              while (hi > lo + 1) {
+                const int mid = (lo + hi) >> 1;
+                if (plk[mid] > lkt) hi = mid; else lo = mid;
+              }
+              const T F = h ? F1[i] : F0[i];
+              const T G = h ? G01[i] : G00[i];
+              const T k3 = (h ? cub1 : cub0) * rx3;
+              if constexpr (F32) {
+                const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
+                const float pl = __expf(pcf[3 * lo]) * __expf(pcf[3 * lo + 1] + dx * psf[lo]) * lc3;
+                const float g = wt * F * F * k3 * pl;
+                atomicAdd(&pbarf[lo], g * (1.0f - dx));
+                atomicAdd(&pbarf[lo + 1], g * dx);
+                tb += wt * 2.0f * F * G * k3 * pl;
+              } else {
+                const double dxd = (lkv - plkd[lo]) * pinv[lo];
+                const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
+                                  (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
+                const double g = wt * F * F * k3 * pl;
+                atomicAdd(&pbard[lo], g * (1 - dxd));
+                atomicAdd(&pbard[lo + 1], g * dxd);
+                tb += wt * 2.0 * F * G * k3 * pl;
+              }
+            }
+          }
+          bp = (double)tb;
+        }
+        for (int o = 16; o > 0; o >>= 1) bp += __shfl_down_sync(0xffffffffu, bp, o);
+        __syncthreads();
+        if ((tid & 31) == 0) red[0][tid >> 5] = bp;
+        __syncthreads();
+        if (tid == 0)
+          for (int w2 = 0; w2 < NL_NT / 32; w2++) b1bar += red[0][w2];
+      } else {
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
-      double part0 = 0.0, part1 = 0.0;
-      const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
-      const float lk0f = (float)lk0, lk1f = (float)lk1;
-      const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
-      T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
-      for (int i = tid; i < nchi; i += NL_NT) {
-        const T rx = rct / xs[i];
-        const T rx3 = rx * rx * rx;
-        for (int h = 0; h < (two ? 2 : 1); h++) {
-          // p_lin(k, 1) (cosmo3D.c:306-358) on the z = 0 slice
-          const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
-          int lo = 0, hi = P.pkl_nk - 1;
-          const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
-          while (hi > lo + 1) {
-            const int mid = (lo + hi) >> 1;
-            if (plk[mid] > lkt) hi = mid; else lo = mid;
-          }
-          const T F = h ? F1[i] : F0[i];
-          const T k3 = (h ? cub1 : cub0) * rx3;
-          if constexpr (sizeof(T) == sizeof(double)) {
-            const double dxd = (lkv - plkd[lo]) * pinv[lo];
-            const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
-                              (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
-            const double v = F * F * k3 * pl;
-            if (h) part1 += v; else part0 += v;
-          } else {
-            // in-cell offset and exponent in FP32 from the per-cell split
-            // (hi, lo, slope) of the slice
-            const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
-            const float del = pcf[3 * lo + 1] + dx * psf[lo];
-            const float pl = __expf(pcf[3 * lo]) * __expf(del) * lc3;
-            const float v = F * F * k3 * pl;
-            if (h) tp1 += v; else tp0 += v;
+        double part0 = 0.0, part1 = 0.0;
+        const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
+        const float lk0f = (float)lk0, lk1f = (float)lk1;
+        const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
+        T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
+        for (int i = tid; i < nchi; i += NL_NT) {
+          const T rx = rct / xs[i];
+          const T rx3 = rx * rx * rx;
+          for (int h = 0; h < (two ? 2 : 1); h++) {
+            // p_lin(k, 1) (cosmo3D.c:306-358) on the z = 0 slice
+            const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
+            int lo = 0, hi = P.pkl_nk - 1;
+            const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
+            while (hi > lo + 1) {
+              const int mid = (lo + hi) >> 1;
+              if (plk[mid] > lkt) hi = mid; else lo = mid;
+            }
+            const T F = h ? F1[i] : F0[i];
+            const T k3 = (h ? cub1 : cub0) * rx3;
+            if constexpr (sizeof(T) == sizeof(double)) {
+              const double dxd = (lkv - plkd[lo]) * pinv[lo];
+              const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
+                                (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
+              const double v = F * F * k3 * pl;
+              if (h) part1 += v; else part0 += v;
+            } else {
+              // in-cell offset and exponent in FP32 from the per-cell split
+              // (hi, lo, slope) of the slice
+              const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
+              const float del = pcf[3 * lo + 1] + dx * psf[lo];
+              const float pl = __expf(pcf[3 * lo]) * __expf(del) * lc3;
+              const float v = F * F * k3 * pl;
+              if (h) tp1 += v; else tp0 += v;
+            }
           }
         }
-      }
-      if constexpr (sizeof(T) == sizeof(float)) {
-        part0 = tp0;
-        part1 = tp1;
-      }
-      // two block sums
-      for (int o = 16; o > 0; o >>= 1) {
-        part0 += __shfl_down_sync(0xffffffffu, part0, o);
-        part1 += __shfl_down_sync(0xffffffffu, part1, o);
-      }
-      __syncthreads();
-      if ((tid & 31) == 0) {
-        red[0][tid >> 5] = part0;
-        red[1][tid >> 5] = part1;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        double t0 = 0.0, t1 = 0.0;
-        for (int w2 = 0; w2 < NL_NT / 32; w2++) {
-          t0 += red[0][w2];
-          t1 += red[1][w2];
+        if constexpr (sizeof(T) == sizeof(float)) {
+          part0 = tp0;
+          part1 = tp1;
         }
-        Cl[k] = t0 * geo.dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
-        if (two) Cl[k2] = t1 * geo.dlnchi * 2. / M_PI + ggl[k2 * 2 + 0] - ggl[k2 * 2 + 1];
+        // two block sums
+        for (int o = 16; o > 0; o >>= 1) {
+          part0 += __shfl_down_sync(0xffffffffu, part0, o);
+          part1 += __shfl_down_sync(0xffffffffu, part1, o);
+        }
+        __syncthreads();
+        if ((tid & 31) == 0) {
+          red[0][tid >> 5] = part0;
+          red[1][tid >> 5] = part1;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double t0 = 0.0, t1 = 0.0;
+          for (int w2 = 0; w2 < NL_NT / 32; w2++) {
+            t0 += red[0][w2];
+            t1 += red[1][w2];
+          }
+          Cl[k] = t0 * geo.dlnchi * 2. / M_PI + ggl[k * 2 + 0] - ggl[k * 2 + 1];
+          if (two) Cl[k2] = t1 * geo.dlnchi * 2. / M_PI + ggl[k2 * 2 + 0] - ggl[k2 * 2 + 1];
+        }
       }
-    }
+      }
     __syncthreads();
+    if (ADJ) continue;
     // convergence at the block end (cosmo2D.c:4741-4750)
     const int L = ke - 1;
     const double denom = ggl[L * 2 + 0];
@@ -713,6 +798,20 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
         LM = ke;
       }
     }
+  }
+  if constexpr (ADJ) {
+    // the slice adjoint onto the table's two z columns, and d/db1
+    __syncthreads();
+    double* lb = lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    for (int i = tid; i < P.pkl_nk; i += NL_NT) {
+      const double v = F32 ? (double)pbarf[i] : pbard[i];
+      if (v != 0.0) {
+        atomicAdd(&lb[(size_t)i * P.pkl_nz + j0], (1 - dyz) * v);
+        atomicAdd(&lb[(size_t)i * P.pkl_nz + j0 + 1], dyz * v);
+      }
+    }
+    if (tid == 0) atomicAdd(&nu_bar[pt].gb[0][q], b1bar);
+    return;
   }
   // hand over to Limber (cosmo2D.c:4760-4765)
   if (tid == 0) {
@@ -738,147 +837,14 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q)
 // where psl is the z = 0 slice of the linear table; the slice adjoint is
 // spread onto the table's two z columns at the end.
 template <typename T>
-__global__ void __launch_bounds__(NL_NT, 2) k_nl_vjp(Params P, NLParams Q, const double* __restrict__ cbar,
-                                                     double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
+static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int pt = blockIdx.x, q = blockIdx.y;
-  const int tid = threadIdx.x;
-  const int nchi = P.nl_nchi;
-  const int LNL = P.lmax_nolimber;
-  const cl2pt_nuisance& nu = P.nu[pt];
-  const double bmag = nu.gb[4][q];
-  const double b1 = nu.gb[0][q];
-  const int nj = (bmag != 0.0) ? 3 : 2;
-  const NLGeom geo = nl_geom(P, pt);
-  double* psl = (double*)smem_raw;
-  double* plkd = psl + P.pkl_nk;
-  double* pinv = plkd + P.pkl_nk;
-  double* pbar = pinv + P.pkl_nk;
-  double* lxk = pbar + P.pkl_nk;
-  ct<T>* fa = (ct<T>*)(lxk + nchi);
-  ct<T>* fb = fa + Q.nmax;
-  T* F = (T*)(fb + Q.nmax);
-  T* G0 = F + nchi;
-  T* xpow = G0 + nchi;
-  T* xx2 = xpow + 3 * nchi;
-  T* rx3 = xx2 + nchi;
-  T* plk = rx3 + nchi;
-  __shared__ double red[NL_NT / 32];
-  const size_t cta = (size_t)pt * P.nl + q;
-  const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;
-  ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;
-  const double* cb = cbar + cta * LNL;
-  const double rc = geo.rc;
-  const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
-  const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
-  const double dyz = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
-  for (int i = tid; i < P.pkl_nk; i += NL_NT) {
-    psl[i] = (1 - dyz) * tabL[(size_t)i * P.pkl_nz + j0] + dyz * tabL[(size_t)i * P.pkl_nz + j0 + 1];
-    plk[i] = (T)P.pkl_lk[i];
-    plkd[i] = P.pkl_lk[i];
-    pinv[i] = (i + 1 < P.pkl_nk) ? 1.0 / (P.pkl_lk[i + 1] - P.pkl_lk[i]) : 0.0;
-    pbar[i] = 0.0;
-  }
-  for (int i = tid; i < nchi; i += NL_NT) {
-    const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
-    for (int j = 0; j < 3; j++) xpow[j * nchi + i] = (T)pow(xr, Q.nu[j]);
-    lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
-    xx2[i] = (T)(xr * xr);
-    rx3[i] = (T)((rc / xr) * (rc / xr) * (rc / xr));
-  }
-  const bool exact_blocks = Q.direct_every != 0;
-  const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
-  const int LM = P.conv_l[cta];
-  const double dlnx = geo.dlnx;
-  double b1bar = 0.0;
-  for (int k = 0; k < LM; k++) {
-    const int ks = (k / 16) * 16;
-    __syncthreads();
-    for (int i = tid; i < nchi; i += NL_NT) F[i] = G0[i] = (T)0;
-    for (int j = 0; j < nj; j++) {
-      const int N = Q.N[j];
-      const int nq = N / 2 + 1;
-      const double lnbase = log(geo.x0 / geo.xlast) - 2 * Q.pad[j] * dlnx + Q.lnk1[k];
-      const double deta = 2.0 * M_PI / (dlnx * N);
-      __syncthreads();
-      ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
-      const bool direct = exact_blocks ? (k < ks + 2) : (k < 2);
-      const int slot = exact_blocks ? ((k - ks) & 1) : (k & 1);
-      const int di = exact_blocks ? (ks / 16) * 2 + (k - ks) : k;
-      const double* gd = gdir + ((size_t)j * Q.ndirect + (direct ? di : 0)) * Q.hstride * 2;
-      for (int i = tid; i < nq; i += NL_NT) {
-        ct<T> g;
-        if (direct) {
-          g = tmk<T>((T)gd[2 * i], (T)gd[2 * i + 1]);
-        } else {
-          const T kk = (T)k, nuj = (T)Q.nu[j], et = (T)(deta * i);
-          ct<T> num, den;
-          if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
-          else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
-          else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
-          g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
-        }
-        gs[slot * Q.hstride + i] = g;
-        double ph = -(deta * i) * lnbase;
-        ph -= 2.0 * M_PI * rint(ph * (0.5 / M_PI));
-        T sp, cp;
-        tsincos<T>((T)ph, &sp, &cp);
-        ct<T> val = tmul(tmul(tout[j * Q.hstride + i], tmk<T>(cp, sp)), g);
-        val.y = -val.y;
-        fa[i] = val;
-        if (i > 0 && i < N - i) fa[N - i] = tmk<T>(val.x, -val.y);
-      }
-      __syncthreads();
-      if (tid == 0) {
-        fa[0].y = (T)0;
-        if ((N & 1) == 0) fa[N / 2].y = (T)0;
-      }
-      __syncthreads();
-      ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
-      const T scale = (T)Q.sck[j * LNL + k];
-      const T magf = (T)bmag * (T)k / (T)(k + 1);
-      for (int i = tid; i < nchi; i += NL_NT) {
-        T fy = r[Q.pad[j] + i].x * scale * xpow[j * nchi + i];
-        if (j == 0) {
-          G0[i] = fy;
-          fy *= (T)b1;
-        }
-        if (j == 2) fy = magf * fy * xx2[i];
-        F[i] += fy;
-      }
-      __syncthreads();
-    }
-    const double wk = cb[k] * geo.dlnchi * 2. / M_PI;
-    if (wk == 0.0) continue;
-    const double cub = (k + 1.) * (k + 1.) * (k + 1.);
-    const double lk1 = Q.l10k1[k];
-    double part = 0.0;
-    for (int i = tid; i < nchi; i += NL_NT) {
-      const double lkv = lk1 + lxk[i];
-      const int lo = bsearch_d(plkd, P.pkl_nk, lkv);
-      const double dxd = (lkv - plkd[lo]) * pinv[lo];
-      const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
-                        (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0);
-      const double k3 = cub * (double)rx3[i];
-      const double f = (double)F[i];
-      const double g = wk * f * f * k3 * pl;
-      atomicAdd(&pbar[lo], g * (1 - dxd));
-      atomicAdd(&pbar[lo + 1], g * dxd);
-      part += 2.0 * f * (double)G0[i] * k3 * pl;
-    }
-    b1bar += wk * block_sum(part, red);
-  }
-  __syncthreads();
-  double* lb = lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
-  for (int i = tid; i < P.pkl_nk; i += NL_NT) {
-    const double v = pbar[i];
-    if (v != 0.0) {
-      atomicAdd(&lb[(size_t)i * P.pkl_nz + j0], (1 - dyz) * v);
-      atomicAdd(&lb[(size_t)i * P.pkl_nz + j0 + 1], dyz * v);
-    }
-  }
-  if (tid == 0) atomicAdd(&nu_bar[pt].gb[0][q], b1bar);
+  const bool f32 = sizeof(T) == sizeof(float);
+  size_t sm = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
+              (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
+                   : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
+  if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
+  return sm;
 }
 
 template <typename T>
@@ -888,10 +854,9 @@ static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cb
   const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl, 1), NL_NT, sm1, s>>>(P, Q, 1);
-  const size_t sm = sizeof(double) * (4 * (size_t)P.pkl_nk + P.nl_nchi) +
-                    sizeof(T) * (2 * 2 * (size_t)Q.nmax + 7 * (size_t)P.nl_nchi + P.pkl_nk) + 64;
-  cudaFuncSetAttribute(k_nl_vjp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_nl_vjp<T><<<dim3(P.B, P.nl), NL_NT, sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+  const size_t sm = nl_loop_smem<T>(P, Q, true);
+  cudaFuncSetAttribute(k_nl_loop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_nl_loop<T, true><<<dim3(P.B, P.nl), NL_NT, sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
 }
 
 void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
@@ -909,12 +874,9 @@ static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
-  const bool f32 = sizeof(T) == sizeof(float);
-  const size_t sm3 = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
-                     (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
-                          : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
-  cudaFuncSetAttribute(k_nl_loop<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-  k_nl_loop<T><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q);
+  const size_t sm3 = nl_loop_smem<T>(P, Q, false);
+  cudaFuncSetAttribute(k_nl_loop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+  k_nl_loop<T, false><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
 }
 
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,

@@ -459,6 +459,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     VJPParams V2 = V;
     V2.cbar_gg = V.cbar_gg2;
     V2.lfac_g = lfac_g_std;
+    V2.lfac_g_sorted = 1;
     const int Kw = Pg->lmax_nolimber + Pg->nnode_g;
     k_vjp_fourier_w<<<dim3((Pg->nl * Kw + 255) / 256, Pg->B), 256, 0, s>>>(*Pg, V2);
     k_vjp_handover<<<dim3(Pg->B, Pg->nl), 256, 0, s>>>(*Pg, V2);

@@ -299,6 +299,20 @@ __device__ __forceinline__ int hsearch_t(const T* __restrict__ x, int n, T v, in
 // shared-memory copies of the point's distance/growth tables and the bin's
 // n(z) spline in the loop precision (the forward's tables and formulas),
 // with hinted searches (monotone in l for one node).
+// First multipole index of a factor table (6 doubles per multipole, entry 5 =
+// (lp+1)/lp, decreasing in l) kept by the chi(a_min) cut
+// fK (lp+1)/lp <= chi(a_min): the cut removes a prefix of the multipoles.
+__device__ __forceinline__ int first_kept(const double* fac, int n, double fK, double chi_amin)
+{
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (fK * fac[6 * mid + 5] > chi_amin) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 template <typename T>
 __global__ void k_vjp_gg(Params P, VJPParams V)
 {
@@ -405,12 +419,13 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   };
   PWalk<T> wk;
   double lbar = 0.0;
-  for (int L0 = 0; L0 < K; L0 += LC) {
+  const int Lk = V.lfac_g_sorted ? first_kept(V.lfac_g, K, nd.fK, chi_amin) : 0;
+  for (int L0 = Lk; L0 < K; L0 += LC) {
     const int L1 = min(K, L0 + LC);
     T lt = 0;
     for (int L = L0; L < L1; L++) {
       const double* fac = V.lfac_g + 6 * L;
-      if (nd.fK * fac[5] > chi_amin) continue;
+      if (!V.lfac_g_sorted && nd.fK * fac[5] > chi_amin) continue;
       const T cv = cbs[L];
       if (cv == (T)0) continue;
       const T s = s_of(fac);
@@ -434,11 +449,10 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
     T lt = 0;
-    for (int L = 0; L < LNL; L++) {
+    for (int L = first_kept(V.lfac_gi, LNL, nd.fK, chi_amin); L < LNL; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
       const double* fac = V.lfac_gi + 6 * L;
-      if (nd.fK * fac[5] > chi_amin) continue;
       const T s = s_of(fac);
       const double lk = fac[0] - nd.lfk;
       T dx, dxl;

@@ -89,6 +89,9 @@ struct VJPParams {
   // per-point one-loop gate [B]
   double *wbar_ssb, *wbar_ss2, *wbar_gsb, *wbar_gs2, *wbar_gsk, *cx_ss;
   int* one_loop_on;
+  // lfac_g holds increasing multipoles (the plan's node table; caller
+  // multipoles of the Fourier path need not be sorted)
+  int lfac_g_sorted;
 };
 size_t vjp_extra_smem(const Params& P);
 // which: 0 ss, 1 gs, 2 gg, -1 the one-loop gate (k_vjp_extra.cu)

@@ -1459,6 +1459,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
     V0.lfac_g = p->d_lfac_g;
+    V0.lfac_g_sorted = 1;
     V0.lfac_gi = p->d_lfac_g + 6 * (size_t)p->nnode_g;
   }
   int launches = 0;
@@ -1512,10 +1513,12 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V.pm = dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr;
     return CL2PT_OK;
   };
+  bool ell_sorted = true;
   if (vr && fourier) {
     // multipole factors of the caller's l for the adjoint sweeps
     std::vector<double> fs, fg;
     for (int i = 0; i < fr->nell; i++) {
+      if (i > 0 && !(fr->ell[i] > fr->ell[i - 1])) ell_sorted = false;
       const double l = fr->ell[i], lp = l + 0.5, tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
       fs.push_back(log10(lp));
       fs.push_back(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
@@ -1604,6 +1607,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         if (st2) return st2;
         V.lfac_ss = p->d_lfac_f;
         V.lfac_g = p->d_lfac_f + 2 * (size_t)fr->nell;
+        V.lfac_g_sorted = ell_sorted ? 1 : 0;
         cl2pt::launch_vjp_fourier(Pf, use_nl ? &Pg : nullptr, V, p->nlq, fr->nell, p->d_ell_f, fr->lmax_shear,
                                   p->d_lfac_g, s, &launches);
       }
