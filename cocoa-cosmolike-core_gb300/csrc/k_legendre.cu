@@ -7,14 +7,152 @@
 // the node values, so the plan folds it into the filters once and the
 // contraction runs over K = (LMIN_tab - 1) + N_ell node columns:
 //     obs[theta, (point, pair)] = sum_K  filter[theta, K] * C[(point, pair), K]
-// as an FP64 NT GEMM (M = filters x theta, N = points x pairs), with the
-// output scattered straight into the per-point observable layout.
+// as an NT GEMM (M = filters x theta, N = points x pairs), with the output
+// scattered straight into the per-point observable layout.  The FP64 plan
+// runs it in FP64; the mixed plan on the FP32 pipe as three split products
+// (filter and C_l each split into an FP32 head and tail:
+// f_hi c_hi + f_hi c_lo + f_lo c_hi) summed in FP32 over 32-node chunks and
+// folded into a two-float (head, tail) accumulator by an error-free sum.
+// The folded node filters cancel mildly (sum |f C| stays within 1.6x of the
+// spectrum's peak |value|), so the result is good to ~1e-9 of the peak at a
+// fraction of the cost of the FP64 pipe (1/64 of the FP32 rate on GB300).
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace cl2pt {
 
 constexpr int BM = 64, BN = 64, BK = 32, CT = 256;
+
+// C_l column value of node k for output column col = point * npair + pair
+// (see k_contract): the tables are [point][pair][node], so the column's row
+// starts at col * (row length)
+__device__ __forceinline__ double contract_col(const Params& P, int mode, int col, int k)
+{
+  if (mode == 0)
+    return (k < P.nnode_ss) ? P.tab_ss[(size_t)col * P.nnode_ss + k]
+                            : P.tab_ss_bb[(size_t)col * P.nnode_ss + (k - P.nnode_ss)];
+  if (mode == 1) return P.tab_gs[(size_t)col * P.nnode_g + k];
+  if (mode == 2) return P.tab_gg[(size_t)col * P.nnode_g + k];
+  const int LNL = P.lmax_nolimber;
+  return (k < LNL) ? P.cnl[(size_t)col * LNL + k] : P.tab_gg[(size_t)col * P.nnode_g + (k - LNL)];
+}
+
+// observable index of (filter row m, column col) in the per-point layout
+__device__ __forceinline__ double* contract_out(const Params& P, int mode, int npair, int m, int col)
+{
+  const int pt = col / npair, pr = col - pt * npair;
+  const int nt = P.ntheta;
+  const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
+  const int n_total = n_xi + n_gt + nt * P.nl;
+  int idx;
+  if (mode == 0) idx = (m < nt) ? pr * nt + m : n_xi / 2 + pr * nt + (m - nt);
+  else if (mode == 1) idx = n_xi + pr * nt + m;
+  else idx = n_xi + n_gt + pr * nt + m;
+  return P.obs + (size_t)pt * n_total + idx;
+}
+
+// error-free FP32 sum a + b = s + e (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Split-FP32 contraction of the mixed plan.  One CTA of 256 threads per
+// (tile of up to 64 filter rows, 64 columns) walks K in 32-node chunks:
+// every thread loads 8 C_l entries (a fixed node offset, 8 columns) and up
+// to 4 float4 of the pre-split filter tile one chunk ahead, splits the C_l
+// entries into head and tail on the way to shared memory, and the first
+// 16 x (rows / 4) threads each own a 4 x 4 block of outputs.
+constexpr int SBK = 32, SBN = 64, SBM = 64, SNT = 256;
+__global__ void __launch_bounds__(SNT, 2) k_contract_s(Params P, SplitFilter F, int M, int K, int mode)
+{
+  __shared__ __align__(16) float Ah[SBK][SBM], Al[SBK][SBM];
+  __shared__ __align__(16) float Bh[SBK][SBN + 4], Bl[SBK][SBN + 4];
+  const int npair = (mode == 0) ? P.pss : (mode == 1) ? P.pgs : P.nl;
+  const int N = P.B * npair;
+  const int n0 = blockIdx.x * SBN, m0 = blockIdx.y * SBM;
+  const int q4 = min(SBM, F.Mp - m0) / 4;  // float4 per filter-tile row
+  const int tid = threadIdx.x;
+  const bool comp = tid < 16 * q4;
+  const int tm = tid / 16, tn = tid % 16;
+  const int kl = tid & 31, nl0 = tid >> 5;
+  double bv[8];
+  float4 av[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const int col = n0 + nl0 + 8 * r, k = k0 + kl;
+      bv[r] = (col < N && k < K) ? contract_col(P, mode, col, k) : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int f = tid + SNT * r;
+      if (f < 64 * q4) {
+        const int w = f >= 32 * q4, rem = f - w * 32 * q4;
+        const int kk = rem / q4, q = rem - kk * q4;
+        av[r] = *(const float4*)((w ? F.lo : F.hi) + (size_t)(k0 + kk) * F.Mp + m0 + 4 * q);
+      }
+    }
+  };
+  float hi[4][4], lo[4][4];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) hi[i][j] = lo[i][j] = 0.0f;
+  load(0);
+  for (int k0 = 0; k0 < F.Ksp; k0 += SBK) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+      const float h = (float)bv[r];
+      Bh[kl][nl0 + 8 * r] = h;
+      Bl[kl][nl0 + 8 * r] = (float)(bv[r] - (double)h);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int f = tid + SNT * r;
+      if (f < 64 * q4) {
+        const int w = f >= 32 * q4, rem = f - w * 32 * q4;
+        const int kk = rem / q4, q = rem - kk * q4;
+        *(float4*)&(w ? Al : Ah)[kk][4 * q] = av[r];
+      }
+    }
+    __syncthreads();
+    if (k0 + SBK < F.Ksp) load(k0 + SBK);
+    if (comp) {
+      float sc[4][4];
+      for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) sc[i][j] = 0.0f;
+#pragma unroll 4
+      for (int kk = 0; kk < SBK; kk++) {
+        const float4 ah = *(const float4*)&Ah[kk][tm * 4], al = *(const float4*)&Al[kk][tm * 4];
+        const float4 bh = *(const float4*)&Bh[kk][tn * 4], bl = *(const float4*)&Bl[kk][tn * 4];
+        const float a_h[4] = {ah.x, ah.y, ah.z, ah.w}, a_l[4] = {al.x, al.y, al.z, al.w};
+        const float b_h[4] = {bh.x, bh.y, bh.z, bh.w}, b_l[4] = {bl.x, bl.y, bl.z, bl.w};
+        for (int i = 0; i < 4; i++)
+          for (int j = 0; j < 4; j++)
+            sc[i][j] = fmaf(a_h[i], b_h[j], fmaf(a_h[i], b_l[j], fmaf(a_l[i], b_h[j], sc[i][j])));
+      }
+      for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+          float sm, e;
+          two_sum(hi[i][j], sc[i][j], sm, e);
+          hi[i][j] = sm;
+          lo[i][j] = __fadd_rn(lo[i][j], e);
+        }
+    }
+    __syncthreads();
+  }
+  if (!comp) return;
+  for (int i = 0; i < 4; i++) {
+    const int m = m0 + tm * 4 + i;
+    if (m >= M) continue;
+    for (int j = 0; j < 4; j++) {
+      const int col = n0 + tn * 4 + j;
+      if (col >= N) continue;
+      *contract_out(P, mode, npair, m, col) = (double)hi[i][j] + (double)lo[i][j];
+    }
+  }
+}
 
 // mode 0: xi (M = 2 ntheta rows G+, G-; N = B*pss); K = nnode_ss, or
 //         2 nnode_ss over [C_ss EE; C_ss BB] with TATT
@@ -28,32 +166,21 @@ __global__ void __launch_bounds__(CT) k_contract(Params P, const double* __restr
   __shared__ double Bs[BK][BN + 1];
   const int npair = (mode == 0) ? P.pss : (mode == 1) ? P.pgs : P.nl;
   const int N = P.B * npair;
-  const int n0 = blockIdx.x * BN;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
   const int tid = threadIdx.x;
   const int tm = tid / 16, tn = tid % 16;
   double acc[4][4];
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
-  const int LNL = P.lmax_nolimber;
   for (int k0 = 0; k0 < K; k0 += BK) {
     for (int idx = tid; idx < BK * BM; idx += CT) {
       const int kk = idx % BK, m = idx / BK;
-      As[kk][m] = (m < M && k0 + kk < K) ? A[(size_t)m * K + k0 + kk] : 0.0;
+      As[kk][m] = (m0 + m < M && k0 + kk < K) ? A[(size_t)(m0 + m) * K + k0 + kk] : 0.0;
     }
     for (int idx = tid; idx < BK * BN; idx += CT) {
       const int kk = idx % BK, n = idx / BK;
       const int col = n0 + n, k = k0 + kk;
-      double v = 0.0;
-      if (col < N && k < K) {
-        const int pt = col / npair, pr = col - pt * npair;
-        if (mode == 0)
-          v = (k < P.nnode_ss) ? P.tab_ss[((size_t)pt * P.pss + pr) * P.nnode_ss + k]
-                               : P.tab_ss_bb[((size_t)pt * P.pss + pr) * P.nnode_ss + (k - P.nnode_ss)];
-        else if (mode == 1) v = P.tab_gs[((size_t)pt * P.pgs + pr) * P.nnode_g + k];
-        else if (mode == 2) v = P.tab_gg[((size_t)pt * P.nl + pr) * P.nnode_g + k];
-        else v = (k < LNL) ? P.cnl[((size_t)pt * P.nl + pr) * LNL + k]
-                           : P.tab_gg[((size_t)pt * P.nl + pr) * P.nnode_g + (k - LNL)];
-      }
+      const double v = (col < N && k < K) ? contract_col(P, mode, col, k) : 0.0;
       Bs[kk][n] = v;
     }
     __syncthreads();
@@ -66,54 +193,53 @@ __global__ void __launch_bounds__(CT) k_contract(Params P, const double* __restr
     }
     __syncthreads();
   }
-  const int nt = P.ntheta;
-  const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
-  const int n_total = n_xi + n_gt + nt * P.nl;
   for (int i = 0; i < 4; i++) {
-    const int m = tm * 4 + i;
+    const int m = m0 + tm * 4 + i;
     if (m >= M) continue;
     for (int j = 0; j < 4; j++) {
       const int col = n0 + tn * 4 + j;
       if (col >= N) continue;
-      const int pt = col / npair, pr = col - pt * npair;
-      double* o = P.obs + (size_t)pt * n_total;
-      int idx;
-      if (mode == 0) idx = (m < nt) ? pr * nt + m : n_xi / 2 + pr * nt + (m - nt);
-      else if (mode == 1) idx = n_xi + pr * nt + m;
-      else idx = n_xi + n_gt + pr * nt + m;
-      o[idx] = acc[i][j];
+      *contract_out(P, mode, npair, m, col) = acc[i][j];
     }
   }
 }
 
+// One contraction: the FP64 kernel in the FP64 plan, the split-FP32 kernel
+// otherwise.
+static void contract(const Params& P, const double* A, const SplitFilter& F, int M, int K, int mode,
+                     int ncols, cudaStream_t s)
+{
+  if (P.prec == CL2PT_PREC_FP64) {
+    k_contract<<<dim3((ncols + BN - 1) / BN, (M + BM - 1) / BM), CT, 0, s>>>(P, A, M, K, mode);
+    return;
+  }
+  k_contract_s<<<dim3((ncols + SBN - 1) / SBN, (M + SBM - 1) / SBM), SNT, 0, s>>>(P, F, M, K, mode);
+}
+
 void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
-                     const double* filt_gg, const double* filt_gg_nl, double* scratch,
+                     const double* filt_gg, const double* filt_gg_nl, const SplitFilter* split,
                      cudaStream_t s, int* launches, const Hook& hk)
 {
-  (void)scratch;
   const int nt = P.ntheta;
   if (P.probes & CL2PT_PROBE_XI) {
-    dim3 g((P.B * P.pss + BN - 1) / BN);
     hk(CL2PT_K_LEGENDRE, 1);
     // with TATT the columns are [EE; BB] and the filters [[G+, G+], [G-, -G-]]
-    k_contract<<<g, CT, 0, s>>>(P, filt_xi, 2 * nt, (P.tatt ? 2 : 1) * P.nnode_ss, 0);
+    contract(P, filt_xi, split[0], 2 * nt, (P.tatt ? 2 : 1) * P.nnode_ss, 0, P.B * P.pss, s);
     hk(CL2PT_K_LEGENDRE, 0);
     (*launches)++;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    dim3 g((P.B * P.pgs + BN - 1) / BN);
     hk(CL2PT_K_LEGENDRE, 1);
-    k_contract<<<g, CT, 0, s>>>(P, filt_gt, nt, P.nnode_g, 1);
+    contract(P, filt_gt, split[1], nt, P.nnode_g, 1, P.B * P.pgs, s);
     hk(CL2PT_K_LEGENDRE, 0);
     (*launches)++;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    dim3 g((P.B * P.nl + BN - 1) / BN);
     hk(CL2PT_K_LEGENDRE, 1);
     if (P.adopt_limber_gg)
-      k_contract<<<g, CT, 0, s>>>(P, filt_gg, nt, P.nnode_g, 2);
+      contract(P, filt_gg, split[2], nt, P.nnode_g, 2, P.B * P.nl, s);
     else
-      k_contract<<<g, CT, 0, s>>>(P, filt_gg_nl, nt, P.lmax_nolimber + P.nnode_g, 3);
+      contract(P, filt_gg_nl, split[3], nt, P.lmax_nolimber + P.nnode_g, 3, P.B * P.nl, s);
     hk(CL2PT_K_LEGENDRE, 0);
     (*launches)++;
   }

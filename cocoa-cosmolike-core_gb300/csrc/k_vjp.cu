@@ -21,7 +21,7 @@
 //                   its redshift power) of the nuisance gradient.
 // Non-Limber w(theta) (C_cl_tomo, cosmo2D.c:4528-4769): the w contraction
 // columns are [C_nl(l < LNL); C_gg nodes]; k_vjp_handover splits their
-// adjoint into the FFTLog part (k_nl_vjp, k_nonlimber.cu), the integer-l
+// adjoint into the FFTLog part (k_nl_loop<T, true>, k_nonlimber.cu), the integer-l
 // Limber spectra (nonlinear and linear) and, above the hand-over multipole,
 // the node table through the interpol1d read-back.
 // Every quantity is recomputed from the node tables of the forward wave;

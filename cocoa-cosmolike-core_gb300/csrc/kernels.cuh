@@ -30,8 +30,18 @@ void launch_fpt_tables(const Params& P, const double* bias, const double* ia, cu
 void launch_extra(const Params& P, const double* ell_ss, const double* ell_g, cudaStream_t s,
                   int* launches, const Hook& hk);
 // xi+-, gamma_t, w on the theta bins: obs[pt][n_total]
+// A folded filter matrix [M][K] for the split-FP32 contraction: FP32 head
+// and tail of each FP64 entry, transposed to [Ksp][Mp] (K rounded up to 32,
+// M to 4) and zero padded.
+struct SplitFilter {
+  const float* hi;
+  const float* lo;
+  int Mp, Ksp;
+};
+// split: the four filters (xi, gamma_t, w Limber, w non-Limber) in split
+// form; the mixed plan contracts with these, the FP64 plan with the FP64 ones
 void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
-                     const double* filt_gg, const double* filt_gg_nl, double* scratch,
+                     const double* filt_gg, const double* filt_gg_nl, const SplitFilter* split,
                      cudaStream_t s, int* launches, const Hook& hk);
 // Fourier data vector dv[pt][nell (pss + pgs + nl)] from the node tables
 void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,

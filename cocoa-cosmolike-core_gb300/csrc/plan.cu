@@ -514,6 +514,28 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dupload(p, &p->d_filt_gt, fgt.data(), fgt.size()));
   TRY(dupload(p, &p->d_filt_gg, fgg.data(), fgg.size()));
   TRY(dupload(p, &p->d_filt_gg_nl, fggnl.data(), fggnl.size()));
+  {
+    // FP32 head/tail of each filter, transposed and zero padded for the
+    // split contraction
+    const std::vector<double>* fl[4] = {&fxi, &fgt, &fgg, &fggnl};
+    const int Ms[4] = {2 * nt, nt, nt, nt};
+    for (int f = 0; f < 4; f++) {
+      const int M = Ms[f], K = (int)(fl[f]->size() / M);
+      const int Mp = (M + 3) / 4 * 4, Ksp = (K + 31) / 32 * 32;
+      std::vector<float> hi((size_t)Mp * Ksp, 0.0f), lo((size_t)Mp * Ksp, 0.0f);
+      for (int m = 0; m < M; m++)
+        for (int k = 0; k < K; k++) {
+          const double v = (*fl[f])[(size_t)m * K + k];
+          const float h = (float)v;
+          hi[(size_t)k * Mp + m] = h;
+          lo[(size_t)k * Mp + m] = (float)(v - (double)h);
+        }
+      TRY(dupload(p, &p->d_sfilt[f][0], hi.data(), hi.size()));
+      TRY(dupload(p, &p->d_sfilt[f][1], lo.data(), lo.size()));
+      p->sfilt_Mp[f] = Mp;
+      p->sfilt_Ksp[f] = Ksp;
+    }
+  }
   int *dz1, *dz2, *dzl, *dzs;
   TRY(dupload(p, &dz1, p->z1, p->pss));
   TRY(dupload(p, &dz2, p->z2, p->pss));
@@ -1625,7 +1647,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                                     cudaMemcpyDeviceToDevice, s));
         }
       }
-      cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, nullptr,
+      cl2pt::SplitFilter sf[4];
+      for (int f = 0; f < 4; f++) sf[f] = {p->d_sfilt[f][0], p->d_sfilt[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};
+      cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, sf,
                              s, &launches, hk);
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
                              ddv + (size_t)w0 * p->n_total, s, &launches, hk);

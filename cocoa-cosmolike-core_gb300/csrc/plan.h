@@ -48,6 +48,10 @@ struct cl2pt_plan {
   double* d_filt_gt = nullptr;   // [ntheta][nnode_g]
   double* d_filt_gg = nullptr;   // [ntheta][nnode_g]       folded from lmin_tab
   double* d_filt_gg_nl = nullptr;// [ntheta][lmax_nolimber + nnode_g] head + folded from LNL
+  // the four filters split for the FP32 contraction: head, tail
+  // [K rounded up to 32][M rounded up to 4]
+  float* d_sfilt[4][2] = {};
+  int sfilt_Mp[4] = {}, sfilt_Ksp[4] = {};
   // per-point inputs staged on device when the batch is on the host
   double *d_in_om = nullptr, *d_in_h0 = nullptr, *d_in_chi = nullptr, *d_in_G = nullptr,
          *d_in_lnP = nullptr, *d_in_lnPL = nullptr;

@@ -76,9 +76,11 @@ def blocks(plan, dv):
             "w": dv[2 * a + plan.n_gammat:]}
 
 
-def run_case(name, npts, prec, seed=1, check_tables=True):
+def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None):
     import oracle as O
     w = workloads.make(name)
+    if tweak is not None:
+        tweak(w)
     tabs, nus = workloads.points(w, npts, seed=seed)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
     om, h0, chi, G, lnP = workloads.stack(tabs)
@@ -162,6 +164,19 @@ def test_small_limber_w(gpu_lib, oracle_built, prec):
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_small_nonlimber_w(gpu_lib, oracle_built, prec):
     worst, _ = run_case("real_3x2pt_small", 2, prec)
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_many_theta_bins(gpu_lib, oracle_built, prec):
+    """40 angular bins: the 2 x 40 xi filter rows span two row tiles of the
+    Legendre contraction."""
+    def tweak(w):
+        w.cfg.ntheta = 40
+    worst, _ = run_case("real_3x2pt_small_limber", 2, prec, check_tables=False, tweak=tweak)
     print(prec, worst)
     for k, v in worst.items():
         assert v <= REL, (k, v, worst)
