@@ -64,6 +64,9 @@ struct Params {
   const double* G;          // [B][G_nz]
   const double* lnP;        // [B][pk_nk*pk_nz]
   const double* lnPL;       // [B][pkl_nk*pkl_nz]
+  // mixed plan: FP32 (head, tail) of every entry of the wave's tables
+  float* lnP2;              // [B][pk_nk*pk_nz][2]
+  float* lnPL2;             // [B][pkl_nk*pkl_nz][2]; lnP2 when lnPL is lnP
   const cl2pt_nuisance* nu; // [B]
   // workspace (device), strided by point
   double* gsrc;             // [B][ns][n_a]

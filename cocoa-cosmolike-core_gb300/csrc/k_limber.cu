@@ -115,8 +115,93 @@ __device__ __forceinline__ Axis<T> load_axis(const double* __restrict__ lk, int 
   return a;
 }
 
+// ---- mixed plan: the table walk without FP64 arithmetic.  GB300 issues
+// FP64 at 1/64 of the FP32 rate, so the per-(l, node) walk runs on FP32
+// head/tail pairs: the table entries are split once per wave
+// (k_split_table), log10 k = log10(l+1/2) - log10(chi) is carried as an
+// exact two-float difference, and the in-cell offset, the corner
+// differences and exp(hi) exp(lo + delta) are formed in FP32 (the absolute
+// error of delta stays ~1e-7, i.e. ~1e-7 relative in P).
+__global__ void k_split_table(const double* __restrict__ src, float2* __restrict__ dst, size_t n)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    const float h = (float)v;
+    dst[i] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+void launch_split_tables(const Params& P, cudaStream_t s, int* launches)
+{
+  k_split_table<<<1216, 256, 0, s>>>(P.lnP, (float2*)P.lnP2, (size_t)P.B * P.pk_nk * P.pk_nz);
+  (*launches)++;
+  if (P.lnPL != P.lnP) {
+    k_split_table<<<1216, 256, 0, s>>>(P.lnPL, (float2*)P.lnPL2, (size_t)P.B * P.pkl_nk * P.pkl_nz);
+    (*launches)++;
+  }
+}
+
+struct AxisF {
+  const float* lk;   // head of log10 k (the search copy)
+  const float* lkl;  // tail
+  const float* inv;  // 1 / cell width
+  int nk;
+};
+__device__ __forceinline__ AxisF load_axis_f(const double* __restrict__ lk, int nk, float* sk, float* skl,
+                                             float* sinv)
+{
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    const float h = (float)lk[i];
+    sk[i] = h;
+    skl[i] = (float)(lk[i] - (double)h);
+    sinv[i] = (i + 1 < nk) ? (float)(1.0 / (lk[i + 1] - lk[i])) : 0.0f;
+  }
+  AxisF a;
+  a.lk = sk;
+  a.lkl = skl;
+  a.inv = sinv;
+  a.nk = nk;
+  return a;
+}
+
+// FP32 head/tail of an FP64 value
+__device__ __forceinline__ float2 split_f(double v)
+{
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
+// u = a - b for two head/tail pairs: TwoSum of the heads (exact) plus the
+// tails
+__device__ __forceinline__ void split_sub(float ah, float al, float bh, float bl, float& uh, float& ul)
+{
+  const float s = __fsub_rn(ah, bh);
+  const float bb = __fsub_rn(s, ah);
+  const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(-bh, bb));
+  uh = s;
+  ul = e + (al - bl);
+}
+
+// p_nonlin / p_lin (cosmo3D.c:306-417) at log10 k = uh + ul from the split
+// table, z cell (j, dy) of the node
+__device__ __forceinline__ float pk_eval_f(const AxisF& ax, const float2* __restrict__ tab, int nz, float uh,
+                                           float ul, int j, float dy)
+{
+  const int i = bsearch_t(ax.lk, ax.nk, uh);
+  const float dx = (__fsub_rn(uh, ax.lk[i]) + (ul - ax.lkl[i])) * ax.inv[i];
+  const float2* r0 = tab + (size_t)i * nz + j;
+  const float2* r1 = r0 + nz;
+  const float2 a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
+  const float d01 = (a01.x - a00.x) + (a01.y - a00.y);
+  const float d10 = (a10.x - a00.x) + (a10.y - a00.y);
+  const float d11 = ((a11.x - a10.x) + (a11.y - a10.y)) - d01;
+  const float del = a00.y + dy * d01 + dx * d10 + dx * dy * d11;
+  return expf(a00.x) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
 struct PdeltaTable {
   const double* tab;
+  const float2* tab2;  // split copy (mixed plan)
   const double* lk;
   const double* z;
   int nk, nz;
@@ -126,9 +211,11 @@ __device__ __forceinline__ PdeltaTable pdelta_table(const Params& P, int pt, boo
   PdeltaTable t;
   if (linear) {
     t.tab = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    t.tab2 = (const float2*)P.lnPL2 + (size_t)pt * P.pkl_nk * P.pkl_nz;
     t.lk = P.pkl_lk; t.z = P.pkl_z; t.nk = P.pkl_nk; t.nz = P.pkl_nz;
   } else {
     t.tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+    t.tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
     t.lk = P.pk_lk; t.z = P.pk_z; t.nk = P.pk_nk; t.nz = P.pk_nz;
   }
   return t;
@@ -151,7 +238,14 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   T* X = Ps + PCH * LT;
   T* ndy = X + (size_t)P.pss * PCH;
   int* nj = (int*)(ndy + PCH);
-  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  // mixed plan: axis tails and widths as floats where the FP64 axis was,
+  // node log10 chi as head/tail pairs
+  Axis<T> ax{};
+  AxisF axf{};
+  float2* nlc2 = (float2*)nlc;
+  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
+  else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
   const double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
@@ -164,7 +258,9 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
     for (int p = tid; p < np; p += LT) {
-      nlc[p] = log10(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
+      const double v = log10(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
+      if constexpr (F32) nlc2[p] = split_f(v);
+      else nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + p0 + p];
       nj[p] = nodej[p0 + p];
     }
@@ -179,8 +275,17 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     __syncthreads();
     if (!valid) continue;
     const double llp = log10(lp);
-    for (int p = 0; p < np; p++)
-      Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+    if constexpr (F32) {
+      const float2 ll = split_f(llp);
+      for (int p = 0; p < np; p++) {
+        float uh, ul;
+        split_sub(ll.x, ll.y, nlc2[p].x, nlc2[p].y, uh, ul);
+        Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
+      }
+    } else {
+      for (int p = 0; p < np; p++)
+        Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+    }
     for (int pair = 0; pair < P.pss; pair++) {
       T acc = 0;
       const T* xr = X + pair * PCH;
@@ -223,7 +328,12 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   T* X = Ps + PCH * LT;                  // [nterm][npair][PCH]
   T* ndy = X + (size_t)2 * CL2PT_MAXB * PCH;
   int* nj = (int*)(ndy + PCH);
-  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  Axis<T> ax{};
+  AxisF axf{};
+  float2* nlc2 = (float2*)nlc;
+  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
+  else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const int off = P.n_ss + q * P.n_ss;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
@@ -242,7 +352,9 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
     for (int p = tid; p < np; p += LT) {
-      nlc[p] = log10(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
+      const double v = log10(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
+      if constexpr (F32) nlc2[p] = split_f(v);
+      else nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
       nj[p] = nodej[off + p0 + p];
     }
@@ -260,8 +372,17 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     __syncthreads();
     if (!valid) continue;
     const double llp = log10(lp);
-    for (int p = 0; p < np; p++)
-      Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+    if constexpr (F32) {
+      const float2 ll = split_f(llp);
+      for (int p = 0; p < np; p++) {
+        float uh, ul;
+        split_sub(ll.x, ll.y, nlc2[p].x, nlc2[p].y, uh, ul);
+        Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
+      }
+    } else {
+      for (int p = 0; p < np; p++)
+        Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+    }
     for (int m = 0; m < np_; m++) {
       T a0 = 0, a1 = 0;
       const T* x0 = X + (0 * CL2PT_MAXB + m) * PCH;
@@ -334,8 +455,23 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   T* sc = sy + nzs;
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
-  const Axis<T> ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
-  const Axis<T> axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  // mixed plan: the node data as floats [9][PCH] where the FP64 node data
+  // was (fK c/H0, weight, z offset in lnP, L, M, r0, z offset in lnPL,
+  // log10(fK c/H0) head and tail), the first kept multipole index of each
+  // node where the thresholds were, axis tails and widths as floats where
+  // the FP64 axes were
+  float* nf = (float*)nd;
+  int* lmin = (int*)thr;
+  Axis<T> ax{}, axl{};
+  AxisF axf{}, axlf{};
+  if constexpr (F32) {
+    axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
+    axlf = load_axis_f(pl.lk, pl.nk, (float*)lkl, (float*)sdl, (float*)sdl + pl.nk);
+  } else {
+    ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
+    axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
+  }
   const double* Z = P.chi_z;
   for (int i = tid; i < nc; i += LTG) {
     cx[i] = (T)Xg[i];
@@ -383,31 +519,75 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     for (int p = tid; p < np; p += LTG) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p0 + p];
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
-      nd[0 * PCH + p] = fK;
-      nd[1 * PCH + p] = node[(size_t)NF_WT * P.node_stride + off + p0 + p] *
+      const double wq = node[(size_t)NF_WT * P.node_stride + off + p0 + p] *
                         node[(size_t)NF_DCHIDA * P.node_stride + off + p0 + p] / (fK * fK);
-      nd[2 * PCH + p] = node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
-      nd[3 * PCH + p] = P.wgg_l[b0 * P.n_gg + p0 + p];
-      nd[4 * PCH + p] = P.wgg_m[b0 * P.n_gg + p0 + p];
-      nd[5 * PCH + p] = P.wgg_r0[b0 * P.n_gg + p0 + p];
+      const double dyz = node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
+      const double Lw = P.wgg_l[b0 * P.n_gg + p0 + p];
+      const double Mw = P.wgg_m[b0 * P.n_gg + p0 + p];
+      const double r0w = P.wgg_r0[b0 * P.n_gg + p0 + p];
       nj[p] = nodej[off + p0 + p];
       const double z = 1.0 / a - 1.0;
       const int jl = bsearch_d(pl.z, pl.nz, z);
       nj[PCH + p] = jl;
-      nd[6 * PCH + p] = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
-      nd[7 * PCH + p] = log10(fK * CL2PT_COVERH0);
+      const double dyl = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
+      const double lfk = log10(fK * CL2PT_COVERH0);
       // chi1 = fK (l+3/2)/(l+1/2) > chi(a_min)  <=>  l+1/2 < fK / (chi(a_min) - fK)
-      // (always when fK >= chi(a_min)): one compare per (l, node)
-      thr[p] = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
+      // (always when fK >= chi(a_min))
+      const double th = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
+      if constexpr (F32) {
+        nf[0 * PCH + p] = (float)(fK * CL2PT_COVERH0);
+        nf[1 * PCH + p] = (float)wq;
+        nf[2 * PCH + p] = (float)dyz;
+        nf[3 * PCH + p] = (float)Lw;
+        nf[4 * PCH + p] = (float)Mw;
+        nf[5 * PCH + p] = (float)r0w;
+        nf[6 * PCH + p] = (float)dyl;
+        const float2 lf = split_f(lfk);
+        nf[7 * PCH + p] = lf.x;
+        nf[8 * PCH + p] = lf.y;
+        // the multipoles cut form a prefix: the first kept index
+        int lo = 0, hi = nL;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          const double lpm = ((mode == 0) ? ell[mid] : (double)mid) + 0.5;
+          if (lpm < th) lo = mid + 1;
+          else hi = mid;
+        }
+        lmin[p] = lo;
+      } else {
+        nd[0 * PCH + p] = fK;
+        nd[1 * PCH + p] = wq;
+        nd[2 * PCH + p] = dyz;
+        nd[3 * PCH + p] = Lw;
+        nd[4 * PCH + p] = Mw;
+        nd[5 * PCH + p] = r0w;
+        nd[6 * PCH + p] = dyl;
+        nd[7 * PCH + p] = lfk;
+        thr[p] = th;
+      }
     }
     __syncthreads();
     if (!valid) continue;
     const double llp = log10(lp);
+    const float2 ll = split_f(llp);
+    float snl = 0.0f, sln = 0.0f;  // mixed plan: this chunk's FP32 sums
     for (int p = 0; p < np; p++) {
-      const double fK = nd[0 * PCH + p];
-      if (lp < thr[p]) continue;  // (l+3/2)/k beyond chi(a_min)
+      T fkc, Lw, Mw, r0w;
+      if constexpr (F32) {
+        if (L < lmin[p]) continue;  // (l+3/2)/k beyond chi(a_min)
+        fkc = nf[0 * PCH + p];
+        Lw = nf[3 * PCH + p];
+        Mw = nf[4 * PCH + p];
+        r0w = nf[5 * PCH + p];
+      } else {
+        if (lp < thr[p]) continue;
+        fkc = (T)(nd[0 * PCH + p] * CL2PT_COVERH0);
+        Lw = (T)nd[3 * PCH + p];
+        Mw = (T)nd[4 * PCH + p];
+        r0w = (T)nd[5 * PCH + p];
+      }
       // a_chi at chi1 (cosmo3D.c:109-133)
-      const T c = (T)(fK * CL2PT_COVERH0) * ratio;
+      const T c = fkc * ratio;
       const int j = bsearch_t(cx, nc, c);
       const T dyc = (c - cx[j]) / (cx[j + 1] - cx[j]);
       const T z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
@@ -431,16 +611,28 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
         const T dq = (sc[i + 1] - sc[i]) / ((T)3 * h);
         n1 = (sy[i] + t * (bq + t * (sc[i] + t * dq))) / lst;
       }
-      const T wrsd = c0 * (T)nd[5 * PCH + p] - c1 * n1 * H1 * f1;
-      const T s = (T)nd[3 * PCH + p] + (T)nd[4 * PCH + p] * pref + wrsd;
-      const double s2w = (double)(s * s) * nd[1 * PCH + p];
-      const double log10k = llp - nd[7 * PCH + p];
-      const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
-      sum_nl += s2w * (double)Pnl;
-      if (mode == 1) {
-        const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
-        sum_lin += s2w * (double)Pl;
+      const T wrsd = c0 * r0w - c1 * n1 * H1 * f1;
+      const T s = Lw + Mw * pref + wrsd;
+      if constexpr (F32) {
+        const float s2w = s * s * nf[1 * PCH + p];
+        float uh, ul;
+        split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
+        snl += s2w * pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p]);
+        if (mode == 1) sln += s2w * pk_eval_f(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p]);
+      } else {
+        const double s2w = (double)(s * s) * nd[1 * PCH + p];
+        const double log10k = llp - nd[7 * PCH + p];
+        const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
+        sum_nl += s2w * (double)Pnl;
+        if (mode == 1) {
+          const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
+          sum_lin += s2w * (double)Pl;
+        }
       }
+    }
+    if constexpr (F32) {
+      sum_nl += (double)snl;
+      sum_lin += (double)sln;
     }
   }
   if (!valid) return;

@@ -19,6 +19,8 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 // Limber C_l tables on the C_l nodes (ss, gs, gg) and, when the non-Limber
 // w(theta) path is on, the Limber gg C_l at integer l < lmax_nolimber for
 // both power spectra.  ell_ss / ell_g: node multipoles (device).
+// mixed plan: split the wave's lnP (and separate lnPL) into P.lnP2 / P.lnPL2
+void launch_split_tables(const Params& P, cudaStream_t s, int* launches);
 void launch_limber(const Params& P, const double* ell_ss, const double* ell_g,
                    cudaStream_t s, int* launches, const Hook& hk);
 // TATT / one-loop extras (k_extra.cu): p_lin on the FAST-PT grid, the

@@ -603,6 +603,10 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
+  if (precision != CL2PT_PREC_FP64) {
+    TRY(dalloc(p, &P.lnP2, (size_t)W * 2 * P.pk_nk * P.pk_nz));
+    TRY(dalloc(p, &P.lnPL2, (size_t)W * 2 * P.pkl_nk * P.pkl_nz));
+  }
   // TATT intrinsic alignments and one-loop galaxy bias: FAST-PT tables per
   // point on the reference's grid (k in [0.05, 1e6] c/H0 units, 1100
   // points; pt_cfastpt.c:53-60, 235-240) and the extra node weights
@@ -1568,6 +1572,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     P.lnPL = lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
     P.nu = nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
+    if (P.prec != CL2PT_PREC_FP64) {
+      if (P.lnPL == P.lnP) P.lnPL2 = P.lnP2;
+      cl2pt::launch_split_tables(P, s, &launches);
+    }
     if (P.tatt || P.one_loop) {
       cl2pt::launch_fpt_plin(P, s, &launches);
       if (P.one_loop) {
