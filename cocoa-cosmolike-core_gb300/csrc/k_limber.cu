@@ -56,11 +56,8 @@ __device__ __forceinline__ T pk_walk(const T* __restrict__ lk, int nk,
   return exp_t<T>(v) * (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
 }
 
-// Table walk used by the kernels.  FP64 plan: the reference formula above.
-// Mixed plan: the cell search runs on an FP32 copy of the log10 k axis, but
-// the in-cell offset and the lnP differences are formed in FP64 and the
-// exponent is split as exp(hi) exp(lo + delta) with hi = (float) lnP_00, so
-// that FP32 rounding of |lnP| ~ 10 does not cost ~1e-6 in P.
+// Table walk of the FP64 plan: the reference formula above on the FP64
+// table (the mixed plan walks the split table, pk_eval_f below).
 template <typename T>
 struct Axis {
   const T* lk;       // search copy (loop precision)
@@ -70,30 +67,9 @@ struct Axis {
 };
 template <typename T>
 __device__ __forceinline__ T pk_eval(const Axis<T>& ax, const double* __restrict__ tab, int nz,
-                                     double log10k, int j, T dy);
-template <>
-__device__ __forceinline__ double pk_eval<double>(const Axis<double>& ax,
-                                                  const double* __restrict__ tab, int nz,
-                                                  double log10k, int j, double dy)
+                                     double log10k, int j, T dy)
 {
-  return pk_walk<double>(ax.lk, ax.nk, tab, nz, log10k, j, dy);
-}
-template <>
-__device__ __forceinline__ float pk_eval<float>(const Axis<float>& ax,
-                                                const double* __restrict__ tab, int nz,
-                                                double log10k, int j, float dy)
-{
-  const int i = bsearch_t(ax.lk, ax.nk, (float)log10k);
-  const float dx = (float)((log10k - ax.lkd[i]) * ax.inv[i]);
-  const double* r0 = tab + (size_t)i * nz + j;
-  const double* r1 = r0 + nz;
-  const double a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
-  const float d01 = (float)(a01 - a00), d10 = (float)(a10 - a00);
-  const float d11 = (float)((a11 - a10) - (a01 - a00));
-  const float hi = (float)a00;
-  const float lo = (float)(a00 - (double)hi);
-  const float del = lo + dy * d01 + dx * d10 + dx * dy * d11;
-  return expf(hi) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+  return pk_walk<T>(ax.lk, ax.nk, tab, nz, (T)log10k, j, dy);
 }
 
 // Load one log10 k axis into shared memory (search copy, FP64 copy and

@@ -416,8 +416,8 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
 }  // namespace
 
 void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, const NLParams& Q, int nell,
-                        const double* ell, double lmax_shear, const double* lfac_g_std, cudaStream_t s,
-                        int* launches)
+                        const double* ell, double lmax_shear, const double* lfac_g_std,
+                        const float* lfacf_g_std, cudaStream_t s, int* launches)
 {
   const int n_total = nell * (Pf.pss + Pf.pgs + Pf.nl);
   launch_gtab_dz(Pf, V.dgsrc, s);
@@ -459,6 +459,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     VJPParams V2 = V;
     V2.cbar_gg = V.cbar_gg2;
     V2.lfac_g = lfac_g_std;
+    V2.lfacf_g = lfacf_g_std;
     V2.lfac_g_sorted = 1;
     const int Kw = Pg->lmax_nolimber + Pg->nnode_g;
     k_vjp_fourier_w<<<dim3((Pg->nl * Kw + 255) / 256, Pg->B), 256, 0, s>>>(*Pg, V2);

@@ -10,11 +10,13 @@
 //     inside a cell and flushed with four FP64 atomics when the cell changes;
 //   * the node-weight adjoints (x_bar per pair, L_bar for the lens weight).
 // Precision follows the plan: in the mixed plan the per-(l, p) arithmetic
-// (table walk, W_RSD, products) is FP32 with the forward's split exponent
-// (exp(hi) exp(lo + delta), cell differences formed in FP64), the table
-// coordinate and the in-cell offset are FP64, and every accumulator is FP64
-// (FP32 partial sums over chunks of LC multipoles); in the FP64 plan all of
-// it is FP64.  Per-multipole factors (log10(l+1/2), the l prefactors, the
+// (table walk, W_RSD, products) is FP32: the walk runs on the wave's split
+// table (FP32 head/tail per entry) with the forward's split exponent
+// exp(hi) exp(lo + delta), the table coordinate log10 k is an exact
+// two-float difference, the per-multipole factors come from FP32 copies,
+// and the accumulators are FP64 (FP32 partial sums over chunks of LC
+// multipoles, FP64 atomics at cell changes); in the FP64 plan all of it is
+// FP64.  Per-multipole factors (log10(l+1/2), the l prefactors, the
 // RSD coefficients) are plan constants (VJPParams::lfac_*).
 #include <algorithm>
 
@@ -85,6 +87,76 @@ __device__ __forceinline__ void pw_acc(PWalk<T>& w, T g, T dx)
   w.acc1 += g * dx;
 }
 
+// ---- mixed plan: the walk without FP64 arithmetic, on the wave's split
+// table (FP32 head/tail per entry) with log10 k = uh + ul as an unevaluated
+// two-float sum; only the scatter atomics stay FP64.
+struct AxF {
+  const float* lk;   // head of log10 k (search copy)
+  const float* lkl;  // tail
+  const float* inv;  // 1 / cell width
+  int nk;
+};
+// the FP32 axis in the space of the FP64 one (2 nk doubles >= 3 nk floats)
+__device__ __forceinline__ AxF load_axis_fx(const double* __restrict__ lk, int nk, double* space)
+{
+  float* h = (float*)space;
+  float* l = h + nk;
+  float* iv = l + nk;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    const float v = (float)lk[i];
+    h[i] = v;
+    l[i] = (float)(lk[i] - (double)v);
+    iv[i] = (i + 1 < nk) ? (float)(1.0 / (lk[i + 1] - lk[i])) : 0.0f;
+  }
+  AxF a;
+  a.lk = h;
+  a.lkl = l;
+  a.inv = iv;
+  a.nk = nk;
+  return a;
+}
+__device__ __forceinline__ float2 split_fx(double v)
+{
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+// u = a - b for head/tail pairs (TwoSum of the heads plus the tails)
+__device__ __forceinline__ void sub_fx(float ah, float al, float bh, float bl, float& uh, float& ul)
+{
+  const float s = __fsub_rn(ah, bh);
+  const float bb = __fsub_rn(s, ah);
+  const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(-bh, bb));
+  uh = s;
+  ul = e + (al - bl);
+}
+__device__ __forceinline__ float pw_eval_f(PWalk<float>& w, const AxF& ax, const float2* __restrict__ tab, int nz,
+                                           int j, double dy, float dyt, float uh, float ul,
+                                           double* __restrict__ bar, float& dx)
+{
+  int i = w.i;
+  if (!(i >= 0 && ax.lk[i] <= uh && (uh < ax.lk[i + 1] || i == ax.nk - 2))) {
+    pw_flush(w, bar, nz, j, dy);
+    int lo = 0, hi = ax.nk - 1;
+    while (hi > lo + 1) {
+      const int mid = (lo + hi) >> 1;
+      if (ax.lk[mid] > uh) hi = mid; else lo = mid;
+    }
+    i = lo;
+    w.i = i;
+    const float2* r0 = tab + (size_t)i * nz + j;
+    const float2* r1 = r0 + nz;
+    const float2 a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
+    w.d01 = (a01.x - a00.x) + (a01.y - a00.y);
+    w.d10 = (a10.x - a00.x) + (a10.y - a00.y);
+    w.d11 = ((a11.x - a10.x) + (a11.y - a10.y)) - w.d01;
+    w.lo = a00.y;
+    w.eh = expf(a00.x);
+  }
+  dx = (__fsub_rn(uh, ax.lk[i]) + (ul - ax.lkl[i])) * ax.inv[i];
+  const float del = w.lo + dyt * w.d01 + dx * (w.d10 + dyt * w.d11);
+  return w.eh * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
 __device__ __forceinline__ void load_axis_d(const double* __restrict__ lk, int nk, double* lkd, double* inv)
 {
   for (int i = threadIdx.x; i < nk; i += blockDim.x) {
@@ -126,7 +198,10 @@ __global__ void k_vjp_ss(Params P, VJPParams V)
   T* xt = (T*)(xb + (size_t)np * nn);  // [np][nn] chunk partial sums
   T* w2 = xt + (size_t)np * nn;     // [np][nn] w_a w_b
   T* cbs = w2 + (size_t)np * nn;    // [np][LC]
-  load_axis_d(P.pk_lk, nk, lkd, inv);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  AxF axf{};
+  if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
+  else load_axis_d(P.pk_lk, nk, lkd, inv);
   const double* w = P.wss + (size_t)pt * P.ns * nn;
   for (int i = p; i < np * nn; i += blockDim.x) {
     const int pr = i / nn, q = i - pr * nn;
@@ -139,6 +214,8 @@ __global__ void k_vjp_ss(Params P, VJPParams V)
   if (act) nd = node_d(P, pt, p);
   const T Ft = (T)nd.F, dyt = (T)nd.dy;
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2* tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   const int Kx = (P.tatt ? 2 : 1) * K;  // with TATT the rows hold [EE; BB]
   const double* cb = V.cbar_ss + (size_t)pt * np * Kx;
@@ -154,9 +231,16 @@ __global__ void k_vjp_ss(Params P, VJPParams V)
     if (!act) continue;
     for (int l = 0; l < nL; l++) {
       const int L = L0 + l;
-      T dx;
-      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, V.lfac_ss[2 * L] - nd.lfk, bar, dx);
-      const T pc = (T)V.lfac_ss[2 * L + 1] * Pv;
+      T dx, pc;
+      if constexpr (F32) {
+        const float4 fa = *(const float4*)(V.lfacf_ss + 8 * L);
+        float uh, ul;
+        sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
+        pc = fa.z * pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
+      } else {
+        const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, V.lfac_ss[2 * L] - nd.lfk, bar, dx);
+        pc = (T)V.lfac_ss[2 * L + 1] * Pv;
+      }
       T pb = 0;
       for (int pr = 0; pr < np; pr++) {
         const T cv = cbs[pr * LC + l];
@@ -211,7 +295,10 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   T* xt = (T*)(xs + (size_t)np * nn);  // [np][nn]
   T* wxs = xt + (size_t)np * nn;       // [np][nn]
   T* cbs = wxs + (size_t)np * nn;      // [np][LC]
-  load_axis_d(P.pk_lk, nk, lkd, inv);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  AxF axf{};
+  if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
+  else load_axis_d(P.pk_lk, nk, lkd, inv);
   const size_t b0 = (size_t)pt * P.nl + q;
   const double* wx = P.wgs_x + b0 * P.ns * nn;
   for (int i = p; i < np * nn; i += blockDim.x) {
@@ -231,6 +318,8 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   }
   const T Ft = (T)nd.F, dyt = (T)nd.dy, Lt = (T)Lw, Mt = (T)Mw;
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2* tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   PWalk<T> wk;
   double lb0 = 0.0, lb1 = 0.0;
@@ -246,11 +335,20 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     T t0 = 0, t1 = 0;
     for (int l = 0; l < nL; l++) {
       const int L = L0 + l;
-      const double* fac = V.lfac_g + 6 * L;
-      T dx;
-      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
-      const T pref = (T)fac[2];
-      const T g = (T)fac[1] * Pv * Ft;
+      T dx, pref, g;
+      if constexpr (F32) {
+        const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
+        float uh, ul;
+        sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
+        const float Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
+        pref = fa.w;
+        g = fa.z * Pv * Ft;
+      } else {
+        const double* fac = V.lfac_g + 6 * L;
+        const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+        pref = (T)fac[2];
+        g = (T)fac[1] * Pv * Ft;
+      }
       const T gl = g * (Lt + pref * Mt);
       T sx = 0;
       for (int m = 0; m < np; m++) {
@@ -339,8 +437,15 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   T* sc = sy + nzs;
   T* cbs = sc + nzs;       // [K] C_bar of this bin
   T* gbs = cbs + K;        // [LNL][2] integer-l adjoints (non-Limber)
-  load_axis_d(P.pk_lk, nk, lkd, inv);
-  if (nonlim) load_axis_d(P.pkl_lk, nkl, lkdl, invl);
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  AxF axf{}, axlf{};
+  if constexpr (F32) {
+    axf = load_axis_fx(P.pk_lk, nk, lkd);
+    if (nonlim) axlf = load_axis_fx(P.pkl_lk, nkl, lkdl);
+  } else {
+    load_axis_d(P.pk_lk, nk, lkd, inv);
+    if (nonlim) load_axis_d(P.pkl_lk, nkl, lkdl, invl);
+  }
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
   const double* Z = P.chi_z;
@@ -382,11 +487,14 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const T cH0 = (T)CL2PT_COVERH0;
   const T fkc = (T)(nd.fK * CL2PT_COVERH0);
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2* tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
+  const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   int hc = 0, hz = 0, hg = 0, hn = 0;
-  // s(l, p) for the multipole factors fac = (log10 lp, pref2, pref, c0, c1, (lp+1)/lp)
-  auto s_of = [&](const double* fac) -> T {
-    const T c = fkc * (T)fac[5];
+  // s(l, p) for the multipole factors pref = l(l+1)/lp^2, the RSD c0, c1
+  // and ratio = (lp+1)/lp
+  auto s_of = [&](T pref, T c0, T c1, T ratio) -> T {
+    const T c = fkc * ratio;
     const int j = hsearch_t(cx, nc, c, hc);
     const T dyc = (c - cx[j]) / (cx[j + 1] - cx[j]);
     const T z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
@@ -414,8 +522,8 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       const T dq = (sc[i + 1] - sc[i]) / ((T)3 * h);
       n1 = (sy[i] + t * (bq + t * (sc[i] + t * dq))) / lst;
     }
-    const T wrsd = (T)fac[3] * r0 - (T)fac[4] * n1 * H1 * f1;
-    return Lt + Mt * (T)fac[2] + wrsd;
+    const T wrsd = c0 * r0 - c1 * n1 * H1 * f1;
+    return Lt + Mt * pref + wrsd;
   };
   PWalk<T> wk;
   double lbar = 0.0;
@@ -428,9 +536,17 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       if (!V.lfac_g_sorted && nd.fK * fac[5] > chi_amin) continue;
       const T cv = cbs[L];
       if (cv == (T)0) continue;
-      const T s = s_of(fac);
-      T dx;
-      const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+      T dx, s, Pv;
+      if constexpr (F32) {
+        const float4 fa = *(const float4*)(V.lfacf_g + 8 * L), fb = *(const float4*)(V.lfacf_g + 8 * L + 4);
+        s = s_of(fa.w, fb.x, fb.y, fb.z);
+        float uh, ul;
+        sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
+        Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
+      } else {
+        s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
+        Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+      }
       const T sp = s * Ft * Pv;
       lt += (T)2 * cv * sp;
       pw_acc<T>(wk, cv * s * sp, dx);
@@ -445,6 +561,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     const double dyl = (z - P.pkl_z[jl]) / (P.pkl_z[jl + 1] - P.pkl_z[jl]);
     const T dylt = (T)dyl;
     const double* tabl = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+    const float2* tabl2 = (const float2*)P.lnPL2 + (size_t)pt * P.pkl_nk * P.pkl_nz;
     double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
@@ -452,12 +569,21 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     for (int L = first_kept(V.lfac_gi, LNL, nd.fK, chi_amin); L < LNL; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
-      const double* fac = V.lfac_gi + 6 * L;
-      const T s = s_of(fac);
-      const double lk = fac[0] - nd.lfk;
-      T dx, dxl;
-      const T Pn = pw_eval<T>(wn, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, lk, bar, dx);
-      const T Pl = pw_eval<T>(wl, lkdl, invl, nkl, tabl, P.pkl_nz, jl, dyl, dylt, lk, barl, dxl);
+      T dx, dxl, s, Pn, Pl;
+      if constexpr (F32) {
+        const float4 fa = *(const float4*)(V.lfacf_gi + 8 * L), fb = *(const float4*)(V.lfacf_gi + 8 * L + 4);
+        s = s_of(fa.w, fb.x, fb.y, fb.z);
+        float uh, ul;
+        sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
+        Pn = pw_eval_f(wn, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
+        Pl = pw_eval_f(wl, axlf, tabl2, P.pkl_nz, jl, dyl, dylt, uh, ul, barl, dxl);
+      } else {
+        const double* fac = V.lfac_gi + 6 * L;
+        s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
+        const double lk = fac[0] - nd.lfk;
+        Pn = pw_eval<T>(wn, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, lk, bar, dx);
+        Pl = pw_eval<T>(wl, lkdl, invl, nkl, tabl, P.pkl_nz, jl, dyl, dylt, lk, barl, dxl);
+      }
       const T sF = s * Ft;
       lt += (T)2 * sF * (cn * Pn + cl * Pl);
       pw_acc<T>(wn, cn * s * sF * Pn, dx);

@@ -88,6 +88,11 @@ struct VJPParams {
   const double* lfac_ss;
   const double* lfac_g;
   const double* lfac_gi;   // the same factors at l = 0..LNL-1
+  // FP32 copies for the mixed plan, 8 floats per multipole: log10(l+1/2) as
+  // head and tail, then the remaining factors in order (ss: 1, g: 5)
+  const float* lfacf_ss;
+  const float* lfacf_g;
+  const float* lfacf_gi;
   // Fourier path: second clustering C_bar (standard nodes of the FFTLog
   // hand-over pass) [B][nl][nnode_g]
   double* cbar_gg2;
@@ -122,7 +127,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
 // pass on the standard nodes with the FFTLog below LMAX_NOLIMBER (lfac_g_std
 // its node factors)
 void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, const NLParams& Q, int nell,
-                        const double* ell, double lmax_shear, const double* lfac_g_std, cudaStream_t s,
-                        int* launches);
+                        const double* ell, double lmax_shear, const double* lfac_g_std,
+                        const float* lfacf_g_std, cudaStream_t s, int* launches);
 
 }  // namespace cl2pt

@@ -246,6 +246,23 @@ void fold(const double* f, int L, int nint, int lfill, const double* lim, int ne
   }
 }
 
+// FP32 copy of a per-multipole factor table of `per` doubles per multipole
+// (log10(l+1/2) first): 8 floats per multipole, log10(l+1/2) as head and
+// tail, then the other factors
+std::vector<float> lfac_f32(const std::vector<double>& f, int per)
+{
+  const size_t n = f.size() / per;
+  std::vector<float> o(8 * n, 0.0f);
+  for (size_t i = 0; i < n; i++) {
+    const double v = f[per * i];
+    const float h = (float)v;
+    o[8 * i] = h;
+    o[8 * i + 1] = (float)(v - (double)h);
+    for (int k = 1; k < per; k++) o[8 * i + 1 + k] = (float)f[per * i + k];
+  }
+  return o;
+}
+
 template <typename T>
 int dupload(cl2pt_plan* p, T** dst, const T* src, size_t n)
 {
@@ -509,6 +526,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     }
     TRY(dupload(p, &p->d_lfac_ss, fs.data(), fs.size()));
     TRY(dupload(p, &p->d_lfac_g, fg.data(), fg.size()));
+    const std::vector<float> fsf = lfac_f32(fs, 2), fgf = lfac_f32(fg, 6);
+    TRY(dupload(p, &p->d_lfacf_ss, fsf.data(), fsf.size()));
+    TRY(dupload(p, &p->d_lfacf_g, fgf.data(), fgf.size()));
   }
   TRY(dupload(p, &p->d_filt_xi, fxi.data(), fxi.size()));
   TRY(dupload(p, &p->d_filt_gt, fgt.data(), fgt.size()));
@@ -935,6 +955,7 @@ static int vjp_prepare(cl2pt_plan* p)
     if (!a && p->d_in_lnPL)
       a = dalloc(p, &p->d_vjp_lnpl, (size_t)p->max_batch * p->P.pkl_nk * p->P.pkl_nz);
     if (!a) a = dalloc(p, &p->d_lfac_f, 8 * (size_t)std::max(p->nnode_ss, p->nnode_g));
+    if (!a) a = dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g));
     if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
     if (a) {
       p->d_vjp_ws = nullptr;
@@ -1487,6 +1508,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.lfac_g = p->d_lfac_g;
     V0.lfac_g_sorted = 1;
     V0.lfac_gi = p->d_lfac_g + 6 * (size_t)p->nnode_g;
+    V0.lfacf_ss = p->d_lfacf_ss;
+    V0.lfacf_g = p->d_lfacf_g;
+    V0.lfacf_gi = p->d_lfacf_g + 8 * (size_t)p->nnode_g;
   }
   int launches = 0;
   struct HookCtx { cl2pt_plan* p; cudaStream_t s; cudaEvent_t (*ev)(cl2pt_plan*); };
@@ -1557,6 +1581,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     }
     CUDA_OK(cudaMemcpyAsync(p->d_lfac_f, fs.data(), sizeof(double) * fs.size(), cudaMemcpyHostToDevice, s));
     CUDA_OK(cudaMemcpyAsync(p->d_lfac_f + 2 * (size_t)fr->nell, fg.data(), sizeof(double) * fg.size(),
+                            cudaMemcpyHostToDevice, s));
+    const std::vector<float> fsf = lfac_f32(fs, 2), fgf = lfac_f32(fg, 6);
+    CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f, fsf.data(), sizeof(float) * fsf.size(), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f + 8 * (size_t)fr->nell, fgf.data(), sizeof(float) * fgf.size(),
                             cudaMemcpyHostToDevice, s));
     // the host vectors must outlive the copies
     CUDA_OK(cudaStreamSynchronize(s));
@@ -1637,9 +1665,11 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         if (st2) return st2;
         V.lfac_ss = p->d_lfac_f;
         V.lfac_g = p->d_lfac_f + 2 * (size_t)fr->nell;
+        V.lfacf_ss = p->d_lfacf_f;
+        V.lfacf_g = p->d_lfacf_f + 8 * (size_t)fr->nell;
         V.lfac_g_sorted = ell_sorted ? 1 : 0;
         cl2pt::launch_vjp_fourier(Pf, use_nl ? &Pg : nullptr, V, p->nlq, fr->nell, p->d_ell_f, fr->lmax_shear,
-                                  p->d_lfac_g, s, &launches);
+                                  p->d_lfac_g, p->d_lfacf_g, s, &launches);
       }
     } else {
       cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);

@@ -92,6 +92,9 @@ struct cl2pt_plan {
   double* d_lfac_ss = nullptr;         // per-multipole constants of the adjoint sweeps
   double* d_lfac_g = nullptr;
   double* d_lfac_f = nullptr;          // the same for the caller's multipoles (Fourier)
+  float* d_lfacf_ss = nullptr;         // FP32 copies (8 floats per multipole)
+  float* d_lfacf_g = nullptr;
+  float* d_lfacf_f = nullptr;
   double* d_chi2 = nullptr;            // [max_batch] chi^2 staging
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
