@@ -51,6 +51,10 @@ struct Params {
   // n(z) splines: zc [nz], y/c [(ntomo+1)][nz]
   int src_nz, lens_nz;
   const double *src_zc, *src_y, *src_c, *lens_zc, *lens_y, *lens_c;
+  // source splines per interval: b, d of spline_d (same layout as src_c)
+  // and a float copy of the nodes (search)
+  const double *src_b, *src_d;
+  const float* src_zcf;
   double src_zmin_all, src_zmax_all, lens_zmax_all;
   double lens_zmin[CL2PT_MAXB], lens_zmax[CL2PT_MAXB], zmean_lens[CL2PT_MAXB];
   // quadrature rules on [-1, 1]
@@ -70,6 +74,7 @@ struct Params {
   const cl2pt_nuisance* nu; // [B]
   // workspace (device), strided by point
   double* gsrc;             // [B][ns][n_a]
+  double* gfine;            // [B][Na][4] source fine grid of g_tomo: z, chi, 1/a^2, 1/chi
   double* glens;            // [B][nl][n_a]
   double* node;             // [B][NODE_FIELDS][node_stride]
   int* node_j;              // [B][node_stride]

@@ -1,9 +1,12 @@
 // k_setup.cu -- per-point FP64 set-up stage of the batched 2-point path.
 //
-//   k_gtab   lens-efficiency tables g(a) of every source bin (g_tomo,
-//            redshift_spline.c:852-923) and, when magnification is on, of
-//            every lens bin (g_lens, redshift_spline.c:1014-1109): one CTA
-//            per (point, bin), the cumulative trapezoid done as a block scan.
+//   k_gfine  the source fine grid of g_tomo per point (z, chi, 1/a^2, 1/chi)
+//   k_gsrc   lens-efficiency tables g(a) of every source bin (g_tomo,
+//            redshift_spline.c:852-923) on that grid, and their tangent in
+//            the bin's photo-z shift: one CTA per (point, bin), the
+//            cumulative trapezoid done as a block scan.
+//   k_gtab   the same for every lens bin when magnification is on (g_lens,
+//            redshift_spline.c:1014-1109).
 //   k_nodes  Gauss-Legendre nodes in a with chi, dchi/da, D, H/H0 at each
 //            node (create_cosmo_nodes, cosmo2D.c:1331-1356) and the radial
 //            weights the Limber integrands need (radial_weights.c:15-105,
@@ -56,10 +59,10 @@ constexpr int GT_NT = 256;
 // shift (the trapezoid sums are linear in n, so n is replaced by
 // d n(z - dz)/d dz); written to dz_out [B][ns][n_a], source bins only.
 template <bool DZ>
-__global__ void __launch_bounds__(GT_NT) k_gtab(Params P, double* dz_out)
+__global__ void __launch_bounds__(GT_NT) k_gtab(Params P, double* dz_out, int bin0)
 {
   const int pt = blockIdx.x;
-  const int bin = blockIdx.y;
+  const int bin = bin0 + blockIdx.y;
   const int lens = bin >= P.ns;
   const int b = lens ? bin - P.ns : bin;
   const cl2pt_nuisance& nu = P.nu[pt];
@@ -158,6 +161,128 @@ __global__ void __launch_bounds__(GT_NT) k_gtab(Params P, double* dz_out)
     runQ = carry[1];
     prevP = carry[2];
     prevQ = lastf[1];
+    __syncthreads();
+  }
+}
+
+// ---- source bins: every source table of a point shares one fine grid
+// (a_lo = 1/(1 + zmax of all source bins)), so z, chi, 1/a^2 and 1/chi are
+// formed once per point (k_gfine) instead of once per bin, the n(z) spline
+// reads per-interval coefficients (P.src_b, P.src_d) after a search on the
+// float copy of its nodes with an FP64 fix-up (the same cell as the FP64
+// search), and each thread integrates GS_PPT consecutive fine points, so
+// the FP64 block scans run once per GS_PPT points.  Arithmetic stays FP64.
+__global__ void __launch_bounds__(GT_NT) k_gfine(Params P, int Na, double amin, double da)
+{
+  const int pt = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Na) return;
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double a = amin + i * da;
+  const double c = chi_all_d(P.chi_z, X, P.chi_nz, a).chi;
+  double2* f = (double2*)(P.gfine + ((size_t)pt * Na + i) * 4);
+  f[0] = make_double2(1.0 / a - 1.0, c);
+  f[1] = make_double2(1.0 / (a * a), 1.0 / c);
+}
+
+// spline cell of the source n(z) nodes: the largest i <= n-2 with
+// zc[i] <= v (bsearch_d's answer), from the float copy plus a fix-up
+__device__ __forceinline__ int src_cell(const Params& P, double v)
+{
+  const float* xf = P.src_zcf;
+  const double* x = P.src_zc;
+  const int n = P.src_nz;
+  const float vf = (float)v;
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xf[mid] > vf) hi = mid; else lo = mid;
+  }
+  while (lo > 0 && x[lo] > v) lo--;
+  while (lo < n - 2 && x[lo + 1] <= v) lo++;
+  return lo;
+}
+
+constexpr int GS_PPT = 4;
+template <bool DZ>
+__global__ void __launch_bounds__(GT_NT) k_gsrc(Params P, double* dz_out, int Na, double da)
+{
+  const int pt = blockIdx.x, b = blockIdx.y;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const int x = 25 * (1 + abs(P.hdi));
+  double* tab = DZ ? dz_out + ((size_t)pt * P.ns + b) * P.n_a : P.gsrc + ((size_t)pt * P.ns + b) * P.n_a;
+  const double2* F = (const double2*)(P.gfine + (size_t)pt * Na * 4);
+  const double dz = nu.src_dz[b];
+  const int row = (b + 1) * P.src_nz;
+  const double* sy = P.src_y + row;
+  const double* sc = P.src_c + row;
+  const double* sb = P.src_b + row;
+  const double* sd = P.src_d + row;
+  const double z0 = P.src_zc[0], z1 = P.src_zc[P.src_nz - 1];
+  __shared__ double sh[32];
+  __shared__ double lastP[GT_NT], lastQ[GT_NT];
+  __shared__ double carry[4];
+  if (threadIdx.x == 0) tab[0] = 0.0;
+  double runP = 0.0, runQ = 0.0, prevP = 0.0, prevQ = 0.0;
+  for (int base = 0; base < Na; base += GT_NT * GS_PPT) {
+    const int i0 = base + GS_PPT * threadIdx.x;
+    double fP[GS_PPT], fQ[GS_PPT], cv[GS_PPT];
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      fP[k] = fQ[k] = cv[k] = 0.0;
+      if (i < Na) {
+        const double2 f0 = F[2 * i], f1 = F[2 * i + 1];  // (z, chi), (1/a^2, 1/chi)
+        const double zz = f0.x - dz;
+        double n = 0.0;
+        if (!(zz < z0 || zz > z1)) {
+          const int j = src_cell(P, zz);
+          const double t = zz - P.src_zc[j];
+          n = DZ ? -(sb[j] + t * (2.0 * sc[j] + 3.0 * t * sd[j]))
+                 : sy[j] + t * (sb[j] + t * (sc[j] + t * sd[j]));
+        }
+        fP[k] = n * f1.x;
+        fQ[k] = fP[k] * f1.y;
+        cv[k] = f0.y;
+      }
+    }
+    lastP[threadIdx.x] = fP[GS_PPT - 1];
+    lastQ[threadIdx.x] = fQ[GS_PPT - 1];
+    __syncthreads();
+    double pP = threadIdx.x ? lastP[threadIdx.x - 1] : prevP;
+    double pQ = threadIdx.x ? lastQ[threadIdx.x - 1] : prevQ;
+    // trapezoids 0.5 da (f[i-1] + f[i]) for i >= 1, summed along the thread
+    double sP[GS_PPT], sQ[GS_PPT], aP = 0.0, aQ = 0.0;
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      if (i >= 1 && i < Na) {
+        aP += 0.5 * da * (pP + fP[k]);
+        aQ += 0.5 * da * (pQ + fQ[k]);
+      }
+      sP[k] = aP;
+      sQ[k] = aQ;
+      pP = fP[k];
+      pQ = fQ[k];
+    }
+    const double eP = block_scan<GT_NT>(aP, sh) - aP + runP;
+    const double eQ = block_scan<GT_NT>(aQ, sh) - aQ + runQ;
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      if (i >= 1 && i < Na && (i % x) == 0) tab[i / x] = (eP + sP[k]) - cv[k] * (eQ + sQ[k]);
+    }
+    if (threadIdx.x == GT_NT - 1) {
+      carry[0] = eP + aP;
+      carry[1] = eQ + aQ;
+      carry[2] = fP[GS_PPT - 1];
+      carry[3] = fQ[GS_PPT - 1];
+    }
+    __syncthreads();
+    runP = carry[0];
+    runQ = carry[1];
+    prevP = carry[2];
+    prevQ = carry[3];
     __syncthreads();
   }
 }
@@ -386,12 +511,25 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
   }
 }
 
+// the source fine grid of g_tomo (k_gtab's a_lo, Na and step for source bins)
+static void src_fine_grid(const Params& P, int* Na, double* amin, double* da)
+{
+  *Na = 25 * (1 + abs(P.hdi)) * (P.n_a - 1) + 1;
+  *amin = 1.0 / (P.src_zmax_all + 1.0);
+  *da = (0.999999 - *amin) / ((double)*Na - 1.0);
+}
+
 void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk)
 {
-  dim3 g1(P.B, P.ns + P.nl);
+  int Na;
+  double amin, da;
+  src_fine_grid(P, &Na, &amin, &da);
   hk(CL2PT_K_GTAB, 1);
-  k_gtab<false><<<g1, GT_NT, 0, s>>>(P, nullptr);
+  k_gfine<<<dim3((Na + GT_NT - 1) / GT_NT, P.B), GT_NT, 0, s>>>(P, Na, amin, da);
+  k_gsrc<false><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, nullptr, Na, da);
+  if (P.nl > 0) k_gtab<false><<<dim3(P.B, P.nl), GT_NT, 0, s>>>(P, nullptr, P.ns);
   hk(CL2PT_K_GTAB, 0);
+  *launches += 2;
   dim3 g2(P.B, 1 + 2 * P.nl);
   hk(CL2PT_K_NODES, 1);
   k_nodes<<<g2, ND_NT, 0, s>>>(P);
@@ -401,7 +539,11 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 
 void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s)
 {
-  k_gtab<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out);
+  // reads the wave's fine grid written by launch_setup
+  int Na;
+  double amin, da;
+  src_fine_grid(P, &Na, &amin, &da);
+  k_gsrc<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out, Na, da);
 }
 
 }  // namespace cl2pt

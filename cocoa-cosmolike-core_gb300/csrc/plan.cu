@@ -499,6 +499,25 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dupload(p, &p->d_lens_zc, p->lens.zc.data(), p->lens.zc.size()));
   TRY(dupload(p, &p->d_lens_y, p->lens.y.data(), p->lens.y.size()));
   TRY(dupload(p, &p->d_lens_c, p->lens.c.data(), p->lens.c.size()));
+  {
+    // per-interval cubic coefficients of the source n(z) splines (b and d
+    // of spline_d) and a float copy of their nodes for the search
+    const std::vector<double>& x = p->src.zc;
+    const int n = (int)x.size(), rows = (int)(p->src.y.size() / n);
+    std::vector<double> sb(p->src.y.size(), 0.0), sdd(p->src.y.size(), 0.0);
+    for (int r = 1; r < rows; r++)
+      for (int i = 0; i + 1 < n; i++) {
+        const double* y = p->src.y.data() + (size_t)r * n;
+        const double* c = p->src.c.data() + (size_t)r * n;
+        const double h = x[i + 1] - x[i];
+        sb[(size_t)r * n + i] = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
+        sdd[(size_t)r * n + i] = (c[i + 1] - c[i]) / (3.0 * h);
+      }
+    std::vector<float> zf(x.begin(), x.end());
+    TRY(dupload(p, &p->d_src_b, sb.data(), sb.size()));
+    TRY(dupload(p, &p->d_src_d, sdd.data(), sdd.size()));
+    TRY(dupload(p, &p->d_src_zcf, zf.data(), zf.size()));
+  }
   TRY(dupload(p, &p->d_gl_ss_x, glx.data(), glx.size()));
   TRY(dupload(p, &p->d_gl_ss_w, glw.data(), glw.size()));
   TRY(dupload(p, &p->d_gl_gg_x, ggx.data(), ggx.size()));
@@ -588,6 +607,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.pkl_lk = p->d_pkl_lk; P.pkl_z = p->d_pkl_z;
   P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
   P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
+  P.src_b = p->d_src_b; P.src_d = p->d_src_d; P.src_zcf = p->d_src_zcf;
   P.lens_zc = p->d_lens_zc; P.lens_y = p->d_lens_y; P.lens_c = p->d_lens_c;
   P.src_zmin_all = p->src.zmin_all; P.src_zmax_all = p->src.zmax_all;
   P.lens_zmax_all = p->lens.zmax_all;
@@ -623,6 +643,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
+  TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
   if (precision != CL2PT_PREC_FP64) {
     TRY(dalloc(p, &P.lnP2, (size_t)W * 2 * P.pk_nk * P.pk_nz));
     TRY(dalloc(p, &P.lnPL2, (size_t)W * 2 * P.pkl_nk * P.pkl_nz));
