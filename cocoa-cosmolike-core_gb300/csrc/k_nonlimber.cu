@@ -64,25 +64,52 @@ __constant__ double c_lanczos[9] = {
     -0.13857109526572011689554707, 9.984369578019570859563e-6,
     1.50563273514931155834e-7};
 
-// ln Gamma(a), Lanczos g = 7 with reflection for Re a < 1/2
-// (cosmo2D.c:4273-4294)
+// ln Gamma(a) for Re a >= 1/2, |a| >= 10: Stirling's series
+// (Abramowitz & Stegun 6.1.40-41) to the B_16 term, remainder below 1e-17
+// relative there; ~1/3 of the FP64 work of the Lanczos sum (one complex
+// reciprocal instead of eight complex divisions, one complex log).
+// Exponentiated only, so its branch of the imaginary part is immaterial.
+__device__ cd lngamma_stirling(cd a)
+{
+  const cd r = cdivc(cmk(1.0, 0.0), a);
+  const cd r2 = cmul(r, r);
+  // B_2n / (2n (2n - 1)), n = 1..8
+  const double c1 = 1.0 / 12, c2 = -1.0 / 360, c3 = 1.0 / 1260, c4 = -1.0 / 1680, c5 = 1.0 / 1188,
+               c6 = -691.0 / 360360, c7 = 1.0 / 156, c8 = -3617.0 / 122400;
+  cd sr = cmk(c8, 0.0);
+  sr = cadd(cmk(c7, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c6, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c5, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c4, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c3, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c2, 0.0), cmul(sr, r2));
+  sr = cadd(cmk(c1, 0.0), cmul(sr, r2));
+  sr = cmul(sr, r);
+  return cadd(csub(cmul(cmk(a.x - 0.5, a.y), clog_(a)), a), cmk(0.5 * log(2 * M_PI) + sr.x, sr.y));
+}
+
+// ln Gamma(1 + m) for Re m >= -1/2 (Lanczos g = 7, the reference's sum;
+// Stirling's series for |1 + m| >= 10)
+__device__ cd lngamma_1p(cd m)
+{
+  if (hypot(m.x + 1.0, m.y) >= 10.0) return lngamma_stirling(cmk(m.x + 1.0, m.y));
+  const double ln2pio2 = 0.5 * log(2 * M_PI);
+  cd tmp = cmk(c_lanczos[0], 0.0);
+  for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(m.x + w, m.y)));
+  const cd t = cmk(m.x + 7.5, m.y);
+  return cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(m.x + 0.5, m.y), clog_(t))), t), clog_(tmp));
+}
+
+// ln Gamma(a) with reflection for Re a < 1/2 (cosmo2D.c:4273-4294)
 __device__ cd lngamma_refl(cd a)
 {
-  const double ln2pio2 = 0.5 * log(2 * M_PI);
   if (a.x < 0.5) {
-    const cd ma = cmk(-a.x, -a.y);
-    cd tmp = cmk(c_lanczos[0], 0.0);
-    for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(ma.x + w, ma.y)));
-    const cd t = cmk(ma.x + 7.5, ma.y);
-    const cd lt = clog_(t);
-    const cd inner = cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(ma.x + 0.5, ma.y), lt)), t), clog_(tmp));
+    // ln pi - ln sin(pi a) - ln Gamma(1 - a)
+    const cd inner = lngamma_1p(cmk(-a.x, -a.y));
     const cd s = clog_(csin_(cscale(a, M_PI)));
     return csub(csub(cmk(log(M_PI), 0.0), s), inner);
   }
-  cd tmp = cmk(c_lanczos[0], 0.0);
-  for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(a.x - 1 + w, a.y)));
-  const cd t = cmk(a.x - 1 + 7.5, a.y);
-  return cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(a.x - 1 + 0.5, a.y), clog_(t))), t), clog_(tmp));
+  return lngamma_1p(cmk(a.x - 1.0, a.y));
 }
 
 // g_l(z) for the three derivative orders (cosmo2D.c:4259-4430)
@@ -420,6 +447,12 @@ __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
   const int pt = blockIdx.x, j = blockIdx.y, d = blockIdx.z;
   const int k = Q.direct_every ? (d / 2) * 16 + (d & 1) : d;
   if (k >= P.lmax_nolimber) return;
+  if (j == 2) {
+    // the magnification kernel is read only by bins with magnification bias
+    bool any = false;
+    for (int q = 0; q < P.nl; q++) any |= P.nu[pt].gb[4][q] != 0.0;
+    if (!any) return;
+  }
   const NLGeom geo = nl_geom(P, pt);
   const int N = Q.N[j];
   const int nq = N / 2 + 1;
@@ -474,6 +507,38 @@ __device__ __forceinline__ ct<T> phasor(double a)
   return tmk<T>(cp, sp);
 }
 
+// Dispatch order of the multipole-loop CTAs, longest first: a CTA runs to
+// its bin's hand-over multipole, which varies ~4x between lens bins, and
+// launching the long ones first shortens the tail of the launch.  The key
+// is conv_l: the previous evaluation's hand-over for the forward loop (a
+// predictor; walker slots move little between calls), the current one for
+// the adjoint.  One CTA counting-sorts the B * nl items into Q.perm by key
+// in 16-multipole buckets, descending; the order only schedules, every
+// CTA computes the same result wherever it lands.
+constexpr int NORD_NB = 64;
+__global__ void __launch_bounds__(1024) k_nl_order(Params P, NLParams Q)
+{
+  __shared__ int cnt[NORD_NB], off[NORD_NB];
+  const int n = P.B * P.nl;
+  for (int b = threadIdx.x; b < NORD_NB; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  auto bucket = [&](int i) {
+    const int v = P.conv_l[i] / 16;
+    return NORD_NB - 1 - (v < 0 ? 0 : (v > NORD_NB - 1 ? NORD_NB - 1 : v));
+  };
+  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&cnt[bucket(i)], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < NORD_NB; b++) {
+      off[b] = acc;
+      acc += cnt[b];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) Q.perm[atomicAdd(&off[bucket(i)], 1)] = i;
+}
+
 // ADJ: the adjoint of the FFTLog part (see section 4 below) on the same
 // multipole walk: the loop stops at the forward's hand-over multipole, keeps
 // the b1-free galaxy term G0 of both multipoles, and accumulates the P_lin
@@ -483,7 +548,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
                                                       double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int pt = blockIdx.x, q = blockIdx.y;
+  // (point, bin) of this CTA from the longest-first dispatch order
+  const int item = Q.perm[blockIdx.y * gridDim.x + blockIdx.x];
+  const int pt = item / P.nl, q = item - (item / P.nl) * P.nl;
   const int tid = threadIdx.x;
   const int nchi = P.nl_nchi;
   const int LNL = P.lmax_nolimber;
@@ -855,6 +922,7 @@ static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cb
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl, 1), NL_NT, sm1, s>>>(P, Q, 1);
   const size_t sm = nl_loop_smem<T>(P, Q, true);
+  k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_nl_loop<T, true><<<dim3(P.B, P.nl), NL_NT, sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
 }
@@ -864,7 +932,7 @@ void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar
 {
   if (P.prec == CL2PT_PREC_FP64) launch_nl_vjp_t<double>(P, Q, cbar, lnpl_bar, nu_bar, s);
   else launch_nl_vjp_t<float>(P, Q, cbar, lnpl_bar, nu_bar, s);
-  (*launches) += 2;
+  (*launches) += 3;
 }
 
 template <typename T>
@@ -875,6 +943,7 @@ static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
   k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
   const size_t sm3 = nl_loop_smem<T>(P, Q, false);
+  k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   k_nl_loop<T, false><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
 }
@@ -886,7 +955,7 @@ void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* l
   if (P.prec == CL2PT_PREC_FP64) launch_nl_t<double>(P, Q, s);
   else launch_nl_t<float>(P, Q, s);
   hk(CL2PT_K_NONLIMBER, 0);
-  (*launches) += 3;
+  (*launches) += 4;
 }
 
 }  // namespace cl2pt

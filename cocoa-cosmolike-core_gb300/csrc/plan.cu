@@ -638,6 +638,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dalloc(p, &P.ggl, (size_t)W * nl * LNL * 2));
   TRY(dalloc(p, &P.cnl, (size_t)W * nl * LNL));
   TRY(dalloc(p, &P.conv_l, (size_t)W * nl));
+  CUDA_OK(cudaMemset(P.conv_l, 0, sizeof(int) * (size_t)W * nl));
   TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
   TRY(dalloc(p, &p->d_err, 4));
   P.err = p->d_err;
@@ -772,6 +773,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       Q.direct_every = (precision == CL2PT_PREC_FP64) ? 1 : 0;
       Q.ndirect = Q.direct_every ? 2 * ((LNL + 15) / 16) : 2;
       TRY(dalloc(p, &Q.gdir, (size_t)W * 3 * Q.ndirect * Q.hstride * 2));
+      TRY(dalloc(p, &Q.perm, (size_t)W * nl));
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
