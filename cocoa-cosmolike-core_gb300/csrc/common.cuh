@@ -68,6 +68,14 @@ struct Params {
   const double* G;          // [B][G_nz]
   const double* lnP;        // [B][pk_nk*pk_nz]
   const double* lnPL;       // [B][pkl_nk*pkl_nz]
+  // mixed plan: FP32 per-multipole factors of the multipole lists the
+  // Limber kernels are launched on, 8 floats per multipole (log10(l+1/2)
+  // head and tail, then ss: l(l-1)(l+1)(l+2)/(l+1/2)^4; g: sqrt((l-1)l(l+1)
+  // (l+2))/(l+1/2)^2, l(l+1)/(l+1/2)^2, RSD c0, RSD c1, (l+3/2)/(l+1/2));
+  // facf_gi: the g factors at l = 0..LNL-1
+  const float* facf_ss;
+  const float* facf_g;
+  const float* facf_gi;
   // mixed plan: FP32 (head, tail) of every entry of the wave's tables
   float* lnP2;              // [B][pk_nk*pk_nz][2]
   float* lnPL2;             // [B][pkl_nk*pkl_nz][2]; lnP2 when lnPL is lnP

@@ -175,6 +175,34 @@ __device__ __forceinline__ float pk_eval_f(const AxisF& ax, const float2* __rest
   return expf(a00.x) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
 }
 
+// Bracketing cell of v on a sorted axis (bsearch_t's answer) walked from
+// the cell h of the previous query (h < 0: full search).  The gg loop sweeps
+// a thread's nodes in order, so consecutive queries sit a few cells apart.
+__device__ __forceinline__ int walk_cell(const float* __restrict__ x, int n, float v, int h)
+{
+  if (h < 0) return bsearch_t(x, n, v);
+  while (h < n - 2 && x[h + 1] <= v) h++;
+  while (h > 0 && x[h] > v) h--;
+  return h;
+}
+
+// pk_eval_f with the k cell walked from the hint h (updated)
+__device__ __forceinline__ float pk_eval_fh(const AxisF& ax, const float2* __restrict__ tab, int nz, float uh,
+                                            float ul, int j, float dy, int& h)
+{
+  const int i = walk_cell(ax.lk, ax.nk, uh, h);
+  h = i;
+  const float dx = (__fsub_rn(uh, ax.lk[i]) + (ul - ax.lkl[i])) * ax.inv[i];
+  const float2* r0 = tab + (size_t)i * nz + j;
+  const float2* r1 = r0 + nz;
+  const float2 a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
+  const float d01 = (a01.x - a00.x) + (a01.y - a00.y);
+  const float d10 = (a10.x - a00.x) + (a10.y - a00.y);
+  const float d11 = ((a11.x - a10.x) + (a11.y - a10.y)) - d01;
+  const float del = a00.y + dy * d01 + dx * d10 + dx * dy * d11;
+  return expf(a00.x) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
 struct PdeltaTable {
   const double* tab;
   const float2* tab2;  // split copy (mixed plan)
@@ -226,9 +254,19 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
   const double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
   const bool valid = L < P.nnode_ss;
-  const double l = valid ? ell[L] : 1.0;
-  const double lp = l + 0.5;
-  const T pref = (T)(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
+  // per-multipole factors: FP32 plan constants in the mixed plan
+  double lp = 1.5;
+  T pref;
+  float2 llf = make_float2(0.0f, 0.0f);
+  if constexpr (F32) {
+    const float4 fa = valid ? *(const float4*)(P.facf_ss + 8 * (size_t)L) : make_float4(0.f, 0.f, 0.f, 0.f);
+    pref = fa.z;
+    llf = make_float2(fa.x, fa.y);
+  } else {
+    const double l = valid ? ell[L] : 1.0;
+    lp = l + 0.5;
+    pref = (T)(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
+  }
   double* out = P.tab_ss + (size_t)pt * P.pss * P.nnode_ss;
   for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
     const int np = min(PCH, P.n_ss - p0);
@@ -250,15 +288,14 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     }
     __syncthreads();
     if (!valid) continue;
-    const double llp = log10(lp);
     if constexpr (F32) {
-      const float2 ll = split_f(llp);
       for (int p = 0; p < np; p++) {
         float uh, ul;
-        split_sub(ll.x, ll.y, nlc2[p].x, nlc2[p].y, uh, ul);
+        split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
         Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
       }
     } else {
+      const double llp = log10(lp);
       for (int p = 0; p < np; p++)
         Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     }
@@ -318,11 +355,21 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   const double* wl = P.wgs_l + b0 * P.n_ss;
   const double* wm = P.wgs_m + b0 * P.n_ss;
   const bool valid = L < P.nnode_g;
-  const double l = valid ? ell[L] : 1.0;
-  const double lp = l + 0.5;
-  const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
-  const T pref2 = (T)((tmp > 0) ? sqrt(tmp) / (lp * lp) : 0.0);
-  const T pref = (T)(l * (l + 1.) / (lp * lp));
+  double lp = 1.5;
+  T pref2, pref;
+  float2 llf = make_float2(0.0f, 0.0f);
+  if constexpr (F32) {
+    const float4 fa = valid ? *(const float4*)(P.facf_g + 8 * (size_t)L) : make_float4(0.f, 0.f, 0.f, 0.f);
+    pref2 = fa.z;
+    pref = fa.w;
+    llf = make_float2(fa.x, fa.y);
+  } else {
+    const double l = valid ? ell[L] : 1.0;
+    lp = l + 0.5;
+    const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
+    pref2 = (T)((tmp > 0) ? sqrt(tmp) / (lp * lp) : 0.0);
+    pref = (T)(l * (l + 1.) / (lp * lp));
+  }
   double* out = P.tab_gs + (size_t)pt * P.pgs * P.nnode_g;
   for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
     const int np = min(PCH, P.n_ss - p0);
@@ -347,15 +394,14 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     }
     __syncthreads();
     if (!valid) continue;
-    const double llp = log10(lp);
     if constexpr (F32) {
-      const float2 ll = split_f(llp);
       for (int p = 0; p < np; p++) {
         float uh, ul;
-        split_sub(ll.x, ll.y, nlc2[p].x, nlc2[p].y, uh, ul);
+        split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
         Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
       }
     } else {
+      const double llp = log10(lp);
       for (int p = 0; p < np; p++)
         Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     }
@@ -429,6 +475,11 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   T* szc = gz + ng;      // n(z) spline nodes, values, coefficients of bin q
   T* sy = szc + nzs;
   T* sc = sy + nzs;
+  // mixed plan: reciprocal chi-cell widths and the n(z) spline's b, d per
+  // interval
+  T* icx = sc + nzs;
+  T* sbq = icx + nc;
+  T* sdq = sbq + nzs;
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
   constexpr bool F32 = sizeof(T) == sizeof(float);
@@ -471,7 +522,16 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     szc[i] = (T)P.lens_zc[i];
     sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
     sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
+    if constexpr (F32) {
+      const double* yq = P.lens_y + (q + 1) * nzs;
+      const double* cq = P.lens_c + (q + 1) * nzs;
+      const double h = (i + 1 < nzs) ? P.lens_zc[i + 1] - P.lens_zc[i] : 1.0;
+      sbq[i] = (i + 1 < nzs) ? (float)((yq[i + 1] - yq[i]) / h - h * (cq[i + 1] + 2.0 * cq[i]) / 3.0) : 0.0f;
+      sdq[i] = (i + 1 < nzs) ? (float)((cq[i + 1] - cq[i]) / (3.0 * h)) : 0.0f;
+    }
   }
+  if constexpr (F32)
+    for (int i = tid; i < nc; i += LTG) icx[i] = (i + 1 < nc) ? (float)(1.0 / (Xg[i + 1] - Xg[i])) : 0.0f;
   const cl2pt_nuisance& nu = P.nu[pt];
   const T ldz = (T)nu.lens_dz[q], lst = (T)nu.lens_stretch[q], lzm = (T)P.zmean_lens[q];
   const int off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
@@ -480,15 +540,31 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   const size_t b0 = (size_t)pt * P.nl + q;
   const int nL = (mode == 0) ? P.nnode_g : P.lmax_nolimber;
   const bool valid = L < nL;
-  const double l = valid ? ((mode == 0) ? ell[L] : (double)L) : 1.0;
-  const double lp = l + 0.5;
-  const T pref = (T)(l * (l + 1.) / (lp * lp));
-  const T c0 = (T)((1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.)));
-  const T c1 = (T)(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
+  double lp = 1.5;
+  T pref, c0, c1, ratio;
+  float2 llf = make_float2(0.0f, 0.0f);
+  if constexpr (F32) {
+    // FP32 plan constants (the C_l nodes, or l = L for the integer-l pass)
+    const float* f = (mode == 0 ? P.facf_g : P.facf_gi) + 8 * (size_t)(valid ? L : 0);
+    const float4 fa = *(const float4*)f, fb = *(const float4*)(f + 4);
+    llf = make_float2(fa.x, fa.y);
+    pref = fa.w;
+    c0 = fb.x;
+    c1 = fb.y;
+    ratio = fb.z;
+  } else {
+    const double l = valid ? ((mode == 0) ? ell[L] : (double)L) : 1.0;
+    lp = l + 0.5;
+    pref = (T)(l * (l + 1.) / (lp * lp));
+    c0 = (T)((1 + 8. * lp) / ((2. * lp + 1.) * (2. * lp + 1.)));
+    c1 = (T)(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
+    ratio = (T)((lp + 1.0) / lp);
+  }
   const double chi_amin = P.chi_amin[pt];
   const T cH0 = (T)CL2PT_COVERH0;
-  const T ratio = (T)((lp + 1.0) / lp);
   double sum_nl = 0.0, sum_lin = 0.0;
+  int hc = -1, hg = -1, hn = -1, hk = -1, hkl = -1;  // mixed plan: cells of the previous node
+  const float ilst = (float)(1.0 / nu.lens_stretch[q]);
   for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
     const int np = min(PCH, P.n_gg - p0);
     __syncthreads();
@@ -544,8 +620,8 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     }
     __syncthreads();
     if (!valid) continue;
-    const double llp = log10(lp);
-    const float2 ll = split_f(llp);
+    const double llp = F32 ? 0.0 : log10(lp);
+    const float2 ll = llf;
     float snl = 0.0f, sln = 0.0f;  // mixed plan: this chunk's FP32 sums
     for (int p = 0; p < np; p++) {
       T fkc, Lw, Mw, r0w;
@@ -561,6 +637,41 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
         Lw = (T)nd[3 * PCH + p];
         Mw = (T)nd[4 * PCH + p];
         r0w = (T)nd[5 * PCH + p];
+      }
+      if constexpr (F32) {
+        // the same lookups with the cells walked from the previous node's,
+        // reciprocal widths and the spline's per-interval b, d
+        const float c = fkc * ratio;
+        hc = walk_cell(cx, nc, c, hc);
+        const int j = hc;
+        const float dyc = (c - cx[j]) * icx[j];
+        const float z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
+        const int jc = bsearch_from(cz, nc, z1, j);
+        const float dy2 = (jc == j) ? dyc : (z1 - cz[jc]) / (cz[jc + 1] - cz[jc]);
+        const float H1 = __fdividef(cH0, cdn[jc] + dy2 * (cup[jc] - cdn[jc]));
+        int jg = jc;
+        float dyg = dy2;
+        if (!same_axis) {
+          hg = walk_cell(gz, ng, z1, hg);
+          jg = hg;
+          dyg = (z1 - gz[jg]) / (gz[jg + 1] - gz[jg]);
+        }
+        const float Gz = gv[jg] + dyg * (gv[jg + 1] - gv[jg]);
+        const float f1 = 1.0f - __fdividef(gs[jg] * (1.0f + z1), Gz);
+        const float zs = (z1 - ldz - lzm) * ilst + lzm;
+        float n1 = 0.0f;
+        if (!(zs <= szc[0] || zs >= szc[nzs - 1])) {
+          hn = walk_cell(szc, nzs, zs, hn);
+          const float t = zs - szc[hn];
+          n1 = (sy[hn] + t * (sbq[hn] + t * (sc[hn] + t * sdq[hn]))) * ilst;
+        }
+        const float s = Lw + Mw * pref + (c0 * r0w - c1 * n1 * H1 * f1);
+        const float s2w = s * s * nf[1 * PCH + p];
+        float uh, ul;
+        split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
+        snl += s2w * pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p], hk);
+        if (mode == 1) sln += s2w * pk_eval_fh(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p], hkl);
+        continue;
       }
       // a_chi at chi1 (cosmo3D.c:109-133)
       const T c = fkc * ratio;
@@ -589,21 +700,13 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
       }
       const T wrsd = c0 * r0w - c1 * n1 * H1 * f1;
       const T s = Lw + Mw * pref + wrsd;
-      if constexpr (F32) {
-        const float s2w = s * s * nf[1 * PCH + p];
-        float uh, ul;
-        split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
-        snl += s2w * pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p]);
-        if (mode == 1) sln += s2w * pk_eval_f(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p]);
-      } else {
-        const double s2w = (double)(s * s) * nd[1 * PCH + p];
-        const double log10k = llp - nd[7 * PCH + p];
-        const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
-        sum_nl += s2w * (double)Pnl;
-        if (mode == 1) {
-          const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
-          sum_lin += s2w * (double)Pl;
-        }
+      const double s2w = (double)(s * s) * nd[1 * PCH + p];
+      const double log10k = llp - nd[7 * PCH + p];
+      const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
+      sum_nl += s2w * (double)Pnl;
+      if (mode == 1) {
+        const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
+        sum_lin += s2w * (double)Pl;
       }
     }
     if constexpr (F32) {
@@ -648,7 +751,7 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
     const size_t sm = sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
-                      sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;
+                      sizeof(T) * (P.pk_nk + P.pkl_nk + 5 * P.chi_nz + 3 * P.G_nz + 5 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);

@@ -608,6 +608,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
   P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
   P.src_b = p->d_src_b; P.src_d = p->d_src_d; P.src_zcf = p->d_src_zcf;
+  P.facf_ss = p->d_lfacf_ss;
+  P.facf_g = p->d_lfacf_g;
+  P.facf_gi = p->d_lfacf_g + 8 * (size_t)p->nnode_g;
   P.lens_zc = p->d_lens_zc; P.lens_y = p->d_lens_y; P.lens_c = p->d_lens_c;
   P.src_zmin_all = p->src.zmin_all; P.src_zmax_all = p->src.zmax_all;
   P.lens_zmax_all = p->lens.zmax_all;
@@ -643,6 +646,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dalloc(p, &p->d_err, 4));
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
+  TRY(dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
   if (precision != CL2PT_PREC_FP64) {
@@ -978,7 +982,6 @@ static int vjp_prepare(cl2pt_plan* p)
     if (!a && p->d_in_lnPL)
       a = dalloc(p, &p->d_vjp_lnpl, (size_t)p->max_batch * p->P.pkl_nk * p->P.pkl_nz);
     if (!a) a = dalloc(p, &p->d_lfac_f, 8 * (size_t)std::max(p->nnode_ss, p->nnode_g));
-    if (!a) a = dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g));
     if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
     if (a) {
       p->d_vjp_ws = nullptr;
@@ -1587,8 +1590,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     return CL2PT_OK;
   };
   bool ell_sorted = true;
-  if (vr && fourier) {
-    // multipole factors of the caller's l for the adjoint sweeps
+  if (fourier && !fr->ell_on_device) {
+    // multipole factors of the caller's l: FP32 copies for the mixed-plan
+    // Limber kernels, FP64 ones for the adjoint sweeps (graph capture
+    // reuses the tables of the eager evaluation before it)
     std::vector<double> fs, fg;
     for (int i = 0; i < fr->nell; i++) {
       if (i > 0 && !(fr->ell[i] > fr->ell[i - 1])) ell_sorted = false;
@@ -1602,9 +1607,11 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       fg.push_back(4. / (2 * lp + 3.) * sqrt((2 * lp + 1.) / (2 * lp + 3.)));
       fg.push_back((lp + 1.0) / lp);
     }
-    CUDA_OK(cudaMemcpyAsync(p->d_lfac_f, fs.data(), sizeof(double) * fs.size(), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_lfac_f + 2 * (size_t)fr->nell, fg.data(), sizeof(double) * fg.size(),
-                            cudaMemcpyHostToDevice, s));
+    if (vr) {
+      CUDA_OK(cudaMemcpyAsync(p->d_lfac_f, fs.data(), sizeof(double) * fs.size(), cudaMemcpyHostToDevice, s));
+      CUDA_OK(cudaMemcpyAsync(p->d_lfac_f + 2 * (size_t)fr->nell, fg.data(), sizeof(double) * fg.size(),
+                              cudaMemcpyHostToDevice, s));
+    }
     const std::vector<float> fsf = lfac_f32(fs, 2), fgf = lfac_f32(fg, 6);
     CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f, fsf.data(), sizeof(float) * fsf.size(), cudaMemcpyHostToDevice, s));
     CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f + 8 * (size_t)fr->nell, fgf.data(), sizeof(float) * fgf.size(),
@@ -1648,6 +1655,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       // FFTLog hand-over below reads the clustering table on the log nodes
       Params Pf = P;
       Pf.nnode_ss = Pf.nnode_g = fr->nell;
+      Pf.facf_ss = p->d_lfacf_f;
+      Pf.facf_g = p->d_lfacf_f + 8 * (size_t)fr->nell;
       Pf.tab_gg = p->d_tab_gg_f;
       Pf.adopt_limber_gg = 1;  // no integer-l spectra in this pass
       cl2pt::launch_limber(Pf, p->d_ell_f, p->d_ell_f, s, &launches, hk);
