@@ -539,6 +539,36 @@ __global__ void __launch_bounds__(1024) k_nl_order(Params P, NLParams Q)
   for (int i = threadIdx.x; i < n; i += blockDim.x) Q.perm[atomicAdd(&off[bucket(i)], 1)] = i;
 }
 
+// FP32 head/tail of an angle reduced to [-pi, pi] in FP64
+__device__ __forceinline__ float2 red_angle(double a)
+{
+  a -= 2.0 * M_PI * rint(a * (0.5 / M_PI));
+  const float h = (float)a;
+  return make_float2(h, (float)(a - (double)h));
+}
+
+// exp(-i m theta) for theta = th.x + th.y in [-pi, pi] and 0 <= m < 2^15,
+// without FP64: m theta as an exact two-float product, reduced by 2 pi in
+// three parts (Cody-Waite; m th.x / 2 pi < 2^14, so n C1 and p - n C1 are
+// exact), then sincosf of the reduced angle (~2e-7 rad from the exact one)
+__device__ __forceinline__ ct<float> phase_f(int m, float2 th)
+{
+  constexpr float C1 = 6.28125f;
+  constexpr float C2 = (float)(6.283185307179586476925 - 6.28125);
+  constexpr float C3 = (float)(6.283185307179586476925 - 6.28125 - (double)C2);
+  const float fm = (float)m;
+  const float p = fm * th.x;
+  const float e = fmaf(fm, th.x, -p);
+  const float n = rintf(p * 0.159154943091895335769f);
+  float r = fmaf(-n, C1, p);
+  r = fmaf(-n, C2, r);
+  r = fmaf(-n, C3, r);
+  r += e + fm * th.y;
+  float sn, cs;
+  sincosf(r, &sn, &cs);
+  return tmk<float>(cs, -sn);
+}
+
 // ADJ: the adjoint of the FFTLog part (see section 4 below) on the same
 // multipole walk: the loop stops at the forward's hand-over multipole, keeps
 // the b1-free galaxy term G0 of both multipoles, and accumulates the P_lin
@@ -632,13 +662,24 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
   const double lnx0last = log(geo.x0 / geo.xlast);
   double deta_j[3];
-  for (int j = 0; j < 3; j++) deta_j[j] = 2.0 * M_PI / (geo.dlnx * Q.N[j]);
+  float dh_j[3], dl_j[3];  // deta as an FP32 head/tail (the recurrence's eta)
+  for (int j = 0; j < 3; j++) {
+    deta_j[j] = 2.0 * M_PI / (geo.dlnx * Q.N[j]);
+    dh_j[j] = (float)deta_j[j];
+    dl_j[j] = (float)(deta_j[j] - (double)dh_j[j]);
+  }
+  // mixed plan: phase increments and step phasors of the current pair, and
+  // the convergence flag, shared by thread 0
+  __shared__ float2 sph[4];
+  __shared__ int sdone;
+  const T bmagt = (T)bmag;
   int LM = LNL, done = 0;
   const int BLOCK = 16;
   const double dlnx = geo.dlnx;
   const T lc3 = (T)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
   // adjoint: the forward's hand-over multipole bounds the walk
   const int LEND = ADJ ? P.conv_l[cta] : LNL;
+  const T wsum = (T)(geo.dlnchi * 2. / M_PI);  // chi-sum weight of C_l
   const T b1t = ADJ ? (T)nu.gb[0][q] : (T)1;
   double b1bar = 0.0;
   const double* cb = ADJ ? cbar + cta * LNL : nullptr;
@@ -655,10 +696,24 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // ln(base y0) = ln(x0 / xlast) - 2 pad dlnx + ln(k+1): per-CTA and
         // per-multipole parts, no transcendental per thread
         const double lnbj = lnx0last - 2 * Q.pad[j] * dlnx;
-        const double lnb0 = lnbj + Q.lnk1[k];
-        const double lnb1 = lnbj + Q.lnk1[two ? k2 : k];
         const double deta = deta_j[j];
-        const float dhf = (float)deta, dlf = (float)(deta - (double)dhf);
+        double lnb0 = 0.0, lnb1 = 0.0;
+        if constexpr (F32) {
+          // one thread reduces the two phase increments theta = deta lnbase
+          // and forms the NL_NT-entry step phasors (FP64), shared below
+          if (tid == 0) {
+            const double t0 = deta * (lnbj + Q.lnk1[k]), t1 = deta * (lnbj + Q.lnk1[two ? k2 : k]);
+            sph[0] = red_angle(t0);
+            sph[1] = red_angle(t1);
+            const ct<T> a0 = phasor<T>(-(double)NL_NT * t0), a1 = phasor<T>(-(double)NL_NT * t1);
+            sph[2] = make_float2(a0.x, a0.y);
+            sph[3] = make_float2(a1.x, a1.y);
+          }
+        } else {
+          lnb0 = lnbj + Q.lnk1[k];
+          lnb1 = lnbj + Q.lnk1[two ? k2 : k];
+        }
+        const float dhf = dh_j[j], dlf = dl_j[j];
         __syncthreads();
         ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
         const bool dir0 = exact_blocks ? (k < ks + 2) : (k < 2);
@@ -670,8 +725,18 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // phases exp(-i eta_i lnbase): the first entry of this thread from an
         // FP64-reduced angle, then the FP32 (FP64 plan: FP64) step to the
         // thread's next entry, i += NL_NT
-        ct<T> e0 = phasor<T>(-(deta * tid) * lnb0), e1 = phasor<T>(-(deta * tid) * lnb1);
-        const ct<T> s0 = phasor<T>(-(deta * NL_NT) * lnb0), s1 = phasor<T>(-(deta * NL_NT) * lnb1);
+        ct<T> e0, e1, s0, s1;
+        if constexpr (F32) {
+          e0 = phase_f(tid, sph[0]);
+          e1 = phase_f(tid, sph[1]);
+          s0 = tmk<T>(sph[2].x, sph[2].y);
+          s1 = tmk<T>(sph[3].x, sph[3].y);
+        } else {
+          e0 = phasor<T>(-(deta * tid) * lnb0);
+          e1 = phasor<T>(-(deta * tid) * lnb1);
+          s0 = phasor<T>(-(deta * NL_NT) * lnb0);
+          s1 = phasor<T>(-(deta * NL_NT) * lnb1);
+        }
         for (int i = tid; i < nq; i += NL_NT) {
           ct<T> c0 = e0, c1 = e1;
           if constexpr (sizeof(T) == sizeof(double)) {
@@ -701,19 +766,27 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         }
         __syncthreads();
         ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
-        const T sc0 = (T)Q.sck[j * LNL + k];
-        const T sc1 = (T)Q.sck[j * LNL + (two ? k2 : k)];
+        T sc0, sc1;
+        if constexpr (F32) {
+          sc0 = Q.sckf[j * LNL + k];
+          sc1 = Q.sckf[j * LNL + (two ? k2 : k)];
+        } else {
+          sc0 = (T)Q.sck[j * LNL + k];
+          sc1 = (T)Q.sck[j * LNL + (two ? k2 : k)];
+        }
         // bmag l(l+1)/(l+1)^2 = bmag l/(l+1)
-        const T mag0 = (T)bmag * (T)k / (T)(k + 1);
-        const T mag1 = (T)bmag * (T)k2 / (T)(k2 + 1);
-        const double num1 = Q.nu[j] - 1.0;
+        const T mag0 = bmagt * (T)k / (T)(k + 1);
+        const T mag1 = bmagt * (T)k2 / (T)(k2 + 1);
+        const float num1f = Q.nu1f[j];
+        const double num1 = F32 ? 0.0 : Q.nu[j] - 1.0;
         for (int i = tid; i < nchi; i += NL_NT) {
           // x^nu (nu = 1 or 1.01) and, for magnification, x^2 more
           const T x = xs[i];
           T xp = x;
-          if (num1 != 0.0) {
-            if constexpr (sizeof(T) == sizeof(float)) xp *= __expf((float)num1 * __logf(x));
-            else xp *= texp<T>((T)(num1 * (lrc - lxk[i]) * 2.302585092994045684));
+          if constexpr (F32) {
+            if (num1f != 0.0f) xp *= __expf(num1f * __logf(x));
+          } else if (num1 != 0.0) {
+            xp *= texp<T>((T)(num1 * (lrc - lxk[i]) * 2.302585092994045684));
           }
           if (j == 2) xp *= x * x;
           const ct<T> z = r[Q.pad[j] + i];
@@ -738,14 +811,13 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // adjoint of C_l = (2/pi) dlnchi sum_i F_i^2 k_i^3 P_i for both
         // multipoles: P_lin slice adjoint (FP32 shared atomics in the mixed
         // plan) and d/db1 through F = b1 G0 + ...
-        const double w0 = cb[k] * geo.dlnchi * 2. / M_PI;
-        const double w1 = two ? cb[k2] * geo.dlnchi * 2. / M_PI : 0.0;
+        const T wt0 = (T)cb[k] * wsum, wt1 = two ? (T)cb[k2] * wsum : (T)0;
         double bp = 0.0;
-        if (w0 != 0.0 || w1 != 0.0) {
-          const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
-          const float lk0f = (float)lk0, lk1f = (float)lk1;
-          const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
-          const T wt0 = (T)w0, wt1 = (T)w1;
+        if (wt0 != (T)0 || wt1 != (T)0) {
+          const double lk0 = F32 ? 0.0 : Q.l10k1[k], lk1 = F32 ? 0.0 : Q.l10k1[two ? k2 : k];
+          const float lk0f = F32 ? Q.l10k1f[k] : 0.0f, lk1f = F32 ? Q.l10k1f[two ? k2 : k] : 0.0f;
+          const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
+          const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;
           T tb = 0;
           for (int i = tid; i < nchi; i += NL_NT) {
             const T rx = rct / xs[i];
@@ -781,9 +853,14 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
               }
             }
           }
+          if constexpr (F32) {
+            for (int o = 16; o > 0; o >>= 1) tb += __shfl_down_sync(0xffffffffu, tb, o);
+          }
           bp = (double)tb;
         }
-        for (int o = 16; o > 0; o >>= 1) bp += __shfl_down_sync(0xffffffffu, bp, o);
+        if constexpr (!F32) {
+          for (int o = 16; o > 0; o >>= 1) bp += __shfl_down_sync(0xffffffffu, bp, o);
+        }
         __syncthreads();
         if ((tid & 31) == 0) red[0][tid >> 5] = bp;
         __syncthreads();
@@ -792,9 +869,10 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
       } else {
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
         double part0 = 0.0, part1 = 0.0;
-        const double lk0 = Q.l10k1[k], lk1 = Q.l10k1[two ? k2 : k];
-        const float lk0f = (float)lk0, lk1f = (float)lk1;
-        const T cub0 = (T)((k + 1.) * (k + 1.) * (k + 1.)), cub1 = (T)((k2 + 1.) * (k2 + 1.) * (k2 + 1.));
+        const double lk0 = F32 ? 0.0 : Q.l10k1[k], lk1 = F32 ? 0.0 : Q.l10k1[two ? k2 : k];
+        const float lk0f = F32 ? Q.l10k1f[k] : 0.0f, lk1f = F32 ? Q.l10k1f[two ? k2 : k] : 0.0f;
+        const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
+        const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;  // exact for k < 255
         T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
         for (int i = tid; i < nchi; i += NL_NT) {
           const T rx = rct / xs[i];
@@ -827,14 +905,19 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
             }
           }
         }
-        if constexpr (sizeof(T) == sizeof(float)) {
+        // two block sums (mixed plan: FP32 within the warp, FP64 across)
+        if constexpr (F32) {
+          for (int o = 16; o > 0; o >>= 1) {
+            tp0 += __shfl_down_sync(0xffffffffu, tp0, o);
+            tp1 += __shfl_down_sync(0xffffffffu, tp1, o);
+          }
           part0 = tp0;
           part1 = tp1;
-        }
-        // two block sums
-        for (int o = 16; o > 0; o >>= 1) {
-          part0 += __shfl_down_sync(0xffffffffu, part0, o);
-          part1 += __shfl_down_sync(0xffffffffu, part1, o);
+        } else {
+          for (int o = 16; o > 0; o >>= 1) {
+            part0 += __shfl_down_sync(0xffffffffu, part0, o);
+            part1 += __shfl_down_sync(0xffffffffu, part1, o);
+          }
         }
         __syncthreads();
         if ((tid & 31) == 0) {
@@ -855,15 +938,22 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
       }
     __syncthreads();
     if (ADJ) continue;
-    // convergence at the block end (cosmo2D.c:4741-4750)
-    const int L = ke - 1;
-    const double denom = ggl[L * 2 + 0];
-    if (fabs(denom) > 1e-300) {
-      const double dev = Cl[L] / denom - 1.0;
-      if (isfinite(dev) && fabs(dev) < 0.01) {
-        done = 1;
-        LM = ke;
+    // convergence at the block end (cosmo2D.c:4741-4750), tested by one
+    // thread and shared
+    if (tid == 0) {
+      const int L = ke - 1;
+      const double denom = ggl[L * 2 + 0];
+      int d = 0;
+      if (fabs(denom) > 1e-300) {
+        const double dev = Cl[L] / denom - 1.0;
+        d = isfinite(dev) && fabs(dev) < 0.01;
       }
+      sdone = d;
+    }
+    __syncthreads();
+    if (sdone) {
+      done = 1;
+      LM = ke;
     }
   }
   if constexpr (ADJ) {

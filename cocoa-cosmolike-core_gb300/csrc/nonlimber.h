@@ -31,6 +31,11 @@ struct NLParams {
   const double* lnk1;
   const double* l10k1;
   const double* sck;
+  // FP32 copies for the mixed plan's loop: log10(k+1), the c2r scales and
+  // nu_j - 1
+  const float* l10k1f;
+  const float* sckf;
+  float nu1f[3];
 };
 
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,

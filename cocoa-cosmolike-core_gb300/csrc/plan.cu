@@ -764,6 +764,13 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       Q.lnk1 = da;
       Q.l10k1 = db;
       Q.sck = dc;
+      const std::vector<float> bf(b.begin(), b.end()), cf(c.begin(), c.end());
+      float *dbf, *dcf;
+      TRY(dupload(p, &dbf, bf.data(), bf.size()));
+      TRY(dupload(p, &dcf, cf.data(), cf.size()));
+      Q.l10k1f = dbf;
+      Q.sckf = dcf;
+      for (int j = 0; j < 3; j++) Q.nu1f[j] = (float)(Q.nu[j] - 1.0);
     }
     Q.hstride = Q.nmax / 2 + 1;
     Q.tout_stride = (size_t)3 * Q.hstride;
