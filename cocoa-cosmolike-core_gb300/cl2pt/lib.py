@@ -184,8 +184,10 @@ class Plan:
             pass
 
     # -------------------------------------------------------------- host
-    def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None):
-        """Host arrays in, host data vectors out ([n][n_total])."""
+    def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None, out=None):
+        """Host arrays in, host data vectors out ([n][n_total]); out: an
+        optional C-contiguous float64 host array of that shape (e.g. pinned)
+        to write into."""
         om = np.ascontiguousarray(omega_m, dtype=np.float64)
         n = om.shape[0]
         hh = np.ascontiguousarray(h0, dtype=np.float64)
@@ -199,7 +201,10 @@ class Plan:
         b.omega_m, b.h0, b.chi, b.G, b.lnP = _p(om), _p(hh), _p(ch), _p(gg), _p(lp)
         b.lnPL = _p(lpl) if lpl is not None else None
         b.nuisance = nus
-        out = np.zeros((n, self.n_total))
+        if out is None:
+            out = np.zeros((n, self.n_total))
+        elif out.shape != (n, self.n_total) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (n, n_total)")
         mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
         pmm = None if pm is None else np.ascontiguousarray(pm, dtype=np.float64)
         check(load().cl2pt_eval_real(self.h, C.byref(b),

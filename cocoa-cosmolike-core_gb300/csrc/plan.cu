@@ -644,6 +644,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   CUDA_OK(cudaMemset(P.conv_l, 0, sizeof(int) * (size_t)W * nl));
   TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
   TRY(dalloc(p, &p->d_err, 4));
+  TRY(dalloc(p, &p->d_inchk, 1));
+  CUDA_OK(cudaMallocHost((void**)&p->h_inchk, sizeof(int)));
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g)));
@@ -799,6 +801,7 @@ extern "C" int cl2pt_plan_destroy(cl2pt_plan* p)
   cl2pt_fastpt_plan_destroy(p->fpt_ia);
   for (void* d : p->dbufs) cudaFree(d);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  if (p->h_inchk) cudaFreeHost(p->h_inchk);
   delete p;
   return CL2PT_OK;
 }
@@ -842,19 +845,25 @@ extern "C" int cl2pt_node_limits(const cl2pt_plan* p, double lim_ss[3], double l
 }
 
 // ------------------------------------------------------------ evaluation
-static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b)
+// The reference rejects non-finite inputs in every setter
+// (generic_interface.cpp:993-1267).  For host batches the scalars and
+// nuisances are checked here; the tables (chi, G, lnP, lnPL: ~1 MB per
+// point) are checked on the device after staging (k_check_finite,
+// internal_eval), or here with tables = true for callers that stage
+// themselves.
+static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b, bool tables = false)
 {
   if (!b || b->n < 1 || b->n > p->max_batch) return CL2PT_ERR_ARG;
   if (!b->omega_m || !b->h0 || !b->chi || !b->G || !b->lnP || !b->nuisance) return CL2PT_ERR_ARG;
   if (b->where != CL2PT_HOST && b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
   if (b->where == CL2PT_HOST) {
-    // host-side validation of the inputs the reference rejects (NaN checks
-    // of every setter, generic_interface.cpp:993-1267)
     const int n = b->n;
     if (!all_finite(b->omega_m, n) || !all_finite(b->h0, n)) return CL2PT_ERR_ARG;
-    if (!all_finite(b->chi, n * p->P.chi_nz) || !all_finite(b->G, n * p->P.G_nz))
-      return CL2PT_ERR_ARG;
-    if (!all_finite(b->lnP, n * p->P.pk_nk * p->P.pk_nz)) return CL2PT_ERR_ARG;
+    if (tables) {
+      if (!all_finite(b->chi, n * p->P.chi_nz) || !all_finite(b->G, n * p->P.G_nz)) return CL2PT_ERR_ARG;
+      if (!all_finite(b->lnP, n * p->P.pk_nk * p->P.pk_nz)) return CL2PT_ERR_ARG;
+      if (b->lnPL && !all_finite(b->lnPL, n * p->P.pkl_nk * p->P.pkl_nz)) return CL2PT_ERR_ARG;
+    }
     for (int i = 0; i < n; i++) {
       const cl2pt_nuisance& nu = b->nuisance[i];
       if (!all_finite((const double*)&nu, sizeof(nu) / sizeof(double))) return CL2PT_ERR_ARG;
@@ -863,6 +872,15 @@ static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b)
     }
   }
   return CL2PT_OK;
+}
+
+// Non-finite entries of a staged input table raise *flag (grid-stride)
+__global__ void k_check_finite(const double* __restrict__ x, size_t n, int* flag)
+{
+  bool bad = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(x[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
 // Fourier mode: the Limber stages run on the caller's multipoles (the
@@ -1209,7 +1227,7 @@ extern "C" int cl2pt_jacobian_real(cl2pt_plan* p, const cl2pt_batch* b, const in
                                    cl2pt_nuisance* jac_nu, void* stream)
 {
   if (!p || !b || b->n != 1 || !jac_lnP || !jac_nu) return CL2PT_ERR_ARG;
-  int st = check_batch(p, b);
+  int st = check_batch(p, b, true);
   if (st) return st;
   if (b->lnPL && !jac_lnPL) return CL2PT_ERR_ARG;
   const int NT = p->n_total;
@@ -1463,6 +1481,18 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP;
     lnPL = (b->lnPL && p->d_in_lnPL) ? p->d_in_lnPL : p->d_in_lnP;
     nu = p->d_in_nu;
+    {
+      // the tables' finiteness check (check_batch) on the staged copies:
+      // one pass at device bandwidth, one flag, before any compute
+      CUDA_OK(cudaMemsetAsync(p->d_inchk, 0, sizeof(int), s));
+      k_check_finite<<<1216, 256, 0, s>>>(chi, (size_t)n * nchi, p->d_inchk);
+      k_check_finite<<<1216, 256, 0, s>>>(G, (size_t)n * nG, p->d_inchk);
+      k_check_finite<<<1216, 256, 0, s>>>(lnP, (size_t)n * nP, p->d_inchk);
+      if (b->lnPL && p->d_in_lnPL) k_check_finite<<<1216, 256, 0, s>>>(lnPL, (size_t)n * nPL, p->d_inchk);
+      CUDA_OK(cudaMemcpyAsync(p->h_inchk, p->d_inchk, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_OK(cudaStreamSynchronize(s));
+      if (*p->h_inchk) return CL2PT_ERR_ARG;
+    }
     if (mask) {
       CUDA_OK(cudaMemcpyAsync(d_mask_stage, mask, n_total * sizeof(int), cudaMemcpyHostToDevice, s));
       dmask = d_mask_stage;

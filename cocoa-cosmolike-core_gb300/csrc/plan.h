@@ -66,6 +66,8 @@ struct cl2pt_plan {
   cl2pt::NLParams nlq;
   int node_stride = 0;
   int* d_err = nullptr;
+  int* d_inchk = nullptr;   // non-finite flag of staged host tables
+  int* h_inchk = nullptr;   // its pinned host copy
   int last_launches = 0;
   // Fourier path: the caller's multipoles, and staging for host batches
   double* d_ell_f = nullptr;        // [max(nnode_ss, nnode_g)]

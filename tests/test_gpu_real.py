@@ -226,16 +226,29 @@ def test_mask_and_calibration(gpu_lib, oracle_built):
 
 @pytest.mark.gpu
 def test_bad_inputs_rejected(gpu_lib):
+    """Non-finite host inputs are rejected (the reference's setter checks):
+    the tables are checked on the device after staging, the scalars and the
+    jacobian's single point on the host; a valid call after a rejected one
+    still evaluates."""
     w = workloads.make("real_3x2pt_small_limber")
-    tabs, nus = workloads.points(w, 1, seed=5)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
+    tabs, nus = workloads.points(w, 2, seed=5)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=2)
     om, h0, chi, G, lnP = workloads.stack(tabs)
-    lnP = lnP.copy()
-    lnP[0, 17] = np.nan
+    good = plan.eval_real(om, h0, chi, G, lnP, nus)
+    for name, idx, val in (("lnP", (0, 17), np.nan), ("lnP", (1, 5000), np.inf),
+                           ("chi", (1, 3), np.nan), ("G", (0, 9), -np.inf), ("om", (1,), np.nan)):
+        arrs = {"om": om.copy(), "chi": chi.copy(), "G": G.copy(), "lnP": lnP.copy()}
+        arrs[name][idx] = val
+        with pytest.raises(lib.CL2PTError):
+            plan.eval_real(arrs["om"], h0, arrs["chi"], arrs["G"], arrs["lnP"], nus)
+    again = plan.eval_real(om, h0, chi, G, lnP, nus)
+    assert np.array_equal(again, good)
+    bad = lnP.copy()
+    bad[0, 3] = np.nan
     with pytest.raises(lib.CL2PTError):
-        plan.eval_real(om, h0, chi, G, lnP, nus)
+        plan.jacobian_real(om[:1], h0[:1], chi[:1], G[:1], bad[:1], nus[:1], rows=[0])
     with pytest.raises(lib.CL2PTError):
-        plan.eval_real(np.zeros(2), h0, chi, G, lnP, nus)  # n > max_batch
+        plan.eval_real(np.zeros(3), h0, chi, G, lnP, nus)  # n > max_batch
 
 
 @pytest.mark.gpu
