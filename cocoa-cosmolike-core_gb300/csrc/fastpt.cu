@@ -31,6 +31,10 @@
 #include "cl2pt_fastpt.h"
 #include "fastpt.h"
 
+namespace cl2pt {
+void launch_check_finite(const double* x, size_t n, int* flag, cudaStream_t s);  // k_setup.cu
+}
+
 using cplx = std::complex<double>;
 
 #define FPT_CUDA_OK(x)                                                                    \
@@ -388,6 +392,7 @@ struct cl2pt_fastpt_plan {
   double* d_out = nullptr;
   size_t d_out_n = 0;
   int* d_err = nullptr;
+  int* d_inchk = nullptr;  // non-finite flag of staged host spectra
 };
 
 namespace {
@@ -710,6 +715,7 @@ int create_base(cl2pt_fastpt_plan* p, const double* x)
   if (int st = up(p, &b.xin, (const double2*)nullptr, (size_t)p->wave * p->n_bias * (half + 1))) return st;
   if (int st = up(p, &b.R, (const double*)nullptr, (size_t)p->wave * p->n_in * Ntot)) return st;
   if (int st = up(p, &p->d_err, (const int*)nullptr, 1)) return st;
+  if (int st = up(p, &p->d_inchk, (const int*)nullptr, 1)) return st;
   b.err = p->d_err;
   if (int st = up(p, &p->d_fx, (const double*)nullptr, (size_t)p->max_spec * N0)) return st;
   return CL2PT_OK;
@@ -832,8 +838,6 @@ int run_program(cl2pt_fastpt_plan* p, Program& g, bool direct, const double* fx,
   const double* dfx = fx;
   double* dout = out;
   if (where == CL2PT_HOST) {
-    for (size_t i = 0; i < in_n; i++)
-      if (!std::isfinite(fx[i])) return CL2PT_ERR_ARG;
     if (p->d_out_n < out_n) {
       if (p->d_out) {
         FPT_CUDA_OK(cudaFree(p->d_out));
@@ -846,6 +850,14 @@ int run_program(cl2pt_fastpt_plan* p, Program& g, bool direct, const double* fx,
     FPT_CUDA_OK(cudaMemcpyAsync(p->d_fx, fx, in_n * sizeof(double), cudaMemcpyHostToDevice, st));
     dfx = p->d_fx;
     dout = p->d_out;
+    // non-finite spectra are rejected before any compute, checked on the
+    // staged copy
+    int bad = 0;
+    FPT_CUDA_OK(cudaMemsetAsync(p->d_inchk, 0, sizeof(int), st));
+    cl2pt::launch_check_finite(dfx, in_n, p->d_inchk, st);
+    FPT_CUDA_OK(cudaMemcpyAsync(&bad, p->d_inchk, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FPT_CUDA_OK(cudaStreamSynchronize(st));
+    if (bad) return CL2PT_ERR_ARG;
   }
   FPT_CUDA_OK(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
   for (int s0 = 0; s0 < nspec; s0 += p->wave) {

@@ -537,6 +537,21 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
   *launches += 2;
 }
 
+// Input validation of host batches after staging (the reference rejects
+// non-finite values in its setters): one grid-stride pass, one flag.
+__global__ void k_check_finite(const double* __restrict__ x, size_t n, int* flag)
+{
+  bool bad = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(x[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+void launch_check_finite(const double* x, size_t n, int* flag, cudaStream_t s)
+{
+  if (n) k_check_finite<<<1216, 256, 0, s>>>(x, n, flag);
+}
+
 void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s)
 {
   // reads the wave's fine grid written by launch_setup

@@ -19,6 +19,8 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 // Limber C_l tables on the C_l nodes (ss, gs, gg) and, when the non-Limber
 // w(theta) path is on, the Limber gg C_l at integer l < lmax_nolimber for
 // both power spectra.  ell_ss / ell_g: node multipoles (device).
+// raise *flag (atomic OR) if any of x[0..n) is not finite (k_setup.cu)
+void launch_check_finite(const double* x, size_t n, int* flag, cudaStream_t s);
 // mixed plan: split the wave's lnP (and separate lnPL) into P.lnP2 / P.lnPL2
 void launch_split_tables(const Params& P, cudaStream_t s, int* launches);
 void launch_limber(const Params& P, const double* ell_ss, const double* ell_g,

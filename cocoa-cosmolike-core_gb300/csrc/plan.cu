@@ -848,7 +848,7 @@ extern "C" int cl2pt_node_limits(const cl2pt_plan* p, double lim_ss[3], double l
 // The reference rejects non-finite inputs in every setter
 // (generic_interface.cpp:993-1267).  For host batches the scalars and
 // nuisances are checked here; the tables (chi, G, lnP, lnPL: ~1 MB per
-// point) are checked on the device after staging (k_check_finite,
+// point) are checked on the device after staging (launch_check_finite,
 // internal_eval), or here with tables = true for callers that stage
 // themselves.
 static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b, bool tables = false)
@@ -872,15 +872,6 @@ static int check_batch(const cl2pt_plan* p, const cl2pt_batch* b, bool tables = 
     }
   }
   return CL2PT_OK;
-}
-
-// Non-finite entries of a staged input table raise *flag (grid-stride)
-__global__ void k_check_finite(const double* __restrict__ x, size_t n, int* flag)
-{
-  bool bad = false;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    bad |= !isfinite(x[i]);
-  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
 // Fourier mode: the Limber stages run on the caller's multipoles (the
@@ -1485,10 +1476,10 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       // the tables' finiteness check (check_batch) on the staged copies:
       // one pass at device bandwidth, one flag, before any compute
       CUDA_OK(cudaMemsetAsync(p->d_inchk, 0, sizeof(int), s));
-      k_check_finite<<<1216, 256, 0, s>>>(chi, (size_t)n * nchi, p->d_inchk);
-      k_check_finite<<<1216, 256, 0, s>>>(G, (size_t)n * nG, p->d_inchk);
-      k_check_finite<<<1216, 256, 0, s>>>(lnP, (size_t)n * nP, p->d_inchk);
-      if (b->lnPL && p->d_in_lnPL) k_check_finite<<<1216, 256, 0, s>>>(lnPL, (size_t)n * nPL, p->d_inchk);
+      cl2pt::launch_check_finite(chi, (size_t)n * nchi, p->d_inchk, s);
+      cl2pt::launch_check_finite(G, (size_t)n * nG, p->d_inchk, s);
+      cl2pt::launch_check_finite(lnP, (size_t)n * nP, p->d_inchk, s);
+      if (b->lnPL && p->d_in_lnPL) cl2pt::launch_check_finite(lnPL, (size_t)n * nPL, p->d_inchk, s);
       CUDA_OK(cudaMemcpyAsync(p->h_inchk, p->d_inchk, sizeof(int), cudaMemcpyDeviceToHost, s));
       CUDA_OK(cudaStreamSynchronize(s));
       if (*p->h_inchk) return CL2PT_ERR_ARG;

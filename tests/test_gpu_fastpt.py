@@ -108,6 +108,21 @@ def test_fastpt_extrapolation_check(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_fastpt_nonfinite_rejected(gpu_lib):
+    """Non-finite host spectra are rejected with CL2PT_ERR_ARG (checked on
+    the staged copy, before any compute); the plan stays usable."""
+    k, P, _ = workloads.fastpt_spectra(3, seed=6)
+    plan = lib.FastPT.for_bias(k, max_spec=3)
+    good = plan.bias(P)
+    for val in (np.nan, np.inf):
+        bad = P.copy()
+        bad[2, 100] = val
+        with pytest.raises(lib.CL2PTError, match="-1"):
+            plan.bias(bad)
+    assert np.array_equal(plan.bias(P), good)
+
+
+@pytest.mark.gpu
 def test_J_abl_dropin(gpu_lib, oracle_built):
     """cl2pt_J_abl with the reference's J_abl arguments (Fy as row
     pointers), twice with the same plan and once with another term list."""
