@@ -76,6 +76,10 @@ struct Params {
   const float* facf_ss;
   const float* facf_g;
   const float* facf_gi;
+  int ell_g_sorted;         // the gg multipole list (ell argument) ascends
+  // mixed plan: FP32 records of the gg nodes [B][nl][GGN_SLOTS][n_gg]
+  // (k_gg_nodes, k_limber.cu)
+  float* ggn;
   // mixed plan: FP32 (head, tail) of every entry of the wave's tables
   float* lnP2;              // [B][pk_nk*pk_nz][2]
   float* lnPL2;             // [B][pkl_nk*pkl_nz][2]; lnP2 when lnPL is lnP

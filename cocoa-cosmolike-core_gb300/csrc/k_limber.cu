@@ -439,6 +439,60 @@ __device__ __forceinline__ int bsearch_from(const T* __restrict__ x, int n, T v,
 
 constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
 
+// Mixed plan: per (point, lens bin) the gg node data the multipole tiles of
+// k_limber_gg read, formed once in FP64 and stored as FP32 records instead
+// of in every tile: slots 0-8 fK c/H0, quadrature weight wt dchi/da / fK^2,
+// z offset in lnP, L, M, r0 weights, z offset in lnP_lin, log10(fK c/H0)
+// head and tail; 9, 10 the lnP and lnP_lin z cells; 11, 12 the first
+// multipole index kept by the chi(a_min) cut on the C_l nodes and on
+// l = 0..LNL-1 (prefixes when the list ascends); 13, 14 the cut's FP64
+// threshold on l + 1/2 (for a list that does not ascend).
+constexpr int GGN_SLOTS = 15;
+__global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __restrict__ ell)
+{
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const size_t b0 = (size_t)pt * P.nl + q;
+  float* rec = P.ggn + b0 * GGN_SLOTS * P.n_gg;
+  const int off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const int* nodej = P.node_j + (size_t)pt * P.node_stride;
+  const double chi_amin = P.chi_amin[pt];
+  const PdeltaTable pl = pdelta_table(P, pt, true);
+  for (int p = threadIdx.x; p < P.n_gg; p += blockDim.x) {
+    const double a = node[(size_t)NF_A * P.node_stride + off + p];
+    const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+    const double wq = node[(size_t)NF_WT * P.node_stride + off + p] *
+                      node[(size_t)NF_DCHIDA * P.node_stride + off + p] / (fK * fK);
+    const double z = 1.0 / a - 1.0;
+    const int jl = bsearch_d(pl.z, pl.nz, z);
+    const double dyl = (z - pl.z[jl]) / (pl.z[jl + 1] - pl.z[jl]);
+    const double lfk = log10(fK * CL2PT_COVERH0);
+    // chi1 = fK (l+3/2)/(l+1/2) > chi(a_min)  <=>  l+1/2 < fK / (chi(a_min) - fK)
+    // (always when fK >= chi(a_min))
+    const double th = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
+    int lm[2];
+    for (int m = 0; m < 2; m++) {
+      const int nL = m == 0 ? P.nnode_g : P.lmax_nolimber;
+      int lo = 0, hi = nL;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const double lpm = (m == 0 ? ell[mid] : (double)mid) + 0.5;
+        if (lpm < th) lo = mid + 1;
+        else hi = mid;
+      }
+      lm[m] = lo;
+    }
+    const float2 lf = split_f(lfk);
+    const long long tb = __double_as_longlong(th);
+    const float v[GGN_SLOTS] = {
+        (float)(fK * CL2PT_COVERH0), (float)wq, (float)node[(size_t)NF_DYZ * P.node_stride + off + p],
+        (float)P.wgg_l[b0 * P.n_gg + p], (float)P.wgg_m[b0 * P.n_gg + p], (float)P.wgg_r0[b0 * P.n_gg + p],
+        (float)dyl, lf.x, lf.y, __int_as_float(nodej[off + p]), __int_as_float(jl), __int_as_float(lm[0]),
+        __int_as_float(lm[1]), __int_as_float((int)(tb & 0xffffffffLL)), __int_as_float((int)(tb >> 32))};
+    for (int f = 0; f < GGN_SLOTS; f++) rec[(size_t)f * P.n_gg + p] = v[f];
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __restrict__ ell,
                                                    int mode)
@@ -489,7 +543,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   // node where the thresholds were, axis tails and widths as floats where
   // the FP64 axes were
   float* nf = (float*)nd;
-  int* lmin = (int*)thr;
+  int* lmin = (int*)(nf + 9 * PCH);
   Axis<T> ax{}, axl{};
   AxisF axf{}, axlf{};
   if constexpr (F32) {
@@ -543,7 +597,11 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   double lp = 1.5;
   T pref, c0, c1, ratio;
   float2 llf = make_float2(0.0f, 0.0f);
+  // the chi(a_min) cut as a first-kept index when the list ascends (the
+  // integer-l pass always), else as the FP64 threshold on l + 1/2
+  const bool cut_idx = mode == 1 || P.ell_g_sorted;
   if constexpr (F32) {
+    if (!cut_idx) lp = (valid ? ell[L] : 1.0) + 0.5;
     // FP32 plan constants (the C_l nodes, or l = L for the integer-l pass)
     const float* f = (mode == 0 ? P.facf_g : P.facf_gi) + 8 * (size_t)(valid ? L : 0);
     const float4 fa = *(const float4*)f, fb = *(const float4*)(f + 4);
@@ -568,7 +626,20 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
     const int np = min(PCH, P.n_gg - p0);
     __syncthreads();
-    for (int p = tid; p < np; p += LTG) {
+    if constexpr (F32) {
+      // the node records of k_gg_nodes: no FP64 in the tile
+      const float* rec = P.ggn + b0 * GGN_SLOTS * P.n_gg + p0;
+      for (int p = tid; p < np; p += LTG) {
+        for (int f = 0; f < 9; f++) nf[f * PCH + p] = rec[(size_t)f * P.n_gg + p];
+        nj[p] = __float_as_int(rec[(size_t)9 * P.n_gg + p]);
+        nj[PCH + p] = __float_as_int(rec[(size_t)10 * P.n_gg + p]);
+        lmin[p] = __float_as_int(rec[(size_t)(mode == 0 ? 11 : 12) * P.n_gg + p]);
+        const unsigned lo = __float_as_uint(rec[(size_t)13 * P.n_gg + p]);
+        const unsigned hi = __float_as_uint(rec[(size_t)14 * P.n_gg + p]);
+        thr[p] = __longlong_as_double(((long long)hi << 32) | lo);
+      }
+    }
+    for (int p = tid; p < np && !F32; p += LTG) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p0 + p];
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
       const double wq = node[(size_t)NF_WT * P.node_stride + off + p0 + p] *
@@ -586,37 +657,15 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
       // chi1 = fK (l+3/2)/(l+1/2) > chi(a_min)  <=>  l+1/2 < fK / (chi(a_min) - fK)
       // (always when fK >= chi(a_min))
       const double th = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
-      if constexpr (F32) {
-        nf[0 * PCH + p] = (float)(fK * CL2PT_COVERH0);
-        nf[1 * PCH + p] = (float)wq;
-        nf[2 * PCH + p] = (float)dyz;
-        nf[3 * PCH + p] = (float)Lw;
-        nf[4 * PCH + p] = (float)Mw;
-        nf[5 * PCH + p] = (float)r0w;
-        nf[6 * PCH + p] = (float)dyl;
-        const float2 lf = split_f(lfk);
-        nf[7 * PCH + p] = lf.x;
-        nf[8 * PCH + p] = lf.y;
-        // the multipoles cut form a prefix: the first kept index
-        int lo = 0, hi = nL;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          const double lpm = ((mode == 0) ? ell[mid] : (double)mid) + 0.5;
-          if (lpm < th) lo = mid + 1;
-          else hi = mid;
-        }
-        lmin[p] = lo;
-      } else {
-        nd[0 * PCH + p] = fK;
-        nd[1 * PCH + p] = wq;
-        nd[2 * PCH + p] = dyz;
-        nd[3 * PCH + p] = Lw;
-        nd[4 * PCH + p] = Mw;
-        nd[5 * PCH + p] = r0w;
-        nd[6 * PCH + p] = dyl;
-        nd[7 * PCH + p] = lfk;
-        thr[p] = th;
-      }
+      nd[0 * PCH + p] = fK;
+      nd[1 * PCH + p] = wq;
+      nd[2 * PCH + p] = dyz;
+      nd[3 * PCH + p] = Lw;
+      nd[4 * PCH + p] = Mw;
+      nd[5 * PCH + p] = r0w;
+      nd[6 * PCH + p] = dyl;
+      nd[7 * PCH + p] = lfk;
+      thr[p] = th;
     }
     __syncthreads();
     if (!valid) continue;
@@ -626,7 +675,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     for (int p = 0; p < np; p++) {
       T fkc, Lw, Mw, r0w;
       if constexpr (F32) {
-        if (L < lmin[p]) continue;  // (l+3/2)/k beyond chi(a_min)
+        if (cut_idx ? L < lmin[p] : lp < thr[p]) continue;  // (l+3/2)/k beyond chi(a_min)
         fkc = nf[0 * PCH + p];
         Lw = nf[3 * PCH + p];
         Mw = nf[4 * PCH + p];
@@ -753,6 +802,10 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     const size_t sm = sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
                       sizeof(T) * (P.pk_nk + P.pkl_nk + 5 * P.chi_nz + 3 * P.G_nz + 5 * P.lens_nz) + 64;
     cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (sizeof(T) == sizeof(float)) {
+      k_gg_nodes<<<dim3(P.B, P.nl), 128, 0, s>>>(P, ell_g);
+      (*launches)++;
+    }
     dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
     k_limber_gg<T><<<g, LTG, sm, s>>>(P, ell_g, 0);

@@ -1026,26 +1026,46 @@ void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar
 }
 
 template <typename T>
-static void launch_nl_t(const Params& P, const NLParams& Q, cudaStream_t s)
+static void launch_nl_prep_t(const Params& P, const NLParams& Q, cudaStream_t s)
 {
   const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
+}
+
+template <typename T>
+static void launch_nl_loop_t(const Params& P, const NLParams& Q, cudaStream_t s)
+{
   const size_t sm3 = nl_loop_smem<T>(P, Q, false);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   k_nl_loop<T, false><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
 }
 
+void launch_nonlimber_prep(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk)
+{
+  hk(CL2PT_K_NONLIMBER, 1);
+  if (P.prec == CL2PT_PREC_FP64) launch_nl_prep_t<double>(P, Q, s);
+  else launch_nl_prep_t<float>(P, Q, s);
+  hk(CL2PT_K_NONLIMBER, 0);
+  (*launches) += 2;
+}
+
+void launch_nonlimber_loop(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk)
+{
+  hk(CL2PT_K_NONLIMBER, 1);
+  if (P.prec == CL2PT_PREC_FP64) launch_nl_loop_t<double>(P, Q, s);
+  else launch_nl_loop_t<float>(P, Q, s);
+  hk(CL2PT_K_NONLIMBER, 0);
+  (*launches) += 2;
+}
+
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
                       const Hook& hk)
 {
-  hk(CL2PT_K_NONLIMBER, 1);
-  if (P.prec == CL2PT_PREC_FP64) launch_nl_t<double>(P, Q, s);
-  else launch_nl_t<float>(P, Q, s);
-  hk(CL2PT_K_NONLIMBER, 0);
-  (*launches) += 4;
+  launch_nonlimber_prep(P, Q, s, launches, hk);
+  launch_nonlimber_loop(P, Q, s, launches, hk);
 }
 
 }  // namespace cl2pt

@@ -40,6 +40,12 @@ struct NLParams {
 
 void launch_nonlimber(const Params& P, const NLParams& Q, cudaStream_t s, int* launches,
                       const Hook& hk);
+// the same in two parts: the kernel transforms and direct Gamma kernels
+// (independent of the Limber tables, so they may run on another stream),
+// then the multipole loop (reads the transforms, the direct kernels and the
+// Limber C_gg tables)
+void launch_nonlimber_prep(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk);
+void launch_nonlimber_loop(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk);
 // Adjoint of the FFTLog part (run after the forward wave): cbar [B][nl][LNL]
 // = dL/dC_l below the hand-over multipole; adds into lnpl_bar [B][pkl_nk *
 // pkl_nz] and nu_bar[pt].gb[0][q] (bias model 0).

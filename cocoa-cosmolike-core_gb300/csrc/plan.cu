@@ -611,6 +611,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.facf_ss = p->d_lfacf_ss;
   P.facf_g = p->d_lfacf_g;
   P.facf_gi = p->d_lfacf_g + 8 * (size_t)p->nnode_g;
+  P.ell_g_sorted = 1;
   P.lens_zc = p->d_lens_zc; P.lens_y = p->d_lens_y; P.lens_c = p->d_lens_c;
   P.src_zmin_all = p->src.zmin_all; P.src_zmax_all = p->src.zmax_all;
   P.lens_zmax_all = p->lens.zmax_all;
@@ -645,10 +646,14 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dalloc(p, &P.obs, (size_t)W * p->n_total));
   TRY(dalloc(p, &p->d_err, 4));
   TRY(dalloc(p, &p->d_inchk, 1));
+  CUDA_OK(cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking));
+  CUDA_OK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  CUDA_OK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   CUDA_OK(cudaMallocHost((void**)&p->h_inchk, sizeof(int)));
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g)));
+  if (precision != CL2PT_PREC_FP64) TRY(dalloc(p, &P.ggn, (size_t)W * nl * 15 * std::max(p->n_gg, 1)));
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
   if (precision != CL2PT_PREC_FP64) {
@@ -802,6 +807,9 @@ extern "C" int cl2pt_plan_destroy(cl2pt_plan* p)
   for (void* d : p->dbufs) cudaFree(d);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   if (p->h_inchk) cudaFreeHost(p->h_inchk);
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->ev_join) cudaEventDestroy(p->ev_join);
+  if (p->s2) cudaStreamDestroy(p->s2);
   delete p;
   return CL2PT_OK;
 }
@@ -1577,7 +1585,12 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     }
     return pp->ev_pool[pp->ev_used++];
   }};
+  // the same hook recording on the second stream
+  HookCtx hc2 = hc;
+  hc2.s = p->s2;
+  cl2pt::Hook hk2;
   if (p->timing) {
+    hk2.ctx = &hc2;
     hk.ctx = &hc;
     hk.fn = [](void* c, int k, int begin) {
       HookCtx* h = (HookCtx*)c;
@@ -1588,12 +1601,19 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         r.stage = k;
         r.a = e;
         r.b = nullptr;
+        r.s = h->s;
         r.launches = 1;
         h->p->recs.push_back(r);
       } else {
-        h->p->recs.back().b = e;
+        // the open record of this stream (records of two streams interleave)
+        for (auto it = h->p->recs.rbegin(); it != h->p->recs.rend(); ++it)
+          if (it->b == nullptr && it->s == h->s) {
+            it->b = e;
+            break;
+          }
       }
     };
+    hk2.fn = hk.fn;
   }
   // per-wave adjoint set-up: zero the accumulated adjoints, offset the views
   auto vjp_wave = [&](const Params& P, int w0, cl2pt::VJPParams& V) -> int {
@@ -1625,6 +1645,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     std::vector<double> fs, fg;
     for (int i = 0; i < fr->nell; i++) {
       if (i > 0 && !(fr->ell[i] > fr->ell[i - 1])) ell_sorted = false;
+      p->ell_f_sorted = ell_sorted ? 1 : 0;
       const double l = fr->ell[i], lp = l + 0.5, tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
       fs.push_back(log10(lp));
       fs.push_back(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
@@ -1685,6 +1706,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       Pf.nnode_ss = Pf.nnode_g = fr->nell;
       Pf.facf_ss = p->d_lfacf_f;
       Pf.facf_g = p->d_lfacf_f + 8 * (size_t)fr->nell;
+      Pf.ell_g_sorted = p->ell_f_sorted;
       Pf.tab_gg = p->d_tab_gg_f;
       Pf.adopt_limber_gg = 1;  // no integer-l spectra in this pass
       cl2pt::launch_limber(Pf, p->d_ell_f, p->d_ell_f, s, &launches, hk);
@@ -1732,10 +1754,21 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                                   p->d_lfac_g, p->d_lfacf_g, s, &launches);
       }
     } else {
+      const bool nlw = (P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg;
+      if (nlw) {
+        // the FFTLog transforms and direct Gamma kernels (FP64-pipe bound,
+        // independent of the Limber tables) overlap the Limber kernels
+        // (FP32-pipe bound) on the plan's second stream
+        CUDA_OK(cudaEventRecord(p->ev_fork, s));
+        CUDA_OK(cudaStreamWaitEvent(p->s2, p->ev_fork, 0));
+        cl2pt::launch_nonlimber_prep(P, p->nlq, p->s2, &launches, hk2);
+        CUDA_OK(cudaEventRecord(p->ev_join, p->s2));
+      }
       cl2pt::launch_limber(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       if (P.tatt || P.one_loop) cl2pt::launch_extra(P, p->d_ell_ss, p->d_ell_g, s, &launches, hk);
-      if ((P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg) {
-        cl2pt::launch_nonlimber(P, p->nlq, s, &launches, hk);
+      if (nlw) {
+        CUDA_OK(cudaStreamWaitEvent(s, p->ev_join, 0));
+        cl2pt::launch_nonlimber_loop(P, p->nlq, s, &launches, hk);
         if (xo && xo->cnl) {
           const size_t m = (size_t)P.B * P.nl;
           CUDA_OK(cudaMemcpyAsync(xo->cnl + (size_t)w0 * P.nl * P.lmax_nolimber, P.cnl,

@@ -99,12 +99,17 @@ struct cl2pt_plan {
   float* d_lfacf_ss = nullptr;         // FP32 copies (8 floats per multipole)
   float* d_lfacf_g = nullptr;
   float* d_lfacf_f = nullptr;
+  int ell_f_sorted = 1;                // the last caller multipole list ascends
   double* d_chi2 = nullptr;            // [max_batch] chi^2 staging
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
-  struct Rec { int stage; cudaEvent_t a, b; int launches; };
+  struct Rec { int stage; cudaEvent_t a, b; int launches; cudaStream_t s; };
+  // second stream for work that overlaps the main one, and its fork/join
+  // events
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<Rec> recs;
   size_t ev_used = 0;
   int last_batch = 0;
