@@ -28,6 +28,7 @@ namespace cl2pt {
 namespace {
 
 constexpr int LC = 32;  // multipoles per shared-memory chunk
+constexpr int VJP_GG_S = 4;  // threads per node of the gg sweep
 
 template <typename T> __device__ __forceinline__ T t_exp(T x);
 template <> __device__ __forceinline__ float t_exp<float>(float x) { return expf(x); }
@@ -102,7 +103,7 @@ __device__ __forceinline__ AxF load_axis_fx(const double* __restrict__ lk, int n
   float* h = (float*)space;
   float* l = h + nk;
   float* iv = l + nk;
-  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+  for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nk; i += blockDim.x * blockDim.y) {
     const float v = (float)lk[i];
     h[i] = v;
     l[i] = (float)(lk[i] - (double)v);
@@ -159,7 +160,7 @@ __device__ __forceinline__ float pw_eval_f(PWalk<float>& w, const AxF& ax, const
 
 __device__ __forceinline__ void load_axis_d(const double* __restrict__ lk, int nk, double* lkd, double* inv)
 {
-  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+  for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nk; i += blockDim.x * blockDim.y) {
     lkd[i] = lk[i];
     inv[i] = (i + 1 < nk) ? 1.0 / (lk[i + 1] - lk[i]) : 0.0;
   }
@@ -415,8 +416,11 @@ template <typename T>
 __global__ void k_vjp_gg(Params P, VJPParams V)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // blockDim (nodes, S): S threads per node, each on a contiguous part of
+  // the multipole range (the tables in shared memory are shared by all)
   const int pt = blockIdx.x, q = blockIdx.y;
-  const int p = threadIdx.x;
+  const int p = threadIdx.x, sub = threadIdx.y, S = blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
   const int nn = P.n_gg, K = P.nnode_g, LNL = P.lmax_nolimber;
   const int nk = P.pk_nk, nkl = P.pkl_nk;
   const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
@@ -449,7 +453,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
   const double* Z = P.chi_z;
-  for (int i = p; i < nc; i += blockDim.x) {
+  for (int i = tid; i < nc; i += nth) {
     cx[i] = (T)Xg[i];
     cz[i] = (T)Z[i];
     if (i + 1 < nc) {
@@ -460,20 +464,20 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       cup[i] = cdn[i] = (T)0;
     }
   }
-  for (int i = p; i < ng; i += blockDim.x) {
+  for (int i = tid; i < ng; i += nth) {
     gv[i] = (T)Gg[i];
     gz[i] = (T)P.G_z[i];
     gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
   }
-  for (int i = p; i < nzs; i += blockDim.x) {
+  for (int i = tid; i < nzs; i += nth) {
     szc[i] = (T)P.lens_zc[i];
     sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
     sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
   }
   const size_t b0 = (size_t)pt * P.nl + q;
-  for (int i = p; i < K; i += blockDim.x) cbs[i] = (T)V.cbar_gg[b0 * K + i];
+  for (int i = tid; i < K; i += nth) cbs[i] = (T)V.cbar_gg[b0 * K + i];
   if (nonlim)
-    for (int i = p; i < 2 * LNL; i += blockDim.x) gbs[i] = (T)V.ggl_bar[b0 * LNL * 2 + i];
+    for (int i = tid; i < 2 * LNL; i += nth) gbs[i] = (T)V.ggl_bar[b0 * LNL * 2 + i];
   __syncthreads();
   if (p >= nn) return;
   const int off = P.n_ss + P.nl * P.n_ss + q * nn;
@@ -528,8 +532,10 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   PWalk<T> wk;
   double lbar = 0.0;
   const int Lk = V.lfac_g_sorted ? first_kept(V.lfac_g, K, nd.fK, chi_amin) : 0;
-  for (int L0 = Lk; L0 < K; L0 += LC) {
-    const int L1 = min(K, L0 + LC);
+  const int cs = (K - Lk + S - 1) / S;
+  const int La = min(K, Lk + sub * cs), Lb = min(K, Lk + (sub + 1) * cs);
+  for (int L0 = La; L0 < Lb; L0 += LC) {
+    const int L1 = min(Lb, L0 + LC);
     T lt = 0;
     for (int L = L0; L < L1; L++) {
       const double* fac = V.lfac_g + 6 * L;
@@ -566,7 +572,10 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
     T lt = 0;
-    for (int L = first_kept(V.lfac_gi, LNL, nd.fK, chi_amin); L < LNL; L++) {
+    const int Li = first_kept(V.lfac_gi, LNL, nd.fK, chi_amin);
+    const int ci = (LNL - Li + S - 1) / S;
+    const int Ia = min(LNL, Li + sub * ci), Ib = min(LNL, Li + (sub + 1) * ci);
+    for (int L = Ia; L < Ib; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
       T dx, dxl, s, Pn, Pl;
@@ -593,7 +602,8 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
     pw_flush(wl, barl, P.pkl_nz, jl, dyl);
   }
-  V.lbar_gg[b0 * nn + p] += lbar;  // zeroed per wave; the Fourier path adds two passes
+  // zeroed per wave; S threads per node, and the Fourier path adds two passes
+  atomicAdd(&V.lbar_gg[b0 * nn + p], lbar);
 }
 
 template <typename T>
@@ -630,7 +640,17 @@ void launch_t(const Params& P, const VJPParams& V, int which, cudaStream_t s)
   } else {
     const size_t sm = gg_smem<T>(P);
     cudaFuncSetAttribute(k_vjp_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_vjp_gg<T><<<dim3(P.B, P.nl), ((P.n_gg + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+    // up to 4 threads per node: a CTA holds ~85 KB of tables, so two CTAs
+    // fit an SM; 4 x 96 threads each keep 24 warps resident instead of 6.
+    // S shrinks with the node count to the block's thread and register
+    // limits.
+    const int nx = ((P.n_gg + rnd - 1) / rnd) * rnd;
+    cudaFuncAttributes fa;
+    int cap = 1024;
+    if (cudaFuncGetAttributes(&fa, k_vjp_gg<T>) == cudaSuccess && fa.numRegs > 0)
+      cap = std::min(cap, std::min(fa.maxThreadsPerBlock, 65536 / fa.numRegs));
+    const int S = std::max(1, std::min(VJP_GG_S, cap / nx));
+    k_vjp_gg<T><<<dim3(P.B, P.nl), dim3(nx, S), sm, s>>>(P, V);
   }
 }
 
