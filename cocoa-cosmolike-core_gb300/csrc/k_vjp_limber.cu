@@ -31,7 +31,6 @@ constexpr int LC = 32;  // multipoles per shared-memory chunk
 constexpr int VJP_GG_S = 4;  // threads per node of the gg sweep
 
 template <typename T> __device__ __forceinline__ T t_exp(T x);
-template <> __device__ __forceinline__ float t_exp<float>(float x) { return expf(x); }
 template <> __device__ __forceinline__ double t_exp<double>(double x) { return exp(x); }
 
 // Walk of one node along l on one lnP table (cosmo3D.c:362-417).
@@ -158,6 +157,43 @@ __device__ __forceinline__ float pw_eval_f(PWalk<float>& w, const AxF& ax, const
   return w.eh * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
 }
 
+// Stateless forms of the walk's evaluation for the chunked sweeps: the cell
+// is the bracketing one (what the walk holds), returned with the in-cell
+// offset for the scatter.  Mixed plan: the split table; FP64 plan: the
+// reference formula in FP64.
+__device__ __forceinline__ float pv_eval_f(const AxF& ax, const float2* __restrict__ tab, int nz, int j, float dyt,
+                                           float uh, float ul, int& cell, float& dx)
+{
+  int lo = 0, hi = ax.nk - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (ax.lk[mid] > uh) hi = mid; else lo = mid;
+  }
+  cell = lo;
+  const float2* r0 = tab + (size_t)lo * nz + j;
+  const float2* r1 = r0 + nz;
+  const float2 a00 = __ldg(r0), a01 = __ldg(r0 + 1), a10 = __ldg(r1), a11 = __ldg(r1 + 1);
+  const float d01 = (a01.x - a00.x) + (a01.y - a00.y);
+  const float d10 = (a10.x - a00.x) + (a10.y - a00.y);
+  const float d11 = ((a11.x - a10.x) + (a11.y - a10.y)) - d01;
+  dx = (__fsub_rn(uh, ax.lk[lo]) + (ul - ax.lkl[lo])) * ax.inv[lo];
+  const float del = a00.y + dyt * d01 + dx * (d10 + dyt * d11);
+  return expf(a00.x) * expf(del) * (float)(1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+__device__ __forceinline__ double pv_eval_d(const double* __restrict__ lkd, const double* __restrict__ inv, int nk,
+                                            const double* __restrict__ tab, int nz, int j, double dy,
+                                            double log10k, int& cell, double& dx)
+{
+  const int i = bsearch_d(lkd, nk, log10k);
+  cell = i;
+  const double* r0 = tab + (size_t)i * nz + j;
+  const double* r1 = r0 + nz;
+  const double a00 = r0[0], a01 = r0[1], a10 = r1[0], a11 = r1[1];
+  dx = (log10k - lkd[i]) * inv[i];
+  const double del = dy * (a01 - a00) + dx * ((a10 - a00) + dy * ((a11 - a10) - (a01 - a00)));
+  return exp(a00) * exp(del) * (1.0 / (CL2PT_COVERH0 * CL2PT_COVERH0 * CL2PT_COVERH0));
+}
+
 __device__ __forceinline__ void load_axis_d(const double* __restrict__ lk, int nk, double* lkd, double* inv)
 {
   for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nk; i += blockDim.x * blockDim.y) {
@@ -186,83 +222,144 @@ __device__ __forceinline__ NodeD node_d(const Params& P, int pt, int idx)
 // ------------------------------------------------------------------ ss
 // C_ss(l) = pref(l) sum_p F w_a w_b P  ->  lnP_bar, xb[pair][p] = sum_l pref C_bar P,
 // then w_bar_i(p) = F sum_{pairs with i} xb w_other.
+// One CTA (SS_NT threads) per point, the multipoles in chunks of LC:
+//   A  P~ = pref P at every (l, node) of the chunk, with its table cell and
+//      in-cell offset (all threads);
+//   B  xb[pair][p] += sum_l C_bar[pair][l] P~[l][p]   (an FP32 GEMM over the
+//      chunk, folded into a two-float (FP32 plan) or FP64 accumulator);
+//   C  g[l][p] = P~ F sum_pair C_bar[pair][l] w_a w_b[pair][p]   (FP32 GEMM);
+//   D  one thread per node scans the chunk in l, summing g over each run of
+//      multipoles in one table cell and flushing it with four FP64 atomics.
+constexpr int SS_NT = 256;
 template <typename T>
-__global__ void k_vjp_ss(Params P, VJPParams V)
+__global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
-  const int p = threadIdx.x;
+  const int tid = threadIdx.x, nth = blockDim.x;
   const int nn = P.n_ss, K = P.nnode_ss, np = P.pss, nk = P.pk_nk;
-  double* lkd = (double*)smem_raw;
-  double* inv = lkd + nk;
-  double* xb = inv + nk;            // [np][nn]
-  T* xt = (T*)(xb + (size_t)np * nn);  // [np][nn] chunk partial sums
-  T* w2 = xt + (size_t)np * nn;     // [np][nn] w_a w_b
-  T* cbs = w2 + (size_t)np * nn;    // [np][LC]
   constexpr bool F32 = sizeof(T) == sizeof(float);
+  double* lkd = (double*)smem_raw;         // [2 nk] FP64 axis (mixed plan: the FP32 axis)
+  double* inv = lkd + nk;
+  double* ndy = inv + nk;                  // [nn] node z offsets
+  double* nlk = ndy + nn;                  // [nn] log10(fK c/H0) (mixed plan: head/tail)
+  double* xb = nlk + nn;                   // [np][nn] (mixed plan: head/tail floats)
+  T* w2 = (T*)(xb + (size_t)np * nn);      // [np][nn] w_a w_b
+  T* cbs = w2 + (size_t)np * nn;           // [np][LC] C_bar of the chunk
+  T* Pt = cbs + (size_t)np * LC;           // [LC][nn] pref P
+  T* G = Pt + (size_t)LC * nn;             // [LC][nn] scatter weight
+  T* dxs = G + (size_t)LC * nn;            // [LC][nn] in-cell offset
+  T* nF = dxs + (size_t)LC * nn;           // [nn] F
+  int* cel = (int*)(nF + nn);              // [LC][nn] table cell
+  int* nj = cel + (size_t)LC * nn;         // [nn] z cell
   AxF axf{};
   if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
   else load_axis_d(P.pk_lk, nk, lkd, inv);
   const double* w = P.wss + (size_t)pt * P.ns * nn;
-  for (int i = p; i < np * nn; i += blockDim.x) {
+  for (int i = tid; i < np * nn; i += nth) {
     const int pr = i / nn, q = i - pr * nn;
     xb[i] = 0.0;
-    xt[i] = (T)0;
     w2[i] = (T)(w[P.z1[pr] * nn + q] * w[P.z2[pr] * nn + q]);
   }
-  const bool act = p < nn;
-  NodeD nd{};
-  if (act) nd = node_d(P, pt, p);
-  const T Ft = (T)nd.F, dyt = (T)nd.dy;
+  for (int i = tid; i < nn; i += nth) {
+    const NodeD nd = node_d(P, pt, i);
+    ndy[i] = nd.dy;
+    nF[i] = (T)nd.F;
+    nj[i] = nd.j;
+    if constexpr (F32) ((float2*)nlk)[i] = split_fx(nd.lfk);
+    else nlk[i] = nd.lfk;
+  }
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
   const float2* tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
-  const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   const int Kx = (P.tatt ? 2 : 1) * K;  // with TATT the rows hold [EE; BB]
   const double* cb = V.cbar_ss + (size_t)pt * np * Kx;
-  PWalk<T> wk;
+  PWalk<T> wk;  // phase D: the run of node tid (tid < nn)
   for (int L0 = 0; L0 < K; L0 += LC) {
     const int nL = min(LC, K - L0);
     __syncthreads();
-    for (int i = p; i < np * LC; i += blockDim.x) {
+    for (int i = tid; i < np * LC; i += nth) {
       const int pr = i / LC, l = i - pr * LC;
       cbs[i] = (l < nL) ? (T)cb[(size_t)pr * Kx + L0 + l] : (T)0;
     }
-    __syncthreads();
-    if (!act) continue;
-    for (int l = 0; l < nL; l++) {
-      const int L = L0 + l;
-      T dx, pc;
-      if constexpr (F32) {
-        const float4 fa = *(const float4*)(V.lfacf_ss + 8 * L);
-        float uh, ul;
-        sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
-        pc = fa.z * pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
-      } else {
-        const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, V.lfac_ss[2 * L] - nd.lfk, bar, dx);
-        pc = (T)V.lfac_ss[2 * L + 1] * Pv;
+    // A
+    for (int e = tid; e < LC * nn; e += nth) {
+      const int l = e / nn, q = e - l * nn;
+      T pv = (T)0, dx = (T)0;
+      int c = -1;
+      if (l < nL) {
+        const int L = L0 + l;
+        if constexpr (F32) {
+          const float4 fa = *(const float4*)(V.lfacf_ss + 8 * L);
+          const float2 lf = ((const float2*)nlk)[q];
+          float uh, ul;
+          sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
+          pv = fa.z * pv_eval_f(axf, tab2, P.pk_nz, nj[q], (float)ndy[q], uh, ul, c, dx);
+        } else {
+          pv = (T)V.lfac_ss[2 * L + 1] *
+               (T)pv_eval_d(lkd, inv, nk, tab, P.pk_nz, nj[q], ndy[q], V.lfac_ss[2 * L] - nlk[q], c, dx);
+        }
       }
-      T pb = 0;
-      for (int pr = 0; pr < np; pr++) {
-        const T cv = cbs[pr * LC + l];
-        pb += cv * w2[pr * nn + p];
-        xt[pr * nn + p] += pc * cv;
-      }
-      pw_acc<T>(wk, pc * Ft * pb, dx);
+      Pt[e] = pv;
+      dxs[e] = dx;
+      cel[e] = c;
     }
-    for (int pr = 0; pr < np; pr++) {
-      xb[pr * nn + p] += (double)xt[pr * nn + p];
-      xt[pr * nn + p] = (T)0;
+    __syncthreads();
+    // B
+    for (int o = tid; o < np * nn; o += nth) {
+      const int pr = o / nn, q = o - pr * nn;
+      T acc = 0;
+      for (int l = 0; l < nL; l++) acc += cbs[pr * LC + l] * Pt[l * nn + q];
+      if constexpr (F32) {
+        float* xh = (float*)(xb + o);
+        float sh, e2;
+        const float a2 = xh[0], b2 = acc;
+        sh = a2 + b2;
+        const float bb = sh - a2;
+        e2 = (a2 - (sh - bb)) + (b2 - bb);
+        xh[0] = sh;
+        xh[1] += e2;
+      } else {
+        xb[o] += acc;
+      }
+    }
+    // C
+    for (int e = tid; e < nL * nn; e += nth) {
+      const int l = e / nn, q = e - l * nn;
+      T pb = 0;
+      for (int pr = 0; pr < np; pr++) pb += cbs[pr * LC + l] * w2[pr * nn + q];
+      G[e] = Pt[e] * nF[q] * pb;
+    }
+    __syncthreads();
+    // D
+    if (tid < nn) {
+      for (int l = 0; l < nL; l++) {
+        const int e = l * nn + tid;
+        if (cel[e] != wk.i) {
+          pw_flush(wk, bar, P.pk_nz, nj[tid], ndy[tid]);
+          wk.i = cel[e];
+        }
+        pw_acc<T>(wk, G[e], dxs[e]);
+      }
     }
   }
-  if (!act) return;
-  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  __syncthreads();
+  if (tid >= nn) return;
+  pw_flush(wk, bar, P.pk_nz, nj[tid], ndy[tid]);
   double* wb = V.wbar_ss + (size_t)pt * P.ns * nn;
+  const double F = (double)nF[tid];
   for (int pr = 0; pr < np; pr++) {
     const int a = P.z1[pr], b = P.z2[pr];
-    const double x = xb[pr * nn + p] * nd.F;
-    wb[a * nn + p] += x * w[b * nn + p];
-    wb[b * nn + p] += x * w[a * nn + p];
+    double xv;
+    if constexpr (F32) {
+      const float* xh = (const float*)(xb + pr * nn + tid);
+      xv = (double)xh[0] + (double)xh[1];
+    } else {
+      xv = xb[pr * nn + tid];
+    }
+    const double x = xv * F;
+    wb[a * nn + tid] += x * w[b * nn + tid];
+    wb[b * nn + tid] += x * w[a * nn + tid];
   }
 }
 
@@ -610,7 +707,8 @@ template <typename T>
 size_t ss_smem(const Params& P)
 {
   const size_t nn = P.n_ss, np = P.pss;
-  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) + 64;
+  return 16 * (size_t)P.pk_nk + 16 * nn + np * nn * (8 + sizeof(T)) + np * LC * sizeof(T) +
+         3 * LC * nn * sizeof(T) + nn * sizeof(T) + (LC * nn + nn) * sizeof(int) + 64;
 }
 template <typename T>
 size_t gs_smem(const Params& P)
@@ -632,7 +730,7 @@ void launch_t(const Params& P, const VJPParams& V, int which, cudaStream_t s)
   if (which == 0) {
     const size_t sm = ss_smem<T>(P);
     cudaFuncSetAttribute(k_vjp_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_vjp_ss<T><<<P.B, ((P.n_ss + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+    k_vjp_ss<T><<<P.B, SS_NT, sm, s>>>(P, V);
   } else if (which == 1) {
     const size_t sm = gs_smem<T>(P);
     cudaFuncSetAttribute(k_vjp_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
