@@ -34,6 +34,8 @@ namespace cl2pt {
 
 namespace {
 
+constexpr int CL2PT_MAX_NTHETA_S = 128;  // angular bins the split transpose stages
+
 // obs_bar and the shear-calibration gradient (add_calib_and_set_mask_X_N,
 // generic_interface.hpp:800-925): xi = obs (1+m_a)(1+m_b);
 // gamma_t = (obs + point mass)(1+m_s) = dv, so d/dm_s = dv / (1+m_s).
@@ -128,6 +130,57 @@ __global__ void k_vjp_contract(Params P, VJPParams V, const double* __restrict__
     if (probe == 2) V.cbar_gg[((size_t)pt * P.nl + pr) * K + k] = acc;
     else V.cbar_w[((size_t)pt * P.nl + pr) * K + k] = acc;
   }
+}
+
+// The same transpose with the split filters (mixed plan): C_bar[col][k] =
+// sum_rows obs_bar[col][row] filter[row][k] as three FP32 products per term
+// (bar_hi f_hi + bar_hi f_lo + bar_lo f_hi; the filter pre-split in [row][k]
+// order, so a warp's reads are coalesced; the column's obs_bar split once
+// per CTA), summed in FP32 over the <= 2 ntheta rows.
+__global__ void k_vjp_contract_s(Params P, VJPParams V, SplitFilter F, int probe, int K)
+{
+  __shared__ float oh[2 * CL2PT_MAX_NTHETA_S], ol[2 * CL2PT_MAX_NTHETA_S];
+  const int npair = (probe == 0) ? P.pss : (probe == 1) ? P.pgs : P.nl;
+  const int col = blockIdx.y;
+  const int pt = col / npair, pr = col - pt * npair;
+  const int nt = P.ntheta;
+  const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
+  const int n_total = n_xi + n_gt + nt * P.nl;
+  const double* ob = V.obs_bar + (size_t)pt * n_total;
+  // the column's obs_bar rows in filter-row order
+  const int M = probe == 0 ? 2 * nt : nt;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    double v;
+    if (probe == 0) v = (m < nt) ? ob[pr * nt + m] : ob[n_xi / 2 + pr * nt + (m - nt)];
+    else if (probe == 1) v = ob[n_xi + pr * nt + m];
+    else v = ob[n_xi + n_gt + pr * nt + m];
+    const float h = (float)v;
+    oh[m] = h;
+    ol[m] = (float)(v - (double)h);
+  }
+  __syncthreads();
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  float acc = 0.0f;
+  for (int m = 0; m < M; m++) {
+    const float fh = __ldg(F.hi + (size_t)m * K + k), fl = __ldg(F.lo + (size_t)m * K + k);
+    acc = fmaf(oh[m], fh, fmaf(oh[m], fl, fmaf(ol[m], fh, acc)));
+  }
+  const double r = acc;
+  if (probe == 0) V.cbar_ss[((size_t)pt * P.pss + pr) * K + k] = r;
+  else if (probe == 1) V.cbar_gs[((size_t)pt * P.pgs + pr) * K + k] = r;
+  else if (probe == 2) V.cbar_gg[((size_t)pt * P.nl + pr) * K + k] = r;
+  else V.cbar_w[((size_t)pt * P.nl + pr) * K + k] = r;
+}
+
+// the transpose contraction of one probe: split FP32 in the mixed plan
+static void vjp_contract(const Params& P, const VJPParams& V, const double* filt, const SplitFilter& F, int probe,
+                         int K, int ncols, cudaStream_t s)
+{
+  if (P.prec == CL2PT_PREC_FP64 || 2 * P.ntheta > 2 * CL2PT_MAX_NTHETA_S)
+    k_vjp_contract<<<dim3((K + 127) / 128, ncols), 128, 0, s>>>(P, V, filt, probe, K);
+  else
+    k_vjp_contract_s<<<dim3((K + 127) / 128, ncols), 128, 0, s>>>(P, V, F, probe, K);
 }
 
 // Adjoint of the non-Limber C_l assembly of one (point, lens bin)
@@ -477,7 +530,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
 }
 
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
-                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
+                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl, const SplitFilter* split,
                 const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk)
 {
   const int nt = P.ntheta;
@@ -493,7 +546,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
   }
   if (P.probes & CL2PT_PROBE_XI) {
     const int Kx = (P.tatt ? 2 : 1) * P.nnode_ss;
-    k_vjp_contract<<<dim3((Kx + 127) / 128, P.B * P.pss), 128, 0, s>>>(P, V, filt_xi, 0, Kx);
+    vjp_contract(P, V, filt_xi, split[0], 0, Kx, P.B * P.pss, s);
     launch_vjp_limber(P, V, 0, s);
     *launches += 2;
     if (P.tatt) {
@@ -502,7 +555,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
     }
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.pgs), 128, 0, s>>>(P, V, filt_gt, 1, P.nnode_g);
+    vjp_contract(P, V, filt_gt, split[1], 1, P.nnode_g, P.B * P.pgs, s);
     launch_vjp_limber(P, V, 1, s);
     *launches += 2;
     if (P.tatt || P.one_loop) {
@@ -512,7 +565,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
     if (P.adopt_limber_gg) {
-      k_vjp_contract<<<dim3((P.nnode_g + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg, 2, P.nnode_g);
+      vjp_contract(P, V, filt_gg, split[2], 2, P.nnode_g, P.B * P.nl, s);
       VJPParams V2 = V;
       V2.ggl_bar = nullptr;
       launch_vjp_limber(P, V2, 2, s);
@@ -523,7 +576,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
       }
     } else {
       const int Kw = P.lmax_nolimber + P.nnode_g;
-      k_vjp_contract<<<dim3((Kw + 127) / 128, P.B * P.nl), 128, 0, s>>>(P, V, filt_gg_nl, 3, Kw);
+      vjp_contract(P, V, filt_gg_nl, split[3], 3, Kw, P.B * P.nl, s);
       k_vjp_handover<<<dim3(P.B, P.nl), 256, 0, s>>>(P, V);
       launch_vjp_limber(P, V, 2, s);
       if (P.one_loop) {

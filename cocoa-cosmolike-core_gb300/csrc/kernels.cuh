@@ -122,7 +122,7 @@ size_t vjp_limber_smem(const Params& P);
 // which: 0 ss, 1 gs, 2 gg (k_vjp_limber.cu)
 void launch_vjp_limber(const Params& P, const VJPParams& V, int which, cudaStream_t s);
 void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const double* filt_xi,
-                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl,
+                const double* filt_gt, const double* filt_gg, const double* filt_gg_nl, const SplitFilter* split,
                 const double* ell_ss, const double* ell_g, cudaStream_t s, int* launches, const Hook& hk);
 // Adjoint of the Fourier vector (k_vjp.cu): Pf is the pass at the caller's
 // multipoles (V.lfac_* hold their factors); Pg, when use_nl, the clustering

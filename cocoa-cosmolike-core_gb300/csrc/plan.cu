@@ -571,6 +571,14 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
         }
       TRY(dupload(p, &p->d_sfilt[f][0], hi.data(), hi.size()));
       TRY(dupload(p, &p->d_sfilt[f][1], lo.data(), lo.size()));
+      std::vector<float> hr((size_t)M * K), lr((size_t)M * K);
+      for (int m = 0; m < M; m++)
+        for (int k = 0; k < K; k++) {
+          hr[(size_t)m * K + k] = hi[(size_t)k * Mp + m];
+          lr[(size_t)m * K + k] = lo[(size_t)k * Mp + m];
+        }
+      TRY(dupload(p, &p->d_sfiltr[f][0], hr.data(), hr.size()));
+      TRY(dupload(p, &p->d_sfiltr[f][1], lr.data(), lr.size()));
       p->sfilt_Mp[f] = Mp;
       p->sfilt_Ksp[f] = Ksp;
     }
@@ -1799,7 +1807,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         cl2pt::VJPParams V;
         const int st2 = vjp_wave(P, w0, V);
         if (st2) return st2;
-        cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl,
+        cl2pt::SplitFilter sfv[4];
+        for (int f = 0; f < 4; f++) sfv[f] = {p->d_sfiltr[f][0], p->d_sfiltr[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};
+        cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, sfv,
                           p->d_ell_ss, p->d_ell_g, s, &launches, hk);
       }
     }

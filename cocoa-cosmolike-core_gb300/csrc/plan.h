@@ -53,6 +53,7 @@ struct cl2pt_plan {
   // the four filters split for the FP32 contraction: head, tail
   // [K rounded up to 32][M rounded up to 4]
   float* d_sfilt[4][2] = {};
+  float* d_sfiltr[4][2] = {};  // the same in [M][K] order (the adjoint's transpose)
   int sfilt_Mp[4] = {}, sfilt_Ksp[4] = {};
   // per-point inputs staged on device when the batch is on the host
   double *d_in_om = nullptr, *d_in_h0 = nullptr, *d_in_chi = nullptr, *d_in_G = nullptr,
