@@ -80,6 +80,11 @@ struct Params {
   // mixed plan: FP32 records of the gg nodes [B][nl][GGN_SLOTS][n_gg]
   // (k_gg_nodes, k_limber.cu)
   float* ggn;
+  // mixed plan, when an adjoint follows (real space): the redshift-space
+  // weight s(l, node) of every gg term the forward sums, 0 where the
+  // chi(a_min) cut drops it [B][nl][n_gg][nnode_g + lmax_nolimber] (C_l
+  // nodes, then l = 0..LNL-1); null otherwise
+  float* s_gg;
   // mixed plan: FP32 (head, tail) of every entry of the wave's tables
   float* lnP2;              // [B][pk_nk*pk_nz][2]
   float* lnPL2;             // [B][pkl_nk*pkl_nz][2]; lnP2 when lnPL is lnP
@@ -128,6 +133,7 @@ struct Params {
 };
 
 enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };
+constexpr int GGN_SLOTS = 15;  // floats per gg node record (k_gg_nodes)
 
 // ---------------------------------------------------------------------
 // FP64 lookups (restating cosmolike/cosmo3D.c and redshift_spline.c)

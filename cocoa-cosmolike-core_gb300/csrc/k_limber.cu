@@ -447,7 +447,6 @@ constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
 // multipole index kept by the chi(a_min) cut on the C_l nodes and on
 // l = 0..LNL-1 (prefixes when the list ascends); 13, 14 the cut's FP64
 // threshold on l + 1/2 (for a list that does not ascend).
-constexpr int GGN_SLOTS = 15;
 __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __restrict__ ell)
 {
   const int pt = blockIdx.x, q = blockIdx.y;
@@ -622,6 +621,9 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   const T cH0 = (T)CL2PT_COVERH0;
   double sum_nl = 0.0, sum_lin = 0.0;
   int hc = -1, hg = -1, hn = -1, hk = -1, hkl = -1;  // mixed plan: cells of the previous node
+  // s(l, node) for the adjoint: this thread's column of the node rows
+  const size_t Ltot = (size_t)P.nnode_g + P.lmax_nolimber;
+  float* sgg = (F32 && P.s_gg && valid) ? P.s_gg + b0 * P.n_gg * Ltot + (mode == 0 ? 0 : P.nnode_g) + L : nullptr;
   const float ilst = (float)(1.0 / nu.lens_stretch[q]);
   for (int p0 = 0; p0 < P.n_gg; p0 += PCH) {
     const int np = min(PCH, P.n_gg - p0);
@@ -675,7 +677,10 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     for (int p = 0; p < np; p++) {
       T fkc, Lw, Mw, r0w;
       if constexpr (F32) {
-        if (cut_idx ? L < lmin[p] : lp < thr[p]) continue;  // (l+3/2)/k beyond chi(a_min)
+        if (cut_idx ? L < lmin[p] : lp < thr[p]) {  // (l+3/2)/k beyond chi(a_min)
+          if (sgg) sgg[(size_t)(p0 + p) * Ltot] = 0.0f;
+          continue;
+        }
         fkc = nf[0 * PCH + p];
         Lw = nf[3 * PCH + p];
         Mw = nf[4 * PCH + p];
@@ -715,6 +720,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
           n1 = (sy[hn] + t * (sbq[hn] + t * (sc[hn] + t * sdq[hn]))) * ilst;
         }
         const float s = Lw + Mw * pref + (c0 * r0w - c1 * n1 * H1 * f1);
+        if (sgg) sgg[(size_t)(p0 + p) * Ltot] = s;
         const float s2w = s * s * nf[1 * PCH + p];
         float uh, ul;
         split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);

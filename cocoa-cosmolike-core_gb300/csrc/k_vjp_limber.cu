@@ -522,11 +522,17 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const int nk = P.pk_nk, nkl = P.pkl_nk;
   const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
   const bool nonlim = V.ggl_bar != nullptr;
+  constexpr bool F32 = sizeof(T) == sizeof(float);
+  // stored: the forward's s(l, node) (mixed plan, real space); the distance,
+  // growth and n(z) tables are then neither loaded nor allocated
+  const bool stored = F32 && P.s_gg != nullptr;
   double* lkd = (double*)smem_raw;
   double* inv = lkd + nk;
   double* lkdl = inv + nk;
   double* invl = lkdl + nkl;
-  T* cx = (T*)(invl + nkl);
+  T* cbs = (T*)(invl + nkl);  // [K] C_bar of this bin
+  T* gbs = cbs + K;           // [LNL][2] integer-l adjoints (non-Limber)
+  T* cx = gbs + 2 * LNL;
   T* cz = cx + nc;
   T* cdn = cz + nc;
   T* cup = cdn + nc;
@@ -536,9 +542,6 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   T* szc = gz + ng;
   T* sy = szc + nzs;
   T* sc = sy + nzs;
-  T* cbs = sc + nzs;       // [K] C_bar of this bin
-  T* gbs = cbs + K;        // [LNL][2] integer-l adjoints (non-Limber)
-  constexpr bool F32 = sizeof(T) == sizeof(float);
   AxF axf{}, axlf{};
   if constexpr (F32) {
     axf = load_axis_fx(P.pk_lk, nk, lkd);
@@ -550,7 +553,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
   const double* Z = P.chi_z;
-  for (int i = tid; i < nc; i += nth) {
+  for (int i = tid; i < nc && !stored; i += nth) {
     cx[i] = (T)Xg[i];
     cz[i] = (T)Z[i];
     if (i + 1 < nc) {
@@ -561,12 +564,12 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       cup[i] = cdn[i] = (T)0;
     }
   }
-  for (int i = tid; i < ng; i += nth) {
+  for (int i = tid; i < ng && !stored; i += nth) {
     gv[i] = (T)Gg[i];
     gz[i] = (T)P.G_z[i];
     gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
   }
-  for (int i = tid; i < nzs; i += nth) {
+  for (int i = tid; i < nzs && !stored; i += nth) {
     szc[i] = (T)P.lens_zc[i];
     sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
     sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
@@ -628,7 +631,12 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   };
   PWalk<T> wk;
   double lbar = 0.0;
-  const int Lk = V.lfac_g_sorted ? first_kept(V.lfac_g, K, nd.fK, chi_amin) : 0;
+  // stored: the row of s for this node and the forward's first kept indices
+  const size_t Ltot = (size_t)K + LNL;
+  const float* sg = stored ? P.s_gg + (b0 * nn + p) * Ltot : nullptr;
+  const float* rec = stored ? P.ggn + b0 * GGN_SLOTS * nn + p : nullptr;
+  const int Lk = stored ? __float_as_int(rec[(size_t)11 * nn])
+                        : (V.lfac_g_sorted ? first_kept(V.lfac_g, K, nd.fK, chi_amin) : 0);
   const int cs = (K - Lk + S - 1) / S;
   const int La = min(K, Lk + sub * cs), Lb = min(K, Lk + (sub + 1) * cs);
   for (int L0 = La; L0 < Lb; L0 += LC) {
@@ -641,8 +649,13 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       if (cv == (T)0) continue;
       T dx, s, Pv;
       if constexpr (F32) {
-        const float4 fa = *(const float4*)(V.lfacf_g + 8 * L), fb = *(const float4*)(V.lfacf_g + 8 * L + 4);
-        s = s_of(fa.w, fb.x, fb.y, fb.z);
+        const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
+        if (stored) {
+          s = sg[L];
+        } else {
+          const float4 fb = *(const float4*)(V.lfacf_g + 8 * L + 4);
+          s = s_of(fa.w, fb.x, fb.y, fb.z);
+        }
         float uh, ul;
         sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
         Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
@@ -669,7 +682,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
     T lt = 0;
-    const int Li = first_kept(V.lfac_gi, LNL, nd.fK, chi_amin);
+    const int Li = stored ? __float_as_int(rec[(size_t)12 * nn]) : first_kept(V.lfac_gi, LNL, nd.fK, chi_amin);
     const int ci = (LNL - Li + S - 1) / S;
     const int Ia = min(LNL, Li + sub * ci), Ib = min(LNL, Li + (sub + 1) * ci);
     for (int L = Ia; L < Ib; L++) {
@@ -677,8 +690,13 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       if (cn == (T)0 && cl == (T)0) continue;
       T dx, dxl, s, Pn, Pl;
       if constexpr (F32) {
-        const float4 fa = *(const float4*)(V.lfacf_gi + 8 * L), fb = *(const float4*)(V.lfacf_gi + 8 * L + 4);
-        s = s_of(fa.w, fb.x, fb.y, fb.z);
+        const float4 fa = *(const float4*)(V.lfacf_gi + 8 * L);
+        if (stored) {
+          s = sg[K + L];
+        } else {
+          const float4 fb = *(const float4*)(V.lfacf_gi + 8 * L + 4);
+          s = s_of(fa.w, fb.x, fb.y, fb.z);
+        }
         float uh, ul;
         sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
         Pn = pw_eval_f(wn, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
@@ -719,8 +737,9 @@ size_t gs_smem(const Params& P)
 template <typename T>
 size_t gg_smem(const Params& P)
 {
-  return 16 * ((size_t)P.pk_nk + P.pkl_nk) +
-         sizeof(T) * (4 * (size_t)P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz + P.nnode_g + 2 * P.lmax_nolimber) + 64;
+  const bool stored = sizeof(T) == sizeof(float) && P.s_gg != nullptr;
+  return 16 * ((size_t)P.pk_nk + P.pkl_nk) + sizeof(T) * ((size_t)P.nnode_g + 2 * P.lmax_nolimber) +
+         (stored ? 0 : sizeof(T) * (4 * (size_t)P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz)) + 64;
 }
 
 template <typename T>

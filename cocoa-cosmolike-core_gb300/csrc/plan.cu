@@ -1015,6 +1015,17 @@ static int vjp_prepare(cl2pt_plan* p)
       a = dalloc(p, &p->d_vjp_lnpl, (size_t)p->max_batch * p->P.pkl_nk * p->P.pkl_nz);
     if (!a) a = dalloc(p, &p->d_lfac_f, 8 * (size_t)std::max(p->nnode_ss, p->nnode_g));
     if (!a) a = dalloc(p, &p->d_vjp_ws, nws);
+    if (!a && p->P.prec != CL2PT_PREC_FP64 && (p->cfg.probes & CL2PT_PROBE_WTHETA)) {
+      // optional: without it the adjoint recomputes s(l, node)
+      float* sg = nullptr;
+      const size_t n = (size_t)p->wave * p->cfg.n_lens * p->n_gg * (p->nnode_g + p->cfg.lmax_nolimber);
+      if (cudaMalloc(&sg, n * sizeof(float)) == cudaSuccess) {
+        p->dbufs.push_back(sg);
+        p->d_sgg = sg;
+      } else {
+        cudaGetLastError();
+      }
+    }
     if (a) {
       p->d_vjp_ws = nullptr;
       return a;
@@ -1762,6 +1773,8 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                                   p->d_lfac_g, p->d_lfacf_g, s, &launches);
       }
     } else {
+      // the forward keeps s(l, node) of its gg terms for the adjoint
+      if (vr) P.s_gg = p->d_sgg;
       const bool nlw = (P.probes & CL2PT_PROBE_WTHETA) && !P.adopt_limber_gg;
       if (nlw) {
         // the FFTLog transforms and direct Gamma kernels (FP64-pipe bound,

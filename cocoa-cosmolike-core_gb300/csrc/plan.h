@@ -101,6 +101,7 @@ struct cl2pt_plan {
   float* d_lfacf_g = nullptr;
   float* d_lfacf_f = nullptr;
   int ell_f_sorted = 1;                // the last caller multipole list ascends
+  float* d_sgg = nullptr;              // s(l, node) of the gg terms for the adjoint (mixed plan)
   double* d_chi2 = nullptr;            // [max_batch] chi^2 staging
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
