@@ -509,45 +509,86 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   // int [2][PCH], then T arrays: P axes, distance table (chi, z, and the
   // per-cell slopes chi_all interpolates), growth table (value, slope, z),
   // n(z) spline of bin q.
+  constexpr bool F32 = sizeof(T) == sizeof(float);
   double* nd = (double*)smem_raw;
   double* thr = nd + 8 * PCH;  // [PCH] per-node l+1/2 threshold of the chi(a_min) cut
-  double* sd = thr + PCH;
-  double* si = sd + pd.nk;
-  double* sdl = si + pd.nk;
-  double* sil = sdl + pl.nk;
-  int* nj = (int*)(sil + pl.nk);
-  T* lk = (T*)(nj + 2 * PCH);
-  T* lkl = lk + pd.nk;
-  T* cx = lkl + pl.nk;   // chi (Mpc/h)
-  T* cz = cx + nc;       // z
-  T* cdn = cz + nc;      // chi_all 'down' slope of cell j (dchi/dz)
-  T* cup = cdn + nc;     // chi_all 'up' slope of cell j
-  T* gv = cup + nc;      // growth G
-  T* gs = gv + ng;       // growth slope of cell j
-  T* gz = gs + ng;       // growth z axis (when it differs from the distance axis)
-  T* szc = gz + ng;      // n(z) spline nodes, values, coefficients of bin q
-  T* sy = szc + nzs;
-  T* sc = sy + nzs;
-  // mixed plan: reciprocal chi-cell widths and the n(z) spline's b, d per
-  // interval
-  T* icx = sc + nzs;
-  T* sbq = icx + nc;
-  T* sdq = sbq + nzs;
+  double *sd = nullptr, *si = nullptr, *sdl = nullptr, *sil = nullptr;
+  int* nj;
+  T *lk, *lkl = nullptr, *cx, *cz, *cdn, *cup, *gv, *gs, *gz, *szc, *sy, *sc;
+  T *icx = nullptr, *sbq = nullptr, *sdq = nullptr;
+  float *lkt = nullptr, *lki = nullptr, *lklt = nullptr, *lkli = nullptr;
+  if constexpr (F32) {
+    // mixed plan, compact (gg_smem): FP32 axes (head, tail, 1/width) of
+    // lnP and, in the integer-l pass only, of lnP_lin; the growth z axis
+    // only when it differs from the distance one; reciprocal chi-cell
+    // widths and the n(z) spline's b, d per interval
+    nj = (int*)(thr + PCH);
+    float* f = (float*)(nj + 2 * PCH);
+    lk = f;
+    lkt = f + pd.nk;
+    lki = f + 2 * pd.nk;
+    f += 3 * pd.nk;
+    if (mode == 1) {
+      lkl = f;
+      lklt = f + pl.nk;
+      lkli = f + 2 * pl.nk;
+      f += 3 * pl.nk;
+    }
+    cx = f;
+    cz = cx + nc;
+    cdn = cz + nc;
+    cup = cdn + nc;
+    icx = cup + nc;
+    gv = icx + nc;
+    gs = gv + ng;
+    f = gs + ng;
+    if (same_axis) {
+      gz = cz;
+    } else {
+      gz = f;
+      f += ng;
+    }
+    szc = f;
+    sy = szc + nzs;
+    sc = sy + nzs;
+    sbq = sc + nzs;
+    sdq = sbq + nzs;
+  } else {
+    // shared: node data [8][PCH], FP64 axes + inverse widths of both P
+    // tables, int [2][PCH], then T arrays: P axes, distance table (chi, z,
+    // and the per-cell slopes chi_all interpolates), growth table (value,
+    // slope, z), n(z) spline of bin q
+    sd = thr + PCH;
+    si = sd + pd.nk;
+    sdl = si + pd.nk;
+    sil = sdl + pl.nk;
+    nj = (int*)(sil + pl.nk);
+    lk = (T*)(nj + 2 * PCH);
+    lkl = lk + pd.nk;
+    cx = lkl + pl.nk;   // chi (Mpc/h)
+    cz = cx + nc;       // z
+    cdn = cz + nc;      // chi_all 'down' slope of cell j (dchi/dz)
+    cup = cdn + nc;     // chi_all 'up' slope of cell j
+    gv = cup + nc;      // growth G
+    gs = gv + ng;       // growth slope of cell j
+    gz = gs + ng;       // growth z axis (when it differs from the distance axis)
+    szc = gz + ng;      // n(z) spline nodes, values, coefficients of bin q
+    sy = szc + nzs;
+    sc = sy + nzs;
+  }
   const double* Xg = P.chi + (size_t)pt * P.chi_nz;
   const double* Gg = P.G + (size_t)pt * P.G_nz;
-  constexpr bool F32 = sizeof(T) == sizeof(float);
   // mixed plan: the node data as floats [9][PCH] where the FP64 node data
   // was (fK c/H0, weight, z offset in lnP, L, M, r0, z offset in lnPL,
-  // log10(fK c/H0) head and tail), the first kept multipole index of each
-  // node where the thresholds were, axis tails and widths as floats where
-  // the FP64 axes were
+  // log10(fK c/H0) head and tail), then the first kept multipole index of
+  // each node
   float* nf = (float*)nd;
   int* lmin = (int*)(nf + 9 * PCH);
   Axis<T> ax{}, axl{};
   AxisF axf{}, axlf{};
   if constexpr (F32) {
-    axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
-    axlf = load_axis_f(pl.lk, pl.nk, (float*)lkl, (float*)sdl, (float*)sdl + pl.nk);
+    axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
+    if (mode == 1) axlf = load_axis_f(pl.lk, pl.nk, (float*)lkl, lklt, lkli);
   } else {
     ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
     axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
@@ -568,7 +609,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   }
   for (int i = tid; i < ng; i += LTG) {
     gv[i] = (T)Gg[i];
-    gz[i] = (T)P.G_z[i];
+    if (!F32 || !same_axis) gz[i] = (T)P.G_z[i];
     gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
   }
   for (int i = tid; i < nzs; i += LTG) {
@@ -778,6 +819,18 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   }
 }
 
+// shared memory of k_limber_gg (the kernel's two layouts)
+template <typename T>
+static size_t gg_smem(const Params& P, int mode)
+{
+  if (sizeof(T) == sizeof(float))
+    return sizeof(double) * 9 * PCH + sizeof(int) * 2 * PCH +
+           sizeof(float) * (3 * (size_t)P.pk_nk + (mode == 1 ? 3 * (size_t)P.pkl_nk : 0) + 5 * (size_t)P.chi_nz +
+                            (P.G_same_axis ? 2 : 3) * (size_t)P.G_nz + 5 * (size_t)P.lens_nz) + 64;
+  return sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
+         sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;
+}
+
 template <typename T>
 static void launch_limber_t(const Params& P, const double* ell_ss, const double* ell_g,
                             cudaStream_t s, int* launches, const Hook& hk)
@@ -805,9 +858,8 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
-    const size_t sm = sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
-                      sizeof(T) * (P.pk_nk + P.pkl_nk + 5 * P.chi_nz + 3 * P.G_nz + 5 * P.lens_nz) + 64;
-    cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = gg_smem<T>(P, 0), sm1 = gg_smem<T>(P, 1);
+    cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(sm, sm1));
     if (sizeof(T) == sizeof(float)) {
       k_gg_nodes<<<dim3(P.B, P.nl), 128, 0, s>>>(P, ell_g);
       (*launches)++;
@@ -820,7 +872,7 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     if (!P.adopt_limber_gg) {
       dim3 g2(P.B, (P.lmax_nolimber + LTG - 1) / LTG, P.nl);
       hk(CL2PT_K_LIMBER_GGL, 1);
-      k_limber_gg<T><<<g2, LTG, sm, s>>>(P, ell_g, 1);
+      k_limber_gg<T><<<g2, LTG, sm1, s>>>(P, ell_g, 1);
       hk(CL2PT_K_LIMBER_GGL, 0);
       (*launches)++;
     }
