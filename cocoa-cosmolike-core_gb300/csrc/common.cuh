@@ -85,6 +85,14 @@ struct Params {
   // chi(a_min) cut drops it [B][nl][n_gg][nnode_g + lmax_nolimber] (C_l
   // nodes, then l = 0..LNL-1); null otherwise
   float* s_gg;
+  // mixed plan: FP32 records of the ss node set and of each lens bin's gs
+  // node set [B][1 + nl][4][n_ss] (log10(fK c/H0) head and tail, z offset in
+  // lnP, z cell) and their Limber weights: ss [B][n_ss][pss rounded up to
+  // 8] (pair-minor), gs [B][nl][2][CL2PT_MAXB][n_ss] (lens L and M terms,
+  // pairs of the bin) (k_ls_nodes, k_limber.cu)
+  float* lsn;
+  float* ssx;
+  float* gsx;
   // mixed plan: FP32 (head, tail) of every entry of the wave's tables
   float* lnP2;              // [B][pk_nk*pk_nz][2]
   float* lnPL2;             // [B][pkl_nk*pkl_nz][2]; lnP2 when lnPL is lnP

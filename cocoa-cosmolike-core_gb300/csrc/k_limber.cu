@@ -225,6 +225,59 @@ __device__ __forceinline__ PdeltaTable pdelta_table(const Params& P, int pt, boo
   return t;
 }
 
+// Mixed plan: the ss and gs node data every multipole tile reads, formed
+// once in FP64 per point (ss set, blockIdx.y = 0) and per (point, lens bin)
+// (gs set of bin q, blockIdx.y = 1 + q) and stored as FP32 records and
+// weights (Params::lsn, ssx, gsx) instead of in every tile.
+__global__ void __launch_bounds__(128) k_ls_nodes(Params P)
+{
+  const int pt = blockIdx.x, set = blockIdx.y, q = set - 1;
+  const int nn = P.n_ss;
+  const int off = set == 0 ? 0 : P.n_ss + q * P.n_ss;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const int* nodej = P.node_j + (size_t)pt * P.node_stride;
+  float* rec = P.lsn + ((size_t)pt * (1 + P.nl) + set) * 4 * nn;
+  for (int p = threadIdx.x; p < nn; p += blockDim.x) {
+    const float2 lf = split_f(log10(node[(size_t)NF_FK * P.node_stride + off + p] * CL2PT_COVERH0));
+    rec[p] = lf.x;
+    rec[nn + p] = lf.y;
+    rec[2 * nn + p] = (float)node[(size_t)NF_DYZ * P.node_stride + off + p];
+    rec[3 * nn + p] = __int_as_float(nodej[off + p]);
+  }
+  auto fw = [&](int p) {
+    const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+    return node[(size_t)NF_WT * P.node_stride + off + p] * node[(size_t)NF_DCHIDA * P.node_stride + off + p] /
+           (fK * fK);
+  };
+  if (set == 0) {
+    const int PP = (P.pss + 7) & ~7;
+    const double* w = P.wss + (size_t)pt * P.ns * nn;
+    float* x = P.ssx + (size_t)pt * nn * PP;
+    for (int i = threadIdx.x; i < nn * PP; i += blockDim.x) {
+      const int p = i / PP, pr = i - p * PP;
+      x[i] = pr < P.pss ? (float)(fw(p) * w[P.z1[pr] * nn + p] * w[P.z2[pr] * nn + p]) : 0.0f;
+    }
+  } else {
+    const size_t b0 = (size_t)pt * P.nl + q;
+    const double* wx = P.wgs_x + b0 * P.ns * nn;
+    const double* wl = P.wgs_l + b0 * nn;
+    const double* wm = P.wgs_m + b0 * nn;
+    float* x = P.gsx + b0 * 2 * CL2PT_MAXB * nn;
+    // the pairs of bin q in the order k_limber_gs numbers them
+    int m = 0;
+    for (int k = 0; k < P.pgs; k++) {
+      if (P.zl[k] != q) continue;
+      const int zs = P.zs[k];
+      for (int p = threadIdx.x; p < nn; p += blockDim.x) {
+        const double f = fw(p) * wx[zs * nn + p];
+        x[(size_t)(0 * CL2PT_MAXB + m) * nn + p] = (float)(f * wl[p]);
+        x[(size_t)(1 * CL2PT_MAXB + m) * nn + p] = (float)(f * wm[p]);
+      }
+      m++;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- ss
 template <typename T>
 __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __restrict__ ell)
@@ -234,21 +287,38 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   const int tid = threadIdx.x;
   const int L = blockIdx.y * LT + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
-  double* sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
-  double* si = sd + pd.nk;
-  double* nlc = si + pd.nk;
-  T* lk = (T*)(nlc + PCH);
-  T* Ps = lk + pd.nk;
-  T* X = Ps + PCH * LT;
-  T* ndy = X + (size_t)P.pss * PCH;
-  int* nj = (int*)(ndy + PCH);
   constexpr bool F32 = sizeof(T) == sizeof(float);
-  // mixed plan: axis tails and widths as floats where the FP64 axis was,
-  // node log10 chi as head/tail pairs
+  const int PP = (P.pss + 7) & ~7;  // mixed plan: pairs padded to 8 (weights pair-minor)
+  double *sd, *si = nullptr, *nlc;
+  T *lk, *Ps, *X, *ndy;
+  int* nj;
+  float *lkt = nullptr, *lki = nullptr;
+  if constexpr (F32) {
+    // node log10 chi (head, tail), z offsets and cells, the FP32 axis
+    // (head, tail, 1/width), P~ [PCH][LT], weights [PCH][PP]
+    nlc = (double*)smem_raw;
+    sd = nlc;
+    ndy = (T*)(nlc + PCH);
+    nj = (int*)(ndy + PCH);
+    lk = (T*)(nj + PCH);
+    lkt = (float*)lk + pd.nk;
+    lki = lkt + pd.nk;
+    Ps = (T*)(((uintptr_t)(lki + pd.nk) + 15) & ~(uintptr_t)15);  // 16-byte rows for the float4 reads
+    X = Ps + PCH * LT;
+  } else {
+    sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
+    si = sd + pd.nk;
+    nlc = si + pd.nk;
+    lk = (T*)(nlc + PCH);
+    Ps = lk + pd.nk;
+    X = Ps + PCH * LT;
+    ndy = X + (size_t)P.pss * PCH;
+    nj = (int*)(ndy + PCH);
+  }
   Axis<T> ax{};
   AxisF axf{};
   float2* nlc2 = (float2*)nlc;
-  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
+  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
   else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
@@ -268,17 +338,28 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     pref = (T)(l * (l - 1.) * (l + 1.) * (l + 2.) / (lp * lp * lp * lp));
   }
   double* out = P.tab_ss + (size_t)pt * P.pss * P.nnode_ss;
+  int hk = -1;  // mixed plan: the k cell of the previous node
   for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
-    for (int p = tid; p < np; p += LT) {
+    if constexpr (F32) {
+      // the node records and weights of k_ls_nodes
+      const float* rec = P.lsn + (size_t)pt * (1 + P.nl) * 4 * P.n_ss + p0;
+      for (int p = tid; p < np; p += LT) {
+        nlc2[p] = make_float2(rec[p], rec[P.n_ss + p]);
+        ndy[p] = rec[2 * P.n_ss + p];
+        nj[p] = __float_as_int(rec[3 * P.n_ss + p]);
+      }
+      const float* xs = P.ssx + ((size_t)pt * P.n_ss + p0) * PP;
+      for (int i = tid; i < np * PP; i += LT) X[i] = xs[i];
+    }
+    for (int p = tid; p < np && !F32; p += LT) {
       const double v = log10(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
-      if constexpr (F32) nlc2[p] = split_f(v);
-      else nlc[p] = v;
+      nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + p0 + p];
       nj[p] = nodej[p0 + p];
     }
-    for (int idx = tid; idx < P.pss * np; idx += LT) {
+    for (int idx = tid; idx < P.pss * np && !F32; idx += LT) {
       const int pair = idx / np, p = idx - pair * np;
       const double fK = node[(size_t)NF_FK * P.node_stride + p0 + p];
       const double dch = node[(size_t)NF_DCHIDA * P.node_stride + p0 + p];
@@ -292,8 +373,30 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
       for (int p = 0; p < np; p++) {
         float uh, ul;
         split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
-        Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
+        Ps[p * LT + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
       }
+      // the pair contraction, 8 pairs per pass held in registers
+      for (int g = 0; g < PP; g += 8) {
+        float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int p = 0; p < np; p++) {
+          const float ps = Ps[p * LT + tid];
+          const float4 xa = *(const float4*)&X[p * PP + g], xb = *(const float4*)&X[p * PP + g + 4];
+          a[0] += xa.x * ps;
+          a[1] += xa.y * ps;
+          a[2] += xa.z * ps;
+          a[3] += xa.w * ps;
+          a[4] += xb.x * ps;
+          a[5] += xb.y * ps;
+          a[6] += xb.z * ps;
+          a[7] += xb.w * ps;
+        }
+        for (int c = 0; c < 8 && g + c < P.pss; c++) {
+          const double v = (double)(pref * a[c]);
+          double* o = out + (size_t)(g + c) * P.nnode_ss + L;
+          *o = (p0 == 0) ? v : *o + v;
+        }
+      }
+      continue;
     } else {
       const double llp = log10(lp);
       for (int p = 0; p < np; p++)
@@ -333,19 +436,37 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   __syncthreads();
   const int np_ = npair;
   const int nterm = use_m ? 2 : 1;
-  double* sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
-  double* si = sd + pd.nk;
-  double* nlc = si + pd.nk;
-  T* lk = (T*)(nlc + PCH);
-  T* Ps = lk + pd.nk;
-  T* X = Ps + PCH * LT;                  // [nterm][npair][PCH]
-  T* ndy = X + (size_t)2 * CL2PT_MAXB * PCH;
-  int* nj = (int*)(ndy + PCH);
   constexpr bool F32 = sizeof(T) == sizeof(float);
+  double *sd, *si = nullptr, *nlc;
+  T *lk, *Ps, *X, *ndy;
+  int* nj;
+  float *lkt = nullptr, *lki = nullptr;
+  if constexpr (F32) {
+    // node records, the FP32 axis (head, tail, 1/width), P [PCH][LT],
+    // weights [2][MAXB][PCH]
+    nlc = (double*)smem_raw;
+    sd = nlc;
+    ndy = (T*)(nlc + PCH);
+    nj = (int*)(ndy + PCH);
+    lk = (T*)(nj + PCH);
+    lkt = (float*)lk + pd.nk;
+    lki = lkt + pd.nk;
+    Ps = (T*)(lki + pd.nk);
+    X = Ps + PCH * LT;
+  } else {
+    sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
+    si = sd + pd.nk;
+    nlc = si + pd.nk;
+    lk = (T*)(nlc + PCH);
+    Ps = lk + pd.nk;
+    X = Ps + PCH * LT;                  // [nterm][npair][PCH]
+    ndy = X + (size_t)2 * CL2PT_MAXB * PCH;
+    nj = (int*)(ndy + PCH);
+  }
   Axis<T> ax{};
   AxisF axf{};
   float2* nlc2 = (float2*)nlc;
-  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, (float*)sd, (float*)sd + pd.nk);
+  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
   else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const int off = P.n_ss + q * P.n_ss;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
@@ -371,17 +492,33 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     pref = (T)(l * (l + 1.) / (lp * lp));
   }
   double* out = P.tab_gs + (size_t)pt * P.pgs * P.nnode_g;
+  int hk = -1;  // mixed plan: the k cell of the previous node
   for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
     const int np = min(PCH, P.n_ss - p0);
     __syncthreads();
-    for (int p = tid; p < np; p += LT) {
+    if constexpr (F32) {
+      // the node records and weights of k_ls_nodes
+      const float* rec = P.lsn + ((size_t)pt * (1 + P.nl) + 1 + q) * 4 * P.n_ss + p0;
+      for (int p = tid; p < np; p += LT) {
+        nlc2[p] = make_float2(rec[p], rec[P.n_ss + p]);
+        ndy[p] = rec[2 * P.n_ss + p];
+        nj[p] = __float_as_int(rec[3 * P.n_ss + p]);
+      }
+      const float* xs = P.gsx + b0 * 2 * CL2PT_MAXB * P.n_ss + p0;
+      for (int idx = tid; idx < nterm * np_ * np; idx += LT) {
+        const int t = idx / (np_ * np);
+        const int r = idx - t * np_ * np;
+        const int m = r / np, p = r - m * np;
+        X[(t * CL2PT_MAXB + m) * PCH + p] = xs[(size_t)(t * CL2PT_MAXB + m) * P.n_ss + p];
+      }
+    }
+    for (int p = tid; p < np && !F32; p += LT) {
       const double v = log10(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
-      if constexpr (F32) nlc2[p] = split_f(v);
-      else nlc[p] = v;
+      nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
       nj[p] = nodej[off + p0 + p];
     }
-    for (int idx = tid; idx < nterm * np_ * np; idx += LT) {
+    for (int idx = tid; idx < nterm * np_ * np && !F32; idx += LT) {
       const int t = idx / (np_ * np);
       const int r = idx - t * np_ * np;
       const int m = r / np, p = r - m * np;
@@ -398,7 +535,7 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
       for (int p = 0; p < np; p++) {
         float uh, ul;
         split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
-        Ps[p * LT + tid] = pk_eval_f(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p]);
+        Ps[p * LT + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
       }
     } else {
       const double llp = log10(lp);
@@ -835,10 +972,18 @@ template <typename T>
 static void launch_limber_t(const Params& P, const double* ell_ss, const double* ell_g,
                             cudaStream_t s, int* launches, const Hook& hk)
 {
+  const bool f32 = sizeof(T) == sizeof(float);
+  if (f32 && (P.probes & (CL2PT_PROBE_XI | CL2PT_PROBE_GAMMAT))) {
+    k_ls_nodes<<<dim3(P.B, 1 + P.nl), 128, 0, s>>>(P);
+    (*launches)++;
+  }
+  // mixed plan: node records + FP32 axis + P~ + weights (ss: [PCH][pss
+  // rounded to 8]; gs: [2][MAXB][PCH]), 16 bytes of alignment slack
+  const size_t sm_f32 = sizeof(double) * PCH + 8 * PCH + 12 * (size_t)P.pk_nk + 4 * PCH * LT + 16;
   if (P.probes & CL2PT_PROBE_XI) {
-    const size_t sm = sizeof(double) * (2 * P.pk_nk + PCH) +
-                      sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + PCH) +
-                      sizeof(int) * PCH + 64;
+    const size_t sm = f32 ? sm_f32 + 4 * (size_t)PCH * ((P.pss + 7) & ~7)
+                          : sizeof(double) * (2 * P.pk_nk + PCH) +
+                                sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + PCH) + sizeof(int) * PCH + 64;
     cudaFuncSetAttribute(k_limber_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_ss + LT - 1) / LT);
     hk(CL2PT_K_LIMBER_SS, 1);
@@ -847,9 +992,10 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    const size_t sm = sizeof(double) * (2 * P.pk_nk + PCH) +
-                      sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + PCH) +
-                      sizeof(int) * PCH + 64;
+    const size_t sm = f32 ? sm_f32 + 4 * (size_t)2 * CL2PT_MAXB * PCH
+                          : sizeof(double) * (2 * P.pk_nk + PCH) +
+                                sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + PCH) +
+                                sizeof(int) * PCH + 64;
     cudaFuncSetAttribute(k_limber_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
     hk(CL2PT_K_LIMBER_GS, 1);

@@ -661,7 +661,12 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g)));
-  if (precision != CL2PT_PREC_FP64) TRY(dalloc(p, &P.ggn, (size_t)W * nl * 15 * std::max(p->n_gg, 1)));
+  if (precision != CL2PT_PREC_FP64) {
+    TRY(dalloc(p, &P.ggn, (size_t)W * nl * cl2pt::GGN_SLOTS * std::max(p->n_gg, 1)));
+    TRY(dalloc(p, &P.lsn, (size_t)W * (1 + nl) * 4 * p->n_ss));
+    TRY(dalloc(p, &P.ssx, (size_t)W * p->n_ss * ((p->pss + 7) & ~7)));
+    TRY(dalloc(p, &P.gsx, (size_t)W * std::max(nl, 1) * 2 * CL2PT_MAXB * p->n_ss));
+  }
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
   if (precision != CL2PT_PREC_FP64) {
