@@ -144,8 +144,9 @@ __device__ __forceinline__ cd gl_ratio(int deriv, double nu, double eta, int k)
 constexpr int NL_NT = 256;
 // threads per CTA of the multipole loop: its transforms (900-3000 points)
 // give each thread a few entries per Stockham stage between barriers, so
-// smaller CTAs, four per SM, keep more independent work in flight
-constexpr int NL_LT = 128;
+// 128-thread CTAs, four per SM, keep more independent work in flight when
+// four fit the SM's shared memory; 256 otherwise (two per SM)
+static int nl_loop_threads(size_t smem) { return smem + 1024 <= 228 * 1024 / 4 ? 128 : 256; }
 
 // One Stockham transform of size N (factors fac[0..nf-1]) on in/out
 // (shared), twiddles tw[k] = exp(+2 pi i k / N); sign -1 = forward.
@@ -578,14 +579,14 @@ __device__ __forceinline__ ct<float> phase_f(int m, float2 th)
 // the b1-free galaxy term G0 of both multipoles, and accumulates the P_lin
 // slice adjoint and d/db1 from cbar = dL/dC_l instead of writing C_l.
 template <typename T, bool ADJ>
-__global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
+__global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
                                                       double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // (point, bin) of this CTA from the longest-first dispatch order
   const int item = Q.perm[blockIdx.y * gridDim.x + blockIdx.x];
   const int pt = item / P.nl, q = item - (item / P.nl) * P.nl;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, nlt = blockDim.x;  // 128 or 256 (nl_loop_threads)
   const int nchi = P.nl_nchi;
   const int LNL = P.lmax_nolimber;
   const cl2pt_nuisance& nu = P.nu[pt];
@@ -615,7 +616,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
   double* pinv = plkd + P.pkl_nk;
   double* lxk = pinv + P.pkl_nk;
   double* pbard = lxk + nchi;
-  __shared__ double red[2][NL_LT / 32];
+  __shared__ double red[2][NL_NT / 32];
   const size_t cta = (size_t)pt * P.nl + q;
   const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
   ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;              // [3][2][hstride]
@@ -628,7 +629,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
   {
     const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
     const double dy = dyz;
-    for (int i = tid; i < P.pkl_nk; i += NL_LT) {
+    for (int i = tid; i < P.pkl_nk; i += nlt) {
       if (ADJ) {
         if (F32) pbarf[i] = 0.0f;
         else pbard[i] = 0.0;
@@ -642,7 +643,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
     }
     if constexpr (F32) {
       __syncthreads();
-      for (int i = tid; i < P.pkl_nk; i += NL_LT) {
+      for (int i = tid; i < P.pkl_nk; i += nlt) {
         const float h = (float)psl[i];
         pcf[3 * i] = h;
         pcf[3 * i + 1] = (float)(psl[i] - (double)h);
@@ -654,7 +655,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
   }
   // x and log10(rc / (x coverH0)) at the reversed index nchi-1-i
   // (y = (l+1)/x[nchi-1-i])
-  for (int i = tid; i < nchi; i += NL_LT) {
+  for (int i = tid; i < nchi; i += nlt) {
     const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
     if (F32) lxkf[i] = (float)log10(rc / (xr * CL2PT_COVERH0));
     else lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
@@ -693,7 +694,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
       const int k2 = k + 1;
       const bool two = k2 < ke;
       __syncthreads();
-      for (int i = tid; i < nchi; i += NL_LT) F0[i] = F1[i] = (T)0;
+      for (int i = tid; i < nchi; i += nlt) F0[i] = F1[i] = (T)0;
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
@@ -704,12 +705,12 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         double lnb0 = 0.0, lnb1 = 0.0;
         if constexpr (F32) {
           // one thread reduces the two phase increments theta = deta lnbase
-          // and forms the NL_LT-entry step phasors (FP64), shared below
+          // and forms the blockDim-entry step phasors (FP64), shared below
           if (tid == 0) {
             const double t0 = deta * (lnbj + Q.lnk1[k]), t1 = deta * (lnbj + Q.lnk1[two ? k2 : k]);
             sph[0] = red_angle(t0);
             sph[1] = red_angle(t1);
-            const ct<T> a0 = phasor<T>(-(double)NL_LT * t0), a1 = phasor<T>(-(double)NL_LT * t1);
+            const ct<T> a0 = phasor<T>(-(double)nlt * t0), a1 = phasor<T>(-(double)nlt * t1);
             sph[2] = make_float2(a0.x, a0.y);
             sph[3] = make_float2(a1.x, a1.y);
           }
@@ -728,7 +729,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         const double* gd1 = gdir + ((size_t)j * Q.ndirect + (dir1 ? di0 + 1 : 0)) * Q.hstride * 2;
         // phases exp(-i eta_i lnbase): the first entry of this thread from an
         // FP64-reduced angle, then the FP32 (FP64 plan: FP64) step to the
-        // thread's next entry, i += NL_LT
+        // thread's next entry, i += nlt
         ct<T> e0, e1, s0, s1;
         if constexpr (F32) {
           e0 = phase_f(tid, sph[0]);
@@ -738,10 +739,10 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         } else {
           e0 = phasor<T>(-(deta * tid) * lnb0);
           e1 = phasor<T>(-(deta * tid) * lnb1);
-          s0 = phasor<T>(-(deta * NL_LT) * lnb0);
-          s1 = phasor<T>(-(deta * NL_LT) * lnb1);
+          s0 = phasor<T>(-(deta * nlt) * lnb0);
+          s1 = phasor<T>(-(deta * nlt) * lnb1);
         }
-        for (int i = tid; i < nq; i += NL_LT) {
+        for (int i = tid; i < nq; i += nlt) {
           ct<T> c0 = e0, c1 = e1;
           if constexpr (sizeof(T) == sizeof(double)) {
             // FP64 plan: exact reduction per entry, as before
@@ -783,7 +784,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         const T mag1 = bmagt * (T)k2 / (T)(k2 + 1);
         const float num1f = Q.nu1f[j];
         const double num1 = F32 ? 0.0 : Q.nu[j] - 1.0;
-        for (int i = tid; i < nchi; i += NL_LT) {
+        for (int i = tid; i < nchi; i += nlt) {
           // x^nu (nu = 1 or 1.01) and, for magnification, x^2 more
           const T x = xs[i];
           T xp = x;
@@ -823,7 +824,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
           const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
           const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;
           T tb = 0;
-          for (int i = tid; i < nchi; i += NL_LT) {
+          for (int i = tid; i < nchi; i += nlt) {
             const T rx = rct / xs[i];
             const T rx3 = rx * rx * rx;
             for (int h = 0; h < (two ? 2 : 1); h++) {
@@ -869,7 +870,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         if ((tid & 31) == 0) red[0][tid >> 5] = bp;
         __syncthreads();
         if (tid == 0)
-          for (int w2 = 0; w2 < NL_LT / 32; w2++) b1bar += red[0][w2];
+          for (int w2 = 0; w2 < nlt / 32; w2++) b1bar += red[0][w2];
       } else {
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
         double part0 = 0.0, part1 = 0.0;
@@ -878,7 +879,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
         const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;  // exact for k < 255
         T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
-        for (int i = tid; i < nchi; i += NL_LT) {
+        for (int i = tid; i < nchi; i += nlt) {
           const T rx = rct / xs[i];
           const T rx3 = rx * rx * rx;
           for (int h = 0; h < (two ? 2 : 1); h++) {
@@ -931,7 +932,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
         __syncthreads();
         if (tid == 0) {
           double t0 = 0.0, t1 = 0.0;
-          for (int w2 = 0; w2 < NL_LT / 32; w2++) {
+          for (int w2 = 0; w2 < nlt / 32; w2++) {
             t0 += red[0][w2];
             t1 += red[1][w2];
           }
@@ -964,7 +965,7 @@ __global__ void __launch_bounds__(NL_LT, 4) k_nl_loop(Params P, NLParams Q, cons
     // the slice adjoint onto the table's two z columns, and d/db1
     __syncthreads();
     double* lb = lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
-    for (int i = tid; i < P.pkl_nk; i += NL_LT) {
+    for (int i = tid; i < P.pkl_nk; i += nlt) {
       const double v = F32 ? (double)pbarf[i] : pbard[i];
       if (v != 0.0) {
         atomicAdd(&lb[(size_t)i * P.pkl_nz + j0], (1 - dyz) * v);
@@ -1018,7 +1019,7 @@ static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cb
   const size_t sm = nl_loop_smem<T>(P, Q, true);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_nl_loop<T, true><<<dim3(P.B, P.nl), NL_LT, sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+  k_nl_loop<T, true><<<dim3(P.B, P.nl), nl_loop_threads(sm), sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
 }
 
 void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
@@ -1044,7 +1045,7 @@ static void launch_nl_loop_t(const Params& P, const NLParams& Q, cudaStream_t s)
   const size_t sm3 = nl_loop_smem<T>(P, Q, false);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-  k_nl_loop<T, false><<<dim3(P.B, P.nl), NL_LT, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+  k_nl_loop<T, false><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
 }
 
 void launch_nonlimber_prep(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk)
