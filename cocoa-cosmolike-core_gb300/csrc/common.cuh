@@ -71,7 +71,8 @@ struct Params {
   // mixed plan: FP32 per-multipole factors of the multipole lists the
   // Limber kernels are launched on, 8 floats per multipole (log10(l+1/2)
   // head and tail, then ss: l(l-1)(l+1)(l+2)/(l+1/2)^4; g: sqrt((l-1)l(l+1)
-  // (l+2))/(l+1/2)^2, l(l+1)/(l+1/2)^2, RSD c0, RSD c1, (l+3/2)/(l+1/2));
+  // (l+2))/(l+1/2)^2, l(l+1)/(l+1/2)^2, RSD c0, RSD c1, (l+3/2)/(l+1/2),
+  // (l+1/2)^2);
   // facf_gi: the g factors at l = 0..LNL-1
   const float* facf_ss;
   const float* facf_g;
@@ -88,8 +89,8 @@ struct Params {
   // mixed plan: FP32 records of the ss node set and of each lens bin's gs
   // node set [B][1 + nl][4][n_ss] (log10(fK c/H0) head and tail, z offset in
   // lnP, z cell) and their Limber weights: ss [B][n_ss][pss rounded up to
-  // 8] (pair-minor), gs [B][nl][2][CL2PT_MAXB][n_ss] (lens L and M terms,
-  // pairs of the bin) (k_ls_nodes, k_limber.cu)
+  // 8] (pair-minor), gs [B][nl][3][CL2PT_MAXB][n_ss] (lens L, magnification
+  // M and one-loop bK terms, pairs of the bin) (k_ls_nodes, k_limber.cu)
   float* lsn;
   float* ssx;
   float* gsx;
@@ -135,13 +136,18 @@ struct Params {
   double* wgs_b;            // [B][nl][ns][n_ss] WS C1 b_TA D^2
   double* wgs_2;            // [B][nl][ns][n_ss] WS C2 D^2
   double* wgs_1l;           // [B][nl][2][n_ss] 0.5 D^4 WGAL (b2, bs2) (0 without b2)
+  // the one-loop bK k^2 P terms (cosmo2D.c:1993-1995, 2599-2605), with
+  // k = (l+1/2)/fK: per node the factor of (l+1/2)^2 P (0 without b2):
+  // gs WGAL bK / fK^2 (times WK); gg 2 b1 bK WGAL^2 / fK^2
+  double* wgs_bk;           // [B][nl][n_ss]
+  double* wgg_bk;           // [B][nl][n_gg]
   double* wgg_1l;           // [B][nl][5][n_gg] WGAL^2 D^4 (b1 b2, b2^2/4, b1 bs2,
                             //   b2 bs2/2, bs2^2/4) (0 without b2)
   double* tab_ss_bb;        // [B][pss][nnode_ss] C_ss BB (TATT)
 };
 
 enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };
-constexpr int GGN_SLOTS = 15;  // floats per gg node record (k_gg_nodes)
+constexpr int GGN_SLOTS = 16;  // floats per gg node record (k_gg_nodes)
 
 // ---------------------------------------------------------------------
 // FP64 lookups (restating cosmolike/cosmo3D.c and redshift_spline.c)

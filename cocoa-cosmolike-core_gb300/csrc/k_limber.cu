@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(128) k_ls_nodes(Params P)
     const double* wx = P.wgs_x + b0 * P.ns * nn;
     const double* wl = P.wgs_l + b0 * nn;
     const double* wm = P.wgs_m + b0 * nn;
-    float* x = P.gsx + b0 * 2 * CL2PT_MAXB * nn;
+    float* x = P.gsx + b0 * 3 * CL2PT_MAXB * nn;
     // the pairs of bin q in the order k_limber_gs numbers them
     int m = 0;
     for (int k = 0; k < P.pgs; k++) {
@@ -272,6 +272,9 @@ __global__ void __launch_bounds__(128) k_ls_nodes(Params P)
         const double f = fw(p) * wx[zs * nn + p];
         x[(size_t)(0 * CL2PT_MAXB + m) * nn + p] = (float)(f * wl[p]);
         x[(size_t)(1 * CL2PT_MAXB + m) * nn + p] = (float)(f * wm[p]);
+        // one-loop bK: the lensing kernel WK alone (cosmo2D.c:1998-2003)
+        x[(size_t)(2 * CL2PT_MAXB + m) * nn + p] =
+            P.one_loop ? (float)(fw(p) * P.wgs_k[(b0 * P.ns + zs) * nn + p] * P.wgs_bk[b0 * nn + p]) : 0.0f;
       }
       m++;
     }
@@ -425,17 +428,19 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   // pairs of this lens bin
   __shared__ int kk[CL2PT_MAXB], ss_[CL2PT_MAXB];
-  __shared__ int npair, use_m;
+  __shared__ int npair, use_m, use_k;
   if (tid == 0) {
     int n = 0;
     for (int k = 0; k < P.pgs; k++)
       if (P.zl[k] == q) { kk[n] = k; ss_[n] = P.zs[k]; n++; }
     npair = n;
     use_m = (P.nu[pt].gb[4][q] != 0.0);
+    use_k = P.one_loop && P.nu[pt].gb[5][q] != 0.0;
   }
   __syncthreads();
   const int np_ = npair;
-  const int nterm = use_m ? 2 : 1;
+  // weight rows: 0 L, 1 magnification M, 2 one-loop bK
+  const int nterm = use_k ? 3 : (use_m ? 2 : 1);
   constexpr bool F32 = sizeof(T) == sizeof(float);
   double *sd, *si = nullptr, *nlc;
   T *lk, *Ps, *X, *ndy;
@@ -460,7 +465,7 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
     lk = (T*)(nlc + PCH);
     Ps = lk + pd.nk;
     X = Ps + PCH * LT;                  // [nterm][npair][PCH]
-    ndy = X + (size_t)2 * CL2PT_MAXB * PCH;
+    ndy = X + (size_t)3 * CL2PT_MAXB * PCH;
     nj = (int*)(ndy + PCH);
   }
   Axis<T> ax{};
@@ -477,19 +482,21 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   const double* wm = P.wgs_m + b0 * P.n_ss;
   const bool valid = L < P.nnode_g;
   double lp = 1.5;
-  T pref2, pref;
+  T pref2, pref, lp2 = (T)0;  // lp2: (l+1/2)^2 of the bK term
   float2 llf = make_float2(0.0f, 0.0f);
   if constexpr (F32) {
     const float4 fa = valid ? *(const float4*)(P.facf_g + 8 * (size_t)L) : make_float4(0.f, 0.f, 0.f, 0.f);
     pref2 = fa.z;
     pref = fa.w;
     llf = make_float2(fa.x, fa.y);
+    lp2 = valid ? P.facf_g[8 * (size_t)L + 7] : 0.0f;
   } else {
     const double l = valid ? ell[L] : 1.0;
     lp = l + 0.5;
     const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
     pref2 = (T)((tmp > 0) ? sqrt(tmp) / (lp * lp) : 0.0);
     pref = (T)(l * (l + 1.) / (lp * lp));
+    lp2 = (T)(lp * lp);
   }
   double* out = P.tab_gs + (size_t)pt * P.pgs * P.nnode_g;
   int hk = -1;  // mixed plan: the k cell of the previous node
@@ -504,7 +511,7 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
         ndy[p] = rec[2 * P.n_ss + p];
         nj[p] = __float_as_int(rec[3 * P.n_ss + p]);
       }
-      const float* xs = P.gsx + b0 * 2 * CL2PT_MAXB * P.n_ss + p0;
+      const float* xs = P.gsx + b0 * 3 * CL2PT_MAXB * P.n_ss + p0;
       for (int idx = tid; idx < nterm * np_ * np; idx += LT) {
         const int t = idx / (np_ * np);
         const int r = idx - t * np_ * np;
@@ -525,6 +532,12 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
       const double dch = node[(size_t)NF_DCHIDA * P.node_stride + off + p0 + p];
       const double wt = node[(size_t)NF_WT * P.node_stride + off + p0 + p];
+      if (t == 2) {
+        X[(t * CL2PT_MAXB + m) * PCH + p] = (T)(wt * dch / (fK * fK) *
+                                                P.wgs_k[(b0 * P.ns + ss_[m]) * P.n_ss + p0 + p] *
+                                                P.wgs_bk[b0 * P.n_ss + p0 + p]);
+        continue;
+      }
       const double lens = t == 0 ? wl[p0 + p] : wm[p0 + p];
       X[(t * CL2PT_MAXB + m) * PCH + p] =
           (T)(wt * dch / (fK * fK) * wx[ss_[m] * P.n_ss + p0 + p] * lens);
@@ -543,14 +556,18 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
         Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     }
     for (int m = 0; m < np_; m++) {
-      T a0 = 0, a1 = 0;
+      T a0 = 0, a1 = 0, a2 = 0;
       const T* x0 = X + (0 * CL2PT_MAXB + m) * PCH;
       for (int p = 0; p < np; p++) a0 += x0[p] * Ps[p * LT + tid];
       if (use_m) {
         const T* x1 = X + (1 * CL2PT_MAXB + m) * PCH;
         for (int p = 0; p < np; p++) a1 += x1[p] * Ps[p * LT + tid];
       }
-      const double v = (double)(pref2 * (a0 + pref * a1));
+      if (use_k) {
+        const T* x2 = X + (2 * CL2PT_MAXB + m) * PCH;
+        for (int p = 0; p < np; p++) a2 += x2[p] * Ps[p * LT + tid];
+      }
+      const double v = (double)(pref2 * (a0 + pref * a1 + lp2 * a2));
       double* o = out + (size_t)kk[m] * P.nnode_g + L;
       *o = (p0 == 0) ? v : *o + v;
     }
@@ -583,7 +600,8 @@ constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
 // head and tail; 9, 10 the lnP and lnP_lin z cells; 11, 12 the first
 // multipole index kept by the chi(a_min) cut on the C_l nodes and on
 // l = 0..LNL-1 (prefixes when the list ascends); 13, 14 the cut's FP64
-// threshold on l + 1/2 (for a list that does not ascend).
+// threshold on l + 1/2 (for a list that does not ascend); 15 the one-loop
+// bK weight 2 b1 bK WGAL^2 / fK^2 of (l+1/2)^2 (0 without one-loop bias).
 __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __restrict__ ell)
 {
   const int pt = blockIdx.x, q = blockIdx.y;
@@ -624,7 +642,8 @@ __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __rest
         (float)(fK * CL2PT_COVERH0), (float)wq, (float)node[(size_t)NF_DYZ * P.node_stride + off + p],
         (float)P.wgg_l[b0 * P.n_gg + p], (float)P.wgg_m[b0 * P.n_gg + p], (float)P.wgg_r0[b0 * P.n_gg + p],
         (float)dyl, lf.x, lf.y, __int_as_float(nodej[off + p]), __int_as_float(jl), __int_as_float(lm[0]),
-        __int_as_float(lm[1]), __int_as_float((int)(tb & 0xffffffffLL)), __int_as_float((int)(tb >> 32))};
+        __int_as_float(lm[1]), __int_as_float((int)(tb & 0xffffffffLL)), __int_as_float((int)(tb >> 32)),
+        P.one_loop ? (float)P.wgg_bk[b0 * P.n_gg + p] : 0.0f};
     for (int f = 0; f < GGN_SLOTS; f++) rec[(size_t)f * P.n_gg + p] = v[f];
   }
 }
@@ -649,7 +668,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   constexpr bool F32 = sizeof(T) == sizeof(float);
   double* nd = (double*)smem_raw;
   double* thr = nd + 8 * PCH;  // [PCH] per-node l+1/2 threshold of the chi(a_min) cut
-  double *sd = nullptr, *si = nullptr, *sdl = nullptr, *sil = nullptr;
+  double *sd = nullptr, *si = nullptr, *sdl = nullptr, *sil = nullptr, *nbk = nullptr;
   int* nj;
   T *lk, *lkl = nullptr, *cx, *cz, *cdn, *cup, *gv, *gs, *gz, *szc, *sy, *sc;
   T *icx = nullptr, *sbq = nullptr, *sdq = nullptr;
@@ -695,7 +714,8 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     // tables, int [2][PCH], then T arrays: P axes, distance table (chi, z,
     // and the per-cell slopes chi_all interpolates), growth table (value,
     // slope, z), n(z) spline of bin q
-    sd = thr + PCH;
+    nbk = thr + PCH;  // [PCH] one-loop bK weights
+    sd = nbk + PCH;
     si = sd + pd.nk;
     sdl = si + pd.nk;
     sil = sdl + pl.nk;
@@ -777,6 +797,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   // the chi(a_min) cut as a first-kept index when the list ascends (the
   // integer-l pass always), else as the FP64 threshold on l + 1/2
   const bool cut_idx = mode == 1 || P.ell_g_sorted;
+  float lp2f = 0.0f;  // mixed plan: (l+1/2)^2 of the bK term
   if constexpr (F32) {
     if (!cut_idx) lp = (valid ? ell[L] : 1.0) + 0.5;
     // FP32 plan constants (the C_l nodes, or l = L for the integer-l pass)
@@ -787,6 +808,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     c0 = fb.x;
     c1 = fb.y;
     ratio = fb.z;
+    lp2f = fb.w;
   } else {
     const double l = valid ? ((mode == 0) ? ell[L] : (double)L) : 1.0;
     lp = l + 0.5;
@@ -814,6 +836,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
         nj[p] = __float_as_int(rec[(size_t)9 * P.n_gg + p]);
         nj[PCH + p] = __float_as_int(rec[(size_t)10 * P.n_gg + p]);
         lmin[p] = __float_as_int(rec[(size_t)(mode == 0 ? 11 : 12) * P.n_gg + p]);
+        nf[10 * PCH + p] = rec[(size_t)15 * P.n_gg + p];
         const unsigned lo = __float_as_uint(rec[(size_t)13 * P.n_gg + p]);
         const unsigned hi = __float_as_uint(rec[(size_t)14 * P.n_gg + p]);
         thr[p] = __longlong_as_double(((long long)hi << 32) | lo);
@@ -846,6 +869,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
       nd[6 * PCH + p] = dyl;
       nd[7 * PCH + p] = lfk;
       thr[p] = th;
+      nbk[p] = P.one_loop ? P.wgg_bk[b0 * P.n_gg + p0 + p] : 0.0;
     }
     __syncthreads();
     if (!valid) continue;
@@ -899,11 +923,14 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
         }
         const float s = Lw + Mw * pref + (c0 * r0w - c1 * n1 * H1 * f1);
         if (sgg) sgg[(size_t)(p0 + p) * Ltot] = s;
-        const float s2w = s * s * nf[1 * PCH + p];
+        // the one-loop bK term enters the nonlinear-P integrand only
+        // (cosmo2D.c:2568)
+        const float s2 = s * s * nf[1 * PCH + p];
+        const float s2w = s2 + nf[10 * PCH + p] * lp2f * nf[1 * PCH + p];
         float uh, ul;
         split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
         snl += s2w * pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p], hk);
-        if (mode == 1) sln += s2w * pk_eval_fh(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p], hkl);
+        if (mode == 1) sln += s2 * pk_eval_fh(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p], hkl);
         continue;
       }
       // a_chi at chi1 (cosmo3D.c:109-133)
@@ -933,13 +960,16 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
       }
       const T wrsd = c0 * r0w - c1 * n1 * H1 * f1;
       const T s = Lw + Mw * pref + wrsd;
-      const double s2w = (double)(s * s) * nd[1 * PCH + p];
+      // the one-loop bK term enters the nonlinear-P integrand only
+      // (cosmo2D.c:2568)
+      const double s2 = (double)(s * s) * nd[1 * PCH + p];
+      const double s2w = s2 + nbk[p] * lp * lp * nd[1 * PCH + p];
       const double log10k = llp - nd[7 * PCH + p];
       const T Pnl = pk_eval<T>(ax, pd.tab, pd.nz, log10k, nj[p], (T)nd[2 * PCH + p]);
       sum_nl += s2w * (double)Pnl;
       if (mode == 1) {
         const T Pl = pk_eval<T>(axl, pl.tab, pl.nz, log10k, nj[PCH + p], (T)nd[6 * PCH + p]);
-        sum_lin += s2w * (double)Pl;
+        sum_lin += s2 * (double)Pl;
       }
     }
     if constexpr (F32) {
@@ -964,7 +994,7 @@ static size_t gg_smem(const Params& P, int mode)
     return sizeof(double) * 9 * PCH + sizeof(int) * 2 * PCH +
            sizeof(float) * (3 * (size_t)P.pk_nk + (mode == 1 ? 3 * (size_t)P.pkl_nk : 0) + 5 * (size_t)P.chi_nz +
                             (P.G_same_axis ? 2 : 3) * (size_t)P.G_nz + 5 * (size_t)P.lens_nz) + 64;
-  return sizeof(double) * (9 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
+  return sizeof(double) * (10 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
          sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;
 }
 
@@ -992,9 +1022,9 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    const size_t sm = f32 ? sm_f32 + 4 * (size_t)2 * CL2PT_MAXB * PCH
+    const size_t sm = f32 ? sm_f32 + 4 * (size_t)3 * CL2PT_MAXB * PCH
                           : sizeof(double) * (2 * P.pk_nk + PCH) +
-                                sizeof(T) * (P.pk_nk + PCH * LT + (size_t)2 * CL2PT_MAXB * PCH + PCH) +
+                                sizeof(T) * (P.pk_nk + PCH * LT + (size_t)3 * CL2PT_MAXB * PCH + PCH) +
                                 sizeof(int) * PCH + 64;
     cudaFuncSetAttribute(k_limber_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);

@@ -409,11 +409,11 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
   const bool hb2 = has_b2(P, nu);
   if (set == 0 && threadIdx.x == 0) {
     P.chi_amin[pt] = chi_all_d(P.chi_z, X, P.chi_nz, P.a_min).chi;
-    // b2 != 0 needs the one-loop path; b3 and bK need terms not built here
-    // (the tabulated P_d1p3 of the reference, 2 b1 bK k^2 P)
+    // b2 != 0 needs the one-loop path; b3 needs the reference's tabulated
+    // P_d1p3, which is not part of this build
     bool bad = hb2 && !P.one_loop;
     for (int i = 0; i < P.nl; i++)
-      if (hb2 && (nu.gb[3][i] != 0.0 || nu.gb[5][i] != 0.0)) bad = true;
+      if (hb2 && nu.gb[3][i] != 0.0) bad = true;
     if (bad) atomicOr(P.err, 1);
   }
   const double nlb = (hb2 && P.one_loop) ? 1.0 : 0.0;
@@ -468,6 +468,7 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
       if (P.one_loop) {
         P.wgs_1l[(b0 * 2 + 0) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gb2_d(P, nu, q, b1);
         P.wgs_1l[(b0 * 2 + 1) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gbs2_d(P, nu, q, b1);
+        P.wgs_bk[b0 * P.n_ss + p] = nlb * WGAL * nu.gb[5][q] / (fK * fK);
       }
       double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
       for (int s = 0; s < P.ns; s++) {
@@ -499,6 +500,7 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
         o[2 * P.n_gg] = c * b1 * bs2;
         o[3 * P.n_gg] = c * 0.5 * b2 * bs2;
         o[4 * P.n_gg] = c * 0.25 * bs2 * bs2;
+        P.wgg_bk[b0 * P.n_gg + p] = nlb * 2.0 * b1 * nu.gb[5][q] * WGAL * WGAL / (fK * fK);
       }
       // RSD term at a0 = a_chi(chi_0), chi_0 = (l+1/2)/k = fK
       // (cosmo2D.c:2540-2547, radial_weights.c:87-105)

@@ -46,6 +46,16 @@ __global__ void k_vjp_assemble(Params P, VJPParams V)
   const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
   const int n_total = n_xi + n_gt + nt * P.nl;
   const cl2pt_nuisance& nu = P.nu[pt];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && P.one_loop) {
+    // the adjoint does not carry the one-loop bK k^2 P terms (active when
+    // b2 != 0): such a point is reported through the device error flag
+    bool b2 = false, bk = false;
+    for (int q = 0; q < P.nl; q++) {
+      b2 |= nu.gb[1][q] != 0.0;
+      bk |= nu.gb[5][q] != 0.0;
+    }
+    if (b2 && bk) atomicOr(P.err, 1);
+  }
   const double* o = P.obs + (size_t)pt * n_total;
   const double* v = V.cot + (size_t)pt * n_total;
   const double* dv = V.dv + (size_t)pt * n_total;

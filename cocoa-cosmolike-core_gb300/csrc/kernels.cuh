@@ -91,7 +91,8 @@ struct VJPParams {
   const double* lfac_g;
   const double* lfac_gi;   // the same factors at l = 0..LNL-1
   // FP32 copies for the mixed plan, 8 floats per multipole: log10(l+1/2) as
-  // head and tail, then the remaining factors in order (ss: 1, g: 5)
+  // head and tail, then the remaining factors in order (ss: 1, g: 5, then
+  // (l+1/2)^2)
   const float* lfacf_ss;
   const float* lfacf_g;
   const float* lfacf_gi;

@@ -545,7 +545,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     }
     TRY(dupload(p, &p->d_lfac_ss, fs.data(), fs.size()));
     TRY(dupload(p, &p->d_lfac_g, fg.data(), fg.size()));
-    const std::vector<float> fsf = lfac_f32(fs, 2), fgf = lfac_f32(fg, 6);
+    const std::vector<float> fsf = lfac_f32(fs, 2);
+    std::vector<float> fgf = lfac_f32(fg, 6);
+    for (size_t i = 0; i < lg.size(); i++) fgf[8 * i + 7] = (float)((lg[i] + 0.5) * (lg[i] + 0.5));  // (l+1/2)^2
     TRY(dupload(p, &p->d_lfacf_ss, fsf.data(), fsf.size()));
     TRY(dupload(p, &p->d_lfacf_g, fgf.data(), fgf.size()));
   }
@@ -665,7 +667,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     TRY(dalloc(p, &P.ggn, (size_t)W * nl * cl2pt::GGN_SLOTS * std::max(p->n_gg, 1)));
     TRY(dalloc(p, &P.lsn, (size_t)W * (1 + nl) * 4 * p->n_ss));
     TRY(dalloc(p, &P.ssx, (size_t)W * p->n_ss * ((p->pss + 7) & ~7)));
-    TRY(dalloc(p, &P.gsx, (size_t)W * std::max(nl, 1) * 2 * CL2PT_MAXB * p->n_ss));
+    TRY(dalloc(p, &P.gsx, (size_t)W * std::max(nl, 1) * 3 * CL2PT_MAXB * p->n_ss));
   }
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
@@ -701,6 +703,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(dalloc(p, &P.fpt_b, (size_t)W * 5 * nf));
       TRY(dalloc(p, &P.wgs_1l, (size_t)W * nl * 2 * p->n_ss));
       TRY(dalloc(p, &P.wgg_1l, (size_t)W * nl * 5 * p->n_gg));
+      TRY(dalloc(p, &P.wgs_bk, (size_t)W * nl * p->n_ss));
+      TRY(dalloc(p, &P.wgg_bk, (size_t)W * nl * p->n_gg));
     }
     if (P.tatt) {
       TRY(cl2pt_fastpt_ia_plan_create(kx.data(), nf, &fc, W, &p->fpt_ia));
@@ -1685,7 +1689,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       CUDA_OK(cudaMemcpyAsync(p->d_lfac_f + 2 * (size_t)fr->nell, fg.data(), sizeof(double) * fg.size(),
                               cudaMemcpyHostToDevice, s));
     }
-    const std::vector<float> fsf = lfac_f32(fs, 2), fgf = lfac_f32(fg, 6);
+    const std::vector<float> fsf = lfac_f32(fs, 2);
+    std::vector<float> fgf = lfac_f32(fg, 6);
+    for (int i = 0; i < fr->nell; i++) fgf[8 * i + 7] = (float)((fr->ell[i] + 0.5) * (fr->ell[i] + 0.5));
     CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f, fsf.data(), sizeof(float) * fsf.size(), cudaMemcpyHostToDevice, s));
     CUDA_OK(cudaMemcpyAsync(p->d_lfacf_f + 8 * (size_t)fr->nell, fgf.data(), sizeof(float) * fgf.size(),
                             cudaMemcpyHostToDevice, s));

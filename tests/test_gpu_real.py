@@ -76,12 +76,15 @@ def blocks(plan, dv):
             "w": dv[2 * a + plan.n_gammat:]}
 
 
-def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None):
+def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None):
     import oracle as O
     w = workloads.make(name)
     if tweak is not None:
         tweak(w)
     tabs, nus = workloads.points(w, npts, seed=seed)
+    if nu_tweak is not None:
+        for i, nu in enumerate(nus):
+            nu_tweak(i, nu)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     dv = plan.eval_real(om, h0, chi, G, lnP, nus)
@@ -167,6 +170,37 @@ def test_small_nonlimber_w(gpu_lib, oracle_built, prec):
     print(prec, worst)
     for k, v in worst.items():
         assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_one_loop_bk(gpu_lib, oracle_built, prec):
+    """One-loop bias with bK (the bK k^2 P terms of C_gs and C_gg,
+    cosmo2D.c:1993-1995, 2599-2605) against the oracle; bK ~ U(0, 2e-8) in
+    c/H0 units puts the term at a few tenths of C_gg near l ~ 10^3."""
+    rng = np.random.default_rng(17)
+
+    def set_bk(i, nu):
+        for q in range(5):
+            nu.gb[5][q] = float(rng.uniform(0.0, 2e-8))
+    worst, _ = run_case("real_3x2pt_tatt_small", 2, prec, seed=11, nu_tweak=set_bk)
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+def test_one_loop_bk_not_in_adjoint(gpu_lib):
+    """The adjoint does not carry the bK terms: a point with b2 and bK both
+    set is reported as an error instead of a partial gradient."""
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 1, seed=11)
+    nus[0].gb[5][0] = 1e-8
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    plan.eval_real(om, h0, chi, G, lnP, nus)  # the forward carries them
+    with pytest.raises(lib.CL2PTError):
+        plan.vjp_real(om, h0, chi, G, lnP, nus, np.ones((1, plan.n_total)))
 
 
 @pytest.mark.gpu
