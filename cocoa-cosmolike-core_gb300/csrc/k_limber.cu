@@ -98,21 +98,40 @@ __device__ __forceinline__ Axis<T> load_axis(const double* __restrict__ lk, int 
 // exact two-float difference, and the in-cell offset, the corner
 // differences and exp(hi) exp(lo + delta) are formed in FP32 (the absolute
 // error of delta stays ~1e-7, i.e. ~1e-7 relative in P).
+// (two entries per thread and step, 16-byte loads and stores, when the
+// caller's table starts on a 16-byte boundary (the destination is the
+// plan's own); one entry per step otherwise)
 __global__ void k_split_table(const double* __restrict__ src, float2* __restrict__ dst, size_t n)
 {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double v = src[i];
+  if ((reinterpret_cast<uintptr_t>(src) & 15) != 0) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const double v = src[i];
+      const float h = (float)v;
+      dst[i] = make_float2(h, (float)(v - (double)h));
+    }
+    return;
+  }
+  const size_t n2 = n / 2;
+  const double2* s2 = (const double2*)src;
+  float4* d4 = (float4*)dst;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 v = __ldcs(s2 + i);
+    const float h0 = (float)v.x, h1 = (float)v.y;
+    __stcs(d4 + i, make_float4(h0, (float)(v.x - (double)h0), h1, (float)(v.y - (double)h1)));
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const double v = src[n - 1];
     const float h = (float)v;
-    dst[i] = make_float2(h, (float)(v - (double)h));
+    dst[n - 1] = make_float2(h, (float)(v - (double)h));
   }
 }
 
 void launch_split_tables(const Params& P, cudaStream_t s, int* launches)
 {
-  k_split_table<<<1216, 256, 0, s>>>(P.lnP, (float2*)P.lnP2, (size_t)P.B * P.pk_nk * P.pk_nz);
+  k_split_table<<<2432, 256, 0, s>>>(P.lnP, (float2*)P.lnP2, (size_t)P.B * P.pk_nk * P.pk_nz);
   (*launches)++;
   if (P.lnPL != P.lnP) {
-    k_split_table<<<1216, 256, 0, s>>>(P.lnPL, (float2*)P.lnPL2, (size_t)P.B * P.pkl_nk * P.pkl_nz);
+    k_split_table<<<2432, 256, 0, s>>>(P.lnPL, (float2*)P.lnPL2, (size_t)P.B * P.pkl_nk * P.pkl_nz);
     (*launches)++;
   }
 }

@@ -358,17 +358,20 @@ __device__ __forceinline__ NLGeom nl_geom(const Params& P, int pt)
 }
 
 // ---- 1. forward transforms (cfftlog_ells_p1, cosmo2D.c:4047-4130), FP64:
-// one CTA per (point, lens bin, radial kernel j).
+// one CTA per (point, lens bin) for the radial kernels j in [j0, j1): the
+// per-sample factors (a(chi), H, D, n_lens, f, b1) are formed once into
+// shared memory, then each kernel is filled, transformed and windowed.
 // unit_b1: the galaxy kernel with b1 = 1 (the adjoint pass differentiates
 // the linear-bias factor out of it; bias model 0 only).
 template <typename T>
-__global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int unit_b1)
+__global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int unit_b1, int j0, int j1)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int pt = blockIdx.x, q = blockIdx.y, j = blockIdx.z;
+  const int pt = blockIdx.x, q = blockIdx.y;
   const int tid = threadIdx.x;
   const cl2pt_nuisance& nu = P.nu[pt];
-  if (j == 2 && nu.gb[4][q] == 0.0) return;  // magnification kernel unused
+  const bool mag = nu.gb[4][q] != 0.0;  // the magnification kernel is read only with bmag != 0
+  if (!mag && j1 > 2) j1 = 2;
   const int nchi = P.nl_nchi;
   const double* X = P.chi + (size_t)pt * P.chi_nz;
   const double* Gv = P.G + (size_t)pt * P.G_nz;
@@ -378,68 +381,76 @@ __global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int 
   const double rc = geo.rc;
   cd* bufA = (cd*)smem_raw;
   cd* bufB = bufA + Q.nmax;
+  // per sample: fx_j of the three kernels (0 outside the bin's z range)
+  double* fx = (double*)(bufB + Q.nmax);  // [3][nchi]
   const double* glens = P.glens + ((size_t)pt * P.nl + q) * P.n_a;
   const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
-  const int N = Q.N[j];
-  for (int i = tid; i < N; i += NL_NT) {
-    double v = 0.0;
-    const int qq = i - Q.pad[j];
-    if (qq >= 0 && qq < nchi) {
-      const double xq = geo.x0 * exp(geo.dlnchi * qq);
-      const double chi = xq / rc;
-      const double a = a_chi_d(P.chi_z, X, P.chi_nz, chi);
-      const double z = 1. / a - 1.;
-      if (!(z < P.lens_zmin[q] || z > P.lens_zmax[q])) {
-        const double H = 1.0 / ((a * a) * chi_all_d(P.chi_z, X, P.chi_nz, a).dchida);
-        const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
-        const double pf = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]);
-        double fx;
-        if (j == 0) {
-          double b1;
-          if (unit_b1) {
-            b1 = 1.0;
-          } else switch (P.bias_model[0]) {
-            case 0: b1 = nu.gb[0][q]; break;
-            case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
-            case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
-            case 4: b1 = nu.gb[0][0] * pow(1 + z, nu.gb[0][1]); break;
-            default: {
-              const double zev = growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)) /
-                                 growfac_d(P.G_z, Gv, P.G_nz, g1,
-                                           1. / (1. + 0.5 * (P.lens_zmin[q] + P.lens_zmax[q])));
-              b1 = (nu.gb[0][q] - 1.) / zev + 1.;
-            }
+  const double lnx0 = log(geo.x0);
+  for (int m = tid; m < nchi; m += NL_NT) {
+    double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+    const double xq = geo.x0 * exp(geo.dlnchi * m);
+    const double chi = xq / rc;
+    const double a = a_chi_d(P.chi_z, X, P.chi_nz, chi);
+    const double z = 1. / a - 1.;
+    if (!(z < P.lens_zmin[q] || z > P.lens_zmax[q])) {
+      const double H = 1.0 / ((a * a) * chi_all_d(P.chi_z, X, P.chi_nz, a).dchida);
+      const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+      const double pf = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]);
+      if (j0 <= 0 && 0 < j1) {
+        double b1;
+        if (unit_b1) {
+          b1 = 1.0;
+        } else switch (P.bias_model[0]) {
+          case 0: b1 = nu.gb[0][q]; break;
+          case 1: b1 = nu.gb[0][q] * ((1.0 + z) / (1. + P.zmean_lens[q])); break;
+          case 3: b1 = nu.gb[0][0] / growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)); break;
+          case 4: b1 = nu.gb[0][0] * pow(1 + z, nu.gb[0][1]); break;
+          default: {
+            const double zev = growfac_d(P.G_z, Gv, P.G_nz, g1, 1. / (z + 1.)) /
+                               growfac_d(P.G_z, Gv, P.G_nz, g1,
+                                         1. / (1. + 0.5 * (P.lens_zmin[q] + P.lens_zmax[q])));
+            b1 = (nu.gb[0][q] - 1.) / zev + 1.;
           }
-          fx = chi * pf * D * H * b1;
-        } else if (j == 1) {
-          fx = -chi * pf * D * H * f_growth_d(P.G_z, Gv, P.G_nz, z);
-        } else {
-          // W_mag with the coarse g_lens table (interpol1d)
-          const double amax = 0.999999;
-          const double dac = (amax - amin_lensg) / ((double)P.n_a - 1.0);
-          const double gl = (a < amin_lensg || a > 1.0 - dac)
-                                ? 0.0 : interpol1d_d(glens, P.n_a, amin_lensg, dac, a);
-          const double WM = (1.5 * om * chi / a) * gl;
-          fx = (WM / chi / (rc * rc)) * D;
         }
-        v = fx / pow(xq, Q.nu[j]);
+        f0 = chi * pf * D * H * b1;
+      }
+      if (j0 <= 1 && 1 < j1) f1 = -chi * pf * D * H * f_growth_d(P.G_z, Gv, P.G_nz, z);
+      if (j1 > 2) {
+        // W_mag with the coarse g_lens table (interpol1d)
+        const double amax = 0.999999;
+        const double dac = (amax - amin_lensg) / ((double)P.n_a - 1.0);
+        const double gl = (a < amin_lensg || a > 1.0 - dac) ? 0.0 : interpol1d_d(glens, P.n_a, amin_lensg, dac, a);
+        const double WM = (1.5 * om * chi / a) * gl;
+        f2 = (WM / chi / (rc * rc)) * D;
       }
     }
-    bufA[i] = cmk(v, 0.0);
+    // divided by x^nu_j = exp(nu_j ln x), ln x = ln x0 + m dlnchi
+    const double lnx = lnx0 + geo.dlnchi * m;
+    fx[m] = f0 / exp(Q.nu[0] * lnx);
+    fx[nchi + m] = f1 / exp(Q.nu[1] * lnx);
+    fx[2 * nchi + m] = f2 / exp(Q.nu[2] * lnx);
   }
-  __syncthreads();
-  cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
-  const int halfN = N / 2;
-  const int kmax = (int)(halfN * 0.25);
-  ct<T>* tout = (ct<T>*)Q.tout + ((size_t)pt * P.nl + q) * Q.tout_stride;
-  for (int i = tid; i <= halfN; i += NL_NT) {
-    cd v = r[i];
-    const int k = halfN - i;  // window on the right side
-    if (k <= kmax) {
-      const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
-      v = cscale(v, W);
+  for (int j = j0; j < j1; j++) {
+    const int N = Q.N[j];
+    __syncthreads();
+    for (int i = tid; i < N; i += NL_NT) {
+      const int qq = i - Q.pad[j];
+      bufA[i] = cmk((qq >= 0 && qq < nchi) ? fx[j * nchi + qq] : 0.0, 0.0);
     }
-    tout[j * Q.hstride + i] = tmk<T>((T)v.x, (T)v.y);
+    __syncthreads();
+    cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
+    const int halfN = N / 2;
+    const int kmax = (int)(halfN * 0.25);
+    ct<T>* tout = (ct<T>*)Q.tout + ((size_t)pt * P.nl + q) * Q.tout_stride;
+    for (int i = tid; i <= halfN; i += NL_NT) {
+      cd v = r[i];
+      const int k = halfN - i;  // window on the right side
+      if (k <= kmax) {
+        const double W = (double)k / kmax - sin(2. * M_PI * k / kmax) / (2. * M_PI);
+        v = cscale(v, W);
+      }
+      tout[j * Q.hstride + i] = tmk<T>((T)v.x, (T)v.y);
+    }
   }
 }
 
@@ -1013,9 +1024,9 @@ template <typename T>
 static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
                             cl2pt_nuisance* nu_bar, cudaStream_t s)
 {
-  const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
+  const size_t sm1 = sizeof(double) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi) + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-  k_nl_forward<T><<<dim3(P.B, P.nl, 1), NL_NT, sm1, s>>>(P, Q, 1);
+  k_nl_forward<T><<<dim3(P.B, P.nl), NL_NT, sm1, s>>>(P, Q, 1, 0, 1);
   const size_t sm = nl_loop_smem<T>(P, Q, true);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
   cudaFuncSetAttribute(k_nl_loop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1033,9 +1044,9 @@ void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar
 template <typename T>
 static void launch_nl_prep_t(const Params& P, const NLParams& Q, cudaStream_t s)
 {
-  const size_t sm1 = sizeof(double) * 2 * 2 * Q.nmax + 64;
+  const size_t sm1 = sizeof(double) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi) + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-  k_nl_forward<T><<<dim3(P.B, P.nl, 3), NL_NT, sm1, s>>>(P, Q, 0);
+  k_nl_forward<T><<<dim3(P.B, P.nl), NL_NT, sm1, s>>>(P, Q, 0, 0, 3);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
 }
 
