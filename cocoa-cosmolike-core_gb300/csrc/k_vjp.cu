@@ -46,16 +46,6 @@ __global__ void k_vjp_assemble(Params P, VJPParams V)
   const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
   const int n_total = n_xi + n_gt + nt * P.nl;
   const cl2pt_nuisance& nu = P.nu[pt];
-  if (blockIdx.x == 0 && threadIdx.x == 0 && P.one_loop) {
-    // the adjoint does not carry the one-loop bK k^2 P terms (active when
-    // b2 != 0): such a point is reported through the device error flag
-    bool b2 = false, bk = false;
-    for (int q = 0; q < P.nl; q++) {
-      b2 |= nu.gb[1][q] != 0.0;
-      bk |= nu.gb[5][q] != 0.0;
-    }
-    if (b2 && bk) atomicOr(P.err, 1);
-  }
   const double* o = P.obs + (size_t)pt * n_total;
   const double* v = V.cot + (size_t)pt * n_total;
   const double* dv = V.dv + (size_t)pt * n_total;
@@ -341,15 +331,27 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
     const int q = set - 1 - P.nl;
     const int nn = P.n_gg, off = P.n_ss + P.nl * P.n_ss + q * nn;
     const size_t b0 = (size_t)pt * P.nl + q;
-    double acc = 0.0;
+    // one-loop bK weight 2 b1 bK W_gal^2 / fK^2 (bias model 0: b1 per bin)
+    const bool kon = P.one_loop && V.one_loop_on[pt];
+    double acc = 0.0, acck = 0.0;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p];
       const double H = node[(size_t)NF_H * P.node_stride + off + p];
       const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       acc += V.lbar_gg[b0 * nn + p] * WGAL;
+      if (kon) {
+        const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+        const double c = V.kbar_gg[b0 * nn + p] * 2.0 * WGAL * WGAL / (fK * fK);
+        acc += c * nu.gb[5][q];
+        acck += c * nu.gb[0][q];
+      }
     }
     const double s = block_sum_d(acc, red);
-    if (threadIdx.x == 0) atomicAdd(&g.gb[0][q], s);
+    const double sk = kon ? block_sum_d(acck, red) : 0.0;
+    if (threadIdx.x == 0) {
+      atomicAdd(&g.gb[0][q], s);
+      if (kon) atomicAdd(&g.gb[5][q], sk);
+    }
     return;
   }
   if (set == 0 && !(P.probes & CL2PT_PROBE_XI)) return;
@@ -464,15 +466,25 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
   }
   if (set > 0) {
     const size_t b0 = (size_t)pt * P.nl + q;
-    double acc = 0.0;
+    // one-loop bK weight W_gal bK / fK^2
+    const bool kon = P.one_loop && V.one_loop_on[pt];
+    double acc = 0.0, acck = 0.0;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p];
       const double H = node[(size_t)NF_H * P.node_stride + off + p];
       const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       acc += V.lbar_gs[(b0 * 2 + 0) * nn + p] * WGAL;
+      if (kon) {
+        const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+        acck += V.kbar_gs[b0 * nn + p] * WGAL / (fK * fK);
+      }
     }
     const double s = block_sum_d(acc, red);
-    if (threadIdx.x == 0) atomicAdd(&g.gb[0][q], s);
+    const double sk = kon ? block_sum_d(acck, red) : 0.0;
+    if (threadIdx.x == 0) {
+      atomicAdd(&g.gb[0][q], s);
+      if (kon) atomicAdd(&g.gb[5][q], sk);
+    }
   }
 }
 

@@ -364,7 +364,9 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
 }
 
 // ------------------------------------------------------------------ gs
-// C_gs(l) = pref2 sum_p F x_s (L + pref M) P; CTA = (point, lens q)
+// C_gs(l) = pref2 sum_p F [x_s (L + pref M) + (l+1/2)^2 W_K,s K] P, with the
+// one-loop bK weight K = W_gal bK / fK^2 (0 off the one-loop gate); CTA =
+// (point, lens q)
 template <typename T>
 __global__ void k_vjp_gs(Params P, VJPParams V)
 {
@@ -393,6 +395,12 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   T* xt = (T*)(xs + (size_t)np * nn);  // [np][nn]
   T* wxs = xt + (size_t)np * nn;       // [np][nn]
   T* cbs = wxs + (size_t)np * nn;      // [np][LC]
+  // one-loop bK (only with the gate on): per source the sums over l of
+  // (l+1/2)^2 pref2 F P C_bar (FP64 and chunk), and W_K
+  const bool kon = P.one_loop && V.one_loop_on[pt];
+  double* ys = (double*)(cbs + (size_t)np * LC);
+  T* yt = (T*)(ys + (kon ? (size_t)np * nn : 0));
+  T* wks = yt + (kon ? (size_t)np * nn : 0);
   constexpr bool F32 = sizeof(T) == sizeof(float);
   AxF axf{};
   if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
@@ -404,6 +412,11 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     xs[i] = 0.0;
     xt[i] = (T)0;
     wxs[i] = (T)wx[ss_[m] * nn + r];
+    if (kon) {
+      ys[i] = 0.0;
+      yt[i] = (T)0;
+      wks[i] = (T)P.wgs_k[(b0 * P.ns + ss_[m]) * nn + r];
+    }
   }
   const bool act = p < nn;
   const int off = P.n_ss + q * P.n_ss;
@@ -414,7 +427,8 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     Lw = P.wgs_l[b0 * nn + p];
     Mw = P.wgs_m[b0 * nn + p];
   }
-  const T Ft = (T)nd.F, dyt = (T)nd.dy, Lt = (T)Lw, Mt = (T)Mw;
+  const double Kw = (kon && act) ? P.wgs_bk[b0 * nn + p] : 0.0;
+  const T Ft = (T)nd.F, dyt = (T)nd.dy, Lt = (T)Lw, Mt = (T)Mw, Kt = (T)Kw;
   const double* tab = P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
   const float2* tab2 = (const float2*)P.lnP2 + (size_t)pt * P.pk_nk * P.pk_nz;
   const float2 lf = split_fx(nd.lfk);
@@ -433,7 +447,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     T t0 = 0, t1 = 0;
     for (int l = 0; l < nL; l++) {
       const int L = L0 + l;
-      T dx, pref, g;
+      T dx, pref, g, lp2 = (T)0;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
         float uh, ul;
@@ -441,22 +455,36 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
         const float Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
         pref = fa.w;
         g = fa.z * Pv * Ft;
+        if (kon) lp2 = V.lfacf_g[8 * L + 7];
       } else {
         const double* fac = V.lfac_g + 6 * L;
         const T Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
         pref = (T)fac[2];
         g = (T)fac[1] * Pv * Ft;
+        if (kon) lp2 = (T)exp10(2.0 * fac[0]);
       }
       const T gl = g * (Lt + pref * Mt);
-      T sx = 0;
-      for (int m = 0; m < np; m++) {
-        const T cv = cbs[m * LC + l];
-        sx += cv * wxs[m * nn + p];
-        xt[m * nn + p] += gl * cv;
+      T sx = 0, sk = 0;
+      if (kon) {
+        const T gk = g * lp2;
+        for (int m = 0; m < np; m++) {
+          const T cv = cbs[m * LC + l];
+          sx += cv * wxs[m * nn + p];
+          sk += cv * wks[m * nn + p];
+          xt[m * nn + p] += gl * cv;
+          yt[m * nn + p] += gk * cv;
+        }
+        sk *= gk * Kt;
+      } else {
+        for (int m = 0; m < np; m++) {
+          const T cv = cbs[m * LC + l];
+          sx += cv * wxs[m * nn + p];
+          xt[m * nn + p] += gl * cv;
+        }
       }
       t0 += g * sx;
       t1 += g * pref * sx;
-      pw_acc<T>(wk, gl * sx, dx);
+      pw_acc<T>(wk, gl * sx + sk, dx);
     }
     lb0 += (double)t0;
     lb1 += (double)t1;
@@ -464,11 +492,27 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
       xs[m * nn + p] += (double)xt[m * nn + p];
       xt[m * nn + p] = (T)0;
     }
+    if (kon) {
+      for (int m = 0; m < np; m++) {
+        ys[m * nn + p] += (double)yt[m * nn + p];
+        yt[m * nn + p] = (T)0;
+      }
+    }
   }
   if (!act) return;
   pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
   double* xbar = V.wbar_gx + b0 * P.ns * nn;
   for (int m = 0; m < np; m++) xbar[ss_[m] * nn + p] += xs[m * nn + p];
+  if (kon) {
+    // W_K (source photo-z) and K adjoints of the bK term
+    double kb = 0.0;
+    for (int m = 0; m < np; m++) {
+      const size_t o = (b0 * P.ns + ss_[m]) * nn + p;
+      kb += P.wgs_k[o] * ys[m * nn + p];
+      V.wbar_gsk[o] += Kw * ys[m * nn + p];
+    }
+    V.kbar_gs[b0 * nn + p] += kb;
+  }
   V.lbar_gs[(b0 * 2 + 0) * nn + p] = lb0;
   V.lbar_gs[(b0 * 2 + 1) * nn + p] = lb1;
 }
@@ -584,6 +628,10 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const NodeD nd = node_d(P, pt, off + p);
   const T Ft = (T)nd.F, dyt = (T)nd.dy;
   const T Lt = (T)P.wgg_l[b0 * nn + p], Mt = (T)P.wgg_m[b0 * nn + p], r0 = (T)P.wgg_r0[b0 * nn + p];
+  // one-loop bK: (l+1/2)^2 K F P in the nonlinear-P integrand, K = 2 b1 bK
+  // W_gal^2 / fK^2 (0 off the one-loop gate)
+  const bool kon = P.one_loop && V.one_loop_on[pt];
+  const T Kt = kon ? (T)P.wgg_bk[b0 * nn + p] : (T)0;
   const cl2pt_nuisance& nu = P.nu[pt];
   const T ldz = (T)nu.lens_dz[q], lst = (T)nu.lens_stretch[q], lzm = (T)P.zmean_lens[q];
   const double chi_amin = P.chi_amin[pt];
@@ -630,7 +678,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     return Lt + Mt * pref + wrsd;
   };
   PWalk<T> wk;
-  double lbar = 0.0;
+  double lbar = 0.0, kbar = 0.0;
   // stored: the row of s for this node and the forward's first kept indices
   const size_t Ltot = (size_t)K + LNL;
   const float* sg = stored ? P.s_gg + (b0 * nn + p) * Ltot : nullptr;
@@ -641,13 +689,13 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const int La = min(K, Lk + sub * cs), Lb = min(K, Lk + (sub + 1) * cs);
   for (int L0 = La; L0 < Lb; L0 += LC) {
     const int L1 = min(Lb, L0 + LC);
-    T lt = 0;
+    T lt = 0, kt = 0;
     for (int L = L0; L < L1; L++) {
       const double* fac = V.lfac_g + 6 * L;
       if (!V.lfac_g_sorted && nd.fK * fac[5] > chi_amin) continue;
       const T cv = cbs[L];
       if (cv == (T)0) continue;
-      T dx, s, Pv;
+      T dx, s, Pv, lp2 = (T)0;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
         if (stored) {
@@ -659,15 +707,20 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
         float uh, ul;
         sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
         Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
+        if (kon) lp2 = V.lfacf_g[8 * L + 7];
       } else {
         s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
         Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
+        if (kon) lp2 = (T)exp10(2.0 * fac[0]);
       }
       const T sp = s * Ft * Pv;
+      const T kp = cv * lp2 * Ft * Pv;
       lt += (T)2 * cv * sp;
-      pw_acc<T>(wk, cv * s * sp, dx);
+      kt += kp;
+      pw_acc<T>(wk, cv * s * sp + kp * Kt, dx);
     }
     lbar += (double)lt;
+    kbar += (double)kt;
   }
   pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
   if (nonlim) {
@@ -681,16 +734,17 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
-    T lt = 0;
+    T lt = 0, kt = 0;
     const int Li = stored ? __float_as_int(rec[(size_t)12 * nn]) : first_kept(V.lfac_gi, LNL, nd.fK, chi_amin);
     const int ci = (LNL - Li + S - 1) / S;
     const int Ia = min(LNL, Li + sub * ci), Ib = min(LNL, Li + (sub + 1) * ci);
     for (int L = Ia; L < Ib; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
-      T dx, dxl, s, Pn, Pl;
+      T dx, dxl, s, Pn, Pl, lp2 = (T)0;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_gi + 8 * L);
+        if (kon) lp2 = V.lfacf_gi[8 * L + 7];
         if (stored) {
           s = sg[K + L];
         } else {
@@ -704,21 +758,27 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       } else {
         const double* fac = V.lfac_gi + 6 * L;
         s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
+        if (kon) lp2 = (T)exp10(2.0 * fac[0]);
         const double lk = fac[0] - nd.lfk;
         Pn = pw_eval<T>(wn, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, lk, bar, dx);
         Pl = pw_eval<T>(wl, lkdl, invl, nkl, tabl, P.pkl_nz, jl, dyl, dylt, lk, barl, dxl);
       }
       const T sF = s * Ft;
+      // the bK term is in the nonlinear-P integrand only
+      const T kp = cn * lp2 * Ft * Pn;
       lt += (T)2 * sF * (cn * Pn + cl * Pl);
-      pw_acc<T>(wn, cn * s * sF * Pn, dx);
+      kt += kp;
+      pw_acc<T>(wn, cn * s * sF * Pn + kp * Kt, dx);
       pw_acc<T>(wl, cl * s * sF * Pl, dxl);
     }
     lbar += (double)lt;
+    kbar += (double)kt;
     pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
     pw_flush(wl, barl, P.pkl_nz, jl, dyl);
   }
   // zeroed per wave; S threads per node, and the Fourier path adds two passes
   atomicAdd(&V.lbar_gg[b0 * nn + p], lbar);
+  if (kon) atomicAdd(&V.kbar_gg[b0 * nn + p], kbar);
 }
 
 template <typename T>
@@ -732,7 +792,8 @@ template <typename T>
 size_t gs_smem(const Params& P)
 {
   const size_t nn = P.n_ss, np = P.ns;
-  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) + 64;
+  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) +
+         (P.one_loop ? np * nn * (8 + 2 * sizeof(T)) : 0) + 64;
 }
 template <typename T>
 size_t gg_smem(const Params& P)

@@ -108,6 +108,9 @@ struct VJPParams {
   // there) [B][nl][ns][n_ss]; coefficient sums [B][5][pss][n_ss]; the
   // per-point one-loop gate [B]
   double *wbar_ssb, *wbar_ss2, *wbar_gsb, *wbar_gs2, *wbar_gsk, *cx_ss;
+  // one-loop bK: adjoints of the node weights W_gal bK / fK^2 (gs)
+  // [B][nl][n_ss] and 2 b1 bK W_gal^2 / fK^2 (gg) [B][nl][n_gg]
+  double *kbar_gs, *kbar_gg;
   int* one_loop_on;
   // lfac_g holds increasing multipoles (the plan's node table; caller
   // multipoles of the Fourier path need not be sorted)

@@ -150,10 +150,15 @@ int cl2pt_graph_destroy(cl2pt_graph* graph);
  *                                  may be NULL
  *   nu_bar   [n]                   the nuisance gradient in the cl2pt_nuisance
  *                                  layout: shear_m, src_dz (source photo-z
- *                                  shifts), gb[0] (b1) and ia[0] (A1 per
- *                                  source bin in redshift-binning mode; A1 and
- *                                  eta in ia[0][0..1] in redshift-evolution
- *                                  mode); other fields 0.
+ *                                  shifts), gb[0] (b1), ia[0] (A1 per source
+ *                                  bin in redshift-binning mode; A1 and eta
+ *                                  in ia[0][0..1] in redshift-evolution
+ *                                  mode); with TATT also ia[1] (A2, eta_2)
+ *                                  and ia[2] (b_TA); with one-loop bias
+ *                                  gb[1] (b2), gb[2] (bs2) and gb[5] (bK),
+ *                                  the one-loop gate (any b2 != 0) held at
+ *                                  its value; other fields (lens_dz,
+ *                                  lens_stretch, bmag) 0.
  * Every pointer follows batch->where.  The reference has no derivatives;
  * this replaces the central finite differences a caller would take of
  * compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159).  The

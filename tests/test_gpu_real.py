@@ -190,20 +190,6 @@ def test_one_loop_bk(gpu_lib, oracle_built, prec):
 
 
 @pytest.mark.gpu
-def test_one_loop_bk_not_in_adjoint(gpu_lib):
-    """The adjoint does not carry the bK terms: a point with b2 and bK both
-    set is reported as an error instead of a partial gradient."""
-    w = workloads.make("real_3x2pt_tatt_small")
-    tabs, nus = workloads.points(w, 1, seed=11)
-    nus[0].gb[5][0] = 1e-8
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
-    om, h0, chi, G, lnP = workloads.stack(tabs)
-    plan.eval_real(om, h0, chi, G, lnP, nus)  # the forward carries them
-    with pytest.raises(lib.CL2PTError):
-        plan.vjp_real(om, h0, chi, G, lnP, nus, np.ones((1, plan.n_total)))
-
-
-@pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_many_theta_bins(gpu_lib, oracle_built, prec):
     """40 angular bins: the 2 x 40 xi filter rows span two row tiles of the

@@ -389,21 +389,36 @@ def test_vjp_nonlimber_vs_oracle_fd(gpu_lib, oracle_built):
 def tatt_params(w):
     ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
     ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
-    ps += [("gb", k, q) for k in range(3) for q in range(w.cfg.n_lens)]
+    ps += [("gb", k, q) for k in (0, 1, 2, 5) for q in range(w.cfg.n_lens)]
     ps += [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0)]
     return ps
+
+
+def fd_step(field, i, x0):
+    """Central-difference step: bK (gb[5]) is ~1e-8 in c/H0 units."""
+    return H * max(abs(x0), 1e-8 if (field, i) == ("gb", 5) else 0.1)
+
+
+def set_bk(nus, w, seed):
+    """bK ~ U(0, 2e-8) on every point but the first (whose bK stays 0: with
+    the one-loop gate on, its bK gradient is still nonzero)."""
+    rng = np.random.default_rng(seed)
+    for nu in nus[1:]:
+        for q in range(w.cfg.n_lens):
+            nu.gb[5][q] = float(rng.uniform(0.0, 2e-8))
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_MIXED])
 def test_vjp_tatt_one_loop(gpu_lib, prec):
     """TATT intrinsic alignments (A1, eta_1, A2, eta_2, b_TA) and one-loop
-    bias (b2, bs2) with non-Limber w(theta): every nuisance gradient and a
-    direction in the nonlinear table (with a separate linear table, whose
+    bias (b2, bs2, bK) with non-Limber w(theta): every nuisance gradient and
+    a direction in the nonlinear table (with a separate linear table, whose
     FAST-PT dependence the adjoint leaves out) against differences of the
     FP64 forward."""
     w = workloads.make("real_3x2pt_tatt_small")
     tabs, nus = workloads.points(w, 2, seed=41)
+    set_bk(nus, w, 41)
     p64 = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=2, linear_table=True)
     plan = p64 if prec == lib.PREC_FP64 else lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2,
                                                       linear_table=True)
@@ -418,7 +433,7 @@ def test_vjp_tatt_one_loop(gpu_lib, prec):
         sl = slice(pt, pt + 1)
         for field, i, j in tatt_params(w):
             x0 = nu_get(nus[pt], field, i, j)
-            h = H * max(abs(x0), 0.1)
+            h = fd_step(field, i, x0)
             f = []
             for sgn in (1, -1):
                 nu = clone(nus[pt])

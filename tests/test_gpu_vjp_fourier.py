@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from cl2pt import abi, lib, workloads
-from test_gpu_vjp import GRAD_REL, H, clone, flat_index, nu_get, nu_set
+from test_gpu_vjp import GRAD_REL, H, clone, fd_step, flat_index, nu_get, nu_set, set_bk
 
 
 def case(name, prec, seed, ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, ell=None, linear_table=False):
@@ -31,7 +31,7 @@ def params(w):
     ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
     ps += [("gb", 0, q) for q in range(w.cfg.n_lens)]
     if w.cfg.ia_model == abi.IA_TATT:
-        ps += [("gb", k, q) for k in (1, 2) for q in range(w.cfg.n_lens)]
+        ps += [("gb", k, q) for k in (1, 2, 5) for q in range(w.cfg.n_lens)]
         ps += [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0)]
     else:
         ps += [("ia", 0, 0), ("ia", 0, 1)]
@@ -58,7 +58,7 @@ def check(w, tabs, nus, p64, plan, ell, tol, lmax_shear=1e30, separate_linear=Fa
                                                                   lmax_shear=lmax_shear, lnPL=lpl)[0])
         for field, i, j in params(w):
             x0 = nu_get(nus[pt], field, i, j)
-            h = H * max(abs(x0), 0.1)
+            h = fd_step(field, i, x0)
             fs = []
             for sgn in (1, -1):
                 nu = clone(nus[pt])
@@ -100,9 +100,11 @@ def test_vjp_fourier_nonlimber(gpu_lib, prec):
 
 @pytest.mark.gpu
 def test_vjp_fourier_tatt(gpu_lib):
-    """TATT + one-loop bias on the Fourier vector (FP64)."""
+    """TATT + one-loop bias (bK set on the second point) on the Fourier
+    vector (FP64)."""
     ell = np.exp(np.log(20.0) + (np.arange(10) + 0.5) * (np.log(3000.0) - np.log(20.0)) / 10)
     w, tabs, nus, p64, plan, ell = case("real_3x2pt_tatt_small", lib.PREC_FP64, seed=63, ell=ell,
                                         linear_table=True)
+    set_bk(nus, w, 63)
     worst = check(w, tabs, nus, p64, plan, ell, GRAD_REL, separate_linear=True)
     print("Fourier TATT max rel gradient error", worst)
