@@ -102,9 +102,12 @@ def make(name: str) -> Workload:
     raise KeyError(name)
 
 
-def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True):
-    """n parameter points: (list of CosmoTables, list of abi.Nuisance)."""
+def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True, bmag: bool = False):
+    """n parameter points: (list of CosmoTables, list of abi.Nuisance).
+    bmag: also draw a magnification bias bmag ~ U(-1, 3) per lens bin (from
+    a stream of its own, so the other draws do not change)."""
     rng = np.random.default_rng(SEED0 + seed)
+    rng_m = np.random.default_rng(SEED0 + 900 + seed)
     ns, nl = w.cfg.n_source, w.cfg.n_lens
     tabs, nus = [], []
     for _ in range(n):
@@ -124,6 +127,9 @@ def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True):
             b1=rng.uniform(1.2, 2.2, nl),
             **extra,
         )
+        if bmag:
+            for q, v in enumerate(rng_m.uniform(-1.0, 3.0, nl)):
+                nu.gb[4][q] = float(v)
         tabs.append(t)
         nus.append(nu)
     return tabs, nus

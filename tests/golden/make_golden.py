@@ -20,7 +20,7 @@ sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
-         "fastpt_bias", "fastpt_ia", "real_3x2pt_tatt_small"]
+         "fastpt_bias", "fastpt_ia", "real_3x2pt_tatt_small", "real_3x2pt_small_mag"]
 
 # J_abJ1J2Jk rows {alpha, beta, J1, J2, Jk} checked on the batched FAST-PT grid
 JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]
@@ -47,9 +47,11 @@ def run_case(case, which="ref"):
         r = np.array(JK_ROWS)
         out["J_abJ1J2Jk"] = o.J_abJ1J2Jk(k, P[0], r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
         return out
-    w = workloads.make(case)
+    # <workload>_mag: the workload's points with magnification bias
+    mag = case.endswith("_mag")
+    w = workloads.make(case[:-4] if mag else case)
     o.setup(w.cfg, w.src, w.lens)
-    tabs, nus = workloads.points(w, 2, seed=11)
+    tabs, nus = workloads.points(w, 2, seed=11, bmag=mag)
     for i in range(2):
         o.set_point(tabs[i], nus[i])
         if case == "cosmic_shear_fourier":

@@ -45,10 +45,10 @@ def test_cosmic_shear_fourier_vs_reference(gpu_lib, prec):
         assert err <= REL, (i, err)
 
 
-def fourier_case(name, npts, prec, ell, seed=3):
+def fourier_case(name, npts, prec, ell, seed=3, bmag=False):
     import oracle as O
     w = workloads.make(name)
-    tabs, nus = workloads.points(w, npts, seed=seed)
+    tabs, nus = workloads.points(w, npts, seed=seed, bmag=bmag)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     lmax_shear = 0.7 * np.max(ell)
@@ -80,6 +80,19 @@ def test_fourier_3x2pt_nonlimber(gpu_lib, oracle_built, prec):
     clustering from the FFTLog C_l), shear cut at 0.7 l_max."""
     ell = fourier_ells(26, 20.0, 5000.0)
     worst, _ = fourier_case("real_3x2pt_small", 2, prec, ell)
+    print(prec, worst)
+    assert worst <= REL, worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_fourier_magnification(gpu_lib, oracle_built, prec):
+    """Magnification bias bmag ~ U(-1, 3) per lens bin: the W_mag terms of
+    C_gs and C_gg (Limber), the FFTLog magnification kernel below
+    LMAX_NOLIMBER, and the lens integration ranges that open to the
+    sources' z_min when bmag != 0 (redshift_spline.c:50-79)."""
+    ell = fourier_ells(26, 20.0, 5000.0)
+    worst, _ = fourier_case("real_3x2pt_small", 2, prec, ell, bmag=True)
     print(prec, worst)
     assert worst <= REL, worst
 

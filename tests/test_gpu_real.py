@@ -76,12 +76,12 @@ def blocks(plan, dv):
             "w": dv[2 * a + plan.n_gammat:]}
 
 
-def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None):
+def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None, bmag=False):
     import oracle as O
     w = workloads.make(name)
     if tweak is not None:
         tweak(w)
-    tabs, nus = workloads.points(w, npts, seed=seed)
+    tabs, nus = workloads.points(w, npts, seed=seed, bmag=bmag)
     if nu_tweak is not None:
         for i, nu in enumerate(nus):
             nu_tweak(i, nu)
@@ -184,6 +184,20 @@ def test_one_loop_bk(gpu_lib, oracle_built, prec):
         for q in range(5):
             nu.gb[5][q] = float(rng.uniform(0.0, 2e-8))
     worst, _ = run_case("real_3x2pt_tatt_small", 2, prec, seed=11, nu_tweak=set_bk)
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_magnification(gpu_lib, oracle_built, prec):
+    """Magnification bias bmag ~ U(-1, 3) per lens bin (the points of the
+    real_3x2pt_small_mag fixture, whose oracle is pinned to the reference):
+    W_mag in gamma_t and in the Limber w(theta), the FFTLog magnification
+    kernel of the non-Limber C_l, and the lens ranges that bmag != 0 opens
+    to the sources' z_min (redshift_spline.c:50-79)."""
+    worst, _ = run_case("real_3x2pt_small", 2, prec, seed=11, bmag=True)
     print(prec, worst)
     for k, v in worst.items():
         assert v <= REL, (k, v, worst)
