@@ -587,8 +587,9 @@ __device__ __forceinline__ ct<float> phase_f(int m, float2 th)
 
 // ADJ: the adjoint of the FFTLog part (see section 4 below) on the same
 // multipole walk: the loop stops at the forward's hand-over multipole, keeps
-// the b1-free galaxy term G0 of both multipoles, and accumulates the P_lin
-// slice adjoint and d/db1 from cbar = dL/dC_l instead of writing C_l.
+// the b1-free galaxy term G0 and the bmag-free magnification term M0 of both
+// multipoles, and accumulates the P_lin slice adjoint, d/db1 and d/dbmag
+// from cbar = dL/dC_l instead of writing C_l.
 template <typename T, bool ADJ>
 __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
                                                       double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
@@ -608,7 +609,8 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   //   mixed plan: [lxk: nchi float][pcf: 3 nk float, psf: nk float] and the
   //     FP64 slice psl only during set-up, in fb;
   //   FP64 plan:  [psl, plkd, pinv: nk double][lxk: nchi double]
-  //   adjoint: [G00, G01: nchi T] after xs, the slice adjoint [nk] last
+  //   adjoint: [G00, G01, M00, M01: nchi T] after xs, the slice adjoint
+  //   [nk] last
   ct<T>* fa = (ct<T>*)smem_raw;
   ct<T>* fb = fa + Q.nmax;
   T* F0 = (T*)(fb + Q.nmax);
@@ -616,7 +618,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   T* xs = F1 + nchi;
   T* G00 = xs + nchi;
   T* G01 = G00 + nchi;
-  T* plk = ADJ ? G01 + nchi : xs + nchi;
+  T* M00 = G01 + nchi;
+  T* M01 = M00 + nchi;
+  T* plk = ADJ ? M01 + nchi : xs + nchi;
   constexpr bool F32 = sizeof(T) == sizeof(float);
   float* lxkf = (float*)(plk + P.pkl_nk);
   float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
@@ -697,7 +701,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   const int LEND = ADJ ? P.conv_l[cta] : LNL;
   const T wsum = (T)(geo.dlnchi * 2. / M_PI);  // chi-sum weight of C_l
   const T b1t = ADJ ? (T)nu.gb[0][q] : (T)1;
-  double b1bar = 0.0;
+  double b1bar = 0.0, magbar = 0.0;
   const double* cb = ADJ ? cbar + cta * LNL : nullptr;
   for (int ks = 0; ks < LEND && !done; ks += BLOCK) {
     const int ke = (ks + BLOCK < LEND) ? ks + BLOCK : LEND;
@@ -793,6 +797,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // bmag l(l+1)/(l+1)^2 = bmag l/(l+1)
         const T mag0 = bmagt * (T)k / (T)(k + 1);
         const T mag1 = bmagt * (T)k2 / (T)(k2 + 1);
+        const T un0 = (T)k / (T)(k + 1), un1 = (T)k2 / (T)(k2 + 1);  // adjoint: bmag = 1
         const float num1f = Q.nu1f[j];
         const double num1 = F32 ? 0.0 : Q.nu[j] - 1.0;
         for (int i = tid; i < nchi; i += nlt) {
@@ -808,6 +813,10 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           const ct<T> z = r[Q.pad[j] + i];
           T f0 = z.x * sc0 * xp, f1 = z.y * sc1 * xp;
           if (j == 2) {
+            if (ADJ) {
+              M00[i] = f0 * un0;
+              M01[i] = f1 * un1;
+            }
             f0 *= mag0;
             f1 *= mag1;
           }
@@ -828,13 +837,14 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // multipoles: P_lin slice adjoint (FP32 shared atomics in the mixed
         // plan) and d/db1 through F = b1 G0 + ...
         const T wt0 = (T)cb[k] * wsum, wt1 = two ? (T)cb[k2] * wsum : (T)0;
-        double bp = 0.0;
+        const bool magk = nj == 3;
+        double bp = 0.0, mp = 0.0;
         if (wt0 != (T)0 || wt1 != (T)0) {
           const double lk0 = F32 ? 0.0 : Q.l10k1[k], lk1 = F32 ? 0.0 : Q.l10k1[two ? k2 : k];
           const float lk0f = F32 ? Q.l10k1f[k] : 0.0f, lk1f = F32 ? Q.l10k1f[two ? k2 : k] : 0.0f;
           const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
           const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;
-          T tb = 0;
+          T tb = 0, tm = 0;
           for (int i = tid; i < nchi; i += nlt) {
             const T rx = rct / xs[i];
             const T rx3 = rx * rx * rx;
@@ -850,6 +860,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
               }
               const T F = h ? F1[i] : F0[i];
               const T G = h ? G01[i] : G00[i];
+              const T M = magk ? (h ? M01[i] : M00[i]) : (T)0;
               const T k3 = (h ? cub1 : cub0) * rx3;
               if constexpr (F32) {
                 const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
@@ -857,7 +868,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
                 const float g = wt * F * F * k3 * pl;
                 atomicAdd(&pbarf[lo], g * (1.0f - dx));
                 atomicAdd(&pbarf[lo + 1], g * dx);
-                tb += wt * 2.0f * F * G * k3 * pl;
+                const float u = wt * 2.0f * F * k3 * pl;
+                tb += u * G;
+                tm += u * M;
               } else {
                 const double dxd = (lkv - plkd[lo]) * pinv[lo];
                 const double pl = exp(psl[lo] + dxd * (psl[lo + 1] - psl[lo])) /
@@ -865,23 +878,38 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
                 const double g = wt * F * F * k3 * pl;
                 atomicAdd(&pbard[lo], g * (1 - dxd));
                 atomicAdd(&pbard[lo + 1], g * dxd);
-                tb += wt * 2.0 * F * G * k3 * pl;
+                const double u = wt * 2.0 * F * k3 * pl;
+                tb += u * G;
+                tm += u * M;
               }
             }
           }
           if constexpr (F32) {
-            for (int o = 16; o > 0; o >>= 1) tb += __shfl_down_sync(0xffffffffu, tb, o);
+            for (int o = 16; o > 0; o >>= 1) {
+              tb += __shfl_down_sync(0xffffffffu, tb, o);
+              tm += __shfl_down_sync(0xffffffffu, tm, o);
+            }
           }
           bp = (double)tb;
+          mp = (double)tm;
         }
         if constexpr (!F32) {
-          for (int o = 16; o > 0; o >>= 1) bp += __shfl_down_sync(0xffffffffu, bp, o);
+          for (int o = 16; o > 0; o >>= 1) {
+            bp += __shfl_down_sync(0xffffffffu, bp, o);
+            mp += __shfl_down_sync(0xffffffffu, mp, o);
+          }
         }
         __syncthreads();
-        if ((tid & 31) == 0) red[0][tid >> 5] = bp;
+        if ((tid & 31) == 0) {
+          red[0][tid >> 5] = bp;
+          red[1][tid >> 5] = mp;
+        }
         __syncthreads();
         if (tid == 0)
-          for (int w2 = 0; w2 < nlt / 32; w2++) b1bar += red[0][w2];
+          for (int w2 = 0; w2 < nlt / 32; w2++) {
+            b1bar += red[0][w2];
+            magbar += red[1][w2];
+          }
       } else {
       // chi sums of F^2 k^3 P_lin(k, a = 1), both multipoles
         double part0 = 0.0, part1 = 0.0;
@@ -983,7 +1011,10 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         atomicAdd(&lb[(size_t)i * P.pkl_nz + j0 + 1], dyz * v);
       }
     }
-    if (tid == 0) atomicAdd(&nu_bar[pt].gb[0][q], b1bar);
+    if (tid == 0) {
+      atomicAdd(&nu_bar[pt].gb[0][q], b1bar);
+      if (nj == 3) atomicAdd(&nu_bar[pt].gb[4][q], magbar);
+    }
     return;
   }
   // hand over to Limber (cosmo2D.c:4760-4765)
@@ -1006,6 +1037,8 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
 // unit_b1).  Given cbar[l] = dL/dC_l, one CTA per (point, bin) walks the
 // same multipole recurrence as k_nl_loop and accumulates
 //   dL/db1     += cbar (2/pi) dlnchi sum_i 2 F_i G0_i k_i^3 P_i
+//   dL/dbmag   += cbar (2/pi) dlnchi sum_i 2 F_i M0_i k_i^3 P_i  (bmag != 0;
+//                 M0 = l(l+1) F_2 / y^2, the magnification term with bmag = 1)
 //   dL/dpsl[m] += cbar (2/pi) dlnchi sum_i F_i^2 k_i^3 P_i (lerp weight)
 // where psl is the z = 0 slice of the linear table; the slice adjoint is
 // spread onto the table's two z columns at the end.
@@ -1016,7 +1049,7 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
   size_t sm = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
               (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
                    : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
-  if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
+  if (adj) sm += sizeof(T) * 4 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
   return sm;
 }
 

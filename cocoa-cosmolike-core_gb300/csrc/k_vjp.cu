@@ -313,6 +313,19 @@ __device__ __forceinline__ double block_sum_d(double v, double* red)
 
 constexpr int NB_NT = 128;
 
+// W_mag at a node (radial_weights.c:42-53): 1.5 Omega_m fK / a g_lens(a),
+// g_lens of the bin from the coarse table (as k_nodes forms it)
+__device__ __forceinline__ double w_mag(const Params& P, int pt, int q, double om, double fK, double a)
+{
+  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
+  return 1.5 * om * fK / a * g_lookup(P.glens + ((size_t)pt * P.nl + q) * P.n_a, P.n_a, amin_lensg, a, false);
+}
+
+// bmag: the reference widens a lens bin's integration range when bmag != 0
+// (redshift_spline.c:50-79), so the data vector jumps at bmag = 0 and has
+// no derivative there; the gradient is formed for bins with bmag != 0 and
+// left 0 at bmag = 0.
+
 // Node-weight adjoints -> nuisance gradient.  NLA (IA.c:238-296):
 // w = W_K - W_S C1, C1 = A(a) 0.01389 Omega_m / D with A = A1[s]
 // (redshift binning) or A1 ((1/a)/1.62)^eta (redshift evolution).
@@ -331,26 +344,31 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
     const int q = set - 1 - P.nl;
     const int nn = P.n_gg, off = P.n_ss + P.nl * P.n_ss + q * nn;
     const size_t b0 = (size_t)pt * P.nl + q;
-    // one-loop bK weight 2 b1 bK W_gal^2 / fK^2 (bias model 0: b1 per bin)
+    // one-loop bK weight 2 b1 bK W_gal^2 / fK^2 (bias model 0: b1 per bin);
+    // magnification weight M = W_mag bmag
     const bool kon = P.one_loop && V.one_loop_on[pt];
-    double acc = 0.0, acck = 0.0;
+    const bool mon = nu.gb[4][q] != 0.0;
+    double acc = 0.0, acck = 0.0, accm = 0.0;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p];
       const double H = node[(size_t)NF_H * P.node_stride + off + p];
+      const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
       const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       acc += V.lbar_gg[b0 * nn + p] * WGAL;
       if (kon) {
-        const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
         const double c = V.kbar_gg[b0 * nn + p] * 2.0 * WGAL * WGAL / (fK * fK);
         acc += c * nu.gb[5][q];
         acck += c * nu.gb[0][q];
       }
+      if (mon) accm += V.mbar_gg[b0 * nn + p] * w_mag(P, pt, q, om, fK, a);
     }
     const double s = block_sum_d(acc, red);
     const double sk = kon ? block_sum_d(acck, red) : 0.0;
+    const double sm = mon ? block_sum_d(accm, red) : 0.0;
     if (threadIdx.x == 0) {
       atomicAdd(&g.gb[0][q], s);
       if (kon) atomicAdd(&g.gb[5][q], sk);
+      if (mon) atomicAdd(&g.gb[4][q], sm);
     }
     return;
   }
@@ -466,24 +484,26 @@ __global__ void __launch_bounds__(NB_NT) k_vjp_nodes(Params P, VJPParams V)
   }
   if (set > 0) {
     const size_t b0 = (size_t)pt * P.nl + q;
-    // one-loop bK weight W_gal bK / fK^2
+    // one-loop bK weight W_gal bK / fK^2; magnification weight M = W_mag bmag
     const bool kon = P.one_loop && V.one_loop_on[pt];
-    double acc = 0.0, acck = 0.0;
+    const bool mon = nu.gb[4][q] != 0.0;
+    double acc = 0.0, acck = 0.0, accm = 0.0;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p];
       const double H = node[(size_t)NF_H * P.node_stride + off + p];
+      const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
       const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       acc += V.lbar_gs[(b0 * 2 + 0) * nn + p] * WGAL;
-      if (kon) {
-        const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
-        acck += V.kbar_gs[b0 * nn + p] * WGAL / (fK * fK);
-      }
+      if (kon) acck += V.kbar_gs[b0 * nn + p] * WGAL / (fK * fK);
+      if (mon) accm += V.lbar_gs[(b0 * 2 + 1) * nn + p] * w_mag(P, pt, q, om, fK, a);
     }
     const double s = block_sum_d(acc, red);
     const double sk = kon ? block_sum_d(acck, red) : 0.0;
+    const double sm = mon ? block_sum_d(accm, red) : 0.0;
     if (threadIdx.x == 0) {
       atomicAdd(&g.gb[0][q], s);
       if (kon) atomicAdd(&g.gb[5][q], sk);
+      if (mon) atomicAdd(&g.gb[4][q], sm);
     }
   }
 }

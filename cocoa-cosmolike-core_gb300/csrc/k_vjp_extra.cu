@@ -10,7 +10,8 @@
 //              Dm, E of k_extra_ss), then u_bar (added to the NLA w_bar),
 //              b_bar (W_S C1 b_TA D^2) and c_bar (W_S C2 D^2) per source bin;
 //   k_vjpx_gs  C_gs: b_bar, c_bar, W_K_bar per source bin, the lens-weight
-//              adjoint (added to L_bar of b1) and the b2, bs2 gradients;
+//              adjoints (added to L_bar of b1 and M_bar of bmag) and the b2,
+//              bs2 gradients;
 //   k_vjpx_gg  C_gg one-loop bias (node l, and integer l below LMAX_NOLIMBER
 //              for the non-Limber hand-over): the b1, b2, bs2 gradients.
 // One CTA per (point[, lens bin]), one thread per node; rows and chunks of
@@ -216,7 +217,7 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
       gs2 = P.wgs_1l[(b0 * 2 + 1) * nn + p];
     }
   }
-  double Lbar = 0, g2bar = 0, gs2bar = 0;
+  double Lbar = 0, Mbar = 0, g2bar = 0, gs2bar = 0;
   for (int L0 = 0; L0 < K; L0 += XLC) {
     const int nL = min(XLC, K - L0);
     __syncthreads();
@@ -262,6 +263,7 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
         V.wbar_gsb[o] += -D2 * F * (Lg * X0 + Mg * X4);
         V.wbar_gs2[o] += 5. * D2 * F * (Lg * X1 + Mg * X5);
         Lbar += F * D2 * (-bw * X0 + 5. * cw * X1);
+        Mbar += F * D2 * (-bw * X4 + 5. * cw * X5);
       }
       if (P.one_loop) {
         const double WK = P.wgs_k[o];
@@ -274,6 +276,7 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
   double sb2 = 0, sbs2 = 0;
   if (act) {
     V.lbar_gs[(b0 * 2 + 0) * nn + p] += Lbar;
+    V.lbar_gs[(b0 * 2 + 1) * nn + p] += Mbar;
     // g2 = 0.5 D^4 W_gal b2, gs2 = 0.5 D^4 W_gal bs2 (one-loop gate held)
     if (P.one_loop && V.one_loop_on[pt]) {
       const cl2pt_nuisance& nu = P.nu[pt];

@@ -678,7 +678,8 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     return Lt + Mt * pref + wrsd;
   };
   PWalk<T> wk;
-  double lbar = 0.0, kbar = 0.0;
+  // lbar: adjoint of s; mbar: of the magnification weight M (ds/dM = pref)
+  double lbar = 0.0, kbar = 0.0, mbar = 0.0;
   // stored: the row of s for this node and the forward's first kept indices
   const size_t Ltot = (size_t)K + LNL;
   const float* sg = stored ? P.s_gg + (b0 * nn + p) * Ltot : nullptr;
@@ -689,13 +690,13 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   const int La = min(K, Lk + sub * cs), Lb = min(K, Lk + (sub + 1) * cs);
   for (int L0 = La; L0 < Lb; L0 += LC) {
     const int L1 = min(Lb, L0 + LC);
-    T lt = 0, kt = 0;
+    T lt = 0, kt = 0, mt = 0;
     for (int L = L0; L < L1; L++) {
       const double* fac = V.lfac_g + 6 * L;
       if (!V.lfac_g_sorted && nd.fK * fac[5] > chi_amin) continue;
       const T cv = cbs[L];
       if (cv == (T)0) continue;
-      T dx, s, Pv, lp2 = (T)0;
+      T dx, s, Pv, lp2 = (T)0, pref;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
         if (stored) {
@@ -708,19 +709,23 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
         sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
         Pv = pw_eval_f(wk, axf, tab2, P.pk_nz, nd.j, nd.dy, dyt, uh, ul, bar, dx);
         if (kon) lp2 = V.lfacf_g[8 * L + 7];
+        pref = fa.w;
       } else {
         s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
         Pv = pw_eval<T>(wk, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, fac[0] - nd.lfk, bar, dx);
         if (kon) lp2 = (T)exp10(2.0 * fac[0]);
+        pref = (T)fac[2];
       }
       const T sp = s * Ft * Pv;
       const T kp = cv * lp2 * Ft * Pv;
       lt += (T)2 * cv * sp;
+      mt += (T)2 * cv * sp * pref;
       kt += kp;
       pw_acc<T>(wk, cv * s * sp + kp * Kt, dx);
     }
     lbar += (double)lt;
     kbar += (double)kt;
+    mbar += (double)mt;
   }
   pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
   if (nonlim) {
@@ -734,17 +739,18 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     double* barl = V.lnpl_bar + (size_t)pt * P.pkl_nk * P.pkl_nz;
     PWalk<T> wn, wl;
     hc = hz = hg = hn = 0;
-    T lt = 0, kt = 0;
+    T lt = 0, kt = 0, mt = 0;
     const int Li = stored ? __float_as_int(rec[(size_t)12 * nn]) : first_kept(V.lfac_gi, LNL, nd.fK, chi_amin);
     const int ci = (LNL - Li + S - 1) / S;
     const int Ia = min(LNL, Li + sub * ci), Ib = min(LNL, Li + (sub + 1) * ci);
     for (int L = Ia; L < Ib; L++) {
       const T cn = gbs[2 * L], cl = gbs[2 * L + 1];
       if (cn == (T)0 && cl == (T)0) continue;
-      T dx, dxl, s, Pn, Pl, lp2 = (T)0;
+      T dx, dxl, s, Pn, Pl, lp2 = (T)0, pref;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_gi + 8 * L);
         if (kon) lp2 = V.lfacf_gi[8 * L + 7];
+        pref = fa.w;
         if (stored) {
           s = sg[K + L];
         } else {
@@ -759,6 +765,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
         const double* fac = V.lfac_gi + 6 * L;
         s = s_of((T)fac[2], (T)fac[3], (T)fac[4], (T)fac[5]);
         if (kon) lp2 = (T)exp10(2.0 * fac[0]);
+        pref = (T)fac[2];
         const double lk = fac[0] - nd.lfk;
         Pn = pw_eval<T>(wn, lkd, inv, nk, tab, P.pk_nz, nd.j, nd.dy, dyt, lk, bar, dx);
         Pl = pw_eval<T>(wl, lkdl, invl, nkl, tabl, P.pkl_nz, jl, dyl, dylt, lk, barl, dxl);
@@ -766,19 +773,23 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       const T sF = s * Ft;
       // the bK term is in the nonlinear-P integrand only
       const T kp = cn * lp2 * Ft * Pn;
-      lt += (T)2 * sF * (cn * Pn + cl * Pl);
+      const T ls = (T)2 * sF * (cn * Pn + cl * Pl);
+      lt += ls;
+      mt += ls * pref;
       kt += kp;
       pw_acc<T>(wn, cn * s * sF * Pn + kp * Kt, dx);
       pw_acc<T>(wl, cl * s * sF * Pl, dxl);
     }
     lbar += (double)lt;
     kbar += (double)kt;
+    mbar += (double)mt;
     pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
     pw_flush(wl, barl, P.pkl_nz, jl, dyl);
   }
   // zeroed per wave; S threads per node, and the Fourier path adds two passes
   atomicAdd(&V.lbar_gg[b0 * nn + p], lbar);
   if (kon) atomicAdd(&V.kbar_gg[b0 * nn + p], kbar);
+  if (nu.gb[4][q] != 0.0) atomicAdd(&V.mbar_gg[b0 * nn + p], mbar);
 }
 
 template <typename T>

@@ -111,6 +111,9 @@ struct VJPParams {
   // one-loop bK: adjoints of the node weights W_gal bK / fK^2 (gs)
   // [B][nl][n_ss] and 2 b1 bK W_gal^2 / fK^2 (gg) [B][nl][n_gg]
   double *kbar_gs, *kbar_gg;
+  // magnification: adjoint of the gg weight M = W_mag bmag [B][nl][n_gg]
+  // (the gs one is lbar_gs row 1)
+  double* mbar_gg;
   int* one_loop_on;
   // lfac_g holds increasing multipoles (the plan's node table; caller
   // multipoles of the Fourier path need not be sorted)

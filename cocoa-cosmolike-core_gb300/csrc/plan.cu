@@ -1014,7 +1014,7 @@ static int vjp_prepare(cl2pt_plan* p)
                        W * nl * p->nnode_g + W * ns * p->n_ss + W * nl * ns * p->n_ss + W * nl * 2 * p->n_ss +
                        W * nl * p->n_gg + W * nl * (LNL + p->nnode_g) + W * nl * LNL * 2 + W * nl * LNL +
                        W * ns * c.n_a + 2 * W * ns * p->n_ss + 3 * W * nl * ns * p->n_ss +
-                       5 * W * p->pss * p->n_ss + W * nl * p->nnode_g + W * nl * (p->n_ss + p->n_gg) + W;
+                       5 * W * p->pss * p->n_ss + W * nl * p->nnode_g + W * nl * (p->n_ss + 2 * p->n_gg) + W;
     // (a failed allocation leaves the plan usable for evaluation)
     int a = dalloc(p, &p->d_vjp_cot, (size_t)p->max_batch * p->n_total);
     p->vjp_cot_cap = (size_t)p->max_batch * p->n_total;
@@ -1594,6 +1594,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.cbar_gg2 = w; w += (size_t)W * nl * p->nnode_g;
     V0.kbar_gs = w; w += (size_t)W * nl * p->n_ss;
     V0.kbar_gg = w; w += (size_t)W * nl * p->n_gg;
+    V0.mbar_gg = w; w += (size_t)W * nl * p->n_gg;
     V0.one_loop_on = (int*)w;
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
@@ -1653,6 +1654,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     CUDA_OK(cudaMemsetAsync(V0.lbar_gg, 0, sizeof(double) * (size_t)P.B * nl * p->n_gg, s));
     // a lens bin without gs pairs leaves its rows to this
     CUDA_OK(cudaMemsetAsync(V0.lbar_gs, 0, sizeof(double) * (size_t)P.B * nl * 2 * p->n_ss, s));
+    CUDA_OK(cudaMemsetAsync(V0.mbar_gg, 0, sizeof(double) * (size_t)P.B * nl * p->n_gg, s));
     if (P.one_loop) {
       CUDA_OK(cudaMemsetAsync(V0.kbar_gs, 0, sizeof(double) * (size_t)P.B * nl * p->n_ss, s));
       CUDA_OK(cudaMemsetAsync(V0.kbar_gg, 0, sizeof(double) * (size_t)P.B * nl * p->n_gg, s));

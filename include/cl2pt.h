@@ -157,14 +157,22 @@ int cl2pt_graph_destroy(cl2pt_graph* graph);
  *                                  and ia[2] (b_TA); with one-loop bias
  *                                  gb[1] (b2), gb[2] (bs2) and gb[5] (bK),
  *                                  the one-loop gate (any b2 != 0) held at
- *                                  its value; other fields (lens_dz,
- *                                  lens_stretch, bmag) 0.
+ *                                  its value; gb[4] (bmag) for lens bins
+ *                                  with bmag != 0 (at bmag = 0 the lens
+ *                                  integration range switches,
+ *                                  redshift_spline.c:50-79, so the data
+ *                                  vector jumps there: 0); other fields
+ *                                  (lens_dz, lens_stretch) 0.  The FAST-PT
+ *                                  tables' dependence on the linear table
+ *                                  (TATT, one-loop bias) is not
+ *                                  differentiated.
  * Every pointer follows batch->where.  The reference has no derivatives;
  * this replaces the central finite differences a caller would take of
  * compute_Mx2pt_N_masked<0,3> (generic_interface.hpp:1137-1159).  The
  * non-Limber hand-over multipole of w(theta) is a discrete choice and is held
- * at its forward value.  Supported: NLA intrinsic alignments, bias model 0,
- * the nonlinear run mode; other plans return CL2PT_ERR_UNSUPPORTED. */
+ * at its forward value.  Supported: NLA and TATT intrinsic alignments, bias
+ * model 0 (with or without one-loop terms), the nonlinear run mode; other
+ * plans return CL2PT_ERR_UNSUPPORTED. */
 int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);

@@ -23,10 +23,11 @@ ORACLE_REL = 1e-4  # analytic vs FD of the oracle
 H = 1e-4
 
 
-def setup_case(ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, seed=21, prec=lib.PREC_FP64, name="real_3x2pt_small_limber"):
+def setup_case(ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, seed=21, prec=lib.PREC_FP64, name="real_3x2pt_small_limber",
+               bmag=False):
     w = workloads.make(name)
     w.cfg.ia_mode = ia_mode
-    tabs, nus = workloads.points(w, npts, seed=seed)
+    tabs, nus = workloads.points(w, npts, seed=seed, bmag=bmag)
     rng = np.random.default_rng(seed)
     for nu in nus:
         if ia_mode == abi.IA_REDSHIFT_EVOLUTION:
@@ -60,10 +61,13 @@ def flat_index(field, i, j=None):
     return (off + i) * abi.MAX_BINS + j
 
 
-def param_list(w, ia_mode):
+def param_list(w, ia_mode, mag=False):
+    """mag: also bmag (gb[4]), for points with bmag != 0 in every lens bin."""
     ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
     ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
     ps += [("gb", 0, q) for q in range(w.cfg.n_lens)]
+    if mag:
+        ps += [("gb", 4, q) for q in range(w.cfg.n_lens)]
     if ia_mode == abi.IA_REDSHIFT_EVOLUTION:
         ps += [("ia", 0, 0), ("ia", 0, 1)]
     elif ia_mode == abi.IA_REDSHIFT_BINNING:
@@ -320,6 +324,51 @@ def test_vjp_nonlimber_vs_gpu_fd(gpu_lib, prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_MIXED])
+def test_vjp_magnification(gpu_lib, prec):
+    """Magnification bias bmag != 0 in every lens bin, non-Limber w(theta):
+    d/dbmag through the gs and gg Limber weights W_mag bmag and the FFTLog
+    magnification kernel, with every other gradient, against differences of
+    the FP64 forward."""
+    w, tabs, nus, p64 = setup_case(abi.IA_REDSHIFT_EVOLUTION, name="real_3x2pt_small", seed=35, bmag=True)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(18)
+    v = rng.normal(size=(len(tabs), p64.n_total))
+    plan = p64 if prec == lib.PREC_FP64 else lib.Plan(w.cfg, w.src, w.lens, w.base, prec,
+                                                      max_batch=len(tabs))
+    dv, lbar, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    tol = GRAD_REL if prec == lib.PREC_FP64 else 1e-5
+    for pt in range(len(tabs)):
+        for field, i, j in param_list(w, abi.IA_REDSHIFT_EVOLUTION, mag=True):
+            x0 = nu_get(nus[pt], field, i, j)
+            h = H * max(abs(x0), 0.1)
+            f = []
+            for sgn in (1, -1):
+                nu = clone(nus[pt])
+                nu_set(nu, field, i, j, x0 + sgn * h)
+                f.append(float(v[pt] @ p64.eval_real(om[pt:pt + 1], h0[pt:pt + 1], chi[pt:pt + 1],
+                                                     G[pt:pt + 1], lnP[pt:pt + 1], [nu])[0]))
+            fd = (f[0] - f[1]) / (2 * h)
+            an = nbar[pt, flat_index(field, i, j)]
+            assert abs(an - fd) <= tol * abs(fd), (field, i, j, an, fd)
+        u = rng.normal(size=lnP.shape[1])
+        fd = lnp_direction_fd(p64, tabs, nus, v, pt, u)
+        assert abs(lbar[pt] @ u - fd) <= tol * abs(fd), (lbar[pt] @ u, fd)
+
+
+@pytest.mark.gpu
+def test_vjp_bmag_zero_is_zero(gpu_lib):
+    """At bmag = 0 the lens integration range differs from the one of any
+    bmag != 0 (redshift_spline.c:50-79): the data vector jumps there and its
+    bmag gradient entry is 0."""
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION, name="real_3x2pt_small", seed=35, npts=1)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    v = np.random.default_rng(3).normal(size=(1, plan.n_total))
+    _, _, nbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v)
+    assert all(nbar[0, flat_index("gb", 4, q)] == 0.0 for q in range(w.cfg.n_lens))
+
+
+@pytest.mark.gpu
 def test_vjp_separate_linear_table(gpu_lib):
     """With a separate linear table the linear-table terms go to lnPL_bar;
     with identical tables lnP_bar + lnPL_bar equals the single-table
@@ -389,7 +438,7 @@ def test_vjp_nonlimber_vs_oracle_fd(gpu_lib, oracle_built):
 def tatt_params(w):
     ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
     ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
-    ps += [("gb", k, q) for k in (0, 1, 2, 5) for q in range(w.cfg.n_lens)]
+    ps += [("gb", k, q) for k in (0, 1, 2, 4, 5) for q in range(w.cfg.n_lens)]
     ps += [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0)]
     return ps
 
@@ -412,12 +461,12 @@ def set_bk(nus, w, seed):
 @pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_MIXED])
 def test_vjp_tatt_one_loop(gpu_lib, prec):
     """TATT intrinsic alignments (A1, eta_1, A2, eta_2, b_TA) and one-loop
-    bias (b2, bs2, bK) with non-Limber w(theta): every nuisance gradient and
-    a direction in the nonlinear table (with a separate linear table, whose
-    FAST-PT dependence the adjoint leaves out) against differences of the
-    FP64 forward."""
+    bias (b2, bs2, bK) and magnification (bmag) with non-Limber w(theta):
+    every nuisance gradient and a direction in the nonlinear table (with a
+    separate linear table, whose FAST-PT dependence the adjoint leaves out)
+    against differences of the FP64 forward."""
     w = workloads.make("real_3x2pt_tatt_small")
-    tabs, nus = workloads.points(w, 2, seed=41)
+    tabs, nus = workloads.points(w, 2, seed=41, bmag=True)
     set_bk(nus, w, 41)
     p64 = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=2, linear_table=True)
     plan = p64 if prec == lib.PREC_FP64 else lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2,

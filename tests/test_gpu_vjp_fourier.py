@@ -9,11 +9,11 @@ from cl2pt import abi, lib, workloads
 from test_gpu_vjp import GRAD_REL, H, clone, fd_step, flat_index, nu_get, nu_set, set_bk
 
 
-def case(name, prec, seed, ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, ell=None, linear_table=False):
+def case(name, prec, seed, ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, ell=None, linear_table=False, bmag=False):
     w = workloads.make(name)
     if w.cfg.ia_model == abi.IA_NLA:
         w.cfg.ia_mode = ia_mode
-    tabs, nus = workloads.points(w, npts, seed=seed)
+    tabs, nus = workloads.points(w, npts, seed=seed, bmag=bmag)
     rng = np.random.default_rng(seed)
     if w.cfg.ia_model == abi.IA_NLA and ia_mode == abi.IA_REDSHIFT_EVOLUTION:
         for nu in nus:
@@ -26,10 +26,12 @@ def case(name, prec, seed, ia_mode=abi.IA_REDSHIFT_EVOLUTION, npts=2, ell=None, 
     return w, tabs, nus, p64, plan, ell
 
 
-def params(w):
+def params(w, mag=False):
     ps = [("shear_m", s, None) for s in range(w.cfg.n_source)]
     ps += [("src_dz", s, None) for s in range(w.cfg.n_source)]
     ps += [("gb", 0, q) for q in range(w.cfg.n_lens)]
+    if mag:
+        ps += [("gb", 4, q) for q in range(w.cfg.n_lens)]
     if w.cfg.ia_model == abi.IA_TATT:
         ps += [("gb", k, q) for k in (1, 2, 5) for q in range(w.cfg.n_lens)]
         ps += [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0)]
@@ -38,7 +40,7 @@ def params(w):
     return ps
 
 
-def check(w, tabs, nus, p64, plan, ell, tol, lmax_shear=1e30, separate_linear=False):
+def check(w, tabs, nus, p64, plan, ell, tol, lmax_shear=1e30, separate_linear=False, mag=False):
     """separate_linear: pass the linear table on its own (TATT / one-loop:
     the FAST-PT tables read it and their dependence is not differentiated, so
     the lnP direction is checked on the nonlinear table alone)."""
@@ -56,7 +58,7 @@ def check(w, tabs, nus, p64, plan, ell, tol, lmax_shear=1e30, separate_linear=Fa
         lpl = None if lnPL is None else lnPL[sl]
         f = lambda nu, lp=lnP[sl]: float(v[pt] @ p64.eval_fourier(om[sl], h0[sl], chi[sl], G[sl], lp, [nu], ell,
                                                                   lmax_shear=lmax_shear, lnPL=lpl)[0])
-        for field, i, j in params(w):
+        for field, i, j in params(w, mag):
             x0 = nu_get(nus[pt], field, i, j)
             h = fd_step(field, i, x0)
             fs = []
@@ -99,12 +101,24 @@ def test_vjp_fourier_nonlimber(gpu_lib, prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_FP64, lib.PREC_MIXED])
+def test_vjp_fourier_magnification(gpu_lib, prec):
+    """bmag != 0 in every lens bin on the serving layout at reduced size
+    (Limber W_mag terms at the caller's multipoles, the FFTLog
+    magnification kernel below LMAX_NOLIMBER)."""
+    w, tabs, nus, p64, plan, ell = case("fourier_serving_small", prec, seed=65, bmag=True)
+    worst = check(w, tabs, nus, p64, plan, ell, GRAD_REL if prec == lib.PREC_FP64 else 2e-5,
+                  lmax_shear=0.7 * w.ell[-1], mag=True)
+    print("Fourier magnification max rel gradient error", worst)
+
+
+@pytest.mark.gpu
 def test_vjp_fourier_tatt(gpu_lib):
-    """TATT + one-loop bias (bK set on the second point) on the Fourier
-    vector (FP64)."""
+    """TATT + one-loop bias (bK set on the second point) and magnification
+    on the Fourier vector (FP64)."""
     ell = np.exp(np.log(20.0) + (np.arange(10) + 0.5) * (np.log(3000.0) - np.log(20.0)) / 10)
     w, tabs, nus, p64, plan, ell = case("real_3x2pt_tatt_small", lib.PREC_FP64, seed=63, ell=ell,
-                                        linear_table=True)
+                                        linear_table=True, bmag=True)
     set_bk(nus, w, 63)
-    worst = check(w, tabs, nus, p64, plan, ell, GRAD_REL, separate_linear=True)
+    worst = check(w, tabs, nus, p64, plan, ell, GRAD_REL, separate_linear=True, mag=True)
     print("Fourier TATT max rel gradient error", worst)
