@@ -19,6 +19,14 @@
                          (scale_cuts) keep 40-100% of each data vector
   fourier_serving_small  a reduced serving workload (4 + 3 bins, 500 chi
                          points) for fast checks
+  real_3x2pt_small_nla   real_3x2pt_small with NLA intrinsic alignments in
+                         the redshift-evolution mode (A1 ~ U(0.3, 1),
+                         eta ~ U(-1.5, 1.5)), lens photo-z stretch
+                         ~ U(0.9, 1.1) and b1 evolving as (1+z)/(1+<z>)
+                         (bias model 1)
+  real_3x2pt_small_nlabin real_3x2pt_small with NLA in the redshift-binning
+                         mode (A1 ~ U(-1, 1) per source bin), lens stretch
+                         and the growth-scaled b1 of bias model 2
 
 Per-point variation: every walker gets its own P(k,z) amplitude/tilt,
 source photo-z shifts N(0, 0.02), shear calibration N(0, 0.01) and lens
@@ -44,6 +52,7 @@ class Workload:
     base: synthetic.CosmoTables
     ell: np.ndarray | None = None  # Fourier multipoles
     tatt: bool = False             # TATT IA + nonlinear galaxy bias nuisances
+    nla: bool = False              # NLA amplitudes and lens stretch drawn per point
 
 
 def _fourier_ells(nell, lmin, lmax):
@@ -99,6 +108,15 @@ def make(name: str) -> Workload:
         w.name = name
         w.tatt = True
         return w
+    if name in ("real_3x2pt_small_nla", "real_3x2pt_small_nlabin"):
+        w = make("real_3x2pt_small")
+        binned = name.endswith("bin")
+        w.cfg.ia_model = abi.IA_NLA
+        w.cfg.ia_mode = abi.IA_REDSHIFT_BINNING if binned else abi.IA_REDSHIFT_EVOLUTION
+        w.cfg.bias_model[0] = 2 if binned else 1
+        w.name = name
+        w.nla = True
+        return w
     raise KeyError(name)
 
 
@@ -108,6 +126,7 @@ def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True, bmag: bo
     a stream of its own, so the other draws do not change)."""
     rng = np.random.default_rng(SEED0 + seed)
     rng_m = np.random.default_rng(SEED0 + 900 + seed)
+    rng_a = np.random.default_rng(SEED0 + 950 + seed)
     ns, nl = w.cfg.n_source, w.cfg.n_lens
     tabs, nus = [], []
     for _ in range(n):
@@ -130,6 +149,15 @@ def points(w: Workload, n: int, seed: int = 0, vary_cosmo: bool = True, bmag: bo
         if bmag:
             for q, v in enumerate(rng_m.uniform(-1.0, 3.0, nl)):
                 nu.gb[4][q] = float(v)
+        if w.nla:
+            if w.cfg.ia_mode == abi.IA_REDSHIFT_BINNING:
+                for s_, v in enumerate(rng_a.uniform(-1.0, 1.0, ns)):
+                    nu.ia[0][s_] = float(v)
+            else:
+                nu.ia[0][0] = float(rng_a.uniform(0.3, 1.0))
+                nu.ia[0][1] = float(rng_a.uniform(-1.5, 1.5))
+            for q, v in enumerate(rng_a.uniform(0.9, 1.1, nl)):
+                nu.lens_stretch[q] = float(v)
         tabs.append(t)
         nus.append(nu)
     return tabs, nus

@@ -99,6 +99,17 @@ def test_fourier_magnification(gpu_lib, oracle_built, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_fourier_nla_stretch_bias_model(gpu_lib, oracle_built, prec):
+    """NLA (redshift evolution), lens stretch and bias model 1 on the
+    Fourier vector."""
+    ell = fourier_ells(26, 20.0, 5000.0)
+    worst, _ = fourier_case("real_3x2pt_small_nla", 2, prec, ell)
+    print(prec, worst)
+    assert worst <= REL, worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_fourier_unsorted_ells(gpu_lib, oracle_built, prec):
     """Caller multipoles in any order, down to l = 3 where the chi(a_min)
     cut of C_gg removes nodes (the mixed plan's cut falls back from a

@@ -205,6 +205,20 @@ def test_magnification(gpu_lib, oracle_built, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+@pytest.mark.parametrize("name", ["real_3x2pt_small_nla", "real_3x2pt_small_nlabin"])
+def test_nla_stretch_bias_models(gpu_lib, oracle_built, prec, name):
+    """NLA intrinsic alignments (redshift evolution; per-bin amplitudes),
+    lens photo-z stretch and the z-dependent b1 of bias models 1 and 2 (the
+    points of the fixtures of the same names, whose oracle is pinned to the
+    reference)."""
+    worst, _ = run_case(name, 2, prec, seed=11)
+    print(prec, name, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_many_theta_bins(gpu_lib, oracle_built, prec):
     """40 angular bins: the 2 x 40 xi filter rows span two row tiles of the
     Legendre contraction."""
