@@ -114,12 +114,16 @@ class CosmoTables:
     log10k: np.ndarray
     pk_z: np.ndarray
     lnP: np.ndarray  # [nk, nz]
-    # linear table (identical to lnP for these synthetic inputs)
+    # linear table (identical to lnP unless made with nl_boost)
     lnPL: np.ndarray
 
 
 def make_cosmo_tables(c: Cosmo = Cosmo(), nk: int = 600, nz: int = 200,
-                      log10k_range=(-4.0, 2.0), z_range=(0.0, 4.0)) -> CosmoTables:
+                      log10k_range=(-4.0, 2.0), z_range=(0.0, 4.0), nl_boost: bool = False) -> CosmoTables:
+    """nl_boost: the nonlinear table is the linear one times a smooth
+    small-scale boost 1 + 0.6 (k/k_nl)^1.5, k_nl = 0.25 (1+z)^1.2 h/Mpc
+    (a halofit-like shape), so the two tables differ; otherwise they are
+    the same."""
     zg = background_z_grid()
     chi = chi_of_z(zg, c)
     D = growth_D(zg, c)
@@ -128,9 +132,13 @@ def make_cosmo_tables(c: Cosmo = Cosmo(), nk: int = 600, nz: int = 200,
     pz = np.linspace(z_range[0], z_range[1], nz)
     p0 = plin_z0(10.0 ** log10k, c)
     Dz = np.interp(pz, zg, D)
-    lnP = np.log(p0)[:, None] + 2.0 * np.log(Dz)[None, :]
+    lnPL = np.log(p0)[:, None] + 2.0 * np.log(Dz)[None, :]
+    lnP = lnPL.copy()
+    if nl_boost:
+        x = 10.0 ** log10k[:, None] / (0.25 * (1.0 + pz[None, :]) ** 1.2)
+        lnP += np.log1p(0.6 * x ** 1.5)
     return CosmoTables(c.omega_m, c.h, zg, chi, zg.copy(), G, log10k, pz,
-                       np.ascontiguousarray(lnP), np.ascontiguousarray(lnP.copy()))
+                       np.ascontiguousarray(lnP), np.ascontiguousarray(lnPL))
 
 
 def perturb_tables(base: CosmoTables, rng: np.random.Generator, amp_sigma=0.02) -> CosmoTables:
@@ -139,9 +147,9 @@ def perturb_tables(base: CosmoTables, rng: np.random.Generator, amp_sigma=0.02) 
     P(k, z) table."""
     dlnA = rng.normal(0.0, amp_sigma)
     tilt = rng.normal(0.0, 0.01)
-    lnP = base.lnP + 2.0 * dlnA + tilt * (base.log10k[:, None] - 0.0) * math.log(10.0)
-    return dataclasses.replace(base, lnP=np.ascontiguousarray(lnP),
-                               lnPL=np.ascontiguousarray(lnP.copy()))
+    d = 2.0 * dlnA + tilt * (base.log10k[:, None] - 0.0) * math.log(10.0)
+    return dataclasses.replace(base, lnP=np.ascontiguousarray(base.lnP + d),
+                               lnPL=np.ascontiguousarray(base.lnPL + d))
 
 
 NZ_ROWS = 300

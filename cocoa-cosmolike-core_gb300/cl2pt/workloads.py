@@ -8,7 +8,9 @@
                          1000 log-spaced C_l nodes; P(k,z) 600 x 200;
                          b1 ~ U(1.2, 2.2); non-Limber w(theta)
   real_3x2pt_small       a reduced real_3x2pt (4 + 3 bins, 10 theta bins,
-                         l <= 5000, 200 nodes) for fast checks
+                         l <= 5000, 200 nodes) for fast checks, whose
+                         nonlinear table carries a small-scale boost over
+                         the linear one (the reduced workloads pass both)
   real_3x2pt_tatt[_small] the same with TATT intrinsic alignments
                          (redshift evolution: A1, A2, eta, b_TA) and
                          nonlinear galaxy bias (b2, bs2)
@@ -27,6 +29,11 @@
   real_3x2pt_small_nlabin real_3x2pt_small with NLA in the redshift-binning
                          mode (A1 ~ U(-1, 1) per source bin), lens stretch
                          and the growth-scaled b1 of bias model 2
+  real_3x2pt_small_hdi   real_3x2pt_small with high_def_integration = 1
+                         (larger Gauss-Legendre sets) and the ggl pairs
+                         (lens 0, source 3) and (lens 1, source 2) excluded
+  real_3x2pt_small_lin   real_3x2pt_small in the linear run mode (every
+                         spectrum from p_lin)
 
 Per-point variation: every walker gets its own P(k,z) amplitude/tilt,
 source photo-z shifts N(0, 0.02), shear calibration N(0, 0.01) and lens
@@ -80,7 +87,7 @@ def make(name: str) -> Workload:
     if name == "real_3x2pt_small":
         cfg = abi.make_config(n_source=4, n_lens=3, ntheta=10, theta_min=2.5,
                               theta_max=250.0, lmax=5000, n_ell=200)
-        base = synthetic.make_cosmo_tables(nk=400, nz=100)
+        base = synthetic.make_cosmo_tables(nk=400, nz=100, nl_boost=True)
         return Workload(name, cfg, synthetic.source_nz(4), synthetic.lens_nz(3), base)
     if name == "real_3x2pt_small_limber":
         w = make("real_3x2pt_small")
@@ -95,7 +102,7 @@ def make(name: str) -> Workload:
     if name == "fourier_serving_small":
         cfg = abi.make_config(n_source=4, n_lens=3, lmax_nolimber=200, nl_nchi=500, lmax=20000,
                               n_ell=200)
-        base = synthetic.make_cosmo_tables(nk=400, nz=100)
+        base = synthetic.make_cosmo_tables(nk=400, nz=100, nl_boost=True)
         return Workload(name, cfg, synthetic.source_nz(4), synthetic.lens_nz(3), base,
                         _fourier_ells(12, 20.0, 15000.0))
     if name in ("real_3x2pt_tatt", "real_3x2pt_tatt_small"):
@@ -107,6 +114,21 @@ def make(name: str) -> Workload:
         w.cfg.one_loop_bias = 1
         w.name = name
         w.tatt = True
+        return w
+    if name == "real_3x2pt_small_hdi":
+        w = make("real_3x2pt_small")
+        w.cfg.high_def_integration = 1
+        ex = [(0, 3), (1, 2)]
+        w.cfg.n_ggl_exclude = len(ex)
+        for i, (zl, zs) in enumerate(ex):
+            w.cfg.ggl_exclude[2 * i] = zl
+            w.cfg.ggl_exclude[2 * i + 1] = zs
+        w.name = name
+        return w
+    if name == "real_3x2pt_small_lin":
+        w = make("real_3x2pt_small")
+        w.cfg.linear_pk = 1
+        w.name = name
         return w
     if name in ("real_3x2pt_small_nla", "real_3x2pt_small_nlabin"):
         w = make("real_3x2pt_small")
@@ -178,6 +200,18 @@ def scale_cuts(w: Workload, n: int, seed: int = 0):
             idx.extend(sp * nell + np.arange(m))
         ptr.append(len(idx))
     return np.asarray(ptr, dtype=np.int32), np.asarray(idx, dtype=np.int32)
+
+
+def stack_lin(tabs):
+    """The points' linear tables lnPL, [n][nk * nz] (numpy)."""
+    return np.stack([np.ascontiguousarray(t.lnPL).reshape(-1) for t in tabs])
+
+
+def one_table(tabs):
+    """The points with the nonlinear table replaced by the linear one (for
+    callers that pass a single table, which then also feeds the FAST-PT
+    tables)."""
+    return [dataclasses.replace(t, lnP=np.ascontiguousarray(t.lnPL.copy())) for t in tabs]
 
 
 def stack(tabs):

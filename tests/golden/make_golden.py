@@ -21,7 +21,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
          "fastpt_bias", "fastpt_ia", "real_3x2pt_tatt_small", "real_3x2pt_small_mag",
-         "real_3x2pt_small_nla", "real_3x2pt_small_nlabin"]
+         "real_3x2pt_small_nla", "real_3x2pt_small_nlabin", "real_3x2pt_small_hdi",
+         "real_3x2pt_small_lin"]
 
 # J_abJ1J2Jk rows {alpha, beta, J1, J2, Jk} checked on the batched FAST-PT grid
 JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]

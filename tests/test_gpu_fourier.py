@@ -49,10 +49,11 @@ def fourier_case(name, npts, prec, ell, seed=3, bmag=False):
     import oracle as O
     w = workloads.make(name)
     tabs, nus = workloads.points(w, npts, seed=seed, bmag=bmag)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts, linear_table=True)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     lmax_shear = 0.7 * np.max(ell)
-    dv = plan.eval_fourier(om, h0, chi, G, lnP, nus, ell, lmax_shear=lmax_shear)
+    dv = plan.eval_fourier(om, h0, chi, G, lnP, nus, ell, lmax_shear=lmax_shear,
+                           lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
     tatt = w.cfg.ia_model == abi.IA_TATT

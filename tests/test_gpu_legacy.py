@@ -17,7 +17,9 @@ from test_gpu_real import REL, rel_err, rel_err_spectra
 def legacy_case(gpu_lib, oracle_built):
     import oracle as O
     w = workloads.make("real_3x2pt_small")
+    # the legacy setters take one table: both spectra are the linear one
     tabs, nus = workloads.points(w, 1, seed=17)
+    tabs = workloads.one_table(tabs)
     lg = L.load()
     keep = L.set_state(lg, w, tabs[0], nus[0], lib.PREC_MIXED)
     o = O.Oracle("orc")

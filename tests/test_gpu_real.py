@@ -85,9 +85,9 @@ def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=N
     if nu_tweak is not None:
         for i, nu in enumerate(nus):
             nu_tweak(i, nu)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts, linear_table=True)
     om, h0, chi, G, lnP = workloads.stack(tabs)
-    dv = plan.eval_real(om, h0, chi, G, lnP, nus)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
     worst = {}
@@ -322,9 +322,9 @@ def test_tatt_one_loop_vs_reference_golden(gpu_lib, oracle_built):
                                 "real_3x2pt_tatt_small.npz"))
     w = workloads.make("real_3x2pt_tatt_small")
     tabs, nus = workloads.points(w, 2, seed=11)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=2)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=2, linear_table=True)
     om, h0, chi, G, lnP = workloads.stack(tabs)
-    dv = plan.eval_real(om, h0, chi, G, lnP, nus)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
     for i in range(2):
@@ -348,9 +348,9 @@ def test_cl_nonlimber_batched(gpu_lib, oracle_built):
     import oracle as O
     w = workloads.make("real_3x2pt_small")
     tabs, nus = workloads.points(w, 3, seed=23)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=3)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=3, linear_table=True)
     om, h0, chi, G, lnP = workloads.stack(tabs)
-    cl, conv = plan.cl_nonlimber(om, h0, chi, G, lnP, nus)
+    cl, conv = plan.cl_nonlimber(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
     for i in range(3):
