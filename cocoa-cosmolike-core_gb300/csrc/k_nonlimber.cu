@@ -609,8 +609,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   //   mixed plan: [lxk: nchi float][pcf: 3 nk float, psf: nk float] and the
   //     FP64 slice psl only during set-up, in fb;
   //   FP64 plan:  [psl, plkd, pinv: nk double][lxk: nchi double]
-  //   adjoint: [G00, G01, M00, M01: nchi T] after xs, the slice adjoint
-  //   [nk] last
+  //   adjoint: [G00, G01: nchi T] after xs, the slice adjoint [nk] last;
+  //   the magnification terms M00, M01 in the FFT buffer that the last
+  //   (j = 2) transform leaves free, until the pair's sums read them
   ct<T>* fa = (ct<T>*)smem_raw;
   ct<T>* fb = fa + Q.nmax;
   T* F0 = (T*)(fb + Q.nmax);
@@ -618,9 +619,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   T* xs = F1 + nchi;
   T* G00 = xs + nchi;
   T* G01 = G00 + nchi;
-  T* M00 = G01 + nchi;
-  T* M01 = M00 + nchi;
-  T* plk = ADJ ? M01 + nchi : xs + nchi;
+  T* M00 = nullptr;
+  T* M01 = nullptr;
+  T* plk = ADJ ? G01 + nchi : xs + nchi;
   constexpr bool F32 = sizeof(T) == sizeof(float);
   float* lxkf = (float*)(plk + P.pkl_nk);
   float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
@@ -786,6 +787,11 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         }
         __syncthreads();
         ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
+        if (ADJ && j == 2) {
+          // 2 nmax T >= 2 nchi T of scratch (N >= nchi + 2 pad)
+          M00 = (T*)((r == fa) ? fb : fa);
+          M01 = M00 + nchi;
+        }
         T sc0, sc1;
         if constexpr (F32) {
           sc0 = Q.sckf[j * LNL + k];
@@ -1049,7 +1055,7 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
   size_t sm = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
               (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
                    : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
-  if (adj) sm += sizeof(T) * 4 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
+  if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
   return sm;
 }
 
