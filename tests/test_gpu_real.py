@@ -219,6 +219,19 @@ def test_nla_stretch_bias_models(gpu_lib, oracle_built, prec, name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+@pytest.mark.parametrize("name", ["real_3x2pt_small_hdi", "real_3x2pt_small_lin"])
+def test_hdi_exclusions_linear_mode(gpu_lib, oracle_built, prec, name):
+    """high_def_integration = 1 (larger Gauss-Legendre sets) with two ggl
+    pairs excluded, and the linear run mode (every spectrum from p_lin):
+    the points of the fixtures of the same names."""
+    worst, _ = run_case(name, 2, prec, seed=11)
+    print(prec, name, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_many_theta_bins(gpu_lib, oracle_built, prec):
     """40 angular bins: the 2 x 40 xi filter rows span two row tiles of the
     Legendre contraction."""
