@@ -231,6 +231,34 @@ def test_hdi_exclusions_linear_mode(gpu_lib, oracle_built, prec, name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("probes,keys", [(abi.PROBE_XI, ("xi+", "xi-")),
+                                         (abi.PROBE_GAMMAT | abi.PROBE_WTHETA, ("gammat", "w"))])
+def test_probe_subsets(gpu_lib, oracle_built, probes, keys):
+    """A plan with some probes off (like.shear_shear / shear_pos / pos_pos):
+    the enabled blocks against the oracle with the same switches, the
+    disabled ones zero, at the full vector's offsets."""
+    import oracle as O
+    w = workloads.make("real_3x2pt_small")
+    w.cfg.probes = probes
+    tabs, nus = workloads.points(w, 2, seed=13)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=2, linear_table=True)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    for i in range(2):
+        o.set_point(tabs[i], nus[i])
+        ref = blocks(plan, o.data_vector_real())
+        got = blocks(plan, dv[i])
+        for k in got:
+            if k in keys:
+                err = rel_err_env(got[k], ref[k], None, floor=PAIR_FLOOR, ntheta=w.cfg.ntheta)
+                assert err <= REL, (k, err)
+            else:
+                assert np.all(got[k] == 0.0), k
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_many_theta_bins(gpu_lib, oracle_built, prec):
     """40 angular bins: the 2 x 40 xi filter rows span two row tiles of the
