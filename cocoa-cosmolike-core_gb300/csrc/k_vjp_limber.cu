@@ -395,9 +395,11 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   T* xt = (T*)(xs + (size_t)np * nn);  // [np][nn]
   T* wxs = xt + (size_t)np * nn;       // [np][nn]
   T* cbs = wxs + (size_t)np * nn;      // [np][LC]
-  // one-loop bK (only with the gate on): per source the sums over l of
-  // (l+1/2)^2 pref2 F P C_bar (FP64 and chunk), and W_K
+  // one-loop bK (only with the gate on): the node's sum over l and sources
+  // of (l+1/2)^2 pref2 F P C_bar W_K (the K adjoint); with bK != 0 also per
+  // source the sums without W_K (FP64 and chunk), for the W_K adjoint
   const bool kon = P.one_loop && V.one_loop_on[pt];
+  const bool kvec = kon && P.nu[pt].gb[5][q] != 0.0;
   double* ys = (double*)(cbs + (size_t)np * LC);
   T* yt = (T*)(ys + (kon ? (size_t)np * nn : 0));
   T* wks = yt + (kon ? (size_t)np * nn : 0);
@@ -434,7 +436,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   PWalk<T> wk;
-  double lb0 = 0.0, lb1 = 0.0;
+  double lb0 = 0.0, lb1 = 0.0, kbs = 0.0;
   for (int L0 = 0; L0 < K; L0 += LC) {
     const int nL = min(LC, K - L0);
     __syncthreads();
@@ -444,7 +446,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     }
     __syncthreads();
     if (!act) continue;
-    T t0 = 0, t1 = 0;
+    T t0 = 0, t1 = 0, tk = 0;
     for (int l = 0; l < nL; l++) {
       const int L = L0 + l;
       T dx, pref, g, lp2 = (T)0;
@@ -465,7 +467,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
       }
       const T gl = g * (Lt + pref * Mt);
       T sx = 0, sk = 0;
-      if (kon) {
+      if (kvec) {
         const T gk = g * lp2;
         for (int m = 0; m < np; m++) {
           const T cv = cbs[m * LC + l];
@@ -474,7 +476,18 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
           xt[m * nn + p] += gl * cv;
           yt[m * nn + p] += gk * cv;
         }
+        tk += gk * sk;
         sk *= gk * Kt;
+      } else if (kon) {
+        // bK = 0: K = 0, so no W_K adjoint and no lnP term
+        for (int m = 0; m < np; m++) {
+          const T cv = cbs[m * LC + l];
+          sx += cv * wxs[m * nn + p];
+          sk += cv * wks[m * nn + p];
+          xt[m * nn + p] += gl * cv;
+        }
+        tk += g * lp2 * sk;
+        sk = (T)0;
       } else {
         for (int m = 0; m < np; m++) {
           const T cv = cbs[m * LC + l];
@@ -488,11 +501,12 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
     }
     lb0 += (double)t0;
     lb1 += (double)t1;
+    kbs += (double)tk;
     for (int m = 0; m < np; m++) {
       xs[m * nn + p] += (double)xt[m * nn + p];
       xt[m * nn + p] = (T)0;
     }
-    if (kon) {
+    if (kvec) {
       for (int m = 0; m < np; m++) {
         ys[m * nn + p] += (double)yt[m * nn + p];
         yt[m * nn + p] = (T)0;
@@ -504,14 +518,10 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   double* xbar = V.wbar_gx + b0 * P.ns * nn;
   for (int m = 0; m < np; m++) xbar[ss_[m] * nn + p] += xs[m * nn + p];
   if (kon) {
-    // W_K (source photo-z) and K adjoints of the bK term
-    double kb = 0.0;
-    for (int m = 0; m < np; m++) {
-      const size_t o = (b0 * P.ns + ss_[m]) * nn + p;
-      kb += P.wgs_k[o] * ys[m * nn + p];
-      V.wbar_gsk[o] += Kw * ys[m * nn + p];
-    }
-    V.kbar_gs[b0 * nn + p] += kb;
+    // K adjoint of the bK term, and with bK != 0 the W_K (source photo-z) one
+    if (kvec)
+      for (int m = 0; m < np; m++) V.wbar_gsk[(b0 * P.ns + ss_[m]) * nn + p] += Kw * ys[m * nn + p];
+    V.kbar_gs[b0 * nn + p] += kbs;
   }
   V.lbar_gs[(b0 * 2 + 0) * nn + p] = lb0;
   V.lbar_gs[(b0 * 2 + 1) * nn + p] = lb1;
