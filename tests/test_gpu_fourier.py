@@ -111,6 +111,18 @@ def test_fourier_nla_stretch_bias_model(gpu_lib, oracle_built, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+@pytest.mark.parametrize("name", ["real_3x2pt_small_hdi", "real_3x2pt_small_lin", "real_3x2pt_small_nlabin"])
+def test_fourier_config_variants(gpu_lib, oracle_built, prec, name):
+    """high_def_integration = 1 with ggl exclusions, the linear run mode, and
+    NLA per-bin amplitudes with bias model 2, on the Fourier vector."""
+    ell = fourier_ells(26, 20.0, 5000.0)
+    worst, _ = fourier_case(name, 2, prec, ell)
+    print(prec, name, worst)
+    assert worst <= REL, worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
 def test_fourier_unsorted_ells(gpu_lib, oracle_built, prec):
     """Caller multipoles in any order, down to l = 3 where the chi(a_min)
     cut of C_gg removes nodes (the mixed plan's cut falls back from a
