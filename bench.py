@@ -136,6 +136,40 @@ def cpu_sample(w, data, budget_s=12.0, min_pts=2, threads=None):
     return n, el
 
 
+def parity_spot(w, data, dv, idxs, n_xi, n_gt, nt):
+    """Spot check of the timed batch's data vectors against the FP64 oracle:
+    the largest relative error per entry (plain, and with entries below
+    1e-4 of their spectrum's peak held to that floor, the zero-crossing
+    rule) and the number of entries above 1e-4 plain."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    worst_f = worst_p = 0.0
+    above = total = 0
+    for i in idxs:
+        o.set_point(data["tabs"][i], data["nus"][i])
+        ref = o.data_vector_real()
+        a = n_xi // 2
+        for lo, hi in ((0, a), (a, n_xi), (n_xi, n_xi + n_gt), (n_xi + n_gt, len(ref))):
+            if hi <= lo:
+                continue
+            r = ref[lo:hi].reshape(-1, nt)
+            g = dv[i, lo:hi].reshape(-1, nt)
+            err = np.abs(g - r)
+            peak = np.abs(r).max(axis=1, keepdims=True)
+            plain = err / np.maximum(np.abs(r), 1e-300)
+            floored = err / np.maximum(np.abs(r), 1e-4 * peak + 1e-300)
+            worst_f = max(worst_f, float(floored.max()))
+            worst_p = max(worst_p, float(plain.max()))
+            above += int(np.count_nonzero(plain > 1e-4))
+            total += plain.size
+    return {"points": [int(i) for i in idxs], "entries": total,
+            "max_rel_err_floored": worst_f, "max_rel_err_plain": worst_p,
+            "entries_above_1e-4_plain": above,
+            "rule": "floored: entries below 1e-4 of their spectrum's peak are held to 1e-4 of the peak"}
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm on the host cores."""
     rank, world, _ = dist_env()
@@ -373,18 +407,6 @@ def run_serving(args):
     plan.close()
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def profile_traffic(name, points):
-    """DRAM bytes per launch from a committed ncu summary (scaled to the
-    points of one launch), or None."""
-    try:
-        txt = open(os.path.join(ROOT, "profiles", name)).read()
-        b = float(txt.split("traffic_bytes_per_launch:")[1].split()[0])
-        n = float(txt.split("points_per_launch:")[1].split()[0])
-        return b * points / n
-    except (OSError, IndexError, ValueError):
-        return None
 
 
 def plan_fourier_size(plan, nell):
@@ -638,29 +660,65 @@ def main():
         vg4 = value_grad(plan4, w4, data4, *t4, T(data4["nub"]), None, stream, args)
         plan4.close()
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel group.  The library records one
+    # event pair per launch group per wave (and, for the FFTLog stage, one
+    # for its second-stream transforms as well), so the per-step group time
+    # is the figure to divide by: achieved = algorithmic bytes per point x
+    # the points of one step / that group's event time per step.
     hbm, src = peaks()
     top = max(kms, key=lambda k: kms[k])
-    per_launch_ms = kms[top] / max(kl[top], 1)
+    step_ms = kms[top] / args.steps
+    wave = min(B, 256)
+    waves = -(-B // wave)
     nk, nz = plan.shapes["nk"], plan.shapes["nz"]
     pss, pgs, pgg = plan.n_xi // (2 * w.cfg.ntheta), plan.n_gammat // w.cfg.ntheta, w.cfg.n_lens
     nnode = w.cfg.lmin_tab - 1 + w.cfg.n_ell
-    # algorithmic bytes per point for each kernel (roofline rules)
+    nt = w.cfg.ntheta
+    # algorithmic bytes per point of each kernel group (the counting rules:
+    # compulsory P(k,z) table read + node-table write for the Limber
+    # kernels, the C_l tables read + observables written for the
+    # contraction, the radial kernels + C_l for the FFTLog stage)
     per_point = {
         "k_limber_ss": 8 * nk * nz + 8 * pss * nnode,
         "k_limber_gs": 8 * nk * nz + 8 * pgs * nnode,
         "k_limber_gg": 8 * nk * nz + 8 * pgg * nnode,
         "k_limber_ggl": 8 * nk * nz + 16 * pgg * w.cfg.lmax_nolimber,
-        "k_nonlimber": 8 * (plan.shapes["chi"] + plan.shapes["G"]) + 16 * nk + 8 * pgg * w.cfg.lmax_nolimber,
-        "k_contract": 8 * (pss + pgs + pgg) * nnode + 8 * plan.n_total,
+        "k_nonlimber": 8 * w.cfg.nl_nchi * 3 * pgg + 8 * pgg * w.cfg.lmax_nolimber,
+        "k_contract": 8 * (pss + pgs + pgg) * nnode + 8 * pgg * w.cfg.lmax_nolimber + 8 * plan.n_total,
         "k_gtab": 8 * plan.shapes["chi"] + 8 * w.cfg.n_source * w.cfg.n_a,
         "k_nodes": 8 * (plan.shapes["chi"] + plan.shapes["G"]),
         "k_assemble": 16 * plan.n_total,
     }
-    pts_per_launch = min(B, 256)
-    alg = per_point[top] * pts_per_launch
-    achieved = alg / (per_launch_ms / 1e3) / 1e9
-    traffic = profile_traffic("k_nl_loop_real_3x2pt_traffic.md", pts_per_launch) if top == "k_nonlimber" else None
+    alg_step = per_point.get(top, 0) * B
+    achieved = alg_step / (step_ms / 1e3) / 1e9 if step_ms > 0 else None
+    # arithmetic of the same group by the counting rules (integrand
+    # evaluations x a fixed cost for the Limber kernels, 2 K per output for
+    # the contraction, 2.5 N log2 N per real transform + 10 N_chi per
+    # multipole and radial kernel for the FFTLog loop), against the nominal
+    # FP32 rate (SMs x 128 lanes x 2 x the sampled SM clock)
+    conv = np.concatenate([plan.nonlimber(i)[1] for i in range(min(wave, B))]) \
+        if top == "k_nonlimber" else None
+    nl_n = [900, 1500, 1500] if w.cfg.nl_nchi == 500 else None
+    flops_pt = {
+        "k_limber_ss": 12.0 * nnode * pss * 64,
+        "k_limber_gs": 20.0 * nnode * pgs * 64,
+        "k_limber_gg": 30.0 * nnode * pgg * 96,
+        "k_contract": 2.0 * nnode * nt * (2 * pss + pgs + pgg),
+    }
+    if conv is not None and nl_n is not None:
+        per_l = sum(2.5 * n * np.log2(n) + 10 * w.cfg.nl_nchi for n in nl_n[:2])
+        flops_pt["k_nonlimber"] = float(conv.mean()) * pgg * per_l
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    pipe = None
+    if top in flops_pt and step_ms > 0:
+        tf = flops_pt[top] * B / (step_ms / 1e3) / 1e12
+        pipe = {"unit": "TFLOP/s", "achieved": tf, "peak": fp32_peak, "frac": tf / fp32_peak,
+                "peak_source": f"nominal FP32: {sms} SMs x 128 lanes x 2 x {mhz:.0f} MHz",
+                "flops_per_point": flops_pt[top]}
+        if conv is not None:
+            pipe["mean_handover_multipole"] = float(conv.mean())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -674,10 +732,11 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                     "traffic_source": "profiles/k_nl_loop_real_3x2pt_traffic.md (ncu, multipole-loop launch)"
-                     if traffic else None,
-                     "algorithmic_bytes_per_launch": alg, "peak_source": src},
+                     "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_point": per_point.get(top),
+                     "algorithmic_bytes_per_launch": per_point.get(top, 0) * wave,
+                     "launches_per_step": waves, "group_ms_per_step": step_ms,
+                     "peak_source": src, "pipe": pipe},
         "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items()},
         "clocks": clocks,
         "fp64_plain_gpu": {"value": fp64, "unit": UNIT,
@@ -689,6 +748,10 @@ def main():
     if vg4 is not None:
         vg4["value"] *= world
         line["value_grad_tatt"] = vg4
+    if rank == 0 and not args.no_cpu:
+        dv_last = out.cpu().numpy()
+        line["parity"] = parity_spot(w, data, dv_last, [0, B // 3, (2 * B) // 3, B - 1], plan.n_xi,
+                                     plan.n_gammat, w.cfg.ntheta)
     if rank == 0 and world == 1 and not args.no_cpu:
         n, t = cpu_sample(w, data, budget_s=12.0)
         line["cpu_baseline"] = {"value": n / t, "unit": UNIT, "cores": os.cpu_count(),

@@ -3,9 +3,8 @@
 // Some callers of a likelihood library cannot call cudaMalloc at the point
 // where they need J_abl: a host framework that has already reserved the
 // device's memory for its own pool (so a fresh allocation fails or
-// fragments that pool), a process running under a fixed device-memory
-// quota, or code that must not allocate between the start and the end of
-// a stream capture.  cl2pt_J_abl_noalloc serves them: the caller passes
+// fragments that pool), or a process running under a fixed device-memory
+// quota.  cl2pt_J_abl_noalloc serves them: the caller passes
 // its own device input and output arrays, and everything else the
 // transform needs -- the FFT twiddles and digit-reversal maps, the
 // Gamma-ratio kernels, the term program and the convolution workspace --
@@ -25,7 +24,11 @@
 // other host threads) therefore race and must be serialised by the
 // caller.  The first call on each device resolves the array's address
 // with cudaGetSymbolAddress and sets the FFT kernels' shared-memory limit;
-// make that first call before any stream capture begins.
+// make that first call before any stream capture begins.  The resolved
+// address is cached per device for the life of the process: it assumes the
+// device's primary context is not torn down (no cudaDeviceReset) between
+// calls.  Each call copies x to the device, reads the error flag back and
+// waits for the caller's stream before it returns.
 #include <cuda_runtime.h>
 #include <math_constants.h>
 

@@ -116,7 +116,7 @@ int cl2pt_J_abl(const double* x, const double* fx, long N, const int* alpha,
 /* J_abl without any device allocation.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc when they need J_abl
  * (a host framework that has reserved the device memory for its own pool,
- * a fixed device-memory quota, a stream being captured).  fx [N] and
+ * or a fixed device-memory quota).  fx [N] and
  * Fy [Nterms][N] are the caller's DEVICE arrays; x, alpha, beta, ell and
  * config are host values as in cl2pt_J_abl.  All tables and workspace are
  * rebuilt per call in one static 10 MiB device array that every GPU
@@ -125,9 +125,10 @@ int cl2pt_J_abl(const double* x, const double* fx, long N, const int* alpha,
  * requests return CL2PT_ERR_ARG with a message on stderr).  Calls share
  * that array: calls whose work overlaps on the GPU race, so serialise
  * them.  The first call on each device looks up the array's address and
- * sets kernel attributes; make it before any stream capture.  The call
- * waits for its stream and returns CL2PT_ERR_FFT on an extrapolation
- * failure. */
+ * sets kernel attributes; make it before any stream capture.  That
+ * address is cached for the life of the process (no cudaDeviceReset
+ * between calls).  The call waits for its stream and returns
+ * CL2PT_ERR_FFT on an extrapolation failure. */
 int cl2pt_J_abl_noalloc(const double* x, const double* fx, long N, const int* alpha,
                         const int* beta, const int* ell, int Nterms,
                         const cl2pt_fastpt_config* config, double* Fy, void* stream);

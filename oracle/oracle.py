@@ -24,7 +24,16 @@ from cl2pt import abi  # noqa: E402
 
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libcosmolike_ref.so")
-REFERENCE_TREE = "/root/reference"
+
+
+def reference_tree() -> str:
+    """Root of the reference source tree: $CL2PT_REFERENCE_TREE, else the
+    recipe's default (the Makefile's REF)."""
+    env = os.environ.get("CL2PT_REFERENCE_TREE")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -35,11 +44,12 @@ def build(ref: bool | None = None, quiet: bool = True) -> None:
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"], check=True,
                    stdout=out)
+    tree = reference_tree()
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_TREE, "cosmolike"))
+        ref = bool(tree) and os.path.isdir(os.path.join(tree, "cosmolike"))
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"-j{os.cpu_count() or 4}",
-                        f"REF={REFERENCE_TREE}"], check=True, stdout=out)
+                        f"REF={tree}"], check=True, stdout=out)
 
 
 def _p(a):

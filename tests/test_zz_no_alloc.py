@@ -3,8 +3,10 @@
 
 Two calls in a row on different spectra (and a third with another term
 list), so contents the shared array keeps from the previous call cannot
-leak into the next result.  Tolerance: the FAST-PT bar (1e-6 relative per
-entry, entries below 1e-4 of a spectrum's peak held to that floor).
+leak into the next result; the first result is also checked against the
+CPU oracle (the reference's J_abl restated in C).  Tolerance: the FAST-PT
+bar (1e-6 relative per entry, entries below 1e-4 of a spectrum's peak held
+to that floor).
 """
 import ctypes as C
 
@@ -36,14 +38,15 @@ def noalloc(x, fx_dev, alpha, beta, ell, out_dev, cfg, stream):
 
 
 @pytest.mark.gpu
-def test_J_abl_noalloc_matches_J_abl(gpu_lib):
+def test_J_abl_noalloc_matches_J_abl(gpu_lib, oracle_built):
     import torch
+    import oracle as O
     k, P, _ = workloads.fastpt_spectra(3, seed=21)
     a, b, l, _, _ = lib.bias_terms()
     cfg = lib.fastpt_config()
     stream = torch.cuda.current_stream().cuda_stream
     cases = [(P[0], a, b, l), (P[1], a, b, l), (P[2], [0, 1, 2], [0, -1, 0], [2, 1, 0])]
-    for fx, aa, bb, ll in cases:
+    for i, (fx, aa, bb, ll) in enumerate(cases):
         ref = lib.J_abl(k, fx, aa, bb, ll, cfg)  # the allocating entry point
         fx_d = torch.tensor(fx, device="cuda")
         out = torch.full((len(aa), len(k)), float("nan"), dtype=torch.float64, device="cuda")
@@ -52,6 +55,11 @@ def test_J_abl_noalloc_matches_J_abl(gpu_lib):
         err = rel_rows(out.cpu().numpy(), ref)
         print("noalloc vs J_abl", err)
         assert err <= REL, err
+        if i == 0:
+            orc = O.Oracle("orc").J_abl(k, fx, aa, bb, ll)
+            err_o = rel_rows(out.cpu().numpy(), orc)
+            print("noalloc vs oracle", err_o)
+            assert err_o <= REL, err_o
 
 
 @pytest.mark.gpu
@@ -63,5 +71,25 @@ def test_J_abl_noalloc_rejects_oversize(gpu_lib):
     out = torch.zeros((17, len(k)), dtype=torch.float64, device="cuda")
     z = np.zeros(17, dtype=np.int32)
     assert noalloc(k, fx_d.data_ptr(), z, z, z, out.data_ptr(), cfg, None) == -1  # > 16 terms
-    big = lib.fastpt_config(npad=3000)  # N = 2048 + 7000 > 7262 points
+    # padded size N = N0 + 2 N_pad + N_extrap_low + N_extrap_high must stay
+    # within FPT_NOALLOC_MAX_N = 7231 (Ntot >= 2N + 1 <= 14464 points)
+    big = lib.fastpt_config(npad=2093)  # N = 2048 + 4186 + 1000 = 7234 > 7231
     assert noalloc(k, fx_d.data_ptr(), z[:1], z[:1], z[:1], out.data_ptr(), big, None) == -1
+
+
+@pytest.mark.gpu
+def test_J_abl_noalloc_at_the_limit(gpu_lib):
+    """npad = 2076 gives N = 7200 (7-smooth), Ntot = 14406: just inside the
+    static array's bound, so it is accepted and matches cl2pt_J_abl."""
+    import torch
+    k, P, _ = workloads.fastpt_spectra(1, seed=23)
+    a, b, l, _, _ = lib.bias_terms()
+    cfg = lib.fastpt_config(npad=2076)
+    ref = lib.J_abl(k, P[0], a, b, l, cfg)
+    fx_d = torch.tensor(P[0], device="cuda")
+    out = torch.full((len(a), len(k)), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    assert noalloc(k, fx_d.data_ptr(), a, b, l, out.data_ptr(), cfg, stream) == 0
+    err = rel_rows(out.cpu().numpy(), ref)
+    print("noalloc at the limit vs J_abl", err)
+    assert err <= REL, err
