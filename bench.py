@@ -31,6 +31,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "cocoa-cosmolike-core_gb300"))
 
 METRIC = "3x2pt data vectors/s (real-space, <=1e-4 rel err vs FP64)"
+# Legendre contraction forms of the mixed plan (cl2pt.h CL2PT_CONTRACT_*)
+CONTRACTS = {"fp32": 0, "tf32x3": 1, "bf16x3": 2, "bf16x6": 3}
 UNIT = "data vectors/s"
 
 
@@ -540,6 +542,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
+    ap.add_argument("--contract", default="tf32x3", choices=sorted(CONTRACTS),
+                    help="Legendre contraction of the mixed plan")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -563,6 +567,7 @@ def main():
     B = args.batch
     data = make_batch(w, B, seed=walker_seed(100, rank))
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=B)
+    plan.set_contraction(CONTRACTS[args.contract])
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     d_om, d_h0, d_chi, d_G, d_lnP = (T(data[k]) for k in ("om", "h0", "chi", "G", "lnP"))
     d_nu = T(data["nub"])
@@ -601,6 +606,7 @@ def main():
     launches = plan.launches() * args.steps
     ms = max_over_ranks(ms, dev)
     value = world * B * args.steps / (ms / 1e3)
+    dv_timed = out.cpu().numpy()  # the last timed step's data vectors
 
     # ---- e2e through the C ABI with pinned host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -724,7 +730,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
         "data": "synthetic (EH no-wiggle P(k,z) per point, LCDM chi/D, seeded n(z) and nuisances)",
-        "config": {"workload": args.workload, "points_per_step_per_gpu": B,
+        "config": {"workload": args.workload, "points_per_step_per_gpu": B, "contraction": args.contract,
                    "n_data": plan.n_total, "lmax": w.cfg.lmax, "n_ell": w.cfg.n_ell,
                    "pk_table": [nk, nz], "l2": "inputs > L2 (no flush)",
                    "parallelism": f"replicas x{world}"},
@@ -749,8 +755,7 @@ def main():
         vg4["value"] *= world
         line["value_grad_tatt"] = vg4
     if rank == 0 and not args.no_cpu:
-        dv_last = out.cpu().numpy()
-        line["parity"] = parity_spot(w, data, dv_last, [0, B // 3, (2 * B) // 3, B - 1], plan.n_xi,
+        line["parity"] = parity_spot(w, data, dv_timed, [0, B // 3, (2 * B) // 3, B - 1], plan.n_xi,
                                      plan.n_gammat, w.cfg.ntheta)
     if rank == 0 and world == 1 and not args.no_cpu:
         n, t = cpu_sample(w, data, budget_s=12.0)

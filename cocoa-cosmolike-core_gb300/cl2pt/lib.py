@@ -16,6 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcl2pt.so")
 
 PREC_MIXED, PREC_FP64 = 0, 1
+# Legendre contraction of a mixed plan (CL2PT_CONTRACT_*)
+CONTRACT_FP32, CONTRACT_TF32X3, CONTRACT_BF16X3, CONTRACT_BF16X6 = 0, 1, 2, 3
 # kernel ids of cl2pt_kernel_times (CL2PT_K_* in include/cl2pt.h)
 KERNELS = ["k_gtab", "k_nodes", "k_limber_ss", "k_limber_gs", "k_limber_gg", "k_limber_ggl",
            "k_nonlimber", "k_contract", "k_assemble", "k_vjp"]
@@ -64,6 +66,8 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_plan_create.argtypes = [C.POINTER(abi.Config), C.POINTER(abi.NZ), C.POINTER(abi.NZ),
                                       C.POINTER(Grid), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
     lib.cl2pt_plan_destroy.argtypes = [C.c_void_p]
+    lib.cl2pt_plan_set_contraction.argtypes = [C.c_void_p, C.c_int]
+    lib.cl2pt_plan_get_contraction.argtypes = [C.c_void_p, _ip]
     lib.cl2pt_real_sizes.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
     lib.cl2pt_eval_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]
@@ -171,6 +175,16 @@ class Plan:
         sz = [C.c_int() for _ in range(4)]
         check(lib.cl2pt_real_sizes(h, *[C.byref(s) for s in sz]))
         self.n_xi, self.n_gammat, self.n_w, self.n_total = (s.value for s in sz)
+
+    def set_contraction(self, mode: int):
+        """CONTRACT_FP32 (CUDA cores) or a tensor-core form (CONTRACT_TF32X3,
+        CONTRACT_BF16X3, CONTRACT_BF16X6) for the Legendre contraction."""
+        check(load().cl2pt_plan_set_contraction(self.h, mode), "cl2pt_plan_set_contraction")
+
+    def contraction(self) -> int:
+        m = C.c_int()
+        check(load().cl2pt_plan_get_contraction(self.h, C.byref(m)))
+        return m.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -17,39 +17,12 @@
 // spectrum's peak |value|), so the result is good to ~1e-9 of the peak at a
 // fraction of the cost of the FP64 pipe (1/64 of the FP32 rate on GB300).
 #include "common.cuh"
+#include "contract.cuh"
 #include "kernels.cuh"
 
 namespace cl2pt {
 
 constexpr int BM = 64, BN = 64, BK = 32, CT = 256;
-
-// C_l column value of node k for output column col = point * npair + pair
-// (see k_contract): the tables are [point][pair][node], so the column's row
-// starts at col * (row length)
-__device__ __forceinline__ double contract_col(const Params& P, int mode, int col, int k)
-{
-  if (mode == 0)
-    return (k < P.nnode_ss) ? P.tab_ss[(size_t)col * P.nnode_ss + k]
-                            : P.tab_ss_bb[(size_t)col * P.nnode_ss + (k - P.nnode_ss)];
-  if (mode == 1) return P.tab_gs[(size_t)col * P.nnode_g + k];
-  if (mode == 2) return P.tab_gg[(size_t)col * P.nnode_g + k];
-  const int LNL = P.lmax_nolimber;
-  return (k < LNL) ? P.cnl[(size_t)col * LNL + k] : P.tab_gg[(size_t)col * P.nnode_g + (k - LNL)];
-}
-
-// observable index of (filter row m, column col) in the per-point layout
-__device__ __forceinline__ double* contract_out(const Params& P, int mode, int npair, int m, int col)
-{
-  const int pt = col / npair, pr = col - pt * npair;
-  const int nt = P.ntheta;
-  const int n_xi = 2 * nt * P.pss, n_gt = nt * P.pgs;
-  const int n_total = n_xi + n_gt + nt * P.nl;
-  int idx;
-  if (mode == 0) idx = (m < nt) ? pr * nt + m : n_xi / 2 + pr * nt + (m - nt);
-  else if (mode == 1) idx = n_xi + pr * nt + m;
-  else idx = n_xi + n_gt + pr * nt + m;
-  return P.obs + (size_t)pt * n_total + idx;
-}
 
 // error-free FP32 sum a + b = s + e (Knuth's TwoSum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)

@@ -1,7 +1,11 @@
 // kernels.cuh -- launchers of the cl2pt pipeline stages.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
 
 #include "common.cuh"
 
@@ -47,6 +51,23 @@ struct SplitFilter {
 void launch_legendre(const Params& P, const double* filt_xi, const double* filt_gt,
                      const double* filt_gg, const double* filt_gg_nl, const SplitFilter* split,
                      cudaStream_t s, int* launches, const Hook& hk);
+// The same contraction on the tcgen05 tensor cores (k_contract_tc.cu):
+// one filter matrix as S pieces of the MMA input type, [S][Np][Kpad]
+// (M rows padded to Np = 16k <= 64, K to whole 128-byte chunks), and its
+// TMA tensor map (128-byte swizzle).  kind 0: TF32 pieces; 1: BF16 pieces.
+struct TCFilter {
+  CUtensorMap map;
+  int M, Np, K, Kpad;
+};
+// host: the pieces of filt [M][K] (-1 when M > 64), the tensor map over
+// their device copy (-1 when the driver's encoder is unavailable)
+int tc_contract_pieces(int kind, int S, const double* filt, int M, int K, std::vector<uint8_t>& out, int* Np,
+                       int* Kpad);
+int tc_contract_map(int kind, int S, void* dev, int Np, int Kpad, CUtensorMap* map);
+// f: the four filters (xi, gamma_t, w Limber, w non-Limber); S = 2 or 3
+// pieces (3 only with kind 1)
+void launch_legendre_tc(const Params& P, const TCFilter* f, int kind, int S, cudaStream_t s, int* launches,
+                        const Hook& hk);
 // Fourier data vector dv[pt][nell (pss + pgs + nl)] from the node tables
 void launch_assemble_fourier(const Params& P, int nell, const double* ell, double lmax_shear, int use_nl,
                              const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk);

@@ -322,6 +322,8 @@ bool increasing(const double* p, int n)
     }                               \
   } while (0)
 
+extern "C" int cl2pt_plan_set_contraction(cl2pt_plan* p, int mode);
+
 extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
                                  const cl2pt_nz* lens, const cl2pt_grid* grid, int precision,
                                  int max_batch, cl2pt_plan** out)
@@ -551,6 +553,12 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     TRY(dupload(p, &p->d_lfacf_ss, fsf.data(), fsf.size()));
     TRY(dupload(p, &p->d_lfacf_g, fgf.data(), fgf.size()));
   }
+  p->filt_host[0] = fxi;
+  p->filt_host[1] = fgt;
+  p->filt_host[2] = fgg;
+  p->filt_host[3] = fggnl;
+  p->filt_M[0] = 2 * nt;
+  p->filt_M[1] = p->filt_M[2] = p->filt_M[3] = nt;
   TRY(dupload(p, &p->d_filt_xi, fxi.data(), fxi.size()));
   TRY(dupload(p, &p->d_filt_gt, fgt.data(), fgt.size()));
   TRY(dupload(p, &p->d_filt_gg, fgg.data(), fgg.size()));
@@ -812,6 +820,15 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
+  // mixed plans contract on the tensor cores (TF32x3) when the filters fit
+  // the tensor-core form (2 ntheta <= 64 rows); otherwise on the CUDA cores
+  if (precision == CL2PT_PREC_MIXED && 2 * nt <= 64) {
+    const int st = cl2pt_plan_set_contraction(p, CL2PT_CONTRACT_TF32X3);
+    if (st != CL2PT_OK && st != CL2PT_ERR_UNSUPPORTED) {
+      cl2pt_plan_destroy(p);
+      return st;
+    }
+  }
   *out = p;
   return CL2PT_OK;
 }
@@ -858,6 +875,44 @@ extern "C" const char* cl2pt_status_string(int s)
 }
 
 extern "C" int cl2pt_last_launch_count(const cl2pt_plan* p) { return p ? p->last_launches : 0; }
+
+extern "C" int cl2pt_plan_set_contraction(cl2pt_plan* p, int mode)
+{
+  if (!p || mode < CL2PT_CONTRACT_FP32 || mode > CL2PT_CONTRACT_BF16X6) return CL2PT_ERR_ARG;
+  if (mode == CL2PT_CONTRACT_FP32) {
+    p->contract = mode;
+    return CL2PT_OK;
+  }
+  if (p->prec != CL2PT_PREC_MIXED) return CL2PT_ERR_UNSUPPORTED;
+  if (p->tcf_mode != mode) {
+    const int kind = (mode == CL2PT_CONTRACT_TF32X3) ? 0 : 1, S = (mode == CL2PT_CONTRACT_BF16X6) ? 3 : 2;
+    for (int f = 0; f < 4; f++) {
+      const int M = p->filt_M[f], K = (int)(p->filt_host[f].size() / M);
+      std::vector<uint8_t> pieces;
+      int Np = 0, Kpad = 0;
+      if (cl2pt::tc_contract_pieces(kind, S, p->filt_host[f].data(), M, K, pieces, &Np, &Kpad))
+        return CL2PT_ERR_UNSUPPORTED;  // more than 64 filter rows
+      uint8_t* d = nullptr;
+      if (int st = dupload(p, &d, pieces.data(), pieces.size())) return st;
+      cl2pt::TCFilter& T = p->tcf[f];
+      if (cl2pt::tc_contract_map(kind, S, d, Np, Kpad, &T.map)) return CL2PT_ERR_CUDA;
+      T.M = M;
+      T.Np = Np;
+      T.K = K;
+      T.Kpad = Kpad;
+    }
+    p->tcf_mode = mode;
+  }
+  p->contract = mode;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_plan_get_contraction(const cl2pt_plan* p, int* mode)
+{
+  if (!p || !mode) return CL2PT_ERR_ARG;
+  *mode = p->contract;
+  return CL2PT_OK;
+}
 
 extern "C" int cl2pt_node_limits(const cl2pt_plan* p, double lim_ss[3], double lim_g[3])
 {
@@ -1820,10 +1875,15 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
                                     cudaMemcpyDeviceToDevice, s));
         }
       }
-      cl2pt::SplitFilter sf[4];
-      for (int f = 0; f < 4; f++) sf[f] = {p->d_sfilt[f][0], p->d_sfilt[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};
-      cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, sf,
-                             s, &launches, hk);
+      if (p->contract != CL2PT_CONTRACT_FP32 && P.prec == CL2PT_PREC_MIXED) {
+        cl2pt::launch_legendre_tc(P, p->tcf, p->contract == CL2PT_CONTRACT_TF32X3 ? 0 : 1,
+                                  p->contract == CL2PT_CONTRACT_BF16X6 ? 3 : 2, s, &launches, hk);
+      } else {
+        cl2pt::SplitFilter sf[4];
+        for (int f = 0; f < 4; f++) sf[f] = {p->d_sfilt[f][0], p->d_sfilt[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};
+        cl2pt::launch_legendre(P, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, sf,
+                               s, &launches, hk);
+      }
       cl2pt::launch_assemble(P, dmask, dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr,
                              ddv + (size_t)w0 * p->n_total, s, &launches, hk);
       if (lq) {

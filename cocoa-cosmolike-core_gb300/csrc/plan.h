@@ -55,6 +55,14 @@ struct cl2pt_plan {
   float* d_sfilt[4][2] = {};
   float* d_sfiltr[4][2] = {};  // the same in [M][K] order (the adjoint's transpose)
   int sfilt_Mp[4] = {}, sfilt_Ksp[4] = {};
+  // the Legendre contraction of the mixed plan (CL2PT_CONTRACT_*); the
+  // tensor-core form of the four filters, built when first selected, from
+  // host copies of the FP64 filters ([M][K] each)
+  int contract = CL2PT_CONTRACT_FP32;
+  cl2pt::TCFilter tcf[4];
+  int tcf_mode = -1;
+  std::vector<double> filt_host[4];
+  int filt_M[4] = {};
   // per-point inputs staged on device when the batch is on the host
   double *d_in_om = nullptr, *d_in_h0 = nullptr, *d_in_chi = nullptr, *d_in_G = nullptr,
          *d_in_lnP = nullptr, *d_in_lnPL = nullptr;

@@ -33,6 +33,17 @@ enum {
   CL2PT_PREC_FP64 = 1   /* every stage in FP64 (the plain FP64 GPU form)    */
 };
 
+/* The bin-averaged Legendre contraction of a mixed plan (the FP64 plan
+ * always contracts in FP64).  Each filter and C_l entry is split into
+ * pieces whose pairwise products approximate the FP64 product; partial
+ * sums are folded into FP64 every 32 (TF32) or 64 (BF16) C_l nodes. */
+enum {
+  CL2PT_CONTRACT_FP32 = 0,   /* FP32 head/tail pieces, 3 products, CUDA cores */
+  CL2PT_CONTRACT_TF32X3 = 1, /* tcgen05 tensor cores: TF32 pieces, 3 products */
+  CL2PT_CONTRACT_BF16X3 = 2, /* tcgen05 tensor cores: 2 BF16 pieces, 3 products */
+  CL2PT_CONTRACT_BF16X6 = 3  /* tcgen05 tensor cores: 3 BF16 pieces, 6 products */
+};
+
 /* Where the arrays of a batch live. */
 enum { CL2PT_HOST = 0, CL2PT_DEVICE = 1 };
 
@@ -276,6 +287,17 @@ int cl2pt_kernel_times(cl2pt_plan* plan, double* ms, int* launches);
 
 /* Number of kernel launches issued by the last eval call. */
 int cl2pt_last_launch_count(const cl2pt_plan* plan);
+
+/* Select the Legendre contraction of a mixed plan (CL2PT_CONTRACT_*; the
+ * reference's xi_pm_tomo / w_gammat_tomo / w_gg_tomo sums,
+ * cosmo2D.c:500-534, 680-699, 859-878).  The tensor-core forms need at
+ * most 64 filter rows (2 ntheta <= 64) and return CL2PT_ERR_UNSUPPORTED
+ * otherwise and for FP64 plans; the first selection of a form builds its
+ * split filters on the device.  The adjoint keeps the FP32 form.  A
+ * mixed plan starts with CL2PT_CONTRACT_TF32X3 where the form fits, with
+ * CL2PT_CONTRACT_FP32 otherwise. */
+int cl2pt_plan_set_contraction(cl2pt_plan* plan, int mode);
+int cl2pt_plan_get_contraction(const cl2pt_plan* plan, int* mode);
 
 /* The C_l node grids of the plan: nodes nint .. of the ss (gs, gg) tables
  * sit at l = exp(lim[0] + i lim[2]), lim[1] = ln of the last node

@@ -76,7 +76,8 @@ def blocks(plan, dv):
             "w": dv[2 * a + plan.n_gammat:]}
 
 
-def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None, bmag=False):
+def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None, bmag=False,
+             contract=None):
     import oracle as O
     w = workloads.make(name)
     if tweak is not None:
@@ -86,6 +87,8 @@ def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=N
         for i, nu in enumerate(nus):
             nu_tweak(i, nu)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts, linear_table=True)
+    if contract is not None:
+        plan.set_contraction(contract)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
@@ -278,6 +281,90 @@ def test_full_real_3x2pt(gpu_lib, oracle_built):
     print(worst)
     for k, v in worst.items():
         assert v <= REL, (k, v, worst)
+
+
+def plain_and_floored(plan, dv, ref, ntheta):
+    """(max relative error per entry, the same with the zero-crossing
+    floor, entries above 1e-4 plain) over the four observables."""
+    worst_p = worst_f = 0.0
+    above = 0
+    for k, v in blocks(plan, dv).items():
+        r = blocks(plan, ref)[k].reshape(-1, ntheta)
+        g = v.reshape(-1, ntheta)
+        err = np.abs(g - r)
+        plain = err / np.maximum(np.abs(r), 1e-300)
+        peak = np.max(np.abs(r), axis=1, keepdims=True)
+        worst_p = max(worst_p, float(plain.max()))
+        worst_f = max(worst_f, float((err / np.maximum(np.abs(r), PAIR_FLOOR * peak)).max()))
+        above += int(np.count_nonzero(plain > REL))
+    return worst_p, worst_f, above
+
+
+# Tensor-core contraction forms and the bar each is held to: TF32x3 and
+# BF16x6 carry ~22 and ~24 bits per product and meet the 1e-4 bar; BF16x3
+# (two 8-bit pieces, ~16 bits per product) is recorded against a loose
+# bound only -- its error is the figure the test prints.
+CONTRACT_BARS = [(lib.CONTRACT_TF32X3, REL), (lib.CONTRACT_BF16X6, REL), (lib.CONTRACT_BF16X3, 1e-2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,bar", CONTRACT_BARS)
+def test_tensor_core_contraction(gpu_lib, oracle_built, mode, bar):
+    """The tcgen05 Legendre contraction on the full real_3x2pt workload
+    (K = 1019 nodes for xi and gamma_t, 150 + 1019 for the non-Limber w)
+    against the FP64 oracle, and against the CUDA-core FP32 form."""
+    import oracle as O
+    w = workloads.make("real_3x2pt")
+    tabs, nus = workloads.points(w, 3, seed=11)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=3)
+    assert plan.contraction() == lib.CONTRACT_TF32X3  # the mixed plan's default
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    plan.set_contraction(lib.CONTRACT_FP32)
+    dv_fp32 = plan.eval_real(om, h0, chi, G, lnP, nus)
+    plan.set_contraction(mode)
+    assert plan.contraction() == mode
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus)
+    dv2 = plan.eval_real(om, h0, chi, G, lnP, nus)
+    assert np.array_equal(dv, dv2)  # deterministic
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    wp = wf = 0.0
+    above = 0
+    for i in range(3):
+        o.set_point(tabs[i], nus[i])
+        ref = o.data_vector_real()
+        p_, f_, a_ = plain_and_floored(plan, dv[i], ref, w.cfg.ntheta)
+        wp, wf, above = max(wp, p_), max(wf, f_), above + a_
+    f32 = max(plain_and_floored(plan, dv[i], dv_fp32[i], w.cfg.ntheta)[1] for i in range(3))
+    print(f"contraction {mode}: max rel err vs oracle {wf:.3e} (floored), {wp:.3e} (plain, "
+          f"{above} entries > 1e-4); vs the FP32 form {f32:.3e}")
+    assert wf <= bar, wf
+
+
+@pytest.mark.gpu
+def test_tensor_core_contraction_variants(gpu_lib, oracle_built):
+    """TATT ([EE; BB] columns, K = 2 x nodes), a Limber w(theta), a batch
+    whose column count is not a multiple of the 128-column tile, and the
+    form's limit (more than 64 filter rows is refused)."""
+    worst, _ = run_case("real_3x2pt_tatt_small", 3, lib.PREC_MIXED, check_tables=False,
+                        contract=lib.CONTRACT_TF32X3)
+    print("tatt", worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+    def limber(w):
+        w.cfg.adopt_limber_gg = 1
+    worst, _ = run_case("real_3x2pt_small_limber", 5, lib.PREC_MIXED, check_tables=False, tweak=limber,
+                        contract=lib.CONTRACT_TF32X3)
+    print("limber w", worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+    w = workloads.make("real_3x2pt_small_limber")
+    w.cfg.ntheta = 40
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
+    with pytest.raises(RuntimeError):
+        plan.set_contraction(lib.CONTRACT_TF32X3)
+    assert plan.contraction() == lib.CONTRACT_FP32
 
 
 @pytest.mark.gpu
