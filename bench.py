@@ -244,9 +244,12 @@ def value_grad(plan, w, data, d_om, d_h0, d_chi, d_G, d_lnP, d_nu, out, stream, 
     tatt = w.cfg.ia_model == 1
     what = "shear m, source dz, b1" + (", b2, bs2, A1, eta1, A2, eta2, b_TA" if tatt else
                                       (", A1" if w.cfg.ia_mode else ""))
+    paths = "Limber table walks, FFTLog z=0 slice, non-Limber hand-over"
+    if tatt or w.cfg.one_loop_bias:
+        paths += ", and the FAST-PT one-loop/TATT tables through p_lin(k, z=0)"
     res = {"value": B * args.steps / (ms / 1e3), "unit": "value+gradient evaluations/s",
            "ms_per_step": ms / args.steps, "workload": w.name, "points_per_step": B,
-           "grad_wrt": f"lnP table ({plan.shapes['nk']}x{plan.shapes['nz']}) and {n_nu} nuisance "
+           "grad_wrt": f"lnP table ({plan.shapes['nk']}x{plan.shapes['nz']}; {paths}) and {n_nu} nuisance "
                        f"parameters ({what})",
            "n_nuisance": n_nu, "launches_per_step": plan.launches(),
            "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items() if v > 0}}

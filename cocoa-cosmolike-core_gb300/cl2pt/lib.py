@@ -114,6 +114,9 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_fastpt_bias.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                       C.c_void_p]
     lib.cl2pt_fastpt_check_errors.argtypes = [C.c_void_p]
+    for name in ("cl2pt_fastpt_J_abl_vjp", "cl2pt_fastpt_bias_vjp", "cl2pt_fastpt_ia_vjp"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p]
     lib.cl2pt_fastpt_bias_terms.argtypes = [_ip, _ip, _ip, _ip, _dp]
     lib.cl2pt_J_abl.argtypes = [_dp, _dp, C.c_long, _ip, _ip, _ip, _ip, C.c_int,
                                 C.POINTER(FastPTConfig), C.POINTER(_dp)]
@@ -691,6 +694,26 @@ class FastPT:
     def J_abl(self, fx):
         """fx [n][N0] (host) -> [n][nterms][N0]."""
         return self._run(load().cl2pt_fastpt_J_abl, fx, self.nterms)
+
+    def _vjp(self, fn, fx, obar, nout):
+        fx = np.ascontiguousarray(np.atleast_2d(fx), dtype=np.float64)
+        ob = np.ascontiguousarray(obar, dtype=np.float64).reshape(fx.shape[0], nout, len(self.x))
+        g = np.zeros_like(fx)
+        check(fn(self.h, fx.ctypes.data, fx.shape[0], ob.ctypes.data, g.ctypes.data, HOST, None), "fastpt vjp")
+        return g
+
+    def J_vjp(self, fx, obar):
+        """Gradient [n][N0] of <obar, J(fx)> for the per-term outputs
+        (J_abl and J_abJ1J2Jk plans; obar [n][nterms][N0])."""
+        return self._vjp(load().cl2pt_fastpt_J_abl_vjp, fx, obar, self.nterms)
+
+    def bias_vjp(self, fx, obar):
+        """Gradient [n][N0] of <obar, bias(fx)>, obar [n][5][N0]."""
+        return self._vjp(load().cl2pt_fastpt_bias_vjp, fx, obar, 5)
+
+    def ia_vjp(self, fx, obar):
+        """Gradient [n][N0] of <obar, ia(fx)>, obar [n][10][N0]."""
+        return self._vjp(load().cl2pt_fastpt_ia_vjp, fx, obar, 10)
 
     def bias(self, fx):
         """fx [n][N0] (host) -> [n][5][N0]: P_d1d2, P_d2d2, P_d1s2, P_d2s2, P_s2s2."""

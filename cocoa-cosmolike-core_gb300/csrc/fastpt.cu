@@ -371,6 +371,9 @@ struct Program {
   std::vector<int2> ipair, gpair;
   cl2pt::FPTDev dev{};
   bool built = false;
+  // adjoint (cl2pt_fastpt_*_vjp): term lists and scratch, built on first use
+  cl2pt::FPTAdj adj{};
+  bool adj_built = false;
 };
 
 struct cl2pt_fastpt_plan {
@@ -393,6 +396,14 @@ struct cl2pt_fastpt_plan {
   size_t d_out_n = 0;
   int* d_err = nullptr;
   int* d_inchk = nullptr;  // non-finite flag of staged host spectra
+  // host copies the adjoint needs: the bias of each input, the direct
+  // convolutions' two kernels (the second scaled as in its transform)
+  std::vector<int> in_bias_h;
+  std::vector<double> dir_k1, dir_k2;
+  // adjoint staging: forward outputs of the recomputed wave, host batches
+  double* d_vjp_out = nullptr;
+  double* d_vjp_ob = nullptr;
+  double* d_vjp_fxb = nullptr;
 };
 
 namespace {
@@ -651,7 +662,8 @@ int create_base(cl2pt_fastpt_plan* p, const double* x)
   }
   p->n_in = (int)ulist.size();
   std::vector<double2> G((size_t)p->n_in * (half + 1));
-  std::vector<int> in_bias(p->n_in, 0);
+  std::vector<int>& in_bias = p->in_bias_h;
+  in_bias.assign(p->n_in, 0);
   for (int u = 0; u < p->n_in; u++) {
     double mu, q;
     if (p->kind == KIND_JABL) {
@@ -749,6 +761,9 @@ int create_direct(cl2pt_fastpt_plan* p, const double* x)
   const double sc = (m1 > 0 && m2 > 0) ? std::ldexp(1.0, std::ilogb(m1) - std::ilogb(m2)) : 1.0;
   std::vector<double2> f(M, make_double2(0.0, 0.0));
   for (long i = 0; i < 2 * N0 - 1; i++) f[i] = make_double2(f1[i], sc * f2[i]);
+  p->dir_k1.assign(f1.begin(), f1.begin() + (2 * N0 - 1));
+  p->dir_k2.resize(2 * N0 - 1);
+  for (long i = 0; i < 2 * N0 - 1; i++) p->dir_k2[i] = sc * f2[i];
   std::vector<double> c1(N0), c2(N0);
   for (long i = 0; i < N0; i++) {
     const double k3 = x[i] * x[i] * x[i];
@@ -877,7 +892,170 @@ int run_program(cl2pt_fastpt_plan* p, Program& g, bool direct, const double* fx,
   return CL2PT_OK;
 }
 
+// The adjoint's term lists (terms per input, inputs per bias, the k-power
+// class of each row), its scratch for one wave and, for the TATT plan, the
+// transforms of the two direct-convolution kernels.
+int build_adjoint(cl2pt_fastpt_plan* p, Program& g, bool direct)
+{
+  if (!g.built)
+    if (int st = upload_program(p, g)) return st;
+  const int n_in = p->n_in, n_bias = p->n_bias;
+  std::vector<int> row_kp(g.n_row);
+  for (int q = 0; q < g.n_grp; q++)
+    for (int r = g.grp_start[q]; r < g.grp_start[q + 1]; r++) row_kp[r] = g.grp_kp[q];
+  std::vector<std::vector<int>> rows_of(n_in), other_of(n_in);
+  std::vector<std::vector<double>> c_of(n_in);
+  for (int j = 0; j < g.n_row; j++)
+    for (int t = g.row_start[j]; t < g.row_start[j + 1]; t++) {
+      const int ua = g.t_ua[t], ub = g.t_ub[t];
+      rows_of[ua].push_back(j);
+      other_of[ua].push_back(ub);
+      c_of[ua].push_back(g.t_c[t]);
+      rows_of[ub].push_back(j);
+      other_of[ub].push_back(ua);
+      c_of[ub].push_back(g.t_c[t]);
+    }
+  std::vector<int> in_start(1, 0), in_row, in_other;
+  std::vector<double> in_c;
+  for (int u = 0; u < n_in; u++) {
+    in_row.insert(in_row.end(), rows_of[u].begin(), rows_of[u].end());
+    in_other.insert(in_other.end(), other_of[u].begin(), other_of[u].end());
+    in_c.insert(in_c.end(), c_of[u].begin(), c_of[u].end());
+    in_start.push_back((int)in_row.size());
+  }
+  std::vector<int> bias_start(1, 0), bias_in;
+  for (int b = 0; b < n_bias; b++) {
+    for (int u = 0; u < n_in; u++)
+      if (p->in_bias_h[u] == b) bias_in.push_back(u);
+    bias_start.push_back((int)bias_in.size());
+  }
+  cl2pt::FPTAdj& a = g.adj;
+  int *d_rk, *d_is, *d_ir, *d_io, *d_bs, *d_bi;
+  double* d_ic;
+  if (int st = up(p, &d_rk, row_kp.data(), row_kp.size())) return st;
+  if (int st = up(p, &d_is, in_start.data(), in_start.size())) return st;
+  if (int st = up(p, &d_ir, in_row.data(), in_row.size())) return st;
+  if (int st = up(p, &d_io, in_other.data(), in_other.size())) return st;
+  if (int st = up(p, &d_ic, in_c.data(), in_c.size())) return st;
+  if (int st = up(p, &d_bs, bias_start.data(), bias_start.size())) return st;
+  if (int st = up(p, &d_bi, bias_in.data(), bias_in.size())) return st;
+  a.row_kp = d_rk;
+  a.in_start = d_is;
+  a.in_row = d_ir;
+  a.in_other = d_io;
+  a.in_c = d_ic;
+  a.bias_start = d_bs;
+  a.bias_in = d_bi;
+  const size_t W = (size_t)p->wave;
+  if (int st = up(p, &a.sbar, (const double*)nullptr, W * g.n_row * p->Ntot)) return st;
+  if (int st = up(p, &a.xbar, (const double2*)nullptr, W * n_in * (p->half + 1))) return st;
+  if (int st = up(p, &a.ebar, (const double*)nullptr, W * n_bias * p->N)) return st;
+  if (direct && p->has_direct) {
+    const int M = p->direct.M;
+    for (int r = 0; r < 2; r++) {
+      const std::vector<double>& k = r ? p->dir_k2 : p->dir_k1;
+      std::vector<double2> kc(M, make_double2(0.0, 0.0));
+      for (size_t i = 0; i < k.size(); i++) kc[i] = make_double2(k[i], 0.0);
+      double2* d_k;
+      if (int st = up(p, &d_k, kc.data(), kc.size())) return st;
+      cl2pt::launch_fastpt_kernel_fft(p->direct, d_k, nullptr);
+      FPT_CUDA_OK(cudaGetLastError());
+      (r ? a.F2 : a.F1) = d_k;
+    }
+    FPT_CUDA_OK(cudaDeviceSynchronize());
+  }
+  if (cl2pt::fptv_smem_setup()) return CL2PT_ERR_CUDA;
+  g.adj_built = true;
+  return CL2PT_OK;
+}
+
+// Adjoint of run_program: fx [nspec][N0] and the outputs' cotangent obar
+// [nspec][n_out][N0] -> fxbar [nspec][N0].  recompute: run the forward of
+// each wave first (the adjoint reads its transforms); without it the
+// caller has just run the forward of these spectra, which must fit one
+// wave.
+int run_vjp(cl2pt_fastpt_plan* p, Program& g, bool direct, const double* fx, int nspec, const double* obar,
+            double* fxbar, int where, void* stream, bool recompute)
+{
+  if (!p || !fx || !obar || !fxbar || nspec < 1 || nspec > p->max_spec) return CL2PT_ERR_ARG;
+  if (where != CL2PT_HOST && where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
+  if (!recompute && nspec > p->wave) return CL2PT_ERR_ARG;
+  if (!g.adj_built)
+    if (int st = build_adjoint(p, g, direct)) return st;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t in_n = (size_t)nspec * p->N0, ob_n = (size_t)nspec * g.n_out * p->N0;
+  if (recompute && !p->d_vjp_out)
+    if (int s2 = up(p, &p->d_vjp_out, (const double*)nullptr, (size_t)p->wave * g.n_out * p->N0)) return s2;
+  const double* dfx = fx;
+  const double* dob = obar;
+  double* dfb = fxbar;
+  if (where == CL2PT_HOST) {
+    if (!p->d_vjp_ob) {
+      size_t mx = 0;
+      for (const Program* q : {&p->per_term, &p->combined}) mx = std::max(mx, (size_t)q->n_out);
+      if (int s2 = up(p, &p->d_vjp_ob, (const double*)nullptr, (size_t)p->max_spec * mx * p->N0)) return s2;
+      if (int s2 = up(p, &p->d_vjp_fxb, (const double*)nullptr, (size_t)p->max_spec * p->N0)) return s2;
+    }
+    FPT_CUDA_OK(cudaMemcpyAsync(p->d_fx, fx, in_n * sizeof(double), cudaMemcpyHostToDevice, st));
+    FPT_CUDA_OK(cudaMemcpyAsync(p->d_vjp_ob, obar, ob_n * sizeof(double), cudaMemcpyHostToDevice, st));
+    dfx = p->d_fx;
+    dob = p->d_vjp_ob;
+    dfb = p->d_vjp_fxb;
+  }
+  FPT_CUDA_OK(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
+  for (int s0 = 0; s0 < nspec; s0 += p->wave) {
+    const int S = std::min(p->wave, nspec - s0);
+    if (recompute) cl2pt::launch_fastpt(g.dev, dfx + (size_t)s0 * p->N0, S, p->d_vjp_out, st);
+    cl2pt::launch_fastpt_vjp(g.dev, g.adj, dfx + (size_t)s0 * p->N0, S, dob + (size_t)s0 * g.n_out * p->N0,
+                             dfb + (size_t)s0 * p->N0, st);
+  }
+  if (direct && p->has_direct) cl2pt::launch_fastpt_direct_vjp(p->direct, g.adj, dfx, nspec, dob, dfb, st);
+  FPT_CUDA_OK(cudaGetLastError());
+  if (where == CL2PT_HOST) {
+    FPT_CUDA_OK(cudaMemcpyAsync(fxbar, p->d_vjp_fxb, in_n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int err = 0;
+    FPT_CUDA_OK(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FPT_CUDA_OK(cudaStreamSynchronize(st));
+    if (err) return CL2PT_ERR_FFT;
+  }
+  return CL2PT_OK;
+}
+
 }  // namespace
+
+// for cl2pt's own adjoint: the forward of these spectra (nspec <= one
+// wave) has just run on the same stream
+int cl2pt_fastpt_vjp_after_forward(cl2pt_fastpt_plan* p, const double* fx, int nspec, const double* obar,
+                                   double* fxbar, void* stream)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (p->comb == COMB_BIAS) return run_vjp(p, p->combined, false, fx, nspec, obar, fxbar, CL2PT_DEVICE, stream, false);
+  if (p->comb == COMB_IA) return run_vjp(p, p->combined, true, fx, nspec, obar, fxbar, CL2PT_DEVICE, stream, false);
+  return run_vjp(p, p->per_term, false, fx, nspec, obar, fxbar, CL2PT_DEVICE, stream, false);
+}
+
+extern "C" int cl2pt_fastpt_J_abl_vjp(cl2pt_fastpt_plan* p, const double* fx, int nspec, const double* Fy_bar,
+                                      double* fx_bar, int where, void* stream)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  return run_vjp(p, p->per_term, false, fx, nspec, Fy_bar, fx_bar, where, stream, true);
+}
+
+extern "C" int cl2pt_fastpt_bias_vjp(cl2pt_fastpt_plan* p, const double* fx, int nspec, const double* out_bar,
+                                     double* fx_bar, int where, void* stream)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (p->comb != COMB_BIAS) return CL2PT_ERR_STATE;
+  return run_vjp(p, p->combined, false, fx, nspec, out_bar, fx_bar, where, stream, true);
+}
+
+extern "C" int cl2pt_fastpt_ia_vjp(cl2pt_fastpt_plan* p, const double* fx, int nspec, const double* out_bar,
+                                   double* fx_bar, int where, void* stream)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (p->comb != COMB_IA) return CL2PT_ERR_STATE;
+  return run_vjp(p, p->combined, true, fx, nspec, out_bar, fx_bar, where, stream, true);
+}
 
 extern "C" int cl2pt_fastpt_plan_destroy(cl2pt_fastpt_plan* p)
 {

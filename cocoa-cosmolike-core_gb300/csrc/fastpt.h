@@ -73,6 +73,23 @@ struct FPTDirect {
   const double* c2;         // [N0] and of the second
 };
 
+// Adjoint of a program (k_fastpt_vjp.cu): host-built term lists and the
+// adjoint's scratch for one wave of spectra.
+struct FPTAdj {
+  const int* row_kp;        // [n_row] k-power class of each row's group
+  const int* in_start;      // [n_in + 1] terms using each input (either side)
+  const int* in_row;        // row of that term
+  const int* in_other;      // the term's other input
+  const double* in_c;       // the term's coefficient (t_c)
+  const int* bias_start;    // [n_bias + 1] inputs of each bias
+  const int* bias_in;
+  double* sbar;             // [S][n_row][Ntot] adjoint of each row spectrum (DIF order)
+  double2* xbar;            // [S][n_in][half + 1] adjoint of each input's half-spectrum
+  double* ebar;             // [S][n_bias][N] adjoint of the extrapolated spectrum, per bias
+  const double2* F1;        // direct plans: DFT of each kernel (DIF order)
+  const double2* F2;
+};
+
 constexpr int FPT_THREADS = 512;
 
 int fpt_smem_setup();
@@ -81,5 +98,13 @@ void launch_fastpt(const FPTDev& p, const double* fx, int S, double* out, cudaSt
 void launch_fastpt_direct(const FPTDirect& d, const double* fx, int S, double* out, cudaStream_t st);
 // F = DIF of (f1 + i f2) zero-padded to M, in place on dev_f (M complex)
 void launch_fastpt_kernel_fft(const FPTDirect& d, double2* dev_f, cudaStream_t st);
+// adjoint of launch_fastpt for spectra fx [S][N0] whose forward just ran
+// (p.R holds its transforms): obar [S][n_out][N0] -> fxbar [S][N0]
+// (overwritten); the direct convolutions' part is added by the second call
+int fptv_smem_setup();
+void launch_fastpt_vjp(const FPTDev& p, const FPTAdj& a, const double* fx, int S, const double* obar,
+                       double* fxbar, cudaStream_t st);
+void launch_fastpt_direct_vjp(const FPTDirect& d, const FPTAdj& a, const double* fx, int S, const double* obar,
+                              double* fxbar, cudaStream_t st);
 
 }  // namespace cl2pt

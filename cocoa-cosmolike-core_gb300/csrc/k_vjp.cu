@@ -527,6 +527,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     (*launches)++;
     if (Pf.tatt) {
       launch_vjp_extra(Pf, V, 0, s);
+      launch_vjp_fpt_rows(Pf, V, 0, s);
       (*launches)++;
     }
   }
@@ -535,6 +536,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     (*launches)++;
     if (Pf.tatt || Pf.one_loop) {
       launch_vjp_extra(Pf, V, 1, s);
+      launch_vjp_fpt_rows(Pf, V, 1, s);
       (*launches)++;
     }
   }
@@ -545,6 +547,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     (*launches)++;
     if (Pf.one_loop) {
       launch_vjp_extra(Pf, V1, 2, s);
+      launch_vjp_fpt_rows(Pf, V1, 2, s);
       (*launches)++;
     }
   }
@@ -563,6 +566,7 @@ void launch_vjp_fourier(const Params& Pf, const Params* Pg, const VJPParams& V, 
     *launches += 3;
     if (Pg->one_loop) {
       launch_vjp_extra(*Pg, V2, 2, s);
+      launch_vjp_fpt_rows(*Pg, V2, 2, s);
       (*launches)++;
     }
     launch_nonlimber_vjp(*Pg, Q, V2.cnl_bar, V2.lnpl_bar, V2.nu_bar, s, launches);
@@ -593,6 +597,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
     *launches += 2;
     if (P.tatt) {
       launch_vjp_extra(P, V, 0, s);
+      launch_vjp_fpt_rows(P, V, 0, s);
       (*launches)++;
     }
   }
@@ -602,6 +607,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
     *launches += 2;
     if (P.tatt || P.one_loop) {
       launch_vjp_extra(P, V, 1, s);
+      launch_vjp_fpt_rows(P, V, 1, s);
       (*launches)++;
     }
   }
@@ -614,6 +620,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
       *launches += 2;
       if (P.one_loop) {
         launch_vjp_extra(P, V2, 2, s);
+        launch_vjp_fpt_rows(P, V2, 2, s);
         (*launches)++;
       }
     } else {
@@ -623,6 +630,7 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
       launch_vjp_limber(P, V, 2, s);
       if (P.one_loop) {
         launch_vjp_extra(P, V, 2, s);
+        launch_vjp_fpt_rows(P, V, 2, s);
         (*launches)++;
       }
       launch_nonlimber_vjp(P, Q, V.cnl_bar, V.lnpl_bar, V.nu_bar, s, launches);

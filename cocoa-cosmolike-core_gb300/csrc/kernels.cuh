@@ -136,6 +136,12 @@ struct VJPParams {
   // (the gs one is lbar_gs row 1)
   double* mbar_gg;
   int* one_loop_on;
+  // the FAST-PT tables' share (k_vjp_fpt.cu; null when the plan has no TATT
+  // or one-loop terms): cotangents of the table rows the integrands read,
+  // TATT [B][8][fpt_n] and bias [B][5][fpt_n]; of the FAST-PT outputs, TATT
+  // [B][10][fpt_n] and bias [B][5][fpt_n]; of p_lin on the FAST-PT grid
+  // from each [B][fpt_n]
+  double *rbar_ia, *rbar_b, *obar_fia, *obar_fb, *plinbar_ia, *plinbar_b;
   // lfac_g holds increasing multipoles (the plan's node table; caller
   // multipoles of the Fourier path need not be sorted)
   int lfac_g_sorted;
@@ -143,6 +149,13 @@ struct VJPParams {
 size_t vjp_extra_smem(const Params& P);
 // which: 0 ss, 1 gs, 2 gg, -1 the one-loop gate (k_vjp_extra.cu)
 void launch_vjp_extra(const Params& P, const VJPParams& V, int which, cudaStream_t s);
+// the FAST-PT tables' share of the adjoint (k_vjp_fpt.cu): row cotangents
+// after the extras' adjoint of each family (which: 0 ss, 1 gs, 2 gg), the
+// row-assembly adjoint, then (after the FAST-PT adjoint) p_lin's
+size_t vjp_fpt_smem(const Params& P);
+void launch_vjp_fpt_rows(const Params& P, const VJPParams& V, int which, cudaStream_t s);
+void launch_vjp_fpt_tables(const Params& P, const VJPParams& V, cudaStream_t s);
+void launch_vjp_fpt_plin(const Params& P, const VJPParams& V, cudaStream_t s);
 // the photo-z tangent of the source lens-efficiency tables (k_setup.cu)
 void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s);
 struct NLParams;

@@ -323,6 +323,9 @@ bool increasing(const double* p, int n)
   } while (0)
 
 extern "C" int cl2pt_plan_set_contraction(cl2pt_plan* p, int mode);
+// fastpt.cu: the FAST-PT adjoint right after the forward of the same spectra
+int cl2pt_fastpt_vjp_after_forward(cl2pt_fastpt_plan* p, const double* fx, int nspec, const double* obar,
+                                   double* fxbar, void* stream);
 
 extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
                                  const cl2pt_nz* lens, const cl2pt_grid* grid, int precision,
@@ -1062,6 +1065,12 @@ static int vjp_prepare(cl2pt_plan* p)
     return CL2PT_ERR_UNSUPPORTED;
   if (cl2pt::vjp_limber_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if ((p->P.tatt || p->P.one_loop) && cl2pt::vjp_extra_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
+  if ((p->P.tatt || p->P.one_loop) && cl2pt::vjp_fpt_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
+  if ((p->P.tatt || p->P.one_loop) && !p->d_vjp_fpt) {
+    // the FAST-PT tables' share: row, output and p_lin cotangents per wave
+    const size_t n = (size_t)p->wave * p->P.fpt_n;
+    if (int a = dalloc(p, &p->d_vjp_fpt, 30 * n)) return a;
+  }
   if (!p->d_vjp_ws) {
     const size_t W = p->wave, ns = c.n_source, nl = c.n_lens;
     const size_t LNL = c.lmax_nolimber;
@@ -1651,6 +1660,17 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V0.kbar_gg = w; w += (size_t)W * nl * p->n_gg;
     V0.mbar_gg = w; w += (size_t)W * nl * p->n_gg;
     V0.one_loop_on = (int*)w;
+    V0.rbar_ia = V0.rbar_b = V0.obar_fia = V0.obar_fb = V0.plinbar_ia = V0.plinbar_b = nullptr;
+    if (p->d_vjp_fpt) {
+      const size_t nf = (size_t)W * p->P.fpt_n;
+      double* f = p->d_vjp_fpt;
+      V0.rbar_ia = f; f += 8 * nf;
+      V0.rbar_b = f; f += 5 * nf;
+      V0.obar_fia = f; f += 10 * nf;
+      V0.obar_fb = f; f += 5 * nf;
+      V0.plinbar_ia = f; f += nf;
+      V0.plinbar_b = f;
+    }
     V0.mask = dmask;
     V0.lfac_ss = p->d_lfac_ss;
     V0.lfac_g = p->d_lfac_g;
@@ -1720,6 +1740,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
       for (double* q : {V0.wbar_ssb, V0.wbar_ss2}) CUDA_OK(cudaMemsetAsync(q, 0, a1, s));
       for (double* q : {V0.wbar_gsb, V0.wbar_gs2, V0.wbar_gsk}) CUDA_OK(cudaMemsetAsync(q, 0, a2, s));
       CUDA_OK(cudaMemsetAsync(V0.cx_ss, 0, sizeof(double) * (size_t)5 * P.B * p->pss * p->n_ss, s));
+      if (V0.rbar_ia) CUDA_OK(cudaMemsetAsync(V0.rbar_ia, 0, sizeof(double) * (size_t)13 * P.B * P.fpt_n, s));
     }
     V = V0;
     V.cot = vcot + (size_t)w0 * n_total;
@@ -1728,6 +1749,28 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     V.lnpl_bar = vlnpl + (size_t)w0 * (sep_lin ? nPL : nP);
     V.nu_bar = vnu + w0;
     V.pm = dpm ? dpm + (size_t)w0 * p->cfg.n_lens : nullptr;
+    return CL2PT_OK;
+  };
+  // the FAST-PT tables' share of the adjoint, after the Limber sweeps of
+  // a wave: row cotangents -> FAST-PT output cotangents -> (the FAST-PT
+  // adjoint, whose forward ran for this wave) p_lin on the FAST-PT grid ->
+  // the linear table
+  auto vjp_fpt_tail = [&](const Params& P, const cl2pt::VJPParams& V) -> int {
+    if (!(P.tatt || P.one_loop) || !V.rbar_ia) return CL2PT_OK;
+    cl2pt::launch_vjp_fpt_tables(P, V, s);
+    launches++;
+    if (P.one_loop) {
+      if (int e = cl2pt_fastpt_vjp_after_forward(p->fpt_bias, P.fpt_plin, P.B, V.obar_fb, V.plinbar_b, s))
+        return e;
+      launches += 4;
+    }
+    if (P.tatt) {
+      if (int e = cl2pt_fastpt_vjp_after_forward(p->fpt_ia, P.fpt_plin, P.B, V.obar_fia, V.plinbar_ia, s))
+        return e;
+      launches += 5;
+    }
+    cl2pt::launch_vjp_fpt_plin(P, V, s);
+    launches++;
     return CL2PT_OK;
   };
   bool ell_sorted = true;
@@ -1847,6 +1890,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         V.lfac_g_sorted = ell_sorted ? 1 : 0;
         cl2pt::launch_vjp_fourier(Pf, use_nl ? &Pg : nullptr, V, p->nlq, fr->nell, p->d_ell_f, fr->lmax_shear,
                                   p->d_lfac_g, p->d_lfacf_g, s, &launches);
+        if (int st3 = vjp_fpt_tail(P, V)) return st3;
       }
     } else {
       // the forward keeps s(l, node) of its gg terms for the adjoint
@@ -1905,6 +1949,7 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         for (int f = 0; f < 4; f++) sfv[f] = {p->d_sfiltr[f][0], p->d_sfiltr[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};
         cl2pt::launch_vjp(P, V, p->nlq, p->d_filt_xi, p->d_filt_gt, p->d_filt_gg, p->d_filt_gg_nl, sfv,
                           p->d_ell_ss, p->d_ell_g, s, &launches, hk);
+        if (int st3 = vjp_fpt_tail(P, V)) return st3;
       }
     }
   }

@@ -98,6 +98,7 @@ struct cl2pt_plan {
   // adjoint (cl2pt_vjp_real): per-wave workspace and host staging, allocated
   // on first use
   double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
+  double* d_vjp_fpt = nullptr;         // FAST-PT tables' share (TATT / one-loop plans)
   double* d_vjp_cot = nullptr;         // [max_batch][n_total] (grown for Fourier vectors)
   size_t vjp_cot_cap = 0;
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]

@@ -48,6 +48,25 @@ int cl2pt_fastpt_plan_destroy(cl2pt_fastpt_plan* plan);
 int cl2pt_fastpt_J_abl(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
                        double* Fy, int where, void* stream);
 
+/* Vector-Jacobian products of the three evaluations above: the gradient
+ * fx_bar [nspec][N] of <out_bar, out(fx)> with respect to the input
+ * spectra, for the cotangent out_bar of the outputs (J_abl and J_abJ1J2Jk
+ * plans: [nspec][nterms][N]; cl2pt_fastpt_bias: [nspec][5][N];
+ * cl2pt_fastpt_ia: [nspec][10][N]).  No counterpart in the reference,
+ * which is differentiated by finite differences; the forward is recomputed
+ * per wave of spectra (its transforms are the adjoint's input), the
+ * power-law extrapolation at both ends is differentiated, and a spectrum
+ * that fails the extrapolation check reports CL2PT_ERR_FFT as above. */
+int cl2pt_fastpt_J_abl_vjp(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                           const double* Fy_bar, double* fx_bar, int where,
+                           void* stream);
+int cl2pt_fastpt_bias_vjp(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                          const double* out_bar, double* fx_bar, int where,
+                          void* stream);
+int cl2pt_fastpt_ia_vjp(cl2pt_fastpt_plan* plan, const double* fx, int nspec,
+                        const double* out_bar, double* fx_bar, int where,
+                        void* stream);
+
 /* Waits for the device and reports the extrapolation check of the calls
  * made with CL2PT_DEVICE arrays since the last call (CL2PT_ERR_FFT if a
  * spectrum failed it; its outputs are NaN). */

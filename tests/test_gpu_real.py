@@ -368,6 +368,18 @@ def test_tensor_core_contraction_variants(gpu_lib, oracle_built):
 
 
 @pytest.mark.gpu
+def test_full_real_3x2pt_tatt(gpu_lib, oracle_built):
+    """The differentiable layout at full size (real_3x2pt_tatt: 10 source +
+    5 lens bins, l <= 50000 from 1000 nodes, TATT IA, one-loop b2/bs2,
+    source photo-z shifts and m) on 2 points, with the TATT envelope of
+    the module docstring."""
+    worst, _ = run_case("real_3x2pt_tatt", 2, lib.PREC_MIXED, seed=9, check_tables=False)
+    print(worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+
+
+@pytest.mark.gpu
 def test_batch_independence(gpu_lib):
     """A point's data vector does not depend on its batch neighbours or on
     the wave it lands in."""

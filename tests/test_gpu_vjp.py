@@ -270,7 +270,7 @@ def test_vjp_torch_autograd(gpu_lib):
     np.testing.assert_allclose(l2.cpu().numpy(), lbar, rtol=1e-12, atol=1e-14 * np.abs(lbar).max())
 
 
-def lnp_direction_fd(plan, tabs, nus, v, pt, u, lnPL=None, which="lnP"):
+def lnp_direction_fd(plan, tabs, nus, v, pt, u, lnPL=None, which="lnP", step=None):
     """Central difference of v . dv along u in lnP (or in lnPL).  The
     non-Limber hand-over multipole is a discrete choice the gradient holds
     fixed: with non-Limber w(theta) the step shrinks until it is the same at
@@ -286,7 +286,7 @@ def lnp_direction_fd(plan, tabs, nus, v, pt, u, lnPL=None, which="lnP"):
             b = b + s * h * u
         return a, b
 
-    h = H
+    h = H if step is None else step
     for _ in range(4):
         try:
             conv = []
@@ -484,9 +484,9 @@ def set_bk(nus, w, seed):
 def test_vjp_tatt_one_loop(gpu_lib, prec):
     """TATT intrinsic alignments (A1, eta_1, A2, eta_2, b_TA) and one-loop
     bias (b2, bs2, bK) and magnification (bmag) with non-Limber w(theta):
-    every nuisance gradient and a direction in the nonlinear table (with a
-    separate linear table, whose FAST-PT dependence the adjoint leaves out)
-    against differences of the FP64 forward."""
+    every nuisance gradient and a direction in each of the nonlinear and
+    the separate linear table (the latter through the FAST-PT adjoint as
+    well) against differences of the FP64 forward."""
     w = workloads.make("real_3x2pt_tatt_small")
     tabs, nus = workloads.points(w, 2, seed=41, bmag=True)
     set_bk(nus, w, 41)
@@ -497,7 +497,7 @@ def test_vjp_tatt_one_loop(gpu_lib, prec):
     lnPL = np.stack([t.lnPL.reshape(-1) for t in tabs])
     rng = np.random.default_rng(16)
     v = rng.normal(size=(2, plan.n_total))
-    dv, lbar, nbar, _ = plan.vjp_real(om, h0, chi, G, lnP, nus, v, lnPL=lnPL)
+    dv, lbar, nbar, lplbar = plan.vjp_real(om, h0, chi, G, lnP, nus, v, lnPL=lnPL)
     tol = GRAD_REL if prec == lib.PREC_FP64 else 2e-5
     worst = 0.0
     for pt in range(2):
@@ -519,7 +519,104 @@ def test_vjp_tatt_one_loop(gpu_lib, prec):
         u = rng.normal(size=lnP.shape[1])
         fd = lnp_direction_fd(p64, tabs, nus, v, pt, u, lnPL=lnPL, which="lnP")
         assert abs(lbar[pt] @ u - fd) <= tol * abs(fd), (lbar[pt] @ u, fd)
+        # the linear table: FFTLog P_lin slice, Limber_lin hand-over and,
+        # through p_lin(k, z = 0), every FAST-PT table.  The TATT delta-E2
+        # and mix-B tables are direct FP64 convolutions whose rounding (the
+        # reference algorithm's own) puts ~1e-9 relative noise on the data
+        # vector, so the difference needs a step of 4e-4 and a smooth
+        # direction (a random one also jitters the slopes of the FAST-PT
+        # log-extrapolation, which acts through 500 extrapolated points);
+        # it is then good to ~1e-5
+        nk, nz = tabs[pt].lnP.shape
+        us = (np.sin(7 * np.linspace(0, 1, nk)[:, None] + 1.0) * np.cos(3 * np.linspace(0, 1, nz)[None, :]))
+        fd = lnp_direction_fd(p64, tabs, nus, v, pt, us.reshape(-1), lnPL=lnPL, which="lnPL", step=4 * H)
+        an = float(lplbar[pt] @ us.reshape(-1))
+        worst = max(worst, abs(an - fd) / abs(fd))
+        assert abs(an - fd) <= max(tol, 5e-5) * abs(fd), (an, fd)
     print("TATT/one-loop max rel gradient error", worst)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tables", ["one", "two"])
+def test_vjp_tatt_one_loop_vs_oracle_fd(gpu_lib, oracle_built, tables):
+    """TATT and one-loop bias against central differences of the FP64
+    oracle (the reference's algorithm): A1, eta_1, A2, eta_2, b_TA, b2 and
+    bs2, shear m and source dz, and lnP directions -- with one table (lnP
+    is also the linear spectrum: the Limber walks, the FFTLog slice and the
+    FAST-PT tables all move) and with a separate linear table (lnP and lnPL
+    differentiated separately)."""
+    import dataclasses
+    import oracle as O
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 1, seed=57)
+    two = tables == "two"
+    if not two:
+        tabs = workloads.one_table(tabs)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=1, linear_table=two)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    lnPL = np.stack([t.lnPL.reshape(-1) for t in tabs]) if two else None
+    rng = np.random.default_rng(58)
+    v = rng.normal(size=(1, plan.n_total))
+    res = plan.vjp_real(om, h0, chi, G, lnP, nus, v, lnPL=lnPL)
+    lbar, nbar = res[1], res[2]
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    worst = 0.0
+    params = [("ia", 0, 0), ("ia", 0, 1), ("ia", 1, 0), ("ia", 1, 1), ("ia", 2, 0),
+              ("gb", 1, 0), ("gb", 1, 2), ("gb", 2, 1), ("gb", 0, 1), ("shear_m", 1, None), ("src_dz", 2, None)]
+    for field, i, j in params:
+        x0 = nu_get(nus[0], field, i, j)
+        h = H * max(abs(x0), 0.1)
+        f = []
+        for sg in (1, -1):
+            nu = clone(nus[0])
+            nu_set(nu, field, i, j, x0 + sg * h)
+            o.set_point(tabs[0], nu)
+            f.append(float(v[0] @ o.data_vector_real()))
+        fd = (f[0] - f[1]) / (2 * h)
+        an = nbar[0, flat_index(field, i, j)]
+        err = abs(an - fd) / abs(fd)
+        print(field, i, j, an, fd, err)
+        worst = max(worst, err)
+        assert err <= ORACLE_REL, (field, i, j, an, fd)
+    # lnP directions: smooth in k so the oracle's rounding stays out of
+    # the difference; the step is held where the non-Limber hand-over
+    # multipoles do not move (lnp_direction_fd's rule, checked on the GPU)
+    nk, nz = tabs[0].lnP.shape
+    kk = np.linspace(0.0, 1.0, nk)[:, None]
+    zz = np.linspace(0.0, 1.0, nz)[None, :]
+    u = (np.sin(7 * kk + 1.0) * np.cos(3 * zz) + 0.3 * rng.normal(size=(nk, nz))).reshape(-1)
+    which = ["lnP", "lnPL"] if two else ["lnP"]
+    for wh in which:
+        hstep = H
+        for _ in range(4):
+            conv = []
+            for sg in (1, -1):
+                a = lnP + (sg * hstep * u if wh == "lnP" else 0.0)
+                b = None if not two else lnPL + (sg * hstep * u if wh == "lnPL" else 0.0)
+                conv.append(plan.cl_nonlimber(om, h0, chi, G, a, nus, lnPL=b)[1])
+            if np.array_equal(conv[0], conv[1]):
+                break
+            hstep /= 4
+        f = []
+        for sg in (1, -1):
+            t = tabs[0]
+            lp = t.lnP.reshape(-1) + (sg * hstep * u if wh == "lnP" else 0.0)
+            if two:
+                ll = t.lnPL.reshape(-1) + (sg * hstep * u if wh == "lnPL" else 0.0)
+            else:
+                ll = lp
+            t2 = dataclasses.replace(t, lnP=np.ascontiguousarray(lp.reshape(t.lnP.shape)),
+                                     lnPL=np.ascontiguousarray(ll.reshape(t.lnP.shape)))
+            o.set_point(t2, nus[0])
+            f.append(float(v[0] @ o.data_vector_real()))
+        fd = (f[0] - f[1]) / (2 * hstep)
+        an = float((lbar if wh == "lnP" else res[3])[0] @ u)
+        err = abs(an - fd) / abs(fd)
+        print(wh, an, fd, err)
+        worst = max(worst, err)
+        assert err <= ORACLE_REL, (wh, an, fd)
+    print(f"TATT/one-loop ({tables} table): max rel gradient error vs oracle FD {worst:.2e}")
 
 
 @pytest.mark.gpu
