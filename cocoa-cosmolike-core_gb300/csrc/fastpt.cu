@@ -929,7 +929,28 @@ int build_adjoint(cl2pt_fastpt_plan* p, Program& g, bool direct)
       if (p->in_bias_h[u] == b) bias_in.push_back(u);
     bias_start.push_back((int)bias_in.size());
   }
+  // pairs sharing one complex transform and the group of each row
+  std::vector<int2> grp_pair, row_pair, in_pair;
+  for (int q = 0; q < g.n_grp; q += 2) grp_pair.push_back(make_int2(q, q + 1 < g.n_grp ? q + 1 : -1));
+  for (int j = 0; j < g.n_row; j += 2) row_pair.push_back(make_int2(j, j + 1 < g.n_row ? j + 1 : -1));
+  for (int u = 0; u < n_in; u += 2) in_pair.push_back(make_int2(u, u + 1 < n_in ? u + 1 : -1));
+  std::vector<int> row_grp(g.n_row);
+  for (int q = 0; q < g.n_grp; q++)
+    for (int r = g.grp_start[q]; r < g.grp_start[q + 1]; r++) row_grp[r] = q;
   cl2pt::FPTAdj& a = g.adj;
+  int* d_rg;
+  int2 *d_gpa, *d_rpa, *d_ipa;
+  if (int st = up(p, &d_rg, row_grp.data(), row_grp.size())) return st;
+  if (int st = up(p, &d_gpa, grp_pair.data(), grp_pair.size())) return st;
+  if (int st = up(p, &d_rpa, row_pair.data(), row_pair.size())) return st;
+  if (int st = up(p, &d_ipa, in_pair.data(), in_pair.size())) return st;
+  a.row_grp = d_rg;
+  a.grp_pair = d_gpa;
+  a.row_pair = d_rpa;
+  a.in_pair = d_ipa;
+  a.n_gpa = (int)grp_pair.size();
+  a.n_rpa = (int)row_pair.size();
+  a.n_ipa = (int)in_pair.size();
   int *d_rk, *d_is, *d_ir, *d_io, *d_bs, *d_bi;
   double* d_ic;
   if (int st = up(p, &d_rk, row_kp.data(), row_kp.size())) return st;
@@ -947,6 +968,7 @@ int build_adjoint(cl2pt_fastpt_plan* p, Program& g, bool direct)
   a.bias_start = d_bs;
   a.bias_in = d_bi;
   const size_t W = (size_t)p->wave;
+  if (int st = up(p, &a.Dg, (const double2*)nullptr, W * g.n_grp * (p->N + 1))) return st;
   if (int st = up(p, &a.sbar, (const double*)nullptr, W * g.n_row * p->Ntot)) return st;
   if (int st = up(p, &a.xbar, (const double2*)nullptr, W * n_in * (p->half + 1))) return st;
   if (int st = up(p, &a.ebar, (const double*)nullptr, W * n_bias * p->N)) return st;

@@ -83,6 +83,12 @@ struct FPTAdj {
   const double* in_c;       // the term's coefficient (t_c)
   const int* bias_start;    // [n_bias + 1] inputs of each bias
   const int* bias_in;
+  const int2* grp_pair;     // [n_gpa] groups sharing one size-N transform (g1, g2 | -1)
+  const int2* row_pair;     // [n_rpa] rows sharing one size-Ntot transform (j1, j2 | -1)
+  const int2* in_pair;      // [n_ipa] inputs sharing one size-Ntot transform (u1, u2 | -1)
+  int n_gpa, n_rpa, n_ipa;
+  const int* row_grp;       // [n_row] group of each row
+  double2* Dg;              // [S][n_grp][N + 1] adjoint of each group's folded c2r input
   double* sbar;             // [S][n_row][Ntot] adjoint of each row spectrum (DIF order)
   double2* xbar;            // [S][n_in][half + 1] adjoint of each input's half-spectrum
   double* ebar;             // [S][n_bias][N] adjoint of the extrapolated spectrum, per bias

@@ -8,20 +8,23 @@
 // padded spectrum except two: the term products R_a R_b (bilinear) and the
 // power-law extrapolation at both ends (cfastpt.c:1066-1126).  Backwards,
 // per spectrum:
-//   k_fptv_row   per row j: the output cotangent times the k power on the
-//                even samples of the size-2N grid; its size-N transform
-//                gives the adjoint of the folded c2r input D(m)
-//                (2 X(m) inside, X(0) at m = 0 and N, real there); times
-//                conj(H_j) it is the adjoint of the row's lag sequence,
-//                whose size-Ntot transform (real part) is the adjoint of
-//                the row spectrum s_j at each DIF position.
+//   k_fptv_grp   per group g: the output cotangent times the k power on
+//                the even samples of the size-2N grid; its size-N transform
+//                gives the adjoint of the folded c2r input D(m) (2 X(m)
+//                inside, X(0) at m = 0 and N, real there).
+//   k_fptv_row   per row j: D_g(j) conj(H_j) is the adjoint of the row's lag
+//                sequence, whose size-Ntot transform (real part) is the
+//                adjoint of the row spectrum s_j at each DIF position.
 //   k_fptv_in    per input u: R_bar_u = sum over the terms that use u of
 //                c_t s_bar_row(t) R_other (the forward's transforms, still
 //                in the program's scratch); times the centring phase, one
-//                inverse transform back to the padded Hermitian sequence;
-//                both halves fold onto the biased spectrum's half-spectrum
+//                inverse transform back to the padded Hermitian sequence,
+//                folded onto the biased spectrum's half-spectrum
 //                (x_bar[i] = x_bar_u[half + i] conj(G_u[i]) +
 //                conj(x_bar_u[half - i] G_u[i])).
+//   Pairs of groups, rows and inputs share one complex transform each (the
+//   real-sequence, Hermitian-part and J-symmetry splits noted at each
+//   kernel).
 //   k_fptv_bias  per bias: the inputs' half-spectra summed, one inverse
 //                size-N transform (real part), divided by x^nu.
 //   k_fptv_out   per spectrum: the biases summed onto the input grid plus
@@ -42,74 +45,217 @@ using fft64::conj2;
 
 namespace {
 
-constexpr int VMAX = 16;  // (N + 1) / FPT_THREADS <= GENERIC_MAX_PER_THREAD
+// Packing balance (as in k_fastpt.cu): the second of two packed sequences
+// is scaled by the power of two that brings its largest entry to the
+// first's, so the larger one's rounding does not swamp it; undone after the
+// split.  Block maxima of (a, b); red: 64 doubles of shared memory.
+__device__ __forceinline__ void vmax2(double& a, double& b, double* red)
+{
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    red[w] = a;
+    red[32 + w] = b;
+  }
+  __syncthreads();
+  a = 0.0;
+  b = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+    a = fmax(a, red[i]);
+    b = fmax(b, red[32 + i]);
+  }
+}
 
+__device__ __forceinline__ double vscale(double m1, double m2)
+{
+  if (!(m1 > 0.0) || !(m2 > 0.0) || !isfinite(m1) || !isfinite(m2)) return 1.0;
+  return scalbn(1.0, max(-960, min(960, ilogb(m1) - ilogb(m2))));
+}
+
+__device__ __forceinline__ double amx(double2 a) { return fmax(fabs(a.x), fabs(a.y)); }
+
+// per group pair: the output cotangents times the k power on the even
+// samples of the size-2N grid (real, two groups packed as re + i im), one
+// size-N transform, split into each group's D(m), m = 0..N
 __global__ void __launch_bounds__(FPT_THREADS, 1)
-    k_fptv_row(FPTDev p, FPTAdj a, const double* __restrict__ obar)
+    k_fptv_grp(FPTDev p, FPTAdj a, const double* __restrict__ obar)
 {
   extern __shared__ double2 sbuf[];
-  const int j = blockIdx.x, s = blockIdx.y;
-  const int N = p.N, N0 = p.N0, T = p.Ntot, off = p.off;
-  const double* ob = obar + ((size_t)s * p.n_out + p.row_out[j]) * N0;
-  const double* kp = p.kpow + (size_t)a.row_kp[j] * N0;
+  const int2 gp = a.grp_pair[blockIdx.x];
+  const int s = blockIdx.y;
+  const bool two = gp.y >= 0;
+  const int N = p.N, N0 = p.N0, off = p.off;
+  const double* o1 = obar + ((size_t)s * p.n_out + p.grp_out[gp.x]) * N0;
+  const double* o2 = obar + ((size_t)s * p.n_out + p.grp_out[two ? gp.y : gp.x]) * N0;
+  const double* k1 = p.kpow + (size_t)p.grp_kp[gp.x] * N0;
+  const double* k2 = p.kpow + (size_t)p.grp_kp[two ? gp.y : gp.x] * N0;
+  __shared__ double red[64];
+  double m1 = 0.0, m2 = 0.0;
   for (int n = threadIdx.x; n < N; n += blockDim.x) {
-    const double v = (n >= off && n < off + N0) ? ob[n - off] * kp[n - off] : 0.0;
-    sbuf[n] = make_double2(v, 0.0);
+    double v1 = 0.0, v2 = 0.0;
+    if (n >= off && n < off + N0) {
+      v1 = o1[n - off] * k1[n - off];
+      if (two) v2 = o2[n - off] * k2[n - off];
+    }
+    m1 = fmax(m1, fabs(v1));
+    m2 = fmax(m2, fabs(v2));
+    sbuf[n] = make_double2(v1, v2);
+  }
+  double sc = 1.0;
+  if (two) {
+    vmax2(m1, m2, red);
+    sc = vscale(m1, m2);
+    if (sc != 1.0)
+      for (int n = threadIdx.x; n < N; n += blockDim.x) sbuf[n].y *= sc;
   }
   __syncthreads();
   fft64::dif<-1>(sbuf, p.dN, p.twN);
-  const double2* Hj = p.H + (size_t)p.row_p[j] * (N + 1);
-  double2 rb[VMAX];
-#pragma unroll
-  for (int k = 0; k < VMAX; k++) {
-    const int m = threadIdx.x + k * FPT_THREADS;
-    if (m <= N) {
-      double2 D;
-      if (m == 0 || m == N) {
-        D = make_double2(sbuf[p.posN[0]].x, 0.0);
-      } else {
-        const double2 X = sbuf[p.posN[m]];
-        D = make_double2(2.0 * X.x, 2.0 * X.y);
-      }
-      rb[k] = cmulc(D, __ldg(Hj + m));
+  const double isc = 1.0 / sc;
+  double2* D1 = a.Dg + ((size_t)s * p.n_grp + gp.x) * (N + 1);
+  double2* D2 = a.Dg + ((size_t)s * p.n_grp + (two ? gp.y : gp.x)) * (N + 1);
+  for (int m = threadIdx.x; m <= N; m += blockDim.x) {
+    const int mm = (m == 0 || m == N) ? 0 : m;
+    const double2 z = sbuf[p.posN[mm]], zc = sbuf[p.posN[mm == 0 ? 0 : N - mm]];
+    // the transforms of the two real sequences
+    const double2 x1 = make_double2(0.5 * (z.x + zc.x), 0.5 * (z.y - zc.y));
+    const double2 x2 = make_double2(0.5 * isc * (z.y + zc.y), -0.5 * isc * (z.x - zc.x));
+    if (m == 0 || m == N) {
+      D1[m] = make_double2(x1.x, 0.0);
+      if (two) D2[m] = make_double2(x2.x, 0.0);
+    } else {
+      D1[m] = make_double2(2.0 * x1.x, 2.0 * x1.y);
+      if (two) D2[m] = make_double2(2.0 * x2.x, 2.0 * x2.y);
     }
   }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < VMAX; k++) {
-    const int m = threadIdx.x + k * FPT_THREADS;
-    if (m <= N) sbuf[m] = rb[k];
-  }
-  for (int m = N + 1 + threadIdx.x; m < T; m += blockDim.x) sbuf[m] = make_double2(0.0, 0.0);
-  __syncthreads();
-  fft64::dif<-1>(sbuf, p.dT, p.twT);
-  double* sb = a.sbar + ((size_t)s * p.n_row + j) * T;
-  for (int q = threadIdx.x; q < T; q += blockDim.x) sb[q] = sbuf[q].x;
 }
 
+// per row pair: r_bar_j = D_g(j) conj(H_j) on m = 0..N.  The row spectrum's
+// adjoint is Re FFT(r_bar_j) = FFT(h_j) with h_j the Hermitian part
+// (r_bar_j[m] + conj(r_bar_j[-m])) / 2, whose transform is real: two rows'
+// h packed as h_1 + i h_2 share one size-Ntot transform, whose real and
+// imaginary parts are the two answers (r_bar_j lives on m <= N and its
+// mirror on m >= Ntot - N, which do not overlap as Ntot > 2N)
+__global__ void __launch_bounds__(FPT_THREADS, 1) k_fptv_row(FPTDev p, FPTAdj a)
+{
+  extern __shared__ double2 sbuf[];
+  const int2 rp = a.row_pair[blockIdx.x];
+  const int s = blockIdx.y;
+  const bool two = rp.y >= 0;
+  const int N = p.N, T = p.Ntot;
+  const double2* D1 = a.Dg + ((size_t)s * p.n_grp + a.row_grp[rp.x]) * (N + 1);
+  const double2* D2 = a.Dg + ((size_t)s * p.n_grp + a.row_grp[two ? rp.y : rp.x]) * (N + 1);
+  const double2* H1 = p.H + (size_t)p.row_p[rp.x] * (N + 1);
+  const double2* H2 = p.H + (size_t)p.row_p[two ? rp.y : rp.x] * (N + 1);
+  __shared__ double red[64];
+  double sc = 1.0;
+  if (two) {
+    double m1 = 0.0, m2 = 0.0;
+    for (int m = threadIdx.x; m <= N; m += blockDim.x) {
+      m1 = fmax(m1, amx(cmulc(D1[m], __ldg(H1 + m))));
+      m2 = fmax(m2, amx(cmulc(D2[m], __ldg(H2 + m))));
+    }
+    vmax2(m1, m2, red);
+    sc = vscale(m1, m2);
+  }
+  for (int m = threadIdx.x; m < T; m += blockDim.x) {
+    double2 h1 = make_double2(0.0, 0.0), h2 = h1;
+    const int mr = (m <= N) ? m : ((m >= T - N) ? T - m : -1);
+    if (mr >= 0) {
+      h1 = cmulc(D1[mr], __ldg(H1 + mr));
+      if (two) h2 = cmulc(D2[mr], __ldg(H2 + mr));
+      if (m == 0) {
+        h1.y = 0.0;
+        h2.y = 0.0;
+      } else {
+        h1 = fft64::scal(0.5, m <= N ? h1 : conj2(h1));
+        h2 = fft64::scal(0.5, m <= N ? h2 : conj2(h2));
+      }
+      h2 = fft64::scal(sc, h2);
+    }
+    sbuf[m] = make_double2(h1.x - h2.y, h1.y + h2.x);
+  }
+  __syncthreads();
+  fft64::dif<-1>(sbuf, p.dT, p.twT);
+  double* sb1 = a.sbar + ((size_t)s * p.n_row + rp.x) * T;
+  double* sb2 = a.sbar + ((size_t)s * p.n_row + (two ? rp.y : rp.x)) * T;
+  for (int q = threadIdx.x; q < T; q += blockDim.x) {
+    const double2 z = sbuf[q];
+    sb1[q] = z.x;
+    if (two) sb2[q] = z.y / sc;
+  }
+}
+
+// per input pair: R_bar_u = sum over the terms that use u of c_t
+// s_bar_row(t) R_other, times the centring phase; the two inputs packed as
+// re + i im, one inverse size-Ntot transform.  Each input's adjoint sequence
+// y_u is J-symmetric about N/2 (y_u[N - n] = conj(y_u[n]), as the forward's
+// padded sequences are), so y_1 = (y + J y) / 2 and y_2 = (y - J y) / 2i, and
+// the fold onto the half-spectrum is x_bar[i] = (i ? 2 : 1) y_u[half + i]
+// conj(G_u[i]).
 __global__ void __launch_bounds__(FPT_THREADS, 1) k_fptv_in(FPTDev p, FPTAdj a)
 {
   extern __shared__ double2 sbuf[];
-  const int u = blockIdx.x, s = blockIdx.y;
-  const int T = p.Ntot, h = p.half;
+  const int2 ip = a.in_pair[blockIdx.x];
+  const int s = blockIdx.y;
+  const bool two = ip.y >= 0;
+  const int T = p.Ntot, h = p.half, N = p.N;
   const double* Rs = p.R + (size_t)s * p.n_in * T;
   const double* Sb = a.sbar + (size_t)s * p.n_row * T;
-  const int e0 = a.in_start[u], e1 = a.in_start[u + 1];
+  const int e10 = a.in_start[ip.x], e11 = a.in_start[ip.x + 1];
+  const int e20 = two ? a.in_start[ip.y] : 0, e21 = two ? a.in_start[ip.y + 1] : 0;
+  auto sum = [&](int e0, int e1, int q) {
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    int e = e0;
+    for (; e + 3 < e1; e += 4) {
+      c0 = fma(a.in_c[e] * Sb[(size_t)a.in_row[e] * T + q], Rs[(size_t)a.in_other[e] * T + q], c0);
+      c1 = fma(a.in_c[e + 1] * Sb[(size_t)a.in_row[e + 1] * T + q], Rs[(size_t)a.in_other[e + 1] * T + q], c1);
+      c2 = fma(a.in_c[e + 2] * Sb[(size_t)a.in_row[e + 2] * T + q], Rs[(size_t)a.in_other[e + 2] * T + q], c2);
+      c3 = fma(a.in_c[e + 3] * Sb[(size_t)a.in_row[e + 3] * T + q], Rs[(size_t)a.in_other[e + 3] * T + q], c3);
+    }
+    for (; e < e1; e++)
+      c0 = fma(a.in_c[e] * Sb[(size_t)a.in_row[e] * T + q], Rs[(size_t)a.in_other[e] * T + q], c0);
+    return (c0 + c1) + (c2 + c3);
+  };
+  __shared__ double red[64];
+  double m1 = 0.0, m2 = 0.0;
   for (int q = threadIdx.x; q < T; q += blockDim.x) {
-    double acc = 0.0;
-    for (int e = e0; e < e1; e++)
-      acc = fma(a.in_c[e] * Sb[(size_t)a.in_row[e] * T + q], Rs[(size_t)a.in_other[e] * T + q], acc);
-    sbuf[q] = fft64::scal(acc, __ldg(p.phT + q));
+    const double r1 = sum(e10, e11, q), r2 = two ? sum(e20, e21, q) : 0.0;
+    m1 = fmax(m1, fabs(r1));
+    m2 = fmax(m2, fabs(r2));
+    sbuf[q] = make_double2(r1, r2);
+  }
+  double sc = 1.0;
+  if (two) {
+    vmax2(m1, m2, red);
+    sc = vscale(m1, m2);
+  }
+  for (int q = threadIdx.x; q < T; q += blockDim.x) {
+    const double r1 = sbuf[q].x, r2 = sc * sbuf[q].y;
+    const double2 ph = __ldg(p.phT + q);
+    // ph (r1 + i r2)
+    sbuf[q] = make_double2(ph.x * r1 - ph.y * r2, ph.y * r1 + ph.x * r2);
   }
   __syncthreads();
   fft64::dit<1>(sbuf, p.dT, p.twT);
-  const double2* G = p.G + (size_t)u * (h + 1);
-  double2* xb = a.xbar + ((size_t)s * p.n_in + u) * (h + 1);
+  const double2* G1 = p.G + (size_t)ip.x * (h + 1);
+  const double2* G2 = p.G + (size_t)(two ? ip.y : ip.x) * (h + 1);
+  double2* xb1 = a.xbar + ((size_t)s * p.n_in + ip.x) * (h + 1);
+  double2* xb2 = a.xbar + ((size_t)s * p.n_in + (two ? ip.y : ip.x)) * (h + 1);
   for (int i = threadIdx.x; i <= h; i += blockDim.x) {
-    const double2 g = __ldg(G + i);
-    double2 v = cmulc(sbuf[h + i], g);
-    if (i > 0) v = fft64::cadd(v, conj2(cmul(sbuf[h - i], g)));
-    xb[i] = v;
+    const double2 y = sbuf[h + i], yc = conj2(sbuf[N - (h + i)]);
+    const double f = i ? 2.0 : 1.0;
+    const double2 y1 = make_double2(0.5 * f * (y.x + yc.x), 0.5 * f * (y.y + yc.y));
+    xb1[i] = cmulc(y1, __ldg(G1 + i));
+    if (two) {
+      // (y - J y) / 2i
+      const double g = 0.5 * f / sc;
+      const double2 y2 = make_double2(g * (y.y - yc.y), -g * (y.x - yc.x));
+      xb2[i] = cmulc(y2, __ldg(G2 + i));
+    }
   }
 }
 
@@ -259,8 +405,8 @@ __global__ void __launch_bounds__(FPT_THREADS, 1) k_fptv_direct(FPTDirect d, FPT
 int fptv_smem_setup()
 {
   const int mx = 232448 - 1024;
-  const void* ks[] = {(const void*)k_fptv_row, (const void*)k_fptv_in, (const void*)k_fptv_bias,
-                      (const void*)k_fptv_direct};
+  const void* ks[] = {(const void*)k_fptv_grp, (const void*)k_fptv_row, (const void*)k_fptv_in,
+                      (const void*)k_fptv_bias, (const void*)k_fptv_direct};
   for (const void* k : ks)
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, mx) != cudaSuccess) return -1;
   return 0;
@@ -270,8 +416,9 @@ void launch_fastpt_vjp(const FPTDev& p, const FPTAdj& a, const double* fx, int S
                        double* fxbar, cudaStream_t st)
 {
   const size_t smN = (size_t)p.N * sizeof(double2), smT = (size_t)p.Ntot * sizeof(double2);
-  k_fptv_row<<<dim3(p.n_row, S), FPT_THREADS, smT, st>>>(p, a, obar);
-  k_fptv_in<<<dim3(p.n_in, S), FPT_THREADS, smT, st>>>(p, a);
+  k_fptv_grp<<<dim3(a.n_gpa, S), FPT_THREADS, smN, st>>>(p, a, obar);
+  k_fptv_row<<<dim3(a.n_rpa, S), FPT_THREADS, smT, st>>>(p, a);
+  k_fptv_in<<<dim3(a.n_ipa, S), FPT_THREADS, smT, st>>>(p, a);
   k_fptv_bias<<<dim3(p.n_bias, S), FPT_THREADS, smN, st>>>(p, a);
   k_fptv_out<<<S, FPT_THREADS, 0, st>>>(p, a, fx, fxbar);
 }
