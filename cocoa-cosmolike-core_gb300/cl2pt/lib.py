@@ -67,6 +67,7 @@ def load(path: str = LIB_PATH):
                                       C.POINTER(Grid), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
     lib.cl2pt_plan_destroy.argtypes = [C.c_void_p]
     lib.cl2pt_plan_set_contraction.argtypes = [C.c_void_p, C.c_int]
+    lib.cl2pt_plan_set_d1p3.argtypes = [C.c_void_p, _dp, C.c_int]
     lib.cl2pt_plan_get_contraction.argtypes = [C.c_void_p, _ip]
     lib.cl2pt_real_sizes.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
     lib.cl2pt_eval_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
@@ -183,6 +184,12 @@ class Plan:
         """CONTRACT_FP32 (CUDA cores) or a tensor-core form (CONTRACT_TF32X3,
         CONTRACT_BF16X3, CONTRACT_BF16X6) for the Legendre contraction."""
         check(load().cl2pt_plan_set_contraction(self.h, mode), "cl2pt_plan_set_contraction")
+
+    def set_d1p3(self, p_d1p3):
+        """P_d1p3 on the plan's FAST-PT grid (1100 values, the reference's
+        FPTbias row 5) for the one-loop b3 terms."""
+        a = np.ascontiguousarray(p_d1p3, dtype=np.float64)
+        check(load().cl2pt_plan_set_d1p3(self.h, _p(a), len(a)), "cl2pt_plan_set_d1p3")
 
     def contraction(self) -> int:
         m = C.c_int()

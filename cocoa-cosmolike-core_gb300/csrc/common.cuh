@@ -130,19 +130,21 @@ struct Params {
   double* fpt_ia;           // [B][8][fpt_n] TATT rows: tt_E, ta_dE1+ta_dE2, ta_0E0E,
                             //   mix_A+mix_B, mix_DEE, tt_B, ta_0B0B, mix_DBB
   double* fpt_b;            // [B][5][fpt_n] d1d2, d2d2-2s4, d1s2, d2s2-4/3 s4, s2s2-8/9 s4
+  const double* fpt_d1p3;   // [fpt_n] P_d1p3 on the FAST-PT grid, the caller's
+                            // (cl2pt_plan_set_d1p3); null: not set, b3 must be 0
   double* wss_b;            // [B][ns][n_ss]   WS C1 b_TA D^2 at ss nodes
   double* wss_2;            // [B][ns][n_ss]   WS C2 D^2
   double* wgs_k;            // [B][nl][ns][n_ss] WK at gs nodes
   double* wgs_b;            // [B][nl][ns][n_ss] WS C1 b_TA D^2
   double* wgs_2;            // [B][nl][ns][n_ss] WS C2 D^2
-  double* wgs_1l;           // [B][nl][2][n_ss] 0.5 D^4 WGAL (b2, bs2) (0 without b2)
+  double* wgs_1l;           // [B][nl][3][n_ss] 0.5 D^4 WGAL (b2, bs2, b3) (0 without b2)
   // the one-loop bK k^2 P terms (cosmo2D.c:1993-1995, 2599-2605), with
   // k = (l+1/2)/fK: per node the factor of (l+1/2)^2 P (0 without b2):
   // gs WGAL bK / fK^2 (times WK); gg 2 b1 bK WGAL^2 / fK^2
   double* wgs_bk;           // [B][nl][n_ss]
   double* wgg_bk;           // [B][nl][n_gg]
-  double* wgg_1l;           // [B][nl][5][n_gg] WGAL^2 D^4 (b1 b2, b2^2/4, b1 bs2,
-                            //   b2 bs2/2, bs2^2/4) (0 without b2)
+  double* wgg_1l;           // [B][nl][6][n_gg] WGAL^2 D^4 (b1 b2, b2^2/4, b1 bs2,
+                            //   b2 bs2/2, bs2^2/4, b1 b3) (0 without b2)
   double* tab_ss_bb;        // [B][pss][nnode_ss] C_ss BB (TATT)
 };
 

@@ -15,7 +15,8 @@
 //   B  the plan's FP64 filters, split the same way once when the plan is
 //      made, loaded per chunk by TMA (cp.async.bulk.tensor.2d, 128-byte
 //      swizzle) completing on an mbarrier;
-//   D  two FP32 accumulators in tensor memory, used by alternate chunks.
+//   D  FP32 accumulators in tensor memory, two chunks in flight, each with
+//      one block for the leading products p_0 q_0 and one for the rest.
 //      The products p_i q_j with i + j < S (S = 2: three products -- TF32x3
 //      or BF16x3; S = 3: six -- BF16x6) accumulate over one chunk; then every
 //      thread reads its column's row of D back (tcgen05.ld) and folds it into
@@ -53,7 +54,7 @@ constexpr int TC_THREADS = 512;    // 16 warps
 constexpr int TC_KSPLIT = 2;       // CTAs sharing one 128-column tile (halves of K)
 constexpr int TC_ROWB = 128;       // bytes of K per operand row and chunk
 constexpr int TC_ACC_COLS = 64;    // TMEM columns per accumulator
-constexpr int TC_TMEM_COLS = 128;  // two accumulators
+constexpr int TC_TMEM_COLS = 256;  // two chunks in flight x two product orders
 constexpr long long TC_WAIT_CYCLES = 1LL << 31;
 constexpr int TC_ERR_TIMEOUT = 1 << 4;
 
@@ -350,8 +351,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (!mbar_wait(bar_tma + 8 * sb, (uint32_t)(c / NSB) & 1u)) return false;
     tma_seen = c + 1;
     tc_fence_after();
-    const uint32_t d = tmem + (uint32_t)(c & 1) * TC_ACC_COLS;
-    uint32_t acc = 0;
+    // the leading products p_0 q_0 and the correction products (i + j > 0)
+    // accumulate in separate TMEM blocks, so the small terms keep their own
+    // FP32 precision until the fold
+    const uint32_t d = tmem + (uint32_t)(c & 1) * 2 * TC_ACC_COLS;
+    uint32_t acc0 = 0, acc1 = 0;
 #pragma unroll
     for (int kk = 0; kk < 4; kk++)
 #pragma unroll
@@ -360,8 +364,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int j = 0; j < S - i; j++) {
           const uint64_t a = sw128_desc(sA + (sa * S + i) * szA + 32 * kk);
           const uint64_t b = sw128_desc(sB + (sb * S + j) * szB + 32 * kk);
-          umma<KIND>(d, a, b, idesc, acc);
-          acc = 1;
+          if (i + j == 0) {
+            umma<KIND>(d, a, b, idesc, acc0);
+            acc0 = 1;
+          } else {
+            umma<KIND>(d + TC_ACC_COLS, a, b, idesc, acc1);
+            acc1 = 1;
+          }
         }
     umma_commit(bar_mma + 8 * (c & 1));
     mma_committed = c + 1;
@@ -445,20 +454,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   auto fold = [&](int c) -> bool {
     if (!mbar_wait_warp(bar_mma + 8 * (c & 1), (uint32_t)(c >> 1) & 1u)) return false;
     tc_fence_after();
-    const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c & 1) * TC_ACC_COLS + (uint32_t)(h * nh);
+    const uint32_t ta =
+        tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c & 1) * 2 * TC_ACC_COLS + (uint32_t)(h * nh);
+    // the correction block first, then the leading one
 #pragma unroll
-    for (int t = 0; t < 4; t++)
-      if (4 * t < nh) {
-        float f[4];
-        tmem_ld4(ta + 4 * t, f);
+    for (int o = 1; o >= 0; o--)
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-          float sm, e;
-          two_sum_f(ahi[4 * t + i], f[i], sm, e);
-          ahi[4 * t + i] = sm;
-          alo[4 * t + i] = __fadd_rn(alo[4 * t + i], e);
+      for (int t = 0; t < 4; t++)
+        if (4 * t < nh) {
+          float f[4];
+          tmem_ld4(ta + o * TC_ACC_COLS + 4 * t, f);
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            float sm, e;
+            two_sum_f(ahi[4 * t + i], f[i], sm, e);
+            ahi[4 * t + i] = sm;
+            alo[4 * t + i] = __fadd_rn(alo[4 * t + i], e);
+          }
         }
-      }
     tc_fence_before();
     folded = c + 1;
     return true;

@@ -188,9 +188,9 @@ __global__ void __launch_bounds__(LX) k_extra_ss(Params P, const double* __restr
 
 // ----------------------------------------------------------------- gs
 // per (lens q, source s): t0 (no l factor) = -b D^2 L taE + 5 c D^2 L mix
-//   + W_K (g2 d1d2 + gs2 d1s2);  t1 (times l(l+1)/(l+1/2)^2) = -b D^2 M taE
-//   + 5 c D^2 M mix, with L = W_gal b1, M = W_mag bmag, g2/gs2 the
-//   one-loop node weights 0.5 D^4 W_gal (b2, bs2)
+//   + W_K (g2 d1d2 + gs2 d1s2 + g3 d1p3);  t1 (times l(l+1)/(l+1/2)^2) = -b D^2 M taE
+//   + 5 c D^2 M mix, with L = W_gal b1, M = W_mag bmag, g2/gs2/g3 the
+//   one-loop node weights 0.5 D^4 W_gal (b2, bs2, b3)
 template <typename T>
 __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restrict__ ell, int nchunk)
 {
@@ -217,9 +217,9 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
     npr = m;
   }
   const int nrow = (P.tatt ? 2 : 0) + (P.one_loop ? 2 : 0);
-  T* rows = (T*)smem_raw;                  // taE, mix (TATT), d1d2, d1s2 (one-loop)
-  T* X = rows + 4 * n;                     // [6][PC][nn]
-  double* lnf = (double*)(X + 6 * PC * nn + 1);
+  T* rows = (T*)smem_raw;                  // taE, mix (TATT), d1d2, d1s2, d1p3 (one-loop)
+  T* X = rows + 5 * n;                     // [7][PC][nn]
+  double* lnf = (double*)(X + 7 * PC * nn + 1);
   lnf = (double*)(((size_t)lnf + 7) & ~(size_t)7);
   if (P.tatt) {
     load_rows<T>(rows, P.fpt_ia + ((size_t)pt * 8 + 1) * n, 1, n);
@@ -228,6 +228,8 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
   if (P.one_loop) {
     load_rows<T>(rows + 2 * n, P.fpt_b + ((size_t)pt * 5 + 0) * n, 1, n);
     load_rows<T>(rows + 3 * n, P.fpt_b + ((size_t)pt * 5 + 2) * n, 1, n);
+    if (P.fpt_d1p3) load_rows<T>(rows + 4 * n, P.fpt_d1p3, 1, n);
+    else for (int i = tid; i < n; i += LX) rows[4 * n + i] = (T)0;
   }
   __syncthreads();
   const int np_ = npr;
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
   const size_t b0 = (size_t)pt * P.nl + q;
   for (int idx = tid; idx < PC * nn; idx += LX) {
     const int k = idx / nn, p = idx - k * nn;
-    double x[6] = {0, 0, 0, 0, 0, 0};
+    double x[7] = {0, 0, 0, 0, 0, 0, 0};
     if (k < np_) {
       const int s = ss_[k];
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
@@ -255,12 +257,13 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
       }
       if (P.one_loop) {
         const double WK = P.wgs_k[o];
-        x[2] = WK * P.wgs_1l[(b0 * 2 + 0) * nn + p] * F;
-        x[3] = WK * P.wgs_1l[(b0 * 2 + 1) * nn + p] * F;
+        x[2] = WK * P.wgs_1l[(b0 * 3 + 0) * nn + p] * F;
+        x[3] = WK * P.wgs_1l[(b0 * 3 + 1) * nn + p] * F;
+        x[6] = WK * P.wgs_1l[(b0 * 3 + 2) * nn + p] * F;
       }
     }
 #pragma unroll
-    for (int m = 0; m < 6; m++) X[(m * PC + k) * nn + p] = (T)x[m];
+    for (int m = 0; m < 7; m++) X[(m * PC + k) * nn + p] = (T)x[m];
   }
   for (int p = tid; p < nn; p += LX) lnf[p] = log(node[(size_t)NF_FK * P.node_stride + off + p]);
   __syncthreads();
@@ -277,10 +280,12 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
     const T mix = P.tatt ? fpt_val<T>(rows + n, c, n) : (T)0;
     const T d1d2 = P.one_loop ? fpt_val<T>(rows + 2 * n, c, n) : (T)0;
     const T d1s2 = P.one_loop ? fpt_val<T>(rows + 3 * n, c, n) : (T)0;
+    const T d1p3 = P.one_loop ? fpt_val<T>(rows + 4 * n, c, n) : (T)0;
 #pragma unroll
     for (int k = 0; k < PC; k++) {
       a0[k] += X[(0 * PC + k) * nn + p] * taE + X[(1 * PC + k) * nn + p] * mix +
-               X[(2 * PC + k) * nn + p] * d1d2 + X[(3 * PC + k) * nn + p] * d1s2;
+               X[(2 * PC + k) * nn + p] * d1d2 + X[(3 * PC + k) * nn + p] * d1s2 +
+               X[(6 * PC + k) * nn + p] * d1p3;
       a1[k] += X[(4 * PC + k) * nn + p] * taE + X[(5 * PC + k) * nn + p] * mix;
     }
   }
@@ -296,7 +301,7 @@ __global__ void __launch_bounds__(LX) k_extra_gs(Params P, const double* __restr
 
 // ----------------------------------------------------------------- gg
 // sum over nodes of wt dchi/da / chi^2 W_gal^2 D^4 (b1 b2 d1d2 + b2^2/4
-// d2d2' + b1 bs2 d1s2 + b2 bs2/2 d2s2' + bs2^2/4 s2s2'); nodes past
+// d2d2' + b1 bs2 d1s2 + b2 bs2/2 d2s2' + bs2^2/4 s2s2' + b1 b3 d1p3); nodes past
 // chi(a_min) give nothing (the reference returns 0 for the whole
 // integrand there).  mode 0: C_l nodes (tab_gg); mode 1: integer l below
 // LMAX_NOLIMBER, nonlinear column of ggl.
@@ -309,20 +314,22 @@ __global__ void __launch_bounds__(LX) k_extra_gg(Params P, const double* __restr
   const int tid = threadIdx.x;
   const int L = blockIdx.y * LX + tid;
   const int n = P.fpt_n, nn = P.n_gg;
-  T* rows = (T*)smem_raw;                  // [5][n]
-  T* X = rows + 5 * n;                     // [5][nn]
-  double* nd = (double*)(X + 5 * nn + 1);  // [2][nn]: ln chi, chi
+  T* rows = (T*)smem_raw;                  // [6][n]: the five bias rows, d1p3
+  T* X = rows + 6 * n;                     // [6][nn]
+  double* nd = (double*)(X + 6 * nn + 1);  // [2][nn]: ln chi, chi
   nd = (double*)(((size_t)nd + 7) & ~(size_t)7);
   load_rows<T>(rows, P.fpt_b + (size_t)pt * 5 * n, 5, n);
+  if (P.fpt_d1p3) load_rows<T>(rows + 5 * n, P.fpt_d1p3, 1, n);
+  else for (int i = tid; i < n; i += LX) rows[5 * n + i] = (T)0;
   const int off = P.n_ss + P.nl * P.n_ss + q * nn;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const size_t b0 = (size_t)pt * P.nl + q;
-  for (int idx = tid; idx < 5 * nn; idx += LX) {
+  for (int idx = tid; idx < 6 * nn; idx += LX) {
     const int m = idx / nn, p = idx - m * nn;
     const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
     const double F = node[(size_t)NF_WT * P.node_stride + off + p] *
                      node[(size_t)NF_DCHIDA * P.node_stride + off + p] / (fK * fK);
-    X[m * nn + p] = (T)(P.wgg_1l[(b0 * 5 + m) * nn + p] * F);
+    X[m * nn + p] = (T)(P.wgg_1l[(b0 * 6 + m) * nn + p] * F);
   }
   for (int p = tid; p < nn; p += LX) {
     const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
@@ -341,7 +348,7 @@ __global__ void __launch_bounds__(LX) k_extra_gg(Params P, const double* __restr
     const Lerp c = fpt_cell(P, llp - nd[p]);
     if (!c.in) continue;
 #pragma unroll
-    for (int m = 0; m < 5; m++) acc += X[m * nn + p] * fpt_val<T>(rows + m * n, c, n);
+    for (int m = 0; m < 6; m++) acc += X[m * nn + p] * fpt_val<T>(rows + m * n, c, n);
   }
   if (mode == 0) P.tab_gg[b0 * P.nnode_g + L] += (double)acc;
   else P.ggl[(b0 * P.lmax_nolimber + L) * 2 + 0] += (double)acc;
@@ -363,7 +370,7 @@ void launch_extra_t(const Params& P, const double* ell_ss, const double* ell_g, 
   }
   if ((P.tatt || P.one_loop) && (P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
     const int nchunk = (P.ns + PC - 1) / PC;  // a lens bin pairs with at most ns sources
-    const size_t sm = al(sizeof(T) * (4 * (size_t)n + 6 * PC * (size_t)P.n_ss + 1)) + sizeof(double) * P.n_ss;
+    const size_t sm = al(sizeof(T) * (5 * (size_t)n + 7 * PC * (size_t)P.n_ss + 1)) + sizeof(double) * P.n_ss;
     dim3 g(P.B, (P.nnode_g + LX - 1) / LX, P.nl * nchunk);
     hk(CL2PT_K_LIMBER_GS, 1);
     k_extra_gs<T><<<g, LX, sm, s>>>(P, ell_g, nchunk);
@@ -373,7 +380,7 @@ void launch_extra_t(const Params& P, const double* ell_ss, const double* ell_g, 
   if (P.one_loop && (P.probes & CL2PT_PROBE_WTHETA)) {
     // FP64 in both plans: at high k the sigma_4-subtracted rows are nearly
     // constant and the five terms cancel to ~1e-3 of their size
-    const size_t sm = al(sizeof(double) * (5 * (size_t)n + 5 * (size_t)P.n_gg + 1)) + 2 * sizeof(double) * P.n_gg;
+    const size_t sm = al(sizeof(double) * (6 * (size_t)n + 6 * (size_t)P.n_gg + 1)) + 2 * sizeof(double) * P.n_gg;
     dim3 g(P.B, (P.nnode_g + LX - 1) / LX, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
     k_extra_gg<double><<<g, LX, sm, s>>>(P, ell_g, 0);

@@ -555,6 +555,22 @@ __global__ void __launch_bounds__(1024) k_nl_order(Params P, NLParams Q)
   for (int i = threadIdx.x; i < n; i += blockDim.x) Q.perm[atomicAdd(&off[bucket(i)], 1)] = i;
 }
 
+// The z = 0 slice P_lin(k_i, z = 0) of each point's linear table
+// (p_lin(k, 1), cosmo3D.c:306-358, linear in z between the table's two
+// columns around z = 0), once per point into a contiguous row: the table
+// is k-major, so the column is a strided gather that every lens-bin CTA of
+// the loop would otherwise repeat.
+__global__ void k_nl_slice(Params P, NLParams Q)
+{
+  const int pt = blockIdx.x;
+  const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
+  const double dy = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
+  const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
+  double* out = Q.pslice + (size_t)pt * P.pkl_nk;
+  for (int i = threadIdx.x; i < P.pkl_nk; i += blockDim.x)
+    out[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
+}
+
 // FP32 head/tail of an angle reduced to [-pi, pi] in FP64
 __device__ __forceinline__ float2 red_angle(double a)
 {
@@ -643,14 +659,13 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   const int j0 = bsearch_d(P.pkl_z, P.pkl_nz, 0.0);
   const double dyz = (0.0 - P.pkl_z[j0]) / (P.pkl_z[j0 + 1] - P.pkl_z[j0]);
   {
-    const double* tabL = P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz;
-    const double dy = dyz;
+    const double* sl = Q.pslice + (size_t)pt * P.pkl_nk;  // k_nl_slice
     for (int i = tid; i < P.pkl_nk; i += nlt) {
       if (ADJ) {
         if (F32) pbarf[i] = 0.0f;
         else pbard[i] = 0.0;
       }
-      psl[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
+      psl[i] = sl[i];
       plk[i] = (T)P.pkl_lk[i];
       if (!F32) {
         plkd[i] = P.pkl_lk[i];
@@ -1087,6 +1102,7 @@ static void launch_nl_prep_t(const Params& P, const NLParams& Q, cudaStream_t s)
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl), NL_NT, sm1, s>>>(P, Q, 0, 0, 3);
   k_nl_gdirect<<<dim3(P.B, 3, Q.ndirect), NL_NT, 0, s>>>(P, Q);
+  k_nl_slice<<<P.B, 256, 0, s>>>(P, Q);
 }
 
 template <typename T>
@@ -1104,7 +1120,7 @@ void launch_nonlimber_prep(const Params& P, const NLParams& Q, cudaStream_t s, i
   if (P.prec == CL2PT_PREC_FP64) launch_nl_prep_t<double>(P, Q, s);
   else launch_nl_prep_t<float>(P, Q, s);
   hk(CL2PT_K_NONLIMBER, 0);
-  (*launches) += 2;
+  (*launches) += 3;
 }
 
 void launch_nonlimber_loop(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk)

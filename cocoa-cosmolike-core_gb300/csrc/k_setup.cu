@@ -344,6 +344,12 @@ __device__ __forceinline__ double gbs2_d(const Params& P, const cl2pt_nuisance& 
   if (P.bias_model[2] == 0) return nu.gb[2][ni];
   return -4. / 7. * (b1 - 1.0);
 }
+// b3 of the selected model (bias.c: b3 = b1 - 1 for bias model 1)
+__device__ __forceinline__ double gb3_d(const Params& P, const cl2pt_nuisance& nu, int ni, double b1)
+{
+  if (P.bias_model[3] == 0) return nu.gb[3][ni];
+  return b1 - 1.0;
+}
 // the reference adds the one-loop bias terms when any lens bin has b2 != 0
 __device__ __forceinline__ bool has_b2(const Params& P, const cl2pt_nuisance& nu)
 {
@@ -409,11 +415,11 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
   const bool hb2 = has_b2(P, nu);
   if (set == 0 && threadIdx.x == 0) {
     P.chi_amin[pt] = chi_all_d(P.chi_z, X, P.chi_nz, P.a_min).chi;
-    // b2 != 0 needs the one-loop path; b3 needs the reference's tabulated
-    // P_d1p3, which is not part of this build
+    // b2 != 0 needs the one-loop path; b3 needs the P_d1p3 table
+    // (cl2pt_plan_set_d1p3)
     bool bad = hb2 && !P.one_loop;
     for (int i = 0; i < P.nl; i++)
-      if (hb2 && nu.gb[3][i] != 0.0) bad = true;
+      if (hb2 && !P.fpt_d1p3 && (nu.gb[3][i] != 0.0 || P.bias_model[3] != 0)) bad = true;
     if (bad) atomicOr(P.err, 1);
   }
   const double nlb = (hb2 && P.one_loop) ? 1.0 : 0.0;
@@ -466,8 +472,10 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
       P.wgs_l[b0 * P.n_ss + p] = WGAL * b1;
       P.wgs_m[b0 * P.n_ss + p] = WMAG * bmag;
       if (P.one_loop) {
-        P.wgs_1l[(b0 * 2 + 0) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gb2_d(P, nu, q, b1);
-        P.wgs_1l[(b0 * 2 + 1) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gbs2_d(P, nu, q, b1);
+        P.wgs_1l[(b0 * 3 + 0) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gb2_d(P, nu, q, b1);
+        P.wgs_1l[(b0 * 3 + 1) * P.n_ss + p] = nlb * 0.5 * D2 * D2 * WGAL * gbs2_d(P, nu, q, b1);
+        P.wgs_1l[(b0 * 3 + 2) * P.n_ss + p] =
+            P.fpt_d1p3 ? nlb * 0.5 * D2 * D2 * WGAL * gb3_d(P, nu, q, b1) : 0.0;
         P.wgs_bk[b0 * P.n_ss + p] = nlb * WGAL * nu.gb[5][q] / (fK * fK);
       }
       double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
@@ -494,12 +502,13 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
       if (P.one_loop) {
         const double b2 = gb2_d(P, nu, q, b1), bs2 = gbs2_d(P, nu, q, b1);
         const double c = nlb * WGAL * WGAL * D2 * D2;
-        double* o = P.wgg_1l + b0 * 5 * P.n_gg + p;
+        double* o = P.wgg_1l + b0 * 6 * P.n_gg + p;
         o[0 * P.n_gg] = c * b1 * b2;
         o[1 * P.n_gg] = c * 0.25 * b2 * b2;
         o[2 * P.n_gg] = c * b1 * bs2;
         o[3 * P.n_gg] = c * 0.5 * b2 * bs2;
         o[4 * P.n_gg] = c * 0.25 * bs2 * bs2;
+        o[5 * P.n_gg] = P.fpt_d1p3 ? c * b1 * gb3_d(P, nu, q, b1) : 0.0;
         P.wgg_bk[b0 * P.n_gg + p] = nlb * 2.0 * b1 * nu.gb[5][q] * WGAL * WGAL / (fK * fK);
       }
       // RSD term at a0 = a_chi(chi_0), chi_0 = (l+1/2)/k = fK

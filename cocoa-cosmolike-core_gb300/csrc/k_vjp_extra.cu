@@ -192,15 +192,16 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
   __syncthreads();
   const int np = npq;
   if (np == 0) return;
-  T* rows = (T*)smem_raw;                  // [4][n] taE, mix, d1d2, d1s2
-  T* rv = rows + 4 * (size_t)n;            // [4][XLC][nn]
-  T* cb0 = rv + 4 * (size_t)XLC * nn;      // [np][XLC] pref2 C_bar
+  T* rows = (T*)smem_raw;                  // [5][n] taE, mix, d1d2, d1s2, d1p3
+  T* rv = rows + 5 * (size_t)n;            // [5][XLC][nn]
+  T* cb0 = rv + 5 * (size_t)XLC * nn;      // [np][XLC] pref2 C_bar
   T* cb1 = cb0 + (size_t)np * XLC;         // [np][XLC] pref2 pref C_bar
   for (int i = p; i < n; i += blockDim.x) {
     rows[i] = P.tatt ? (T)P.fpt_ia[((size_t)pt * 8 + 1) * n + i] : (T)0;
     rows[n + i] = P.tatt ? (T)P.fpt_ia[((size_t)pt * 8 + 3) * n + i] : (T)0;
     rows[2 * n + i] = P.one_loop ? (T)P.fpt_b[((size_t)pt * 5 + 0) * n + i] : (T)0;
     rows[3 * n + i] = P.one_loop ? (T)P.fpt_b[((size_t)pt * 5 + 2) * n + i] : (T)0;
+    rows[4 * n + i] = (P.one_loop && P.fpt_d1p3) ? (T)P.fpt_d1p3[i] : (T)0;
   }
   const bool act = p < nn;
   const int off = P.n_ss + q * P.n_ss;
@@ -208,16 +209,17 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
   if (act) F = node_F(P, pt, off + p, &fK, &D, &a, &H);
   const double lnf = log(fK), D2 = D * D;
   const size_t b0 = (size_t)pt * P.nl + q;
-  double Lg = 0, Mg = 0, g2 = 0, gs2 = 0;
+  double Lg = 0, Mg = 0, g2 = 0, gs2 = 0, g3 = 0;
   if (act) {
     Lg = P.wgs_l[b0 * nn + p];
     Mg = P.wgs_m[b0 * nn + p];
     if (P.one_loop) {
-      g2 = P.wgs_1l[(b0 * 2 + 0) * nn + p];
-      gs2 = P.wgs_1l[(b0 * 2 + 1) * nn + p];
+      g2 = P.wgs_1l[(b0 * 3 + 0) * nn + p];
+      gs2 = P.wgs_1l[(b0 * 3 + 1) * nn + p];
+      g3 = P.wgs_1l[(b0 * 3 + 2) * nn + p];
     }
   }
-  double Lbar = 0, Mbar = 0, g2bar = 0, gs2bar = 0;
+  double Lbar = 0, Mbar = 0, g2bar = 0, gs2bar = 0, g3bar = 0;
   for (int L0 = 0; L0 < K; L0 += XLC) {
     const int nL = min(XLC, K - L0);
     __syncthreads();
@@ -236,28 +238,29 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
     if (act) {
       for (int l = 0; l < nL; l++) {
         const XCell c = x_cell(P, V.lfac_g[6 * (L0 + l)] * LN10 - lnf);
-        for (int r = 0; r < 4; r++) rv[((size_t)r * XLC + l) * nn + p] = x_val<T>(rows + (size_t)r * n, c, n);
+        for (int r = 0; r < 5; r++) rv[((size_t)r * XLC + l) * nn + p] = x_val<T>(rows + (size_t)r * n, c, n);
       }
     }
     __syncthreads();
     if (!act) continue;
     for (int m = 0; m < np; m++) {
-      T x0 = 0, x1 = 0, x2 = 0, x3 = 0, x4 = 0, x5 = 0;
+      T x0 = 0, x1 = 0, x2 = 0, x3 = 0, x4 = 0, x5 = 0, x6 = 0;
       for (int l = 0; l < nL; l++) {
         const T c0 = cb0[m * XLC + l], c1 = cb1[m * XLC + l];
         const T* v = rv + (size_t)l * nn + p;
         const size_t st = (size_t)XLC * nn;
-        const T taE = v[0], mix = v[st], d1d2 = v[2 * st], d1s2 = v[3 * st];
+        const T taE = v[0], mix = v[st], d1d2 = v[2 * st], d1s2 = v[3 * st], d1p3 = v[4 * st];
         x0 += c0 * taE;
         x1 += c0 * mix;
         x2 += c0 * d1d2;
         x3 += c0 * d1s2;
+        x6 += c0 * d1p3;
         x4 += c1 * taE;
         x5 += c1 * mix;
       }
       const int s = ss_[m];
       const size_t o = (b0 * P.ns + s) * nn + p;
-      const double X0 = x0, X1 = x1, X2 = x2, X3 = x3, X4 = x4, X5 = x5;
+      const double X0 = x0, X1 = x1, X2 = x2, X3 = x3, X4 = x4, X5 = x5, X6 = x6;
       if (P.tatt) {
         const double bw = P.wgs_b[o], cw = P.wgs_2[o];
         V.wbar_gsb[o] += -D2 * F * (Lg * X0 + Mg * X4);
@@ -267,13 +270,14 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
       }
       if (P.one_loop) {
         const double WK = P.wgs_k[o];
-        V.wbar_gsk[o] += F * (g2 * X2 + gs2 * X3);
+        V.wbar_gsk[o] += F * (g2 * X2 + gs2 * X3 + g3 * X6);
         g2bar += WK * F * X2;
         gs2bar += WK * F * X3;
+        g3bar += WK * F * X6;
       }
     }
   }
-  double sb2 = 0, sbs2 = 0;
+  double sb2 = 0, sbs2 = 0, sb3 = 0;
   if (act) {
     V.lbar_gs[(b0 * 2 + 0) * nn + p] += Lbar;
     V.lbar_gs[(b0 * 2 + 1) * nn + p] += Mbar;
@@ -283,14 +287,17 @@ __global__ void k_vjpx_gs(Params P, VJPParams V)
       const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
       sb2 = g2bar * 0.5 * D2 * D2 * WGAL;
       sbs2 = gs2bar * 0.5 * D2 * D2 * WGAL;
+      sb3 = g3bar * 0.5 * D2 * D2 * WGAL;
     }
   }
   if (P.one_loop) {
     const double t2 = bsum(sb2, red);
     const double ts = bsum(sbs2, red);
+    const double t3 = bsum(sb3, red);
     if (threadIdx.x == 0) {
       atomicAdd(&V.nu_bar[pt].gb[1][q], t2);
       atomicAdd(&V.nu_bar[pt].gb[2][q], ts);
+      if (P.fpt_d1p3) atomicAdd(&V.nu_bar[pt].gb[3][q], t3);
     }
   }
 }
@@ -302,24 +309,25 @@ __global__ void k_vjpx_gg(Params P, VJPParams V)
   __shared__ double red[32];
   const int pt = blockIdx.x, q = blockIdx.y, p = threadIdx.x;
   const int n = P.fpt_n, nn = P.n_gg, K = P.nnode_g, LNL = P.lmax_nolimber;
-  double* rows = (double*)smem_raw;  // [5][n]
+  double* rows = (double*)smem_raw;  // [6][n]: the five bias rows, d1p3
   const double* src = P.fpt_b + (size_t)pt * 5 * n;
   for (int i = p; i < 5 * n; i += blockDim.x) rows[i] = src[i];
+  for (int i = p; i < n; i += blockDim.x) rows[5 * n + i] = P.fpt_d1p3 ? P.fpt_d1p3[i] : 0.0;
   __syncthreads();
   const size_t b0 = (size_t)pt * P.nl + q;
-  double g[3] = {0, 0, 0};
+  double g[4] = {0, 0, 0, 0};
   if (p < nn && V.one_loop_on[pt]) {
     const int off = P.n_ss + P.nl * P.n_ss + q * nn;
     double fK, D, a, H;
     const double F = node_F(P, pt, off + p, &fK, &D, &a, &H);
     const double lnf = log(fK);
     const double chi_amin = P.chi_amin[pt];
-    double X[5] = {0, 0, 0, 0, 0};
+    double X[6] = {0, 0, 0, 0, 0, 0};
     auto add = [&](const double* fac, double cv) {
       if (cv == 0.0 || fK * fac[5] > chi_amin) return;
       const XCell c = x_cell(P, fac[0] * LN10 - lnf);
       if (!c.in) return;
-      for (int m = 0; m < 5; m++) X[m] += cv * x_val<double>(rows + (size_t)m * n, c, n);
+      for (int m = 0; m < 6; m++) X[m] += cv * x_val<double>(rows + (size_t)m * n, c, n);
     };
     const double* cb = V.cbar_gg + b0 * K;
     for (int L = 0; L < K; L++) add(V.lfac_g + 6 * L, cb[L]);
@@ -327,16 +335,18 @@ __global__ void k_vjpx_gg(Params P, VJPParams V)
       const double* gb = V.ggl_bar + b0 * LNL * 2;
       for (int L = 0; L < LNL; L++) add(V.lfac_gi + 6 * L, gb[2 * L]);
     }
-    // wgg_1l = W_gal^2 D^4 (b1 b2, b2^2/4, b1 bs2, b2 bs2/2, bs2^2/4)
+    // wgg_1l = W_gal^2 D^4 (b1 b2, b2^2/4, b1 bs2, b2 bs2/2, bs2^2/4, b1 b3)
     const cl2pt_nuisance& nu = P.nu[pt];
     const double WGAL = nz_lens_d(P, 1. / a - 1., q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
     const double c = WGAL * WGAL * D * D * D * D * F;
     const double b1 = nu.gb[0][q], b2 = nu.gb[1][q], bs2 = nu.gb[2][q];
-    g[0] = c * (X[0] * b2 + X[2] * bs2);
+    const double b3 = P.fpt_d1p3 ? nu.gb[3][q] : 0.0;
+    g[0] = c * (X[0] * b2 + X[2] * bs2 + X[5] * b3);
     g[1] = c * (X[0] * b1 + X[1] * 0.5 * b2 + X[3] * 0.5 * bs2);
     g[2] = c * (X[2] * b1 + X[3] * 0.5 * b2 + X[4] * 0.5 * bs2);
+    g[3] = P.fpt_d1p3 ? c * X[5] * b1 : 0.0;
   }
-  for (int k = 0; k < 3; k++) {
+  for (int k = 0; k < 4; k++) {
     const double t = bsum(g[k], red);
     if (threadIdx.x == 0) atomicAdd(&V.nu_bar[pt].gb[k][q], t);
   }
@@ -361,7 +371,7 @@ size_t xss_smem(const Params& P)
 template <typename T>
 size_t xgs_smem(const Params& P)
 {
-  return sizeof(T) * (4 * (size_t)P.fpt_n + 4 * (size_t)XLC * P.n_ss + 2 * (size_t)P.ns * XLC) + 64;
+  return sizeof(T) * (5 * (size_t)P.fpt_n + 5 * (size_t)XLC * P.n_ss + 2 * (size_t)P.ns * XLC) + 64;
 }
 
 template <typename T>
@@ -383,7 +393,7 @@ void launch_x(const Params& P, const VJPParams& V, int which, cudaStream_t s)
 
 size_t vjp_extra_smem(const Params& P)
 {
-  size_t m = sizeof(double) * 5 * (size_t)P.fpt_n + 64;
+  size_t m = sizeof(double) * 6 * (size_t)P.fpt_n + 64;
   if (P.prec == CL2PT_PREC_FP64) m = std::max(m, std::max(xss_smem<double>(P), xgs_smem<double>(P)));
   else m = std::max(m, std::max(xss_smem<float>(P), xgs_smem<float>(P)));
   return m;
@@ -397,7 +407,7 @@ void launch_vjp_extra(const Params& P, const VJPParams& V, int which, cudaStream
     return;
   }
   if (which == 2) {
-    const size_t sm = sizeof(double) * 5 * (size_t)P.fpt_n + 64;
+    const size_t sm = sizeof(double) * 6 * (size_t)P.fpt_n + 64;
     cudaFuncSetAttribute(k_vjpx_gg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_vjpx_gg<<<dim3(P.B, P.nl), ((P.n_gg + 31) / 32) * 32, sm, s>>>(P, V);
     return;

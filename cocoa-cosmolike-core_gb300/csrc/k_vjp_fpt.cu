@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(RT) k_vjpr_gs(Params P, VJPParams V)
     }
     if (P.one_loop) {
       const double WK = P.wgs_k[o];
-      x[2] = WK * P.wgs_1l[(b0 * 2 + 0) * nn + p] * F;
-      x[3] = WK * P.wgs_1l[(b0 * 2 + 1) * nn + p] * F;
+      x[2] = WK * P.wgs_1l[(b0 * 3 + 0) * nn + p] * F;
+      x[3] = WK * P.wgs_1l[(b0 * 3 + 1) * nn + p] * F;
     }
 #pragma unroll
     for (int r = 0; r < 6; r++) X[r * st + (size_t)m * nn + p] = (T)x[r];
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(RT) k_vjpr_gg(Params P, VJPParams V)
     const int m = idx / nn, p = idx - m * nn;
     double fK, D;
     const double F = node_F(P, pt, off + p, &fK, &D);
-    X[m * nn + p] = P.wgg_1l[(b0 * 5 + m) * nn + p] * F;
+    X[m * nn + p] = P.wgg_1l[(b0 * 6 + m) * nn + p] * F;
     if (m == 0) {
       nd[p] = log(fK);
       nd[nn + p] = fK;

@@ -22,6 +22,8 @@ struct NLParams {
   void* gstate;     // [CTA][3][2][hstride] complex recurrence state (loop precision)
   double* gdir;     // [point][3][ndirect][hstride] directly evaluated g_l (FP64 complex)
   int* perm;        // [point * bin] dispatch order of the multipole loop CTAs
+  double* pslice;   // [point][pkl_nk] z = 0 slice of the linear table (k_nl_slice),
+                    // read by all of a point's lens-bin CTAs
   int ndirect;      // multipoles evaluated directly per kernel
   int direct_every; // 1: restart the recurrence every 16-block (FP64 plan)
   size_t gst_stride;

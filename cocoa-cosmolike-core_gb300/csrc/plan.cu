@@ -342,8 +342,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     return CL2PT_ERR_ARG;
   if (precision != CL2PT_PREC_MIXED && precision != CL2PT_PREC_FP64) return CL2PT_ERR_ARG;
   if (cfg->ia_mode == CL2PT_IA_NLA_LF) return CL2PT_ERR_UNSUPPORTED;
-  // b3 from b1 would need the reference's tabulated P_d1p3
-  if (cfg->one_loop_bias && cfg->bias_model[3] != 0) return CL2PT_ERR_UNSUPPORTED;
+  if (cfg->bias_model[3] != 0 && cfg->bias_model[3] != 1) return CL2PT_ERR_ARG;
   if (cfg->bias_model[4] != 0 || cfg->bias_model[5] != 0) return CL2PT_ERR_ARG;
   if (grid->chi_nz < 5 || grid->G_nz < 2 || grid->pk_nk < 2 || grid->pk_nz < 2)
     return CL2PT_ERR_ARG;
@@ -712,8 +711,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(cl2pt_fastpt_plan_create(kx.data(), nf, a, bt, l, 13, &fc, W, &p->fpt_bias));
       TRY(dalloc(p, &p->d_fpt_bias_out, (size_t)W * 5 * nf));
       TRY(dalloc(p, &P.fpt_b, (size_t)W * 5 * nf));
-      TRY(dalloc(p, &P.wgs_1l, (size_t)W * nl * 2 * p->n_ss));
-      TRY(dalloc(p, &P.wgg_1l, (size_t)W * nl * 5 * p->n_gg));
+      TRY(dalloc(p, &P.wgs_1l, (size_t)W * nl * 3 * p->n_ss));
+      TRY(dalloc(p, &P.wgg_1l, (size_t)W * nl * 6 * p->n_gg));
       TRY(dalloc(p, &P.wgs_bk, (size_t)W * nl * p->n_ss));
       TRY(dalloc(p, &P.wgg_bk, (size_t)W * nl * p->n_gg));
     }
@@ -820,6 +819,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       Q.ndirect = Q.direct_every ? 2 * ((LNL + 15) / 16) : 2;
       TRY(dalloc(p, &Q.gdir, (size_t)W * 3 * Q.ndirect * Q.hstride * 2));
       TRY(dalloc(p, &Q.perm, (size_t)W * nl));
+      TRY(dalloc(p, &Q.pslice, (size_t)W * P.pkl_nk));
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
@@ -888,7 +888,8 @@ extern "C" int cl2pt_plan_set_contraction(cl2pt_plan* p, int mode)
   }
   if (p->prec != CL2PT_PREC_MIXED) return CL2PT_ERR_UNSUPPORTED;
   if (p->tcf_mode != mode) {
-    const int kind = (mode == CL2PT_CONTRACT_TF32X3) ? 0 : 1, S = (mode == CL2PT_CONTRACT_BF16X6) ? 3 : 2;
+    const int kind = mode == CL2PT_CONTRACT_TF32X3 ? 0 : 1;
+    const int S = mode == CL2PT_CONTRACT_BF16X6 ? 3 : 2;
     for (int f = 0; f < 4; f++) {
       const int M = p->filt_M[f], K = (int)(p->filt_host[f].size() / M);
       std::vector<uint8_t> pieces;
@@ -907,6 +908,20 @@ extern "C" int cl2pt_plan_set_contraction(cl2pt_plan* p, int mode)
     p->tcf_mode = mode;
   }
   p->contract = mode;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_plan_set_d1p3(cl2pt_plan* p, const double* p_d1p3, int n)
+{
+  if (!p || !p_d1p3) return CL2PT_ERR_ARG;
+  if (!p->P.one_loop) return CL2PT_ERR_STATE;
+  if (n != p->P.fpt_n) return CL2PT_ERR_ARG;
+  for (int i = 0; i < n; i++)
+    if (!std::isfinite(p_d1p3[i])) return CL2PT_ERR_ARG;
+  if (!p->d_fpt_d1p3)
+    if (int st = dalloc(p, &p->d_fpt_d1p3, (size_t)n)) return st;
+  CUDA_OK(cudaMemcpy(p->d_fpt_d1p3, p_d1p3, sizeof(double) * n, cudaMemcpyHostToDevice));
+  p->P.fpt_d1p3 = p->d_fpt_d1p3;
   return CL2PT_OK;
 }
 
@@ -1061,7 +1076,8 @@ extern "C" int cl2pt_eval_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell,
 static int vjp_prepare(cl2pt_plan* p)
 {
   const cl2pt_config& c = p->cfg;
-  if (c.bias_model[0] != 0 || c.bias_model[1] != 0 || c.bias_model[2] != 0 || c.linear_pk)
+  if (c.bias_model[0] != 0 || c.bias_model[1] != 0 || c.bias_model[2] != 0 || c.bias_model[3] != 0 ||
+      c.linear_pk)
     return CL2PT_ERR_UNSUPPORTED;
   if (cl2pt::vjp_limber_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
   if ((p->P.tatt || p->P.one_loop) && cl2pt::vjp_extra_smem(p->P) > 232448 - 1024) return CL2PT_ERR_UNSUPPORTED;
@@ -1920,8 +1936,9 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
         }
       }
       if (p->contract != CL2PT_CONTRACT_FP32 && P.prec == CL2PT_PREC_MIXED) {
-        cl2pt::launch_legendre_tc(P, p->tcf, p->contract == CL2PT_CONTRACT_TF32X3 ? 0 : 1,
-                                  p->contract == CL2PT_CONTRACT_BF16X6 ? 3 : 2, s, &launches, hk);
+        const int c = p->contract;
+        cl2pt::launch_legendre_tc(P, p->tcf, c == CL2PT_CONTRACT_TF32X3 ? 0 : 1, c == CL2PT_CONTRACT_BF16X6 ? 3 : 2,
+                                  s, &launches, hk);
       } else {
         cl2pt::SplitFilter sf[4];
         for (int f = 0; f < 4; f++) sf[f] = {p->d_sfilt[f][0], p->d_sfilt[f][1], p->sfilt_Mp[f], p->sfilt_Ksp[f]};

@@ -99,6 +99,7 @@ struct cl2pt_plan {
   // on first use
   double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
   double* d_vjp_fpt = nullptr;         // FAST-PT tables' share (TATT / one-loop plans)
+  double* d_fpt_d1p3 = nullptr;        // the caller's P_d1p3 on the FAST-PT grid
   double* d_vjp_cot = nullptr;         // [max_batch][n_total] (grown for Fourier vectors)
   size_t vjp_cot_cap = 0;
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]

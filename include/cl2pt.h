@@ -288,6 +288,17 @@ int cl2pt_kernel_times(cl2pt_plan* plan, double* ms, int* launches);
 /* Number of kernel launches issued by the last eval call. */
 int cl2pt_last_launch_count(const cl2pt_plan* plan);
 
+/* The one-loop b3 spectrum P_d1p3 of a one-loop plan (cl2pt_config
+ * one_loop_bias), on the plan's FAST-PT k grid: n = 1100 values at
+ * ln k_i = ln 0.05 + i (ln 1e6 - ln 0.05) / 1100 (k c/H0, k in h/Mpc).
+ * The reference interpolates a table it embeds onto that grid
+ * (FPTbias.tab[5], cosmolike/pt_cfastpt.c:161-169) and uses it with b3 in
+ * the C_gs and C_gg integrands (cosmo2D.c:1890-2073, 2490-2608); here the
+ * caller supplies it.  Until it is set, a point with b3 != 0 (or bias
+ * model 1 for b3) reports a device error.  CL2PT_ERR_STATE for plans
+ * without one-loop terms. */
+int cl2pt_plan_set_d1p3(cl2pt_plan* plan, const double* p_d1p3, int n);
+
 /* Select the Legendre contraction of a mixed plan (CL2PT_CONTRACT_*; the
  * reference's xi_pm_tomo / w_gammat_tomo / w_gg_tomo sums,
  * cosmo2D.c:500-534, 680-699, 859-878).  The tensor-core forms need at

@@ -195,6 +195,15 @@ class Oracle:
         f(_p(out), C.byref(n))
         return out.reshape(8, n.value)
 
+    def set_d1d3_table(self, tab, lnkmin, lnkmax):
+        """The P_d1p3 table the oracle interpolates in ln k (the reference
+        embeds one; the default is none, i.e. zero)."""
+        t = np.ascontiguousarray(tab, dtype=np.float64)
+        self._keep.append(t)
+        f = getattr(self.lib, self.which + "_set_d1d3_table")
+        f.argtypes = [_dp, C.c_int, C.c_double, C.c_double]
+        return f(_p(t), len(t), lnkmin, lnkmax)
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

@@ -77,7 +77,9 @@ def blocks(plan, dv):
 
 
 def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None, bmag=False,
-             contract=None):
+             contract=None, d1p3=None):
+    """d1p3: a P_d1p3 table on the FAST-PT grid for the one-loop b3 terms,
+    given to both the plan and the oracle."""
     import oracle as O
     w = workloads.make(name)
     if tweak is not None:
@@ -89,10 +91,14 @@ def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=N
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=npts, linear_table=True)
     if contract is not None:
         plan.set_contraction(contract)
+    if d1p3 is not None:
+        plan.set_d1p3(d1p3)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
+    if d1p3 is not None:
+        o.set_d1d3_table(d1p3, np.log(0.05), np.log(1e6))
     worst = {}
     nint = w.cfg.lmin_tab - 1
     tatt = w.cfg.ia_model == abi.IA_TATT
@@ -153,6 +159,8 @@ def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=N
                 ocl, oconv = o.C_cl_tomo()
                 worst["C_nonlimber"] = max(worst.get("C_nonlimber", 0), rel_err(gcl[:, 1:], ocl[:, 1:]))
                 assert np.array_equal(gconv, oconv), (gconv, oconv)
+    if d1p3 is not None:
+        o.set_d1d3_table(np.zeros(0), 0.0, 0.0)  # the oracle's state is per process
     return worst, plan
 
 
@@ -190,6 +198,59 @@ def test_one_loop_bk(gpu_lib, oracle_built, prec):
     print(prec, worst)
     for k, v in worst.items():
         assert v <= REL, (k, v, worst)
+
+
+def reference_d1p3():
+    """The reference's P_d1p3 on the FAST-PT grid: row 5 of its own
+    get_FPT_bias output (the table it embeds, interpolated,
+    pt_cfastpt.c:161-169)."""
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    return np.load(os.path.join(here, "golden", "fastpt_bias.npz"))["fpt_bias"][5]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_one_loop_b3(gpu_lib, oracle_built, prec):
+    """One-loop b3 ~ U(-1, 1) per lens bin (the b3 P_d1p3 terms of C_gs and
+    C_gg, cosmo2D.c:1890-2073, 2490-2608) with the reference's P_d1p3, on
+    plan and oracle; b3 moves gamma_t and w by far more than the bar."""
+    rng = np.random.default_rng(23)
+    b3 = rng.uniform(-1.0, 1.0, size=(2, 5))
+
+    def set_b3(i, nu):
+        for q in range(5):
+            nu.gb[3][q] = float(b3[i, q])
+    tab = reference_d1p3()
+    worst, plan = run_case("real_3x2pt_tatt_small", 2, prec, seed=11, nu_tweak=set_b3, d1p3=tab,
+                           check_tables=False)
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 2, seed=11)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    dv0 = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
+    for i, nu in enumerate(nus):
+        set_b3(i, nu)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
+    change = np.max(np.abs(dv - dv0)) / np.max(np.abs(dv0))
+    print("b3 effect", change)
+    assert change > 1e-3
+
+
+@pytest.mark.gpu
+def test_b3_needs_d1p3(gpu_lib):
+    """Without a P_d1p3 table a point with b3 != 0 is a device error."""
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 1, seed=3)
+    nus[0].gb[3][0] = 0.5
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    with pytest.raises(lib.CL2PTError):
+        plan.eval_real(om, h0, chi, G, lnP, nus)
+    plan.set_d1p3(reference_d1p3())
+    assert np.all(np.isfinite(plan.eval_real(om, h0, chi, G, lnP, nus)))
 
 
 @pytest.mark.gpu

@@ -620,6 +620,55 @@ def test_vjp_tatt_one_loop_vs_oracle_fd(gpu_lib, oracle_built, tables):
 
 
 @pytest.mark.gpu
+def test_vjp_b3(gpu_lib, oracle_built):
+    """The one-loop b3 terms with the reference's P_d1p3: the b3 and b1
+    gradients against differences of the FP64 forward (1e-6) and the b3
+    gradient against differences of the oracle (1e-4)."""
+    import os
+    import oracle as O
+    here = os.path.dirname(os.path.abspath(__file__))
+    tab = np.load(os.path.join(here, "golden", "fastpt_bias.npz"))["fpt_bias"][5]
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 1, seed=61)
+    rng = np.random.default_rng(62)
+    for q in range(w.cfg.n_lens):
+        nus[0].gb[3][q] = float(rng.uniform(-1.0, 1.0))
+    p64 = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_FP64, max_batch=1)
+    p64.set_d1p3(tab)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    v = rng.normal(size=(1, p64.n_total))
+    _, lbar, nbar = p64.vjp_real(om, h0, chi, G, lnP, nus, v)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    o.set_d1d3_table(tab, np.log(0.05), np.log(1e6))
+    worst = 0.0
+    for field, i, j in [("gb", 3, q) for q in range(w.cfg.n_lens)] + [("gb", 0, 1), ("gb", 0, 3)]:
+        x0 = nu_get(nus[0], field, i, j)
+        # the data vector is linear in b3 and quadratic in b1, so a central
+        # difference is exact at any step: a large one keeps the forward's
+        # rounding out of it
+        h = 0.05 * max(abs(x0), 0.5)
+        f, fo = [], []
+        for sg in (1, -1):
+            nu = clone(nus[0])
+            nu_set(nu, field, i, j, x0 + sg * h)
+            f.append(float(v[0] @ p64.eval_real(om, h0, chi, G, lnP, [nu])[0]))
+            if i == 3 and j < 2:
+                o.set_point(tabs[0], nu)
+                fo.append(float(v[0] @ o.data_vector_real()))
+        fd = (f[0] - f[1]) / (2 * h)
+        an = nbar[0, flat_index(field, i, j)]
+        err = abs(an - fd) / max(abs(fd), 1e-9 * abs(f[0]))
+        worst = max(worst, err)
+        assert err <= GRAD_REL, (field, i, j, an, fd)
+        if fo:
+            fdo = (fo[0] - fo[1]) / (2 * h)
+            assert abs(an - fdo) <= ORACLE_REL * abs(fdo), (field, i, j, an, fdo)
+    o.set_d1d3_table(np.zeros(0), 0.0, 0.0)
+    print("b3 max rel gradient error", worst)
+
+
+@pytest.mark.gpu
 def test_jacobian_rows(gpu_lib):
     """cl2pt_jacobian_real: rows of the Jacobian equal the VJP of the one-hot
     cotangent, the value equals the forward, a chunked pass (max_batch
