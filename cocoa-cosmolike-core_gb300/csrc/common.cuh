@@ -81,6 +81,19 @@ struct Params {
   // mixed plan: FP32 records of the gg nodes [B][nl][GGN_SLOTS][n_gg]
   // (k_gg_nodes, k_limber.cu)
   float* ggn;
+  // mixed plan: FP32 forms of the tables the Limber tiles search, formed
+  // once instead of in every tile (k_limber.cu): the log10 k axes of both
+  // P tables [3][nk] (head, tail, 1 / width; k_prep_consts, when the plan
+  // is made), the lens n(z) splines [nl][5][lens_nz] (nodes, values,
+  // second-derivative coefficients, per-interval b and d), and per point
+  // the distance and growth tables [B][ggt_stride] (chi, z, chi_all's down
+  // and up slopes, 1 / chi-cell width [chi_nz each]; G, G slope, G's z
+  // axis [G_nz each]; k_gg_nodes)
+  float* axk;
+  float* axkl;
+  float* lensf;
+  float* ggt;
+  int ggt_stride;
   // mixed plan, when an adjoint follows (real space): the redshift-space
   // weight s(l, node) of every gg term the forward sums, 0 where the
   // chi(a_min) cut drops it [B][nl][n_gg][nnode_g + lmax_nolimber] (C_l
@@ -150,6 +163,23 @@ struct Params {
 
 enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };
 constexpr int GGN_SLOTS = 16;  // floats per gg node record (k_gg_nodes)
+
+// FP64 value of an FP32 one by integer arithmetic (exact, as the hardware
+// conversion).  GB300 issues FP64 instructions, conversions included, at
+// 1/64 of the FP32 rate, so FP32 kernels that write FP64 results convert
+// this way; zeros keep their sign, subnormals, infinities and NaNs take the
+// hardware conversion.
+__device__ __forceinline__ double f32_to_f64_int(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  if ((u & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)s);
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long b =
+      s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
 
 // ---------------------------------------------------------------------
 // FP64 lookups (restating cosmolike/cosmo3D.c and redshift_spline.c)

@@ -14,6 +14,7 @@
 //            weights held in shared memory (broadcast reads).
 // gg carries the l-dependent redshift-space term W_RSD (evaluated at
 // a_chi((l+3/2)/k)), so it is summed node by node instead.
+#include <type_traits>
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -157,6 +158,62 @@ __device__ __forceinline__ AxisF load_axis_f(const double* __restrict__ lk, int 
   a.inv = sinv;
   a.nk = nk;
   return a;
+}
+
+// load_axis_f's arrays from the plan's precomputed copy src = [3][nk]
+// (Params::axk / axkl)
+__device__ __forceinline__ AxisF copy_axis_f(const float* __restrict__ src, int nk, float* sk, float* skl,
+                                             float* sinv)
+{
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    sk[i] = src[i];
+    skl[i] = src[nk + i];
+    sinv[i] = src[2 * nk + i];
+  }
+  AxisF a;
+  a.lk = sk;
+  a.lkl = skl;
+  a.inv = sinv;
+  a.nk = nk;
+  return a;
+}
+
+// The mixed plan's FP32 constants (Params::axk, axkl, lensf), formed once
+// when the plan is made with the same FP64 arithmetic the tiles used to
+// repeat: entries [0, 3 pk_nk) the lnP axis, then 3 pkl_nk the lnP_lin
+// axis, then nl * lens_nz entries of the lens splines.
+__global__ void k_prep_consts(Params P)
+{
+  const int n0 = P.pk_nk, n1 = P.pkl_nk, nzs = P.lens_nz;
+  const int total = n0 + n1 + P.nl * nzs;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    if (e < n0 + n1) {
+      const bool lin = e >= n0;
+      const int nk = lin ? n1 : n0, i = lin ? e - n0 : e;
+      const double* lk = lin ? P.pkl_lk : P.pk_lk;
+      float* d = lin ? P.axkl : P.axk;
+      const float h = (float)lk[i];
+      d[i] = h;
+      d[nk + i] = (float)(lk[i] - (double)h);
+      d[2 * nk + i] = (i + 1 < nk) ? (float)(1.0 / (lk[i + 1] - lk[i])) : 0.0f;
+      continue;
+    }
+    const int q = (e - n0 - n1) / nzs, i = (e - n0 - n1) - q * nzs;
+    const double* yq = P.lens_y + (q + 1) * nzs;
+    const double* cq = P.lens_c + (q + 1) * nzs;
+    float* d = P.lensf + (size_t)q * 5 * nzs;
+    d[i] = (float)P.lens_zc[i];
+    d[nzs + i] = (float)yq[i];
+    d[2 * nzs + i] = (float)cq[i];
+    const double h = (i + 1 < nzs) ? P.lens_zc[i + 1] - P.lens_zc[i] : 1.0;
+    d[3 * nzs + i] = (i + 1 < nzs) ? (float)((yq[i + 1] - yq[i]) / h - h * (cq[i + 1] + 2.0 * cq[i]) / 3.0) : 0.0f;
+    d[4 * nzs + i] = (i + 1 < nzs) ? (float)((cq[i + 1] - cq[i]) / (3.0 * h)) : 0.0f;
+  }
+}
+
+void launch_prep_consts(const Params& P, cudaStream_t s)
+{
+  k_prep_consts<<<64, 256, 0, s>>>(P);
 }
 
 // FP32 head/tail of an FP64 value
@@ -340,7 +397,7 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   Axis<T> ax{};
   AxisF axf{};
   float2* nlc2 = (float2*)nlc;
-  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
+  if constexpr (F32) axf = copy_axis_f(P.linear_pk ? P.axkl : P.axk, pd.nk, (float*)lk, lkt, lki);
   else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
@@ -413,7 +470,7 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
           a[7] += xb.w * ps;
         }
         for (int c = 0; c < 8 && g + c < P.pss; c++) {
-          const double v = (double)(pref * a[c]);
+          const double v = f32_to_f64_int(pref * a[c]);
           double* o = out + (size_t)(g + c) * P.nnode_ss + L;
           *o = (p0 == 0) ? v : *o + v;
         }
@@ -490,7 +547,7 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   Axis<T> ax{};
   AxisF axf{};
   float2* nlc2 = (float2*)nlc;
-  if constexpr (F32) axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
+  if constexpr (F32) axf = copy_axis_f(P.linear_pk ? P.axkl : P.axk, pd.nk, (float*)lk, lkt, lki);
   else ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
   const int off = P.n_ss + q * P.n_ss;
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
@@ -586,7 +643,10 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
         const T* x2 = X + (2 * CL2PT_MAXB + m) * PCH;
         for (int p = 0; p < np; p++) a2 += x2[p] * Ps[p * LT + tid];
       }
-      const double v = (double)(pref2 * (a0 + pref * a1 + lp2 * a2));
+      const T r = pref2 * (a0 + pref * a1 + lp2 * a2);
+      double v;
+      if constexpr (F32) v = f32_to_f64_int(r);
+      else v = r;
       double* o = out + (size_t)kk[m] * P.nnode_g + L;
       *o = (p0 == 0) ? v : *o + v;
     }
@@ -611,6 +671,48 @@ __device__ __forceinline__ int bsearch_from(const T* __restrict__ x, int n, T v,
 }
 
 constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
+static_assert(9 * PCH >= 2 * LTG, "k_limber_gg reduces its halves in the node-data space");
+
+// chi_all's slopes of cell i (cosmo3D.c:60-72), formed in FP64: 'up' and
+// 'down'
+__device__ __forceinline__ void chi_slopes(const double* __restrict__ Xg, const double* __restrict__ Z, int nc,
+                                           int i, double& up, double& dn)
+{
+  if (i + 1 >= nc) {
+    up = dn = 0.0;
+    return;
+  }
+  const int j2 = (i + 2 < nc) ? i + 2 : nc - 1;
+  up = (Xg[j2] - Xg[i]) / (Z[j2] - Z[i]);
+  dn = (i > 0) ? (Xg[i + 1] - Xg[i - 1]) / (Z[i + 1] - Z[i - 1]) : (Xg[i + 1] - Xg[i]) / (Z[i + 1] - Z[i]);
+}
+
+// FP64 plan: the gg tile's distance, growth and n(z) tables in shared memory
+template <typename T>
+__device__ __forceinline__ void gg_tables_f64(const double* __restrict__ Xg, const double* __restrict__ Gg,
+                                              const Params& P, int q, T* cx, T* cz, T* cdn, T* cup, T* gv, T* gs,
+                                              T* gz, T* szc, T* sy, T* sc)
+{
+  const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    double up, dn;
+    chi_slopes(Xg, P.chi_z, nc, i, up, dn);
+    cx[i] = (T)Xg[i];
+    cz[i] = (T)P.chi_z[i];
+    cup[i] = (T)up;
+    cdn[i] = (T)dn;
+  }
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) {
+    gv[i] = (T)Gg[i];
+    gz[i] = (T)P.G_z[i];
+    gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
+  }
+  for (int i = threadIdx.x; i < nzs; i += blockDim.x) {
+    szc[i] = (T)P.lens_zc[i];
+    sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
+    sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
+  }
+}
 
 // Mixed plan: per (point, lens bin) the gg node data the multipole tiles of
 // k_limber_gg read, formed once in FP64 and stored as FP32 records instead
@@ -631,6 +733,27 @@ __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __rest
   const int* nodej = P.node_j + (size_t)pt * P.node_stride;
   const double chi_amin = P.chi_amin[pt];
   const PdeltaTable pl = pdelta_table(P, pt, true);
+  if (q == 0) {
+    // the point's FP32 distance and growth tables (Params::ggt)
+    const double* Xg = P.chi + (size_t)pt * P.chi_nz;
+    const double* Gg = P.G + (size_t)pt * P.G_nz;
+    const int nc = P.chi_nz, ng = P.G_nz;
+    float* gt = P.ggt + (size_t)pt * P.ggt_stride;
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      double up, dn;
+      chi_slopes(Xg, P.chi_z, nc, i, up, dn);
+      gt[i] = (float)Xg[i];
+      gt[nc + i] = (float)P.chi_z[i];
+      gt[2 * nc + i] = (float)dn;
+      gt[3 * nc + i] = (float)up;
+      gt[4 * nc + i] = (i + 1 < nc) ? (float)(1.0 / (Xg[i + 1] - Xg[i])) : 0.0f;
+    }
+    for (int i = threadIdx.x; i < ng; i += blockDim.x) {
+      gt[5 * nc + i] = (float)Gg[i];
+      gt[5 * nc + ng + i] = (float)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
+      gt[5 * nc + 2 * ng + i] = (float)P.G_z[i];
+    }
+  }
   for (int p = threadIdx.x; p < P.n_gg; p += blockDim.x) {
     const double a = node[(size_t)NF_A * P.node_stride + off + p];
     const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
@@ -667,15 +790,22 @@ __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __rest
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __restrict__ ell,
-                                                   int mode)
+// NH = 2 only in the mixed plan (the FP64 node walk is not split)
+template <typename T, int NH>
+__global__ void __launch_bounds__(NH * LTG) k_limber_gg(Params P, const double* __restrict__ ell,
+                                                        int mode)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
   const int q = blockIdx.z;
   const int tid = threadIdx.x;
-  const int L = blockIdx.y * LTG + tid;
+  const int nth = blockDim.x;
+  // NH = 2 (the mixed plan's integer-l pass: LNL multipoles, fewer than a
+  // tile): two halves of the CTA over the two halves of each node chunk,
+  // so that the CTA's threads all work; NH = 1: one thread per multipole
+  const int lt = nth / NH;
+  const int half = (NH == 2 && tid >= lt) ? 1 : 0;
+  const int L = blockIdx.y * lt + (tid - half * lt);
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   const PdeltaTable pl = pdelta_table(P, pt, true);
   const int nc = P.chi_nz, ng = P.G_nz, nzs = P.lens_nz;
@@ -763,45 +893,38 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
   Axis<T> ax{}, axl{};
   AxisF axf{}, axlf{};
   if constexpr (F32) {
-    axf = load_axis_f(pd.lk, pd.nk, (float*)lk, lkt, lki);
-    if (mode == 1) axlf = load_axis_f(pl.lk, pl.nk, (float*)lkl, lklt, lkli);
+    axf = copy_axis_f(P.linear_pk ? P.axkl : P.axk, pd.nk, (float*)lk, lkt, lki);
+    if (mode == 1) axlf = copy_axis_f(P.axkl, pl.nk, (float*)lkl, lklt, lkli);
   } else {
     ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
     axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
   }
-  const double* Z = P.chi_z;
-  for (int i = tid; i < nc; i += LTG) {
-    cx[i] = (T)Xg[i];
-    cz[i] = (T)Z[i];
-    if (i + 1 < nc) {
-      // slopes of chi_all (cosmo3D.c:60-72), formed in FP64
-      const int j2 = (i + 2 < nc) ? i + 2 : nc - 1;
-      cup[i] = (T)((Xg[j2] - Xg[i]) / (Z[j2] - Z[i]));
-      cdn[i] = (T)((i > 0) ? (Xg[i + 1] - Xg[i - 1]) / (Z[i + 1] - Z[i - 1])
-                           : (Xg[i + 1] - Xg[i]) / (Z[i + 1] - Z[i]));
-    } else {
-      cup[i] = cdn[i] = (T)0;
+  if constexpr (F32) {
+    // the point's tables of k_gg_nodes and the plan's lens splines
+    const float* gt = P.ggt + (size_t)pt * P.ggt_stride;
+    for (int i = tid; i < nc; i += nth) {
+      cx[i] = gt[i];
+      cz[i] = gt[nc + i];
+      cdn[i] = gt[2 * nc + i];
+      cup[i] = gt[3 * nc + i];
+      icx[i] = gt[4 * nc + i];
     }
-  }
-  for (int i = tid; i < ng; i += LTG) {
-    gv[i] = (T)Gg[i];
-    if (!F32 || !same_axis) gz[i] = (T)P.G_z[i];
-    gs[i] = (T)((i + 1 < ng) ? (Gg[i + 1] - Gg[i]) / (P.G_z[i + 1] - P.G_z[i]) : 0.0);
-  }
-  for (int i = tid; i < nzs; i += LTG) {
-    szc[i] = (T)P.lens_zc[i];
-    sy[i] = (T)P.lens_y[(q + 1) * nzs + i];
-    sc[i] = (T)P.lens_c[(q + 1) * nzs + i];
-    if constexpr (F32) {
-      const double* yq = P.lens_y + (q + 1) * nzs;
-      const double* cq = P.lens_c + (q + 1) * nzs;
-      const double h = (i + 1 < nzs) ? P.lens_zc[i + 1] - P.lens_zc[i] : 1.0;
-      sbq[i] = (i + 1 < nzs) ? (float)((yq[i + 1] - yq[i]) / h - h * (cq[i + 1] + 2.0 * cq[i]) / 3.0) : 0.0f;
-      sdq[i] = (i + 1 < nzs) ? (float)((cq[i + 1] - cq[i]) / (3.0 * h)) : 0.0f;
+    for (int i = tid; i < ng; i += nth) {
+      gv[i] = gt[5 * nc + i];
+      gs[i] = gt[5 * nc + ng + i];
+      if (!same_axis) gz[i] = gt[5 * nc + 2 * ng + i];
     }
+    const float* lz = P.lensf + (size_t)q * 5 * nzs;
+    for (int i = tid; i < nzs; i += nth) {
+      szc[i] = lz[i];
+      sy[i] = lz[nzs + i];
+      sc[i] = lz[2 * nzs + i];
+      sbq[i] = lz[3 * nzs + i];
+      sdq[i] = lz[4 * nzs + i];
+    }
+  } else {
+    gg_tables_f64<T>(Xg, Gg, P, q, cx, cz, cdn, cup, gv, gs, gz, szc, sy, sc);
   }
-  if constexpr (F32)
-    for (int i = tid; i < nc; i += LTG) icx[i] = (i + 1 < nc) ? (float)(1.0 / (Xg[i + 1] - Xg[i])) : 0.0f;
   const cl2pt_nuisance& nu = P.nu[pt];
   const T ldz = (T)nu.lens_dz[q], lst = (T)nu.lens_stretch[q], lzm = (T)P.zmean_lens[q];
   const int off = P.n_ss + P.nl * P.n_ss + q * P.n_gg;
@@ -850,7 +973,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     if constexpr (F32) {
       // the node records of k_gg_nodes: no FP64 in the tile
       const float* rec = P.ggn + b0 * GGN_SLOTS * P.n_gg + p0;
-      for (int p = tid; p < np; p += LTG) {
+      for (int p = tid; p < np; p += nth) {
         for (int f = 0; f < 9; f++) nf[f * PCH + p] = rec[(size_t)f * P.n_gg + p];
         nj[p] = __float_as_int(rec[(size_t)9 * P.n_gg + p]);
         nj[PCH + p] = __float_as_int(rec[(size_t)10 * P.n_gg + p]);
@@ -861,7 +984,7 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
         thr[p] = __longlong_as_double(((long long)hi << 32) | lo);
       }
     }
-    for (int p = tid; p < np && !F32; p += LTG) {
+    for (int p = tid; p < np && !F32; p += nth) {
       const double a = node[(size_t)NF_A * P.node_stride + off + p0 + p];
       const double fK = node[(size_t)NF_FK * P.node_stride + off + p0 + p];
       const double wq = node[(size_t)NF_WT * P.node_stride + off + p0 + p] *
@@ -893,65 +1016,70 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     __syncthreads();
     if (!valid) continue;
     const double llp = F32 ? 0.0 : log10(lp);
-    const float2 ll = llf;
     float snl = 0.0f, sln = 0.0f;  // mixed plan: this chunk's FP32 sums
-    for (int p = 0; p < np; p++) {
-      T fkc, Lw, Mw, r0w;
-      if constexpr (F32) {
-        if (cut_idx ? L < lmin[p] : lp < thr[p]) {  // (l+3/2)/k beyond chi(a_min)
-          if (sgg) sgg[(size_t)(p0 + p) * Ltot] = 0.0f;
-          continue;
+    if constexpr (F32) {
+      // one copy of the node walk per form of the chi(a_min) cut -- the
+      // first-kept index, or the FP64 threshold for a list that does not
+      // ascend -- so that the usual case issues no FP64 compare per node
+      const int pb = (np * half) / NH, pe = (np * (half + 1)) / NH;
+      auto walk = [&](auto idx_cut) {
+        for (int p = pb; p < pe; p++) {
+          if (decltype(idx_cut)::value ? L < lmin[p] : lp < thr[p]) {  // (l+3/2)/k beyond chi(a_min)
+            if (sgg) sgg[(size_t)(p0 + p) * Ltot] = 0.0f;
+            continue;
+          }
+          const float fkc = nf[0 * PCH + p];
+          const float Lw = nf[3 * PCH + p];
+          const float Mw = nf[4 * PCH + p];
+          const float r0w = nf[5 * PCH + p];
+          // the same lookups with the cells walked from the previous
+          // node's, reciprocal widths and the spline's per-interval b, d
+          const float c = fkc * ratio;
+          hc = walk_cell(cx, nc, c, hc);
+          const int j = hc;
+          const float dyc = (c - cx[j]) * icx[j];
+          const float z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
+          const int jc = bsearch_from(cz, nc, z1, j);
+          const float dy2 = (jc == j) ? dyc : (z1 - cz[jc]) / (cz[jc + 1] - cz[jc]);
+          const float H1 = __fdividef(cH0, cdn[jc] + dy2 * (cup[jc] - cdn[jc]));
+          int jg = jc;
+          float dyg = dy2;
+          if (!same_axis) {
+            hg = walk_cell(gz, ng, z1, hg);
+            jg = hg;
+            dyg = (z1 - gz[jg]) / (gz[jg + 1] - gz[jg]);
+          }
+          const float Gz = gv[jg] + dyg * (gv[jg + 1] - gv[jg]);
+          const float f1 = 1.0f - __fdividef(gs[jg] * (1.0f + z1), Gz);
+          const float zs = (z1 - ldz - lzm) * ilst + lzm;
+          float n1 = 0.0f;
+          if (!(zs <= szc[0] || zs >= szc[nzs - 1])) {
+            hn = walk_cell(szc, nzs, zs, hn);
+            const float t = zs - szc[hn];
+            n1 = (sy[hn] + t * (sbq[hn] + t * (sc[hn] + t * sdq[hn]))) * ilst;
+          }
+          const float s = Lw + Mw * pref + (c0 * r0w - c1 * n1 * H1 * f1);
+          if (sgg) sgg[(size_t)(p0 + p) * Ltot] = s;
+          // the one-loop bK term enters the nonlinear-P integrand only
+          // (cosmo2D.c:2568)
+          const float s2 = s * s * nf[1 * PCH + p];
+          const float s2w = s2 + nf[10 * PCH + p] * lp2f * nf[1 * PCH + p];
+          float uh, ul;
+          split_sub(llf.x, llf.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
+          snl += s2w * pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p], hk);
+          if (mode == 1)
+            sln += s2 * pk_eval_fh(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p], hkl);
         }
-        fkc = nf[0 * PCH + p];
-        Lw = nf[3 * PCH + p];
-        Mw = nf[4 * PCH + p];
-        r0w = nf[5 * PCH + p];
-      } else {
-        if (lp < thr[p]) continue;
-        fkc = (T)(nd[0 * PCH + p] * CL2PT_COVERH0);
-        Lw = (T)nd[3 * PCH + p];
-        Mw = (T)nd[4 * PCH + p];
-        r0w = (T)nd[5 * PCH + p];
-      }
-      if constexpr (F32) {
-        // the same lookups with the cells walked from the previous node's,
-        // reciprocal widths and the spline's per-interval b, d
-        const float c = fkc * ratio;
-        hc = walk_cell(cx, nc, c, hc);
-        const int j = hc;
-        const float dyc = (c - cx[j]) * icx[j];
-        const float z1 = cz[j] + dyc * (cz[j + 1] - cz[j]);
-        const int jc = bsearch_from(cz, nc, z1, j);
-        const float dy2 = (jc == j) ? dyc : (z1 - cz[jc]) / (cz[jc + 1] - cz[jc]);
-        const float H1 = __fdividef(cH0, cdn[jc] + dy2 * (cup[jc] - cdn[jc]));
-        int jg = jc;
-        float dyg = dy2;
-        if (!same_axis) {
-          hg = walk_cell(gz, ng, z1, hg);
-          jg = hg;
-          dyg = (z1 - gz[jg]) / (gz[jg + 1] - gz[jg]);
-        }
-        const float Gz = gv[jg] + dyg * (gv[jg + 1] - gv[jg]);
-        const float f1 = 1.0f - __fdividef(gs[jg] * (1.0f + z1), Gz);
-        const float zs = (z1 - ldz - lzm) * ilst + lzm;
-        float n1 = 0.0f;
-        if (!(zs <= szc[0] || zs >= szc[nzs - 1])) {
-          hn = walk_cell(szc, nzs, zs, hn);
-          const float t = zs - szc[hn];
-          n1 = (sy[hn] + t * (sbq[hn] + t * (sc[hn] + t * sdq[hn]))) * ilst;
-        }
-        const float s = Lw + Mw * pref + (c0 * r0w - c1 * n1 * H1 * f1);
-        if (sgg) sgg[(size_t)(p0 + p) * Ltot] = s;
-        // the one-loop bK term enters the nonlinear-P integrand only
-        // (cosmo2D.c:2568)
-        const float s2 = s * s * nf[1 * PCH + p];
-        const float s2w = s2 + nf[10 * PCH + p] * lp2f * nf[1 * PCH + p];
-        float uh, ul;
-        split_sub(ll.x, ll.y, nf[7 * PCH + p], nf[8 * PCH + p], uh, ul);
-        snl += s2w * pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], nf[2 * PCH + p], hk);
-        if (mode == 1) sln += s2 * pk_eval_fh(axlf, pl.tab2, pl.nz, uh, ul, nj[PCH + p], nf[6 * PCH + p], hkl);
-        continue;
-      }
+      };
+      if (cut_idx) walk(std::true_type{});
+      else walk(std::false_type{});
+    }
+    for (int p = 0; p < np && !F32; p++) {
+      if (lp < thr[p]) continue;
+      const T fkc = (T)(nd[0 * PCH + p] * CL2PT_COVERH0);
+      const T Lw = (T)nd[3 * PCH + p];
+      const T Mw = (T)nd[4 * PCH + p];
+      const T r0w = (T)nd[5 * PCH + p];
       // a_chi at chi1 (cosmo3D.c:109-133)
       const T c = fkc * ratio;
       const int j = bsearch_t(cx, nc, c);
@@ -994,6 +1122,22 @@ __global__ void __launch_bounds__(LTG) k_limber_gg(Params P, const double* __res
     if constexpr (F32) {
       sum_nl += (double)snl;
       sum_lin += (double)sln;
+    }
+  }
+  if constexpr (NH == 2) {
+    // the second half's sums onto the first's, through the node-data space
+    // (9 PCH doubles >= 2 lt)
+    double* red2 = (double*)smem_raw;
+    __syncthreads();
+    if (half == 1 && valid) {
+      red2[tid - lt] = sum_nl;
+      red2[lt + tid - lt] = sum_lin;
+    }
+    __syncthreads();
+    if (half == 1) return;
+    if (valid) {
+      sum_nl += red2[tid];
+      sum_lin += red2[lt + tid];
     }
   }
   if (!valid) return;
@@ -1054,20 +1198,25 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
   }
   if (P.probes & CL2PT_PROBE_WTHETA) {
     const size_t sm = gg_smem<T>(P, 0), sm1 = gg_smem<T>(P, 1);
-    cudaFuncSetAttribute(k_limber_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(sm, sm1));
+    cudaFuncSetAttribute(k_limber_gg<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(sm, sm1));
+    if constexpr (sizeof(T) == sizeof(float))
+      cudaFuncSetAttribute(k_limber_gg<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
     if (sizeof(T) == sizeof(float)) {
       k_gg_nodes<<<dim3(P.B, P.nl), 128, 0, s>>>(P, ell_g);
       (*launches)++;
     }
     dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
-    k_limber_gg<T><<<g, LTG, sm, s>>>(P, ell_g, 0);
+    k_limber_gg<T, 1><<<g, LTG, sm, s>>>(P, ell_g, 0);
     hk(CL2PT_K_LIMBER_GG, 0);
     (*launches)++;
     if (!P.adopt_limber_gg) {
-      dim3 g2(P.B, (P.lmax_nolimber + LTG - 1) / LTG, P.nl);
+      // mixed plan: two threads per multipole (k_limber_gg's halves)
+      const int lt1 = f32 ? std::min(LTG, (P.lmax_nolimber + 31) / 32 * 32) : LTG;
+      dim3 g2(P.B, (P.lmax_nolimber + lt1 - 1) / lt1, P.nl);
       hk(CL2PT_K_LIMBER_GGL, 1);
-      k_limber_gg<T><<<g2, LTG, sm1, s>>>(P, ell_g, 1);
+      if constexpr (sizeof(T) == sizeof(float)) k_limber_gg<T, 2><<<g2, 2 * lt1, sm1, s>>>(P, ell_g, 1);
+      else k_limber_gg<T, 1><<<g2, LTG, sm1, s>>>(P, ell_g, 1);
       hk(CL2PT_K_LIMBER_GGL, 0);
       (*launches)++;
     }

@@ -25,14 +25,16 @@
 
 namespace cl2pt {
 
+// FP64 complex arithmetic, on the device and (for the plan's tables) the host
+#define NL_HD __host__ __device__ __forceinline__
 struct cd { double x, y; };
-__device__ __forceinline__ cd cmk(double a, double b) { cd r; r.x = a; r.y = b; return r; }
-__device__ __forceinline__ cd cadd(cd a, cd b) { return cmk(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ cd csub(cd a, cd b) { return cmk(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ cd cmul(cd a, cd b) { return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ cd cscale(cd a, double s) { return cmk(a.x * s, a.y * s); }
-__device__ __forceinline__ cd cconj(cd a) { return cmk(a.x, -a.y); }
-__device__ __forceinline__ cd cdivc(cd a, cd b)
+NL_HD cd cmk(double a, double b) { cd r; r.x = a; r.y = b; return r; }
+NL_HD cd cadd(cd a, cd b) { return cmk(a.x + b.x, a.y + b.y); }
+NL_HD cd csub(cd a, cd b) { return cmk(a.x - b.x, a.y - b.y); }
+NL_HD cd cmul(cd a, cd b) { return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+NL_HD cd cscale(cd a, double s) { return cmk(a.x * s, a.y * s); }
+NL_HD cd cconj(cd a) { return cmk(a.x, -a.y); }
+NL_HD cd cdivc(cd a, cd b)
 {
   // Smith's algorithm
   if (fabs(b.x) >= fabs(b.y)) {
@@ -42,34 +44,52 @@ __device__ __forceinline__ cd cdivc(cd a, cd b)
   const double r = b.x / b.y, d = b.x * r + b.y;
   return cmk((a.x * r + a.y) / d, (a.y * r - a.x) / d);
 }
-__device__ __forceinline__ cd clog_(cd a) { return cmk(log(hypot(a.x, a.y)), atan2(a.y, a.x)); }
-__device__ __forceinline__ cd cexp_(cd a)
+NL_HD void sincos_hd(double a, double* s, double* c)
+{
+#ifdef __CUDA_ARCH__
+  sincos(a, s, c);
+#else
+  *s = sin(a);
+  *c = cos(a);
+#endif
+}
+NL_HD cd clog_(cd a) { return cmk(log(hypot(a.x, a.y)), atan2(a.y, a.x)); }
+NL_HD cd cexp_(cd a)
 {
   const double m = exp(a.x);
   double s, c;
-  sincos(a.y, &s, &c);
+  sincos_hd(a.y, &s, &c);
   return cmk(m * c, m * s);
 }
-__device__ __forceinline__ cd csin_(cd a)
+NL_HD cd csin_(cd a)
 {
   double s, c;
-  sincos(a.x, &s, &c);
+  sincos_hd(a.x, &s, &c);
   return cmk(s * cosh(a.y), c * sinh(a.y));
 }
 
-__constant__ double c_lanczos[9] = {
-    0.99999999999980993227684700473478, 676.520368121885098567009190444019,
-    -1259.13921672240287047156078755283, 771.3234287776530788486528258894,
-    -176.61502916214059906584551354, 12.507343278686904814458936853,
-    -0.13857109526572011689554707, 9.984369578019570859563e-6,
-    1.50563273514931155834e-7};
+// coefficients of the Lanczos sum, g = 7, n = 9 (the reference's ln Gamma)
+NL_HD double lanczos_c(int w)
+{
+  switch (w) {
+    case 0: return 0.99999999999980993227684700473478;
+    case 1: return 676.520368121885098567009190444019;
+    case 2: return -1259.13921672240287047156078755283;
+    case 3: return 771.3234287776530788486528258894;
+    case 4: return -176.61502916214059906584551354;
+    case 5: return 12.507343278686904814458936853;
+    case 6: return -0.13857109526572011689554707;
+    case 7: return 9.984369578019570859563e-6;
+    default: return 1.50563273514931155834e-7;
+  }
+}
 
 // ln Gamma(a) for Re a >= 1/2, |a| >= 10: Stirling's series
 // (Abramowitz & Stegun 6.1.40-41) to the B_16 term, remainder below 1e-17
 // relative there; ~1/3 of the FP64 work of the Lanczos sum (one complex
 // reciprocal instead of eight complex divisions, one complex log).
 // Exponentiated only, so its branch of the imaginary part is immaterial.
-__device__ cd lngamma_stirling(cd a)
+NL_HD cd lngamma_stirling(cd a)
 {
   const cd r = cdivc(cmk(1.0, 0.0), a);
   const cd r2 = cmul(r, r);
@@ -90,18 +110,19 @@ __device__ cd lngamma_stirling(cd a)
 
 // ln Gamma(1 + m) for Re m >= -1/2 (Lanczos g = 7, the reference's sum;
 // Stirling's series for |1 + m| >= 10)
-__device__ cd lngamma_1p(cd m)
+NL_HD cd lngamma_1p(cd m)
 {
   if (hypot(m.x + 1.0, m.y) >= 10.0) return lngamma_stirling(cmk(m.x + 1.0, m.y));
   const double ln2pio2 = 0.5 * log(2 * M_PI);
-  cd tmp = cmk(c_lanczos[0], 0.0);
-  for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(c_lanczos[w], 0.0), cmk(m.x + w, m.y)));
+  cd tmp = cmk(lanczos_c(0), 0.0);
+#pragma unroll
+  for (int w = 1; w < 9; w++) tmp = cadd(tmp, cdivc(cmk(lanczos_c(w), 0.0), cmk(m.x + w, m.y)));
   const cd t = cmk(m.x + 7.5, m.y);
   return cadd(csub(cadd(cmk(ln2pio2, 0.0), cmul(cmk(m.x + 0.5, m.y), clog_(t))), t), clog_(tmp));
 }
 
 // ln Gamma(a) with reflection for Re a < 1/2 (cosmo2D.c:4273-4294)
-__device__ cd lngamma_refl(cd a)
+NL_HD cd lngamma_refl(cd a)
 {
   if (a.x < 0.5) {
     // ln pi - ln sin(pi a) - ln Gamma(1 - a)
@@ -147,52 +168,6 @@ constexpr int NL_NT = 256;
 // 128-thread CTAs, four per SM, keep more independent work in flight when
 // four fit the SM's shared memory; 256 otherwise (two per SM)
 static int nl_loop_threads(size_t smem) { return smem + 1024 <= 228 * 1024 / 4 ? 128 : 256; }
-
-// One Stockham transform of size N (factors fac[0..nf-1]) on in/out
-// (shared), twiddles tw[k] = exp(+2 pi i k / N); sign -1 = forward.
-// Returns the buffer holding the result.
-__device__ cd* block_fft(cd* in, cd* out, int N, const int* fac, int nf, const cd* __restrict__ tw,
-                         int sign)
-{
-  int Ns = 1;
-  for (int s = 0; s < nf; s++) {
-    const int R = fac[s];
-    const int NR = N / R;
-    const int tstep = N / (Ns * R);
-    for (int j = threadIdx.x; j < NR; j += NL_NT) {
-      const int k = j % Ns;
-      cd v[7];
-      for (int r = 0; r < R; r++) {
-        cd x = in[j + r * NR];
-        if (r && k) {
-          cd w = tw[(r * k * tstep) % N];
-          if (sign < 0) w.y = -w.y;
-          x = cmul(x, w);
-        }
-        v[r] = x;
-      }
-      // radix-R DFT with roots tw[m N / R]
-      cd o[7];
-      for (int t = 0; t < R; t++) {
-        cd acc = v[0];
-        for (int r = 1; r < R; r++) {
-          cd w = tw[((r * t) % R) * NR];
-          if (sign < 0) w.y = -w.y;
-          acc = cadd(acc, cmul(v[r], w));
-        }
-        o[t] = acc;
-      }
-      const int dst = (j / Ns) * Ns * R + k;
-      for (int r = 0; r < R; r++) out[dst + r * Ns] = o[r];
-    }
-    __syncthreads();
-    cd* t = in;
-    in = out;
-    out = t;
-    Ns *= R;
-  }
-  return in;
-}
 
 __device__ double block_sum(double v, double* sh)
 {
@@ -279,11 +254,11 @@ __device__ __forceinline__ void dft4(ct<T>* v, int sign)
 // registers): out[(j/Ns) Ns R + k + r Ns] = DFT_R over r of
 // in[j + r N/R] w^(r k tstep), k = j mod Ns.
 template <typename T, int R>
-__device__ __forceinline__ void stockham_stage(const ct<T>* __restrict__ in, ct<T>* __restrict__ out, int N,
-                                               int Ns, const ct<T>* __restrict__ tw, int sign)
+__device__ __forceinline__ void stockham_stage(const ct<T>* __restrict__ in, ct<T>* __restrict__ out,
+                                               const NLStage& S, const ct<T>* __restrict__ tw, int sign)
 {
-  const int NR = N / R;
-  const int tstep = N / (Ns * R);
+  const int NR = S.NR, Ns = S.Ns;
+  const int tstep = S.ts;
   ct<T> w[R];
 #pragma unroll
   for (int m = 0; m < R; m++) {
@@ -292,7 +267,8 @@ __device__ __forceinline__ void stockham_stage(const ct<T>* __restrict__ in, ct<
     w[m] = x;
   }
   for (int j = threadIdx.x; j < NR; j += blockDim.x) {
-    const int k = j % Ns;
+    const int g = (int)((__umulhi((unsigned)j, S.m) + (unsigned)j) >> S.l);  // j / Ns
+    const int k = j - g * Ns;
     ct<T> v[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -307,34 +283,32 @@ __device__ __forceinline__ void stockham_stage(const ct<T>* __restrict__ in, ct<
     if constexpr (R == 2) dft2(v);
     else if constexpr (R == 4) dft4(v, sign);
     else dft_small<T, R>(v, w);
-    const int dst = (j / Ns) * Ns * R + k;
+    const int dst = g * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; r++) out[dst + r * Ns] = v[r];
   }
 }
 
-// Stockham transform of size N in the loop precision over the factors
-// fac[0..nf-1] (4, 2, 3, 5, 7), ping-ponging in/out; returns the buffer
-// holding the result.
+// Stockham transform in the loop precision over the stages st[0..nf-1]
+// (radices 4, 2, 3, 5, 7), ping-ponging in/out; returns the buffer holding
+// the result.
 template <typename T>
-__device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, int N, const int* fac, int nf,
-                              const ct<T>* __restrict__ tw, int sign)
+__device__ ct<T>* block_fft_t(ct<T>* in, ct<T>* out, const NLStage* st, int nf, const ct<T>* __restrict__ tw,
+                              int sign)
 {
-  int Ns = 1;
   for (int s = 0; s < nf; s++) {
-    const int R = fac[s];
-    switch (R) {
-      case 2: stockham_stage<T, 2>(in, out, N, Ns, tw, sign); break;
-      case 3: stockham_stage<T, 3>(in, out, N, Ns, tw, sign); break;
-      case 4: stockham_stage<T, 4>(in, out, N, Ns, tw, sign); break;
-      case 5: stockham_stage<T, 5>(in, out, N, Ns, tw, sign); break;
-      default: stockham_stage<T, 7>(in, out, N, Ns, tw, sign); break;
+    const NLStage& S = st[s];
+    switch (S.R) {
+      case 2: stockham_stage<T, 2>(in, out, S, tw, sign); break;
+      case 3: stockham_stage<T, 3>(in, out, S, tw, sign); break;
+      case 4: stockham_stage<T, 4>(in, out, S, tw, sign); break;
+      case 5: stockham_stage<T, 5>(in, out, S, tw, sign); break;
+      default: stockham_stage<T, 7>(in, out, S, tw, sign); break;
     }
     __syncthreads();
     ct<T>* t = in;
     in = out;
     out = t;
-    Ns *= R;
   }
   return in;
 }
@@ -357,10 +331,11 @@ __device__ __forceinline__ NLGeom nl_geom(const Params& P, int pt)
   return g;
 }
 
-// ---- 1. forward transforms (cfftlog_ells_p1, cosmo2D.c:4047-4130), FP64:
-// one CTA per (point, lens bin) for the radial kernels j in [j0, j1): the
+// ---- 1. forward transforms (cfftlog_ells_p1, cosmo2D.c:4047-4130): one
+// CTA per (point, lens bin) for the radial kernels j in [j0, j1): the
 // per-sample factors (a(chi), H, D, n_lens, f, b1) are formed once into
-// shared memory, then each kernel is filled, transformed and windowed.
+// shared memory in FP64, then each kernel is filled, transformed and
+// windowed (FP64; FP32 in the mixed plan, whose spectra are FP32).
 // unit_b1: the galaxy kernel with b1 = 1 (the adjoint pass differentiates
 // the linear-bias factor out of it; bias model 0 only).
 template <typename T>
@@ -426,22 +401,48 @@ __global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int 
     }
     // divided by x^nu_j = exp(nu_j ln x), ln x = ln x0 + m dlnchi
     const double lnx = lnx0 + geo.dlnchi * m;
-    fx[m] = f0 / exp(Q.nu[0] * lnx);
-    fx[nchi + m] = f1 / exp(Q.nu[1] * lnx);
-    fx[2 * nchi + m] = f2 / exp(Q.nu[2] * lnx);
+    fx[m] = (f0 != 0.0) ? f0 / exp(Q.nu[0] * lnx) : 0.0;
+    fx[nchi + m] = (f1 != 0.0) ? f1 / exp(Q.nu[1] * lnx) : 0.0;
+    fx[2 * nchi + m] = (f2 != 0.0) ? f2 / exp(Q.nu[2] * lnx) : 0.0;
   }
   for (int j = j0; j < j1; j++) {
     const int N = Q.N[j];
+    const int halfN = N / 2;
+    const int kmax = (int)(halfN * 0.25);
+    ct<T>* tout = (ct<T>*)Q.tout + ((size_t)pt * P.nl + q) * Q.tout_stride;
     __syncthreads();
+    if constexpr (sizeof(T) == sizeof(float)) {
+      // mixed plan: the transform and the window in FP32 (the spectra are
+      // stored in FP32 and the multipole loop transforms in FP32), in the
+      // FP64 buffer's space
+      ct<float>* fa = (ct<float>*)bufA;
+      ct<float>* fb = fa + Q.nmax;
+      for (int i = tid; i < N; i += NL_NT) {
+        const int qq = i - Q.pad[j];
+        fa[i] = tmk<float>((qq >= 0 && qq < nchi) ? (float)fx[j * nchi + qq] : 0.0f, 0.0f);
+      }
+      __syncthreads();
+      const ct<float>* r = block_fft_t<float>(fa, fb, Q.st[j], Q.nfac[j], (const ct<float>*)Q.twt[j], -1);
+      const float ikmax = 1.0f / (float)kmax;
+      for (int i = tid; i <= halfN; i += NL_NT) {
+        ct<float> v = r[i];
+        const int k = halfN - i;  // window on the right side
+        if (k <= kmax) {
+          const float x = (float)k * ikmax;
+          const float W = x - sinf(6.28318530717958647692f * x) * 0.159154943091895335769f;
+          v = tmk<float>(v.x * W, v.y * W);
+        }
+        tout[j * Q.hstride + i] = tmk<T>(v.x, v.y);
+      }
+      continue;
+    }
     for (int i = tid; i < N; i += NL_NT) {
       const int qq = i - Q.pad[j];
       bufA[i] = cmk((qq >= 0 && qq < nchi) ? fx[j * nchi + qq] : 0.0, 0.0);
     }
     __syncthreads();
-    cd* r = block_fft(bufA, bufB, N, Q.fac[j], Q.nfac[j], (const cd*)Q.tw[j], -1);
-    const int halfN = N / 2;
-    const int kmax = (int)(halfN * 0.25);
-    ct<T>* tout = (ct<T>*)Q.tout + ((size_t)pt * P.nl + q) * Q.tout_stride;
+    const cd* r = (const cd*)block_fft_t<double>((ct<double>*)bufA, (ct<double>*)bufB, Q.st[j], Q.nfac[j],
+                                                 (const ct<double>*)Q.tw[j], -1);
     for (int i = tid; i <= halfN; i += NL_NT) {
       cd v = r[i];
       const int k = halfN - i;  // window on the right side
@@ -454,10 +455,86 @@ __global__ void __launch_bounds__(NL_NT) k_nl_forward(Params P, NLParams Q, int 
   }
 }
 
-// ---- 2. Gamma-ratio kernels evaluated directly (Lanczos, FP64) at the
-// multipoles where the recurrence (re)starts: l = 0, 1 in the mixed plan;
-// the first two multipoles of every 16-block in the FP64 plan, as the
-// reference does.  One CTA per (point, radial kernel, start multipole).
+// Gamma part of g_l for the mixed plan's table (NLParams::gtab):
+// T(eta) = (z - d) ln 2 + ln Gamma(w + 1) - ln Gamma(v), z = nu + i eta,
+// w = (l + z - d) / 2, v = (3 + d + l - z) / 2, d the derivative order, so
+// that g_l = exp(T) poly_d(z) / w with poly_0 = 1, poly_1 = -(z - 1),
+// poly_2 = (z - 1)(z - 2) -- the factors with zeros or poles near eta = 0
+// stay outside the interpolated part.
+NL_HD cd gl_gamma_part(int deriv, double nu, double eta, int l)
+{
+  const cd w1 = cmk(0.5 * (l + nu - deriv) + 1.0, 0.5 * eta);
+  const cd v = cmk(0.5 * (3 + deriv + l - nu), -0.5 * eta);
+  return csub(cadd(cscale(cmk(nu - deriv, eta), log(2.)), lngamma_refl(w1)), lngamma_refl(v));
+}
+
+void nl_gamma_tables(const NLParams& Q, double inv_h, int m, std::vector<double>& out)
+{
+  out.assign((size_t)3 * 2 * m * 2, 0.0);
+  for (int j = 0; j < 3; j++)
+    for (int l = 0; l < 2; l++) {
+      double* o = out.data() + (size_t)(j * 2 + l) * m * 2;
+      double prev = 0.0;
+      for (int i = 0; i < m; i++) {
+        const cd t = gl_gamma_part(Q.deriv[j], Q.nu[j], (i - 3) / inv_h, l);
+        double im = t.y;
+        // continuous imaginary part (steps of ~0.2 rad between entries)
+        if (i) im += 2 * M_PI * nearbyint((prev - im) / (2 * M_PI));
+        o[2 * i] = t.x;
+        o[2 * i + 1] = im;
+        prev = im;
+      }
+    }
+}
+
+// g_l at eta from the table tb = NLParams::gtab + (j, l): 6-point Lagrange
+// interpolation of T in FP64, then exp(T) and the rational factor in FP32
+// (the loop consumes g in FP32).  nu1 = nu - 1 in FP32.  false: eta beyond
+// the table.
+__device__ __forceinline__ bool gl_table(const NLParams& Q, const double* __restrict__ tb, int deriv, float nu1,
+                                         int l, double eta, ct<float>* g)
+{
+  const double u = eta * Q.gtab_inv_h + 3.0;
+  const int m = (int)u;
+  if (m < 2 || m + 3 >= Q.gtab_m) return false;
+  const double t = u - (double)m;
+  const double e0 = t + 2.0, e1 = t + 1.0, e2 = t, e3 = t - 1.0, e4 = t - 2.0, e5 = t - 3.0;
+  const double p01 = e0 * e1, p23 = e2 * e3, p45 = e4 * e5;
+  // w_a = prod_{b != a} (t - b) / prod_{b != a} (a - b), nodes a = -2..3
+  const double w[6] = {e1 * p23 * p45 * (-1.0 / 120.0), e0 * p23 * p45 * (1.0 / 24.0),
+                       p01 * e3 * p45 * (-1.0 / 12.0),  p01 * e2 * p45 * (1.0 / 12.0),
+                       p01 * p23 * e5 * (-1.0 / 24.0),  p01 * p23 * e4 * (1.0 / 120.0)};
+  const double2* r = (const double2*)tb + (m - 2);
+  double re = 0.0, im = 0.0;
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    const double2 v = __ldg(r + a);
+    re = fma(w[a], v.x, re);
+    im = fma(w[a], v.y, im);
+  }
+  const double ph = im - 2.0 * M_PI * rint(im * (0.5 / M_PI));
+  float sn, cs;
+  sincosf((float)ph, &sn, &cs);
+  const float mag = expf((float)re);
+  const float et = (float)eta;
+  ct<float> poly;
+  if (deriv == 0) poly = tmk<float>(1.0f, 0.0f);
+  else if (deriv == 1) poly = tmk<float>(-nu1, -et);
+  else poly = tmk<float>(nu1 * (nu1 - 1.0f) - et * et, et * (2.0f * nu1 - 1.0f));
+  // poly / w, w = (l + 1 + nu1 - d + i eta) / 2
+  const float wr = 0.5f * ((float)(l + 1 - deriv) + nu1), wi = 0.5f * et;
+  const float rw = 1.0f / (wr * wr + wi * wi);
+  const ct<float> fac = tmk<float>((poly.x * wr + poly.y * wi) * rw, (poly.y * wr - poly.x * wi) * rw);
+  *g = tmul(tmk<float>(mag * cs, mag * sn), fac);
+  return true;
+}
+
+// ---- 2. Gamma-ratio kernels at the multipoles where the recurrence
+// (re)starts: l = 0, 1 in the mixed plan, from the plan's tables of their
+// Gamma part (gl_table; entries beyond the tables directly); the first two
+// multipoles of every 16-block in the FP64 plan, as the reference does,
+// evaluated directly (Lanczos, FP64).  One CTA per (point, radial kernel,
+// start multipole).
 __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
 {
   const int pt = blockIdx.x, j = blockIdx.y, d = blockIdx.z;
@@ -474,7 +551,14 @@ __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
   const int nq = N / 2 + 1;
   const double deta = 2.0 * M_PI / (geo.dlnx * N);
   double* out = Q.gdir + (((size_t)pt * 3 + j) * Q.ndirect + d) * Q.hstride * 2;
+  const double* tb = (Q.gtab && k < 2) ? Q.gtab + (size_t)(j * 2 + k) * Q.gtab_m * 2 : nullptr;
   for (int i = threadIdx.x; i < nq; i += NL_NT) {
+    ct<float> gf;
+    if (tb && gl_table(Q, tb, Q.deriv[j], Q.nu1f[j], k, deta * i, &gf)) {
+      out[2 * i] = f32_to_f64_int(gf.x);
+      out[2 * i + 1] = f32_to_f64_int(gf.y);
+      continue;
+    }
     const cd g = gl_direct(Q.deriv[j], Q.nu[j], deta * i, k);
     out[2 * i] = g.x;
     out[2 * i + 1] = g.y;
@@ -489,7 +573,7 @@ __global__ void __launch_bounds__(NL_NT) k_nl_gdirect(Params P, NLParams Q)
 // formed on the fly from ln x.
 template <typename T>
 __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int slot, bool direct,
-                                     const double* gd, int i, int k, double deta, float dh, float dl)
+                                     const double* gd, int i, float fi, int k, double deta, float dh, float dl)
 {
   ct<T> g;
   if (direct) {
@@ -497,17 +581,31 @@ __device__ __forceinline__ ct<T> nl_g(const NLParams& Q, int j, ct<T>* gs, int s
   } else {
     T et;
     if constexpr (sizeof(T) == sizeof(float)) {
-      // eta = deta i from a two-float split (dh, dl) of deta
-      et = fmaf(dh, (float)i, dl * (float)i);
+      // eta = deta i from a two-float split (dh, dl) of deta; fi = i as a
+      // float, counted by the caller (no conversion per entry)
+      et = fmaf(dh, fi, dl * fi);
     } else {
       et = deta * i;
     }
-    const T kk = (T)k, nuj = (T)Q.nu[j];
+    const T kk = (T)k;
+    T nuj;
+    if constexpr (sizeof(T) == sizeof(float)) nuj = Q.nuf[j];  // no FP64 conversion per entry
+    else nuj = Q.nu[j];
     ct<T> num, den;
     if (Q.deriv[j] == 0) { num = tmk<T>(kk - 2 + nuj, et); den = tmk<T>(kk + 1 - nuj, -et); }
     else if (Q.deriv[j] == 1) { num = tmk<T>(kk - 3 + nuj, et); den = tmk<T>(kk + 2 - nuj, -et); }
     else { num = tmk<T>(kk - 4 + nuj, et); den = tmk<T>(kk + 3 - nuj, -et); }
-    g = tmul(gs[slot * Q.hstride + i], tdiv(num, den));
+    ct<T> ratio;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      // num / den = num conj(den) / |den|^2: one reciprocal instead of
+      // Smith's two divisions (|den| >= k + 1 - nu >= 2 at the recurrence's
+      // multipoles k >= 2; |den|^2 stays far inside the FP32 range)
+      const float r = __frcp_rn(fmaf(den.x, den.x, den.y * den.y));
+      ratio = tmk<T>((num.x * den.x + num.y * den.y) * r, (num.y * den.x - num.x * den.y) * r);
+    } else {
+      ratio = tdiv(num, den);
+    }
+    g = tmul(gs[slot * Q.hstride + i], ratio);
   }
   gs[slot * Q.hstride + i] = g;
   return g;
@@ -555,11 +653,21 @@ __global__ void __launch_bounds__(1024) k_nl_order(Params P, NLParams Q)
   for (int i = threadIdx.x; i < n; i += blockDim.x) Q.perm[atomicAdd(&off[bucket(i)], 1)] = i;
 }
 
-// The z = 0 slice P_lin(k_i, z = 0) of each point's linear table
-// (p_lin(k, 1), cosmo3D.c:306-358, linear in z between the table's two
-// columns around z = 0), once per point into a contiguous row: the table
-// is k-major, so the column is a strided gather that every lens-bin CTA of
-// the loop would otherwise repeat.
+// FP32 head/tail of an angle reduced to [-pi, pi] in FP64
+__device__ __forceinline__ float2 red_angle(double a)
+{
+  a -= 2.0 * M_PI * rint(a * (0.5 / M_PI));
+  const float h = (float)a;
+  return make_float2(h, (float)(a - (double)h));
+}
+
+// Per point, what every lens-bin CTA of the loop would otherwise repeat:
+// the z = 0 slice P_lin(k_i, z = 0) of the linear table (p_lin(k, 1),
+// cosmo3D.c:306-358, linear in z between the table's two columns around
+// z = 0) as a contiguous row (the table is k-major, so the column is a
+// strided gather), and in the mixed plan the phase increments of every
+// (radial kernel, multipole) (NLParams::phase) -- FP64 work that one
+// thread of each loop CTA used to do while the others waited.
 __global__ void k_nl_slice(Params P, NLParams Q)
 {
   const int pt = blockIdx.x;
@@ -569,26 +677,28 @@ __global__ void k_nl_slice(Params P, NLParams Q)
   double* out = Q.pslice + (size_t)pt * P.pkl_nk;
   for (int i = threadIdx.x; i < P.pkl_nk; i += blockDim.x)
     out[i] = (1 - dy) * tabL[(size_t)i * P.pkl_nz + j0] + dy * tabL[(size_t)i * P.pkl_nz + j0 + 1];
+  if (!Q.phase) return;
+  const NLGeom geo = nl_geom(P, pt);
+  const double lnx0last = log(geo.x0 / geo.xlast);
+  const int LNL = P.lmax_nolimber;
+  for (int e = threadIdx.x; e < 3 * LNL; e += blockDim.x) {
+    const int j = e / LNL, k = e - j * LNL;
+    const double deta = 2.0 * M_PI / (geo.dlnx * Q.N[j]);
+    const double lnbj = lnx0last - 2 * Q.pad[j] * geo.dlnx;
+    Q.phase[((size_t)pt * 3 + j) * LNL + k] = red_angle(deta * (lnbj + Q.lnk1[k]));
+  }
 }
 
-// FP32 head/tail of an angle reduced to [-pi, pi] in FP64
-__device__ __forceinline__ float2 red_angle(double a)
-{
-  a -= 2.0 * M_PI * rint(a * (0.5 / M_PI));
-  const float h = (float)a;
-  return make_float2(h, (float)(a - (double)h));
-}
-
-// exp(-i m theta) for theta = th.x + th.y in [-pi, pi] and 0 <= m < 2^15,
+// exp(-i m theta) for theta = th.x + th.y in [-pi, pi] and integer m = fm
+// in [0, 2^15),
 // without FP64: m theta as an exact two-float product, reduced by 2 pi in
 // three parts (Cody-Waite; m th.x / 2 pi < 2^14, so n C1 and p - n C1 are
 // exact), then sincosf of the reduced angle (~2e-7 rad from the exact one)
-__device__ __forceinline__ ct<float> phase_f(int m, float2 th)
+__device__ __forceinline__ ct<float> phase_f(float fm, float2 th)
 {
   constexpr float C1 = 6.28125f;
   constexpr float C2 = (float)(6.283185307179586476925 - 6.28125);
   constexpr float C3 = (float)(6.283185307179586476925 - 6.28125 - (double)C2);
-  const float fm = (float)m;
   const float p = fm * th.x;
   const float e = fmaf(fm, th.x, -p);
   const float n = rintf(p * 0.159154943091895335769f);
@@ -599,6 +709,24 @@ __device__ __forceinline__ ct<float> phase_f(int m, float2 th)
   float sn, cs;
   sincosf(r, &sn, &cs);
   return tmk<float>(cs, -sn);
+}
+
+// Cell of the z = 0 slice's FP32 log10 k axis (the bracketing search's
+// answer: largest i <= nk - 2 with plk[i] <= v, else 0) from a table of
+// the cells at NL_LUT(nk) equally spaced values, walked up or down to the
+// exact cell -- a step or two on the usual log-spaced axes instead of the
+// ~10 dependent steps of the search.  scale = (NL_LUT - 1) / (plk[nk-1] -
+// plk[0]); the rounding to the nearest table entry is integer arithmetic
+// (0 <= u < 2^22), not a conversion.
+__host__ __device__ constexpr int nl_lut_size(int nk) { return 2 * nk; }
+__device__ __forceinline__ int slice_cell(const float* __restrict__ plk, int nk, const unsigned short* lut,
+                                          float scale, float umax, float v)
+{
+  const float u = fminf(fmaxf((v - plk[0]) * scale, 0.0f), umax);
+  int lo = lut[__float_as_int(u + 12582912.0f) - 0x4B400000];
+  while (lo < nk - 2 && plk[lo + 1] <= v) lo++;
+  while (lo > 0 && plk[lo] > v) lo--;
+  return lo;
 }
 
 // ADJ: the adjoint of the FFTLog part (see section 4 below) on the same
@@ -615,6 +743,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   const int item = Q.perm[blockIdx.y * gridDim.x + blockIdx.x];
   const int pt = item / P.nl, q = item - (item / P.nl) * P.nl;
   const int tid = threadIdx.x, nlt = blockDim.x;  // 128 or 256 (nl_loop_threads)
+  const float ftid = (float)tid, fnlt = (float)nlt;
   const int nchi = P.nl_nchi;
   const int LNL = P.lmax_nolimber;
   const cl2pt_nuisance& nu = P.nu[pt];
@@ -643,6 +772,9 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
   float* psf = pcf + 3 * P.pkl_nk;  // slope of the slice per cell
   float* pbarf = psf + P.pkl_nk;
+  // mixed plan: (rc / x_i)^3 and the slice-cell table (nl_slice_lut)
+  float* rx3f = pbarf + P.pkl_nk;
+  unsigned short* lut = (unsigned short*)(rx3f + nchi);
   double* psl = F32 ? (double*)fb : (double*)(plk + P.pkl_nk);
   double* plkd = psl + P.pkl_nk;
   double* pinv = plkd + P.pkl_nk;
@@ -694,6 +826,26 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   }
   const double lrc = log10(rc / CL2PT_COVERH0);
   const T rct = (T)rc;
+  const int nlut = nl_lut_size(P.pkl_nk);
+  float lscale = 0.0f, lumax = 0.0f;
+  if constexpr (F32) {
+    __syncthreads();  // plk and xs
+    lscale = (float)(nlut - 1) / (plk[P.pkl_nk - 1] - plk[0]);
+    lumax = (float)(nlut - 1);
+    for (int b = tid; b < nlut; b += nlt) {
+      const float v = plk[0] + (float)b / lscale;
+      int lo = 0, hi = P.pkl_nk - 1;
+      while (hi > lo + 1) {
+        const int mid = (lo + hi) >> 1;
+        if (plk[mid] > v) hi = mid; else lo = mid;
+      }
+      lut[b] = (unsigned short)lo;
+    }
+    for (int i = tid; i < nchi; i += nlt) {
+      const float rx = rct / xs[i];
+      rx3f[i] = rx * rx * rx;
+    }
+  }
   const bool exact_blocks = Q.direct_every != 0;
   const double* gdir = Q.gdir + ((size_t)pt * 3) * Q.ndirect * Q.hstride * 2;
   const double lnx0last = log(geo.x0 / geo.xlast);
@@ -704,9 +856,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
     dh_j[j] = (float)deta_j[j];
     dl_j[j] = (float)(deta_j[j] - (double)dh_j[j]);
   }
-  // mixed plan: phase increments and step phasors of the current pair, and
   // the convergence flag, shared by thread 0
-  __shared__ float2 sph[4];
   __shared__ int sdone;
   const T bmagt = (T)bmag;
   int LM = LNL, done = 0;
@@ -724,33 +874,25 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
     for (int k = ks; k < ke; k += 2) {
       const int k2 = k + 1;
       const bool two = k2 < ke;
+      // bmag l(l+1)/(l+1)^2 = bmag l/(l+1), and with bmag = 1 (adjoint)
+      const T un0 = (T)k / (T)(k + 1), un1 = (T)k2 / (T)(k2 + 1);
+      const T mag0 = bmagt * (T)k / (T)(k + 1);
+      const T mag1 = bmagt * (T)k2 / (T)(k2 + 1);
       __syncthreads();
       for (int i = tid; i < nchi; i += nlt) F0[i] = F1[i] = (T)0;
       for (int j = 0; j < nj; j++) {
         const int N = Q.N[j];
         const int nq = N / 2 + 1;
         // ln(base y0) = ln(x0 / xlast) - 2 pad dlnx + ln(k+1): per-CTA and
-        // per-multipole parts, no transcendental per thread
-        const double lnbj = lnx0last - 2 * Q.pad[j] * dlnx;
+        // per-multipole parts, no transcendental per thread (FP64 plan)
         const double deta = deta_j[j];
         double lnb0 = 0.0, lnb1 = 0.0;
-        if constexpr (F32) {
-          // one thread reduces the two phase increments theta = deta lnbase
-          // and forms the blockDim-entry step phasors (FP64), shared below
-          if (tid == 0) {
-            const double t0 = deta * (lnbj + Q.lnk1[k]), t1 = deta * (lnbj + Q.lnk1[two ? k2 : k]);
-            sph[0] = red_angle(t0);
-            sph[1] = red_angle(t1);
-            const ct<T> a0 = phasor<T>(-(double)nlt * t0), a1 = phasor<T>(-(double)nlt * t1);
-            sph[2] = make_float2(a0.x, a0.y);
-            sph[3] = make_float2(a1.x, a1.y);
-          }
-        } else {
+        if constexpr (!F32) {
+          const double lnbj = lnx0last - 2 * Q.pad[j] * dlnx;
           lnb0 = lnbj + Q.lnk1[k];
           lnb1 = lnbj + Q.lnk1[two ? k2 : k];
         }
         const float dhf = dh_j[j], dlf = dl_j[j];
-        __syncthreads();
         ct<T>* gs = gst + (size_t)j * 2 * Q.hstride;
         const bool dir0 = exact_blocks ? (k < ks + 2) : (k < 2);
         const bool dir1 = exact_blocks ? (k2 < ks + 2) : (k2 < 2);
@@ -763,17 +905,23 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         // thread's next entry, i += nlt
         ct<T> e0, e1, s0, s1;
         if constexpr (F32) {
-          e0 = phase_f(tid, sph[0]);
-          e1 = phase_f(tid, sph[1]);
-          s0 = tmk<T>(sph[2].x, sph[2].y);
-          s1 = tmk<T>(sph[3].x, sph[3].y);
+          // the point's phase increments theta (k_nl_slice); the step to the
+          // thread's next entry is exp(-i nlt theta) by the same FP32
+          // reduction
+          const float2* ph = Q.phase + ((size_t)pt * 3 + j) * LNL;
+          const float2 th0 = ph[k], th1 = ph[two ? k2 : k];
+          e0 = phase_f(ftid, th0);
+          e1 = phase_f(ftid, th1);
+          s0 = phase_f(fnlt, th0);
+          s1 = phase_f(fnlt, th1);
         } else {
           e0 = phasor<T>(-(deta * tid) * lnb0);
           e1 = phasor<T>(-(deta * tid) * lnb1);
           s0 = phasor<T>(-(deta * nlt) * lnb0);
           s1 = phasor<T>(-(deta * nlt) * lnb1);
         }
-        for (int i = tid; i < nq; i += nlt) {
+        float fi = ftid;
+        for (int i = tid; i < nq; i += nlt, fi += fnlt) {
           ct<T> c0 = e0, c1 = e1;
           if constexpr (sizeof(T) == sizeof(double)) {
             // FP64 plan: exact reduction per entry, as before
@@ -783,12 +931,12 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           e0 = tmul(e0, s0);
           e1 = tmul(e1, s1);
           const ct<T> tv = tout[j * Q.hstride + i];
-          const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, k, deta, dhf, dlf);
+          const ct<T> g0 = nl_g<T>(Q, j, gs, sl0, dir0, gd0, i, fi, k, deta, dhf, dlf);
           ct<T> v0 = tmul(tmul(tv, c0), g0);
           v0.y = -v0.y;  // conj
           ct<T> v1 = tmk<T>((T)0, (T)0);
           if (two) {
-            const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, k2, deta, dhf, dlf);
+            const ct<T> g1 = nl_g<T>(Q, j, gs, sl0 ^ 1, dir1, gd1, i, fi, k2, deta, dhf, dlf);
             v1 = tmul(tmul(tv, c1), g1);
             v1.y = -v1.y;
           }
@@ -801,7 +949,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           }
         }
         __syncthreads();
-        ct<T>* r = block_fft_t<T>(fa, fb, N, Q.fac[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
+        ct<T>* r = block_fft_t<T>(fa, fb, Q.st[j], Q.nfac[j], (const ct<T>*)Q.twt[j], +1);
         if (ADJ && j == 2) {
           // 2 nmax T >= 2 nchi T of scratch (N >= nchi + 2 pad)
           M00 = (T*)((r == fa) ? fb : fa);
@@ -815,10 +963,6 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           sc0 = (T)Q.sck[j * LNL + k];
           sc1 = (T)Q.sck[j * LNL + (two ? k2 : k)];
         }
-        // bmag l(l+1)/(l+1)^2 = bmag l/(l+1)
-        const T mag0 = bmagt * (T)k / (T)(k + 1);
-        const T mag1 = bmagt * (T)k2 / (T)(k2 + 1);
-        const T un0 = (T)k / (T)(k + 1), un1 = (T)k2 / (T)(k2 + 1);  // adjoint: bmag = 1
         const float num1f = Q.nu1f[j];
         const double num1 = F32 ? 0.0 : Q.nu[j] - 1.0;
         for (int i = tid; i < nchi; i += nlt) {
@@ -867,17 +1011,27 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;
           T tb = 0, tm = 0;
           for (int i = tid; i < nchi; i += nlt) {
-            const T rx = rct / xs[i];
-            const T rx3 = rx * rx * rx;
+            T rx3;
+            if constexpr (F32) {
+              rx3 = rx3f[i];
+            } else {
+              const T rx = rct / xs[i];
+              rx3 = rx * rx * rx;
+            }
             for (int h = 0; h < (two ? 2 : 1); h++) {
               const T wt = h ? wt1 : wt0;
               if (wt == (T)0) continue;
               const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
               const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
-              int lo = 0, hi = P.pkl_nk - 1;
-              while (hi > lo + 1) {
-                const int mid = (lo + hi) >> 1;
-                if (plk[mid] > lkt) hi = mid; else lo = mid;
+              int lo = 0;
+              if constexpr (F32) {
+                lo = slice_cell((const float*)plk, P.pkl_nk, lut, lscale, lumax, lkt);
+              } else {
+                int hi = P.pkl_nk - 1;
+                while (hi > lo + 1) {
+                  const int mid = (lo + hi) >> 1;
+                  if (plk[mid] > lkt) hi = mid; else lo = mid;
+                }
               }
               const T F = h ? F1[i] : F0[i];
               const T G = h ? G01[i] : G00[i];
@@ -940,16 +1094,26 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;  // exact for k < 255
         T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
         for (int i = tid; i < nchi; i += nlt) {
-          const T rx = rct / xs[i];
-          const T rx3 = rx * rx * rx;
+          T rx3;
+          if constexpr (F32) {
+            rx3 = rx3f[i];
+          } else {
+            const T rx = rct / xs[i];
+            rx3 = rx * rx * rx;
+          }
           for (int h = 0; h < (two ? 2 : 1); h++) {
             // p_lin(k, 1) (cosmo3D.c:306-358) on the z = 0 slice
             const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
-            int lo = 0, hi = P.pkl_nk - 1;
             const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
-            while (hi > lo + 1) {
-              const int mid = (lo + hi) >> 1;
-              if (plk[mid] > lkt) hi = mid; else lo = mid;
+            int lo = 0;
+            if constexpr (F32) {
+              lo = slice_cell((const float*)plk, P.pkl_nk, lut, lscale, lumax, lkt);
+            } else {
+              int hi = P.pkl_nk - 1;
+              while (hi > lo + 1) {
+                const int mid = (lo + hi) >> 1;
+                if (plk[mid] > lkt) hi = mid; else lo = mid;
+              }
             }
             const T F = h ? F1[i] : F0[i];
             const T k3 = (h ? cub1 : cub0) * rx3;
@@ -1070,7 +1234,10 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
   size_t sm = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
               (f32 ? sizeof(float) * (4 * (size_t)P.pkl_nk + P.nl_nchi)
                    : sizeof(double) * (3 * (size_t)P.pkl_nk + P.nl_nchi)) + 64;
-  if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? sizeof(float) : sizeof(double)) * (size_t)P.pkl_nk;
+  // mixed plan: the slice adjoint's place (always reserved), (rc/x)^3 and
+  // the slice-cell table
+  if (f32) sm += sizeof(float) * ((size_t)P.pkl_nk + P.nl_nchi) + sizeof(unsigned short) * nl_lut_size(P.pkl_nk);
+  if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? 0 : sizeof(double) * (size_t)P.pkl_nk);
   return sm;
 }
 

@@ -96,17 +96,18 @@ struct AxF {
   const float* inv;  // 1 / cell width
   int nk;
 };
-// the FP32 axis in the space of the FP64 one (2 nk doubles >= 3 nk floats)
-__device__ __forceinline__ AxF load_axis_fx(const double* __restrict__ lk, int nk, double* space)
+// the FP32 axis in the space of the FP64 one (2 nk doubles >= 3 nk floats),
+// copied from the plan's precomputed form src = [3][nk] (Params::axk,
+// axkl: head, tail, 1 / width)
+__device__ __forceinline__ AxF load_axis_fx(const float* __restrict__ src, int nk, double* space)
 {
   float* h = (float*)space;
   float* l = h + nk;
   float* iv = l + nk;
   for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < nk; i += blockDim.x * blockDim.y) {
-    const float v = (float)lk[i];
-    h[i] = v;
-    l[i] = (float)(lk[i] - (double)v);
-    iv[i] = (i + 1 < nk) ? (float)(1.0 / (lk[i + 1] - lk[i])) : 0.0f;
+    h[i] = src[i];
+    l[i] = src[nk + i];
+    iv[i] = src[2 * nk + i];
   }
   AxF a;
   a.lk = h;
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
   int* cel = (int*)(nF + nn);              // [LC][nn] table cell
   int* nj = cel + (size_t)LC * nn;         // [nn] z cell
   AxF axf{};
-  if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
+  if constexpr (F32) axf = load_axis_fx(P.axk, nk, lkd);
   else load_axis_d(P.pk_lk, nk, lkd, inv);
   const double* w = P.wss + (size_t)pt * P.ns * nn;
   for (int i = tid; i < np * nn; i += nth) {
@@ -405,7 +406,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   T* wks = yt + (kon ? (size_t)np * nn : 0);
   constexpr bool F32 = sizeof(T) == sizeof(float);
   AxF axf{};
-  if constexpr (F32) axf = load_axis_fx(P.pk_lk, nk, lkd);
+  if constexpr (F32) axf = load_axis_fx(P.axk, nk, lkd);
   else load_axis_d(P.pk_lk, nk, lkd, inv);
   const size_t b0 = (size_t)pt * P.nl + q;
   const double* wx = P.wgs_x + b0 * P.ns * nn;
@@ -598,8 +599,8 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   T* sc = sy + nzs;
   AxF axf{}, axlf{};
   if constexpr (F32) {
-    axf = load_axis_fx(P.pk_lk, nk, lkd);
-    if (nonlim) axlf = load_axis_fx(P.pkl_lk, nkl, lkdl);
+    axf = load_axis_fx(P.axk, nk, lkd);
+    if (nonlim) axlf = load_axis_fx(P.axkl, nkl, lkdl);
   } else {
     load_axis_d(P.pk_lk, nk, lkd, inv);
     if (nonlim) load_axis_d(P.pkl_lk, nkl, lkdl, invl);

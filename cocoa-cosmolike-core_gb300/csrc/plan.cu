@@ -678,6 +678,11 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
     TRY(dalloc(p, &P.lsn, (size_t)W * (1 + nl) * 4 * p->n_ss));
     TRY(dalloc(p, &P.ssx, (size_t)W * p->n_ss * ((p->pss + 7) & ~7)));
     TRY(dalloc(p, &P.gsx, (size_t)W * std::max(nl, 1) * 3 * CL2PT_MAXB * p->n_ss));
+    TRY(dalloc(p, &P.axk, (size_t)3 * P.pk_nk));
+    TRY(dalloc(p, &P.axkl, (size_t)3 * std::max(P.pkl_nk, 1)));
+    TRY(dalloc(p, &P.lensf, (size_t)std::max(nl, 1) * 5 * P.lens_nz));
+    P.ggt_stride = 5 * P.chi_nz + 3 * P.G_nz;
+    TRY(dalloc(p, &P.ggt, (size_t)W * P.ggt_stride));
   }
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
@@ -766,6 +771,18 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
         while (m % fs[f] == 0 && nf < 16) { Q.fac[j][nf++] = fs[f]; m /= fs[f]; }
       if (m != 1) TRY(CL2PT_ERR_ARG);
       Q.nfac[j] = nf;
+      for (int f = 0, Ns = 1; f < nf; Ns *= Q.fac[j][f], f++) {
+        cl2pt::NLStage& st = Q.st[j][f];
+        st.R = Q.fac[j][f];
+        st.Ns = Ns;
+        st.NR = (int)(Nn / st.R);
+        st.ts = (int)(Nn / ((long)Ns * st.R));
+        int l = 0;
+        while ((1L << l) < Ns) l++;
+        st.l = l;
+        st.m = (unsigned)((((unsigned long long)1 << 32) * (((unsigned long long)1 << l) - (unsigned long long)Ns)) /
+                              (unsigned long long)Ns + 1ull);
+      }
       std::vector<double> tw(2 * (size_t)Nn);
       for (long k = 0; k < Nn; k++) {
         const double ang = 2.0 * M_PI * (double)k / (double)Nn;
@@ -804,7 +821,10 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(dupload(p, &dcf, cf.data(), cf.size()));
       Q.l10k1f = dbf;
       Q.sckf = dcf;
-      for (int j = 0; j < 3; j++) Q.nu1f[j] = (float)(Q.nu[j] - 1.0);
+      for (int j = 0; j < 3; j++) {
+        Q.nu1f[j] = (float)(Q.nu[j] - 1.0);
+        Q.nuf[j] = (float)Q.nu[j];
+      }
     }
     Q.hstride = Q.nmax / 2 + 1;
     Q.tout_stride = (size_t)3 * Q.hstride;
@@ -820,9 +840,33 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(dalloc(p, &Q.gdir, (size_t)W * 3 * Q.ndirect * Q.hstride * 2));
       TRY(dalloc(p, &Q.perm, (size_t)W * nl));
       TRY(dalloc(p, &Q.pslice, (size_t)W * P.pkl_nk));
+      if (!Q.direct_every) {
+        float* ph = nullptr;
+        TRY(dalloc(p, &ph, (size_t)W * 3 * LNL * 2));
+        Q.phase = (float2*)ph;
+      }
+      if (!Q.direct_every) {
+        // the Gamma part of g_0, g_1 on eta in [-3h, eta_max + 4h], h = 1/32
+        // (6-point interpolation error ~1e-9 relative); eta_max = pi /
+        // dlnchi bounded with ln(chi(z=4) / chi(z=0.002)) >= 5, entries
+        // beyond it evaluated directly
+        const double inv_h = 32.0;
+        Q.gtab_inv_h = inv_h;
+        Q.gtab_m = (int)ceil(M_PI * (cfg->nl_nchi - 1) / 5.0 * inv_h) + 8;
+        std::vector<double> gt;
+        cl2pt::nl_gamma_tables(Q, inv_h, Q.gtab_m, gt);
+        double* dgt;
+        TRY(dupload(p, &dgt, gt.data(), gt.size()));
+        Q.gtab = dgt;
+      }
     }
   }
   CUDA_OK(cudaMemset(p->d_err, 0, 4));
+  if (precision != CL2PT_PREC_FP64) {
+    cl2pt::launch_prep_consts(P, 0);
+    CUDA_OK(cudaGetLastError());
+    CUDA_OK(cudaStreamSynchronize(0));
+  }
   // mixed plans contract on the tensor cores (TF32x3) when the filters fit
   // the tensor-core form (2 ntheta <= 64 rows); otherwise on the CUDA cores
   if (precision == CL2PT_PREC_MIXED && 2 * nt <= 64) {
