@@ -29,6 +29,7 @@ namespace {
 
 constexpr int LC = 32;  // multipoles per shared-memory chunk
 constexpr int VJP_GG_S = 4;  // threads per node of the gg sweep
+constexpr int VJP_GS_S = 4;  // threads per node of the gs sweep
 
 template <typename T> __device__ __forceinline__ T t_exp(T x);
 template <> __device__ __forceinline__ double t_exp<double>(double x) { return exp(x); }
@@ -53,6 +54,64 @@ __device__ __forceinline__ void pw_flush(PWalk<T>& w, double* __restrict__ bar, 
   atomicAdd(b1, a1 * (1 - dy));
   atomicAdd(b1 + 1, a1 * dy);
   w.acc0 = w.acc1 = (T)0;
+}
+
+// Mixed plan: the run sums are FP32, so their lerp weights are applied in
+// FP32 and the products reach the FP64 atomics by an integer conversion --
+// no FP64 arithmetic per flush (GB300 issues FP64 at 1/64 of the FP32 rate).
+__device__ __forceinline__ void pw_flush(PWalk<float>& w, double* __restrict__ bar, int nz, int j, double dy)
+{
+  if (w.i < 0 || (w.acc0 == 0.0f && w.acc1 == 0.0f)) return;
+  double* b0 = bar + (size_t)w.i * nz + j;
+  double* b1 = b0 + nz;
+  const float dyf = (float)dy, ody = 1.0f - dyf;
+  atomicAdd(b0, f32_to_f64_int(w.acc0 * ody));
+  atomicAdd(b0 + 1, f32_to_f64_int(w.acc0 * dyf));
+  atomicAdd(b1, f32_to_f64_int(w.acc1 * ody));
+  atomicAdd(b1 + 1, f32_to_f64_int(w.acc1 * dyf));
+  w.acc0 = w.acc1 = 0.0f;
+}
+
+// Accumulator of per-chunk partial sums: FP64 in the FP64 plan, an
+// error-free two-float sum (TwoSum) in the mixed plan
+template <typename T> struct Fold;
+template <> struct Fold<double> {
+  double v = 0.0;
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ double get() const { return v; }
+};
+template <> struct Fold<float> {
+  float h = 0.0f, l = 0.0f;
+  __device__ __forceinline__ void add(float x)
+  {
+    const float s = __fadd_rn(h, x);
+    const float bb = __fsub_rn(s, h);
+    l += __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    h = s;
+  }
+  __device__ __forceinline__ double get() const { return f32_to_f64_int(h) + f32_to_f64_int(l); }
+};
+// the same on an 8-byte slot in shared memory (FP64, or head/tail floats)
+template <typename T>
+__device__ __forceinline__ void fold_into(double* slot, T x)
+{
+  if constexpr (sizeof(T) == sizeof(double)) {
+    *slot += x;
+  } else {
+    float* f = (float*)slot;
+    Fold<float> a;
+    a.h = f[0];
+    a.l = f[1];
+    a.add(x);
+    f[0] = a.h;
+    f[1] = a.l;
+  }
+}
+template <typename T>
+__device__ __forceinline__ double fold_value(const double* slot)
+{
+  if constexpr (sizeof(T) == sizeof(double)) return *slot;
+  else return f32_to_f64_int(((const float*)slot)[0]) + f32_to_f64_int(((const float*)slot)[1]);
 }
 
 // P at log10 k (FP64 coordinate); dx returned for the scatter weights.
@@ -367,7 +426,12 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
 // ------------------------------------------------------------------ gs
 // C_gs(l) = pref2 sum_p F [x_s (L + pref M) + (l+1/2)^2 W_K,s K] P, with the
 // one-loop bK weight K = W_gal bK / fK^2 (0 off the one-loop gate); CTA =
-// (point, lens q)
+// (point, lens q), blockDim (nodes, S): S threads per node, each walking a
+// contiguous part of the multipole range (its own table walk and scatter),
+// the C_bar rows of the bin's pairs staged per chunk of LC multipoles of
+// every part.  Per-chunk FP32 partial sums fold into FP64 (FP64 plan) or
+// two-float (mixed plan) accumulators per (part, pair, node), summed over
+// the parts at the end.
 template <typename T>
 __global__ void k_vjp_gs(Params P, VJPParams V)
 {
@@ -375,9 +439,10 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   __shared__ int kk[CL2PT_MAXB], ss_[CL2PT_MAXB];
   __shared__ int npq;
   const int pt = blockIdx.x, q = blockIdx.y;
-  const int p = threadIdx.x;
+  const int p = threadIdx.x, sub = threadIdx.y, S = blockDim.y, nx = blockDim.x;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
   const int nn = P.n_ss, K = P.nnode_g, nk = P.pk_nk;
-  if (p == 0) {
+  if (tid == 0) {
     int m = 0;
     for (int k = 0; k < P.pgs; k++)
       if (P.zl[k] == q) {
@@ -390,35 +455,41 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   __syncthreads();
   const int np = npq;
   if (np == 0) return;
-  double* lkd = (double*)smem_raw;
-  double* inv = lkd + nk;
-  double* xs = inv + nk;               // [np][nn]
-  T* xt = (T*)(xs + (size_t)np * nn);  // [np][nn]
-  T* wxs = xt + (size_t)np * nn;       // [np][nn]
-  T* cbs = wxs + (size_t)np * nn;      // [np][LC]
-  // one-loop bK (only with the gate on): the node's sum over l and sources
-  // of (l+1/2)^2 pref2 F P C_bar W_K (the K adjoint); with bK != 0 also per
-  // source the sums without W_K (FP64 and chunk), for the W_K adjoint
+  constexpr bool F32 = sizeof(T) == sizeof(float);
   const bool kon = P.one_loop && V.one_loop_on[pt];
   const bool kvec = kon && P.nu[pt].gb[5][q] != 0.0;
-  double* ys = (double*)(cbs + (size_t)np * LC);
-  T* yt = (T*)(ys + (kon ? (size_t)np * nn : 0));
-  T* wks = yt + (kon ? (size_t)np * nn : 0);
-  constexpr bool F32 = sizeof(T) == sizeof(float);
+  // shared (gs_smem): axis [2 nk] doubles; fold accumulators xs [S][np][nn]
+  // (8 bytes: FP64, or head/tail floats), ys likewise when kon; per-part
+  // reductions red [3][S][nx] doubles; chunk partials xt [S][np][nn] (T),
+  // yt likewise when kon; weights wxs, wks [np][nn] (T); C_bar chunk cbs
+  // [S][np][LC] (T)
+  const size_t SPN = (size_t)S * np * nn;
+  double* lkd = (double*)smem_raw;
+  double* inv = lkd + nk;
+  double* xs = inv + nk;
+  double* ys = xs + SPN;
+  double* red = ys + (kon ? SPN : 0);
+  T* xt = (T*)(red + 3 * (size_t)S * nx);
+  T* yt = xt + SPN;
+  T* wxs = yt + (kon ? SPN : 0);
+  T* wks = wxs + (size_t)np * nn;
+  T* cbs = wks + (kon ? (size_t)np * nn : 0);
   AxF axf{};
   if constexpr (F32) axf = load_axis_fx(P.axk, nk, lkd);
   else load_axis_d(P.pk_lk, nk, lkd, inv);
   const size_t b0 = (size_t)pt * P.nl + q;
   const double* wx = P.wgs_x + b0 * P.ns * nn;
-  for (int i = p; i < np * nn; i += blockDim.x) {
+  for (int i = tid; i < np * nn; i += nth) {
     const int m = i / nn, r = i - m * nn;
+    wxs[i] = (T)wx[ss_[m] * nn + r];
+    if (kon) wks[i] = (T)P.wgs_k[(b0 * P.ns + ss_[m]) * nn + r];
+  }
+  for (size_t i = tid; i < SPN; i += nth) {
     xs[i] = 0.0;
     xt[i] = (T)0;
-    wxs[i] = (T)wx[ss_[m] * nn + r];
     if (kon) {
       ys[i] = 0.0;
       yt[i] = (T)0;
-      wks[i] = (T)P.wgs_k[(b0 * P.ns + ss_[m]) * nn + r];
     }
   }
   const bool act = p < nn;
@@ -437,19 +508,27 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
   const float2 lf = split_fx(nd.lfk);
   double* bar = V.lnp_bar + (size_t)pt * P.pk_nk * P.pk_nz;
   PWalk<T> wk;
-  double lb0 = 0.0, lb1 = 0.0, kbs = 0.0;
-  for (int L0 = 0; L0 < K; L0 += LC) {
-    const int nL = min(LC, K - L0);
+  Fold<T> lb0, lb1, kbs;
+  // this part's multipoles [La, Lb)
+  const int cs = (K + S - 1) / S;
+  const int La = min(K, sub * cs), Lb = min(K, La + cs);
+  T* xtr = xt + (size_t)sub * np * nn;
+  T* ytr = yt + (size_t)sub * np * nn;
+  for (int c0 = 0; c0 < cs; c0 += LC) {
     __syncthreads();
-    for (int i = p; i < np * LC; i += blockDim.x) {
-      const int m = i / LC, l = i - m * LC;
-      cbs[i] = (l < nL) ? (T)V.cbar_gs[((size_t)pt * P.pgs + kk[m]) * K + L0 + l] : (T)0;
+    for (int i = tid; i < S * np * LC; i += nth) {
+      const int sb = i / (np * LC), r = i - sb * np * LC;
+      const int m = r / LC, l = r - m * LC;
+      const int L = sb * cs + c0 + l, Le = min(K, (sb + 1) * cs);
+      cbs[i] = (L < Le) ? (T)V.cbar_gs[((size_t)pt * P.pgs + kk[m]) * K + L] : (T)0;
     }
     __syncthreads();
-    if (!act) continue;
+    const int nL = min(LC, Lb - (La + c0));
+    if (!act || nL <= 0) continue;
+    const T* cb = cbs + (size_t)sub * np * LC;
     T t0 = 0, t1 = 0, tk = 0;
     for (int l = 0; l < nL; l++) {
-      const int L = L0 + l;
+      const int L = La + c0 + l;
       T dx, pref, g, lp2 = (T)0;
       if constexpr (F32) {
         const float4 fa = *(const float4*)(V.lfacf_g + 8 * L);
@@ -471,61 +550,81 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
       if (kvec) {
         const T gk = g * lp2;
         for (int m = 0; m < np; m++) {
-          const T cv = cbs[m * LC + l];
+          const T cv = cb[m * LC + l];
           sx += cv * wxs[m * nn + p];
           sk += cv * wks[m * nn + p];
-          xt[m * nn + p] += gl * cv;
-          yt[m * nn + p] += gk * cv;
+          xtr[m * nn + p] += gl * cv;
+          ytr[m * nn + p] += gk * cv;
         }
         tk += gk * sk;
         sk *= gk * Kt;
       } else if (kon) {
         // bK = 0: K = 0, so no W_K adjoint and no lnP term
         for (int m = 0; m < np; m++) {
-          const T cv = cbs[m * LC + l];
+          const T cv = cb[m * LC + l];
           sx += cv * wxs[m * nn + p];
           sk += cv * wks[m * nn + p];
-          xt[m * nn + p] += gl * cv;
+          xtr[m * nn + p] += gl * cv;
         }
         tk += g * lp2 * sk;
         sk = (T)0;
       } else {
         for (int m = 0; m < np; m++) {
-          const T cv = cbs[m * LC + l];
+          const T cv = cb[m * LC + l];
           sx += cv * wxs[m * nn + p];
-          xt[m * nn + p] += gl * cv;
+          xtr[m * nn + p] += gl * cv;
         }
       }
       t0 += g * sx;
       t1 += g * pref * sx;
       pw_acc<T>(wk, gl * sx + sk, dx);
     }
-    lb0 += (double)t0;
-    lb1 += (double)t1;
-    kbs += (double)tk;
+    lb0.add(t0);
+    lb1.add(t1);
+    kbs.add(tk);
+    double* xsr = xs + (size_t)sub * np * nn;
     for (int m = 0; m < np; m++) {
-      xs[m * nn + p] += (double)xt[m * nn + p];
-      xt[m * nn + p] = (T)0;
+      fold_into<T>(xsr + m * nn + p, xtr[m * nn + p]);
+      xtr[m * nn + p] = (T)0;
     }
     if (kvec) {
+      double* ysr = ys + (size_t)sub * np * nn;
       for (int m = 0; m < np; m++) {
-        ys[m * nn + p] += (double)yt[m * nn + p];
-        yt[m * nn + p] = (T)0;
+        fold_into<T>(ysr + m * nn + p, ytr[m * nn + p]);
+        ytr[m * nn + p] = (T)0;
       }
     }
   }
-  if (!act) return;
-  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  if (act) pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  red[(0 * S + sub) * nx + p] = lb0.get();
+  red[(1 * S + sub) * nx + p] = lb1.get();
+  red[(2 * S + sub) * nx + p] = kbs.get();
+  __syncthreads();
+  if (!act || sub != 0) return;
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  for (int sb = 0; sb < S; sb++) {
+    r0 += red[(0 * S + sb) * nx + p];
+    r1 += red[(1 * S + sb) * nx + p];
+    r2 += red[(2 * S + sb) * nx + p];
+  }
   double* xbar = V.wbar_gx + b0 * P.ns * nn;
-  for (int m = 0; m < np; m++) xbar[ss_[m] * nn + p] += xs[m * nn + p];
+  for (int m = 0; m < np; m++) {
+    double v = 0.0;
+    for (int sb = 0; sb < S; sb++) v += fold_value<T>(xs + ((size_t)sb * np + m) * nn + p);
+    xbar[ss_[m] * nn + p] += v;
+  }
   if (kon) {
     // K adjoint of the bK term, and with bK != 0 the W_K (source photo-z) one
     if (kvec)
-      for (int m = 0; m < np; m++) V.wbar_gsk[(b0 * P.ns + ss_[m]) * nn + p] += Kw * ys[m * nn + p];
-    V.kbar_gs[b0 * nn + p] += kbs;
+      for (int m = 0; m < np; m++) {
+        double v = 0.0;
+        for (int sb = 0; sb < S; sb++) v += fold_value<T>(ys + ((size_t)sb * np + m) * nn + p);
+        V.wbar_gsk[(b0 * P.ns + ss_[m]) * nn + p] += Kw * v;
+      }
+    V.kbar_gs[b0 * nn + p] += r2;
   }
-  V.lbar_gs[(b0 * 2 + 0) * nn + p] = lb0;
-  V.lbar_gs[(b0 * 2 + 1) * nn + p] = lb1;
+  V.lbar_gs[(b0 * 2 + 0) * nn + p] = r0;
+  V.lbar_gs[(b0 * 2 + 1) * nn + p] = r1;
 }
 
 // ------------------------------------------------------------------ gg
@@ -690,7 +789,10 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   };
   PWalk<T> wk;
   // lbar: adjoint of s; mbar: of the magnification weight M (ds/dM = pref)
-  double lbar = 0.0, kbar = 0.0, mbar = 0.0;
+  Fold<T> lbar, kbar, mbar;
+  // the chi(a_min) cut per multipole only for a list that does not ascend
+  // (a sorted one starts at the first kept index Lk)
+  const bool cut_each = !V.lfac_g_sorted;
   // stored: the row of s for this node and the forward's first kept indices
   const size_t Ltot = (size_t)K + LNL;
   const float* sg = stored ? P.s_gg + (b0 * nn + p) * Ltot : nullptr;
@@ -704,7 +806,9 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     T lt = 0, kt = 0, mt = 0;
     for (int L = L0; L < L1; L++) {
       const double* fac = V.lfac_g + 6 * L;
-      if (!V.lfac_g_sorted && nd.fK * fac[5] > chi_amin) continue;
+      if (cut_each) {
+        if (nd.fK * fac[5] > chi_amin) continue;
+      }
       const T cv = cbs[L];
       if (cv == (T)0) continue;
       T dx, s, Pv, lp2 = (T)0, pref;
@@ -734,9 +838,9 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       kt += kp;
       pw_acc<T>(wk, cv * s * sp + kp * Kt, dx);
     }
-    lbar += (double)lt;
-    kbar += (double)kt;
-    mbar += (double)mt;
+    lbar.add(lt);
+    kbar.add(kt);
+    mbar.add(mt);
   }
   pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
   if (nonlim) {
@@ -791,16 +895,16 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
       pw_acc<T>(wn, cn * s * sF * Pn + kp * Kt, dx);
       pw_acc<T>(wl, cl * s * sF * Pl, dxl);
     }
-    lbar += (double)lt;
-    kbar += (double)kt;
-    mbar += (double)mt;
+    lbar.add(lt);
+    kbar.add(kt);
+    mbar.add(mt);
     pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
     pw_flush(wl, barl, P.pkl_nz, jl, dyl);
   }
   // zeroed per wave; S threads per node, and the Fourier path adds two passes
-  atomicAdd(&V.lbar_gg[b0 * nn + p], lbar);
-  if (kon) atomicAdd(&V.kbar_gg[b0 * nn + p], kbar);
-  if (nu.gb[4][q] != 0.0) atomicAdd(&V.mbar_gg[b0 * nn + p], mbar);
+  atomicAdd(&V.lbar_gg[b0 * nn + p], lbar.get());
+  if (kon) atomicAdd(&V.kbar_gg[b0 * nn + p], kbar.get());
+  if (nu.gb[4][q] != 0.0) atomicAdd(&V.mbar_gg[b0 * nn + p], mbar.get());
 }
 
 template <typename T>
@@ -810,12 +914,15 @@ size_t ss_smem(const Params& P)
   return 16 * (size_t)P.pk_nk + 16 * nn + np * nn * (8 + sizeof(T)) + np * LC * sizeof(T) +
          3 * LC * nn * sizeof(T) + nn * sizeof(T) + (LC * nn + nn) * sizeof(int) + 64;
 }
+// k_vjp_gs's layout for S parts per node (np <= ns pairs per lens bin)
 template <typename T>
-size_t gs_smem(const Params& P)
+size_t gs_smem(const Params& P, int S)
 {
-  const size_t nn = P.n_ss, np = P.ns;
-  return 16 * (size_t)P.pk_nk + np * nn * (8 + 2 * sizeof(T)) + np * LC * sizeof(T) +
-         (P.one_loop ? np * nn * (8 + 2 * sizeof(T)) : 0) + 64;
+  const size_t nn = P.n_ss, np = P.ns, nx = (P.n_ss + 31) / 32 * 32;
+  const size_t spn = (size_t)S * np * nn;
+  const size_t kon = P.one_loop ? 1 : 0;
+  return 16 * (size_t)P.pk_nk + spn * 8 * (1 + kon) + 3 * (size_t)S * nx * 8 +
+         sizeof(T) * (spn * (1 + kon) + np * nn * (1 + kon) + (size_t)S * np * LC) + 64;
 }
 template <typename T>
 size_t gg_smem(const Params& P)
@@ -834,9 +941,14 @@ void launch_t(const Params& P, const VJPParams& V, int which, cudaStream_t s)
     cudaFuncSetAttribute(k_vjp_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_vjp_ss<T><<<P.B, SS_NT, sm, s>>>(P, V);
   } else if (which == 1) {
-    const size_t sm = gs_smem<T>(P);
+    // up to VJP_GS_S parts per node, fewer when their accumulators would
+    // leave room for less than two CTAs per SM
+    const int nx = ((P.n_ss + rnd - 1) / rnd) * rnd;
+    int S = VJP_GS_S;
+    while (S > 1 && gs_smem<T>(P, S) > 110 * 1024) S--;
+    const size_t sm = gs_smem<T>(P, S);
     cudaFuncSetAttribute(k_vjp_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_vjp_gs<T><<<dim3(P.B, P.nl), ((P.n_ss + rnd - 1) / rnd) * rnd, sm, s>>>(P, V);
+    k_vjp_gs<T><<<dim3(P.B, P.nl), dim3(nx, S), sm, s>>>(P, V);
   } else {
     const size_t sm = gg_smem<T>(P);
     cudaFuncSetAttribute(k_vjp_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -860,9 +972,9 @@ size_t vjp_limber_smem(const Params& P)
 {
   size_t m = 0;
   if (P.prec == CL2PT_PREC_FP64) {
-    m = std::max(ss_smem<double>(P), std::max(gs_smem<double>(P), gg_smem<double>(P)));
+    m = std::max(ss_smem<double>(P), std::max(gs_smem<double>(P, 1), gg_smem<double>(P)));
   } else {
-    m = std::max(ss_smem<float>(P), std::max(gs_smem<float>(P), gg_smem<float>(P)));
+    m = std::max(ss_smem<float>(P), std::max(gs_smem<float>(P, 1), gg_smem<float>(P)));
   }
   return m;
 }
