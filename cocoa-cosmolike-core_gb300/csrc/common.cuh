@@ -27,6 +27,29 @@ struct NodeSet {
   double* dyz;     // z fraction inside the cell
 };
 
+// Division by a divisor d >= 1 fixed when the plan is made, as a multiply-
+// high and a shift: n / d = (umulhi(n, m) + n) >> l for 0 <= n < 2^31
+// (m = floor(2^32 (2^l - d) / d) + 1, 2^l >= d).  GB300 forms integer
+// division from conversions that issue at the FP64 rate, so index loops
+// over runtime-sized tiles divide this way.
+struct FastDiv {
+  unsigned m;
+  int l;
+};
+inline FastDiv make_fastdiv(int d)
+{
+  FastDiv f;
+  f.l = 0;
+  while ((1L << f.l) < d) f.l++;
+  f.m = (unsigned)((((unsigned long long)1 << 32) * (((unsigned long long)1 << f.l) - (unsigned long long)d)) /
+                       (unsigned long long)d + 1ull);
+  return f;
+}
+__device__ __forceinline__ int fdiv(int n, const FastDiv& f)
+{
+  return (int)((__umulhi((unsigned)n, f.m) + (unsigned)n) >> f.l);
+}
+
 // Everything a kernel needs, by value (device pointers only).
 struct Params {
   // configuration scalars (cl2pt_config)
@@ -94,6 +117,7 @@ struct Params {
   float* lensf;
   float* ggt;
   int ggt_stride;
+  FastDiv fd_nss;           // n_ss as a FastDiv (adjoint index loops)
   // mixed plan, when an adjoint follows (real space): the redshift-space
   // weight s(l, node) of every gg term the forward sums, 0 where the
   // chi(a_min) cut drops it [B][nl][n_gg][nnode_g + lmax_nolimber] (C_l

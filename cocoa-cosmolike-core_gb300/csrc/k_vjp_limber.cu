@@ -312,6 +312,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
   T* nF = dxs + (size_t)LC * nn;           // [nn] F
   int* cel = (int*)(nF + nn);              // [LC][nn] table cell
   int* nj = cel + (size_t)LC * nn;         // [nn] z cell
+  float* ndf = (float*)(nj + nn);          // [nn] node z offsets in FP32
   AxF axf{};
   if constexpr (F32) axf = load_axis_fx(P.axk, nk, lkd);
   else load_axis_d(P.pk_lk, nk, lkd, inv);
@@ -324,6 +325,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
   for (int i = tid; i < nn; i += nth) {
     const NodeD nd = node_d(P, pt, i);
     ndy[i] = nd.dy;
+    ndf[i] = (float)nd.dy;
     nF[i] = (T)nd.F;
     nj[i] = nd.j;
     if constexpr (F32) ((float2*)nlk)[i] = split_fx(nd.lfk);
@@ -344,7 +346,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
     }
     // A
     for (int e = tid; e < LC * nn; e += nth) {
-      const int l = e / nn, q = e - l * nn;
+      const int l = fdiv(e, P.fd_nss), q = e - l * nn;
       T pv = (T)0, dx = (T)0;
       int c = -1;
       if (l < nL) {
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
           const float2 lf = ((const float2*)nlk)[q];
           float uh, ul;
           sub_fx(fa.x, fa.y, lf.x, lf.y, uh, ul);
-          pv = fa.z * pv_eval_f(axf, tab2, P.pk_nz, nj[q], (float)ndy[q], uh, ul, c, dx);
+          pv = fa.z * pv_eval_f(axf, tab2, P.pk_nz, nj[q], ndf[q], uh, ul, c, dx);
         } else {
           pv = (T)V.lfac_ss[2 * L + 1] *
                (T)pv_eval_d(lkd, inv, nk, tab, P.pk_nz, nj[q], ndy[q], V.lfac_ss[2 * L] - nlk[q], c, dx);
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
     __syncthreads();
     // B
     for (int o = tid; o < np * nn; o += nth) {
-      const int pr = o / nn, q = o - pr * nn;
+      const int pr = fdiv(o, P.fd_nss), q = o - pr * nn;
       T acc = 0;
       for (int l = 0; l < nL; l++) acc += cbs[pr * LC + l] * Pt[l * nn + q];
       if constexpr (F32) {
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
     }
     // C
     for (int e = tid; e < nL * nn; e += nth) {
-      const int l = e / nn, q = e - l * nn;
+      const int l = fdiv(e, P.fd_nss), q = e - l * nn;
       T pb = 0;
       for (int pr = 0; pr < np; pr++) pb += cbs[pr * LC + l] * w2[pr * nn + q];
       G[e] = Pt[e] * nF[q] * pb;
@@ -912,7 +914,7 @@ size_t ss_smem(const Params& P)
 {
   const size_t nn = P.n_ss, np = P.pss;
   return 16 * (size_t)P.pk_nk + 16 * nn + np * nn * (8 + sizeof(T)) + np * LC * sizeof(T) +
-         3 * LC * nn * sizeof(T) + nn * sizeof(T) + (LC * nn + nn) * sizeof(int) + 64;
+         3 * LC * nn * sizeof(T) + nn * sizeof(T) + (LC * nn + nn) * sizeof(int) + nn * sizeof(float) + 64;
 }
 // k_vjp_gs's layout for S parts per node (np <= ns pairs per lens bin)
 template <typename T>

@@ -616,6 +616,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.prec = precision;
   P.pss = p->pss; P.pgs = p->pgs; P.pgg = p->pgg;
   P.n_a = cfg->n_a; P.n_ss = p->n_ss; P.n_gg = p->n_gg;
+  P.fd_nss = cl2pt::make_fastdiv(p->n_ss);
   P.nnode_ss = p->nnode_ss; P.nnode_g = p->nnode_g; P.nint = p->nint;
   for (int i = 0; i < 3; i++) { P.lim_ss[i] = p->lim_ss[i]; P.lim_g[i] = p->lim_g[i]; }
   P.chi_nz = grid->chi_nz; P.G_nz = grid->G_nz;
