@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "libcl2pt.so")
 PREC_MIXED, PREC_FP64 = 0, 1
 # Legendre contraction of a mixed plan (CL2PT_CONTRACT_*)
 CONTRACT_FP32, CONTRACT_TF32X3, CONTRACT_BF16X3, CONTRACT_BF16X6 = 0, 1, 2, 3
+FFTLOG_STATE_AUTO, FFTLOG_STATE_GLOBAL, FFTLOG_STATE_SHARED = 0, 1, 2
 # kernel ids of cl2pt_kernel_times (CL2PT_K_* in include/cl2pt.h)
 KERNELS = ["k_gtab", "k_nodes", "k_limber_ss", "k_limber_gs", "k_limber_gg", "k_limber_ggl",
            "k_nonlimber", "k_contract", "k_assemble", "k_vjp"]
@@ -95,6 +96,12 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_fourier_graph_create.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_double,
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.POINTER(C.c_void_p)]
+    lib.cl2pt_plan_set_fftlog_state.argtypes = [C.c_void_p, C.c_int]
+    lib.cl2pt_plan_set_baryon_ratio.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp]
+    lib.cl2pt_plan_autotune.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_int, _ip, _ip,
+                                        C.POINTER(C.c_double)]
+    lib.cl2pt_real_graph_create.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.POINTER(C.c_void_p)]
     lib.cl2pt_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
     lib.cl2pt_graph_launch_count.argtypes = [C.c_void_p]
     lib.cl2pt_graph_destroy.argtypes = [C.c_void_p]
@@ -495,6 +502,54 @@ class Plan:
         # keep the tensors the graph reads alive with it
         return Graph(g, (omega_m, h0, chi, G, lnP, nuisance, out, mask, row_ptr, idx, lnPL, self))
 
+    def set_baryon_ratio(self, log10k, a, log10r):
+        """p_nonlin x 10^(log10r interpolated on (log10 k [h/Mpc], a))
+        (cl2pt_plan_set_baryon_ratio); log10r is [len(a)][len(log10k)];
+        an empty log10k turns it off."""
+        lk = np.ascontiguousarray(log10k, dtype=np.float64)
+        av = np.ascontiguousarray(a, dtype=np.float64)
+        lr = np.ascontiguousarray(log10r, dtype=np.float64)
+        if len(lk) == 0:
+            check(load().cl2pt_plan_set_baryon_ratio(self.h, 0, None, 0, None, None), "cl2pt_plan_set_baryon_ratio")
+            return
+        assert lr.shape == (len(av), len(lk))
+        check(load().cl2pt_plan_set_baryon_ratio(self.h, len(lk), _p(lk), len(av), _p(av), _p(lr)),
+              "cl2pt_plan_set_baryon_ratio")
+
+    def set_fftlog_state(self, mode):
+        """Where the FFTLog loop keeps its spectra and state (FFTLOG_STATE_*)."""
+        check(load().cl2pt_plan_set_fftlog_state(self.h, int(mode)), "cl2pt_plan_set_fftlog_state")
+
+    def autotune(self, omega_m, h0, chi, G, lnP, nuisance, reps=3, lnPL=None, stream=None):
+        """Time the candidate configurations on these CUDA tensors, keep the
+        fastest (cl2pt_plan_autotune); returns (contraction, fftlog_state, ms)."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        c, st, ms = C.c_int(), C.c_int(), C.c_double()
+        check(load().cl2pt_plan_autotune(self.h, C.byref(b), stream, int(reps), C.byref(c), C.byref(st),
+                                         C.byref(ms)), "cl2pt_plan_autotune")
+        return c.value, st.value, ms.value
+
+    def real_graph(self, omega_m, h0, chi, G, lnP, nuisance, out, mask=None, pm=None, lnPL=None,
+                   stream=None):
+        """Capture a real-space evaluation over these CUDA tensors as a graph
+        (see cl2pt_real_graph_create); returns a Graph."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        g = C.c_void_p()
+        ptr = lambda t: None if t is None else t.data_ptr()
+        check(load().cl2pt_real_graph_create(self.h, C.byref(b), ptr(mask), ptr(pm), out.data_ptr(), stream,
+                                             C.byref(g)), "cl2pt_real_graph_create")
+        return Graph(g, (omega_m, h0, chi, G, lnP, nuisance, out, mask, pm, lnPL, self))
+
     # ------------------------------------------------------------ device
     def eval_real_device(self, omega_m, h0, chi, G, lnP, nuisance, out, mask=None, pm=None,
                          lnPL=None, stream=None):
@@ -580,7 +635,7 @@ class Likelihood:
 
 
 class Graph:
-    """A captured Fourier evaluation (cl2pt_graph)."""
+    """A captured evaluation (cl2pt_graph: Fourier or real space)."""
 
     def __init__(self, h, keep):
         self.h = h

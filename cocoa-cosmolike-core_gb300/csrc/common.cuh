@@ -117,6 +117,10 @@ struct Params {
   float* lensf;
   float* ggt;
   int ggt_stride;
+  // mixed plan, one-loop bias: per (point, lens bin, gg node) the one-loop
+  // gg integrand's rows combined on the FAST-PT grid, A_p(k) = sum_m X_m(p)
+  // row_m(k) [B][nl][n_gg][fpt_n] (k_extra_gg_rows, formed in FP64)
+  float* fpt_gga;
   FastDiv fd_nss;           // n_ss as a FastDiv (adjoint index loops)
   // mixed plan, when an adjoint follows (real space): the redshift-space
   // weight s(l, node) of every gg term the forward sums, 0 where the
@@ -187,6 +191,22 @@ struct Params {
 
 enum { NF_A = 0, NF_WT, NF_FK, NF_DCHIDA, NF_D, NF_H, NF_DYZ, NF_COUNT };
 constexpr int GGN_SLOTS = 16;  // floats per gg node record (k_gg_nodes)
+
+// Nearest FP32 of an FP64 value by integer arithmetic on its bits (no FP64
+// or conversion instruction).  Results below the FP32 normal range flush
+// to zero and above it go to infinity; ties round up.
+__device__ __forceinline__ float f64_to_f32_bits(double v)
+{
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
+  const uint32_t sgn = hi & 0x80000000u;
+  const uint32_t ex = (hi >> 20) & 0x7FFu;
+  const uint32_t man = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  uint32_t f = ((ex - 896u) << 23) + man + ((lo >> 28) & 1u);
+  f = (ex <= 896u) ? 0u : f;
+  f = (ex >= 1151u) ? 0x7F800000u : f;
+  return __uint_as_float(sgn | f);
+}
 
 // FP64 value of an FP32 one by integer arithmetic (exact, as the hardware
 // conversion).  GB300 issues FP64 instructions, conversions included, at

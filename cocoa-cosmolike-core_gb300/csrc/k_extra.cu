@@ -21,6 +21,7 @@
 // The NLA / linear-bias part of every integrand is the base pass
 // (k_limber.cu); these kernels add the rest.  Table rows are read by the
 // reference's rule: linear in ln k on the uniform grid, 0 outside it.
+#include <type_traits>
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -354,6 +355,132 @@ __global__ void __launch_bounds__(LX) k_extra_gg(Params P, const double* __restr
   else P.ggl[(b0 * P.lmax_nolimber + L) * 2 + 0] += (double)acc;
 }
 
+// Mixed plan: the same sum with the cancellation taken in FP64 once per
+// node and FAST-PT grid cell instead of per multipole.  The integrand is
+// linear in the six rows, so interpolating A_p(k) = sum_m X_m(p) row_m(k)
+// equals interpolating each row and summing (the reference's order, up to
+// rounding); A_p is formed in FP64 on the grid (k_extra_gg_rows, where the
+// five bias terms cancel to ~1e-3) and stored in FP32, and the multipole
+// tiles interpolate it in FP32 (k_extra_gg_f).
+constexpr int XR_NT = 128;  // grid cells per CTA of k_extra_gg_rows
+__global__ void __launch_bounds__(XR_NT) k_extra_gg_rows(Params P)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.y;
+  const int n = P.fpt_n, nn = P.n_gg;
+  double* X = (double*)smem_raw;  // [6][nn]
+  const int off = P.n_ss + P.nl * P.n_ss + q * nn;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const size_t b0 = (size_t)pt * P.nl + q;
+  for (int idx = threadIdx.x; idx < 6 * nn; idx += blockDim.x) {
+    const int m = idx / nn, p = idx - m * nn;
+    const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+    const double F = node[(size_t)NF_WT * P.node_stride + off + p] *
+                     node[(size_t)NF_DCHIDA * P.node_stride + off + p] / (fK * fK);
+    X[m * nn + p] = P.wgg_1l[(b0 * 6 + m) * nn + p] * F;
+  }
+  __syncthreads();
+  const int c = blockIdx.z * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double r[6];
+  for (int m = 0; m < 5; m++) r[m] = P.fpt_b[((size_t)pt * 5 + m) * n + c];
+  r[5] = P.fpt_d1p3 ? P.fpt_d1p3[c] : 0.0;
+  float* out = P.fpt_gga + b0 * nn * (size_t)n + c;
+  for (int p = 0; p < nn; p++) {
+    double a = 0.0;
+#pragma unroll
+    for (int m = 0; m < 6; m++) a += X[m * nn + p] * r[m];
+    out[(size_t)p * n] = f64_to_f32_bits(a);
+  }
+}
+
+// the multipole tiles of the mixed plan: FP32 interpolation of A_p at
+// ln k = ln(l + 1/2) - ln chi_p on the FAST-PT grid (fpt_cell's rules:
+// outside the grid 0, in the last cell the last value), summed over the
+// nodes the chi(a_min) cut keeps.  The grid coordinate r = (ln k - lim0) /
+// dlnk = a_l - b_p is an exact two-float difference of a per-multipole and a
+// per-node part (formed in FP64 once), so the in-cell weight keeps ~1e-7 of
+// a cell; the node sum is a two-float (TwoSum) accumulation.
+__device__ __forceinline__ float2 split2(double v)
+{
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__global__ void __launch_bounds__(LX) k_extra_gg_f(Params P, const double* __restrict__ ell, int mode)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pt = blockIdx.x, q = blockIdx.z;
+  const int L = blockIdx.y * LX + threadIdx.x;
+  const int n = P.fpt_n, nn = P.n_gg;
+  float2* bq = (float2*)smem_raw;                    // [nn] ln chi / dlnk (head, tail)
+  int* lmin = (int*)(bq + nn);                       // [nn] first kept multipole index
+  double* thr = (double*)(((size_t)(lmin + nn) + 7) & ~(size_t)7);  // [nn] cut threshold on l + 1/2
+  const int off = P.n_ss + P.nl * P.n_ss + q * nn;
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  const size_t b0 = (size_t)pt * P.nl + q;
+  const double chi_amin = P.chi_amin[pt];
+  const int nL = (mode == 0) ? P.nnode_g : P.lmax_nolimber;
+  const bool sorted = mode == 1 || P.ell_g_sorted;
+  for (int p = threadIdx.x; p < nn; p += blockDim.x) {
+    const double fK = node[(size_t)NF_FK * P.node_stride + off + p];
+    bq[p] = split2(log(fK) / P.fpt_lim2);
+    // fK (lp + 1)/lp > chi(a_min)  <=>  lp < fK / (chi(a_min) - fK)
+    // (every multipole when fK >= chi(a_min))
+    const double th = (chi_amin > fK) ? fK / (chi_amin - fK) : 1e300;
+    thr[p] = th;
+    int lo = 0, hi = nL;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      const double lpm = (mode == 0 ? ell[mid] : (double)mid) + 0.5;
+      if (lpm < th) lo = mid + 1;
+      else hi = mid;
+    }
+    lmin[p] = lo;
+  }
+  __syncthreads();
+  if (L >= nL) return;
+  const double l = (mode == 0) ? ell[L] : (double)L, lp = l + 0.5;
+  const float2 al = split2((log(lp) - P.fpt_lim0) / P.fpt_lim2);
+  const float rmax = (float)n;  // r at ln k = lim1
+  const float* A = P.fpt_gga + b0 * nn * (size_t)n;
+  float acc_h = 0.0f, acc_l = 0.0f;
+  auto walk = [&](auto idx_cut) {
+    for (int p = 0; p < nn; p++) {
+      if (decltype(idx_cut)::value ? L < lmin[p] : lp < thr[p]) continue;
+      // r = a - b as an unevaluated sum rs + rt (TwoSum of the heads)
+      const float rs = __fsub_rn(al.x, bq[p].x);
+      const float bb = __fsub_rn(rs, al.x);
+      const float rt = __fadd_rn(__fsub_rn(al.x, __fsub_rn(rs, bb)), __fsub_rn(-bq[p].x, bb)) + (al.y - bq[p].y);
+      const float r = rs + rt;
+      if (r < 0.0f || r > rmax) continue;
+      // floor(r) without a conversion (round r - 1/2), then the exact
+      // in-cell offset from the two-float r
+      int c = __float_as_int((r - 0.5f) + 12582912.0f) - 0x4B400000;
+      float w = (rs - (float)c) + rt;
+      if (w < 0.0f) { c -= 1; w += 1.0f; }
+      if (w >= 1.0f) { c += 1; w -= 1.0f; }
+      c = max(c, 0);
+      const float* a = A + (size_t)p * n;
+      float v;
+      if (c + 1 >= n) {
+        v = a[n - 1];
+      } else {
+        const float a0 = a[c];
+        v = w * (a[c + 1] - a0) + a0;
+      }
+      const float sh = __fadd_rn(acc_h, v);
+      const float b2 = __fsub_rn(sh, acc_h);
+      acc_l += __fadd_rn(__fsub_rn(acc_h, __fsub_rn(sh, b2)), __fsub_rn(v, b2));
+      acc_h = sh;
+    }
+  };
+  if (sorted) walk(std::true_type{});
+  else walk(std::false_type{});
+  const double v = f32_to_f64_int(acc_h) + f32_to_f64_int(acc_l);
+  if (mode == 0) P.tab_gg[b0 * P.nnode_g + L] += v;
+  else P.ggl[(b0 * P.lmax_nolimber + L) * 2 + 0] += v;
+}
+
 template <typename T>
 void launch_extra_t(const Params& P, const double* ell_ss, const double* ell_g, cudaStream_t s,
                     int* launches, const Hook& hk)
@@ -377,9 +504,28 @@ void launch_extra_t(const Params& P, const double* ell_ss, const double* ell_g, 
     hk(CL2PT_K_LIMBER_GS, 0);
     (*launches)++;
   }
-  if (P.one_loop && (P.probes & CL2PT_PROBE_WTHETA)) {
-    // FP64 in both plans: at high k the sigma_4-subtracted rows are nearly
-    // constant and the five terms cancel to ~1e-3 of their size
+  if (P.one_loop && (P.probes & CL2PT_PROBE_WTHETA) && sizeof(T) == sizeof(float)) {
+    // mixed plan: the cancelling sum in FP64 per node and grid cell, then
+    // FP32 interpolation per multipole
+    const size_t smr = sizeof(double) * 6 * (size_t)P.n_gg;
+    k_extra_gg_rows<<<dim3(P.B, P.nl, (n + XR_NT - 1) / XR_NT), XR_NT, smr, s>>>(P);
+    (*launches)++;
+    const size_t smf = (sizeof(float2) + sizeof(int) + sizeof(double)) * (size_t)P.n_gg + 16;  // bq, lmin, thr
+    dim3 g(P.B, (P.nnode_g + LX - 1) / LX, P.nl);
+    hk(CL2PT_K_LIMBER_GG, 1);
+    k_extra_gg_f<<<g, LX, smf, s>>>(P, ell_g, 0);
+    hk(CL2PT_K_LIMBER_GG, 0);
+    (*launches)++;
+    if (!P.adopt_limber_gg) {
+      dim3 g1(P.B, (P.lmax_nolimber + LX - 1) / LX, P.nl);
+      hk(CL2PT_K_LIMBER_GGL, 1);
+      k_extra_gg_f<<<g1, LX, smf, s>>>(P, ell_g, 1);
+      hk(CL2PT_K_LIMBER_GGL, 0);
+      (*launches)++;
+    }
+  } else if (P.one_loop && (P.probes & CL2PT_PROBE_WTHETA)) {
+    // FP64 plan: at high k the sigma_4-subtracted rows are nearly constant
+    // and the five terms cancel to ~1e-3 of their size
     const size_t sm = al(sizeof(double) * (6 * (size_t)n + 6 * (size_t)P.n_gg + 1)) + 2 * sizeof(double) * P.n_gg;
     dim3 g(P.B, (P.nnode_g + LX - 1) / LX, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
@@ -403,7 +549,7 @@ int extra_smem_setup()
   const int mx = 232448 - 1024;  // 227 KB per CTA less room for static shared memory
   const void* ks[] = {(const void*)k_extra_ss<float>, (const void*)k_extra_ss<double>,
                       (const void*)k_extra_gs<float>, (const void*)k_extra_gs<double>,
-                      (const void*)k_extra_gg<double>};
+                      (const void*)k_extra_gg<double>, (const void*)k_extra_gg_rows};
   for (const void* k : ks)
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, mx) != cudaSuccess) return -1;
   return 0;

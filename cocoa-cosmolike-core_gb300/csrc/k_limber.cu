@@ -211,6 +211,18 @@ __global__ void k_prep_consts(Params P)
   }
 }
 
+__global__ void k_add_table(const double* __restrict__ src, const double* __restrict__ add,
+                            double* __restrict__ dst, size_t n, size_t total)
+{
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    dst[e] = src[e] + add[e % n];
+}
+
+void launch_add_table(const double* src, const double* add, double* dst, int B, size_t n, cudaStream_t s)
+{
+  k_add_table<<<1216, 256, 0, s>>>(src, add, dst, n, (size_t)B * n);
+}
+
 void launch_prep_consts(const Params& P, cudaStream_t s)
 {
   k_prep_consts<<<64, 256, 0, s>>>(P);

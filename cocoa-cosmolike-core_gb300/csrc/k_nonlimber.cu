@@ -734,7 +734,10 @@ __device__ __forceinline__ int slice_cell(const float* __restrict__ plk, int nk,
 // the b1-free galaxy term G0 and the bmag-free magnification term M0 of both
 // multipoles, and accumulates the P_lin slice adjoint, d/db1 and d/dbmag
 // from cbar = dL/dC_l instead of writing C_l.
-template <typename T, bool ADJ>
+// SMS: the CTA's spectra (3 kernels) and Gamma-recurrence state (3 kernels
+// x 2 multipoles) live in shared memory instead of global memory (L2): the
+// mixed plan when they fit beside the rest at two CTAs per SM.
+template <typename T, bool ADJ, bool SMS>
 __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
                                                       double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
 {
@@ -784,6 +787,14 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   const size_t cta = (size_t)pt * P.nl + q;
   const ct<T>* tout = (const ct<T>*)Q.tout + cta * Q.tout_stride;  // [3][hstride]
   ct<T>* gst = (ct<T>*)Q.gstate + cta * Q.gst_stride;              // [3][2][hstride]
+  if constexpr (SMS) {
+    // after the slice-cell table, 16-byte aligned: spectra [3][hstride],
+    // recurrence state [3][2][hstride]
+    ct<T>* tsm = (ct<T>*)(((uintptr_t)(lut + nl_lut_size(P.pkl_nk)) + 15) & ~(uintptr_t)15);
+    for (int i = tid; i < 3 * Q.hstride; i += nlt) tsm[i] = tout[i];
+    tout = tsm;
+    gst = tsm + 3 * Q.hstride;
+  }
   double* Cl = P.cnl + cta * LNL;
   const double* ggl = P.ggl + cta * LNL * 2;
   const double rc = geo.rc;
@@ -1228,7 +1239,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
 // where psl is the z = 0 slice of the linear table; the slice adjoint is
 // spread onto the table's two z columns at the end.
 template <typename T>
-static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
+static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj, bool sms = false)
 {
   const bool f32 = sizeof(T) == sizeof(float);
   size_t sm = sizeof(T) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi + P.pkl_nk) +
@@ -1238,7 +1249,21 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj)
   // the slice-cell table
   if (f32) sm += sizeof(float) * ((size_t)P.pkl_nk + P.nl_nchi) + sizeof(unsigned short) * nl_lut_size(P.pkl_nk);
   if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? 0 : sizeof(double) * (size_t)P.pkl_nk);
+  if (sms) sm += 2 * sizeof(T) * 9 * (size_t)Q.hstride + 16;
   return sm;
+}
+
+// the mixed plan keeps the spectra and the recurrence state in shared
+// memory, on request (CL2PT_FFTLOG_STATE_SHARED, or the autotuner's
+// choice), when two CTAs (of NL_NT threads) still fit an SM.  The default is
+// global memory: on GB300 at the real_3x2pt workload the four 128-thread
+// CTAs per SM of that form measured faster (8.8 vs 9.7 ms per 512 points).
+constexpr size_t NL_SMS_MAX = 113 * 1024;
+template <typename T>
+static bool nl_use_sms(const Params& P, const NLParams& Q, bool adj)
+{
+  return sizeof(T) == sizeof(float) && Q.state_mode == CL2PT_FFTLOG_STATE_SHARED &&
+         nl_loop_smem<T>(P, Q, adj, true) <= NL_SMS_MAX;
 }
 
 template <typename T>
@@ -1248,10 +1273,16 @@ static void launch_nl_vjp_t(const Params& P, const NLParams& Q, const double* cb
   const size_t sm1 = sizeof(double) * (2 * 2 * (size_t)Q.nmax + 3 * (size_t)P.nl_nchi) + 64;
   cudaFuncSetAttribute(k_nl_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_nl_forward<T><<<dim3(P.B, P.nl), NL_NT, sm1, s>>>(P, Q, 1, 0, 1);
-  const size_t sm = nl_loop_smem<T>(P, Q, true);
+  const bool sms = nl_use_sms<T>(P, Q, true);
+  const size_t sm = nl_loop_smem<T>(P, Q, true, sms);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
-  cudaFuncSetAttribute(k_nl_loop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_nl_loop<T, true><<<dim3(P.B, P.nl), nl_loop_threads(sm), sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+  if (sms) {
+    cudaFuncSetAttribute(k_nl_loop<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_nl_loop<T, true, true><<<dim3(P.B, P.nl), nl_loop_threads(sm), sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+  } else {
+    cudaFuncSetAttribute(k_nl_loop<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_nl_loop<T, true, false><<<dim3(P.B, P.nl), nl_loop_threads(sm), sm, s>>>(P, Q, cbar, lnpl_bar, nu_bar);
+  }
 }
 
 void launch_nonlimber_vjp(const Params& P, const NLParams& Q, const double* cbar, double* lnpl_bar,
@@ -1275,10 +1306,16 @@ static void launch_nl_prep_t(const Params& P, const NLParams& Q, cudaStream_t s)
 template <typename T>
 static void launch_nl_loop_t(const Params& P, const NLParams& Q, cudaStream_t s)
 {
-  const size_t sm3 = nl_loop_smem<T>(P, Q, false);
+  const bool sms = nl_use_sms<T>(P, Q, false);
+  const size_t sm3 = nl_loop_smem<T>(P, Q, false, sms);
   k_nl_order<<<1, 1024, 0, s>>>(P, Q);
-  cudaFuncSetAttribute(k_nl_loop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-  k_nl_loop<T, false><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+  if (sms) {
+    cudaFuncSetAttribute(k_nl_loop<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    k_nl_loop<T, false, true><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+  } else {
+    cudaFuncSetAttribute(k_nl_loop<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    k_nl_loop<T, false, false><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+  }
 }
 
 void launch_nonlimber_prep(const Params& P, const NLParams& Q, cudaStream_t s, int* launches, const Hook& hk)

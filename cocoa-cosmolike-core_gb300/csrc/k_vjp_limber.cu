@@ -29,6 +29,7 @@ namespace {
 
 constexpr int LC = 32;  // multipoles per shared-memory chunk
 constexpr int VJP_GG_S = 4;  // threads per node of the gg sweep
+constexpr int VJP_GG_NT = 384;  // k_vjp_gg threads per CTA at most (two CTAs per SM)
 constexpr int VJP_GS_S = 4;  // threads per node of the gs sweep
 
 template <typename T> __device__ __forceinline__ T t_exp(T x);
@@ -40,6 +41,10 @@ struct PWalk {
   int i = -1;       // current k cell
   T lo, d01, d10, d11, eh;
   T acc0 = 0, acc1 = 0;  // sum over the run of g (1 - dx), g dx
+  // mixed plan: the upper k row of the last flushed run, held back so that
+  // the next run (one cell up) adds into it before it is scattered
+  int prow = -1;
+  T pv = 0;
 };
 
 template <typename T>
@@ -58,18 +63,39 @@ __device__ __forceinline__ void pw_flush(PWalk<T>& w, double* __restrict__ bar, 
 
 // Mixed plan: the run sums are FP32, so their lerp weights are applied in
 // FP32 and the products reach the FP64 atomics by an integer conversion --
-// no FP64 arithmetic per flush (GB300 issues FP64 at 1/64 of the FP32 rate).
+// no FP64 arithmetic per flush (GB300 issues FP64 at 1/64 of the FP32
+// rate).  A run at cell i adds acc0 to k row i and acc1 to row i + 1; the
+// walks climb in k, so row i + 1 is held back (prow, pv) for the next run
+// and each row is scattered once: two atomics per run instead of four.
+__device__ __forceinline__ void pw_row(double* __restrict__ bar, int nz, int row, int j, float dyf, float v)
+{
+  if (v == 0.0f) return;
+  double* b = bar + (size_t)row * nz + j;
+  atomicAdd(b, f32_to_f64_int(v * (1.0f - dyf)));
+  atomicAdd(b + 1, f32_to_f64_int(v * dyf));
+}
 __device__ __forceinline__ void pw_flush(PWalk<float>& w, double* __restrict__ bar, int nz, int j, double dy)
 {
   if (w.i < 0 || (w.acc0 == 0.0f && w.acc1 == 0.0f)) return;
-  double* b0 = bar + (size_t)w.i * nz + j;
-  double* b1 = b0 + nz;
-  const float dyf = (float)dy, ody = 1.0f - dyf;
-  atomicAdd(b0, f32_to_f64_int(w.acc0 * ody));
-  atomicAdd(b0 + 1, f32_to_f64_int(w.acc0 * dyf));
-  atomicAdd(b1, f32_to_f64_int(w.acc1 * ody));
-  atomicAdd(b1 + 1, f32_to_f64_int(w.acc1 * dyf));
+  const float dyf = (float)dy;
+  float v = w.acc0;
+  if (w.prow == w.i) v += w.pv;
+  else if (w.prow >= 0) pw_row(bar, nz, w.prow, j, dyf, w.pv);
+  pw_row(bar, nz, w.i, j, dyf, v);
+  w.prow = w.i + 1;
+  w.pv = w.acc1;
   w.acc0 = w.acc1 = 0.0f;
+}
+// the end of a walk: its last run and the held-back row
+template <typename T>
+__device__ __forceinline__ void pw_finish(PWalk<T>& w, double* __restrict__ bar, int nz, int j, double dy)
+{
+  pw_flush(w, bar, nz, j, dy);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (w.prow >= 0) pw_row(bar, nz, w.prow, j, (float)dy, w.pv);
+    w.prow = -1;
+    w.pv = 0.0f;
+  }
 }
 
 // Accumulator of per-chunk partial sums: FP64 in the FP64 plan, an
@@ -407,7 +433,7 @@ __global__ void __launch_bounds__(SS_NT) k_vjp_ss(Params P, VJPParams V)
   }
   __syncthreads();
   if (tid >= nn) return;
-  pw_flush(wk, bar, P.pk_nz, nj[tid], ndy[tid]);
+  pw_finish(wk, bar, P.pk_nz, nj[tid], ndy[tid]);
   double* wb = V.wbar_ss + (size_t)pt * P.ns * nn;
   const double F = (double)nF[tid];
   for (int pr = 0; pr < np; pr++) {
@@ -597,7 +623,7 @@ __global__ void k_vjp_gs(Params P, VJPParams V)
       }
     }
   }
-  if (act) pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  if (act) pw_finish(wk, bar, P.pk_nz, nd.j, nd.dy);
   red[(0 * S + sub) * nx + p] = lb0.get();
   red[(1 * S + sub) * nx + p] = lb1.get();
   red[(2 * S + sub) * nx + p] = kbs.get();
@@ -666,13 +692,14 @@ __device__ __forceinline__ int first_kept(const double* fac, int n, double fK, d
 }
 
 template <typename T>
-__global__ void k_vjp_gg(Params P, VJPParams V)
+__global__ void __launch_bounds__(VJP_GG_NT, 2) k_vjp_gg(Params P, VJPParams V)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // blockDim (nodes, S): S threads per node, each on a contiguous part of
-  // the multipole range (the tables in shared memory are shared by all)
+  // the multipole range (the tables in shared memory are shared by all);
+  // node sets wider than blockDim.x are swept in turns
   const int pt = blockIdx.x, q = blockIdx.y;
-  const int p = threadIdx.x, sub = threadIdx.y, S = blockDim.y;
+  const int sub = threadIdx.y, S = blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
   const int nn = P.n_gg, K = P.nnode_g, LNL = P.lmax_nolimber;
   const int nk = P.pk_nk, nkl = P.pkl_nk;
@@ -735,7 +762,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
   if (nonlim)
     for (int i = tid; i < 2 * LNL; i += nth) gbs[i] = (T)V.ggl_bar[b0 * LNL * 2 + i];
   __syncthreads();
-  if (p >= nn) return;
+  for (int p = threadIdx.x; p < nn; p += blockDim.x) {
   const int off = P.n_ss + P.nl * P.n_ss + q * nn;
   const NodeD nd = node_d(P, pt, off + p);
   const T Ft = (T)nd.F, dyt = (T)nd.dy;
@@ -844,7 +871,7 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     kbar.add(kt);
     mbar.add(mt);
   }
-  pw_flush(wk, bar, P.pk_nz, nd.j, nd.dy);
+  pw_finish(wk, bar, P.pk_nz, nd.j, nd.dy);
   if (nonlim) {
     // integer l < LNL: nonlinear and linear Limber C_gg of the hand-over
     const double z = 1.0 / nd.a - 1.0;
@@ -900,13 +927,14 @@ __global__ void k_vjp_gg(Params P, VJPParams V)
     lbar.add(lt);
     kbar.add(kt);
     mbar.add(mt);
-    pw_flush(wn, bar, P.pk_nz, nd.j, nd.dy);
-    pw_flush(wl, barl, P.pkl_nz, jl, dyl);
+    pw_finish(wn, bar, P.pk_nz, nd.j, nd.dy);
+    pw_finish(wl, barl, P.pkl_nz, jl, dyl);
   }
   // zeroed per wave; S threads per node, and the Fourier path adds two passes
   atomicAdd(&V.lbar_gg[b0 * nn + p], lbar.get());
   if (kon) atomicAdd(&V.kbar_gg[b0 * nn + p], kbar.get());
   if (nu.gb[4][q] != 0.0) atomicAdd(&V.mbar_gg[b0 * nn + p], mbar.get());
+  }
 }
 
 template <typename T>
@@ -954,16 +982,12 @@ void launch_t(const Params& P, const VJPParams& V, int which, cudaStream_t s)
   } else {
     const size_t sm = gg_smem<T>(P);
     cudaFuncSetAttribute(k_vjp_gg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    // up to 4 threads per node: a CTA holds ~85 KB of tables, so two CTAs
-    // fit an SM; 4 x 96 threads each keep 24 warps resident instead of 6.
-    // S shrinks with the node count to the block's thread and register
-    // limits.
-    const int nx = ((P.n_gg + rnd - 1) / rnd) * rnd;
-    cudaFuncAttributes fa;
-    int cap = 1024;
-    if (cudaFuncGetAttributes(&fa, k_vjp_gg<T>) == cudaSuccess && fa.numRegs > 0)
-      cap = std::min(cap, std::min(fa.maxThreadsPerBlock, 65536 / fa.numRegs));
-    const int S = std::max(1, std::min(VJP_GG_S, cap / nx));
+    // up to 4 threads per node and at most VJP_GG_NT threads per CTA, so
+    // that two CTAs fit an SM by registers (the launch bound) and shared
+    // memory (~25 KB with the forward's stored s, ~85 KB without); wider
+    // node sets are swept in turns of 128 nodes
+    const int nx = std::min(((P.n_gg + rnd - 1) / rnd) * rnd, 128);
+    const int S = std::max(1, std::min(VJP_GG_S, VJP_GG_NT / nx));
     k_vjp_gg<T><<<dim3(P.B, P.nl), dim3(nx, S), sm, s>>>(P, V);
   }
 }

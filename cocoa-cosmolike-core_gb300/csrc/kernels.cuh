@@ -27,6 +27,9 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 void launch_check_finite(const double* x, size_t n, int* flag, cudaStream_t s);
 // mixed plan: split the wave's lnP (and separate lnPL) into P.lnP2 / P.lnPL2
 void launch_split_tables(const Params& P, cudaStream_t s, int* launches);
+// dst[pt][e] = src[pt][e] + add[e] for B points of n entries (the baryon
+// ratio on the wave's nonlinear table)
+void launch_add_table(const double* src, const double* add, double* dst, int B, size_t n, cudaStream_t s);
 // the mixed plan's FP32 axis and lens-spline constants (Params::axk, axkl,
 // lensf), once when the plan is made
 void launch_prep_consts(const Params& P, cudaStream_t s);

@@ -63,6 +63,7 @@ struct NLParams {
   const double* gtab;
   double gtab_inv_h;
   int gtab_m;
+  int state_mode;   // CL2PT_FFTLOG_STATE_*: where the loop keeps its spectra and state
 };
 
 // Host: the tables of NLParams::gtab for the kernels' nu and derivative

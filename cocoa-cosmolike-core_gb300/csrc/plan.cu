@@ -721,6 +721,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
       TRY(dalloc(p, &P.wgg_1l, (size_t)W * nl * 6 * p->n_gg));
       TRY(dalloc(p, &P.wgs_bk, (size_t)W * nl * p->n_ss));
       TRY(dalloc(p, &P.wgg_bk, (size_t)W * nl * p->n_gg));
+      if (precision != CL2PT_PREC_FP64) TRY(dalloc(p, &P.fpt_gga, (size_t)W * nl * p->n_gg * nf));
     }
     if (P.tatt) {
       TRY(cl2pt_fastpt_ia_plan_create(kx.data(), nf, &fc, W, &p->fpt_ia));
@@ -970,10 +971,61 @@ extern "C" int cl2pt_plan_set_d1p3(cl2pt_plan* p, const double* p_d1p3, int n)
   return CL2PT_OK;
 }
 
+extern "C" int cl2pt_plan_set_baryon_ratio(cl2pt_plan* p, int nk, const double* lk, int na, const double* a,
+                                           const double* lr)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (nk == 0) {
+    p->bary_on = false;
+    return CL2PT_OK;
+  }
+  if (nk < 2 || na < 2 || !lk || !a || !lr) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nk; i++)
+    if (!std::isfinite(lk[i]) || (i && !(lk[i] > lk[i - 1]))) return CL2PT_ERR_ARG;
+  for (int j = 0; j < na; j++)
+    if (!std::isfinite(a[j]) || (j && !(a[j] > a[j - 1]))) return CL2PT_ERR_ARG;
+  for (size_t e = 0; e < (size_t)nk * na; e++)
+    if (!std::isfinite(lr[e])) return CL2PT_ERR_ARG;
+  auto bs = [](const double* x, int n, double v) {
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+      const int mid = (lo + hi) >> 1;
+      if (x[mid] > v) hi = mid; else lo = mid;
+    }
+    return lo;
+  };
+  const int nkp = (int)p->pk_lk.size(), nzp = (int)p->pk_z.size();
+  std::vector<double> lnr((size_t)nkp * nzp);
+  for (int i = 0; i < nkp; i++)
+    for (int j = 0; j < nzp; j++) {
+      const double x = p->pk_lk[i], av = 1.0 / (1.0 + p->pk_z[j]);
+      const int xi = bs(lk, nk, x), yi = bs(a, na, av);
+      const double t = (x - lk[xi]) / (lk[xi + 1] - lk[xi]);
+      const double u = (av - a[yi]) / (a[yi + 1] - a[yi]);
+      const double r = (1 - t) * (1 - u) * lr[(size_t)yi * nk + xi] + t * (1 - u) * lr[(size_t)yi * nk + xi + 1] +
+                       (1 - t) * u * lr[(size_t)(yi + 1) * nk + xi] + t * u * lr[(size_t)(yi + 1) * nk + xi + 1];
+      lnr[(size_t)i * nzp + j] = r * M_LN10;
+    }
+  if (!p->d_bary_lnr) {
+    if (int st = dalloc(p, &p->d_bary_lnr, lnr.size())) return st;
+    if (int st = dalloc(p, &p->d_lnP_bary, (size_t)p->wave * lnr.size())) return st;
+  }
+  CUDA_OK(cudaMemcpy(p->d_bary_lnr, lnr.data(), sizeof(double) * lnr.size(), cudaMemcpyHostToDevice));
+  p->bary_on = true;
+  return CL2PT_OK;
+}
+
 extern "C" int cl2pt_plan_get_contraction(const cl2pt_plan* p, int* mode)
 {
   if (!p || !mode) return CL2PT_ERR_ARG;
   *mode = p->contract;
+  return CL2PT_OK;
+}
+
+extern "C" int cl2pt_plan_set_fftlog_state(cl2pt_plan* p, int mode)
+{
+  if (!p || mode < CL2PT_FFTLOG_STATE_AUTO || mode > CL2PT_FFTLOG_STATE_SHARED) return CL2PT_ERR_ARG;
+  p->nlq.state_mode = mode;
   return CL2PT_OK;
 }
 
@@ -1092,6 +1144,65 @@ extern "C" int cl2pt_eval_real(cl2pt_plan* p, const cl2pt_batch* b, const int* m
   int st = check_batch(p, b);
   if (st) return st;
   return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int cl2pt_plan_autotune(cl2pt_plan* p, const cl2pt_batch* b, void* stream, int reps, int* contract,
+                                   int* fftlog_state, double* best_ms)
+{
+  if (!p || !b || b->where != CL2PT_DEVICE || reps < 1) return CL2PT_ERR_ARG;
+  if (p->prec != CL2PT_PREC_MIXED) return CL2PT_ERR_UNSUPPORTED;
+  int st = check_batch(p, b);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* dv = nullptr;
+  CUDA_OK(cudaMalloc((void**)&dv, sizeof(double) * (size_t)b->n * p->n_total));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int forms[3] = {CL2PT_CONTRACT_TF32X3, CL2PT_CONTRACT_BF16X6, CL2PT_CONTRACT_FP32};
+  const int states[2] = {CL2PT_FFTLOG_STATE_SHARED, CL2PT_FFTLOG_STATE_GLOBAL};
+  const int c0 = p->contract, s0 = p->nlq.state_mode;
+  int bc = c0, bs = s0;
+  float best = -1.0f;
+  for (int f : forms) {
+    if (cl2pt_plan_set_contraction(p, f) != CL2PT_OK) continue;  // filters beyond the tensor-core tiles
+    for (int sm : states) {
+      p->nlq.state_mode = sm;
+      st = internal_eval(p, b, nullptr, nullptr, dv, s, nullptr);  // warm-up (attributes, maps)
+      if (st) break;
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && !st; r++) st = internal_eval(p, b, nullptr, nullptr, dv, s, nullptr);
+      cudaEventRecord(e1, s);
+      if (st) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        st = CL2PT_ERR_CUDA;
+        break;
+      }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (best < 0.0f || ms < best) {
+        best = ms;
+        bc = f;
+        bs = sm;
+      }
+    }
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(dv);
+  if (st || best < 0.0f) {
+    cl2pt_plan_set_contraction(p, c0);
+    p->nlq.state_mode = s0;
+    return st ? st : CL2PT_ERR_CUDA;
+  }
+  cl2pt_plan_set_contraction(p, bc);
+  p->nlq.state_mode = bs;
+  if (contract) *contract = bc;
+  if (fftlog_state) *fftlog_state = bs;
+  if (best_ms) *best_ms = best;
+  return CL2PT_OK;
 }
 
 extern "C" int cl2pt_fourier_sizes(const cl2pt_plan* p, int nell, int* n_ss, int* n_gs, int* n_gg,
@@ -1524,35 +1635,21 @@ struct cl2pt_graph {
   int launches = 0;
 };
 
-extern "C" int cl2pt_fourier_graph_create(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
-                                          double lmax_shear, const int* mask, const int* row_ptr,
-                                          const int* idx, double* dv, void* stream, cl2pt_graph** out)
+// Capture one evaluation (real space: fr == nullptr) as a graph: one eager
+// evaluation first (uploads, kernel attributes, lazily allocated staging),
+// then the same call under stream capture.
+static int graph_capture(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm, double* full,
+                         cudaStream_t s, FourierReq* fr, cl2pt_graph** out)
 {
-  if (!p || !b || !out || !dv || !stream || b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
-  if ((row_ptr == nullptr) != (idx == nullptr)) return CL2PT_ERR_ARG;
-  int st = check_batch(p, b);
-  if (st) return st;
-  if (!ell || nell < 1 || nell > std::min(p->nnode_ss, p->nnode_g)) return CL2PT_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  FourierReq fr;
-  fr.nell = nell;
-  fr.ell = ell;
-  fr.lmax_shear = lmax_shear;
-  fr.csr_ptr = row_ptr;
-  fr.csr_idx = idx;
-  fr.csr_out = row_ptr ? dv : nullptr;
-  double* full = row_ptr ? nullptr : dv;
-  // one eager evaluation: uploads the multipoles, sets kernel attributes and
-  // allocates the staging the captured launches use
-  st = internal_eval(p, b, mask, nullptr, full, s, &fr);
+  int st = internal_eval(p, b, mask, pm, full, s, fr);
   if (st) return st;
   CUDA_OK(cudaStreamSynchronize(s));
-  fr.ell_on_device = true;
+  if (fr) fr->ell_on_device = true;
   const bool timing = p->timing;
   p->timing = false;
   cl2pt_graph* G = new cl2pt_graph();
   CUDA_OK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  st = internal_eval(p, b, mask, nullptr, full, s, &fr);
+  st = internal_eval(p, b, mask, pm, full, s, fr);
   const cudaError_t ec = cudaStreamEndCapture(s, &G->g);
   p->timing = timing;
   if (st || ec != cudaSuccess) {
@@ -1569,6 +1666,34 @@ extern "C" int cl2pt_fourier_graph_create(cl2pt_plan* p, const cl2pt_batch* b, i
   }
   *out = G;
   return CL2PT_OK;
+}
+
+extern "C" int cl2pt_fourier_graph_create(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell,
+                                          double lmax_shear, const int* mask, const int* row_ptr,
+                                          const int* idx, double* dv, void* stream, cl2pt_graph** out)
+{
+  if (!p || !b || !out || !dv || !stream || b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
+  if ((row_ptr == nullptr) != (idx == nullptr)) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  if (!ell || nell < 1 || nell > std::min(p->nnode_ss, p->nnode_g)) return CL2PT_ERR_ARG;
+  FourierReq fr;
+  fr.nell = nell;
+  fr.ell = ell;
+  fr.lmax_shear = lmax_shear;
+  fr.csr_ptr = row_ptr;
+  fr.csr_idx = idx;
+  fr.csr_out = row_ptr ? dv : nullptr;
+  return graph_capture(p, b, mask, nullptr, row_ptr ? nullptr : dv, (cudaStream_t)stream, &fr, out);
+}
+
+extern "C" int cl2pt_real_graph_create(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
+                                       double* dv, void* stream, cl2pt_graph** out)
+{
+  if (!p || !b || !out || !dv || !stream || b->where != CL2PT_DEVICE) return CL2PT_ERR_ARG;
+  int st = check_batch(p, b);
+  if (st) return st;
+  return graph_capture(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, out);
 }
 
 extern "C" int cl2pt_graph_launch(cl2pt_graph* g, void* stream)
@@ -1876,6 +2001,13 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     P.G = G + (size_t)w0 * nG;
     P.lnP = lnP + (size_t)w0 * nP;
     P.lnPL = lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    if (p->bary_on) {
+      // p_nonlin x the baryon ratio: the wave's nonlinear table plus ln R
+      // (the linear table stays the caller's)
+      cl2pt::launch_add_table(P.lnP, p->d_bary_lnr, p->d_lnP_bary, P.B, nP, s);
+      P.lnP = p->d_lnP_bary;
+      launches++;
+    }
     P.nu = nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
     if (P.prec != CL2PT_PREC_FP64) {

@@ -100,6 +100,11 @@ struct cl2pt_plan {
   double* d_vjp_ws = nullptr;          // obs_bar, C_l adjoints, node-weight adjoints
   double* d_vjp_fpt = nullptr;         // FAST-PT tables' share (TATT / one-loop plans)
   double* d_fpt_d1p3 = nullptr;        // the caller's P_d1p3 on the FAST-PT grid
+  // baryon P(k) ratio (cl2pt_plan_set_baryon_ratio): ln R on the lnP table's
+  // grid [pk_nk * pk_nz], and the wave's nonlinear table with it [wave][..]
+  double* d_bary_lnr = nullptr;
+  double* d_lnP_bary = nullptr;
+  bool bary_on = false;
   double* d_vjp_cot = nullptr;         // [max_batch][n_total] (grown for Fourier vectors)
   size_t vjp_cot_cap = 0;
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]

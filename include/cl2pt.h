@@ -144,6 +144,13 @@ int cl2pt_fourier_graph_create(cl2pt_plan* plan, const cl2pt_batch* batch, int n
                                const double* ell, double lmax_shear, const int* mask,
                                const int* row_ptr, const int* idx, double* dv,
                                void* stream, cl2pt_graph** graph);
+/* The real-space evaluation (cl2pt_eval_real on device buffers: batch->where
+ * == CL2PT_DEVICE, device mask / point masses or NULL, dv [n][n_total])
+ * captured the same way: one graph of the whole multi-stream pipeline
+ * (set-up, Limber, FFTLog on a second stream, contraction, assembly) per
+ * batch shape, replayed with cl2pt_graph_launch. */
+int cl2pt_real_graph_create(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
+                            const double* pm, double* dv, void* stream, cl2pt_graph** graph);
 int cl2pt_graph_launch(cl2pt_graph* graph, void* stream);
 /* Kernel launches one replay performs. */
 int cl2pt_graph_launch_count(const cl2pt_graph* graph);
@@ -299,6 +306,20 @@ int cl2pt_last_launch_count(const cl2pt_plan* plan);
  * without one-loop terms. */
 int cl2pt_plan_set_d1p3(cl2pt_plan* plan, const double* p_d1p3, int n);
 
+/* The baryon-contamination P(k) ratio (PkRatio_baryons, cosmolike/
+ * cosmo3D.c:481-499): p_nonlin is multiplied by 10^r(log10 k, a), r the
+ * bilinear interpolation (extrapolated from the edge cells, as
+ * gsl_interp2d_eval_extrap with gsl_interp2d_bilinear) of log10r[j * nk + i]
+ * on the axes log10k[nk] (k in h/Mpc, increasing) and a[na] (increasing).
+ * The plan evaluates ln R once on the nonlinear table's own (log10 k, z)
+ * grid and adds it to each wave's copy of that table, so the Limber
+ * interpolation of the sum stands for the reference's product of two
+ * interpolations (the difference is second order in the table spacing);
+ * p_lin is untouched, and d/dlnP passes through unchanged.  nk = 0 turns the
+ * ratio off. */
+int cl2pt_plan_set_baryon_ratio(cl2pt_plan* plan, int nk, const double* log10k, int na, const double* a,
+                                const double* log10r);
+
 /* Select the Legendre contraction of a mixed plan (CL2PT_CONTRACT_*; the
  * reference's xi_pm_tomo / w_gammat_tomo / w_gg_tomo sums,
  * cosmo2D.c:500-534, 680-699, 859-878).  The tensor-core forms need at
@@ -309,6 +330,25 @@ int cl2pt_plan_set_d1p3(cl2pt_plan* plan, const double* p_d1p3, int n);
  * CL2PT_CONTRACT_FP32 otherwise. */
 int cl2pt_plan_set_contraction(cl2pt_plan* plan, int mode);
 int cl2pt_plan_get_contraction(const cl2pt_plan* plan, int* mode);
+
+/* Where the mixed plan's FFTLog multipole loop keeps its spectra and
+ * Gamma-recurrence state: CL2PT_FFTLOG_STATE_AUTO (the default: global
+ * memory, unless cl2pt_plan_autotune chose otherwise), _GLOBAL (global
+ * memory, four 128-thread CTAs per SM) or _SHARED (shared memory, two
+ * 256-thread CTAs per SM, when it fits; else global). */
+enum { CL2PT_FFTLOG_STATE_AUTO = 0, CL2PT_FFTLOG_STATE_GLOBAL = 1, CL2PT_FFTLOG_STATE_SHARED = 2 };
+int cl2pt_plan_set_fftlog_state(cl2pt_plan* plan, int mode);
+
+/* The plan's own autotuner: times cl2pt_eval_real on the caller's batch
+ * (device buffers, batch->where == CL2PT_DEVICE) for every candidate
+ * configuration -- the contraction forms TF32x3, BF16x6 and FP32 (all within
+ * the 1e-4 bar) times the two FFTLog state placements -- with one warm-up and
+ * reps timed evaluations each (CUDA events on the given stream), keeps the
+ * fastest, and returns it (contract, fftlog_state; either may be NULL) and
+ * its time per evaluation in ms (best_ms, may be NULL).  Mixed plans only
+ * (CL2PT_ERR_UNSUPPORTED otherwise). */
+int cl2pt_plan_autotune(cl2pt_plan* plan, const cl2pt_batch* batch, void* stream, int reps, int* contract,
+                        int* fftlog_state, double* best_ms);
 
 /* The C_l node grids of the plan: nodes nint .. of the ss (gs, gg) tables
  * sit at l = exp(lim[0] + i lim[2]), lim[1] = ln of the last node

@@ -81,6 +81,9 @@ static struct {
   double* d1d3;
   int d1d3_n;
   double d1d3_lnkmin, d1d3_lnkmax;
+  /* baryon P(k) ratio (bary.*, baryons.c): log10 ratio on (log10 k [h/Mpc], a) */
+  int bary_nk, bary_na;
+  double *bary_lk, *bary_a, *bary_lr; /* lr[j * nk + i] */
 } g;
 
 /* ------------------------------------------------------------------------ */
@@ -349,9 +352,26 @@ static double p_lin(double k, double a)
 {
   return pk_table(k, a, g.pkl_nk, g.pkl_nz, g.pkl_lk, g.pkl_z, g.lnPL);
 }
+/* PkRatio_baryons (cosmo3D.c:481-499): 10^(bilinear interpolation of the
+ * log10 ratio at (log10(k / coverH0), a)), extrapolated from the edge cells
+ * (gsl_interp2d_eval_extrap with gsl_interp2d_bilinear; z[j * nk + i]) */
+static double pk_ratio_baryons(double k, double a)
+{
+  const double x = log10(k / COVERH0);
+  const int i = num_bsearch(g.bary_lk, g.bary_nk, x);
+  const int j = num_bsearch(g.bary_a, g.bary_na, a);
+  const double t = (x - g.bary_lk[i]) / (g.bary_lk[i + 1] - g.bary_lk[i]);
+  const double u = (a - g.bary_a[j]) / (g.bary_a[j + 1] - g.bary_a[j]);
+  const int nk = g.bary_nk;
+  const double r = (1 - t) * (1 - u) * g.bary_lr[j * nk + i] + t * (1 - u) * g.bary_lr[j * nk + i + 1] +
+                   (1 - t) * u * g.bary_lr[(j + 1) * nk + i] + t * u * g.bary_lr[(j + 1) * nk + i + 1];
+  return pow(10.0, r);
+}
+/* p_nonlin (cosmo3D.c:362-417): the table, times the baryon ratio when set */
 double orc_p_nonlin(double k, double a)
 {
-  return pk_table(k, a, g.pk_nk, g.pk_nz, g.pk_lk, g.pk_z, g.lnP);
+  const double ans = pk_table(k, a, g.pk_nk, g.pk_nz, g.pk_lk, g.pk_z, g.lnP);
+  return g.bary_nk ? ans * pk_ratio_baryons(k, a) : ans;
 }
 /* Pdelta: cosmo3D.c:424-445 */
 static double Pdelta(double k, double a)
@@ -1630,6 +1650,24 @@ int orc_set_point(const cl2pt_cosmo* c, const cl2pt_nuisance* nu)
   g.nu = *nu;
   g.oneplusz0_ia = (g.cfg.ia_mode == CL2PT_IA_REDSHIFT_EVOLUTION) ? 1.62 : 0.0;
   g.have_point = 1;
+  invalidate_point();
+  return CL2PT_OK;
+}
+
+int orc_set_baryon_ratio(int nk, const double* log10k, int na, const double* a, const double* log10r)
+{
+  free(g.bary_lk);
+  free(g.bary_a);
+  free(g.bary_lr);
+  g.bary_lk = g.bary_a = g.bary_lr = NULL;
+  g.bary_nk = g.bary_na = 0;
+  if (nk >= 2 && na >= 2) {
+    g.bary_lk = dup(log10k, nk);
+    g.bary_a = dup(a, na);
+    g.bary_lr = dup(log10r, (size_t)nk * na);
+    g.bary_nk = nk;
+    g.bary_na = na;
+  }
   invalidate_point();
   return CL2PT_OK;
 }

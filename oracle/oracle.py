@@ -204,6 +204,17 @@ class Oracle:
         f.argtypes = [_dp, C.c_int, C.c_double, C.c_double]
         return f(_p(t), len(t), lnkmin, lnkmax)
 
+    def set_baryon_ratio(self, log10k, a, log10r):
+        """The baryon P(k) ratio applied to p_nonlin (PkRatio_baryons): log10
+        ratio [len(a)][len(log10k)] on log10 k (h/Mpc) x a; empty: off."""
+        lk = np.ascontiguousarray(log10k, dtype=np.float64)
+        av = np.ascontiguousarray(a, dtype=np.float64)
+        lr = np.ascontiguousarray(log10r, dtype=np.float64)
+        self._keep += [lk, av, lr]
+        f = getattr(self.lib, self.which + "_set_baryon_ratio")
+        f.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp]
+        return f(len(lk), _p(lk), len(av), _p(av), _p(lr))
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

@@ -77,9 +77,10 @@ def blocks(plan, dv):
 
 
 def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=None, bmag=False,
-             contract=None, d1p3=None):
+             contract=None, d1p3=None, baryon=None):
     """d1p3: a P_d1p3 table on the FAST-PT grid for the one-loop b3 terms,
-    given to both the plan and the oracle."""
+    given to both the plan and the oracle; baryon: (log10 k, a, log10 R) of a
+    baryon P(k) ratio, likewise."""
     import oracle as O
     w = workloads.make(name)
     if tweak is not None:
@@ -93,12 +94,16 @@ def run_case(name, npts, prec, seed=1, check_tables=True, tweak=None, nu_tweak=N
         plan.set_contraction(contract)
     if d1p3 is not None:
         plan.set_d1p3(d1p3)
+    if baryon is not None:
+        plan.set_baryon_ratio(*baryon)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=workloads.stack_lin(tabs))
     o = O.Oracle("orc")
     o.setup(w.cfg, w.src, w.lens)
     if d1p3 is not None:
         o.set_d1d3_table(d1p3, np.log(0.05), np.log(1e6))
+    if baryon is not None:
+        o.set_baryon_ratio(*baryon)
     worst = {}
     nint = w.cfg.lmin_tab - 1
     tatt = w.cfg.ia_model == abi.IA_TATT
@@ -251,6 +256,41 @@ def test_b3_needs_d1p3(gpu_lib):
         plan.eval_real(om, h0, chi, G, lnP, nus)
     plan.set_d1p3(reference_d1p3())
     assert np.all(np.isfinite(plan.eval_real(om, h0, chi, G, lnP, nus)))
+
+
+def baryon_table():
+    """A smooth hydro-like suppression of P(k): up to -25 % at high k, weaker
+    at high z, on a coarse (log10 k [h/Mpc], a) grid that the lnP tables'
+    range exceeds on both sides (the edge cells extrapolate)."""
+    lk = np.linspace(-2.5, 1.5, 41)
+    a = np.linspace(0.25, 1.0, 16)
+    x = 0.5 * (1.0 + np.tanh((lk - 0.2) / 0.35))
+    lr = np.log10(1.0 - 0.25 * x[None, :] * a[:, None] ** 0.7) + 0.01 * np.sin(3.0 * lk)[None, :]
+    return lk, a, lr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_baryon_ratio(gpu_lib, oracle_built, prec):
+    """p_nonlin times a baryon P(k) ratio (PkRatio_baryons): the data vector
+    and the C_l node tables against the oracle, which applies the ratio per
+    evaluation as the reference does (the plan folds ln R into its copy of
+    the nonlinear table on the table's own grid)."""
+    worst, plan = run_case("real_3x2pt_small", 2, prec, seed=31, baryon=baryon_table())
+    print(prec, worst)
+    for k, v in worst.items():
+        assert v <= REL, (k, v, worst)
+    # the ratio matters, and turning it off restores the plain vector
+    w = workloads.make("real_3x2pt_small")
+    tabs, nus = workloads.points(w, 2, seed=31)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    lnPL = workloads.stack_lin(tabs)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=lnPL)
+    plan.set_baryon_ratio([], [], [])
+    dv0 = plan.eval_real(om, h0, chi, G, lnP, nus, lnPL=lnPL)
+    assert np.max(np.abs(dv - dv0) / np.maximum(np.abs(dv0), 1e-300)) > 1e-2
+    p0 = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2, linear_table=True)
+    assert np.array_equal(dv0, p0.eval_real(om, h0, chi, G, lnP, nus, lnPL=lnPL))
 
 
 @pytest.mark.gpu
