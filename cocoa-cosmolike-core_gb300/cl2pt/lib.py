@@ -97,6 +97,9 @@ def load(path: str = LIB_PATH):
                                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.POINTER(C.c_void_p)]
     lib.cl2pt_plan_set_fftlog_state.argtypes = [C.c_void_p, C.c_int]
+    lib.cl2pt_scut_ss_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_int, _dp, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+    lib.cl2pt_scut_ss_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
     lib.cl2pt_plan_set_baryon_ratio.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp]
     lib.cl2pt_plan_autotune.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_int, _ip, _ip,
                                         C.POINTER(C.c_double)]
@@ -186,6 +189,8 @@ class Plan:
         sz = [C.c_int() for _ in range(4)]
         check(lib.cl2pt_real_sizes(h, *[C.byref(s) for s in sz]))
         self.n_xi, self.n_gammat, self.n_w, self.n_total = (s.value for s in sz)
+        ns = cfg.n_source
+        self.pss = ns * (ns + 1) // 2  # shear pairs (N_shear order)
 
     def set_contraction(self, mode: int):
         """CONTRACT_FP32 (CUDA cores) or a tensor-core form (CONTRACT_TF32X3,
@@ -215,6 +220,43 @@ class Plan:
             pass
 
     # -------------------------------------------------------------- host
+    def _host_batch(self, omega_m, h0, chi, G, lnP, nuisance, lnPL=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (omega_m, h0, chi, G, lnP)]
+        lpl = None if lnPL is None else np.ascontiguousarray(lnPL, dtype=np.float64)
+        n = arrs[0].shape[0]
+        nus = (abi.Nuisance * n)(*nuisance)
+        b = Batch()
+        b.n, b.where = n, HOST
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (_p(a) for a in arrs)
+        b.lnPL = _p(lpl) if lpl is not None else None
+        b.nuisance = nus
+        return b, (arrs, lpl, nus)
+
+    def scut_ss_dlnk(self, omega_m, h0, chi, G, lnP, nuisance, k, l, lnPL=None):
+        """Scale-cut diagnostics of C_ss (cl2pt_scut_ss_dlnk): dC/dlnk and
+        dlnC/dlnk [n][2][pss][len(k)][len(l)], k in h/Mpc."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        l = np.ascontiguousarray(l, dtype=np.float64)
+        n = b.n
+        dC = np.zeros((n, 2, self.pss, len(k), len(l)))
+        dlnC = np.zeros_like(dC)
+        check(load().cl2pt_scut_ss_dlnk(self.h, C.byref(b), len(k), _p(k), len(l), _p(l), dC.ctypes.data,
+                                        dlnC.ctypes.data, None), "cl2pt_scut_ss_dlnk")
+        return dC, dlnC
+
+    def scut_ss_rf(self, omega_m, h0, chi, G, lnP, nuisance, kmax, l, lnPL=None):
+        """RF_C_ss at the requests (kmax[i], l[i]) (cl2pt_scut_ss_rf):
+        [n][2][pss][len(kmax)]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        kmax = np.ascontiguousarray(kmax, dtype=np.float64)
+        l = np.ascontiguousarray(l, dtype=np.float64)
+        assert len(kmax) == len(l)
+        rf = np.zeros((b.n, 2, self.pss, len(kmax)))
+        check(load().cl2pt_scut_ss_rf(self.h, C.byref(b), len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
+              "cl2pt_scut_ss_rf")
+        return rf
+
     def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None, out=None):
         """Host arrays in, host data vectors out ([n][n_total]); out: an
         optional C-contiguous float64 host array of that shape (e.g. pinned)

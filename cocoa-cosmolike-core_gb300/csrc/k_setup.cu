@@ -12,6 +12,8 @@
 //            weights the Limber integrands need (radial_weights.c:15-105,
 //            bias.c:17-210, IA.c:238-415), for the ss node set and the gs/gg
 //            node sets of every lens bin: one CTA per (point, node set).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -546,6 +548,147 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
   k_nodes<<<g2, ND_NT, 0, s>>>(P);
   hk(CL2PT_K_NODES, 0);
   *launches += 2;
+}
+
+// ---- scale-cut diagnostics of the cosmic-shear C_l (cosmolike/
+// cosmo2D_scuts.c), FP64, for the plans without TATT: the C_ss integrand
+// (int_for_C_ss_tomo_limber, cosmo2D.c:1521-1556) at any a, in its C_l form
+// (dchida / fK^2) or its dC/dlnk form (dchida / fK, cosmo2D.c:1509-1514);
+// no B modes without TATT.
+__device__ double ss_integrand_d(const Params& P, int pt, double a, double l, int n1, int n2, int EE, bool deriv)
+{
+  if (!EE) return 0.0;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double om = P.omega_m[pt];
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
+  const double ell = l + 0.5;
+  const Chis c = chi_all_d(P.chi_z, X, P.chi_nz, a);
+  const double fK = c.chi;
+  const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+  const double hh = 1.0 / ((a * a) * c.dchida);
+  const double k = ell / fK;
+  const double PK = P.linear_pk
+                        ? pk_d(P.pkl_lk, P.pkl_nk, P.pkl_z, P.pkl_nz, P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz, k, a)
+                        : pk_d(P.pk_lk, P.pk_nk, P.pk_z, P.pk_nz, P.lnP + (size_t)pt * P.pk_nk * P.pk_nz, k, a);
+  const double pref = l * (l - 1.) * (l + 1.) * (l + 2.) / (ell * ell * ell * ell);
+  const double* gsrc = P.gsrc + (size_t)pt * P.ns * P.n_a;
+  const double amin_src = 1.0 / (P.src_zmax_all + 1.0);
+  const double pre = 1.5 * om * fK / a;
+  const double WK1 = pre * g_lookup(gsrc + n1 * P.n_a, P.n_a, amin_src, a, true);
+  const double WK2 = pre * g_lookup(gsrc + n2 * P.n_a, P.n_a, amin_src, a, true);
+  const double z = 1.0 / a - 1.0;
+  const double WS1 = nz_source_d(P, z, n1, nu.src_dz[n1]) * hh;
+  const double WS2 = nz_source_d(P, z, n2, nu.src_dz[n2]) * hh;
+  const double C11 = ia_a1(P, nu, om, a, D, n1), C12 = ia_a1(P, nu, om, a, D, n2);
+  const double ans = WK1 * WK2 * PK - WS1 * WK2 * C11 * PK - WS2 * WK1 * C12 * PK + WS1 * WS2 * C11 * C12 * PK;
+  return deriv ? ans * (c.dchida / fK) * pref : ans * (c.dchida / (fK * fK)) * pref;
+}
+
+// dC_ss_dlnk_tomo_limber_nointerp (cosmo2D_scuts.c:42-74): the dC/dlnk
+// integrand at chi(a) = (l + 1/2) / k (k in h/Mpc), 0 outside the sources'
+// range
+__device__ double dCss_dlnk_d(const Params& P, int pt, double k, double l, int n1, int n2, int EE)
+{
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double a = a_chi_d(P.chi_z, X, P.chi_nz, (l + 0.5) / (k * CL2PT_COVERH0));
+  const double amin = 1. / (P.src_zmax_all + 1.);
+  const double amax = 1. / (1. + fmax(P.src_zmin_all, 1e-6));
+  return (a > amin && a < amax) ? ss_integrand_d(P, pt, a, l, n1, n2, EE, true) : 0.0;
+}
+
+// C_ss_tomo_limber_nointerp (cosmo2D.c:1562-1604) at the multipoles l[0..nl):
+// the Gauss-Legendre sum over the point's ss node set; out [B][pss][2][nl]
+// (EE, BB).  One CTA per (point, pair), threads over the multipoles.
+__global__ void k_scut_css(Params P, int nl, const double* __restrict__ l, double* __restrict__ out)
+{
+  const int pt = blockIdx.x, pr = blockIdx.y;
+  const int n1 = P.z1[pr], n2 = P.z2[pr];
+  const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
+  for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+    double s = 0.0;
+    for (int p = 0; p < P.n_ss; p++)
+      s += node[(size_t)NF_WT * P.node_stride + p] *
+           ss_integrand_d(P, pt, node[(size_t)NF_A * P.node_stride + p], l[i], n1, n2, 1, false);
+    double* o = out + (((size_t)pt * P.pss + pr) * 2) * nl;
+    o[i] = s;
+    o[nl + i] = 0.0;
+  }
+}
+
+// dC/dlnk and dlnC/dlnk = dC / C (the nointerp branch of int_RF_C_ss,
+// cosmo2D_scuts.c:257-284) on the grid k[0..nk) x l[0..nl); dC, dlnC
+// [B][2][pss][nk][nl] (either may be null); css from k_scut_css.
+__global__ void k_scut_dlnk(Params P, int nk, const double* __restrict__ k, int nl, const double* __restrict__ l,
+                            const double* __restrict__ css, double* __restrict__ dC, double* __restrict__ dlnC)
+{
+  const int pt = blockIdx.x, pr = blockIdx.y % P.pss, e = blockIdx.y / P.pss;  // e: 0 EE, 1 BB
+  const int n1 = P.z1[pr], n2 = P.z2[pr];
+  for (int idx = blockIdx.z * blockDim.x + threadIdx.x; idx < nk * nl; idx += gridDim.z * blockDim.x) {
+    const int ik = idx / nl, il = idx - ik * nl;
+    const double d = dCss_dlnk_d(P, pt, k[ik], l[il], n1, n2, e == 0);
+    const size_t o = (((size_t)pt * 2 + e) * P.pss + pr) * (size_t)nk * nl + idx;
+    if (dC) dC[o] = d;
+    if (dlnC) {
+      const double C = (fabs(d) > 1e-30) ? css[(((size_t)pt * P.pss + pr) * 2 + e) * nl + il] : 1.0;
+      dlnC[o] = (fabs(C) > 1e-30) ? d / C : 0.0;
+    }
+  }
+}
+
+// RF_C_ss_tomo_limber_nointerp (cosmo2D_scuts.c:329-375) for the requests
+// (kmax[i], l[i]): the fraction of int |dlnC/dlnk| dlnk below ln kmax, as
+// Gauss-Legendre sums over t in [1e-5, 1] (tx, tw: the caller's rule, 256
+// nodes at high_def_integration 0) with ln k = ln kmax - (1 - t)/t and
+// +-(1 - t)/t; rf [B][2][pss][nreq]; css from k_scut_css at the requests'
+// multipoles.  One warp per (point, EE/BB, pair, request).
+__global__ void k_scut_rf(Params P, int nreq, const double* __restrict__ kmax, const double* __restrict__ l,
+                          int nt, const double* __restrict__ tx, const double* __restrict__ tw,
+                          const double* __restrict__ css, double* __restrict__ rf)
+{
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int total = P.B * 2 * P.pss * nreq;
+  if (warp >= total) return;
+  const int i = warp % nreq, r = warp / nreq;
+  const int pr = r % P.pss, r2 = r / P.pss;
+  const int e = r2 % 2, pt = r2 / 2;
+  const int n1 = P.z1[pr], n2 = P.z2[pr];
+  const double C0 = css[(((size_t)pt * P.pss + pr) * 2 + e) * nreq + i];
+  auto dlnC = [&](double kk) {
+    const double d = dCss_dlnk_d(P, pt, kk, l[i], n1, n2, e == 0);
+    const double C = (fabs(d) > 1e-30) ? C0 : 1.0;
+    return (fabs(C) > 1e-30) ? d / C : 0.0;
+  };
+  const double lnkmax = log(kmax[i]);
+  double num = 0.0, den = 0.0;
+  for (int m = lane; m < nt; m += 32) {
+    const double t = tx[m], s = (1. - t) / t, w = tw[m] / (t * t);
+    num += w * fabs(dlnC(exp(lnkmax - s)));
+    den += w * (fabs(dlnC(exp(s))) + fabs(dlnC(exp(-s))));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    num += __shfl_down_sync(0xffffffffu, num, o);
+    den += __shfl_down_sync(0xffffffffu, den, o);
+  }
+  if (lane == 0) rf[warp] = num / den;
+}
+
+void launch_scut_css(const Params& P, int nl, const double* l, double* out, cudaStream_t s)
+{
+  k_scut_css<<<dim3(P.B, P.pss), 128, 0, s>>>(P, nl, l, out);
+}
+void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const double* l, const double* css,
+                      double* dC, double* dlnC, cudaStream_t s)
+{
+  const int tiles = std::min(64, (nk * nl + 127) / 128);
+  k_scut_dlnk<<<dim3(P.B, 2 * P.pss, tiles), 128, 0, s>>>(P, nk, k, nl, l, css, dC, dlnC);
+}
+void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
+                    const double* tw, const double* css, double* rf, cudaStream_t s)
+{
+  const int warps = P.B * 2 * P.pss * nreq;
+  k_scut_rf<<<(warps * 32 + 255) / 256, 256, 0, s>>>(P, nreq, kmax, l, nt, tx, tw, css, rf);
 }
 
 // Input validation of host batches after staging (the reference rejects

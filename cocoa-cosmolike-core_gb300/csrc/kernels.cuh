@@ -27,6 +27,14 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
 void launch_check_finite(const double* x, size_t n, int* flag, cudaStream_t s);
 // mixed plan: split the wave's lnP (and separate lnPL) into P.lnP2 / P.lnPL2
 void launch_split_tables(const Params& P, cudaStream_t s, int* launches);
+// scale-cut diagnostics of C_ss (k_setup.cu): C_ss at l[0..nl) [B][pss][2][nl];
+// dC/dlnk and dlnC/dlnk on k x l [B][2][pss][nk][nl]; RF per (kmax, l)
+// request [B][2][pss][nreq]
+void launch_scut_css(const Params& P, int nl, const double* l, double* out, cudaStream_t s);
+void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const double* l, const double* css,
+                      double* dC, double* dlnC, cudaStream_t s);
+void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
+                    const double* tw, const double* css, double* rf, cudaStream_t s);
 // dst[pt][e] = src[pt][e] + add[e] for B points of n entries (the baryon
 // ratio on the wave's nonlinear table)
 void launch_add_table(const double* src, const double* add, double* dst, int B, size_t n, cudaStream_t s);

@@ -1205,6 +1205,135 @@ extern "C" int cl2pt_plan_autotune(cl2pt_plan* p, const cl2pt_batch* b, void* st
   return CL2PT_OK;
 }
 
+// Scale-cut diagnostics of C_ss (cosmolike/cosmo2D_scuts.c): the batch's
+// inputs on the device (the plan's staging for host batches), then per wave
+// the set-up stage (lens efficiencies, the ss node set) and the diagnostic
+// kernels; kreq/lreq the requests, what 0: the (k, l) grid (dC, dlnC), 1:
+// the RF requests (kmax[i], l[i]) into o1.
+static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const double* k, int nl,
+                    const double* l, double* o0, double* o1, cudaStream_t s)
+{
+  if (!p || !b) return CL2PT_ERR_ARG;
+  if (p->P.tatt) return CL2PT_ERR_UNSUPPORTED;  // B modes and TATT terms of the diagnostics are not built
+  if (int st = check_batch(p, b, true)) return st;
+  if (nk < 1 || nl < 1 || !k || !l) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nk; i++)
+    if (!(k[i] > 0) || !std::isfinite(k[i])) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nl; i++)
+    if (!(l[i] >= 0) || !std::isfinite(l[i])) return CL2PT_ERR_ARG;
+  const int n = b->n;
+  const Params& T = p->P;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const double *om = b->omega_m, *h0 = b->h0, *chi = b->chi, *G = b->G, *lnP = b->lnP, *lnPL = b->lnPL;
+  const cl2pt_nuisance* nu = b->nuisance;
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaMemcpyAsync(p->d_in_om, om, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_h0, h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_chi, chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_G, G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_lnP, lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (lnPL) {
+      if (!p->d_in_lnPL) return CL2PT_ERR_ARG;
+      CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL, lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
+      lnPL = p->d_in_lnPL;
+    }
+    CUDA_OK(cudaMemcpyAsync(p->d_in_nu, nu, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
+    om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP; nu = p->d_in_nu;
+  }
+  if (!lnPL) lnPL = lnP;
+  const int npr = std::max(T.pss, 1);
+  const int W = p->wave;
+  const size_t per = what == 0 ? (size_t)2 * npr * nk * nl : (size_t)2 * npr * nl;
+  double *dk = nullptr, *dl = nullptr, *dcss = nullptr, *d0 = nullptr, *d1 = nullptr, *dtx = nullptr;
+  std::vector<double> tx, tw;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&dk, sizeof(double) * nk));
+  fail(cudaMalloc((void**)&dl, sizeof(double) * nl));
+  fail(cudaMalloc((void**)&dcss, sizeof(double) * (size_t)W * npr * 2 * nl));
+  fail(cudaMalloc((void**)&d0, sizeof(double) * (size_t)W * per));
+  if (what == 0) fail(cudaMalloc((void**)&d1, sizeof(double) * (size_t)W * per));
+  if (what == 1) {
+    // the 256-point rule of the reference at high_def_integration 0 (512, 1024 above) on [1e-5, 1]
+    const int hdi = std::abs(p->cfg.high_def_integration);
+    const int nt = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
+    std::vector<double> x, w;
+    gl_rule(nt, x, w);
+    tx.resize(nt);
+    tw.resize(nt);
+    for (int m = 0; m < nt; m++) {
+      tx[m] = 0.5 * (1.0 - 1e-5) * x[m] + 0.5 * (1.0 + 1e-5);
+      tw[m] = 0.5 * (1.0 - 1e-5) * w[m];
+    }
+    fail(cudaMalloc((void**)&dtx, sizeof(double) * 2 * nt));
+    if (!st) {
+      fail(cudaMemcpy(dtx, tx.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
+      fail(cudaMemcpy(dtx + nt, tw.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
+    }
+  }
+  if (!st) {
+    fail(cudaMemcpyAsync(dk, k, sizeof(double) * nk, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dl, l, sizeof(double) * nl, cudaMemcpyHostToDevice, s));
+  }
+  cl2pt::Hook hk;
+  int launches = 0;
+  for (int w0 = 0; w0 < n && !st; w0 += W) {
+    Params P = T;
+    P.B = std::min(W, n - w0);
+    P.omega_m = om + w0;
+    P.h0 = h0 + w0;
+    P.chi = chi + (size_t)w0 * nchi;
+    P.G = G + (size_t)w0 * nG;
+    P.lnP = lnP + (size_t)w0 * nP;
+    P.lnPL = lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    if (p->bary_on) {
+      cl2pt::launch_add_table(P.lnP, p->d_bary_lnr, p->d_lnP_bary, P.B, nP, s);
+      P.lnP = p->d_lnP_bary;
+    }
+    P.nu = nu + w0;
+    cl2pt::launch_setup(P, s, &launches, hk);
+    cl2pt::launch_scut_css(P, nl, dl, dcss, s);
+    if (what == 0) cl2pt::launch_scut_dlnk(P, nk, dk, nl, dl, dcss, d0, d1, s);
+    else cl2pt::launch_scut_rf(P, nl, dk, dl, (int)tx.size(), dtx, dtx + tx.size(), dcss, d0, s);
+    fail(cudaGetLastError());
+    const size_t bytes = sizeof(double) * per * P.B;
+    const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (what == 0) {
+      if (o0) fail(cudaMemcpyAsync(o0 + (size_t)w0 * per, d0, bytes, kind, s));
+      if (o1) fail(cudaMemcpyAsync(o1 + (size_t)w0 * per, d1, bytes, kind, s));
+    } else {
+      fail(cudaMemcpyAsync(o1 + (size_t)w0 * per, d0, bytes, kind, s));
+    }
+    fail(cudaStreamSynchronize(s));
+  }
+  cudaFree(dk);
+  cudaFree(dl);
+  cudaFree(dcss);
+  cudaFree(d0);
+  cudaFree(d1);
+  cudaFree(dtx);
+  if (!st) {
+    int e = 0;
+    fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) st = CL2PT_ERR_DEVICE;
+  }
+  return st;
+}
+
+extern "C" int cl2pt_scut_ss_dlnk(cl2pt_plan* p, const cl2pt_batch* b, int nk, const double* k, int nl,
+                                  const double* l, double* dC, double* dlnC, void* stream)
+{
+  if (!dC && !dlnC) return CL2PT_ERR_ARG;
+  return scut_run(p, b, 0, nk, k, nl, l, dC, dlnC, (cudaStream_t)stream);
+}
+
+extern "C" int cl2pt_scut_ss_rf(cl2pt_plan* p, const cl2pt_batch* b, int nreq, const double* kmax,
+                                const double* l, double* rf, void* stream)
+{
+  if (!rf) return CL2PT_ERR_ARG;
+  return scut_run(p, b, 1, nreq, kmax, nreq, l, nullptr, rf, (cudaStream_t)stream);
+}
+
 extern "C" int cl2pt_fourier_sizes(const cl2pt_plan* p, int nell, int* n_ss, int* n_gs, int* n_gg,
                                    int* n_total)
 {

@@ -331,6 +331,25 @@ int cl2pt_plan_set_baryon_ratio(cl2pt_plan* plan, int nk, const double* log10k, 
 int cl2pt_plan_set_contraction(cl2pt_plan* plan, int mode);
 int cl2pt_plan_get_contraction(const cl2pt_plan* plan, int* mode);
 
+/* Scale-cut diagnostics of the cosmic-shear C_l (cosmolike/cosmo2D_scuts.c;
+ * plans without TATT: CL2PT_ERR_UNSUPPORTED), FP64, for every point of the
+ * batch, E/B mode e (0 EE, 1 BB; BB is 0 without TATT) and shear pair p in
+ * the plan's pair order (N_shear):
+ *   cl2pt_scut_ss_dlnk: dC[n][2][pss][nk][nl] = dC_ss/dlnk at (k[i], l[j])
+ *     (dC_ss_dlnk_tomo_limber_nointerp, cosmo2D_scuts.c:42-74; k in h/Mpc)
+ *     and dlnC[...] = dC / C_ss(l) with C_ss_tomo_limber_nointerp (the
+ *     nointerp branch of int_RF_C_ss, :257-284); either output may be NULL;
+ *   cl2pt_scut_ss_rf: rf[n][2][pss][nreq] = RF_C_ss_tomo_limber_nointerp
+ *     (:329-375) at (kmax[i], l[i]): the fraction of the integral of
+ *     |dlnC/dlnk| over ln k that lies below ln kmax, with the nointerp
+ *     dlnC/dlnk at every l (the reference reads its (ln k, ln l) table for
+ *     l > LMIN_tab).
+ * k, l, kmax in host memory; outputs follow batch->where. */
+int cl2pt_scut_ss_dlnk(cl2pt_plan* plan, const cl2pt_batch* batch, int nk, const double* k, int nl,
+                       const double* l, double* dC, double* dlnC, void* stream);
+int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const double* kmax, const double* l,
+                     double* rf, void* stream);
+
 /* Where the mixed plan's FFTLog multipole loop keeps its spectra and
  * Gamma-recurrence state: CL2PT_FFTLOG_STATE_AUTO (the default: global
  * memory, unless cl2pt_plan_autotune chose otherwise), _GLOBAL (global

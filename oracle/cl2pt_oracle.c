@@ -640,7 +640,7 @@ static double fptb_row(int row, double lnk)
 /* int_for_C_ss_tomo_limber_core: cosmo2D.c:1370-1515 (deriv = 0) */
 static double ss_core(double a, double fK, double PK, double D, double dchida,
                       double ell_pref, double l, int n1, int n2, double WK1,
-                      double WK2, double WS1, double WS2, int EE)
+                      double WK2, double WS1, double WS2, int EE, int deriv)
 {
   const double ell = l + 0.5;
   const double k = ell / fK;
@@ -683,11 +683,14 @@ static double ss_core(double a, double fK, double PK, double D, double dchida,
       ans = 0.0;
     }
   }
-  return ans * (dchida / (fK * fK)) * ell_pref;
+  /* deriv: dC/dlnk, the scale-cut diagnostics' form (cosmo2D.c:1509-1514) */
+  return deriv ? ans * (dchida / fK) * ell_pref : ans * (dchida / (fK * fK)) * ell_pref;
 }
 
 /* int_for_C_ss_tomo_limber: cosmo2D.c:1521-1556 */
-static double int_ss(double a, int n1, int n2, double l, int EE)
+static double int_ss_d(double a, int n1, int n2, double l, int EE, int deriv);
+static double int_ss(double a, int n1, int n2, double l, int EE) { return int_ss_d(a, n1, n2, l, EE, 0); }
+static double int_ss_d(double a, int n1, int n2, double l, int EE, int deriv)
 {
   const double ell = l + 0.5;
   const chis_t c = chi_all(a);
@@ -699,7 +702,7 @@ static double int_ss(double a, int n1, int n2, double l, int EE)
   const double ell4 = ell * ell * ell * ell;
   const double pref = l * (l - 1.) * (l + 1.) * (l + 2.) / ell4;
   return ss_core(a, fK, PK, D, c.dchida, pref, l, n1, n2, W_kappa(a, fK, n1),
-                 W_kappa(a, fK, n2), W_source(a, n1, hh), W_source(a, n2, hh), EE);
+                 W_kappa(a, fK, n2), W_source(a, n1, hh), W_source(a, n2, hh), EE, deriv);
 }
 
 /* int_for_C_gs_tomo_limber_core: cosmo2D.c:1890-2073 (RSD_GS off) */
@@ -840,6 +843,45 @@ double orc_C_ss_nointerp(double l, int ni, int nj, int EE)
   const double amax = 1. / (1. + fmax(g.src.zmin_all, 1e-6));
   return glint(gl_size_ss(), amin, amax, 0, ni, nj, l, EE);
 }
+/* dC_ss_dlnk_tomo_limber_nointerp (cosmo2D_scuts.c:42-74): the C_ss
+ * integrand in its dC/dlnk form at the a where chi(a) = (l + 1/2) / k
+ * (k in h/Mpc), 0 outside the source range */
+double orc_dC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)
+{
+  const double ell = l + 0.5;
+  const double a = orc_a_chi(ell / (k * COVERH0));
+  const double amin = 1. / (g.src.zmax_all + 1.);
+  const double amax = 1. / (1. + fmax(g.src.zmin_all, 1e-6));
+  return (a > amin && a < amax) ? int_ss_d(a, ni, nj, l, EE, 1) : 0.0;
+}
+/* dlnC/dlnk as the nointerp branch of int_RF_C_ss (cosmo2D_scuts.c:257-284) */
+static double dlnC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)
+{
+  const double dC = orc_dC_ss_dlnk_nointerp(k, l, ni, nj, EE);
+  const double C = (fabs(dC) > 1e-30) ? orc_C_ss_nointerp(l, ni, nj, EE) : 1.0;
+  return (fabs(C) > 1e-30) ? dC / C : 0.0;
+}
+/* RF_C_ss_tomo_limber_nointerp (cosmo2D_scuts.c:329-375), every multipole
+ * through the nointerp branch: the fraction of int |dlnC/dlnk| dlnk below
+ * ln kmax, both integrals as 256-point Gauss-Legendre sums in t on
+ * [1e-5, 1] with ln k = ln kmax - (1 - t)/t (numerator) and +-(1 - t)/t
+ * (denominator) */
+double orc_RF_C_ss_nointerp(double kmax, double l, int ni, int nj, int EE)
+{
+  const glrule* r = rule(256);
+  const double lnkmax = log(kmax);
+  double num = 0.0, den = 0.0;
+  for (int m = 0; m < 256; m++) {
+    double t, w;
+    num_gl_point(1e-5, 1.0, m, 256, r->x, r->w, &t, &w);
+    const double s = (1. - t) / t;
+    num += w * fabs(dlnC_ss_dlnk_nointerp(exp(lnkmax - s), l, ni, nj, EE)) / (t * t);
+    den += w * (fabs(dlnC_ss_dlnk_nointerp(exp(s), l, ni, nj, EE)) +
+                fabs(dlnC_ss_dlnk_nointerp(exp(-s), l, ni, nj, EE))) / (t * t);
+  }
+  return num / den;
+}
+
 /* C_gs_tomo_limber_nointerp: cosmo2D.c:2125-2182 */
 double orc_C_gs_nointerp(double l, int nl, int ns)
 {
@@ -937,10 +979,10 @@ static void build_tables(void)
           const double WK1 = W[b1 * np + p], WK2 = W[b2 * np + p];
           const double WS1 = W[(ns + b1) * np + p], WS2 = W[(ns + b2) * np + p];
           sEE += ss_core(cn.a[p], cn.fK[p], PK[i * np + p], cn.D[p], cn.dchida[p], ep[i], lx[i],
-                         b1, b2, WK1, WK2, WS1, WS2, 1) * cn.wt[p];
+                         b1, b2, WK1, WK2, WS1, WS2, 1, 0) * cn.wt[p];
           if (g.cfg.ia_model == CL2PT_IA_TATT)
             sBB += ss_core(cn.a[p], cn.fK[p], PK[i * np + p], cn.D[p], cn.dchida[p], ep[i], lx[i],
-                           b1, b2, WK1, WK2, WS1, WS2, 0) * cn.wt[p];
+                           b1, b2, WK1, WK2, WS1, WS2, 0, 0) * cn.wt[p];
         }
         g.tab_ss[(0 * g.pss + k) * nell + i] = sEE;
         g.tab_ss[(1 * g.pss + k) * nell + i] = sBB;

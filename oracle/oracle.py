@@ -215,6 +215,20 @@ class Oracle:
         f.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp]
         return f(len(lk), _p(lk), len(av), _p(av), _p(lr))
 
+    def dC_ss_dlnk(self, k, l, ni, nj, EE=1):
+        """dC_ss_dlnk_tomo_limber_nointerp (the point must be set)."""
+        f = self.lib.orc_dC_ss_dlnk_nointerp
+        f.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
+        f.restype = C.c_double
+        return f(float(k), float(l), int(ni), int(nj), int(EE))
+
+    def RF_C_ss(self, kmax, l, ni, nj, EE=1):
+        """RF_C_ss_tomo_limber_nointerp with the nointerp dlnC/dlnk at every l."""
+        f = self.lib.orc_RF_C_ss_nointerp
+        f.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
+        f.restype = C.c_double
+        return f(float(kmax), float(l), int(ni), int(nj), int(EE))
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

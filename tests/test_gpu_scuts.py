@@ -1,0 +1,77 @@
+"""Scale-cut diagnostics of the cosmic-shear C_l (cosmolike/cosmo2D_scuts.c):
+dC_ss/dlnk and dlnC_ss/dlnk on a (k, l) grid and the response fraction RF
+against the FP64 oracle's restatement (dC_ss_dlnk_tomo_limber_nointerp,
+the nointerp dlnC of int_RF_C_ss, RF_C_ss_tomo_limber_nointerp), both plans
+(the diagnostics run in FP64 in both)."""
+import numpy as np
+import pytest
+
+from cl2pt import abi, lib, workloads
+
+
+def case(prec, seed=41):
+    w = workloads.make("real_3x2pt_small_nla")
+    tabs, nus = workloads.points(w, 2, seed=seed)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2, linear_table=True)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    return w, tabs, nus, plan, (om, h0, chi, G, lnP), workloads.stack_lin(tabs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_dlnk_vs_oracle(gpu_lib, oracle_built, prec):
+    import oracle as O
+    w, tabs, nus, plan, args, lnPL = case(prec)
+    k = np.exp(np.linspace(np.log(1e-3), np.log(30.0), 23))
+    l = np.array([2.0, 10.0, 37.5, 150.0, 800.0, 4000.0])
+    dC, dlnC = plan.scut_ss_dlnk(*args, nus, k, l, lnPL=lnPL)
+    assert np.all(dC[:, 1] == 0.0)  # no B modes without TATT
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    ns = w.cfg.n_source
+    pairs = [(i, j) for i in range(ns) for j in range(i, ns)]
+    worst = 0.0
+    for pt in range(2):
+        o.set_point(tabs[pt], nus[pt])
+        for p, (i, j) in enumerate(pairs):
+            C = np.array([o.C_ss_nointerp(lv, i, j, 1) for lv in l])
+            ref = np.array([[o.dC_ss_dlnk(kv, lv, i, j) for lv in l] for kv in k])
+            g = dC[pt, 0, p]
+            scale = np.abs(ref).max()
+            worst = max(worst, float(np.max(np.abs(g - ref)) / scale))
+            refl = np.where(np.abs(C)[None, :] > 1e-30, ref / np.where(np.abs(ref) > 1e-30, C[None, :], 1.0), 0.0)
+            assert np.allclose(dlnC[pt, 0, p], refl, rtol=1e-9, atol=1e-12 * np.abs(refl).max())
+    print("dC/dlnk max error / peak", worst)
+    assert worst <= 1e-9
+
+
+@pytest.mark.gpu
+def test_rf_vs_oracle(gpu_lib, oracle_built):
+    import oracle as O
+    w, tabs, nus, plan, args, lnPL = case(lib.PREC_FP64, seed=42)
+    kmax = np.array([0.05, 0.3, 1.0, 5.0])
+    l = np.array([30.0, 200.0, 1000.0, 300.0])
+    rf = plan.scut_ss_rf(*args, nus, kmax, l, lnPL=lnPL)
+    o = O.Oracle("orc")
+    o.setup(w.cfg, w.src, w.lens)
+    ns = w.cfg.n_source
+    pairs = [(i, j) for i in range(ns) for j in range(i, ns)]
+    o.set_point(tabs[1], nus[1])
+    for p in (0, len(pairs) - 1):
+        i, j = pairs[p]
+        ref = np.array([o.RF_C_ss(km, lv, i, j) for km, lv in zip(kmax, l)])
+        assert np.allclose(rf[1, 0, p], ref, rtol=1e-9, atol=1e-12), (p, rf[1, 0, p], ref)
+        assert np.all(ref > 0)
+    # RF grows with kmax at fixed l
+    r2 = plan.scut_ss_rf(*args, nus, [0.1, 0.5, 2.0], [300.0] * 3, lnPL=lnPL)
+    assert np.all(np.diff(r2[0, 0, 0]) > 0)
+
+
+@pytest.mark.gpu
+def test_scuts_reject_tatt(gpu_lib):
+    w = workloads.make("real_3x2pt_tatt_small")
+    tabs, nus = workloads.points(w, 1, seed=3)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    with pytest.raises(lib.CL2PTError):
+        plan.scut_ss_dlnk(om, h0, chi, G, lnP, nus, [0.1], [100.0])
