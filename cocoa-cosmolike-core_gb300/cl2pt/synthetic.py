@@ -94,12 +94,13 @@ def chi_of_z(z: np.ndarray, c: Cosmo) -> np.ndarray:
     return C_OVER_H0 * np.interp(z, zf, cum)
 
 
-def background_z_grid() -> np.ndarray:
-    """z grid for the distance and growth tables.  It runs to z = 60 so that
-    every lookup the 2-point path makes (down to a_min = 1/41, z = 40) stays
-    strictly inside the table."""
+def background_z_grid(z_max: float = 60.0) -> np.ndarray:
+    """z grid for the distance and growth tables.  By default it runs to
+    z = 60 so that every lookup the 2-point path makes (down to a_min = 1/41,
+    z = 40) stays strictly inside the table; the CMB-lensing spectra need
+    chi(z = 1090), so their tables run further (z_max)."""
     lo = np.linspace(0.0, 4.5, 1800)
-    hi = np.geomspace(4.5, 60.0, 201)[1:]
+    hi = np.geomspace(4.5, z_max, 201 if z_max <= 60.0 else 301)[1:]
     return np.concatenate([lo, hi])
 
 
@@ -119,12 +120,13 @@ class CosmoTables:
 
 
 def make_cosmo_tables(c: Cosmo = Cosmo(), nk: int = 600, nz: int = 200,
-                      log10k_range=(-4.0, 2.0), z_range=(0.0, 4.0), nl_boost: bool = False) -> CosmoTables:
+                      log10k_range=(-4.0, 2.0), z_range=(0.0, 4.0), nl_boost: bool = False,
+                      z_max: float = 60.0) -> CosmoTables:
     """nl_boost: the nonlinear table is the linear one times a smooth
     small-scale boost 1 + 0.6 (k/k_nl)^1.5, k_nl = 0.25 (1+z)^1.2 h/Mpc
     (a halofit-like shape), so the two tables differ; otherwise they are
     the same."""
-    zg = background_z_grid()
+    zg = background_z_grid(z_max)
     chi = chi_of_z(zg, c)
     D = growth_D(zg, c)
     G = D * (1.0 + zg)

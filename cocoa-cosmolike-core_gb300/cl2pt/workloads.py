@@ -11,6 +11,9 @@
                          l <= 5000, 200 nodes) for fast checks, whose
                          nonlinear table carries a small-scale boost over
                          the linear one (the reduced workloads pass both)
+  cmb_lensing[_tatt]_small the 6x2pt CMB-lensing spectra C_gk, C_ks, C_kk of
+                         real_3x2pt[_tatt]_small's samples at 16 log-spaced
+                         l in 2-5000, on distance tables to z = 1100
   real_3x2pt_tatt[_small] the same with TATT intrinsic alignments
                          (redshift evolution: A1, A2, eta, b_TA) and
                          nonlinear galaxy bias (b2, bs2)
@@ -89,6 +92,15 @@ def make(name: str) -> Workload:
                               theta_max=250.0, lmax=5000, n_ell=200)
         base = synthetic.make_cosmo_tables(nk=400, nz=100, nl_boost=True)
         return Workload(name, cfg, synthetic.source_nz(4), synthetic.lens_nz(3), base)
+    if name in ("cmb_lensing_small", "cmb_lensing_tatt_small"):
+        # the 6x2pt CMB-lensing spectra: real_3x2pt_small's samples (with
+        # TATT and one-loop galaxy bias in the _tatt case) on distance and
+        # growth tables that reach the last-scattering surface
+        w = make(name.replace("cmb_lensing", "real_3x2pt"))
+        w.base = synthetic.make_cosmo_tables(nk=400, nz=100, nl_boost=True, z_max=1100.0)
+        w.ell = _fourier_ells(16, 2.0, 5000.0)
+        w.name = name
+        return w
     if name == "real_3x2pt_small_limber":
         w = make("real_3x2pt_small")
         w.cfg.adopt_limber_gg = 1

@@ -882,6 +882,99 @@ double orc_RF_C_ss_nointerp(double kmax, double l, int ni, int nj, int EE)
   return num / den;
 }
 
+/* ---- CMB lensing (6x2pt) */
+/* W_k (radial_weights.c:107-114) with g_cmb (redshift_spline.c:1111-1125):
+ * the lensing efficiency of the last-scattering surface, chi_cmb =
+ * chi(1/1091), flat f_K */
+static double W_k(double a, double fK)
+{
+  const double chi_cmb = orc_chi(1. / 1091.);
+  return (1.5 * g.omega_m * fK / a) * ((chi_cmb - orc_chi(a)) / chi_cmb);
+}
+/* int_for_C_gk_tomo_limber (cosmo2D.c:2857-2955; HOD and RSD off) */
+static double int_gk(double a, int nl, double l, int nlb)
+{
+  const chis_t c = chi_all(a);
+  const double hh = hoverh0v2(a, c.dchida);
+  const double ell = l + 0.5;
+  const double fK = c.chi;
+  const double k = ell / fK;
+  const double z = 1. / a - 1.;
+  const double b1 = gb1(z, nl), bmag = gbmag(z, nl);
+  const double WK = W_k(a, fK), WGAL = W_gal(a, nl, hh), WMAG = W_mag(a, fK, nl);
+  const double pref = l * (l + 1.) / (ell * ell);
+  const double PK = Pdelta(k, a);
+  const double res = WK * (WGAL * b1 + WMAG * pref * bmag) * PK;
+  double oneloop = 0.0;
+  if (nlb) {
+    need_fptb();
+    const double D = orc_growfac(a);
+    const double g4 = D * D * D * D;
+    const double lnk = log(k);
+    const double d1d2 = fptb_row(0, lnk), d1s2 = fptb_row(2, lnk), d1p3 = fptb_row(5, lnk);
+    oneloop = WK * WGAL *
+              (g4 * (0.5 * gb2(z, nl) * d1d2 + 0.5 * gbs2(z, nl) * d1s2 + 0.5 * gb3(z, nl) * d1p3) +
+               (gbK(z, nl) * k * k * PK));
+  }
+  return ((res + oneloop) * c.dchida / (fK * fK)) * pref;
+}
+/* int_for_C_ks_tomo_limber (cosmo2D.c:3180-3222) */
+static double int_ks(double a, int ni, double l)
+{
+  const double ell = l + 0.5;
+  const double D = orc_growfac(a);
+  const chis_t c = chi_all(a);
+  const double hh = hoverh0v2(a, c.dchida);
+  const double fK = c.chi;
+  const double k = ell / fK;
+  const double PK = Pdelta(k, a);
+  const double WK1 = W_kappa(a, fK, ni), WK2 = W_k(a, fK);
+  const double pref1 = l * (l + 1.) / (ell * ell);
+  const double tmp = (l - 1.) * l * (l + 1.) * (l + 2.);
+  const double pref2 = (tmp > 0) ? sqrt(tmp) / (ell * ell) : 0.0;
+  double r[2];
+  IA_A1(a, D, ni, ni, r);
+  const double WS1 = W_source(a, ni, hh) * r[0];
+  return ((WK1 - WS1) * WK2 * PK * c.dchida / (fK * fK)) * pref1 * pref2;
+}
+/* int_for_C_kk_limber (cosmo2D.c:3428-3447) */
+static double int_kk(double a, double l)
+{
+  const chis_t c = chi_all(a);
+  const double ell = l + 0.5;
+  const double fK = c.chi;
+  const double k = ell / fK;
+  const double WK = W_k(a, fK);
+  const double PK = Pdelta(k, a);
+  const double pref = l * (l + 1.0) / (ell * ell);
+  return WK * WK * PK * (c.dchida / (fK * fK)) * pref * pref;
+}
+static double glint_cmb(int kind, double amin, double amax, int i, double l)
+{
+  const int n = gl_size_gg();
+  const glrule* r = rule(n);
+  double s = 0.0;
+  for (int p = 0; p < n; p++) {
+    double x, w;
+    num_gl_point(amin, amax, p, n, r->x, r->w, &x, &w);
+    s += w * (kind == 0 ? int_gk(x, i, l, has_b2_galaxies()) : kind == 1 ? int_ks(x, i, l) : int_kk(x, l));
+  }
+  return s;
+}
+/* C_gk_tomo_limber_nointerp (cosmo2D.c:2960-3005): the lens range */
+double orc_C_gk_nointerp(double l, int ni) { return glint_cmb(0, orc_amin_lens(ni), orc_amax_lens(ni), ni, l); }
+/* C_ks_tomo_limber_nointerp (cosmo2D.c:3224-3270): amin_source, amax_source
+ * (redshift_spline.c:27-39) */
+double orc_C_ks_nointerp(double l, int ni)
+{
+  return glint_cmb(1, 1. / (g.src.zmax_all + 1.), 1. / (1. + fmax(g.src.zmin_all, 0.001)), ni, l);
+}
+/* C_kk_limber_nointerp (cosmo2D.c:3449-3482) */
+double orc_C_kk_nointerp(double l)
+{
+  return glint_cmb(2, g.cfg.a_min * (1. + 1.e-5), 0.99999, 0, l);
+}
+
 /* C_gs_tomo_limber_nointerp: cosmo2D.c:2125-2182 */
 double orc_C_gs_nointerp(double l, int nl, int ns)
 {

@@ -229,6 +229,17 @@ class Oracle:
         f.restype = C.c_double
         return f(float(kmax), float(l), int(ni), int(nj), int(EE))
 
+    def C_cmb(self, which, l, ni=0):
+        """CMB-lensing C_l (C_gk_tomo_limber_nointerp / C_ks / C_kk): which in
+        'gk', 'ks', 'kk'."""
+        f = getattr(self.lib, "%s_C_%s_nointerp" % (self.which, which))
+        f.restype = C.c_double
+        if which == "kk":
+            f.argtypes = [C.c_double]
+            return f(float(l))
+        f.argtypes = [C.c_double, C.c_int]
+        return f(float(l), int(ni))
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

@@ -246,6 +246,10 @@ double ref_C_gg_nointerp(double l, int ni, int use_linear_ps)
 {
   return C_gg_tomo_limber_linpsopt_nointerp(l, ni, ni, use_linear_ps, 0);
 }
+/* CMB-lensing cross spectra (the 6x2pt probes), quadrature forms */
+double ref_C_gk_nointerp(double l, int ni) { return C_gk_tomo_limber_nointerp(l, ni, 0); }
+double ref_C_ks_nointerp(double l, int ni) { return C_ks_tomo_limber_nointerp(l, ni, 0); }
+double ref_C_kk_nointerp(double l) { return C_kk_limber_nointerp(l, 0); }
 double ref_C_ss_limber(double l, int ni, int nj, int EE)
 {
   return C_ss_tomo_limber(l, ni, nj, EE);

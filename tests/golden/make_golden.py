@@ -22,7 +22,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
          "fastpt_bias", "fastpt_ia", "real_3x2pt_tatt_small", "real_3x2pt_small_mag",
          "real_3x2pt_small_nla", "real_3x2pt_small_nlabin", "real_3x2pt_small_hdi",
-         "real_3x2pt_small_lin"]
+         "real_3x2pt_small_lin", "cmb_lensing_small", "cmb_lensing_tatt_small"]
 
 # J_abJ1J2Jk rows {alpha, beta, J1, J2, Jk} checked on the batched FAST-PT grid
 JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]
@@ -48,6 +48,16 @@ def run_case(case, which="ref"):
         k, P, _ = workloads.fastpt_spectra(1, seed=1)
         r = np.array(JK_ROWS)
         out["J_abJ1J2Jk"] = o.J_abJ1J2Jk(k, P[0], r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
+        return out
+    if case.startswith("cmb_lensing"):
+        w = workloads.make(case)
+        o.setup(w.cfg, w.src, w.lens)
+        tabs, nus = workloads.points(w, 2, seed=11)
+        for i in range(2):
+            o.set_point(tabs[i], nus[i])
+            out[f"Cgk_{i}"] = np.array([[o.C_cmb("gk", l, n) for l in w.ell] for n in range(w.cfg.n_lens)])
+            out[f"Cks_{i}"] = np.array([[o.C_cmb("ks", l, n) for l in w.ell] for n in range(w.cfg.n_source)])
+            out[f"Ckk_{i}"] = np.array([o.C_cmb("kk", l) for l in w.ell])
         return out
     # <workload>_mag: the workload's points with magnification bias
     mag = case.endswith("_mag")
