@@ -100,6 +100,8 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_scut_ss_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_int, _dp, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
     lib.cl2pt_scut_ss_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
+    lib.cl2pt_cmb_cl.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p]
     lib.cl2pt_plan_set_baryon_ratio.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp]
     lib.cl2pt_plan_autotune.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_int, _ip, _ip,
                                         C.POINTER(C.c_double)]
@@ -256,6 +258,20 @@ class Plan:
         check(load().cl2pt_scut_ss_rf(self.h, C.byref(b), len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
               "cl2pt_scut_ss_rf")
         return rf
+
+    def cmb_cl(self, omega_m, h0, chi, G, lnP, nuisance, ell, lnPL=None):
+        """CMB-lensing spectra of the 6x2pt probes (cl2pt_cmb_cl) at the
+        multipoles ell: C_gk [n][n_lens][nell], C_ks [n][n_source][nell],
+        C_kk [n][nell]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        n, ne = b.n, len(ell)
+        gk = np.zeros((n, self.cfg.n_lens, ne))
+        ks = np.zeros((n, self.cfg.n_source, ne))
+        kk = np.zeros((n, ne))
+        check(load().cl2pt_cmb_cl(self.h, C.byref(b), ne, _p(ell), gk.ctypes.data, ks.ctypes.data,
+                                  kk.ctypes.data, None), "cl2pt_cmb_cl")
+        return gk, ks, kk
 
     def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None, out=None):
         """Host arrays in, host data vectors out ([n][n_total]); out: an

@@ -691,6 +691,158 @@ void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double*
   k_scut_rf<<<(warps * 32 + 255) / 256, 256, 0, s>>>(P, nreq, kmax, l, nt, tx, tw, css, rf);
 }
 
+// ---- CMB-lensing spectra of the 6x2pt probes, FP64: C_gk, C_ks and C_kk
+// (C_gk_tomo_limber_nointerp, C_ks_tomo_limber_nointerp,
+// C_kk_limber_nointerp, cosmo2D.c:2960-3005, 3224-3257, 3449-3482) at the
+// caller's multipoles, Gauss-Legendre in a over the gg rule's nodes.  The
+// CMB lensing efficiency is W_k = 1.5 Om fK / a (chi_cmb - chi(a)) / chi_cmb
+// with chi_cmb = chi(1/1091) (W_k and g_cmb, radial_weights.c:107-114,
+// redshift_spline.c:1111-1125, flat f_K).  One CTA per (point, spectrum,
+// 128 multipoles); each node chunk's l-independent weights are formed once
+// in shared memory, then every thread sums its multipole over the chunk.
+// Spectrum rows: [0, nl) C_gk of lens bin q, [nl, nl + ns) C_ks of source
+// bin s, nl + ns C_kk; out [B][nl + ns + 1][nell].
+constexpr int CMB_NT = 128, CMB_PC = 128;
+
+// fptb_row (cosmo2D.c:2921-2932): linear in ln k on the FAST-PT grid, 0 off it
+__device__ __forceinline__ double fpt_lerp_d(const Params& P, const double* row, double lnk)
+{
+  if (lnk < P.fpt_lim0 || lnk > P.fpt_lim1) return 0.0;
+  const double r = (lnk - P.fpt_lim0) / P.fpt_lim2;
+  const int i = (int)floor(r);
+  if (i + 1 >= P.fpt_n) return row[P.fpt_n - 1];
+  return (r - i) * (row[i + 1] - row[i]) + row[i];
+}
+
+__global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const double* __restrict__ ell,
+                                                   double* __restrict__ out)
+{
+  // per node: a, fK, and the weights of P(k) (L: clustering / lensing, M:
+  // magnification, K: one-loop bK k^2) and of the one-loop rows d1d2,
+  // d1s2, d1p3
+  __shared__ double sa[CMB_PC], sf[CMB_PC], sL[CMB_PC], sM[CMB_PC], sK[CMB_PC], s2[CMB_PC], ss2[CMB_PC],
+      s3[CMB_PC];
+  __shared__ int s_bad;
+  const int pt = blockIdx.x, set = blockIdx.y;
+  const int kind = set < P.nl ? 0 : (set < P.nl + P.ns ? 1 : 2);  // 0 gk, 1 ks, 2 kk
+  const int q = kind == 0 ? set : (kind == 1 ? set - P.nl : 0);
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const double om = P.omega_m[pt];
+  const double* X = P.chi + (size_t)pt * P.chi_nz;
+  const double* Gv = P.G + (size_t)pt * P.G_nz;
+  const double g1 = G_at_d(P.G_z, Gv, P.G_nz, 0.0, nullptr);
+  const double* gsrc = P.gsrc + (size_t)pt * P.ns * P.n_a;
+  const double* glens = P.glens + (size_t)pt * P.nl * P.n_a;
+  const double amin_src = 1.0 / (P.src_zmax_all + 1.0);
+  const double amin_lensg = 1.0 / (P.lens_zmax_all + 1.0);
+  double amin, amax;
+  if (kind == 0) {
+    amin = amin_lens_d(P, nu, q);
+    amax = amax_lens_d(P, nu, q);
+  } else if (kind == 1) {
+    amin = amin_src;
+    amax = 1. / (1. + fmax(P.src_zmin_all, 0.001));
+  } else {
+    amin = P.a_min * (1. + 1.e-5);
+    amax = 0.99999;
+  }
+  if (!(amin > 0) || !(amin < amax) || !(amax < 1)) {
+    if (threadIdx.x == 0) atomicOr(P.err, 1);
+    return;
+  }
+  const double chi_cmb = chi_all_d(P.chi_z, X, P.chi_nz, 1. / 1091.).chi;
+  const bool nlb = kind == 0 && P.one_loop && has_b2(P, nu);
+  const double* pkt = P.linear_pk ? P.lnPL + (size_t)pt * P.pkl_nk * P.pkl_nz
+                                  : P.lnP + (size_t)pt * P.pk_nk * P.pk_nz;
+  const double* b_d1d2 = nlb ? P.fpt_b + ((size_t)pt * 5 + 0) * P.fpt_n : nullptr;
+  const double* b_d1s2 = nlb ? P.fpt_b + ((size_t)pt * 5 + 2) * P.fpt_n : nullptr;
+  const int il = blockIdx.z * CMB_NT + threadIdx.x;
+  const double l = il < nell ? ell[il] : 0.0;
+  const double L = l + 0.5;
+  const double pref1 = l * (l + 1.) / (L * L);
+  const double t4 = (l - 1.) * l * (l + 1.) * (l + 2.);
+  const double pref2 = (t4 > 0) ? sqrt(t4) / (L * L) : 0.0;
+  const double A = 0.5 * (amax - amin), Bc = 0.5 * (amax + amin);
+  const int n = P.n_gg;
+  double acc = 0.0;
+  if (threadIdx.x == 0) s_bad = 0;
+  for (int p0 = 0; p0 < n; p0 += CMB_PC) {
+    const int nc = min(CMB_PC, n - p0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < nc; j += CMB_NT) {
+      const double a = Bc + A * P.gl_gg_x[p0 + j];
+      const Chis c = chi_all_d(P.chi_z, X, P.chi_nz, a);
+      const double fK = c.chi;
+      const double WK = (1.5 * om * fK / a) * ((chi_cmb - fK) / chi_cmb);
+      const double sw = A * P.gl_gg_w[p0 + j] * c.dchida / (fK * fK);
+      const double z = 1.0 / a - 1.0;
+      double wL = 0.0, wM = 0.0, wK = 0.0, w2 = 0.0, ws2 = 0.0, w3 = 0.0;
+      if (kind == 0) {
+        const double H = 1.0 / ((a * a) * c.dchida);
+        const double WGAL = nz_lens_d(P, z, q, nu.lens_dz[q], nu.lens_stretch[q]) * H;
+        const double bmag = nu.gb[4][q];
+        const double WMAG =
+            (bmag != 0.0) ? (1.5 * om * fK / a) * g_lookup(glens + q * P.n_a, P.n_a, amin_lensg, a, false) : 0.0;
+        const double b1 = gb1_d(P, nu, z, q, g1, P.G_z, Gv);
+        wL = sw * WK * WGAL * b1;
+        wM = sw * WK * WMAG * bmag;
+        if (nlb) {
+          const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+          const double g4 = D * D * D * D;
+          const double u = sw * WK * WGAL;
+          w2 = u * g4 * 0.5 * gb2_d(P, nu, q, b1);
+          ws2 = u * g4 * 0.5 * gbs2_d(P, nu, q, b1);
+          w3 = P.fpt_d1p3 ? u * g4 * 0.5 * gb3_d(P, nu, q, b1) : 0.0;
+          wK = u * nu.gb[5][q];
+        }
+      } else if (kind == 1) {
+        const double H = 1.0 / ((a * a) * c.dchida);
+        const double D = growfac_d(P.G_z, Gv, P.G_nz, g1, a);
+        const double WK1 = (1.5 * om * fK / a) * g_lookup(gsrc + q * P.n_a, P.n_a, amin_src, a, true);
+        const double WS1 = nz_source_d(P, z, q, nu.src_dz[q]) * H * ia_a1(P, nu, om, a, D, q);
+        wL = sw * (WK1 - WS1) * WK;
+      } else {
+        wL = sw * WK * WK;
+      }
+      if (!(a > 0 && a < 1) || !(chi_cmb > fK)) atomicOr(&s_bad, 1);
+      sa[j] = a;
+      sf[j] = fK;
+      sL[j] = wL;
+      sM[j] = wM;
+      sK[j] = wK;
+      s2[j] = w2;
+      ss2[j] = ws2;
+      s3[j] = w3;
+    }
+    __syncthreads();
+    if (il < nell) {
+      for (int j = 0; j < nc; j++) {
+        const double k = L / sf[j];
+        const double PK = P.linear_pk ? pk_d(P.pkl_lk, P.pkl_nk, P.pkl_z, P.pkl_nz, pkt, k, sa[j])
+                                      : pk_d(P.pk_lk, P.pk_nk, P.pk_z, P.pk_nz, pkt, k, sa[j]);
+        double v = (sL[j] + pref1 * sM[j] + sK[j] * k * k) * PK;
+        if (nlb) {
+          const double lnk = log(k);
+          v += s2[j] * fpt_lerp_d(P, b_d1d2, lnk) + ss2[j] * fpt_lerp_d(P, b_d1s2, lnk);
+          if (P.fpt_d1p3) v += s3[j] * fpt_lerp_d(P, P.fpt_d1p3, lnk);
+        }
+        acc += v;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_bad) atomicOr(P.err, 1);
+  if (il < nell) {
+    const double pref = kind == 0 ? pref1 : (kind == 1 ? pref1 * pref2 : pref1 * pref1);
+    out[((size_t)pt * (P.nl + P.ns + 1) + set) * nell + il] = acc * pref;
+  }
+}
+
+void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cudaStream_t s)
+{
+  k_cmb_cl<<<dim3(P.B, P.nl + P.ns + 1, (nell + CMB_NT - 1) / CMB_NT), CMB_NT, 0, s>>>(P, nell, ell, out);
+}
+
 // Input validation of host batches after staging (the reference rejects
 // non-finite values in its setters): one grid-stride pass, one flag.
 __global__ void k_check_finite(const double* __restrict__ x, size_t n, int* flag)

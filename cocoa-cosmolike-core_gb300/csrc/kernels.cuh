@@ -35,6 +35,9 @@ void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const do
                       double* dC, double* dlnC, cudaStream_t s);
 void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
                     const double* tw, const double* css, double* rf, cudaStream_t s);
+// C_gk, C_ks, C_kk of the 6x2pt probes at ell[0..nell) (device), out
+// [B][nl + ns + 1][nell]
+void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cudaStream_t s);
 // dst[pt][e] = src[pt][e] + add[e] for B points of n entries (the baryon
 // ratio on the wave's nonlinear table)
 void launch_add_table(const double* src, const double* add, double* dst, int B, size_t n, cudaStream_t s);

@@ -1205,6 +1205,38 @@ extern "C" int cl2pt_plan_autotune(cl2pt_plan* p, const cl2pt_batch* b, void* st
   return CL2PT_OK;
 }
 
+// The batch's per-point inputs on the device: the caller's pointers for a
+// device batch, else copies into the plan's staging buffers on stream s
+// (the diagnostics entry points; lnPL falls back to lnP).
+struct DevBatch {
+  const double *om, *h0, *chi, *G, *lnP, *lnPL;
+  const cl2pt_nuisance* nu;
+};
+static int stage_batch_inputs(cl2pt_plan* p, const cl2pt_batch* b, cudaStream_t s, DevBatch* d)
+{
+  const int n = b->n;
+  const Params& T = p->P;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  *d = {b->omega_m, b->h0, b->chi, b->G, b->lnP, b->lnPL, b->nuisance};
+  if (b->where == CL2PT_HOST) {
+    CUDA_OK(cudaMemcpyAsync(p->d_in_om, b->omega_m, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_h0, b->h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_chi, b->chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_G, b->G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
+    CUDA_OK(cudaMemcpyAsync(p->d_in_lnP, b->lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (b->lnPL) {
+      if (!p->d_in_lnPL) return CL2PT_ERR_ARG;
+      CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL, b->lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
+      d->lnPL = p->d_in_lnPL;
+    }
+    CUDA_OK(cudaMemcpyAsync(p->d_in_nu, b->nuisance, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
+    d->om = p->d_in_om; d->h0 = p->d_in_h0; d->chi = p->d_in_chi; d->G = p->d_in_G; d->lnP = p->d_in_lnP;
+    d->nu = p->d_in_nu;
+  }
+  if (!d->lnPL) d->lnPL = d->lnP;
+  return CL2PT_OK;
+}
+
 // Scale-cut diagnostics of C_ss (cosmolike/cosmo2D_scuts.c): the batch's
 // inputs on the device (the plan's staging for host batches), then per wave
 // the set-up stage (lens efficiencies, the ss node set) and the diagnostic
@@ -1223,23 +1255,11 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
     if (!(l[i] >= 0) || !std::isfinite(l[i])) return CL2PT_ERR_ARG;
   const int n = b->n;
   const Params& T = p->P;
+  DevBatch d;
+  if (int st = stage_batch_inputs(p, b, s, &d)) return st;
+  const double *om = d.om, *h0 = d.h0, *chi = d.chi, *G = d.G, *lnP = d.lnP, *lnPL = d.lnPL;
+  const cl2pt_nuisance* nu = d.nu;
   const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
-  const double *om = b->omega_m, *h0 = b->h0, *chi = b->chi, *G = b->G, *lnP = b->lnP, *lnPL = b->lnPL;
-  const cl2pt_nuisance* nu = b->nuisance;
-  if (b->where == CL2PT_HOST) {
-    CUDA_OK(cudaMemcpyAsync(p->d_in_om, om, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_h0, h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_chi, chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_G, G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_lnP, lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (lnPL) {
-      if (!p->d_in_lnPL) return CL2PT_ERR_ARG;
-      CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL, lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
-      lnPL = p->d_in_lnPL;
-    }
-    CUDA_OK(cudaMemcpyAsync(p->d_in_nu, nu, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
-    om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP; nu = p->d_in_nu;
-  }
   if (!lnPL) lnPL = lnP;
   const int npr = std::max(T.pss, 1);
   const int W = p->wave;
@@ -1332,6 +1352,85 @@ extern "C" int cl2pt_scut_ss_rf(cl2pt_plan* p, const cl2pt_batch* b, int nreq, c
 {
   if (!rf) return CL2PT_ERR_ARG;
   return scut_run(p, b, 1, nreq, kmax, nreq, l, nullptr, rf, (cudaStream_t)stream);
+}
+
+// CMB-lensing spectra of the 6x2pt probes (C_gk, C_ks, C_kk) at the
+// caller's multipoles: per wave the set-up stage (lens efficiencies, the
+// one-loop bias tables when the plan has them) and k_cmb_cl, whose rows are
+// split into the three outputs.
+extern "C" int cl2pt_cmb_cl(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell, double* C_gk,
+                            double* C_ks, double* C_kk, void* stream)
+{
+  if (!p || !b || nell < 1 || !ell || (!C_gk && !C_ks && !C_kk)) return CL2PT_ERR_ARG;
+  if (int st = check_batch(p, b, true)) return st;
+  for (int i = 0; i < nell; i++)
+    if (!(ell[i] >= 0) || !std::isfinite(ell[i])) return CL2PT_ERR_ARG;
+  // the distance table must reach the last-scattering surface, z = 1090
+  if (p->chi_z.empty() || !(p->chi_z.back() >= 1090.0)) return CL2PT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = b->n;
+  const Params& T = p->P;
+  DevBatch d;
+  if (int st = stage_batch_inputs(p, b, s, &d)) return st;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const int nl = T.nl, ns = T.ns, nrow = nl + ns + 1;
+  const int W = p->wave;
+  double *dl = nullptr, *dout = nullptr;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&dl, sizeof(double) * nell));
+  fail(cudaMalloc((void**)&dout, sizeof(double) * (size_t)W * nrow * nell));
+  if (!st) fail(cudaMemcpyAsync(dl, ell, sizeof(double) * nell, cudaMemcpyHostToDevice, s));
+  const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  const size_t row = sizeof(double) * nell;
+  cl2pt::Hook hk;
+  int launches = 0;
+  for (int w0 = 0; w0 < n && !st; w0 += W) {
+    Params P = T;
+    P.B = std::min(W, n - w0);
+    P.omega_m = d.om + w0;
+    P.h0 = d.h0 + w0;
+    P.chi = d.chi + (size_t)w0 * nchi;
+    P.G = d.G + (size_t)w0 * nG;
+    P.lnP = d.lnP + (size_t)w0 * nP;
+    P.lnPL = d.lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    if (p->bary_on) {
+      cl2pt::launch_add_table(P.lnP, p->d_bary_lnr, p->d_lnP_bary, P.B, nP, s);
+      P.lnP = p->d_lnP_bary;
+    }
+    P.nu = d.nu + w0;
+    cl2pt::launch_setup(P, s, &launches, hk);
+    if (P.one_loop) {
+      cl2pt::launch_fpt_plin(P, s, &launches);
+      if (int st2 = cl2pt_fastpt_bias(p->fpt_bias, P.fpt_plin, P.B, p->d_fpt_bias_out, CL2PT_DEVICE, s)) {
+        st = st2;
+        break;
+      }
+      Params Pb = P;
+      Pb.tatt = 0;  // the bias rows alone
+      cl2pt::launch_fpt_tables(Pb, p->d_fpt_bias_out, nullptr, s, &launches);
+    }
+    cl2pt::launch_cmb_cl(P, nell, dl, dout, s);
+    fail(cudaGetLastError());
+    const size_t pitch = row * nrow;
+    if (C_gk && nl > 0)
+      fail(cudaMemcpy2DAsync(C_gk + (size_t)w0 * nl * nell, row * nl, dout, pitch, row * nl, P.B, kind, s));
+    if (C_ks && ns > 0)
+      fail(cudaMemcpy2DAsync(C_ks + (size_t)w0 * ns * nell, row * ns, dout + (size_t)nl * nell, pitch, row * ns,
+                             P.B, kind, s));
+    if (C_kk)
+      fail(cudaMemcpy2DAsync(C_kk + (size_t)w0 * nell, row, dout + (size_t)(nl + ns) * nell, pitch, row, P.B, kind,
+                             s));
+    fail(cudaStreamSynchronize(s));
+  }
+  cudaFree(dl);
+  cudaFree(dout);
+  if (!st) {
+    int e = 0;
+    fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) st = CL2PT_ERR_DEVICE;
+  }
+  return st;
 }
 
 extern "C" int cl2pt_fourier_sizes(const cl2pt_plan* p, int nell, int* n_ss, int* n_gs, int* n_gg,

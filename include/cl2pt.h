@@ -350,6 +350,20 @@ int cl2pt_scut_ss_dlnk(cl2pt_plan* plan, const cl2pt_batch* batch, int nk, const
 int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const double* kmax, const double* l,
                      double* rf, void* stream);
 
+/* CMB-lensing spectra of the 6x2pt probes at the multipoles ell[0..nell)
+ * (host memory), each by the reference's Gauss-Legendre rule in a with the
+ * clustering rule's node count:
+ *   C_gk[n][n_lens][nell]   C_gk_tomo_limber_nointerp (cosmo2D.c:2960-3005;
+ *                           one-loop bias terms with b2 != 0)
+ *   C_ks[n][n_source][nell] C_ks_tomo_limber_nointerp (cosmo2D.c:3224-3257)
+ *   C_kk[n][nell]           C_kk_limber_nointerp (cosmo2D.c:3449-3482)
+ * with the CMB lensing efficiency W_k = 1.5 Om f_K / a g_cmb(a) of a source
+ * at chi(1/1091) (radial_weights.c:107-114, redshift_spline.c:1111-1125).
+ * The plan's distance table must reach z = 1090 (else CL2PT_ERR_ARG).  Any
+ * output may be NULL (not all three); outputs follow batch->where. */
+int cl2pt_cmb_cl(cl2pt_plan* plan, const cl2pt_batch* batch, int nell, const double* ell, double* C_gk,
+                 double* C_ks, double* C_kk, void* stream);
+
 /* Where the mixed plan's FFTLog multipole loop keeps its spectra and
  * Gamma-recurrence state: CL2PT_FFTLOG_STATE_AUTO (the default: global
  * memory, unless cl2pt_plan_autotune chose otherwise), _GLOBAL (global
