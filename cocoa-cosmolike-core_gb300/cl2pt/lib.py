@@ -102,6 +102,8 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_scut_ss_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
     lib.cl2pt_cmb_cl.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]
+    lib.cl2pt_plan_set_cmb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp]
+    lib.cl2pt_cmb_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_plan_set_baryon_ratio.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp]
     lib.cl2pt_plan_autotune.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_int, _ip, _ip,
                                         C.POINTER(C.c_double)]
@@ -272,6 +274,25 @@ class Plan:
         check(load().cl2pt_cmb_cl(self.h, C.byref(b), ne, _p(ell), gk.ctypes.data, ks.ctypes.data,
                                   kk.ctypes.data, None), "cl2pt_cmb_cl")
         return gk, ks, kk
+
+    def set_cmb(self, lmin, lmax, fwhm_arcmin, healpixwin=None):
+        """The CMB map filter of w_gk / w_ks (cl2pt_plan_set_cmb): beam fwhm
+        in arcmin on lmin <= l <= lmax, optional HEALPix window per l."""
+        win = None if healpixwin is None else np.ascontiguousarray(healpixwin, dtype=np.float64)
+        check(load().cl2pt_plan_set_cmb(self.h, int(lmin), int(lmax), float(fwhm_arcmin),
+                                        0 if win is None else len(win), None if win is None else _p(win)),
+              "cl2pt_plan_set_cmb")
+
+    def cmb_real(self, omega_m, h0, chi, G, lnP, nuisance, lnPL=None):
+        """Real-space CMB-lensing cross-correlations (cl2pt_cmb_real):
+        w_gk [n][n_lens][ntheta], w_ks [n][n_source][ntheta]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        nt = self.cfg.ntheta
+        wgk = np.zeros((b.n, self.cfg.n_lens, nt))
+        wks = np.zeros((b.n, self.cfg.n_source, nt))
+        check(load().cl2pt_cmb_real(self.h, C.byref(b), wgk.ctypes.data, wks.ctypes.data, None),
+              "cl2pt_cmb_real")
+        return wgk, wks
 
     def eval_real(self, omega_m, h0, chi, G, lnP, nuisance, mask=None, pm=None, lnPL=None, out=None):
         """Host arrays in, host data vectors out ([n][n_total]); out: an

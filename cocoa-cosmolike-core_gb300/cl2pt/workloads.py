@@ -214,6 +214,16 @@ def scale_cuts(w: Workload, n: int, seed: int = 0):
     return np.asarray(ptr, dtype=np.int32), np.asarray(idx, dtype=np.int32)
 
 
+def cmb_map_filter():
+    """The CMB map filter of the real-space CMB-lensing cross-correlations
+    (init_cmb_cross_correlation's arguments): l in [2, 3000], a 5 arcmin
+    Gaussian beam, and a smooth stand-in for the HEALPix pixel window,
+    exp(-(l / 4000)^2) for l < 4500 (the reference reads the window of the
+    survey's nside from a file; none ships with it)."""
+    return dict(lmin=2, lmax=3000, fwhm_arcmin=5.0,
+                healpixwin=np.exp(-(np.arange(4500) / 4000.0) ** 2))
+
+
 def stack_lin(tabs):
     """The points' linear tables lnPL, [n][nk * nz] (numpy)."""
     return np.stack([np.ascontiguousarray(t.lnPL).reshape(-1) for t in tabs])

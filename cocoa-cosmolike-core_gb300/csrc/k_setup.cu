@@ -843,6 +843,32 @@ void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cu
   k_cmb_cl<<<dim3(P.B, P.nl + P.ns + 1, (nell + CMB_NT - 1) / CMB_NT), CMB_NT, 0, s>>>(P, nell, ell, out);
 }
 
+// w_gk_tomo / w_ks_tomo (cosmo2D.c:913-1296, limber = 1): the C_gk and C_ks
+// rows of k_cmb_cl on the lens C_l nodes (C [B][nl + ns + 1][nn]) summed
+// against the CMB-filtered, node-folded Legendre filters F [2][nt][nn]
+// (w(theta) filter for C_gk, gamma_t filter for C_ks); w [B][nl + ns][nt].
+// One warp per (point, spectrum, theta bin), FP64.
+__global__ void k_cmb_wtheta(int B, int nl, int ns, int nn, const double* __restrict__ C,
+                             const double* __restrict__ F, int nt, double* __restrict__ w)
+{
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nr = nl + ns;
+  if (warp >= B * nr * nt) return;
+  const int i = warp % nt, r = (warp / nt) % nr, pt = warp / (nt * nr);
+  const double* c = C + ((size_t)pt * (nr + 1) + r) * nn;
+  const double* f = F + ((size_t)(r < nl ? 0 : 1) * nt + i) * nn;
+  double acc = 0.0;
+  for (int j = lane; j < nn; j += 32) acc += f[j] * c[j];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) w[((size_t)pt * nr + r) * nt + i] = acc;
+}
+
+void launch_cmb_wtheta(const Params& P, int nn, const double* C, const double* F, int nt, double* w, cudaStream_t s)
+{
+  const int warps = P.B * (P.nl + P.ns) * nt;
+  if (warps > 0) k_cmb_wtheta<<<(warps * 32 + 255) / 256, 256, 0, s>>>(P.B, P.nl, P.ns, nn, C, F, nt, w);
+}
+
 // Input validation of host batches after staging (the reference rejects
 // non-finite values in its setters): one grid-stride pass, one flag.
 __global__ void k_check_finite(const double* __restrict__ x, size_t n, int* flag)

@@ -38,6 +38,9 @@ void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double*
 // C_gk, C_ks, C_kk of the 6x2pt probes at ell[0..nell) (device), out
 // [B][nl + ns + 1][nell]
 void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cudaStream_t s);
+// w_gk, w_ks from k_cmb_cl's rows on the nn lens C_l nodes and the folded
+// CMB filters F [2][nt][nn]; w [B][nl + ns][nt]
+void launch_cmb_wtheta(const Params& P, int nn, const double* C, const double* F, int nt, double* w, cudaStream_t s);
 // dst[pt][e] = src[pt][e] + add[e] for B points of n entries (the baryon
 // ratio on the wave's nonlinear table)
 void launch_add_table(const double* src, const double* add, double* dst, int B, size_t n, cudaStream_t s);

@@ -229,6 +229,17 @@ void legendre_filters(int L, double xmin, double xmax, double* Gp, double* Gm, d
   }
 }
 
+// cos of the edges of theta bin i (log-spaced bins, set_bin_average,
+// basics.c:382-400)
+void theta_bin_x(const cl2pt_config& c, int i, double* xmin, double* xmax)
+{
+  const double vtmin = c.theta_min_arcmin * 2.90888208665721580e-4;
+  const double vtmax = c.theta_max_arcmin * 2.90888208665721580e-4;
+  const double logdt = (log(vtmax) - log(vtmin)) / c.ntheta;
+  *xmin = cos(exp(log(vtmin) + (i + 0.) * logdt));
+  *xmax = cos(exp(log(vtmin) + (i + 1.) * logdt));
+}
+
 // Fold a per-l filter f[1..L-1] onto C_l nodes: integer multipoles
 // 1..nint stay as they are (columns 0..nint-1), multipoles lfill..L-1 are
 // spread on the n_ell log nodes (columns nint..) with the fill's weights.
@@ -434,12 +445,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   std::vector<double> fxi((size_t)2 * nt * p->nnode_ss, 0.0), fgt((size_t)nt * p->nnode_g, 0.0),
       fgg((size_t)nt * p->nnode_g, 0.0), fggnl((size_t)nt * (LNL + p->nnode_g), 0.0);
   {
-    const double vtmin = cfg->theta_min_arcmin * 2.90888208665721580e-4;
-    const double vtmax = cfg->theta_max_arcmin * 2.90888208665721580e-4;
-    const double logdt = (log(vtmax) - log(vtmin)) / nt;
     auto work = [&](int i) {
-      const double xmin = cos(exp(log(vtmin) + (i + 0.) * logdt));
-      const double xmax = cos(exp(log(vtmin) + (i + 1.) * logdt));
+      double xmin, xmax;
+      theta_bin_x(*cfg, i, &xmin, &xmax);
       std::vector<double> Gp(L), Gm(L), Pgt(L), Pgg(L);
       legendre_filters(L, xmin, xmax, Gp.data(), Gm.data(), Pgt.data(), Pgg.data());
       fold(Gp.data(), L, p->nint, cfg->lmin_tab, p->lim_ss, cfg->n_ell,
@@ -1015,6 +1023,47 @@ extern "C" int cl2pt_plan_set_baryon_ratio(cl2pt_plan* p, int nk, const double* 
   return CL2PT_OK;
 }
 
+extern "C" int cl2pt_plan_set_cmb(cl2pt_plan* p, int lmin, int lmax, double fwhm_arcmin, int healpixwin_ncls,
+                                  const double* healpixwin)
+{
+  if (!p) return CL2PT_ERR_ARG;
+  if (!std::isfinite(fwhm_arcmin) || fwhm_arcmin < 0 || healpixwin_ncls < 0 || (healpixwin_ncls > 0 && !healpixwin))
+    return CL2PT_ERR_ARG;
+  if (!all_finite(healpixwin, healpixwin_ncls)) return CL2PT_ERR_ARG;
+  const cl2pt_config& c = p->cfg;
+  const int nt = c.ntheta, L = c.lmax, nn = p->nnode_g;
+  // beam_cmb x w_pixel (cosmo2D.c:270-282), fwhm in rad as the reference
+  // stores it (generic_interface.cpp:518-519)
+  const double s = fwhm_arcmin * 2.90888208665721580e-4 / sqrt(16.0 * log(2.0));
+  std::vector<double> cmbf(L, 0.0);
+  for (int l = 0; l < L; l++) {
+    double f = (l < lmin || l > lmax) ? 0.0 : exp(-l * (l + 1.0) * s * s);
+    if (healpixwin_ncls > 0) f *= (l < healpixwin_ncls) ? healpixwin[l] : 0.0;
+    cmbf[l] = f;
+  }
+  // w_gk with the w(theta) filter, w_ks with the gamma_t filter
+  // (cosmo2D.c:975-981, 1166-1172), both times the map filter, folded on
+  // the lens C_l nodes (C_gk / C_ks tables share their ln l grid)
+  std::vector<double> F((size_t)2 * nt * nn, 0.0);
+  std::vector<double> Gp(L), Gm(L), Pgt(L), Pgg(L);
+  for (int i = 0; i < nt; i++) {
+    double xmin, xmax;
+    theta_bin_x(c, i, &xmin, &xmax);
+    legendre_filters(L, xmin, xmax, Gp.data(), Gm.data(), Pgt.data(), Pgg.data());
+    for (int l = 0; l < L; l++) {
+      Pgg[l] *= cmbf[l];
+      Pgt[l] *= cmbf[l];
+    }
+    fold(Pgg.data(), L, p->nint, c.lmin_tab, p->lim_g, c.n_ell, F.data() + (size_t)i * nn);
+    fold(Pgt.data(), L, p->nint, c.lmin_tab, p->lim_g, c.n_ell, F.data() + (size_t)(nt + i) * nn);
+  }
+  if (!p->d_cmb_filt)
+    if (int st = dalloc(p, &p->d_cmb_filt, F.size())) return st;
+  CUDA_OK(cudaMemcpy(p->d_cmb_filt, F.data(), sizeof(double) * F.size(), cudaMemcpyHostToDevice));
+  p->cmb_on = true;
+  return CL2PT_OK;
+}
+
 extern "C" int cl2pt_plan_get_contraction(const cl2pt_plan* p, int* mode)
 {
   if (!p || !mode) return CL2PT_ERR_ARG;
@@ -1354,35 +1403,36 @@ extern "C" int cl2pt_scut_ss_rf(cl2pt_plan* p, const cl2pt_batch* b, int nreq, c
   return scut_run(p, b, 1, nreq, kmax, nreq, l, nullptr, rf, (cudaStream_t)stream);
 }
 
-// CMB-lensing spectra of the 6x2pt probes (C_gk, C_ks, C_kk) at the
-// caller's multipoles: per wave the set-up stage (lens efficiencies, the
-// one-loop bias tables when the plan has them) and k_cmb_cl, whose rows are
-// split into the three outputs.
-extern "C" int cl2pt_cmb_cl(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell, double* C_gk,
-                            double* C_ks, double* C_kk, void* stream)
+// CMB-lensing spectra of the 6x2pt probes: per wave the set-up stage (lens
+// efficiencies, the one-loop bias tables when the plan has them), then
+// k_cmb_cl at the multipoles; real == false: C_gk, C_ks, C_kk at the
+// caller's multipoles (o0, o1, o2); real == true: the spectra on the lens
+// C_l nodes and their sums with the CMB-filtered Legendre filters, w_gk
+// and w_ks (o0, o1).
+static int cmb_run(cl2pt_plan* p, const cl2pt_batch* b, bool real, int nell, const double* ell, double* o0,
+                   double* o1, double* o2, cudaStream_t s)
 {
-  if (!p || !b || nell < 1 || !ell || (!C_gk && !C_ks && !C_kk)) return CL2PT_ERR_ARG;
   if (int st = check_batch(p, b, true)) return st;
-  for (int i = 0; i < nell; i++)
-    if (!(ell[i] >= 0) || !std::isfinite(ell[i])) return CL2PT_ERR_ARG;
   // the distance table must reach the last-scattering surface, z = 1090
   if (p->chi_z.empty() || !(p->chi_z.back() >= 1090.0)) return CL2PT_ERR_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
   const int n = b->n;
   const Params& T = p->P;
   DevBatch d;
   if (int st = stage_batch_inputs(p, b, s, &d)) return st;
   const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
-  const int nl = T.nl, ns = T.ns, nrow = nl + ns + 1;
+  const int nl = T.nl, ns = T.ns, nrow = nl + ns + 1, nt = p->cfg.ntheta;
   const int W = p->wave;
-  double *dl = nullptr, *dout = nullptr;
+  double *dl = nullptr, *dout = nullptr, *dw = nullptr;
   int st = CL2PT_OK;
   auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
-  fail(cudaMalloc((void**)&dl, sizeof(double) * nell));
+  if (!real) {
+    fail(cudaMalloc((void**)&dl, sizeof(double) * nell));
+    if (!st) fail(cudaMemcpyAsync(dl, ell, sizeof(double) * nell, cudaMemcpyHostToDevice, s));
+  } else {
+    fail(cudaMalloc((void**)&dw, sizeof(double) * (size_t)W * (nl + ns) * nt));
+  }
   fail(cudaMalloc((void**)&dout, sizeof(double) * (size_t)W * nrow * nell));
-  if (!st) fail(cudaMemcpyAsync(dl, ell, sizeof(double) * nell, cudaMemcpyHostToDevice, s));
   const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  const size_t row = sizeof(double) * nell;
   cl2pt::Hook hk;
   int launches = 0;
   for (int w0 = 0; w0 < n && !st; w0 += W) {
@@ -1410,27 +1460,55 @@ extern "C" int cl2pt_cmb_cl(cl2pt_plan* p, const cl2pt_batch* b, int nell, const
       Pb.tatt = 0;  // the bias rows alone
       cl2pt::launch_fpt_tables(Pb, p->d_fpt_bias_out, nullptr, s, &launches);
     }
-    cl2pt::launch_cmb_cl(P, nell, dl, dout, s);
+    cl2pt::launch_cmb_cl(P, nell, real ? p->d_ell_g : dl, dout, s);
     fail(cudaGetLastError());
-    const size_t pitch = row * nrow;
-    if (C_gk && nl > 0)
-      fail(cudaMemcpy2DAsync(C_gk + (size_t)w0 * nl * nell, row * nl, dout, pitch, row * nl, P.B, kind, s));
-    if (C_ks && ns > 0)
-      fail(cudaMemcpy2DAsync(C_ks + (size_t)w0 * ns * nell, row * ns, dout + (size_t)nl * nell, pitch, row * ns,
-                             P.B, kind, s));
-    if (C_kk)
-      fail(cudaMemcpy2DAsync(C_kk + (size_t)w0 * nell, row, dout + (size_t)(nl + ns) * nell, pitch, row, P.B, kind,
-                             s));
+    if (real) {
+      cl2pt::launch_cmb_wtheta(P, nell, dout, p->d_cmb_filt, nt, dw, s);
+      fail(cudaGetLastError());
+      const size_t row = sizeof(double) * nt, pitch = row * (nl + ns);
+      if (o0 && nl > 0)
+        fail(cudaMemcpy2DAsync(o0 + (size_t)w0 * nl * nt, row * nl, dw, pitch, row * nl, P.B, kind, s));
+      if (o1 && ns > 0)
+        fail(cudaMemcpy2DAsync(o1 + (size_t)w0 * ns * nt, row * ns, dw + (size_t)nl * nt, pitch, row * ns, P.B,
+                               kind, s));
+    } else {
+      const size_t row = sizeof(double) * nell, pitch = row * nrow;
+      if (o0 && nl > 0)
+        fail(cudaMemcpy2DAsync(o0 + (size_t)w0 * nl * nell, row * nl, dout, pitch, row * nl, P.B, kind, s));
+      if (o1 && ns > 0)
+        fail(cudaMemcpy2DAsync(o1 + (size_t)w0 * ns * nell, row * ns, dout + (size_t)nl * nell, pitch, row * ns,
+                               P.B, kind, s));
+      if (o2)
+        fail(cudaMemcpy2DAsync(o2 + (size_t)w0 * nell, row, dout + (size_t)(nl + ns) * nell, pitch, row, P.B,
+                               kind, s));
+    }
     fail(cudaStreamSynchronize(s));
   }
   cudaFree(dl);
   cudaFree(dout);
+  cudaFree(dw);
   if (!st) {
     int e = 0;
     fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) st = CL2PT_ERR_DEVICE;
   }
   return st;
+}
+
+extern "C" int cl2pt_cmb_cl(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell, double* C_gk,
+                            double* C_ks, double* C_kk, void* stream)
+{
+  if (!p || !b || nell < 1 || !ell || (!C_gk && !C_ks && !C_kk)) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nell; i++)
+    if (!(ell[i] >= 0) || !std::isfinite(ell[i])) return CL2PT_ERR_ARG;
+  return cmb_run(p, b, false, nell, ell, C_gk, C_ks, C_kk, (cudaStream_t)stream);
+}
+
+extern "C" int cl2pt_cmb_real(cl2pt_plan* p, const cl2pt_batch* b, double* w_gk, double* w_ks, void* stream)
+{
+  if (!p || !b || (!w_gk && !w_ks)) return CL2PT_ERR_ARG;
+  if (!p->cmb_on) return CL2PT_ERR_STATE;
+  return cmb_run(p, b, true, p->nnode_g, nullptr, w_gk, w_ks, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int cl2pt_fourier_sizes(const cl2pt_plan* p, int nell, int* n_ss, int* n_gs, int* n_gg,

@@ -105,6 +105,11 @@ struct cl2pt_plan {
   double* d_bary_lnr = nullptr;
   double* d_lnP_bary = nullptr;
   bool bary_on = false;
+  // CMB map filter of the real-space CMB-lensing cross-correlations
+  // (cl2pt_plan_set_cmb): the w(theta) and gamma_t filters times the beam
+  // and pixel window, folded on the C_l nodes, [2][ntheta][nnode_g]
+  double* d_cmb_filt = nullptr;
+  bool cmb_on = false;
   double* d_vjp_cot = nullptr;         // [max_batch][n_total] (grown for Fourier vectors)
   size_t vjp_cot_cap = 0;
   double* d_vjp_lnp = nullptr;         // [max_batch][pk_nk * pk_nz]

@@ -364,6 +364,23 @@ int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const
 int cl2pt_cmb_cl(cl2pt_plan* plan, const cl2pt_batch* batch, int nell, const double* ell, double* C_gk,
                  double* C_ks, double* C_kk, void* stream);
 
+/* The CMB map filter of the real-space CMB-lensing cross-correlations
+ * (init_cmb_cross_correlation, generic_interface.cpp:507-523): a Gaussian
+ * beam of fwhm_arcmin on lmin <= l <= lmax (beam_cmb, cosmo2D.c:270-273)
+ * times, when healpixwin_ncls > 0, the HEALPix pixel window healpixwin[l]
+ * for l < healpixwin_ncls (0 above; w_pixel, :275-280; the reference reads
+ * it from column 1 of a file). */
+int cl2pt_plan_set_cmb(cl2pt_plan* plan, int lmin, int lmax, double fwhm_arcmin, int healpixwin_ncls,
+                       const double* healpixwin);
+/* Real-space CMB-lensing cross-correlations on the plan's theta bins,
+ * w_gk[n][n_lens][ntheta] (w_gk_tomo, cosmo2D.c:913-1101: the w(theta)
+ * filter) and w_ks[n][n_source][ntheta] (w_ks_tomo, :1105-1296: the
+ * gamma_t filter), limber = 1: C_l at integer l below lmin_tab, the
+ * n_ell-node ln l table filled linearly above, times the map filter.
+ * Needs cl2pt_plan_set_cmb (else CL2PT_ERR_STATE) and a distance table to
+ * z = 1090; either output may be NULL; outputs follow batch->where. */
+int cl2pt_cmb_real(cl2pt_plan* plan, const cl2pt_batch* batch, double* w_gk, double* w_ks, void* stream);
+
 /* Where the mixed plan's FFTLog multipole loop keeps its spectra and
  * Gamma-recurrence state: CL2PT_FFTLOG_STATE_AUTO (the default: global
  * memory, unless cl2pt_plan_autotune chose otherwise), _GLOBAL (global

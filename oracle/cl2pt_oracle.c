@@ -1322,6 +1322,84 @@ int orc_w_gammat(double* out)
   return CL2PT_OK;
 }
 
+/* ---- real-space CMB-lensing cross-correlations (6x2pt) */
+/* the CMB map filter: beam_cmb x w_pixel (cosmo2D.c:270-282); fwhm in rad
+ * (init_cmb_cross_correlation, generic_interface.cpp:507-523, takes it in
+ * arcmin), the pixel window only when one is set */
+static struct { double fwhm; int lmin, lmax, ncls; double* win; } cmbp;
+int orc_set_cmb(int lmin, int lmax, double fwhm_rad, int ncls, const double* win)
+{
+  cmbp.fwhm = fwhm_rad;
+  cmbp.lmin = lmin;
+  cmbp.lmax = lmax;
+  free(cmbp.win);
+  cmbp.win = NULL;
+  cmbp.ncls = ncls > 0 ? ncls : 0;
+  if (cmbp.ncls) {
+    cmbp.win = malloc(sizeof(double) * cmbp.ncls);
+    memcpy(cmbp.win, win, sizeof(double) * cmbp.ncls);
+  }
+  return CL2PT_OK;
+}
+static double cmb_filter(int l)
+{
+  const double s = cmbp.fwhm / sqrt(16.0 * log(2.0));
+  double f = (l < cmbp.lmin || l > cmbp.lmax) ? 0.0 : exp(-l * (l + 1.0) * s * s);
+  if (cmbp.ncls > 0) f *= (l < cmbp.ncls) ? cmbp.win[l] : 0.0;
+  return f;
+}
+/* w_gk_tomo (cosmo2D.c:913-1101; kind 0, w(theta) filter, lens bins) and
+ * w_ks_tomo (1105-1296; kind 1, gamma_t filter, source bins), limber = 1:
+ * C_l x filter at integer l below LMIN_tab, the N_ell-node table in ln l
+ * (C_gk_tomo_limber / C_ks_tomo_limber, lim from LMIN_tab to LMAX + 1)
+ * filled linearly above, times the filter; out [nbin][ntheta] */
+static int w_cmb(int kind, double* out)
+{
+  if (!g.have_point) return CL2PT_ERR_STATE;
+  if (!g.have_filters) build_filters();
+  /* the lazily built tables, before the threads read them */
+  if (!g.have_g) build_g_tables();
+  if (kind == 0 && has_b2_galaxies()) need_fptb();
+  const int L = g.cfg.lmax, nt = g.cfg.ntheta, nell = g.cfg.n_ell;
+  const int nb = kind == 0 ? g.cfg.n_lens : g.cfg.n_source;
+  double lim[3];
+  lim[0] = log(fmax(g.cfg.lmin_tab, 1.0));
+  lim[1] = log(L + 1);
+  lim[2] = (lim[1] - lim[0]) / ((double)nell - 1.0);
+  double* cmbf = malloc(sizeof(double) * L);
+  for (int l = 0; l < L; l++) cmbf[l] = cmb_filter(l);
+  double* Cl = calloc((size_t)nb * L, sizeof(double));
+  double* tab = malloc(sizeof(double) * (size_t)nb * nell);
+  #pragma omp parallel for collapse(2) schedule(static, 1)
+  for (int k = 0; k < nb; k++)
+    for (int i = 0; i < nell; i++) {
+      const double lx = exp(lim[0] + i * lim[2]);
+      tab[k * nell + i] = kind == 0 ? orc_C_gk_nointerp(lx, k) : orc_C_ks_nointerp(lx, k);
+    }
+  #pragma omp parallel for collapse(2) schedule(static, 1)
+  for (int k = 0; k < nb; k++)
+    for (int l = 1; l < g.cfg.lmin_tab; l++)
+      Cl[k * L + l] = (kind == 0 ? orc_C_gk_nointerp(l, k) : orc_C_ks_nointerp(l, k)) * cmbf[l];
+  for (int k = 0; k < nb; k++) {
+    fill(tab + k * nell, lim, nell, g.cfg.lmin_tab, L, Cl + k * L);
+    for (int l = g.cfg.lmin_tab; l < L; l++) Cl[k * L + l] *= cmbf[l];
+  }
+  #pragma omp parallel for collapse(2) schedule(static, 1)
+  for (int k = 0; k < nb; k++)
+    for (int i = 0; i < nt; i++) {
+      const double* P = g.filt + ((kind == 0 ? 3 : 2) * nt + i) * L;
+      double s = 0.0;
+      for (int l = 1; l < L; l++) s += P[l] * Cl[k * L + l];
+      out[k * nt + i] = s;
+    }
+  free(cmbf);
+  free(Cl);
+  free(tab);
+  return CL2PT_OK;
+}
+int orc_w_gk(double* out) { return w_cmb(0, out); }
+int orc_w_ks(double* out) { return w_cmb(1, out); }
+
 /* ------------------------------------------------------------------------ */
 /* non-Limber clustering: C_cl_tomo + cfftlog_ells_p1/p2, cosmo2D.c:3995-4769 */
 /* ------------------------------------------------------------------------ */

@@ -240,6 +240,30 @@ class Oracle:
         f.argtypes = [C.c_double, C.c_int]
         return f(float(l), int(ni))
 
+    def set_cmb(self, lmin, lmax, fwhm_arcmin, healpixwin=None):
+        """The CMB map filter of w_gk / w_ks (init_cmb_cross_correlation):
+        beam fwhm in arcmin, l range, optional HEALPix window per l."""
+        win = None if healpixwin is None else np.ascontiguousarray(healpixwin, dtype=np.float64)
+        f = getattr(self.lib, self.which + "_set_cmb")
+        f.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, _dp]
+        self._cmbwin = win
+        st = f(int(lmin), int(lmax), float(fwhm_arcmin) * 2.90888208665721580e-4,
+               0 if win is None else len(win), None if win is None else _p(win))
+        if st != 0:
+            raise RuntimeError(f"set_cmb failed: {st}")
+
+    def w_cmb(self, which):
+        """Real-space CMB-lensing cross-correlations w_gk [n_lens][ntheta]
+        or w_ks [n_source][ntheta] (which: 'gk', 'ks')."""
+        nb = self.cfg.n_lens if which == "gk" else self.cfg.n_source
+        out = np.zeros((nb, self.cfg.ntheta))
+        f = getattr(self.lib, "%s_w_%s" % (self.which, which))
+        f.argtypes = [_dp]
+        st = f(_p(out))
+        if st != 0:
+            raise RuntimeError(f"w_{which} failed: {st}")
+        return out
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

@@ -250,6 +250,35 @@ double ref_C_gg_nointerp(double l, int ni, int use_linear_ps)
 double ref_C_gk_nointerp(double l, int ni) { return C_gk_tomo_limber_nointerp(l, ni, 0); }
 double ref_C_ks_nointerp(double l, int ni) { return C_ks_tomo_limber_nointerp(l, ni, 0); }
 double ref_C_kk_nointerp(double l) { return C_kk_limber_nointerp(l, 0); }
+/* init_cmb_cross_correlation (generic_interface.cpp:507-523) with the
+ * window as an array (column 1 of its file); fwhm in rad */
+int ref_set_cmb(int lmin, int lmax, double fwhm_rad, int ncls, const double* win)
+{
+  cmb.fwhm = fwhm_rad;
+  cmb.lmink_wxk = lmin;
+  cmb.lmaxk_wxk = lmax;
+  if (cmb.healpixwin != NULL) free(cmb.healpixwin);
+  cmb.healpixwin = NULL;
+  cmb.healpixwin_ncls = ncls > 0 ? ncls : 0;
+  if (cmb.healpixwin_ncls) {
+    cmb.healpixwin = (double*) malloc(sizeof(double) * cmb.healpixwin_ncls);
+    memcpy(cmb.healpixwin, win, sizeof(double) * cmb.healpixwin_ncls);
+  }
+  cmb.random = (double) next_token();
+  return 0;
+}
+int ref_w_gk(double* out)
+{
+  for (int i = 0; i < redshift.clustering_nbin; i++)
+    for (int t = 0; t < Ntable.Ntheta; t++) out[i * Ntable.Ntheta + t] = w_gk_tomo(t, i, 1);
+  return 0;
+}
+int ref_w_ks(double* out)
+{
+  for (int i = 0; i < redshift.shear_nbin; i++)
+    for (int t = 0; t < Ntable.Ntheta; t++) out[i * Ntable.Ntheta + t] = w_ks_tomo(t, i, 1);
+  return 0;
+}
 double ref_C_ss_limber(double l, int ni, int nj, int EE)
 {
   return C_ss_tomo_limber(l, ni, nj, EE);

@@ -52,9 +52,13 @@ def run_case(case, which="ref"):
     if case.startswith("cmb_lensing"):
         w = workloads.make(case)
         o.setup(w.cfg, w.src, w.lens)
+        f = workloads.cmb_map_filter()
+        o.set_cmb(f["lmin"], f["lmax"], f["fwhm_arcmin"], f["healpixwin"])
         tabs, nus = workloads.points(w, 2, seed=11)
         for i in range(2):
             o.set_point(tabs[i], nus[i])
+            out[f"wgk_{i}"] = o.w_cmb("gk")
+            out[f"wks_{i}"] = o.w_cmb("ks")
             out[f"Cgk_{i}"] = np.array([[o.C_cmb("gk", l, n) for l in w.ell] for n in range(w.cfg.n_lens)])
             out[f"Cks_{i}"] = np.array([[o.C_cmb("ks", l, n) for l in w.ell] for n in range(w.cfg.n_source)])
             out[f"Ckk_{i}"] = np.array([o.C_cmb("kk", l) for l in w.ell])
