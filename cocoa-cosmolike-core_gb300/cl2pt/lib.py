@@ -103,6 +103,9 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_cmb_cl.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]
     lib.cl2pt_plan_set_cmb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp]
+    lib.cl2pt_cmb_kk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_void_p, C.c_void_p]
+    lib.cl2pt_cmb_kk_bandpower.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                           C.c_void_p, C.c_void_p]
     lib.cl2pt_cmb_real.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p, C.c_void_p]
     lib.cl2pt_plan_set_baryon_ratio.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp]
     lib.cl2pt_plan_autotune.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_int, _ip, _ip,
@@ -274,6 +277,25 @@ class Plan:
         check(load().cl2pt_cmb_cl(self.h, C.byref(b), ne, _p(ell), gk.ctypes.data, ks.ctypes.data,
                                   kk.ctypes.data, None), "cl2pt_cmb_cl")
         return gk, ks, kk
+
+    def cmb_kk(self, omega_m, h0, chi, G, lnP, nuisance, ell, lnPL=None):
+        """C_kk [n][nell] by the 6x2pt data vector's rule (cl2pt_cmb_kk)."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        out = np.zeros((b.n, len(ell)))
+        check(load().cl2pt_cmb_kk(self.h, C.byref(b), len(ell), _p(ell), out.ctypes.data, None), "cl2pt_cmb_kk")
+        return out
+
+    def cmb_kk_bandpower(self, omega_m, h0, chi, G, lnP, nuisance, lminbp, lmaxbp, binmat, offset, lnPL=None):
+        """kk bandpowers [n][nbp] (cl2pt_cmb_kk_bandpower); binmat
+        [nbp][lmaxbp - lminbp + 1]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        bm = np.ascontiguousarray(binmat, dtype=np.float64)
+        off = np.ascontiguousarray(offset, dtype=np.float64)
+        out = np.zeros((b.n, bm.shape[0]))
+        check(load().cl2pt_cmb_kk_bandpower(self.h, C.byref(b), bm.shape[0], int(lminbp), int(lmaxbp), _p(bm),
+                                            _p(off), out.ctypes.data, None), "cl2pt_cmb_kk_bandpower")
+        return out
 
     def set_cmb(self, lmin, lmax, fwhm_arcmin, healpixwin=None):
         """The CMB map filter of w_gk / w_ks (cl2pt_plan_set_cmb): beam fwhm

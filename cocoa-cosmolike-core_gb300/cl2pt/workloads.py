@@ -224,6 +224,21 @@ def cmb_map_filter():
                 healpixwin=np.exp(-(np.arange(4500) / 4000.0) ** 2))
 
 
+def cmb_kk_bandpowers():
+    """A kk bandpower binning of the shape the reference reads from its
+    binning-matrix file: 8 log-spaced top-hat bands over L = 8..2000 with
+    weights 1/width, and a small seeded theory offset per band."""
+    lminbp, lmaxbp, nbp = 8, 2000, 8
+    edges = np.unique(np.round(np.geomspace(lminbp, lmaxbp + 1, nbp + 1)).astype(int))
+    L = np.arange(lminbp, lmaxbp + 1)
+    M = np.zeros((len(edges) - 1, len(L)))
+    for j in range(len(edges) - 1):
+        sel = (L >= edges[j]) & (L < edges[j + 1])
+        M[j, sel] = 1.0 / sel.sum()
+    off = np.random.default_rng(SEED0 + 77).normal(0.0, 1e-9, len(edges) - 1)
+    return lminbp, lmaxbp, M, off
+
+
 def stack_lin(tabs):
     """The points' linear tables lnPL, [n][nk * nz] (numpy)."""
     return np.stack([np.ascontiguousarray(t.lnPL).reshape(-1) for t in tabs])

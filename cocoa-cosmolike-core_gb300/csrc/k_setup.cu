@@ -714,7 +714,7 @@ __device__ __forceinline__ double fpt_lerp_d(const Params& P, const double* row,
   return (r - i) * (row[i + 1] - row[i]) + row[i];
 }
 
-__global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const double* __restrict__ ell,
+__global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const double* __restrict__ ell, int row0,
                                                    double* __restrict__ out)
 {
   // per node: a, fK, and the weights of P(k) (L: clustering / lensing, M:
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const dou
   __shared__ double sa[CMB_PC], sf[CMB_PC], sL[CMB_PC], sM[CMB_PC], sK[CMB_PC], s2[CMB_PC], ss2[CMB_PC],
       s3[CMB_PC];
   __shared__ int s_bad;
-  const int pt = blockIdx.x, set = blockIdx.y;
+  const int pt = blockIdx.x, set = row0 + blockIdx.y;
   const int kind = set < P.nl ? 0 : (set < P.nl + P.ns ? 1 : 2);  // 0 gk, 1 ks, 2 kk
   const int q = kind == 0 ? set : (kind == 1 ? set - P.nl : 0);
   const cl2pt_nuisance& nu = P.nu[pt];
@@ -834,13 +834,74 @@ __global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const dou
   if (threadIdx.x == 0 && s_bad) atomicOr(P.err, 1);
   if (il < nell) {
     const double pref = kind == 0 ? pref1 : (kind == 1 ? pref1 * pref2 : pref1 * pref1);
-    out[((size_t)pt * (P.nl + P.ns + 1) + set) * nell + il] = acc * pref;
+    out[((size_t)pt * gridDim.y + blockIdx.y) * nell + il] = acc * pref;
   }
 }
 
-void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cudaStream_t s)
+void launch_cmb_cl(const Params& P, int nell, const double* ell, int row0, int nrows, double* out, cudaStream_t s)
 {
-  k_cmb_cl<<<dim3(P.B, P.nl + P.ns + 1, (nell + CMB_NT - 1) / CMB_NT), CMB_NT, 0, s>>>(P, nell, ell, out);
+  k_cmb_cl<<<dim3(P.B, nrows, (nell + CMB_NT - 1) / CMB_NT), CMB_NT, 0, s>>>(P, nell, ell, row0, out);
+}
+
+// C_kk as the 6x2pt data vector reads it (generic_interface.hpp:1084-1118)
+// from k_cmb_cl's kk row on the list [direct multipoles][n_ell table
+// nodes] (C [B][nd + nn]): request i takes direct value src[i] (l <=
+// lmin_tab: C_kk_limber_nointerp) or, for src[i] < 0, C_kk_limber's
+// interpolation, linear in ln l on the nodes (interpol1d, the end values
+// outside the table); out [B][nreq]
+__global__ void k_cmb_kk_eval(int B, int nd, int nn, const double* __restrict__ C, int nreq,
+                              const double* __restrict__ req, const int* __restrict__ src, double lim0, double lim2,
+                              double* __restrict__ out)
+{
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * nreq) return;
+  const int pt = idx / nreq, i = idx - pt * nreq;
+  const double* c = C + (size_t)pt * (nd + nn);
+  double v;
+  if (src[i] >= 0) {
+    v = c[src[i]];
+  } else {
+    const double* t = c + nd;
+    const double x = log(req[i]);
+    if (x < lim0) {
+      v = t[0];
+    } else {
+      const double r = (x - lim0) / lim2;
+      const int j = (int)floor(r);
+      v = (j + 1 >= nn) ? t[nn - 1] : (r - j) * (t[j + 1] - t[j]) + t[j];
+    }
+  }
+  out[idx] = v;
+}
+
+// kk bandpowers (generic_interface.hpp:1097-1118): bp[j] = sum_L C_kk(L)
+// M[j][L - lminbp] - offset[j] with Ck [B][nL] from k_cmb_kk_eval; one warp
+// per (point, band), FP64
+__global__ void k_cmb_bandpower(int B, int nL, const double* __restrict__ Ck, int nbp, const double* __restrict__ M,
+                                const double* __restrict__ off, double* __restrict__ bp)
+{
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= B * nbp) return;
+  const int pt = warp / nbp, j = warp - pt * nbp;
+  const double* c = Ck + (size_t)pt * nL;
+  const double* m = M + (size_t)j * nL;
+  double acc = 0.0;
+  for (int L = lane; L < nL; L += 32) acc += c[L] * m[L];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) bp[warp] = acc - off[j];
+}
+
+void launch_cmb_kk_eval(int B, int nd, int nn, const double* C, int nreq, const double* req, const int* src,
+                        double lim0, double lim2, double* out, cudaStream_t s)
+{
+  const int n = B * nreq;
+  if (n > 0) k_cmb_kk_eval<<<(n + 127) / 128, 128, 0, s>>>(B, nd, nn, C, nreq, req, src, lim0, lim2, out);
+}
+void launch_cmb_bandpower(int B, int nL, const double* Ck, int nbp, const double* M, const double* off, double* bp,
+                          cudaStream_t s)
+{
+  const int warps = B * nbp;
+  if (warps > 0) k_cmb_bandpower<<<(warps * 32 + 255) / 256, 256, 0, s>>>(B, nL, Ck, nbp, M, off, bp);
 }
 
 // w_gk_tomo / w_ks_tomo (cosmo2D.c:913-1296, limber = 1): the C_gk and C_ks

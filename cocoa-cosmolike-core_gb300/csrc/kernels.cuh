@@ -35,9 +35,16 @@ void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const do
                       double* dC, double* dlnC, cudaStream_t s);
 void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
                     const double* tw, const double* css, double* rf, cudaStream_t s);
-// C_gk, C_ks, C_kk of the 6x2pt probes at ell[0..nell) (device), out
-// [B][nl + ns + 1][nell]
-void launch_cmb_cl(const Params& P, int nell, const double* ell, double* out, cudaStream_t s);
+// C_gk, C_ks, C_kk of the 6x2pt probes at ell[0..nell) (device): spectrum
+// rows [row0, row0 + nrows) of [0, nl) gk, [nl, nl + ns) ks, nl + ns kk;
+// out [B][nrows][nell]
+void launch_cmb_cl(const Params& P, int nell, const double* ell, int row0, int nrows, double* out, cudaStream_t s);
+// C_kk by the data vector's rule from the kk row on [direct][nodes], and
+// the kk bandpowers
+void launch_cmb_kk_eval(int B, int nd, int nn, const double* C, int nreq, const double* req, const int* src,
+                        double lim0, double lim2, double* out, cudaStream_t s);
+void launch_cmb_bandpower(int B, int nL, const double* Ck, int nbp, const double* M, const double* off, double* bp,
+                          cudaStream_t s);
 // w_gk, w_ks from k_cmb_cl's rows on the nn lens C_l nodes and the folded
 // CMB filters F [2][nt][nn]; w [B][nl + ns][nt]
 void launch_cmb_wtheta(const Params& P, int nn, const double* C, const double* F, int nt, double* w, cudaStream_t s);

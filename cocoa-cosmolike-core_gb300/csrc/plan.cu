@@ -1384,7 +1384,10 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
   if (!st) {
     int e = 0;
     fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) st = CL2PT_ERR_DEVICE;
+    if (e) {
+      st = CL2PT_ERR_DEVICE;
+      cudaMemset(p->d_err, 0, sizeof(int));  // the next call starts clean
+    }
   }
   return st;
 }
@@ -1460,7 +1463,7 @@ static int cmb_run(cl2pt_plan* p, const cl2pt_batch* b, bool real, int nell, con
       Pb.tatt = 0;  // the bias rows alone
       cl2pt::launch_fpt_tables(Pb, p->d_fpt_bias_out, nullptr, s, &launches);
     }
-    cl2pt::launch_cmb_cl(P, nell, real ? p->d_ell_g : dl, dout, s);
+    cl2pt::launch_cmb_cl(P, nell, real ? p->d_ell_g : dl, 0, nrow, dout, s);
     fail(cudaGetLastError());
     if (real) {
       cl2pt::launch_cmb_wtheta(P, nell, dout, p->d_cmb_filt, nt, dw, s);
@@ -1490,9 +1493,121 @@ static int cmb_run(cl2pt_plan* p, const cl2pt_batch* b, bool real, int nell, con
   if (!st) {
     int e = 0;
     fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) st = CL2PT_ERR_DEVICE;
+    if (e) {
+      st = CL2PT_ERR_DEVICE;
+      cudaMemset(p->d_err, 0, sizeof(int));  // the next call starts clean
+    }
   }
   return st;
+}
+
+// C_kk as the 6x2pt data vector reads it, at nreq multipoles (kk) or summed
+// into bandpowers (M [nbp][lmaxbp - lminbp + 1], offset [nbp]; bp): the kk
+// row of k_cmb_cl on [the requests at l <= lmin_tab][the n_ell ln l table
+// nodes of C_kk_limber, LMIN_tab to LMAX + 1], then the rule's evaluation.
+static int cmb_kk_run(cl2pt_plan* p, const cl2pt_batch* b, int nreq, const double* req, int nbp,
+                      const double* M, const double* off, double* kk, double* bp, cudaStream_t s)
+{
+  if (int st = check_batch(p, b, true)) return st;
+  if (p->chi_z.empty() || !(p->chi_z.back() >= 1090.0)) return CL2PT_ERR_ARG;
+  const int n = b->n;
+  const Params& T = p->P;
+  DevBatch d;
+  if (int st = stage_batch_inputs(p, b, s, &d)) return st;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const int nn = p->cfg.n_ell;
+  std::vector<double> list;
+  std::vector<int> src(nreq, -1);
+  for (int i = 0; i < nreq; i++)
+    if (req[i] <= p->cfg.lmin_tab) {
+      src[i] = (int)list.size();
+      list.push_back(req[i]);
+    }
+  const int nd = (int)list.size();
+  for (int i = 0; i < nn; i++) list.push_back(exp(p->lim_g[0] + i * p->lim_g[2]));
+  const int nlist = (int)list.size(), W = p->wave;
+  double *dlist = nullptr, *dreq = nullptr, *dC = nullptr, *dk = nullptr, *dM = nullptr, *dbp = nullptr;
+  int* dsrc = nullptr;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&dlist, sizeof(double) * nlist));
+  fail(cudaMalloc((void**)&dreq, sizeof(double) * nreq));
+  fail(cudaMalloc((void**)&dsrc, sizeof(int) * nreq));
+  fail(cudaMalloc((void**)&dC, sizeof(double) * (size_t)W * nlist));
+  fail(cudaMalloc((void**)&dk, sizeof(double) * (size_t)W * nreq));
+  if (bp) {
+    fail(cudaMalloc((void**)&dM, sizeof(double) * ((size_t)nbp * nreq + nbp)));
+    fail(cudaMalloc((void**)&dbp, sizeof(double) * (size_t)W * nbp));
+  }
+  if (!st) {
+    fail(cudaMemcpyAsync(dlist, list.data(), sizeof(double) * nlist, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dreq, req, sizeof(double) * nreq, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dsrc, src.data(), sizeof(int) * nreq, cudaMemcpyHostToDevice, s));
+    if (bp) {
+      fail(cudaMemcpyAsync(dM, M, sizeof(double) * (size_t)nbp * nreq, cudaMemcpyHostToDevice, s));
+      fail(cudaMemcpyAsync(dM + (size_t)nbp * nreq, off, sizeof(double) * nbp, cudaMemcpyHostToDevice, s));
+    }
+  }
+  const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  for (int w0 = 0; w0 < n && !st; w0 += W) {
+    Params P = T;
+    P.B = std::min(W, n - w0);
+    P.omega_m = d.om + w0;
+    P.h0 = d.h0 + w0;
+    P.chi = d.chi + (size_t)w0 * nchi;
+    P.G = d.G + (size_t)w0 * nG;
+    P.lnP = d.lnP + (size_t)w0 * nP;
+    P.lnPL = d.lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    if (p->bary_on) {
+      cl2pt::launch_add_table(P.lnP, p->d_bary_lnr, p->d_lnP_bary, P.B, nP, s);
+      P.lnP = p->d_lnP_bary;
+    }
+    P.nu = d.nu + w0;
+    // the kk row needs neither lens efficiencies nor bias tables
+    cl2pt::launch_cmb_cl(P, nlist, dlist, T.nl + T.ns, 1, dC, s);
+    cl2pt::launch_cmb_kk_eval(P.B, nd, nn, dC, nreq, dreq, dsrc, p->lim_g[0], p->lim_g[2], dk, s);
+    if (bp) cl2pt::launch_cmb_bandpower(P.B, nreq, dk, nbp, dM, dM + (size_t)nbp * nreq, dbp, s);
+    fail(cudaGetLastError());
+    if (kk) fail(cudaMemcpyAsync(kk + (size_t)w0 * nreq, dk, sizeof(double) * P.B * nreq, kind, s));
+    if (bp) fail(cudaMemcpyAsync(bp + (size_t)w0 * nbp, dbp, sizeof(double) * P.B * nbp, kind, s));
+    fail(cudaStreamSynchronize(s));
+  }
+  cudaFree(dlist);
+  cudaFree(dreq);
+  cudaFree(dsrc);
+  cudaFree(dC);
+  cudaFree(dk);
+  cudaFree(dM);
+  cudaFree(dbp);
+  if (!st) {
+    int e = 0;
+    fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+      st = CL2PT_ERR_DEVICE;
+      cudaMemset(p->d_err, 0, sizeof(int));  // the next call starts clean
+    }
+  }
+  return st;
+}
+
+extern "C" int cl2pt_cmb_kk(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell, double* C_kk,
+                            void* stream)
+{
+  if (!p || !b || nell < 1 || !ell || !C_kk) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nell; i++)
+    if (!(ell[i] > 0) || !std::isfinite(ell[i])) return CL2PT_ERR_ARG;
+  return cmb_kk_run(p, b, nell, ell, 0, nullptr, nullptr, C_kk, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int cl2pt_cmb_kk_bandpower(cl2pt_plan* p, const cl2pt_batch* b, int nbp, int lminbp, int lmaxbp,
+                                      const double* binmat, const double* offset, double* bp, void* stream)
+{
+  if (!p || !b || nbp < 1 || lminbp < 1 || lmaxbp < lminbp || !binmat || !offset || !bp) return CL2PT_ERR_ARG;
+  const int nL = lmaxbp - lminbp + 1;
+  if (!all_finite(binmat, nbp * nL) || !all_finite(offset, nbp)) return CL2PT_ERR_ARG;
+  std::vector<double> L(nL);
+  for (int i = 0; i < nL; i++) L[i] = (double)(lminbp + i);
+  return cmb_kk_run(p, b, nL, L.data(), nbp, binmat, offset, nullptr, bp, (cudaStream_t)stream);
 }
 
 extern "C" int cl2pt_cmb_cl(cl2pt_plan* p, const cl2pt_batch* b, int nell, const double* ell, double* C_gk,

@@ -364,6 +364,18 @@ int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const
 int cl2pt_cmb_cl(cl2pt_plan* plan, const cl2pt_batch* batch, int nell, const double* ell, double* C_gk,
                  double* C_ks, double* C_kk, void* stream);
 
+/* C_kk as the 6x2pt data vector reads it (generic_interface.hpp:1084-1118):
+ * C_kk_limber_nointerp at l <= lmin_tab, else C_kk_limber (cosmo2D.c:
+ * 3484-3516), linear in ln l on n_ell nodes from lmin_tab to lmax + 1 (the
+ * end values outside).  cl2pt_cmb_kk: at ell[0..nell) (host, > 0), C_kk
+ * [n][nell]; cl2pt_cmb_kk_bandpower: bp[n][nbp] = sum over L = lminbp ..
+ * lmaxbp of C_kk(L) binmat[j][L - lminbp] minus offset[j] (the bandpower
+ * branch, with the reference's binning matrix and theory offset). */
+int cl2pt_cmb_kk(cl2pt_plan* plan, const cl2pt_batch* batch, int nell, const double* ell, double* C_kk,
+                 void* stream);
+int cl2pt_cmb_kk_bandpower(cl2pt_plan* plan, const cl2pt_batch* batch, int nbp, int lminbp, int lmaxbp,
+                           const double* binmat, const double* offset, double* bp, void* stream);
+
 /* The CMB map filter of the real-space CMB-lensing cross-correlations
  * (init_cmb_cross_correlation, generic_interface.cpp:507-523): a Gaussian
  * beam of fwhm_arcmin on lmin <= l <= lmax (beam_cmb, cosmo2D.c:270-273)

@@ -1400,6 +1400,52 @@ static int w_cmb(int kind, double* out)
 int orc_w_gk(double* out) { return w_cmb(0, out); }
 int orc_w_ks(double* out) { return w_cmb(1, out); }
 
+/* C_kk as the 6x2pt data vector reads it (generic_interface.hpp:1084-1118):
+ * C_kk_limber_nointerp at l <= LMIN_tab, else C_kk_limber (cosmo2D.c:
+ * 3484-3516), linear in ln l on the N_ell-node table from LMIN_tab to
+ * LMAX + 1 (interpol1d: the end values outside it) */
+static double* kk_table(double* lim)
+{
+  const int nell = g.cfg.n_ell;
+  lim[0] = log(fmax(g.cfg.lmin_tab, 1.0));
+  lim[1] = log(g.cfg.lmax + 1);
+  lim[2] = (lim[1] - lim[0]) / ((double)nell - 1.0);
+  double* tab = malloc(sizeof(double) * nell);
+  #pragma omp parallel for schedule(static, 1)
+  for (int i = 0; i < nell; i++) tab[i] = orc_C_kk_nointerp(exp(lim[0] + i * lim[2]));
+  return tab;
+}
+static double kk_dv(const double* tab, const double* lim, double l)
+{
+  return (l <= g.cfg.lmin_tab) ? orc_C_kk_nointerp(l) : interpol1d(tab, g.cfg.n_ell, lim[0], lim[1], lim[2], log(l));
+}
+int orc_C_kk_dv(int n, const double* ell, double* out)
+{
+  if (!g.have_point) return CL2PT_ERR_STATE;
+  double lim[3];
+  double* tab = kk_table(lim);
+  for (int i = 0; i < n; i++) out[i] = kk_dv(tab, lim, ell[i]);
+  free(tab);
+  return CL2PT_OK;
+}
+/* the kk bandpowers (generic_interface.hpp:1097-1118): sum over
+ * L = lminbp..lmaxbp of C_kk(L) x binmat[j][L - lminbp], minus offset[j] */
+int orc_kk_bandpower(int nbp, int lminbp, int lmaxbp, const double* binmat, const double* offset, double* out)
+{
+  if (!g.have_point) return CL2PT_ERR_STATE;
+  double lim[3];
+  double* tab = kk_table(lim);
+  const int nL = lmaxbp - lminbp + 1;
+  for (int j = 0; j < nbp; j++) out[j] = 0.0;
+  for (int L = lminbp; L < lmaxbp + 1; L++) {
+    const double c = kk_dv(tab, lim, (double)L);
+    for (int j = 0; j < nbp; j++) out[j] += c * binmat[(size_t)j * nL + (L - lminbp)];
+  }
+  for (int j = 0; j < nbp; j++) out[j] -= offset[j];
+  free(tab);
+  return CL2PT_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* non-Limber clustering: C_cl_tomo + cfftlog_ells_p1/p2, cosmo2D.c:3995-4769 */
 /* ------------------------------------------------------------------------ */

@@ -264,6 +264,28 @@ class Oracle:
             raise RuntimeError(f"w_{which} failed: {st}")
         return out
 
+    def C_kk_dv(self, ell):
+        """C_kk at ell by the 6x2pt data vector's rule (nointerp at
+        l <= lmin_tab, the ln l table above)."""
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        out = np.zeros(len(ell))
+        f = getattr(self.lib, self.which + "_C_kk_dv")
+        f.argtypes = [C.c_int, _dp, _dp]
+        if f(len(ell), _p(ell), _p(out)) != 0:
+            raise RuntimeError("C_kk_dv failed")
+        return out
+
+    def kk_bandpower(self, lminbp, lmaxbp, binmat, offset):
+        """kk bandpowers: binmat [nbp][lmaxbp - lminbp + 1], offset [nbp]."""
+        bm = np.ascontiguousarray(binmat, dtype=np.float64)
+        off = np.ascontiguousarray(offset, dtype=np.float64)
+        out = np.zeros(bm.shape[0])
+        f = getattr(self.lib, self.which + "_kk_bandpower")
+        f.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        if f(bm.shape[0], int(lminbp), int(lmaxbp), _p(bm), _p(off), _p(out)) != 0:
+            raise RuntimeError("kk_bandpower failed")
+        return out
+
     def set_direct_conv_size(self, n):
         """Transform length of the TATT direct convolutions (0: the reference's)."""
         self.lib.orc_set_direct_conv_size.argtypes = [C.c_long]

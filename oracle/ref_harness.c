@@ -279,6 +279,26 @@ int ref_w_ks(double* out)
     for (int t = 0; t < Ntable.Ntheta; t++) out[i * Ntable.Ntheta + t] = w_ks_tomo(t, i, 1);
   return 0;
 }
+/* the 6x2pt data vector's C_kk rule and bandpowers
+ * (generic_interface.hpp:1084-1118), restated around the reference's own
+ * C_kk_limber_nointerp / C_kk_limber */
+int ref_C_kk_dv(int n, const double* ell, double* out)
+{
+  for (int i = 0; i < n; i++)
+    out[i] = (ell[i] <= limits.LMIN_tab) ? C_kk_limber_nointerp(ell[i], 0) : C_kk_limber(ell[i]);
+  return 0;
+}
+int ref_kk_bandpower(int nbp, int lminbp, int lmaxbp, const double* binmat, const double* offset, double* out)
+{
+  const int nL = lmaxbp - lminbp + 1;
+  for (int j = 0; j < nbp; j++) out[j] = 0.0;
+  for (int L = lminbp; L < lmaxbp + 1; L++) {
+    const double c = (L <= limits.LMIN_tab) ? C_kk_limber_nointerp((double) L, 0) : C_kk_limber((double) L);
+    for (int j = 0; j < nbp; j++) out[j] += c * binmat[(size_t) j * nL + (L - lminbp)];
+  }
+  for (int j = 0; j < nbp; j++) out[j] -= offset[j];
+  return 0;
+}
 double ref_C_ss_limber(double l, int ni, int nj, int EE)
 {
   return C_ss_tomo_limber(l, ni, nj, EE);

@@ -59,6 +59,9 @@ def run_case(case, which="ref"):
             o.set_point(tabs[i], nus[i])
             out[f"wgk_{i}"] = o.w_cmb("gk")
             out[f"wks_{i}"] = o.w_cmb("ks")
+            kl = np.concatenate([w.ell, [float(w.cfg.lmin_tab), w.cfg.lmin_tab + 0.5, 7000.0]])
+            out[f"Ckk_dv_{i}"] = o.C_kk_dv(kl)
+            out[f"kk_bp_{i}"] = o.kk_bandpower(*workloads.cmb_kk_bandpowers())
             out[f"Cgk_{i}"] = np.array([[o.C_cmb("gk", l, n) for l in w.ell] for n in range(w.cfg.n_lens)])
             out[f"Cks_{i}"] = np.array([[o.C_cmb("ks", l, n) for l in w.ell] for n in range(w.cfg.n_source)])
             out[f"Ckk_{i}"] = np.array([o.C_cmb("kk", l) for l in w.ell])

@@ -127,3 +127,24 @@ def test_cmb_real_vs_reference_golden(gpu_lib, case):
     plan.set_cmb(f["lmin"], f["lmax"], 10.0)
     wgk2, _ = plan.cmb_real(*args, lnPL=workloads.stack_lin(tabs))
     assert not np.allclose(wgk2, wgk)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["cmb_lensing_small", "cmb_lensing_tatt_small"])
+def test_cmb_kk_dv_and_bandpowers(gpu_lib, case):
+    """C_kk by the 6x2pt data vector's rule (nointerp at l <= lmin_tab, the
+    ln l table above, its end value beyond l_max) and the kk bandpowers,
+    against the reference's own outputs."""
+    w = workloads.make(case)
+    tabs, nus = workloads.points(w, 2, seed=11)
+    plan = _plan(w, lib.PREC_MIXED, 2, linear_table=True)
+    args = (*workloads.stack(tabs), nus)
+    lnPL = workloads.stack_lin(tabs)
+    kl = np.concatenate([w.ell, [float(w.cfg.lmin_tab), w.cfg.lmin_tab + 0.5, 7000.0]])
+    kk = plan.cmb_kk(*args, kl, lnPL=lnPL)
+    bp = plan.cmb_kk_bandpower(*args, *workloads.cmb_kk_bandpowers(), lnPL=lnPL)
+    g = dict(np.load(os.path.join(GOLD, case + ".npz")))
+    for i in range(2):
+        _close(kk[i][None], g[f"Ckk_dv_{i}"][None], "kk_dv")
+        _close(bp[i][None], g[f"kk_bp_{i}"][None], "kk_bp")
+    assert kk[0, -1] == kk[0, -1] and np.all(bp != 0)
