@@ -214,6 +214,19 @@ def scale_cuts(w: Workload, n: int, seed: int = 0):
     return np.asarray(ptr, dtype=np.int32), np.asarray(idx, dtype=np.int32)
 
 
+def scale_cut_requests():
+    """Requests of the scale-cut diagnostics tests: a (k, l) grid for
+    dC_ss/dlnk, (kmax, l) pairs for RF_C_ss, a 60-node
+    ln k grid on [1e-5, 1e2] h/Mpc for the real-space dlnxi/dlnk (the
+    reference's Ntable.dCX_dlnk_* with 60 instead of 190 nodes), and kmax
+    values for RF_xi."""
+    return dict(k=np.exp(np.linspace(np.log(1e-3), np.log(30.0), 23)),
+                l=np.array([2.0, 10.0, 37.5, 150.0, 800.0, 4000.0]),
+                pairs=[(0, 0), (0, 3), (2, 3), (3, 3)],
+                rf_kmax=np.array([0.05, 0.3, 1.0, 5.0]), rf_l=np.array([3.0, 8.0, 15.0, 20.0]),
+                nlnk=60, kmin=1e-5, kmax=1e2, xi_kmax=np.array([0.05, 0.3, 1.0, 5.0]))
+
+
 def cmb_map_filter():
     """The CMB map filter of the real-space CMB-lensing cross-correlations
     (init_cmb_cross_correlation's arguments): l in [2, 3000], a 5 arcmin

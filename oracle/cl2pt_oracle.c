@@ -868,12 +868,14 @@ static double dlnC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)
  * (denominator) */
 double orc_RF_C_ss_nointerp(double kmax, double l, int ni, int nj, int EE)
 {
-  const glrule* r = rule(256);
+  const int hdi = abs(g.cfg.high_def_integration);
+  const int n = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
+  const glrule* r = rule(n);
   const double lnkmax = log(kmax);
   double num = 0.0, den = 0.0;
-  for (int m = 0; m < 256; m++) {
+  for (int m = 0; m < n; m++) {
     double t, w;
-    num_gl_point(1e-5, 1.0, m, 256, r->x, r->w, &t, &w);
+    num_gl_point(1e-5, 1.0, m, n, r->x, r->w, &t, &w);
     const double s = (1. - t) / t;
     num += w * fabs(dlnC_ss_dlnk_nointerp(exp(lnkmax - s), l, ni, nj, EE)) / (t * t);
     den += w * (fabs(dlnC_ss_dlnk_nointerp(exp(s), l, ni, nj, EE)) +
@@ -1444,6 +1446,153 @@ int orc_kk_bandpower(int nbp, int lminbp, int lmaxbp, const double* binmat, cons
   for (int j = 0; j < nbp; j++) out[j] -= offset[j];
   free(tab);
   return CL2PT_OK;
+}
+
+/* ---- real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740),
+ * the limber = 1 path without TATT (no B modes) */
+static struct {
+  int nlnk;
+  double lim[3];
+  double* tab; /* [2][pss][ntheta][nlnk]: dlnxi+/dlnk, dlnxi-/dlnk */
+} xis;
+static double interpol2d_r(const double* f, int nx, double ax, double bx, double dx, double x, int ny, double ay,
+                           double by, double dy, double y)
+{ /* interpol2d (basics.c:518-562) on a row-major [nx][ny] table */
+  if (x < ax || x > bx) return 0.;
+  const double t = (x - ax) / dx;
+  const int i = (int)floor(t);
+  const double dt = t - i;
+  if (y < ay) return ((1. - dt) * f[i * ny] + dt * f[(i + 1) * ny]) + (y - ay);
+  if (y > by) return ((1. - dt) * f[i * ny + ny - 1] + dt * f[(i + 1) * ny + ny - 1]) + (y - by);
+  const double sv = (y - ay) / dy;
+  const int j = (int)floor(sv);
+  const double ds = sv - j;
+  if (i + 1 == nx && j + 1 == ny) return (1. - dt) * (1. - ds) * f[i * ny + j];
+  if (i + 1 == nx) return (1. - dt) * (1. - ds) * f[i * ny + j] + (1. - dt) * ds * f[i * ny + j + 1];
+  if (j + 1 == ny) return (1. - dt) * (1. - ds) * f[i * ny + j] + dt * (1. - ds) * f[(i + 1) * ny + j];
+  return (1. - dt) * (1. - ds) * f[i * ny + j] + (1. - dt) * ds * f[i * ny + j + 1] +
+         dt * (1. - ds) * f[(i + 1) * ny + j] + dt * ds * f[(i + 1) * ny + j + 1];
+}
+/* The table of dlnxi_dlnk_pm_tomo (:570-647) on the nlnk ln k nodes of
+ * [kmin, kmax] (Ntable.dCX_dlnk_*): each node from
+ * dlnxi_dlnk_pm_tomo_nointerp (:380-568), whose dC/dlnk per l takes the
+ * nointerp integrand below LMIN_tab and dC_ss_dlnk_tomo_limber's bilinear
+ * (ln k, ln l) table above (:80-155), summed with the G+- filters and
+ * divided by xi+- (xi_pm_tomo, limber = 1). out [2][pss][ntheta][nlnk]. */
+int orc_dlnxi_table(int nlnk, double kmin, double kmax, double* out)
+{
+  if (!g.have_point) return CL2PT_ERR_STATE;
+  if (!g.have_filters) build_filters();
+  if (!g.have_tables) build_tables();
+  if (!g.have_g) build_g_tables();
+  const int L = g.cfg.lmax, nt = g.cfg.ntheta, nell = g.cfg.n_ell, np = g.pss, lmin = 1;
+  double ll[3], lk[3];
+  ll[0] = log(fmax(g.cfg.lmin_tab, 1.0));
+  ll[1] = log(L + 1.);
+  ll[2] = (ll[1] - ll[0]) / ((double)nell - 1.);
+  lk[0] = log(kmin);
+  lk[1] = log(kmax);
+  lk[2] = (lk[1] - lk[0]) / ((double)nlnk - 1.);
+  /* dC_ss_dlnk_tomo_limber's table [2][pss][nlnk][nell] */
+  double* T = malloc(sizeof(double) * 2 * np * nlnk * nell);
+  #pragma omp parallel for collapse(3) schedule(static, 1)
+  for (int f = 0; f < nlnk; f++)
+    for (int q = 0; q < np; q++)
+      for (int i = 0; i < nell; i++) {
+        const double kx = exp(lk[0] + f * lk[2]), lx = exp(ll[0] + i * ll[2]);
+        T[((size_t)(0 * np + q) * nlnk + f) * nell + i] = orc_dC_ss_dlnk_nointerp(kx, lx, g.z1[q], g.z2[q], 1);
+        T[((size_t)(1 * np + q) * nlnk + f) * nell + i] = orc_dC_ss_dlnk_nointerp(kx, lx, g.z1[q], g.z2[q], 0);
+      }
+  /* dCldlnk [2][pss][L][nlnk] */
+  double* D = calloc((size_t)2 * np * L * nlnk, sizeof(double));
+  #pragma omp parallel for collapse(3) schedule(static, 1)
+  for (int p = 0; p < 2; p++)
+    for (int q = 0; q < nlnk; q++)
+      for (int z = 0; z < np; z++)
+        for (int l = lmin; l < L; l++) {
+          const double kin = exp(lk[0] + q * lk[2]);
+          double v;
+          if (l < g.cfg.lmin_tab) {
+            v = orc_dC_ss_dlnk_nointerp(kin, (double)l, g.z1[z], g.z2[z], 1 - p);
+          } else {
+            const double lnl = log((double)l), lnk = log(kin);
+            v = (lnk < lk[0] || lnk > lk[1]) ? 0.0
+                : (lnl < ll[0] || lnl > ll[1])
+                    ? 0.0
+                    : interpol2d_r(T + (size_t)(p * np + z) * nlnk * nell, nlnk, lk[0], lk[1], lk[2], lnk, nell,
+                                   ll[0], ll[1], ll[2], lnl);
+          }
+          D[((size_t)(p * np + z) * L + l) * nlnk + q] = v;
+        }
+  double* xp = malloc(sizeof(double) * np * nt);
+  double* xm = malloc(sizeof(double) * np * nt);
+  orc_xi_pm(xp, xm);
+  #pragma omp parallel for collapse(2) schedule(static, 1)
+  for (int f = 0; f < nlnk; f++)
+    for (int z = 0; z < np; z++) {
+      const double lnk = log(exp(lk[0] + f * lk[2]));
+      for (int i = 0; i < nt; i++) {
+        double a0 = 0.0, a1 = 0.0;
+        if (lnk > lk[0] && lnk < lk[1]) {
+          const double* Gp = g.filt + (0 * nt + i) * L;
+          const double* Gm = g.filt + (1 * nt + i) * L;
+          double s0 = 0.0, s1 = 0.0;
+          for (int l = lmin; l < L; l++) {
+            const double c0 = interpol1d(D + ((size_t)(0 * np + z) * L + l) * nlnk, nlnk, lk[0], lk[1], lk[2], lnk);
+            const double c1 = interpol1d(D + ((size_t)(1 * np + z) * L + l) * nlnk, nlnk, lk[0], lk[1], lk[2], lnk);
+            s0 += Gp[l] * (c0 + c1);
+            s1 += Gm[l] * (c0 - c1);
+          }
+          a0 = s0;
+          a1 = s1;
+          /* the reference divides by xi_pm_tomo(p, ...) with p = 0 for the
+           * xi+ slot and 1 for xi-; xi_pm_tomo returns xi+ for pm > 0 only
+           * (cosmo2D.c:555), so dxi+/dlnk is divided by xi- and dxi-/dlnk
+           * by xi+ (cosmo2D_scuts.c:553-557); kept as the reference has it */
+          if (fabs(a0) > 1.e-50) a0 = (fabs(xm[z * nt + i]) > 1.e-50) ? a0 / xm[z * nt + i] : 0.0;
+          if (fabs(a1) > 1.e-50) a1 = (fabs(xp[z * nt + i]) > 1.e-50) ? a1 / xp[z * nt + i] : 0.0;
+        }
+        out[((size_t)(0 * np + z) * nt + i) * nlnk + f] = a0;
+        out[((size_t)(1 * np + z) * nt + i) * nlnk + f] = a1;
+      }
+    }
+  free(T);
+  free(D);
+  free(xp);
+  free(xm);
+  free(xis.tab);
+  xis.tab = malloc(sizeof(double) * 2 * np * nt * nlnk);
+  memcpy(xis.tab, out, sizeof(double) * 2 * np * nt * nlnk);
+  xis.nlnk = nlnk;
+  memcpy(xis.lim, lk, sizeof lk);
+  return CL2PT_OK;
+}
+/* RF_xi_tomo_limber_nointerp (:697-740) with int_RF_xi / int_norm_RF_xi
+ * (:649-695) on the last orc_dlnxi_table: p 0 xi+, 1 xi-; shear pair q */
+static double dlnxi_at(int p, int q, int i, double k)
+{
+  const double lnk = log(k);
+  const int nt = g.cfg.ntheta;
+  return (lnk < xis.lim[0] || lnk > xis.lim[1])
+             ? 0.0
+             : interpol1d(xis.tab + ((size_t)(p * g.pss + q) * nt + i) * xis.nlnk, xis.nlnk, xis.lim[0], xis.lim[1],
+                          xis.lim[2], lnk);
+}
+double orc_RF_xi(double kmax, int p, int i, int q)
+{
+  if (!xis.tab) return 0.0;
+  const int hdi = abs(g.cfg.high_def_integration);
+  const int n = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
+  const glrule* r = rule(n);
+  const double lnkmax = log(kmax);
+  double num = 0.0, den = 0.0;
+  for (int m = 0; m < n; m++) {
+    double t, w;
+    num_gl_point(1e-5, 1.0, m, n, r->x, r->w, &t, &w);
+    num += w * fabs(dlnxi_at(p, q, i, exp(lnkmax - (1. - t) / t))) / (t * t);
+    den += w * (fabs(dlnxi_at(p, q, i, exp((1. - t) / t))) + fabs(dlnxi_at(p, q, i, exp(-(1. - t) / t)))) / (t * t);
+  }
+  return num / den;
 }
 
 /* ------------------------------------------------------------------------ */

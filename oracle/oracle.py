@@ -217,14 +217,14 @@ class Oracle:
 
     def dC_ss_dlnk(self, k, l, ni, nj, EE=1):
         """dC_ss_dlnk_tomo_limber_nointerp (the point must be set)."""
-        f = self.lib.orc_dC_ss_dlnk_nointerp
+        f = getattr(self.lib, self.which + "_dC_ss_dlnk_nointerp")
         f.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
         f.restype = C.c_double
         return f(float(k), float(l), int(ni), int(nj), int(EE))
 
     def RF_C_ss(self, kmax, l, ni, nj, EE=1):
         """RF_C_ss_tomo_limber_nointerp with the nointerp dlnC/dlnk at every l."""
-        f = self.lib.orc_RF_C_ss_nointerp
+        f = getattr(self.lib, self.which + "_RF_C_ss_nointerp")
         f.argtypes = [C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
         f.restype = C.c_double
         return f(float(kmax), float(l), int(ni), int(nj), int(EE))
@@ -263,6 +263,25 @@ class Oracle:
         if st != 0:
             raise RuntimeError(f"w_{which} failed: {st}")
         return out
+
+    def dlnxi_table(self, nlnk, kmin, kmax):
+        """dlnxi+-/dlnk [2][pss][ntheta][nlnk] on the nlnk ln k nodes of
+        [kmin, kmax] (dlnxi_dlnk_pm_tomo); also the table RF_xi reads."""
+        npair = self.npairs[0]
+        out = np.zeros((2, npair, self.cfg.ntheta, nlnk))
+        f = getattr(self.lib, self.which + "_dlnxi_table")
+        f.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+        if f(int(nlnk), float(kmin), float(kmax), _p(out)) != 0:
+            raise RuntimeError("dlnxi_table failed")
+        return out
+
+    def RF_xi(self, kmax, p, i, q):
+        """RF_xi_tomo_limber_nointerp for xi+ (p 0) or xi- (p 1), theta bin
+        i, shear pair q, on the last dlnxi_table grid."""
+        f = getattr(self.lib, self.which + "_RF_xi")
+        f.argtypes = [C.c_double, C.c_int, C.c_int, C.c_int]
+        f.restype = C.c_double
+        return f(float(kmax), int(p), int(i), int(q))
 
     def C_kk_dv(self, ell):
         """C_kk at ell by the 6x2pt data vector's rule (nointerp at

@@ -29,6 +29,7 @@
 #include "basics.h"
 #include "bias.h"
 #include "cosmo2D.h"
+#include "cosmo2D_scuts.h"
 #include "cosmo3D.h"
 #include "IA.h"
 #include "pt_cfastpt.h"
@@ -298,6 +299,46 @@ int ref_kk_bandpower(int nbp, int lminbp, int lmaxbp, const double* binmat, cons
   }
   for (int j = 0; j < nbp; j++) out[j] -= offset[j];
   return 0;
+}
+/* the real-space scale-cut diagnostics on the ln k grid Ntable.dCX_dlnk_*:
+ * dlnxi_dlnk_pm_tomo at the grid's nodes, out [2][pss][ntheta][nlnk]
+ * (p 0 xi+, 1 xi-), and RF_xi_tomo_limber_nointerp (cosmo2D_scuts.c:
+ * 380-740) */
+int ref_dlnxi_table(int nlnk, double kmin, double kmax, double* out)
+{
+  Ntable.dCX_dlnk_nlnk = nlnk;
+  Ntable.dCX_dlnk_kmin = kmin;
+  Ntable.dCX_dlnk_kmax = kmax;
+  Ntable.random = (double) next_token();
+  /* the lazily built tables (g_tomo, the C_ss tables) first, serially:
+   * dC_ss_dlnk_tomo_limber's own warm-up call sits at k = kmin, where the
+   * integrand returns before reading them, and its OpenMP loop would build
+   * them concurrently */
+  (void) xi_pm_tomo(1, 0, Z1(0), Z2(0), 1);
+  (void) dC_ss_dlnk_tomo_limber_nointerp(0.1, 100.0, Z1(0), Z2(0), 1);
+  const double l0 = log(kmin), l2 = (log(kmax) - l0) / ((double) nlnk - 1.);
+  const int np = tomo.shear_Npowerspectra, nt = Ntable.Ntheta;
+  for (int p = 0; p < 2; p++)
+    for (int q = 0; q < np; q++)
+      for (int i = 0; i < nt; i++)
+        for (int f = 0; f < nlnk; f++)
+          out[((size_t)(p * np + q) * nt + i) * nlnk + f] =
+              dlnxi_dlnk_pm_tomo(exp(l0 + f * l2), p == 0 ? 1 : -1, i, Z1(q), Z2(q));
+  return 0;
+}
+/* the Fourier scale-cut diagnostics (cosmo2D_scuts.c:42-74, 329-375); the
+ * reference's RF reads its interpolated dlnC table above LMIN_tab */
+double ref_dC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)
+{
+  return dC_ss_dlnk_tomo_limber_nointerp(k, l, ni, nj, EE);
+}
+double ref_RF_C_ss_nointerp(double kmax, double l, int ni, int nj, int EE)
+{
+  return RF_C_ss_tomo_limber_nointerp(kmax, l, ni, nj, EE, 0);
+}
+double ref_RF_xi(double kmax, int p, int i, int q)
+{
+  return RF_xi_tomo_limber_nointerp(kmax, p == 0 ? 1 : -1, i, Z1(q), Z2(q), 0);
 }
 double ref_C_ss_limber(double l, int ni, int nj, int EE)
 {
