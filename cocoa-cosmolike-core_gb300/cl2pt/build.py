@@ -21,7 +21,10 @@ LEGACY = os.path.join(HERE, "libcl2pt_legacy.so")
 LEGACY_SRC = os.path.join(CSRC, "legacy", "legacy.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INC}", f"-I{CSRC}"]
+# host code without floating-point contraction, so that plan-time tables
+# (filters, node flags) round the same on x86-64 and aarch64
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", f"-I{INC}",
+         f"-I{CSRC}"]
 
 
 def nvcc() -> str:
@@ -51,7 +54,7 @@ def headers():
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
-    hs = headers()
+    hs = headers() + [os.path.abspath(__file__)]  # a change of flags rebuilds
     jobs = []
     objs = []
     for src in sources():

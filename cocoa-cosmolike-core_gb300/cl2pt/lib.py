@@ -100,6 +100,10 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_scut_ss_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_int, _dp, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
     lib.cl2pt_scut_ss_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
+    lib.cl2pt_scut_xi_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_double, C.c_double, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+    lib.cl2pt_scut_xi_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_double, C.c_double, C.c_int, _dp,
+                                     C.c_void_p, C.c_void_p]
     lib.cl2pt_cmb_cl.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]
     lib.cl2pt_plan_set_cmb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp]
@@ -262,6 +266,25 @@ class Plan:
         rf = np.zeros((b.n, 2, self.pss, len(kmax)))
         check(load().cl2pt_scut_ss_rf(self.h, C.byref(b), len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
               "cl2pt_scut_ss_rf")
+        return rf
+
+    def scut_xi_dlnk(self, omega_m, h0, chi, G, lnP, nuisance, nlnk=190, kmin=1e-5, kmax=1e2, lnPL=None):
+        """Real-space scale-cut diagnostics (cl2pt_scut_xi_dlnk): dxi/dlnk
+        and the dlnxi/dlnk table [n][2][pss][ntheta][nlnk]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        dxi = np.zeros((b.n, 2, self.pss, self.cfg.ntheta, nlnk))
+        dln = np.zeros_like(dxi)
+        check(load().cl2pt_scut_xi_dlnk(self.h, C.byref(b), nlnk, kmin, kmax, dxi.ctypes.data, dln.ctypes.data,
+                                        None), "cl2pt_scut_xi_dlnk")
+        return dxi, dln
+
+    def scut_xi_rf(self, omega_m, h0, chi, G, lnP, nuisance, kmax_req, nlnk=190, kmin=1e-5, kmax=1e2, lnPL=None):
+        """RF_xi at kmax_req (cl2pt_scut_xi_rf): [n][2][pss][ntheta][nreq]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        kr = np.ascontiguousarray(kmax_req, dtype=np.float64)
+        rf = np.zeros((b.n, 2, self.pss, self.cfg.ntheta, len(kr)))
+        check(load().cl2pt_scut_xi_rf(self.h, C.byref(b), nlnk, kmin, kmax, len(kr), _p(kr), rf.ctypes.data, None),
+              "cl2pt_scut_xi_rf")
         return rf
 
     def cmb_cl(self, omega_m, h0, chi, G, lnP, nuisance, ell, lnPL=None):

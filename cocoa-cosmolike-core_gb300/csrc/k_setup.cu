@@ -674,6 +674,131 @@ __global__ void k_scut_rf(Params P, int nreq, const double* __restrict__ kmax, c
   if (lane == 0) rf[warp] = num / den;
 }
 
+// ---- real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740),
+// limber = 1, FP64.
+// xi+- (xi_pm_tomo) from k_scut_css's C_ss on the ss C_l nodes (css [B][pss]
+// [2][nn]) and the plan's folded G+- filters F [2 nt][nn]: xi [B][2][pss][nt].
+// One warp per (point, +-, pair, theta bin).
+__global__ void k_scut_xi(int B, int pss, int nt, int nn, const double* __restrict__ css,
+                          const double* __restrict__ F, double* __restrict__ xi)
+{
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= B * 2 * pss * nt) return;
+  const int i = warp % nt, r = warp / nt;
+  const int pr = r % pss, r2 = r / pss;
+  const int pm = r2 % 2, pt = r2 / 2;
+  const double* cE = css + (((size_t)pt * pss + pr) * 2) * nn;
+  const double* cB = cE + nn;
+  const double* f = F + ((size_t)pm * nt + i) * nn;
+  const double sg = pm == 0 ? 1.0 : -1.0;
+  double acc = 0.0;
+  for (int j = lane; j < nn; j += 32) acc += f[j] * (cE[j] + sg * cB[j]);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) xi[warp] = acc;
+}
+
+// dxi+-/dlnk at the nlnk ln k nodes (dlnxi_dlnk_pm_tomo_nointerp,
+// :380-568): dC [B][2][pss][nlnk][nn] from k_scut_dlnk on the lens C_l
+// nodes (integer l below lmin_tab, then the n_ell ln l nodes), summed with
+// the G+- filters folded on those nodes (Fg [2][nt][nn]); node flags per k:
+// kin[f] (the sums run; else 0) and ktab[f] (dC_ss_dlnk_tomo_limber's table
+// answers; else the ln l nodes, j >= nint, count 0).  dlnxi = dxi / xi with
+// the reference's pairing (xi+ slot over xi-, xi- slot over xi+).
+// dxi, dlnxi [B][2][pss][nt][nlnk] (either may be null).  One warp per
+// (point, +-, pair, theta bin, k node).
+__global__ void k_scut_xi_dlnk(int B, int pss, int nt, int nlnk, int nn, int nint, const double* __restrict__ dC,
+                               const double* __restrict__ Fg, const unsigned char* __restrict__ kin,
+                               const unsigned char* __restrict__ ktab, const double* __restrict__ xi,
+                               double* __restrict__ dxi, double* __restrict__ dlnxi)
+{
+  const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= (long)B * 2 * pss * nt * nlnk) return;
+  const int f = (int)(warp % nlnk);
+  long r = warp / nlnk;
+  const int i = (int)(r % nt);
+  r /= nt;
+  const int pr = (int)(r % pss);
+  r /= pss;
+  const int pm = (int)(r % 2), pt = (int)(r / 2);
+  double acc = 0.0;
+  if (kin[f]) {
+    const double* cE = dC + ((((size_t)pt * 2 + 0) * pss + pr) * nlnk + f) * nn;
+    const double* cB = dC + ((((size_t)pt * 2 + 1) * pss + pr) * nlnk + f) * nn;
+    const double* g = Fg + ((size_t)pm * nt + i) * nn;
+    const double sg = pm == 0 ? 1.0 : -1.0;
+    const int jend = ktab[f] ? nn : nint;
+    for (int j = lane; j < jend; j += 32) acc += g[j] * (cE[j] + sg * cB[j]);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    if (dxi) dxi[warp] = acc;
+    if (dlnxi) {
+      double v = acc;
+      if (kin[f] && fabs(acc) > 1.e-50) {
+        const double x = xi[(((size_t)pt * 2 + (1 - pm)) * pss + pr) * nt + i];
+        v = (fabs(x) > 1.e-50) ? acc / x : 0.0;
+      }
+      dlnxi[warp] = v;
+    }
+  }
+}
+
+// RF_xi_tomo_limber_nointerp (:649-740) at the requests kmax[0..nreq) for
+// every (+-, pair, theta bin) from the dlnxi table (dlnxi_dlnk_pm_tomo:
+// linear in ln k on the nodes, 0 outside [lk0, lk1]); GL rule (tx, tw) on
+// [1e-5, 1]; rf [B][2][pss][nt][nreq].  One warp per output.
+__global__ void k_scut_xi_rf(int B, int pss, int nt, int nlnk, double lk0, double lk1, double lk2,
+                             const double* __restrict__ dlnxi, int nreq, const double* __restrict__ kmax, int ntq,
+                             const double* __restrict__ tx, const double* __restrict__ tw, double* __restrict__ rf)
+{
+  const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= (long)B * 2 * pss * nt * nreq) return;
+  const int q = (int)(warp % nreq);
+  const double* tab = dlnxi + (size_t)(warp / nreq) * nlnk;
+  auto at = [&](double k) {
+    const double lnk = log(k);
+    if (lnk < lk0 || lnk > lk1) return 0.0;
+    const double r = (lnk - lk0) / lk2;
+    const int i = (int)floor(r);
+    return (i + 1 >= nlnk) ? tab[nlnk - 1] : (r - i) * (tab[i + 1] - tab[i]) + tab[i];
+  };
+  const double lnkmax = log(kmax[q]);
+  double num = 0.0, den = 0.0;
+  for (int m = lane; m < ntq; m += 32) {
+    const double t = tx[m], s = (1. - t) / t, w = tw[m] / (t * t);
+    num += w * fabs(at(exp(lnkmax - s)));
+    den += w * (fabs(at(exp(s))) + fabs(at(exp(-s))));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    num += __shfl_down_sync(0xffffffffu, num, o);
+    den += __shfl_down_sync(0xffffffffu, den, o);
+  }
+  if (lane == 0) rf[warp] = num / den;
+}
+
+void launch_scut_xi(const Params& P, int nn, const double* css, const double* F, int nt, double* xi, cudaStream_t s)
+{
+  const long warps = (long)P.B * 2 * P.pss * nt;
+  k_scut_xi<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(P.B, P.pss, nt, nn, css, F, xi);
+}
+void launch_scut_xi_dlnk(const Params& P, int nt, int nlnk, int nn, int nint, const double* dC, const double* Fg,
+                         const unsigned char* kin, const unsigned char* ktab, const double* xi, double* dxi,
+                         double* dlnxi, cudaStream_t s)
+{
+  const long warps = (long)P.B * 2 * P.pss * nt * nlnk;
+  k_scut_xi_dlnk<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(P.B, P.pss, nt, nlnk, nn, nint, dC, Fg, kin,
+                                                                       ktab, xi, dxi, dlnxi);
+}
+void launch_scut_xi_rf(const Params& P, int nt, int nlnk, const double* lk, const double* dlnxi, int nreq,
+                       const double* kmax, int ntq, const double* tx, const double* tw, double* rf, cudaStream_t s)
+{
+  const long warps = (long)P.B * 2 * P.pss * nt * nreq;
+  k_scut_xi_rf<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(P.B, P.pss, nt, nlnk, lk[0], lk[1], lk[2], dlnxi,
+                                                                     nreq, kmax, ntq, tx, tw, rf);
+}
+
 void launch_scut_css(const Params& P, int nl, const double* l, double* out, cudaStream_t s)
 {
   k_scut_css<<<dim3(P.B, P.pss), 128, 0, s>>>(P, nl, l, out);

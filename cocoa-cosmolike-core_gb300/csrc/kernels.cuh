@@ -35,6 +35,14 @@ void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const do
                       double* dC, double* dlnC, cudaStream_t s);
 void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
                     const double* tw, const double* css, double* rf, cudaStream_t s);
+// real-space scale-cut diagnostics: xi+- from C_ss on the ss nodes,
+// dxi+-/dlnk and dlnxi+-/dlnk on a ln k grid, RF_xi
+void launch_scut_xi(const Params& P, int nn, const double* css, const double* F, int nt, double* xi, cudaStream_t s);
+void launch_scut_xi_dlnk(const Params& P, int nt, int nlnk, int nn, int nint, const double* dC, const double* Fg,
+                         const unsigned char* kin, const unsigned char* ktab, const double* xi, double* dxi,
+                         double* dlnxi, cudaStream_t s);
+void launch_scut_xi_rf(const Params& P, int nt, int nlnk, const double* lk, const double* dlnxi, int nreq,
+                       const double* kmax, int ntq, const double* tx, const double* tw, double* rf, cudaStream_t s);
 // C_gk, C_ks, C_kk of the 6x2pt probes at ell[0..nell) (device): spectrum
 // rows [row0, row0 + nrows) of [0, nl) gk, [nl, nl + ns) ks, nl + ns kk;
 // out [B][nrows][nell]

@@ -1392,6 +1392,160 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
   return st;
 }
 
+// Real-space scale-cut diagnostics of xi+- (cosmolike/cosmo2D_scuts.c:
+// 380-740) on the ln k grid of nlnk nodes over [kmin, kmax] (the
+// reference's Ntable.dCX_dlnk_*): per sub-wave the set-up stage, C_ss on
+// the ss C_l nodes and xi+-, dC/dlnk on (k nodes) x (lens C_l nodes), the
+// folded G+- sums (dxi, dlnxi [n][2][pss][ntheta][nlnk]) and, when nreq > 0,
+// RF_xi at the requests (rf [n][2][pss][ntheta][nreq]).  The sub-wave is
+// sized so that the dC grid stays within about 2 GB.
+static int xi_scut_run(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmin, double kmax, double* dxi,
+                       double* dlnxi, int nreq, const double* kreq, double* rf, cudaStream_t s)
+{
+  if (!p || !b) return CL2PT_ERR_ARG;
+  if (p->P.tatt) return CL2PT_ERR_UNSUPPORTED;  // B modes and TATT terms of the diagnostics are not built
+  if (nlnk < 2 || !(kmin > 0) || !(kmax > kmin) || !std::isfinite(kmax)) return CL2PT_ERR_ARG;
+  for (int i = 0; i < nreq; i++)
+    if (!(kreq[i] > 0) || !std::isfinite(kreq[i])) return CL2PT_ERR_ARG;
+  if (int st = check_batch(p, b, true)) return st;
+  const int n = b->n;
+  const Params& T = p->P;
+  DevBatch d;
+  if (int st = stage_batch_inputs(p, b, s, &d)) return st;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  const cl2pt_config& c = p->cfg;
+  const int nt = c.ntheta, L = c.lmax, nng = p->nnode_g, nns = p->nnode_ss, pss = std::max(T.pss, 1);
+  // the k nodes, as the reference forms them, and their flags
+  double lk[3];
+  lk[0] = log(kmin);
+  lk[1] = log(kmax);
+  lk[2] = (lk[1] - lk[0]) / ((double)nlnk - 1.);
+  std::vector<double> kx(nlnk);
+  std::vector<unsigned char> kin(nlnk), ktab(nlnk);
+  for (int f = 0; f < nlnk; f++) {
+    kx[f] = exp(lk[0] + f * lk[2]);
+    const double lnk = log(kx[f]);
+    kin[f] = (lnk > lk[0] && lnk < lk[1]) ? 1 : 0;     // dlnxi_dlnk_pm_tomo_nointerp's sum runs
+    ktab[f] = (lnk < lk[0] || lnk > lk[1]) ? 0 : 1;    // dC_ss_dlnk_tomo_limber's table answers
+  }
+  // G+- folded on the lens C_l nodes (the (k, ln l) table shares their ln l grid)
+  std::vector<double> Fg((size_t)2 * nt * nng, 0.0);
+  {
+    std::vector<double> Gp(L), Gm(L), Pgt(L), Pgg(L);
+    for (int i = 0; i < nt; i++) {
+      double xmin, xmax;
+      theta_bin_x(c, i, &xmin, &xmax);
+      legendre_filters(L, xmin, xmax, Gp.data(), Gm.data(), Pgt.data(), Pgg.data());
+      fold(Gp.data(), L, p->nint, c.lmin_tab, p->lim_g, c.n_ell, Fg.data() + (size_t)i * nng);
+      fold(Gm.data(), L, p->nint, c.lmin_tab, p->lim_g, c.n_ell, Fg.data() + (size_t)(nt + i) * nng);
+    }
+  }
+  std::vector<double> tx, tw;
+  if (nreq > 0) {
+    const int hdi = std::abs(c.high_def_integration);
+    const int ntq = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
+    std::vector<double> x, w;
+    gl_rule(ntq, x, w);
+    tx.resize(ntq);
+    tw.resize(ntq);
+    for (int m = 0; m < ntq; m++) {
+      tx[m] = 0.5 * (1.0 - 1e-5) * x[m] + 0.5 * (1.0 + 1e-5);
+      tw[m] = 0.5 * (1.0 - 1e-5) * w[m];
+    }
+  }
+  const size_t per_dC = (size_t)2 * pss * nlnk * nng;
+  const int W = std::max(1, std::min(p->wave, (int)std::min<size_t>((size_t)2e9 / (8 * per_dC), 1 << 20)));
+  const size_t per_tab = (size_t)2 * pss * nt * nlnk;
+  double *dk = nullptr, *dFg = nullptr, *dcss = nullptr, *dxiv = nullptr, *ddC = nullptr, *ddxi = nullptr,
+         *ddln = nullptr, *dkr = nullptr, *dtx = nullptr, *drf = nullptr;
+  unsigned char* dflags = nullptr;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&dk, sizeof(double) * nlnk));
+  fail(cudaMalloc((void**)&dflags, 2 * nlnk));
+  fail(cudaMalloc((void**)&dFg, sizeof(double) * Fg.size()));
+  fail(cudaMalloc((void**)&dcss, sizeof(double) * (size_t)W * pss * 2 * nns));
+  fail(cudaMalloc((void**)&dxiv, sizeof(double) * (size_t)W * 2 * pss * nt));
+  fail(cudaMalloc((void**)&ddC, sizeof(double) * (size_t)W * per_dC));
+  fail(cudaMalloc((void**)&ddxi, sizeof(double) * (size_t)W * per_tab));
+  fail(cudaMalloc((void**)&ddln, sizeof(double) * (size_t)W * per_tab));
+  if (nreq > 0) {
+    fail(cudaMalloc((void**)&dkr, sizeof(double) * nreq));
+    fail(cudaMalloc((void**)&dtx, sizeof(double) * 2 * tx.size()));
+    fail(cudaMalloc((void**)&drf, sizeof(double) * (size_t)W * 2 * pss * nt * nreq));
+  }
+  if (!st) {
+    fail(cudaMemcpyAsync(dk, kx.data(), sizeof(double) * nlnk, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dflags, kin.data(), nlnk, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dflags + nlnk, ktab.data(), nlnk, cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(dFg, Fg.data(), sizeof(double) * Fg.size(), cudaMemcpyHostToDevice, s));
+    if (nreq > 0) {
+      fail(cudaMemcpyAsync(dkr, kreq, sizeof(double) * nreq, cudaMemcpyHostToDevice, s));
+      fail(cudaMemcpyAsync(dtx, tx.data(), sizeof(double) * tx.size(), cudaMemcpyHostToDevice, s));
+      fail(cudaMemcpyAsync(dtx + tx.size(), tw.data(), sizeof(double) * tw.size(), cudaMemcpyHostToDevice, s));
+    }
+  }
+  const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  cl2pt::Hook hk;
+  int launches = 0;
+  for (int w0 = 0; w0 < n && !st; w0 += W) {
+    Params P = T;
+    P.B = std::min(W, n - w0);
+    P.omega_m = d.om + w0;
+    P.h0 = d.h0 + w0;
+    P.chi = d.chi + (size_t)w0 * nchi;
+    P.G = d.G + (size_t)w0 * nG;
+    P.lnP = d.lnP + (size_t)w0 * nP;
+    P.lnPL = d.lnPL + (size_t)w0 * (b->lnPL ? nPL : nP);
+    if (p->bary_on) {
+      cl2pt::launch_add_table(P.lnP, p->d_bary_lnr, p->d_lnP_bary, P.B, nP, s);
+      P.lnP = p->d_lnP_bary;
+    }
+    P.nu = d.nu + w0;
+    cl2pt::launch_setup(P, s, &launches, hk);
+    cl2pt::launch_scut_css(P, nns, p->d_ell_ss, dcss, s);
+    cl2pt::launch_scut_xi(P, nns, dcss, p->d_filt_xi, nt, dxiv, s);
+    cl2pt::launch_scut_dlnk(P, nlnk, dk, nng, p->d_ell_g, nullptr, ddC, nullptr, s);
+    cl2pt::launch_scut_xi_dlnk(P, nt, nlnk, nng, p->nint, ddC, dFg, dflags, dflags + nlnk, dxiv, ddxi, ddln, s);
+    if (nreq > 0)
+      cl2pt::launch_scut_xi_rf(P, nt, nlnk, lk, ddln, nreq, dkr, (int)tx.size(), dtx, dtx + tx.size(), drf, s);
+    fail(cudaGetLastError());
+    if (dxi) fail(cudaMemcpyAsync(dxi + (size_t)w0 * per_tab, ddxi, sizeof(double) * per_tab * P.B, kind, s));
+    if (dlnxi) fail(cudaMemcpyAsync(dlnxi + (size_t)w0 * per_tab, ddln, sizeof(double) * per_tab * P.B, kind, s));
+    if (rf) {
+      const size_t pr = (size_t)2 * pss * nt * nreq;
+      fail(cudaMemcpyAsync(rf + (size_t)w0 * pr, drf, sizeof(double) * pr * P.B, kind, s));
+    }
+    fail(cudaStreamSynchronize(s));
+  }
+  for (void* q : {(void*)dk, (void*)dflags, (void*)dFg, (void*)dcss, (void*)dxiv, (void*)ddC, (void*)ddxi,
+                  (void*)ddln, (void*)dkr, (void*)dtx, (void*)drf})
+    cudaFree(q);
+  if (!st) {
+    int e = 0;
+    fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+      st = CL2PT_ERR_DEVICE;
+      cudaMemset(p->d_err, 0, sizeof(int));  // the next call starts clean
+    }
+  }
+  return st;
+}
+
+extern "C" int cl2pt_scut_xi_dlnk(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmin, double kmax,
+                                  double* dxi, double* dlnxi, void* stream)
+{
+  if (!dxi && !dlnxi) return CL2PT_ERR_ARG;
+  return xi_scut_run(p, b, nlnk, kmin, kmax, dxi, dlnxi, 0, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int cl2pt_scut_xi_rf(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmin, double kmax, int nreq,
+                                const double* kmax_req, double* rf, void* stream)
+{
+  if (!rf || nreq < 1 || !kmax_req) return CL2PT_ERR_ARG;
+  return xi_scut_run(p, b, nlnk, kmin, kmax, nullptr, nullptr, nreq, kmax_req, rf, (cudaStream_t)stream);
+}
+
 extern "C" int cl2pt_scut_ss_dlnk(cl2pt_plan* p, const cl2pt_batch* b, int nk, const double* k, int nl,
                                   const double* l, double* dC, double* dlnC, void* stream)
 {

@@ -349,6 +349,22 @@ int cl2pt_scut_ss_dlnk(cl2pt_plan* plan, const cl2pt_batch* batch, int nk, const
                        const double* l, double* dC, double* dlnC, void* stream);
 int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const double* kmax, const double* l,
                      double* rf, void* stream);
+/* Real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740,
+ * limber = 1, NLA / no-IA plans) on the ln k grid of nlnk nodes over
+ * [kmin, kmax] h/Mpc (the reference's Ntable.dCX_dlnk_nlnk / _kmin / _kmax,
+ * by default 190, 1e-5, 1e2), p = 0 for xi+ and 1 for xi-:
+ *   cl2pt_scut_xi_dlnk: dxi[n][2][pss][ntheta][nlnk] = dxi/dlnk at the
+ *     nodes (dlnxi_dlnk_pm_tomo_nointerp before its division) and
+ *     dlnxi[...] the table of dlnxi_dlnk_pm_tomo: dxi divided as the
+ *     reference divides it, the xi+ slot by xi- and the xi- slot by xi+
+ *     (its xi_pm_tomo(p, ...) call with p = 0, 1); either may be NULL;
+ *   cl2pt_scut_xi_rf: rf[n][2][pss][ntheta][nreq] = RF_xi_tomo_limber_
+ *     nointerp at kmax_req[i] from that table.
+ * Outputs follow batch->where. */
+int cl2pt_scut_xi_dlnk(cl2pt_plan* plan, const cl2pt_batch* batch, int nlnk, double kmin, double kmax, double* dxi,
+                       double* dlnxi, void* stream);
+int cl2pt_scut_xi_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nlnk, double kmin, double kmax, int nreq,
+                     const double* kmax_req, double* rf, void* stream);
 
 /* CMB-lensing spectra of the 6x2pt probes at the multipoles ell[0..nell)
  * (host memory), each by the reference's Gauss-Legendre rule in a with the

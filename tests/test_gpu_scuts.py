@@ -75,3 +75,32 @@ def test_scuts_reject_tatt(gpu_lib):
     om, h0, chi, G, lnP = workloads.stack(tabs)
     with pytest.raises(lib.CL2PTError):
         plan.scut_ss_dlnk(om, h0, chi, G, lnP, nus, [0.1], [100.0])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
+def test_scuts_vs_reference_golden(gpu_lib, prec):
+    """dC_ss/dlnk, the real-space dlnxi/dlnk table and RF_xi against the
+    reference's own outputs (tests/golden/scale_cuts_small.npz)."""
+    import os
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scale_cuts_small.npz")))
+    w, tabs, nus, plan, args, lnPL = case(prec)
+    sc = workloads.scale_cut_requests()
+    ns = w.cfg.n_source
+    pairs = [(i, j) for i in range(ns) for j in range(i, ns)]
+    dC, _ = plan.scut_ss_dlnk(*args, nus, sc["k"], sc["l"], lnPL=lnPL)
+    dxi, dln = plan.scut_xi_dlnk(*args, nus, sc["nlnk"], sc["kmin"], sc["kmax"], lnPL=lnPL)
+    rf = plan.scut_xi_rf(*args, nus, sc["xi_kmax"], sc["nlnk"], sc["kmin"], sc["kmax"], lnPL=lnPL)
+    assert np.all(dxi[:, :, :, :, 0] == 0.0)  # k = 1e-5: no source at chi = (l + 1/2) / k
+    worst = {}
+    for pt in range(2):
+        ref = g[f"dC_{pt}"]
+        got = np.array([dC[pt, 0, pairs.index(pq)] for pq in sc["pairs"]])
+        worst["dC"] = max(worst.get("dC", 0.0), float(np.max(np.abs(got - ref)) / np.abs(ref).max()))
+        ref = g[f"dlnxi_{pt}"]
+        scale = np.abs(ref).max(axis=-1, keepdims=True) + 1e-300
+        worst["dlnxi"] = max(worst.get("dlnxi", 0.0), float(np.max(np.abs(dln[pt] - ref) / scale)))
+        ref = g[f"rfxi_{pt}"]
+        worst["rf"] = max(worst.get("rf", 0.0), float(np.max(np.abs(rf[pt] - ref))))
+    print("scale cuts vs reference", worst)
+    assert worst["dC"] <= 1e-9 and worst["dlnxi"] <= 1e-8 and worst["rf"] <= 1e-8
