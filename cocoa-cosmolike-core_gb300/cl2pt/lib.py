@@ -100,6 +100,8 @@ def load(path: str = LIB_PATH):
     lib.cl2pt_scut_ss_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, C.c_int, _dp, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
     lib.cl2pt_scut_ss_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
+    lib.cl2pt_scut_ss_rf_grid.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_double, C.c_double, C.c_int,
+                                          _dp, _dp, C.c_void_p, C.c_void_p]
     lib.cl2pt_scut_xi_dlnk.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_double, C.c_double, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
     lib.cl2pt_scut_xi_rf.argtypes = [C.c_void_p, C.POINTER(Batch), C.c_int, C.c_double, C.c_double, C.c_int, _dp,
@@ -256,16 +258,22 @@ class Plan:
                                         dlnC.ctypes.data, None), "cl2pt_scut_ss_dlnk")
         return dC, dlnC
 
-    def scut_ss_rf(self, omega_m, h0, chi, G, lnP, nuisance, kmax, l, lnPL=None):
-        """RF_C_ss at the requests (kmax[i], l[i]) (cl2pt_scut_ss_rf):
-        [n][2][pss][len(kmax)]."""
+    def scut_ss_rf(self, omega_m, h0, chi, G, lnP, nuisance, kmax, l, lnPL=None, grid=None):
+        """RF_C_ss at the requests (kmax[i], l[i]) (cl2pt_scut_ss_rf, or
+        cl2pt_scut_ss_rf_grid with grid = (nlnk, kmin, kmax) for the dlnC
+        table above lmin_tab): [n][2][pss][len(kmax)]."""
         b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
         kmax = np.ascontiguousarray(kmax, dtype=np.float64)
         l = np.ascontiguousarray(l, dtype=np.float64)
         assert len(kmax) == len(l)
         rf = np.zeros((b.n, 2, self.pss, len(kmax)))
-        check(load().cl2pt_scut_ss_rf(self.h, C.byref(b), len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
-              "cl2pt_scut_ss_rf")
+        if grid is None:
+            check(load().cl2pt_scut_ss_rf(self.h, C.byref(b), len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
+                  "cl2pt_scut_ss_rf")
+        else:
+            check(load().cl2pt_scut_ss_rf_grid(self.h, C.byref(b), int(grid[0]), float(grid[1]), float(grid[2]),
+                                               len(kmax), _p(kmax), _p(l), rf.ctypes.data, None),
+                  "cl2pt_scut_ss_rf_grid")
         return rf
 
     def scut_xi_dlnk(self, omega_m, h0, chi, G, lnP, nuisance, nlnk=190, kmin=1e-5, kmax=1e2, lnPL=None):

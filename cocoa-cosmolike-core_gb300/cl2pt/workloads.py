@@ -223,7 +223,7 @@ def scale_cut_requests():
     return dict(k=np.exp(np.linspace(np.log(1e-3), np.log(30.0), 23)),
                 l=np.array([2.0, 10.0, 37.5, 150.0, 800.0, 4000.0]),
                 pairs=[(0, 0), (0, 3), (2, 3), (3, 3)],
-                rf_kmax=np.array([0.05, 0.3, 1.0, 5.0]), rf_l=np.array([3.0, 8.0, 15.0, 20.0]),
+                rf_kmax=np.array([0.05, 0.3, 1.0, 5.0]), rf_l=np.array([30.0, 200.0, 1000.0, 300.0]),
                 nlnk=60, kmin=1e-5, kmax=1e2, xi_kmax=np.array([0.05, 0.3, 1.0, 5.0]))
 
 

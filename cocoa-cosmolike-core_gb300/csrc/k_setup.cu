@@ -637,15 +637,77 @@ __global__ void k_scut_dlnk(Params P, int nk, const double* __restrict__ k, int 
   }
 }
 
+// interpol2d (basics.c:518-562) on a row-major [nx][ny] table
+__device__ double interpol2d_d(const double* f, int nx, double ax, double bx, double dx, double x, int ny, double ay,
+                               double by, double dy, double y)
+{
+  if (x < ax || x > bx) return 0.;
+  const double t = (x - ax) / dx;
+  const int i = (int)floor(t);
+  const double dt = t - i;
+  if (y < ay) return ((1. - dt) * f[i * ny] + dt * f[(i + 1) * ny]) + (y - ay);
+  if (y > by) return ((1. - dt) * f[i * ny + ny - 1] + dt * f[(i + 1) * ny + ny - 1]) + (y - by);
+  const double sv = (y - ay) / dy;
+  const int j = (int)floor(sv);
+  const double ds = sv - j;
+  if (i + 1 == nx && j + 1 == ny) return (1. - dt) * (1. - ds) * f[i * ny + j];
+  if (i + 1 == nx) return (1. - dt) * (1. - ds) * f[i * ny + j] + (1. - dt) * ds * f[i * ny + j + 1];
+  if (j + 1 == ny) return (1. - dt) * (1. - ds) * f[i * ny + j] + dt * (1. - ds) * f[(i + 1) * ny + j];
+  return (1. - dt) * (1. - ds) * f[i * ny + j] + (1. - dt) * ds * f[i * ny + j + 1] +
+         dt * (1. - ds) * f[(i + 1) * ny + j] + dt * ds * f[(i + 1) * ny + j + 1];
+}
+
+// dlnC_ss_dlnk_tomo_limber's (ln k, ln l) table (cosmo2D_scuts.c:157-255),
+// in place over k_scut_dlnk's grid dC [B][2][pss][nlnk][nell] on the k nodes
+// x the lens C_l table's ln l nodes: dC (0 where the dC table would not
+// answer: kok[f], lok[i]) over C_ss_tomo_limber at that l (linear in ln l on
+// the ss table, css_ss [B][pss][2][nns] from k_scut_css on the ss C_l nodes,
+// its ln l part from column nint; lnl[i] the nodes' ln l).
+__global__ void k_scut_dlnC_tab(int B, int pss, int nlnk, int nell, int nns, int nint, const double* __restrict__ css_ss,
+                                double* __restrict__ dC, const unsigned char* __restrict__ kok,
+                                const unsigned char* __restrict__ lok, const double* __restrict__ lnl, double ls0,
+                                double ls2)
+{
+  const long n = (long)B * 2 * pss * nlnk * nell;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx % nell);
+    long r = idx / nell;
+    const int f = (int)(r % nlnk);
+    r /= nlnk;
+    const int pr = (int)(r % pss);
+    r /= pss;
+    const int e = (int)(r % 2), pt = (int)(r / 2);
+    const double d = (kok[f] && lok[i]) ? dC[idx] : 0.0;
+    double C = 1.0;
+    if (fabs(d) > 1e-30) {
+      const double* t = css_ss + (((size_t)pt * pss + pr) * 2 + e) * nns + nint;
+      const int nt = nns - nint;
+      const double x = lnl[i];
+      if (x < ls0) {
+        C = t[0];
+      } else {
+        const double rr = (x - ls0) / ls2;
+        const int j = (int)floor(rr);
+        C = (j + 1 >= nt) ? t[nt - 1] : (rr - j) * (t[j + 1] - t[j]) + t[j];
+      }
+    }
+    dC[idx] = (fabs(C) > 1e-30) ? d / C : 0.0;
+  }
+}
+
 // RF_C_ss_tomo_limber_nointerp (cosmo2D_scuts.c:329-375) for the requests
 // (kmax[i], l[i]): the fraction of int |dlnC/dlnk| dlnk below ln kmax, as
 // Gauss-Legendre sums over t in [1e-5, 1] (tx, tw: the caller's rule, 256
 // nodes at high_def_integration 0) with ln k = ln kmax - (1 - t)/t and
-// +-(1 - t)/t; rf [B][2][pss][nreq]; css from k_scut_css at the requests'
-// multipoles.  One warp per (point, EE/BB, pair, request).
+// +-(1 - t)/t; rf [B][2][pss][nreq].  dlnC/dlnk: for l > lmin_tab (when tab
+// is given) dlnC_ss_dlnk_tomo_limber, bilinear on tab [B][2][pss][nlnk][nell]
+// over the grid lims (ln k: lim[0..2], ln l: lim[3..5]), 0 outside; else the
+// nointerp ratio with css from k_scut_css at the requests' multipoles.  One
+// warp per (point, EE/BB, pair, request).
 __global__ void k_scut_rf(Params P, int nreq, const double* __restrict__ kmax, const double* __restrict__ l,
                           int nt, const double* __restrict__ tx, const double* __restrict__ tw,
-                          const double* __restrict__ css, double* __restrict__ rf)
+                          const double* __restrict__ css, const double* __restrict__ tab, int nlnk, int nell,
+                          const double* __restrict__ lim, double* __restrict__ rf)
 {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int total = P.B * 2 * P.pss * nreq;
@@ -655,7 +717,17 @@ __global__ void k_scut_rf(Params P, int nreq, const double* __restrict__ kmax, c
   const int e = r2 % 2, pt = r2 / 2;
   const int n1 = P.z1[pr], n2 = P.z2[pr];
   const double C0 = css[(((size_t)pt * P.pss + pr) * 2 + e) * nreq + i];
+  const bool use_tab = tab != nullptr && l[i] > P.lmin_tab;
+  const double lnl = log(l[i]);
+  const double* tb = use_tab ? tab + (((size_t)pt * 2 + e) * P.pss + pr) * (size_t)nlnk * nell : nullptr;
   auto dlnC = [&](double kk) {
+    if (use_tab) {
+      const double lnk = log(kk);
+      return (lnk < lim[0] || lnk > lim[1]) ? 0.0
+             : (lnl < lim[3] || lnl > lim[4])
+                 ? 0.0
+                 : interpol2d_d(tb, nlnk, lim[0], lim[1], lim[2], lnk, nell, lim[3], lim[4], lim[5], lnl);
+    }
     const double d = dCss_dlnk_d(P, pt, kk, l[i], n1, n2, e == 0);
     const double C = (fabs(d) > 1e-30) ? C0 : 1.0;
     return (fabs(C) > 1e-30) ? d / C : 0.0;
@@ -810,10 +882,19 @@ void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const do
   k_scut_dlnk<<<dim3(P.B, 2 * P.pss, tiles), 128, 0, s>>>(P, nk, k, nl, l, css, dC, dlnC);
 }
 void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
-                    const double* tw, const double* css, double* rf, cudaStream_t s)
+                    const double* tw, const double* css, const double* tab, int nlnk, int nell, const double* lim,
+                    double* rf, cudaStream_t s)
 {
   const int warps = P.B * 2 * P.pss * nreq;
-  k_scut_rf<<<(warps * 32 + 255) / 256, 256, 0, s>>>(P, nreq, kmax, l, nt, tx, tw, css, rf);
+  k_scut_rf<<<(warps * 32 + 255) / 256, 256, 0, s>>>(P, nreq, kmax, l, nt, tx, tw, css, tab, nlnk, nell, lim, rf);
+}
+void launch_scut_dlnC_tab(const Params& P, int nlnk, int nell, int nns, int nint, const double* css_ss, double* dC,
+                          const unsigned char* kok, const unsigned char* lok, const double* lnl, double ls0,
+                          double ls2, cudaStream_t s)
+{
+  const long n = (long)P.B * 2 * P.pss * nlnk * nell;
+  const int blocks = (int)std::min<long>((n + 255) / 256, 152L * 16);
+  k_scut_dlnC_tab<<<blocks, 256, 0, s>>>(P.B, P.pss, nlnk, nell, nns, nint, css_ss, dC, kok, lok, lnl, ls0, ls2);
 }
 
 // ---- CMB-lensing spectra of the 6x2pt probes, FP64: C_gk, C_ks and C_kk

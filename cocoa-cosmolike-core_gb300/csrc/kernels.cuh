@@ -34,7 +34,12 @@ void launch_scut_css(const Params& P, int nl, const double* l, double* out, cuda
 void launch_scut_dlnk(const Params& P, int nk, const double* k, int nl, const double* l, const double* css,
                       double* dC, double* dlnC, cudaStream_t s);
 void launch_scut_rf(const Params& P, int nreq, const double* kmax, const double* l, int nt, const double* tx,
-                    const double* tw, const double* css, double* rf, cudaStream_t s);
+                    const double* tw, const double* css, const double* tab, int nlnk, int nell, const double* lim,
+                    double* rf, cudaStream_t s);
+// dlnC_ss_dlnk_tomo_limber's (ln k, ln l) table, in place over the dC grid
+void launch_scut_dlnC_tab(const Params& P, int nlnk, int nell, int nns, int nint, const double* css_ss, double* dC,
+                          const unsigned char* kok, const unsigned char* lok, const double* lnl, double ls0,
+                          double ls2, cudaStream_t s);
 // real-space scale-cut diagnostics: xi+- from C_ss on the ss nodes,
 // dxi+-/dlnk and dlnxi+-/dlnk on a ln k grid, RF_xi
 void launch_scut_xi(const Params& P, int nn, const double* css, const double* F, int nt, double* xi, cudaStream_t s);

@@ -1292,7 +1292,8 @@ static int stage_batch_inputs(cl2pt_plan* p, const cl2pt_batch* b, cudaStream_t 
 // kernels; kreq/lreq the requests, what 0: the (k, l) grid (dC, dlnC), 1:
 // the RF requests (kmax[i], l[i]) into o1.
 static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const double* k, int nl,
-                    const double* l, double* o0, double* o1, cudaStream_t s)
+                    const double* l, double* o0, double* o1, cudaStream_t s, int nlnk = 190, double gkmin = 1e-5,
+                    double gkmax = 1e2)
 {
   if (!p || !b) return CL2PT_ERR_ARG;
   if (p->P.tatt) return CL2PT_ERR_UNSUPPORTED;  // B modes and TATT terms of the diagnostics are not built
@@ -1311,12 +1312,53 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
   const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
   if (!lnPL) lnPL = lnP;
   const int npr = std::max(T.pss, 1);
-  const int W = p->wave;
+  // the RF above lmin_tab reads dlnC_ss_dlnk_tomo_limber's (ln k, ln l)
+  // table on the grid (nlnk, gkmin, gkmax) x the lens C_l table's ln l nodes
+  bool need_tab = false;
+  if (what == 1) {
+    if (nlnk < 2 || !(gkmin > 0) || !(gkmax > gkmin) || !std::isfinite(gkmax)) return CL2PT_ERR_ARG;
+    for (int i = 0; i < nl; i++) need_tab |= l[i] > p->cfg.lmin_tab;
+  }
+  const int nell = p->cfg.n_ell, nns = p->nnode_ss;
+  const size_t per_tab = (size_t)2 * npr * nlnk * nell;
+  const int W = need_tab ? std::max(1, std::min(p->wave, (int)std::min<size_t>((size_t)2e9 / (8 * per_tab), 1 << 20)))
+                         : p->wave;
   const size_t per = what == 0 ? (size_t)2 * npr * nk * nl : (size_t)2 * npr * nl;
   double *dk = nullptr, *dl = nullptr, *dcss = nullptr, *d0 = nullptr, *d1 = nullptr, *dtx = nullptr;
+  double *dcss_ss = nullptr, *dtab = nullptr, *dgrid = nullptr;  // grid: kx[nlnk], lnl[nell], lim[6]
+  unsigned char* dok = nullptr;
   std::vector<double> tx, tw;
   int st = CL2PT_OK;
   auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  if (need_tab) {
+    std::vector<double> grid(nlnk + nell + 6);
+    std::vector<unsigned char> ok(nlnk + nell);
+    double* lim = grid.data() + nlnk + nell;
+    lim[0] = log(gkmin);
+    lim[1] = log(gkmax);
+    lim[2] = (lim[1] - lim[0]) / ((double)nlnk - 1.);
+    lim[3] = p->lim_g[0];
+    lim[4] = p->lim_g[1];
+    lim[5] = p->lim_g[2];
+    for (int f = 0; f < nlnk; f++) {
+      grid[f] = exp(lim[0] + f * lim[2]);
+      const double lnk = log(grid[f]);
+      ok[f] = (lnk < lim[0] || lnk > lim[1]) ? 0 : 1;
+    }
+    for (int i = 0; i < nell; i++) {
+      const double lnl = log(exp(lim[3] + i * lim[5]));
+      grid[nlnk + i] = lnl;
+      ok[nlnk + i] = (lnl < lim[3] || lnl > lim[4]) ? 0 : 1;
+    }
+    fail(cudaMalloc((void**)&dcss_ss, sizeof(double) * (size_t)W * npr * 2 * nns));
+    fail(cudaMalloc((void**)&dtab, sizeof(double) * (size_t)W * per_tab));
+    fail(cudaMalloc((void**)&dgrid, sizeof(double) * grid.size()));
+    fail(cudaMalloc((void**)&dok, ok.size()));
+    if (!st) {
+      fail(cudaMemcpy(dgrid, grid.data(), sizeof(double) * grid.size(), cudaMemcpyHostToDevice));
+      fail(cudaMemcpy(dok, ok.data(), ok.size(), cudaMemcpyHostToDevice));
+    }
+  }
   fail(cudaMalloc((void**)&dk, sizeof(double) * nk));
   fail(cudaMalloc((void**)&dl, sizeof(double) * nl));
   fail(cudaMalloc((void**)&dcss, sizeof(double) * (size_t)W * npr * 2 * nl));
@@ -1363,7 +1405,16 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
     cl2pt::launch_setup(P, s, &launches, hk);
     cl2pt::launch_scut_css(P, nl, dl, dcss, s);
     if (what == 0) cl2pt::launch_scut_dlnk(P, nk, dk, nl, dl, dcss, d0, d1, s);
-    else cl2pt::launch_scut_rf(P, nl, dk, dl, (int)tx.size(), dtx, dtx + tx.size(), dcss, d0, s);
+    else {
+      if (need_tab) {
+        cl2pt::launch_scut_css(P, nns, p->d_ell_ss, dcss_ss, s);
+        cl2pt::launch_scut_dlnk(P, nlnk, dgrid, nell, p->d_ell_g + p->nint, nullptr, dtab, nullptr, s);
+        cl2pt::launch_scut_dlnC_tab(P, nlnk, nell, nns, p->nint, dcss_ss, dtab, dok, dok + nlnk, dgrid + nlnk,
+                                    p->lim_ss[0], p->lim_ss[2], s);
+      }
+      cl2pt::launch_scut_rf(P, nl, dk, dl, (int)tx.size(), dtx, dtx + tx.size(), dcss, dtab, nlnk, nell,
+                            dgrid ? dgrid + nlnk + nell : nullptr, d0, s);
+    }
     fail(cudaGetLastError());
     const size_t bytes = sizeof(double) * per * P.B;
     const cudaMemcpyKind kind = b->where == CL2PT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -1381,6 +1432,10 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
   cudaFree(d0);
   cudaFree(d1);
   cudaFree(dtx);
+  cudaFree(dcss_ss);
+  cudaFree(dtab);
+  cudaFree(dgrid);
+  cudaFree(dok);
   if (!st) {
     int e = 0;
     fail(cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1558,6 +1613,13 @@ extern "C" int cl2pt_scut_ss_rf(cl2pt_plan* p, const cl2pt_batch* b, int nreq, c
 {
   if (!rf) return CL2PT_ERR_ARG;
   return scut_run(p, b, 1, nreq, kmax, nreq, l, nullptr, rf, (cudaStream_t)stream);
+}
+
+extern "C" int cl2pt_scut_ss_rf_grid(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmin, double kmax,
+                                     int nreq, const double* kmax_req, const double* l, double* rf, void* stream)
+{
+  if (!rf) return CL2PT_ERR_ARG;
+  return scut_run(p, b, 1, nreq, kmax_req, nreq, l, nullptr, rf, (cudaStream_t)stream, nlnk, kmin, kmax);
 }
 
 // CMB-lensing spectra of the 6x2pt probes: per wave the set-up stage (lens

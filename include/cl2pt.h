@@ -341,14 +341,19 @@ int cl2pt_plan_get_contraction(const cl2pt_plan* plan, int* mode);
  *     nointerp branch of int_RF_C_ss, :257-284); either output may be NULL;
  *   cl2pt_scut_ss_rf: rf[n][2][pss][nreq] = RF_C_ss_tomo_limber_nointerp
  *     (:329-375) at (kmax[i], l[i]): the fraction of the integral of
- *     |dlnC/dlnk| over ln k that lies below ln kmax, with the nointerp
- *     dlnC/dlnk at every l (the reference reads its (ln k, ln l) table for
- *     l > LMIN_tab).
+ *     |dlnC/dlnk| over ln k that lies below ln kmax; dlnC/dlnk is the
+ *     nointerp ratio for l <= lmin_tab and, above, dlnC_ss_dlnk_tomo_limber's
+ *     (ln k, ln l) table (:157-255) on the reference's default ln k grid
+ *     (190 nodes on [1e-5, 1e2] h/Mpc); cl2pt_scut_ss_rf_grid takes the
+ *     grid (Ntable.dCX_dlnk_nlnk / _kmin / _kmax).  (The reference itself
+ *     exits for l <= LMIN_tab: its quadrature sends k to 0.)
  * k, l, kmax in host memory; outputs follow batch->where. */
 int cl2pt_scut_ss_dlnk(cl2pt_plan* plan, const cl2pt_batch* batch, int nk, const double* k, int nl,
                        const double* l, double* dC, double* dlnC, void* stream);
 int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const double* kmax, const double* l,
                      double* rf, void* stream);
+int cl2pt_scut_ss_rf_grid(cl2pt_plan* plan, const cl2pt_batch* batch, int nlnk, double kmin, double kmax, int nreq,
+                          const double* kmax_req, const double* l, double* rf, void* stream);
 /* Real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740,
  * limber = 1, NLA / no-IA plans) on the ln k grid of nlnk nodes over
  * [kmin, kmax] h/Mpc (the reference's Ntable.dCX_dlnk_nlnk / _kmin / _kmax,

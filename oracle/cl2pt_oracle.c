@@ -866,8 +866,28 @@ static double dlnC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)
  * ln kmax, both integrals as 256-point Gauss-Legendre sums in t on
  * [1e-5, 1] with ln k = ln kmax - (1 - t)/t (numerator) and +-(1 - t)/t
  * (denominator) */
+static double dlnC_ss_limber(double k, double l, int ni, int nj, int EE);
+/* RF_C_ss_tomo_limber_nointerp (cosmo2D_scuts.c:329-375) with int_RF_C_ss /
+ * int_norm_RF_C_ss (:257-327): dlnC/dlnk from the (ln k, ln l) table
+ * (dlnC_ss_dlnk_tomo_limber) for l > LMIN_tab, else the nointerp ratio */
 double orc_RF_C_ss_nointerp(double kmax, double l, int ni, int nj, int EE)
 {
+  if (l > g.cfg.lmin_tab) {
+    const int hdi = abs(g.cfg.high_def_integration);
+    const int n = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
+    const glrule* r = rule(n);
+    const double lnkmax = log(kmax);
+    double num = 0.0, den = 0.0;
+    for (int m = 0; m < n; m++) {
+      double t, w;
+      num_gl_point(1e-5, 1.0, m, n, r->x, r->w, &t, &w);
+      const double s = (1. - t) / t;
+      num += w * fabs(dlnC_ss_limber(exp(lnkmax - s), l, ni, nj, EE)) / (t * t);
+      den += w * (fabs(dlnC_ss_limber(exp(s), l, ni, nj, EE)) + fabs(dlnC_ss_limber(exp(-s), l, ni, nj, EE))) /
+             (t * t);
+    }
+    return num / den;
+  }
   const int hdi = abs(g.cfg.high_def_integration);
   const int n = hdi == 0 ? 256 : (hdi == 1 ? 512 : 1024);
   const glrule* r = rule(n);
@@ -1567,6 +1587,76 @@ int orc_dlnxi_table(int nlnk, double kmin, double kmax, double* out)
   memcpy(xis.lim, lk, sizeof lk);
   return CL2PT_OK;
 }
+/* the ln k grid of the dC/dlnk tables (Ntable.dCX_dlnk_nlnk / _kmin /
+ * _kmax, structs.c:276-278) and dlnC_ss_dlnk_tomo_limber's table
+ * (cosmo2D_scuts.c:157-255): dC from dC_ss_dlnk_tomo_limber's bilinear table
+ * at each node over C_ss_tomo_limber there, [2][pss][nlnk][n_ell] */
+static struct {
+  int nlnk, have;
+  double kmin, kmax, lk[3], ll[3];
+  double* tab;
+} dlc = {190, 0, 1e-5, 1e2, {0}, {0}, NULL};
+int orc_set_dlnk_grid(int nlnk, double kmin, double kmax)
+{
+  dlc.nlnk = nlnk;
+  dlc.kmin = kmin;
+  dlc.kmax = kmax;
+  dlc.have = 0;
+  return CL2PT_OK;
+}
+static void build_dlnC(void)
+{
+  if (!g.have_tables) build_tables();
+  if (!g.have_g) build_g_tables();
+  const int nell = g.cfg.n_ell, np = g.pss, nlnk = dlc.nlnk;
+  double* ll = dlc.ll;
+  double* lk = dlc.lk;
+  ll[0] = log(fmax(g.cfg.lmin_tab, 1.0));
+  ll[1] = log(g.cfg.lmax + 1.);
+  ll[2] = (ll[1] - ll[0]) / ((double)nell - 1.);
+  lk[0] = log(dlc.kmin);
+  lk[1] = log(dlc.kmax);
+  lk[2] = (lk[1] - lk[0]) / ((double)nlnk - 1.);
+  double* T = malloc(sizeof(double) * 2 * np * nlnk * nell);
+  #pragma omp parallel for collapse(3) schedule(static, 1)
+  for (int f = 0; f < nlnk; f++)
+    for (int q = 0; q < np; q++)
+      for (int i = 0; i < nell; i++) {
+        const double kx = exp(lk[0] + f * lk[2]), lx = exp(ll[0] + i * ll[2]);
+        T[((size_t)(0 * np + q) * nlnk + f) * nell + i] = orc_dC_ss_dlnk_nointerp(kx, lx, g.z1[q], g.z2[q], 1);
+        T[((size_t)(1 * np + q) * nlnk + f) * nell + i] = orc_dC_ss_dlnk_nointerp(kx, lx, g.z1[q], g.z2[q], 0);
+      }
+  free(dlc.tab);
+  dlc.tab = malloc(sizeof(double) * 2 * np * nlnk * nell);
+  for (int p = 0; p < 2; p++)
+    for (int q = 0; q < np; q++)
+      for (int f = 0; f < nlnk; f++)
+        for (int i = 0; i < nell; i++) {
+          const double lx = exp(ll[0] + i * ll[2]), kx = exp(lk[0] + f * lk[2]);
+          const double lnl = log(lx), lnk = log(kx);
+          const double dC = (lnk < lk[0] || lnk > lk[1]) ? 0.0
+                            : (lnl < ll[0] || lnl > ll[1])
+                                ? 0.0
+                                : interpol2d_r(T + (size_t)(p * np + q) * nlnk * nell, nlnk, lk[0], lk[1], lk[2],
+                                               lnk, nell, ll[0], ll[1], ll[2], lnl);
+          const double C = (fabs(dC) > 1e-30) ? orc_C_ss_limber(lx, g.z1[q], g.z2[q], 1 - p) : 1.0;
+          dlc.tab[((size_t)(p * np + q) * nlnk + f) * nell + i] = (fabs(C) > 1e-30) ? dC / C : 0.0;
+        }
+  free(T);
+  dlc.have = 1;
+}
+static double dlnC_ss_limber(double k, double l, int ni, int nj, int EE)
+{
+  if (!dlc.have) build_dlnC();
+  const int q = g.nshear[ni][nj];
+  const double lnl = log(l), lnk = log(k);
+  return (lnk < dlc.lk[0] || lnk > dlc.lk[1]) ? 0.0
+         : (lnl < dlc.ll[0] || lnl > dlc.ll[1])
+             ? 0.0
+             : interpol2d_r(dlc.tab + (size_t)((EE ? 0 : 1) * g.pss + q) * dlc.nlnk * g.cfg.n_ell, dlc.nlnk,
+                            dlc.lk[0], dlc.lk[1], dlc.lk[2], lnk, g.cfg.n_ell, dlc.ll[0], dlc.ll[1], dlc.ll[2], lnl);
+}
+
 /* RF_xi_tomo_limber_nointerp (:697-740) with int_RF_xi / int_norm_RF_xi
  * (:649-695) on the last orc_dlnxi_table: p 0 xi+, 1 xi-; shear pair q */
 static double dlnxi_at(int p, int q, int i, double k)
@@ -1976,6 +2066,7 @@ int orc_data_vector_fourier(int nell, const double* ell, double lmax_shear,
 /* ------------------------------------------------------------------------ */
 static void invalidate_point(void)
 {
+  dlc.have = 0;
   g.have_g = 0;
   g.have_tables = 0;
   g.have_fptb = 0;

@@ -264,6 +264,14 @@ class Oracle:
             raise RuntimeError(f"w_{which} failed: {st}")
         return out
 
+    def set_dlnk_grid(self, nlnk=190, kmin=1e-5, kmax=1e2):
+        """The ln k grid of the dC/dlnk tables (Ntable.dCX_dlnk_*); the
+        point must be set (the reference builds its tables on demand)."""
+        f = getattr(self.lib, self.which + "_set_dlnk_grid")
+        f.argtypes = [C.c_int, C.c_double, C.c_double]
+        if f(int(nlnk), float(kmin), float(kmax)) != 0:
+            raise RuntimeError("set_dlnk_grid failed")
+
     def dlnxi_table(self, nlnk, kmin, kmax):
         """dlnxi+-/dlnk [2][pss][ntheta][nlnk] on the nlnk ln k nodes of
         [kmin, kmax] (dlnxi_dlnk_pm_tomo); also the table RF_xi reads."""

@@ -326,6 +326,19 @@ int ref_dlnxi_table(int nlnk, double kmin, double kmax, double* out)
               dlnxi_dlnk_pm_tomo(exp(l0 + f * l2), p == 0 ? 1 : -1, i, Z1(q), Z2(q));
   return 0;
 }
+/* the ln k grid of the dC/dlnk tables */
+int ref_set_dlnk_grid(int nlnk, double kmin, double kmax)
+{
+  Ntable.dCX_dlnk_nlnk = nlnk;
+  Ntable.dCX_dlnk_kmin = kmin;
+  Ntable.dCX_dlnk_kmax = kmax;
+  Ntable.random = (double) next_token();
+  /* the lazily built tables first, serially (see ref_dlnxi_table) */
+  (void) xi_pm_tomo(1, 0, Z1(0), Z2(0), 1);
+  (void) C_ss_tomo_limber(100.0, Z1(0), Z2(0), 1);
+  (void) dC_ss_dlnk_tomo_limber_nointerp(0.1, 100.0, Z1(0), Z2(0), 1);
+  return 0;
+}
 /* the Fourier scale-cut diagnostics (cosmo2D_scuts.c:42-74, 329-375); the
  * reference's RF reads its interpolated dlnC table above LMIN_tab */
 double ref_dC_ss_dlnk_nointerp(double k, double l, int ni, int nj, int EE)

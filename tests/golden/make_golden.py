@@ -51,9 +51,10 @@ def run_case(case, which="ref"):
         return out
     if case == "scale_cuts_small":
         # cosmo2D_scuts.c on real_3x2pt_small_nla's points: dC_ss/dlnk on a
-        # (k, l) grid, and the real-space dlnxi/dlnk table and RF_xi.  (The
-        # reference's RF_C_ss exits at l <= lmin_tab: its quadrature nodes
-        # near t = 1e-5 underflow k to 0, which dC_ss_dlnk rejects.)
+        # (k, l) grid, RF_C_ss at l > lmin_tab (from its dlnC table), and the
+        # real-space dlnxi/dlnk table and RF_xi.  (The reference's RF_C_ss
+        # exits at l <= lmin_tab: its quadrature nodes near t = 1e-5
+        # underflow k to 0, which dC_ss_dlnk rejects.)
         w = workloads.make("real_3x2pt_small_nla")
         o.setup(w.cfg, w.src, w.lens)
         tabs, nus = workloads.points(w, 2, seed=41)
@@ -61,6 +62,9 @@ def run_case(case, which="ref"):
         for i in range(2):
             o.set_point(tabs[i], nus[i])
             out[f"dC_{i}"] = np.array([[[o.dC_ss_dlnk(k, l, a, b) for l in sc["l"]] for k in sc["k"]]
+                                       for a, b in sc["pairs"]])
+            o.set_dlnk_grid(sc["nlnk"], sc["kmin"], sc["kmax"])
+            out[f"rf_{i}"] = np.array([[o.RF_C_ss(km, l, a, b) for km, l in zip(sc["rf_kmax"], sc["rf_l"])]
                                        for a, b in sc["pairs"]])
             out[f"dlnxi_{i}"] = o.dlnxi_table(sc["nlnk"], sc["kmin"], sc["kmax"])
             out[f"rfxi_{i}"] = np.array([[[[o.RF_xi(km, p, t, q) for km in sc["xi_kmax"]]

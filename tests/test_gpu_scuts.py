@@ -91,6 +91,8 @@ def test_scuts_vs_reference_golden(gpu_lib, prec):
     dC, _ = plan.scut_ss_dlnk(*args, nus, sc["k"], sc["l"], lnPL=lnPL)
     dxi, dln = plan.scut_xi_dlnk(*args, nus, sc["nlnk"], sc["kmin"], sc["kmax"], lnPL=lnPL)
     rf = plan.scut_xi_rf(*args, nus, sc["xi_kmax"], sc["nlnk"], sc["kmin"], sc["kmax"], lnPL=lnPL)
+    rfc = plan.scut_ss_rf(*args, nus, sc["rf_kmax"], sc["rf_l"], lnPL=lnPL,
+                          grid=(sc["nlnk"], sc["kmin"], sc["kmax"]))
     assert np.all(dxi[:, :, :, :, 0] == 0.0)  # k = 1e-5: no source at chi = (l + 1/2) / k
     worst = {}
     for pt in range(2):
@@ -102,5 +104,8 @@ def test_scuts_vs_reference_golden(gpu_lib, prec):
         worst["dlnxi"] = max(worst.get("dlnxi", 0.0), float(np.max(np.abs(dln[pt] - ref) / scale)))
         ref = g[f"rfxi_{pt}"]
         worst["rf"] = max(worst.get("rf", 0.0), float(np.max(np.abs(rf[pt] - ref))))
+        ref = g[f"rf_{pt}"]
+        got = np.array([rfc[pt, 0, pairs.index(pq)] for pq in sc["pairs"]])
+        worst["rf_C"] = max(worst.get("rf_C", 0.0), float(np.max(np.abs(got - ref))))
     print("scale cuts vs reference", worst)
-    assert worst["dC"] <= 1e-9 and worst["dlnxi"] <= 1e-8 and worst["rf"] <= 1e-8
+    assert worst["dC"] <= 1e-9 and worst["dlnxi"] <= 1e-8 and worst["rf"] <= 1e-8 and worst["rf_C"] <= 1e-9
