@@ -2080,6 +2080,11 @@ int orc_setup(const cl2pt_config* cfg, const cl2pt_nz* src, const cl2pt_nz* lens
   if (cfg->n_source > MAXB || cfg->n_lens > MAXB) return CL2PT_ERR_ARG;
   if (cfg->ia_mode == CL2PT_IA_NLA_LF) return CL2PT_ERR_UNSUPPORTED;
   g.cfg = *cfg;
+  /* a fresh set-up starts without the optional state of an earlier one
+   * (the baryon ratio, the CMB map filter, the dC/dlnk grid) */
+  orc_set_baryon_ratio(0, NULL, 0, NULL, NULL);
+  orc_set_cmb(0, 0, 0.0, 0, NULL);
+  orc_set_dlnk_grid(190, 1e-5, 1e2);
   int st = load_nz(&g.src, src, 1);
   if (st) return st;
   st = load_nz(&g.lens, lens, 0);

@@ -69,6 +69,12 @@ int orc_data_vector_real(const int* mask, const double* pm, double* dv);
 int orc_data_vector_fourier(int nell, const double* ell, double lmax_shear,
                             int use_nonlimber, const int* mask, double* dv);
 
+/* optional state (reset by orc_setup): the baryon P(k) ratio of p_nonlin,
+ * the CMB map filter of w_gk / w_ks, the ln k grid of the dC/dlnk tables */
+int orc_set_baryon_ratio(int nk, const double* log10k, int na, const double* a, const double* log10r);
+int orc_set_cmb(int lmin, int lmax, double fwhm_rad, int ncls, const double* win);
+int orc_set_dlnk_grid(int nlnk, double kmin, double kmax);
+
 /* FAST-PT (fastpt_oracle.c) */
 void orc_J_abl(const double* x, const double* fx, long N, const int* alpha,
                const int* beta, const int* ell, int nterms, double nu,
