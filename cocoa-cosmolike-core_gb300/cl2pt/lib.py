@@ -78,6 +78,8 @@ def load(path: str = LIB_PATH):
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
     lib.cl2pt_like_create.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.POINTER(C.c_void_p)]
+    lib.cl2pt_baryon_pcas.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Batch), C.c_int, C.c_int, _dp, C.c_int, _dp,
+                                      _dp, C.c_void_p, C.c_void_p]
     lib.cl2pt_like_destroy.argtypes = [C.c_void_p]
     lib.cl2pt_loglike_real.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Batch), C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -440,6 +442,18 @@ class Plan:
         check(load().cl2pt_like_create(self.h, mk.ctypes.data if mk is not None else None, _p(d), _p(ic),
                                        C.byref(h)), "cl2pt_like_create")
         return Likelihood(h, self)
+
+    def baryon_pcas(self, like, omega_m, h0, chi, G, lnP, nuisance, log10k, a, log10r, lnPL=None):
+        """Baryon PCs [nscen][n_total] of one point (cl2pt_baryon_pcas);
+        log10r [nscen][len(a)][len(log10k)]."""
+        b, keep = self._host_batch(omega_m, h0, chi, G, lnP, nuisance, lnPL)
+        lk = np.ascontiguousarray(log10k, dtype=np.float64)
+        av = np.ascontiguousarray(a, dtype=np.float64)
+        lr = np.ascontiguousarray(log10r, dtype=np.float64)
+        R = np.zeros((lr.shape[0], self.n_total))
+        check(load().cl2pt_baryon_pcas(self.h, like.h, C.byref(b), lr.shape[0], len(lk), _p(lk), len(av), _p(av),
+                                       _p(lr), R.ctypes.data, None), "cl2pt_baryon_pcas")
+        return R
 
     def loglike_real(self, like, omega_m, h0, chi, G, lnP, nuisance, pm=None, grad=False, lnPL=None):
         """chi2 [n] (host arrays); with grad also (lnP_bar, nu_bar) of

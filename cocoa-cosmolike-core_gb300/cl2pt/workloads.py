@@ -227,6 +227,26 @@ def scale_cut_requests():
                 nlnk=60, kmin=1e-5, kmax=1e2, xi_kmax=np.array([0.05, 0.3, 1.0, 5.0]))
 
 
+def baryon_scenarios(n: int = 4):
+    """n synthetic baryon-feedback scenarios standing in for the hydro
+    simulations the reference reads (PkRatio_baryons tables): log10 of a
+    smooth suppression 1 - A x(k) a^p with x(k) a tanh step at log10 k0
+    and width w, per scenario (A, k0, w, p) spread over (0.1-0.3, -0.3-0.6,
+    0.25-0.45, 0.3-1.2), plus a small seeded bump; on a (log10 k [h/Mpc], a)
+    grid of 41 x 16 that the P(k, z) tables exceed on both sides."""
+    lk = np.linspace(-2.5, 1.5, 41)
+    a = np.linspace(0.25, 1.0, 16)
+    rng = np.random.default_rng(SEED0 + 91)
+    out = []
+    for i in range(n):
+        t = i / max(n - 1, 1)
+        A, k0, wd, pw = 0.1 + 0.2 * t, -0.3 + 0.9 * t, 0.25 + 0.2 * (1 - t), 0.3 + 0.9 * t
+        x = 0.5 * (1.0 + np.tanh((lk - k0) / wd))
+        bump = 0.02 * rng.uniform(0.5, 1.0) * np.exp(-0.5 * ((lk - rng.uniform(-0.5, 0.5)) / 0.3) ** 2)
+        out.append(np.log10(1.0 - A * x[None, :] * a[:, None] ** pw) + bump[None, :] * a[:, None])
+    return lk, a, np.ascontiguousarray(np.stack(out))
+
+
 def cmb_map_filter():
     """The CMB map filter of the real-space CMB-lensing cross-correlations
     (init_cmb_cross_correlation's arguments): l in [2, 3000], a 5 arcmin

@@ -113,6 +113,10 @@ void launch_assemble_fourier(const Params& P, int nell, const double* ell, doubl
                              const int* mask, double* dv, cudaStream_t s, int* launches, const Hook& hk);
 // masked chi^2 of points [npt] and, when cot is not null, the cotangent of
 // ln L = -chi^2/2 on the kept entries (k_like.cu)
+// baryon PCA from the data vectors dv [n + 1][n_total] (row 0 without
+// baryons): work holds n n_total + n nsq + 2 n^2 + n doubles; R [n][n_total]
+void launch_pca(const double* dv, int n, int n_total, const int* idx, int nsq, const float* cinv_hi,
+                const float* cinv_lo, double* work, double* R, cudaStream_t s);
 void launch_chi2(const double* dv, int n_total, int npt, const int* idx, const double* data, int nsq,
                  const float* cinv_hi, const float* cinv_lo, double* chi2, double* cot, cudaStream_t s);
 // ragged output of points w0 .. w0+B-1 from their full vectors (k_legendre.cu)

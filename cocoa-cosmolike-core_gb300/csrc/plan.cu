@@ -2000,6 +2000,69 @@ extern "C" int cl2pt_like_destroy(cl2pt_like* L)
   return CL2PT_OK;
 }
 
+// Baryon PCA (compute_baryon_pcas_Mx2pt_N, generic_interface.hpp:1168-1225,
+// real space): the masked data vector of the one point in batch without
+// baryons and with each scenario's P(k) ratio (log10r [nscen][na][nk] on
+// the common (log10 k, a) grid), then launch_pca (k_like.cu) on the
+// differences; R [nscen][n_total], zero on masked entries, PC i in row i.
+// The plan's own baryon ratio is restored afterwards.
+extern "C" int cl2pt_baryon_pcas(cl2pt_plan* p, const cl2pt_like* L, const cl2pt_batch* b, int nscen, int nk,
+                                 const double* log10k, int na, const double* a, const double* log10r, double* R,
+                                 void* stream)
+{
+  if (!p || !L || !b || !R || b->n != 1 || nscen < 1 || nscen > 64 || !log10r) return CL2PT_ERR_ARG;
+  if (L->n_total != p->n_total) return CL2PT_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nt = p->n_total;
+  const size_t nlr = p->pk_lk.size() * p->pk_z.size();
+  // the plan's baryon state, restored at the end
+  const bool bary0 = p->bary_on;
+  std::vector<double> lnr0;
+  if (bary0) {
+    lnr0.resize(nlr);
+    CUDA_OK(cudaMemcpy(lnr0.data(), p->d_bary_lnr, sizeof(double) * nlr, cudaMemcpyDeviceToHost));
+  }
+  const bool host = b->where == CL2PT_HOST;
+  std::vector<double> hdv(host ? (size_t)(nscen + 1) * nt : 0);
+  double *ddv = nullptr, *dwork = nullptr, *dR = nullptr;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&ddv, sizeof(double) * (size_t)(nscen + 1) * nt));
+  fail(cudaMalloc((void**)&dwork, sizeof(double) * ((size_t)nscen * (nt + L->nsq) + nscen + 2 * (size_t)nscen * nscen)));
+  fail(cudaMalloc((void**)&dR, sizeof(double) * (size_t)nscen * nt));
+  for (int i = -1; i < nscen && !st; i++) {
+    if (i < 0) {
+      p->bary_on = false;
+    } else if (int e = cl2pt_plan_set_baryon_ratio(p, nk, log10k, na, a, log10r + (size_t)i * na * nk)) {
+      st = e;
+      break;
+    }
+    double* out = host ? hdv.data() + (size_t)(i + 1) * nt : ddv + (size_t)(i + 1) * nt;
+    if (int e = cl2pt_eval_real(p, b, L->mask.data(), nullptr, out, stream)) st = e;
+  }
+  if (!st && host) fail(cudaMemcpyAsync(ddv, hdv.data(), sizeof(double) * hdv.size(), cudaMemcpyHostToDevice, s));
+  if (!st) {
+    cl2pt::launch_pca(ddv, nscen, nt, L->d_idx, L->nsq, L->d_hi, L->d_lo, dwork, dR, s);
+    fail(cudaGetLastError());
+    fail(cudaMemcpyAsync(R, dR, sizeof(double) * (size_t)nscen * nt,
+                         host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    fail(cudaStreamSynchronize(s));
+  }
+  cudaFree(ddv);
+  cudaFree(dwork);
+  cudaFree(dR);
+  // restore the plan's baryon ratio
+  if (bary0) {
+    if (cudaMemcpy(p->d_bary_lnr, lnr0.data(), sizeof(double) * nlr, cudaMemcpyHostToDevice) != cudaSuccess &&
+        !st)
+      st = CL2PT_ERR_CUDA;
+    p->bary_on = true;
+  } else {
+    p->bary_on = false;
+  }
+  return st;
+}
+
 extern "C" int cl2pt_loglike_real(cl2pt_plan* p, const cl2pt_like* L, const cl2pt_batch* b, const double* pm,
                                   double* chi2, double* lnP_bar, double* lnPL_bar, cl2pt_nuisance* nu_bar,
                                   void* stream)

@@ -211,6 +211,20 @@ typedef struct cl2pt_like cl2pt_like;
 int cl2pt_like_create(cl2pt_plan* plan, const int* mask, const double* data, const double* inv_cov,
                       cl2pt_like** like);
 int cl2pt_like_destroy(cl2pt_like* like);
+/* Baryon PCA of the real-space data vector (compute_baryon_pcas_Mx2pt_N,
+ * generic_interface.hpp:1168-1225): for the one point of batch (n = 1),
+ * the masked data vector without baryons and with each of nscen baryon
+ * scenarios (PkRatio_baryons tables log10r [nscen][na][nk] on one
+ * (log10 k [h/Mpc], a) grid, as cl2pt_plan_set_baryon_ratio takes them),
+ * their differences D whitened by the like's covariance, and the PCs L U_i
+ * of the SVD L^-1 D = U S V^T (C = L L^T), i = 0..nscen-1 by descending
+ * singular value: R [nscen][n_total], zero on masked entries, each PC's
+ * sign as the eigen solver leaves it (singular vectors are defined up to
+ * sign).  The plan's own baryon ratio is left as it was.  R follows
+ * batch->where. */
+int cl2pt_baryon_pcas(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch, int nscen, int nk,
+                      const double* log10k, int na, const double* a, const double* log10r, double* R,
+                      void* stream);
 int cl2pt_loglike_real(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch,
                        const double* pm, double* chi2, double* lnP_bar, double* lnPL_bar,
                        cl2pt_nuisance* nu_bar, void* stream);
