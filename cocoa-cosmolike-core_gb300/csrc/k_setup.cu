@@ -550,14 +550,25 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
   *launches += 2;
 }
 
+// fptb_row (cosmo2D.c:2921-2932): linear in ln k on the FAST-PT grid, 0 off it
+__device__ __forceinline__ double fpt_lerp_d(const Params& P, const double* row, double lnk)
+{
+  if (lnk < P.fpt_lim0 || lnk > P.fpt_lim1) return 0.0;
+  const double r = (lnk - P.fpt_lim0) / P.fpt_lim2;
+  const int i = (int)floor(r);
+  if (i + 1 >= P.fpt_n) return row[P.fpt_n - 1];
+  return (r - i) * (row[i + 1] - row[i]) + row[i];
+}
+
 // ---- scale-cut diagnostics of the cosmic-shear C_l (cosmolike/
-// cosmo2D_scuts.c), FP64, for the plans without TATT: the C_ss integrand
-// (int_for_C_ss_tomo_limber, cosmo2D.c:1521-1556) at any a, in its C_l form
-// (dchida / fK^2) or its dC/dlnk form (dchida / fK, cosmo2D.c:1509-1514);
-// no B modes without TATT.
+// cosmo2D_scuts.c), FP64: the C_ss integrand (int_for_C_ss_tomo_limber,
+// cosmo2D.c:1521-1556, with the TATT terms of int_for_C_ss_tomo_limber_core,
+// :1370-1515, from the point's FAST-PT IA rows P.fpt_ia) at any a, in its
+// C_l form (dchida / fK^2) or its dC/dlnk form (dchida / fK, :1509-1514);
+// EE = 0: the B modes (0 without TATT).
 __device__ double ss_integrand_d(const Params& P, int pt, double a, double l, int n1, int n2, int EE, bool deriv)
 {
-  if (!EE) return 0.0;
+  if (!EE && !P.tatt) return 0.0;
   const cl2pt_nuisance& nu = P.nu[pt];
   const double om = P.omega_m[pt];
   const double* X = P.chi + (size_t)pt * P.chi_nz;
@@ -582,7 +593,31 @@ __device__ double ss_integrand_d(const Params& P, int pt, double a, double l, in
   const double WS1 = nz_source_d(P, z, n1, nu.src_dz[n1]) * hh;
   const double WS2 = nz_source_d(P, z, n2, nu.src_dz[n2]) * hh;
   const double C11 = ia_a1(P, nu, om, a, D, n1), C12 = ia_a1(P, nu, om, a, D, n2);
-  const double ans = WK1 * WK2 * PK - WS1 * WK2 * C11 * PK - WS2 * WK1 * C12 * PK + WS1 * WS2 * C11 * C12 * PK;
+  double ans;
+  if (P.tatt) {
+    // FAST-PT IA rows (linear in ln k, 0 off the grid) times D^4: 0 tt_E,
+    // 1 ta_dE1 + ta_dE2, 2 ta_0E0E, 3 mix_A + mix_B, 4 mix_D_EE, 5 tt_B,
+    // 6 ta_0B0B, 7 mix_D_BB
+    const double* rows = P.fpt_ia + (size_t)pt * 8 * P.fpt_n;
+    const double lnk = log(k), g4 = D * D * D * D;
+    auto row = [&](int r) { return g4 * fpt_lerp_d(P, rows + (size_t)r * P.fpt_n, lnk); };
+    const double C21 = ia_a2(P, nu, om, a, D, n1), C22 = ia_a2(P, nu, om, a, D, n2);
+    const double bta1 = ia_bta(P, nu, n1), bta2 = ia_bta(P, nu, n2);
+    if (EE) {
+      const double tt = row(0), taE = row(1), ta = row(2), mix = row(3), mixEE = row(4);
+      ans = WK1 * WK2 * PK - WS1 * WK2 * (C11 * PK + C11 * bta1 * taE - 5 * C21 * mix) -
+            WS2 * WK1 * (C12 * PK + C12 * bta2 * taE - 5 * C22 * mix) +
+            WS1 * WS2 * (C11 * C12 * PK + C11 * C12 * (bta1 * bta2 * ta + (bta1 + bta2) * taE) -
+                         5. * (C11 * C22 + C12 * C21) * mix - 5. * (C11 * bta1 * C22 + C12 * bta2 * C21) * mixEE +
+                         25. * C21 * C22 * tt);
+    } else {
+      const double tt = row(5), ta = row(6), mix = row(7);
+      ans = WS1 * WS2 *
+            (C11 * C12 * bta1 * bta2 * ta - 5. * (C11 * bta1 * C22 + C12 * bta2 * C21) * mix + 25. * C21 * C22 * tt);
+    }
+  } else {
+    ans = WK1 * WK2 * PK - WS1 * WK2 * C11 * PK - WS2 * WK1 * C12 * PK + WS1 * WS2 * C11 * C12 * PK;
+  }
   return deriv ? ans * (c.dchida / fK) * pref : ans * (c.dchida / (fK * fK)) * pref;
 }
 
@@ -600,20 +635,23 @@ __device__ double dCss_dlnk_d(const Params& P, int pt, double k, double l, int n
 
 // C_ss_tomo_limber_nointerp (cosmo2D.c:1562-1604) at the multipoles l[0..nl):
 // the Gauss-Legendre sum over the point's ss node set; out [B][pss][2][nl]
-// (EE, BB).  One CTA per (point, pair), threads over the multipoles.
+// (EE, BB; BB 0 without TATT).  One CTA per (point, pair), threads over the
+// multipoles.
 __global__ void k_scut_css(Params P, int nl, const double* __restrict__ l, double* __restrict__ out)
 {
   const int pt = blockIdx.x, pr = blockIdx.y;
   const int n1 = P.z1[pr], n2 = P.z2[pr];
   const double* node = P.node + (size_t)pt * NF_COUNT * P.node_stride;
   for (int i = threadIdx.x; i < nl; i += blockDim.x) {
-    double s = 0.0;
-    for (int p = 0; p < P.n_ss; p++)
-      s += node[(size_t)NF_WT * P.node_stride + p] *
-           ss_integrand_d(P, pt, node[(size_t)NF_A * P.node_stride + p], l[i], n1, n2, 1, false);
+    double se = 0.0, sb = 0.0;
+    for (int p = 0; p < P.n_ss; p++) {
+      const double w = node[(size_t)NF_WT * P.node_stride + p], a = node[(size_t)NF_A * P.node_stride + p];
+      se += w * ss_integrand_d(P, pt, a, l[i], n1, n2, 1, false);
+      if (P.tatt) sb += w * ss_integrand_d(P, pt, a, l[i], n1, n2, 0, false);
+    }
     double* o = out + (((size_t)pt * P.pss + pr) * 2) * nl;
-    o[i] = s;
-    o[nl + i] = 0.0;
+    o[i] = se;
+    o[nl + i] = sb;
   }
 }
 
@@ -749,9 +787,11 @@ __global__ void k_scut_rf(Params P, int nreq, const double* __restrict__ kmax, c
 // ---- real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740),
 // limber = 1, FP64.
 // xi+- (xi_pm_tomo) from k_scut_css's C_ss on the ss C_l nodes (css [B][pss]
-// [2][nn]) and the plan's folded G+- filters F [2 nt][nn]: xi [B][2][pss][nt].
-// One warp per (point, +-, pair, theta bin).
-__global__ void k_scut_xi(int B, int pss, int nt, int nn, const double* __restrict__ css,
+// [2][nn]) and the plan's folded G+- filters F: [2 nt][nn], or with TATT the
+// plan's [2 nt][2 nn] rows over [EE; BB] (G+ on both halves for xi+, G- and
+// -G- for xi-); xi [B][2][pss][nt].  One warp per (point, +-, pair, theta
+// bin).
+__global__ void k_scut_xi(int B, int pss, int nt, int nn, int tatt, const double* __restrict__ css,
                           const double* __restrict__ F, double* __restrict__ xi)
 {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -761,10 +801,14 @@ __global__ void k_scut_xi(int B, int pss, int nt, int nn, const double* __restri
   const int pm = r2 % 2, pt = r2 / 2;
   const double* cE = css + (((size_t)pt * pss + pr) * 2) * nn;
   const double* cB = cE + nn;
-  const double* f = F + ((size_t)pm * nt + i) * nn;
-  const double sg = pm == 0 ? 1.0 : -1.0;
   double acc = 0.0;
-  for (int j = lane; j < nn; j += 32) acc += f[j] * (cE[j] + sg * cB[j]);
+  if (tatt) {
+    const double* f = F + ((size_t)pm * nt + i) * 2 * nn;
+    for (int j = lane; j < nn; j += 32) acc += f[j] * cE[j] + f[nn + j] * cB[j];
+  } else {
+    const double* f = F + ((size_t)pm * nt + i) * nn;
+    for (int j = lane; j < nn; j += 32) acc += f[j] * cE[j];
+  }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if (lane == 0) xi[warp] = acc;
 }
@@ -853,7 +897,7 @@ __global__ void k_scut_xi_rf(int B, int pss, int nt, int nlnk, double lk0, doubl
 void launch_scut_xi(const Params& P, int nn, const double* css, const double* F, int nt, double* xi, cudaStream_t s)
 {
   const long warps = (long)P.B * 2 * P.pss * nt;
-  k_scut_xi<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(P.B, P.pss, nt, nn, css, F, xi);
+  k_scut_xi<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(P.B, P.pss, nt, nn, P.tatt, css, F, xi);
 }
 void launch_scut_xi_dlnk(const Params& P, int nt, int nlnk, int nn, int nint, const double* dC, const double* Fg,
                          const unsigned char* kin, const unsigned char* ktab, const double* xi, double* dxi,
@@ -909,16 +953,6 @@ void launch_scut_dlnC_tab(const Params& P, int nlnk, int nell, int nns, int nint
 // Spectrum rows: [0, nl) C_gk of lens bin q, [nl, nl + ns) C_ks of source
 // bin s, nl + ns C_kk; out [B][nl + ns + 1][nell].
 constexpr int CMB_NT = 128, CMB_PC = 128;
-
-// fptb_row (cosmo2D.c:2921-2932): linear in ln k on the FAST-PT grid, 0 off it
-__device__ __forceinline__ double fpt_lerp_d(const Params& P, const double* row, double lnk)
-{
-  if (lnk < P.fpt_lim0 || lnk > P.fpt_lim1) return 0.0;
-  const double r = (lnk - P.fpt_lim0) / P.fpt_lim2;
-  const int i = (int)floor(r);
-  if (i + 1 >= P.fpt_n) return row[P.fpt_n - 1];
-  return (r - i) * (row[i + 1] - row[i]) + row[i];
-}
 
 __global__ void __launch_bounds__(CMB_NT) k_cmb_cl(Params P, int nell, const double* __restrict__ ell, int row0,
                                                    double* __restrict__ out)

@@ -1286,6 +1286,20 @@ static int stage_batch_inputs(cl2pt_plan* p, const cl2pt_batch* b, cudaStream_t 
   return CL2PT_OK;
 }
 
+// The FAST-PT IA rows the TATT terms of the diagnostics' C_ss integrand
+// read (P.fpt_ia), for a TATT plan: p_lin(k, z = 0), the IA spectra, the
+// row sums (the bias rows are not needed here).
+static int scut_tatt_tables(cl2pt_plan* p, const Params& P, cudaStream_t s, int* launches)
+{
+  if (!P.tatt) return CL2PT_OK;
+  cl2pt::launch_fpt_plin(P, s, launches);
+  if (int st = cl2pt_fastpt_ia(p->fpt_ia, P.fpt_plin, P.B, p->d_fpt_ia_out, CL2PT_DEVICE, s)) return st;
+  Params Pi = P;
+  Pi.one_loop = 0;
+  cl2pt::launch_fpt_tables(Pi, nullptr, p->d_fpt_ia_out, s, launches);
+  return CL2PT_OK;
+}
+
 // Scale-cut diagnostics of C_ss (cosmolike/cosmo2D_scuts.c): the batch's
 // inputs on the device (the plan's staging for host batches), then per wave
 // the set-up stage (lens efficiencies, the ss node set) and the diagnostic
@@ -1296,7 +1310,6 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
                     double gkmax = 1e2)
 {
   if (!p || !b) return CL2PT_ERR_ARG;
-  if (p->P.tatt) return CL2PT_ERR_UNSUPPORTED;  // B modes and TATT terms of the diagnostics are not built
   if (int st = check_batch(p, b, true)) return st;
   if (nk < 1 || nl < 1 || !k || !l) return CL2PT_ERR_ARG;
   for (int i = 0; i < nk; i++)
@@ -1403,6 +1416,10 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
     }
     P.nu = nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
+    if (int e = scut_tatt_tables(p, P, s, &launches)) {
+      st = e;
+      break;
+    }
     cl2pt::launch_scut_css(P, nl, dl, dcss, s);
     if (what == 0) cl2pt::launch_scut_dlnk(P, nk, dk, nl, dl, dcss, d0, d1, s);
     else {
@@ -1458,7 +1475,6 @@ static int xi_scut_run(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmi
                        double* dlnxi, int nreq, const double* kreq, double* rf, cudaStream_t s)
 {
   if (!p || !b) return CL2PT_ERR_ARG;
-  if (p->P.tatt) return CL2PT_ERR_UNSUPPORTED;  // B modes and TATT terms of the diagnostics are not built
   if (nlnk < 2 || !(kmin > 0) || !(kmax > kmin) || !std::isfinite(kmax)) return CL2PT_ERR_ARG;
   for (int i = 0; i < nreq; i++)
     if (!(kreq[i] > 0) || !std::isfinite(kreq[i])) return CL2PT_ERR_ARG;
@@ -1558,6 +1574,10 @@ static int xi_scut_run(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmi
     }
     P.nu = d.nu + w0;
     cl2pt::launch_setup(P, s, &launches, hk);
+    if (int e = scut_tatt_tables(p, P, s, &launches)) {
+      st = e;
+      break;
+    }
     cl2pt::launch_scut_css(P, nns, p->d_ell_ss, dcss, s);
     cl2pt::launch_scut_xi(P, nns, dcss, p->d_filt_xi, nt, dxiv, s);
     cl2pt::launch_scut_dlnk(P, nlnk, dk, nng, p->d_ell_g, nullptr, ddC, nullptr, s);

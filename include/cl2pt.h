@@ -347,7 +347,8 @@ int cl2pt_plan_get_contraction(const cl2pt_plan* plan, int* mode);
 
 /* Scale-cut diagnostics of the cosmic-shear C_l (cosmolike/cosmo2D_scuts.c;
  * plans without TATT: CL2PT_ERR_UNSUPPORTED), FP64, for every point of the
- * batch, E/B mode e (0 EE, 1 BB; BB is 0 without TATT) and shear pair p in
+ * batch, E/B mode e (0 EE, 1 BB; BB is 0 without TATT; with TATT both
+ * carry the TATT terms of int_for_C_ss_tomo_limber_core) and shear pair p in
  * the plan's pair order (N_shear):
  *   cl2pt_scut_ss_dlnk: dC[n][2][pss][nk][nl] = dC_ss/dlnk at (k[i], l[j])
  *     (dC_ss_dlnk_tomo_limber_nointerp, cosmo2D_scuts.c:42-74; k in h/Mpc)
@@ -369,7 +370,7 @@ int cl2pt_scut_ss_rf(cl2pt_plan* plan, const cl2pt_batch* batch, int nreq, const
 int cl2pt_scut_ss_rf_grid(cl2pt_plan* plan, const cl2pt_batch* batch, int nlnk, double kmin, double kmax, int nreq,
                           const double* kmax_req, const double* l, double* rf, void* stream);
 /* Real-space scale-cut diagnostics of xi+- (cosmo2D_scuts.c:380-740,
- * limber = 1, NLA / no-IA plans) on the ln k grid of nlnk nodes over
+ * limber = 1; with TATT the B modes enter as in xi_pm_tomo) on the ln k grid of nlnk nodes over
  * [kmin, kmax] h/Mpc (the reference's Ntable.dCX_dlnk_nlnk / _kmin / _kmax,
  * by default 190, 1e-5, 1e2), p = 0 for xi+ and 1 for xi-:
  *   cl2pt_scut_xi_dlnk: dxi[n][2][pss][ntheta][nlnk] = dxi/dlnk at the

@@ -22,7 +22,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 CASES = ["cosmic_shear_fourier", "real_3x2pt_small", "real_3x2pt_small_limber", "real_3x2pt",
          "fastpt_bias", "fastpt_ia", "real_3x2pt_tatt_small", "real_3x2pt_small_mag",
          "real_3x2pt_small_nla", "real_3x2pt_small_nlabin", "real_3x2pt_small_hdi",
-         "real_3x2pt_small_lin", "cmb_lensing_small", "cmb_lensing_tatt_small", "scale_cuts_small"]
+         "real_3x2pt_small_lin", "cmb_lensing_small", "cmb_lensing_tatt_small", "scale_cuts_small",
+         "scale_cuts_tatt_small"]
 
 # J_abJ1J2Jk rows {alpha, beta, J1, J2, Jk} checked on the batched FAST-PT grid
 JK_ROWS = [[0, 0, 0, 0, 0], [1, -1, 2, 1, 1], [-1, 1, 1, 3, 2], [0, 0, 4, 2, 2]]
@@ -49,24 +50,30 @@ def run_case(case, which="ref"):
         r = np.array(JK_ROWS)
         out["J_abJ1J2Jk"] = o.J_abJ1J2Jk(k, P[0], r[:, 0], r[:, 1], r[:, 2], r[:, 3], r[:, 4])
         return out
-    if case == "scale_cuts_small":
+    if case in ("scale_cuts_small", "scale_cuts_tatt_small"):
         # cosmo2D_scuts.c on real_3x2pt_small_nla's points: dC_ss/dlnk on a
         # (k, l) grid, RF_C_ss at l > lmin_tab (from its dlnC table), and the
         # real-space dlnxi/dlnk table and RF_xi.  (The reference's RF_C_ss
         # exits at l <= lmin_tab: its quadrature nodes near t = 1e-5
         # underflow k to 0, which dC_ss_dlnk rejects.)
-        w = workloads.make("real_3x2pt_small_nla")
+        # (the _tatt case: real_3x2pt_tatt_small's points, B modes as well)
+        tatt = "tatt" in case
+        w = workloads.make("real_3x2pt_tatt_small" if tatt else "real_3x2pt_small_nla")
         o.setup(w.cfg, w.src, w.lens)
         tabs, nus = workloads.points(w, 2, seed=41)
         sc = workloads.scale_cut_requests()
         for i in range(2):
             o.set_point(tabs[i], nus[i])
-            out[f"dC_{i}"] = np.array([[[o.dC_ss_dlnk(k, l, a, b) for l in sc["l"]] for k in sc["k"]]
-                                       for a, b in sc["pairs"]])
+            for e, tag in ((1, ""), (0, "B")) if tatt else ((1, ""),):
+                out[f"dC{tag}_{i}"] = np.array([[[o.dC_ss_dlnk(k, l, a, b, e) for l in sc["l"]] for k in sc["k"]]
+                                                for a, b in sc["pairs"]])
             o.set_dlnk_grid(sc["nlnk"], sc["kmin"], sc["kmax"])
-            out[f"rf_{i}"] = np.array([[o.RF_C_ss(km, l, a, b) for km, l in zip(sc["rf_kmax"], sc["rf_l"])]
-                                       for a, b in sc["pairs"]])
+            for e, tag in ((1, ""), (0, "B")) if tatt else ((1, ""),):
+                out[f"rf{tag}_{i}"] = np.array([[o.RF_C_ss(km, l, a, b, e)
+                                                 for km, l in zip(sc["rf_kmax"], sc["rf_l"])]
+                                                for a, b in sc["pairs"]])
             out[f"dlnxi_{i}"] = o.dlnxi_table(sc["nlnk"], sc["kmin"], sc["kmax"])
+            out[f"xi_{i}"] = np.stack(o.xi_pm())  # [2][pss][ntheta], the divisors
             out[f"rfxi_{i}"] = np.array([[[[o.RF_xi(km, p, t, q) for km in sc["xi_kmax"]]
                                            for t in range(w.cfg.ntheta)] for q in range(o.npairs[0])]
                                          for p in range(2)])

@@ -68,23 +68,21 @@ def test_rf_vs_oracle(gpu_lib, oracle_built):
 
 
 @pytest.mark.gpu
-def test_scuts_reject_tatt(gpu_lib):
-    w = workloads.make("real_3x2pt_tatt_small")
-    tabs, nus = workloads.points(w, 1, seed=3)
-    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=1)
-    om, h0, chi, G, lnP = workloads.stack(tabs)
-    with pytest.raises(lib.CL2PTError):
-        plan.scut_ss_dlnk(om, h0, chi, G, lnP, nus, [0.1], [100.0])
-
-
-@pytest.mark.gpu
+@pytest.mark.parametrize("gold", ["scale_cuts_small", "scale_cuts_tatt_small"])
 @pytest.mark.parametrize("prec", [lib.PREC_MIXED, lib.PREC_FP64])
-def test_scuts_vs_reference_golden(gpu_lib, prec):
-    """dC_ss/dlnk, the real-space dlnxi/dlnk table and RF_xi against the
-    reference's own outputs (tests/golden/scale_cuts_small.npz)."""
+def test_scuts_vs_reference_golden(gpu_lib, prec, gold):
+    """dC_ss/dlnk, RF_C_ss above lmin_tab, the real-space dlnxi/dlnk table
+    and RF_xi against the reference's own outputs (tests/golden/<gold>.npz;
+    the _tatt case with TATT intrinsic alignments: B modes, and the TATT
+    terms of the E-mode integrand from the FAST-PT IA tables)."""
     import os
-    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scale_cuts_small.npz")))
-    w, tabs, nus, plan, args, lnPL = case(prec)
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", gold + ".npz")))
+    tatt = "tatt" in gold
+    w = workloads.make("real_3x2pt_tatt_small" if tatt else "real_3x2pt_small_nla")
+    tabs, nus = workloads.points(w, 2, seed=41)
+    plan = lib.Plan(w.cfg, w.src, w.lens, w.base, prec, max_batch=2, linear_table=True)
+    args = workloads.stack(tabs)
+    lnPL = workloads.stack_lin(tabs)
     sc = workloads.scale_cut_requests()
     ns = w.cfg.n_source
     pairs = [(i, j) for i in range(ns) for j in range(i, ns)]
@@ -96,16 +94,29 @@ def test_scuts_vs_reference_golden(gpu_lib, prec):
     assert np.all(dxi[:, :, :, :, 0] == 0.0)  # k = 1e-5: no source at chi = (l + 1/2) / k
     worst = {}
     for pt in range(2):
-        ref = g[f"dC_{pt}"]
-        got = np.array([dC[pt, 0, pairs.index(pq)] for pq in sc["pairs"]])
-        worst["dC"] = max(worst.get("dC", 0.0), float(np.max(np.abs(got - ref)) / np.abs(ref).max()))
+        for e, tag in ((0, ""), (1, "B")) if tatt else ((0, ""),):
+            ref = g[f"dC{tag}_{pt}"]
+            got = np.array([dC[pt, e, pairs.index(pq)] for pq in sc["pairs"]])
+            worst["dC" + tag] = max(worst.get("dC" + tag, 0.0), float(np.max(np.abs(got - ref)) / np.abs(ref).max()))
+            ref = g[f"rf{tag}_{pt}"]
+            got = np.array([rfc[pt, e, pairs.index(pq)] for pq in sc["pairs"]])
+            worst["rf_C" + tag] = max(worst.get("rf_C" + tag, 0.0), float(np.max(np.abs(got - ref))))
         ref = g[f"dlnxi_{pt}"]
+        # the divisor of each slot (xi- for the xi+ slot and vice versa)
+        xdiv = g[f"xi_{pt}"][::-1][:, :, :, None]
+        # dxi/dlnk undivided (well conditioned everywhere)
+        rd = ref * xdiv
+        scale = np.abs(rd).max(axis=-1, keepdims=True) + 1e-300
+        worst["dxi"] = max(worst.get("dxi", 0.0), float(np.max(np.abs(dxi[pt] - rd) / scale)))
+        # the ratio where the divisor is not at a zero crossing of xi(theta)
+        ok = np.abs(xdiv) > 1e-2 * np.abs(xdiv).max(axis=2, keepdims=True)
         scale = np.abs(ref).max(axis=-1, keepdims=True) + 1e-300
-        worst["dlnxi"] = max(worst.get("dlnxi", 0.0), float(np.max(np.abs(dln[pt] - ref) / scale)))
+        worst["dlnxi"] = max(worst.get("dlnxi", 0.0), float(np.max(np.where(ok, np.abs(dln[pt] - ref) / scale, 0.0))))
         ref = g[f"rfxi_{pt}"]
         worst["rf"] = max(worst.get("rf", 0.0), float(np.max(np.abs(rf[pt] - ref))))
-        ref = g[f"rf_{pt}"]
-        got = np.array([rfc[pt, 0, pairs.index(pq)] for pq in sc["pairs"]])
-        worst["rf_C"] = max(worst.get("rf_C", 0.0), float(np.max(np.abs(got - ref))))
-    print("scale cuts vs reference", worst)
-    assert worst["dC"] <= 1e-9 and worst["dlnxi"] <= 1e-8 and worst["rf"] <= 1e-8 and worst["rf_C"] <= 1e-9
+    print(gold, "scale cuts vs reference", worst)
+    # TATT: the FAST-PT IA rows are the GPU's own (2e-7 of the reference's,
+    # the rows' FP64 conditioning), so the TATT terms carry that error
+    tol = 1e-6 if tatt else 1e-9
+    for k, v in worst.items():
+        assert v <= (100 * tol if k in ("dxi", "dlnxi", "rf") else tol), (k, v, worst)

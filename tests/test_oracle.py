@@ -85,7 +85,8 @@ def _gold(name):
                                   "fastpt_ia", "real_3x2pt_tatt_small", "real_3x2pt_small_mag",
                                   "real_3x2pt_small_nla", "real_3x2pt_small_nlabin",
                                   "real_3x2pt_small_hdi", "real_3x2pt_small_lin",
-                                  "cmb_lensing_small", "cmb_lensing_tatt_small", "scale_cuts_small"])
+                                  "cmb_lensing_small", "cmb_lensing_tatt_small", "scale_cuts_small",
+                                  "scale_cuts_tatt_small"])
 def test_oracle_matches_reference_golden(oracle_built, case):
     """The restatement reproduces the reference's outputs (fixtures made by
     running the reference's own sources)."""
