@@ -78,6 +78,7 @@ def load(path: str = LIB_PATH):
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
     lib.cl2pt_like_create.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.POINTER(C.c_void_p)]
+    lib.cl2pt_plan_set_lens_photoz_grad.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
     lib.cl2pt_baryon_pcas.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Batch), C.c_int, C.c_int, _dp, C.c_int, _dp,
                                       _dp, C.c_void_p, C.c_void_p]
     lib.cl2pt_like_destroy.argtypes = [C.c_void_p]
@@ -211,6 +212,12 @@ class Plan:
         """CONTRACT_FP32 (CUDA cores) or a tensor-core form (CONTRACT_TF32X3,
         CONTRACT_BF16X3, CONTRACT_BF16X6) for the Legendre contraction."""
         check(load().cl2pt_plan_set_contraction(self.h, mode), "cl2pt_plan_set_contraction")
+
+    def set_lens_photoz_grad(self, on=True, h_dz=0.0, h_stretch=0.0):
+        """Lens photo-z shift / stretch gradients in the adjoint by central
+        differences of the forward (cl2pt_plan_set_lens_photoz_grad)."""
+        check(load().cl2pt_plan_set_lens_photoz_grad(self.h, int(bool(on)), float(h_dz), float(h_stretch)),
+              "cl2pt_plan_set_lens_photoz_grad")
 
     def set_d1p3(self, p_d1p3):
         """P_d1p3 on the plan's FAST-PT grid (1100 values, the reference's

@@ -642,4 +642,57 @@ void launch_vjp(const Params& P, const VJPParams& V, const NLParams& Q, const do
   hk(CL2PT_K_VJP, 0);
 }
 
+// ---- lens photo-z shift / stretch gradients by central differences of the
+// forward (cl2pt_plan_set_lens_photoz_grad).
+// out[i] = nu[i] with lens_dz[q] (par 0) or lens_stretch[q] (par 1) + d
+__global__ void k_nu_perturb(const cl2pt_nuisance* __restrict__ nu, int n, int q, int par, double d,
+                             cl2pt_nuisance* __restrict__ out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  cl2pt_nuisance v = nu[i];
+  if (par == 0) v.lens_dz[q] += d;
+  else v.lens_stretch[q] += d;
+  out[i] = v;
+}
+// nu_bar[i].(lens_dz | lens_stretch)[q] += inv2h sum_e cot[i][e] (dvp - dvm)[i][e]
+// (nu_bar on the device); one block per point
+__global__ void k_fd_dot(const double* __restrict__ cot, const double* __restrict__ dvp,
+                         const double* __restrict__ dvm, int nt, double inv2h, int q, int par,
+                         cl2pt_nuisance* __restrict__ nu_bar, double* __restrict__ g)
+{
+  __shared__ double red[8];
+  const int i = blockIdx.x;
+  const size_t o = (size_t)i * nt;
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < nt; e += blockDim.x) {
+    const double d = dvp[o + e] - dvm[o + e];
+    if (d != 0.0) acc += cot[o + e] * d;  // masked entries: no difference, any cotangent
+  }
+  for (int k = 16; k > 0; k >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, k);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    t *= inv2h;
+    if (g) g[i] = t;
+    if (nu_bar) {
+      if (par == 0) nu_bar[i].lens_dz[q] += t;
+      else nu_bar[i].lens_stretch[q] += t;
+    }
+  }
+}
+
+void launch_nu_perturb(const cl2pt_nuisance* nu, int n, int q, int par, double d, cl2pt_nuisance* out,
+                       cudaStream_t s)
+{
+  k_nu_perturb<<<(n + 127) / 128, 128, 0, s>>>(nu, n, q, par, d, out);
+}
+void launch_fd_dot(const double* cot, const double* dvp, const double* dvm, int n, int nt, double inv2h, int q,
+                   int par, cl2pt_nuisance* nu_bar, double* g, cudaStream_t s)
+{
+  k_fd_dot<<<n, 256, 0, s>>>(cot, dvp, dvm, nt, inv2h, q, par, nu_bar, g);
+}
+
 }  // namespace cl2pt

@@ -117,6 +117,12 @@ void launch_assemble_fourier(const Params& P, int nell, const double* ell, doubl
 // baryons): work holds n n_total + n nsq + 2 n^2 + n doubles; R [n][n_total]
 void launch_pca(const double* dv, int n, int n_total, const int* idx, int nsq, const float* cinv_hi,
                 const float* cinv_lo, double* work, double* R, cudaStream_t s);
+// lens photo-z gradients by central differences: perturbed nuisance
+// copies, and the cotangent-weighted difference of two data-vector batches
+void launch_nu_perturb(const cl2pt_nuisance* nu, int n, int q, int par, double d, cl2pt_nuisance* out,
+                       cudaStream_t s);
+void launch_fd_dot(const double* cot, const double* dvp, const double* dvm, int n, int nt, double inv2h, int q,
+                   int par, cl2pt_nuisance* nu_bar, double* g, cudaStream_t s);
 void launch_chi2(const double* dv, int n_total, int npt, const int* idx, const double* data, int nsq,
                  const float* cinv_hi, const float* cinv_lo, double* chi2, double* cot, cudaStream_t s);
 // ragged output of points w0 .. w0+B-1 from their full vectors (k_legendre.cu)

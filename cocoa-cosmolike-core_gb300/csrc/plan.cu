@@ -679,6 +679,15 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   CUDA_OK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   CUDA_OK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
   CUDA_OK(cudaMallocHost((void**)&p->h_inchk, sizeof(int)));
+  {
+    const int nw = (max_batch + W - 1) / W;
+    CUDA_OK(cudaStreamCreateWithFlags(&p->s_copy, cudaStreamNonBlocking));
+    CUDA_OK(cudaEventCreateWithFlags(&p->ev_copy0, cudaEventDisableTiming));
+    p->ev_in.resize(nw);
+    for (int w = 0; w < nw; w++) CUDA_OK(cudaEventCreateWithFlags(&p->ev_in[w], cudaEventDisableTiming));
+    TRY(dalloc(p, &p->d_wchk, nw));
+    CUDA_OK(cudaMallocHost((void**)&p->h_wchk, sizeof(int) * nw));
+  }
   P.err = p->d_err;
   TRY(dalloc(p, &p->d_ell_f, (size_t)std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &p->d_lfacf_f, 16 * (size_t)std::max(p->nnode_ss, p->nnode_g)));
@@ -898,6 +907,10 @@ extern "C" int cl2pt_plan_destroy(cl2pt_plan* p)
   for (void* d : p->dbufs) cudaFree(d);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   if (p->h_inchk) cudaFreeHost(p->h_inchk);
+  if (p->h_wchk) cudaFreeHost(p->h_wchk);
+  for (cudaEvent_t e : p->ev_in) cudaEventDestroy(e);
+  if (p->ev_copy0) cudaEventDestroy(p->ev_copy0);
+  if (p->s_copy) cudaStreamDestroy(p->s_copy);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->ev_join) cudaEventDestroy(p->ev_join);
   if (p->s2) cudaStreamDestroy(p->s2);
@@ -1936,6 +1949,99 @@ static int vjp_prepare(cl2pt_plan* p)
   return CL2PT_OK;
 }
 
+// Gradients with respect to the lens photo-z shifts and stretches, by
+// central differences of the forward (the plan's own pipeline) along each
+// of the 2 n_lens directions, contracted with the cotangent: the reference
+// moves each lens bin's Gauss-Legendre nodes with |dz| and the stretch
+// (amin_lens / amax_lens, redshift_spline.c:50-79), so its sums are not
+// smooth at dz = 0, where the central difference gives the symmetric
+// derivative.  cot: the cotangent (host or device as the batch), or null
+// for the one the chi^2 kernel left in p->d_vjp_cot.  Adds into nu_bar.
+static int lens_fd_grad(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm, const double* cot,
+                        cl2pt_nuisance* nu_bar, cudaStream_t s)
+{
+  if (!p->lens_fd || p->cfg.n_lens < 1) return CL2PT_OK;
+  const int n = b->n, nt = p->n_total, nl = p->cfg.n_lens;
+  const bool host = b->where == CL2PT_HOST;
+  const Params& T = p->P;
+  const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
+  cl2pt_batch db = *b;
+  db.where = CL2PT_DEVICE;
+  double *dvp = nullptr, *dvm = nullptr, *dcot = nullptr, *dpm = nullptr, *dg = nullptr;
+  int* dmask = nullptr;
+  cl2pt_nuisance* dnu = nullptr;
+  int st = CL2PT_OK;
+  auto fail = [&](cudaError_t e) { if (e != cudaSuccess && !st) st = CL2PT_ERR_CUDA; };
+  fail(cudaMalloc((void**)&dvp, sizeof(double) * (size_t)n * nt));
+  fail(cudaMalloc((void**)&dvm, sizeof(double) * (size_t)n * nt));
+  fail(cudaMalloc((void**)&dnu, sizeof(cl2pt_nuisance) * n));
+  fail(cudaMalloc((void**)&dg, sizeof(double) * n));
+  if (host && !st) {
+    // the inputs in the plan's staging buffers, as a device batch
+    fail(cudaMemcpyAsync(p->d_in_om, b->omega_m, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(p->d_in_h0, b->h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(p->d_in_chi, b->chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(p->d_in_G, b->G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
+    fail(cudaMemcpyAsync(p->d_in_lnP, b->lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (b->lnPL) {
+      if (!p->d_in_lnPL) st = CL2PT_ERR_ARG;
+      else fail(cudaMemcpyAsync(p->d_in_lnPL, b->lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    fail(cudaMemcpyAsync(p->d_in_nu, b->nuisance, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
+    db.omega_m = p->d_in_om; db.h0 = p->d_in_h0; db.chi = p->d_in_chi; db.G = p->d_in_G; db.lnP = p->d_in_lnP;
+    db.lnPL = b->lnPL ? p->d_in_lnPL : nullptr;
+    db.nuisance = p->d_in_nu;
+    if (cot) {
+      fail(cudaMalloc((void**)&dcot, sizeof(double) * (size_t)n * nt));
+      if (!st) fail(cudaMemcpyAsync(dcot, cot, sizeof(double) * (size_t)n * nt, cudaMemcpyHostToDevice, s));
+    }
+    if (mask) {
+      fail(cudaMalloc((void**)&dmask, sizeof(int) * nt));
+      if (!st) fail(cudaMemcpyAsync(dmask, mask, sizeof(int) * nt, cudaMemcpyHostToDevice, s));
+    }
+    if (pm) {
+      fail(cudaMalloc((void**)&dpm, sizeof(double) * (size_t)n * nl));
+      if (!st) fail(cudaMemcpyAsync(dpm, pm, sizeof(double) * (size_t)n * nl, cudaMemcpyHostToDevice, s));
+    }
+  }
+  const double* ucot = cot ? (host ? dcot : cot) : p->d_vjp_cot;
+  const int* umask = host ? dmask : mask;
+  const double* upm = host ? dpm : pm;
+  std::vector<double> hg(host ? n : 0);
+  for (int q = 0; q < nl && !st; q++)
+    for (int par = 0; par < 2 && !st; par++) {
+      const double h = p->lens_fd_h[par];
+      for (int sg = 0; sg < 2 && !st; sg++) {
+        cl2pt::launch_nu_perturb(db.nuisance, n, q, par, sg ? -h : h, dnu, s);
+        cl2pt_batch d2 = db;
+        d2.nuisance = dnu;
+        if (int e = internal_eval(p, &d2, umask, upm, sg ? dvm : dvp, s, nullptr)) st = e;
+      }
+      if (st) break;
+      cl2pt::launch_fd_dot(ucot, dvp, dvm, n, nt, 0.5 / h, q, par, host ? nullptr : nu_bar, dg, s);
+      fail(cudaGetLastError());
+      if (host) {
+        fail(cudaMemcpyAsync(hg.data(), dg, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        fail(cudaStreamSynchronize(s));
+        for (int i = 0; i < n && !st; i++) (par ? nu_bar[i].lens_stretch[q] : nu_bar[i].lens_dz[q]) += hg[i];
+      }
+    }
+  fail(cudaStreamSynchronize(s));
+  for (void* x : {(void*)dvp, (void*)dvm, (void*)dcot, (void*)dpm, (void*)dg, (void*)dmask, (void*)dnu})
+    cudaFree(x);
+  return st;
+}
+
+extern "C" int cl2pt_plan_set_lens_photoz_grad(cl2pt_plan* p, int on, double h_dz, double h_stretch)
+{
+  if (!p || !std::isfinite(h_dz) || !std::isfinite(h_stretch)) return CL2PT_ERR_ARG;
+  const bool f64 = p->P.prec == CL2PT_PREC_FP64;
+  p->lens_fd = on != 0;
+  p->lens_fd_h[0] = h_dz > 0 ? h_dz : (f64 ? 1e-4 : 2e-3);
+  p->lens_fd_h[1] = h_stretch > 0 ? h_stretch : (f64 ? 1e-4 : 2e-3);
+  return CL2PT_OK;
+}
+
 extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,
                               const double* cot, double* dv, double* lnP_bar, double* lnPL_bar,
                               cl2pt_nuisance* nu_bar, void* stream)
@@ -1952,7 +2058,9 @@ extern "C" int cl2pt_vjp_real(cl2pt_plan* p, const cl2pt_batch* b, const int* ma
   vr.lnp_bar = lnP_bar;
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
-  return internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+  st = internal_eval(p, b, mask, pm, dv, (cudaStream_t)stream, nullptr, &vr);
+  if (st) return st;
+  return lens_fd_grad(p, b, mask, pm, cot, nu_bar, (cudaStream_t)stream);
 }
 
 extern "C" int cl2pt_like_create(cl2pt_plan* p, const int* mask, const double* data, const double* inv_cov,
@@ -2122,6 +2230,9 @@ extern "C" int cl2pt_loglike_real(cl2pt_plan* p, const cl2pt_like* L, const cl2p
     for (int i = 0; i < n; i++)
       if (!(chi2[i] >= 0.0)) return CL2PT_ERR_DEVICE;  // the reference rejects chi2 < 0
   }
+  // the lens photo-z part of the gradient, with the cotangent -C^-1 Delta
+  // that the chi^2 kernel left on the device
+  if (grad) return lens_fd_grad(p, b, mask, pm, nullptr, nu_bar, s);
   return CL2PT_OK;
 }
 
@@ -2466,30 +2577,57 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
   const int* dmask = nullptr;
   const double* dpm = nullptr;
   double* ddv;
-  if (b->where == CL2PT_HOST) {
-    CUDA_OK(cudaMemcpyAsync(p->d_in_om, b->omega_m, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_h0, b->h0, n * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_chi, b->chi, n * nchi * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_G, b->G, n * nG * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_lnP, b->lnP, n * nP * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (b->lnPL && p->d_in_lnPL)
-      CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL, b->lnPL, n * nPL * sizeof(double), cudaMemcpyHostToDevice, s));
-    CUDA_OK(cudaMemcpyAsync(p->d_in_nu, b->nuisance, n * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice, s));
-    om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP;
-    lnPL = (b->lnPL && p->d_in_lnPL) ? p->d_in_lnPL : p->d_in_lnP;
-    nu = p->d_in_nu;
+  const bool staged = b->where == CL2PT_HOST;
+  // on every return: the copy stream has finished reading the caller's
+  // host arrays
+  struct CopyDrain {
+    cudaStream_t c;
+    bool on;
+    ~CopyDrain()
     {
-      // the tables' finiteness check (check_batch) on the staged copies:
-      // one pass at device bandwidth, one flag, before any compute
-      CUDA_OK(cudaMemsetAsync(p->d_inchk, 0, sizeof(int), s));
-      cl2pt::launch_check_finite(chi, (size_t)n * nchi, p->d_inchk, s);
-      cl2pt::launch_check_finite(G, (size_t)n * nG, p->d_inchk, s);
-      cl2pt::launch_check_finite(lnP, (size_t)n * nP, p->d_inchk, s);
-      if (b->lnPL && p->d_in_lnPL) cl2pt::launch_check_finite(lnPL, (size_t)n * nPL, p->d_inchk, s);
-      CUDA_OK(cudaMemcpyAsync(p->h_inchk, p->d_inchk, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CUDA_OK(cudaStreamSynchronize(s));
-      if (*p->h_inchk) return CL2PT_ERR_ARG;
+      if (on) cudaStreamSynchronize(c);
     }
+  } drain{p->s_copy, staged};
+  if (staged) {
+    // per wave, on the copy stream: the wave's inputs, their finiteness
+    // check (check_batch's, one pass at device bandwidth, one flag per
+    // wave) and an event; wave w's kernels wait for it, and the host reads
+    // its flag before launching them, so no kernel reads a non-finite
+    // table while the copies of later waves overlap earlier waves' compute
+    const int W = p->wave;
+    const bool lin = b->lnPL && p->d_in_lnPL;
+    CUDA_OK(cudaEventRecord(p->ev_copy0, s));
+    CUDA_OK(cudaStreamWaitEvent(p->s_copy, p->ev_copy0, 0));
+    CUDA_OK(cudaMemsetAsync(p->d_wchk, 0, sizeof(int) * p->ev_in.size(), p->s_copy));
+    for (int w0 = 0, w = 0; w0 < n; w0 += W, w++) {
+      const size_t m = (size_t)std::min(W, n - w0);
+      cudaStream_t c = p->s_copy;
+      CUDA_OK(cudaMemcpyAsync(p->d_in_om + w0, b->omega_m + w0, m * sizeof(double), cudaMemcpyHostToDevice, c));
+      CUDA_OK(cudaMemcpyAsync(p->d_in_h0 + w0, b->h0 + w0, m * sizeof(double), cudaMemcpyHostToDevice, c));
+      CUDA_OK(cudaMemcpyAsync(p->d_in_chi + w0 * nchi, b->chi + w0 * nchi, m * nchi * sizeof(double),
+                              cudaMemcpyHostToDevice, c));
+      CUDA_OK(cudaMemcpyAsync(p->d_in_G + w0 * nG, b->G + w0 * nG, m * nG * sizeof(double), cudaMemcpyHostToDevice,
+                              c));
+      CUDA_OK(cudaMemcpyAsync(p->d_in_lnP + w0 * nP, b->lnP + w0 * nP, m * nP * sizeof(double),
+                              cudaMemcpyHostToDevice, c));
+      if (lin)
+        CUDA_OK(cudaMemcpyAsync(p->d_in_lnPL + w0 * nPL, b->lnPL + w0 * nPL, m * nPL * sizeof(double),
+                                cudaMemcpyHostToDevice, c));
+      CUDA_OK(cudaMemcpyAsync(p->d_in_nu + w0, b->nuisance + w0, m * sizeof(cl2pt_nuisance), cudaMemcpyHostToDevice,
+                              c));
+      cl2pt::launch_check_finite(p->d_in_chi + w0 * nchi, m * nchi, p->d_wchk + w, c);
+      cl2pt::launch_check_finite(p->d_in_G + w0 * nG, m * nG, p->d_wchk + w, c);
+      cl2pt::launch_check_finite(p->d_in_lnP + w0 * nP, m * nP, p->d_wchk + w, c);
+      if (lin) cl2pt::launch_check_finite(p->d_in_lnPL + w0 * nPL, m * nPL, p->d_wchk + w, c);
+      CUDA_OK(cudaMemcpyAsync(p->h_wchk + w, p->d_wchk + w, sizeof(int), cudaMemcpyDeviceToHost, c));
+      CUDA_OK(cudaEventRecord(p->ev_in[w], c));
+    }
+    om = p->d_in_om; h0 = p->d_in_h0; chi = p->d_in_chi; G = p->d_in_G; lnP = p->d_in_lnP;
+    lnPL = lin ? p->d_in_lnPL : p->d_in_lnP;
+    nu = p->d_in_nu;
+    // wave 0's check before anything else is queued
+    CUDA_OK(cudaEventSynchronize(p->ev_in[0]));
+    if (p->h_wchk[0]) return CL2PT_ERR_ARG;
     if (mask) {
       CUDA_OK(cudaMemcpyAsync(d_mask_stage, mask, n_total * sizeof(int), cudaMemcpyHostToDevice, s));
       dmask = d_mask_stage;
@@ -2713,6 +2851,16 @@ static int internal_eval(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, c
     CUDA_OK(cudaStreamSynchronize(s));
   }
   for (int w0 = 0; w0 < n; w0 += p->wave) {
+    if (staged) {
+      // this wave's staged inputs: finite (read on the host) and in place
+      const int w = w0 / p->wave;
+      CUDA_OK(cudaEventSynchronize(p->ev_in[w]));
+      if (p->h_wchk[w]) {
+        CUDA_OK(cudaStreamSynchronize(s));
+        return CL2PT_ERR_ARG;
+      }
+      CUDA_OK(cudaStreamWaitEvent(s, p->ev_in[w], 0));
+    }
     Params P = T;
     P.B = std::min(p->wave, n - w0);
     P.omega_m = om + w0;

@@ -126,12 +126,23 @@ struct cl2pt_plan {
   cl2pt_nuisance* d_vjp_nu = nullptr;  // [max_batch]
   // stage timing
   bool timing = false;
+  // lens photo-z gradients by central differences (cl2pt_plan_set_lens_photoz_grad)
+  bool lens_fd = false;
+  double lens_fd_h[2] = {0.0, 0.0};  // steps in lens_dz, lens_stretch
   std::vector<cudaEvent_t> ev_pool;
   struct Rec { int stage; cudaEvent_t a, b; int launches; cudaStream_t s; };
   // second stream for work that overlaps the main one, and its fork/join
   // events
   cudaStream_t s2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // host batches: each wave's inputs are copied and checked on s_copy
+  // while the waves before it compute; ev_in[w] marks wave w ready, with
+  // its non-finite flag in d_wchk[w] / h_wchk[w] (pinned)
+  cudaStream_t s_copy = nullptr;
+  cudaEvent_t ev_copy0 = nullptr;
+  std::vector<cudaEvent_t> ev_in;
+  int* d_wchk = nullptr;
+  int* h_wchk = nullptr;
   std::vector<Rec> recs;
   size_t ev_used = 0;
   int last_batch = 0;

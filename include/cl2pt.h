@@ -191,6 +191,16 @@ int cl2pt_graph_destroy(cl2pt_graph* graph);
  * at its forward value.  Supported: NLA and TATT intrinsic alignments, bias
  * model 0 (with or without one-loop terms), the nonlinear run mode; other
  * plans return CL2PT_ERR_UNSUPPORTED. */
+/* Gradients with respect to the lens photo-z shifts (lens_dz) and
+ * stretches (lens_stretch) in cl2pt_vjp_real and cl2pt_loglike_real's
+ * gradient: off by default (those entries of nu_bar stay 0).  When on, each
+ * of the 2 n_lens directions is differentiated by a central difference of
+ * the plan's own forward (steps h_dz, h_stretch; <= 0: 1e-4 in the FP64
+ * plan, 2e-3 in the mixed one), contracted with the cotangent: 4 n_lens
+ * extra forward evaluations of the batch.  The reference moves each lens
+ * bin's quadrature nodes with |dz| (redshift_spline.c:50-79), so at dz = 0
+ * this is the symmetric derivative. */
+int cl2pt_plan_set_lens_photoz_grad(cl2pt_plan* plan, int on, double h_dz, double h_stretch);
 int cl2pt_vjp_real(cl2pt_plan* plan, const cl2pt_batch* batch, const int* mask,
                    const double* pm, const double* cot, double* dv, double* lnP_bar,
                    double* lnPL_bar, cl2pt_nuisance* nu_bar, void* stream);

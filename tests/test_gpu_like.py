@@ -63,3 +63,25 @@ def test_chi2_and_gradient(gpu_lib):
             an = nbar[pt, flat_index(field, i, j)]
             assert abs(an - fd) <= 1e-5 * max(abs(fd), 1e-9 * abs(f[0]) / h), (field, i, j, an, fd)
     like.close()
+
+
+@pytest.mark.gpu
+def test_loglike_lens_photoz_gradient(gpu_lib):
+    """With the lens photo-z gradients on, the likelihood's gradient carries
+    them too, equal to the adjoint's with the cotangent -C^-1 (dv - data)."""
+    w, tabs, nus, plan = setup_case(abi.IA_REDSHIFT_EVOLUTION, npts=2, seed=72, name="real_3x2pt_small")
+    tabs = workloads.one_table(tabs)
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    rng = np.random.default_rng(4)
+    dv_ref = plan.eval_real(om[:1], h0[:1], chi[:1], G[:1], lnP[:1], nus[:1])[0]
+    mask, data, inv = make_like(plan, dv_ref, rng)
+    like = plan.likelihood(data, inv, mask)
+    plan.set_lens_photoz_grad(True)
+    c2, lbar, nbar = plan.loglike_real(like, om, h0, chi, G, lnP, nus, grad=True)
+    dv = plan.eval_real(om, h0, chi, G, lnP, nus, mask=mask)
+    d = np.where(mask == 1, dv - data, 0.0)
+    cot = -(d @ inv) * (mask == 1)
+    _, _, n2 = plan.vjp_real(om, h0, chi, G, lnP, nus, cot, mask=mask)
+    idx = [flat_index(f, q) for f in ("lens_dz", "lens_stretch") for q in range(w.cfg.n_lens)]
+    assert np.all(nbar[:, idx] != 0.0)
+    np.testing.assert_allclose(nbar[:, idx], n2[:, idx], rtol=1e-6, atol=1e-9 * np.abs(n2[:, idx]).max())
