@@ -1958,10 +1958,10 @@ static int vjp_prepare(cl2pt_plan* p)
 // derivative.  cot: the cotangent (host or device as the batch), or null
 // for the one the chi^2 kernel left in p->d_vjp_cot.  Adds into nu_bar.
 static int lens_fd_grad(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm, const double* cot,
-                        cl2pt_nuisance* nu_bar, cudaStream_t s)
+                        cl2pt_nuisance* nu_bar, cudaStream_t s, const FourierReq* fr = nullptr, int nt_f = 0)
 {
   if (!p->lens_fd || p->cfg.n_lens < 1) return CL2PT_OK;
-  const int n = b->n, nt = p->n_total, nl = p->cfg.n_lens;
+  const int n = b->n, nt = fr ? nt_f : p->n_total, nl = p->cfg.n_lens;
   const bool host = b->where == CL2PT_HOST;
   const Params& T = p->P;
   const size_t nchi = T.chi_nz, nG = T.G_nz, nP = (size_t)T.pk_nk * T.pk_nz, nPL = (size_t)T.pkl_nk * T.pkl_nz;
@@ -2015,7 +2015,7 @@ static int lens_fd_grad(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, co
         cl2pt::launch_nu_perturb(db.nuisance, n, q, par, sg ? -h : h, dnu, s);
         cl2pt_batch d2 = db;
         d2.nuisance = dnu;
-        if (int e = internal_eval(p, &d2, umask, upm, sg ? dvm : dvp, s, nullptr)) st = e;
+        if (int e = internal_eval(p, &d2, umask, upm, sg ? dvm : dvp, s, fr)) st = e;
       }
       if (st) break;
       cl2pt::launch_fd_dot(ucot, dvp, dvm, n, nt, 0.5 / h, q, par, host ? nullptr : nu_bar, dg, s);
@@ -2313,7 +2313,9 @@ extern "C" int cl2pt_vjp_fourier(cl2pt_plan* p, const cl2pt_batch* b, int nell, 
   vr.lnp_bar = lnP_bar;
   vr.lnpl_bar = lnPL_bar;
   vr.nu_bar = nu_bar;
-  return internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr, &vr);
+  st = internal_eval(p, b, mask, nullptr, dv, (cudaStream_t)stream, &fr, &vr);
+  if (st) return st;
+  return lens_fd_grad(p, b, mask, nullptr, cot, nu_bar, (cudaStream_t)stream, &fr, n_total);
 }
 
 extern "C" int cl2pt_jacobian_real(cl2pt_plan* p, const cl2pt_batch* b, const int* mask, const double* pm,

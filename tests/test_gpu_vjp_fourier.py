@@ -122,3 +122,36 @@ def test_vjp_fourier_tatt(gpu_lib):
     set_bk(nus, w, 63)
     worst = check(w, tabs, nus, p64, plan, ell, GRAD_REL, separate_linear=True, mag=True)
     print("Fourier TATT max rel gradient error", worst)
+
+
+@pytest.mark.gpu
+def test_vjp_fourier_lens_photoz(gpu_lib):
+    """Lens photo-z shift and stretch gradients of the Fourier vector
+    (cl2pt_plan_set_lens_photoz_grad) against central differences of the
+    FP64 forward with the same step."""
+    w, tabs, nus, p64, plan, ell = case("fourier_serving_small", lib.PREC_FP64, seed=67)
+    rng = np.random.default_rng(9)
+    for q in range(w.cfg.n_lens):
+        nus[0].lens_stretch[q] = float(rng.uniform(0.9, 1.1))
+    om, h0, chi, G, lnP = workloads.stack(tabs)
+    lm = 0.7 * w.ell[-1]
+    dv0 = p64.eval_fourier(om, h0, chi, G, lnP, nus, ell, lmax_shear=lm)
+    v = rng.normal(size=dv0.shape)
+    plan.set_lens_photoz_grad(True, 1e-4, 1e-4)
+    nbar = plan.vjp_fourier(om, h0, chi, G, lnP, nus, ell, v, lmax_shear=lm)[2]
+    worst = 0.0
+    for pt in range(len(tabs)):
+        sl = slice(pt, pt + 1)
+        for field in ("lens_dz", "lens_stretch"):
+            for q in range(w.cfg.n_lens):
+                fs = []
+                for s in (1, -1):
+                    nu = clone(nus[pt])
+                    getattr(nu, field)[q] += s * 1e-4
+                    fs.append(float(v[pt] @ p64.eval_fourier(om[sl], h0[sl], chi[sl], G[sl], lnP[sl], [nu], ell,
+                                                             lmax_shear=lm)[0]))
+                fd = (fs[0] - fs[1]) / 2e-4
+                an = nbar[pt, flat_index(field, q)]
+                worst = max(worst, abs(an - fd) / abs(fd))
+                assert abs(an - fd) <= 1e-9 * abs(fd), (pt, field, q, an, fd)
+    print("Fourier lens photo-z gradient max rel err vs the forward's differences", worst)
