@@ -619,7 +619,9 @@ def main():
         plan.eval_real(h["om"], h["h0"], h["chi"], h["G"], h["lnP"], data["nus"], out=dv_host)
     torch.cuda.synchronize()
     barrier()
-    e2e_steps = max(2, args.steps // 2)
+    # as many calls as the device-timed steps: a wall-clock number over a
+    # few calls is sensitive to other work on the host
+    e2e_steps = max(5, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         plan.eval_real(h["om"], h["h0"], h["chi"], h["G"], h["lnP"], data["nus"], out=dv_host)
