@@ -78,6 +78,10 @@ struct Params {
   // and a float copy of the nodes (search)
   const double *src_b, *src_d;
   const float* src_zcf;
+  // mixed plan, k_gsrc_f: the source nodes' FP32 tails (src_zcf the heads)
+  // and per-interval (y, b, c, d) of every source row as floats
+  const float* src_zcl;
+  const float4* src_cf;
   double src_zmin_all, src_zmax_all, lens_zmax_all;
   double lens_zmin[CL2PT_MAXB], lens_zmax[CL2PT_MAXB], zmean_lens[CL2PT_MAXB];
   // quadrature rules on [-1, 1]
@@ -142,6 +146,7 @@ struct Params {
   // workspace (device), strided by point
   double* gsrc;             // [B][ns][n_a]
   double* gfine;            // [B][Na][4] source fine grid of g_tomo: z, chi, 1/a^2, 1/chi
+  float4* gfine_f;          // mixed plan: [B][Na] (z head, z tail, 1/a^2, 1/chi) as floats
   double* glens;            // [B][nl][n_a]
   double* node;             // [B][NODE_FIELDS][node_stride]
   int* node_j;              // [B][node_stride]

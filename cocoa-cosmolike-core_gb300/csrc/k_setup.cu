@@ -183,8 +183,13 @@ __global__ void __launch_bounds__(GT_NT) k_gfine(Params P, int Na, double amin, 
   const double a = amin + i * da;
   const double c = chi_all_d(P.chi_z, X, P.chi_nz, a).chi;
   double2* f = (double2*)(P.gfine + ((size_t)pt * Na + i) * 4);
-  f[0] = make_double2(1.0 / a - 1.0, c);
-  f[1] = make_double2(1.0 / (a * a), 1.0 / c);
+  const double z = 1.0 / a - 1.0, ia2 = 1.0 / (a * a), ic = 1.0 / c;
+  f[0] = make_double2(z, c);
+  f[1] = make_double2(ia2, ic);
+  if (P.gfine_f) {
+    const float zh = (float)z;
+    P.gfine_f[(size_t)pt * Na + i] = make_float4(zh, (float)(z - (double)zh), (float)ia2, (float)ic);
+  }
 }
 
 // spline cell of the source n(z) nodes: the largest i <= n-2 with
@@ -205,7 +210,171 @@ __device__ __forceinline__ int src_cell(const Params& P, double v)
   return lo;
 }
 
+// mixed plan: k_gsrc's sums in FP32 -- z - dz and the in-cell offset from
+// two-float (head, tail) pairs, the spline from float coefficients, the
+// trapezoid increments summed as two-float (TwoSum) values through the
+// thread, the block scan and the chunk carries -- and the output P - chi Q
+// formed in FP64 at the n_a table points only.  The FP64 pipe (1/64 of the
+// FP32 rate on GB300) otherwise bounds the kernel.
+struct TF {
+  float h, l;
+};
+__device__ __forceinline__ TF tf_add(TF a, TF b)
+{
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float e = (a.h - (s - bb)) + (b.h - bb);
+  const float lo = e + a.l + b.l;
+  const float h = s + lo;
+  return {h, lo - (h - s)};
+}
+__device__ __forceinline__ TF tf_shfl_up(TF v, int o)
+{
+  return {__shfl_up_sync(0xffffffffu, v.h, o), __shfl_up_sync(0xffffffffu, v.l, o)};
+}
+// inclusive block scan of two-float values (NT threads)
+template <int NT>
+__device__ TF block_scan_tf(TF v, TF* sh)
+{
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const TF y = tf_shfl_up(v, o);
+    if (lane >= o) v = tf_add(v, y);
+  }
+  if (lane == 31) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    TF s = lane < NT / 32 ? sh[lane] : TF{0.0f, 0.0f};
+    for (int o = 1; o < NT / 32; o <<= 1) {
+      const TF y = tf_shfl_up(s, o);
+      if (lane >= o) s = tf_add(s, y);
+    }
+    if (lane < NT / 32) sh[lane] = s;
+  }
+  __syncthreads();
+  const TF r = w > 0 ? tf_add(v, sh[w - 1]) : v;
+  __syncthreads();
+  return r;
+}
+// the source spline cell of z = zh + zl (src_cell's answer): a search on
+// the node heads, fixed up by comparing two-float values
+__device__ __forceinline__ bool tf_gt(float ah, float al, float bh, float bl)
+{
+  return ah > bh || (ah == bh && al > bl);
+}
+__device__ __forceinline__ int src_cell_f(const Params& P, float zh, float zl)
+{
+  const float* xh = P.src_zcf;
+  const float* xl = P.src_zcl;
+  const int n = P.src_nz;
+  int lo = 0, hi = n - 1;
+  while (hi > lo + 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xh[mid] > zh) hi = mid; else lo = mid;
+  }
+  while (lo > 0 && tf_gt(xh[lo], xl[lo], zh, zl)) lo--;
+  while (lo < n - 2 && !tf_gt(xh[lo + 1], xl[lo + 1], zh, zl)) lo++;
+  return lo;
+}
+
 constexpr int GS_PPT = 4;
+// DZ: the tangent in the bin's photo-z shift (as k_gsrc<true>), to dz_out
+template <bool DZ>
+__global__ void __launch_bounds__(GT_NT) k_gsrc_f(Params P, double* dz_out, int Na, double da)
+{
+  const int pt = blockIdx.x, b = blockIdx.y;
+  const cl2pt_nuisance& nu = P.nu[pt];
+  const int x = 25 * (1 + abs(P.hdi));
+  double* tab = DZ ? dz_out + ((size_t)pt * P.ns + b) * P.n_a : P.gsrc + ((size_t)pt * P.ns + b) * P.n_a;
+  const float4* F = P.gfine_f + (size_t)pt * Na;
+  const double2* Fd = (const double2*)(P.gfine + (size_t)pt * Na * 4);
+  const double dz = nu.src_dz[b];
+  const float dzh = (float)dz, dzl = (float)(dz - (double)dzh);
+  const float4* cf = P.src_cf + (size_t)(b + 1) * P.src_nz;
+  const float z0h = P.src_zcf[0], z0l = P.src_zcl[0];
+  const float z1h = P.src_zcf[P.src_nz - 1], z1l = P.src_zcl[P.src_nz - 1];
+  const float hda = (float)(0.5 * da);
+  __shared__ TF sh[32];
+  __shared__ float lastP[GT_NT], lastQ[GT_NT];
+  __shared__ TF carry[2];
+  __shared__ float carryf[2];
+  if (threadIdx.x == 0) tab[0] = 0.0;
+  TF runP = {0.0f, 0.0f}, runQ = {0.0f, 0.0f};
+  float prevP = 0.0f, prevQ = 0.0f;
+  for (int base = 0; base < Na; base += GT_NT * GS_PPT) {
+    const int i0 = base + GS_PPT * threadIdx.x;
+    float fP[GS_PPT], fQ[GS_PPT];
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      fP[k] = fQ[k] = 0.0f;
+      if (i < Na) {
+        const float4 f = F[i];  // (z head, z tail, 1/a^2, 1/chi)
+        // zz = z - dz as a two-float value
+        const float sh0 = f.x - dzh;
+        const float bb = sh0 - f.x;
+        const float e = (f.x - (sh0 - bb)) + (-dzh - bb) + (f.y - dzl);
+        const float zh = sh0 + e, zl = e - (zh - sh0);
+        float n = 0.0f;
+        if (!(tf_gt(z0h, z0l, zh, zl) || tf_gt(zh, zl, z1h, z1l))) {
+          const int j = src_cell_f(P, zh, zl);
+          const float t = (zh - P.src_zcf[j]) + (zl - P.src_zcl[j]);
+          const float4 c = cf[j];  // y, b, c, d
+          n = DZ ? -fmaf(t, fmaf(3.0f * t, c.w, 2.0f * c.z), c.y) : fmaf(t, fmaf(t, fmaf(t, c.w, c.z), c.y), c.x);
+        }
+        fP[k] = n * f.z;
+        fQ[k] = fP[k] * f.w;
+      }
+    }
+    lastP[threadIdx.x] = fP[GS_PPT - 1];
+    lastQ[threadIdx.x] = fQ[GS_PPT - 1];
+    __syncthreads();
+    float pP = threadIdx.x ? lastP[threadIdx.x - 1] : prevP;
+    float pQ = threadIdx.x ? lastQ[threadIdx.x - 1] : prevQ;
+    TF sP[GS_PPT], sQ[GS_PPT], aP = {0.0f, 0.0f}, aQ = {0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      if (i >= 1 && i < Na) {
+        aP = tf_add(aP, TF{hda * (pP + fP[k]), 0.0f});
+        aQ = tf_add(aQ, TF{hda * (pQ + fQ[k]), 0.0f});
+      }
+      sP[k] = aP;
+      sQ[k] = aQ;
+      pP = fP[k];
+      pQ = fQ[k];
+    }
+    // exclusive prefix of the thread sums plus the carry of earlier chunks
+    TF eP = block_scan_tf<GT_NT>(aP, sh);
+    eP = tf_add(eP, TF{-aP.h, -aP.l});
+    eP = tf_add(eP, runP);
+    TF eQ = block_scan_tf<GT_NT>(aQ, sh);
+    eQ = tf_add(eQ, TF{-aQ.h, -aQ.l});
+    eQ = tf_add(eQ, runQ);
+#pragma unroll
+    for (int k = 0; k < GS_PPT; k++) {
+      const int i = i0 + k;
+      if (i >= 1 && i < Na && (i % x) == 0) {
+        const TF P1 = tf_add(eP, sP[k]), Q1 = tf_add(eQ, sQ[k]);
+        const double Pd = (double)P1.h + (double)P1.l, Qd = (double)Q1.h + (double)Q1.l;
+        tab[i / x] = Pd - Fd[2 * i].y * Qd;
+      }
+    }
+    if (threadIdx.x == GT_NT - 1) {
+      carry[0] = tf_add(eP, aP);
+      carry[1] = tf_add(eQ, aQ);
+      carryf[0] = fP[GS_PPT - 1];
+      carryf[1] = fQ[GS_PPT - 1];
+    }
+    __syncthreads();
+    runP = carry[0];
+    runQ = carry[1];
+    prevP = carryf[0];
+    prevQ = carryf[1];
+    __syncthreads();
+  }
+}
+
 template <bool DZ>
 __global__ void __launch_bounds__(GT_NT) k_gsrc(Params P, double* dz_out, int Na, double da)
 {
@@ -539,7 +708,8 @@ void launch_setup(const Params& P, cudaStream_t s, int* launches, const Hook& hk
   src_fine_grid(P, &Na, &amin, &da);
   hk(CL2PT_K_GTAB, 1);
   k_gfine<<<dim3((Na + GT_NT - 1) / GT_NT, P.B), GT_NT, 0, s>>>(P, Na, amin, da);
-  k_gsrc<false><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, nullptr, Na, da);
+  if (P.gfine_f) k_gsrc_f<false><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, nullptr, Na, da);
+  else k_gsrc<false><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, nullptr, Na, da);
   if (P.nl > 0) k_gtab<false><<<dim3(P.B, P.nl), GT_NT, 0, s>>>(P, nullptr, P.ns);
   hk(CL2PT_K_GTAB, 0);
   *launches += 2;
@@ -1191,7 +1361,8 @@ void launch_gtab_dz(const Params& P, double* dz_out, cudaStream_t s)
   int Na;
   double amin, da;
   src_fine_grid(P, &Na, &amin, &da);
-  k_gsrc<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out, Na, da);
+  if (P.gfine_f) k_gsrc_f<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out, Na, da);
+  else k_gsrc<true><<<dim3(P.B, P.ns), GT_NT, 0, s>>>(P, dz_out, Na, da);
 }
 
 }  // namespace cl2pt

@@ -525,10 +525,16 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
         sb[(size_t)r * n + i] = (y[i + 1] - y[i]) / h - h * (c[i + 1] + 2.0 * c[i]) / 3.0;
         sdd[(size_t)r * n + i] = (c[i + 1] - c[i]) / (3.0 * h);
       }
-    std::vector<float> zf(x.begin(), x.end());
+    std::vector<float> zf(x.begin(), x.end()), zl(n);
+    for (int i = 0; i < n; i++) zl[i] = (float)(x[i] - (double)zf[i]);
+    std::vector<float4> cf(p->src.y.size());
+    for (size_t e = 0; e < cf.size(); e++)
+      cf[e] = make_float4((float)p->src.y[e], (float)sb[e], (float)p->src.c[e], (float)sdd[e]);
     TRY(dupload(p, &p->d_src_b, sb.data(), sb.size()));
     TRY(dupload(p, &p->d_src_d, sdd.data(), sdd.size()));
     TRY(dupload(p, &p->d_src_zcf, zf.data(), zf.size()));
+    TRY(dupload(p, &p->d_src_zcl, zl.data(), zl.size()));
+    TRY(dupload(p, &p->d_src_cf, cf.data(), cf.size()));
   }
   TRY(dupload(p, &p->d_gl_ss_x, glx.data(), glx.size()));
   TRY(dupload(p, &p->d_gl_ss_w, glw.data(), glw.size()));
@@ -637,6 +643,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
   P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
   P.src_b = p->d_src_b; P.src_d = p->d_src_d; P.src_zcf = p->d_src_zcf;
+  P.src_zcl = p->d_src_zcl; P.src_cf = p->d_src_cf;
   P.facf_ss = p->d_lfacf_ss;
   P.facf_g = p->d_lfacf_g;
   P.facf_gi = p->d_lfacf_g + 8 * (size_t)p->nnode_g;
@@ -704,6 +711,8 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   }
   TRY(dalloc(p, &p->d_tab_gg_f, (size_t)W * nl * std::max(p->nnode_ss, p->nnode_g)));
   TRY(dalloc(p, &P.gfine, (size_t)W * 4 * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
+  if (precision != CL2PT_PREC_FP64)
+    TRY(dalloc(p, &P.gfine_f, (size_t)W * (25 * (1 + std::abs(cfg->high_def_integration)) * (cfg->n_a - 1) + 1)));
   if (precision != CL2PT_PREC_FP64) {
     TRY(dalloc(p, &P.lnP2, (size_t)W * 2 * P.pk_nk * P.pk_nz));
     TRY(dalloc(p, &P.lnPL2, (size_t)W * 2 * P.pkl_nk * P.pkl_nz));

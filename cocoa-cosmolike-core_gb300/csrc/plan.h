@@ -44,6 +44,8 @@ struct cl2pt_plan {
   double *d_lens_zc = nullptr, *d_lens_y = nullptr, *d_lens_c = nullptr;
   double *d_src_b = nullptr, *d_src_d = nullptr;  // source spline b, d per interval
   float* d_src_zcf = nullptr;                      // float copy of the source nodes
+  float* d_src_zcl = nullptr;                      // their FP32 tails
+  float4* d_src_cf = nullptr;                      // (y, b, c, d) per interval as floats
   double *d_gl_ss_x = nullptr, *d_gl_ss_w = nullptr, *d_gl_gg_x = nullptr, *d_gl_gg_w = nullptr;
   double *d_ell_ss = nullptr, *d_ell_g = nullptr;       // C_l node multipoles
   double* d_filt_xi = nullptr;   // [2][ntheta][nnode_ss]   G+, G- folded
