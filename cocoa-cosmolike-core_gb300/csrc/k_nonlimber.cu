@@ -737,9 +737,20 @@ __device__ __forceinline__ int slice_cell(const float* __restrict__ plk, int nk,
 // SMS: the CTA's spectra (3 kernels) and Gamma-recurrence state (3 kernels
 // x 2 multipoles) live in shared memory instead of global memory (L2): the
 // mixed plan when they fit beside the rest at two CTAs per SM.
+// The mixed plan's forward without shared-memory state (the default) runs
+// 128-thread CTAs, five per SM: its shared layout drops the slice adjoint,
+// the per-cell slope (formed from the neighbouring cells' head and tail)
+// and the log10 k offsets (linear in the sample index), and the compiler
+// keeps it within 96 registers.
 template <typename T, bool ADJ, bool SMS>
-__global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar,
-                                                      double* __restrict__ lnpl_bar, cl2pt_nuisance* nu_bar)
+constexpr bool nl_lean_launch() { return sizeof(T) == sizeof(float) && !ADJ && !SMS; }
+constexpr int NL_LEAN_NT = 128, NL_LEAN_CTAS = 5;
+
+template <typename T, bool ADJ, bool SMS>
+__global__ void __launch_bounds__(nl_lean_launch<T, ADJ, SMS>() ? NL_LEAN_NT : NL_NT,
+                                  nl_lean_launch<T, ADJ, SMS>() ? NL_LEAN_CTAS : 2)
+    k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar, double* __restrict__ lnpl_bar,
+              cl2pt_nuisance* nu_bar)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // (point, bin) of this CTA from the longest-first dispatch order
@@ -771,12 +782,15 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   T* M01 = nullptr;
   T* plk = ADJ ? G01 + nchi : xs + nchi;
   constexpr bool F32 = sizeof(T) == sizeof(float);
-  float* lxkf = (float*)(plk + P.pkl_nk);
-  float* pcf = lxkf + nchi;  // per cell (hi, lo, 1/width)
-  float* psf = pcf + 3 * P.pkl_nk;  // slope of the slice per cell
-  float* pbarf = psf + P.pkl_nk;
+  // LEAN (mixed-plan forward): no lxkf (linear in i), psf (from pcf) or
+  // pbarf (adjoint only)
+  constexpr bool LEAN = F32 && !ADJ;
+  float* lxkf = LEAN ? nullptr : (float*)(plk + P.pkl_nk);
+  float* pcf = LEAN ? (float*)(plk + P.pkl_nk) : lxkf + nchi;  // per cell (hi, lo, 1/width)
+  float* psf = LEAN ? nullptr : pcf + 3 * P.pkl_nk;  // slope of the slice per cell
+  float* pbarf = LEAN ? nullptr : psf + P.pkl_nk;
   // mixed plan: (rc / x_i)^3 and the slice-cell table (nl_slice_lut)
-  float* rx3f = pbarf + P.pkl_nk;
+  float* rx3f = LEAN ? pcf + 3 * P.pkl_nk : pbarf + P.pkl_nk;
   unsigned short* lut = (unsigned short*)(rx3f + nchi);
   double* psl = F32 ? (double*)fb : (double*)(plk + P.pkl_nk);
   double* plkd = psl + P.pkl_nk;
@@ -823,7 +837,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         pcf[3 * i + 1] = (float)(psl[i] - (double)h);
         // the cell width of the FP32 axis, so dx = 1 at the upper edge
         pcf[3 * i + 2] = (i + 1 < P.pkl_nk) ? 1.0f / ((float)P.pkl_lk[i + 1] - (float)P.pkl_lk[i]) : 0.0f;
-        psf[i] = (i + 1 < P.pkl_nk) ? (float)(psl[i + 1] - psl[i]) : 0.0f;
+        if (!LEAN) psf[i] = (i + 1 < P.pkl_nk) ? (float)(psl[i + 1] - psl[i]) : 0.0f;
       }
     }
   }
@@ -831,10 +845,14 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
   // (y = (l+1)/x[nchi-1-i])
   for (int i = tid; i < nchi; i += nlt) {
     const double xr = geo.x0 * exp(geo.dlnchi * (nchi - 1 - i));
-    if (F32) lxkf[i] = (float)log10(rc / (xr * CL2PT_COVERH0));
-    else lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
+    if (!F32) lxk[i] = log10(rc / (xr * CL2PT_COVERH0));
+    else if (!LEAN) lxkf[i] = (float)log10(rc / (xr * CL2PT_COVERH0));
     xs[i] = (T)xr;
   }
+  // LEAN: log10(rc / (x coverH0)) at the reversed index = lx0 + i lx1
+  const double lx1d = geo.dlnchi * 0.434294481903251827651;  // dlnchi log10(e)
+  const float lx0f = (float)(log10(rc / (geo.x0 * CL2PT_COVERH0)) - (nchi - 1) * lx1d);
+  const float lx1f = (float)lx1d;
   const double lrc = log10(rc / CL2PT_COVERH0);
   const T rct = (T)rc;
   const int nlut = nl_lut_size(P.pkl_nk);
@@ -1104,7 +1122,8 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
         const T kp0 = (T)(k + 1), kp1 = (T)(k2 + 1);
         const T cub0 = kp0 * kp0 * kp0, cub1 = kp1 * kp1 * kp1;  // exact for k < 255
         T tp0 = 0, tp1 = 0;  // mixed plan: per-thread FP32 partial sums
-        for (int i = tid; i < nchi; i += nlt) {
+        float fiv = ftid;    // i as a float, counted (no conversion per entry)
+        for (int i = tid; i < nchi; i += nlt, fiv += fnlt) {
           T rx3;
           if constexpr (F32) {
             rx3 = rx3f[i];
@@ -1115,7 +1134,7 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
           for (int h = 0; h < (two ? 2 : 1); h++) {
             // p_lin(k, 1) (cosmo3D.c:306-358) on the z = 0 slice
             const double lkv = F32 ? 0.0 : (h ? lk1 : lk0) + lxk[i];
-            const T lkt = F32 ? (T)((h ? lk1f : lk0f) + lxkf[i]) : (T)lkv;
+            const T lkt = F32 ? (T)((h ? lk1f : lk0f) + (LEAN ? fmaf(fiv, lx1f, lx0f) : lxkf[i])) : (T)lkv;
             int lo = 0;
             if constexpr (F32) {
               lo = slice_cell((const float*)plk, P.pkl_nk, lut, lscale, lumax, lkt);
@@ -1138,7 +1157,12 @@ __global__ void __launch_bounds__(NL_NT, 2) k_nl_loop(Params P, NLParams Q, cons
               // in-cell offset and exponent in FP32 from the per-cell split
               // (hi, lo, slope) of the slice
               const float dx = (lkt - plk[lo]) * pcf[3 * lo + 2];
-              const float del = pcf[3 * lo + 1] + dx * psf[lo];
+              // slope of the cell: (hi, lo) differences of its ends (LEAN)
+              const float slope = LEAN ? (lo + 1 < P.pkl_nk ? (pcf[3 * lo + 3] - pcf[3 * lo]) +
+                                                                    (pcf[3 * lo + 4] - pcf[3 * lo + 1])
+                                                              : 0.0f)
+                                       : psf[lo];
+              const float del = pcf[3 * lo + 1] + dx * slope;
               const float pl = __expf(pcf[3 * lo]) * __expf(del) * lc3;
               const float v = F * F * k3 * pl;
               if (h) tp1 += v; else tp0 += v;
@@ -1248,6 +1272,8 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj, bool sm
   // mixed plan: the slice adjoint's place (always reserved), (rc/x)^3 and
   // the slice-cell table
   if (f32) sm += sizeof(float) * ((size_t)P.pkl_nk + P.nl_nchi) + sizeof(unsigned short) * nl_lut_size(P.pkl_nk);
+  // the forward's lean layout: no slice adjoint, slope or log10 k offsets
+  if (f32 && !adj) sm -= sizeof(float) * (2 * (size_t)P.pkl_nk + P.nl_nchi);
   if (adj) sm += sizeof(T) * 2 * (size_t)P.nl_nchi + (f32 ? 0 : sizeof(double) * (size_t)P.pkl_nk);
   if (sms) sm += 2 * sizeof(T) * 9 * (size_t)Q.hstride + 16;
   return sm;
@@ -1314,7 +1340,8 @@ static void launch_nl_loop_t(const Params& P, const NLParams& Q, cudaStream_t s)
     k_nl_loop<T, false, true><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
   } else {
     cudaFuncSetAttribute(k_nl_loop<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-    k_nl_loop<T, false, false><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+    const int nt3 = nl_lean_launch<T, false, false>() ? NL_LEAN_NT : nl_loop_threads(sm3);
+    k_nl_loop<T, false, false><<<dim3(P.B, P.nl), nt3, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
   }
 }
 
