@@ -683,6 +683,10 @@ __device__ __forceinline__ int bsearch_from(const T* __restrict__ x, int n, T v,
 }
 
 constexpr int LTG = 256;  // multipoles per CTA of the gg kernel
+// the mixed plan's node pass: 512 multipoles (threads) per CTA, two CTAs
+// per SM (32 warps; three 256-thread CTAs, 24 warps, are what its shared
+// tables allow)
+constexpr int LTG_NODES_F32 = 512;
 static_assert(9 * PCH >= 2 * LTG, "k_limber_gg reduces its halves in the node-data space");
 
 // chi_all's slopes of cell i (cosmo3D.c:60-72), formed in FP64: 'up' and
@@ -804,8 +808,8 @@ __global__ void __launch_bounds__(128) k_gg_nodes(Params P, const double* __rest
 
 // NH = 2 only in the mixed plan (the FP64 node walk is not split)
 template <typename T, int NH>
-__global__ void __launch_bounds__(NH * LTG) k_limber_gg(Params P, const double* __restrict__ ell,
-                                                        int mode)
+__global__ void __launch_bounds__(sizeof(T) == sizeof(float) ? LTG_NODES_F32 : NH * LTG)
+    k_limber_gg(Params P, const double* __restrict__ ell, int mode)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
@@ -1217,9 +1221,10 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
       k_gg_nodes<<<dim3(P.B, P.nl), 128, 0, s>>>(P, ell_g);
       (*launches)++;
     }
-    dim3 g(P.B, (P.nnode_g + LTG - 1) / LTG, P.nl);
+    const int ltn = f32 ? LTG_NODES_F32 : LTG;
+    dim3 g(P.B, (P.nnode_g + ltn - 1) / ltn, P.nl);
     hk(CL2PT_K_LIMBER_GG, 1);
-    k_limber_gg<T, 1><<<g, LTG, sm, s>>>(P, ell_g, 0);
+    k_limber_gg<T, 1><<<g, ltn, sm, s>>>(P, ell_g, 0);
     hk(CL2PT_K_LIMBER_GG, 0);
     (*launches)++;
     if (!P.adopt_limber_gg) {
