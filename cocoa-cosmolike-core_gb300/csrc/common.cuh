@@ -213,6 +213,53 @@ __device__ __forceinline__ float f64_to_f32_bits(double v)
   return __uint_as_float(sgn | f);
 }
 
+// The FP32 head (nearest, ties to even) and tail (the rest, rounded to
+// nearest) of an FP64 value by integer arithmetic on its bits: the same
+// pair as h = (float)v, t = (float)(v - (double)h) for finite values whose
+// parts are FP32 normals (below that both flush to zero), without FP64 or
+// conversion instructions (1/64 of the FP32 rate on GB300).
+__device__ __forceinline__ float2 split_f64_bits(double v)
+{
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
+  const uint32_t sgn = hi & 0x80000000u;
+  const uint32_t ex = (hi >> 20) & 0x7FFu;
+  const uint32_t man = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  // head: the 29 dropped mantissa bits rounded to nearest even
+  const bool up = ((lo >> 28) & 1u) && ((lo & 0x0FFFFFFFu) != 0u || (man & 1u));
+  uint32_t f = ((ex - 896u) << 23) + man + (up ? 1u : 0u);
+  f = (ex <= 896u) ? 0u : f;
+  f = (ex >= 1151u) ? 0x7F800000u : f;
+  const float h = __uint_as_float(sgn | f);
+  // tail: the dropped bits (less 2^29 when the head rounded up) in units of
+  // 2^(ex - 1075), rounded to 24 bits (ties to even)
+  const int32_t d = (int32_t)(lo & 0x1FFFFFFFu);
+  const int32_t r = up ? d - (1 << 29) : d;
+  const uint32_t ar = (uint32_t)(r < 0 ? -r : r);
+  if (ar == 0u || ex <= 896u || ex >= 1151u) return make_float2(h, 0.0f);
+  const uint32_t tsgn = r < 0 ? (sgn ^ 0x80000000u) : sgn;
+  const int nb = 32 - __clz(ar);
+  uint32_t m;
+  int e2 = (int)ex - 1075;
+  if (nb <= 24) {
+    m = ar << (24 - nb);
+    e2 -= 24 - nb;
+  } else {
+    const int sh = nb - 24;
+    m = ar >> sh;
+    const uint32_t rem = ar & ((1u << sh) - 1u), half = 1u << (sh - 1);
+    if (rem > half || (rem == half && (m & 1u))) m++;
+    e2 += sh;
+    if (m == (1u << 24)) {
+      m >>= 1;
+      e2++;
+    }
+  }
+  const int biased = e2 + 23 + 127;
+  if (biased <= 0) return make_float2(h, 0.0f);
+  return make_float2(h, __uint_as_float(tsgn | ((uint32_t)biased << 23) | (m & 0x7FFFFFu)));
+}
+
 // FP64 value of an FP32 one by integer arithmetic (exact, as the hardware
 // conversion).  GB300 issues FP64 instructions, conversions included, at
 // 1/64 of the FP32 rate, so FP32 kernels that write FP64 results convert

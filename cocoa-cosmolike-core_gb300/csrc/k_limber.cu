@@ -105,11 +105,8 @@ __device__ __forceinline__ Axis<T> load_axis(const double* __restrict__ lk, int 
 __global__ void k_split_table(const double* __restrict__ src, float2* __restrict__ dst, size_t n)
 {
   if ((reinterpret_cast<uintptr_t>(src) & 15) != 0) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      const double v = src[i];
-      const float h = (float)v;
-      dst[i] = make_float2(h, (float)(v - (double)h));
-    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+      dst[i] = split_f64_bits(src[i]);
     return;
   }
   const size_t n2 = n / 2;
@@ -117,14 +114,10 @@ __global__ void k_split_table(const double* __restrict__ src, float2* __restrict
   float4* d4 = (float4*)dst;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
     const double2 v = __ldcs(s2 + i);
-    const float h0 = (float)v.x, h1 = (float)v.y;
-    __stcs(d4 + i, make_float4(h0, (float)(v.x - (double)h0), h1, (float)(v.y - (double)h1)));
+    const float2 a = split_f64_bits(v.x), b = split_f64_bits(v.y);
+    __stcs(d4 + i, make_float4(a.x, a.y, b.x, b.y));
   }
-  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    const double v = src[n - 1];
-    const float h = (float)v;
-    dst[n - 1] = make_float2(h, (float)(v - (double)h));
-  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) dst[n - 1] = split_f64_bits(src[n - 1]);
 }
 
 void launch_split_tables(const Params& P, cudaStream_t s, int* launches)
