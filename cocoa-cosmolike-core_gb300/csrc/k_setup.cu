@@ -277,6 +277,22 @@ __device__ __forceinline__ int src_cell_f(const Params& P, float zh, float zl)
   return lo;
 }
 
+// nz_source_d in FP32 for the mixed plan: z - dz as a two-float value, the
+// float spline of the bin (0 outside the nodes' range)
+__device__ __forceinline__ float nz_source_tf(const Params& P, float zh, float zl, int b, float dzh, float dzl)
+{
+  const float sh0 = zh - dzh;
+  const float bb = sh0 - zh;
+  const float e = (zh - (sh0 - bb)) + (-dzh - bb) + (zl - dzl);
+  const float h = sh0 + e, l = e - (h - sh0);
+  const int n = P.src_nz;
+  if (tf_gt(P.src_zcf[0], P.src_zcl[0], h, l) || tf_gt(h, l, P.src_zcf[n - 1], P.src_zcl[n - 1])) return 0.0f;
+  const int j = src_cell_f(P, h, l);
+  const float t = (h - P.src_zcf[j]) + (l - P.src_zcl[j]);
+  const float4 c = P.src_cf[(size_t)(b + 1) * n + j];
+  return fmaf(t, fmaf(t, fmaf(t, c.w, c.z), c.y), c.x);
+}
+
 constexpr int GS_PPT = 4;
 // DZ: the tangent in the bin's photo-z shift (as k_gsrc<true>), to dz_out
 template <bool DZ>
@@ -621,12 +637,23 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
     nj[off + p] = jz;
     const double pre = 1.5 * om * fK / a;
     const double D2 = D * D;
+    // the source weights' per-node parts: C1 of the redshift-evolution mode
+    // is the same for every bin; the mixed plan evaluates n(z) in FP32
+    const bool ia_bin = P.ia_mode == CL2PT_IA_REDSHIFT_BINNING;
+    const double c1_all = ia_bin ? 0.0 : ia_a1(P, nu, om, a, D, 0);
+    const bool f32w = P.gfine_f != nullptr;
+    const float2 zs = f32w ? split_f64_bits(z) : make_float2(0.0f, 0.0f);
+    auto ws_of = [&](int s) -> double {
+      if (!f32w) return nz_source_d(P, z, s, nu.src_dz[s]) * H;
+      const float2 dzs = split_f64_bits(nu.src_dz[s]);
+      return f32_to_f64_int(nz_source_tf(P, zs.x, zs.y, s, dzs.x, dzs.y)) * H;
+    };
     if (set == 0) {
       double* w = P.wss + (size_t)pt * P.ns * P.n_ss;
       for (int s = 0; s < P.ns; s++) {
         const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
-        const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
-        const double C1 = ia_a1(P, nu, om, a, D, s);
+        const double WS = ws_of(s);
+        const double C1 = ia_bin ? ia_a1(P, nu, om, a, D, s) : c1_all;
         w[s * P.n_ss + p] = WK - WS * C1;
         if (P.tatt) {
           const size_t o = ((size_t)pt * P.ns + s) * P.n_ss + p;
@@ -652,8 +679,8 @@ __global__ void __launch_bounds__(ND_NT) k_nodes(Params P)
       double* wx = P.wgs_x + b0 * P.ns * P.n_ss;
       for (int s = 0; s < P.ns; s++) {
         const double WK = pre * g_lookup(gsrc + s * P.n_a, P.n_a, amin_src, a, true);
-        const double WS = nz_source_d(P, z, s, nu.src_dz[s]) * H;
-        const double C1 = ia_a1(P, nu, om, a, D, s);
+        const double WS = ws_of(s);
+        const double C1 = ia_bin ? ia_a1(P, nu, om, a, D, s) : c1_all;
         wx[s * P.n_ss + p] = WK - WS * C1;
         const size_t o = (b0 * P.ns + s) * P.n_ss + p;
         if (P.tatt || P.one_loop) P.wgs_k[o] = WK;
