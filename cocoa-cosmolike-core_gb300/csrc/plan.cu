@@ -1425,6 +1425,7 @@ static int scut_run(cl2pt_plan* p, const cl2pt_batch* b, int what, int nk, const
   int launches = 0;
   for (int w0 = 0; w0 < n && !st; w0 += W) {
     Params P = T;
+    P.gfine_f = nullptr;  // the FP64 set-up: lens efficiencies and node weights as the FP64 plan
     P.B = std::min(W, n - w0);
     P.omega_m = om + w0;
     P.h0 = h0 + w0;
@@ -1583,6 +1584,7 @@ static int xi_scut_run(cl2pt_plan* p, const cl2pt_batch* b, int nlnk, double kmi
   int launches = 0;
   for (int w0 = 0; w0 < n && !st; w0 += W) {
     Params P = T;
+    P.gfine_f = nullptr;  // the FP64 set-up: lens efficiencies and node weights as the FP64 plan
     P.B = std::min(W, n - w0);
     P.omega_m = d.om + w0;
     P.h0 = d.h0 + w0;
@@ -1698,6 +1700,7 @@ static int cmb_run(cl2pt_plan* p, const cl2pt_batch* b, bool real, int nell, con
   int launches = 0;
   for (int w0 = 0; w0 < n && !st; w0 += W) {
     Params P = T;
+    P.gfine_f = nullptr;  // the FP64 set-up: lens efficiencies and node weights as the FP64 plan
     P.B = std::min(W, n - w0);
     P.omega_m = d.om + w0;
     P.h0 = d.h0 + w0;
