@@ -498,14 +498,17 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
 }
 
 // ---------------------------------------------------------------- gs
-template <typename T>
-__global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __restrict__ ell)
+// LTK multipoles (threads) per CTA, PCHK quadrature nodes per shared chunk:
+// the mixed plan runs 256 x 32 (four CTAs, 32 warps, per SM in the same
+// shared memory as 128 x 64), the FP64 plan 128 x 64
+template <typename T, int LTK, int PCHK>
+__global__ void __launch_bounds__(LTK) k_limber_gs(Params P, const double* __restrict__ ell)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
   const int q = blockIdx.z;
   const int tid = threadIdx.x;
-  const int L = blockIdx.y * LT + tid;
+  const int L = blockIdx.y * LTK + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   // pairs of this lens bin
   __shared__ int kk[CL2PT_MAXB], ss_[CL2PT_MAXB];
@@ -528,26 +531,26 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   int* nj;
   float *lkt = nullptr, *lki = nullptr;
   if constexpr (F32) {
-    // node records, the FP32 axis (head, tail, 1/width), P [PCH][LT],
-    // weights [2][MAXB][PCH]
+    // node records, the FP32 axis (head, tail, 1/width), P [PCHK][LTK],
+    // weights [2][MAXB][PCHK]
     nlc = (double*)smem_raw;
     sd = nlc;
-    ndy = (T*)(nlc + PCH);
-    nj = (int*)(ndy + PCH);
-    lk = (T*)(nj + PCH);
+    ndy = (T*)(nlc + PCHK);
+    nj = (int*)(ndy + PCHK);
+    lk = (T*)(nj + PCHK);
     lkt = (float*)lk + pd.nk;
     lki = lkt + pd.nk;
     Ps = (T*)(lki + pd.nk);
-    X = Ps + PCH * LT;
+    X = Ps + PCHK * LTK;
   } else {
     sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
     si = sd + pd.nk;
     nlc = si + pd.nk;
-    lk = (T*)(nlc + PCH);
+    lk = (T*)(nlc + PCHK);
     Ps = lk + pd.nk;
-    X = Ps + PCH * LT;                  // [nterm][npair][PCH]
-    ndy = X + (size_t)3 * CL2PT_MAXB * PCH;
-    nj = (int*)(ndy + PCH);
+    X = Ps + PCHK * LTK;                  // [nterm][npair][PCHK]
+    ndy = X + (size_t)3 * CL2PT_MAXB * PCHK;
+    nj = (int*)(ndy + PCHK);
   }
   Axis<T> ax{};
   AxisF axf{};
@@ -581,32 +584,32 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
   }
   double* out = P.tab_gs + (size_t)pt * P.pgs * P.nnode_g;
   int hk = -1;  // mixed plan: the k cell of the previous node
-  for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
-    const int np = min(PCH, P.n_ss - p0);
+  for (int p0 = 0; p0 < P.n_ss; p0 += PCHK) {
+    const int np = min(PCHK, P.n_ss - p0);
     __syncthreads();
     if constexpr (F32) {
       // the node records and weights of k_ls_nodes
       const float* rec = P.lsn + ((size_t)pt * (1 + P.nl) + 1 + q) * 4 * P.n_ss + p0;
-      for (int p = tid; p < np; p += LT) {
+      for (int p = tid; p < np; p += LTK) {
         nlc2[p] = make_float2(rec[p], rec[P.n_ss + p]);
         ndy[p] = rec[2 * P.n_ss + p];
         nj[p] = __float_as_int(rec[3 * P.n_ss + p]);
       }
       const float* xs = P.gsx + b0 * 3 * CL2PT_MAXB * P.n_ss + p0;
-      for (int idx = tid; idx < nterm * np_ * np; idx += LT) {
+      for (int idx = tid; idx < nterm * np_ * np; idx += LTK) {
         const int t = idx / (np_ * np);
         const int r = idx - t * np_ * np;
         const int m = r / np, p = r - m * np;
-        X[(t * CL2PT_MAXB + m) * PCH + p] = xs[(size_t)(t * CL2PT_MAXB + m) * P.n_ss + p];
+        X[(t * CL2PT_MAXB + m) * PCHK + p] = xs[(size_t)(t * CL2PT_MAXB + m) * P.n_ss + p];
       }
     }
-    for (int p = tid; p < np && !F32; p += LT) {
+    for (int p = tid; p < np && !F32; p += LTK) {
       const double v = log10(node[(size_t)NF_FK * P.node_stride + off + p0 + p] * CL2PT_COVERH0);
       nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + off + p0 + p];
       nj[p] = nodej[off + p0 + p];
     }
-    for (int idx = tid; idx < nterm * np_ * np && !F32; idx += LT) {
+    for (int idx = tid; idx < nterm * np_ * np && !F32; idx += LTK) {
       const int t = idx / (np_ * np);
       const int r = idx - t * np_ * np;
       const int m = r / np, p = r - m * np;
@@ -614,13 +617,13 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
       const double dch = node[(size_t)NF_DCHIDA * P.node_stride + off + p0 + p];
       const double wt = node[(size_t)NF_WT * P.node_stride + off + p0 + p];
       if (t == 2) {
-        X[(t * CL2PT_MAXB + m) * PCH + p] = (T)(wt * dch / (fK * fK) *
+        X[(t * CL2PT_MAXB + m) * PCHK + p] = (T)(wt * dch / (fK * fK) *
                                                 P.wgs_k[(b0 * P.ns + ss_[m]) * P.n_ss + p0 + p] *
                                                 P.wgs_bk[b0 * P.n_ss + p0 + p]);
         continue;
       }
       const double lens = t == 0 ? wl[p0 + p] : wm[p0 + p];
-      X[(t * CL2PT_MAXB + m) * PCH + p] =
+      X[(t * CL2PT_MAXB + m) * PCHK + p] =
           (T)(wt * dch / (fK * fK) * wx[ss_[m] * P.n_ss + p0 + p] * lens);
     }
     __syncthreads();
@@ -629,24 +632,24 @@ __global__ void __launch_bounds__(LT) k_limber_gs(Params P, const double* __rest
       for (int p = 0; p < np; p++) {
         float uh, ul;
         split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
-        Ps[p * LT + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
+        Ps[p * LTK + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
       }
     } else {
       const double llp = log10(lp);
       for (int p = 0; p < np; p++)
-        Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+        Ps[p * LTK + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     }
     for (int m = 0; m < np_; m++) {
       T a0 = 0, a1 = 0, a2 = 0;
-      const T* x0 = X + (0 * CL2PT_MAXB + m) * PCH;
-      for (int p = 0; p < np; p++) a0 += x0[p] * Ps[p * LT + tid];
+      const T* x0 = X + (0 * CL2PT_MAXB + m) * PCHK;
+      for (int p = 0; p < np; p++) a0 += x0[p] * Ps[p * LTK + tid];
       if (use_m) {
-        const T* x1 = X + (1 * CL2PT_MAXB + m) * PCH;
-        for (int p = 0; p < np; p++) a1 += x1[p] * Ps[p * LT + tid];
+        const T* x1 = X + (1 * CL2PT_MAXB + m) * PCHK;
+        for (int p = 0; p < np; p++) a1 += x1[p] * Ps[p * LTK + tid];
       }
       if (use_k) {
-        const T* x2 = X + (2 * CL2PT_MAXB + m) * PCH;
-        for (int p = 0; p < np; p++) a2 += x2[p] * Ps[p * LT + tid];
+        const T* x2 = X + (2 * CL2PT_MAXB + m) * PCHK;
+        for (int p = 0; p < np; p++) a2 += x2[p] * Ps[p * LTK + tid];
       }
       const T r = pref2 * (a0 + pref * a1 + lp2 * a2);
       double v;
@@ -1194,14 +1197,16 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   if ((P.probes & CL2PT_PROBE_GAMMAT) && P.pgs > 0) {
-    const size_t sm = f32 ? sm_f32 + 4 * (size_t)3 * CL2PT_MAXB * PCH
+    constexpr int GS_LT = f32 ? 256 : LT, GS_PCH = f32 ? 32 : PCH;
+    const size_t sm = f32 ? sizeof(double) * GS_PCH + 8 * GS_PCH + 12 * (size_t)P.pk_nk + 4 * GS_PCH * GS_LT + 16 +
+                                4 * (size_t)3 * CL2PT_MAXB * GS_PCH
                           : sizeof(double) * (2 * P.pk_nk + PCH) +
                                 sizeof(T) * (P.pk_nk + PCH * LT + (size_t)3 * CL2PT_MAXB * PCH + PCH) +
                                 sizeof(int) * PCH + 64;
-    cudaFuncSetAttribute(k_limber_gs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    dim3 g(P.B, (P.nnode_g + LT - 1) / LT, P.nl);
+    cudaFuncSetAttribute(k_limber_gs<T, GS_LT, GS_PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    dim3 g(P.B, (P.nnode_g + GS_LT - 1) / GS_LT, P.nl);
     hk(CL2PT_K_LIMBER_GS, 1);
-    k_limber_gs<T><<<g, LT, sm, s>>>(P, ell_g);
+    k_limber_gs<T, GS_LT, GS_PCH><<<g, GS_LT, sm, s>>>(P, ell_g);
     hk(CL2PT_K_LIMBER_GS, 0);
     (*launches)++;
   }
