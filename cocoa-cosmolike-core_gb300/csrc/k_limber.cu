@@ -363,13 +363,15 @@ __global__ void __launch_bounds__(128) k_ls_nodes(Params P)
 }
 
 // ---------------------------------------------------------------- ss
-template <typename T>
-__global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __restrict__ ell)
+// LTK multipoles (threads) per CTA, PCHK nodes per shared chunk (as the gs
+// kernel: 256 x 32 in the mixed plan, 128 x 64 in the FP64 plan)
+template <typename T, int LTK, int PCHK>
+__global__ void __launch_bounds__(LTK) k_limber_ss(Params P, const double* __restrict__ ell)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int pt = blockIdx.x;
   const int tid = threadIdx.x;
-  const int L = blockIdx.y * LT + tid;
+  const int L = blockIdx.y * LTK + tid;
   const PdeltaTable pd = pdelta_table(P, pt, P.linear_pk != 0);
   constexpr bool F32 = sizeof(T) == sizeof(float);
   const int PP = (P.pss + 7) & ~7;  // mixed plan: pairs padded to 8 (weights pair-minor)
@@ -379,25 +381,25 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   float *lkt = nullptr, *lki = nullptr;
   if constexpr (F32) {
     // node log10 chi (head, tail), z offsets and cells, the FP32 axis
-    // (head, tail, 1/width), P~ [PCH][LT], weights [PCH][PP]
+    // (head, tail, 1/width), P~ [PCHK][LTK], weights [PCHK][PP]
     nlc = (double*)smem_raw;
     sd = nlc;
-    ndy = (T*)(nlc + PCH);
-    nj = (int*)(ndy + PCH);
-    lk = (T*)(nj + PCH);
+    ndy = (T*)(nlc + PCHK);
+    nj = (int*)(ndy + PCHK);
+    lk = (T*)(nj + PCHK);
     lkt = (float*)lk + pd.nk;
     lki = lkt + pd.nk;
     Ps = (T*)(((uintptr_t)(lki + pd.nk) + 15) & ~(uintptr_t)15);  // 16-byte rows for the float4 reads
-    X = Ps + PCH * LT;
+    X = Ps + PCHK * LTK;
   } else {
     sd = (double*)smem_raw;     // FP64 axis, inverse widths, node log10 chi
     si = sd + pd.nk;
     nlc = si + pd.nk;
-    lk = (T*)(nlc + PCH);
+    lk = (T*)(nlc + PCHK);
     Ps = lk + pd.nk;
-    X = Ps + PCH * LT;
-    ndy = X + (size_t)P.pss * PCH;
-    nj = (int*)(ndy + PCH);
+    X = Ps + PCHK * LTK;
+    ndy = X + (size_t)P.pss * PCHK;
+    nj = (int*)(ndy + PCHK);
   }
   Axis<T> ax{};
   AxisF axf{};
@@ -423,32 +425,32 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
   }
   double* out = P.tab_ss + (size_t)pt * P.pss * P.nnode_ss;
   int hk = -1;  // mixed plan: the k cell of the previous node
-  for (int p0 = 0; p0 < P.n_ss; p0 += PCH) {
-    const int np = min(PCH, P.n_ss - p0);
+  for (int p0 = 0; p0 < P.n_ss; p0 += PCHK) {
+    const int np = min(PCHK, P.n_ss - p0);
     __syncthreads();
     if constexpr (F32) {
       // the node records and weights of k_ls_nodes
       const float* rec = P.lsn + (size_t)pt * (1 + P.nl) * 4 * P.n_ss + p0;
-      for (int p = tid; p < np; p += LT) {
+      for (int p = tid; p < np; p += LTK) {
         nlc2[p] = make_float2(rec[p], rec[P.n_ss + p]);
         ndy[p] = rec[2 * P.n_ss + p];
         nj[p] = __float_as_int(rec[3 * P.n_ss + p]);
       }
       const float* xs = P.ssx + ((size_t)pt * P.n_ss + p0) * PP;
-      for (int i = tid; i < np * PP; i += LT) X[i] = xs[i];
+      for (int i = tid; i < np * PP; i += LTK) X[i] = xs[i];
     }
-    for (int p = tid; p < np && !F32; p += LT) {
+    for (int p = tid; p < np && !F32; p += LTK) {
       const double v = log10(node[(size_t)NF_FK * P.node_stride + p0 + p] * CL2PT_COVERH0);
       nlc[p] = v;
       ndy[p] = (T)node[(size_t)NF_DYZ * P.node_stride + p0 + p];
       nj[p] = nodej[p0 + p];
     }
-    for (int idx = tid; idx < P.pss * np && !F32; idx += LT) {
+    for (int idx = tid; idx < P.pss * np && !F32; idx += LTK) {
       const int pair = idx / np, p = idx - pair * np;
       const double fK = node[(size_t)NF_FK * P.node_stride + p0 + p];
       const double dch = node[(size_t)NF_DCHIDA * P.node_stride + p0 + p];
       const double wt = node[(size_t)NF_WT * P.node_stride + p0 + p];
-      X[pair * PCH + p] = (T)(wt * dch / (fK * fK) * w[P.z1[pair] * P.n_ss + p0 + p] *
+      X[pair * PCHK + p] = (T)(wt * dch / (fK * fK) * w[P.z1[pair] * P.n_ss + p0 + p] *
                               w[P.z2[pair] * P.n_ss + p0 + p]);
     }
     __syncthreads();
@@ -457,13 +459,13 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
       for (int p = 0; p < np; p++) {
         float uh, ul;
         split_sub(llf.x, llf.y, nlc2[p].x, nlc2[p].y, uh, ul);
-        Ps[p * LT + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
+        Ps[p * LTK + tid] = pk_eval_fh(axf, pd.tab2, pd.nz, uh, ul, nj[p], ndy[p], hk);
       }
       // the pair contraction, 8 pairs per pass held in registers
       for (int g = 0; g < PP; g += 8) {
         float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (int p = 0; p < np; p++) {
-          const float ps = Ps[p * LT + tid];
+          const float ps = Ps[p * LTK + tid];
           const float4 xa = *(const float4*)&X[p * PP + g], xb = *(const float4*)&X[p * PP + g + 4];
           a[0] += xa.x * ps;
           a[1] += xa.y * ps;
@@ -484,12 +486,12 @@ __global__ void __launch_bounds__(LT) k_limber_ss(Params P, const double* __rest
     } else {
       const double llp = log10(lp);
       for (int p = 0; p < np; p++)
-        Ps[p * LT + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
+        Ps[p * LTK + tid] = pk_eval<T>(ax, pd.tab, pd.nz, llp - nlc[p], nj[p], ndy[p]);
     }
     for (int pair = 0; pair < P.pss; pair++) {
       T acc = 0;
-      const T* xr = X + pair * PCH;
-      for (int p = 0; p < np; p++) acc += xr[p] * Ps[p * LT + tid];
+      const T* xr = X + pair * PCHK;
+      for (int p = 0; p < np; p++) acc += xr[p] * Ps[p * LTK + tid];
       const double v = (double)(pref * acc);
       double* o = out + (size_t)pair * P.nnode_ss + L;
       *o = (p0 == 0) ? v : *o + v;
@@ -1183,16 +1185,17 @@ static void launch_limber_t(const Params& P, const double* ell_ss, const double*
     (*launches)++;
   }
   // mixed plan: node records + FP32 axis + P~ + weights (ss: [PCH][pss
-  // rounded to 8]; gs: [2][MAXB][PCH]), 16 bytes of alignment slack
-  const size_t sm_f32 = sizeof(double) * PCH + 8 * PCH + 12 * (size_t)P.pk_nk + 4 * PCH * LT + 16;
+  // rounded to 8]; gs: [3][MAXB][PCH]), 16 bytes of alignment slack
   if (P.probes & CL2PT_PROBE_XI) {
-    const size_t sm = f32 ? sm_f32 + 4 * (size_t)PCH * ((P.pss + 7) & ~7)
+    constexpr int SS_LT = f32 ? 256 : LT, SS_PCH = f32 ? 32 : PCH;
+    const size_t sm = f32 ? sizeof(double) * SS_PCH + 8 * SS_PCH + 12 * (size_t)P.pk_nk + 4 * SS_PCH * SS_LT + 16 +
+                                4 * (size_t)SS_PCH * ((P.pss + 7) & ~7)
                           : sizeof(double) * (2 * P.pk_nk + PCH) +
                                 sizeof(T) * (P.pk_nk + PCH * LT + (size_t)P.pss * PCH + PCH) + sizeof(int) * PCH + 64;
-    cudaFuncSetAttribute(k_limber_ss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    dim3 g(P.B, (P.nnode_ss + LT - 1) / LT);
+    cudaFuncSetAttribute(k_limber_ss<T, SS_LT, SS_PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    dim3 g(P.B, (P.nnode_ss + SS_LT - 1) / SS_LT);
     hk(CL2PT_K_LIMBER_SS, 1);
-    k_limber_ss<T><<<g, LT, sm, s>>>(P, ell_ss);
+    k_limber_ss<T, SS_LT, SS_PCH><<<g, SS_LT, sm, s>>>(P, ell_ss);
     hk(CL2PT_K_LIMBER_SS, 0);
     (*launches)++;
   }
