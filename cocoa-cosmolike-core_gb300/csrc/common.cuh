@@ -69,6 +69,7 @@ struct Params {
   int chi_nz, G_nz, pk_nk, pk_nz, pkl_nk, pkl_nz;
   const double *chi_z, *G_z, *pk_lk, *pk_z, *pkl_lk, *pkl_z;
   int G_same_axis;         // growth table shares the distance table's z axis
+  int pkl_same_axis;       // the linear P table shares the nonlinear one's log10 k axis
   double pk_lk0, pk_dlk;   // uniform-grid description when pk_uniform
   int pk_uniform;
   // n(z) splines: zc [nz], y/c [(ntomo+1)][nz]

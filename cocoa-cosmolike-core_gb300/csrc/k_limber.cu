@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(sizeof(T) == sizeof(float) ? LTG_NODES_F32 : N
     lkt = f + pd.nk;
     lki = f + 2 * pd.nk;
     f += 3 * pd.nk;
-    if (mode == 1) {
+    if (mode == 1 && !P.pkl_same_axis) {
       lkl = f;
       lklt = f + pl.nk;
       lkli = f + 2 * pl.nk;
@@ -908,7 +908,7 @@ __global__ void __launch_bounds__(sizeof(T) == sizeof(float) ? LTG_NODES_F32 : N
   AxisF axf{}, axlf{};
   if constexpr (F32) {
     axf = copy_axis_f(P.linear_pk ? P.axkl : P.axk, pd.nk, (float*)lk, lkt, lki);
-    if (mode == 1) axlf = copy_axis_f(P.axkl, pl.nk, (float*)lkl, lklt, lkli);
+    if (mode == 1) axlf = P.pkl_same_axis ? axf : copy_axis_f(P.axkl, pl.nk, (float*)lkl, lklt, lkli);
   } else {
     ax = load_axis<T>(pd.lk, pd.nk, lk, sd, si);
     axl = load_axis<T>(pl.lk, pl.nk, lkl, sdl, sil);
@@ -1169,7 +1169,8 @@ static size_t gg_smem(const Params& P, int mode)
 {
   if (sizeof(T) == sizeof(float))
     return sizeof(double) * 9 * PCH + sizeof(int) * 2 * PCH +
-           sizeof(float) * (3 * (size_t)P.pk_nk + (mode == 1 ? 3 * (size_t)P.pkl_nk : 0) + 5 * (size_t)P.chi_nz +
+           sizeof(float) * (3 * (size_t)P.pk_nk + (mode == 1 && !P.pkl_same_axis ? 3 * (size_t)P.pkl_nk : 0) +
+                            5 * (size_t)P.chi_nz +
                             (P.G_same_axis ? 2 : 3) * (size_t)P.G_nz + 5 * (size_t)P.lens_nz) + 64;
   return sizeof(double) * (10 * PCH + 2 * P.pk_nk + 2 * P.pkl_nk) + sizeof(int) * 2 * PCH +
          sizeof(T) * (P.pk_nk + P.pkl_nk + 4 * P.chi_nz + 3 * P.G_nz + 3 * P.lens_nz) + 64;

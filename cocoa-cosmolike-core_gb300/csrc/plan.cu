@@ -638,7 +638,9 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   P.pkl_nk = (int)p->pkl_lk.size(); P.pkl_nz = (int)p->pkl_z.size();
   P.chi_z = p->d_chi_z; P.G_z = p->d_G_z;
   P.G_same_axis = (p->chi_z.size() == p->G_z.size()) &&
-                  std::equal(p->chi_z.begin(), p->chi_z.end(), p->G_z.begin()); P.pk_lk = p->d_pk_lk; P.pk_z = p->d_pk_z;
+                  std::equal(p->chi_z.begin(), p->chi_z.end(), p->G_z.begin());
+  P.pkl_same_axis = (p->pkl_lk.size() == p->pk_lk.size()) &&
+                    std::equal(p->pkl_lk.begin(), p->pkl_lk.end(), p->pk_lk.begin()); P.pk_lk = p->d_pk_lk; P.pk_z = p->d_pk_z;
   P.pkl_lk = p->d_pkl_lk; P.pkl_z = p->d_pkl_z;
   P.src_nz = p->src.nzbins; P.lens_nz = p->lens.nzbins;
   P.src_zc = p->d_src_zc; P.src_y = p->d_src_y; P.src_c = p->d_src_c;
