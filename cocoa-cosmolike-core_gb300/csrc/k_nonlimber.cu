@@ -1282,8 +1282,9 @@ static size_t nl_loop_smem(const Params& P, const NLParams& Q, bool adj, bool sm
 // the mixed plan keeps the spectra and the recurrence state in shared
 // memory, on request (CL2PT_FFTLOG_STATE_SHARED, or the autotuner's
 // choice), when two CTAs (of NL_NT threads) still fit an SM.  The default is
-// global memory: on GB300 at the real_3x2pt workload the four 128-thread
-// CTAs per SM of that form measured faster (8.8 vs 9.7 ms per 512 points).
+// global memory: on GB300 at the real_3x2pt workload the 128-thread CTAs of
+// that form measured faster (8.8 vs 9.7 ms per 512 points at four CTAs per
+// SM; five since the lean layout).
 constexpr size_t NL_SMS_MAX = 113 * 1024;
 template <typename T>
 static bool nl_use_sms(const Params& P, const NLParams& Q, bool adj)

@@ -442,7 +442,7 @@ int cl2pt_cmb_real(cl2pt_plan* plan, const cl2pt_batch* batch, double* w_gk, dou
 /* Where the mixed plan's FFTLog multipole loop keeps its spectra and
  * Gamma-recurrence state: CL2PT_FFTLOG_STATE_AUTO (the default: global
  * memory, unless cl2pt_plan_autotune chose otherwise), _GLOBAL (global
- * memory, four 128-thread CTAs per SM) or _SHARED (shared memory, two
+ * memory, five 128-thread CTAs per SM) or _SHARED (shared memory, two
  * 256-thread CTAs per SM, when it fits; else global). */
 enum { CL2PT_FFTLOG_STATE_AUTO = 0, CL2PT_FFTLOG_STATE_GLOBAL = 1, CL2PT_FFTLOG_STATE_SHARED = 2 };
 int cl2pt_plan_set_fftlog_state(cl2pt_plan* plan, int mode);
