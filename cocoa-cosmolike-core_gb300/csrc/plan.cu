@@ -616,7 +616,7 @@ extern "C" int cl2pt_plan_create(const cl2pt_config* cfg, const cl2pt_nz* src,
   TRY(dupload(p, &dzs, p->zs, std::max(p->pgs, 1)));
 
   // workspace sized for one wave of points
-  p->wave = std::min(max_batch, 256);
+  p->wave = std::min(max_batch, 512);
   const int W = p->wave, ns = cfg->n_source, nl = cfg->n_lens;
   p->node_stride = p->n_ss + nl * p->n_ss + nl * p->n_gg;
   Params& P = p->P;

@@ -66,14 +66,14 @@ def test_cmb_magnification_and_linear_mode(gpu_lib, oracle_built):
 
 @pytest.mark.gpu
 def test_cmb_batch_waves_and_null_outputs(gpu_lib):
-    """More points than one wave of the plan (256 points), and outputs left
+    """More points than one wave of the plan (512 points), and outputs left
     out, give the same spectra as one point at a time."""
-    n = 258
+    n = 514
     w = workloads.make("cmb_lensing_small")
     tabs, nus = workloads.points(w, n, seed=9)
     plan = _plan(w, lib.PREC_MIXED, n)
     gk, ks, kk = plan.cmb_cl(*workloads.stack(tabs), nus, w.ell)
-    for i in (0, 255, 256, 257):
+    for i in (0, 511, 512, 513):
         g1, k1, kk1 = plan.cmb_cl(*workloads.stack(tabs[i:i + 1]), nus[i:i + 1], w.ell)
         assert np.array_equal(g1[0], gk[i]) and np.array_equal(k1[0], ks[i]) and np.array_equal(kk1[0], kk[i])
     om, h0, chi, G, lnP = workloads.stack(tabs)

@@ -548,21 +548,21 @@ def test_bad_inputs_rejected(gpu_lib):
 
 @pytest.mark.gpu
 def test_staged_waves(gpu_lib):
-    """Host batches of more than one wave (256 points): each wave's inputs
+    """Host batches of more than one wave (512 points): each wave's inputs
     are copied and checked while earlier waves compute.  The vector of
     every point equals its one-point evaluation; a non-finite table in the
     last wave is rejected, and the plan evaluates afterwards."""
-    n = 258
+    n = 514
     w = workloads.make("real_3x2pt_small_limber")
     tabs, nus = workloads.points(w, n, seed=8)
     plan = lib.Plan(w.cfg, w.src, w.lens, w.base, lib.PREC_MIXED, max_batch=n)
     om, h0, chi, G, lnP = workloads.stack(tabs)
     dv = plan.eval_real(om, h0, chi, G, lnP, nus)
-    for i in (0, 255, 256, 257):
+    for i in (0, 511, 512, 513):
         one = plan.eval_real(om[i:i + 1], h0[i:i + 1], chi[i:i + 1], G[i:i + 1], lnP[i:i + 1], nus[i:i + 1])
         assert np.array_equal(one[0], dv[i])
     bad = lnP.copy()
-    bad[257, 11] = np.nan
+    bad[513, 11] = np.nan
     with pytest.raises(lib.CL2PTError):
         plan.eval_real(om, h0, chi, G, bad, nus)
     assert np.array_equal(plan.eval_real(om, h0, chi, G, lnP, nus), dv)
