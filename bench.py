@@ -679,7 +679,8 @@ def main():
     hbm, src = peaks()
     top = max(kms, key=lambda k: kms[k])
     step_ms = kms[top] / args.steps
-    wave = min(B, 256)
+    # the plan evaluates a batch in waves of up to 512 points
+    wave = min(B, 512)
     waves = -(-B // wave)
     nk, nz = plan.shapes["nk"], plan.shapes["nz"]
     pss, pgs, pgg = plan.n_xi // (2 * w.cfg.ntheta), plan.n_gammat // w.cfg.ntheta, w.cfg.n_lens
