@@ -100,7 +100,8 @@ struct TCFilter {
   int M, Np, K, Kpad;
 };
 // host: the pieces of filt [M][K] (-1 when M > 64), the tensor map over
-// their device copy (-1 when the driver's encoder is unavailable)
+// their device copy (-1 when the CUDA driver's tensor-map encoder is
+// unavailable)
 int tc_contract_pieces(int kind, int S, const double* filt, int M, int K, std::vector<uint8_t>& out, int* Np,
                        int* Kpad);
 int tc_contract_map(int kind, int S, void* dev, int Np, int Kpad, CUtensorMap* map);
