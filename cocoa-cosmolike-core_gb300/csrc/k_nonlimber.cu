@@ -741,14 +741,17 @@ __device__ __forceinline__ int slice_cell(const float* __restrict__ plk, int nk,
 // 128-thread CTAs, five per SM: its shared layout drops the slice adjoint,
 // the per-cell slope (formed from the neighbouring cells' head and tail)
 // and the log10 k offsets (linear in the sample index), and the compiler
-// keeps it within 96 registers.
-template <typename T, bool ADJ, bool SMS>
-constexpr bool nl_lean_launch() { return sizeof(T) == sizeof(float) && !ADJ && !SMS; }
+// keeps it within 96 registers.  WIDE: the same layout in 256-thread CTAs,
+// for transforms whose layout leaves room for fewer than four 128-thread
+// CTAs per SM (the 2048-sample radial grids of the Fourier serving
+// workload), as nl_loop_threads picks for the other forms.
+template <typename T, bool ADJ, bool SMS, bool WIDE = false>
+constexpr bool nl_lean_launch() { return sizeof(T) == sizeof(float) && !ADJ && !SMS && !WIDE; }
 constexpr int NL_LEAN_NT = 128, NL_LEAN_CTAS = 5;
 
-template <typename T, bool ADJ, bool SMS>
-__global__ void __launch_bounds__(nl_lean_launch<T, ADJ, SMS>() ? NL_LEAN_NT : NL_NT,
-                                  nl_lean_launch<T, ADJ, SMS>() ? NL_LEAN_CTAS : 2)
+template <typename T, bool ADJ, bool SMS, bool WIDE = false>
+__global__ void __launch_bounds__(nl_lean_launch<T, ADJ, SMS, WIDE>() ? NL_LEAN_NT : NL_NT,
+                                  nl_lean_launch<T, ADJ, SMS, WIDE>() ? NL_LEAN_CTAS : 2)
     k_nl_loop(Params P, NLParams Q, const double* __restrict__ cbar, double* __restrict__ lnpl_bar,
               cl2pt_nuisance* nu_bar)
 {
@@ -1339,6 +1342,10 @@ static void launch_nl_loop_t(const Params& P, const NLParams& Q, cudaStream_t s)
   if (sms) {
     cudaFuncSetAttribute(k_nl_loop<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     k_nl_loop<T, false, true><<<dim3(P.B, P.nl), nl_loop_threads(sm3), sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
+  } else if (nl_lean_launch<T, false, false>() && nl_loop_threads(sm3) == NL_NT) {
+    // fewer than four 128-thread CTAs fit an SM: 256-thread CTAs
+    cudaFuncSetAttribute(k_nl_loop<T, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    k_nl_loop<T, false, false, true><<<dim3(P.B, P.nl), NL_NT, sm3, s>>>(P, Q, nullptr, nullptr, nullptr);
   } else {
     cudaFuncSetAttribute(k_nl_loop<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     const int nt3 = nl_lean_launch<T, false, false>() ? NL_LEAN_NT : nl_loop_threads(sm3);
