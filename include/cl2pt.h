@@ -221,6 +221,9 @@ typedef struct cl2pt_like cl2pt_like;
 int cl2pt_like_create(cl2pt_plan* plan, const int* mask, const double* data, const double* inv_cov,
                       cl2pt_like** like);
 int cl2pt_like_destroy(cl2pt_like* like);
+int cl2pt_loglike_real(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch,
+                       const double* pm, double* chi2, double* lnP_bar, double* lnPL_bar,
+                       cl2pt_nuisance* nu_bar, void* stream);
 /* Baryon PCA of the real-space data vector (compute_baryon_pcas_Mx2pt_N,
  * generic_interface.hpp:1168-1225): for the one point of batch (n = 1),
  * the masked data vector without baryons and with each of nscen baryon
@@ -235,9 +238,6 @@ int cl2pt_like_destroy(cl2pt_like* like);
 int cl2pt_baryon_pcas(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch, int nscen, int nk,
                       const double* log10k, int na, const double* a, const double* log10r, double* R,
                       void* stream);
-int cl2pt_loglike_real(cl2pt_plan* plan, const cl2pt_like* like, const cl2pt_batch* batch,
-                       const double* pm, double* chi2, double* lnP_bar, double* lnPL_bar,
-                       cl2pt_nuisance* nu_bar, void* stream);
 
 /* Batched non-Limber clustering C_l (C_cl_tomo, cosmo2D.c:4528-4769, for
  * every point of the batch): cl [n][n_lens][lmax_nolimber] -- the FFTLog
