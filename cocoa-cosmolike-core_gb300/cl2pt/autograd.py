@@ -10,6 +10,10 @@ adjoint kernels; nothing but the inputs is kept between the passes.
 
 `value_and_vjp` is the fused form a sampler uses: one call returns the value
 and the gradient of cot . dv.
+
+`fourier_data_vector(plan, ..., ell)` is the same for the Fourier 3x2pt
+vector at the multipoles ell (cl2pt_eval_fourier forward, cl2pt_vjp_fourier
+backward).
 """
 from __future__ import annotations
 
@@ -70,3 +74,35 @@ def value_and_vjp(plan: Plan, omega_m, h0, chi, G, lnP, nu, cot, mask=None, pm=N
     plan.vjp_real_device(omega_m, h0, chi, G, lnP, nu, cot.contiguous(), dv, lbar, nbar,
                          mask=mask, pm=pm, stream=_stream())
     return dv, lbar, nbar
+
+
+class FourierDataVector(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, plan: Plan, omega_m, h0, chi, G, lnP, nu, ell, lmax_shear=1e30, mask=None):
+        for t, nm in ((omega_m, "omega_m"), (h0, "h0"), (chi, "chi"), (G, "G"), (lnP, "lnP"), (nu, "nu")):
+            _check(t, nm)
+        if nu.shape[-1] != NU_LEN:
+            raise ValueError(f"nu: expected [n][{NU_LEN}]")
+        n = omega_m.shape[0]
+        out = torch.empty(n, plan.fourier_n_total(len(ell)), dtype=torch.float64, device=omega_m.device)
+        plan.eval_fourier_device(omega_m, h0, chi, G, lnP, nu, ell, out, lmax_shear=lmax_shear, mask=mask,
+                                 stream=_stream())
+        ctx.plan, ctx.ell, ctx.lmax_shear, ctx.mask = plan, ell, lmax_shear, mask
+        ctx.save_for_backward(omega_m, h0, chi, G, lnP, nu)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        omega_m, h0, chi, G, lnP, nu = ctx.saved_tensors
+        g = g.contiguous()
+        lbar = torch.empty_like(lnP)
+        nbar = torch.empty_like(nu)
+        ctx.plan.vjp_fourier_device(omega_m, h0, chi, G, lnP, nu, ctx.ell, g, None, lbar, nbar,
+                                    lmax_shear=ctx.lmax_shear, mask=ctx.mask, stream=_stream())
+        return None, None, None, None, None, lbar, nbar, None, None, None
+
+
+def fourier_data_vector(plan: Plan, omega_m, h0, chi, G, lnP, nu, ell, lmax_shear=1e30, mask=None):
+    """Differentiable Fourier vector [n][plan.fourier_n_total(len(ell))],
+    differentiable in lnP and nu (see the module docstring)."""
+    return FourierDataVector.apply(plan, omega_m, h0, chi, G, lnP, nu, ell, lmax_shear, mask)

@@ -542,6 +542,28 @@ class Plan:
             return dv, lbar, nb, lbarl
         return dv, lbar, nb
 
+    def fourier_n_total(self, nell) -> int:
+        """Length of the Fourier vector at nell multipoles."""
+        nt = C.c_int()
+        check(load().cl2pt_fourier_sizes(self.h, int(nell), None, None, None, C.byref(nt)))
+        return nt.value
+
+    def eval_fourier_device(self, omega_m, h0, chi, G, lnP, nuisance, ell, out, lmax_shear=1e30, mask=None,
+                            lnPL=None, stream=None):
+        """Device form of eval_fourier: torch CUDA tensors in and out as in
+        eval_real_device (out [n][fourier_n_total(len(ell))]); ell a host
+        array."""
+        b = Batch()
+        b.n, b.where = int(omega_m.shape[0]), DEVICE
+        cast = lambda t: C.cast(C.c_void_p(t.data_ptr()), _dp)
+        b.omega_m, b.h0, b.chi, b.G, b.lnP = (cast(t) for t in (omega_m, h0, chi, G, lnP))
+        b.lnPL = cast(lnPL) if lnPL is not None else None
+        b.nuisance = C.cast(C.c_void_p(nuisance.data_ptr()), C.POINTER(abi.Nuisance))
+        ell = np.ascontiguousarray(ell, dtype=np.float64)
+        st = load().cl2pt_eval_fourier(self.h, C.byref(b), len(ell), _p(ell), float(lmax_shear),
+                                       None if mask is None else mask.data_ptr(), out.data_ptr(), stream)
+        check(st, "cl2pt_eval_fourier")
+
     def vjp_fourier_device(self, omega_m, h0, chi, G, lnP, nuisance, ell, cot, dv, lnP_bar, nu_bar,
                            lmax_shear=1e30, mask=None, lnPL=None, lnPL_bar=None, stream=None):
         """Device form of vjp_fourier (CUDA tensors as in vjp_real_device)."""
